@@ -1,0 +1,273 @@
+"""Generate golden vectors by running the reference's own ghost-cell code.
+
+Run once in a container that holds the reference checkout:
+
+    python tests/golden/make_golden.py [--reference /root/reference]
+
+The reference's ``solver/`` is copied to a temporary directory, its compiled
+``mac_engine`` is built from ``solver/src/bindings.cpp`` (the shipped Windows
+binary is deleted, never loaded), ``numba`` is replaced by a stand-in whose
+``njit`` returns the plain Python function (numba is not installed here), and
+``matplotlib`` by a no-op module.  The outputs are small ``.npz`` files in this
+directory; the tests read only those files.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+import sysconfig
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+
+NUMBA_STUB = '''
+def njit(*args, **kwargs):
+    def wrap(function):
+        function.py_func = function
+        function.nopython_signatures = [()]
+        return function
+    if args and callable(args[0]) and not kwargs:
+        return wrap(args[0])
+    return wrap
+prange = range
+'''
+PYPLOT_STUB = '''
+def __getattr__(name):
+    return lambda *a, **k: None
+'''
+
+
+def build_harness(reference: Path, work: Path) -> Path:
+    solver = work / 'solver'
+    shutil.copytree(reference / 'solver', solver, ignore=shutil.ignore_patterns('*.pyd', '__pycache__'))
+    shutil.copytree(reference / 'postprocessing', work / 'postprocessing',
+                    ignore=shutil.ignore_patterns('__pycache__'))
+    stubs = work / 'stubs'
+    (stubs / 'matplotlib').mkdir(parents=True)
+    (stubs / 'numba.py').write_text(NUMBA_STUB)
+    (stubs / 'matplotlib' / '__init__.py').write_text('')
+    (stubs / 'matplotlib' / 'pyplot.py').write_text(PYPLOT_STUB)
+    import pybind11
+    suffix = sysconfig.get_config_var('EXT_SUFFIX')
+    inc = sysconfig.get_paths()['include']
+    subprocess.run(['g++', '-O3', '-std=c++17', '-fopenmp', '-shared', '-fPIC', f'-I{inc}',
+                    f'-I{pybind11.get_include()}', str(solver / 'src' / 'bindings.cpp'),
+                    '-o', str(solver / f'mac_engine{suffix}')], check=True)
+    sys.path[:0] = [str(stubs), str(solver), str(work)]
+    os.environ['FFT_WORKERS'] = '1'
+    return solver
+
+
+def csr_parts(m):
+    m = m.tocsr()
+    return dict(data=m.data.copy(), indices=m.indices.astype(np.int64), indptr=m.indptr.astype(np.int64),
+                shape=np.array(m.shape))
+
+
+def ghost_rows(E, ids):
+    """The rows of an extension matrix that are not identity rows of active entries."""
+    E = E.tocsr()
+    identity = np.zeros(E.shape[0], bool)
+    identity[ids] = True
+    rows = np.flatnonzero(~identity & (np.diff(E.indptr) > 0))
+    sub = E[rows]
+    sub.sort_indices()
+    return dict(rows=rows.astype(np.int64), indptr=sub.indptr.astype(np.int64),
+                cols=sub.indices.astype(np.int64), vals=sub.data.copy())
+
+
+def save(name, **arrays):
+    flat = {}
+    for key, value in arrays.items():
+        if isinstance(value, dict):
+            for k2, v2 in value.items():
+                flat[f'{key}__{k2}'] = np.asarray(v2)
+        else:
+            flat[key] = np.asarray(value)
+    np.savez_compressed(HERE / f'{name}.npz', **flat)
+    print('wrote', name, sum(v.nbytes for v in flat.values()), 'bytes raw')
+
+
+def geometry_record(s):
+    g = s.gg
+    return dict(ui=g.ui.astype(np.int64), vi=g.vi.astype(np.int64), pi=g.pi.astype(np.int64),
+                Eu=ghost_rows(g.E[:s.u.size, :len(g.ui)], g.ui), Ev=ghost_rows(g.E[s.u.size:, len(g.ui):], g.vi),
+                P=ghost_rows(g.P, g.pi))
+
+
+def schur_rows_of(actual, indices, rect):
+    """Same rule as the reference's boundary_row_inverse, restated to expose the rows."""
+    import scipy.sparse as sp
+    indices = np.asarray(indices)
+    covered = np.ones(rect.shape[0], bool)
+    covered[indices] = False
+    coo = actual.tocoo()
+    ext = sp.csr_matrix((coo.data, (indices[coo.row], indices[coo.col])), shape=rect.shape)
+    virt = rect.tocoo()
+    keep = covered[virt.row] & covered[virt.col]
+    ext += sp.csr_matrix((virt.data[keep], (virt.row[keep], virt.col[keep])), shape=rect.shape)
+    delta = (ext - rect).tocsr()
+    tol = 8 * np.finfo(float).eps * max(1., float(np.max(abs(rect.diagonal()))))
+    delta.data[abs(delta.data) < tol] = 0.
+    delta.eliminate_zeros()
+    return np.flatnonzero(np.diff(delta.indptr)).astype(np.int64)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--reference', type=Path, default=Path('/root/reference'))
+    ap.add_argument('--skip-large', action='store_true')
+    args = ap.parse_args()
+    work = Path(tempfile.mkdtemp(prefix='ghost_golden_'))
+    try:
+        build_harness(args.reference, work)
+        run_all(args)
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
+def run_all(args):
+    import scipy.sparse as sp
+    from main import MAC_CylinderFlow
+    import optimized_ghost_cell as ghost
+    import rectangular_inverse
+    import mac_engine
+
+    # 1. the reference's own small test grid (tests/test_numba_ghost_cell.py:12-14)
+    def small(**kw):
+        return MAC_CylinderFlow(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., boundary='ghost_cell',
+                                time_scheme='ab2_cn', verbose=False, **kw)
+
+    s = small()
+    g = s.gg
+    rng = np.random.default_rng(6)
+    q = rng.normal(size=g.qsize)
+    p_rand = rng.normal(size=s.p.shape)
+    adv = g.advection(q).copy()
+    dif = g.diffusion(q).copy()
+    grad = g.gradient(p_rand).copy()
+    div = g.divergence(q).copy()
+    hq = g.H_matvec(q, 0.003).copy()
+    uu, vv = g.unpack(q)
+    uu, vv = uu.copy(), vv.copy()
+    proj, phi = g.project(q, .003)
+    proj, phi = proj.copy(), phi.copy()
+    rhs_p = rng.normal(size=len(g.pi))
+    sol_p = g.pressure_solve(rhs_p).copy()
+    jp, ip = np.unravel_index(g.pi, s.p.shape)
+    rect_p = rectangular_inverse.rectangle(s.nx, s.ny, s.dx, s.dy, 'pressure', rho=s.rho)[0]
+    rows_p = schur_rows_of(g.A, g.pi, rect_p)
+    nq = len(g.ui)
+    dt_h = 0.001
+    ju, iu = np.unravel_index(g.ui, s.u.shape)
+    jv, iv = np.unravel_index(g.vi, s.v.shape)
+    rect_u = rectangular_inverse.rectangle(s.nx, s.ny, s.dx, s.dy, 'u', s.nu, dt_h, s.rho)[0]
+    rect_v = rectangular_inverse.rectangle(s.nx, s.ny, s.dx, s.dy, 'v', s.nu, dt_h, s.rho)[0]
+    act_u = (sp.eye(nq, format='csc') - .5 * dt_h * g.L[:nq, :nq]).tocsc()
+    act_v = (sp.eye(g.qsize - nq, format='csc') - .5 * dt_h * g.L[nq:, nq:]).tocsc()
+    rows_u = schur_rows_of(act_u, ju * s.nx + iu - 1, rect_u)
+    rows_v = schur_rows_of(act_v, (jv - 1) * s.nx + iv, rect_v)
+    geo = geometry_record(s)
+    init_u, init_v = s.u.copy(), s.v.copy()
+    steps = []
+    for k in range(5):
+        s.solve(n_steps=1, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
+        d = s.last_step_diagnostics
+        steps.append((s.u.copy(), s.v.copy(), s.p.copy(), d['cd'], d['cl'], d['max_divergence'], d['cfl'],
+                      d['cd_pressure'], d['cd_viscous'], d['cl_pressure'], d['cl_viscous'],
+                      d['coupled_momentum_residual_linf'], d['momentum_residual_linf']))
+    forces = g.surface_forces(s.u, s.v, s.p, s.nu * s.rho)
+    stats = mac_engine.calculate_mac_divergence_cpp(s.u, s.v, s.mask, s.dx, s.dy)
+    save('small_88x16', q=q, p_rand=p_rand, advection=adv, diffusion=dif, gradient=grad, divergence=div,
+         H_q=hq, unpack_u=uu, unpack_v=vv, project_q=proj, project_phi=phi, rhs_p=rhs_p, sol_p=sol_p,
+         schur_rows_p=rows_p, schur_rows_u=rows_u, schur_rows_v=rows_v, helmholtz_dt=dt_h, **geo,
+         init_u=init_u, init_v=init_v,
+         step_u=np.array([t[0] for t in steps]), step_v=np.array([t[1] for t in steps]),
+         step_p=np.array([t[2] for t in steps]), step_scalars=np.array([t[3:] for t in steps]),
+         forces=np.array(forces), mac_divergence=np.array(stats[:1] + stats[1:2] + stats[3:4]),
+         mac_divergence_counts=np.array([stats[2], stats[4]]),
+         surface_points=g.surface_points, pressure_surface=csr_parts(g.pressure_surface),
+         du_dn=csr_parts(g.du_dn), dv_dn=csr_parts(g.dv_dn))
+
+    # 2. the 40x30 grid with the extension options (tests/test_gemini_followup.py:24-26,64-66)
+    for tag, opts in (('bq', dict(ghost_velocity_interpolation='biquadratic')),
+                      ('qp', dict(ghost_pressure_extension='quadratic')),
+                      ('iter', dict(pressure_solver='iterative'))):
+        s = MAC_CylinderFlow(nx=40, ny=30, Lx=4., Ly=3., xc=1.5, yc=1.5, boundary='ghost_cell',
+                             time_scheme='ab2_cn', verbose=False, **opts)
+        geo = geometry_record(s)
+        s.solve(n_steps=3, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
+        d = s.last_step_diagnostics
+        save(f'opt40x30_{tag}', **geo, u=s.u, v=s.v, p=s.p,
+             scalars=np.array([d['cd'], d['cl'], d['max_divergence'], d['pressure_iterations']]))
+
+    # 3. analytic traction fields (tests/test_numba_ghost_cell.py:49-69)
+    out = []
+    for nx, ny in ((40, 30), (80, 60), (120, 90)):
+        s = MAC_CylinderFlow(nx=nx, ny=ny, Lx=4., Ly=3., xc=1.5, yc=1.5, boundary='ghost_cell',
+                             time_scheme='ab2_cn', verbose=False)
+        gc, g = s.gc, s.gg
+        xx, yy = np.meshgrid(gc.xu, gc.yu)
+        rr = np.hypot(xx - s.xc, yy - s.yc)
+        u = -(rr - s.D / 2) * (yy - s.yc) / rr
+        xx, yy = np.meshgrid(gc.xv, gc.yv)
+        rr = np.hypot(xx - s.xc, yy - s.yc)
+        v = (rr - s.D / 2) * (xx - s.xc) / rr
+        p = np.broadcast_to(gc.xp, s.p.shape)
+        out.append(g.surface_forces(u, v, p, s.nu * s.rho))
+    save('traction', forces=np.array(out))
+
+    # 4. rectangle transforms on a small grid (solver/rectangular_inverse.py)
+    rec = {}
+    for kind in ('pressure', 'u', 'v'):
+        _, solve, shape = rectangular_inverse.rectangle(24, 10, 0.3, 0.25, kind, 0.02, 0.004, 1.3)
+        b = np.random.default_rng(3).normal(size=shape)
+        rec[f'{kind}_in'] = b
+        rec[f'{kind}_out'] = solve(b.copy())
+    save('rectangle_24x10', **rec)
+
+    if args.skip_large:
+        return
+    # 5. the 400x200 Re=40 case with seeded noise, two steps (config of the plain FP64 method)
+    s = MAC_CylinderFlow(nx=400, ny=200, Lx=20., Ly=10., D=1., xc=5., yc=5., nu=1 / 40, rho=1., U_inf=1.,
+                         inflow='uniform', boundary='ghost_cell', time_scheme='ab2_cn',
+                         pressure_solver='direct', verbose=False)
+    g = s.gg
+    q = g.pack(s.u, s.v).copy()
+    q += 1e-3 * np.random.default_rng(0).standard_normal(q.size)
+    u0, v0 = g.unpack(q)
+    s.u[:], s.v[:] = u0, v0
+    geo = geometry_record(s)
+    pick = np.random.default_rng(1)
+    su = np.sort(pick.choice(s.u.size, 4000, replace=False))
+    sv = np.sort(pick.choice(s.v.size, 4000, replace=False))
+    spp = np.sort(pick.choice(s.p.size, 4000, replace=False))
+    scal, fields = [], []
+    for k in range(2):
+        s.solve(n_steps=1, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+        d = s.last_step_diagnostics
+        scal.append([d['cd'], d['cl'], d['max_divergence'], d['cfl'], d['cd_pressure'], d['cd_viscous']])
+        fields.append((s.u.ravel()[su].copy(), s.v.ravel()[sv].copy(), s.p.ravel()[spp].copy(),
+                       np.abs(s.u).max(), np.abs(s.v).max(), np.abs(s.p).max(),
+                       float(np.sqrt(np.mean(s.u ** 2))), float(np.sqrt(np.mean(s.v ** 2))),
+                       float(np.sqrt(np.mean(s.p ** 2)))))
+    save('config1_400x200', active_u=np.packbits(g.E[:s.u.size].getnnz(axis=1) > 0),
+         ui_count=len(g.ui), vi_count=len(g.vi), pi_count=len(g.pi),
+         Eu=geo['Eu'], Ev=geo['Ev'], P=geo['P'],
+         ui=np.packbits(np.isin(np.arange(s.u.size), g.ui)), vi=np.packbits(np.isin(np.arange(s.v.size), g.vi)),
+         pi=np.packbits(np.isin(np.arange(s.p.size), g.pi)),
+         sample_u=su, sample_v=sv, sample_p=spp,
+         u_samples=np.array([f[0] for f in fields]), v_samples=np.array([f[1] for f in fields]),
+         p_samples=np.array([f[2] for f in fields]), norms=np.array([f[3:] for f in fields]),
+         scalars=np.array(scal), pressure_rank=g.pressure_inverse_info['rank'],
+         helmholtz_ranks=np.array([i['rank'] for i in g.helmholtz_inverse_info]))
+
+
+if __name__ == '__main__':
+    main()
