@@ -1,0 +1,133 @@
+"""ctypes binding of libghostmac.so (declarations in include/ghostmac.h).
+
+The library is loaded from this package directory.  There is no fallback:
+if it is missing or cannot be loaded the import fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / 'libghostmac.so'
+
+GM_OK, GM_EVALUE, GM_ERUNTIME, GM_EFLOAT, GM_ECUDA, GM_ENOTIMPL = range(6)
+OP_PACK, OP_UNPACK, OP_ADVECTION, OP_DIFFUSION, OP_GRADIENT, OP_DIVERGENCE, OP_H_MATVEC, OP_PRESSURE_EXTEND = range(1, 9)
+GATE_NAMES = {1: 'projection', 2: 'momentum', 3: 'pressure', 4: 'pressure_rhs', 5: 'step', 6: 'force',
+              7: 'cfl_screen', 8: 'finite'}
+
+SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_last_error', 'gm_get_sizes',
+           'gm_set_stream', 'gm_get_indices', 'gm_get_ghost_stencils', 'gm_get_schur_rows',
+           'gm_get_surface_points', 'gm_set_state', 'gm_get_state', 'gm_set_inlet', 'gm_set_history',
+           'gm_get_history', 'gm_step', 'gm_apply', 'gm_project', 'gm_pressure_solve', 'gm_rectangle_solve',
+           'gm_surface_forces', 'gm_divergence_stats')
+
+
+class Config(C.Structure):
+    _fields_ = [('nx', C.c_int32), ('ny', C.c_int32), ('Lx', C.c_double), ('Ly', C.c_double), ('D', C.c_double),
+                ('xc', C.c_double), ('yc', C.c_double), ('nu', C.c_double), ('rho', C.c_double),
+                ('U_inf', C.c_double), ('inflow', C.c_int32), ('U_m', C.c_double),
+                ('pressure_solver', C.c_int32), ('pressure_extension', C.c_int32),
+                ('velocity_interpolation', C.c_int32), ('precision', C.c_int32)]
+
+
+class Sizes(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ('nx', 'ny', 'usize', 'vsize', 'psize', 'nu_active', 'nv_active',
+                                         'np_active', 'qsize', 'n_surface', 'rank_p', 'rank_u', 'rank_v',
+                                         'ghost_u', 'ghost_v', 'ghost_p')] + \
+               [('dx', C.c_double), ('dy', C.c_double), ('U_ref', C.c_double)]
+
+
+class StepDiag(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ('time', 'dt', 'max_divergence', 'cfl', 'cd', 'cl', 'cd_pressure',
+                                          'cd_viscous', 'cl_pressure', 'cl_viscous', 'momentum_residual_linf',
+                                          'coupled_momentum_residual_linf', 'pressure_residual_linf',
+                                          'pressure_residual_relative_l2')] + \
+               [('forces', C.c_double * 6)] + \
+               [(n, C.c_int32) for n in ('pressure_solve_count', 'pressure_iterations',
+                                         'pressure_refinement_iterations', 'momentum_refinement_iterations',
+                                         'status', 'gate')]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ('residual_linf', 'residual_relative_l2', 'residual_target_linf',
+                                          'roundoff_bound_linf', 'backward_error_linf')] + \
+               [(n, C.c_int32) for n in ('iterations', 'refinement_iterations', 'status', 'rank')]
+
+
+def _load():
+    if not LIB_PATH.exists():
+        raise ImportError(f'{LIB_PATH} is missing: build it with cfd-cylinder-flow-ghost-cell_gb300/build.py')
+    lib = C.CDLL(str(LIB_PATH))
+    P, I32, I64, D = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+    pp = C.POINTER(C.c_void_p)
+    sig = {
+        'gm_create': ([C.POINTER(Config), pp], C.c_int),
+        'gm_create_host': ([C.POINTER(Config), pp], C.c_int),
+        'gm_prepare_dt': ([P, D], C.c_int),
+        'gm_destroy': ([P], C.c_int),
+        'gm_last_error': ([P], C.c_char_p),
+        'gm_get_sizes': ([P, C.POINTER(Sizes)], C.c_int),
+        'gm_set_stream': ([P, P], C.c_int),
+        'gm_get_indices': ([P, P, P, P], C.c_int),
+        'gm_get_ghost_stencils': ([P, I32, C.POINTER(I64), C.POINTER(I64), P, P, P, P], C.c_int),
+        'gm_get_schur_rows': ([P, I32, C.POINTER(I64), P], C.c_int),
+        'gm_get_surface_points': ([P, P], C.c_int),
+        'gm_set_state': ([P, P, P, P], C.c_int),
+        'gm_get_state': ([P, P, P, P], C.c_int),
+        'gm_set_inlet': ([P, P], C.c_int),
+        'gm_set_history': ([P, I32, P, P, D], C.c_int),
+        'gm_get_history': ([P, C.POINTER(I32), P, P, C.POINTER(D)], C.c_int),
+        'gm_step': ([P, D, I32, I64, D, C.POINTER(StepDiag)], C.c_int),
+        'gm_apply': ([P, I32, D, P, P], C.c_int),
+        'gm_project': ([P, D, P, P, P, C.POINTER(SolveInfo)], C.c_int),
+        'gm_pressure_solve': ([P, P, P, C.POINTER(SolveInfo)], C.c_int),
+        'gm_rectangle_solve': ([P, I32, D, P, P], C.c_int),
+        'gm_surface_forces': ([P, P, P, P, D, P], C.c_int),
+        'gm_divergence_stats': ([P, P, P, P, P], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    return lib
+
+
+lib = _load()
+
+
+class GhostError(Exception):
+    pass
+
+
+def check(rc: int, handle=None):
+    """Map a GM_E* status to the reference's exception classes."""
+    if rc == GM_OK:
+        return
+    msg = lib.gm_last_error(handle).decode(errors='replace')
+    if rc == GM_EVALUE:
+        raise ValueError(msg)
+    if rc == GM_ERUNTIME:
+        raise RuntimeError(msg)
+    if rc == GM_EFLOAT:
+        raise FloatingPointError(msg)
+    if rc == GM_ENOTIMPL:
+        raise NotImplementedError(msg)
+    raise GhostError(msg)
+
+
+def ptr(a):
+    """Data pointer of a C-contiguous float64/int64 numpy array or a CUDA torch tensor."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags['C_CONTIGUOUS']:
+            raise ValueError('arrays must be C-contiguous')
+        return a.ctypes.data
+    if hasattr(a, 'data_ptr'):
+        if not a.is_contiguous():
+            raise ValueError('tensors must be contiguous')
+        return a.data_ptr()
+    raise TypeError(f'unsupported array type {type(a)!r}')

@@ -1,0 +1,1132 @@
+// C ABI of libghostmac.so: handle lifetime, device upload, Schur precompute and
+// the AB2/CN step sequence (solver/time_integration.py:7-145 as orchestrated by
+// solver/optimized_ghost_cell.py:236-278 and solver/main.py:271-429).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/ghostmac.h"
+#include "geometry.hpp"
+#include "kernels.cuh"
+
+using namespace gmk;
+
+namespace {
+
+std::string g_create_error;
+
+struct CudaError : std::exception {
+  std::string msg;
+  explicit CudaError(std::string m) : msg(std::move(m)) {}
+};
+struct GateError : std::exception {
+  int cls;
+  std::string msg;
+  GateError(int c, std::string m) : cls(c), msg(std::move(m)) {}
+};
+
+#define CK(call)                                                                                    \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e_));     \
+  } while (0)
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { if (p) cudaFree(p); }
+  void alloc(size_t count) {
+    if (p) { cudaFree(p); p = nullptr; }
+    n = count;
+    if (count) CK(cudaMalloc(&p, count * sizeof(T)));
+  }
+  void upload(const std::vector<T>& v, cudaStream_t st) {
+    alloc(v.size());
+    if (!v.empty()) CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+  }
+  void zero(cudaStream_t st) { if (n) CK(cudaMemsetAsync(p, 0, n * sizeof(T), st)); }
+};
+
+struct Csrd {
+  DBuf<int64_t> rows, ptr, col;
+  DBuf<double> val;
+  int n = 0;
+};
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// radix plan of an FFT length
+FftPlan make_plan(int M) {
+  FftPlan p{};
+  p.M = M;
+  int m = M, s = 0;
+  while (m % 8 == 0) { p.radix[s++] = 8; m /= 8; }
+  while (m % 4 == 0) { p.radix[s++] = 4; m /= 4; }
+  while (m % 2 == 0) { p.radix[s++] = 2; m /= 2; }
+  while (m % 5 == 0) { p.radix[s++] = 5; m /= 5; }
+  while (m % 3 == 0) { p.radix[s++] = 3; m /= 3; }
+  for (int f = 7; m > 1; f += 2)
+    while (m % f == 0) {
+      if (f > 64) throw CudaError("FFT length has a prime factor above 64");
+      p.radix[s++] = f;
+      m /= f;
+    }
+  p.nstages = s;
+  return p;
+}
+
+std::vector<double> cexp_table(int count, double scale_num, double scale_den, double offset, int sign) {
+  // entries exp(sign * i * pi * (k*scale_num + offset) / scale_den), interleaved (re, im)
+  std::vector<double> t(2 * (size_t)count);
+  for (int k = 0; k < count; ++k) {
+    long double a = 3.14159265358979323846264338327950288L * ((long double)k * scale_num + offset) / scale_den;
+    t[2 * k] = (double)std::cos(a);
+    t[2 * k + 1] = sign * (double)std::sin(a);
+  }
+  return t;
+}
+
+struct RectDev {
+  TransformTables tt{};
+  RectView view{};
+  DBuf<double> Wx, prex, postx, Wy, prey, posty, recip;
+  // Schur data
+  int rank = 0;
+  DBuf<int64_t> rows, cptr, ccol;
+  DBuf<double> cval, sinv;
+};
+
+}  // namespace
+
+struct gm_handle {
+  gm::Geometry g;
+  gm::HelmholtzSetup hs;
+  bool helm_ready = false;
+  double helm_dt = 0;
+  std::string err;
+  cudaStream_t st = nullptr;
+  bool own_stream = true;
+  int device = 0;
+  size_t smem_optin = 48 * 1024;
+  CaseDev cd{};
+  // geometry on device
+  DBuf<uint8_t> cls_f, cls_p, mask;  // cls_f: u then v class maps
+  const uint8_t* cls_u = nullptr;
+  const uint8_t* cls_v = nullptr;
+  DBuf<double> inlet;
+  Csrd gf, gp, irr[3];
+  DBuf<int32_t> a_nnz;
+  DBuf<int64_t> sp_ptr, sp_col, su_ptr, su_col, sv_ptr, sv_col, d_ui, d_vi, d_pi;
+  DBuf<double> sp_val, su_val, sv_val, nwx, nwy, nxx, nyy;
+  RectDev rp, ru, rv;
+  // state and work buffers (face grid F, pressure grid P)
+  DBuf<double> U, Unext, hist, now, rhs, star, fres, ffirst, fw2, fmid, fhalf, faction, fproj, fproj2, ftmp;
+  DBuf<double> phalf, phalf_next, pout, prhs, pphi, pres, pfirst, pw2, pinc, ptmp, spectral;
+  DBuf<StepCtl> ctl;
+  DBuf<unsigned long long> state_max;  // persistent max|u|, max|v| of the current state
+  StepCtl* host_ctl = nullptr;
+  bool has_history = false;
+  bool host_only = false;
+  double prev_dt = 0;
+  int64_t F = 0, Pn = 0;
+  // scratch for host<->device arrays
+  DBuf<double> io[4];
+};
+
+namespace {
+
+void set_error(gm_handle* h, const std::string& m) {
+  if (h) h->err = m;
+  else g_create_error = m;
+}
+
+Gate gate_of(gm_handle* h, int slot = 0, int sweep = 0) { return Gate{h->ctl.p, slot, sweep}; }
+
+void upload_csr(Csrd& d, const std::vector<int64_t>& rows, const gm::Csr& c, cudaStream_t st,
+                int64_t col_offset = 0, int64_t row_offset = 0) {
+  d.n = (int)c.rows();
+  std::vector<int64_t> r(rows), cols(c.col);
+  for (auto& x : r) x += row_offset;
+  for (auto& x : cols) x += col_offset;
+  d.rows.upload(r, st);
+  d.ptr.upload(c.ptr, st);
+  d.col.upload(cols, st);
+  d.val.upload(c.val, st);
+}
+
+// x / y tables of a rectangle kind
+void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
+  const gm::Geometry& g = h->g;
+  const int nx = g.nx, ny = g.ny;
+  int rows = kind == 2 ? ny - 1 : ny, cols = nx;
+  int tx_f, tx_i, ty_f, ty_i;
+  double fy;
+  if (kind == 0) { tx_f = DCT4; tx_i = DCT4; ty_f = DCT2; ty_i = DCT3; fy = 0.0; }
+  else if (kind == 1) { tx_f = DST3; tx_i = DST2; ty_f = DST2; ty_i = DST3; fy = 1.0; }
+  else { tx_f = DST4; tx_i = DST4; ty_f = DST1; ty_i = DST1; fy = 1.0; }
+  TransformTables& tt = rd.tt;
+  tt.tx_fwd = tx_f; tt.tx_inv = tx_i; tt.ty_fwd = ty_f; tt.ty_inv = ty_i;
+  int Mx = r2r_fft_length(tx_f, cols), My = r2r_fft_length(ty_f, rows);
+  tt.plan_x = make_plan(Mx);
+  tt.plan_y = make_plan(My);
+  cudaStream_t st = h->st;
+  rd.Wx.upload(cexp_table(Mx, 2.0, Mx, 0.0, -1), st);
+  rd.Wy.upload(cexp_table(My, 2.0, My, 0.0, -1), st);
+  // type IV: pre exp(-i pi (4m+1)/(4n)), post exp(-i pi k/n); Makhoul: (cos, sin)(pi k/(2n))
+  if (r2r_family(tx_f) == 2) {
+    rd.prex.upload(cexp_table(cols / 2, 4.0, 4.0 * cols, 1.0, -1), st);
+    rd.postx.upload(cexp_table(cols / 2, 1.0, cols, 0.0, -1), st);
+  } else {
+    rd.prex.upload(cexp_table(1, 0, 1, 0, 1), st);
+    rd.postx.upload(cexp_table(cols, 1.0, 2.0 * cols, 0.0, +1), st);
+  }
+  if (r2r_family(ty_f) == 0) {
+    rd.prey.upload(cexp_table(1, 0, 1, 0, 1), st);
+    rd.posty.upload(cexp_table(rows, 1.0, 2.0 * rows, 0.0, +1), st);
+  } else {
+    rd.prey.upload(cexp_table(1, 0, 1, 0, 1), st);
+    rd.posty.upload(cexp_table(1, 0, 1, 0, 1), st);
+  }
+  tt.Wx = rd.Wx.p; tt.prex = rd.prex.p; tt.postx = rd.postx.p;
+  tt.prex_inv = rd.prex.p; tt.postx_inv = rd.postx.p;
+  tt.Wy = rd.Wy.p; tt.prey = rd.prey.p; tt.posty = rd.posty.p;
+  // eigenvalue table (solver/rectangular_inverse.py:39-46) with the 1/(4 nx ny) of the inverse transforms
+  std::vector<double> recip((size_t)rows * cols);
+  const double PI = 3.141592653589793;
+  for (int ky = 0; ky < rows; ++ky) {
+    double sy = ((double)ky + fy) * PI / (2 * ny);
+    double ry = 4 * std::pow(std::sin(sy), 2) / (g.dy * g.dy);
+    for (int kx = 0; kx < cols; ++kx) {
+      double sx = ((double)kx + 0.5) * PI / (2 * nx);
+      double rate = ry + 4 * std::pow(std::sin(sx), 2) / (g.dx * g.dx);
+      double div = kind == 0 ? -rate / g.rho : 1 + ((0.5 * dt) * g.nu) * rate;
+      recip[(size_t)ky * cols + kx] = 1.0 / (div * (4.0 * nx * ny));
+    }
+  }
+  rd.recip.upload(recip, st);
+  tt.recip = rd.recip.p;
+  // lines per block and shared memory
+  auto smem_for = [](int type, int n, int lpb) {
+    size_t stage = ((size_t)lpb * n * sizeof(double) + 15) / 16 * 16;
+    return stage + 2 * (size_t)r2r_buffer_elems(type, n, lpb) * sizeof(cplx<double>);
+  };
+  auto pick = [&](int type, int n, int lines, size_t& smem) {
+    int lpb = 8;
+    while (lpb > 1 && ((lines + lpb - 1) / lpb < 2 * 152 || smem_for(type, n, lpb) > h->smem_optin)) lpb /= 2;
+    if (r2r_paired(type) && lpb == 1 && lines > 1) lpb = 2;
+    while (lpb > 1 && smem_for(type, n, lpb) > h->smem_optin) lpb /= 2;
+    smem = smem_for(type, n, lpb);
+    return lpb;
+  };
+  size_t sx1, sx2, sy1;
+  int lx1 = pick(tx_f, cols, rows, sx1);
+  int lx2 = pick(tx_i, cols, rows, sx2);
+  tt.lpb_x = std::min(lx1, lx2);
+  tt.smem_x = std::max(smem_for(tx_f, cols, tt.lpb_x), smem_for(tx_i, cols, tt.lpb_x));
+  tt.lpb_y = pick(ty_f, rows, cols, sy1);
+  tt.smem_y = smem_for(ty_f, rows, tt.lpb_y);
+  if (tt.smem_x > h->smem_optin || tt.smem_y > h->smem_optin) throw CudaError("transform does not fit in shared memory");
+  // view
+  rd.view.rows = rows;
+  rd.view.cols = cols;
+  if (kind == 0) { rd.view.base = 0; rd.view.pitch = nx; rd.view.cls = h->cls_p.p; }
+  else if (kind == 1) { rd.view.base = 1; rd.view.pitch = nx + 1; rd.view.cls = h->cls_f.p; }
+  else { rd.view.base = h->g.usize + nx; rd.view.pitch = nx; rd.view.cls = h->cls_f.p; }
+}
+
+// Schur matrix S = I + C T^{-1} U by impulse solves, LU, explicit inverse (solver/pressure_schur.py:92-101)
+void build_schur(gm_handle* h, RectDev& rd, const std::vector<int64_t>& rows, const gm::Csr& C, double* field_buf) {
+  cudaStream_t st = h->st;
+  rd.rank = (int)rows.size();
+  rd.rows.upload(rows, st);
+  rd.cptr.upload(C.ptr, st);
+  rd.ccol.upload(C.col, st);
+  rd.cval.upload(C.val, st);
+  const int n = rd.rank;
+  if (n == 0) { rd.sinv.alloc(0); return; }
+  DBuf<double> S;
+  S.alloc((size_t)n * n);
+  // field_buf is a full-grid buffer used as the impulse; h->ftmp / ptmp holds T^{-1} e
+  double* first = (rd.view.cls == h->cls_p.p) ? h->ptmp.p : h->ftmp.p;
+  size_t span = (rd.view.cls == h->cls_p.p) ? (size_t)h->Pn : (size_t)h->F;
+  CK(cudaMemsetAsync(field_buf, 0, span * sizeof(double), st));
+  const double one = 1.0, zero = 0.0;
+  Gate open{nullptr, 0, 0};
+  for (int c = 0; c < n; ++c) {
+    int64_t rc = rows[c];
+    int64_t fi = rd.view.base + (rc / rd.view.cols) * rd.view.pitch + rc % rd.view.cols;
+    CK(cudaMemcpyAsync(field_buf + fi, &one, sizeof(double), cudaMemcpyHostToDevice, st));
+    launch_rect_inverse(rd.tt, rd.view, field_buf, false, h->spectral.p, first, nullptr, nullptr, open, st);
+    launch_schur_column(first, rd.view, n, rd.cptr.p, rd.ccol.p, rd.cval.p, S.p, c, st);
+    CK(cudaMemcpyAsync(field_buf + fi, &zero, sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  CK(cudaGetLastError());
+  std::vector<double> hs((size_t)n * n);
+  CK(cudaMemcpyAsync(hs.data(), S.p, hs.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  for (int i = 0; i < n; ++i) hs[(size_t)i * n + i] += 1.0;
+  std::vector<int> piv(n);
+  if (!gm::lu_factor(n, hs.data(), piv.data())) throw GateError(GM_ERUNTIME, "Singular boundary Schur matrix");
+  std::vector<double> inv((size_t)n * n);
+  gm::lu_inverse(n, hs.data(), piv.data(), inv.data());
+  rd.sinv.upload(inv, st);
+}
+
+void fill_case_dev(gm_handle* h) {
+  const gm::Geometry& g = h->g;
+  CaseDev& c = h->cd;
+  c.nx = g.nx; c.ny = g.ny; c.dx = g.dx; c.dy = g.dy; c.rho = g.rho; c.nu = g.nu;
+  c.usize = g.usize; c.vsize = g.vsize; c.psize = g.psize;
+  c.cls_u = h->cls_u; c.cls_v = h->cls_v; c.cls_p = h->cls_p.p;
+  c.inlet = h->inlet.p;
+  c.n_ghost_f = h->gf.n; c.gf_rows = h->gf.rows.p; c.gf_ptr = h->gf.ptr.p; c.gf_col = h->gf.col.p; c.gf_val = h->gf.val.p;
+  c.n_ghost_p = h->gp.n; c.gp_rows = h->gp.rows.p; c.gp_ptr = h->gp.ptr.p; c.gp_col = h->gp.col.p; c.gp_val = h->gp.val.p;
+  for (int k = 0; k < 3; ++k) {
+    c.n_irr[k] = h->irr[k].n; c.irr_rows[k] = h->irr[k].rows.p; c.irr_ptr[k] = h->irr[k].ptr.p;
+    c.irr_col[k] = h->irr[k].col.p; c.irr_val[k] = h->irr[k].val.p;
+  }
+  c.a_nnz = h->a_nnz.p;
+  c.n_surf = g.n_surface;
+  c.sp_ptr = h->sp_ptr.p; c.sp_col = h->sp_col.p; c.sp_val = h->sp_val.p;
+  c.su_ptr = h->su_ptr.p; c.su_col = h->su_col.p; c.su_val = h->su_val.p;
+  c.sv_ptr = h->sv_ptr.p; c.sv_col = h->sv_col.p; c.sv_val = h->sv_val.p;
+  c.nwx = h->nwx.p; c.nwy = h->nwy.p; c.nxx = h->nxx.p; c.nyy = h->nyy.p;
+  c.D = g.D; c.U_ref = g.U_ref;
+}
+
+void build_class_maps(gm_handle* h) {
+  const gm::Geometry& g = h->g;
+  std::vector<uint8_t> cu(g.usize), cv(g.vsize), cp(g.psize);
+  for (int64_t f = 0; f < g.usize; ++f) cu[f] = (g.act_u[f] ? CLS_ACTIVE : 0) | (g.ghost_of_u[f] >= 0 ? CLS_GHOST : 0);
+  for (int64_t f = 0; f < g.vsize; ++f) cv[f] = (g.act_v[f] ? CLS_ACTIVE : 0) | (g.ghost_of_v[f] >= 0 ? CLS_GHOST : 0);
+  for (int64_t f = 0; f < g.psize; ++f) cp[f] = (g.act_p[f] ? CLS_ACTIVE : 0) | (g.ghost_of_p[f] >= 0 ? CLS_GHOST : 0);
+  for (int64_t r : g.a_rows) cp[r] |= CLS_IRREG;
+  if (h->helm_ready) {
+    for (int64_t r : h->hs.rows_irr[0]) cu[r] |= CLS_IRREG;
+    for (int64_t r : h->hs.rows_irr[1]) cv[r] |= CLS_IRREG;
+  }
+  std::vector<uint8_t> cf(cu);
+  cf.insert(cf.end(), cv.begin(), cv.end());
+  if (h->cls_f.n != cf.size()) h->cls_f.alloc(cf.size());
+  CK(cudaMemcpyAsync(h->cls_f.p, cf.data(), cf.size(), cudaMemcpyHostToDevice, h->st));
+  if (h->cls_p.n != cp.size()) h->cls_p.alloc(cp.size());
+  CK(cudaMemcpyAsync(h->cls_p.p, cp.data(), cp.size(), cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->cls_u = h->cls_f.p;
+  h->cls_v = h->cls_f.p + g.usize;
+}
+
+// device copy-in/out helpers
+const double* dev_in(gm_handle* h, int slot, const double* p, size_t n) {
+  if (is_device_ptr(p)) return p;
+  if (h->io[slot].n < n) h->io[slot].alloc(n);
+  CK(cudaMemcpyAsync(h->io[slot].p, p, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  return h->io[slot].p;
+}
+struct DevOut {
+  gm_handle* h;
+  double* user;
+  double* dev;
+  size_t n;
+  bool copy;
+  DevOut(gm_handle* hh, int slot, double* p, size_t count) : h(hh), user(p), n(count) {
+    copy = !is_device_ptr(p);
+    if (copy) {
+      if (h->io[slot].n < n) h->io[slot].alloc(n);
+      dev = h->io[slot].p;
+    } else {
+      dev = p;
+    }
+  }
+  void finish() {
+    if (copy && user) CK(cudaMemcpyAsync(user, dev, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  }
+};
+
+void check_ctl(gm_handle* h, const char* where) {
+  CK(cudaMemcpyAsync(h->host_ctl, h->ctl.p, sizeof(StepCtl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  const StepCtl& c = *h->host_ctl;
+  if (c.err) {
+    static const char* names[] = {"", "Ghost projection failed", "CN momentum solve failed", "Pressure solve failed",
+                                  "Pressure RHS must be finite", "Ghost step failed divergence/CFL gate",
+                                  "Non-finite force", "Explicit timestep unsafe", "Finite fields and a positive timestep are required"};
+    std::string m = std::string(names[c.gate < 9 ? c.gate : 0]) + " (" + where + ")";
+    throw GateError(c.err, m);
+  }
+}
+
+// --- building blocks of the step ---------------------------------------------
+
+void ghost_faces(gm_handle* h, double* U, const Gate& gt) {
+  launch_ghost(U, h->gf.n, h->gf.rows.p, h->gf.ptr.p, h->gf.col.p, h->gf.val.p, gt, h->st);
+}
+void ghost_p(gm_handle* h, double* P, const Gate& gt) {
+  launch_ghost(P, h->gp.n, h->gp.rows.p, h->gp.ptr.p, h->gp.col.p, h->gp.val.p, gt, h->st);
+}
+
+// one boundary-row solve of kind k into x with residual checks (solver/pressure_schur.py:103-124)
+void schur_solve(gm_handle* h, RectDev& rd, int kind, double hc, const double* b, double* x, double* res,
+                 double* first, double* w2, int slot) {
+  cudaStream_t st = h->st;
+  SolveCtl* sc = &h->ctl.p->solve[slot];
+  for (int sweep = 0; sweep < 3; ++sweep) {
+    Gate gt = gate_of(h, slot, sweep);
+    const double* rhs = sweep == 0 ? b : res;
+    launch_rect_inverse(rd.tt, rd.view, rhs, true, h->spectral.p, first, nullptr, nullptr, gt, st);
+    launch_schur(first, rd.view, rd.rank, rd.rows.p, rd.cptr.p, rd.ccol.p, rd.cval.p, rd.sinv.p, w2, gt, st);
+    launch_rect_inverse(rd.tt, rd.view, w2, false, h->spectral.p, x, first, sweep == 0 ? nullptr : x, gt, st);
+    launch_residual(h->cd, kind, hc, b, x, res, sc, sweep, sweep == 0, gt, st);
+  }
+}
+
+// project(q, dt) (solver/optimized_ghost_cell.py:218-229); q is a face grid with active values
+void project(gm_handle* h, double* q, double dt, double* out, double* phi, int slot, int divk) {
+  cudaStream_t st = h->st;
+  Gate g0 = gate_of(h);
+  launch_set_inlet(h->cd, q, false, st);
+  ghost_faces(h, q, g0);
+  launch_divergence(h->cd, q, h->prhs.p, dt, nullptr, nullptr, 1, g0, st);
+  schur_solve(h, h->rp, 0, 0.0, h->prhs.p, phi, h->pres.p, h->pfirst.p, h->pw2.p, slot);
+  launch_gate_pressure(h->ctl.p, slot, st);
+  ghost_p(h, phi, g0);
+  launch_project_update(h->cd, q, phi, dt, out, nullptr, g0, st);
+  ghost_faces(h, out, g0);
+  launch_divergence(h->cd, out, nullptr, 0.0, nullptr, &h->ctl.p->div_max[divk], 0, g0, st);
+  launch_gate_projection(h->ctl.p, divk, st);
+}
+
+void ensure_helmholtz(gm_handle* h, double dt) {
+  if (h->helm_ready && h->helm_dt == dt) return;
+  int ec = 0;
+  std::string err;
+  gm::HelmholtzSetup hs;
+  if (!gm::build_helmholtz(h->g, dt, hs, ec, err)) throw GateError(ec ? ec : GM_EVALUE, err);
+  h->hs = std::move(hs);
+  h->helm_ready = true;
+  h->helm_dt = dt;
+  if (h->host_only) return;
+  build_class_maps(h);
+  upload_csr(h->irr[1], h->hs.rows_irr[0], h->hs.irr[0], h->st);
+  upload_csr(h->irr[2], h->hs.rows_irr[1], h->hs.irr[1], h->st);
+  // v irregular rows are v-grid flat indices (columns too)
+  fill_case_dev(h);
+  build_rect_tables(h, h->ru, 1, dt);
+  build_rect_tables(h, h->rv, 2, dt);
+  build_schur(h, h->ru, h->hs.schur_rows[0], h->hs.schur_c[0], h->fw2.p);
+  build_schur(h, h->rv, h->hs.schur_rows[1], h->hs.schur_c[1], h->fw2.p);
+  CK(cudaMemsetAsync(h->fw2.p, 0, h->F * sizeof(double), h->st));
+  CK(cudaStreamSynchronize(h->st));
+}
+
+// One AB2/CN step (solver/time_integration.py:7-145) on the handle state.
+void step_once(gm_handle* h, double dt, bool screen) {
+  cudaStream_t st = h->st;
+  const double hdt = 0.5 * dt;
+  const double hc = (0.5 * dt) * h->g.nu;
+  Gate g0 = gate_of(h);
+  CK(cudaMemsetAsync(h->ctl.p, 0, sizeof(StepCtl), st));
+  launch_cfl_screen(h->ctl.p, &h->state_max.p[0], &h->state_max.p[1], dt, h->g.dx, h->g.dy, screen ? 1 : 0, st);
+  const bool first = !h->has_history;
+  // pressure at the previous half step: the stored half pressure, or p at active cells
+  // when there is no history (solver/optimized_ghost_cell.py:256); ghost values for G p
+  if (first) launch_copy_active(h->cls_p.p, h->Pn, h->pout.p, h->phalf.p, g0, st);
+  ghost_p(h, h->phalf.p, g0);
+  MomentumArgs ma{};
+  ma.U = h->U.p;
+  ma.P = h->phalf.p;
+  ma.dt = dt;
+  if (first) {
+    ma.mode = 1;
+    ma.now = h->now.p;
+    ma.out = h->fmid.p;
+    launch_momentum(h->cd, ma, g0, st);
+    project(h, h->fmid.p, 0.5 * dt, h->fhalf.p, h->pphi.p, S_P0, 0);
+    ma.mode = 2;
+    ma.Uhalf = h->fhalf.p;
+    ma.now = nullptr;
+    ma.out = h->rhs.p;
+    launch_momentum(h->cd, ma, g0, st);
+  } else {
+    ma.mode = 0;
+    ma.alpha = dt / (2 * h->prev_dt);
+    ma.prev = h->hist.p;
+    ma.now = h->now.p;
+    ma.out = h->rhs.p;
+    launch_momentum(h->cd, ma, g0, st);
+  }
+  // CN Helmholtz solves for u and v (solver/optimized_ghost_cell.py:247-254)
+  schur_solve(h, h->ru, 1, hc, h->rhs.p, h->star.p, h->fres.p, h->ffirst.p, h->fw2.p, S_HELM_U);
+  schur_solve(h, h->rv, 2, hc, h->rhs.p, h->star.p, h->fres.p, h->ffirst.p, h->fw2.p, S_HELM_V);
+  launch_gate_momentum(h->ctl.p, st);
+  // projection of the CN velocity, defect correction and the pressure increment
+  project(h, h->star.p, dt, h->Unext.p, h->pphi.p, S_P1, 1);
+  launch_defect(h->cd, h->Unext.p, h->rhs.p, hdt, h->faction.p, h->fproj.p, g0, st);
+  project(h, h->fproj.p, dt, h->fproj2.p, h->pinc.p, S_P2, 2);
+  ghost_p(h, h->pinc.p, g0);
+  double factor = first ? 1.0 : dt / (dt + h->prev_dt);
+  launch_pressure_out(h->cd, h->phalf.p, h->pinc.p, factor, dt, h->faction.p, h->rhs.p, h->phalf_next.p, h->pout.p,
+                      &h->ctl.p->coupled_max, g0, st);
+  ghost_p(h, h->pout.p, g0);
+  // diagnostics on the new state, forces and the step gates (solver/main.py:383-415)
+  launch_maxabs(h->cd, h->Unext.p, &h->ctl.p->umax, &h->ctl.p->vmax, g0, st);
+  launch_forces(h->cd, h->Unext.p, h->pout.p, h->g.nu * h->g.rho, dt, h->ctl.p, 1, nullptr, g0, st);
+  CK(cudaGetLastError());
+}
+
+void commit_step(gm_handle* h, double dt) {
+  std::swap(h->U.p, h->Unext.p);
+  std::swap(h->phalf.p, h->phalf_next.p);
+  std::swap(h->hist.p, h->now.p);
+  h->has_history = true;
+  h->prev_dt = dt;
+  CK(cudaMemcpyAsync(h->state_max.p, &h->ctl.p->umax, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, h->st));
+}
+
+void fill_diag(gm_handle* h, const StepCtl& c, double t, double dt, bool first, gm_step_diag* d) {
+  std::memset(d, 0, sizeof *d);
+  d->time = t;
+  d->dt = dt;
+  d->max_divergence = bits2d(c.div_max[1]);
+  d->cfl = dt * (bits2d(c.umax) / h->g.dx + bits2d(c.vmax) / h->g.dy);
+  double denom = ((0.5 * h->g.rho) * (h->g.U_ref * h->g.U_ref)) * h->g.D;
+  d->cd = c.cd;
+  d->cl = c.cl;
+  d->cd_pressure = c.forces[2] / denom;
+  d->cd_viscous = c.forces[4] / denom;
+  d->cl_pressure = c.forces[3] / denom;
+  d->cl_viscous = c.forces[5] / denom;
+  for (int q = 0; q < 6; ++q) d->forces[q] = c.forces[q];
+  double mres = 0;
+  int mref = 0;
+  for (int s = 0; s < 2; ++s) {
+    const SolveCtl& sc = c.solve[s];
+    double b = bits2d(sc.bmax), tg = std::max(1e-10, 32 * 2.220446049250313e-16 * std::max(1.0, b));
+    int k = 0;
+    if (bits2d(sc.rmax[0]) > tg) { k = 1; if (bits2d(sc.rmax[1]) > tg) k = 2; }
+    mres = std::max(mres, bits2d(sc.rmax[k]));
+    mref += k;
+  }
+  d->momentum_residual_linf = mres;
+  d->momentum_refinement_iterations = mref;
+  d->coupled_momentum_residual_linf = bits2d(c.coupled_max);
+  int count = 0, refine = 0;
+  double plinf = 0, prel = 0;
+  for (int s = first ? 2 : 3; s < 5; ++s) {
+    const SolveCtl& sc = c.solve[s];
+    double b = bits2d(sc.bmax), tg = std::max(1e-10, 32 * 2.220446049250313e-16 * std::max(1.0, b));
+    int k = 0;
+    if (bits2d(sc.rmax[0]) > tg) { k = 1; if (bits2d(sc.rmax[1]) > tg) k = 2; }
+    ++count;
+    refine += k;
+    plinf = std::max(plinf, bits2d(sc.rmax[k]));
+    double den = std::max(std::sqrt(sc.bsq), 2.2250738585072014e-308);
+    prel = std::max(prel, std::sqrt(sc.rsq[k]) / den);
+  }
+  d->pressure_solve_count = count;
+  d->pressure_refinement_iterations = refine;
+  d->pressure_iterations = 0;
+  d->pressure_residual_linf = plinf;
+  d->pressure_residual_relative_l2 = prel;
+  d->status = c.err;
+  d->gate = c.gate;
+}
+
+}  // namespace
+
+namespace {
+int run_guarded(gm_handle* h, const std::function<void()>& f) {
+  try {
+    f();
+    return GM_OK;
+  } catch (const GateError& e) {
+    set_error(h, e.msg);
+    return e.cls;
+  } catch (const CudaError& e) {
+    set_error(h, e.msg);
+    return GM_ECUDA;
+  } catch (const std::exception& e) {
+    set_error(h, e.what());
+    return GM_ECUDA;
+  }
+}
+
+void initial_state(gm_handle* h) {
+  // u = inlet rows with the faces of masked cells zero, v = 0, p = 0 (solver/main.py:166-177)
+  const gm::Geometry& g = h->g;
+  std::vector<double> F(h->F, 0.0);
+  for (int j = 0; j < g.ny; ++j)
+    for (int i = 0; i <= g.nx; ++i) F[(size_t)j * (g.nx + 1) + i] = g.u_inlet[j];
+  for (int j = 0; j < g.ny; ++j)
+    for (int i = 0; i < g.nx; ++i)
+      if (g.mask[(size_t)j * g.nx + i]) {
+        F[(size_t)j * (g.nx + 1) + i] = 0.0;
+        F[(size_t)j * (g.nx + 1) + i + 1] = 0.0;
+        F[g.usize + (size_t)j * g.nx + i] = 0.0;
+        F[g.usize + (size_t)(j + 1) * g.nx + i] = 0.0;
+      }
+  CK(cudaMemcpyAsync(h->ftmp.p, F.data(), F.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  // q = pack(u, v); project(q, 1) (solver/main.py:229-230)
+  Gate g0{nullptr, 0, 0};
+  launch_copy_active(h->cls_f.p, h->F, h->ftmp.p, h->fmid.p, g0, h->st);
+  CK(cudaMemsetAsync(h->ctl.p, 0, sizeof(StepCtl), h->st));
+  project(h, h->fmid.p, 1.0, h->U.p, h->pphi.p, S_P1, 1);
+  check_ctl(h, "initial projection");
+  CK(cudaMemsetAsync(h->phalf.p, 0, h->Pn * sizeof(double), h->st));
+  CK(cudaMemsetAsync(h->pout.p, 0, h->Pn * sizeof(double), h->st));
+  launch_maxabs(h->cd, h->U.p, &h->state_max.p[0], &h->state_max.p[1], Gate{nullptr, 0, 0}, h->st);
+  CK(cudaStreamSynchronize(h->st));
+}
+
+}  // namespace
+
+// =============================================================================
+// C ABI
+// =============================================================================
+extern "C" {
+
+const char* gm_last_error(const gm_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+
+int gm_create(const gm_config* cfg, gm_handle** out) {
+  if (!cfg || !out) { g_create_error = "null argument"; return GM_EVALUE; }
+  *out = nullptr;
+  auto h = std::make_unique<gm_handle>();
+  gm::Geometry& g = h->g;
+  g.nx = cfg->nx; g.ny = cfg->ny; g.Lx = cfg->Lx; g.Ly = cfg->Ly; g.D = cfg->D; g.xc = cfg->xc; g.yc = cfg->yc;
+  g.nu = cfg->nu; g.rho = cfg->rho; g.U_inf = cfg->U_inf; g.inflow = cfg->inflow; g.U_m = cfg->U_m;
+  g.pressure_solver = cfg->pressure_solver; g.pressure_extension = cfg->pressure_extension;
+  g.velocity_interpolation = cfg->velocity_interpolation;
+  if (cfg->precision != 0) { g_create_error = "precision mode not built in this library"; return GM_ENOTIMPL; }
+  if (cfg->pressure_solver == 1) { g_create_error = "iterative pressure solver not built in this library"; return GM_ENOTIMPL; }
+  if (cfg->nx % 2 != 0) { g_create_error = "odd nx is not supported by the type-IV transform"; return GM_ENOTIMPL; }
+  int ec = 0;
+  if (!gm::build_geometry(g, ec)) { g_create_error = g.error; return ec ? ec : GM_EVALUE; }
+  gm_handle* H = h.get();
+  int rc = run_guarded(nullptr, [&] {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); throw CudaError("no CUDA device"); }
+    CK(cudaGetDevice(&H->device));
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, H->device));
+    H->smem_optin = (size_t)optin;
+    configure_kernels(optin);
+    CK(cudaGetLastError());
+    CK(cudaStreamCreateWithFlags(&H->st, cudaStreamNonBlocking));
+    cudaStream_t st = H->st;
+    H->F = g.usize + g.vsize;
+    H->Pn = g.psize;
+    build_class_maps(H);
+    H->mask.upload(g.mask, st);
+    H->inlet.upload(g.u_inlet, st);
+    // ghost stencils: u rows and v rows on the face grid
+    {
+      gm::Csr f;
+      std::vector<int64_t> rows;
+      for (size_t r = 0; r < g.gu_rows.size(); ++r) {
+        rows.push_back(g.gu_rows[r]);
+        for (int64_t e = g.gu.ptr[r]; e < g.gu.ptr[r + 1]; ++e) { f.col.push_back(g.gu.col[e]); f.val.push_back(g.gu.val[e]); }
+        f.ptr.push_back((int64_t)f.col.size());
+      }
+      for (size_t r = 0; r < g.gv_rows.size(); ++r) {
+        rows.push_back(g.usize + g.gv_rows[r]);
+        for (int64_t e = g.gv.ptr[r]; e < g.gv.ptr[r + 1]; ++e) { f.col.push_back(g.usize + g.gv.col[e]); f.val.push_back(g.gv.val[e]); }
+        f.ptr.push_back((int64_t)f.col.size());
+      }
+      upload_csr(H->gf, rows, f, st);
+    }
+    upload_csr(H->gp, g.gp_rows, g.gp, st);
+    upload_csr(H->irr[0], g.a_rows, g.a_irr, st);
+    H->a_nnz.upload(g.a_nnz_row, st);
+    H->sp_ptr.upload(g.surf_p.ptr, st); H->sp_col.upload(g.surf_p.col, st); H->sp_val.upload(g.surf_p.val, st);
+    H->su_ptr.upload(g.dudn.ptr, st); H->su_col.upload(g.dudn.col, st); H->su_val.upload(g.dudn.val, st);
+    H->sv_ptr.upload(g.dvdn.ptr, st); H->sv_col.upload(g.dvdn.col, st); H->sv_val.upload(g.dvdn.val, st);
+    H->nwx.upload(g.normal_wx, st); H->nwy.upload(g.normal_wy, st);
+    H->nxx.upload(g.normal_x, st); H->nyy.upload(g.normal_y, st);
+    H->d_ui.upload(g.ui, st); H->d_vi.upload(g.vi, st); H->d_pi.upload(g.pi, st);
+    for (DBuf<double>* b : {&H->U, &H->Unext, &H->hist, &H->now, &H->rhs, &H->star, &H->fres, &H->ffirst, &H->fw2,
+                            &H->fmid, &H->fhalf, &H->faction, &H->fproj, &H->fproj2, &H->ftmp}) {
+      b->alloc(H->F);
+      b->zero(st);
+    }
+    for (DBuf<double>* b : {&H->phalf, &H->phalf_next, &H->pout, &H->prhs, &H->pphi, &H->pres, &H->pfirst, &H->pw2,
+                            &H->pinc, &H->ptmp}) {
+      b->alloc(H->Pn);
+      b->zero(st);
+    }
+    H->spectral.alloc(std::max<int64_t>(H->Pn, (int64_t)g.ny * g.nx));
+    H->ctl.alloc(1);
+    H->ctl.zero(st);
+    H->state_max.alloc(2);
+    H->state_max.zero(st);
+    CK(cudaMallocHost(&H->host_ctl, sizeof(StepCtl)));
+    fill_case_dev(H);
+    build_rect_tables(H, H->rp, 0, 0.0);
+    build_schur(H, H->rp, g.schur_p_rows, g.schur_p_c, H->pw2.p);
+    CK(cudaMemsetAsync(H->pw2.p, 0, H->Pn * sizeof(double), st));
+    initial_state(H);
+  });
+  if (rc != GM_OK) return rc;
+  *out = h.release();
+  return GM_OK;
+}
+
+int gm_create_host(const gm_config* cfg, gm_handle** out) {
+  if (!cfg || !out) { g_create_error = "null argument"; return GM_EVALUE; }
+  *out = nullptr;
+  auto h = std::make_unique<gm_handle>();
+  gm::Geometry& g = h->g;
+  g.nx = cfg->nx; g.ny = cfg->ny; g.Lx = cfg->Lx; g.Ly = cfg->Ly; g.D = cfg->D; g.xc = cfg->xc; g.yc = cfg->yc;
+  g.nu = cfg->nu; g.rho = cfg->rho; g.U_inf = cfg->U_inf; g.inflow = cfg->inflow; g.U_m = cfg->U_m;
+  g.pressure_solver = cfg->pressure_solver; g.pressure_extension = cfg->pressure_extension;
+  g.velocity_interpolation = cfg->velocity_interpolation;
+  int ec = 0;
+  if (!gm::build_geometry(g, ec)) { g_create_error = g.error; return ec ? ec : GM_EVALUE; }
+  h->host_only = true;
+  *out = h.release();
+  return GM_OK;
+}
+
+int gm_prepare_dt(gm_handle* h, double dt) {
+  if (!h) return GM_EVALUE;
+  if (!(std::isfinite(dt) && dt > 0)) { h->err = "dt must be finite and positive"; return GM_EVALUE; }
+  return run_guarded(h, [&] { ensure_helmholtz(h, dt); });
+}
+
+int gm_destroy(gm_handle* h) {
+  if (!h) return GM_OK;
+  if (h->st) cudaStreamSynchronize(h->st);
+  if (h->host_ctl) cudaFreeHost(h->host_ctl);
+  cudaStream_t st = h->st;
+  bool own = h->own_stream;
+  delete h;
+  if (st && own) cudaStreamDestroy(st);
+  return GM_OK;
+}
+
+int gm_set_stream(gm_handle* h, void* stream) {
+  if (!h) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  return run_guarded(h, [&] {
+    CK(cudaStreamSynchronize(h->st));
+    if (h->own_stream) CK(cudaStreamDestroy(h->st));
+    h->st = (cudaStream_t)stream;
+    h->own_stream = false;
+  });
+}
+
+int gm_get_sizes(const gm_handle* h, gm_sizes* o) {
+  if (!h || !o) return GM_EVALUE;
+  const gm::Geometry& g = h->g;
+  o->nx = g.nx; o->ny = g.ny; o->usize = g.usize; o->vsize = g.vsize; o->psize = g.psize;
+  o->nu_active = (int64_t)g.ui.size(); o->nv_active = (int64_t)g.vi.size(); o->np_active = (int64_t)g.pi.size();
+  o->qsize = o->nu_active + o->nv_active;
+  o->n_surface = g.n_surface;
+  o->rank_p = (int64_t)g.schur_p_rows.size();
+  o->rank_u = h->helm_ready ? (int64_t)h->hs.schur_rows[0].size() : -1;
+  o->rank_v = h->helm_ready ? (int64_t)h->hs.schur_rows[1].size() : -1;
+  o->ghost_u = (int64_t)g.gu_rows.size(); o->ghost_v = (int64_t)g.gv_rows.size(); o->ghost_p = (int64_t)g.gp_rows.size();
+  o->dx = g.dx; o->dy = g.dy; o->U_ref = g.U_ref;
+  return GM_OK;
+}
+
+int gm_get_indices(const gm_handle* h, int64_t* ui, int64_t* vi, int64_t* pi) {
+  if (!h) return GM_EVALUE;
+  if (ui) std::copy(h->g.ui.begin(), h->g.ui.end(), ui);
+  if (vi) std::copy(h->g.vi.begin(), h->g.vi.end(), vi);
+  if (pi) std::copy(h->g.pi.begin(), h->g.pi.end(), pi);
+  return GM_OK;
+}
+
+int gm_get_ghost_stencils(const gm_handle* h, int32_t which, int64_t* n_rows, int64_t* nnz, int64_t* rows,
+                          int64_t* ptr, int64_t* cols, double* vals) {
+  if (!h || which < 0 || which > 2) return GM_EVALUE;
+  const gm::Geometry& g = h->g;
+  const std::vector<int64_t>& r = which == 0 ? g.gu_rows : (which == 1 ? g.gv_rows : g.gp_rows);
+  const gm::Csr& c = which == 0 ? g.gu : (which == 1 ? g.gv : g.gp);
+  if (n_rows) *n_rows = (int64_t)r.size();
+  if (nnz) *nnz = c.nnz();
+  if (rows) std::copy(r.begin(), r.end(), rows);
+  if (ptr) std::copy(c.ptr.begin(), c.ptr.end(), ptr);
+  if (cols) std::copy(c.col.begin(), c.col.end(), cols);
+  if (vals) std::copy(c.val.begin(), c.val.end(), vals);
+  return GM_OK;
+}
+
+int gm_get_schur_rows(const gm_handle* h, int32_t which, int64_t* n, int64_t* rows) {
+  if (!h || which < 0 || which > 2) return GM_EVALUE;
+  const std::vector<int64_t>* r = nullptr;
+  if (which == 0) r = &h->g.schur_p_rows;
+  else if (h->helm_ready) r = &h->hs.schur_rows[which - 1];
+  else { if (n) *n = -1; return GM_OK; }
+  if (n) *n = (int64_t)r->size();
+  if (rows) std::copy(r->begin(), r->end(), rows);
+  return GM_OK;
+}
+
+int gm_get_surface_points(const gm_handle* h, double* yx) {
+  if (!h || !yx) return GM_EVALUE;
+  for (int k = 0; k < h->g.n_surface; ++k) { yx[2 * k] = h->g.surf_y[k]; yx[2 * k + 1] = h->g.surf_x[k]; }
+  return GM_OK;
+}
+
+int gm_set_state(gm_handle* h, const double* u, const double* v, const double* p) {
+  if (!h) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  return run_guarded(h, [&] {
+    const gm::Geometry& g = h->g;
+    cudaStream_t st = h->st;
+    if (u || v) {
+      // the state is unpack(pack(u, v)): active entries taken, ghosts and inlet rebuilt
+      CK(cudaMemcpyAsync(h->ftmp.p, h->U.p, h->F * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if (u) CK(cudaMemcpyAsync(h->ftmp.p, dev_in(h, 0, u, g.usize), g.usize * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if (v) CK(cudaMemcpyAsync(h->ftmp.p + g.usize, dev_in(h, 1, v, g.vsize), g.vsize * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      Gate g0{nullptr, 0, 0};
+      launch_copy_active(h->cls_f.p, h->F, h->ftmp.p, h->U.p, g0, st);
+      launch_set_inlet(h->cd, h->U.p, false, st);
+      ghost_faces(h, h->U.p, g0);
+      CK(cudaMemsetAsync(h->state_max.p, 0, 2 * sizeof(unsigned long long), st));
+      launch_maxabs(h->cd, h->U.p, &h->state_max.p[0], &h->state_max.p[1], g0, st);
+    }
+    if (p) CK(cudaMemcpyAsync(h->pout.p, dev_in(h, 2, p, g.psize), g.psize * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    CK(cudaStreamSynchronize(st));
+  });
+}
+
+int gm_get_state(gm_handle* h, double* u, double* v, double* p) {
+  if (!h) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  return run_guarded(h, [&] {
+    const gm::Geometry& g = h->g;
+    cudaStream_t st = h->st;
+    if (u) {
+      if (is_device_ptr(u)) CK(cudaMemcpyAsync(u, h->U.p, g.usize * 8, cudaMemcpyDeviceToDevice, st));
+      else CK(cudaMemcpyAsync(u, h->U.p, g.usize * 8, cudaMemcpyDeviceToHost, st));
+    }
+    if (v) {
+      if (is_device_ptr(v)) CK(cudaMemcpyAsync(v, h->U.p + g.usize, g.vsize * 8, cudaMemcpyDeviceToDevice, st));
+      else CK(cudaMemcpyAsync(v, h->U.p + g.usize, g.vsize * 8, cudaMemcpyDeviceToHost, st));
+    }
+    if (p) {
+      if (is_device_ptr(p)) CK(cudaMemcpyAsync(p, h->pout.p, g.psize * 8, cudaMemcpyDeviceToDevice, st));
+      else CK(cudaMemcpyAsync(p, h->pout.p, g.psize * 8, cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+  });
+}
+
+int gm_set_inlet(gm_handle* h, const double* u_inlet) {
+  if (!h || !u_inlet) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  return run_guarded(h, [&] {
+    CK(cudaMemcpyAsync(h->inlet.p, dev_in(h, 0, u_inlet, h->g.ny), h->g.ny * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    launch_set_inlet(h->cd, h->U.p, false, h->st);
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+int gm_set_history(gm_handle* h, int32_t has_history, const double* prev_adv, const double* half_p, double prev_dt) {
+  if (!h) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  return run_guarded(h, [&] {
+    if (!has_history) { h->has_history = false; h->prev_dt = 0; return; }
+    if (!prev_adv || !half_p || !(std::isfinite(prev_dt) && prev_dt > 0))
+      throw GateError(GM_EVALUE, "AB2 history requires advection, half pressure and a finite positive previous timestep");
+    const gm::Geometry& g = h->g;
+    cudaStream_t st = h->st;
+    const int64_t nu = (int64_t)g.ui.size(), nv = (int64_t)g.vi.size(), np = (int64_t)g.pi.size();
+    const double* q = dev_in(h, 0, prev_adv, nu + nv);
+    CK(cudaMemsetAsync(h->hist.p, 0, h->F * sizeof(double), st));
+    launch_scatter(q, h->d_ui.p, nu, h->hist.p, st);
+    launch_scatter(q + nu, h->d_vi.p, nv, h->hist.p + g.usize, st);
+    const double* ph = dev_in(h, 1, half_p, np);
+    CK(cudaMemsetAsync(h->phalf.p, 0, h->Pn * sizeof(double), st));
+    launch_scatter(ph, h->d_pi.p, np, h->phalf.p, st);
+    CK(cudaStreamSynchronize(st));
+    h->has_history = true;
+    h->prev_dt = prev_dt;
+  });
+}
+
+int gm_get_history(gm_handle* h, int32_t* has_history, double* prev_adv, double* half_p, double* prev_dt) {
+  if (!h) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  return run_guarded(h, [&] {
+    if (has_history) *has_history = h->has_history ? 1 : 0;
+    if (prev_dt) *prev_dt = h->prev_dt;
+    if (!h->has_history) return;
+    const gm::Geometry& g = h->g;
+    const int64_t nu = (int64_t)g.ui.size(), nv = (int64_t)g.vi.size(), np = (int64_t)g.pi.size();
+    if (prev_adv) {
+      DevOut o(h, 0, prev_adv, nu + nv);
+      launch_gather(h->hist.p, h->d_ui.p, nu, o.dev, h->st);
+      launch_gather(h->hist.p + g.usize, h->d_vi.p, nv, o.dev + nu, h->st);
+      o.finish();
+    }
+    if (half_p) {
+      DevOut o(h, 1, half_p, np);
+      launch_gather(h->phalf.p, h->d_pi.p, np, o.dev, h->st);
+      o.finish();
+    }
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+int gm_step(gm_handle* h, double dt, int32_t n_steps, int64_t first_step_index, double start_time,
+            gm_step_diag* diag) {
+  if (!h) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  if (!(std::isfinite(dt) && dt > 0) || n_steps <= 0) { h->err = "dt must be finite and positive"; return GM_EVALUE; }
+  return run_guarded(h, [&] {
+    ensure_helmholtz(h, dt);
+    for (int s = 0; s < n_steps; ++s) {
+      bool first = !h->has_history;
+      bool screen = ((first_step_index + s) % 100) == 0;
+      step_once(h, dt, screen);
+      CK(cudaMemcpyAsync(h->host_ctl, h->ctl.p, sizeof(StepCtl), cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+      double t = start_time + (s + 1) * dt;
+      if (diag) fill_diag(h, *h->host_ctl, t, dt, first, &diag[s]);
+      if (h->host_ctl->err) check_ctl(h, "step");
+      commit_step(h, dt);
+    }
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+int gm_apply(gm_handle* h, int32_t op, double param, const double* x, double* y) {
+  if (!h || !x || !y) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  return run_guarded(h, [&] {
+    const gm::Geometry& g = h->g;
+    cudaStream_t st = h->st;
+    const int64_t nu = (int64_t)g.ui.size(), nv = (int64_t)g.vi.size(), np = (int64_t)g.pi.size(), nq = nu + nv;
+    Gate g0{nullptr, 0, 0};
+    auto unpack_into = [&](const double* q, double* F) {
+      CK(cudaMemsetAsync(F, 0, h->F * sizeof(double), st));
+      launch_scatter(q, h->d_ui.p, nu, F, st);
+      launch_scatter(q + nu, h->d_vi.p, nv, F + g.usize, st);
+      launch_set_inlet(h->cd, F, false, st);
+      ghost_faces(h, F, g0);
+    };
+    auto pack_from = [&](const double* F, double* q) {
+      launch_gather(F, h->d_ui.p, nu, q, st);
+      launch_gather(F + g.usize, h->d_vi.p, nv, q + nu, st);
+    };
+    switch (op) {
+      case GM_OP_PACK: {
+        const double* F = dev_in(h, 0, x, h->F);
+        DevOut o(h, 1, y, nq);
+        pack_from(F, o.dev);
+        o.finish();
+        break;
+      }
+      case GM_OP_UNPACK: {
+        const double* q = dev_in(h, 0, x, nq);
+        DevOut o(h, 1, y, h->F);
+        unpack_into(q, o.dev);
+        o.finish();
+        break;
+      }
+      case GM_OP_ADVECTION:
+      case GM_OP_DIFFUSION:
+      case GM_OP_H_MATVEC: {
+        const double* q = dev_in(h, 0, x, nq);
+        unpack_into(q, h->ftmp.p);
+        if (op == GM_OP_ADVECTION) launch_advection(h->cd, h->ftmp.p, h->fmid.p, g0, st);
+        else if (op == GM_OP_DIFFUSION) launch_diffusion(h->cd, h->ftmp.p, h->fmid.p, true, 0.0, g0, st);
+        else launch_diffusion(h->cd, h->ftmp.p, h->fmid.p, false, 0.5 * param, g0, st);
+        DevOut o(h, 1, y, nq);
+        pack_from(h->fmid.p, o.dev);
+        o.finish();
+        break;
+      }
+      case GM_OP_GRADIENT:
+      case GM_OP_PRESSURE_EXTEND: {
+        const double* pp = dev_in(h, 0, x, np);
+        CK(cudaMemsetAsync(h->ptmp.p, 0, h->Pn * sizeof(double), st));
+        launch_scatter(pp, h->d_pi.p, np, h->ptmp.p, st);
+        ghost_p(h, h->ptmp.p, g0);
+        if (op == GM_OP_GRADIENT) {
+          launch_gradient(h->cd, h->ptmp.p, h->fmid.p, g0, st);
+          DevOut o(h, 1, y, nq);
+          pack_from(h->fmid.p, o.dev);
+          o.finish();
+        } else {
+          DevOut o(h, 1, y, h->Pn);
+          CK(cudaMemcpyAsync(o.dev, h->ptmp.p, h->Pn * sizeof(double), cudaMemcpyDeviceToDevice, st));
+          o.finish();
+        }
+        break;
+      }
+      case GM_OP_DIVERGENCE: {
+        const double* q = dev_in(h, 0, x, nq);
+        unpack_into(q, h->ftmp.p);
+        launch_divergence(h->cd, h->ftmp.p, h->ptmp.p, 0.0, nullptr, nullptr, 0, g0, st);
+        DevOut o(h, 1, y, np);
+        launch_gather(h->ptmp.p, h->d_pi.p, np, o.dev, st);
+        o.finish();
+        break;
+      }
+      default:
+        throw GateError(GM_EVALUE, "unknown operator");
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+  });
+}
+
+static void solve_info_from(gm_handle* h, int slot, gm_solve_info* info) {
+  if (!info) return;
+  const SolveCtl& sc = h->host_ctl->solve[slot];
+  double b = bits2d(sc.bmax), tg = std::max(1e-10, 32 * 2.220446049250313e-16 * std::max(1.0, b));
+  int k = 0;
+  if (bits2d(sc.rmax[0]) > tg) { k = 1; if (bits2d(sc.rmax[1]) > tg) k = 2; }
+  double bound = bits2d(sc.bound[k]);
+  double t64 = std::max(1e-10, 64 * 2.220446049250313e-16 * std::max(1.0, b));
+  info->residual_linf = bits2d(sc.rmax[k]);
+  info->residual_relative_l2 = std::sqrt(sc.rsq[k]) / std::max(std::sqrt(sc.bsq), 2.2250738585072014e-308);
+  info->roundoff_bound_linf = bound;
+  info->residual_target_linf = std::max(t64, bound);
+  info->backward_error_linf = 0;
+  info->iterations = 0;
+  info->refinement_iterations = k;
+  info->status = 0;
+  info->rank = (int32_t)h->rp.rank;
+}
+
+int gm_project(gm_handle* h, double dt, const double* q, double* q_out, double* phi, gm_solve_info* info) {
+  if (!h || !q) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  return run_guarded(h, [&] {
+    const gm::Geometry& g = h->g;
+    cudaStream_t st = h->st;
+    const int64_t nu = (int64_t)g.ui.size(), nv = (int64_t)g.vi.size(), np = (int64_t)g.pi.size(), nq = nu + nv;
+    const double* qd = dev_in(h, 0, q, nq);
+    CK(cudaMemsetAsync(h->fmid.p, 0, h->F * sizeof(double), st));
+    launch_scatter(qd, h->d_ui.p, nu, h->fmid.p, st);
+    launch_scatter(qd + nu, h->d_vi.p, nv, h->fmid.p + g.usize, st);
+    CK(cudaMemsetAsync(h->ctl.p, 0, sizeof(StepCtl), st));
+    project(h, h->fmid.p, dt, h->fproj2.p, h->pinc.p, S_P1, 1);
+    CK(cudaMemcpyAsync(h->host_ctl, h->ctl.p, sizeof(StepCtl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    solve_info_from(h, S_P1, info);
+    check_ctl(h, "project");
+    if (q_out) {
+      DevOut o(h, 1, q_out, nq);
+      launch_gather(h->fproj2.p, h->d_ui.p, nu, o.dev, st);
+      launch_gather(h->fproj2.p + g.usize, h->d_vi.p, nv, o.dev + nu, st);
+      o.finish();
+    }
+    if (phi) {
+      DevOut o(h, 2, phi, np);
+      launch_gather(h->pinc.p, h->d_pi.p, np, o.dev, st);
+      o.finish();
+    }
+    CK(cudaStreamSynchronize(st));
+  });
+}
+
+int gm_pressure_solve(gm_handle* h, const double* rhs, double* phi, gm_solve_info* info) {
+  if (!h || !rhs || !phi) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  return run_guarded(h, [&] {
+    const gm::Geometry& g = h->g;
+    cudaStream_t st = h->st;
+    const int64_t np = (int64_t)g.pi.size();
+    const double* b = dev_in(h, 0, rhs, np);
+    CK(cudaMemsetAsync(h->prhs.p, 0, h->Pn * sizeof(double), st));
+    launch_scatter(b, h->d_pi.p, np, h->prhs.p, st);
+    CK(cudaMemsetAsync(h->ctl.p, 0, sizeof(StepCtl), st));
+    schur_solve(h, h->rp, 0, 0.0, h->prhs.p, h->pphi.p, h->pres.p, h->pfirst.p, h->pw2.p, S_P1);
+    launch_gate_pressure(h->ctl.p, S_P1, st);
+    CK(cudaMemcpyAsync(h->host_ctl, h->ctl.p, sizeof(StepCtl), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    solve_info_from(h, S_P1, info);
+    check_ctl(h, "pressure solve");
+    DevOut o(h, 1, phi, np);
+    launch_gather(h->pphi.p, h->d_pi.p, np, o.dev, st);
+    o.finish();
+    CK(cudaStreamSynchronize(st));
+  });
+}
+
+int gm_rectangle_solve(gm_handle* h, int32_t kind, double dt, const double* b, double* x) {
+  if (!h || !b || !x || kind < 0 || kind > 2) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  return run_guarded(h, [&] {
+    if (kind > 0) ensure_helmholtz(h, dt);
+    RectDev& rd = kind == 0 ? h->rp : (kind == 1 ? h->ru : h->rv);
+    const int64_t n = (int64_t)rd.view.rows * rd.view.cols;
+    const double* bd = dev_in(h, 0, b, n);
+    RectView dense = rd.view;
+    dense.base = 0;
+    dense.pitch = dense.cols;
+    dense.cls = nullptr;
+    DevOut o(h, 1, x, n);
+    launch_rect_inverse(rd.tt, dense, bd, false, h->spectral.p, o.dev, nullptr, nullptr, Gate{nullptr, 0, 0}, h->st);
+    o.finish();
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->st));
+  });
+}
+
+int gm_surface_forces(gm_handle* h, const double* u, const double* v, const double* p, double mu, double out[6]) {
+  if (!h || !u || !v || !p || !out) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  return run_guarded(h, [&] {
+    const gm::Geometry& g = h->g;
+    cudaStream_t st = h->st;
+    CK(cudaMemcpyAsync(h->ftmp.p, dev_in(h, 0, u, g.usize), g.usize * 8, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(h->ftmp.p + g.usize, dev_in(h, 1, v, g.vsize), g.vsize * 8, cudaMemcpyDeviceToDevice, st));
+    const double* pd = dev_in(h, 2, p, g.psize);
+    DBuf<double> o6;
+    o6.alloc(6);
+    launch_forces(h->cd, h->ftmp.p, pd, mu, 0.0, nullptr, 0, o6.p, Gate{nullptr, 0, 0}, st);
+    CK(cudaMemcpyAsync(out, o6.p, 6 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  });
+}
+
+int gm_divergence_stats(gm_handle* h, const double* u, const double* v, double out[3], int64_t counts[2]) {
+  if (!h || !u || !v || !out || !counts) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  return run_guarded(h, [&] {
+    const gm::Geometry& g = h->g;
+    cudaStream_t st = h->st;
+    CK(cudaMemcpyAsync(h->ftmp.p, dev_in(h, 0, u, g.usize), g.usize * 8, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(h->ftmp.p + g.usize, dev_in(h, 1, v, g.vsize), g.vsize * 8, cudaMemcpyDeviceToDevice, st));
+    DBuf<double> o5;
+    o5.alloc(5);
+    o5.zero(st);
+    launch_divergence_stats(h->cd, h->ftmp.p, h->mask.p, o5.p, st);
+    double r[5];
+    CK(cudaMemcpyAsync(r, o5.p, sizeof r, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    unsigned long long mb;
+    std::memcpy(&mb, &r[0], 8);
+    out[0] = bits2d(mb);
+    out[1] = r[1];
+    out[2] = r[3];
+    counts[0] = (int64_t)std::llround(r[2]);
+    counts[1] = (int64_t)std::llround(r[4]);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,837 @@
+// Kernels of the ghost-cell AB2/CN step (sm_103a).  See kernels.cuh for the layout.
+#include <cmath>
+#include <cstdio>
+
+#include "kernels.cuh"
+
+namespace gmk {
+
+static constexpr int TPB = 256;
+static constexpr double EPS64 = 2.220446049250313e-16;
+
+// ---------------------------------------------------------------------------
+// reductions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+// Block-wide max of non-negative doubles (as bits) and optional sum; thread 0 commits atomically.
+__device__ void block_commit_max(unsigned long long v, unsigned long long* dst) {
+  __shared__ unsigned long long sm[32];
+  v = warp_max_u64(v);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sm[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    v = lane < nw ? sm[lane] : 0ull;
+    v = warp_max_u64(v);
+    if (lane == 0 && v) atomicMax(dst, v);
+  }
+}
+__device__ void block_commit_sum(double v, double* dst) {
+  __shared__ double sm[32];
+  v = warp_sum(v);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sm[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    v = lane < nw ? sm[lane] : 0.0;
+    v = warp_sum(v);
+    if (lane == 0 && v != 0.0) atomicAdd(dst, v);
+  }
+}
+__device__ __forceinline__ unsigned long long absbits(double v) { return dbits(fabs(v)); }
+
+static inline unsigned blocks_for(int64_t n, int tpb = TPB) { return (unsigned)((n + tpb - 1) / tpb); }
+
+// ---------------------------------------------------------------------------
+// separable inverse: x pass (rows) and y pass (columns with eigenvalue scaling)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_xpass(int n, int rows, int type, FftPlan plan, R2RTables<T> tb, const double* __restrict__ in,
+                        int64_t ibase, int64_t ipitch, const uint8_t* __restrict__ icls, double* __restrict__ out,
+                        int64_t obase, int64_t opitch, const uint8_t* __restrict__ ocls, const double* __restrict__ sub,
+                        const double* __restrict__ add, int lpb, Gate gate) {
+  if (!gate_open(gate)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int l0 = blockIdx.x * lpb;
+  const int nl = min(lpb, rows - l0);
+  T* stage = reinterpret_cast<T*>(smem_raw);
+  size_t stage_bytes = ((size_t)lpb * n * sizeof(T) + 15) / 16 * 16;
+  cplx<T>* a = reinterpret_cast<cplx<T>*>(smem_raw + stage_bytes);
+  cplx<T>* b = a + r2r_buffer_elems(type, n, lpb);
+  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
+    int l = t / n, e = t - l * n;
+    int64_t fi = ibase + (int64_t)(l0 + l) * ipitch + e;
+    double v = in[fi];
+    if (icls && !(icls[fi] & CLS_ACTIVE)) v = 0.0;
+    stage[t] = (T)v;
+  }
+  __syncthreads();
+  r2r_lines<T>(type, stage, n, nl, a, b, plan, tb);
+  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
+    int l = t / n, e = t - l * n;
+    int64_t fo = obase + (int64_t)(l0 + l) * opitch + e;
+    double v = (double)stage[t];
+    if (sub) {
+      if (ocls && !(ocls[fo] & CLS_ACTIVE)) { out[fo] = 0.0; continue; }
+      double d = sub[fo] - v;
+      out[fo] = add ? add[fo] + d : d;
+    } else {
+      out[fo] = v;
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_ypass(int n /*rows*/, int cols, int tf, int ti, FftPlan plan, R2RTables<T> tb,
+                        const double* __restrict__ recip, double* __restrict__ S, int lpb, Gate gate) {
+  if (!gate_open(gate)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int c0 = blockIdx.x * lpb;
+  const int nl = min(lpb, cols - c0);
+  T* stage = reinterpret_cast<T*>(smem_raw);
+  size_t stage_bytes = ((size_t)lpb * n * sizeof(T) + 15) / 16 * 16;
+  cplx<T>* a = reinterpret_cast<cplx<T>*>(smem_raw + stage_bytes);
+  cplx<T>* b = a + r2r_buffer_elems(tf, n, lpb);
+  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
+    int l = t % nl, e = t / nl;
+    stage[l * n + e] = (T)S[(int64_t)e * cols + c0 + l];
+  }
+  __syncthreads();
+  r2r_lines<T>(tf, stage, n, nl, a, b, plan, tb);
+  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
+    int l = t % nl, e = t / nl;
+    stage[l * n + e] = stage[l * n + e] * (T)recip[(int64_t)e * cols + c0 + l];
+  }
+  __syncthreads();
+  r2r_lines<T>(ti, stage, n, nl, a, b, plan, tb);
+  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
+    int l = t % nl, e = t / nl;
+    S[(int64_t)e * cols + c0 + l] = (double)stage[l * n + e];
+  }
+}
+
+void configure_kernels(int smem_optin) {
+  cudaFuncSetAttribute(k_xpass<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin);
+  cudaFuncSetAttribute(k_ypass<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin);
+  cudaFuncSetAttribute(k_xpass<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin);
+  cudaFuncSetAttribute(k_ypass<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin);
+}
+
+void launch_rect_inverse(const TransformTables& tt, const RectView& v, const double* b, bool mask_in,
+                         double* spectral, double* out, const double* sub, const double* add, const Gate& gate,
+                         cudaStream_t st) {
+  using C = cplx<double>;
+  R2RTables<double> tx{(const C*)tt.Wx, (const C*)tt.prex, (const C*)tt.postx};
+  R2RTables<double> txi{(const C*)tt.Wx, (const C*)tt.prex_inv, (const C*)tt.postx_inv};
+  R2RTables<double> ty{(const C*)tt.Wy, (const C*)tt.prey, (const C*)tt.posty};
+  unsigned gx = (unsigned)((v.rows + tt.lpb_x - 1) / tt.lpb_x);
+  k_xpass<double><<<gx, 128, tt.smem_x, st>>>(v.cols, v.rows, tt.tx_fwd, tt.plan_x, tx, b, v.base, v.pitch,
+                                              mask_in ? v.cls : nullptr, spectral, 0, v.cols, nullptr, nullptr,
+                                              nullptr, tt.lpb_x, gate);
+  unsigned gy = (unsigned)((v.cols + tt.lpb_y - 1) / tt.lpb_y);
+  k_ypass<double><<<gy, 128, tt.smem_y, st>>>(v.rows, v.cols, tt.ty_fwd, tt.ty_inv, tt.plan_y, ty, tt.recip,
+                                              spectral, tt.lpb_y, gate);
+  k_xpass<double><<<gx, 128, tt.smem_x, st>>>(v.cols, v.rows, tt.tx_inv, tt.plan_x, txi, spectral, 0, v.cols,
+                                              nullptr, out, v.base, v.pitch, v.cls, sub, add, tt.lpb_x, gate);
+}
+
+// ---------------------------------------------------------------------------
+// boundary Schur correction: c = S^{-1} (C first), scattered into w2
+// ---------------------------------------------------------------------------
+static constexpr int SCHUR_ROWS = 16;
+__global__ void k_schur(const double* __restrict__ first, RectView v, int rank, const int64_t* __restrict__ rows,
+                        const int64_t* __restrict__ cp, const int64_t* __restrict__ cc, const double* __restrict__ cv,
+                        const double* __restrict__ sinv, double* __restrict__ w2, Gate gate) {
+  if (!gate_open(gate)) return;
+  extern __shared__ double y[];
+  for (int k = threadIdx.x; k < rank; k += blockDim.x) {
+    double acc = 0.0;
+    for (int64_t e = cp[k]; e < cp[k + 1]; ++e) {
+      int64_t rc = cc[e];
+      int64_t fi = v.base + (rc / v.cols) * v.pitch + (rc % v.cols);
+      acc += cv[e] * first[fi];
+    }
+    y[k] = acc;
+  }
+  __syncthreads();
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  int r0 = blockIdx.x * SCHUR_ROWS;
+  for (int r = r0 + warp; r < min(rank, r0 + SCHUR_ROWS); r += nw) {
+    double acc = 0.0;
+    for (int k = lane; k < rank; k += 32) acc += sinv[(int64_t)r * rank + k] * y[k];
+    acc = warp_sum(acc);
+    if (lane == 0) {
+      int64_t rc = rows[r];
+      w2[v.base + (rc / v.cols) * v.pitch + (rc % v.cols)] = acc;
+    }
+  }
+}
+
+void launch_schur(const double* first, const RectView& view, int rank, const int64_t* rows, const int64_t* c_ptr,
+                  const int64_t* c_col, const double* c_val, const double* sinv, double* w2, const Gate& gate,
+                  cudaStream_t st) {
+  if (rank <= 0) return;
+  unsigned g = (unsigned)((rank + SCHUR_ROWS - 1) / SCHUR_ROWS);
+  k_schur<<<g, 256, rank * sizeof(double), st>>>(first, view, rank, rows, c_ptr, c_col, c_val, sinv, w2, gate);
+}
+
+// ---------------------------------------------------------------------------
+// ghost extension rows
+// ---------------------------------------------------------------------------
+__global__ void k_ghost(double* __restrict__ f, int n, const int64_t* __restrict__ rows, const int64_t* __restrict__ ptr,
+                        const int64_t* __restrict__ col, const double* __restrict__ val, Gate gate) {
+  if (!gate_open(gate)) return;
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  double acc = 0.0;
+  for (int64_t e = ptr[r]; e < ptr[r + 1]; ++e) acc += val[e] * f[col[e]];
+  f[rows[r]] = acc;
+}
+
+void launch_ghost(double* field, int n, const int64_t* rows, const int64_t* ptr, const int64_t* col,
+                  const double* val, const Gate& gate, cudaStream_t st) {
+  if (n <= 0) return;
+  k_ghost<<<blocks_for(n, 128), 128, 0, st>>>(field, n, rows, ptr, col, val, gate);
+}
+
+// ---------------------------------------------------------------------------
+// stencils on the staggered grid
+// ---------------------------------------------------------------------------
+struct Grid {
+  int nx, ny;
+  int64_t usize;
+  __device__ __forceinline__ int64_t u(int j, int i) const { return (int64_t)j * (nx + 1) + i; }
+  __device__ __forceinline__ int64_t v(int j, int i) const { return usize + (int64_t)j * nx + i; }
+  __device__ __forceinline__ int64_t p(int j, int i) const { return (int64_t)j * nx + i; }
+};
+
+// -N(u) at u face (j,i), i>=1, before /(dx dy) (solver/numba_kernels.py:17-74 with nu=0)
+__device__ __forceinline__ double adv_u(const double* __restrict__ U, const Grid& g, int j, int i, double dx, double dy) {
+  const int nx = g.nx, ny = g.ny;
+  auto fxy = [&](int jj, int ii) -> double {  // corner flux at (jj, ii), jj in [0, ny]
+    if (jj == 0 || jj == ny) return 0.0;
+    double vf;
+    if (ii == 0) vf = U[g.v(jj, 0)];
+    else if (ii == nx) vf = U[g.v(jj, nx - 1)];
+    else vf = 0.5 * (U[g.v(jj, ii - 1)] + U[g.v(jj, ii)]);
+    double ua = 0.5 * (U[g.u(jj - 1, ii)] + U[g.u(jj, ii)]);
+    return -((vf * ua) * dx);
+  };
+  double uW = U[g.u(j, i - 1)], uC = U[g.u(j, i)];
+  double fl = 0.5 * (uW + uC);
+  double fxxW = -((fl * fl) * dy);
+  if (i < nx) {
+    double fr = 0.5 * (uC + U[g.u(j, i + 1)]);
+    double fxxE = -((fr * fr) * dy);
+    return (fxxE - fxxW) + (fxy(j + 1, i) - fxy(j, i));
+  }
+  return (-uC * uC) * dy - fxxW + 0.5 * (fxy(j + 1, nx) - fxy(j, nx));
+}
+
+// -N(v) at v face (j,i), 1<=j<=ny-1 (solver/numba_kernels.py:77-142 with nu=0)
+__device__ __forceinline__ double adv_v(const double* __restrict__ U, const Grid& g, int j, int i, double dx, double dy) {
+  const int nx = g.nx;
+  auto fyx = [&](int jj, int ii) -> double {  // corner flux at (jj, ii), ii in [0, nx]
+    if (ii == 0) return 0.0;
+    double uf = 0.5 * (U[g.u(jj - 1, ii)] + U[g.u(jj, ii)]);
+    if (ii == nx) return (-uf * U[g.v(jj, nx - 1)]) * dy;
+    double va = 0.5 * (U[g.v(jj, ii - 1)] + U[g.v(jj, ii)]);
+    return -((uf * va) * dy);
+  };
+  double vS = U[g.v(j - 1, i)], vC = U[g.v(j, i)], vN = U[g.v(j + 1, i)];
+  double fb = 0.5 * (vS + vC), ft = 0.5 * (vC + vN);
+  double fyyS = -((fb * fb) * dx), fyyN = -((ft * ft) * dx);
+  return (fyx(j, i + 1) - fyx(j, i)) + (fyyN - fyyS);
+}
+
+// nu * raw_l (5-point with channel-wall, inlet and outlet rules) at a u face (solver/optimized_ghost_cell.py:116-120)
+__device__ __forceinline__ double lap_u(const double* __restrict__ U, const Grid& g, int j, int i, double idx2, double idy2,
+                                        bool inlet) {
+  const int nx = g.nx, ny = g.ny;
+  double acc = 0.0;
+  if (j > 0) acc += idy2 * U[g.u(j - 1, i)];
+  if (i > 1 || inlet) acc += (i == nx ? 2.0 * idx2 : idx2) * U[g.u(j, i - 1)];
+  acc += (-2.0 * idx2 - ((j == 0 || j == ny - 1) ? 3.0 : 2.0) * idy2) * U[g.u(j, i)];
+  if (i < nx) acc += idx2 * U[g.u(j, i + 1)];
+  if (j < ny - 1) acc += idy2 * U[g.u(j + 1, i)];
+  return acc;
+}
+// at a v face (solver/optimized_ghost_cell.py:121-123); walls v=0 are stored as zeros
+__device__ __forceinline__ double lap_v(const double* __restrict__ U, const Grid& g, int j, int i, double idx2, double idy2) {
+  const int nx = g.nx;
+  double acc = idy2 * U[g.v(j - 1, i)];
+  if (i > 0) acc += idx2 * U[g.v(j, i - 1)];
+  acc += (-(i == 0 ? 3.0 : (i == nx - 1 ? 1.0 : 2.0)) * idx2 - 2.0 * idy2) * U[g.v(j, i)];
+  if (i < nx - 1) acc += idx2 * U[g.v(j, i + 1)];
+  acc += idy2 * U[g.v(j + 1, i)];
+  return acc;
+}
+// G p at faces from a pressure grid with ghost values (solver/optimized_ghost_cell.py:94-107)
+__device__ __forceinline__ double grad_u(const double* __restrict__ P, const Grid& g, int j, int i, double gx) {
+  if (i < g.nx) return gx * P[g.p(j, i)] - gx * P[g.p(j, i - 1)];
+  return (-2.0 * gx) * P[g.p(j, g.nx - 1)];
+}
+__device__ __forceinline__ double grad_v(const double* __restrict__ P, const Grid& g, int j, int i, double gy) {
+  return gy * P[g.p(j, i)] - gy * P[g.p(j - 1, i)];
+}
+
+// decode a face-grid thread index
+__device__ __forceinline__ bool face_of(int64_t t, const Grid& g, int& comp, int& j, int& i) {
+  if (t < g.usize) { comp = 0; j = (int)(t / (g.nx + 1)); i = (int)(t % (g.nx + 1)); return true; }
+  int64_t r = t - g.usize;
+  if (r >= (int64_t)(g.ny + 1) * g.nx) return false;
+  comp = 1; j = (int)(r / g.nx); i = (int)(r % g.nx);
+  return true;
+}
+
+__global__ void k_momentum(CaseDev c, MomentumArgs a, Gate gate) {
+  if (!gate_open(gate)) return;
+  const Grid g{c.nx, c.ny, c.usize};
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int comp, j, i;
+  if (!face_of(t, g, comp, j, i)) return;
+  const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
+  if (!(cls & CLS_ACTIVE)) {
+    double z = (comp == 0 && i == 0) ? c.inlet[j] : 0.0;
+    if (a.mode != 2 && a.now) a.now[t] = 0.0;
+    a.out[t] = a.mode == 1 ? z : 0.0;
+    return;
+  }
+  const double dx = c.dx, dy = c.dy, idx2 = 1.0 / (dx * dx), idy2 = 1.0 / (dy * dy);
+  const double inv_area = 1.0 / (dx * dy);
+  double q = a.U[t];
+  double lq, gp, now = 0.0, off = 0.0;
+  if (comp == 0) {
+    lq = c.nu * lap_u(a.U, g, j, i, idx2, idy2, true);
+    gp = grad_u(a.P, g, j, i, (1.0 / dx) / c.rho);
+    if (a.mode != 2) {
+      now = adv_u(a.U, g, j, i, dx, dy) / (dx * dy);
+      if (i == c.nx) now *= 2;
+    }
+    if (i == 1) off = c.nu * (idx2 * c.inlet[j]);
+  } else {
+    lq = c.nu * lap_v(a.U, g, j, i, idx2, idy2);
+    gp = grad_v(a.P, g, j, i, (1.0 / dy) / c.rho);
+    if (a.mode != 2) now = adv_v(a.U, g, j, i, dx, dy) / (dx * dy);
+  }
+  (void)inv_area;
+  if (a.mode == 1) {
+    a.now[t] = now;
+    a.out[t] = q + (0.5 * a.dt) * ((now + lq) - gp);
+    return;
+  }
+  double expl;
+  if (a.mode == 0) {
+    expl = (1.0 + a.alpha) * now - a.alpha * a.prev[t];
+    a.now[t] = now;
+  } else {
+    if (comp == 0) {
+      expl = adv_u(a.Uhalf, g, j, i, dx, dy) / (dx * dy);
+      if (i == c.nx) expl *= 2;
+    } else {
+      expl = adv_v(a.Uhalf, g, j, i, dx, dy) / (dx * dy);
+    }
+  }
+  a.out[t] = q + a.dt * (expl + 0.5 * lq - gp) + (0.5 * a.dt) * off;
+}
+
+void launch_momentum(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st) {
+  k_momentum<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, gate);
+}
+
+__global__ void k_advection(CaseDev c, const double* __restrict__ U, double* __restrict__ out, Gate gate) {
+  if (!gate_open(gate)) return;
+  const Grid g{c.nx, c.ny, c.usize};
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int comp, j, i;
+  if (!face_of(t, g, comp, j, i)) return;
+  const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
+  if (!(cls & CLS_ACTIVE)) { out[t] = 0.0; return; }
+  double r;
+  if (comp == 0) {
+    r = adv_u(U, g, j, i, c.dx, c.dy) / (c.dx * c.dy);
+    if (i == c.nx) r *= 2;
+  } else {
+    r = adv_v(U, g, j, i, c.dx, c.dy) / (c.dx * c.dy);
+  }
+  out[t] = r;
+}
+void launch_advection(const CaseDev& c, const double* U, double* out, const Gate& gate, cudaStream_t st) {
+  k_advection<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, U, out, gate);
+}
+
+__global__ void k_diffusion(CaseDev c, const double* __restrict__ U, double* __restrict__ out, int with_inlet,
+                            double hdt, Gate gate) {
+  if (!gate_open(gate)) return;
+  const Grid g{c.nx, c.ny, c.usize};
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int comp, j, i;
+  if (!face_of(t, g, comp, j, i)) return;
+  const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
+  if (!(cls & CLS_ACTIVE)) { out[t] = 0.0; return; }
+  const double idx2 = 1.0 / (c.dx * c.dx), idy2 = 1.0 / (c.dy * c.dy);
+  double l = comp == 0 ? c.nu * lap_u(U, g, j, i, idx2, idy2, with_inlet != 0) : c.nu * lap_v(U, g, j, i, idx2, idy2);
+  out[t] = hdt == 0.0 ? l : U[t] - hdt * l;
+}
+void launch_diffusion(const CaseDev& c, const double* U, double* out, bool with_inlet, double hdt, const Gate& gate,
+                      cudaStream_t st) {
+  k_diffusion<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, U, out, with_inlet ? 1 : 0, hdt, gate);
+}
+
+__global__ void k_gradient(CaseDev c, const double* __restrict__ P, double* __restrict__ out, Gate gate) {
+  if (!gate_open(gate)) return;
+  const Grid g{c.nx, c.ny, c.usize};
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int comp, j, i;
+  if (!face_of(t, g, comp, j, i)) return;
+  const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
+  if (!(cls & CLS_ACTIVE)) { out[t] = 0.0; return; }
+  out[t] = comp == 0 ? grad_u(P, g, j, i, (1.0 / c.dx) / c.rho) : grad_v(P, g, j, i, (1.0 / c.dy) / c.rho);
+}
+void launch_gradient(const CaseDev& c, const double* P, double* out, const Gate& gate, cudaStream_t st) {
+  k_gradient<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, P, out, gate);
+}
+
+// ---------------------------------------------------------------------------
+// residual of the pressure operator A or the Helmholtz operators
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int find_row(const int64_t* rows, int n, int64_t key) {
+  int lo = 0, hi = n - 1;
+  while (lo <= hi) {
+    int mid = (lo + hi) >> 1;
+    int64_t v = rows[mid];
+    if (v == key) return mid;
+    if (v < key) lo = mid + 1; else hi = mid - 1;
+  }
+  return -1;
+}
+
+__global__ void k_residual(CaseDev c, int kind, double hc, const double* __restrict__ b, const double* __restrict__ x,
+                           double* __restrict__ res, SolveCtl* sc, int check, int first, Gate gate) {
+  if (!gate_open(gate)) return;
+  const int nx = c.nx, ny = c.ny;
+  int64_t npts = kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize);
+  int64_t base = kind == 2 ? c.usize : 0;  // face-grid offset of the v field
+  const uint8_t* cls = kind == 0 ? c.cls_p : (kind == 1 ? c.cls_u : c.cls_v);
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long rm = 0, bm = 0, bd = 0, xb = 0;
+  double rs = 0.0, bs = 0.0;
+  if (t < npts) {
+    uint8_t k = cls[t];
+    int64_t f = base + t;
+    if (!(k & CLS_ACTIVE)) {
+      res[f] = 0.0;
+    } else {
+      const double xv = x[f], bv = b[f];
+      double ax = 0.0, aabs = 0.0;
+      int nnz = 0;
+      int row = (k & CLS_IRREG) ? find_row(c.irr_rows[kind], c.n_irr[kind], t) : -1;
+      if (row >= 0) {
+        const int64_t* cp = c.irr_ptr[kind];
+        for (int64_t e = cp[row]; e < cp[row + 1]; ++e) {
+          double xv2 = x[base + c.irr_col[kind][e]];
+          double a = c.irr_val[kind][e];
+          ax += a * xv2;
+          aabs += fabs(a) * fabs(xv2);
+        }
+        nnz = (int)(cp[row + 1] - cp[row]);
+      } else if (kind == 0) {
+        int j = (int)(t / nx), i = (int)(t % nx);
+        const double idx2 = 1.0 / (c.dx * c.dx), idy2 = 1.0 / (c.dy * c.dy);
+        double mx = (i == 0 ? -1.0 : (i == nx - 1 ? -3.0 : -2.0)) * idx2;
+        double my = (j == 0 || j == ny - 1 ? -1.0 : -2.0) * idy2;
+        double acc = (mx + my) * xv, aa = fabs(mx + my) * fabs(xv);
+        if (i > 0) { double y = x[t - 1]; acc += idx2 * y; aa += idx2 * fabs(y); }
+        if (i < nx - 1) { double y = x[t + 1]; acc += idx2 * y; aa += idx2 * fabs(y); }
+        if (j > 0) { double y = x[t - nx]; acc += idy2 * y; aa += idy2 * fabs(y); }
+        if (j < ny - 1) { double y = x[t + nx]; acc += idy2 * y; aa += idy2 * fabs(y); }
+        ax = acc / c.rho;
+        aabs = aa / c.rho;
+        nnz = c.a_nnz[t];
+      } else if (kind == 1) {
+        int j = (int)(t / (nx + 1)), i = (int)(t % (nx + 1));
+        const double idx2 = 1.0 / (c.dx * c.dx), idy2 = 1.0 / (c.dy * c.dy);
+        double lap = (-2.0 * idx2 + (j == 0 || j == ny - 1 ? -3.0 : -2.0) * idy2) * xv;
+        if (i > 1) lap += (i == nx ? 2.0 * idx2 : idx2) * x[f - 1];
+        if (i < nx) lap += idx2 * x[f + 1];
+        if (j > 0) lap += idy2 * x[f - (nx + 1)];
+        if (j < ny - 1) lap += idy2 * x[f + (nx + 1)];
+        ax = xv - hc * lap;
+      } else {
+        int j = (int)(t / nx), i = (int)(t % nx);
+        const double idx2 = 1.0 / (c.dx * c.dx), idy2 = 1.0 / (c.dy * c.dy);
+        double lap = ((i == 0 ? -3.0 : (i == nx - 1 ? -1.0 : -2.0)) * idx2 - 2.0 * idy2) * xv;
+        if (i > 0) lap += idx2 * x[f - 1];
+        if (i < nx - 1) lap += idx2 * x[f + 1];
+        if (j > 1) lap += idy2 * x[f - nx];
+        if (j < ny - 1) lap += idy2 * x[f + nx];
+        ax = xv - hc * lap;
+      }
+      double r = bv - ax;
+      res[f] = r;
+      rm = absbits(r);
+      rs = r * r;
+      if (kind == 0) bd = dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + fabs(bv)));
+      if (first) { bm = absbits(bv); bs = bv * bv; }
+      if (!isfinite(xv)) xb = 1;
+    }
+  }
+  block_commit_max(rm, &sc->rmax[check]);
+  block_commit_sum(rs, &sc->rsq[check]);
+  if (kind == 0) block_commit_max(bd, &sc->bound[check]);
+  if (first) {
+    block_commit_max(bm, &sc->bmax);
+    block_commit_sum(bs, &sc->bsq);
+  }
+  block_commit_max(xb, &sc->xbad);
+}
+
+void launch_residual(const CaseDev& c, int kind, double hc, const double* b, const double* x, double* res,
+                     SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st) {
+  int64_t n = kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize);
+  k_residual<<<blocks_for(n), TPB, 0, st>>>(c, kind, hc, b, x, res, sc, check, first_check ? 1 : 0, gate);
+}
+
+// ---------------------------------------------------------------------------
+// projection pieces
+// ---------------------------------------------------------------------------
+__global__ void k_divergence(CaseDev c, const double* __restrict__ U, double* __restrict__ out, double dt,
+                             unsigned long long* divmax, int gate_nonfinite, StepCtl* ctl, Gate gate) {
+  if (!gate_open(gate)) return;
+  const Grid g{c.nx, c.ny, c.usize};
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long dm = 0;
+  bool bad = false;
+  if (t < c.psize) {
+    if (c.cls_p[t] & CLS_ACTIVE) {
+      int j = (int)(t / c.nx), i = (int)(t % c.nx);
+      double d = (U[g.u(j, i + 1)] - U[g.u(j, i)]) / c.dx + (U[g.v(j + 1, i)] - U[g.v(j, i)]) / c.dy;
+      dm = absbits(d);
+      if (out) {
+        double o = dt != 0.0 ? d / dt : d;
+        out[t] = o;
+        bad = !isfinite(o);
+      }
+    } else if (out) {
+      out[t] = 0.0;
+    }
+  }
+  if (gate_nonfinite && bad && ctl) raise_gate(ctl, 1, 4);
+  if (divmax) block_commit_max(dm, divmax);
+}
+void launch_divergence(const CaseDev& c, const double* U, double* out, double scale, SolveCtl* sc,
+                       unsigned long long* divmax, int gate_on_nonfinite, const Gate& gate, cudaStream_t st) {
+  (void)sc;
+  k_divergence<<<blocks_for(c.psize), TPB, 0, st>>>(c, U, out, scale, divmax, gate_on_nonfinite, gate.ctl, gate);
+}
+
+__global__ void k_project_update(CaseDev c, const double* __restrict__ q, const double* __restrict__ phi, double dt,
+                                 double* __restrict__ out, Gate gate) {
+  if (!gate_open(gate)) return;
+  const Grid g{c.nx, c.ny, c.usize};
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int comp, j, i;
+  if (!face_of(t, g, comp, j, i)) return;
+  const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
+  if (!(cls & CLS_ACTIVE)) {
+    out[t] = (comp == 0 && i == 0) ? c.inlet[j] : 0.0;
+    return;
+  }
+  double gphi = comp == 0 ? grad_u(phi, g, j, i, (1.0 / c.dx) / c.rho) : grad_v(phi, g, j, i, (1.0 / c.dy) / c.rho);
+  out[t] = q[t] - dt * gphi;
+}
+void launch_project_update(const CaseDev& c, const double* q, const double* phi, double dt, double* out,
+                           const SolveCtl* psolve, const Gate& gate, cudaStream_t st) {
+  (void)psolve;
+  k_project_update<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, q, phi, dt, out, gate);
+}
+
+__global__ void k_defect(CaseDev c, const double* __restrict__ r, const double* __restrict__ rhs, double hdt,
+                         double* __restrict__ action, double* __restrict__ proj, Gate gate) {
+  if (!gate_open(gate)) return;
+  const Grid g{c.nx, c.ny, c.usize};
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int comp, j, i;
+  if (!face_of(t, g, comp, j, i)) return;
+  const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
+  if (!(cls & CLS_ACTIVE)) {
+    action[t] = 0.0;
+    proj[t] = (comp == 0 && i == 0) ? c.inlet[j] : 0.0;
+    return;
+  }
+  const double idx2 = 1.0 / (c.dx * c.dx), idy2 = 1.0 / (c.dy * c.dy);
+  double l = comp == 0 ? c.nu * lap_u(r, g, j, i, idx2, idy2, false) : c.nu * lap_v(r, g, j, i, idx2, idy2);
+  double hr = r[t] - hdt * l;
+  action[t] = hr;
+  proj[t] = r[t] + (rhs[t] - hr);
+}
+void launch_defect(const CaseDev& c, const double* result, const double* rhs, double hdt, double* action,
+                   double* proj, const Gate& gate, cudaStream_t st) {
+  k_defect<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, result, rhs, hdt, action, proj, gate);
+}
+
+__global__ void k_pressure_out(CaseDev c, const double* __restrict__ p, const double* __restrict__ inc, double factor,
+                               double dt, const double* __restrict__ action, const double* __restrict__ rhs,
+                               double* __restrict__ half, double* __restrict__ pout, unsigned long long* coupled,
+                               Gate gate) {
+  if (!gate_open(gate)) return;
+  const Grid g{c.nx, c.ny, c.usize};
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t nf = c.usize + c.vsize;
+  unsigned long long cm = 0;
+  if (t < nf) {
+    int comp, j, i;
+    face_of(t, g, comp, j, i);
+    const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
+    if (cls & CLS_ACTIVE) {
+      double gi = comp == 0 ? grad_u(inc, g, j, i, (1.0 / c.dx) / c.rho) : grad_v(inc, g, j, i, (1.0 / c.dy) / c.rho);
+      double r = action[t] - rhs[t] + dt * gi;
+      cm = absbits(r);
+    }
+  } else if (t < nf + c.psize) {
+    int64_t k = t - nf;
+    if (c.cls_p[k] & CLS_ACTIVE) {
+      double h = p[k] + inc[k];
+      half[k] = h;
+      pout[k] = h + factor * inc[k];
+    } else {
+      half[k] = 0.0;
+      pout[k] = 0.0;
+    }
+  }
+  block_commit_max(cm, coupled);
+}
+void launch_pressure_out(const CaseDev& c, const double* p, const double* inc, double factor, double dt,
+                         const double* action, const double* rhs, double* half, double* pout,
+                         unsigned long long* coupled, const Gate& gate, cudaStream_t st) {
+  k_pressure_out<<<blocks_for(c.usize + c.vsize + c.psize), TPB, 0, st>>>(c, p, inc, factor, dt, action, rhs, half,
+                                                                          pout, coupled, gate);
+}
+
+__global__ void k_maxabs(CaseDev c, const double* __restrict__ U, unsigned long long* umax, unsigned long long* vmax,
+                         Gate gate) {
+  if (!gate_open(gate)) return;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long a = 0, b = 0;
+  if (t < c.usize) a = absbits(U[t]);
+  else if (t < c.usize + c.vsize) b = absbits(U[t]);
+  block_commit_max(a, umax);
+  block_commit_max(b, vmax);
+}
+void launch_maxabs(const CaseDev& c, const double* U, unsigned long long* umax, unsigned long long* vmax,
+                   const Gate& gate, cudaStream_t st) {
+  k_maxabs<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, U, umax, vmax, gate);
+}
+
+// ---------------------------------------------------------------------------
+// surface forces (solver/optimized_ghost_cell.py:280-286) and step gates (solver/main.py:401-415)
+// ---------------------------------------------------------------------------
+__global__ void k_forces(CaseDev c, const double* __restrict__ U, const double* __restrict__ P, double mu, double dt,
+                         StepCtl* ctl, int check_gates, double* out6, Gate gate) {
+  if (!gate_open(gate)) return;
+  double fpx = 0, fpy = 0, tx = 0, ty = 0;
+  for (int k = threadIdx.x; k < c.n_surf; k += blockDim.x) {
+    double ps = 0, du = 0, dv = 0;
+    for (int64_t e = c.sp_ptr[k]; e < c.sp_ptr[k + 1]; ++e) ps += c.sp_val[e] * P[c.sp_col[e]];
+    for (int64_t e = c.su_ptr[k]; e < c.su_ptr[k + 1]; ++e) du += c.su_val[e] * U[c.su_col[e]];
+    for (int64_t e = c.sv_ptr[k]; e < c.sv_ptr[k + 1]; ++e) dv += c.sv_val[e] * U[c.usize + c.sv_col[e]];
+    double nxk = c.nxx[k], nyk = c.nyy[k];
+    double dn = du * nxk + dv * nyk;
+    tx += mu * (du + nxk * dn);
+    ty += mu * (dv + nyk * dn);
+    fpx += ps * c.nwx[k];
+    fpy += ps * c.nwy[k];
+  }
+  __shared__ double red[4][32];
+  double v[4] = {fpx, fpy, tx, ty};
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int q = 0; q < 4; ++q) {
+    double s = warp_sum(v[q]);
+    if (lane == 0) red[q][wid] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    double s[4] = {0, 0, 0, 0};
+    for (int q = 0; q < 4; ++q)
+      for (int w = 0; w < nw; ++w) s[q] += red[q][w];
+    const double PI = 3.141592653589793;
+    double w = PI * c.D / c.n_surf;
+    double fp[2] = {-s[0], -s[1]};
+    double fv[2] = {s[2] * w, s[3] * w};
+    double f6[6] = {fp[0] + fv[0], fp[1] + fv[1], fp[0], fp[1], fv[0], fv[1]};
+    if (out6)
+      for (int q = 0; q < 6; ++q) out6[q] = f6[q];
+    if (ctl) {
+      for (int q = 0; q < 6; ++q) ctl->forces[q] = f6[q];
+      double denom = ((0.5 * c.rho) * (c.U_ref * c.U_ref)) * c.D;
+      double cd = f6[0] / denom, cl = f6[1] / denom;
+      ctl->cd = cd;
+      ctl->cl = cl;
+      if (check_gates) {
+        if (!isfinite(cd) || !isfinite(cl)) {
+          raise_gate(ctl, 3, 6);
+        } else {
+          double div = bits2d(ctl->div_max[1]);
+          double cfl = dt * (bits2d(ctl->umax) / c.dx + bits2d(ctl->vmax) / c.dy);
+          if (!(div < 1e-10) || !(cfl < 0.5)) raise_gate(ctl, 2, 5);
+        }
+      }
+    }
+  }
+}
+void launch_forces(const CaseDev& c, const double* U, const double* P, double mu, double dt, StepCtl* ctl,
+                   int check_gates, double* out6, const Gate& gate, cudaStream_t st) {
+  k_forces<<<1, 256, 0, st>>>(c, U, P, mu, dt, ctl, check_gates, out6, gate);
+}
+
+__global__ void k_gate_momentum(StepCtl* ctl) {
+  if (ctl->err) return;
+  double r = 0, bm = 0;
+  bool bad = false;
+  for (int s = 0; s < 2; ++s) {
+    const SolveCtl* sc = &ctl->solve[s];
+    double rr = bits2d(sc->rmax[last_check(sc)]);
+    double bb = bits2d(sc->bmax);
+    if (!(rr <= r)) r = rr;  // propagates NaN
+    if (bb > bm) bm = bb;
+    if (sc->xbad) bad = true;
+  }
+  double thr = 1e-10 * (bm > 1.0 ? bm : 1.0);
+  if (bad || !(r <= thr)) raise_gate(ctl, 2, 2);
+}
+void launch_gate_momentum(StepCtl* ctl, cudaStream_t st) { k_gate_momentum<<<1, 1, 0, st>>>(ctl); }
+
+__global__ void k_gate_pressure(StepCtl* ctl, int slot) {
+  if (ctl->err) return;
+  const SolveCtl* sc = &ctl->solve[slot];
+  int k = last_check(sc);
+  double linf = bits2d(sc->rmax[k]), bound = bits2d(sc->bound[k]), bm = bits2d(sc->bmax);
+  if (!isfinite(bm)) { raise_gate(ctl, 1, 4); return; }  // solver/pressure_schur.py:33-34
+  double t = 64 * EPS64 * (bm > 1.0 ? bm : 1.0);
+  t = t > 1e-10 ? t : 1e-10;
+  t = bound > t ? bound : t;
+  if (sc->xbad || !(linf <= t)) raise_gate(ctl, 2, 3);
+}
+void launch_gate_pressure(StepCtl* ctl, int slot, cudaStream_t st) { k_gate_pressure<<<1, 1, 0, st>>>(ctl, slot); }
+
+__global__ void k_gate_projection(StepCtl* ctl, int k) {
+  if (ctl->err) return;
+  double d = bits2d(ctl->div_max[k]);
+  if (!(d <= 1e-10)) raise_gate(ctl, 2, 1);
+}
+void launch_gate_projection(StepCtl* ctl, int k, cudaStream_t st) { k_gate_projection<<<1, 1, 0, st>>>(ctl, k); }
+
+// CFL screen of solver/main.py:273-278 (screen != 0) and the finite-field check of
+// solver/time_integration.py:15-17 on the velocity maxima of the current state.
+__global__ void k_cfl_screen(StepCtl* ctl, const unsigned long long* umax, const unsigned long long* vmax, double dt,
+                             double dx, double dy, int screen) {
+  if (ctl->err) return;
+  double rate = bits2d(*umax) / dx + bits2d(*vmax) / dy;
+  if (screen && (!isfinite(rate) || dt * rate > 0.5)) raise_gate(ctl, 2, 7);
+  else if (!isfinite(rate)) raise_gate(ctl, 1, 8);
+}
+void launch_cfl_screen(StepCtl* ctl, const unsigned long long* umax, const unsigned long long* vmax, double dt,
+                       double dx, double dy, int screen, cudaStream_t st) {
+  k_cfl_screen<<<1, 1, 0, st>>>(ctl, umax, vmax, dt, dx, dy, screen);
+}
+
+__global__ void k_copy_active(const uint8_t* __restrict__ cls, int64_t n, const double* __restrict__ src,
+                              double* __restrict__ dst, Gate gate) {
+  if (!gate_open(gate)) return;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) dst[t] = (cls[t] & CLS_ACTIVE) ? src[t] : 0.0;
+}
+void launch_copy_active(const uint8_t* cls, int64_t n, const double* src, double* dst, const Gate& gate,
+                        cudaStream_t st) {
+  k_copy_active<<<blocks_for(n), TPB, 0, st>>>(cls, n, src, dst, gate);
+}
+
+__global__ void k_set_inlet(CaseDev c, double* U, int zero) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < c.ny) U[(int64_t)j * (c.nx + 1)] = zero ? 0.0 : c.inlet[j];
+}
+void launch_set_inlet(const CaseDev& c, double* U, bool zero, cudaStream_t st) {
+  k_set_inlet<<<blocks_for(c.ny, 128), 128, 0, st>>>(c, U, zero ? 1 : 0);
+}
+
+// mac_engine.calculate_mac_divergence_cpp (solver/src/bindings.cpp:343-390)
+__global__ void k_div_stats(CaseDev c, const double* __restrict__ U, const uint8_t* __restrict__ mask, double* out5) {
+  const Grid g{c.nx, c.ny, c.usize};
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long m = 0;
+  double s = 0, cs = 0, n = 0, cn = 0;
+  if (t < c.psize && !mask[t]) {
+    int j = (int)(t / c.nx), i = (int)(t % c.nx);
+    double d = (U[g.u(j, i + 1)] - U[g.u(j, i)]) / c.dx + (U[g.v(j + 1, i)] - U[g.v(j, i)]) / c.dy;
+    m = absbits(d);
+    s = d * d;
+    n = 1;
+    bool core = true;
+    if (i > 0 && mask[t - 1]) core = false;
+    if (i < c.nx - 1 && mask[t + 1]) core = false;
+    if (j > 0 && mask[t - c.nx]) core = false;
+    if (j < c.ny - 1 && mask[t + c.nx]) core = false;
+    if (core) { cs = d * d; cn = 1; }
+  }
+  block_commit_max(m, reinterpret_cast<unsigned long long*>(&out5[0]));
+  block_commit_sum(s, &out5[1]);
+  block_commit_sum(n, &out5[2]);
+  block_commit_sum(cs, &out5[3]);
+  block_commit_sum(cn, &out5[4]);
+}
+void launch_divergence_stats(const CaseDev& c, const double* U, const uint8_t* mask, double* out5, cudaStream_t st) {
+  k_div_stats<<<blocks_for(c.psize), TPB, 0, st>>>(c, U, mask, out5);
+}
+
+__global__ void k_gather(const double* __restrict__ src, const int64_t* __restrict__ idx, int64_t n,
+                         double* __restrict__ dst) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) dst[t] = src[idx[t]];
+}
+__global__ void k_scatter(const double* __restrict__ src, const int64_t* __restrict__ idx, int64_t n,
+                          double* __restrict__ dst) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) dst[idx[t]] = src[t];
+}
+void launch_gather(const double* src, const int64_t* idx, int64_t n, double* dst, cudaStream_t st) {
+  if (n > 0) k_gather<<<blocks_for(n), TPB, 0, st>>>(src, idx, n, dst);
+}
+void launch_scatter(const double* src, const int64_t* idx, int64_t n, double* dst, cudaStream_t st) {
+  if (n > 0) k_scatter<<<blocks_for(n), TPB, 0, st>>>(src, idx, n, dst);
+}
+
+__global__ void k_schur_column(const double* __restrict__ first, RectView v, int rank, const int64_t* __restrict__ cp,
+                               const int64_t* __restrict__ cc, const double* __restrict__ cv, double* __restrict__ S,
+                               int col) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rank) return;
+  double acc = 0.0;
+  for (int64_t e = cp[r]; e < cp[r + 1]; ++e) {
+    int64_t rc = cc[e];
+    acc += cv[e] * first[v.base + (rc / v.cols) * v.pitch + (rc % v.cols)];
+  }
+  S[(int64_t)r * rank + col] = acc;
+}
+void launch_schur_column(const double* first, const RectView& view, int rank, const int64_t* c_ptr,
+                         const int64_t* c_col, const double* c_val, double* S, int col, cudaStream_t st) {
+  if (rank > 0) k_schur_column<<<blocks_for(rank, 128), 128, 0, st>>>(first, view, rank, c_ptr, c_col, c_val, S, col);
+}
+
+}  // namespace gmk

@@ -1,0 +1,246 @@
+// Device data layout and kernel launchers of the ghost-cell AB2/CN step.
+//
+// Fields live on the staggered grid in HBM, float64, C order:
+//   u : ny x (nx+1)   v : (ny+1) x nx   (one buffer "face grid", u then v)
+//   p : ny x nx
+// A face-grid buffer that represents an unpacked velocity holds the active
+// values, the ghost values (extension stencils), the inlet column and zero
+// walls; a buffer that represents a packed vector holds the active values and
+// zeros elsewhere.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "transforms.cuh"
+
+namespace gmk {
+
+// class bits of every grid point
+enum : uint8_t { CLS_ACTIVE = 1, CLS_IRREG = 2, CLS_GHOST = 4 };
+
+// Reduction slots of one monitored solve (zeroed at the start of every step).
+struct SolveCtl {
+  unsigned long long bmax;       // max |b| (bits of a non-negative double)
+  unsigned long long rmax[3];    // max |b - A x| after apply / sweep 1 / sweep 2
+  unsigned long long bound[3];   // roundoff bound max_i w_i (|A||x| + |b|)_i
+  double rsq[3];                 // sum (b - A x)^2
+  double bsq;                    // sum b^2
+  unsigned long long xbad;       // non-finite solution flag
+};
+
+// Per-step control and diagnostics, one per step in flight.
+struct StepCtl {
+  int err;                       // first failing GM_E* class (0 none)
+  int gate;                      // failing gate id
+  SolveCtl solve[5];             // 0 helm u, 1 helm v, 2 pressure (start-up), 3 pressure #1, 4 pressure #2
+  unsigned long long div_max[3]; // projection divergence checks (start-up, #1, #2)
+  unsigned long long coupled_max;
+  unsigned long long umax, vmax; // max |u|, |v| over the whole grids after the step
+  double forces[6];
+  double cd, cl;
+};
+
+enum Slot { S_HELM_U = 0, S_HELM_V = 1, S_P0 = 2, S_P1 = 3, S_P2 = 4 };
+
+__device__ __forceinline__ unsigned long long dbits(double v) { return __double_as_longlong(v); }
+__host__ __device__ inline double bits2d(unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  memcpy(&d, &b, sizeof d);
+  return d;
+#endif
+}
+
+// Target of the inner refinement loop (solver/pressure_schur.py:115).
+__device__ __forceinline__ double inner_target(const SolveCtl* s) {
+  double b = bits2d(s->bmax);
+  double m = b > 1.0 ? b : 1.0;
+  double t = 32 * 2.220446049250313e-16 * m;
+  return t > 1e-10 ? t : 1e-10;
+}
+// Whether refinement sweep k (1 or 2) runs: the previous check exceeded the target.
+__device__ __forceinline__ bool sweep_needed(const SolveCtl* s, int k) {
+  double tg = inner_target(s);
+  for (int c = 0; c < k; ++c)
+    if (!(bits2d(s->rmax[c]) > tg)) return false;
+  return true;
+}
+// index of the last residual check that ran
+__device__ __forceinline__ int last_check(const SolveCtl* s) {
+  if (sweep_needed(s, 2)) return 2;
+  if (sweep_needed(s, 1)) return 1;
+  return 0;
+}
+
+// Gate for conditionally executed kernels.
+struct Gate {
+  StepCtl* ctl;    // error flag lives here (nullptr: always run)
+  int slot;        // solve slot for sweep gating
+  int sweep;       // 0: unconditional, k: run only if sweep k is needed
+};
+__device__ __forceinline__ bool gate_open_thread(const Gate& g) {
+  if (!g.ctl) return true;
+  if (*(volatile int*)&g.ctl->err) return false;
+  if (g.sweep == 0) return true;
+  return sweep_needed(&g.ctl->solve[g.slot], g.sweep);
+}
+// Block-uniform gate: thread 0 decides, every thread of the block gets the same answer
+// (the error word may change while the kernel runs).
+__device__ __forceinline__ bool gate_open(const Gate& g) {
+  __shared__ int open_flag;
+  if (threadIdx.x == 0) open_flag = gate_open_thread(g) ? 1 : 0;
+  __syncthreads();
+  return open_flag != 0;
+}
+__device__ __forceinline__ void raise_gate(StepCtl* ctl, int err_class, int gate) {
+  if (atomicCAS(&ctl->err, 0, err_class) == 0) ctl->gate = gate;
+}
+
+// Static geometry of one case on the device.
+struct CaseDev {
+  int nx, ny;
+  double dx, dy, rho, nu;
+  int64_t usize, vsize, psize;
+  const uint8_t* cls_u;     // usize
+  const uint8_t* cls_v;     // vsize
+  const uint8_t* cls_p;     // psize
+  double* inlet;            // ny (device, mutable by set_inlet)
+  // ghost extension rows on the face grid (u rows then v rows, flat face-grid index)
+  int n_ghost_f;
+  const int64_t* gf_rows; const int64_t* gf_ptr; const int64_t* gf_col; const double* gf_val;
+  int n_ghost_p;
+  const int64_t* gp_rows; const int64_t* gp_ptr; const int64_t* gp_col; const double* gp_val;
+  // irregular rows: pressure A (p grid), Helmholtz u (u grid), v (v grid)
+  int n_irr[3];
+  const int64_t* irr_rows[3]; const int64_t* irr_ptr[3]; const int64_t* irr_col[3]; const double* irr_val[3];
+  const int32_t* a_nnz;     // psize: nnz of A rows (roundoff weights)
+  // surface quadrature
+  int n_surf;
+  const int64_t* sp_ptr; const int64_t* sp_col; const double* sp_val;
+  const int64_t* su_ptr; const int64_t* su_col; const double* su_val;
+  const int64_t* sv_ptr; const int64_t* sv_col; const double* sv_val;
+  const double* nwx; const double* nwy; const double* nxx; const double* nyy;
+  double D, U_ref;
+};
+
+// Helmholtz coefficients (per dt)
+struct HelmDev {
+  double c;  // 0.5 * dt * nu
+};
+
+// ---- separable inverse on a rectangle view --------------------------------
+struct RectView {
+  int rows, cols;
+  int64_t base, pitch;        // offset of (0,0) in the field grid and its row pitch
+  const uint8_t* cls;         // class map of the field grid (mask for loads/stores)
+};
+
+struct TransformTables {      // device tables of one rectangle kind (FP64)
+  FftPlan plan_x, plan_y;
+  int tx_fwd, tx_inv, ty_fwd, ty_inv;
+  const void* Wx; const void* prex; const void* postx;
+  const void* Wy; const void* prey; const void* posty;
+  // For the inverse x transform (may differ in type IV vs Makhoul but same n):
+  const void* prex_inv; const void* postx_inv;
+  const double* recip;        // rows x cols: 1 / (divisor * 4 nx ny)
+  int lpb_x, lpb_y;           // lines per block
+  size_t smem_x, smem_y;
+};
+
+// ---- launchers (kernels.cu) ------------------------------------------------
+void configure_kernels(int smem_optin);
+// x = T^{-1} b on the rectangle view; b is read through the active mask when
+// mask_in is set; the output epilogue is
+//   out = active ? (add + sub - T^{-1} b) : 0   when sub != nullptr
+//   out = T^{-1} b                              otherwise.
+void launch_rect_inverse(const TransformTables& tt, const RectView& view, const double* b, bool mask_in,
+                         double* spectral, double* out, const double* sub, const double* add, const Gate& gate,
+                         cudaStream_t st);
+
+void launch_schur(const double* first, const RectView& view, int rank, const int64_t* rows, const int64_t* c_ptr,
+                  const int64_t* c_col, const double* c_val, const double* sinv, double* w2, const Gate& gate,
+                  cudaStream_t st);
+
+void launch_ghost(double* field, int n, const int64_t* rows, const int64_t* ptr, const int64_t* col,
+                  const double* val, const Gate& gate, cudaStream_t st);
+
+// residual of the operator of kind (0 pressure A, 1 Helmholtz u, 2 Helmholtz v)
+// res = b - Op x on active points; reductions into sc at check index k
+void launch_residual(const CaseDev& c, int kind, double hc, const double* b, const double* x, double* res,
+                     SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st);
+
+// momentum right-hand side; mode 0 steady AB2, 1 start-up part A, 2 start-up part B
+struct MomentumArgs {
+  const double* U;        // unpacked velocity (face grid)
+  const double* Uhalf;    // unpacked half-step velocity (mode 2)
+  const double* P;        // pressure grid with ghost values
+  const double* prev;     // previous advection (mode 0)
+  double* now;            // advection output (modes 0, 1)
+  double* out;            // rhs (modes 0, 2) or midpoint (mode 1)
+  double dt, alpha;
+  int mode;
+};
+void launch_momentum(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st);
+
+// single operators on face grids (for the operator API)
+void launch_advection(const CaseDev& c, const double* U, double* out, const Gate& gate, cudaStream_t st);
+void launch_diffusion(const CaseDev& c, const double* U, double* out, bool with_inlet, double hdt, const Gate& gate,
+                      cudaStream_t st);  // hdt==0: L U (+offset); else U - hdt*L U (H matvec)
+void launch_gradient(const CaseDev& c, const double* P, double* out, const Gate& gate, cudaStream_t st);
+
+// divergence at active p cells of an unpacked face grid: out = div * scale; max|out| -> bmax of sc (if sc),
+// max|div| -> *divmax (if divmax); non-finite -> gate error
+void launch_divergence(const CaseDev& c, const double* U, double* out, double scale, SolveCtl* sc,
+                       unsigned long long* divmax, int gate_on_nonfinite, const Gate& gate, cudaStream_t st);
+
+// out = q - dt * G phi on active faces (phi grid ghost-filled); pressure gate of slot checked first
+void launch_project_update(const CaseDev& c, const double* q, const double* phi, double dt, double* out,
+                           const SolveCtl* psolve, const Gate& gate, cudaStream_t st);
+
+// action = H result; proj = result + (rhs - action)
+void launch_defect(const CaseDev& c, const double* result, const double* rhs, double hdt, double* action,
+                   double* proj, const Gate& gate, cudaStream_t st);
+
+// half = p + inc; out = half + factor*inc (active p); coupled = max|action - rhs + dt G inc|
+void launch_pressure_out(const CaseDev& c, const double* p, const double* inc, double factor, double dt,
+                         const double* action, const double* rhs, double* half, double* pout,
+                         unsigned long long* coupled, const Gate& gate, cudaStream_t st);
+
+void launch_maxabs(const CaseDev& c, const double* U, unsigned long long* umax, unsigned long long* vmax,
+                   const Gate& gate, cudaStream_t st);
+
+// forces and coefficients; raises the force/step gates
+void launch_forces(const CaseDev& c, const double* U, const double* P, double mu, double dt, StepCtl* ctl,
+                   int check_gates, double* out6, const Gate& gate, cudaStream_t st);
+
+// CN momentum gate (after both Helmholtz solves)
+void launch_gate_momentum(StepCtl* ctl, cudaStream_t st);
+// projection divergence gate on div_max[k]
+void launch_gate_projection(StepCtl* ctl, int k, cudaStream_t st);
+// CFL screen: dt*(umax/dx + vmax/dy) > 0.5 -> error (values from a previous maxabs)
+void launch_cfl_screen(StepCtl* ctl, const unsigned long long* umax, const unsigned long long* vmax, double dt,
+                       double dx, double dy, int screen, cudaStream_t st);
+
+void launch_gate_pressure(StepCtl* ctl, int slot, cudaStream_t st);
+// dst[k] = src[idx[k]] and dst[idx[k]] = src[k]
+void launch_gather(const double* src, const int64_t* idx, int64_t n, double* dst, cudaStream_t st);
+void launch_scatter(const double* src, const int64_t* idx, int64_t n, double* dst, cudaStream_t st);
+// column col of (S - I): S[r*rank+col] = sum_e C[r,e] first[e]
+void launch_schur_column(const double* first, const RectView& view, int rank, const int64_t* c_ptr,
+                         const int64_t* c_col, const double* c_val, double* S, int col, cudaStream_t st);
+
+// zero/copy helpers
+void launch_copy_active(const uint8_t* cls, int64_t n, const double* src, double* dst, const Gate& gate,
+                        cudaStream_t st);
+
+// set the inlet column of a face grid
+void launch_set_inlet(const CaseDev& c, double* U, bool zero, cudaStream_t st);
+
+// fluid-cell divergence statistics on a mask (mac_engine diagnostic)
+void launch_divergence_stats(const CaseDev& c, const double* U, const uint8_t* mask, double* out5,
+                             cudaStream_t st);
+
+}  // namespace gmk

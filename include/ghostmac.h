@@ -1,0 +1,187 @@
+/*
+ * ghostmac.h — C ABI of the GB300 ghost-cell MAC AB2/CN library (libghostmac.so).
+ *
+ * One handle holds one cylinder case: a 2-D staggered (MAC) grid, nx x ny pressure
+ * cells, u on vertical faces (ny x (nx+1)), v on horizontal faces ((ny+1) x nx),
+ * all arrays float64 and C order.  Setup (classification, ghost stencils, operators,
+ * boundary Schur factor) runs once in gm_create; every step runs on the GPU.
+ *
+ * Pointers: every array argument may be a host pointer or a CUDA device pointer
+ * (detected per call with cudaPointerGetAttributes).  Host arrays are copied.
+ * Return value: GM_OK or an error class; gm_last_error() gives the message.
+ * The classes map 1:1 to the reference's exceptions: GM_EVALUE -> ValueError,
+ * GM_ERUNTIME -> RuntimeError (a failed gate), GM_EFLOAT -> FloatingPointError.
+ * A handle is not thread safe; it owns one CUDA stream.
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths relative to the reference repository invisce/cfd-cylinder-flow-ghost-cell).
+ */
+#ifndef GHOSTMAC_H
+#define GHOSTMAC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GM_OK 0
+#define GM_EVALUE 1     /* ValueError: bad configuration or input */
+#define GM_ERUNTIME 2   /* RuntimeError: a solver gate failed */
+#define GM_EFLOAT 3     /* FloatingPointError: non-finite force */
+#define GM_ECUDA 4      /* CUDA error or no device */
+#define GM_ENOTIMPL 5   /* option not built in this library */
+
+typedef struct gm_handle gm_handle;
+
+/* Constructor arguments of MAC_CylinderFlow restricted to the ghost_cell/ab2_cn
+ * path (solver/main.py:40-44). */
+typedef struct gm_config {
+  int32_t nx, ny;
+  double Lx, Ly, D, xc, yc, nu, rho, U_inf;
+  int32_t inflow;                 /* 0 uniform, 1 parabolic */
+  double U_m;                     /* parabolic peak; <= 0 selects 1.5*U_inf */
+  int32_t pressure_solver;        /* 0 direct (DCT/DST + boundary Schur), 1 iterative (GMRES) */
+  int32_t pressure_extension;     /* 0 neumann, 1 quadratic */
+  int32_t velocity_interpolation; /* 0 bilinear, 1 biquadratic */
+  int32_t precision;              /* 0 plain FP64, 1 FP32 transforms with FP64 refinement */
+} gm_config;
+
+typedef struct gm_sizes {
+  int64_t nx, ny, usize, vsize, psize;
+  int64_t nu_active, nv_active, np_active, qsize;
+  int64_t n_surface;               /* surface quadrature points */
+  int64_t rank_p, rank_u, rank_v;  /* boundary Schur ranks (u, v after the first step) */
+  int64_t ghost_u, ghost_v, ghost_p;
+  double dx, dy, U_ref;
+} gm_sizes;
+
+/* Per-step diagnostics: the keys of MAC_CylinderFlow.last_step_diagnostics
+ * (solver/main.py:407-413, solver/optimized_ghost_cell.py:269-276,
+ * solver/time_integration.py:143-145). */
+typedef struct gm_step_diag {
+  double time, dt, max_divergence, cfl;
+  double cd, cl, cd_pressure, cd_viscous, cl_pressure, cl_viscous;
+  double momentum_residual_linf, coupled_momentum_residual_linf;
+  double pressure_residual_linf, pressure_residual_relative_l2;
+  double forces[6];               /* fx, fy, fx_p, fy_p, fx_v, fy_v */
+  int32_t pressure_solve_count, pressure_iterations, pressure_refinement_iterations;
+  int32_t momentum_refinement_iterations;
+  int32_t status;                 /* 0 ok, else the GM_E* class of the failure */
+  int32_t gate;                   /* which gate failed (GM_GATE_*), 0 if none */
+} gm_step_diag;
+
+#define GM_GATE_PROJECTION 1   /* solver/optimized_ghost_cell.py:226-228 */
+#define GM_GATE_MOMENTUM 2     /* solver/time_integration.py:102-104 */
+#define GM_GATE_PRESSURE 3     /* solver/pressure_schur.py:69-70 */
+#define GM_GATE_PRESSURE_RHS 4 /* solver/pressure_schur.py:33-34 */
+#define GM_GATE_STEP 5         /* solver/main.py:414-415 */
+#define GM_GATE_FORCE 6        /* solver/main.py:404-405 */
+#define GM_GATE_CFL_SCREEN 7   /* solver/main.py:273-278 */
+#define GM_GATE_FINITE 8       /* solver/time_integration.py:15-17 */
+
+typedef struct gm_solve_info {
+  double residual_linf, residual_relative_l2, residual_target_linf, roundoff_bound_linf,
+      backward_error_linf;
+  int32_t iterations, refinement_iterations, status, rank;
+} gm_solve_info;
+
+/* --- lifecycle ------------------------------------------------------------ */
+
+/* Replaces MAC_CylinderFlow.__init__ ghost/ab2_cn branch (solver/main.py:40-242):
+ * builds the mask check, inlet profile, GhostCellIntegrator
+ * (solver/optimized_ghost_cell.py:61-150) and the initial projection
+ * (solver/main.py:229-230).  The initial state is then readable with gm_get_state. */
+int gm_create(const gm_config* cfg, gm_handle** out);
+int gm_destroy(gm_handle* h);
+/* Setup only, on the host: classification, stencils, operators and Schur rows without
+ * touching a GPU.  The geometry accessors below work on such a handle; state, step and
+ * operator calls return GM_ECUDA. */
+int gm_create_host(const gm_config* cfg, gm_handle** out);
+/* Build the CN Helmholtz data for a timestep (solver/optimized_ghost_cell.py:243-255);
+ * gm_step does this itself when dt changes.  On a host-only handle only the rows are built. */
+int gm_prepare_dt(gm_handle* h, double dt);
+/* Message of the last error on this handle (or of the last failed gm_create when h is NULL). */
+const char* gm_last_error(const gm_handle* h);
+int gm_get_sizes(const gm_handle* h, gm_sizes* out);
+/* Optional: run this handle's work on an external stream (e.g. torch.cuda.current_stream()). */
+int gm_set_stream(gm_handle* h, void* cuda_stream);
+
+/* --- geometry (host arrays) ------------------------------------------------ */
+
+/* Active flat indices ui, vi, pi (solver/optimized_ghost_cell.py:66-79). */
+int gm_get_indices(const gm_handle* h, int64_t* ui, int64_t* vi, int64_t* pi);
+/* Ghost rows of the extension operators E (u, v) and P (pressure):
+ * which = 0 (u), 1 (v), 2 (p).  rows: grid flat index of each ghost point;
+ * ptr (n+1), cols (grid flat indices of active points), vals.  Pass NULL to
+ * query the counts through *n_rows and *nnz (solver/optimized_ghost_cell.py:14-58). */
+int gm_get_ghost_stencils(const gm_handle* h, int32_t which, int64_t* n_rows, int64_t* nnz,
+                          int64_t* rows, int64_t* ptr, int64_t* cols, double* vals);
+/* Boundary Schur rows (rectangle flat indices) for which = 0 (pressure),
+ * 1 (u Helmholtz), 2 (v Helmholtz) (solver/pressure_schur.py:77-91). */
+int gm_get_schur_rows(const gm_handle* h, int32_t which, int64_t* n, int64_t* rows);
+/* Circle quadrature points (y, x) pairs (solver/cut_cell_solver.py:70-77). */
+int gm_get_surface_points(const gm_handle* h, double* yx);
+
+/* --- state ----------------------------------------------------------------- */
+
+/* u (ny x nx+1), v (ny+1 x nx), p (ny x nx); any may be NULL to skip. */
+int gm_set_state(gm_handle* h, const double* u, const double* v, const double* p);
+int gm_get_state(gm_handle* h, double* u, double* v, double* p);
+/* Inlet profile u_inlet[ny] (solver/main.py:281-286 writes it; solver/optimized_ghost_cell.py:238-242 reads it). */
+int gm_set_inlet(gm_handle* h, const double* u_inlet);
+/* AB2/CN history for checkpoints (solver/main.py:511-516, 558-566):
+ * previous_advection[qsize], half_pressure[np_active], previous_dt.
+ * has_history = 0 clears it (next step uses the projected midpoint start-up). */
+int gm_set_history(gm_handle* h, int32_t has_history, const double* previous_advection,
+                   const double* half_pressure, double previous_dt);
+int gm_get_history(gm_handle* h, int32_t* has_history, double* previous_advection,
+                   double* half_pressure, double* previous_dt);
+
+/* --- the step ----------------------------------------------------------------- */
+
+/* n_steps of MAC_CylinderFlow.solve's loop body for this path (solver/main.py:271-429:
+ * CFL screen every 100 steps counted from first_step_index, gg.advance
+ * (solver/optimized_ghost_cell.py:236-278 -> solver/time_integration.py:7-145),
+ * surface forces, coefficient and divergence/CFL gates).  The inlet is held fixed.
+ * diag receives n_steps records (host pointer).  A failed gate stops the run:
+ * the return value is its class and diag[k].status/gate tell where. */
+int gm_step(gm_handle* h, double dt, int32_t n_steps, int64_t first_step_index, double start_time,
+            gm_step_diag* diag);
+
+/* --- operators (GhostCellIntegrator methods, solver/optimized_ghost_cell.py:174-234) --- */
+
+#define GM_OP_PACK 1        /* (u|v grids, usize+vsize) -> q          :174-177 */
+#define GM_OP_UNPACK 2      /* q -> (u|v grids) with ghosts and inlet :179-184 */
+#define GM_OP_ADVECTION 3   /* q -> -N(q)                            :186-199 */
+#define GM_OP_DIFFUSION 4   /* q -> L q + diff_offset                :201-205 */
+#define GM_OP_GRADIENT 5    /* packed p (np_active) -> G p           :207-210 */
+#define GM_OP_DIVERGENCE 6  /* q -> D q + div_offset                 :212-216 */
+#define GM_OP_H_MATVEC 7    /* q -> q - dt/2 L q (param = dt)        :231-234 */
+#define GM_OP_PRESSURE_EXTEND 8 /* packed p -> P p (full grid)       :278    */
+int gm_apply(gm_handle* h, int32_t op, double param, const double* x, double* y);
+
+/* project(q, dt) -> (q - dt G phi, phi) with the divergence gate
+ * (solver/optimized_ghost_cell.py:218-229). */
+int gm_project(gm_handle* h, double dt, const double* q, double* q_out, double* phi,
+               gm_solve_info* info);
+/* Monitored pressure solve A phi = rhs (solver/pressure_schur.py:16-72 via
+ * solver/optimized_ghost_cell.py:110-111): rhs, phi of length np_active. */
+int gm_pressure_solve(gm_handle* h, const double* rhs, double* phi, gm_solve_info* info);
+/* Separable rectangle inverse (solver/rectangular_inverse.py:8-58): kind 0 pressure,
+ * 1 u, 2 v; for u and v, nu_dt = (nu, dt) of the Helmholtz operator.  b and x are
+ * rectangle grids (ny x nx, or (ny-1) x nx for v). */
+int gm_rectangle_solve(gm_handle* h, int32_t kind, double dt, const double* b, double* x);
+/* surface_forces(u, v, p, mu) -> fx, fy, fx_p, fy_p, fx_v, fy_v
+ * (solver/optimized_ghost_cell.py:280-286). */
+int gm_surface_forces(gm_handle* h, const double* u, const double* v, const double* p, double mu,
+                      double out[6]);
+/* Fluid-cell divergence statistics of mac_engine.calculate_mac_divergence_cpp
+ * (solver/src/bindings.cpp:343-390): out = max, sum div^2, core sum div^2; counts = count, core count. */
+int gm_divergence_stats(gm_handle* h, const double* u, const double* v, double out[3], int64_t counts[2]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GHOSTMAC_H */

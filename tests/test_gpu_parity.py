@@ -1,0 +1,195 @@
+"""GPU parity of libghostmac.so against the oracle and the reference's golden vectors.
+
+Every comparison goes through the C ABI (ctypes) on a GB300.  Tolerances
+(max-norm, relative to max(1, |reference|)):
+  single operators and transforms ............ 1e-12
+  projected fields, pressure solves ........... 1e-11
+  fields after a few AB2/CN steps ............. 1e-10
+  force coefficients .......................... 1e-8 (relative)
+  discrete divergence ......................... < 1e-10 absolute
+Indices and stencils are compared bit-exactly by tests/test_geometry_host.py.
+"""
+import numpy as np
+import pytest
+
+import ghost_oracle as go
+from conftest import GOLDEN, load_package
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return float(np.max(np.abs(a - b))) / max(1.0, float(np.max(np.abs(b))))
+
+
+@pytest.fixture(scope='module')
+def pkg():
+    return load_package()
+
+
+def small(pkg, **kw):
+    return pkg.MAC_CylinderFlow(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., verbose=False, **kw)
+
+
+@pytest.fixture(scope='module')
+def G():
+    return np.load(GOLDEN / 'small_88x16.npz')
+
+
+def test_rectangle_transforms(pkg):
+    G = np.load(GOLDEN / 'rectangle_24x10.npz')
+    s = pkg.MAC_CylinderFlow(nx=24, ny=10, Lx=7.2, Ly=2.5, D=1.0, xc=3.6, yc=1.25, nu=0.02, rho=1.3, verbose=False)
+    for kind in ('pressure', 'u', 'v'):
+        x = s.gg.rectangle_solve(kind, G[f'{kind}_in'], dt=0.004)
+        assert rel(x, G[f'{kind}_out']) < 1e-12, kind
+
+
+@pytest.mark.parametrize('n', [(40, 30), (88, 16), (400, 200), (256, 128), (820, 410)])
+def test_rectangle_transforms_sizes(pkg, n):
+    nx, ny = n
+    h = 0.05
+    s = pkg.MAC_CylinderFlow(nx=nx, ny=ny, Lx=nx * h, Ly=ny * h, D=1.0, xc=nx * h / 4, yc=ny * h / 2, nu=0.01,
+                             verbose=False)
+    rng = np.random.default_rng(nx)
+    for kind in ('pressure', 'u', 'v'):
+        _, solve, shape = go.rectangle(nx, ny, s.dx, s.dy, kind, 0.01, 0.002, 1.0, self_check=False)
+        b = rng.normal(size=shape)
+        assert rel(s.gg.rectangle_solve(kind, b, dt=0.002), solve(b.copy())) < 1e-12, kind
+
+
+def test_operators_match_golden(pkg, G):
+    s = small(pkg)
+    g = s.gg
+    assert np.array_equal(g.ui, G['ui']) and np.array_equal(g.pi, G['pi'])
+    q = G['q']
+    assert rel(g.advection(q), G['advection']) < 1e-12
+    assert rel(g.diffusion(q), G['diffusion']) < 1e-12
+    assert rel(g.gradient(G['p_rand']), G['gradient']) < 1e-12
+    assert rel(g.divergence(q), G['divergence']) < 1e-12
+    assert rel(g.H_matvec(q, 0.003), G['H_q']) < 1e-12
+    u, v = g.unpack(q)
+    assert rel(u, G['unpack_u']) < 1e-14 and rel(v, G['unpack_v']) < 1e-14
+    assert rel(g.pack(u, v), q) == 0.0
+    assert rel(g.pressure_solve(G['rhs_p']), G['sol_p']) < 1e-11
+    pq, phi = g.project(q, .003)
+    assert rel(pq, G['project_q']) < 1e-11 and rel(phi, G['project_phi']) < 1e-11
+    assert np.max(np.abs(g.divergence(pq))) < 1e-10
+    assert rel(s.u, G['init_u']) < 1e-12 and rel(s.v, G['init_v']) < 1e-12
+
+
+def test_steps_match_golden(pkg, G):
+    s = small(pkg)
+    for k in range(5):
+        s.solve(n_steps=1, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
+        d = s.last_step_diagnostics
+        sc = G['step_scalars'][k]
+        assert rel(s.u, G['step_u'][k]) < 1e-10, k
+        assert rel(s.v, G['step_v'][k]) < 1e-10, k
+        assert rel(s.p, G['step_p'][k]) < 1e-10, k
+        assert abs(d['cd'] - sc[0]) <= 1e-8 * abs(sc[0]) and abs(d['cl'] - sc[1]) <= 1e-8 * max(abs(sc[1]), 1e-3)
+        assert d['max_divergence'] < 1e-10
+    assert rel(s.gg.surface_forces(s.u, s.v, s.p, s.nu * s.rho), G['forces']) < 1e-10
+    stats = s.divergence_stats()
+    assert abs(stats[0] - G['mac_divergence'][0]) < 1e-12
+    assert [stats[2], stats[4]] == list(G['mac_divergence_counts'])
+
+
+def test_multi_step_call_equals_single_steps(pkg):
+    a, b = small(pkg), small(pkg)
+    a.solve(n_steps=6, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
+    for _ in range(6):
+        b.solve(n_steps=1, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
+    for key in ('u', 'v', 'p'):
+        assert np.array_equal(getattr(a, key), getattr(b, key)), key
+
+
+@pytest.mark.parametrize('tag,opts', [('bq', dict(ghost_velocity_interpolation='biquadratic')),
+                                      ('qp', dict(ghost_pressure_extension='quadratic'))])
+def test_option_paths(pkg, tag, opts):
+    G = np.load(GOLDEN / f'opt40x30_{tag}.npz')
+    s = pkg.MAC_CylinderFlow(nx=40, ny=30, Lx=4., Ly=3., xc=1.5, yc=1.5, verbose=False, **opts)
+    s.solve(n_steps=3, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
+    assert rel(s.u, G['u']) < 1e-10 and rel(s.p, G['p']) < 1e-9
+    assert abs(s.last_step_diagnostics['cd'] - G['scalars'][0]) < 1e-8 * abs(G['scalars'][0])
+    assert s.last_step_diagnostics['max_divergence'] < 1e-10
+
+
+def test_traction_known_answers(pkg):
+    G = np.load(GOLDEN / 'traction.npz')
+    for k, (nx, ny) in enumerate(((40, 30), (80, 60), (120, 90))):
+        s = pkg.MAC_CylinderFlow(nx=nx, ny=ny, Lx=4., Ly=3., xc=1.5, yc=1.5, verbose=False)
+        xu, yu = np.arange(nx + 1) * s.dx, (np.arange(ny) + .5) * s.dy
+        xv, yv = (np.arange(nx) + .5) * s.dx, np.arange(ny + 1) * s.dy
+        xx, yy = np.meshgrid(xu, yu)
+        rr = np.hypot(xx - s.xc, yy - s.yc)
+        u = -(rr - s.D / 2) * (yy - s.yc) / rr
+        xx, yy = np.meshgrid(xv, yv)
+        rr = np.hypot(xx - s.xc, yy - s.yc)
+        v = (rr - s.D / 2) * (xx - s.xc) / rr
+        p = np.ascontiguousarray(np.broadcast_to(xv, s.p.shape))
+        f = s.gg.surface_forces(u, v, p, s.nu * s.rho)
+        assert rel(f, G['forces'][k]) < 1e-12
+        assert abs(f[2] + np.pi * (s.D / 2) ** 2) < 1e-10 and abs(f[3]) < 1e-10
+
+
+def test_config1_two_steps(pkg):
+    G = np.load(GOLDEN / 'config1_400x200.npz')
+    s = pkg.MAC_CylinderFlow(nx=400, ny=200, Lx=20., Ly=10., D=1., xc=5., yc=5., nu=1 / 40, verbose=False)
+    q = s.gg.pack(s.u, s.v)
+    q += 1e-3 * np.random.default_rng(0).standard_normal(q.size)
+    s.u[:], s.v[:] = s.gg.unpack(q)
+    for k in range(2):
+        s.solve(n_steps=1, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+        assert rel(s.u.ravel()[G['sample_u']], G['u_samples'][k]) < 1e-10
+        assert rel(s.v.ravel()[G['sample_v']], G['v_samples'][k]) < 1e-10
+        assert rel(s.p.ravel()[G['sample_p']], G['p_samples'][k]) < 1e-10
+        d = s.last_step_diagnostics
+        assert abs(d['cd'] - G['scalars'][k][0]) < 1e-8 * abs(G['scalars'][k][0])
+        assert d['max_divergence'] < 1e-10
+
+
+def test_oracle_parity_with_noise_20_steps(pkg):
+    """Same seeded inputs through the oracle and the GPU for 20 steps (tolerance 1e-10)."""
+    kw = dict(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., nu=0.02)
+    s = pkg.MAC_CylinderFlow(verbose=False, **kw)
+    c = go.CylinderCase(**kw)
+    q = c.ops.pack(c.u, c.v)
+    q += 1e-2 * np.random.default_rng(5).standard_normal(q.size)
+    c.u, c.v = c.ops.unpack(q)
+    s.u[:], s.v[:] = c.u, c.v
+    s.solve(n_steps=20, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+    c.solve(20, .002)
+    for key in ('u', 'v', 'p'):
+        assert rel(getattr(s, key), getattr(c, key)) < 1e-10, key
+    assert abs(s.last_step_diagnostics['cd'] / c.last_step_diagnostics['cd'] - 1) < 1e-8
+
+
+def test_checkpoint_restart(pkg, tmp_path):
+    cont, div = small(pkg), small(pkg)
+    cont.solve(n_steps=20, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
+    div.solve(n_steps=7, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
+    path = tmp_path / 'ck.npz'
+    div.save_checkpoint(path)
+    res = pkg.MAC_CylinderFlow.from_checkpoint(path)
+    res.solve(n_steps=13, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
+    for key in ('u', 'v', 'p'):
+        assert np.max(np.abs(getattr(cont, key) - getattr(res, key))) < 1e-11, key
+    with np.load(path, allow_pickle=False) as data:
+        arrays = {k: data[k].copy() for k in data.files if k != 'half_pressure'}
+    np.savez(path, **arrays)
+    with pytest.raises(ValueError):
+        pkg.MAC_CylinderFlow.from_checkpoint(path)
+
+
+def test_gates_raise(pkg):
+    s = small(pkg)
+    with pytest.raises(RuntimeError):
+        s.solve(n_steps=1, dt=1.0, perturb_transient=False, save_artifacts=False, verbose=False)
+    s = small(pkg)
+    s.u[3, 5] = np.nan
+    with pytest.raises((ValueError, RuntimeError)):
+        s.solve(n_steps=1, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
+    s = small(pkg)
+    s.solve(n_steps=2, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
+    assert s.last_step_diagnostics['max_divergence'] < 1e-10
