@@ -1,0 +1,301 @@
+"""Benchmark of the ghost-cell MAC AB2/CN step on GB300: cell-updates/s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+One step = one AB2/CN time step of one cylinder case (momentum right-hand side,
+two CN Helmholtz solves, two pressure projections with the FFT + boundary Schur
+solver, force quadrature and the divergence/CFL gates), exactly the loop body of
+MAC_CylinderFlow.solve for boundary='ghost_cell', time_scheme='ab2_cn'.
+Synthetic seeded inputs: the reference case geometry with a seeded Gaussian
+perturbation (no external data).
+
+Our arm prints one JSON line: device-timed throughput (CUDA events on the
+library's stream, L2 flushed between timed steps), an end-to-end figure through
+the public MAC_CylinderFlow.solve API with host arrays, the roofline of the
+dominant kernel, the CPU baseline (the oracle port on this host) and the SM
+clocks sampled during the timed region.  --impl reference times the CPU oracle
+port of the reference algorithm on the host cores for the same workload.
+Under torchrun each rank runs an independent replica (the case does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+METRIC = 'cell-updates/s at div<1e-10: FP32+refine/learned-PC vs plain FP64, same GB300'
+
+WORKLOADS = {
+    # 40D x 41D wide domain, cylinder at (10D, 20.5D), Re=100, seeded 1e-2 v perturbation
+    'wide_800x820_re100': dict(nx=800, ny=820, Lx=40.0, Ly=41.0, D=1.0, xc=10.0, yc=20.5, nu=0.01, dt=0.002,
+                               noise='v', amp=1e-2, seed=0),
+    # 20D x 10D channel, cylinder at (5D, 5D), Re=40, seeded 1e-3 noise on u and v
+    'channel_400x200_re40': dict(nx=400, ny=200, Lx=20.0, Ly=10.0, D=1.0, xc=5.0, yc=5.0, nu=1 / 40, dt=0.002,
+                                 noise='uv', amp=1e-3, seed=0),
+}
+DEFAULT_WORKLOAD = 'wide_800x820_re100'
+KERNEL_CLASSES = {1: 'transform x pass (k_xpass)', 2: 'transform y pass (k_ypass)', 3: 'momentum rhs (k_momentum)',
+                  4: 'operator residual (k_residual)'}
+
+
+def load_package():
+    sys.path.insert(0, str(ROOT))
+    import __graft_entry__ as ge
+    return ge.load_package()
+
+
+def peaks():
+    p = ROOT / 'MEASURED_PEAKS.json'
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d['hbm_gbs']), 'measured'
+    return 6800.0, 'fallback'
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,'
+             'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+             'clocks_event_reasons.sw_power_cap')
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), f'--query-gpu={q}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(',')])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if len(r) >= 7 and r[0].replace('.', '').isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 7 and r[1].replace('.', '').isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[k] for r in self.rows if len(r) >= 7 for k in range(4) if r[3 + k] == 'Active'})
+        return dict(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(mx) if mx else None,
+                    reasons=reasons, samples=len(sm))
+
+
+def seeded_state(s, w):
+    """Seeded Gaussian perturbation of the active faces (the reference has no noise API)."""
+    rng = np.random.default_rng(w['seed'])
+    q = s.gg.pack(s.u, s.v)
+    nu = len(s.gg.ui)
+    if w['noise'] == 'uv':
+        q += w['amp'] * rng.standard_normal(q.size)
+    else:
+        q[nu:] += w['amp'] * rng.standard_normal(q.size - nu)
+    u, v = s.gg.unpack(q)
+    s.u[:], s.v[:] = u, v
+
+
+def oracle_rate(w, steps, seconds, workers):
+    """Cell-updates/s of the CPU oracle port of the reference algorithm (setup and the first,
+    Helmholtz-building step excluded)."""
+    sys.path.insert(0, str(ROOT / 'oracle'))
+    import ghost_oracle as go
+    import scipy.fft
+    kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
+    with scipy.fft.set_workers(workers):
+        c = go.CylinderCase(**kw)
+        rng = np.random.default_rng(w['seed'])
+        q = c.ops.pack(c.u, c.v)
+        if w['noise'] == 'uv':
+            q += w['amp'] * rng.standard_normal(q.size)
+        else:
+            q[len(c.ops.ui):] += w['amp'] * rng.standard_normal(q.size - len(c.ops.ui))
+        c.u, c.v = c.ops.unpack(q)
+        c.solve(1, w['dt'])
+        done, t0 = 0, time.perf_counter()
+        while done < steps and (time.perf_counter() - t0) < seconds:
+            c.solve(1, w['dt'])
+            done += 1
+        el = time.perf_counter() - t0
+    return w['nx'] * w['ny'] * done / el, done, el
+
+
+def run_reference(args, w, rank):
+    if rank != 0:
+        return
+    workers = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        pass  # the oracle's first step (Helmholtz build) is taken inside oracle_rate
+    rate, done, el = oracle_rate(w, args.steps, 120.0, workers)
+    line = dict(metric=METRIC, value=rate, unit='cell-updates/s', n_gpus=args.gpus, steps=done, warmup=args.warmup,
+                ms_per_step=el / max(done, 1) * 1e3, higher_is_better=True, scaling='weak', vs_baseline=None,
+                dtype='f64', data='synthetic', impl='reference',
+                config=dict(workload=args.workload, grid=f"{w['nx']}x{w['ny']}", dt=w['dt'], precision='fp64'),
+                cpu_baseline=dict(value=rate, unit='cell-updates/s', cores=workers, kind='port',
+                                  sample=f'{done} AB2/CN steps of {args.workload} after setup and the start-up step'),
+                e2e=dict(value=rate, unit='cell-updates/s', h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, w, rank, world):
+    import torch
+    pkg = load_package()
+    L = pkg._lib
+    dev = int(os.environ.get('LOCAL_RANK', 0))
+    torch.cuda.set_device(dev)
+    kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
+    dt = w['dt']
+    cells = w['nx'] * w['ny']
+    s = pkg.MAC_CylinderFlow(verbose=False, **kw)
+    seeded_state(s, w)
+    stream = torch.cuda.Stream()
+    L.check(L.lib.gm_set_stream(s._h, C.c_void_p(stream.cuda_stream)), s._h)
+    s._push()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device='cuda')  # 256 MB > L2 (129 MB)
+
+    def one_step(k):
+        rc, diag = s.step_raw(dt, 1, first_index=k, start_time=s.time + 0.0)
+        if rc != L.GM_OK:
+            L.check(rc, s._h)
+        s.time = diag[0].time
+        return diag[0]
+
+    # warm-up; pick the dominant kernel class by per-step event time
+    for k in range(max(args.warmup, 3)):
+        one_step(k)
+    per_class = {}
+    for cls in KERNEL_CLASSES:
+        L.lib.gm_kernel_timing(cls, 1, None, None)
+        one_step(0)
+        tot, cnt = C.c_double(), C.c_int64()
+        L.lib.gm_kernel_timing(cls, 0, C.byref(tot), C.byref(cnt))
+        per_class[cls] = (tot.value, cnt.value)
+    L.lib.gm_kernel_timing(0, 0, None, None)
+    dominant = max(per_class, key=lambda c: per_class[c][0])
+    # timed region: K steps, each bracketed by CUDA events on the library stream, L2 flushed between
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    L.lib.gm_kernel_timing(dominant, 1, None, None)
+    launches0 = L.lib.gm_kernel_launches()
+    times = []
+    with ClockSampler(dev) as clocks:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            d = one_step(k + 1)
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            assert d.max_divergence < 1e-10
+    torch.cuda.synchronize()
+    launches = L.lib.gm_kernel_launches() - launches0
+    tot, cnt = C.c_double(), C.c_int64()
+    L.lib.gm_kernel_timing(dominant, 0, C.byref(tot), C.byref(cnt))
+    L.lib.gm_kernel_timing(0, 0, None, None)
+    step_ms = sum(times) / len(times)
+    if world > 1:
+        t = torch.tensor([step_ms], device='cuda')
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = cells * world / (step_ms * 1e-3)
+    # roofline of the dominant kernel: algorithmic bytes per launch / mean launch time
+    nx, ny = w['nx'], w['ny']
+    F = ny * (nx + 1) + (ny + 1) * nx
+    bytes_per_launch = {1: 16.0 * nx * ny, 2: 16.0 * nx * ny, 3: 8.0 * (4 * F + nx * ny), 4: 24.0 * nx * ny}[dominant]
+    mean_ms = tot.value / max(cnt.value, 1)
+    peak, peak_kind = peaks()
+    achieved = bytes_per_launch / (mean_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / 'profiles' / 'traffic.json'
+    if tfile.exists():
+        traffic = json.loads(tfile.read_text()).get(f'{args.workload}:{dominant}')
+    # end to end through the public API with host numpy arrays
+    e2e_steps = max(1, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.solve(n_steps=1, dt=dt, perturb_transient=False, save_artifacts=False, verbose=False)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    state_bytes = 8 * (ny * (nx + 1) + (ny + 1) * nx + nx * ny)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rate, done, el = oracle_rate(w, 50, 20.0, 1)
+        cpu = dict(value=rate, unit='cell-updates/s', cores=1, kind='port',
+                   sample=f'{done} AB2/CN steps of {args.workload} ({el:.1f} s) after setup and the start-up step')
+    if rank == 0:
+        line = dict(metric=METRIC, value=value, unit='cell-updates/s', n_gpus=world, steps=args.steps,
+                    warmup=args.warmup, ms_per_step=step_ms, higher_is_better=True, scaling='weak',
+                    vs_baseline=None, dtype='f64', data='synthetic',
+                    config=dict(workload=args.workload, grid=f'{nx}x{ny}', dt=dt, precision='fp64 plain',
+                                cases_per_gpu=1, parallelism='replicas', l2='flushed (256 MB write) between timed steps',
+                                pressure='DCT/DST fast inverse + boundary Schur (direct)'),
+                    roofline=dict(bound='hbm', achieved=achieved, peak=peak, unit='GB/s', frac=achieved / peak,
+                                  traffic=traffic, kernel=KERNEL_CLASSES[dominant], peak_source=peak_kind,
+                                  launches_timed=int(cnt.value), mean_launch_ms=mean_ms,
+                                  bytes_per_launch=bytes_per_launch),
+                    step_roofline=dict(algorithmic_bytes_per_cell_update=880, achieved_gbs=880.0 * cells / (step_ms * 1e-3) / 1e9),
+                    cpu_baseline=cpu,
+                    e2e=dict(value=cells / e2e_s, unit='cell-updates/s', h2d_bytes_per_step=state_bytes + 8 * ny,
+                             d2h_bytes_per_step=state_bytes + C.sizeof(L.StepDiag)),
+                    clocks=clocks.summary(), gpu_launches=int(launches),
+                    kernel_class_ms_per_step={KERNEL_CLASSES[c]: v[0] for c, v in per_class.items()})
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
+    ap.add_argument('--workload', choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    w = WORKLOADS[args.workload]
+    world = int(os.environ.get('WORLD_SIZE', 1))
+    rank = int(os.environ.get('RANK', 0))
+    if args.impl == 'reference':
+        run_reference(args, w, rank)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', 0)))
+        dist.init_process_group('nccl')
+    run_ours(args, w, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -22,7 +22,7 @@ SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_las
            'gm_set_stream', 'gm_get_indices', 'gm_get_ghost_stencils', 'gm_get_schur_rows',
            'gm_get_surface_points', 'gm_set_state', 'gm_get_state', 'gm_set_inlet', 'gm_set_history',
            'gm_get_history', 'gm_step', 'gm_apply', 'gm_project', 'gm_pressure_solve', 'gm_rectangle_solve',
-           'gm_surface_forces', 'gm_divergence_stats')
+           'gm_surface_forces', 'gm_divergence_stats', 'gm_kernel_launches', 'gm_kernel_timing')
 
 
 class Config(C.Structure):
@@ -87,6 +87,8 @@ def _load():
         'gm_rectangle_solve': ([P, I32, D, P, P], C.c_int),
         'gm_surface_forces': ([P, P, P, P, D, P], C.c_int),
         'gm_divergence_stats': ([P, P, P, P, P], C.c_int),
+        'gm_kernel_launches': ([], I64),
+        'gm_kernel_timing': ([I32, I32, C.POINTER(D), C.POINTER(I64)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

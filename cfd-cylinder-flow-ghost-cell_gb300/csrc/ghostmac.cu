@@ -625,9 +625,10 @@ int gm_create(const gm_config* cfg, gm_handle** out) {
     CK(cudaGetDevice(&H->device));
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, H->device));
-    H->smem_optin = (size_t)optin;
-    configure_kernels(optin);
-    CK(cudaGetLastError());
+    int dyn = configure_kernels(optin);
+    cudaGetLastError();
+    if (dyn < 48 * 1024) throw CudaError("cannot enable large shared memory for the transform kernels");
+    H->smem_optin = (size_t)dyn;
     CK(cudaStreamCreateWithFlags(&H->st, cudaStreamNonBlocking));
     cudaStream_t st = H->st;
     H->F = g.usize + g.vsize;
@@ -901,6 +902,7 @@ int gm_step(gm_handle* h, double dt, int32_t n_steps, int64_t first_step_index, 
       step_once(h, dt, screen);
       CK(cudaMemcpyAsync(h->host_ctl, h->ctl.p, sizeof(StepCtl), cudaMemcpyDeviceToHost, h->st));
       CK(cudaStreamSynchronize(h->st));
+      ktimer_collect();
       double t = start_time + (s + 1) * dt;
       if (diag) fill_diag(h, *h->host_ctl, t, dt, first, &diag[s]);
       if (h->host_ctl->err) check_ctl(h, "step");
@@ -1127,6 +1129,23 @@ int gm_divergence_stats(gm_handle* h, const double* u, const double* v, double o
     counts[0] = (int64_t)std::llround(r[2]);
     counts[1] = (int64_t)std::llround(r[4]);
   });
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int64_t gm_kernel_launches(void) { return (int64_t)kernel_launch_count(); }
+
+int gm_kernel_timing(int32_t kernel_class, int32_t enable, double* total_ms, int64_t* count) {
+  if (enable) ktimer_enable(kernel_class);
+  double t = 0;
+  long long n = 0;
+  ktimer_read(&t, &n);
+  if (total_ms) *total_ms = t;
+  if (count) *count = (int64_t)n;
+  if (!enable && kernel_class == 0) ktimer_enable(0);
+  return GM_OK;
 }
 
 }  // extern "C"

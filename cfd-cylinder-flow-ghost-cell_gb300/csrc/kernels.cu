@@ -1,4 +1,7 @@
 // Kernels of the ghost-cell AB2/CN step (sm_103a).  See kernels.cuh for the layout.
+#include <algorithm>
+#include <atomic>
+#include <vector>
 #include <cmath>
 #include <cstdio>
 
@@ -57,6 +60,54 @@ __device__ void block_commit_sum(double v, double* dst) {
 __device__ __forceinline__ unsigned long long absbits(double v) { return dbits(fabs(v)); }
 
 static inline unsigned blocks_for(int64_t n, int tpb = TPB) { return (unsigned)((n + tpb - 1) / tpb); }
+
+// Host-side count of kernel launches issued by this library (all launchers call note_launch).
+static std::atomic<long long> g_launches{0};
+static inline void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long long kernel_launch_count() { return g_launches.load(); }
+
+// Optional CUDA-event timing of one kernel class on its own stream (used by the
+// benchmark to time the dominant kernel inside the timed region).
+namespace {
+struct KTimer {
+  int cls = 0;
+  std::vector<cudaEvent_t> ev;
+  int used = 0;
+  double total_ms = 0;
+  long long count = 0;
+};
+KTimer g_kt;
+}  // namespace
+static inline void kt_mark(int cls, cudaStream_t st) {
+  if (g_kt.cls != cls || g_kt.used >= (int)g_kt.ev.size()) return;
+  cudaEventRecord(g_kt.ev[g_kt.used++], st);
+}
+void ktimer_enable(int cls) {
+  if (g_kt.ev.empty()) {
+    g_kt.ev.resize(1024);
+    for (auto& e : g_kt.ev) cudaEventCreate(&e);
+  }
+  g_kt.cls = cls;
+  g_kt.used = 0;
+  g_kt.total_ms = 0;
+  g_kt.count = 0;
+}
+// Folds the recorded pairs into the totals (the stream must be synchronised).
+void ktimer_collect() {
+  for (int i = 0; i + 1 < g_kt.used; i += 2) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, g_kt.ev[i], g_kt.ev[i + 1]) == cudaSuccess) {
+      g_kt.total_ms += ms;
+      g_kt.count += 1;
+    }
+  }
+  cudaGetLastError();
+  g_kt.used = 0;
+}
+void ktimer_read(double* total_ms, long long* count) {
+  *total_ms = g_kt.total_ms;
+  *count = g_kt.count;
+}
 
 // ---------------------------------------------------------------------------
 // separable inverse: x pass (rows) and y pass (columns with eigenvalue scaling)
@@ -126,11 +177,23 @@ __global__ void k_ypass(int n /*rows*/, int cols, int tf, int ti, FftPlan plan, 
   }
 }
 
-void configure_kernels(int smem_optin) {
-  cudaFuncSetAttribute(k_xpass<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin);
-  cudaFuncSetAttribute(k_ypass<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin);
-  cudaFuncSetAttribute(k_xpass<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin);
-  cudaFuncSetAttribute(k_ypass<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin);
+// Opts the transform kernels into the large dynamic shared memory carve-out; returns the
+// dynamic bytes every one of them may use (the opt-in limit minus their static shared memory).
+template <typename K>
+static int allow_dynamic_smem(K kernel, int optin) {
+  cudaFuncAttributes a;
+  if (cudaFuncGetAttributes(&a, kernel) != cudaSuccess) return 0;
+  int dyn = optin - (int)a.sharedSizeBytes;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess) return 0;
+  return dyn;
+}
+int configure_kernels(int smem_optin) {
+  int d = smem_optin;
+  d = std::min(d, allow_dynamic_smem(k_xpass<double>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ypass<double>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_xpass<float>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ypass<float>, smem_optin));
+  return d;
 }
 
 void launch_rect_inverse(const TransformTables& tt, const RectView& v, const double* b, bool mask_in,
@@ -141,14 +204,23 @@ void launch_rect_inverse(const TransformTables& tt, const RectView& v, const dou
   R2RTables<double> txi{(const C*)tt.Wx, (const C*)tt.prex_inv, (const C*)tt.postx_inv};
   R2RTables<double> ty{(const C*)tt.Wy, (const C*)tt.prey, (const C*)tt.posty};
   unsigned gx = (unsigned)((v.rows + tt.lpb_x - 1) / tt.lpb_x);
+  note_launch();
+  kt_mark(1, st);
   k_xpass<double><<<gx, 128, tt.smem_x, st>>>(v.cols, v.rows, tt.tx_fwd, tt.plan_x, tx, b, v.base, v.pitch,
                                               mask_in ? v.cls : nullptr, spectral, 0, v.cols, nullptr, nullptr,
                                               nullptr, tt.lpb_x, gate);
+  kt_mark(1, st);
   unsigned gy = (unsigned)((v.cols + tt.lpb_y - 1) / tt.lpb_y);
+  note_launch();
+  kt_mark(2, st);
   k_ypass<double><<<gy, 128, tt.smem_y, st>>>(v.rows, v.cols, tt.ty_fwd, tt.ty_inv, tt.plan_y, ty, tt.recip,
                                               spectral, tt.lpb_y, gate);
+  kt_mark(2, st);
+  note_launch();
+  kt_mark(1, st);
   k_xpass<double><<<gx, 128, tt.smem_x, st>>>(v.cols, v.rows, tt.tx_inv, tt.plan_x, txi, spectral, 0, v.cols,
                                               nullptr, out, v.base, v.pitch, v.cls, sub, add, tt.lpb_x, gate);
+  kt_mark(1, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -188,6 +260,7 @@ void launch_schur(const double* first, const RectView& view, int rank, const int
                   cudaStream_t st) {
   if (rank <= 0) return;
   unsigned g = (unsigned)((rank + SCHUR_ROWS - 1) / SCHUR_ROWS);
+  note_launch();
   k_schur<<<g, 256, rank * sizeof(double), st>>>(first, view, rank, rows, c_ptr, c_col, c_val, sinv, w2, gate);
 }
 
@@ -207,6 +280,7 @@ __global__ void k_ghost(double* __restrict__ f, int n, const int64_t* __restrict
 void launch_ghost(double* field, int n, const int64_t* rows, const int64_t* ptr, const int64_t* col,
                   const double* val, const Gate& gate, cudaStream_t st) {
   if (n <= 0) return;
+  note_launch();
   k_ghost<<<blocks_for(n, 128), 128, 0, st>>>(field, n, rows, ptr, col, val, gate);
 }
 
@@ -352,7 +426,10 @@ __global__ void k_momentum(CaseDev c, MomentumArgs a, Gate gate) {
 }
 
 void launch_momentum(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st) {
+  note_launch();
+  kt_mark(3, st);
   k_momentum<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, gate);
+  kt_mark(3, st);
 }
 
 __global__ void k_advection(CaseDev c, const double* __restrict__ U, double* __restrict__ out, Gate gate) {
@@ -373,6 +450,7 @@ __global__ void k_advection(CaseDev c, const double* __restrict__ U, double* __r
   out[t] = r;
 }
 void launch_advection(const CaseDev& c, const double* U, double* out, const Gate& gate, cudaStream_t st) {
+  note_launch();
   k_advection<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, U, out, gate);
 }
 
@@ -391,6 +469,7 @@ __global__ void k_diffusion(CaseDev c, const double* __restrict__ U, double* __r
 }
 void launch_diffusion(const CaseDev& c, const double* U, double* out, bool with_inlet, double hdt, const Gate& gate,
                       cudaStream_t st) {
+  note_launch();
   k_diffusion<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, U, out, with_inlet ? 1 : 0, hdt, gate);
 }
 
@@ -405,6 +484,7 @@ __global__ void k_gradient(CaseDev c, const double* __restrict__ P, double* __re
   out[t] = comp == 0 ? grad_u(P, g, j, i, (1.0 / c.dx) / c.rho) : grad_v(P, g, j, i, (1.0 / c.dy) / c.rho);
 }
 void launch_gradient(const CaseDev& c, const double* P, double* out, const Gate& gate, cudaStream_t st) {
+  note_launch();
   k_gradient<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, P, out, gate);
 }
 
@@ -505,7 +585,10 @@ __global__ void k_residual(CaseDev c, int kind, double hc, const double* __restr
 void launch_residual(const CaseDev& c, int kind, double hc, const double* b, const double* x, double* res,
                      SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st) {
   int64_t n = kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize);
+  note_launch();
+  kt_mark(4, st);
   k_residual<<<blocks_for(n), TPB, 0, st>>>(c, kind, hc, b, x, res, sc, check, first_check ? 1 : 0, gate);
+  kt_mark(4, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -538,6 +621,7 @@ __global__ void k_divergence(CaseDev c, const double* __restrict__ U, double* __
 void launch_divergence(const CaseDev& c, const double* U, double* out, double scale, SolveCtl* sc,
                        unsigned long long* divmax, int gate_on_nonfinite, const Gate& gate, cudaStream_t st) {
   (void)sc;
+  note_launch();
   k_divergence<<<blocks_for(c.psize), TPB, 0, st>>>(c, U, out, scale, divmax, gate_on_nonfinite, gate.ctl, gate);
 }
 
@@ -559,6 +643,7 @@ __global__ void k_project_update(CaseDev c, const double* __restrict__ q, const 
 void launch_project_update(const CaseDev& c, const double* q, const double* phi, double dt, double* out,
                            const SolveCtl* psolve, const Gate& gate, cudaStream_t st) {
   (void)psolve;
+  note_launch();
   k_project_update<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, q, phi, dt, out, gate);
 }
 
@@ -583,6 +668,7 @@ __global__ void k_defect(CaseDev c, const double* __restrict__ r, const double* 
 }
 void launch_defect(const CaseDev& c, const double* result, const double* rhs, double hdt, double* action,
                    double* proj, const Gate& gate, cudaStream_t st) {
+  note_launch();
   k_defect<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, result, rhs, hdt, action, proj, gate);
 }
 
@@ -620,6 +706,7 @@ __global__ void k_pressure_out(CaseDev c, const double* __restrict__ p, const do
 void launch_pressure_out(const CaseDev& c, const double* p, const double* inc, double factor, double dt,
                          const double* action, const double* rhs, double* half, double* pout,
                          unsigned long long* coupled, const Gate& gate, cudaStream_t st) {
+  note_launch();
   k_pressure_out<<<blocks_for(c.usize + c.vsize + c.psize), TPB, 0, st>>>(c, p, inc, factor, dt, action, rhs, half,
                                                                           pout, coupled, gate);
 }
@@ -636,6 +723,7 @@ __global__ void k_maxabs(CaseDev c, const double* __restrict__ U, unsigned long 
 }
 void launch_maxabs(const CaseDev& c, const double* U, unsigned long long* umax, unsigned long long* vmax,
                    const Gate& gate, cudaStream_t st) {
+  note_launch();
   k_maxabs<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, U, umax, vmax, gate);
 }
 
@@ -698,6 +786,7 @@ __global__ void k_forces(CaseDev c, const double* __restrict__ U, const double* 
 }
 void launch_forces(const CaseDev& c, const double* U, const double* P, double mu, double dt, StepCtl* ctl,
                    int check_gates, double* out6, const Gate& gate, cudaStream_t st) {
+  note_launch();
   k_forces<<<1, 256, 0, st>>>(c, U, P, mu, dt, ctl, check_gates, out6, gate);
 }
 
@@ -716,7 +805,10 @@ __global__ void k_gate_momentum(StepCtl* ctl) {
   double thr = 1e-10 * (bm > 1.0 ? bm : 1.0);
   if (bad || !(r <= thr)) raise_gate(ctl, 2, 2);
 }
-void launch_gate_momentum(StepCtl* ctl, cudaStream_t st) { k_gate_momentum<<<1, 1, 0, st>>>(ctl); }
+void launch_gate_momentum(StepCtl* ctl, cudaStream_t st) {
+  note_launch();
+  k_gate_momentum<<<1, 1, 0, st>>>(ctl);
+}
 
 __global__ void k_gate_pressure(StepCtl* ctl, int slot) {
   if (ctl->err) return;
@@ -729,14 +821,20 @@ __global__ void k_gate_pressure(StepCtl* ctl, int slot) {
   t = bound > t ? bound : t;
   if (sc->xbad || !(linf <= t)) raise_gate(ctl, 2, 3);
 }
-void launch_gate_pressure(StepCtl* ctl, int slot, cudaStream_t st) { k_gate_pressure<<<1, 1, 0, st>>>(ctl, slot); }
+void launch_gate_pressure(StepCtl* ctl, int slot, cudaStream_t st) {
+  note_launch();
+  k_gate_pressure<<<1, 1, 0, st>>>(ctl, slot);
+}
 
 __global__ void k_gate_projection(StepCtl* ctl, int k) {
   if (ctl->err) return;
   double d = bits2d(ctl->div_max[k]);
   if (!(d <= 1e-10)) raise_gate(ctl, 2, 1);
 }
-void launch_gate_projection(StepCtl* ctl, int k, cudaStream_t st) { k_gate_projection<<<1, 1, 0, st>>>(ctl, k); }
+void launch_gate_projection(StepCtl* ctl, int k, cudaStream_t st) {
+  note_launch();
+  k_gate_projection<<<1, 1, 0, st>>>(ctl, k);
+}
 
 // CFL screen of solver/main.py:273-278 (screen != 0) and the finite-field check of
 // solver/time_integration.py:15-17 on the velocity maxima of the current state.
@@ -749,6 +847,7 @@ __global__ void k_cfl_screen(StepCtl* ctl, const unsigned long long* umax, const
 }
 void launch_cfl_screen(StepCtl* ctl, const unsigned long long* umax, const unsigned long long* vmax, double dt,
                        double dx, double dy, int screen, cudaStream_t st) {
+  note_launch();
   k_cfl_screen<<<1, 1, 0, st>>>(ctl, umax, vmax, dt, dx, dy, screen);
 }
 
@@ -760,6 +859,7 @@ __global__ void k_copy_active(const uint8_t* __restrict__ cls, int64_t n, const 
 }
 void launch_copy_active(const uint8_t* cls, int64_t n, const double* src, double* dst, const Gate& gate,
                         cudaStream_t st) {
+  note_launch();
   k_copy_active<<<blocks_for(n), TPB, 0, st>>>(cls, n, src, dst, gate);
 }
 
@@ -768,6 +868,7 @@ __global__ void k_set_inlet(CaseDev c, double* U, int zero) {
   if (j < c.ny) U[(int64_t)j * (c.nx + 1)] = zero ? 0.0 : c.inlet[j];
 }
 void launch_set_inlet(const CaseDev& c, double* U, bool zero, cudaStream_t st) {
+  note_launch();
   k_set_inlet<<<blocks_for(c.ny, 128), 128, 0, st>>>(c, U, zero ? 1 : 0);
 }
 
@@ -797,6 +898,7 @@ __global__ void k_div_stats(CaseDev c, const double* __restrict__ U, const uint8
   block_commit_sum(cn, &out5[4]);
 }
 void launch_divergence_stats(const CaseDev& c, const double* U, const uint8_t* mask, double* out5, cudaStream_t st) {
+  note_launch();
   k_div_stats<<<blocks_for(c.psize), TPB, 0, st>>>(c, U, mask, out5);
 }
 
@@ -811,10 +913,16 @@ __global__ void k_scatter(const double* __restrict__ src, const int64_t* __restr
   if (t < n) dst[idx[t]] = src[t];
 }
 void launch_gather(const double* src, const int64_t* idx, int64_t n, double* dst, cudaStream_t st) {
-  if (n > 0) k_gather<<<blocks_for(n), TPB, 0, st>>>(src, idx, n, dst);
+  if (n > 0) {
+    note_launch();
+    k_gather<<<blocks_for(n), TPB, 0, st>>>(src, idx, n, dst);
+  }
 }
 void launch_scatter(const double* src, const int64_t* idx, int64_t n, double* dst, cudaStream_t st) {
-  if (n > 0) k_scatter<<<blocks_for(n), TPB, 0, st>>>(src, idx, n, dst);
+  if (n > 0) {
+    note_launch();
+    k_scatter<<<blocks_for(n), TPB, 0, st>>>(src, idx, n, dst);
+  }
 }
 
 __global__ void k_schur_column(const double* __restrict__ first, RectView v, int rank, const int64_t* __restrict__ cp,
@@ -831,7 +939,10 @@ __global__ void k_schur_column(const double* __restrict__ first, RectView v, int
 }
 void launch_schur_column(const double* first, const RectView& view, int rank, const int64_t* c_ptr,
                          const int64_t* c_col, const double* c_val, double* S, int col, cudaStream_t st) {
-  if (rank > 0) k_schur_column<<<blocks_for(rank, 128), 128, 0, st>>>(first, view, rank, c_ptr, c_col, c_val, S, col);
+  if (rank > 0) {
+    note_launch();
+    k_schur_column<<<blocks_for(rank, 128), 128, 0, st>>>(first, view, rank, c_ptr, c_col, c_val, S, col);
+  }
 }
 
 }  // namespace gmk

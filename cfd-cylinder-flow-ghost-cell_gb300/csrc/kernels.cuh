@@ -151,7 +151,12 @@ struct TransformTables {      // device tables of one rectangle kind (FP64)
 };
 
 // ---- launchers (kernels.cu) ------------------------------------------------
-void configure_kernels(int smem_optin);
+int configure_kernels(int smem_optin);
+long long kernel_launch_count();
+// kernel classes for event timing: 1 x pass, 2 y pass, 3 momentum, 4 residual
+void ktimer_enable(int cls);
+void ktimer_collect();
+void ktimer_read(double* total_ms, long long* count);
 // x = T^{-1} b on the rectangle view; b is read through the active mask when
 // mask_in is set; the output epilogue is
 //   out = active ? (add + sub - T^{-1} b) : 0   when sub != nullptr

@@ -181,6 +181,16 @@ int gm_surface_forces(gm_handle* h, const double* u, const double* v, const doub
  * (solver/src/bindings.cpp:343-390): out = max, sum div^2, core sum div^2; counts = count, core count. */
 int gm_divergence_stats(gm_handle* h, const double* u, const double* v, double out[3], int64_t counts[2]);
 
+/* --- instrumentation (no reference counterpart) -------------------------------- */
+
+/* Number of CUDA kernels this library has launched in this process. */
+int64_t gm_kernel_launches(void);
+/* CUDA-event timing of one kernel class on the stream it runs on: 1 transform x pass,
+ * 2 transform y pass, 3 momentum right-hand side, 4 operator residual.  enable = 1 starts
+ * (and clears) timing of that class; every call returns the totals so far.  Class 0
+ * with enable = 0 stops timing. */
+int gm_kernel_timing(int32_t kernel_class, int32_t enable, double* total_ms, int64_t* count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,17 +39,17 @@ def G():
 
 def test_rectangle_transforms(pkg):
     G = np.load(GOLDEN / 'rectangle_24x10.npz')
-    s = pkg.MAC_CylinderFlow(nx=24, ny=10, Lx=7.2, Ly=2.5, D=1.0, xc=3.6, yc=1.25, nu=0.02, rho=1.3, verbose=False)
+    s = pkg.MAC_CylinderFlow(nx=24, ny=10, Lx=7.2, Ly=2.5, D=0.4, xc=3.6, yc=1.25, nu=0.02, rho=1.3, verbose=False)
     for kind in ('pressure', 'u', 'v'):
         x = s.gg.rectangle_solve(kind, G[f'{kind}_in'], dt=0.004)
         assert rel(x, G[f'{kind}_out']) < 1e-12, kind
 
 
-@pytest.mark.parametrize('n', [(40, 30), (88, 16), (400, 200), (256, 128), (820, 410)])
+@pytest.mark.parametrize('n', [(40, 30, 0.5), (88, 16, 0.3), (400, 200, 1.0), (256, 128, 1.0), (820, 410, 1.0)])
 def test_rectangle_transforms_sizes(pkg, n):
-    nx, ny = n
+    nx, ny, D = n
     h = 0.05
-    s = pkg.MAC_CylinderFlow(nx=nx, ny=ny, Lx=nx * h, Ly=ny * h, D=1.0, xc=nx * h / 4, yc=ny * h / 2, nu=0.01,
+    s = pkg.MAC_CylinderFlow(nx=nx, ny=ny, Lx=nx * h, Ly=ny * h, D=D, xc=nx * h / 4, yc=ny * h / 2, nu=0.01,
                              verbose=False)
     rng = np.random.default_rng(nx)
     for kind in ('pressure', 'u', 'v'):
