@@ -264,7 +264,7 @@ def run_ours(args, w, rank, world):
                     cpu_baseline=cpu,
                     e2e=dict(value=cells / e2e_s, unit='cell-updates/s', h2d_bytes_per_step=state_bytes + 8 * ny,
                              d2h_bytes_per_step=state_bytes + C.sizeof(L.StepDiag)),
-                    clocks=clocks.summary(), gpu_launches=int(launches),
+                    clocks=clocks.summary(), gpu_launches=int(launches), launches_before_timed=int(launches0),
                     kernel_class_ms_per_step={KERNEL_CLASSES[c]: v[0] for c, v in per_class.items()})
         print(json.dumps(line), flush=True)
 
