@@ -22,7 +22,9 @@ SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_las
            'gm_set_stream', 'gm_get_indices', 'gm_get_ghost_stencils', 'gm_get_schur_rows',
            'gm_get_surface_points', 'gm_set_state', 'gm_get_state', 'gm_set_inlet', 'gm_set_history',
            'gm_get_history', 'gm_step', 'gm_apply', 'gm_project', 'gm_pressure_solve', 'gm_rectangle_solve',
-           'gm_surface_forces', 'gm_divergence_stats', 'gm_kernel_launches', 'gm_kernel_timing')
+           'gm_surface_forces', 'gm_divergence_stats', 'gm_kernel_launches', 'gm_kernel_timing',
+           'gm_divergence_stats_noalloc')
+NOALLOC_MAX_CELLS = 1048576
 
 
 class Config(C.Structure):
@@ -89,6 +91,7 @@ def _load():
         'gm_divergence_stats': ([P, P, P, P, P], C.c_int),
         'gm_kernel_launches': ([], I64),
         'gm_kernel_timing': ([I32, I32, C.POINTER(D), C.POINTER(I64)], C.c_int),
+        'gm_divergence_stats_noalloc': ([P, P, P, I32, I32, D, D, P, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

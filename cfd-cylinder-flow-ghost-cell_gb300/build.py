@@ -50,6 +50,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
           '-o', str(BUILD / 'kernels.o')]),
         ([nvcc, *ARCH, '-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', *inc, '-c', str(SRC / 'ghostmac.cu'),
           '-o', str(BUILD / 'ghostmac.o')]),
+        ([nvcc, *ARCH, '-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', *inc, '-c', str(SRC / 'noalloc.cu'),
+          '-o', str(BUILD / 'noalloc.o')]),
     ]
     procs = [subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True) for cmd in jobs]
     failed = []
@@ -63,7 +65,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         raise RuntimeError('build failed:\n' + '\n'.join(f'{c}\n{o}' for c, o in failed))
     tmp = OUT.with_suffix('.so.tmp')
     link = [nvcc, *ARCH, '-shared', '-o', str(tmp), str(BUILD / 'geometry.o'), str(BUILD / 'kernels.o'),
-            str(BUILD / 'ghostmac.o'), '-lcudart']
+            str(BUILD / 'ghostmac.o'), str(BUILD / 'noalloc.o'), '-lcudart']
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode:
         raise RuntimeError('link failed:\n' + r.stdout + r.stderr)

@@ -18,9 +18,21 @@
 
 using namespace gmk;
 
+// Last error of a call made without a handle (gm_create, gm_create_host and the
+// allocation-free entry point); a fixed buffer so that setting it allocates nothing.
+static char g_global_error[512];
+void gm_internal_set_error(const char* msg) {
+  std::strncpy(g_global_error, msg ? msg : "", sizeof g_global_error - 1);
+  g_global_error[sizeof g_global_error - 1] = 0;
+}
+
 namespace {
 
-std::string g_create_error;
+struct GlobalError {
+  GlobalError& operator=(const std::string& m) { gm_internal_set_error(m.c_str()); return *this; }
+  GlobalError& operator=(const char* m) { gm_internal_set_error(m); return *this; }
+};
+GlobalError g_create_error;
 
 struct CudaError : std::exception {
   std::string msg;
@@ -601,7 +613,7 @@ void initial_state(gm_handle* h) {
 // =============================================================================
 extern "C" {
 
-const char* gm_last_error(const gm_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+const char* gm_last_error(const gm_handle* h) { return h ? h->err.c_str() : g_global_error; }
 
 
 int gm_create(const gm_config* cfg, gm_handle** out) {

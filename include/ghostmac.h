@@ -181,6 +181,22 @@ int gm_surface_forces(gm_handle* h, const double* u, const double* v, const doub
  * (solver/src/bindings.cpp:343-390): out = max, sum div^2, core sum div^2; counts = count, core count. */
 int gm_divergence_stats(gm_handle* h, const double* u, const double* v, double out[3], int64_t counts[2]);
 
+/* --- allocation-free entry point ------------------------------------------------ */
+
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc (code
+ * running inside another runtime's fixed device-memory arena, or tools that only
+ * borrow device arrays): the fluid-cell divergence statistics of gm_divergence_stats
+ * computed from caller-owned DEVICE arrays u (ny x nx+1), v (ny+1 x nx) and mask
+ * (ny x nx bytes, nonzero = solid) without any allocation.  Its scratch is a static
+ * device array sized for at most GM_NOALLOC_MAX_CELLS cells (larger grids return
+ * GM_EVALUE), held by every GPU that loads the library.  The first call on a device
+ * looks up that array's address for the device (make it before any stream capture);
+ * calls that overlap on the GPU share the array and race.  out = max |div|,
+ * sum div^2, core sum div^2; counts = fluid cells, core cells.  Errors: gm_last_error(NULL). */
+#define GM_NOALLOC_MAX_CELLS 1048576
+int gm_divergence_stats_noalloc(const double* u, const double* v, const uint8_t* mask, int32_t nx, int32_t ny,
+                                double dx, double dy, double out[3], int64_t counts[2], void* cuda_stream);
+
 /* --- instrumentation (no reference counterpart) -------------------------------- */
 
 /* Number of CUDA kernels this library has launched in this process. */
