@@ -117,7 +117,7 @@ std::vector<double> cexp_table(int count, double scale_num, double scale_den, do
 struct RectDev {
   TransformTables tt{};
   RectView view{};
-  DBuf<double> Wx, prex, postx, Wy, prey, posty, recip;
+  DBuf<double> Wx, prex, postx, t0, t1, t2;
   // Schur data
   int rank = 0;
   DBuf<int64_t> rows, cptr, ccol;
@@ -182,24 +182,86 @@ void upload_csr(Csrd& d, const std::vector<int64_t>& rows, const gm::Csr& c, cud
   d.val.upload(c.val, st);
 }
 
-// x / y tables of a rectangle kind
+// Chunk layout of an n-row column: P chunks of inner rows separated by P-1 interface rows.
+YChunks make_chunks(int n) {
+  YChunks c{};
+  int P = std::max(1, (n + 1) / (32 + 1));
+  P = std::min(P, YCHUNK_MAX);
+  int inner = n - (P - 1);  // rows that are not interfaces
+  int r = 0;
+  for (int p = 0; p < P; ++p) {
+    int m = inner / P + (p < inner % P ? 1 : 0);
+    c.start[p] = r;
+    c.end[p] = r + m - 1;
+    r += m + 1;  // skip the interface row after the chunk
+  }
+  c.P = P;
+  return c;
+}
+
+// Partition-method tables of the column systems (see k_ysolve).  main(j) is the
+// diagonal of row j for this x-mode, gamma the constant off-diagonal.
+void ysolve_tables(const YChunks& ch, int n, int cols, int kx, const std::vector<double>& main, double gamma,
+                   double* t0, double* t1, double* t2) {
+  auto at = [&](int j) { return (size_t)j * cols + kx; };
+  std::vector<double> inv(n, 0.0), v(n, 0.0), w(n, 0.0), tmp(n);
+  for (int p = 0; p < ch.P; ++p) {
+    int a = ch.start[p], b = ch.end[p];
+    double piv = main[a];
+    inv[a] = 1.0 / piv;
+    for (int j = a + 1; j <= b; ++j) {
+      piv = main[j] - gamma * gamma * inv[j - 1];
+      inv[j] = 1.0 / piv;
+    }
+    // spikes: A_in v = gamma e_a (p > 0), A_in w = gamma e_b (p < P-1)
+    auto solve_unit = [&](int at_row, std::vector<double>& out) {
+      double prev = 0;
+      for (int j = a; j <= b; ++j) {
+        double d = (j == at_row) ? gamma : 0.0;
+        prev = (d - gamma * prev) * inv[j];
+        tmp[j] = prev;
+      }
+      out[b] = tmp[b];
+      for (int j = b - 1; j >= a; --j) out[j] = tmp[j] - gamma * inv[j] * out[j + 1];
+    };
+    if (p > 0) solve_unit(a, v);
+    if (p < ch.P - 1) solve_unit(b, w);
+    for (int j = a; j <= b; ++j) { t0[at(j)] = inv[j]; t1[at(j)] = v[j]; t2[at(j)] = w[j]; }
+  }
+  // interface system: sub_q y_{q-1} + main_q y_q + sup_q y_{q+1} = rhs_q
+  double cr_prev = 0;
+  for (int q = 0; q < ch.P - 1; ++q) {
+    int e = ch.end[q] + 1;
+    int bL = ch.end[q], aR = ch.start[q + 1];
+    double sub = -gamma * v[bL];
+    double mid = main[e] - gamma * w[bL] - gamma * v[aR];
+    double sup = -gamma * w[aR];
+    double piv = mid - sub * cr_prev;
+    double rinv = 1.0 / piv;
+    double cr = sup * rinv;
+    t0[at(e)] = rinv;
+    t1[at(e)] = sub;
+    t2[at(e)] = cr;
+    cr_prev = cr;
+  }
+}
+
+// x transform tables and y partition tables of a rectangle kind
+// (solver/rectangular_inverse.py:8-58: same operator, y direction solved exactly per x-mode)
 void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
   const gm::Geometry& g = h->g;
   const int nx = g.nx, ny = g.ny;
   int rows = kind == 2 ? ny - 1 : ny, cols = nx;
-  int tx_f, tx_i, ty_f, ty_i;
-  double fy;
-  if (kind == 0) { tx_f = DCT4; tx_i = DCT4; ty_f = DCT2; ty_i = DCT3; fy = 0.0; }
-  else if (kind == 1) { tx_f = DST3; tx_i = DST2; ty_f = DST2; ty_i = DST3; fy = 1.0; }
-  else { tx_f = DST4; tx_i = DST4; ty_f = DST1; ty_i = DST1; fy = 1.0; }
+  int tx_f, tx_i;
+  if (kind == 0) { tx_f = DCT4; tx_i = DCT4; }
+  else if (kind == 1) { tx_f = DST3; tx_i = DST2; }
+  else { tx_f = DST4; tx_i = DST4; }
   TransformTables& tt = rd.tt;
-  tt.tx_fwd = tx_f; tt.tx_inv = tx_i; tt.ty_fwd = ty_f; tt.ty_inv = ty_i;
-  int Mx = r2r_fft_length(tx_f, cols), My = r2r_fft_length(ty_f, rows);
+  tt.tx_fwd = tx_f; tt.tx_inv = tx_i;
+  int Mx = r2r_fft_length(tx_f, cols);
   tt.plan_x = make_plan(Mx);
-  tt.plan_y = make_plan(My);
   cudaStream_t st = h->st;
   rd.Wx.upload(cexp_table(Mx, 2.0, Mx, 0.0, -1), st);
-  rd.Wy.upload(cexp_table(My, 2.0, My, 0.0, -1), st);
   // type IV: pre exp(-i pi (4m+1)/(4n)), post exp(-i pi k/n); Makhoul: (cos, sin)(pi k/(2n))
   if (r2r_family(tx_f) == 2) {
     rd.prex.upload(cexp_table(cols / 2, 4.0, 4.0 * cols, 1.0, -1), st);
@@ -208,52 +270,53 @@ void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
     rd.prex.upload(cexp_table(1, 0, 1, 0, 1), st);
     rd.postx.upload(cexp_table(cols, 1.0, 2.0 * cols, 0.0, +1), st);
   }
-  if (r2r_family(ty_f) == 0) {
-    rd.prey.upload(cexp_table(1, 0, 1, 0, 1), st);
-    rd.posty.upload(cexp_table(rows, 1.0, 2.0 * rows, 0.0, +1), st);
-  } else {
-    rd.prey.upload(cexp_table(1, 0, 1, 0, 1), st);
-    rd.posty.upload(cexp_table(1, 0, 1, 0, 1), st);
-  }
   tt.Wx = rd.Wx.p; tt.prex = rd.prex.p; tt.postx = rd.postx.p;
   tt.prex_inv = rd.prex.p; tt.postx_inv = rd.postx.p;
-  tt.Wy = rd.Wy.p; tt.prey = rd.prey.p; tt.posty = rd.posty.p;
-  // eigenvalue table (solver/rectangular_inverse.py:39-46) with the 1/(4 nx ny) of the inverse transforms
-  std::vector<double> recip((size_t)rows * cols);
+  // column systems: pressure (L_y + lambda_x)/rho; Helmholtz (1 - c lambda_x) - c L_y, c = dt/2 nu
   const double PI = 3.141592653589793;
-  for (int ky = 0; ky < rows; ++ky) {
-    double sy = ((double)ky + fy) * PI / (2 * ny);
-    double ry = 4 * std::pow(std::sin(sy), 2) / (g.dy * g.dy);
-    for (int kx = 0; kx < cols; ++kx) {
-      double sx = ((double)kx + 0.5) * PI / (2 * nx);
-      double rate = ry + 4 * std::pow(std::sin(sx), 2) / (g.dx * g.dx);
-      double div = kind == 0 ? -rate / g.rho : 1 + ((0.5 * dt) * g.nu) * rate;
-      recip[(size_t)ky * cols + kx] = 1.0 / (div * (4.0 * nx * ny));
-    }
+  const double idy2 = 1.0 / (g.dy * g.dy);
+  std::vector<double> ly(rows);
+  for (int j = 0; j < rows; ++j) {
+    double m = -2.0;
+    if (kind == 0 && (j == 0 || j == rows - 1)) m = -1.0;
+    if (kind == 1 && (j == 0 || j == rows - 1)) m = -3.0;
+    ly[j] = m * idy2;
   }
-  rd.recip.upload(recip, st);
-  tt.recip = rd.recip.p;
-  // lines per block and shared memory
+  const double c = (0.5 * dt) * g.nu;
+  tt.gamma = kind == 0 ? idy2 / g.rho : -c * idy2;
+  tt.yscale = 1.0 / (2.0 * nx);
+  tt.ych = make_chunks(rows);
+  std::vector<double> t0((size_t)rows * cols), t1((size_t)rows * cols), t2((size_t)rows * cols), mainj(rows);
+  for (int kx = 0; kx < cols; ++kx) {
+    double sx = ((double)kx + 0.5) * PI / (2 * nx);
+    double lam = -4 * std::pow(std::sin(sx), 2) / (g.dx * g.dx);
+    for (int j = 0; j < rows; ++j) mainj[j] = kind == 0 ? (ly[j] + lam) / g.rho : 1.0 - c * (lam + ly[j]);
+    ysolve_tables(tt.ych, rows, cols, kx, mainj, tt.gamma, t0.data(), t1.data(), t2.data());
+  }
+  rd.t0.upload(t0, st);
+  rd.t1.upload(t1, st);
+  rd.t2.upload(t2, st);
+  tt.t0 = rd.t0.p; tt.t1 = rd.t1.p; tt.t2 = rd.t2.p;
+  // launch shapes
   auto smem_for = [](int type, int n, int lpb) {
     size_t stage = ((size_t)lpb * n * sizeof(double) + 15) / 16 * 16;
     return stage + 2 * (size_t)r2r_buffer_elems(type, n, lpb) * sizeof(cplx<double>);
   };
-  auto pick = [&](int type, int n, int lines, size_t& smem) {
+  auto pick = [&](int type, int n, int lines) {
     int lpb = 8;
     while (lpb > 1 && ((lines + lpb - 1) / lpb < 2 * 152 || smem_for(type, n, lpb) > h->smem_optin)) lpb /= 2;
-    if (r2r_paired(type) && lpb == 1 && lines > 1) lpb = 2;
-    while (lpb > 1 && smem_for(type, n, lpb) > h->smem_optin) lpb /= 2;
-    smem = smem_for(type, n, lpb);
     return lpb;
   };
-  size_t sx1, sx2, sy1;
-  int lx1 = pick(tx_f, cols, rows, sx1);
-  int lx2 = pick(tx_i, cols, rows, sx2);
-  tt.lpb_x = std::min(lx1, lx2);
+  tt.lpb_x = std::min(pick(tx_f, cols, rows), pick(tx_i, cols, rows));
   tt.smem_x = std::max(smem_for(tx_f, cols, tt.lpb_x), smem_for(tx_i, cols, tt.lpb_x));
-  tt.lpb_y = pick(ty_f, rows, cols, sy1);
-  tt.smem_y = smem_for(ty_f, rows, tt.lpb_y);
-  if (tt.smem_x > h->smem_optin || tt.smem_y > h->smem_optin) throw CudaError("transform does not fit in shared memory");
+  int P = tt.ych.P;
+  int L = std::max(1, std::min(32, 128 / P));
+  while (L > 1 && ((cols + L - 1) / L < 2 * 152 || (size_t)L * rows * sizeof(double) > h->smem_optin)) L /= 2;
+  tt.lpb_y = L;
+  tt.threads_y = ((L * P + 31) / 32) * 32;
+  tt.smem_y = (size_t)L * rows * sizeof(double);
+  if (tt.smem_x > h->smem_optin || tt.smem_y > h->smem_optin || tt.threads_y > 1024)
+    throw CudaError("separable inverse does not fit the launch limits");
   // view
   rd.view.rows = rows;
   rd.view.cols = cols;

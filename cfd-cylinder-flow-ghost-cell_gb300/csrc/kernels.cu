@@ -148,32 +148,85 @@ __global__ void k_xpass(int n, int rows, int type, FftPlan plan, R2RTables<T> tb
   }
 }
 
+// ---------------------------------------------------------------------------
+// y direction of the separable inverse: for every x-mode kx the column system
+// (L_y + lambda_x(kx)) z = s / (2 nx) (pressure) or ((1 - c lambda_x) - c L_y) z = s / (2 nx)
+// (Helmholtz) is tridiagonal with a constant off-diagonal.  It is solved by a
+// partition method: P chunks of inner rows separated by interface rows; each
+// thread runs Thomas on one chunk with precomputed pivots, one thread per column
+// solves the tridiagonal interface system, then the chunks add their two spike
+// corrections.  Tables (rows x cols, same layout as the spectral array):
+//   inner rows:     t0 = 1/pivot, t1 = left spike v, t2 = right spike w
+//   interface rows: t0 = 1/pivot, t1 = sub-diagonal, t2 = sup/pivot of the interface system
+// ---------------------------------------------------------------------------
 template <typename T>
-__global__ void k_ypass(int n /*rows*/, int cols, int tf, int ti, FftPlan plan, R2RTables<T> tb,
-                        const double* __restrict__ recip, double* __restrict__ S, int lpb, Gate gate) {
+__global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale, const T* __restrict__ t0,
+                         const T* __restrict__ t1, const T* __restrict__ t2, T* __restrict__ S, int lpb, Gate gate) {
   if (!gate_open(gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* col = reinterpret_cast<T*>(smem_raw);  // lpb x n
   const int c0 = blockIdx.x * lpb;
   const int nl = min(lpb, cols - c0);
-  T* stage = reinterpret_cast<T*>(smem_raw);
-  size_t stage_bytes = ((size_t)lpb * n * sizeof(T) + 15) / 16 * 16;
-  cplx<T>* a = reinterpret_cast<cplx<T>*>(smem_raw + stage_bytes);
-  cplx<T>* b = a + r2r_buffer_elems(tf, n, lpb);
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
     int l = t % nl, e = t / nl;
-    stage[l * n + e] = (T)S[(int64_t)e * cols + c0 + l];
+    col[l * n + e] = S[(int64_t)e * cols + c0 + l] * scale;
   }
   __syncthreads();
-  r2r_lines<T>(tf, stage, n, nl, a, b, plan, tb);
-  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
-    int l = t % nl, e = t / nl;
-    stage[l * n + e] = stage[l * n + e] * (T)recip[(int64_t)e * cols + c0 + l];
+  const int P = ch.P;
+  const int l = threadIdx.x % lpb, p = threadIdx.x / lpb;
+  const bool work = l < nl && p < P;
+  int a = 0, b = -1;
+  if (work) { a = ch.start[p]; b = ch.end[p]; }
+  T* x = col + l * n;
+  const int64_t cc = c0 + l;
+  // phase 1: chunk-local Thomas -> g
+  if (work) {
+    T prev = 0;
+    for (int j = a; j <= b; ++j) {
+      T inv = t0[(int64_t)j * cols + cc];
+      prev = (x[j] - gamma * prev) * inv;
+      x[j] = prev;
+    }
+    T next = 0;
+    for (int j = b - 1; j >= a; --j) {
+      T c = gamma * t0[(int64_t)j * cols + cc];
+      next = x[j] - c * x[j + 1];
+      x[j] = next;
+    }
   }
   __syncthreads();
-  r2r_lines<T>(ti, stage, n, nl, a, b, plan, tb);
+  // phase 2: interface system, one thread per column
+  if (p == 0 && l < nl && P > 1) {
+    T z = 0;
+    for (int q = 0; q < P - 1; ++q) {
+      int e = ch.end[q] + 1;
+      int64_t o = (int64_t)e * cols + cc;
+      T rhs = x[e] - gamma * x[e - 1] - gamma * x[e + 1];
+      z = (rhs - t1[o] * z) * t0[o];
+      x[e] = z;
+    }
+    T y = 0;
+    for (int q = P - 2; q >= 0; --q) {
+      int e = ch.end[q] + 1;
+      int64_t o = (int64_t)e * cols + cc;
+      y = x[e] - t2[o] * y;
+      x[e] = y;
+    }
+  }
+  __syncthreads();
+  // phase 3: spike corrections of the inner rows
+  if (work && P > 1) {
+    T yl = p > 0 ? x[ch.end[p - 1] + 1] : (T)0;
+    T yr = p < P - 1 ? x[b + 1] : (T)0;
+    for (int j = a; j <= b; ++j) {
+      int64_t o = (int64_t)j * cols + cc;
+      x[j] = x[j] - yl * t1[o] - yr * t2[o];
+    }
+  }
+  __syncthreads();
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
-    int l = t % nl, e = t / nl;
-    S[(int64_t)e * cols + c0 + l] = (double)stage[l * n + e];
+    int ll = t % nl, e = t / nl;
+    S[(int64_t)e * cols + c0 + ll] = col[ll * n + e];
   }
 }
 
@@ -190,9 +243,9 @@ static int allow_dynamic_smem(K kernel, int optin) {
 int configure_kernels(int smem_optin) {
   int d = smem_optin;
   d = std::min(d, allow_dynamic_smem(k_xpass<double>, smem_optin));
-  d = std::min(d, allow_dynamic_smem(k_ypass<double>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve<double>, smem_optin));
   d = std::min(d, allow_dynamic_smem(k_xpass<float>, smem_optin));
-  d = std::min(d, allow_dynamic_smem(k_ypass<float>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve<float>, smem_optin));
   return d;
 }
 
@@ -202,7 +255,6 @@ void launch_rect_inverse(const TransformTables& tt, const RectView& v, const dou
   using C = cplx<double>;
   R2RTables<double> tx{(const C*)tt.Wx, (const C*)tt.prex, (const C*)tt.postx};
   R2RTables<double> txi{(const C*)tt.Wx, (const C*)tt.prex_inv, (const C*)tt.postx_inv};
-  R2RTables<double> ty{(const C*)tt.Wy, (const C*)tt.prey, (const C*)tt.posty};
   unsigned gx = (unsigned)((v.rows + tt.lpb_x - 1) / tt.lpb_x);
   note_launch();
   kt_mark(1, st);
@@ -213,8 +265,9 @@ void launch_rect_inverse(const TransformTables& tt, const RectView& v, const dou
   unsigned gy = (unsigned)((v.cols + tt.lpb_y - 1) / tt.lpb_y);
   note_launch();
   kt_mark(2, st);
-  k_ypass<double><<<gy, 128, tt.smem_y, st>>>(v.rows, v.cols, tt.ty_fwd, tt.ty_inv, tt.plan_y, ty, tt.recip,
-                                              spectral, tt.lpb_y, gate);
+  k_ysolve<double><<<gy, tt.threads_y, tt.smem_y, st>>>(v.rows, v.cols, tt.ych, tt.gamma, tt.yscale,
+                                                        (const double*)tt.t0, (const double*)tt.t1,
+                                                        (const double*)tt.t2, spectral, tt.lpb_y, gate);
   kt_mark(2, st);
   note_launch();
   kt_mark(1, st);

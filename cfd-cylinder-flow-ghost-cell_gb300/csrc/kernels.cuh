@@ -138,15 +138,26 @@ struct RectView {
   const uint8_t* cls;         // class map of the field grid (mask for loads/stores)
 };
 
-struct TransformTables {      // device tables of one rectangle kind (FP64)
-  FftPlan plan_x, plan_y;
-  int tx_fwd, tx_inv, ty_fwd, ty_inv;
+// Chunk layout of the column systems of the y solve: inner rows [start[p], end[p]],
+// interface row end[p] + 1 between chunk p and p + 1.
+static constexpr int YCHUNK_MAX = 64;
+struct YChunks {
+  int P;
+  int start[YCHUNK_MAX];
+  int end[YCHUNK_MAX];
+};
+
+struct TransformTables {      // device tables of one rectangle kind (T = double or float)
+  FftPlan plan_x;
+  int tx_fwd, tx_inv;
   const void* Wx; const void* prex; const void* postx;
-  const void* Wy; const void* prey; const void* posty;
-  // For the inverse x transform (may differ in type IV vs Makhoul but same n):
   const void* prex_inv; const void* postx_inv;
-  const double* recip;        // rows x cols: 1 / (divisor * 4 nx ny)
-  int lpb_x, lpb_y;           // lines per block
+  // y direction: partitioned tridiagonal solve per x-mode
+  YChunks ych;
+  double gamma;               // constant off-diagonal of the column systems
+  double yscale;              // 1 / (2 nx): normalisation of the inverse x transform
+  const void* t0; const void* t1; const void* t2;  // rows x cols partition tables
+  int lpb_x, lpb_y, threads_y;
   size_t smem_x, smem_y;
 };
 

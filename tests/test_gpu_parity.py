@@ -2,7 +2,8 @@
 
 Every comparison goes through the C ABI (ctypes) on a GB300.  Tolerances
 (max-norm, relative to max(1, |reference|)):
-  single operators and transforms ............ 1e-12
+  single operators, Helmholtz transforms ...... 1e-12
+  pressure rectangle inverse ................... 1e-10 (condition number up to 1e6)
   projected fields, pressure solves ........... 1e-11
   fields after a few AB2/CN steps ............. 1e-10
   force coefficients .......................... 1e-8 (relative)
@@ -16,6 +17,12 @@ import ghost_oracle as go
 from conftest import GOLDEN, load_package
 
 pytestmark = pytest.mark.gpu
+
+
+# The pressure rectangle (Neumann walls, Dirichlet outlet) has condition ~(L/h)^2 up to 1e6:
+# two backward-stable inverses agree to ~cond * eps, not to eps.  Helmholtz rectangles are
+# well conditioned.
+RECT_TOL = dict(pressure=1e-10, u=1e-12, v=1e-12)
 
 
 def rel(a, b):
@@ -42,7 +49,7 @@ def test_rectangle_transforms(pkg):
     s = pkg.MAC_CylinderFlow(nx=24, ny=10, Lx=7.2, Ly=2.5, D=0.4, xc=3.6, yc=1.25, nu=0.02, rho=1.3, verbose=False)
     for kind in ('pressure', 'u', 'v'):
         x = s.gg.rectangle_solve(kind, G[f'{kind}_in'], dt=0.004)
-        assert rel(x, G[f'{kind}_out']) < 1e-12, kind
+        assert rel(x, G[f'{kind}_out']) < RECT_TOL[kind], kind
 
 
 @pytest.mark.parametrize('n', [(40, 30, 0.5), (88, 16, 0.3), (400, 200, 1.0), (256, 128, 1.0), (820, 410, 1.0)])
@@ -55,7 +62,7 @@ def test_rectangle_transforms_sizes(pkg, n):
     for kind in ('pressure', 'u', 'v'):
         _, solve, shape = go.rectangle(nx, ny, s.dx, s.dy, kind, 0.01, 0.002, 1.0, self_check=False)
         b = rng.normal(size=shape)
-        assert rel(s.gg.rectangle_solve(kind, b, dt=0.002), solve(b.copy())) < 1e-12, kind
+        assert rel(s.gg.rectangle_solve(kind, b, dt=0.002), solve(b.copy())) < RECT_TOL[kind], kind
 
 
 def test_operators_match_golden(pkg, G):
