@@ -118,6 +118,9 @@ struct RectDev {
   TransformTables tt{};
   RectView view{};
   DBuf<double> Wx, prex, postx, t0, t1, t2;
+  // FP32 copies for the mixed-precision mode
+  TransformTables tt32{};
+  DBuf<float> Wx32, prex32, postx32, t0_32, t1_32, t2_32;
   // Schur data
   int rank = 0;
   DBuf<int64_t> rows, cptr, ccol;
@@ -150,11 +153,14 @@ struct gm_handle {
   // state and work buffers (face grid F, pressure grid P)
   DBuf<double> U, Unext, hist, now, rhs, star, fres, ffirst, fw2, fmid, fhalf, faction, fproj, fproj2, ftmp;
   DBuf<double> phalf, phalf_next, pout, prhs, pphi, pres, pfirst, pw2, pinc, ptmp, spectral;
+  DBuf<float> spectral32, ffirst32, pfirst32;
   DBuf<StepCtl> ctl;
   DBuf<unsigned long long> state_max;  // persistent max|u|, max|v| of the current state
   StepCtl* host_ctl = nullptr;
   bool has_history = false;
   bool host_only = false;
+  int precision = 0;  // 0 plain FP64, 1 FP32 inverse with FP64 refinement
+  int nchk = 3;       // residual checks per solve (1 + refinement sweeps)
   double prev_dt = 0;
   int64_t F = 0, Pn = 0;
   // scratch for host<->device arrays
@@ -181,6 +187,8 @@ void upload_csr(Csrd& d, const std::vector<int64_t>& rows, const gm::Csr& c, cud
   d.col.upload(cols, st);
   d.val.upload(c.val, st);
 }
+
+std::vector<float> to_f32(const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); }
 
 // Chunk layout of an n-row column: P chunks of inner rows separated by P-1 interface rows.
 YChunks make_chunks(int n) {
@@ -297,6 +305,11 @@ void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
   rd.t1.upload(t1, st);
   rd.t2.upload(t2, st);
   tt.t0 = rd.t0.p; tt.t1 = rd.t1.p; tt.t2 = rd.t2.p;
+  if (h->precision == 1) {
+    rd.t0_32.upload(to_f32(t0), st);
+    rd.t1_32.upload(to_f32(t1), st);
+    rd.t2_32.upload(to_f32(t2), st);
+  }
   // launch shapes
   auto smem_for = [](int type, int n, int lpb) {
     size_t stage = ((size_t)lpb * n * sizeof(double) + 15) / 16 * 16;
@@ -317,6 +330,35 @@ void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
   tt.smem_y = (size_t)L * rows * sizeof(double);
   if (tt.smem_x > h->smem_optin || tt.smem_y > h->smem_optin || tt.threads_y > 1024)
     throw CudaError("separable inverse does not fit the launch limits");
+  if (h->precision == 1) {
+    // FP32 tables and launch shapes (same plans, half the shared memory per line)
+    TransformTables& t32 = rd.tt32;
+    t32 = tt;
+    std::vector<double> w(2 * (size_t)Mx), pre, post;
+    rd.Wx32.upload(to_f32(cexp_table(Mx, 2.0, Mx, 0.0, -1)), st);
+    if (r2r_family(tx_f) == 2) {
+      rd.prex32.upload(to_f32(cexp_table(cols / 2, 4.0, 4.0 * cols, 1.0, -1)), st);
+      rd.postx32.upload(to_f32(cexp_table(cols / 2, 1.0, cols, 0.0, -1)), st);
+    } else {
+      rd.prex32.upload(to_f32(cexp_table(1, 0, 1, 0, 1)), st);
+      rd.postx32.upload(to_f32(cexp_table(cols, 1.0, 2.0 * cols, 0.0, +1)), st);
+    }
+    t32.Wx = rd.Wx32.p; t32.prex = rd.prex32.p; t32.postx = rd.postx32.p;
+    t32.prex_inv = rd.prex32.p; t32.postx_inv = rd.postx32.p;
+    t32.t0 = rd.t0_32.p; t32.t1 = rd.t1_32.p; t32.t2 = rd.t2_32.p;
+    auto smem32 = [](int type, int n, int lpb) {
+      size_t stage = ((size_t)lpb * n * sizeof(float) + 15) / 16 * 16;
+      return stage + 2 * (size_t)r2r_buffer_elems(type, n, lpb) * sizeof(cplx<float>);
+    };
+    auto pick32 = [&](int type, int n, int lines) {
+      int lpb = 8;
+      while (lpb > 1 && ((lines + lpb - 1) / lpb < 2 * 152 || smem32(type, n, lpb) > h->smem_optin)) lpb /= 2;
+      return lpb;
+    };
+    t32.lpb_x = std::min(pick32(tx_f, cols, rows), pick32(tx_i, cols, rows));
+    t32.smem_x = std::max(smem32(tx_f, cols, t32.lpb_x), smem32(tx_i, cols, t32.lpb_x));
+    t32.smem_y = (size_t)t32.lpb_y * rows * sizeof(float);
+  }
   // view
   rd.view.rows = rows;
   rd.view.cols = cols;
@@ -457,16 +499,27 @@ void ghost_p(gm_handle* h, double* P, const Gate& gt) {
 }
 
 // one boundary-row solve of kind k into x with residual checks (solver/pressure_schur.py:103-124)
+// In the FP32 mode every application of the inverse runs in FP32 and the residual
+// b - A x in FP64, so the refinement sweeps recover an FP64 solution.
 void schur_solve(gm_handle* h, RectDev& rd, int kind, double hc, const double* b, double* x, double* res,
                  double* first, double* w2, int slot) {
   cudaStream_t st = h->st;
   SolveCtl* sc = &h->ctl.p->solve[slot];
-  for (int sweep = 0; sweep < 3; ++sweep) {
+  const bool mixed = h->precision == 1;
+  float* first32 = kind == 0 ? h->pfirst32.p : h->ffirst32.p;
+  for (int sweep = 0; sweep < h->nchk; ++sweep) {
     Gate gt = gate_of(h, slot, sweep);
     const double* rhs = sweep == 0 ? b : res;
-    launch_rect_inverse(rd.tt, rd.view, rhs, true, h->spectral.p, first, nullptr, nullptr, gt, st);
-    launch_schur(first, rd.view, rd.rank, rd.rows.p, rd.cptr.p, rd.ccol.p, rd.cval.p, rd.sinv.p, w2, gt, st);
-    launch_rect_inverse(rd.tt, rd.view, w2, false, h->spectral.p, x, first, sweep == 0 ? nullptr : x, gt, st);
+    if (mixed) {
+      launch_rect_inverse_f32(rd.tt32, rd.view, rhs, true, h->spectral32.p, first32, gt, st);
+      launch_schur_f32(first32, rd.view, rd.rank, rd.rows.p, rd.cptr.p, rd.ccol.p, rd.cval.p, rd.sinv.p, w2, gt, st);
+      launch_rect_inverse_f32_final(rd.tt32, rd.view, w2, h->spectral32.p, x, first32, sweep == 0 ? nullptr : x, gt,
+                                    st);
+    } else {
+      launch_rect_inverse(rd.tt, rd.view, rhs, true, h->spectral.p, first, nullptr, nullptr, gt, st);
+      launch_schur(first, rd.view, rd.rank, rd.rows.p, rd.cptr.p, rd.ccol.p, rd.cval.p, rd.sinv.p, w2, gt, st);
+      launch_rect_inverse(rd.tt, rd.view, w2, false, h->spectral.p, x, first, sweep == 0 ? nullptr : x, gt, st);
+    }
     launch_residual(h->cd, kind, hc, b, x, res, sc, sweep, sweep == 0, gt, st);
   }
 }
@@ -479,7 +532,7 @@ void project(gm_handle* h, double* q, double dt, double* out, double* phi, int s
   ghost_faces(h, q, g0);
   launch_divergence(h->cd, q, h->prhs.p, dt, nullptr, nullptr, 1, g0, st);
   schur_solve(h, h->rp, 0, 0.0, h->prhs.p, phi, h->pres.p, h->pfirst.p, h->pw2.p, slot);
-  launch_gate_pressure(h->ctl.p, slot, st);
+  launch_gate_pressure(h->ctl.p, slot, h->nchk, st);
   ghost_p(h, phi, g0);
   launch_project_update(h->cd, q, phi, dt, out, nullptr, g0, st);
   ghost_faces(h, out, g0);
@@ -510,6 +563,11 @@ void ensure_helmholtz(gm_handle* h, double dt) {
   CK(cudaStreamSynchronize(h->st));
 }
 
+void momentum(gm_handle* h, const MomentumArgs& ma, const Gate& g0) {
+  if (h->precision == 1) launch_momentum_f32(h->cd, ma, g0, h->st);
+  else launch_momentum(h->cd, ma, g0, h->st);
+}
+
 // One AB2/CN step (solver/time_integration.py:7-145) on the handle state.
 void step_once(gm_handle* h, double dt, bool screen) {
   cudaStream_t st = h->st;
@@ -531,25 +589,25 @@ void step_once(gm_handle* h, double dt, bool screen) {
     ma.mode = 1;
     ma.now = h->now.p;
     ma.out = h->fmid.p;
-    launch_momentum(h->cd, ma, g0, st);
+    momentum(h, ma, g0);
     project(h, h->fmid.p, 0.5 * dt, h->fhalf.p, h->pphi.p, S_P0, 0);
     ma.mode = 2;
     ma.Uhalf = h->fhalf.p;
     ma.now = nullptr;
     ma.out = h->rhs.p;
-    launch_momentum(h->cd, ma, g0, st);
+    momentum(h, ma, g0);
   } else {
     ma.mode = 0;
     ma.alpha = dt / (2 * h->prev_dt);
     ma.prev = h->hist.p;
     ma.now = h->now.p;
     ma.out = h->rhs.p;
-    launch_momentum(h->cd, ma, g0, st);
+    momentum(h, ma, g0);
   }
   // CN Helmholtz solves for u and v (solver/optimized_ghost_cell.py:247-254)
   schur_solve(h, h->ru, 1, hc, h->rhs.p, h->star.p, h->fres.p, h->ffirst.p, h->fw2.p, S_HELM_U);
   schur_solve(h, h->rv, 2, hc, h->rhs.p, h->star.p, h->fres.p, h->ffirst.p, h->fw2.p, S_HELM_V);
-  launch_gate_momentum(h->ctl.p, st);
+  launch_gate_momentum(h->ctl.p, h->nchk, st);
   // projection of the CN velocity, defect correction and the pressure increment
   project(h, h->star.p, dt, h->Unext.p, h->pphi.p, S_P1, 1);
   launch_defect(h->cd, h->Unext.p, h->rhs.p, hdt, h->faction.p, h->fproj.p, g0, st);
@@ -594,7 +652,7 @@ void fill_diag(gm_handle* h, const StepCtl& c, double t, double dt, bool first, 
     const SolveCtl& sc = c.solve[s];
     double b = bits2d(sc.bmax), tg = std::max(1e-10, 32 * 2.220446049250313e-16 * std::max(1.0, b));
     int k = 0;
-    if (bits2d(sc.rmax[0]) > tg) { k = 1; if (bits2d(sc.rmax[1]) > tg) k = 2; }
+    while (k + 1 < h->nchk && bits2d(sc.rmax[k]) > tg) ++k;
     mres = std::max(mres, bits2d(sc.rmax[k]));
     mref += k;
   }
@@ -607,7 +665,7 @@ void fill_diag(gm_handle* h, const StepCtl& c, double t, double dt, bool first, 
     const SolveCtl& sc = c.solve[s];
     double b = bits2d(sc.bmax), tg = std::max(1e-10, 32 * 2.220446049250313e-16 * std::max(1.0, b));
     int k = 0;
-    if (bits2d(sc.rmax[0]) > tg) { k = 1; if (bits2d(sc.rmax[1]) > tg) k = 2; }
+    while (k + 1 < h->nchk && bits2d(sc.rmax[k]) > tg) ++k;
     ++count;
     refine += k;
     plinf = std::max(plinf, bits2d(sc.rmax[k]));
@@ -688,7 +746,9 @@ int gm_create(const gm_config* cfg, gm_handle** out) {
   g.nu = cfg->nu; g.rho = cfg->rho; g.U_inf = cfg->U_inf; g.inflow = cfg->inflow; g.U_m = cfg->U_m;
   g.pressure_solver = cfg->pressure_solver; g.pressure_extension = cfg->pressure_extension;
   g.velocity_interpolation = cfg->velocity_interpolation;
-  if (cfg->precision != 0) { g_create_error = "precision mode not built in this library"; return GM_ENOTIMPL; }
+  if (cfg->precision != 0 && cfg->precision != 1) { g_create_error = "precision must be 0 (FP64) or 1 (FP32 with FP64 refinement)"; return GM_EVALUE; }
+  h->precision = cfg->precision;
+  h->nchk = cfg->precision == 1 ? MAXCHK : 3;
   if (cfg->pressure_solver == 1) { g_create_error = "iterative pressure solver not built in this library"; return GM_ENOTIMPL; }
   if (cfg->nx % 2 != 0) { g_create_error = "odd nx is not supported by the type-IV transform"; return GM_ENOTIMPL; }
   int ec = 0;
@@ -747,6 +807,13 @@ int gm_create(const gm_config* cfg, gm_handle** out) {
       b->zero(st);
     }
     H->spectral.alloc(std::max<int64_t>(H->Pn, (int64_t)g.ny * g.nx));
+    if (H->precision == 1) {
+      H->spectral32.alloc(H->spectral.n);
+      H->ffirst32.alloc(H->F);
+      H->ffirst32.zero(st);
+      H->pfirst32.alloc(H->Pn);
+      H->pfirst32.zero(st);
+    }
     H->ctl.alloc(1);
     H->ctl.zero(st);
     H->state_max.alloc(2);
@@ -1074,7 +1141,7 @@ static void solve_info_from(gm_handle* h, int slot, gm_solve_info* info) {
   const SolveCtl& sc = h->host_ctl->solve[slot];
   double b = bits2d(sc.bmax), tg = std::max(1e-10, 32 * 2.220446049250313e-16 * std::max(1.0, b));
   int k = 0;
-  if (bits2d(sc.rmax[0]) > tg) { k = 1; if (bits2d(sc.rmax[1]) > tg) k = 2; }
+  while (k + 1 < h->nchk && bits2d(sc.rmax[k]) > tg) ++k;
   double bound = bits2d(sc.bound[k]);
   double t64 = std::max(1e-10, 64 * 2.220446049250313e-16 * std::max(1.0, b));
   info->residual_linf = bits2d(sc.rmax[k]);
@@ -1132,7 +1199,7 @@ int gm_pressure_solve(gm_handle* h, const double* rhs, double* phi, gm_solve_inf
     launch_scatter(b, h->d_pi.p, np, h->prhs.p, st);
     CK(cudaMemsetAsync(h->ctl.p, 0, sizeof(StepCtl), st));
     schur_solve(h, h->rp, 0, 0.0, h->prhs.p, h->pphi.p, h->pres.p, h->pfirst.p, h->pw2.p, S_P1);
-    launch_gate_pressure(h->ctl.p, S_P1, st);
+    launch_gate_pressure(h->ctl.p, S_P1, h->nchk, st);
     CK(cudaMemcpyAsync(h->host_ctl, h->ctl.p, sizeof(StepCtl), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     solve_info_from(h, S_P1, info);

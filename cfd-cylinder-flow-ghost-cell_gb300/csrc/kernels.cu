@@ -112,10 +112,10 @@ void ktimer_read(double* total_ms, long long* count) {
 // ---------------------------------------------------------------------------
 // separable inverse: x pass (rows) and y pass (columns with eigenvalue scaling)
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void k_xpass(int n, int rows, int type, FftPlan plan, R2RTables<T> tb, const double* __restrict__ in,
-                        int64_t ibase, int64_t ipitch, const uint8_t* __restrict__ icls, double* __restrict__ out,
-                        int64_t obase, int64_t opitch, const uint8_t* __restrict__ ocls, const double* __restrict__ sub,
+template <typename T, typename TI, typename TO, typename TS>
+__global__ void k_xpass(int n, int rows, int type, FftPlan plan, R2RTables<T> tb, const TI* __restrict__ in,
+                        int64_t ibase, int64_t ipitch, const uint8_t* __restrict__ icls, TO* __restrict__ out,
+                        int64_t obase, int64_t opitch, const uint8_t* __restrict__ ocls, const TS* __restrict__ sub,
                         const double* __restrict__ add, int lpb, Gate gate) {
   if (!gate_open(gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -128,8 +128,8 @@ __global__ void k_xpass(int n, int rows, int type, FftPlan plan, R2RTables<T> tb
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
     int l = t / n, e = t - l * n;
     int64_t fi = ibase + (int64_t)(l0 + l) * ipitch + e;
-    double v = in[fi];
-    if (icls && !(icls[fi] & CLS_ACTIVE)) v = 0.0;
+    TI v = in[fi];
+    if (icls && !(icls[fi] & CLS_ACTIVE)) v = (TI)0;
     stage[t] = (T)v;
   }
   __syncthreads();
@@ -137,13 +137,13 @@ __global__ void k_xpass(int n, int rows, int type, FftPlan plan, R2RTables<T> tb
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
     int l = t / n, e = t - l * n;
     int64_t fo = obase + (int64_t)(l0 + l) * opitch + e;
-    double v = (double)stage[t];
+    T v = stage[t];
     if (sub) {
-      if (ocls && !(ocls[fo] & CLS_ACTIVE)) { out[fo] = 0.0; continue; }
-      double d = sub[fo] - v;
-      out[fo] = add ? add[fo] + d : d;
+      if (ocls && !(ocls[fo] & CLS_ACTIVE)) { out[fo] = (TO)0; continue; }
+      double d = (double)((T)sub[fo] - v);
+      out[fo] = (TO)(add ? add[fo] + d : d);
     } else {
-      out[fo] = v;
+      out[fo] = (TO)v;
     }
   }
 }
@@ -242,9 +242,11 @@ static int allow_dynamic_smem(K kernel, int optin) {
 }
 int configure_kernels(int smem_optin) {
   int d = smem_optin;
-  d = std::min(d, allow_dynamic_smem(k_xpass<double>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_xpass<double, double, double, double>, smem_optin));
   d = std::min(d, allow_dynamic_smem(k_ysolve<double>, smem_optin));
-  d = std::min(d, allow_dynamic_smem(k_xpass<float>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_xpass<float, double, float, float>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_xpass<float, float, float, float>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_xpass<float, float, double, float>, smem_optin));
   d = std::min(d, allow_dynamic_smem(k_ysolve<float>, smem_optin));
   return d;
 }
@@ -258,9 +260,9 @@ void launch_rect_inverse(const TransformTables& tt, const RectView& v, const dou
   unsigned gx = (unsigned)((v.rows + tt.lpb_x - 1) / tt.lpb_x);
   note_launch();
   kt_mark(1, st);
-  k_xpass<double><<<gx, 128, tt.smem_x, st>>>(v.cols, v.rows, tt.tx_fwd, tt.plan_x, tx, b, v.base, v.pitch,
-                                              mask_in ? v.cls : nullptr, spectral, 0, v.cols, nullptr, nullptr,
-                                              nullptr, tt.lpb_x, gate);
+  k_xpass<double, double, double, double><<<gx, 128, tt.smem_x, st>>>(
+      v.cols, v.rows, tt.tx_fwd, tt.plan_x, tx, b, v.base, v.pitch, mask_in ? v.cls : nullptr, spectral, 0, v.cols,
+      nullptr, (const double*)nullptr, nullptr, tt.lpb_x, gate);
   kt_mark(1, st);
   unsigned gy = (unsigned)((v.cols + tt.lpb_y - 1) / tt.lpb_y);
   note_launch();
@@ -271,8 +273,64 @@ void launch_rect_inverse(const TransformTables& tt, const RectView& v, const dou
   kt_mark(2, st);
   note_launch();
   kt_mark(1, st);
-  k_xpass<double><<<gx, 128, tt.smem_x, st>>>(v.cols, v.rows, tt.tx_inv, tt.plan_x, txi, spectral, 0, v.cols,
-                                              nullptr, out, v.base, v.pitch, v.cls, sub, add, tt.lpb_x, gate);
+  k_xpass<double, double, double, double><<<gx, 128, tt.smem_x, st>>>(
+      v.cols, v.rows, tt.tx_inv, tt.plan_x, txi, spectral, 0, v.cols, nullptr, out, v.base, v.pitch, v.cls, sub, add,
+      tt.lpb_x, gate);
+  kt_mark(1, st);
+}
+
+void launch_rect_inverse_f32(const TransformTables& tt, const RectView& v, const double* b, bool mask_in,
+                             float* spectral, float* first, const Gate& gate, cudaStream_t st) {
+  using C = cplx<float>;
+  R2RTables<float> tx{(const C*)tt.Wx, (const C*)tt.prex, (const C*)tt.postx};
+  R2RTables<float> txi{(const C*)tt.Wx, (const C*)tt.prex_inv, (const C*)tt.postx_inv};
+  unsigned gx = (unsigned)((v.rows + tt.lpb_x - 1) / tt.lpb_x);
+  note_launch();
+  kt_mark(1, st);
+  k_xpass<float, double, float, float><<<gx, 128, tt.smem_x, st>>>(
+      v.cols, v.rows, tt.tx_fwd, tt.plan_x, tx, b, v.base, v.pitch, mask_in ? v.cls : nullptr, spectral, 0, v.cols,
+      nullptr, (const float*)nullptr, nullptr, tt.lpb_x, gate);
+  kt_mark(1, st);
+  unsigned gy = (unsigned)((v.cols + tt.lpb_y - 1) / tt.lpb_y);
+  note_launch();
+  kt_mark(2, st);
+  k_ysolve<float><<<gy, tt.threads_y, tt.smem_y, st>>>(v.rows, v.cols, tt.ych, (float)tt.gamma, (float)tt.yscale,
+                                                       (const float*)tt.t0, (const float*)tt.t1, (const float*)tt.t2,
+                                                       spectral, tt.lpb_y, gate);
+  kt_mark(2, st);
+  note_launch();
+  kt_mark(1, st);
+  k_xpass<float, float, float, float><<<gx, 128, tt.smem_x, st>>>(
+      v.cols, v.rows, tt.tx_inv, tt.plan_x, txi, spectral, 0, v.cols, nullptr, first, v.base, v.pitch, nullptr,
+      (const float*)nullptr, nullptr, tt.lpb_x, gate);
+  kt_mark(1, st);
+}
+
+void launch_rect_inverse_f32_final(const TransformTables& tt, const RectView& v, const double* w2, float* spectral,
+                                   double* out, const float* sub, const double* add, const Gate& gate,
+                                   cudaStream_t st) {
+  using C = cplx<float>;
+  R2RTables<float> tx{(const C*)tt.Wx, (const C*)tt.prex, (const C*)tt.postx};
+  R2RTables<float> txi{(const C*)tt.Wx, (const C*)tt.prex_inv, (const C*)tt.postx_inv};
+  unsigned gx = (unsigned)((v.rows + tt.lpb_x - 1) / tt.lpb_x);
+  note_launch();
+  kt_mark(1, st);
+  k_xpass<float, double, float, float><<<gx, 128, tt.smem_x, st>>>(
+      v.cols, v.rows, tt.tx_fwd, tt.plan_x, tx, w2, v.base, v.pitch, nullptr, spectral, 0, v.cols, nullptr,
+      (const float*)nullptr, nullptr, tt.lpb_x, gate);
+  kt_mark(1, st);
+  unsigned gy = (unsigned)((v.cols + tt.lpb_y - 1) / tt.lpb_y);
+  note_launch();
+  kt_mark(2, st);
+  k_ysolve<float><<<gy, tt.threads_y, tt.smem_y, st>>>(v.rows, v.cols, tt.ych, (float)tt.gamma, (float)tt.yscale,
+                                                       (const float*)tt.t0, (const float*)tt.t1, (const float*)tt.t2,
+                                                       spectral, tt.lpb_y, gate);
+  kt_mark(2, st);
+  note_launch();
+  kt_mark(1, st);
+  k_xpass<float, float, double, float><<<gx, 128, tt.smem_x, st>>>(
+      v.cols, v.rows, tt.tx_inv, tt.plan_x, txi, spectral, 0, v.cols, nullptr, out, v.base, v.pitch, v.cls, sub, add,
+      tt.lpb_x, gate);
   kt_mark(1, st);
 }
 
@@ -280,7 +338,8 @@ void launch_rect_inverse(const TransformTables& tt, const RectView& v, const dou
 // boundary Schur correction: c = S^{-1} (C first), scattered into w2
 // ---------------------------------------------------------------------------
 static constexpr int SCHUR_ROWS = 16;
-__global__ void k_schur(const double* __restrict__ first, RectView v, int rank, const int64_t* __restrict__ rows,
+template <typename TF>
+__global__ void k_schur(const TF* __restrict__ first, RectView v, int rank, const int64_t* __restrict__ rows,
                         const int64_t* __restrict__ cp, const int64_t* __restrict__ cc, const double* __restrict__ cv,
                         const double* __restrict__ sinv, double* __restrict__ w2, Gate gate) {
   if (!gate_open(gate)) return;
@@ -290,7 +349,7 @@ __global__ void k_schur(const double* __restrict__ first, RectView v, int rank, 
     for (int64_t e = cp[k]; e < cp[k + 1]; ++e) {
       int64_t rc = cc[e];
       int64_t fi = v.base + (rc / v.cols) * v.pitch + (rc % v.cols);
-      acc += cv[e] * first[fi];
+      acc += cv[e] * (double)first[fi];
     }
     y[k] = acc;
   }
@@ -314,7 +373,15 @@ void launch_schur(const double* first, const RectView& view, int rank, const int
   if (rank <= 0) return;
   unsigned g = (unsigned)((rank + SCHUR_ROWS - 1) / SCHUR_ROWS);
   note_launch();
-  k_schur<<<g, 256, rank * sizeof(double), st>>>(first, view, rank, rows, c_ptr, c_col, c_val, sinv, w2, gate);
+  k_schur<double><<<g, 256, rank * sizeof(double), st>>>(first, view, rank, rows, c_ptr, c_col, c_val, sinv, w2, gate);
+}
+void launch_schur_f32(const float* first, const RectView& view, int rank, const int64_t* rows, const int64_t* c_ptr,
+                      const int64_t* c_col, const double* c_val, const double* sinv, double* w2, const Gate& gate,
+                      cudaStream_t st) {
+  if (rank <= 0) return;
+  unsigned g = (unsigned)((rank + SCHUR_ROWS - 1) / SCHUR_ROWS);
+  note_launch();
+  k_schur<float><<<g, 256, rank * sizeof(double), st>>>(first, view, rank, rows, c_ptr, c_col, c_val, sinv, w2, gate);
 }
 
 // ---------------------------------------------------------------------------
@@ -348,74 +415,83 @@ struct Grid {
   __device__ __forceinline__ int64_t p(int j, int i) const { return (int64_t)j * nx + i; }
 };
 
-// -N(u) at u face (j,i), i>=1, before /(dx dy) (solver/numba_kernels.py:17-74 with nu=0)
-__device__ __forceinline__ double adv_u(const double* __restrict__ U, const Grid& g, int j, int i, double dx, double dy) {
+// -N(u) at u face (j,i), i>=1, before /(dx dy) (solver/numba_kernels.py:17-74 with nu=0);
+// arithmetic in T (double for the plain path, float in the FP32 mode)
+template <typename T>
+__device__ __forceinline__ T adv_u(const double* __restrict__ U, const Grid& g, int j, int i, T dx, T dy) {
   const int nx = g.nx, ny = g.ny;
-  auto fxy = [&](int jj, int ii) -> double {  // corner flux at (jj, ii), jj in [0, ny]
-    if (jj == 0 || jj == ny) return 0.0;
-    double vf;
-    if (ii == 0) vf = U[g.v(jj, 0)];
-    else if (ii == nx) vf = U[g.v(jj, nx - 1)];
-    else vf = 0.5 * (U[g.v(jj, ii - 1)] + U[g.v(jj, ii)]);
-    double ua = 0.5 * (U[g.u(jj - 1, ii)] + U[g.u(jj, ii)]);
+  const T h = (T)0.5;
+  auto fxy = [&](int jj, int ii) -> T {  // corner flux at (jj, ii), jj in [0, ny]
+    if (jj == 0 || jj == ny) return (T)0;
+    T vf;
+    if (ii == 0) vf = (T)U[g.v(jj, 0)];
+    else if (ii == nx) vf = (T)U[g.v(jj, nx - 1)];
+    else vf = h * ((T)U[g.v(jj, ii - 1)] + (T)U[g.v(jj, ii)]);
+    T ua = h * ((T)U[g.u(jj - 1, ii)] + (T)U[g.u(jj, ii)]);
     return -((vf * ua) * dx);
   };
-  double uW = U[g.u(j, i - 1)], uC = U[g.u(j, i)];
-  double fl = 0.5 * (uW + uC);
-  double fxxW = -((fl * fl) * dy);
+  T uW = (T)U[g.u(j, i - 1)], uC = (T)U[g.u(j, i)];
+  T fl = h * (uW + uC);
+  T fxxW = -((fl * fl) * dy);
   if (i < nx) {
-    double fr = 0.5 * (uC + U[g.u(j, i + 1)]);
-    double fxxE = -((fr * fr) * dy);
+    T fr = h * (uC + (T)U[g.u(j, i + 1)]);
+    T fxxE = -((fr * fr) * dy);
     return (fxxE - fxxW) + (fxy(j + 1, i) - fxy(j, i));
   }
-  return (-uC * uC) * dy - fxxW + 0.5 * (fxy(j + 1, nx) - fxy(j, nx));
+  return (-uC * uC) * dy - fxxW + h * (fxy(j + 1, nx) - fxy(j, nx));
 }
 
 // -N(v) at v face (j,i), 1<=j<=ny-1 (solver/numba_kernels.py:77-142 with nu=0)
-__device__ __forceinline__ double adv_v(const double* __restrict__ U, const Grid& g, int j, int i, double dx, double dy) {
+template <typename T>
+__device__ __forceinline__ T adv_v(const double* __restrict__ U, const Grid& g, int j, int i, T dx, T dy) {
   const int nx = g.nx;
-  auto fyx = [&](int jj, int ii) -> double {  // corner flux at (jj, ii), ii in [0, nx]
-    if (ii == 0) return 0.0;
-    double uf = 0.5 * (U[g.u(jj - 1, ii)] + U[g.u(jj, ii)]);
-    if (ii == nx) return (-uf * U[g.v(jj, nx - 1)]) * dy;
-    double va = 0.5 * (U[g.v(jj, ii - 1)] + U[g.v(jj, ii)]);
+  const T h = (T)0.5;
+  auto fyx = [&](int jj, int ii) -> T {  // corner flux at (jj, ii), ii in [0, nx]
+    if (ii == 0) return (T)0;
+    T uf = h * ((T)U[g.u(jj - 1, ii)] + (T)U[g.u(jj, ii)]);
+    if (ii == nx) return (-uf * (T)U[g.v(jj, nx - 1)]) * dy;
+    T va = h * ((T)U[g.v(jj, ii - 1)] + (T)U[g.v(jj, ii)]);
     return -((uf * va) * dy);
   };
-  double vS = U[g.v(j - 1, i)], vC = U[g.v(j, i)], vN = U[g.v(j + 1, i)];
-  double fb = 0.5 * (vS + vC), ft = 0.5 * (vC + vN);
-  double fyyS = -((fb * fb) * dx), fyyN = -((ft * ft) * dx);
+  T vS = (T)U[g.v(j - 1, i)], vC = (T)U[g.v(j, i)], vN = (T)U[g.v(j + 1, i)];
+  T fb = h * (vS + vC), ft = h * (vC + vN);
+  T fyyS = -((fb * fb) * dx), fyyN = -((ft * ft) * dx);
   return (fyx(j, i + 1) - fyx(j, i)) + (fyyN - fyyS);
 }
 
-// nu * raw_l (5-point with channel-wall, inlet and outlet rules) at a u face (solver/optimized_ghost_cell.py:116-120)
-__device__ __forceinline__ double lap_u(const double* __restrict__ U, const Grid& g, int j, int i, double idx2, double idy2,
-                                        bool inlet) {
+// raw_l (5-point with channel-wall, inlet and outlet rules) at a u face (solver/optimized_ghost_cell.py:116-120)
+template <typename T>
+__device__ __forceinline__ T lap_u(const double* __restrict__ U, const Grid& g, int j, int i, T idx2, T idy2,
+                                   bool inlet) {
   const int nx = g.nx, ny = g.ny;
-  double acc = 0.0;
-  if (j > 0) acc += idy2 * U[g.u(j - 1, i)];
-  if (i > 1 || inlet) acc += (i == nx ? 2.0 * idx2 : idx2) * U[g.u(j, i - 1)];
-  acc += (-2.0 * idx2 - ((j == 0 || j == ny - 1) ? 3.0 : 2.0) * idy2) * U[g.u(j, i)];
-  if (i < nx) acc += idx2 * U[g.u(j, i + 1)];
-  if (j < ny - 1) acc += idy2 * U[g.u(j + 1, i)];
+  T acc = 0;
+  if (j > 0) acc += idy2 * (T)U[g.u(j - 1, i)];
+  if (i > 1 || inlet) acc += (i == nx ? (T)2 * idx2 : idx2) * (T)U[g.u(j, i - 1)];
+  acc += ((T)-2 * idx2 - ((j == 0 || j == ny - 1) ? (T)3 : (T)2) * idy2) * (T)U[g.u(j, i)];
+  if (i < nx) acc += idx2 * (T)U[g.u(j, i + 1)];
+  if (j < ny - 1) acc += idy2 * (T)U[g.u(j + 1, i)];
   return acc;
 }
 // at a v face (solver/optimized_ghost_cell.py:121-123); walls v=0 are stored as zeros
-__device__ __forceinline__ double lap_v(const double* __restrict__ U, const Grid& g, int j, int i, double idx2, double idy2) {
+template <typename T>
+__device__ __forceinline__ T lap_v(const double* __restrict__ U, const Grid& g, int j, int i, T idx2, T idy2) {
   const int nx = g.nx;
-  double acc = idy2 * U[g.v(j - 1, i)];
-  if (i > 0) acc += idx2 * U[g.v(j, i - 1)];
-  acc += (-(i == 0 ? 3.0 : (i == nx - 1 ? 1.0 : 2.0)) * idx2 - 2.0 * idy2) * U[g.v(j, i)];
-  if (i < nx - 1) acc += idx2 * U[g.v(j, i + 1)];
-  acc += idy2 * U[g.v(j + 1, i)];
+  T acc = idy2 * (T)U[g.v(j - 1, i)];
+  if (i > 0) acc += idx2 * (T)U[g.v(j, i - 1)];
+  acc += (-(i == 0 ? (T)3 : (i == nx - 1 ? (T)1 : (T)2)) * idx2 - (T)2 * idy2) * (T)U[g.v(j, i)];
+  if (i < nx - 1) acc += idx2 * (T)U[g.v(j, i + 1)];
+  acc += idy2 * (T)U[g.v(j + 1, i)];
   return acc;
 }
 // G p at faces from a pressure grid with ghost values (solver/optimized_ghost_cell.py:94-107)
-__device__ __forceinline__ double grad_u(const double* __restrict__ P, const Grid& g, int j, int i, double gx) {
-  if (i < g.nx) return gx * P[g.p(j, i)] - gx * P[g.p(j, i - 1)];
-  return (-2.0 * gx) * P[g.p(j, g.nx - 1)];
+template <typename T>
+__device__ __forceinline__ T grad_u(const double* __restrict__ P, const Grid& g, int j, int i, T gx) {
+  if (i < g.nx) return gx * (T)P[g.p(j, i)] - gx * (T)P[g.p(j, i - 1)];
+  return ((T)-2 * gx) * (T)P[g.p(j, g.nx - 1)];
 }
-__device__ __forceinline__ double grad_v(const double* __restrict__ P, const Grid& g, int j, int i, double gy) {
-  return gy * P[g.p(j, i)] - gy * P[g.p(j - 1, i)];
+template <typename T>
+__device__ __forceinline__ T grad_v(const double* __restrict__ P, const Grid& g, int j, int i, T gy) {
+  return gy * (T)P[g.p(j, i)] - gy * (T)P[g.p(j - 1, i)];
 }
 
 // decode a face-grid thread index
@@ -427,6 +503,7 @@ __device__ __forceinline__ bool face_of(int64_t t, const Grid& g, int& comp, int
   return true;
 }
 
+template <typename T>
 __global__ void k_momentum(CaseDev c, MomentumArgs a, Gate gate) {
   if (!gate_open(gate)) return;
   const Grid g{c.nx, c.ny, c.usize};
@@ -440,48 +517,55 @@ __global__ void k_momentum(CaseDev c, MomentumArgs a, Gate gate) {
     a.out[t] = a.mode == 1 ? z : 0.0;
     return;
   }
-  const double dx = c.dx, dy = c.dy, idx2 = 1.0 / (dx * dx), idy2 = 1.0 / (dy * dy);
-  const double inv_area = 1.0 / (dx * dy);
-  double q = a.U[t];
-  double lq, gp, now = 0.0, off = 0.0;
+  const T dx = (T)c.dx, dy = (T)c.dy, idx2 = (T)(1.0 / (c.dx * c.dx)), idy2 = (T)(1.0 / (c.dy * c.dy));
+  const T area = (T)(c.dx * c.dy), nu = (T)c.nu, dt = (T)a.dt;
+  const double q = a.U[t];
+  T lq, gp, now = 0, off = 0;
   if (comp == 0) {
-    lq = c.nu * lap_u(a.U, g, j, i, idx2, idy2, true);
-    gp = grad_u(a.P, g, j, i, (1.0 / dx) / c.rho);
+    lq = nu * lap_u<T>(a.U, g, j, i, idx2, idy2, true);
+    gp = grad_u<T>(a.P, g, j, i, (T)((1.0 / c.dx) / c.rho));
     if (a.mode != 2) {
-      now = adv_u(a.U, g, j, i, dx, dy) / (dx * dy);
-      if (i == c.nx) now *= 2;
+      now = adv_u<T>(a.U, g, j, i, dx, dy) / area;
+      if (i == c.nx) now *= (T)2;
     }
-    if (i == 1) off = c.nu * (idx2 * c.inlet[j]);
+    if (i == 1) off = nu * (idx2 * (T)c.inlet[j]);
   } else {
-    lq = c.nu * lap_v(a.U, g, j, i, idx2, idy2);
-    gp = grad_v(a.P, g, j, i, (1.0 / dy) / c.rho);
-    if (a.mode != 2) now = adv_v(a.U, g, j, i, dx, dy) / (dx * dy);
+    lq = nu * lap_v<T>(a.U, g, j, i, idx2, idy2);
+    gp = grad_v<T>(a.P, g, j, i, (T)((1.0 / c.dy) / c.rho));
+    if (a.mode != 2) now = adv_v<T>(a.U, g, j, i, dx, dy) / area;
   }
-  (void)inv_area;
   if (a.mode == 1) {
-    a.now[t] = now;
-    a.out[t] = q + (0.5 * a.dt) * ((now + lq) - gp);
+    a.now[t] = (double)now;
+    a.out[t] = q + (double)(((T)0.5 * dt) * ((now + lq) - gp));
     return;
   }
-  double expl;
+  T expl;
   if (a.mode == 0) {
-    expl = (1.0 + a.alpha) * now - a.alpha * a.prev[t];
-    a.now[t] = now;
+    const T alpha = (T)a.alpha;
+    expl = ((T)1 + alpha) * now - alpha * (T)a.prev[t];
+    a.now[t] = (double)now;
   } else {
     if (comp == 0) {
-      expl = adv_u(a.Uhalf, g, j, i, dx, dy) / (dx * dy);
-      if (i == c.nx) expl *= 2;
+      expl = adv_u<T>(a.Uhalf, g, j, i, dx, dy) / area;
+      if (i == c.nx) expl *= (T)2;
     } else {
-      expl = adv_v(a.Uhalf, g, j, i, dx, dy) / (dx * dy);
+      expl = adv_v<T>(a.Uhalf, g, j, i, dx, dy) / area;
     }
   }
-  a.out[t] = q + a.dt * (expl + 0.5 * lq - gp) + (0.5 * a.dt) * off;
+  // rhs = q + dt (explicit + L q / 2 - G p) + dt/2 offset (solver/numba_kernels.py:596-601)
+  a.out[t] = (q + (double)(dt * (expl + (T)0.5 * lq - gp))) + (double)(((T)0.5 * dt) * off);
 }
 
 void launch_momentum(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st) {
   note_launch();
   kt_mark(3, st);
-  k_momentum<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, gate);
+  k_momentum<double><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, gate);
+  kt_mark(3, st);
+}
+void launch_momentum_f32(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st) {
+  note_launch();
+  kt_mark(3, st);
+  k_momentum<float><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, gate);
   kt_mark(3, st);
 }
 
@@ -495,10 +579,10 @@ __global__ void k_advection(CaseDev c, const double* __restrict__ U, double* __r
   if (!(cls & CLS_ACTIVE)) { out[t] = 0.0; return; }
   double r;
   if (comp == 0) {
-    r = adv_u(U, g, j, i, c.dx, c.dy) / (c.dx * c.dy);
+    r = adv_u<double>(U, g, j, i, c.dx, c.dy) / (c.dx * c.dy);
     if (i == c.nx) r *= 2;
   } else {
-    r = adv_v(U, g, j, i, c.dx, c.dy) / (c.dx * c.dy);
+    r = adv_v<double>(U, g, j, i, c.dx, c.dy) / (c.dx * c.dy);
   }
   out[t] = r;
 }
@@ -517,7 +601,7 @@ __global__ void k_diffusion(CaseDev c, const double* __restrict__ U, double* __r
   const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
   if (!(cls & CLS_ACTIVE)) { out[t] = 0.0; return; }
   const double idx2 = 1.0 / (c.dx * c.dx), idy2 = 1.0 / (c.dy * c.dy);
-  double l = comp == 0 ? c.nu * lap_u(U, g, j, i, idx2, idy2, with_inlet != 0) : c.nu * lap_v(U, g, j, i, idx2, idy2);
+  double l = comp == 0 ? c.nu * lap_u<double>(U, g, j, i, idx2, idy2, with_inlet != 0) : c.nu * lap_v<double>(U, g, j, i, idx2, idy2);
   out[t] = hdt == 0.0 ? l : U[t] - hdt * l;
 }
 void launch_diffusion(const CaseDev& c, const double* U, double* out, bool with_inlet, double hdt, const Gate& gate,
@@ -534,7 +618,7 @@ __global__ void k_gradient(CaseDev c, const double* __restrict__ P, double* __re
   if (!face_of(t, g, comp, j, i)) return;
   const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
   if (!(cls & CLS_ACTIVE)) { out[t] = 0.0; return; }
-  out[t] = comp == 0 ? grad_u(P, g, j, i, (1.0 / c.dx) / c.rho) : grad_v(P, g, j, i, (1.0 / c.dy) / c.rho);
+  out[t] = comp == 0 ? grad_u<double>(P, g, j, i, (1.0 / c.dx) / c.rho) : grad_v<double>(P, g, j, i, (1.0 / c.dy) / c.rho);
 }
 void launch_gradient(const CaseDev& c, const double* P, double* out, const Gate& gate, cudaStream_t st) {
   note_launch();
@@ -690,7 +774,7 @@ __global__ void k_project_update(CaseDev c, const double* __restrict__ q, const 
     out[t] = (comp == 0 && i == 0) ? c.inlet[j] : 0.0;
     return;
   }
-  double gphi = comp == 0 ? grad_u(phi, g, j, i, (1.0 / c.dx) / c.rho) : grad_v(phi, g, j, i, (1.0 / c.dy) / c.rho);
+  double gphi = comp == 0 ? grad_u<double>(phi, g, j, i, (1.0 / c.dx) / c.rho) : grad_v<double>(phi, g, j, i, (1.0 / c.dy) / c.rho);
   out[t] = q[t] - dt * gphi;
 }
 void launch_project_update(const CaseDev& c, const double* q, const double* phi, double dt, double* out,
@@ -714,7 +798,7 @@ __global__ void k_defect(CaseDev c, const double* __restrict__ r, const double* 
     return;
   }
   const double idx2 = 1.0 / (c.dx * c.dx), idy2 = 1.0 / (c.dy * c.dy);
-  double l = comp == 0 ? c.nu * lap_u(r, g, j, i, idx2, idy2, false) : c.nu * lap_v(r, g, j, i, idx2, idy2);
+  double l = comp == 0 ? c.nu * lap_u<double>(r, g, j, i, idx2, idy2, false) : c.nu * lap_v<double>(r, g, j, i, idx2, idy2);
   double hr = r[t] - hdt * l;
   action[t] = hr;
   proj[t] = r[t] + (rhs[t] - hr);
@@ -739,7 +823,7 @@ __global__ void k_pressure_out(CaseDev c, const double* __restrict__ p, const do
     face_of(t, g, comp, j, i);
     const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
     if (cls & CLS_ACTIVE) {
-      double gi = comp == 0 ? grad_u(inc, g, j, i, (1.0 / c.dx) / c.rho) : grad_v(inc, g, j, i, (1.0 / c.dy) / c.rho);
+      double gi = comp == 0 ? grad_u<double>(inc, g, j, i, (1.0 / c.dx) / c.rho) : grad_v<double>(inc, g, j, i, (1.0 / c.dy) / c.rho);
       double r = action[t] - rhs[t] + dt * gi;
       cm = absbits(r);
     }
@@ -843,13 +927,13 @@ void launch_forces(const CaseDev& c, const double* U, const double* P, double mu
   k_forces<<<1, 256, 0, st>>>(c, U, P, mu, dt, ctl, check_gates, out6, gate);
 }
 
-__global__ void k_gate_momentum(StepCtl* ctl) {
+__global__ void k_gate_momentum(StepCtl* ctl, int nchk) {
   if (ctl->err) return;
   double r = 0, bm = 0;
   bool bad = false;
   for (int s = 0; s < 2; ++s) {
     const SolveCtl* sc = &ctl->solve[s];
-    double rr = bits2d(sc->rmax[last_check(sc)]);
+    double rr = bits2d(sc->rmax[last_check(sc, nchk)]);
     double bb = bits2d(sc->bmax);
     if (!(rr <= r)) r = rr;  // propagates NaN
     if (bb > bm) bm = bb;
@@ -858,15 +942,15 @@ __global__ void k_gate_momentum(StepCtl* ctl) {
   double thr = 1e-10 * (bm > 1.0 ? bm : 1.0);
   if (bad || !(r <= thr)) raise_gate(ctl, 2, 2);
 }
-void launch_gate_momentum(StepCtl* ctl, cudaStream_t st) {
+void launch_gate_momentum(StepCtl* ctl, int nchk, cudaStream_t st) {
   note_launch();
-  k_gate_momentum<<<1, 1, 0, st>>>(ctl);
+  k_gate_momentum<<<1, 1, 0, st>>>(ctl, nchk);
 }
 
-__global__ void k_gate_pressure(StepCtl* ctl, int slot) {
+__global__ void k_gate_pressure(StepCtl* ctl, int slot, int nchk) {
   if (ctl->err) return;
   const SolveCtl* sc = &ctl->solve[slot];
-  int k = last_check(sc);
+  int k = last_check(sc, nchk);
   double linf = bits2d(sc->rmax[k]), bound = bits2d(sc->bound[k]), bm = bits2d(sc->bmax);
   if (!isfinite(bm)) { raise_gate(ctl, 1, 4); return; }  // solver/pressure_schur.py:33-34
   double t = 64 * EPS64 * (bm > 1.0 ? bm : 1.0);
@@ -874,9 +958,9 @@ __global__ void k_gate_pressure(StepCtl* ctl, int slot) {
   t = bound > t ? bound : t;
   if (sc->xbad || !(linf <= t)) raise_gate(ctl, 2, 3);
 }
-void launch_gate_pressure(StepCtl* ctl, int slot, cudaStream_t st) {
+void launch_gate_pressure(StepCtl* ctl, int slot, int nchk, cudaStream_t st) {
   note_launch();
-  k_gate_pressure<<<1, 1, 0, st>>>(ctl, slot);
+  k_gate_pressure<<<1, 1, 0, st>>>(ctl, slot, nchk);
 }
 
 __global__ void k_gate_projection(StepCtl* ctl, int k) {

@@ -19,14 +19,19 @@ namespace gmk {
 // class bits of every grid point
 enum : uint8_t { CLS_ACTIVE = 1, CLS_IRREG = 2, CLS_GHOST = 4 };
 
+// Residual checks of one solve: check 0 after the first application of the
+// inverse, check k after refinement sweep k.  Plain FP64 runs at most 2 sweeps (as
+// solver/pressure_schur.py:117-122); the FP32 mode refines up to MAXCHK - 1 times.
+static constexpr int MAXCHK = 8;
+
 // Reduction slots of one monitored solve (zeroed at the start of every step).
 struct SolveCtl {
-  unsigned long long bmax;       // max |b| (bits of a non-negative double)
-  unsigned long long rmax[3];    // max |b - A x| after apply / sweep 1 / sweep 2
-  unsigned long long bound[3];   // roundoff bound max_i w_i (|A||x| + |b|)_i
-  double rsq[3];                 // sum (b - A x)^2
-  double bsq;                    // sum b^2
-  unsigned long long xbad;       // non-finite solution flag
+  unsigned long long bmax;            // max |b| (bits of a non-negative double)
+  unsigned long long rmax[MAXCHK];    // max |b - A x| at each check
+  unsigned long long bound[MAXCHK];   // roundoff bound max_i w_i (|A||x| + |b|)_i
+  double rsq[MAXCHK];                 // sum (b - A x)^2
+  double bsq;                         // sum b^2
+  unsigned long long xbad;            // non-finite solution flag
 };
 
 // Per-step control and diagnostics, one per step in flight.
@@ -68,11 +73,12 @@ __device__ __forceinline__ bool sweep_needed(const SolveCtl* s, int k) {
     if (!(bits2d(s->rmax[c]) > tg)) return false;
   return true;
 }
-// index of the last residual check that ran
-__device__ __forceinline__ int last_check(const SolveCtl* s) {
-  if (sweep_needed(s, 2)) return 2;
-  if (sweep_needed(s, 1)) return 1;
-  return 0;
+// index of the last residual check that ran, out of nchk launched checks
+__device__ __forceinline__ int last_check(const SolveCtl* s, int nchk) {
+  double tg = inner_target(s);
+  int k = 0;
+  while (k + 1 < nchk && bits2d(s->rmax[k]) > tg) ++k;
+  return k;
 }
 
 // Gate for conditionally executed kernels.
@@ -175,6 +181,16 @@ void ktimer_read(double* total_ms, long long* count);
 void launch_rect_inverse(const TransformTables& tt, const RectView& view, const double* b, bool mask_in,
                          double* spectral, double* out, const double* sub, const double* add, const Gate& gate,
                          cudaStream_t st);
+// FP32 separable inverse (tables of tt in float): b (float64 field) -> first (float32 field)
+void launch_rect_inverse_f32(const TransformTables& tt, const RectView& view, const double* b, bool mask_in,
+                             float* spectral, float* first, const Gate& gate, cudaStream_t st);
+// FP32 separable inverse of w2 with the epilogue out = active ? add + (sub - T^{-1} w2) : 0 (float64 out)
+void launch_rect_inverse_f32_final(const TransformTables& tt, const RectView& view, const double* w2,
+                                   float* spectral, double* out, const float* sub, const double* add,
+                                   const Gate& gate, cudaStream_t st);
+void launch_schur_f32(const float* first, const RectView& view, int rank, const int64_t* rows, const int64_t* c_ptr,
+                      const int64_t* c_col, const double* c_val, const double* sinv, double* w2, const Gate& gate,
+                      cudaStream_t st);
 
 void launch_schur(const double* first, const RectView& view, int rank, const int64_t* rows, const int64_t* c_ptr,
                   const int64_t* c_col, const double* c_val, const double* sinv, double* w2, const Gate& gate,
@@ -200,6 +216,8 @@ struct MomentumArgs {
   int mode;
 };
 void launch_momentum(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st);
+// same with the stencil arithmetic in FP32 (inputs, outputs and q + increment in FP64)
+void launch_momentum_f32(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st);
 
 // single operators on face grids (for the operator API)
 void launch_advection(const CaseDev& c, const double* U, double* out, const Gate& gate, cudaStream_t st);
@@ -232,15 +250,15 @@ void launch_maxabs(const CaseDev& c, const double* U, unsigned long long* umax, 
 void launch_forces(const CaseDev& c, const double* U, const double* P, double mu, double dt, StepCtl* ctl,
                    int check_gates, double* out6, const Gate& gate, cudaStream_t st);
 
-// CN momentum gate (after both Helmholtz solves)
-void launch_gate_momentum(StepCtl* ctl, cudaStream_t st);
+// CN momentum gate (after both Helmholtz solves), nchk residual checks per solve
+void launch_gate_momentum(StepCtl* ctl, int nchk, cudaStream_t st);
 // projection divergence gate on div_max[k]
 void launch_gate_projection(StepCtl* ctl, int k, cudaStream_t st);
 // CFL screen: dt*(umax/dx + vmax/dy) > 0.5 -> error (values from a previous maxabs)
 void launch_cfl_screen(StepCtl* ctl, const unsigned long long* umax, const unsigned long long* vmax, double dt,
                        double dx, double dy, int screen, cudaStream_t st);
 
-void launch_gate_pressure(StepCtl* ctl, int slot, cudaStream_t st);
+void launch_gate_pressure(StepCtl* ctl, int slot, int nchk, cudaStream_t st);
 // dst[k] = src[idx[k]] and dst[idx[k]] = src[k]
 void launch_gather(const double* src, const int64_t* idx, int64_t n, double* dst, cudaStream_t st);
 void launch_scatter(const double* src, const int64_t* idx, int64_t n, double* dst, cudaStream_t st);

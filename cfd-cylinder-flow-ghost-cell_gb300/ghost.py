@@ -204,7 +204,10 @@ class MAC_CylinderFlow:
                  nu=0.01, rho=1.0, U_inf=1.0, inflow='uniform', U_m=None,
                  slip_walls=False, verbose=True, boundary='ghost_cell', transport='centered',
                  pressure_solver='direct', marker_spacing_factor=1.5, time_scheme='ab2_cn',
-                 ghost_pressure_extension='neumann', ghost_velocity_interpolation='bilinear'):
+                 ghost_pressure_extension='neumann', ghost_velocity_interpolation='bilinear', precision='fp64'):
+        """Keywords of solver/main.py:40-44.  ``precision`` (this library only): 'fp64' runs the plain
+        FP64 method; 'fp32' runs the separable inverses and the momentum stencils in FP32 and
+        refines every solve against the FP64 operator until the reference's residual targets hold."""
         # argument checks of solver/main.py:45-80
         if boundary not in ('immersed', 'staircase', 'ghost_cell', 'cut_cell') or transport not in ('centered', 'upwind'):
             raise ValueError('Choose boundary=immersed/staircase/ghost_cell/cut_cell and transport=centered/upwind')
@@ -223,12 +226,15 @@ class MAC_CylinderFlow:
             raise ValueError('nx and ny must be integers >= 4')
         if U_m is not None and (not np.isfinite(U_m) or U_m <= 0):
             raise ValueError('U_m must be finite and positive')
+        if precision not in ('fp64', 'fp32'):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
+        self.precision = precision
         self.configuration = dict(nx=nx, ny=ny, Lx=Lx, Ly=Ly, D=D, xc=xc, yc=yc, nu=nu, rho=rho, U_inf=U_inf,
                                   inflow=inflow, U_m=U_m, slip_walls=slip_walls, boundary=boundary,
                                   transport=transport, pressure_solver=pressure_solver,
                                   marker_spacing_factor=marker_spacing_factor, time_scheme=time_scheme,
                                   verbose=False, ghost_pressure_extension=ghost_pressure_extension,
-                                  ghost_velocity_interpolation=ghost_velocity_interpolation)
+                                  ghost_velocity_interpolation=ghost_velocity_interpolation, precision=precision)
         self.boundary, self.transport, self.pressure_solver, self.time_scheme = boundary, transport, pressure_solver, time_scheme
         self.ghost_pressure_extension = ghost_pressure_extension
         self.ghost_velocity_interpolation = ghost_velocity_interpolation
@@ -243,7 +249,7 @@ class MAC_CylinderFlow:
                           pressure_solver=0 if pressure_solver == 'direct' else 1,
                           pressure_extension=0 if ghost_pressure_extension == 'neumann' else 1,
                           velocity_interpolation=0 if ghost_velocity_interpolation == 'bilinear' else 1,
-                          precision=0)
+                          precision=0 if precision == 'fp64' else 1)
         h = C.c_void_p()
         t0 = _time.time()
         check(lib.gm_create(C.byref(cfg), C.byref(h)))

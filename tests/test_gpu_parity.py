@@ -200,3 +200,43 @@ def test_gates_raise(pkg):
     s = small(pkg)
     s.solve(n_steps=2, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
     assert s.last_step_diagnostics['max_divergence'] < 1e-10
+
+
+# ---------------------------------------------------------------------------
+# FP32 separable inverses with FP64 refinement
+# ---------------------------------------------------------------------------
+def test_fp32_mode_matches_fp64_oracle(pkg):
+    """FP32 inverses refined against the FP64 operators: same gates, divergence < 1e-10,
+    fields within 1e-7 and force coefficients within 1e-6 of the FP64 oracle after 20 steps."""
+    kw = dict(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., nu=0.02)
+    s = pkg.MAC_CylinderFlow(verbose=False, precision='fp32', **kw)
+    c = go.CylinderCase(**kw)
+    q = c.ops.pack(c.u, c.v)
+    q += 1e-2 * np.random.default_rng(5).standard_normal(q.size)
+    c.u, c.v = c.ops.unpack(q)
+    s.u[:], s.v[:] = c.u, c.v
+    s.solve(n_steps=20, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+    c.solve(20, .002)
+    d = s.last_step_diagnostics
+    assert d['max_divergence'] < 1e-10
+    for key in ('u', 'v'):
+        assert rel(getattr(s, key), getattr(c, key)) < 1e-7, key
+    assert rel(s.p, c.p) < 1e-6
+    assert abs(d['cd'] / c.last_step_diagnostics['cd'] - 1) < 1e-6
+    assert d['pressure_refinement_iterations'] >= 1
+
+
+def test_fp32_mode_config1(pkg):
+    G = np.load(GOLDEN / 'config1_400x200.npz')
+    s = pkg.MAC_CylinderFlow(nx=400, ny=200, Lx=20., Ly=10., D=1., xc=5., yc=5., nu=1 / 40, verbose=False,
+                             precision='fp32')
+    q = s.gg.pack(s.u, s.v)
+    q += 1e-3 * np.random.default_rng(0).standard_normal(q.size)
+    s.u[:], s.v[:] = s.gg.unpack(q)
+    for k in range(2):
+        s.solve(n_steps=1, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+        assert rel(s.u.ravel()[G['sample_u']], G['u_samples'][k]) < 1e-8
+        assert rel(s.p.ravel()[G['sample_p']], G['p_samples'][k]) < 1e-6
+        d = s.last_step_diagnostics
+        assert abs(d['cd'] - G['scalars'][k][0]) < 1e-6 * abs(G['scalars'][k][0])
+        assert d['max_divergence'] < 1e-10
