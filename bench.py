@@ -169,7 +169,7 @@ def run_ours(args, w, rank, world):
     kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
     dt = w['dt']
     cells = w['nx'] * w['ny']
-    s = pkg.MAC_CylinderFlow(verbose=False, **kw)
+    s = pkg.MAC_CylinderFlow(verbose=False, precision=args.precision, **kw)
     seeded_state(s, w)
     stream = torch.cuda.Stream()
     L.check(L.lib.gm_set_stream(s._h, C.c_void_p(stream.cuda_stream)), s._h)
@@ -252,8 +252,9 @@ def run_ours(args, w, rank, world):
     if rank == 0:
         line = dict(metric=METRIC, value=value, unit='cell-updates/s', n_gpus=world, steps=args.steps,
                     warmup=args.warmup, ms_per_step=step_ms, higher_is_better=True, scaling='weak',
-                    vs_baseline=None, dtype='f64', data='synthetic',
-                    config=dict(workload=args.workload, grid=f'{nx}x{ny}', dt=dt, precision='fp64 plain',
+                    vs_baseline=None, dtype='f64' if args.precision == 'fp64' else 'f32+f64-refine', data='synthetic',
+                    config=dict(workload=args.workload, grid=f'{nx}x{ny}', dt=dt,
+                                precision='fp64 plain' if args.precision == 'fp64' else 'fp32 inverses/stencils, fp64 refinement',
                                 cases_per_gpu=1, parallelism='replicas', l2='flushed (256 MB write) between timed steps',
                                 pressure='DCT/DST fast inverse + boundary Schur (direct)'),
                     roofline=dict(bound='hbm', achieved=achieved, peak=peak, unit='GB/s', frac=achieved / peak,
@@ -277,6 +278,8 @@ def main():
     ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
     ap.add_argument('--workload', choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
+    ap.add_argument('--precision', choices=('fp64', 'fp32'), default='fp64',
+                    help='fp64: plain FP64 method; fp32: FP32 inverses and stencils with FP64 refinement')
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
