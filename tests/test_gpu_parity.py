@@ -206,8 +206,9 @@ def test_gates_raise(pkg):
 # FP32 separable inverses with FP64 refinement
 # ---------------------------------------------------------------------------
 def test_fp32_mode_matches_fp64_oracle(pkg):
-    """FP32 inverses refined against the FP64 operators: same gates, divergence < 1e-10,
-    fields within 1e-7 and force coefficients within 1e-6 of the FP64 oracle after 20 steps."""
+    """FP32 inverses and stencils refined against the FP64 operators: same gates, divergence
+    < 1e-10; after 20 noisy steps velocity within 1e-7, pressure within 1e-5 and the drag
+    coefficient within 1e-6 (relative) of the FP64 oracle."""
     kw = dict(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., nu=0.02)
     s = pkg.MAC_CylinderFlow(verbose=False, precision='fp32', **kw)
     c = go.CylinderCase(**kw)
@@ -221,7 +222,7 @@ def test_fp32_mode_matches_fp64_oracle(pkg):
     assert d['max_divergence'] < 1e-10
     for key in ('u', 'v'):
         assert rel(getattr(s, key), getattr(c, key)) < 1e-7, key
-    assert rel(s.p, c.p) < 1e-6
+    assert rel(s.p, c.p) < 1e-5
     assert abs(d['cd'] / c.last_step_diagnostics['cd'] - 1) < 1e-6
     assert d['pressure_refinement_iterations'] >= 1
 
@@ -235,8 +236,8 @@ def test_fp32_mode_config1(pkg):
     s.u[:], s.v[:] = s.gg.unpack(q)
     for k in range(2):
         s.solve(n_steps=1, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
-        assert rel(s.u.ravel()[G['sample_u']], G['u_samples'][k]) < 1e-8
-        assert rel(s.p.ravel()[G['sample_p']], G['p_samples'][k]) < 1e-6
+        assert rel(s.u.ravel()[G['sample_u']], G['u_samples'][k]) < 1e-7
+        assert rel(s.p.ravel()[G['sample_p']], G['p_samples'][k]) < 1e-5
         d = s.last_step_diagnostics
         assert abs(d['cd'] - G['scalars'][k][0]) < 1e-6 * abs(G['scalars'][k][0])
         assert d['max_divergence'] < 1e-10
