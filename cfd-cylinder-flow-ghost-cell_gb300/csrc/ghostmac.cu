@@ -6,6 +6,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <memory>
@@ -157,6 +159,23 @@ struct gm_handle {
   DBuf<StepCtl> ctl;
   DBuf<unsigned long long> state_max;  // persistent max|u|, max|v| of the current state
   StepCtl* host_ctl = nullptr;
+  // step records and graphs
+  static constexpr int RING_CAP = 64;
+  DBuf<StepCtl> ring;
+  DBuf<int> ridx;
+  DBuf<long long> counter;
+  StepCtl* host_ring = nullptr;
+  cudaStream_t st_body = nullptr;  // capture stream of conditional-node bodies
+  bool use_graphs = true;
+  bool capturing = false;
+  struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    const double* key[6] = {};
+    double dt = 0;
+    long long outer_nodes = 0;  // kernel nodes outside the refinement loops
+    long long body_nodes = 0;   // kernel nodes of one refinement sweep
+  } graphs[2];
+  long long body_nodes_capture = 0;
   bool has_history = false;
   bool host_only = false;
   int precision = 0;  // 0 plain FP64, 1 FP32 inverse with FP64 refinement
@@ -501,25 +520,70 @@ void ghost_p(gm_handle* h, double* P, const Gate& gt) {
 // one boundary-row solve of kind k into x with residual checks (solver/pressure_schur.py:103-124)
 // In the FP32 mode every application of the inverse runs in FP32 and the residual
 // b - A x in FP64, so the refinement sweeps recover an FP64 solution.
-void schur_solve(gm_handle* h, RectDev& rd, int kind, double hc, const double* b, double* x, double* res,
-                 double* first, double* w2, int slot) {
+// One application of the (FP64 or FP32) boundary-corrected inverse: x = [x +] T^{-1} r - T^{-1} U S^{-1} C T^{-1} r.
+void apply_inverse(gm_handle* h, RectDev& rd, int kind, const double* r, double* x, bool accumulate, double* first,
+                   double* w2, const Gate& gt, cudaStream_t st) {
+  if (h->precision == 1) {
+    float* first32 = kind == 0 ? h->pfirst32.p : h->ffirst32.p;
+    launch_rect_inverse_f32(rd.tt32, rd.view, r, true, h->spectral32.p, first32, gt, st);
+    launch_schur_f32(first32, rd.view, rd.rank, rd.rows.p, rd.cptr.p, rd.ccol.p, rd.cval.p, rd.sinv.p, w2, gt, st);
+    launch_rect_inverse_f32_final(rd.tt32, rd.view, w2, h->spectral32.p, x, first32, accumulate ? x : nullptr, gt,
+                                  st);
+  } else {
+    launch_rect_inverse(rd.tt, rd.view, r, true, h->spectral.p, first, nullptr, nullptr, gt, st);
+    launch_schur(first, rd.view, rd.rank, rd.rows.p, rd.cptr.p, rd.ccol.p, rd.cval.p, rd.sinv.p, w2, gt, st);
+    launch_rect_inverse(rd.tt, rd.view, w2, false, h->spectral.p, x, first, accumulate ? x : nullptr, gt, st);
+  }
+}
+
+// The same solve while the step is being captured into a CUDA graph: the refinement
+// sweeps form a WHILE conditional node whose body runs only while the residual check
+// exceeds the target, so no sweep kernel launches when none is needed.
+void schur_solve_graph(gm_handle* h, RectDev& rd, int kind, double hc, const double* b, double* x, double* res,
+                       double* first, double* w2, int slot) {
   cudaStream_t st = h->st;
   SolveCtl* sc = &h->ctl.p->solve[slot];
-  const bool mixed = h->precision == 1;
-  float* first32 = kind == 0 ? h->pfirst32.p : h->ffirst32.p;
+  Gate g0 = gate_of(h, slot, 0);
+  apply_inverse(h, rd, kind, b, x, false, first, w2, g0, st);
+  launch_residual(h->cd, kind, hc, b, x, res, sc, 0, true, g0, st);
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t graph;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, nullptr, nullptr, nullptr));
+  cudaGraphConditionalHandle cond;
+  CK(cudaGraphConditionalHandleCreate(&cond, graph, 0, 0));
+  launch_refine_decide(h->ctl.p, slot, h->nchk, cond, st);
+  CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &nd));
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = cond;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cnode;
+  CK(cudaGraphAddNode(&cnode, graph, deps, nullptr, nd, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CK(cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+  CK(cudaStreamBeginCaptureToGraph(h->st_body, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  long long c0 = kernel_launch_count();
+  apply_inverse(h, rd, kind, res, x, true, first, w2, g0, h->st_body);
+  launch_residual(h->cd, kind, hc, b, x, res, sc, -1, false, g0, h->st_body);
+  launch_refine_decide(h->ctl.p, slot, h->nchk, cond, h->st_body);
+  h->body_nodes_capture = kernel_launch_count() - c0;
+  CK(cudaStreamEndCapture(h->st_body, &body));
+}
+
+void schur_solve(gm_handle* h, RectDev& rd, int kind, double hc, const double* b, double* x, double* res,
+                 double* first, double* w2, int slot) {
+  if (h->capturing) {
+    schur_solve_graph(h, rd, kind, hc, b, x, res, first, w2, slot);
+    return;
+  }
+  cudaStream_t st = h->st;
+  SolveCtl* sc = &h->ctl.p->solve[slot];
   for (int sweep = 0; sweep < h->nchk; ++sweep) {
     Gate gt = gate_of(h, slot, sweep);
-    const double* rhs = sweep == 0 ? b : res;
-    if (mixed) {
-      launch_rect_inverse_f32(rd.tt32, rd.view, rhs, true, h->spectral32.p, first32, gt, st);
-      launch_schur_f32(first32, rd.view, rd.rank, rd.rows.p, rd.cptr.p, rd.ccol.p, rd.cval.p, rd.sinv.p, w2, gt, st);
-      launch_rect_inverse_f32_final(rd.tt32, rd.view, w2, h->spectral32.p, x, first32, sweep == 0 ? nullptr : x, gt,
-                                    st);
-    } else {
-      launch_rect_inverse(rd.tt, rd.view, rhs, true, h->spectral.p, first, nullptr, nullptr, gt, st);
-      launch_schur(first, rd.view, rd.rank, rd.rows.p, rd.cptr.p, rd.ccol.p, rd.cval.p, rd.sinv.p, w2, gt, st);
-      launch_rect_inverse(rd.tt, rd.view, w2, false, h->spectral.p, x, first, sweep == 0 ? nullptr : x, gt, st);
-    }
+    apply_inverse(h, rd, kind, sweep == 0 ? b : res, x, sweep > 0, first, w2, gt, st);
     launch_residual(h->cd, kind, hc, b, x, res, sc, sweep, sweep == 0, gt, st);
   }
 }
@@ -550,6 +614,9 @@ void ensure_helmholtz(gm_handle* h, double dt) {
   h->helm_ready = true;
   h->helm_dt = dt;
   if (h->host_only) return;
+  // the Helmholtz tables are reallocated below: captured step graphs would point at freed buffers
+  for (auto& gr : h->graphs)
+    if (gr.exec) { cudaGraphExecDestroy(gr.exec); gr.exec = nullptr; }
   build_class_maps(h);
   upload_csr(h->irr[1], h->hs.rows_irr[0], h->hs.irr[0], h->st);
   upload_csr(h->irr[2], h->hs.rows_irr[1], h->hs.irr[1], h->st);
@@ -569,13 +636,17 @@ void momentum(gm_handle* h, const MomentumArgs& ma, const Gate& g0) {
 }
 
 // One AB2/CN step (solver/time_integration.py:7-145) on the handle state.
-void step_once(gm_handle* h, double dt, bool screen) {
+// screen: 1/0 run or skip the CFL screen, -1 decide on the device from the step counter.
+// The error word of the control block is sticky: only the per-step slots are cleared, so
+// every kernel after a failed gate (also in later captured steps) does nothing.
+void step_once(gm_handle* h, double dt, int screen) {
   cudaStream_t st = h->st;
   const double hdt = 0.5 * dt;
   const double hc = (0.5 * dt) * h->g.nu;
   Gate g0 = gate_of(h);
-  CK(cudaMemsetAsync(h->ctl.p, 0, sizeof(StepCtl), st));
-  launch_cfl_screen(h->ctl.p, &h->state_max.p[0], &h->state_max.p[1], dt, h->g.dx, h->g.dy, screen ? 1 : 0, st);
+  const size_t keep = offsetof(StepCtl, solve);
+  CK(cudaMemsetAsync(reinterpret_cast<char*>(h->ctl.p) + keep, 0, sizeof(StepCtl) - keep, st));
+  launch_cfl_screen(h->ctl.p, &h->state_max.p[0], &h->state_max.p[1], dt, h->g.dx, h->g.dy, screen, h->counter.p, st);
   const bool first = !h->has_history;
   // pressure at the previous half step: the stored half pressure, or p at active cells
   // when there is no history (solver/optimized_ghost_cell.py:256); ghost values for G p
@@ -620,16 +691,59 @@ void step_once(gm_handle* h, double dt, bool screen) {
   // diagnostics on the new state, forces and the step gates (solver/main.py:383-415)
   launch_maxabs(h->cd, h->Unext.p, &h->ctl.p->umax, &h->ctl.p->vmax, g0, st);
   launch_forces(h->cd, h->Unext.p, h->pout.p, h->g.nu * h->g.rho, dt, h->ctl.p, 1, nullptr, g0, st);
+  launch_step_end(h->ctl.p, h->state_max.p, h->ring.p, h->ridx.p, h->counter.p, gm_handle::RING_CAP, st);
   CK(cudaGetLastError());
 }
 
-void commit_step(gm_handle* h, double dt) {
+void swap_state(gm_handle* h) {
   std::swap(h->U.p, h->Unext.p);
   std::swap(h->phalf.p, h->phalf_next.p);
   std::swap(h->hist.p, h->now.p);
+}
+void commit_step(gm_handle* h, double dt) {
+  swap_state(h);
   h->has_history = true;
   h->prev_dt = dt;
-  CK(cudaMemcpyAsync(h->state_max.p, &h->ctl.p->umax, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, h->st));
+}
+
+// Graph of one steady step for the current buffer assignment and dt (captured on demand,
+// two alternate between the ping-pong buffer assignments).
+cudaGraphExec_t step_graph(gm_handle* h, double dt) {
+  const double* key[6] = {h->U.p, h->Unext.p, h->phalf.p, h->phalf_next.p, h->hist.p, h->now.p};
+  for (auto& gr : h->graphs)
+    if (gr.exec && gr.dt == dt && std::equal(key, key + 6, gr.key)) return gr.exec;
+  gm_handle::StepGraph* slot = !h->graphs[0].exec || h->graphs[0].dt != dt ? &h->graphs[0]
+                               : (!h->graphs[1].exec || h->graphs[1].dt != dt ? &h->graphs[1] : &h->graphs[0]);
+  if (slot->exec) { cudaGraphExecDestroy(slot->exec); slot->exec = nullptr; }
+  const long long c0 = kernel_launch_count();
+  long long body_total = 0;
+  h->capturing = true;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+  try {
+    step_once(h, dt, -1);
+  } catch (...) {
+    h->capturing = false;
+    cudaStreamEndCapture(h->st, &g);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    throw;
+  }
+  h->capturing = false;
+  CK(cudaStreamEndCapture(h->st, &g));
+  const long long captured = kernel_launch_count() - c0;
+  kernel_launch_adjust(-captured);
+  body_total = 4 * h->body_nodes_capture;  // four refinement loops per steady step
+  slot->body_nodes = h->body_nodes_capture;
+  slot->outer_nodes = captured - body_total;
+  cudaGraphExec_t ex = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) throw CudaError(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  slot->exec = ex;
+  slot->dt = dt;
+  std::copy(key, key + 6, slot->key);
+  return ex;
 }
 
 void fill_diag(gm_handle* h, const StepCtl& c, double t, double dt, bool first, gm_step_diag* d) {
@@ -816,6 +930,14 @@ int gm_create(const gm_config* cfg, gm_handle** out) {
     }
     H->ctl.alloc(1);
     H->ctl.zero(st);
+    H->ring.alloc(gm_handle::RING_CAP);
+    H->ridx.alloc(1);
+    H->ridx.zero(st);
+    H->counter.alloc(1);
+    H->counter.zero(st);
+    CK(cudaMallocHost(&H->host_ring, gm_handle::RING_CAP * sizeof(StepCtl)));
+    CK(cudaStreamCreateWithFlags(&H->st_body, cudaStreamNonBlocking));
+    if (const char* e = std::getenv("GHOSTMAC_NO_GRAPHS")) H->use_graphs = !(e[0] == '1');
     H->state_max.alloc(2);
     H->state_max.zero(st);
     CK(cudaMallocHost(&H->host_ctl, sizeof(StepCtl)));
@@ -856,6 +978,10 @@ int gm_destroy(gm_handle* h) {
   if (!h) return GM_OK;
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->host_ctl) cudaFreeHost(h->host_ctl);
+  if (h->host_ring) cudaFreeHost(h->host_ring);
+  for (auto& gr : h->graphs)
+    if (gr.exec) cudaGraphExecDestroy(gr.exec);
+  if (h->st_body) cudaStreamDestroy(h->st_body);
   cudaStream_t st = h->st;
   bool own = h->own_stream;
   delete h;
@@ -1038,19 +1164,63 @@ int gm_step(gm_handle* h, double dt, int32_t n_steps, int64_t first_step_index, 
   if (!(std::isfinite(dt) && dt > 0) || n_steps <= 0) { h->err = "dt must be finite and positive"; return GM_EVALUE; }
   return run_guarded(h, [&] {
     ensure_helmholtz(h, dt);
-    for (int s = 0; s < n_steps; ++s) {
-      bool first = !h->has_history;
-      bool screen = ((first_step_index + s) % 100) == 0;
-      step_once(h, dt, screen);
-      CK(cudaMemcpyAsync(h->host_ctl, h->ctl.p, sizeof(StepCtl), cudaMemcpyDeviceToHost, h->st));
-      CK(cudaStreamSynchronize(h->st));
+    cudaStream_t st = h->st;
+    CK(cudaMemsetAsync(h->ctl.p, 0, sizeof(StepCtl), st));  // clears the sticky error word
+    long long counter = first_step_index;
+    CK(cudaMemcpyAsync(h->counter.p, &counter, sizeof counter, cudaMemcpyHostToDevice, st));
+    int s = 0;
+    while (s < n_steps) {
+      // steps that differ from the steady pattern run launch by launch: the start-up step,
+      // a changed dt, or per-kernel event timing
+      const bool direct = !h->has_history || h->prev_dt != dt || !h->use_graphs || ktimer_active();
+      const bool first = !h->has_history;
+      const int batch = direct ? 1 : std::min(n_steps - s, (int)gm_handle::RING_CAP);
+      CK(cudaMemsetAsync(h->ridx.p, 0, sizeof(int), st));
+      if (direct) {
+        step_once(h, dt, ((first_step_index + s) % 100) == 0 ? 1 : 0);
+        swap_state(h);
+      } else {
+        for (int k = 0; k < batch; ++k) {
+          CK(cudaGraphLaunch(step_graph(h, dt), st));
+          swap_state(h);
+        }
+      }
+      CK(cudaMemcpyAsync(h->host_ring, h->ring.p, batch * sizeof(StepCtl), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
       ktimer_collect();
-      double t = start_time + (s + 1) * dt;
-      if (diag) fill_diag(h, *h->host_ctl, t, dt, first, &diag[s]);
-      if (h->host_ctl->err) check_ctl(h, "step");
-      commit_step(h, dt);
+      int good = 0;
+      while (good < batch && h->host_ring[good].err == 0) ++good;
+      if (!direct) {
+        // kernel nodes the replays executed: outer nodes + one sweep body per refinement iteration
+        const gm_handle::StepGraph& gr = h->graphs[0].exec ? h->graphs[0] : h->graphs[1];
+        long long nodes = 0;
+        for (int k = 0; k < batch; ++k) {
+          const StepCtl& c = h->host_ring[k];
+          int sweeps = 0;
+          for (int sl = 0; sl < 5; ++sl) sweeps += c.solve[sl].k;
+          nodes += gr.outer_nodes + gr.body_nodes * sweeps;
+        }
+        kernel_launch_adjust(nodes);
+      }
+      for (int k = 0; k < std::min(batch, good + 1); ++k)
+        if (diag) fill_diag(h, h->host_ring[k], start_time + (s + k + 1) * dt, dt, first && k == 0, &diag[s + k]);
+      if (good < batch) {
+        // back to the state after the last good step
+        if ((batch - good) % 2) swap_state(h);
+        if (good > 0) { h->has_history = true; h->prev_dt = dt; }
+        *h->host_ctl = h->host_ring[good];
+        static const char* names[] = {"", "Ghost projection failed", "CN momentum solve failed",
+                                      "Pressure solve failed", "Pressure RHS must be finite",
+                                      "Ghost step failed divergence/CFL gate", "Non-finite force",
+                                      "Explicit timestep unsafe",
+                                      "Finite fields and a positive timestep are required"};
+        const StepCtl& c = h->host_ring[good];
+        throw GateError(c.err, std::string(names[c.gate < 9 ? c.gate : 0]) + " (step)");
+      }
+      h->has_history = true;
+      h->prev_dt = dt;
+      s += batch;
     }
-    CK(cudaStreamSynchronize(h->st));
   });
 }
 

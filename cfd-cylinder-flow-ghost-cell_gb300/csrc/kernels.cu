@@ -65,6 +65,9 @@ static inline unsigned blocks_for(int64_t n, int tpb = TPB) { return (unsigned)(
 static std::atomic<long long> g_launches{0};
 static inline void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 long long kernel_launch_count() { return g_launches.load(); }
+// Graph capture records launches that have not run yet; the host corrects the count by the
+// captured nodes and adds the nodes a graph replay executed.
+void kernel_launch_adjust(long long delta) { g_launches.fetch_add(delta, std::memory_order_relaxed); }
 
 // Optional CUDA-event timing of one kernel class on its own stream (used by the
 // benchmark to time the dominant kernel inside the timed region).
@@ -104,6 +107,7 @@ void ktimer_collect() {
   cudaGetLastError();
   g_kt.used = 0;
 }
+bool ktimer_active() { return g_kt.cls != 0; }
 void ktimer_read(double* total_ms, long long* count) {
   *total_ms = g_kt.total_ms;
   *count = g_kt.count;
@@ -642,6 +646,7 @@ __device__ __forceinline__ int find_row(const int64_t* rows, int n, int64_t key)
 __global__ void k_residual(CaseDev c, int kind, double hc, const double* __restrict__ b, const double* __restrict__ x,
                            double* __restrict__ res, SolveCtl* sc, int check, int first, Gate gate) {
   if (!gate_open(gate)) return;
+  if (check < 0) check = *(volatile int*)&sc->k;
   const int nx = c.nx, ny = c.ny;
   int64_t npts = kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize);
   int64_t base = kind == 2 ? c.usize : 0;  // face-grid offset of the v field
@@ -976,16 +981,56 @@ void launch_gate_projection(StepCtl* ctl, int k, cudaStream_t st) {
 // CFL screen of solver/main.py:273-278 (screen != 0) and the finite-field check of
 // solver/time_integration.py:15-17 on the velocity maxima of the current state.
 __global__ void k_cfl_screen(StepCtl* ctl, const unsigned long long* umax, const unsigned long long* vmax, double dt,
-                             double dx, double dy, int screen) {
+                             double dx, double dy, int screen, const long long* counter) {
   if (ctl->err) return;
+  if (screen < 0) screen = (*counter % 100) == 0;
   double rate = bits2d(*umax) / dx + bits2d(*vmax) / dy;
   if (screen && (!isfinite(rate) || dt * rate > 0.5)) raise_gate(ctl, 2, 7);
   else if (!isfinite(rate)) raise_gate(ctl, 1, 8);
 }
 void launch_cfl_screen(StepCtl* ctl, const unsigned long long* umax, const unsigned long long* vmax, double dt,
-                       double dx, double dy, int screen, cudaStream_t st) {
+                       double dx, double dy, int screen, const long long* counter, cudaStream_t st) {
   note_launch();
-  k_cfl_screen<<<1, 1, 0, st>>>(ctl, umax, vmax, dt, dx, dy, screen);
+  k_cfl_screen<<<1, 1, 0, st>>>(ctl, umax, vmax, dt, dx, dy, screen, counter);
+}
+
+__global__ void k_refine_decide(StepCtl* ctl, int slot, int nchk, cudaGraphConditionalHandle cond) {
+  SolveCtl* sc = &ctl->solve[slot];
+  int k = sc->k;
+  bool need = false;
+  if (!ctl->err) need = bits2d(sc->rmax[k]) > inner_target(sc) && k + 1 < nchk;
+  if (need) sc->k = k + 1;
+  cudaGraphSetConditional(cond, need ? 1u : 0u);
+}
+void launch_refine_decide(StepCtl* ctl, int slot, int nchk, cudaGraphConditionalHandle cond, cudaStream_t st) {
+  note_launch();
+  k_refine_decide<<<1, 1, 0, st>>>(ctl, slot, nchk, cond);
+}
+
+__global__ void k_step_end(StepCtl* ctl, unsigned long long* state_max, StepCtl* ring, int* ridx, long long* counter,
+                           int cap) {
+  __shared__ int slot;
+  if (threadIdx.x == 0) {
+    slot = min(*ridx, cap - 1);
+    if (!ctl->err) {
+      state_max[0] = ctl->umax;
+      state_max[1] = ctl->vmax;
+    }
+  }
+  __syncthreads();
+  const int* src = reinterpret_cast<const int*>(ctl);
+  int* dst = reinterpret_cast<int*>(ring + slot);
+  for (int i = threadIdx.x; i < (int)(sizeof(StepCtl) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *ridx = slot + 1;
+    *counter = *counter + 1;
+  }
+}
+void launch_step_end(StepCtl* ctl, unsigned long long* state_max, StepCtl* ring, int* ridx, long long* counter,
+                     int cap, cudaStream_t st) {
+  note_launch();
+  k_step_end<<<1, 128, 0, st>>>(ctl, state_max, ring, ridx, counter, cap);
 }
 
 __global__ void k_copy_active(const uint8_t* __restrict__ cls, int64_t n, const double* __restrict__ src,

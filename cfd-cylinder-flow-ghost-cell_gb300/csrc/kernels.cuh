@@ -32,6 +32,8 @@ struct SolveCtl {
   double rsq[MAXCHK];                 // sum (b - A x)^2
   double bsq;                         // sum b^2
   unsigned long long xbad;            // non-finite solution flag
+  int k;                              // current check index (graph-driven refinement loop)
+  int pad_;
 };
 
 // Per-step control and diagnostics, one per step in flight.
@@ -170,6 +172,7 @@ struct TransformTables {      // device tables of one rectangle kind (T = double
 // ---- launchers (kernels.cu) ------------------------------------------------
 int configure_kernels(int smem_optin);
 long long kernel_launch_count();
+void kernel_launch_adjust(long long delta);
 // kernel classes for event timing: 1 x pass, 2 y pass, 3 momentum, 4 residual
 void ktimer_enable(int cls);
 void ktimer_collect();
@@ -200,7 +203,8 @@ void launch_ghost(double* field, int n, const int64_t* rows, const int64_t* ptr,
                   const double* val, const Gate& gate, cudaStream_t st);
 
 // residual of the operator of kind (0 pressure A, 1 Helmholtz u, 2 Helmholtz v)
-// res = b - Op x on active points; reductions into sc at check index k
+// res = b - Op x on active points; reductions into sc at check index `check`
+// (check < 0: the index sc->k maintained by launch_refine_decide)
 void launch_residual(const CaseDev& c, int kind, double hc, const double* b, const double* x, double* res,
                      SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st);
 
@@ -254,9 +258,10 @@ void launch_forces(const CaseDev& c, const double* U, const double* P, double mu
 void launch_gate_momentum(StepCtl* ctl, int nchk, cudaStream_t st);
 // projection divergence gate on div_max[k]
 void launch_gate_projection(StepCtl* ctl, int k, cudaStream_t st);
-// CFL screen: dt*(umax/dx + vmax/dy) > 0.5 -> error (values from a previous maxabs)
+// CFL screen: dt*(umax/dx + vmax/dy) > 0.5 -> error (values from a previous maxabs);
+// screen = 1/0 runs/skips it, screen = -1 runs it when *counter % 100 == 0
 void launch_cfl_screen(StepCtl* ctl, const unsigned long long* umax, const unsigned long long* vmax, double dt,
-                       double dx, double dy, int screen, cudaStream_t st);
+                       double dx, double dy, int screen, const long long* counter, cudaStream_t st);
 
 void launch_gate_pressure(StepCtl* ctl, int slot, int nchk, cudaStream_t st);
 // dst[k] = src[idx[k]] and dst[idx[k]] = src[k]
@@ -265,6 +270,15 @@ void launch_scatter(const double* src, const int64_t* idx, int64_t n, double* ds
 // column col of (S - I): S[r*rank+col] = sum_e C[r,e] first[e]
 void launch_schur_column(const double* first, const RectView& view, int rank, const int64_t* c_ptr,
                          const int64_t* c_col, const double* c_val, double* S, int col, cudaStream_t st);
+
+// Refinement loop decision for a graph WHILE node: if check sc->k exceeded the inner
+// target and another check is allowed, advance sc->k and set the condition to 1.
+void launch_refine_decide(StepCtl* ctl, int slot, int nchk, cudaGraphConditionalHandle cond, cudaStream_t st);
+// end of a step: if no gate failed, the new state's velocity maxima become the persistent
+// ones; the step's control block is appended to ring[*ridx] and the step counter advances
+void launch_step_end(StepCtl* ctl, unsigned long long* state_max, StepCtl* ring, int* ridx, long long* counter,
+                     int cap, cudaStream_t st);
+bool ktimer_active();
 
 // zero/copy helpers
 void launch_copy_active(const uint8_t* cls, int64_t n, const double* src, double* dst, const Gate& gate,
