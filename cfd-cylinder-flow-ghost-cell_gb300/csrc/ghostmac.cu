@@ -343,17 +343,16 @@ void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
   tt.smem_x = std::max(smem_for(tx_f, cols, tt.lpb_x), smem_for(tx_i, cols, tt.lpb_x));
   int P = tt.ych.P;
   int L = std::max(1, std::min(32, 128 / P));
-  while (L > 1 && ((cols + L - 1) / L < 2 * 152 || (size_t)L * rows * sizeof(double) > h->smem_optin)) L /= 2;
+  while (L > 1 && ((cols + L - 1) / L < 2 * 152 || 2 * (size_t)L * rows * sizeof(double) > h->smem_optin)) L /= 2;
   tt.lpb_y = L;
   tt.threads_y = ((L * P + 31) / 32) * 32;
-  tt.smem_y = (size_t)L * rows * sizeof(double);
+  tt.smem_y = 2 * (size_t)L * rows * sizeof(double);
   if (tt.smem_x > h->smem_optin || tt.smem_y > h->smem_optin || tt.threads_y > 1024)
     throw CudaError("separable inverse does not fit the launch limits");
   if (h->precision == 1) {
     // FP32 tables and launch shapes (same plans, half the shared memory per line)
     TransformTables& t32 = rd.tt32;
     t32 = tt;
-    std::vector<double> w(2 * (size_t)Mx), pre, post;
     rd.Wx32.upload(to_f32(cexp_table(Mx, 2.0, Mx, 0.0, -1)), st);
     if (r2r_family(tx_f) == 2) {
       rd.prex32.upload(to_f32(cexp_table(cols / 2, 4.0, 4.0 * cols, 1.0, -1)), st);
@@ -376,7 +375,7 @@ void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
     };
     t32.lpb_x = std::min(pick32(tx_f, cols, rows), pick32(tx_i, cols, rows));
     t32.smem_x = std::max(smem32(tx_f, cols, t32.lpb_x), smem32(tx_i, cols, t32.lpb_x));
-    t32.smem_y = (size_t)t32.lpb_y * rows * sizeof(float);
+    t32.smem_y = 2 * (size_t)t32.lpb_y * rows * sizeof(float);
   }
   // view
   rd.view.rows = rows;

@@ -60,6 +60,13 @@ __device__ void block_commit_sum(double v, double* dst) {
 __device__ __forceinline__ unsigned long long absbits(double v) { return dbits(fabs(v)); }
 
 static inline unsigned blocks_for(int64_t n, int tpb = TPB) { return (unsigned)((n + tpb - 1) / tpb); }
+// Grid of the reduction kernels: grid-stride loops over at most 4 blocks per SM of a GB300,
+// so each block commits its partial max/sum with one atomic per quantity.
+static inline unsigned reduce_blocks(int64_t n) {
+  unsigned b = blocks_for(n);
+  return b < 608u ? b : 608u;
+}
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) { return a > b ? a : b; }
 
 // Host-side count of kernel launches issued by this library (all launchers call note_launch).
 static std::atomic<long long> g_launches{0};
@@ -168,12 +175,15 @@ __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale,
                          const T* __restrict__ t1, const T* __restrict__ t2, T* __restrict__ S, int lpb, Gate gate) {
   if (!gate_open(gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* col = reinterpret_cast<T*>(smem_raw);  // lpb x n
+  T* col = reinterpret_cast<T*>(smem_raw);  // lpb x n column values
+  T* piv = col + (size_t)lpb * n;            // lpb x n chunk pivots (t0), staged so the
+                                             // sequential sweeps never wait on global loads
   const int c0 = blockIdx.x * lpb;
   const int nl = min(lpb, cols - c0);
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
     int l = t % nl, e = t / nl;
     col[l * n + e] = S[(int64_t)e * cols + c0 + l] * scale;
+    piv[l * n + e] = t0[(int64_t)e * cols + c0 + l];
   }
   __syncthreads();
   const int P = ch.P;
@@ -182,19 +192,18 @@ __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale,
   int a = 0, b = -1;
   if (work) { a = ch.start[p]; b = ch.end[p]; }
   T* x = col + l * n;
+  const T* pv = piv + l * n;
   const int64_t cc = c0 + l;
   // phase 1: chunk-local Thomas -> g
   if (work) {
     T prev = 0;
     for (int j = a; j <= b; ++j) {
-      T inv = t0[(int64_t)j * cols + cc];
-      prev = (x[j] - gamma * prev) * inv;
+      prev = (x[j] - gamma * prev) * pv[j];
       x[j] = prev;
     }
-    T next = 0;
+    T next = x[b];
     for (int j = b - 1; j >= a; --j) {
-      T c = gamma * t0[(int64_t)j * cols + cc];
-      next = x[j] - c * x[j + 1];
+      next = x[j] - (gamma * pv[j]) * next;
       x[j] = next;
     }
   }
@@ -222,6 +231,7 @@ __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale,
   if (work && P > 1) {
     T yl = p > 0 ? x[ch.end[p - 1] + 1] : (T)0;
     T yr = p < P - 1 ? x[b + 1] : (T)0;
+#pragma unroll 4
     for (int j = a; j <= b; ++j) {
       int64_t o = (int64_t)j * cols + cc;
       x[j] = x[j] - yl * t1[o] - yr * t2[o];
@@ -651,10 +661,9 @@ __global__ void k_residual(CaseDev c, int kind, double hc, const double* __restr
   int64_t npts = kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize);
   int64_t base = kind == 2 ? c.usize : 0;  // face-grid offset of the v field
   const uint8_t* cls = kind == 0 ? c.cls_p : (kind == 1 ? c.cls_u : c.cls_v);
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long rm = 0, bm = 0, bd = 0, xb = 0;
   double rs = 0.0, bs = 0.0;
-  if (t < npts) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < npts; t += (int64_t)gridDim.x * blockDim.x) {
     uint8_t k = cls[t];
     int64_t f = base + t;
     if (!(k & CLS_ACTIVE)) {
@@ -707,10 +716,10 @@ __global__ void k_residual(CaseDev c, int kind, double hc, const double* __restr
       }
       double r = bv - ax;
       res[f] = r;
-      rm = absbits(r);
-      rs = r * r;
-      if (kind == 0) bd = dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + fabs(bv)));
-      if (first) { bm = absbits(bv); bs = bv * bv; }
+      rm = umax64(rm, absbits(r));
+      rs += r * r;
+      if (kind == 0) bd = umax64(bd, dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + fabs(bv))));
+      if (first) { bm = umax64(bm, absbits(bv)); bs += bv * bv; }
       if (!isfinite(xv)) xb = 1;
     }
   }
@@ -729,7 +738,7 @@ void launch_residual(const CaseDev& c, int kind, double hc, const double* b, con
   int64_t n = kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize);
   note_launch();
   kt_mark(4, st);
-  k_residual<<<blocks_for(n), TPB, 0, st>>>(c, kind, hc, b, x, res, sc, check, first_check ? 1 : 0, gate);
+  k_residual<<<reduce_blocks(n), TPB, 0, st>>>(c, kind, hc, b, x, res, sc, check, first_check ? 1 : 0, gate);
   kt_mark(4, st);
 }
 
@@ -740,18 +749,17 @@ __global__ void k_divergence(CaseDev c, const double* __restrict__ U, double* __
                              unsigned long long* divmax, int gate_nonfinite, StepCtl* ctl, Gate gate) {
   if (!gate_open(gate)) return;
   const Grid g{c.nx, c.ny, c.usize};
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long dm = 0;
   bool bad = false;
-  if (t < c.psize) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < c.psize; t += (int64_t)gridDim.x * blockDim.x) {
     if (c.cls_p[t] & CLS_ACTIVE) {
       int j = (int)(t / c.nx), i = (int)(t % c.nx);
       double d = (U[g.u(j, i + 1)] - U[g.u(j, i)]) / c.dx + (U[g.v(j + 1, i)] - U[g.v(j, i)]) / c.dy;
-      dm = absbits(d);
+      dm = umax64(dm, absbits(d));
       if (out) {
         double o = dt != 0.0 ? d / dt : d;
         out[t] = o;
-        bad = !isfinite(o);
+        bad = bad || !isfinite(o);
       }
     } else if (out) {
       out[t] = 0.0;
@@ -764,7 +772,7 @@ void launch_divergence(const CaseDev& c, const double* U, double* out, double sc
                        unsigned long long* divmax, int gate_on_nonfinite, const Gate& gate, cudaStream_t st) {
   (void)sc;
   note_launch();
-  k_divergence<<<blocks_for(c.psize), TPB, 0, st>>>(c, U, out, scale, divmax, gate_on_nonfinite, gate.ctl, gate);
+  k_divergence<<<reduce_blocks(c.psize), TPB, 0, st>>>(c, U, out, scale, divmax, gate_on_nonfinite, gate.ctl, gate);
 }
 
 __global__ void k_project_update(CaseDev c, const double* __restrict__ q, const double* __restrict__ phi, double dt,
@@ -820,9 +828,10 @@ __global__ void k_pressure_out(CaseDev c, const double* __restrict__ p, const do
                                Gate gate) {
   if (!gate_open(gate)) return;
   const Grid g{c.nx, c.ny, c.usize};
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t nf = c.usize + c.vsize;
   unsigned long long cm = 0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nf + c.psize;
+       t += (int64_t)gridDim.x * blockDim.x) {
   if (t < nf) {
     int comp, j, i;
     face_of(t, g, comp, j, i);
@@ -830,9 +839,9 @@ __global__ void k_pressure_out(CaseDev c, const double* __restrict__ p, const do
     if (cls & CLS_ACTIVE) {
       double gi = comp == 0 ? grad_u<double>(inc, g, j, i, (1.0 / c.dx) / c.rho) : grad_v<double>(inc, g, j, i, (1.0 / c.dy) / c.rho);
       double r = action[t] - rhs[t] + dt * gi;
-      cm = absbits(r);
+      cm = umax64(cm, absbits(r));
     }
-  } else if (t < nf + c.psize) {
+  } else {
     int64_t k = t - nf;
     if (c.cls_p[k] & CLS_ACTIVE) {
       double h = p[k] + inc[k];
@@ -843,30 +852,33 @@ __global__ void k_pressure_out(CaseDev c, const double* __restrict__ p, const do
       pout[k] = 0.0;
     }
   }
+  }
   block_commit_max(cm, coupled);
 }
 void launch_pressure_out(const CaseDev& c, const double* p, const double* inc, double factor, double dt,
                          const double* action, const double* rhs, double* half, double* pout,
                          unsigned long long* coupled, const Gate& gate, cudaStream_t st) {
   note_launch();
-  k_pressure_out<<<blocks_for(c.usize + c.vsize + c.psize), TPB, 0, st>>>(c, p, inc, factor, dt, action, rhs, half,
+  k_pressure_out<<<reduce_blocks(c.usize + c.vsize + c.psize), TPB, 0, st>>>(c, p, inc, factor, dt, action, rhs, half,
                                                                           pout, coupled, gate);
 }
 
 __global__ void k_maxabs(CaseDev c, const double* __restrict__ U, unsigned long long* umax, unsigned long long* vmax,
                          Gate gate) {
   if (!gate_open(gate)) return;
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long a = 0, b = 0;
-  if (t < c.usize) a = absbits(U[t]);
-  else if (t < c.usize + c.vsize) b = absbits(U[t]);
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < c.usize + c.vsize;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    if (t < c.usize) a = umax64(a, absbits(U[t]));
+    else b = umax64(b, absbits(U[t]));
+  }
   block_commit_max(a, umax);
   block_commit_max(b, vmax);
 }
 void launch_maxabs(const CaseDev& c, const double* U, unsigned long long* umax, unsigned long long* vmax,
                    const Gate& gate, cudaStream_t st) {
   note_launch();
-  k_maxabs<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, U, umax, vmax, gate);
+  k_maxabs<<<reduce_blocks(c.usize + c.vsize), TPB, 0, st>>>(c, U, umax, vmax, gate);
 }
 
 // ---------------------------------------------------------------------------
