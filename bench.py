@@ -232,6 +232,33 @@ def run_ours(args, w, rank, world):
     tot, cnt = C.c_double(), C.c_int64()
     L.lib.gm_kernel_timing(dominant, 0, C.byref(tot), C.byref(cnt))
     L.lib.gm_kernel_timing(0, 0, None, None)
+    # the headline metric compares this mode with the plain FP64 step on the same GPU:
+    # time the plain FP64 case with the same protocol (graph mode, L2 flushed between steps)
+    compare = None
+    if args.precision == 'fp32' and not args.no_compare:
+        s64 = pkg.MAC_CylinderFlow(verbose=False, precision='fp64', **kw)
+        seeded_state(s64, w)
+        L.check(L.lib.gm_set_stream(s64._h, C.c_void_p(stream.cuda_stream)), s64._h)
+        s64._push()
+        for k in range(max(args.warmup, 3)):
+            rc, dg = s64.step_raw(dt, 1, first_index=k)
+            L.check(rc, s64._h)
+        t64 = []
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            rc, dg = s64.step_raw(dt, 1, first_index=k + 1)
+            L.check(rc, s64._h)
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            t64.append(e0.elapsed_time(e1))
+        ms64 = sum(t64) / len(t64)
+        compare = dict(plain_fp64_value=cells / (ms64 * 1e-3), plain_fp64_ms_per_step=ms64,
+                       speedup_vs_plain_fp64=ms64 / step_ms)
+        del s64
     # roofline of the dominant kernel: algorithmic bytes per launch / mean launch time
     nx, ny = w['nx'], w['ny']
     F = ny * (nx + 1) + (ny + 1) * nx
@@ -275,7 +302,8 @@ def run_ours(args, w, rank, world):
                     clocks=clocks.summary(), gpu_launches=int(launches), launches_before_timed=int(launches0),
                     refinement_sweeps_per_step=dict(pressure=float(np.mean([a for a, _ in sweeps])),
                                                     momentum=float(np.mean([b for _, b in sweeps]))),
-                    kernel_class_ms_per_step={KERNEL_CLASSES[c]: v[0] for c, v in per_class.items()})
+                    kernel_class_ms_per_step={KERNEL_CLASSES[c]: v[0] for c, v in per_class.items()},
+                    comparison=compare)
         print(json.dumps(line), flush=True)
 
 
@@ -287,6 +315,7 @@ def main():
     ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
     ap.add_argument('--workload', choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
+    ap.add_argument('--no-compare', action='store_true', help='skip timing the plain FP64 step beside the FP32 mode')
     ap.add_argument('--precision', choices=('fp64', 'fp32'), default='fp64',
                     help='fp64: plain FP64 method; fp32: FP32 inverses and stencils with FP64 refinement')
     args = ap.parse_args()

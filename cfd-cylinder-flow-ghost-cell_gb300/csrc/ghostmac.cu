@@ -329,24 +329,27 @@ void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
     rd.t1_32.upload(to_f32(t1), st);
     rd.t2_32.upload(to_f32(t2), st);
   }
-  // launch shapes
-  auto smem_for = [](int type, int n, int lpb) {
-    size_t stage = ((size_t)lpb * n * sizeof(double) + 15) / 16 * 16;
-    return stage + 2 * (size_t)r2r_buffer_elems(type, n, lpb) * sizeof(cplx<double>);
+  // launch shapes: x passes one warp per line group, up to 4 warps per block; the y solve
+  // takes 16 consecutive columns per block (32 in FP32), i.e. full 128-byte row segments
+  auto warp_smem = [](int type, int n, size_t esz) {
+    const int lpw = r2r_paired(type) ? 2 : 1;
+    size_t stage = ((size_t)lpw * n * esz + 15) / 16 * 16;
+    return stage + 2 * (size_t)r2r_buffer_elems(type, n, lpw) * 2 * esz;
   };
-  auto pick = [&](int type, int n, int lines) {
-    int lpb = 8;
-    while (lpb > 1 && ((lines + lpb - 1) / lpb < 2 * 152 || smem_for(type, n, lpb) > h->smem_optin)) lpb /= 2;
-    return lpb;
+  auto shapes = [&](TransformTables& t, size_t esz) {
+    size_t per = std::max(warp_smem(tx_f, cols, esz), warp_smem(tx_i, cols, esz));
+    int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, h->smem_optin / per));
+    t.lpb_x = wpb;
+    t.smem_x = per * wpb;
+    int P = t.ych.P;
+    int L = esz == 4 ? 32 : 16;
+    L = std::min(L, cols);
+    while (L > 1 && (L * P > 1024 || (size_t)L * rows * esz > h->smem_optin)) L /= 2;
+    t.lpb_y = L;
+    t.threads_y = ((L * P + 31) / 32) * 32;
+    t.smem_y = (size_t)L * rows * esz;
   };
-  tt.lpb_x = std::min(pick(tx_f, cols, rows), pick(tx_i, cols, rows));
-  tt.smem_x = std::max(smem_for(tx_f, cols, tt.lpb_x), smem_for(tx_i, cols, tt.lpb_x));
-  int P = tt.ych.P;
-  int L = std::max(1, std::min(32, 128 / P));
-  while (L > 1 && ((cols + L - 1) / L < 2 * 152 || 2 * (size_t)L * rows * sizeof(double) > h->smem_optin)) L /= 2;
-  tt.lpb_y = L;
-  tt.threads_y = ((L * P + 31) / 32) * 32;
-  tt.smem_y = 2 * (size_t)L * rows * sizeof(double);
+  shapes(tt, sizeof(double));
   if (tt.smem_x > h->smem_optin || tt.smem_y > h->smem_optin || tt.threads_y > 1024)
     throw CudaError("separable inverse does not fit the launch limits");
   if (h->precision == 1) {
@@ -364,18 +367,7 @@ void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
     t32.Wx = rd.Wx32.p; t32.prex = rd.prex32.p; t32.postx = rd.postx32.p;
     t32.prex_inv = rd.prex32.p; t32.postx_inv = rd.postx32.p;
     t32.t0 = rd.t0_32.p; t32.t1 = rd.t1_32.p; t32.t2 = rd.t2_32.p;
-    auto smem32 = [](int type, int n, int lpb) {
-      size_t stage = ((size_t)lpb * n * sizeof(float) + 15) / 16 * 16;
-      return stage + 2 * (size_t)r2r_buffer_elems(type, n, lpb) * sizeof(cplx<float>);
-    };
-    auto pick32 = [&](int type, int n, int lines) {
-      int lpb = 8;
-      while (lpb > 1 && ((lines + lpb - 1) / lpb < 2 * 152 || smem32(type, n, lpb) > h->smem_optin)) lpb /= 2;
-      return lpb;
-    };
-    t32.lpb_x = std::min(pick32(tx_f, cols, rows), pick32(tx_i, cols, rows));
-    t32.smem_x = std::max(smem32(tx_f, cols, t32.lpb_x), smem32(tx_i, cols, t32.lpb_x));
-    t32.smem_y = 2 * (size_t)t32.lpb_y * rows * sizeof(float);
+    shapes(t32, sizeof(float));
   }
   // view
   rd.view.rows = rows;

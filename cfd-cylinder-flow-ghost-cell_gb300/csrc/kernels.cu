@@ -123,38 +123,57 @@ void ktimer_read(double* total_ms, long long* count) {
 // ---------------------------------------------------------------------------
 // separable inverse: x pass (rows) and y pass (columns with eigenvalue scaling)
 // ---------------------------------------------------------------------------
+// Row transforms: one warp per line group (one line for the type-IV transforms, two
+// paired lines for the Makhoul transforms); each warp owns its shared-memory slice and
+// synchronises with __syncwarp only.  Masked load, optional fused epilogue
+//   out = active ? add + (sub - T b) : 0.
+template <typename T>
+__host__ __device__ inline size_t xpass_warp_smem(int type, int n) {
+  const int lpw = r2r_paired(type) ? 2 : 1;
+  size_t stage = ((size_t)lpw * n * sizeof(T) + 15) / 16 * 16;
+  return stage + 2 * (size_t)r2r_buffer_elems(type, n, lpw) * sizeof(cplx<T>);
+}
+
 template <typename T, typename TI, typename TO, typename TS>
 __global__ void k_xpass(int n, int rows, int type, FftPlan plan, R2RTables<T> tb, const TI* __restrict__ in,
                         int64_t ibase, int64_t ipitch, const uint8_t* __restrict__ icls, TO* __restrict__ out,
                         int64_t obase, int64_t opitch, const uint8_t* __restrict__ ocls, const TS* __restrict__ sub,
-                        const double* __restrict__ add, int lpb, Gate gate) {
+                        const double* __restrict__ add, int wpb, Gate gate) {
   if (!gate_open(gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int l0 = blockIdx.x * lpb;
-  const int nl = min(lpb, rows - l0);
-  T* stage = reinterpret_cast<T*>(smem_raw);
-  size_t stage_bytes = ((size_t)lpb * n * sizeof(T) + 15) / 16 * 16;
-  cplx<T>* a = reinterpret_cast<cplx<T>*>(smem_raw + stage_bytes);
-  cplx<T>* b = a + r2r_buffer_elems(type, n, lpb);
-  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
-    int l = t / n, e = t - l * n;
-    int64_t fi = ibase + (int64_t)(l0 + l) * ipitch + e;
-    TI v = in[fi];
-    if (icls && !(icls[fi] & CLS_ACTIVE)) v = (TI)0;
-    stage[t] = (T)v;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lpw = r2r_paired(type) ? 2 : 1;
+  const int l0 = (blockIdx.x * wpb + warp) * lpw;
+  if (warp >= wpb || l0 >= rows) return;  // whole warps leave; no block barrier follows
+  const int nl = min(lpw, rows - l0);
+  unsigned char* mine = smem_raw + (size_t)warp * xpass_warp_smem<T>(type, n);
+  T* stage = reinterpret_cast<T*>(mine);
+  size_t stage_bytes = ((size_t)lpw * n * sizeof(T) + 15) / 16 * 16;
+  cplx<T>* a = reinterpret_cast<cplx<T>*>(mine + stage_bytes);
+  cplx<T>* b = a + r2r_buffer_elems(type, n, lpw);
+  const Grp G{lane, 32, true};
+  for (int l = 0; l < nl; ++l) {
+    const int64_t row = ibase + (int64_t)(l0 + l) * ipitch;
+    for (int e = lane; e < n; e += 32) {
+      TI v = in[row + e];
+      if (icls && !(icls[row + e] & CLS_ACTIVE)) v = (TI)0;
+      stage[l * n + e] = (T)v;
+    }
   }
-  __syncthreads();
-  r2r_lines<T>(type, stage, n, nl, a, b, plan, tb);
-  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
-    int l = t / n, e = t - l * n;
-    int64_t fo = obase + (int64_t)(l0 + l) * opitch + e;
-    T v = stage[t];
-    if (sub) {
-      if (ocls && !(ocls[fo] & CLS_ACTIVE)) { out[fo] = (TO)0; continue; }
-      double d = (double)((T)sub[fo] - v);
-      out[fo] = (TO)(add ? add[fo] + d : d);
-    } else {
-      out[fo] = (TO)v;
+  __syncwarp();
+  r2r_lines<T>(type, stage, n, nl, a, b, plan, tb, G);
+  for (int l = 0; l < nl; ++l) {
+    const int64_t row = obase + (int64_t)(l0 + l) * opitch;
+    for (int e = lane; e < n; e += 32) {
+      const int64_t fo = row + e;
+      T v = stage[l * n + e];
+      if (sub) {
+        if (ocls && !(ocls[fo] & CLS_ACTIVE)) { out[fo] = (TO)0; continue; }
+        double d = (double)((T)sub[fo] - v);
+        out[fo] = (TO)(add ? add[fo] + d : d);
+      } else {
+        out[fo] = (TO)v;
+      }
     }
   }
 }
@@ -176,14 +195,11 @@ __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale,
   if (!gate_open(gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* col = reinterpret_cast<T*>(smem_raw);  // lpb x n column values
-  T* piv = col + (size_t)lpb * n;            // lpb x n chunk pivots (t0), staged so the
-                                             // sequential sweeps never wait on global loads
   const int c0 = blockIdx.x * lpb;
   const int nl = min(lpb, cols - c0);
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
     int l = t % nl, e = t / nl;
     col[l * n + e] = S[(int64_t)e * cols + c0 + l] * scale;
-    piv[l * n + e] = t0[(int64_t)e * cols + c0 + l];
   }
   __syncthreads();
   const int P = ch.P;
@@ -192,18 +208,21 @@ __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale,
   int a = 0, b = -1;
   if (work) { a = ch.start[p]; b = ch.end[p]; }
   T* x = col + l * n;
-  const T* pv = piv + l * n;
   const int64_t cc = c0 + l;
-  // phase 1: chunk-local Thomas -> g
+  // phase 1: chunk-local Thomas -> g.  Consecutive threads take consecutive columns, so
+  // every pivot load of a warp is one contiguous row segment; unrolling lets the loads run
+  // ahead of the recurrence.
   if (work) {
     T prev = 0;
+#pragma unroll 8
     for (int j = a; j <= b; ++j) {
-      prev = (x[j] - gamma * prev) * pv[j];
+      prev = (x[j] - gamma * prev) * t0[(int64_t)j * cols + cc];
       x[j] = prev;
     }
     T next = x[b];
+#pragma unroll 8
     for (int j = b - 1; j >= a; --j) {
-      next = x[j] - (gamma * pv[j]) * next;
+      next = x[j] - (gamma * t0[(int64_t)j * cols + cc]) * next;
       x[j] = next;
     }
   }
@@ -271,10 +290,12 @@ void launch_rect_inverse(const TransformTables& tt, const RectView& v, const dou
   using C = cplx<double>;
   R2RTables<double> tx{(const C*)tt.Wx, (const C*)tt.prex, (const C*)tt.postx};
   R2RTables<double> txi{(const C*)tt.Wx, (const C*)tt.prex_inv, (const C*)tt.postx_inv};
-  unsigned gx = (unsigned)((v.rows + tt.lpb_x - 1) / tt.lpb_x);
+  const int lpw_f = r2r_paired(tt.tx_fwd) ? 2 : 1, lpw_i = r2r_paired(tt.tx_inv) ? 2 : 1;
+  unsigned gx = (unsigned)((v.rows + tt.lpb_x * lpw_f - 1) / (tt.lpb_x * lpw_f));
+  unsigned gxi = (unsigned)((v.rows + tt.lpb_x * lpw_i - 1) / (tt.lpb_x * lpw_i));
   note_launch();
   kt_mark(1, st);
-  k_xpass<double, double, double, double><<<gx, 128, tt.smem_x, st>>>(
+  k_xpass<double, double, double, double><<<gx, 32 * tt.lpb_x, tt.smem_x, st>>>(
       v.cols, v.rows, tt.tx_fwd, tt.plan_x, tx, b, v.base, v.pitch, mask_in ? v.cls : nullptr, spectral, 0, v.cols,
       nullptr, (const double*)nullptr, nullptr, tt.lpb_x, gate);
   kt_mark(1, st);
@@ -287,7 +308,7 @@ void launch_rect_inverse(const TransformTables& tt, const RectView& v, const dou
   kt_mark(2, st);
   note_launch();
   kt_mark(1, st);
-  k_xpass<double, double, double, double><<<gx, 128, tt.smem_x, st>>>(
+  k_xpass<double, double, double, double><<<gxi, 32 * tt.lpb_x, tt.smem_x, st>>>(
       v.cols, v.rows, tt.tx_inv, tt.plan_x, txi, spectral, 0, v.cols, nullptr, out, v.base, v.pitch, v.cls, sub, add,
       tt.lpb_x, gate);
   kt_mark(1, st);
@@ -298,10 +319,12 @@ void launch_rect_inverse_f32(const TransformTables& tt, const RectView& v, const
   using C = cplx<float>;
   R2RTables<float> tx{(const C*)tt.Wx, (const C*)tt.prex, (const C*)tt.postx};
   R2RTables<float> txi{(const C*)tt.Wx, (const C*)tt.prex_inv, (const C*)tt.postx_inv};
-  unsigned gx = (unsigned)((v.rows + tt.lpb_x - 1) / tt.lpb_x);
+  const int lpw_f = r2r_paired(tt.tx_fwd) ? 2 : 1, lpw_i = r2r_paired(tt.tx_inv) ? 2 : 1;
+  unsigned gx = (unsigned)((v.rows + tt.lpb_x * lpw_f - 1) / (tt.lpb_x * lpw_f));
+  unsigned gxi = (unsigned)((v.rows + tt.lpb_x * lpw_i - 1) / (tt.lpb_x * lpw_i));
   note_launch();
   kt_mark(1, st);
-  k_xpass<float, double, float, float><<<gx, 128, tt.smem_x, st>>>(
+  k_xpass<float, double, float, float><<<gx, 32 * tt.lpb_x, tt.smem_x, st>>>(
       v.cols, v.rows, tt.tx_fwd, tt.plan_x, tx, b, v.base, v.pitch, mask_in ? v.cls : nullptr, spectral, 0, v.cols,
       nullptr, (const float*)nullptr, nullptr, tt.lpb_x, gate);
   kt_mark(1, st);
@@ -314,7 +337,7 @@ void launch_rect_inverse_f32(const TransformTables& tt, const RectView& v, const
   kt_mark(2, st);
   note_launch();
   kt_mark(1, st);
-  k_xpass<float, float, float, float><<<gx, 128, tt.smem_x, st>>>(
+  k_xpass<float, float, float, float><<<gxi, 32 * tt.lpb_x, tt.smem_x, st>>>(
       v.cols, v.rows, tt.tx_inv, tt.plan_x, txi, spectral, 0, v.cols, nullptr, first, v.base, v.pitch, nullptr,
       (const float*)nullptr, nullptr, tt.lpb_x, gate);
   kt_mark(1, st);
@@ -326,10 +349,12 @@ void launch_rect_inverse_f32_final(const TransformTables& tt, const RectView& v,
   using C = cplx<float>;
   R2RTables<float> tx{(const C*)tt.Wx, (const C*)tt.prex, (const C*)tt.postx};
   R2RTables<float> txi{(const C*)tt.Wx, (const C*)tt.prex_inv, (const C*)tt.postx_inv};
-  unsigned gx = (unsigned)((v.rows + tt.lpb_x - 1) / tt.lpb_x);
+  const int lpw_f = r2r_paired(tt.tx_fwd) ? 2 : 1, lpw_i = r2r_paired(tt.tx_inv) ? 2 : 1;
+  unsigned gx = (unsigned)((v.rows + tt.lpb_x * lpw_f - 1) / (tt.lpb_x * lpw_f));
+  unsigned gxi = (unsigned)((v.rows + tt.lpb_x * lpw_i - 1) / (tt.lpb_x * lpw_i));
   note_launch();
   kt_mark(1, st);
-  k_xpass<float, double, float, float><<<gx, 128, tt.smem_x, st>>>(
+  k_xpass<float, double, float, float><<<gx, 32 * tt.lpb_x, tt.smem_x, st>>>(
       v.cols, v.rows, tt.tx_fwd, tt.plan_x, tx, w2, v.base, v.pitch, nullptr, spectral, 0, v.cols, nullptr,
       (const float*)nullptr, nullptr, tt.lpb_x, gate);
   kt_mark(1, st);
@@ -342,7 +367,7 @@ void launch_rect_inverse_f32_final(const TransformTables& tt, const RectView& v,
   kt_mark(2, st);
   note_launch();
   kt_mark(1, st);
-  k_xpass<float, float, double, float><<<gx, 128, tt.smem_x, st>>>(
+  k_xpass<float, float, double, float><<<gxi, 32 * tt.lpb_x, tt.smem_x, st>>>(
       v.cols, v.rows, tt.tx_inv, tt.plan_x, txi, spectral, 0, v.cols, nullptr, out, v.base, v.pitch, v.cls, sub, add,
       tt.lpb_x, gate);
   kt_mark(1, st);

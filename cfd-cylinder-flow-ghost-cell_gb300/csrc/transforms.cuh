@@ -35,6 +35,17 @@ __host__ __device__ inline bool r2r_paired(int t) { return r2r_family(t) != 2; }
 
 template <typename T> struct cplx { T x, y; };
 
+// The threads that cooperate on a set of lines: a whole block (barrier __syncthreads)
+// or one warp (barrier __syncwarp).  tid/n index the group's threads.
+struct Grp {
+  int tid, n;
+  bool warp;
+  __device__ __forceinline__ void sync() const {
+    if (warp) __syncwarp();
+    else __syncthreads();
+  }
+};
+
 template <typename T>
 __device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T> b) {
   return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
@@ -124,10 +135,10 @@ __device__ __forceinline__ void dft_small(cplx<T>* v, int dir) {
 // One Stockham stage for radix R (compile-time) over nfft transforms of length M.
 template <typename T, int R>
 __device__ __forceinline__ void stage_fixed(const cplx<T>* __restrict__ in, cplx<T>* __restrict__ out, int M,
-                                            int nfft, int Ns, const cplx<T>* __restrict__ W, int dir) {
+                                            int nfft, int Ns, const cplx<T>* __restrict__ W, int dir, const Grp& G) {
   const int MR = M / R;
   const int tws = M / (Ns * R);
-  for (int t = threadIdx.x; t < nfft * MR; t += blockDim.x) {
+  for (int t = G.tid; t < nfft * MR; t += G.n) {
     int f = t / MR, j = t - f * MR;
     const cplx<T>* src = in + (size_t)f * M;
     cplx<T>* dst = out + (size_t)f * M;
@@ -153,10 +164,10 @@ __device__ __forceinline__ void stage_fixed(const cplx<T>* __restrict__ in, cplx
 // Generic odd radix (any R up to 64): direct R-point DFT per output.
 template <typename T>
 __device__ void stage_generic(const cplx<T>* __restrict__ in, cplx<T>* __restrict__ out, int M, int nfft, int Ns,
-                              int R, const cplx<T>* __restrict__ W, int dir) {
+                              int R, const cplx<T>* __restrict__ W, int dir, const Grp& G) {
   const int MR = M / R;
   const int tws = M / (Ns * R);
-  for (int t = threadIdx.x; t < nfft * MR * R; t += blockDim.x) {
+  for (int t = G.tid; t < nfft * MR * R; t += G.n) {
     int q = t % R;
     int u = t / R;
     int f = u / MR, j = u - f * MR;
@@ -182,19 +193,20 @@ __device__ void stage_generic(const cplx<T>* __restrict__ in, cplx<T>* __restric
 // Runs the FFT on nfft transforms held in a (length M each); the result is in
 // the returned buffer (a or b).  dir = -1 forward, +1 inverse (unnormalised).
 template <typename T>
-__device__ cplx<T>* fft_run(cplx<T>* a, cplx<T>* b, const FftPlan& plan, int nfft, const cplx<T>* W, int dir) {
+__device__ cplx<T>* fft_run(cplx<T>* a, cplx<T>* b, const FftPlan& plan, int nfft, const cplx<T>* W, int dir,
+                           const Grp& G) {
   int Ns = 1;
   for (int s = 0; s < plan.nstages; ++s) {
     int R = plan.radix[s];
     switch (R) {
-      case 2: stage_fixed<T, 2>(a, b, plan.M, nfft, Ns, W, dir); break;
-      case 3: stage_fixed<T, 3>(a, b, plan.M, nfft, Ns, W, dir); break;
-      case 4: stage_fixed<T, 4>(a, b, plan.M, nfft, Ns, W, dir); break;
-      case 5: stage_fixed<T, 5>(a, b, plan.M, nfft, Ns, W, dir); break;
-      case 8: stage_fixed<T, 8>(a, b, plan.M, nfft, Ns, W, dir); break;
-      default: stage_generic<T>(a, b, plan.M, nfft, Ns, R, W, dir); break;
+      case 2: stage_fixed<T, 2>(a, b, plan.M, nfft, Ns, W, dir, G); break;
+      case 3: stage_fixed<T, 3>(a, b, plan.M, nfft, Ns, W, dir, G); break;
+      case 4: stage_fixed<T, 4>(a, b, plan.M, nfft, Ns, W, dir, G); break;
+      case 5: stage_fixed<T, 5>(a, b, plan.M, nfft, Ns, W, dir, G); break;
+      case 8: stage_fixed<T, 8>(a, b, plan.M, nfft, Ns, W, dir, G); break;
+      default: stage_generic<T>(a, b, plan.M, nfft, Ns, R, W, dir, G); break;
     }
-    __syncthreads();
+    G.sync();
     cplx<T>* t = a;
     a = b;
     b = t;
@@ -216,12 +228,12 @@ struct R2RTables {
 // -> complex FFT inputs in buf.  Line l of the transform reads stage[l*n + ...].
 // ---------------------------------------------------------------------------
 template <typename T>
-__device__ void r2r_pre(int type, const T* stage, int n, int nl, cplx<T>* buf, const R2RTables<T>& tb) {
+__device__ void r2r_pre(int type, const T* stage, int n, int nl, cplx<T>* buf, const R2RTables<T>& tb, const Grp& G) {
   const int fam = r2r_family(type);
   if (fam == 2) {
     const int M = n / 2;
     const bool rev = type == DST4;
-    for (int t = threadIdx.x; t < nl * M; t += blockDim.x) {
+    for (int t = G.tid; t < nl * M; t += G.n) {
       int l = t / M, m = t - l * M;
       const T* x = stage + (size_t)l * n;
       int i0 = 2 * m, i1 = n - 1 - 2 * m;
@@ -234,7 +246,7 @@ __device__ void r2r_pre(int type, const T* stage, int n, int nl, cplx<T>* buf, c
     // Makhoul: v[m] = x[2m] (m < ceil(n/2)), v[n-1-m'] = x[2m'+1]
     const int npair = (nl + 1) / 2;
     const bool alt = type == DST2;  // DST-II: x'[m] = (-1)^m x[m]
-    for (int t = threadIdx.x; t < npair * n; t += blockDim.x) {
+    for (int t = G.tid; t < npair * n; t += G.n) {
       int pidx = t / n, m = t - pidx * n;
       int src = m < (n + 1) / 2 ? 2 * m : 2 * (n - 1 - m) + 1;
       T sgn = (alt && (src & 1)) ? (T)-1 : (T)1;
@@ -247,7 +259,7 @@ __device__ void r2r_pre(int type, const T* stage, int n, int nl, cplx<T>* buf, c
     // V[k] = e^{i pi k/(2n)} (X_k - i X_{n-k}), X_n = 0; two lines as V_A + i V_B
     const int npair = (nl + 1) / 2;
     const bool rev = type == DST3;  // DST-III: X'[k] = X[n-1-k]
-    for (int t = threadIdx.x; t < npair * n; t += blockDim.x) {
+    for (int t = G.tid; t < npair * n; t += G.n) {
       int pidx = t / n, k = t - pidx * n;
       int la = 2 * pidx, lb = 2 * pidx + 1;
       int ik = rev ? n - 1 - k : k;
@@ -265,7 +277,7 @@ __device__ void r2r_pre(int type, const T* stage, int n, int nl, cplx<T>* buf, c
     // DST-I: odd extension of length 2(n+1)
     const int N = n + 1, M = 2 * N;
     const int npair = (nl + 1) / 2;
-    for (int t = threadIdx.x; t < npair * M; t += blockDim.x) {
+    for (int t = G.tid; t < npair * M; t += G.n) {
       int pidx = t / M, m = t - pidx * M;
       int la = 2 * pidx, lb = 2 * pidx + 1;
       cplx<T> z = {0, 0};
@@ -284,12 +296,12 @@ __device__ void r2r_pre(int type, const T* stage, int n, int nl, cplx<T>* buf, c
 
 // post-processing: FFT outputs in buf -> real lines in stage
 template <typename T>
-__device__ void r2r_post(int type, const cplx<T>* buf, int n, int nl, T* stage, const R2RTables<T>& tb) {
+__device__ void r2r_post(int type, const cplx<T>* buf, int n, int nl, T* stage, const R2RTables<T>& tb, const Grp& G) {
   const int fam = r2r_family(type);
   if (fam == 2) {
     const int M = n / 2;
     const bool alt = type == DST4;  // y[k] *= (-1)^k
-    for (int t = threadIdx.x; t < nl * M; t += blockDim.x) {
+    for (int t = G.tid; t < nl * M; t += G.n) {
       int l = t / M, k = t - l * M;
       cplx<T> z = cmul(buf[(size_t)l * M + k], tb.post[k]);
       T* y = stage + (size_t)l * n;
@@ -305,7 +317,7 @@ __device__ void r2r_post(int type, const cplx<T>* buf, int n, int nl, T* stage, 
   } else if (fam == 0) {
     const int npair = (nl + 1) / 2;
     const bool rev = type == DST2;  // DST-II: y[k] = Y'[n-1-k]
-    for (int t = threadIdx.x; t < npair * n; t += blockDim.x) {
+    for (int t = G.tid; t < npair * n; t += G.n) {
       int pidx = t / n, k = t - pidx * n;
       cplx<T> Zk = buf[(size_t)pidx * n + k];
       cplx<T> Zc = buf[(size_t)pidx * n + (k == 0 ? 0 : n - k)];
@@ -323,7 +335,7 @@ __device__ void r2r_post(int type, const cplx<T>* buf, int n, int nl, T* stage, 
   } else if (fam == 1) {
     const int npair = (nl + 1) / 2;
     const bool alt = type == DST3;  // DST-III: y[m] *= (-1)^m
-    for (int t = threadIdx.x; t < npair * n; t += blockDim.x) {
+    for (int t = G.tid; t < npair * n; t += G.n) {
       int pidx = t / n, o = t - pidx * n;
       int src = (o & 1) ? n - 1 - (o - 1) / 2 : o / 2;
       cplx<T> z = buf[(size_t)pidx * n + src];
@@ -335,7 +347,7 @@ __device__ void r2r_post(int type, const cplx<T>* buf, int n, int nl, T* stage, 
   } else {
     const int N = n + 1, M = 2 * N;
     const int npair = (nl + 1) / 2;
-    for (int t = threadIdx.x; t < npair * n; t += blockDim.x) {
+    for (int t = G.tid; t < npair * n; t += G.n) {
       int pidx = t / n, k = t - pidx * n;
       cplx<T> z = buf[(size_t)pidx * M + k + 1];
       int la = 2 * pidx, lb = 2 * pidx + 1;
@@ -356,13 +368,13 @@ __host__ __device__ inline int r2r_nfft(int type, int nl) { return r2r_paired(ty
 // Full r2r transform of nl lines held in stage (in place, through buffers a/b).
 template <typename T>
 __device__ void r2r_lines(int type, T* stage, int n, int nl, cplx<T>* a, cplx<T>* b, const FftPlan& plan,
-                          const R2RTables<T>& tb) {
+                          const R2RTables<T>& tb, const Grp& G) {
   const int fam = r2r_family(type);
-  r2r_pre<T>(type, stage, n, nl, a, tb);
-  __syncthreads();
-  cplx<T>* res = fft_run<T>(a, b, plan, r2r_nfft(type, nl), tb.W, fam == 1 ? +1 : -1);
-  r2r_post<T>(type, res, n, nl, stage, tb);
-  __syncthreads();
+  r2r_pre<T>(type, stage, n, nl, a, tb, G);
+  G.sync();
+  cplx<T>* res = fft_run<T>(a, b, plan, r2r_nfft(type, nl), tb.W, fam == 1 ? +1 : -1, G);
+  r2r_post<T>(type, res, n, nl, stage, tb, G);
+  G.sync();
 }
 
 }  // namespace gmk
