@@ -43,6 +43,12 @@ WORKLOADS = {
     'channel_400x200_re40': dict(nx=400, ny=200, Lx=20.0, Ly=10.0, D=1.0, xc=5.0, yc=5.0, nu=1 / 40, dt=0.002,
                                  noise='uv', amp=1e-3, seed=0),
 }
+# 64 seeded cases in one CUDA graph per step: Re ~ U[40,200], D ~ U[0.8,1.2], grid drawn from
+# {256x128, 400x200, 800x410} at h=0.05, centre (Lx/4, Ly/2) jittered by U[-0.5D,0.5D] per axis
+BATCH_WORKLOADS = {
+    'sweep64_batch': dict(batch=64, seed=0, dt=0.002, h=0.05, grids=((256, 128), (400, 200), (800, 410)),
+                          re=(40.0, 200.0), diameter=(0.8, 1.2), jitter=0.5, amp=1e-3),
+}
 DEFAULT_WORKLOAD = 'wide_800x820_re100'
 KERNEL_CLASSES = {1: 'transform x pass (k_xpass)', 2: 'transform y pass (k_ypass)', 3: 'momentum rhs (k_momentum)',
                   4: 'operator residual (k_residual)'}
@@ -116,6 +122,32 @@ def seeded_state(s, w):
         q[nu:] += w['amp'] * rng.standard_normal(q.size - nu)
     u, v = s.gg.unpack(q)
     s.u[:], s.v[:] = u, v
+
+
+def sweep_cases(pkg, w, precision):
+    """The seeded cases of a batch workload; draws that violate the geometry checks of
+    MAC_CylinderFlow (cylinder inside the domain, probes inside the grid) are redrawn."""
+    rng = np.random.default_rng(w['seed'])
+    cases, params = [], []
+    while len(cases) < w['batch']:
+        nx, ny = w['grids'][int(rng.integers(len(w['grids'])))]
+        re = rng.uniform(*w['re'])
+        d = rng.uniform(*w['diameter'])
+        lx, ly = nx * w['h'], ny * w['h']
+        xc = lx / 4 + rng.uniform(-w['jitter'], w['jitter']) * d
+        yc = ly / 2 + rng.uniform(-w['jitter'], w['jitter']) * d
+        kw = dict(nx=nx, ny=ny, Lx=lx, Ly=ly, D=d, xc=xc, yc=yc, nu=1.0 * d / re)
+        try:
+            s = pkg.MAC_CylinderFlow(verbose=False, precision=precision, **kw)
+        except ValueError:
+            continue
+        q = s.gg.pack(s.u, s.v)
+        q += w['amp'] * np.random.default_rng(int(rng.integers(2 ** 31))).standard_normal(q.size)
+        u, v = s.gg.unpack(q)
+        s.u[:], s.v[:] = u, v
+        cases.append(s)
+        params.append(dict(kw, Re=re))
+    return cases, params
 
 
 def oracle_rate(w, steps, seconds, workers):
@@ -307,13 +339,133 @@ def run_ours(args, w, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def run_ours_batch(args, w, rank, world):
+    """Batched sweep: all cases advance together, one graph launch per step."""
+    import torch
+    pkg = load_package()
+    L = pkg._lib
+    dev = int(os.environ.get('LOCAL_RANK', 0))
+    torch.cuda.set_device(dev)
+    dt = w['dt']
+    t0 = time.perf_counter()
+    cases, params = sweep_cases(pkg, w, args.precision)
+    setup_s = time.perf_counter() - t0
+    cells = sum(c.nx * c.ny for c in cases)
+    batch = pkg.CylinderBatch(cases)
+    for c in cases:
+        c._push()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device='cuda')
+
+    def step(b, k):
+        rc, diag, done = b.step_raw(dt, 1, first_index=k)
+        b._check(rc)
+        for i, c in enumerate(b.cases):
+            c.time = diag[i].time
+        return [diag[i] for i in range(len(b.cases))]
+
+    for k in range(max(args.warmup, 3)):
+        step(batch, k)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = L.lib.gm_kernel_launches()
+    times, divs, sweeps = [], [], []
+    with ClockSampler(dev) as clocks:
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t_0 = time.perf_counter()
+            d = step(batch, k + 1)
+            times.append((time.perf_counter() - t_0) * 1e3)
+            divs.append(max(x.max_divergence for x in d))
+            sweeps.append(sum(x.pressure_refinement_iterations + x.momentum_refinement_iterations for x in d) / len(d))
+    launches = L.lib.gm_kernel_launches() - launches0
+    assert max(divs) < 1e-10
+    step_ms = sum(times) / len(times)
+    if world > 1:
+        t = torch.tensor([step_ms], device='cuda')
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = cells * world / (step_ms * 1e-3)
+    # dominant kernel class (per-class event timing of one launch-by-launch batch step)
+    per_class = {}
+    for cls in KERNEL_CLASSES:
+        L.lib.gm_kernel_timing(cls, 1, None, None)
+        step(batch, 0)
+        tot, cnt = C.c_double(), C.c_int64()
+        L.lib.gm_kernel_timing(cls, 0, C.byref(tot), C.byref(cnt))
+        per_class[cls] = (tot.value, cnt.value)
+    L.lib.gm_kernel_timing(0, 0, None, None)
+    dominant = max(per_class, key=lambda c: per_class[c][0])
+    tot, cnt = per_class[dominant]
+    bytes_per_launch = 16.0 * cells / len(cases)  # mean case; read + write of one FP64 grid
+    mean_ms = tot / max(cnt, 1)
+    peak, peak_kind = peaks()
+    achieved = bytes_per_launch / (mean_ms * 1e-3) / 1e9
+    compare = None
+    if args.precision == 'fp32' and not args.no_compare:
+        c64, _ = sweep_cases(pkg, w, 'fp64')
+        b64 = pkg.CylinderBatch(c64)
+        for c in c64:
+            c._push()
+        for k in range(max(args.warmup, 3)):
+            step(b64, k)
+        t64 = []
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t_0 = time.perf_counter()
+            step(b64, k + 1)
+            t64.append((time.perf_counter() - t_0) * 1e3)
+        ms64 = sum(t64) / len(t64)
+        compare = dict(plain_fp64_value=cells / (ms64 * 1e-3), plain_fp64_ms_per_step=ms64,
+                       speedup_vs_plain_fp64=ms64 / step_ms)
+        b64.close()
+        del c64
+    # end to end through CylinderBatch.solve with host arrays (push + step + pull of every case)
+    e2e_steps = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t_0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        batch.solve(1, dt=dt)
+    e2e_s = (time.perf_counter() - t_0) / e2e_steps
+    state_bytes = sum(8 * (c.ny * (c.nx + 1) + (c.ny + 1) * c.nx + c.nx * c.ny) for c in cases)
+    if rank == 0:
+        grids = {}
+        for c in cases:
+            grids[f'{c.nx}x{c.ny}'] = grids.get(f'{c.nx}x{c.ny}', 0) + 1
+        line = dict(metric=METRIC, value=value, unit='cell-updates/s', n_gpus=world, steps=args.steps,
+                    warmup=args.warmup, ms_per_step=step_ms, higher_is_better=True, scaling='weak',
+                    vs_baseline=None, dtype='f64' if args.precision == 'fp64' else 'f32+f64-refine', data='synthetic',
+                    config=dict(workload=args.workload, cases=len(cases), grids=grids, cells_per_step=cells, dt=dt,
+                                precision='fp64 plain' if args.precision == 'fp64' else 'fp32 inverses/stencils, fp64 refinement',
+                                cases_per_gpu=len(cases), parallelism='replicas', setup_s=setup_s,
+                                l2='flushed (256 MB write) between timed steps; step timed on the host around '
+                                   'one graph launch and its status readback',
+                                pressure='DCT/DST fast inverse + boundary Schur (direct)'),
+                    roofline=dict(bound='hbm', achieved=achieved, peak=peak, unit='GB/s', frac=achieved / peak,
+                                  traffic=None, kernel=KERNEL_CLASSES[dominant], peak_source=peak_kind,
+                                  launches_timed=int(cnt), mean_launch_ms=mean_ms, bytes_per_launch=bytes_per_launch),
+                    step_roofline=dict(algorithmic_bytes_per_cell_update=880,
+                                       achieved_gbs=880.0 * cells / (step_ms * 1e-3) / 1e9),
+                    cpu_baseline=None,
+                    e2e=dict(value=cells / e2e_s, unit='cell-updates/s', h2d_bytes_per_step=state_bytes,
+                             d2h_bytes_per_step=state_bytes + len(cases) * C.sizeof(L.StepDiag)),
+                    clocks=clocks.summary(), gpu_launches=int(launches), max_divergence=max(divs),
+                    refinement_sweeps_per_case_step=float(np.mean(sweeps)),
+                    kernel_class_ms_per_step={KERNEL_CLASSES[c]: v[0] for c, v in per_class.items()},
+                    comparison=compare)
+        print(json.dumps(line), flush=True)
+    batch.close()
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
-    ap.add_argument('--workload', choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument('--workload', choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
     ap.add_argument('--no-compare', action='store_true', help='skip timing the plain FP64 step beside the FP32 mode')
     ap.add_argument('--precision', choices=('fp64', 'fp32'), default='fp64',
@@ -321,7 +473,7 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    w = WORKLOADS[args.workload]
+    w = WORKLOADS.get(args.workload) or BATCH_WORKLOADS[args.workload]
     world = int(os.environ.get('WORLD_SIZE', 1))
     rank = int(os.environ.get('RANK', 0))
     if args.impl == 'reference':
@@ -332,7 +484,10 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', 0)))
         dist.init_process_group('nccl')
-    run_ours(args, w, rank, world)
+    if args.workload in BATCH_WORKLOADS:
+        run_ours_batch(args, w, rank, world)
+    else:
+        run_ours(args, w, rank, world)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

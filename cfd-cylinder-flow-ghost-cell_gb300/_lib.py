@@ -23,7 +23,8 @@ SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_las
            'gm_get_surface_points', 'gm_set_state', 'gm_get_state', 'gm_set_inlet', 'gm_set_history',
            'gm_get_history', 'gm_step', 'gm_apply', 'gm_project', 'gm_pressure_solve', 'gm_rectangle_solve',
            'gm_surface_forces', 'gm_divergence_stats', 'gm_kernel_launches', 'gm_kernel_timing',
-           'gm_divergence_stats_noalloc')
+           'gm_divergence_stats_noalloc', 'gm_batch_create', 'gm_batch_destroy', 'gm_batch_last_error',
+           'gm_batch_step')
 NOALLOC_MAX_CELLS = 1048576
 
 
@@ -92,6 +93,10 @@ def _load():
         'gm_kernel_launches': ([], I64),
         'gm_kernel_timing': ([I32, I32, C.POINTER(D), C.POINTER(I64)], C.c_int),
         'gm_divergence_stats_noalloc': ([P, P, P, I32, I32, D, D, P, P, P], C.c_int),
+        'gm_batch_create': ([C.POINTER(C.c_void_p), I32, pp], C.c_int),
+        'gm_batch_destroy': ([P], C.c_int),
+        'gm_batch_last_error': ([P], C.c_char_p),
+        'gm_batch_step': ([P, D, I32, I64, P, C.POINTER(StepDiag), P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -107,20 +112,17 @@ class GhostError(Exception):
     pass
 
 
+def error_for(rc: int, msg: str) -> Exception:
+    """The reference's exception class for a GM_E* status."""
+    return {GM_EVALUE: ValueError, GM_ERUNTIME: RuntimeError, GM_EFLOAT: FloatingPointError,
+            GM_ENOTIMPL: NotImplementedError}.get(rc, GhostError)(msg)
+
+
 def check(rc: int, handle=None):
     """Map a GM_E* status to the reference's exception classes."""
     if rc == GM_OK:
         return
-    msg = lib.gm_last_error(handle).decode(errors='replace')
-    if rc == GM_EVALUE:
-        raise ValueError(msg)
-    if rc == GM_ERUNTIME:
-        raise RuntimeError(msg)
-    if rc == GM_EFLOAT:
-        raise FloatingPointError(msg)
-    if rc == GM_ENOTIMPL:
-        raise NotImplementedError(msg)
-    raise GhostError(msg)
+    raise error_for(rc, lib.gm_last_error(handle).decode(errors='replace'))
 
 
 def ptr(a):

@@ -136,6 +136,7 @@ struct gm_handle {
   gm::HelmholtzSetup hs;
   bool helm_ready = false;
   double helm_dt = 0;
+  long long helm_gen = 0;  // bumped whenever the device Helmholtz tables are rebuilt
   std::string err;
   cudaStream_t st = nullptr;
   bool own_stream = true;
@@ -604,6 +605,7 @@ void ensure_helmholtz(gm_handle* h, double dt) {
   h->hs = std::move(hs);
   h->helm_ready = true;
   h->helm_dt = dt;
+  ++h->helm_gen;
   if (h->host_only) return;
   // the Helmholtz tables are reallocated below: captured step graphs would point at freed buffers
   for (auto& gr : h->graphs)
@@ -690,11 +692,6 @@ void swap_state(gm_handle* h) {
   std::swap(h->U.p, h->Unext.p);
   std::swap(h->phalf.p, h->phalf_next.p);
   std::swap(h->hist.p, h->now.p);
-}
-void commit_step(gm_handle* h, double dt) {
-  swap_state(h);
-  h->has_history = true;
-  h->prev_dt = dt;
 }
 
 // Graph of one steady step for the current buffer assignment and dt (captured on demand,
@@ -1449,6 +1446,210 @@ int gm_kernel_timing(int32_t kernel_class, int32_t enable, double* total_ms, int
   if (count) *count = (int64_t)n;
   if (!enable && kernel_class == 0) ktimer_enable(0);
   return GM_OK;
+}
+
+}  // extern "C"
+
+// =============================================================================
+// Many cases per GPU: every steady step of all cases is one CUDA graph launch in
+// which each case is a concurrent branch (with its own refinement loops).
+// =============================================================================
+struct gm_batch {
+  std::vector<gm_handle*> cases;
+  std::vector<long long> gens;  // Helmholtz table generations the graphs were captured with
+  cudaStream_t root = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<const double*> key;
+    std::vector<long long> gens;
+    double dt = 0;
+    std::vector<long long> outer, body;  // per-case kernel node counts
+  } graphs[2];
+  std::string err;
+};
+
+namespace {
+
+std::vector<const double*> batch_key(gm_batch* b) {
+  std::vector<const double*> k;
+  for (gm_handle* h : b->cases) {
+    const double* t[6] = {h->U.p, h->Unext.p, h->phalf.p, h->phalf_next.p, h->hist.p, h->now.p};
+    k.insert(k.end(), t, t + 6);
+  }
+  return k;
+}
+
+gm_batch::Graph& batch_graph(gm_batch* b, double dt) {
+  std::vector<const double*> key = batch_key(b);
+  std::vector<long long> gens;
+  for (gm_handle* h : b->cases) gens.push_back(h->helm_gen);
+  for (auto& gr : b->graphs)
+    if (gr.exec && gr.dt == dt && gr.key == key && gr.gens == gens) return gr;
+  gm_batch::Graph* slot = !b->graphs[0].exec ? &b->graphs[0] : (!b->graphs[1].exec ? &b->graphs[1] : nullptr);
+  if (!slot) {
+    slot = (b->graphs[0].key == key || b->graphs[0].dt != dt) ? &b->graphs[0] : &b->graphs[1];
+    cudaGraphExecDestroy(slot->exec);
+    slot->exec = nullptr;
+  }
+  slot->outer.assign(b->cases.size(), 0);
+  slot->body.assign(b->cases.size(), 0);
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal));
+  try {
+    CK(cudaEventRecord(b->fork, b->root));
+    for (size_t c = 0; c < b->cases.size(); ++c) {
+      gm_handle* h = b->cases[c];
+      CK(cudaStreamWaitEvent(h->st, b->fork, 0));
+      const long long c0 = kernel_launch_count();
+      h->capturing = true;
+      step_once(h, dt, -1);
+      h->capturing = false;
+      const long long captured = kernel_launch_count() - c0;
+      kernel_launch_adjust(-captured);
+      slot->body[c] = h->body_nodes_capture;
+      slot->outer[c] = captured - 4 * h->body_nodes_capture;
+      CK(cudaEventRecord(b->join[c], h->st));
+      CK(cudaStreamWaitEvent(b->root, b->join[c], 0));
+    }
+  } catch (...) {
+    for (gm_handle* h : b->cases) h->capturing = false;
+    cudaStreamEndCapture(b->root, &g);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    throw;
+  }
+  CK(cudaStreamEndCapture(b->root, &g));
+  cudaGraphExec_t ex = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) throw CudaError(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  slot->exec = ex;
+  slot->dt = dt;
+  slot->key = key;
+  slot->gens = gens;
+  return *slot;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gm_batch_create(gm_handle* const* cases, int32_t n_cases, gm_batch** out) {
+  if (!cases || n_cases <= 0 || !out) { g_create_error = "null argument"; return GM_EVALUE; }
+  *out = nullptr;
+  auto b = std::make_unique<gm_batch>();
+  for (int i = 0; i < n_cases; ++i) {
+    if (!cases[i] || cases[i]->host_only) { g_create_error = "batch cases must be device handles"; return GM_EVALUE; }
+    for (int j = 0; j < i; ++j)
+      if (cases[j] == cases[i]) { g_create_error = "a case appears twice in the batch"; return GM_EVALUE; }
+    b->cases.push_back(cases[i]);
+  }
+  int rc = run_guarded(nullptr, [&] {
+    CK(cudaStreamCreateWithFlags(&b->root, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    b->join.resize(n_cases);
+    for (auto& e : b->join) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  });
+  if (rc != GM_OK) return rc;
+  *out = b.release();
+  return GM_OK;
+}
+
+int gm_batch_destroy(gm_batch* b) {
+  if (!b) return GM_OK;
+  if (b->root) cudaStreamSynchronize(b->root);
+  for (auto& gr : b->graphs)
+    if (gr.exec) cudaGraphExecDestroy(gr.exec);
+  for (auto& e : b->join) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->root) cudaStreamDestroy(b->root);
+  delete b;
+  return GM_OK;
+}
+
+const char* gm_batch_last_error(const gm_batch* b) { return b ? b->err.c_str() : g_global_error; }
+
+int gm_batch_step(gm_batch* b, double dt, int32_t n_steps, int64_t first_step_index, const double* start_times,
+                  gm_step_diag* diag, int32_t* steps_done) {
+  if (!b) return GM_EVALUE;
+  if (!(std::isfinite(dt) && dt > 0) || n_steps <= 0) { b->err = "dt must be finite and positive"; return GM_EVALUE; }
+  const int nc = (int)b->cases.size();
+  if (steps_done) std::fill(steps_done, steps_done + nc, 0);
+  int first_error = GM_OK;
+  try {
+    for (gm_handle* h : b->cases) {
+      ensure_helmholtz(h, dt);
+      CK(cudaMemsetAsync(h->ctl.p, 0, sizeof(StepCtl), h->st));  // clears the sticky error words
+      long long counter = first_step_index;
+      CK(cudaMemcpyAsync(h->counter.p, &counter, sizeof counter, cudaMemcpyHostToDevice, h->st));
+    }
+    int s = 0;
+    while (s < n_steps && first_error == GM_OK) {
+      bool steady = !ktimer_active();
+      for (gm_handle* h : b->cases) steady = steady && h->has_history && h->prev_dt == dt && h->use_graphs;
+      const int batch = steady ? std::min(n_steps - s, (int)gm_handle::RING_CAP) : 1;
+      for (gm_handle* h : b->cases) CK(cudaMemsetAsync(h->ridx.p, 0, sizeof(int), h->st));
+      long long nodes = 0;
+      if (!steady) {
+        // start-up or changed dt: every case launch by launch on its own stream
+        for (gm_handle* h : b->cases) {
+          step_once(h, dt, ((first_step_index + s) % 100) == 0 ? 1 : 0);
+          swap_state(h);
+        }
+      } else {
+        for (gm_handle* h : b->cases) CK(cudaStreamSynchronize(h->st));
+        for (int k = 0; k < batch; ++k) {
+          CK(cudaGraphLaunch(batch_graph(b, dt).exec, b->root));
+          for (gm_handle* h : b->cases) swap_state(h);
+        }
+        CK(cudaStreamSynchronize(b->root));
+      }
+      for (gm_handle* h : b->cases)
+        CK(cudaMemcpyAsync(h->host_ring, h->ring.p, batch * sizeof(StepCtl), cudaMemcpyDeviceToHost, h->st));
+      for (int c = 0; c < nc; ++c) {
+        gm_handle* h = b->cases[c];
+        CK(cudaStreamSynchronize(h->st));
+        const bool first = !h->has_history;
+        int good = 0;
+        while (good < batch && h->host_ring[good].err == 0) ++good;
+        const double t0 = start_times ? start_times[c] : 0.0;
+        for (int k = 0; k < std::min(batch, good + 1); ++k)
+          if (diag) fill_diag(h, h->host_ring[k], t0 + (s + k + 1) * dt, dt, first && k == 0,
+                              &diag[(size_t)c * n_steps + s + k]);
+        if (steady) {
+          const gm_batch::Graph& gr = b->graphs[0].exec ? b->graphs[0] : b->graphs[1];
+          for (int k = 0; k < batch; ++k) {
+            int sweeps = 0;
+            for (int sl = 0; sl < 5; ++sl) sweeps += h->host_ring[k].solve[sl].k;
+            nodes += gr.outer[c] + gr.body[c] * sweeps;
+          }
+        }
+        if (steps_done) steps_done[c] = s + good;
+        if (good > 0) { h->has_history = true; h->prev_dt = dt; }
+        if (good < batch) {
+          // the sticky error word froze this case after its last good step: undo the swaps since
+          if ((batch - good) % 2) swap_state(h);
+          *h->host_ctl = h->host_ring[good];
+          if (first_error == GM_OK) {
+            first_error = h->host_ring[good].err;
+            b->err = "case " + std::to_string(c) + ": gate " + std::to_string(h->host_ring[good].gate) +
+                     " failed at step " + std::to_string(first_step_index + s + good);
+          }
+        }
+      }
+      if (steady) kernel_launch_adjust(nodes);
+      s += batch;
+    }
+  } catch (const GateError& e) {
+    b->err = e.msg;
+    return e.cls;
+  } catch (const std::exception& e) {
+    b->err = e.what();
+    return GM_ECUDA;
+  }
+  return first_error;
 }
 
 }  // extern "C"

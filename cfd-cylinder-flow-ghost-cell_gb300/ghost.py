@@ -474,3 +474,74 @@ class MAC_CylinderFlow:
             if hist['previous_advection'] is not None:
                 solver.gg.set_history(hist['previous_advection'], hist['half_pressure'], prev_dt)
             return solver
+
+
+class CylinderBatch:
+    """Independent ``MAC_CylinderFlow`` cases advanced together on one GPU.
+
+    Every steady step of all cases is one CUDA graph launch in which each case is a
+    concurrent branch with its own refinement loops (gm_batch_step).  The reference steps
+    one case per process; a batch gives the same per-case results as stepping each case
+    alone (the same kernels in the same order per case).  Cases may differ in grid size,
+    geometry, viscosity and precision mode.  The inlet is held at its base profile (no
+    start-up perturbation) while the batch steps.
+    """
+
+    def __init__(self, cases):
+        cases = list(cases)
+        if not cases or not all(isinstance(c, MAC_CylinderFlow) for c in cases):
+            raise ValueError('CylinderBatch takes a non-empty list of MAC_CylinderFlow cases')
+        if len({id(c) for c in cases}) != len(cases):
+            raise ValueError('a case appears twice in the batch')
+        self.cases = cases
+        arr = (C.c_void_p * len(cases))(*[c._h.value for c in cases])
+        b = C.c_void_p()
+        check(lib.gm_batch_create(arr, len(cases), C.byref(b)))
+        self._b = b
+
+    def close(self):
+        b = getattr(self, '_b', None)
+        if b:
+            lib.gm_batch_destroy(b)
+            self._b = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc != _lib.GM_OK:
+            msg = (lib.gm_batch_last_error(self._b) or b'').decode(errors='replace')
+            raise _lib.error_for(rc, msg)
+
+    def step_raw(self, dt, n_steps, first_index=0):
+        """n_steps of every case on the device state; returns (rc, diag[n_cases][n_steps], steps_done)."""
+        n = len(self.cases)
+        diag = (_lib.StepDiag * (n * n_steps))()
+        done = np.zeros(n, np.int32)
+        t0 = np.array([c.time for c in self.cases], np.float64)
+        rc = lib.gm_batch_step(self._b, float(dt), int(n_steps), int(first_index), ptr(t0), diag, ptr(done))
+        return rc, diag, done
+
+    def solve(self, n_steps, dt=0.002, first_index=0):
+        """Advance every case n_steps (the loop of solver/main.py:245-501 without the inlet
+        perturbation); returns per case (times, C_D, C_L)."""
+        if isinstance(n_steps, bool) or not isinstance(n_steps, (int, np.integer)) or n_steps <= 0:
+            raise ValueError('n_steps must be a positive integer')
+        if not np.isfinite(dt) or dt <= 0:
+            raise ValueError('dt must be finite and positive')
+        for c in self.cases:
+            c._push()
+            c.u_inlet[:] = c.u_inlet_base
+            c._set_inlet()
+        rc, diag, done = self.step_raw(dt, n_steps, first_index)
+        out = []
+        for i, c in enumerate(self.cases):
+            recs = [diag[i * n_steps + k] for k in range(int(done[i]))]
+            for d in recs:
+                c.time = d.time
+                c.last_step_diagnostics = c._diag_dict(d)
+            c._pull()
+            out.append((np.array([d.time for d in recs]), np.array([d.cd for d in recs]),
+                        np.array([d.cl for d in recs])))
+        self._check(rc)
+        return out

@@ -181,6 +181,24 @@ int gm_surface_forces(gm_handle* h, const double* u, const double* v, const doub
  * (solver/src/bindings.cpp:343-390): out = max, sum div^2, core sum div^2; counts = count, core count. */
 int gm_divergence_stats(gm_handle* h, const double* u, const double* v, double out[3], int64_t counts[2]);
 
+/* --- many cases per GPU (no reference counterpart: the reference steps one case) --- */
+
+/* A batch of independent cases (handles created with gm_create) stepped together: each
+ * steady step of all cases is one CUDA graph launch with one concurrent branch per case. */
+typedef struct gm_batch gm_batch;
+int gm_batch_create(gm_handle* const* cases, int32_t n_cases, gm_batch** out);
+int gm_batch_destroy(gm_batch* b);
+const char* gm_batch_last_error(const gm_batch* b);
+/* n_steps of every case (as gm_step); start_times[n_cases] may be NULL (time 0);
+ * diag (may be NULL) receives n_cases * n_steps records, case-major (diag[c * n_steps + k]).
+ * When a gate of some case fails, stepping stops at the end of the current graph batch
+ * (at most 64 steps): the failed case is left at its last good step, the others at the
+ * batch end; steps_done[n_cases] (may be NULL) receives each case's completed steps and
+ * the call returns the first failure's code.  The cases must outlive the batch; each
+ * case may still be stepped alone with gm_step between batch calls. */
+int gm_batch_step(gm_batch* b, double dt, int32_t n_steps, int64_t first_step_index, const double* start_times,
+                  gm_step_diag* diag, int32_t* steps_done);
+
 /* --- allocation-free entry point ------------------------------------------------ */
 
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc (code
