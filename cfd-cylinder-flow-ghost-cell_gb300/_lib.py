@@ -91,7 +91,7 @@ def _load():
         'gm_surface_forces': ([P, P, P, P, D, P], C.c_int),
         'gm_divergence_stats': ([P, P, P, P, P], C.c_int),
         'gm_kernel_launches': ([], I64),
-        'gm_kernel_timing': ([I32, I32, C.POINTER(D), C.POINTER(I64)], C.c_int),
+        'gm_kernel_timing': ([I32, I32, C.POINTER(D), C.POINTER(I64), C.POINTER(D)], C.c_int),
         'gm_divergence_stats_noalloc': ([P, P, P, I32, I32, D, D, P, P, P], C.c_int),
         'gm_batch_create': ([C.POINTER(C.c_void_p), I32, pp], C.c_int),
         'gm_batch_destroy': ([P], C.c_int),

@@ -12,6 +12,7 @@
 #include <functional>
 #include <memory>
 #include <string>
+#include <array>
 #include <vector>
 
 #include "../../include/ghostmac.h"
@@ -127,6 +128,12 @@ struct RectDev {
   int rank = 0;
   DBuf<int64_t> rows, cptr, ccol;
   DBuf<double> cval, sinv;
+  int mcount = 0;             // distinct points read by the C rows
+  DBuf<int64_t> mcols;        // their field-grid flat indices
+  DBuf<double> mmat;          // M = S^{-1} C, rank x mcount
+  // band solve of the Schur term (pivots, decay factors, band work array)
+  DBuf<double> bpiv, phi, psi, band;
+  DBuf<float> bpiv32, phi32, psi32, band32;
 };
 
 }  // namespace
@@ -152,10 +159,15 @@ struct gm_handle {
   DBuf<int32_t> a_nnz;
   DBuf<int64_t> sp_ptr, sp_col, su_ptr, su_col, sv_ptr, sv_col, d_ui, d_vi, d_pi;
   DBuf<double> sp_val, su_val, sv_val, nwx, nwy, nxx, nyy;
+  DBuf<double> surf_part;      // per-point force terms
+  DBuf<unsigned> surf_ticket;  // k_forces block counter
   RectDev rp, ru, rv;
   // state and work buffers (face grid F, pressure grid P)
   DBuf<double> U, Unext, hist, now, rhs, star, fres, ffirst, fw2, fmid, fhalf, faction, fproj, fproj2, ftmp;
   DBuf<double> phalf, phalf_next, pout, prhs, pphi, pres, pfirst, pw2, pinc, ptmp, spectral;
+  DBuf<float> pres32, fres32;  // FP32-mode residuals (inputs of the FP32 inverse)
+  DBuf<float> U32, P32;        // FP32-mode copies of the state for the momentum stencils
+  ResidualCoef rcoef[3];       // regular-row coefficients: pressure, Helmholtz u, Helmholtz v
   DBuf<float> spectral32, ffirst32, pfirst32;
   DBuf<StepCtl> ctl;
   DBuf<unsigned long long> state_max;  // persistent max|u|, max|v| of the current state
@@ -167,16 +179,26 @@ struct gm_handle {
   DBuf<long long> counter;
   StepCtl* host_ring = nullptr;
   cudaStream_t st_body = nullptr;  // capture stream of conditional-node bodies
+  // second lane: the v Helmholtz solve runs beside the u solve (own stream, body stream and
+  // spectral work arrays); fork/join by events
+  cudaStream_t st2 = nullptr, st2_body = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  DBuf<double> spectral_b;
+  DBuf<float> spectral32_b;
+  long long body_nodes_slot[5] = {0, 0, 0, 0, 0};  // kernels per refinement sweep of each solve slot
   bool use_graphs = true;
   bool capturing = false;
+  // launch-by-launch steps decide every refinement sweep on the host (one synchronisation
+  // per sweep) instead of launching all sweeps gated: then every launched kernel does work,
+  // which per-kernel timing and profiling need (environment GHOSTMAC_HOST_REFINE=1)
+  bool host_refine = false;
   struct StepGraph {
     cudaGraphExec_t exec = nullptr;
     const double* key[6] = {};
     double dt = 0;
-    long long outer_nodes = 0;  // kernel nodes outside the refinement loops
-    long long body_nodes = 0;   // kernel nodes of one refinement sweep
+    long long outer_nodes = 0;     // kernel nodes outside the refinement loops
+    long long body_nodes[5] = {};  // kernel nodes of one refinement sweep, per solve slot
   } graphs[2];
-  long long body_nodes_capture = 0;
   bool has_history = false;
   bool host_only = false;
   int precision = 0;  // 0 plain FP64, 1 FP32 inverse with FP64 refinement
@@ -274,6 +296,125 @@ void ysolve_tables(const YChunks& ch, int n, int cols, int kx, const std::vector
   }
 }
 
+// Diagonal of the column system of x-mode kx: pressure (L_y + lambda_x)/rho, Helmholtz
+// (1 - c lambda_x) - c L_y with c = dt/2 nu; the off-diagonal is column_gamma.  The wall
+// rows follow the 1-D operators of solver/rectangular_inverse.py:8-58.
+void column_diagonal(const gm::Geometry& g, int kind, double dt, int rows, int kx, std::vector<double>& mainj) {
+  const double PI = 3.141592653589793;
+  const double idy2 = 1.0 / (g.dy * g.dy);
+  const double c = (0.5 * dt) * g.nu;
+  const double sx = ((double)kx + 0.5) * PI / (2 * g.nx);
+  const double lam = -4 * std::pow(std::sin(sx), 2) / (g.dx * g.dx);
+  mainj.resize(rows);
+  for (int j = 0; j < rows; ++j) {
+    double m = -2.0;
+    if (kind == 0 && (j == 0 || j == rows - 1)) m = -1.0;
+    if (kind == 1 && (j == 0 || j == rows - 1)) m = -3.0;
+    const double ly = m * idy2;
+    mainj[j] = kind == 0 ? (ly + lam) / g.rho : 1.0 - c * (lam + ly);
+  }
+}
+double column_gamma(const gm::Geometry& g, int kind, double dt) {
+  const double idy2 = 1.0 / (g.dy * g.dy);
+  return kind == 0 ? idy2 / g.rho : -((0.5 * dt) * g.nu) * idy2;
+}
+
+// T^{-1} b on a rectangle view without the boundary term: x pass, column solves, x pass.
+template <typename T, typename TI, typename TO>
+void plain_inverse(const TransformTables& tt, const RectView& v, const TI* b, bool mask_in, T* spectral, TO* out,
+                   const uint8_t* ocls, const double* add, const Gate& g, cudaStream_t st) {
+  const YCorr<T> none{nullptr, nullptr, nullptr, 0, -1};
+  launch_xpass<T, TI, T>(tt, false, 0, v.rows, b, v.base, v.pitch, mask_in ? v.cls : nullptr, spectral, 0, v.cols,
+                         nullptr, nullptr, none, g, st);
+  launch_ysolve<T>(tt, v.cols, v.rows, spectral, g, st);
+  launch_xpass<T, T, TO>(tt, true, 0, v.rows, spectral, 0, v.cols, nullptr, out, v.base, v.pitch, ocls, add, none, g,
+                         st);
+}
+
+// Launch shapes of the separable inverse, picked by timing: the x pass over line-group
+// sizes of 1-8 warps and 1-4 groups per block, the column solve over 2-8 columns per
+// block.  Every shape computes the same values (each line / column is handled by the same
+// arithmetic whatever the grouping), so only the time differs.
+void autotune_shapes(gm_handle* h, RectDev& rd, int kind, bool fp32) {
+  TransformTables& tt = fp32 ? rd.tt32 : rd.tt;
+  const RectView& v = rd.view;
+  cudaStream_t st = h->st;
+  const size_t per = std::max(xpass_smem_per_group(tt.tx_fwd, v.cols, fp32), xpass_smem_per_group(tt.tx_inv, v.cols, fp32));
+  double* field = kind == 0 ? h->ptmp.p : h->ftmp.p;
+  float* field32 = kind == 0 ? h->pfirst32.p : h->ffirst32.p;
+  const Gate open{nullptr, 0, 0};
+  const YCorr<double> none64{nullptr, nullptr, nullptr, 0, -1};
+  const YCorr<float> none32{nullptr, nullptr, nullptr, 0, -1};
+  CK(cudaMemsetAsync(field, 0, (size_t)(kind == 0 ? h->Pn : h->F) * sizeof(double), st));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  auto time_ms = [&](auto&& body) {
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+      CK(cudaEventRecord(e0, st));
+      body();
+      CK(cudaEventRecord(e1, st));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (rep > 0) best = std::min(best, ms);  // the first run warms caches and code
+    }
+    return best;
+  };
+  // x pass
+  float best = 1e30f;
+  int bt = 32, bg = 1;
+  for (int gt : {32, 64, 128, 256}) {
+    for (int gp : {1, 2, 4}) {
+      if (gt * gp > 512 || per * gp > h->smem_optin) continue;
+      tt.xg_threads = gt;
+      tt.xg_pb = gp;
+      tt.smem_x = per * gp;
+      float ms = time_ms([&] {
+        if (fp32) {
+          launch_xpass<float, double, float>(tt, false, 0, v.rows, field, v.base, v.pitch, nullptr, h->spectral32.p, 0,
+                                             v.cols, nullptr, nullptr, none32, open, st);
+          launch_xpass<float, float, float>(tt, true, 0, v.rows, h->spectral32.p, 0, v.cols, nullptr, field32, v.base,
+                                            v.pitch, nullptr, nullptr, none32, open, st);
+        } else {
+          launch_xpass<double, double, double>(tt, false, 0, v.rows, field, v.base, v.pitch, nullptr, h->spectral.p, 0,
+                                               v.cols, nullptr, nullptr, none64, open, st);
+          launch_xpass<double, double, double>(tt, true, 0, v.rows, h->spectral.p, 0, v.cols, nullptr, field, v.base,
+                                               v.pitch, nullptr, nullptr, none64, open, st);
+        }
+      });
+      if (ms < best) { best = ms; bt = gt; bg = gp; }
+    }
+  }
+  tt.xg_threads = bt;
+  tt.xg_pb = bg;
+  tt.smem_x = per * bg;
+  // column solve
+  best = 1e30f;
+  int bl = 0;
+  for (int L : {2, 4, 8}) {
+    const int thr = ((std::min(L, v.cols) * tt.ych.P + 31) / 32) * 32;
+    const size_t sm = ysolve_smem(v.rows, L, fp32);
+    if (thr > 1024 || sm > h->smem_optin) continue;
+    tt.lpb_y = std::min(L, v.cols);
+    tt.threads_y = thr;
+    tt.smem_y = sm;
+    float ms = time_ms([&] {
+      if (fp32) launch_ysolve<float>(tt, v.cols, v.rows, h->spectral32.p, open, st);
+      else launch_ysolve<double>(tt, v.cols, v.rows, h->spectral.p, open, st);
+    });
+    if (ms < best) { best = ms; bl = L; }
+  }
+  if (bl == 0) throw CudaError("separable inverse does not fit the launch limits");
+  tt.lpb_y = std::min(bl, v.cols);
+  tt.threads_y = ((tt.lpb_y * tt.ych.P + 31) / 32) * 32;
+  tt.smem_y = ysolve_smem(v.rows, bl, fp32);
+  CK(cudaEventDestroy(e0));
+  CK(cudaEventDestroy(e1));
+  CK(cudaGetLastError());
+}
+
 // x transform tables and y partition tables of a rectangle kind
 // (solver/rectangular_inverse.py:8-58: same operator, y direction solved exactly per x-mode)
 void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
@@ -301,24 +442,12 @@ void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
   tt.Wx = rd.Wx.p; tt.prex = rd.prex.p; tt.postx = rd.postx.p;
   tt.prex_inv = rd.prex.p; tt.postx_inv = rd.postx.p;
   // column systems: pressure (L_y + lambda_x)/rho; Helmholtz (1 - c lambda_x) - c L_y, c = dt/2 nu
-  const double PI = 3.141592653589793;
-  const double idy2 = 1.0 / (g.dy * g.dy);
-  std::vector<double> ly(rows);
-  for (int j = 0; j < rows; ++j) {
-    double m = -2.0;
-    if (kind == 0 && (j == 0 || j == rows - 1)) m = -1.0;
-    if (kind == 1 && (j == 0 || j == rows - 1)) m = -3.0;
-    ly[j] = m * idy2;
-  }
-  const double c = (0.5 * dt) * g.nu;
-  tt.gamma = kind == 0 ? idy2 / g.rho : -c * idy2;
+  tt.gamma = column_gamma(g, kind, dt);
   tt.yscale = 1.0 / (2.0 * nx);
   tt.ych = make_chunks(rows);
   std::vector<double> t0((size_t)rows * cols), t1((size_t)rows * cols), t2((size_t)rows * cols), mainj(rows);
   for (int kx = 0; kx < cols; ++kx) {
-    double sx = ((double)kx + 0.5) * PI / (2 * nx);
-    double lam = -4 * std::pow(std::sin(sx), 2) / (g.dx * g.dx);
-    for (int j = 0; j < rows; ++j) mainj[j] = kind == 0 ? (ly[j] + lam) / g.rho : 1.0 - c * (lam + ly[j]);
+    column_diagonal(g, kind, dt, rows, kx, mainj);
     ysolve_tables(tt.ych, rows, cols, kx, mainj, tt.gamma, t0.data(), t1.data(), t2.data());
   }
   rd.t0.upload(t0, st);
@@ -330,29 +459,9 @@ void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
     rd.t1_32.upload(to_f32(t1), st);
     rd.t2_32.upload(to_f32(t2), st);
   }
-  // launch shapes: x passes one warp per line group, up to 4 warps per block; the y solve
-  // takes 16 consecutive columns per block (32 in FP32), i.e. full 128-byte row segments
-  auto warp_smem = [](int type, int n, size_t esz) {
-    const int lpw = r2r_paired(type) ? 2 : 1;
-    size_t stage = ((size_t)lpw * n * esz + 15) / 16 * 16;
-    return stage + 2 * (size_t)r2r_buffer_elems(type, n, lpw) * 2 * esz;
-  };
-  auto shapes = [&](TransformTables& t, size_t esz) {
-    size_t per = std::max(warp_smem(tx_f, cols, esz), warp_smem(tx_i, cols, esz));
-    int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, h->smem_optin / per));
-    t.lpb_x = wpb;
-    t.smem_x = per * wpb;
-    int P = t.ych.P;
-    int L = esz == 4 ? 32 : 16;
-    L = std::min(L, cols);
-    while (L > 1 && (L * P > 1024 || (size_t)L * rows * esz > h->smem_optin)) L /= 2;
-    t.lpb_y = L;
-    t.threads_y = ((L * P + 31) / 32) * 32;
-    t.smem_y = (size_t)L * rows * esz;
-  };
-  shapes(tt, sizeof(double));
-  if (tt.smem_x > h->smem_optin || tt.smem_y > h->smem_optin || tt.threads_y > 1024)
-    throw CudaError("separable inverse does not fit the launch limits");
+  tt.n = cols;
+  tt.bj0 = 0; tt.bj1 = -1; tt.cj0 = 0; tt.cj1 = -1;
+  tt.bpiv = tt.phi = tt.psi = nullptr;
   if (h->precision == 1) {
     // FP32 tables and launch shapes (same plans, half the shared memory per line)
     TransformTables& t32 = rd.tt32;
@@ -368,7 +477,6 @@ void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
     t32.Wx = rd.Wx32.p; t32.prex = rd.prex32.p; t32.postx = rd.postx32.p;
     t32.prex_inv = rd.prex32.p; t32.postx_inv = rd.postx32.p;
     t32.t0 = rd.t0_32.p; t32.t1 = rd.t1_32.p; t32.t2 = rd.t2_32.p;
-    shapes(t32, sizeof(float));
   }
   // view
   rd.view.rows = rows;
@@ -376,15 +484,96 @@ void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
   if (kind == 0) { rd.view.base = 0; rd.view.pitch = nx; rd.view.cls = h->cls_p.p; }
   else if (kind == 1) { rd.view.base = 1; rd.view.pitch = nx + 1; rd.view.cls = h->cls_f.p; }
   else { rd.view.base = h->g.usize + nx; rd.view.pitch = nx; rd.view.cls = h->cls_f.p; }
+  autotune_shapes(h, rd, kind, false);
+  if (h->precision == 1) autotune_shapes(h, rd, kind, true);
+}
+
+// Band solve of the Schur term T^{-1} U c.  U c is nonzero only in the rows bj0..bj1 that
+// hold boundary rows, so after the x transform each column system has its right-hand side
+// in the band.  Eliminating the rows below the band (pivots e, from row 0 up) and above it
+// (pivots f, from the last row down) leaves the band system with modified end pivots, and
+// outside the band the solution decays geometrically from the band's end values:
+//   y[j] = phi[j] y[bj0],  phi[j] = prod_{i=j}^{bj0-1} (-gamma / e_i)       (j < bj0)
+//   y[j] = psi[j] y[bj1],  psi[j] = prod_{i=bj1+1}^{j} (-gamma / f_i)       (j > bj1)
+// The C rows read the uncorrected solution in rows cj0..cj1 only.
+void build_band_tables(gm_handle* h, RectDev& rd, const std::vector<int64_t>& rows, const gm::Csr& C) {
+  TransformTables& tt = rd.tt;
+  const int R = rd.view.rows, cols = rd.view.cols;
+  const int kind = &rd == &h->rp ? 0 : (&rd == &h->ru ? 1 : 2);
+  const double dt = kind == 0 ? 0.0 : h->helm_dt;
+  cudaStream_t st = h->st;
+  if (rows.empty()) {
+    tt.bj0 = 0; tt.bj1 = -1; tt.cj0 = 0; tt.cj1 = -1;
+    rd.tt32.bj0 = 0; rd.tt32.bj1 = -1; rd.tt32.cj0 = 0; rd.tt32.cj1 = -1;
+    return;
+  }
+  int bj0 = R, bj1 = -1, cj0 = R, cj1 = -1;
+  for (int64_t r : rows) { const int j = (int)(r / cols); bj0 = std::min(bj0, j); bj1 = std::max(bj1, j); }
+  for (int64_t c : C.col) { const int j = (int)(c / cols); cj0 = std::min(cj0, j); cj1 = std::max(cj1, j); }
+  const int nb = bj1 - bj0 + 1;
+  const double gamma = tt.gamma;
+  std::vector<double> bpiv((size_t)nb * cols), phi((size_t)std::max(bj0, 1) * cols, 0.0),
+      psi((size_t)std::max(R - 1 - bj1, 1) * cols, 0.0), d, e(R), f(R);
+  for (int kx = 0; kx < cols; ++kx) {
+    column_diagonal(h->g, kind, dt, R, kx, d);
+    if (bj0 > 0) {
+      e[0] = d[0];
+      for (int i = 1; i < bj0; ++i) e[i] = d[i] - gamma * gamma / e[i - 1];
+      double q = 1.0;
+      for (int j = bj0 - 1; j >= 0; --j) {
+        q *= -gamma / e[j];
+        phi[(size_t)j * cols + kx] = q;
+      }
+    }
+    if (bj1 < R - 1) {
+      f[R - 1] = d[R - 1];
+      for (int i = R - 2; i > bj1; --i) f[i] = d[i] - gamma * gamma / f[i + 1];
+      double q = 1.0;
+      for (int j = bj1 + 1; j < R; ++j) {
+        q *= -gamma / f[j];
+        psi[(size_t)(j - bj1 - 1) * cols + kx] = q;
+      }
+    }
+    double prev = 0.0;
+    for (int j = bj0; j <= bj1; ++j) {
+      double dm = d[j];
+      if (j == bj0 && bj0 > 0) dm -= gamma * gamma / e[bj0 - 1];
+      if (j == bj1 && bj1 < R - 1) dm -= gamma * gamma / f[bj1 + 1];
+      const double pv = j == bj0 ? dm : dm - gamma * gamma * prev;
+      prev = 1.0 / pv;
+      bpiv[(size_t)(j - bj0) * cols + kx] = prev;
+    }
+  }
+  rd.bpiv.upload(bpiv, st);
+  rd.phi.upload(phi, st);
+  rd.psi.upload(psi, st);
+  rd.band.alloc((size_t)nb * cols);
+  tt.bj0 = bj0; tt.bj1 = bj1; tt.cj0 = cj0; tt.cj1 = cj1;
+  tt.bpiv = rd.bpiv.p; tt.phi = rd.phi.p; tt.psi = rd.psi.p;
+  if (h->precision == 1) {
+    rd.bpiv32.upload(to_f32(bpiv), st);
+    rd.phi32.upload(to_f32(phi), st);
+    rd.psi32.upload(to_f32(psi), st);
+    rd.band32.alloc((size_t)nb * cols);
+    TransformTables& t32 = rd.tt32;
+    t32.bj0 = bj0; t32.bj1 = bj1; t32.cj0 = cj0; t32.cj1 = cj1;
+    t32.bpiv = rd.bpiv32.p; t32.phi = rd.phi32.p; t32.psi = rd.psi32.p;
+  }
+  CK(cudaStreamSynchronize(st));
 }
 
 // Schur matrix S = I + C T^{-1} U by impulse solves, LU, explicit inverse (solver/pressure_schur.py:92-101)
 void build_schur(gm_handle* h, RectDev& rd, const std::vector<int64_t>& rows, const gm::Csr& C, double* field_buf) {
   cudaStream_t st = h->st;
   rd.rank = (int)rows.size();
-  rd.rows.upload(rows, st);
+  // device copies hold field-grid flat indices (no index arithmetic in the kernels)
+  auto field_index = [&](int64_t rc) { return rd.view.base + (rc / rd.view.cols) * rd.view.pitch + rc % rd.view.cols; };
+  std::vector<int64_t> frows(rows.size()), fcol(C.col.size());
+  for (size_t k = 0; k < rows.size(); ++k) frows[k] = field_index(rows[k]);
+  for (size_t k = 0; k < C.col.size(); ++k) fcol[k] = field_index(C.col[k]);
+  rd.rows.upload(frows, st);
   rd.cptr.upload(C.ptr, st);
-  rd.ccol.upload(C.col, st);
+  rd.ccol.upload(fcol, st);
   rd.cval.upload(C.val, st);
   const int n = rd.rank;
   if (n == 0) { rd.sinv.alloc(0); return; }
@@ -400,7 +589,8 @@ void build_schur(gm_handle* h, RectDev& rd, const std::vector<int64_t>& rows, co
     int64_t rc = rows[c];
     int64_t fi = rd.view.base + (rc / rd.view.cols) * rd.view.pitch + rc % rd.view.cols;
     CK(cudaMemcpyAsync(field_buf + fi, &one, sizeof(double), cudaMemcpyHostToDevice, st));
-    launch_rect_inverse(rd.tt, rd.view, field_buf, false, h->spectral.p, first, nullptr, nullptr, open, st);
+    plain_inverse<double, double, double>(rd.tt, rd.view, field_buf, false, h->spectral.p, first, nullptr, nullptr,
+                                          open, st);
     launch_schur_column(first, rd.view, n, rd.cptr.p, rd.ccol.p, rd.cval.p, S.p, c, st);
     CK(cudaMemcpyAsync(field_buf + fi, &zero, sizeof(double), cudaMemcpyHostToDevice, st));
   }
@@ -414,12 +604,75 @@ void build_schur(gm_handle* h, RectDev& rd, const std::vector<int64_t>& rows, co
   std::vector<double> inv((size_t)n * n);
   gm::lu_inverse(n, hs.data(), piv.data(), inv.data());
   rd.sinv.upload(inv, st);
+  // M = S^{-1} C as a dense rank x m matrix over the m distinct points C reads, so that one
+  // gather and one GEMV give c = S^{-1} (C first) per solve
+  std::vector<int64_t> ucol(C.col.begin(), C.col.end());
+  std::sort(ucol.begin(), ucol.end());
+  ucol.erase(std::unique(ucol.begin(), ucol.end()), ucol.end());
+  const int m = (int)ucol.size();
+  if ((size_t)m * sizeof(double) > 48 * 1024) throw CudaError("boundary Schur term reads too many points");
+  std::vector<double> cd((size_t)n * m, 0.0), M((size_t)n * m, 0.0);
+  for (int r = 0; r < n; ++r)
+    for (int64_t e = C.ptr[r]; e < C.ptr[r + 1]; ++e) {
+      const int q = (int)(std::lower_bound(ucol.begin(), ucol.end(), C.col[e]) - ucol.begin());
+      cd[(size_t)r * m + q] += C.val[e];
+    }
+  for (int r = 0; r < n; ++r)
+    for (int k = 0; k < n; ++k) {
+      const double a = inv[(size_t)r * n + k];
+      if (a == 0.0) continue;
+      const double* src = &cd[(size_t)k * m];
+      double* dst = &M[(size_t)r * m];
+      for (int q = 0; q < m; ++q) dst[q] += a * src[q];
+    }
+  std::vector<int64_t> mcol(m);
+  for (int q = 0; q < m; ++q) mcol[q] = field_index(ucol[q]);
+  rd.mcols.upload(mcol, st);
+  rd.mmat.upload(M, st);
+  rd.mcount = m;
+  build_band_tables(h, rd, rows, C);
+}
+
+// Regular-row coefficients of the residual kernels (see ResidualCoef): the pressure operator
+// (solver/optimized_ghost_cell.py:80-107, A = D G with the outlet -2/dx) and the Helmholtz
+// rows I - c L, c = dt nu / 2 (raw_l of solver/optimized_ghost_cell.py:116-123).
+ResidualCoef residual_coef(const gm::Geometry& g, int kind, double hc) {
+  ResidualCoef r{};
+  const double idx2 = 1.0 / (g.dx * g.dx), idy2 = 1.0 / (g.dy * g.dy), irho = 1.0 / g.rho;
+  if (kind == 0) {
+    const double mx[3] = {-1.0, -2.0, -3.0}, my[2] = {-1.0, -2.0};
+    for (int ic = 0; ic < 3; ++ic)
+      for (int jc = 0; jc < 2; ++jc) r.cc[ic][jc] = (mx[ic] * idx2 + my[jc] * idy2) * irho;
+    for (int ic = 0; ic < 3; ++ic) r.cw[ic] = idx2 * irho;
+    r.ce = idx2 * irho;
+    r.cy = idy2 * irho;
+  } else if (kind == 1) {
+    const double my[2] = {-3.0, -2.0};
+    for (int ic = 0; ic < 3; ++ic)
+      for (int jc = 0; jc < 2; ++jc) r.cc[ic][jc] = 1.0 - hc * (-2.0 * idx2 + my[jc] * idy2);
+    r.cw[0] = r.cw[1] = -hc * idx2;
+    r.cw[2] = -hc * (2.0 * idx2);  // outlet face: raw_l doubles the west coupling
+    r.ce = -hc * idx2;
+    r.cy = -hc * idy2;
+  } else {
+    const double mx[3] = {-3.0, -2.0, -1.0};
+    for (int ic = 0; ic < 3; ++ic)
+      for (int jc = 0; jc < 2; ++jc) r.cc[ic][jc] = 1.0 - hc * (mx[ic] * idx2 - 2.0 * idy2);
+    for (int ic = 0; ic < 3; ++ic) r.cw[ic] = -hc * idx2;
+    r.ce = -hc * idx2;
+    r.cy = -hc * idy2;
+  }
+  return r;
 }
 
 void fill_case_dev(gm_handle* h) {
   const gm::Geometry& g = h->g;
   CaseDev& c = h->cd;
   c.nx = g.nx; c.ny = g.ny; c.dx = g.dx; c.dy = g.dy; c.rho = g.rho; c.nu = g.nu;
+  c.idx = 1.0 / g.dx; c.idy = 1.0 / g.dy;
+  c.idx2 = 1.0 / (g.dx * g.dx); c.idy2 = 1.0 / (g.dy * g.dy);
+  c.gx = (1.0 / g.dx) / g.rho; c.gy = (1.0 / g.dy) / g.rho;
+  c.iarea = 1.0 / (g.dx * g.dy); c.irho = 1.0 / g.rho;
   c.usize = g.usize; c.vsize = g.vsize; c.psize = g.psize;
   c.cls_u = h->cls_u; c.cls_v = h->cls_v; c.cls_p = h->cls_p.p;
   c.inlet = h->inlet.p;
@@ -435,6 +688,13 @@ void fill_case_dev(gm_handle* h) {
   c.su_ptr = h->su_ptr.p; c.su_col = h->su_col.p; c.su_val = h->su_val.p;
   c.sv_ptr = h->sv_ptr.p; c.sv_col = h->sv_col.p; c.sv_val = h->sv_val.p;
   c.nwx = h->nwx.p; c.nwy = h->nwy.p; c.nxx = h->nxx.p; c.nyy = h->nyy.p;
+  c.surf_part = h->surf_part.p; c.surf_ticket = h->surf_ticket.p;
+  h->rcoef[0] = residual_coef(g, 0, 0.0);
+  if (h->helm_ready) {
+    const double hc = (0.5 * h->helm_dt) * g.nu;
+    h->rcoef[1] = residual_coef(g, 1, hc);
+    h->rcoef[2] = residual_coef(g, 2, hc);
+  }
   c.D = g.D; c.U_ref = g.U_ref;
 }
 
@@ -513,31 +773,67 @@ void ghost_p(gm_handle* h, double* P, const Gate& gt) {
 // In the FP32 mode every application of the inverse runs in FP32 and the residual
 // b - A x in FP64, so the refinement sweeps recover an FP64 solution.
 // One application of the (FP64 or FP32) boundary-corrected inverse: x = [x +] T^{-1} r - T^{-1} U S^{-1} C T^{-1} r.
-void apply_inverse(gm_handle* h, RectDev& rd, int kind, const double* r, double* x, bool accumulate, double* first,
-                   double* w2, const Gate& gt, cudaStream_t st) {
+// x = [x +] A_rect^{-1} r with the boundary Schur correction (solver/pressure_schur.py:75-124):
+//   S1 = Y^{-1} F_x r (spectral, all rows); first = F_x^{-1} S1 on the rows the C rows read;
+//   c = S^{-1} C first; B = band solve of F_x (U c); x = F_x^{-1} (S1 - B extended by phi/psi).
+template <typename T>
+void schur_inverse(gm_handle* h, RectDev& rd, const TransformTables& tt, const void* r, bool r_f32, double* x,
+                   bool accumulate, T* spectral, T* first, T* band, double* w2, const Gate& g, cudaStream_t st) {
+  const RectView& v = rd.view;
+  const YCorr<T> none{nullptr, nullptr, nullptr, 0, -1};
+  if constexpr (sizeof(T) == 4) {
+    if (r_f32)
+      launch_xpass<float, float, float>(tt, false, 0, v.rows, (const float*)r, v.base, v.pitch, v.cls, spectral, 0,
+                                        v.cols, nullptr, nullptr, none, g, st);
+    else
+      launch_xpass<float, double, float>(tt, false, 0, v.rows, (const double*)r, v.base, v.pitch, v.cls, spectral, 0,
+                                         v.cols, nullptr, nullptr, none, g, st);
+  } else {
+    launch_xpass<double, double, double>(tt, false, 0, v.rows, (const double*)r, v.base, v.pitch, v.cls, spectral, 0,
+                                         v.cols, nullptr, nullptr, none, g, st);
+  }
+  launch_ysolve<T>(tt, v.cols, v.rows, spectral, g, st);
+  YCorr<T> corr = none;
+  if (rd.rank > 0) {
+    launch_xpass<T, T, T>(tt, true, tt.cj0, tt.cj1 - tt.cj0 + 1, spectral, 0, v.cols, nullptr, first, v.base, v.pitch,
+                          nullptr, nullptr, none, g, st);
+    launch_schur<T>(first, rd.rank, rd.mcount, rd.mcols.p, rd.mmat.p, rd.rows.p, w2, g, st);
+    launch_xpass<T, double, T>(tt, false, tt.bj0, tt.bj1 - tt.bj0 + 1, w2, v.base, v.pitch, nullptr, band,
+                               -(int64_t)tt.bj0 * v.cols, v.cols, nullptr, nullptr, none, g, st);
+    launch_yband<T>(tt, v.cols, band, g, st);
+    corr = YCorr<T>{band, (const T*)tt.phi, (const T*)tt.psi, tt.bj0, tt.bj1};
+  }
+  launch_xpass<T, T, double>(tt, true, 0, v.rows, spectral, 0, v.cols, nullptr, x, v.base, v.pitch, v.cls,
+                             accumulate ? x : nullptr, corr, g, st);
+}
+
+// r is the FP64 right-hand side, or in the FP32 mode the FP32 residual when r_f32 is set
+void apply_inverse(gm_handle* h, int lane, RectDev& rd, int kind, const void* r, bool r_f32, double* x,
+                   bool accumulate, double* first, double* w2, const Gate& gt, cudaStream_t st) {
   if (h->precision == 1) {
     float* first32 = kind == 0 ? h->pfirst32.p : h->ffirst32.p;
-    launch_rect_inverse_f32(rd.tt32, rd.view, r, true, h->spectral32.p, first32, gt, st);
-    launch_schur_f32(first32, rd.view, rd.rank, rd.rows.p, rd.cptr.p, rd.ccol.p, rd.cval.p, rd.sinv.p, w2, gt, st);
-    launch_rect_inverse_f32_final(rd.tt32, rd.view, w2, h->spectral32.p, x, first32, accumulate ? x : nullptr, gt,
-                                  st);
+    float* spec = lane == 0 ? h->spectral32.p : h->spectral32_b.p;
+    schur_inverse<float>(h, rd, rd.tt32, r, r_f32, x, accumulate, spec, first32, rd.band32.p, w2, gt, st);
   } else {
-    launch_rect_inverse(rd.tt, rd.view, r, true, h->spectral.p, first, nullptr, nullptr, gt, st);
-    launch_schur(first, rd.view, rd.rank, rd.rows.p, rd.cptr.p, rd.ccol.p, rd.cval.p, rd.sinv.p, w2, gt, st);
-    launch_rect_inverse(rd.tt, rd.view, w2, false, h->spectral.p, x, first, accumulate ? x : nullptr, gt, st);
+    double* spec = lane == 0 ? h->spectral.p : h->spectral_b.p;
+    schur_inverse<double>(h, rd, rd.tt, r, false, x, accumulate, spec, first, rd.band.p, w2, gt, st);
   }
 }
 
 // The same solve while the step is being captured into a CUDA graph: the refinement
 // sweeps form a WHILE conditional node whose body runs only while the residual check
 // exceeds the target, so no sweep kernel launches when none is needed.
-void schur_solve_graph(gm_handle* h, RectDev& rd, int kind, double hc, const double* b, double* x, double* res,
-                       double* first, double* w2, int slot) {
-  cudaStream_t st = h->st;
+void schur_solve_graph(gm_handle* h, int lane, RectDev& rd, int kind, double hc, const double* b, double* x,
+                       double* res, double* first, double* w2, int slot) {
+  cudaStream_t st = lane == 0 ? h->st : h->st2;
+  cudaStream_t body_st = lane == 0 ? h->st_body : h->st2_body;
   SolveCtl* sc = &h->ctl.p->solve[slot];
   Gate g0 = gate_of(h, slot, 0);
-  apply_inverse(h, rd, kind, b, x, false, first, w2, g0, st);
-  launch_residual(h->cd, kind, hc, b, x, res, sc, 0, true, g0, st);
+  const bool f32 = h->precision == 1;
+  void* resb = f32 ? (void*)(kind == 0 ? h->pres32.p : h->fres32.p) : (void*)res;
+  (void)hc;
+  apply_inverse(h, lane, rd, kind, b, false, x, false, first, w2, g0, st);
+  launch_residual(h->cd, h->rcoef[kind], kind, b, x, resb, f32, sc, 0, true, g0, st);
   cudaStreamCaptureStatus cs;
   cudaGraph_t graph;
   const cudaGraphNode_t* deps = nullptr;
@@ -556,28 +852,45 @@ void schur_solve_graph(gm_handle* h, RectDev& rd, int kind, double hc, const dou
   CK(cudaGraphAddNode(&cnode, graph, deps, nullptr, nd, &cp));
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CK(cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
-  CK(cudaStreamBeginCaptureToGraph(h->st_body, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  CK(cudaStreamBeginCaptureToGraph(body_st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
   long long c0 = kernel_launch_count();
-  apply_inverse(h, rd, kind, res, x, true, first, w2, g0, h->st_body);
-  launch_residual(h->cd, kind, hc, b, x, res, sc, -1, false, g0, h->st_body);
-  launch_refine_decide(h->ctl.p, slot, h->nchk, cond, h->st_body);
-  h->body_nodes_capture = kernel_launch_count() - c0;
-  CK(cudaStreamEndCapture(h->st_body, &body));
+  apply_inverse(h, lane, rd, kind, resb, f32, x, true, first, w2, g0, body_st);
+  launch_residual(h->cd, h->rcoef[kind], kind, b, x, resb, f32, sc, -1, false, g0, body_st);
+  launch_refine_decide(h->ctl.p, slot, h->nchk, cond, body_st);
+  h->body_nodes_slot[slot] = kernel_launch_count() - c0;
+  CK(cudaStreamEndCapture(body_st, &body));
+  if (f32 && kind == 0) launch_pressure_bound(h->cd, h->rcoef[0], b, x, sc, h->nchk, g0, st);
 }
 
-void schur_solve(gm_handle* h, RectDev& rd, int kind, double hc, const double* b, double* x, double* res,
+// One solve A x = b with the FFT + boundary Schur inverse and refinement sweeps to the
+// reference's residual target (solver/pressure_schur.py:16-72, direct branch).
+void schur_solve(gm_handle* h, int lane, RectDev& rd, int kind, double hc, const double* b, double* x, double* res,
                  double* first, double* w2, int slot) {
   if (h->capturing) {
-    schur_solve_graph(h, rd, kind, hc, b, x, res, first, w2, slot);
+    schur_solve_graph(h, lane, rd, kind, hc, b, x, res, first, w2, slot);
     return;
   }
-  cudaStream_t st = h->st;
+  cudaStream_t st = lane == 0 ? h->st : h->st2;
   SolveCtl* sc = &h->ctl.p->solve[slot];
+  const bool f32 = h->precision == 1;
+  void* resb = f32 ? (void*)(kind == 0 ? h->pres32.p : h->fres32.p) : (void*)res;
   for (int sweep = 0; sweep < h->nchk; ++sweep) {
     Gate gt = gate_of(h, slot, sweep);
-    apply_inverse(h, rd, kind, sweep == 0 ? b : res, x, sweep > 0, first, w2, gt, st);
-    launch_residual(h->cd, kind, hc, b, x, res, sc, sweep, sweep == 0, gt, st);
+    apply_inverse(h, lane, rd, kind, sweep == 0 ? (const void*)b : (const void*)resb, sweep > 0 && f32, x, sweep > 0,
+                  first, w2, gt, st);
+    launch_residual(h->cd, h->rcoef[kind], kind, b, x, resb, f32, sc, sweep, sweep == 0, gt, st);
+    if (h->host_refine && sweep + 1 < h->nchk) {
+      // the rule of k_refine_decide, read back on the host
+      SolveCtl hs;
+      CK(cudaMemcpyAsync(&hs, sc, sizeof hs, cudaMemcpyDeviceToHost, st));
+      int err = 0;
+      CK(cudaMemcpyAsync(&err, &h->ctl.p->err, sizeof err, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      const double bm = bits2d(hs.bmax), tg = std::max(1e-10, 32 * 2.220446049250313e-16 * std::max(1.0, bm));
+      if (err || !(bits2d(hs.rmax[sweep]) > tg)) break;
+    }
   }
+  if (f32 && kind == 0) launch_pressure_bound(h->cd, h->rcoef[0], b, x, sc, h->nchk, gate_of(h), st);
 }
 
 // project(q, dt) (solver/optimized_ghost_cell.py:218-229); q is a face grid with active values
@@ -587,7 +900,7 @@ void project(gm_handle* h, double* q, double dt, double* out, double* phi, int s
   launch_set_inlet(h->cd, q, false, st);
   ghost_faces(h, q, g0);
   launch_divergence(h->cd, q, h->prhs.p, dt, nullptr, nullptr, 1, g0, st);
-  schur_solve(h, h->rp, 0, 0.0, h->prhs.p, phi, h->pres.p, h->pfirst.p, h->pw2.p, slot);
+  schur_solve(h, 0, h->rp, 0, 0.0, h->prhs.p, phi, h->pres.p, h->pfirst.p, h->pw2.p, slot);
   launch_gate_pressure(h->ctl.p, slot, h->nchk, st);
   ghost_p(h, phi, g0);
   launch_project_update(h->cd, q, phi, dt, out, nullptr, g0, st);
@@ -666,11 +979,22 @@ void step_once(gm_handle* h, double dt, int screen) {
     ma.prev = h->hist.p;
     ma.now = h->now.p;
     ma.out = h->rhs.p;
+    if (h->precision == 1) {
+      launch_shadow(h->U.p, h->U32.p, h->F, h->phalf.p, h->P32.p, h->Pn, g0, st);
+      ma.U32 = h->U32.p;
+      ma.P32 = h->P32.p;
+    }
     momentum(h, ma, g0);
   }
   // CN Helmholtz solves for u and v (solver/optimized_ghost_cell.py:247-254)
-  schur_solve(h, h->ru, 1, hc, h->rhs.p, h->star.p, h->fres.p, h->ffirst.p, h->fw2.p, S_HELM_U);
-  schur_solve(h, h->rv, 2, hc, h->rhs.p, h->star.p, h->fres.p, h->ffirst.p, h->fw2.p, S_HELM_V);
+  // (independent systems on disjoint parts of the face arrays: u on this stream, v on the
+  // second lane, joined before the momentum gate)
+  CK(cudaEventRecord(h->ev_fork, st));
+  CK(cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
+  schur_solve(h, 0, h->ru, 1, hc, h->rhs.p, h->star.p, h->fres.p, h->ffirst.p, h->fw2.p, S_HELM_U);
+  schur_solve(h, 1, h->rv, 2, hc, h->rhs.p, h->star.p, h->fres.p, h->ffirst.p, h->fw2.p, S_HELM_V);
+  CK(cudaEventRecord(h->ev_join, h->st2));
+  CK(cudaStreamWaitEvent(st, h->ev_join, 0));
   launch_gate_momentum(h->ctl.p, h->nchk, st);
   // projection of the CN velocity, defect correction and the pressure increment
   project(h, h->star.p, dt, h->Unext.p, h->pphi.p, S_P1, 1);
@@ -705,6 +1029,7 @@ cudaGraphExec_t step_graph(gm_handle* h, double dt) {
   if (slot->exec) { cudaGraphExecDestroy(slot->exec); slot->exec = nullptr; }
   const long long c0 = kernel_launch_count();
   long long body_total = 0;
+  std::fill(h->body_nodes_slot, h->body_nodes_slot + 5, 0LL);
   h->capturing = true;
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
@@ -721,8 +1046,10 @@ cudaGraphExec_t step_graph(gm_handle* h, double dt) {
   CK(cudaStreamEndCapture(h->st, &g));
   const long long captured = kernel_launch_count() - c0;
   kernel_launch_adjust(-captured);
-  body_total = 4 * h->body_nodes_capture;  // four refinement loops per steady step
-  slot->body_nodes = h->body_nodes_capture;
+  for (int q = 0; q < 5; ++q) {
+    body_total += h->body_nodes_slot[q];
+    slot->body_nodes[q] = h->body_nodes_slot[q];
+  }
   slot->outer_nodes = captured - body_total;
   cudaGraphExec_t ex = nullptr;
   cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
@@ -855,6 +1182,7 @@ int gm_create(const gm_config* cfg, gm_handle** out) {
   if (cfg->nx % 2 != 0) { g_create_error = "odd nx is not supported by the type-IV transform"; return GM_ENOTIMPL; }
   int ec = 0;
   if (!gm::build_geometry(g, ec)) { g_create_error = g.error; return ec ? ec : GM_EVALUE; }
+  if (g.usize + g.vsize >= (int64_t(1) << 31)) { g_create_error = "grids of 2^31 or more faces are not supported"; return GM_EVALUE; }
   gm_handle* H = h.get();
   int rc = run_guarded(nullptr, [&] {
     int ndev = 0;
@@ -897,6 +1225,9 @@ int gm_create(const gm_config* cfg, gm_handle** out) {
     H->sv_ptr.upload(g.dvdn.ptr, st); H->sv_col.upload(g.dvdn.col, st); H->sv_val.upload(g.dvdn.val, st);
     H->nwx.upload(g.normal_wx, st); H->nwy.upload(g.normal_wy, st);
     H->nxx.upload(g.normal_x, st); H->nyy.upload(g.normal_y, st);
+    H->surf_part.alloc(4 * (size_t)std::max(1, g.n_surface));
+    H->surf_ticket.alloc(1);
+    H->surf_ticket.zero(st);
     H->d_ui.upload(g.ui, st); H->d_vi.upload(g.vi, st); H->d_pi.upload(g.pi, st);
     for (DBuf<double>* b : {&H->U, &H->Unext, &H->hist, &H->now, &H->rhs, &H->star, &H->fres, &H->ffirst, &H->fw2,
                             &H->fmid, &H->fhalf, &H->faction, &H->fproj, &H->fproj2, &H->ftmp}) {
@@ -909,8 +1240,16 @@ int gm_create(const gm_config* cfg, gm_handle** out) {
       b->zero(st);
     }
     H->spectral.alloc(std::max<int64_t>(H->Pn, (int64_t)g.ny * g.nx));
+    H->spectral_b.alloc(H->spectral.n);
     if (H->precision == 1) {
       H->spectral32.alloc(H->spectral.n);
+      H->spectral32_b.alloc(H->spectral.n);
+      H->pres32.alloc(H->Pn);
+      H->pres32.zero(st);
+      H->fres32.alloc(H->F);
+      H->fres32.zero(st);
+      H->U32.alloc(H->F);
+      H->P32.alloc(H->Pn);
       H->ffirst32.alloc(H->F);
       H->ffirst32.zero(st);
       H->pfirst32.alloc(H->Pn);
@@ -925,7 +1264,12 @@ int gm_create(const gm_config* cfg, gm_handle** out) {
     H->counter.zero(st);
     CK(cudaMallocHost(&H->host_ring, gm_handle::RING_CAP * sizeof(StepCtl)));
     CK(cudaStreamCreateWithFlags(&H->st_body, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&H->st2, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&H->st2_body, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&H->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&H->ev_join, cudaEventDisableTiming));
     if (const char* e = std::getenv("GHOSTMAC_NO_GRAPHS")) H->use_graphs = !(e[0] == '1');
+
     H->state_max.alloc(2);
     H->state_max.zero(st);
     CK(cudaMallocHost(&H->host_ctl, sizeof(StepCtl)));
@@ -969,7 +1313,12 @@ int gm_destroy(gm_handle* h) {
   if (h->host_ring) cudaFreeHost(h->host_ring);
   for (auto& gr : h->graphs)
     if (gr.exec) cudaGraphExecDestroy(gr.exec);
+  if (h->st2) cudaStreamSynchronize(h->st2);
   if (h->st_body) cudaStreamDestroy(h->st_body);
+  if (h->st2) cudaStreamDestroy(h->st2);
+  if (h->st2_body) cudaStreamDestroy(h->st2_body);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
   cudaStream_t st = h->st;
   bool own = h->own_stream;
   delete h;
@@ -1150,6 +1499,8 @@ int gm_step(gm_handle* h, double dt, int32_t n_steps, int64_t first_step_index, 
   if (!h) return GM_EVALUE;
   if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
   if (!(std::isfinite(dt) && dt > 0) || n_steps <= 0) { h->err = "dt must be finite and positive"; return GM_EVALUE; }
+  const char* hr = std::getenv("GHOSTMAC_HOST_REFINE");
+  h->host_refine = hr && hr[0] == '1';
   return run_guarded(h, [&] {
     ensure_helmholtz(h, dt);
     cudaStream_t st = h->st;
@@ -1184,9 +1535,8 @@ int gm_step(gm_handle* h, double dt, int32_t n_steps, int64_t first_step_index, 
         long long nodes = 0;
         for (int k = 0; k < batch; ++k) {
           const StepCtl& c = h->host_ring[k];
-          int sweeps = 0;
-          for (int sl = 0; sl < 5; ++sl) sweeps += c.solve[sl].k;
-          nodes += gr.outer_nodes + gr.body_nodes * sweeps;
+          nodes += gr.outer_nodes;
+          for (int sl = 0; sl < 5; ++sl) nodes += gr.body_nodes[sl] * c.solve[sl].k;
         }
         kernel_launch_adjust(nodes);
       }
@@ -1356,7 +1706,7 @@ int gm_pressure_solve(gm_handle* h, const double* rhs, double* phi, gm_solve_inf
     CK(cudaMemsetAsync(h->prhs.p, 0, h->Pn * sizeof(double), st));
     launch_scatter(b, h->d_pi.p, np, h->prhs.p, st);
     CK(cudaMemsetAsync(h->ctl.p, 0, sizeof(StepCtl), st));
-    schur_solve(h, h->rp, 0, 0.0, h->prhs.p, h->pphi.p, h->pres.p, h->pfirst.p, h->pw2.p, S_P1);
+    schur_solve(h, 0, h->rp, 0, 0.0, h->prhs.p, h->pphi.p, h->pres.p, h->pfirst.p, h->pw2.p, S_P1);
     launch_gate_pressure(h->ctl.p, S_P1, h->nchk, st);
     CK(cudaMemcpyAsync(h->host_ctl, h->ctl.p, sizeof(StepCtl), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -1382,7 +1732,8 @@ int gm_rectangle_solve(gm_handle* h, int32_t kind, double dt, const double* b, d
     dense.pitch = dense.cols;
     dense.cls = nullptr;
     DevOut o(h, 1, x, n);
-    launch_rect_inverse(rd.tt, dense, bd, false, h->spectral.p, o.dev, nullptr, nullptr, Gate{nullptr, 0, 0}, h->st);
+    plain_inverse<double, double, double>(rd.tt, dense, bd, false, h->spectral.p, o.dev, nullptr, nullptr,
+                                          Gate{nullptr, 0, 0}, h->st);
     o.finish();
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->st));
@@ -1437,13 +1788,14 @@ extern "C" {
 
 int64_t gm_kernel_launches(void) { return (int64_t)kernel_launch_count(); }
 
-int gm_kernel_timing(int32_t kernel_class, int32_t enable, double* total_ms, int64_t* count) {
-  if (enable) ktimer_enable(kernel_class);
-  double t = 0;
+int gm_kernel_timing(int32_t kernel_class, int32_t enable, double* total_ms, int64_t* count, double* bytes) {
+  if (enable) ktimer_enable(1);
+  double t = 0, by = 0;
   long long n = 0;
-  ktimer_read(&t, &n);
+  ktimer_read(kernel_class, &t, &n, &by);
   if (total_ms) *total_ms = t;
   if (count) *count = (int64_t)n;
+  if (bytes) *bytes = by;
   if (!enable && kernel_class == 0) ktimer_enable(0);
   return GM_OK;
 }
@@ -1465,7 +1817,8 @@ struct gm_batch {
     std::vector<const double*> key;
     std::vector<long long> gens;
     double dt = 0;
-    std::vector<long long> outer, body;  // per-case kernel node counts
+    std::vector<long long> outer;               // per-case kernel nodes outside the refinement loops
+    std::vector<std::array<long long, 5>> body;  // per-case kernel nodes of one sweep, per solve slot
   } graphs[2];
   std::string err;
 };
@@ -1494,7 +1847,7 @@ gm_batch::Graph& batch_graph(gm_batch* b, double dt) {
     slot->exec = nullptr;
   }
   slot->outer.assign(b->cases.size(), 0);
-  slot->body.assign(b->cases.size(), 0);
+  slot->body.assign(b->cases.size(), std::array<long long, 5>{});
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal));
   try {
@@ -1503,13 +1856,18 @@ gm_batch::Graph& batch_graph(gm_batch* b, double dt) {
       gm_handle* h = b->cases[c];
       CK(cudaStreamWaitEvent(h->st, b->fork, 0));
       const long long c0 = kernel_launch_count();
+      std::fill(h->body_nodes_slot, h->body_nodes_slot + 5, 0LL);
       h->capturing = true;
       step_once(h, dt, -1);
       h->capturing = false;
       const long long captured = kernel_launch_count() - c0;
       kernel_launch_adjust(-captured);
-      slot->body[c] = h->body_nodes_capture;
-      slot->outer[c] = captured - 4 * h->body_nodes_capture;
+      long long body_total = 0;
+      for (int q = 0; q < 5; ++q) {
+        slot->body[c][q] = h->body_nodes_slot[q];
+        body_total += h->body_nodes_slot[q];
+      }
+      slot->outer[c] = captured - body_total;
       CK(cudaEventRecord(b->join[c], h->st));
       CK(cudaStreamWaitEvent(b->root, b->join[c], 0));
     }
@@ -1577,6 +1935,8 @@ int gm_batch_step(gm_batch* b, double dt, int32_t n_steps, int64_t first_step_in
   if (!(std::isfinite(dt) && dt > 0) || n_steps <= 0) { b->err = "dt must be finite and positive"; return GM_EVALUE; }
   const int nc = (int)b->cases.size();
   if (steps_done) std::fill(steps_done, steps_done + nc, 0);
+  const char* hr = std::getenv("GHOSTMAC_HOST_REFINE");
+  for (gm_handle* h : b->cases) h->host_refine = hr && hr[0] == '1';
   int first_error = GM_OK;
   try {
     for (gm_handle* h : b->cases) {
@@ -1608,6 +1968,10 @@ int gm_batch_step(gm_batch* b, double dt, int32_t n_steps, int64_t first_step_in
       }
       for (gm_handle* h : b->cases)
         CK(cudaMemcpyAsync(h->host_ring, h->ring.p, batch * sizeof(StepCtl), cudaMemcpyDeviceToHost, h->st));
+      if (!steady) {
+        for (gm_handle* h : b->cases) CK(cudaStreamSynchronize(h->st));
+        ktimer_collect();
+      }
       for (int c = 0; c < nc; ++c) {
         gm_handle* h = b->cases[c];
         CK(cudaStreamSynchronize(h->st));
@@ -1621,9 +1985,8 @@ int gm_batch_step(gm_batch* b, double dt, int32_t n_steps, int64_t first_step_in
         if (steady) {
           const gm_batch::Graph& gr = b->graphs[0].exec ? b->graphs[0] : b->graphs[1];
           for (int k = 0; k < batch; ++k) {
-            int sweeps = 0;
-            for (int sl = 0; sl < 5; ++sl) sweeps += h->host_ring[k].solve[sl].k;
-            nodes += gr.outer[c] + gr.body[c] * sweeps;
+            nodes += gr.outer[c];
+            for (int sl = 0; sl < 5; ++sl) nodes += gr.body[c][sl] * h->host_ring[k].solve[sl].k;
           }
         }
         if (steps_done) steps_done[c] = s + good;

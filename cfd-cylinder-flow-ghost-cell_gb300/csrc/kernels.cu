@@ -76,107 +76,206 @@ long long kernel_launch_count() { return g_launches.load(); }
 // captured nodes and adds the nodes a graph replay executed.
 void kernel_launch_adjust(long long delta) { g_launches.fetch_add(delta, std::memory_order_relaxed); }
 
-// Optional CUDA-event timing of one kernel class on its own stream (used by the
-// benchmark to time the dominant kernel inside the timed region).
+// Optional CUDA-event timing of every launch, summed per kernel class (used by the
+// benchmark for its per-class breakdown and the dominant kernel's launch time).  Classes:
+// 1 x pass, 2 column solves, 3 momentum, 4 residual, 5 Schur GEMV, 6 projection pieces,
+// 7 defect / pressure output, 8 ghost rows, 9 forces / maxima, 10 gates and loop control.
 namespace {
 struct KTimer {
-  int cls = 0;
+  bool on = false;
   std::vector<cudaEvent_t> ev;
+  std::vector<int> cls;
   int used = 0;
-  double total_ms = 0;
-  long long count = 0;
+  std::vector<double> bytes;
+  double total_ms[KT_CLASSES] = {};
+  double total_bytes[KT_CLASSES] = {};
+  long long count[KT_CLASSES] = {};
 };
 KTimer g_kt;
 }  // namespace
-static inline void kt_mark(int cls, cudaStream_t st) {
-  if (g_kt.cls != cls || g_kt.used >= (int)g_kt.ev.size()) return;
+// begin and end marks of one launch; the end mark carries the launch's algorithmic bytes
+static inline void kt_mark(int cls, cudaStream_t st, double bytes = 0.0) {
+  if (!g_kt.on || g_kt.used >= (int)g_kt.ev.size()) return;
+  g_kt.cls[g_kt.used] = cls;
+  g_kt.bytes[g_kt.used] = bytes;
   cudaEventRecord(g_kt.ev[g_kt.used++], st);
 }
-void ktimer_enable(int cls) {
+void ktimer_enable(int on) {
   if (g_kt.ev.empty()) {
-    g_kt.ev.resize(1024);
+    g_kt.ev.resize(4096);
+    g_kt.cls.resize(4096);
+    g_kt.bytes.resize(4096);
     for (auto& e : g_kt.ev) cudaEventCreate(&e);
   }
-  g_kt.cls = cls;
+  g_kt.on = on != 0;
   g_kt.used = 0;
-  g_kt.total_ms = 0;
-  g_kt.count = 0;
+  for (int k = 0; k < KT_CLASSES; ++k) { g_kt.total_ms[k] = 0; g_kt.total_bytes[k] = 0; g_kt.count[k] = 0; }
 }
-// Folds the recorded pairs into the totals (the stream must be synchronised).
+// Folds the recorded pairs (begin and end of one launch are consecutive) into the totals;
+// the streams must be synchronised.
 void ktimer_collect() {
   for (int i = 0; i + 1 < g_kt.used; i += 2) {
     float ms = 0;
     if (cudaEventElapsedTime(&ms, g_kt.ev[i], g_kt.ev[i + 1]) == cudaSuccess) {
-      g_kt.total_ms += ms;
-      g_kt.count += 1;
+      const int c = g_kt.cls[i];
+      if (c >= 0 && c < KT_CLASSES) {
+        g_kt.total_ms[c] += ms;
+        g_kt.total_bytes[c] += g_kt.bytes[i + 1];
+        g_kt.count[c] += 1;
+      }
     }
   }
   cudaGetLastError();
   g_kt.used = 0;
 }
-bool ktimer_active() { return g_kt.cls != 0; }
-void ktimer_read(double* total_ms, long long* count) {
-  *total_ms = g_kt.total_ms;
-  *count = g_kt.count;
+bool ktimer_active() { return g_kt.on; }
+void ktimer_read(int cls, double* total_ms, long long* count, double* bytes) {
+  const bool ok = cls >= 0 && cls < KT_CLASSES;
+  *total_ms = ok ? g_kt.total_ms[cls] : 0.0;
+  *count = ok ? g_kt.count[cls] : 0;
+  *bytes = ok ? g_kt.total_bytes[cls] : 0.0;
 }
 
 // ---------------------------------------------------------------------------
 // separable inverse: x pass (rows) and y pass (columns with eigenvalue scaling)
 // ---------------------------------------------------------------------------
-// Row transforms: one warp per line group (one line for the type-IV transforms, two
-// paired lines for the Makhoul transforms); each warp owns its shared-memory slice and
-// synchronises with __syncwarp only.  Masked load, optional fused epilogue
-//   out = active ? add + (sub - T b) : 0.
+// Row transforms.  A group of `gthreads` threads (one warp, or whole warps on a named
+// barrier) transforms one line group -- two paired lines for the Makhoul and DST-I
+// transforms, one line for the type-IV transforms -- and a block holds `gpb` groups.
+// Rows r0 .. r0+nr-1 are transformed.  Masked load with the optional spectral correction
+// of the boundary term (YCorr); masked store with the optional epilogue out = add + v.
 template <typename T>
-__host__ __device__ inline size_t xpass_warp_smem(int type, int n) {
+__host__ __device__ inline size_t xpass_group_smem(int type, int n) {
   const int lpw = r2r_paired(type) ? 2 : 1;
   size_t stage = ((size_t)lpw * n * sizeof(T) + 15) / 16 * 16;
   return stage + 2 * (size_t)r2r_buffer_elems(type, n, lpw) * sizeof(cplx<T>);
 }
+size_t xpass_smem_per_group(int type, int n, bool fp32) {
+  return fp32 ? xpass_group_smem<float>(type, n) : xpass_group_smem<double>(type, n);
+}
 
-template <typename T, typename TI, typename TO, typename TS>
-__global__ void k_xpass(int n, int rows, int type, FftPlan plan, R2RTables<T> tb, const TI* __restrict__ in,
+static constexpr int XB = 4;  // loads batched per thread in the row passes
+template <typename T, typename TI, typename TO>
+__global__ void k_xpass(int n, int r0, int nr, int type, FftPlan plan, R2RTables<T> tb, const TI* __restrict__ in,
                         int64_t ibase, int64_t ipitch, const uint8_t* __restrict__ icls, TO* __restrict__ out,
-                        int64_t obase, int64_t opitch, const uint8_t* __restrict__ ocls, const TS* __restrict__ sub,
-                        const double* __restrict__ add, int wpb, Gate gate) {
+                        int64_t obase, int64_t opitch, const uint8_t* __restrict__ ocls, const double* __restrict__ add,
+                        YCorr<T> corr, int gthreads, int gpb, Gate gate) {
   if (!gate_open(gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int grp = threadIdx.x / gthreads, tid = threadIdx.x - grp * gthreads;
   const int lpw = r2r_paired(type) ? 2 : 1;
-  const int l0 = (blockIdx.x * wpb + warp) * lpw;
-  if (warp >= wpb || l0 >= rows) return;  // whole warps leave; no block barrier follows
-  const int nl = min(lpw, rows - l0);
-  unsigned char* mine = smem_raw + (size_t)warp * xpass_warp_smem<T>(type, n);
+  const int l0 = (blockIdx.x * gpb + grp) * lpw;
+  if (grp >= gpb || l0 >= nr) return;  // whole groups leave; every group has its own barrier
+  const int nl = min(lpw, nr - l0);
+  unsigned char* mine = smem_raw + (size_t)grp * xpass_group_smem<T>(type, n);
   T* stage = reinterpret_cast<T*>(mine);
-  size_t stage_bytes = ((size_t)lpw * n * sizeof(T) + 15) / 16 * 16;
+  const size_t stage_bytes = ((size_t)lpw * n * sizeof(T) + 15) / 16 * 16;
   cplx<T>* a = reinterpret_cast<cplx<T>*>(mine + stage_bytes);
   cplx<T>* b = a + r2r_buffer_elems(type, n, lpw);
-  const Grp G{lane, 32, true};
+  const Grp G{tid, gthreads, grp + 1};
   for (int l = 0; l < nl; ++l) {
-    const int64_t row = ibase + (int64_t)(l0 + l) * ipitch;
-    for (int e = lane; e < n; e += 32) {
-      TI v = in[row + e];
-      if (icls && !(icls[row + e] & CLS_ACTIVE)) v = (TI)0;
-      stage[l * n + e] = (T)v;
+    const int r = r0 + l0 + l;
+    const int64_t row = ibase + (int64_t)r * ipitch;
+    const T* cb = nullptr;  // band row that scales (or is) the correction of this row
+    const T* cf = nullptr;  // decay factors of this row (nullptr inside the band)
+    if (corr.band) {
+      if (r < corr.j0) {
+        cb = corr.band;
+        cf = corr.phi + (int64_t)r * n;
+      } else if (r > corr.j1) {
+        cb = corr.band + (int64_t)(corr.j1 - corr.j0) * n;
+        cf = corr.psi + (int64_t)(r - corr.j1 - 1) * n;
+      } else {
+        cb = corr.band + (int64_t)(r - corr.j0) * n;
+      }
+    }
+    // XB loads in flight per thread before the first shared-memory store
+    for (int e0 = tid; e0 < n; e0 += XB * gthreads) {
+      TI v[XB];
+      uint8_t mk[XB];
+      T cv[XB];
+#pragma unroll
+      for (int u = 0; u < XB; ++u) {
+        const int e = e0 + u * gthreads;
+        if (e < n) {
+          v[u] = in[row + e];
+          mk[u] = icls ? icls[row + e] : (uint8_t)CLS_ACTIVE;
+          cv[u] = cb ? (cf ? cf[e] * cb[e] : cb[e]) : (T)0;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < XB; ++u) {
+        const int e = e0 + u * gthreads;
+        if (e < n) stage[l * n + e] = ((mk[u] & CLS_ACTIVE) ? (T)v[u] : (T)0) - cv[u];
+      }
     }
   }
-  __syncwarp();
+  G.sync();
   r2r_lines<T>(type, stage, n, nl, a, b, plan, tb, G);
   for (int l = 0; l < nl; ++l) {
-    const int64_t row = obase + (int64_t)(l0 + l) * opitch;
-    for (int e = lane; e < n; e += 32) {
-      const int64_t fo = row + e;
-      T v = stage[l * n + e];
-      if (sub) {
-        if (ocls && !(ocls[fo] & CLS_ACTIVE)) { out[fo] = (TO)0; continue; }
-        double d = (double)((T)sub[fo] - v);
-        out[fo] = (TO)(add ? add[fo] + d : d);
-      } else {
-        out[fo] = (TO)v;
+    const int64_t row = obase + (int64_t)(r0 + l0 + l) * opitch;
+    for (int e0 = tid; e0 < n; e0 += XB * gthreads) {
+      uint8_t mk[XB];
+      double ad[XB];
+#pragma unroll
+      for (int u = 0; u < XB; ++u) {
+        const int64_t fo = row + e0 + u * gthreads;
+        if (e0 + u * gthreads < n) {
+          mk[u] = ocls ? ocls[fo] : (uint8_t)CLS_ACTIVE;
+          ad[u] = add ? add[fo] : 0.0;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < XB; ++u) {
+        const int e = e0 + u * gthreads;
+        if (e >= n) continue;
+        const int64_t fo = row + e;
+        if (!(mk[u] & CLS_ACTIVE)) {
+          out[fo] = (TO)0;
+        } else {
+          const T v = stage[l * n + e];
+          out[fo] = add ? (TO)(ad[u] + (double)v) : (TO)v;
+        }
       }
     }
   }
 }
+
+template <typename T, typename TI, typename TO>
+void launch_xpass(const TransformTables& tt, bool inverse, int r0, int nr, const TI* in, int64_t ibase,
+                  int64_t ipitch, const uint8_t* icls, TO* out, int64_t obase, int64_t opitch, const uint8_t* ocls,
+                  const double* add, const YCorr<T>& corr, const Gate& gate, cudaStream_t st) {
+  if (nr <= 0) return;
+  using C = cplx<T>;
+  const int type = inverse ? tt.tx_inv : tt.tx_fwd;
+  R2RTables<T> tb{(const C*)tt.Wx, (const C*)(inverse ? tt.prex_inv : tt.prex),
+                  (const C*)(inverse ? tt.postx_inv : tt.postx)};
+  const int lpw = r2r_paired(type) ? 2 : 1;
+  const int per_block = tt.xg_pb * lpw;
+  const unsigned grid = (unsigned)((nr + per_block - 1) / per_block);
+  note_launch();
+  kt_mark(1, st);
+  k_xpass<T, TI, TO><<<grid, tt.xg_threads * tt.xg_pb, tt.smem_x, st>>>(
+      tt.n, r0, nr, type, tt.plan_x, tb, in, ibase, ipitch, icls, out, obase, opitch, ocls, add, corr,
+      tt.xg_threads, tt.xg_pb, gate);
+  // algorithmic bytes: one read and one write per point, class maps, the added field and the
+  // correction band (tables of the decay factors once per point)
+  kt_mark(1, st, (double)nr * tt.n * (sizeof(TI) + sizeof(TO) + (icls ? 1 : 0) + (ocls ? 1 : 0) + (add ? 8 : 0) +
+                                      (corr.band ? sizeof(T) : 0)));
+}
+template void launch_xpass<double, double, double>(const TransformTables&, bool, int, int, const double*, int64_t,
+                                                   int64_t, const uint8_t*, double*, int64_t, int64_t,
+                                                   const uint8_t*, const double*, const YCorr<double>&, const Gate&,
+                                                   cudaStream_t);
+template void launch_xpass<float, double, float>(const TransformTables&, bool, int, int, const double*, int64_t,
+                                                 int64_t, const uint8_t*, float*, int64_t, int64_t, const uint8_t*,
+                                                 const double*, const YCorr<float>&, const Gate&, cudaStream_t);
+template void launch_xpass<float, float, float>(const TransformTables&, bool, int, int, const float*, int64_t,
+                                                int64_t, const uint8_t*, float*, int64_t, int64_t, const uint8_t*,
+                                                const double*, const YCorr<float>&, const Gate&, cudaStream_t);
+template void launch_xpass<float, float, double>(const TransformTables&, bool, int, int, const float*, int64_t,
+                                                 int64_t, const uint8_t*, double*, int64_t, int64_t, const uint8_t*,
+                                                 const double*, const YCorr<float>&, const Gate&, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // y direction of the separable inverse: for every x-mode kx the column system
@@ -184,84 +283,195 @@ __global__ void k_xpass(int n, int rows, int type, FftPlan plan, R2RTables<T> tb
 // (Helmholtz) is tridiagonal with a constant off-diagonal.  It is solved by a
 // partition method: P chunks of inner rows separated by interface rows; each
 // thread runs Thomas on one chunk with precomputed pivots, one thread per column
-// solves the tridiagonal interface system, then the chunks add their two spike
+// solves the interface system, and the chunk solutions take the spike
 // corrections.  Tables (rows x cols, same layout as the spectral array):
 //   inner rows:     t0 = 1/pivot, t1 = left spike v, t2 = right spike w
 //   interface rows: t0 = 1/pivot, t1 = sub-diagonal, t2 = sup/pivot of the interface system
+// The data and every coefficient of the two recurrences are staged in shared memory
+// first, so the dependent chains wait on shared-memory latency only.
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale, const T* __restrict__ t0,
                          const T* __restrict__ t1, const T* __restrict__ t2, T* __restrict__ S, int lpb, Gate gate) {
   if (!gate_open(gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* col = reinterpret_cast<T*>(smem_raw);  // lpb x n column values
+  const int ns = n | 1;                                  // odd stride between the columns
+  T* col = reinterpret_cast<T*>(smem_raw);              // lpb x ns values
+  T* piv = col + (size_t)lpb * ns;                       // lpb x ns reciprocal pivots
+  T* isub = piv + (size_t)lpb * ns;                      // lpb x YCHUNK_MAX interface coefficients
+  T* isup = isub + (size_t)lpb * YCHUNK_MAX;
   const int c0 = blockIdx.x * lpb;
   const int nl = min(lpb, cols - c0);
-  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
-    int l = t % nl, e = t / nl;
-    col[l * n + e] = S[(int64_t)e * cols + c0 + l] * scale;
+  const int P = ch.P;
+  for (int t0i = threadIdx.x; t0i < nl * n; t0i += 8 * blockDim.x) {
+    T sv[8], pvv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int t = t0i + u * blockDim.x;
+      if (t < nl * n) {
+        const int l = t % nl, e = t / nl;
+        const int64_t o = (int64_t)e * cols + c0 + l;
+        sv[u] = S[o];
+        pvv[u] = t0[o];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int t = t0i + u * blockDim.x;
+      if (t < nl * n) {
+        const int l = t % nl, e = t / nl;
+        col[l * ns + e] = sv[u] * scale;
+        piv[l * ns + e] = pvv[u];
+      }
+    }
+  }
+  for (int t = threadIdx.x; t < nl * (P - 1); t += blockDim.x) {
+    const int l = t % nl, q = t / nl;
+    const int64_t o = (int64_t)(ch.end[q] + 1) * cols + c0 + l;
+    isub[l * YCHUNK_MAX + q] = t1[o];
+    isup[l * YCHUNK_MAX + q] = t2[o];
   }
   __syncthreads();
-  const int P = ch.P;
   const int l = threadIdx.x % lpb, p = threadIdx.x / lpb;
   const bool work = l < nl && p < P;
   int a = 0, b = -1;
   if (work) { a = ch.start[p]; b = ch.end[p]; }
-  T* x = col + l * n;
+  T* x = col + l * ns;
+  const T* pv = piv + l * ns;
   const int64_t cc = c0 + l;
-  // phase 1: chunk-local Thomas -> g.  Consecutive threads take consecutive columns, so
-  // every pivot load of a warp is one contiguous row segment; unrolling lets the loads run
-  // ahead of the recurrence.
+  // phase 1: chunk-local Thomas
   if (work) {
     T prev = 0;
-#pragma unroll 8
     for (int j = a; j <= b; ++j) {
-      prev = (x[j] - gamma * prev) * t0[(int64_t)j * cols + cc];
+      prev = (x[j] - gamma * prev) * pv[j];
       x[j] = prev;
     }
     T next = x[b];
-#pragma unroll 8
     for (int j = b - 1; j >= a; --j) {
-      next = x[j] - (gamma * t0[(int64_t)j * cols + cc]) * next;
+      next = x[j] - (gamma * pv[j]) * next;
       x[j] = next;
     }
   }
   __syncthreads();
   // phase 2: interface system, one thread per column
   if (p == 0 && l < nl && P > 1) {
+    const T* su = isub + l * YCHUNK_MAX;
+    const T* sp = isup + l * YCHUNK_MAX;
     T z = 0;
     for (int q = 0; q < P - 1; ++q) {
-      int e = ch.end[q] + 1;
-      int64_t o = (int64_t)e * cols + cc;
-      T rhs = x[e] - gamma * x[e - 1] - gamma * x[e + 1];
-      z = (rhs - t1[o] * z) * t0[o];
+      const int e = ch.end[q] + 1;
+      const T rhs = x[e] - gamma * x[e - 1] - gamma * x[e + 1];
+      z = (rhs - su[q] * z) * pv[e];
       x[e] = z;
     }
     T y = 0;
     for (int q = P - 2; q >= 0; --q) {
-      int e = ch.end[q] + 1;
-      int64_t o = (int64_t)e * cols + cc;
-      y = x[e] - t2[o] * y;
+      const int e = ch.end[q] + 1;
+      y = x[e] - sp[q] * y;
       x[e] = y;
     }
   }
   __syncthreads();
-  // phase 3: spike corrections of the inner rows
+  // phase 3: spike corrections of the inner rows (independent loads)
   if (work && P > 1) {
-    T yl = p > 0 ? x[ch.end[p - 1] + 1] : (T)0;
-    T yr = p < P - 1 ? x[b + 1] : (T)0;
-#pragma unroll 4
-    for (int j = a; j <= b; ++j) {
-      int64_t o = (int64_t)j * cols + cc;
-      x[j] = x[j] - yl * t1[o] - yr * t2[o];
+    const T yl = p > 0 ? x[ch.end[p - 1] + 1] : (T)0;
+    const T yr = p < P - 1 ? x[b + 1] : (T)0;
+    for (int j0 = a; j0 <= b; j0 += 8) {
+      T v1[8], v2[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (j0 + u <= b) {
+          const int64_t o = (int64_t)(j0 + u) * cols + cc;
+          v1[u] = t1[o];
+          v2[u] = t2[o];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (j0 + u <= b) x[j0 + u] = x[j0 + u] - yl * v1[u] - yr * v2[u];
     }
   }
   __syncthreads();
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
-    int ll = t % nl, e = t / nl;
-    S[(int64_t)e * cols + c0 + ll] = col[ll * n + e];
+    const int ll = t % nl, e = t / nl;
+    S[(int64_t)e * cols + c0 + ll] = col[ll * ns + e];
   }
 }
+size_t ysolve_smem(int rows, int lpb, bool fp32) {
+  const size_t esz = fp32 ? 4 : 8;
+  return ((size_t)lpb * (rows | 1) * 2 + (size_t)lpb * YCHUNK_MAX * 2) * esz;
+}
+
+template <typename T>
+void launch_ysolve(const TransformTables& tt, int cols, int rows, T* S, const Gate& gate, cudaStream_t st) {
+  const unsigned gy = (unsigned)((cols + tt.lpb_y - 1) / tt.lpb_y);
+  note_launch();
+  kt_mark(2, st);
+  k_ysolve<T><<<gy, tt.threads_y, tt.smem_y, st>>>(rows, cols, tt.ych, (T)tt.gamma, (T)tt.yscale,
+                                                   (const T*)tt.t0, (const T*)tt.t1, (const T*)tt.t2, S, tt.lpb_y,
+                                                   gate);
+  kt_mark(2, st, (double)rows * cols * sizeof(T) * 5);  // data in and out, three table entries per point
+}
+template void launch_ysolve<double>(const TransformTables&, int, int, double*, const Gate&, cudaStream_t);
+template void launch_ysolve<float>(const TransformTables&, int, int, float*, const Gate&, cudaStream_t);
+
+// Band solve of the boundary term: the x-transformed U c occupies rows j0..j1 only, so per
+// x-mode its column solution is the band system (end pivots carry the elimination of the
+// rows outside) followed by geometric decay outside the band (phi / psi tables, applied in
+// the final x pass).  One thread per column; B holds nb x cols values in place.
+template <typename T>
+__global__ void k_yband(int nb, int cols, T gamma, T scale, const T* __restrict__ bpiv, T* __restrict__ B,
+                        Gate gate) {
+  if (!gate_open(gate)) return;
+  // the block's columns of B and of the pivots are staged in shared memory first
+  // (independent coalesced loads); then one thread per column runs the recurrences
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nc = blockDim.x;
+  T* xb = reinterpret_cast<T*>(smem_raw);  // nb x nc
+  T* pb = xb + (size_t)nb * nc;
+  const int k0 = blockIdx.x * nc;
+  for (int t = threadIdx.x; t < nb * nc; t += nc) {
+    const int j = t / nc, kk = t - j * nc;
+    if (k0 + kk < cols) {
+      const int64_t o = (int64_t)j * cols + k0 + kk;
+      xb[t] = B[o] * scale;
+      pb[t] = bpiv[o];
+    }
+  }
+  __syncthreads();
+  const int kk = threadIdx.x;
+  if (k0 + kk < cols) {
+    T z = 0;
+    for (int j = 0; j < nb; ++j) {
+      z = (xb[j * nc + kk] - gamma * z) * pb[j * nc + kk];
+      xb[j * nc + kk] = z;
+    }
+    T y = z;
+    for (int j = nb - 2; j >= 0; --j) {
+      y = xb[j * nc + kk] - (gamma * pb[j * nc + kk]) * y;
+      xb[j * nc + kk] = y;
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nb * nc; t += nc) {
+    const int j = t / nc, c2 = t - j * nc;
+    if (k0 + c2 < cols) B[(int64_t)j * cols + k0 + c2] = xb[t];
+  }
+}
+template <typename T>
+void launch_yband(const TransformTables& tt, int cols, T* B, const Gate& gate, cudaStream_t st) {
+  const int nb = tt.bj1 - tt.bj0 + 1;
+  if (nb <= 0) return;
+  note_launch();
+  kt_mark(2, st);
+  // up to 32 columns per block (whole 128/256-byte row segments), shared memory 2 nb x nc values
+  const int nc = (int)std::max<size_t>(1, std::min<size_t>(32, (48 * 1024) / (2 * (size_t)nb * sizeof(T))));
+  k_yband<T><<<blocks_for(cols, nc), nc, (size_t)2 * nb * nc * sizeof(T), st>>>(nb, cols, (T)tt.gamma, (T)tt.yscale,
+                                                                              (const T*)tt.bpiv, B, gate);
+  kt_mark(2, st, (double)nb * cols * sizeof(T) * 3);
+}
+template void launch_yband<double>(const TransformTables&, int, double*, const Gate&, cudaStream_t);
+template void launch_yband<float>(const TransformTables&, int, float*, const Gate&, cudaStream_t);
 
 // Opts the transform kernels into the large dynamic shared memory carve-out; returns the
 // dynamic bytes every one of them may use (the opt-in limit minus their static shared memory).
@@ -275,153 +485,56 @@ static int allow_dynamic_smem(K kernel, int optin) {
 }
 int configure_kernels(int smem_optin) {
   int d = smem_optin;
-  d = std::min(d, allow_dynamic_smem(k_xpass<double, double, double, double>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_xpass<double, double, double>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_xpass<float, double, float>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_xpass<float, float, float>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_xpass<float, float, double>, smem_optin));
   d = std::min(d, allow_dynamic_smem(k_ysolve<double>, smem_optin));
-  d = std::min(d, allow_dynamic_smem(k_xpass<float, double, float, float>, smem_optin));
-  d = std::min(d, allow_dynamic_smem(k_xpass<float, float, float, float>, smem_optin));
-  d = std::min(d, allow_dynamic_smem(k_xpass<float, float, double, float>, smem_optin));
   d = std::min(d, allow_dynamic_smem(k_ysolve<float>, smem_optin));
   return d;
-}
-
-void launch_rect_inverse(const TransformTables& tt, const RectView& v, const double* b, bool mask_in,
-                         double* spectral, double* out, const double* sub, const double* add, const Gate& gate,
-                         cudaStream_t st) {
-  using C = cplx<double>;
-  R2RTables<double> tx{(const C*)tt.Wx, (const C*)tt.prex, (const C*)tt.postx};
-  R2RTables<double> txi{(const C*)tt.Wx, (const C*)tt.prex_inv, (const C*)tt.postx_inv};
-  const int lpw_f = r2r_paired(tt.tx_fwd) ? 2 : 1, lpw_i = r2r_paired(tt.tx_inv) ? 2 : 1;
-  unsigned gx = (unsigned)((v.rows + tt.lpb_x * lpw_f - 1) / (tt.lpb_x * lpw_f));
-  unsigned gxi = (unsigned)((v.rows + tt.lpb_x * lpw_i - 1) / (tt.lpb_x * lpw_i));
-  note_launch();
-  kt_mark(1, st);
-  k_xpass<double, double, double, double><<<gx, 32 * tt.lpb_x, tt.smem_x, st>>>(
-      v.cols, v.rows, tt.tx_fwd, tt.plan_x, tx, b, v.base, v.pitch, mask_in ? v.cls : nullptr, spectral, 0, v.cols,
-      nullptr, (const double*)nullptr, nullptr, tt.lpb_x, gate);
-  kt_mark(1, st);
-  unsigned gy = (unsigned)((v.cols + tt.lpb_y - 1) / tt.lpb_y);
-  note_launch();
-  kt_mark(2, st);
-  k_ysolve<double><<<gy, tt.threads_y, tt.smem_y, st>>>(v.rows, v.cols, tt.ych, tt.gamma, tt.yscale,
-                                                        (const double*)tt.t0, (const double*)tt.t1,
-                                                        (const double*)tt.t2, spectral, tt.lpb_y, gate);
-  kt_mark(2, st);
-  note_launch();
-  kt_mark(1, st);
-  k_xpass<double, double, double, double><<<gxi, 32 * tt.lpb_x, tt.smem_x, st>>>(
-      v.cols, v.rows, tt.tx_inv, tt.plan_x, txi, spectral, 0, v.cols, nullptr, out, v.base, v.pitch, v.cls, sub, add,
-      tt.lpb_x, gate);
-  kt_mark(1, st);
-}
-
-void launch_rect_inverse_f32(const TransformTables& tt, const RectView& v, const double* b, bool mask_in,
-                             float* spectral, float* first, const Gate& gate, cudaStream_t st) {
-  using C = cplx<float>;
-  R2RTables<float> tx{(const C*)tt.Wx, (const C*)tt.prex, (const C*)tt.postx};
-  R2RTables<float> txi{(const C*)tt.Wx, (const C*)tt.prex_inv, (const C*)tt.postx_inv};
-  const int lpw_f = r2r_paired(tt.tx_fwd) ? 2 : 1, lpw_i = r2r_paired(tt.tx_inv) ? 2 : 1;
-  unsigned gx = (unsigned)((v.rows + tt.lpb_x * lpw_f - 1) / (tt.lpb_x * lpw_f));
-  unsigned gxi = (unsigned)((v.rows + tt.lpb_x * lpw_i - 1) / (tt.lpb_x * lpw_i));
-  note_launch();
-  kt_mark(1, st);
-  k_xpass<float, double, float, float><<<gx, 32 * tt.lpb_x, tt.smem_x, st>>>(
-      v.cols, v.rows, tt.tx_fwd, tt.plan_x, tx, b, v.base, v.pitch, mask_in ? v.cls : nullptr, spectral, 0, v.cols,
-      nullptr, (const float*)nullptr, nullptr, tt.lpb_x, gate);
-  kt_mark(1, st);
-  unsigned gy = (unsigned)((v.cols + tt.lpb_y - 1) / tt.lpb_y);
-  note_launch();
-  kt_mark(2, st);
-  k_ysolve<float><<<gy, tt.threads_y, tt.smem_y, st>>>(v.rows, v.cols, tt.ych, (float)tt.gamma, (float)tt.yscale,
-                                                       (const float*)tt.t0, (const float*)tt.t1, (const float*)tt.t2,
-                                                       spectral, tt.lpb_y, gate);
-  kt_mark(2, st);
-  note_launch();
-  kt_mark(1, st);
-  k_xpass<float, float, float, float><<<gxi, 32 * tt.lpb_x, tt.smem_x, st>>>(
-      v.cols, v.rows, tt.tx_inv, tt.plan_x, txi, spectral, 0, v.cols, nullptr, first, v.base, v.pitch, nullptr,
-      (const float*)nullptr, nullptr, tt.lpb_x, gate);
-  kt_mark(1, st);
-}
-
-void launch_rect_inverse_f32_final(const TransformTables& tt, const RectView& v, const double* w2, float* spectral,
-                                   double* out, const float* sub, const double* add, const Gate& gate,
-                                   cudaStream_t st) {
-  using C = cplx<float>;
-  R2RTables<float> tx{(const C*)tt.Wx, (const C*)tt.prex, (const C*)tt.postx};
-  R2RTables<float> txi{(const C*)tt.Wx, (const C*)tt.prex_inv, (const C*)tt.postx_inv};
-  const int lpw_f = r2r_paired(tt.tx_fwd) ? 2 : 1, lpw_i = r2r_paired(tt.tx_inv) ? 2 : 1;
-  unsigned gx = (unsigned)((v.rows + tt.lpb_x * lpw_f - 1) / (tt.lpb_x * lpw_f));
-  unsigned gxi = (unsigned)((v.rows + tt.lpb_x * lpw_i - 1) / (tt.lpb_x * lpw_i));
-  note_launch();
-  kt_mark(1, st);
-  k_xpass<float, double, float, float><<<gx, 32 * tt.lpb_x, tt.smem_x, st>>>(
-      v.cols, v.rows, tt.tx_fwd, tt.plan_x, tx, w2, v.base, v.pitch, nullptr, spectral, 0, v.cols, nullptr,
-      (const float*)nullptr, nullptr, tt.lpb_x, gate);
-  kt_mark(1, st);
-  unsigned gy = (unsigned)((v.cols + tt.lpb_y - 1) / tt.lpb_y);
-  note_launch();
-  kt_mark(2, st);
-  k_ysolve<float><<<gy, tt.threads_y, tt.smem_y, st>>>(v.rows, v.cols, tt.ych, (float)tt.gamma, (float)tt.yscale,
-                                                       (const float*)tt.t0, (const float*)tt.t1, (const float*)tt.t2,
-                                                       spectral, tt.lpb_y, gate);
-  kt_mark(2, st);
-  note_launch();
-  kt_mark(1, st);
-  k_xpass<float, float, double, float><<<gxi, 32 * tt.lpb_x, tt.smem_x, st>>>(
-      v.cols, v.rows, tt.tx_inv, tt.plan_x, txi, spectral, 0, v.cols, nullptr, out, v.base, v.pitch, v.cls, sub, add,
-      tt.lpb_x, gate);
-  kt_mark(1, st);
 }
 
 // ---------------------------------------------------------------------------
 // boundary Schur correction: c = S^{-1} (C first), scattered into w2
 // ---------------------------------------------------------------------------
 static constexpr int SCHUR_ROWS = 16;
+// c = M first[mcols] with M = S^{-1} C (rank x m, FP64), scattered to w2 at the boundary rows.
+// Every block gathers the m points into shared memory (independent loads), then its warps
+// take SCHUR_ROWS rows of the GEMV (lanes over the row, FP64 accumulation).
 template <typename TF>
-__global__ void k_schur(const TF* __restrict__ first, RectView v, int rank, const int64_t* __restrict__ rows,
-                        const int64_t* __restrict__ cp, const int64_t* __restrict__ cc, const double* __restrict__ cv,
-                        const double* __restrict__ sinv, double* __restrict__ w2, Gate gate) {
+__global__ void k_schur(const TF* __restrict__ first, int rank, int m, const int64_t* __restrict__ mcols,
+                        const double* __restrict__ M, const int64_t* __restrict__ rows, double* __restrict__ w2,
+                        Gate gate) {
   if (!gate_open(gate)) return;
-  extern __shared__ double y[];
-  for (int k = threadIdx.x; k < rank; k += blockDim.x) {
-    double acc = 0.0;
-    for (int64_t e = cp[k]; e < cp[k + 1]; ++e) {
-      int64_t rc = cc[e];
-      int64_t fi = v.base + (rc / v.cols) * v.pitch + (rc % v.cols);
-      acc += cv[e] * (double)first[fi];
-    }
-    y[k] = acc;
-  }
+  extern __shared__ double gsh[];
+  for (int q = threadIdx.x; q < m; q += blockDim.x) gsh[q] = (double)first[mcols[q]];
   __syncthreads();
-  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  int r0 = blockIdx.x * SCHUR_ROWS;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int r0 = blockIdx.x * SCHUR_ROWS;
   for (int r = r0 + warp; r < min(rank, r0 + SCHUR_ROWS); r += nw) {
+    const double* mr = M + (int64_t)r * m;
     double acc = 0.0;
-    for (int k = lane; k < rank; k += 32) acc += sinv[(int64_t)r * rank + k] * y[k];
+#pragma unroll 4
+    for (int q = lane; q < m; q += 32) acc += mr[q] * gsh[q];
     acc = warp_sum(acc);
-    if (lane == 0) {
-      int64_t rc = rows[r];
-      w2[v.base + (rc / v.cols) * v.pitch + (rc % v.cols)] = acc;
-    }
+    if (lane == 0) w2[rows[r]] = acc;
   }
 }
 
-void launch_schur(const double* first, const RectView& view, int rank, const int64_t* rows, const int64_t* c_ptr,
-                  const int64_t* c_col, const double* c_val, const double* sinv, double* w2, const Gate& gate,
-                  cudaStream_t st) {
+template <typename TF>
+void launch_schur(const TF* first, int rank, int m, const int64_t* mcols, const double* M, const int64_t* rows,
+                  double* w2, const Gate& gate, cudaStream_t st) {
   if (rank <= 0) return;
-  unsigned g = (unsigned)((rank + SCHUR_ROWS - 1) / SCHUR_ROWS);
+  const unsigned g = (unsigned)((rank + SCHUR_ROWS - 1) / SCHUR_ROWS);
   note_launch();
-  k_schur<double><<<g, 256, rank * sizeof(double), st>>>(first, view, rank, rows, c_ptr, c_col, c_val, sinv, w2, gate);
+  kt_mark(5, st);
+  k_schur<TF><<<g, 256, (size_t)m * sizeof(double), st>>>(first, rank, m, mcols, M, rows, w2, gate);
+  kt_mark(5, st, (double)m * (sizeof(TF) + 8) + (double)rank * m * 8 + rank * 16.0);
 }
-void launch_schur_f32(const float* first, const RectView& view, int rank, const int64_t* rows, const int64_t* c_ptr,
-                      const int64_t* c_col, const double* c_val, const double* sinv, double* w2, const Gate& gate,
-                      cudaStream_t st) {
-  if (rank <= 0) return;
-  unsigned g = (unsigned)((rank + SCHUR_ROWS - 1) / SCHUR_ROWS);
-  note_launch();
-  k_schur<float><<<g, 256, rank * sizeof(double), st>>>(first, view, rank, rows, c_ptr, c_col, c_val, sinv, w2, gate);
-}
+template void launch_schur<double>(const double*, int, int, const int64_t*, const double*, const int64_t*, double*,
+                                   const Gate&, cudaStream_t);
+template void launch_schur<float>(const float*, int, int, const int64_t*, const double*, const int64_t*, double*,
+                                  const Gate&, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // ghost extension rows
@@ -440,7 +553,9 @@ void launch_ghost(double* field, int n, const int64_t* rows, const int64_t* ptr,
                   const double* val, const Gate& gate, cudaStream_t st) {
   if (n <= 0) return;
   note_launch();
+  kt_mark(8, st);
   k_ghost<<<blocks_for(n, 128), 128, 0, st>>>(field, n, rows, ptr, col, val, gate);
+  kt_mark(8, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -456,8 +571,8 @@ struct Grid {
 
 // -N(u) at u face (j,i), i>=1, before /(dx dy) (solver/numba_kernels.py:17-74 with nu=0);
 // arithmetic in T (double for the plain path, float in the FP32 mode)
-template <typename T>
-__device__ __forceinline__ T adv_u(const double* __restrict__ U, const Grid& g, int j, int i, T dx, T dy) {
+template <typename T, typename S>
+__device__ __forceinline__ T adv_u(const S* __restrict__ U, const Grid& g, int j, int i, T dx, T dy) {
   const int nx = g.nx, ny = g.ny;
   const T h = (T)0.5;
   auto fxy = [&](int jj, int ii) -> T {  // corner flux at (jj, ii), jj in [0, ny]
@@ -481,8 +596,8 @@ __device__ __forceinline__ T adv_u(const double* __restrict__ U, const Grid& g, 
 }
 
 // -N(v) at v face (j,i), 1<=j<=ny-1 (solver/numba_kernels.py:77-142 with nu=0)
-template <typename T>
-__device__ __forceinline__ T adv_v(const double* __restrict__ U, const Grid& g, int j, int i, T dx, T dy) {
+template <typename T, typename S>
+__device__ __forceinline__ T adv_v(const S* __restrict__ U, const Grid& g, int j, int i, T dx, T dy) {
   const int nx = g.nx;
   const T h = (T)0.5;
   auto fyx = [&](int jj, int ii) -> T {  // corner flux at (jj, ii), ii in [0, nx]
@@ -499,8 +614,8 @@ __device__ __forceinline__ T adv_v(const double* __restrict__ U, const Grid& g, 
 }
 
 // raw_l (5-point with channel-wall, inlet and outlet rules) at a u face (solver/optimized_ghost_cell.py:116-120)
-template <typename T>
-__device__ __forceinline__ T lap_u(const double* __restrict__ U, const Grid& g, int j, int i, T idx2, T idy2,
+template <typename T, typename S>
+__device__ __forceinline__ T lap_u(const S* __restrict__ U, const Grid& g, int j, int i, T idx2, T idy2,
                                    bool inlet) {
   const int nx = g.nx, ny = g.ny;
   T acc = 0;
@@ -512,8 +627,8 @@ __device__ __forceinline__ T lap_u(const double* __restrict__ U, const Grid& g, 
   return acc;
 }
 // at a v face (solver/optimized_ghost_cell.py:121-123); walls v=0 are stored as zeros
-template <typename T>
-__device__ __forceinline__ T lap_v(const double* __restrict__ U, const Grid& g, int j, int i, T idx2, T idy2) {
+template <typename T, typename S>
+__device__ __forceinline__ T lap_v(const S* __restrict__ U, const Grid& g, int j, int i, T idx2, T idy2) {
   const int nx = g.nx;
   T acc = idy2 * (T)U[g.v(j - 1, i)];
   if (i > 0) acc += idx2 * (T)U[g.v(j, i - 1)];
@@ -523,27 +638,34 @@ __device__ __forceinline__ T lap_v(const double* __restrict__ U, const Grid& g, 
   return acc;
 }
 // G p at faces from a pressure grid with ghost values (solver/optimized_ghost_cell.py:94-107)
-template <typename T>
-__device__ __forceinline__ T grad_u(const double* __restrict__ P, const Grid& g, int j, int i, T gx) {
+template <typename T, typename S>
+__device__ __forceinline__ T grad_u(const S* __restrict__ P, const Grid& g, int j, int i, T gx) {
   if (i < g.nx) return gx * (T)P[g.p(j, i)] - gx * (T)P[g.p(j, i - 1)];
   return ((T)-2 * gx) * (T)P[g.p(j, g.nx - 1)];
 }
-template <typename T>
-__device__ __forceinline__ T grad_v(const double* __restrict__ P, const Grid& g, int j, int i, T gy) {
+template <typename T, typename S>
+__device__ __forceinline__ T grad_v(const S* __restrict__ P, const Grid& g, int j, int i, T gy) {
   return gy * (T)P[g.p(j, i)] - gy * (T)P[g.p(j - 1, i)];
 }
 
 // decode a face-grid thread index
+// (face grids hold fewer than 2^31 points, checked at set-up: 32-bit division suffices)
 __device__ __forceinline__ bool face_of(int64_t t, const Grid& g, int& comp, int& j, int& i) {
-  if (t < g.usize) { comp = 0; j = (int)(t / (g.nx + 1)); i = (int)(t % (g.nx + 1)); return true; }
+  if (t < g.usize) {
+    const unsigned ut = (unsigned)t, w = (unsigned)(g.nx + 1);
+    comp = 0; j = (int)(ut / w); i = (int)(ut - (unsigned)j * w);
+    return true;
+  }
   int64_t r = t - g.usize;
   if (r >= (int64_t)(g.ny + 1) * g.nx) return false;
-  comp = 1; j = (int)(r / g.nx); i = (int)(r % g.nx);
+  const unsigned ur = (unsigned)r;
+  comp = 1; j = (int)(ur / (unsigned)g.nx); i = (int)(ur - (unsigned)j * g.nx);
   return true;
 }
 
-template <typename T>
-__global__ void k_momentum(CaseDev c, MomentumArgs a, Gate gate) {
+// T: stencil arithmetic; S: storage type the stencils read (double, or the FP32 copies)
+template <typename T, typename S>
+__global__ void k_momentum(CaseDev c, MomentumArgs a, const S* __restrict__ Us, const S* __restrict__ Ps, Gate gate) {
   if (!gate_open(gate)) return;
   const Grid g{c.nx, c.ny, c.usize};
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -556,22 +678,22 @@ __global__ void k_momentum(CaseDev c, MomentumArgs a, Gate gate) {
     a.out[t] = a.mode == 1 ? z : 0.0;
     return;
   }
-  const T dx = (T)c.dx, dy = (T)c.dy, idx2 = (T)(1.0 / (c.dx * c.dx)), idy2 = (T)(1.0 / (c.dy * c.dy));
-  const T area = (T)(c.dx * c.dy), nu = (T)c.nu, dt = (T)a.dt;
+  const T dx = (T)c.dx, dy = (T)c.dy, idx2 = (T)c.idx2, idy2 = (T)c.idy2;
+  const T iarea = (T)c.iarea, nu = (T)c.nu, dt = (T)a.dt;
   const double q = a.U[t];
   T lq, gp, now = 0, off = 0;
   if (comp == 0) {
-    lq = nu * lap_u<T>(a.U, g, j, i, idx2, idy2, true);
-    gp = grad_u<T>(a.P, g, j, i, (T)((1.0 / c.dx) / c.rho));
+    lq = nu * lap_u<T>(Us, g, j, i, idx2, idy2, true);
+    gp = grad_u<T>(Ps, g, j, i, (T)c.gx);
     if (a.mode != 2) {
-      now = adv_u<T>(a.U, g, j, i, dx, dy) / area;
+      now = adv_u<T>(Us, g, j, i, dx, dy) * iarea;
       if (i == c.nx) now *= (T)2;
     }
     if (i == 1) off = nu * (idx2 * (T)c.inlet[j]);
   } else {
-    lq = nu * lap_v<T>(a.U, g, j, i, idx2, idy2);
-    gp = grad_v<T>(a.P, g, j, i, (T)((1.0 / c.dy) / c.rho));
-    if (a.mode != 2) now = adv_v<T>(a.U, g, j, i, dx, dy) / area;
+    lq = nu * lap_v<T>(Us, g, j, i, idx2, idy2);
+    gp = grad_v<T>(Ps, g, j, i, (T)c.gy);
+    if (a.mode != 2) now = adv_v<T>(Us, g, j, i, dx, dy) * iarea;
   }
   if (a.mode == 1) {
     a.now[t] = (double)now;
@@ -585,26 +707,48 @@ __global__ void k_momentum(CaseDev c, MomentumArgs a, Gate gate) {
     a.now[t] = (double)now;
   } else {
     if (comp == 0) {
-      expl = adv_u<T>(a.Uhalf, g, j, i, dx, dy) / area;
+      expl = adv_u<T>(a.Uhalf, g, j, i, dx, dy) * iarea;
       if (i == c.nx) expl *= (T)2;
     } else {
-      expl = adv_v<T>(a.Uhalf, g, j, i, dx, dy) / area;
+      expl = adv_v<T>(a.Uhalf, g, j, i, dx, dy) * iarea;
     }
   }
   // rhs = q + dt (explicit + L q / 2 - G p) + dt/2 offset (solver/numba_kernels.py:596-601)
-  a.out[t] = (q + (double)(dt * (expl + (T)0.5 * lq - gp))) + (double)(((T)0.5 * dt) * off);
+  if constexpr (sizeof(T) == 8)
+    a.out[t] = (q + (double)(dt * (expl + (T)0.5 * lq - gp))) + (double)(((T)0.5 * dt) * off);
+  else  // one conversion and one FP64 add per face
+    a.out[t] = q + (double)(dt * (expl + (T)0.5 * lq - gp) + ((T)0.5 * dt) * off);
+}
+
+__global__ void k_shadow(const double* __restrict__ U, float* __restrict__ U32, int64_t nf,
+                         const double* __restrict__ P, float* __restrict__ P32, int64_t np, Gate gate) {
+  if (!gate_open(gate)) return;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nf + np; t += (int64_t)gridDim.x * blockDim.x) {
+    if (t < nf) U32[t] = (float)U[t];
+    else P32[t - nf] = (float)P[t - nf];
+  }
+}
+void launch_shadow(const double* U, float* U32, int64_t n_f, const double* P, float* P32, int64_t n_p,
+                   const Gate& gate, cudaStream_t st) {
+  note_launch();
+  kt_mark(3, st);
+  k_shadow<<<reduce_blocks(n_f + n_p), TPB, 0, st>>>(U, U32, n_f, P, P32, n_p, gate);
+  kt_mark(3, st);
 }
 
 void launch_momentum(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st) {
   note_launch();
   kt_mark(3, st);
-  k_momentum<double><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, gate);
+  k_momentum<double, double><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, a.U, a.P, gate);
   kt_mark(3, st);
 }
 void launch_momentum_f32(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st) {
   note_launch();
   kt_mark(3, st);
-  k_momentum<float><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, gate);
+  if (a.mode == 0 && a.U32 && a.P32)
+    k_momentum<float, float><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, a.U32, a.P32, gate);
+  else
+    k_momentum<float, double><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, a.U, a.P, gate);
   kt_mark(3, st);
 }
 
@@ -618,10 +762,10 @@ __global__ void k_advection(CaseDev c, const double* __restrict__ U, double* __r
   if (!(cls & CLS_ACTIVE)) { out[t] = 0.0; return; }
   double r;
   if (comp == 0) {
-    r = adv_u<double>(U, g, j, i, c.dx, c.dy) / (c.dx * c.dy);
+    r = adv_u<double>(U, g, j, i, c.dx, c.dy) * c.iarea;
     if (i == c.nx) r *= 2;
   } else {
-    r = adv_v<double>(U, g, j, i, c.dx, c.dy) / (c.dx * c.dy);
+    r = adv_v<double>(U, g, j, i, c.dx, c.dy) * c.iarea;
   }
   out[t] = r;
 }
@@ -639,7 +783,7 @@ __global__ void k_diffusion(CaseDev c, const double* __restrict__ U, double* __r
   if (!face_of(t, g, comp, j, i)) return;
   const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
   if (!(cls & CLS_ACTIVE)) { out[t] = 0.0; return; }
-  const double idx2 = 1.0 / (c.dx * c.dx), idy2 = 1.0 / (c.dy * c.dy);
+  const double idx2 = c.idx2, idy2 = c.idy2;
   double l = comp == 0 ? c.nu * lap_u<double>(U, g, j, i, idx2, idy2, with_inlet != 0) : c.nu * lap_v<double>(U, g, j, i, idx2, idy2);
   out[t] = hdt == 0.0 ? l : U[t] - hdt * l;
 }
@@ -657,7 +801,7 @@ __global__ void k_gradient(CaseDev c, const double* __restrict__ P, double* __re
   if (!face_of(t, g, comp, j, i)) return;
   const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
   if (!(cls & CLS_ACTIVE)) { out[t] = 0.0; return; }
-  out[t] = comp == 0 ? grad_u<double>(P, g, j, i, (1.0 / c.dx) / c.rho) : grad_v<double>(P, g, j, i, (1.0 / c.dy) / c.rho);
+  out[t] = comp == 0 ? grad_u<double>(P, g, j, i, c.gx) : grad_v<double>(P, g, j, i, c.gy);
 }
 void launch_gradient(const CaseDev& c, const double* P, double* out, const Gate& gate, cudaStream_t st) {
   note_launch();
@@ -678,79 +822,92 @@ __device__ __forceinline__ int find_row(const int64_t* rows, int n, int64_t key)
   return -1;
 }
 
-__global__ void k_residual(CaseDev c, int kind, double hc, const double* __restrict__ b, const double* __restrict__ x,
-                           double* __restrict__ res, SolveCtl* sc, int check, int first, Gate gate) {
+// Residual res = b - A x of the pressure operator A (KIND 0, p grid) or the Helmholtz
+// operators I - c L (KIND 1 u faces, KIND 2 v faces), with max |res| and sum res^2 per check.
+// GB300 issues FP64 at 1/64 of the FP32 rate, so the regular rows use coefficients formed on
+// the host (ResidualCoef): two adds and three multiply-adds per point.  RES_F32: the residual
+// is stored in FP32 (the input of the FP32 inverse; its norms are still taken in FP64) and
+// the roundoff bound is left to k_pressure_bound after the refinement loop.
+template <int KIND, bool RES_F32>
+__global__ void k_residual(CaseDev c, ResidualCoef rc, const double* __restrict__ b, const double* __restrict__ x,
+                           void* __restrict__ res_out, SolveCtl* sc, int check, int first, Gate gate) {
   if (!gate_open(gate)) return;
   if (check < 0) check = *(volatile int*)&sc->k;
   const int nx = c.nx, ny = c.ny;
-  int64_t npts = kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize);
-  int64_t base = kind == 2 ? c.usize : 0;  // face-grid offset of the v field
-  const uint8_t* cls = kind == 0 ? c.cls_p : (kind == 1 ? c.cls_u : c.cls_v);
+  const int w = KIND == 1 ? nx + 1 : nx;            // row width of the grid
+  const int64_t npts = KIND == 0 ? c.psize : (KIND == 1 ? c.usize : c.vsize);
+  const int64_t base = KIND == 2 ? c.usize : 0;     // face-grid offset of the v field
+  const uint8_t* cls = KIND == 0 ? c.cls_p : (KIND == 1 ? c.cls_u : c.cls_v);
+  double* res64 = reinterpret_cast<double*>(res_out);
+  float* res32 = reinterpret_cast<float*>(res_out);
   unsigned long long rm = 0, bm = 0, bd = 0, xb = 0;
   double rs = 0.0, bs = 0.0;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < npts; t += (int64_t)gridDim.x * blockDim.x) {
-    uint8_t k = cls[t];
-    int64_t f = base + t;
+    const uint8_t k = cls[t];
+    const int64_t f = base + t;
     if (!(k & CLS_ACTIVE)) {
-      res[f] = 0.0;
-    } else {
-      const double xv = x[f], bv = b[f];
-      double ax = 0.0, aabs = 0.0;
-      int nnz = 0;
-      int row = (k & CLS_IRREG) ? find_row(c.irr_rows[kind], c.n_irr[kind], t) : -1;
-      if (row >= 0) {
-        const int64_t* cp = c.irr_ptr[kind];
-        for (int64_t e = cp[row]; e < cp[row + 1]; ++e) {
-          double xv2 = x[base + c.irr_col[kind][e]];
-          double a = c.irr_val[kind][e];
-          ax += a * xv2;
-          aabs += fabs(a) * fabs(xv2);
-        }
-        nnz = (int)(cp[row + 1] - cp[row]);
-      } else if (kind == 0) {
-        int j = (int)(t / nx), i = (int)(t % nx);
-        const double idx2 = 1.0 / (c.dx * c.dx), idy2 = 1.0 / (c.dy * c.dy);
-        double mx = (i == 0 ? -1.0 : (i == nx - 1 ? -3.0 : -2.0)) * idx2;
-        double my = (j == 0 || j == ny - 1 ? -1.0 : -2.0) * idy2;
-        double acc = (mx + my) * xv, aa = fabs(mx + my) * fabs(xv);
-        if (i > 0) { double y = x[t - 1]; acc += idx2 * y; aa += idx2 * fabs(y); }
-        if (i < nx - 1) { double y = x[t + 1]; acc += idx2 * y; aa += idx2 * fabs(y); }
-        if (j > 0) { double y = x[t - nx]; acc += idy2 * y; aa += idy2 * fabs(y); }
-        if (j < ny - 1) { double y = x[t + nx]; acc += idy2 * y; aa += idy2 * fabs(y); }
-        ax = acc / c.rho;
-        aabs = aa / c.rho;
-        nnz = c.a_nnz[t];
-      } else if (kind == 1) {
-        int j = (int)(t / (nx + 1)), i = (int)(t % (nx + 1));
-        const double idx2 = 1.0 / (c.dx * c.dx), idy2 = 1.0 / (c.dy * c.dy);
-        double lap = (-2.0 * idx2 + (j == 0 || j == ny - 1 ? -3.0 : -2.0) * idy2) * xv;
-        if (i > 1) lap += (i == nx ? 2.0 * idx2 : idx2) * x[f - 1];
-        if (i < nx) lap += idx2 * x[f + 1];
-        if (j > 0) lap += idy2 * x[f - (nx + 1)];
-        if (j < ny - 1) lap += idy2 * x[f + (nx + 1)];
-        ax = xv - hc * lap;
-      } else {
-        int j = (int)(t / nx), i = (int)(t % nx);
-        const double idx2 = 1.0 / (c.dx * c.dx), idy2 = 1.0 / (c.dy * c.dy);
-        double lap = ((i == 0 ? -3.0 : (i == nx - 1 ? -1.0 : -2.0)) * idx2 - 2.0 * idy2) * xv;
-        if (i > 0) lap += idx2 * x[f - 1];
-        if (i < nx - 1) lap += idx2 * x[f + 1];
-        if (j > 1) lap += idy2 * x[f - nx];
-        if (j < ny - 1) lap += idy2 * x[f + nx];
-        ax = xv - hc * lap;
-      }
-      double r = bv - ax;
-      res[f] = r;
-      rm = umax64(rm, absbits(r));
-      rs += r * r;
-      if (kind == 0) bd = umax64(bd, dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + fabs(bv))));
-      if (first) { bm = umax64(bm, absbits(bv)); bs += bv * bv; }
-      if (!isfinite(xv)) xb = 1;
+      if (RES_F32) res32[f] = 0.0f; else res64[f] = 0.0;
+      continue;
     }
+    const double xv = x[f], bv = b[f];
+    double ax, aabs = 0.0;
+    int nnz = 0;
+    const int row = (k & CLS_IRREG) ? find_row(c.irr_rows[KIND], c.n_irr[KIND], t) : -1;
+    if (row >= 0) {
+      const int64_t* cp = c.irr_ptr[KIND];
+      ax = 0.0;
+      for (int64_t e = cp[row]; e < cp[row + 1]; ++e) {
+        const double xv2 = x[base + c.irr_col[KIND][e]];
+        const double a = c.irr_val[KIND][e];
+        ax += a * xv2;
+        if (KIND == 0 && !RES_F32) aabs += fabs(a) * fabs(xv2);
+      }
+      nnz = (int)(cp[row + 1] - cp[row]);
+    } else {
+      const int j = (int)((unsigned)t / (unsigned)w), i = (int)((unsigned)t - (unsigned)j * w);
+      // neighbours outside the operator's stencil read as zero
+      double xw = 0.0, xe = 0.0, xs = 0.0, xn = 0.0;
+      int ic, jc;
+      if (KIND == 0) {
+        if (i > 0) xw = x[f - 1];
+        if (i < nx - 1) xe = x[f + 1];
+        if (j > 0) xs = x[f - w];
+        if (j < ny - 1) xn = x[f + w];
+        ic = i == 0 ? 0 : (i == nx - 1 ? 2 : 1);
+        jc = (j == 0 || j == ny - 1) ? 0 : 1;
+      } else if (KIND == 1) {
+        if (i > 1) xw = x[f - 1];
+        if (i < nx) xe = x[f + 1];
+        if (j > 0) xs = x[f - w];
+        if (j < ny - 1) xn = x[f + w];
+        ic = i == nx ? 2 : 1;
+        jc = (j == 0 || j == ny - 1) ? 0 : 1;
+      } else {
+        if (i > 0) xw = x[f - 1];
+        if (i < nx - 1) xe = x[f + 1];
+        if (j > 1) xs = x[f - w];
+        if (j < ny - 1) xn = x[f + w];
+        ic = i == 0 ? 0 : (i == nx - 1 ? 2 : 1);
+        jc = 1;
+      }
+      // A x = cc x + cw xw + ce xe + cy (xs + xn); Helmholtz rows carry the factors of I - c L
+      ax = rc.cc[ic][jc] * xv + rc.cw[ic] * xw + rc.ce * xe + rc.cy * (xs + xn);
+      if (KIND == 0 && !RES_F32) {
+        aabs = fabs(rc.cc[ic][jc]) * fabs(xv) + rc.ce * (fabs(xw) + fabs(xe)) + rc.cy * (fabs(xs) + fabs(xn));
+        nnz = c.a_nnz[t];
+      }
+    }
+    const double r = bv - ax;
+    if (RES_F32) res32[f] = (float)r; else res64[f] = r;
+    rm = umax64(rm, absbits(r));
+    rs += r * r;
+    if (KIND == 0 && !RES_F32) bd = umax64(bd, dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + fabs(bv))));
+    if (first) { bm = umax64(bm, absbits(bv)); bs += bv * bv; }
+    if (!isfinite(xv)) xb = 1;
   }
   block_commit_max(rm, &sc->rmax[check]);
   block_commit_sum(rs, &sc->rsq[check]);
-  if (kind == 0) block_commit_max(bd, &sc->bound[check]);
+  if (KIND == 0 && !RES_F32) block_commit_max(bd, &sc->bound[check]);
   if (first) {
     block_commit_max(bm, &sc->bmax);
     block_commit_sum(bs, &sc->bsq);
@@ -758,12 +915,62 @@ __global__ void k_residual(CaseDev c, int kind, double hc, const double* __restr
   block_commit_max(xb, &sc->xbad);
 }
 
-void launch_residual(const CaseDev& c, int kind, double hc, const double* b, const double* x, double* res,
-                     SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st) {
-  int64_t n = kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize);
+void launch_residual(const CaseDev& c, const ResidualCoef& rc, int kind, const double* b, const double* x, void* res,
+                     bool res_f32, SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st) {
+  const int64_t n = kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize);
+  const unsigned g = reduce_blocks(n);
+  const int fc = first_check ? 1 : 0;
   note_launch();
   kt_mark(4, st);
-  k_residual<<<reduce_blocks(n), TPB, 0, st>>>(c, kind, hc, b, x, res, sc, check, first_check ? 1 : 0, gate);
+  if (res_f32) {
+    if (kind == 0) k_residual<0, true><<<g, TPB, 0, st>>>(c, rc, b, x, res, sc, check, fc, gate);
+    else if (kind == 1) k_residual<1, true><<<g, TPB, 0, st>>>(c, rc, b, x, res, sc, check, fc, gate);
+    else k_residual<2, true><<<g, TPB, 0, st>>>(c, rc, b, x, res, sc, check, fc, gate);
+  } else {
+    if (kind == 0) k_residual<0, false><<<g, TPB, 0, st>>>(c, rc, b, x, res, sc, check, fc, gate);
+    else if (kind == 1) k_residual<1, false><<<g, TPB, 0, st>>>(c, rc, b, x, res, sc, check, fc, gate);
+    else k_residual<2, false><<<g, TPB, 0, st>>>(c, rc, b, x, res, sc, check, fc, gate);
+  }
+  kt_mark(4, st, (double)n * (8 + 8 + (res_f32 ? 4 : 8) + 1));  // x, b, res, class map
+}
+
+// Roundoff bound max_i (2 nnz_i + 2) eps (|A||x| + |b|)_i of the pressure solution after its
+// refinement loop (solver/pressure_schur.py:48-56), stored at the last check; used by the
+// FP32 mode, whose residual sweeps skip it.
+__global__ void k_pressure_bound(CaseDev c, ResidualCoef rc, const double* __restrict__ b,
+                                 const double* __restrict__ x, SolveCtl* sc, int nchk, Gate gate) {
+  if (!gate_open(gate)) return;
+  const int check = last_check(sc, nchk);
+  const int nx = c.nx, ny = c.ny;
+  unsigned long long bd = 0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < c.psize; t += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t k = c.cls_p[t];
+    if (!(k & CLS_ACTIVE)) continue;
+    const double xv = x[t], bv = b[t];
+    double aabs = 0.0;
+    int nnz;
+    const int row = (k & CLS_IRREG) ? find_row(c.irr_rows[0], c.n_irr[0], t) : -1;
+    if (row >= 0) {
+      const int64_t* cp = c.irr_ptr[0];
+      for (int64_t e = cp[row]; e < cp[row + 1]; ++e) aabs += fabs(c.irr_val[0][e]) * fabs(x[c.irr_col[0][e]]);
+      nnz = (int)(cp[row + 1] - cp[row]);
+    } else {
+      const int j = (int)((unsigned)t / (unsigned)nx), i = (int)((unsigned)t - (unsigned)j * nx);
+      double xw = i > 0 ? x[t - 1] : 0.0, xe = i < nx - 1 ? x[t + 1] : 0.0;
+      double xs = j > 0 ? x[t - nx] : 0.0, xn = j < ny - 1 ? x[t + nx] : 0.0;
+      const int ic = i == 0 ? 0 : (i == nx - 1 ? 2 : 1), jc = (j == 0 || j == ny - 1) ? 0 : 1;
+      aabs = fabs(rc.cc[ic][jc]) * fabs(xv) + rc.ce * (fabs(xw) + fabs(xe)) + rc.cy * (fabs(xs) + fabs(xn));
+      nnz = c.a_nnz[t];
+    }
+    bd = umax64(bd, dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + fabs(bv))));
+  }
+  block_commit_max(bd, &sc->bound[check]);
+}
+void launch_pressure_bound(const CaseDev& c, const ResidualCoef& rc, const double* b, const double* x, SolveCtl* sc,
+                           int nchk, const Gate& gate, cudaStream_t st) {
+  note_launch();
+  kt_mark(4, st);
+  k_pressure_bound<<<reduce_blocks(c.psize), TPB, 0, st>>>(c, rc, b, x, sc, nchk, gate);
   kt_mark(4, st);
 }
 
@@ -778,11 +985,11 @@ __global__ void k_divergence(CaseDev c, const double* __restrict__ U, double* __
   bool bad = false;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < c.psize; t += (int64_t)gridDim.x * blockDim.x) {
     if (c.cls_p[t] & CLS_ACTIVE) {
-      int j = (int)(t / c.nx), i = (int)(t % c.nx);
-      double d = (U[g.u(j, i + 1)] - U[g.u(j, i)]) / c.dx + (U[g.v(j + 1, i)] - U[g.v(j, i)]) / c.dy;
+      int j = (int)((unsigned)t / (unsigned)c.nx), i = (int)((unsigned)t - (unsigned)j * c.nx);
+      double d = (U[g.u(j, i + 1)] - U[g.u(j, i)]) * c.idx + (U[g.v(j + 1, i)] - U[g.v(j, i)]) * c.idy;
       dm = umax64(dm, absbits(d));
       if (out) {
-        double o = dt != 0.0 ? d / dt : d;
+        double o = d * dt;  // dt carries 1/dt (or 1)
         out[t] = o;
         bad = bad || !isfinite(o);
       }
@@ -797,7 +1004,10 @@ void launch_divergence(const CaseDev& c, const double* U, double* out, double sc
                        unsigned long long* divmax, int gate_on_nonfinite, const Gate& gate, cudaStream_t st) {
   (void)sc;
   note_launch();
-  k_divergence<<<reduce_blocks(c.psize), TPB, 0, st>>>(c, U, out, scale, divmax, gate_on_nonfinite, gate.ctl, gate);
+  kt_mark(6, st);
+  k_divergence<<<reduce_blocks(c.psize), TPB, 0, st>>>(c, U, out, scale != 0.0 ? 1.0 / scale : 1.0, divmax,
+                                                      gate_on_nonfinite, gate.ctl, gate);
+  kt_mark(6, st);
 }
 
 __global__ void k_project_update(CaseDev c, const double* __restrict__ q, const double* __restrict__ phi, double dt,
@@ -812,14 +1022,16 @@ __global__ void k_project_update(CaseDev c, const double* __restrict__ q, const 
     out[t] = (comp == 0 && i == 0) ? c.inlet[j] : 0.0;
     return;
   }
-  double gphi = comp == 0 ? grad_u<double>(phi, g, j, i, (1.0 / c.dx) / c.rho) : grad_v<double>(phi, g, j, i, (1.0 / c.dy) / c.rho);
+  double gphi = comp == 0 ? grad_u<double>(phi, g, j, i, c.gx) : grad_v<double>(phi, g, j, i, c.gy);
   out[t] = q[t] - dt * gphi;
 }
 void launch_project_update(const CaseDev& c, const double* q, const double* phi, double dt, double* out,
                            const SolveCtl* psolve, const Gate& gate, cudaStream_t st) {
   (void)psolve;
   note_launch();
+  kt_mark(6, st);
   k_project_update<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, q, phi, dt, out, gate);
+  kt_mark(6, st);
 }
 
 __global__ void k_defect(CaseDev c, const double* __restrict__ r, const double* __restrict__ rhs, double hdt,
@@ -835,7 +1047,7 @@ __global__ void k_defect(CaseDev c, const double* __restrict__ r, const double* 
     proj[t] = (comp == 0 && i == 0) ? c.inlet[j] : 0.0;
     return;
   }
-  const double idx2 = 1.0 / (c.dx * c.dx), idy2 = 1.0 / (c.dy * c.dy);
+  const double idx2 = c.idx2, idy2 = c.idy2;
   double l = comp == 0 ? c.nu * lap_u<double>(r, g, j, i, idx2, idy2, false) : c.nu * lap_v<double>(r, g, j, i, idx2, idy2);
   double hr = r[t] - hdt * l;
   action[t] = hr;
@@ -844,7 +1056,9 @@ __global__ void k_defect(CaseDev c, const double* __restrict__ r, const double* 
 void launch_defect(const CaseDev& c, const double* result, const double* rhs, double hdt, double* action,
                    double* proj, const Gate& gate, cudaStream_t st) {
   note_launch();
+  kt_mark(7, st);
   k_defect<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, result, rhs, hdt, action, proj, gate);
+  kt_mark(7, st);
 }
 
 __global__ void k_pressure_out(CaseDev c, const double* __restrict__ p, const double* __restrict__ inc, double factor,
@@ -862,7 +1076,7 @@ __global__ void k_pressure_out(CaseDev c, const double* __restrict__ p, const do
     face_of(t, g, comp, j, i);
     const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
     if (cls & CLS_ACTIVE) {
-      double gi = comp == 0 ? grad_u<double>(inc, g, j, i, (1.0 / c.dx) / c.rho) : grad_v<double>(inc, g, j, i, (1.0 / c.dy) / c.rho);
+      double gi = comp == 0 ? grad_u<double>(inc, g, j, i, c.gx) : grad_v<double>(inc, g, j, i, c.gy);
       double r = action[t] - rhs[t] + dt * gi;
       cm = umax64(cm, absbits(r));
     }
@@ -884,8 +1098,10 @@ void launch_pressure_out(const CaseDev& c, const double* p, const double* inc, d
                          const double* action, const double* rhs, double* half, double* pout,
                          unsigned long long* coupled, const Gate& gate, cudaStream_t st) {
   note_launch();
+  kt_mark(7, st);
   k_pressure_out<<<reduce_blocks(c.usize + c.vsize + c.psize), TPB, 0, st>>>(c, p, inc, factor, dt, action, rhs, half,
                                                                           pout, coupled, gate);
+  kt_mark(7, st);
 }
 
 __global__ void k_maxabs(CaseDev c, const double* __restrict__ U, unsigned long long* umax, unsigned long long* vmax,
@@ -903,7 +1119,9 @@ __global__ void k_maxabs(CaseDev c, const double* __restrict__ U, unsigned long 
 void launch_maxabs(const CaseDev& c, const double* U, unsigned long long* umax, unsigned long long* vmax,
                    const Gate& gate, cudaStream_t st) {
   note_launch();
+  kt_mark(9, st);
   k_maxabs<<<reduce_blocks(c.usize + c.vsize), TPB, 0, st>>>(c, U, umax, vmax, gate);
+  kt_mark(9, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -912,36 +1130,49 @@ void launch_maxabs(const CaseDev& c, const double* U, unsigned long long* umax, 
 __global__ void k_forces(CaseDev c, const double* __restrict__ U, const double* __restrict__ P, double mu, double dt,
                          StepCtl* ctl, int check_gates, double* out6, Gate gate) {
   if (!gate_open(gate)) return;
-  double fpx = 0, fpy = 0, tx = 0, ty = 0;
-  for (int k = threadIdx.x; k < c.n_surf; k += blockDim.x) {
+  // one warp per quadrature point (lanes over the stencil nonzeros), the per-point terms go to
+  // c.surf_part; the last block to finish sums them in a fixed order (deterministic)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  const int k = blockIdx.x * wpb + warp;
+  if (k < c.n_surf) {
     double ps = 0, du = 0, dv = 0;
-    for (int64_t e = c.sp_ptr[k]; e < c.sp_ptr[k + 1]; ++e) ps += c.sp_val[e] * P[c.sp_col[e]];
-    for (int64_t e = c.su_ptr[k]; e < c.su_ptr[k + 1]; ++e) du += c.su_val[e] * U[c.su_col[e]];
-    for (int64_t e = c.sv_ptr[k]; e < c.sv_ptr[k + 1]; ++e) dv += c.sv_val[e] * U[c.usize + c.sv_col[e]];
-    double nxk = c.nxx[k], nyk = c.nyy[k];
-    double dn = du * nxk + dv * nyk;
-    tx += mu * (du + nxk * dn);
-    ty += mu * (dv + nyk * dn);
-    fpx += ps * c.nwx[k];
-    fpy += ps * c.nwy[k];
+    for (int64_t e = c.sp_ptr[k] + lane; e < c.sp_ptr[k + 1]; e += 32) ps += c.sp_val[e] * P[c.sp_col[e]];
+    for (int64_t e = c.su_ptr[k] + lane; e < c.su_ptr[k + 1]; e += 32) du += c.su_val[e] * U[c.su_col[e]];
+    for (int64_t e = c.sv_ptr[k] + lane; e < c.sv_ptr[k + 1]; e += 32) dv += c.sv_val[e] * U[c.usize + c.sv_col[e]];
+    ps = warp_sum(ps);
+    du = warp_sum(du);
+    dv = warp_sum(dv);
+    if (lane == 0) {
+      const double nxk = c.nxx[k], nyk = c.nyy[k];
+      const double dn = du * nxk + dv * nyk;
+      double* o = c.surf_part + 4 * (int64_t)k;
+      o[0] = ps * c.nwx[k];
+      o[1] = ps * c.nwy[k];
+      o[2] = mu * (du + nxk * dn);
+      o[3] = mu * (dv + nyk * dn);
+    }
   }
-  __shared__ double red[4][32];
-  double v[4] = {fpx, fpy, tx, ty};
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int q = 0; q < 4; ++q) {
-    double s = warp_sum(v[q]);
-    if (lane == 0) red[q][wid] = s;
+  __threadfence();
+  __syncthreads();
+  __shared__ int last;
+  if (threadIdx.x == 0) last = atomicAdd(c.surf_ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  __shared__ double red[4];
+  if (warp < 4) {
+    double acc = 0.0;
+    for (int q = lane; q < c.n_surf; q += 32) acc += __ldcg(c.surf_part + 4 * (int64_t)q + warp);
+    acc = warp_sum(acc);
+    if (lane == 0) red[warp] = acc;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    int nw = (blockDim.x + 31) >> 5;
-    double s[4] = {0, 0, 0, 0};
-    for (int q = 0; q < 4; ++q)
-      for (int w = 0; w < nw; ++w) s[q] += red[q][w];
+    *c.surf_ticket = 0u;
     const double PI = 3.141592653589793;
     double w = PI * c.D / c.n_surf;
-    double fp[2] = {-s[0], -s[1]};
-    double fv[2] = {s[2] * w, s[3] * w};
+    double fp[2] = {-red[0], -red[1]};
+    double fv[2] = {red[2] * w, red[3] * w};
     double f6[6] = {fp[0] + fv[0], fp[1] + fv[1], fp[0], fp[1], fv[0], fv[1]};
     if (out6)
       for (int q = 0; q < 6; ++q) out6[q] = f6[q];
@@ -966,7 +1197,10 @@ __global__ void k_forces(CaseDev c, const double* __restrict__ U, const double* 
 void launch_forces(const CaseDev& c, const double* U, const double* P, double mu, double dt, StepCtl* ctl,
                    int check_gates, double* out6, const Gate& gate, cudaStream_t st) {
   note_launch();
-  k_forces<<<1, 256, 0, st>>>(c, U, P, mu, dt, ctl, check_gates, out6, gate);
+  kt_mark(9, st);
+  const int wpb = 8;
+  k_forces<<<(c.n_surf + wpb - 1) / wpb, 32 * wpb, 0, st>>>(c, U, P, mu, dt, ctl, check_gates, out6, gate);
+  kt_mark(9, st);
 }
 
 __global__ void k_gate_momentum(StepCtl* ctl, int nchk) {
@@ -986,7 +1220,9 @@ __global__ void k_gate_momentum(StepCtl* ctl, int nchk) {
 }
 void launch_gate_momentum(StepCtl* ctl, int nchk, cudaStream_t st) {
   note_launch();
+  kt_mark(10, st);
   k_gate_momentum<<<1, 1, 0, st>>>(ctl, nchk);
+  kt_mark(10, st);
 }
 
 __global__ void k_gate_pressure(StepCtl* ctl, int slot, int nchk) {
@@ -1002,7 +1238,9 @@ __global__ void k_gate_pressure(StepCtl* ctl, int slot, int nchk) {
 }
 void launch_gate_pressure(StepCtl* ctl, int slot, int nchk, cudaStream_t st) {
   note_launch();
+  kt_mark(10, st);
   k_gate_pressure<<<1, 1, 0, st>>>(ctl, slot, nchk);
+  kt_mark(10, st);
 }
 
 __global__ void k_gate_projection(StepCtl* ctl, int k) {
@@ -1012,7 +1250,9 @@ __global__ void k_gate_projection(StepCtl* ctl, int k) {
 }
 void launch_gate_projection(StepCtl* ctl, int k, cudaStream_t st) {
   note_launch();
+  kt_mark(10, st);
   k_gate_projection<<<1, 1, 0, st>>>(ctl, k);
+  kt_mark(10, st);
 }
 
 // CFL screen of solver/main.py:273-278 (screen != 0) and the finite-field check of
@@ -1028,7 +1268,9 @@ __global__ void k_cfl_screen(StepCtl* ctl, const unsigned long long* umax, const
 void launch_cfl_screen(StepCtl* ctl, const unsigned long long* umax, const unsigned long long* vmax, double dt,
                        double dx, double dy, int screen, const long long* counter, cudaStream_t st) {
   note_launch();
+  kt_mark(10, st);
   k_cfl_screen<<<1, 1, 0, st>>>(ctl, umax, vmax, dt, dx, dy, screen, counter);
+  kt_mark(10, st);
 }
 
 __global__ void k_refine_decide(StepCtl* ctl, int slot, int nchk, cudaGraphConditionalHandle cond) {
@@ -1041,7 +1283,9 @@ __global__ void k_refine_decide(StepCtl* ctl, int slot, int nchk, cudaGraphCondi
 }
 void launch_refine_decide(StepCtl* ctl, int slot, int nchk, cudaGraphConditionalHandle cond, cudaStream_t st) {
   note_launch();
+  kt_mark(10, st);
   k_refine_decide<<<1, 1, 0, st>>>(ctl, slot, nchk, cond);
+  kt_mark(10, st);
 }
 
 __global__ void k_step_end(StepCtl* ctl, unsigned long long* state_max, StepCtl* ring, int* ridx, long long* counter,
@@ -1067,7 +1311,9 @@ __global__ void k_step_end(StepCtl* ctl, unsigned long long* state_max, StepCtl*
 void launch_step_end(StepCtl* ctl, unsigned long long* state_max, StepCtl* ring, int* ridx, long long* counter,
                      int cap, cudaStream_t st) {
   note_launch();
+  kt_mark(10, st);
   k_step_end<<<1, 128, 0, st>>>(ctl, state_max, ring, ridx, counter, cap);
+  kt_mark(10, st);
 }
 
 __global__ void k_copy_active(const uint8_t* __restrict__ cls, int64_t n, const double* __restrict__ src,
@@ -1088,7 +1334,9 @@ __global__ void k_set_inlet(CaseDev c, double* U, int zero) {
 }
 void launch_set_inlet(const CaseDev& c, double* U, bool zero, cudaStream_t st) {
   note_launch();
+  kt_mark(6, st);
   k_set_inlet<<<blocks_for(c.ny, 128), 128, 0, st>>>(c, U, zero ? 1 : 0);
+  kt_mark(6, st);
 }
 
 // mac_engine.calculate_mac_divergence_cpp (solver/src/bindings.cpp:343-390)
@@ -1150,10 +1398,7 @@ __global__ void k_schur_column(const double* __restrict__ first, RectView v, int
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= rank) return;
   double acc = 0.0;
-  for (int64_t e = cp[r]; e < cp[r + 1]; ++e) {
-    int64_t rc = cc[e];
-    acc += cv[e] * first[v.base + (rc / v.cols) * v.pitch + (rc % v.cols)];
-  }
+  for (int64_t e = cp[r]; e < cp[r + 1]; ++e) acc += cv[e] * first[cc[e]];  // cc: field-grid flat indices
   S[(int64_t)r * rank + col] = acc;
 }
 void launch_schur_column(const double* first, const RectView& view, int rank, const int64_t* c_ptr,

@@ -111,6 +111,9 @@ __device__ __forceinline__ void raise_gate(StepCtl* ctl, int err_class, int gate
 struct CaseDev {
   int nx, ny;
   double dx, dy, rho, nu;
+  // reciprocals formed once on the host: GB300 issues FP64 at 1/64 of the FP32 rate, so
+  // no per-point kernel divides (1/dx, 1/dy, 1/dx^2, 1/dy^2, (1/dx)/rho, (1/dy)/rho, 1/(dx dy), 1/rho)
+  double idx, idy, idx2, idy2, gx, gy, iarea, irho;
   int64_t usize, vsize, psize;
   const uint8_t* cls_u;     // usize
   const uint8_t* cls_v;     // vsize
@@ -131,6 +134,8 @@ struct CaseDev {
   const int64_t* su_ptr; const int64_t* su_col; const double* su_val;
   const int64_t* sv_ptr; const int64_t* sv_col; const double* sv_val;
   const double* nwx; const double* nwy; const double* nxx; const double* nyy;
+  double* surf_part;        // 4 * n_surf per-point force terms (k_forces scratch)
+  unsigned* surf_ticket;    // blocks finished in k_forces (back to 0 after each launch)
   double D, U_ref;
 };
 
@@ -156,6 +161,7 @@ struct YChunks {
 };
 
 struct TransformTables {      // device tables of one rectangle kind (T = double or float)
+  int n;                      // line length of the x transforms (columns)
   FftPlan plan_x;
   int tx_fwd, tx_inv;
   const void* Wx; const void* prex; const void* postx;
@@ -165,39 +171,57 @@ struct TransformTables {      // device tables of one rectangle kind (T = double
   double gamma;               // constant off-diagonal of the column systems
   double yscale;              // 1 / (2 nx): normalisation of the inverse x transform
   const void* t0; const void* t1; const void* t2;  // rows x cols partition tables
-  int lpb_x, lpb_y, threads_y;
-  size_t smem_x, smem_y;
+  // band of the boundary Schur term: U c lives in rows bj0..bj1, C reads rows cj0..cj1
+  int bj0, bj1, cj0, cj1;
+  const void* bpiv;           // (bj1-bj0+1) x cols reciprocal pivots of the band systems
+  const void* phi;            // bj0 x cols decay factors below the band
+  const void* psi;            // (rows-1-bj1) x cols decay factors above the band
+  // launch shapes (picked by timing candidates at set-up)
+  int xg_threads, xg_pb;      // x pass: threads per line group, groups per block
+  size_t smem_x;
+  int lpb_y, threads_y;       // y solve: columns per block, threads
+  size_t smem_y;
+};
+
+// spectral correction of the boundary term applied in the final x pass (see k_xpass)
+template <typename T>
+struct YCorr {
+  const T* band;              // (j1-j0+1) x cols band solution; nullptr: no correction
+  const T* phi;               // rows < j0: y[j][k] = phi[j][k] * band[0][k]
+  const T* psi;               // rows > j1: y[j][k] = psi[j-j1-1][k] * band[j1-j0][k]
+  int j0, j1;
 };
 
 // ---- launchers (kernels.cu) ------------------------------------------------
 int configure_kernels(int smem_optin);
 long long kernel_launch_count();
 void kernel_launch_adjust(long long delta);
-// kernel classes for event timing: 1 x pass, 2 y pass, 3 momentum, 4 residual
-void ktimer_enable(int cls);
+// per-launch event timing summed per kernel class (classes listed in kernels.cu)
+static constexpr int KT_CLASSES = 11;
+void ktimer_enable(int on);
 void ktimer_collect();
-void ktimer_read(double* total_ms, long long* count);
-// x = T^{-1} b on the rectangle view; b is read through the active mask when
-// mask_in is set; the output epilogue is
-//   out = active ? (add + sub - T^{-1} b) : 0   when sub != nullptr
-//   out = T^{-1} b                              otherwise.
-void launch_rect_inverse(const TransformTables& tt, const RectView& view, const double* b, bool mask_in,
-                         double* spectral, double* out, const double* sub, const double* add, const Gate& gate,
-                         cudaStream_t st);
-// FP32 separable inverse (tables of tt in float): b (float64 field) -> first (float32 field)
-void launch_rect_inverse_f32(const TransformTables& tt, const RectView& view, const double* b, bool mask_in,
-                             float* spectral, float* first, const Gate& gate, cudaStream_t st);
-// FP32 separable inverse of w2 with the epilogue out = active ? add + (sub - T^{-1} w2) : 0 (float64 out)
-void launch_rect_inverse_f32_final(const TransformTables& tt, const RectView& view, const double* w2,
-                                   float* spectral, double* out, const float* sub, const double* add,
-                                   const Gate& gate, cudaStream_t st);
-void launch_schur_f32(const float* first, const RectView& view, int rank, const int64_t* rows, const int64_t* c_ptr,
-                      const int64_t* c_col, const double* c_val, const double* sinv, double* w2, const Gate& gate,
-                      cudaStream_t st);
-
-void launch_schur(const double* first, const RectView& view, int rank, const int64_t* rows, const int64_t* c_ptr,
-                  const int64_t* c_col, const double* c_val, const double* sinv, double* w2, const Gate& gate,
-                  cudaStream_t st);
+bool ktimer_active();
+void ktimer_read(int cls, double* total_ms, long long* count, double* bytes);
+size_t xpass_smem_per_group(int type, int n, bool fp32);
+size_t ysolve_smem(int rows, int lpb, bool fp32);
+// Row transforms of rows r0..r0+nr-1: forward (tx_fwd) or inverse (tx_inv).  Element (r, e)
+// is read at in[ibase + r*ipitch + e] (zero where icls marks the point inactive), minus the
+// correction when corr.band is set, and written to out[obase + r*opitch + e] (zero where
+// ocls marks the point inactive; add[.] + value when add is set).
+template <typename T, typename TI, typename TO>
+void launch_xpass(const TransformTables& tt, bool inverse, int r0, int nr, const TI* in, int64_t ibase,
+                  int64_t ipitch, const uint8_t* icls, TO* out, int64_t obase, int64_t opitch, const uint8_t* ocls,
+                  const double* add, const YCorr<T>& corr, const Gate& gate, cudaStream_t st);
+// column solves of the spectral array S (rows x cols) in place, input scaled by 1/(2 nx)
+template <typename T>
+void launch_ysolve(const TransformTables& tt, int cols, int rows, T* S, const Gate& gate, cudaStream_t st);
+// band column solves of B ((bj1-bj0+1) x cols) in place, input scaled by 1/(2 nx)
+template <typename T>
+void launch_yband(const TransformTables& tt, int cols, T* B, const Gate& gate, cudaStream_t st);
+// boundary Schur term c = M first[mcols] (M = S^{-1} C), written to w2 at the boundary rows
+template <typename TF>
+void launch_schur(const TF* first, int rank, int m, const int64_t* mcols, const double* M, const int64_t* rows,
+                  double* w2, const Gate& gate, cudaStream_t st);
 
 void launch_ghost(double* field, int n, const int64_t* rows, const int64_t* ptr, const int64_t* col,
                   const double* val, const Gate& gate, cudaStream_t st);
@@ -205,8 +229,18 @@ void launch_ghost(double* field, int n, const int64_t* rows, const int64_t* ptr,
 // residual of the operator of kind (0 pressure A, 1 Helmholtz u, 2 Helmholtz v)
 // res = b - Op x on active points; reductions into sc at check index `check`
 // (check < 0: the index sc->k maintained by launch_refine_decide)
-void launch_residual(const CaseDev& c, int kind, double hc, const double* b, const double* x, double* res,
-                     SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st);
+// Host-formed coefficients of the regular rows of one operator: A x at a point is
+//   cc[ic][jc] x + cw[ic] x_west + ce x_east + cy (x_south + x_north)
+// with ic = 0 first column, 1 interior, 2 last column and jc = 0 wall row, 1 interior.
+struct ResidualCoef {
+  double cc[3][2];
+  double cw[3];
+  double ce, cy;
+};
+void launch_residual(const CaseDev& c, const ResidualCoef& rc, int kind, const double* b, const double* x, void* res,
+                     bool res_f32, SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st);
+void launch_pressure_bound(const CaseDev& c, const ResidualCoef& rc, const double* b, const double* x, SolveCtl* sc,
+                           int nchk, const Gate& gate, cudaStream_t st);
 
 // momentum right-hand side; mode 0 steady AB2, 1 start-up part A, 2 start-up part B
 struct MomentumArgs {
@@ -216,12 +250,18 @@ struct MomentumArgs {
   const double* prev;     // previous advection (mode 0)
   double* now;            // advection output (modes 0, 1)
   double* out;            // rhs (modes 0, 2) or midpoint (mode 1)
+  const float* U32;       // FP32 copies of U and P for the stencils (FP32 mode, mode 0)
+  const float* P32;
   double dt, alpha;
   int mode;
 };
 void launch_momentum(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st);
-// same with the stencil arithmetic in FP32 (inputs, outputs and q + increment in FP64)
+// same with the stencil arithmetic in FP32 (outputs and q + increment in FP64); in mode 0 the
+// stencils read the FP32 copies U32 / P32
 void launch_momentum_f32(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st);
+// FP32 copies of the face grid U (n_f points) and the pressure grid P (n_p points)
+void launch_shadow(const double* U, float* U32, int64_t n_f, const double* P, float* P32, int64_t n_p,
+                   const Gate& gate, cudaStream_t st);
 
 // single operators on face grids (for the operator API)
 void launch_advection(const CaseDev& c, const double* U, double* out, const Gate& gate, cudaStream_t st);
@@ -278,7 +318,6 @@ void launch_refine_decide(StepCtl* ctl, int slot, int nchk, cudaGraphConditional
 // ones; the step's control block is appended to ring[*ridx] and the step counter advances
 void launch_step_end(StepCtl* ctl, unsigned long long* state_max, StepCtl* ring, int* ridx, long long* counter,
                      int cap, cudaStream_t st);
-bool ktimer_active();
 
 // zero/copy helpers
 void launch_copy_active(const uint8_t* cls, int64_t n, const double* src, double* dst, const Gate& gate,

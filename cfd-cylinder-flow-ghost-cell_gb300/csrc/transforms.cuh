@@ -35,14 +35,14 @@ __host__ __device__ inline bool r2r_paired(int t) { return r2r_family(t) != 2; }
 
 template <typename T> struct cplx { T x, y; };
 
-// The threads that cooperate on a set of lines: a whole block (barrier __syncthreads)
-// or one warp (barrier __syncwarp).  tid/n index the group's threads.
+// The threads that cooperate on a set of lines: one warp (barrier __syncwarp), or a
+// group of whole warps synchronised by the named barrier `bar` (1..15) over n threads.
+// tid/n index the group's threads.
 struct Grp {
-  int tid, n;
-  bool warp;
+  int tid, n, bar;
   __device__ __forceinline__ void sync() const {
-    if (warp) __syncwarp();
-    else __syncthreads();
+    if (n == 32) __syncwarp();
+    else asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(n) : "memory");
   }
 };
 

@@ -219,11 +219,14 @@ int gm_divergence_stats_noalloc(const double* u, const double* v, const uint8_t*
 
 /* Number of CUDA kernels this library has launched in this process. */
 int64_t gm_kernel_launches(void);
-/* CUDA-event timing of one kernel class on the stream it runs on: 1 transform x pass,
- * 2 transform y pass, 3 momentum right-hand side, 4 operator residual.  enable = 1 starts
- * (and clears) timing of that class; every call returns the totals so far.  Class 0
- * with enable = 0 stops timing. */
-int gm_kernel_timing(int32_t kernel_class, int32_t enable, double* total_ms, int64_t* count);
+/* CUDA-event timing of every launch on the stream it runs on, summed per kernel class:
+ * 1 row transforms, 2 column solves, 3 momentum right-hand side, 4 operator residual,
+ * 5 Schur GEMV, 6 projection pieces, 7 defect and pressure output, 8 ghost rows,
+ * 9 forces and maxima, 10 gates and loop control.  enable = 1 starts (and clears) timing;
+ * every call returns the totals of kernel_class so far (time, launches and the launches'
+ * algorithmic bytes; any output may be NULL); kernel_class 0 with enable = 0 stops timing.
+ * While timing is on, steps run launch by launch (no graphs). */
+int gm_kernel_timing(int32_t kernel_class, int32_t enable, double* total_ms, int64_t* count, double* bytes);
 
 #ifdef __cplusplus
 }
