@@ -249,6 +249,23 @@ def run_ours(args, w, rank, world):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         step_ms = float(t.item())
     value = cells * world / (step_ms * 1e-3)
+    # phase times of graph-replayed steps (timing events captured into the step graphs)
+    os.environ['GHOSTMAC_PHASE_TIMING'] = '1'
+    phases = []
+    for k in range(5):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        one_step(k + 1)
+        if k >= 2:
+            out = (C.c_double * 14)()
+            L.lib.gm_phase_timing(s._h, out)
+            phases.append(list(out))
+    os.environ.pop('GHOSTMAC_PHASE_TIMING', None)
+    phase_names = ['momentum', 'helmholtz_uv', 'projection_1', 'defect', 'projection_2', 'pressure_forces_gates',
+                   'p1_sweep0_row_pass', 'p1_sweep0_column_solve', 'p1_sweep0_band_row_inverse', 'p1_sweep0_schur',
+                   'p1_sweep0_band_row_forward', 'p1_sweep0_band_solve', 'p1_sweep0_final_row_pass',
+                   'p1_sweep0_residual']
+    phase_ms = {n: float(np.mean([p[i] for p in phases])) for i, n in enumerate(phase_names)}
     # dominant kernel class: per-class CUDA-event time of one launch-by-launch step with the
     # refinement sweeps decided on the host (every launched kernel does work; this NVTX range
     # is what the profiles capture), then that class timed over min(K, 10) such steps with L2
@@ -343,7 +360,7 @@ def run_ours(args, w, rank, world):
                     refinement_sweeps_per_step=dict(pressure=float(np.mean([a for a, _ in sweeps])),
                                                     momentum=float(np.mean([b for _, b in sweeps]))),
                     kernel_class_ms_per_step={KERNEL_CLASSES[c]: v[0] for c, v in per_class.items() if v[1]},
-                    comparison=compare)
+                    graph_phase_ms=phase_ms, comparison=compare)
         print(json.dumps(line), flush=True)
 
 
@@ -362,14 +379,21 @@ def run_ours_batch(args, w, rank, world):
     batch = pkg.CylinderBatch(cases)
     for c in cases:
         c._push()
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device='cuda')
 
-    def step(b, k):
-        rc, diag, done = b.step_raw(dt, 1, first_index=k)
+    def step(b, k, n=1):
+        rc, diag, done = b.step_raw(dt, n, first_index=k)
         b._check(rc)
         for i, c in enumerate(b.cases):
-            c.time = diag[i].time
-        return [diag[i] for i in range(len(b.cases))]
+            c.time = diag[i * n + n - 1].time
+        return [diag[i * n + j] for i in range(len(b.cases)) for j in range(n)]
+
+    def timed(b, k0):
+        # K steps in one call: one graph launch per step, one status readback at the end; the
+        # cases' state (about 1 GB) is far larger than L2, so no flush is needed between steps
+        torch.cuda.synchronize()
+        t_0 = time.perf_counter()
+        d = step(b, k0, args.steps)
+        return (time.perf_counter() - t_0) * 1e3 / args.steps, d
 
     for k in range(max(args.warmup, 3)):
         step(batch, k)
@@ -377,19 +401,12 @@ def run_ours_batch(args, w, rank, world):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     launches0 = L.lib.gm_kernel_launches()
-    times, divs, sweeps = [], [], []
     with ClockSampler(dev) as clocks:
-        for k in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            t_0 = time.perf_counter()
-            d = step(batch, k + 1)
-            times.append((time.perf_counter() - t_0) * 1e3)
-            divs.append(max(x.max_divergence for x in d))
-            sweeps.append(sum(x.pressure_refinement_iterations + x.momentum_refinement_iterations for x in d) / len(d))
+        step_ms, d = timed(batch, max(args.warmup, 3))
+    divs = [x.max_divergence for x in d]
+    sweeps = [x.pressure_refinement_iterations + x.momentum_refinement_iterations for x in d]
     launches = L.lib.gm_kernel_launches() - launches0
     assert max(divs) < 1e-10
-    step_ms = sum(times) / len(times)
     if world > 1:
         t = torch.tensor([step_ms], device='cuda')
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -420,14 +437,7 @@ def run_ours_batch(args, w, rank, world):
             c._push()
         for k in range(max(args.warmup, 3)):
             step(b64, k)
-        t64 = []
-        for k in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            t_0 = time.perf_counter()
-            step(b64, k + 1)
-            t64.append((time.perf_counter() - t_0) * 1e3)
-        ms64 = sum(t64) / len(t64)
+        ms64, _ = timed(b64, max(args.warmup, 3))
         compare = dict(plain_fp64_value=cells / (ms64 * 1e-3), plain_fp64_ms_per_step=ms64,
                        speedup_vs_plain_fp64=ms64 / step_ms)
         b64.close()
@@ -450,8 +460,8 @@ def run_ours_batch(args, w, rank, world):
                     config=dict(workload=args.workload, cases=len(cases), grids=grids, cells_per_step=cells, dt=dt,
                                 precision='fp64 plain' if args.precision == 'fp64' else 'fp32 inverses/stencils, fp64 refinement',
                                 cases_per_gpu=len(cases), parallelism='replicas', setup_s=setup_s,
-                                l2='flushed (256 MB write) between timed steps; step timed on the host around '
-                                   'one graph launch and its status readback',
+                                l2='working set (all cases, about 1 GB) larger than L2; K steps timed on the host '
+                                   'around one batch call (one graph launch per step, one status readback)',
                                 pressure='DCT/DST fast inverse + boundary Schur (direct)'),
                     roofline=dict(bound='hbm', achieved=achieved, peak=peak, unit='GB/s', frac=achieved / peak,
                                   traffic=None, kernel=KERNEL_CLASSES[dominant], peak_source=peak_kind,

@@ -24,7 +24,7 @@ SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_las
            'gm_get_history', 'gm_step', 'gm_apply', 'gm_project', 'gm_pressure_solve', 'gm_rectangle_solve',
            'gm_surface_forces', 'gm_divergence_stats', 'gm_kernel_launches', 'gm_kernel_timing',
            'gm_divergence_stats_noalloc', 'gm_batch_create', 'gm_batch_destroy', 'gm_batch_last_error',
-           'gm_batch_step')
+           'gm_batch_step', 'gm_phase_timing')
 NOALLOC_MAX_CELLS = 1048576
 
 
@@ -97,6 +97,7 @@ def _load():
         'gm_batch_destroy': ([P], C.c_int),
         'gm_batch_last_error': ([P], C.c_char_p),
         'gm_batch_step': ([P, D, I32, I64, P, C.POINTER(StepDiag), P], C.c_int),
+        'gm_phase_timing': ([P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

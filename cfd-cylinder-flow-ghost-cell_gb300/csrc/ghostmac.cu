@@ -76,6 +76,7 @@ struct DBuf {
 struct Csrd {
   DBuf<int64_t> rows, ptr, col;
   DBuf<double> val;
+  DBuf<int32_t> index;  // per grid point: its row in this CSR, or -1 (irregular operator rows)
   int n = 0;
 };
 
@@ -103,6 +104,12 @@ FftPlan make_plan(int M) {
       m /= f;
     }
   p.nstages = s;
+  if (M > 65536) throw CudaError("FFT length above 65536");
+  long long Ns = 1;
+  for (int k = 0; k < s; ++k) {
+    p.ns_magic[k] = Ns == 1 ? 0u : (unsigned)(((1ull << 32) + (unsigned long long)Ns - 1) / (unsigned long long)Ns);
+    Ns *= p.radix[k];
+  }
   return p;
 }
 
@@ -192,6 +199,20 @@ struct gm_handle {
   // per sweep) instead of launching all sweeps gated: then every launched kernel does work,
   // which per-kernel timing and profiling need (environment GHOSTMAC_HOST_REFINE=1)
   bool host_refine = false;
+  // optional timing events between the phases of a step (environment GHOSTMAC_PHASE_TIMING=1
+  // when the step graphs are captured): start, momentum, Helmholtz solves, projection 1,
+  // defect, projection 2, end
+  static constexpr int NPHASE_EV = 7;
+  bool phase_on = false;
+  cudaEvent_t phase_ev[NPHASE_EV] = {};
+  double phase_ms[NPHASE_EV - 1] = {};
+  // with phase timing on, the first sweep of projection 1 also times each of its kernels:
+  // row pass, column solve, band row pass, Schur GEMV, band row pass, band solve, final
+  // row pass, residual
+  static constexpr int NSWEEP_EV = 9;
+  bool sweep_marking = false;
+  cudaEvent_t sweep_ev[NSWEEP_EV] = {};
+  double sweep_ms[NSWEEP_EV - 1] = {};
   struct StepGraph {
     cudaGraphExec_t exec = nullptr;
     const double* key[6] = {};
@@ -228,6 +249,12 @@ void upload_csr(Csrd& d, const std::vector<int64_t>& rows, const gm::Csr& c, cud
   d.ptr.upload(c.ptr, st);
   d.col.upload(cols, st);
   d.val.upload(c.val, st);
+}
+// row index of every point of a grid of `npts` points into the irregular rows (or -1)
+void upload_row_index(Csrd& d, const std::vector<int64_t>& rows, int64_t npts, cudaStream_t st) {
+  std::vector<int32_t> idx((size_t)npts, -1);
+  for (size_t k = 0; k < rows.size(); ++k) idx[(size_t)rows[k]] = (int32_t)k;
+  d.index.upload(idx, st);
 }
 
 std::vector<float> to_f32(const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); }
@@ -340,6 +367,7 @@ void autotune_shapes(gm_handle* h, RectDev& rd, int kind, bool fp32) {
   const RectView& v = rd.view;
   cudaStream_t st = h->st;
   const size_t per = std::max(xpass_smem_per_group(tt.tx_fwd, v.cols, fp32), xpass_smem_per_group(tt.tx_inv, v.cols, fp32));
+  const size_t tabs = std::max(xpass_smem_tables(tt.tx_fwd, v.cols, fp32), xpass_smem_tables(tt.tx_inv, v.cols, fp32));
   double* field = kind == 0 ? h->ptmp.p : h->ftmp.p;
   float* field32 = kind == 0 ? h->pfirst32.p : h->ffirst32.p;
   const Gate open{nullptr, 0, 0};
@@ -349,11 +377,13 @@ void autotune_shapes(gm_handle* h, RectDev& rd, int kind, bool fp32) {
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
+  // a shape whose launch the device refuses (threads x registers) is skipped
   auto time_ms = [&](auto&& body) {
     float best = 1e30f;
     for (int rep = 0; rep < 3; ++rep) {
       CK(cudaEventRecord(e0, st));
       body();
+      if (cudaGetLastError() != cudaSuccess) return 1e30f;
       CK(cudaEventRecord(e1, st));
       CK(cudaEventSynchronize(e1));
       float ms = 0;
@@ -365,12 +395,12 @@ void autotune_shapes(gm_handle* h, RectDev& rd, int kind, bool fp32) {
   // x pass
   float best = 1e30f;
   int bt = 32, bg = 1;
-  for (int gt : {32, 64, 128, 256}) {
+  for (int gt : {64, 128, 256, 512}) {
     for (int gp : {1, 2, 4}) {
-      if (gt * gp > 512 || per * gp > h->smem_optin) continue;
+      if (gt * gp > 512 || tabs + per * gp > h->smem_optin) continue;
       tt.xg_threads = gt;
       tt.xg_pb = gp;
-      tt.smem_x = per * gp;
+      tt.smem_x = tabs + per * gp;
       float ms = time_ms([&] {
         if (fp32) {
           launch_xpass<float, double, float>(tt, false, 0, v.rows, field, v.base, v.pitch, nullptr, h->spectral32.p, 0,
@@ -387,17 +417,18 @@ void autotune_shapes(gm_handle* h, RectDev& rd, int kind, bool fp32) {
       if (ms < best) { best = ms; bt = gt; bg = gp; }
     }
   }
+  if (best >= 1e30f) throw CudaError("row transforms do not fit the shared memory");
   tt.xg_threads = bt;
   tt.xg_pb = bg;
-  tt.smem_x = per * bg;
+  tt.smem_x = tabs + per * bg;
   // column solve
   best = 1e30f;
   int bl = 0;
-  for (int L : {2, 4, 8}) {
-    const int thr = ((std::min(L, v.cols) * tt.ych.P + 31) / 32) * 32;
+  for (int L : {2, 4, 8, 16}) {
+    const int thr = ((L * tt.ych.P + 31) / 32) * 32;
     const size_t sm = ysolve_smem(v.rows, L, fp32);
     if (thr > 1024 || sm > h->smem_optin) continue;
-    tt.lpb_y = std::min(L, v.cols);
+    tt.lpb_y = L;
     tt.threads_y = thr;
     tt.smem_y = sm;
     float ms = time_ms([&] {
@@ -407,7 +438,7 @@ void autotune_shapes(gm_handle* h, RectDev& rd, int kind, bool fp32) {
     if (ms < best) { best = ms; bl = L; }
   }
   if (bl == 0) throw CudaError("separable inverse does not fit the launch limits");
-  tt.lpb_y = std::min(bl, v.cols);
+  tt.lpb_y = bl;
   tt.threads_y = ((tt.lpb_y * tt.ych.P + 31) / 32) * 32;
   tt.smem_y = ysolve_smem(v.rows, bl, fp32);
   CK(cudaEventDestroy(e0));
@@ -680,6 +711,7 @@ void fill_case_dev(gm_handle* h) {
   c.n_ghost_p = h->gp.n; c.gp_rows = h->gp.rows.p; c.gp_ptr = h->gp.ptr.p; c.gp_col = h->gp.col.p; c.gp_val = h->gp.val.p;
   for (int k = 0; k < 3; ++k) {
     c.n_irr[k] = h->irr[k].n; c.irr_rows[k] = h->irr[k].rows.p; c.irr_ptr[k] = h->irr[k].ptr.p;
+    c.irr_index[k] = h->irr[k].index.p;
     c.irr_col[k] = h->irr[k].col.p; c.irr_val[k] = h->irr[k].val.p;
   }
   c.a_nnz = h->a_nnz.p;
@@ -776,11 +808,14 @@ void ghost_p(gm_handle* h, double* P, const Gate& gt) {
 // x = [x +] A_rect^{-1} r with the boundary Schur correction (solver/pressure_schur.py:75-124):
 //   S1 = Y^{-1} F_x r (spectral, all rows); first = F_x^{-1} S1 on the rows the C rows read;
 //   c = S^{-1} C first; B = band solve of F_x (U c); x = F_x^{-1} (S1 - B extended by phi/psi).
+void sweep_mark(gm_handle* h, int k, cudaStream_t st);
+
 template <typename T>
 void schur_inverse(gm_handle* h, RectDev& rd, const TransformTables& tt, const void* r, bool r_f32, double* x,
                    bool accumulate, T* spectral, T* first, T* band, double* w2, const Gate& g, cudaStream_t st) {
   const RectView& v = rd.view;
   const YCorr<T> none{nullptr, nullptr, nullptr, 0, -1};
+  sweep_mark(h, 0, st);
   if constexpr (sizeof(T) == 4) {
     if (r_f32)
       launch_xpass<float, float, float>(tt, false, 0, v.rows, (const float*)r, v.base, v.pitch, v.cls, spectral, 0,
@@ -792,19 +827,28 @@ void schur_inverse(gm_handle* h, RectDev& rd, const TransformTables& tt, const v
     launch_xpass<double, double, double>(tt, false, 0, v.rows, (const double*)r, v.base, v.pitch, v.cls, spectral, 0,
                                          v.cols, nullptr, nullptr, none, g, st);
   }
+  sweep_mark(h, 1, st);
   launch_ysolve<T>(tt, v.cols, v.rows, spectral, g, st);
+  sweep_mark(h, 2, st);
   YCorr<T> corr = none;
   if (rd.rank > 0) {
     launch_xpass<T, T, T>(tt, true, tt.cj0, tt.cj1 - tt.cj0 + 1, spectral, 0, v.cols, nullptr, first, v.base, v.pitch,
                           nullptr, nullptr, none, g, st);
+    sweep_mark(h, 3, st);
     launch_schur<T>(first, rd.rank, rd.mcount, rd.mcols.p, rd.mmat.p, rd.rows.p, w2, g, st);
+    sweep_mark(h, 4, st);
     launch_xpass<T, double, T>(tt, false, tt.bj0, tt.bj1 - tt.bj0 + 1, w2, v.base, v.pitch, nullptr, band,
                                -(int64_t)tt.bj0 * v.cols, v.cols, nullptr, nullptr, none, g, st);
+    sweep_mark(h, 5, st);
     launch_yband<T>(tt, v.cols, band, g, st);
     corr = YCorr<T>{band, (const T*)tt.phi, (const T*)tt.psi, tt.bj0, tt.bj1};
+  } else {
+    for (int k = 3; k <= 5; ++k) sweep_mark(h, k, st);
   }
+  sweep_mark(h, 6, st);
   launch_xpass<T, T, double>(tt, true, 0, v.rows, spectral, 0, v.cols, nullptr, x, v.base, v.pitch, v.cls,
                              accumulate ? x : nullptr, corr, g, st);
+  sweep_mark(h, 7, st);
 }
 
 // r is the FP64 right-hand side, or in the FP32 mode the FP32 residual when r_f32 is set
@@ -832,8 +876,11 @@ void schur_solve_graph(gm_handle* h, int lane, RectDev& rd, int kind, double hc,
   const bool f32 = h->precision == 1;
   void* resb = f32 ? (void*)(kind == 0 ? h->pres32.p : h->fres32.p) : (void*)res;
   (void)hc;
+  h->sweep_marking = h->phase_on && slot == S_P1;
   apply_inverse(h, lane, rd, kind, b, false, x, false, first, w2, g0, st);
   launch_residual(h->cd, h->rcoef[kind], kind, b, x, resb, f32, sc, 0, true, g0, st);
+  sweep_mark(h, 8, st);
+  h->sweep_marking = false;
   cudaStreamCaptureStatus cs;
   cudaGraph_t graph;
   const cudaGraphNode_t* deps = nullptr;
@@ -926,6 +973,8 @@ void ensure_helmholtz(gm_handle* h, double dt) {
   build_class_maps(h);
   upload_csr(h->irr[1], h->hs.rows_irr[0], h->hs.irr[0], h->st);
   upload_csr(h->irr[2], h->hs.rows_irr[1], h->hs.irr[1], h->st);
+  upload_row_index(h->irr[1], h->hs.rows_irr[0], h->g.usize, h->st);
+  upload_row_index(h->irr[2], h->hs.rows_irr[1], h->g.vsize, h->st);
   // v irregular rows are v-grid flat indices (columns too)
   fill_case_dev(h);
   build_rect_tables(h, h->ru, 1, dt);
@@ -945,8 +994,19 @@ void momentum(gm_handle* h, const MomentumArgs& ma, const Gate& g0) {
 // screen: 1/0 run or skip the CFL screen, -1 decide on the device from the step counter.
 // The error word of the control block is sticky: only the per-step slots are cleared, so
 // every kernel after a failed gate (also in later captured steps) does nothing.
+void sweep_mark(gm_handle* h, int k, cudaStream_t st) {
+  if (h->sweep_marking) CK(cudaEventRecordWithFlags(h->sweep_ev[k], st, h->capturing ? cudaEventRecordExternal : 0));
+}
+
+void phase_mark(gm_handle* h, int k, cudaStream_t st) {
+  // inside a capture an event record node needs the external flag (a plain record only
+  // orders the captured streams)
+  if (h->phase_on) CK(cudaEventRecordWithFlags(h->phase_ev[k], st, h->capturing ? cudaEventRecordExternal : 0));
+}
+
 void step_once(gm_handle* h, double dt, int screen) {
   cudaStream_t st = h->st;
+  phase_mark(h, 0, st);
   const double hdt = 0.5 * dt;
   const double hc = (0.5 * dt) * h->g.nu;
   Gate g0 = gate_of(h);
@@ -986,6 +1046,7 @@ void step_once(gm_handle* h, double dt, int screen) {
     }
     momentum(h, ma, g0);
   }
+  phase_mark(h, 1, st);
   // CN Helmholtz solves for u and v (solver/optimized_ghost_cell.py:247-254)
   // (independent systems on disjoint parts of the face arrays: u on this stream, v on the
   // second lane, joined before the momentum gate)
@@ -996,10 +1057,14 @@ void step_once(gm_handle* h, double dt, int screen) {
   CK(cudaEventRecord(h->ev_join, h->st2));
   CK(cudaStreamWaitEvent(st, h->ev_join, 0));
   launch_gate_momentum(h->ctl.p, h->nchk, st);
+  phase_mark(h, 2, st);
   // projection of the CN velocity, defect correction and the pressure increment
   project(h, h->star.p, dt, h->Unext.p, h->pphi.p, S_P1, 1);
+  phase_mark(h, 3, st);
   launch_defect(h->cd, h->Unext.p, h->rhs.p, hdt, h->faction.p, h->fproj.p, g0, st);
+  phase_mark(h, 4, st);
   project(h, h->fproj.p, dt, h->fproj2.p, h->pinc.p, S_P2, 2);
+  phase_mark(h, 5, st);
   ghost_p(h, h->pinc.p, g0);
   double factor = first ? 1.0 : dt / (dt + h->prev_dt);
   launch_pressure_out(h->cd, h->phalf.p, h->pinc.p, factor, dt, h->faction.p, h->rhs.p, h->phalf_next.p, h->pout.p,
@@ -1009,6 +1074,7 @@ void step_once(gm_handle* h, double dt, int screen) {
   launch_maxabs(h->cd, h->Unext.p, &h->ctl.p->umax, &h->ctl.p->vmax, g0, st);
   launch_forces(h->cd, h->Unext.p, h->pout.p, h->g.nu * h->g.rho, dt, h->ctl.p, 1, nullptr, g0, st);
   launch_step_end(h->ctl.p, h->state_max.p, h->ring.p, h->ridx.p, h->counter.p, gm_handle::RING_CAP, st);
+  phase_mark(h, 6, st);
   CK(cudaGetLastError());
 }
 
@@ -1219,6 +1285,7 @@ int gm_create(const gm_config* cfg, gm_handle** out) {
     }
     upload_csr(H->gp, g.gp_rows, g.gp, st);
     upload_csr(H->irr[0], g.a_rows, g.a_irr, st);
+    upload_row_index(H->irr[0], g.a_rows, g.psize, st);
     H->a_nnz.upload(g.a_nnz_row, st);
     H->sp_ptr.upload(g.surf_p.ptr, st); H->sp_col.upload(g.surf_p.col, st); H->sp_val.upload(g.surf_p.val, st);
     H->su_ptr.upload(g.dudn.ptr, st); H->su_col.upload(g.dudn.col, st); H->su_val.upload(g.dudn.val, st);
@@ -1318,6 +1385,10 @@ int gm_destroy(gm_handle* h) {
   if (h->st2) cudaStreamDestroy(h->st2);
   if (h->st2_body) cudaStreamDestroy(h->st2_body);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  for (auto& e : h->phase_ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : h->sweep_ev)
+    if (e) cudaEventDestroy(e);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
   cudaStream_t st = h->st;
   bool own = h->own_stream;
@@ -1501,6 +1572,18 @@ int gm_step(gm_handle* h, double dt, int32_t n_steps, int64_t first_step_index, 
   if (!(std::isfinite(dt) && dt > 0) || n_steps <= 0) { h->err = "dt must be finite and positive"; return GM_EVALUE; }
   const char* hr = std::getenv("GHOSTMAC_HOST_REFINE");
   h->host_refine = hr && hr[0] == '1';
+  const char* pt = std::getenv("GHOSTMAC_PHASE_TIMING");
+  const bool phase = pt && pt[0] == '1';
+  if (phase != h->phase_on) {
+    // the events become graph nodes: recapture the step graphs with or without them
+    for (auto& gr : h->graphs)
+      if (gr.exec) { cudaGraphExecDestroy(gr.exec); gr.exec = nullptr; }
+    if (phase && !h->phase_ev[0]) {
+      for (auto& e : h->phase_ev) cudaEventCreate(&e);
+      for (auto& e : h->sweep_ev) cudaEventCreate(&e);
+    }
+    h->phase_on = phase;
+  }
   return run_guarded(h, [&] {
     ensure_helmholtz(h, dt);
     cudaStream_t st = h->st;
@@ -1527,6 +1610,17 @@ int gm_step(gm_handle* h, double dt, int32_t n_steps, int64_t first_step_index, 
       CK(cudaMemcpyAsync(h->host_ring, h->ring.p, batch * sizeof(StepCtl), cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
       ktimer_collect();
+      if (h->phase_on && !first)
+        for (int k = 0; k + 1 < gm_handle::NPHASE_EV; ++k) {
+          float ms = 0;
+          if (cudaEventElapsedTime(&ms, h->phase_ev[k], h->phase_ev[k + 1]) == cudaSuccess) h->phase_ms[k] = ms;
+        }
+      if (h->phase_on && !first)
+        for (int k = 0; k + 1 < gm_handle::NSWEEP_EV; ++k) {
+          float ms = 0;
+          if (cudaEventElapsedTime(&ms, h->sweep_ev[k], h->sweep_ev[k + 1]) == cudaSuccess) h->sweep_ms[k] = ms;
+        }
+      cudaGetLastError();
       int good = 0;
       while (good < batch && h->host_ring[good].err == 0) ++good;
       if (!direct) {
@@ -1787,6 +1881,13 @@ int gm_divergence_stats(gm_handle* h, const double* u, const double* v, double o
 extern "C" {
 
 int64_t gm_kernel_launches(void) { return (int64_t)kernel_launch_count(); }
+
+int gm_phase_timing(const gm_handle* h, double out[14]) {
+  if (!h || !out) return GM_EVALUE;
+  for (int k = 0; k < 6; ++k) out[k] = h->phase_ms[k];
+  for (int k = 0; k < 8; ++k) out[6 + k] = h->sweep_ms[k];
+  return GM_OK;
+}
 
 int gm_kernel_timing(int32_t kernel_class, int32_t enable, double* total_ms, int64_t* count, double* bytes) {
   if (enable) ktimer_enable(1);

@@ -150,8 +150,23 @@ __host__ __device__ inline size_t xpass_group_smem(int type, int n) {
   size_t stage = ((size_t)lpw * n * sizeof(T) + 15) / 16 * 16;
   return stage + 2 * (size_t)r2r_buffer_elems(type, n, lpw) * sizeof(cplx<T>);
 }
+// lengths (complex entries) of the FFT twiddles, the pre- and the post-twiddles of a transform
+__host__ __device__ inline int xpass_tw_len(int type, int n, int which) {
+  const int fam = r2r_family(type);
+  if (which == 0) return r2r_fft_length(type, n);
+  if (which == 1) return fam == 2 ? n / 2 : 1;
+  return fam == 2 ? n / 2 : (fam == 3 ? 1 : n);
+}
+template <typename T>
+__host__ __device__ inline size_t xpass_tw_bytes(int type, int n) {
+  return ((size_t)(xpass_tw_len(type, n, 0) + xpass_tw_len(type, n, 1) + xpass_tw_len(type, n, 2)) * sizeof(cplx<T>) +
+          15) / 16 * 16;
+}
 size_t xpass_smem_per_group(int type, int n, bool fp32) {
   return fp32 ? xpass_group_smem<float>(type, n) : xpass_group_smem<double>(type, n);
+}
+size_t xpass_smem_tables(int type, int n, bool fp32) {
+  return fp32 ? xpass_tw_bytes<float>(type, n) : xpass_tw_bytes<double>(type, n);
 }
 
 static constexpr int XB = 4;  // loads batched per thread in the row passes
@@ -162,12 +177,20 @@ __global__ void k_xpass(int n, int r0, int nr, int type, FftPlan plan, R2RTables
                         YCorr<T> corr, int gthreads, int gpb, Gate gate) {
   if (!gate_open(gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // the twiddle tables go to shared memory first (read by every stage of every group: a
+  // global load per stage would put an L2 round trip on each stage's critical path)
+  const int ntw[3] = {xpass_tw_len(type, n, 0), xpass_tw_len(type, n, 1), xpass_tw_len(type, n, 2)};
+  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
+  for (int q = threadIdx.x; q < ntw[0] + ntw[1] + ntw[2]; q += blockDim.x)
+    tw[q] = q < ntw[0] ? tb.W[q] : (q < ntw[0] + ntw[1] ? tb.pre[q - ntw[0]] : tb.post[q - ntw[0] - ntw[1]]);
+  __syncthreads();
+  const R2RTables<T> ts{tw, tw + ntw[0], tw + ntw[0] + ntw[1]};
   const int grp = threadIdx.x / gthreads, tid = threadIdx.x - grp * gthreads;
   const int lpw = r2r_paired(type) ? 2 : 1;
   const int l0 = (blockIdx.x * gpb + grp) * lpw;
   if (grp >= gpb || l0 >= nr) return;  // whole groups leave; every group has its own barrier
   const int nl = min(lpw, nr - l0);
-  unsigned char* mine = smem_raw + (size_t)grp * xpass_group_smem<T>(type, n);
+  unsigned char* mine = smem_raw + xpass_tw_bytes<T>(type, n) + (size_t)grp * xpass_group_smem<T>(type, n);
   T* stage = reinterpret_cast<T*>(mine);
   const size_t stage_bytes = ((size_t)lpw * n * sizeof(T) + 15) / 16 * 16;
   cplx<T>* a = reinterpret_cast<cplx<T>*>(mine + stage_bytes);
@@ -211,7 +234,7 @@ __global__ void k_xpass(int n, int r0, int nr, int type, FftPlan plan, R2RTables
     }
   }
   G.sync();
-  r2r_lines<T>(type, stage, n, nl, a, b, plan, tb, G);
+  r2r_lines<T>(type, stage, n, nl, a, b, plan, ts, G);
   for (int l = 0; l < nl; ++l) {
     const int64_t row = obase + (int64_t)(r0 + l0 + l) * opitch;
     for (int e0 = tid; e0 < n; e0 += XB * gthreads) {
@@ -290,50 +313,55 @@ template void launch_xpass<float, float, double>(const TransformTables&, bool, i
 // The data and every coefficient of the two recurrences are staged in shared memory
 // first, so the dependent chains wait on shared-memory latency only.
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, int L>
 __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale, const T* __restrict__ t0,
-                         const T* __restrict__ t1, const T* __restrict__ t2, T* __restrict__ S, int lpb, Gate gate) {
+                         const T* __restrict__ t1, const T* __restrict__ t2, T* __restrict__ S, Gate gate) {
+  // L consecutive columns per block (L a power of two: thread -> (column, row/chunk) by shifts)
   if (!gate_open(gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int ns = n | 1;                                  // odd stride between the columns
-  T* col = reinterpret_cast<T*>(smem_raw);              // lpb x ns values
-  T* piv = col + (size_t)lpb * ns;                       // lpb x ns reciprocal pivots
-  T* isub = piv + (size_t)lpb * ns;                      // lpb x YCHUNK_MAX interface coefficients
-  T* isup = isub + (size_t)lpb * YCHUNK_MAX;
-  const int c0 = blockIdx.x * lpb;
-  const int nl = min(lpb, cols - c0);
+  T* col = reinterpret_cast<T*>(smem_raw);              // L x ns values
+  T* piv = col + (size_t)L * ns;                         // L x ns reciprocal pivots
+  T* isub = piv + (size_t)L * ns;                        // L x YCHUNK_MAX interface coefficients
+  T* isup = isub + (size_t)L * YCHUNK_MAX;
+  const int c0 = blockIdx.x * L;
   const int P = ch.P;
-  for (int t0i = threadIdx.x; t0i < nl * n; t0i += 8 * blockDim.x) {
+  const int l = threadIdx.x & (L - 1);                   // column of this thread
+  const int rsub = threadIdx.x / L;                      // row offset (load/store), chunk (solve)
+  const int rstep = blockDim.x / L;
+  const bool colok = c0 + l < cols;
+  const T* s_in = S + c0 + l;
+  const T* p_in = t0 + c0 + l;
+  // load: 8 rows in flight per thread
+  for (int e0 = rsub; e0 < n; e0 += 8 * rstep) {
     T sv[8], pvv[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
-      const int t = t0i + u * blockDim.x;
-      if (t < nl * n) {
-        const int l = t % nl, e = t / nl;
-        const int64_t o = (int64_t)e * cols + c0 + l;
-        sv[u] = S[o];
-        pvv[u] = t0[o];
+      const int e = e0 + u * rstep;
+      if (colok && e < n) {
+        sv[u] = s_in[(int64_t)e * cols];
+        pvv[u] = p_in[(int64_t)e * cols];
       }
     }
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
-      const int t = t0i + u * blockDim.x;
-      if (t < nl * n) {
-        const int l = t % nl, e = t / nl;
+      const int e = e0 + u * rstep;
+      if (colok && e < n) {
         col[l * ns + e] = sv[u] * scale;
         piv[l * ns + e] = pvv[u];
       }
     }
   }
-  for (int t = threadIdx.x; t < nl * (P - 1); t += blockDim.x) {
-    const int l = t % nl, q = t / nl;
-    const int64_t o = (int64_t)(ch.end[q] + 1) * cols + c0 + l;
-    isub[l * YCHUNK_MAX + q] = t1[o];
-    isup[l * YCHUNK_MAX + q] = t2[o];
+  for (int q = rsub; q < P - 1; q += rstep) {
+    if (colok) {
+      const int64_t o = (int64_t)(ch.end[q] + 1) * cols + c0 + l;
+      isub[l * YCHUNK_MAX + q] = t1[o];
+      isup[l * YCHUNK_MAX + q] = t2[o];
+    }
   }
   __syncthreads();
-  const int l = threadIdx.x % lpb, p = threadIdx.x / lpb;
-  const bool work = l < nl && p < P;
+  const int p = rsub;
+  const bool work = colok && p < P;
   int a = 0, b = -1;
   if (work) { a = ch.start[p]; b = ch.end[p]; }
   T* x = col + l * ns;
@@ -354,7 +382,7 @@ __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale,
   }
   __syncthreads();
   // phase 2: interface system, one thread per column
-  if (p == 0 && l < nl && P > 1) {
+  if (p == 0 && colok && P > 1) {
     const T* su = isub + l * YCHUNK_MAX;
     const T* sp = isup + l * YCHUNK_MAX;
     T z = 0;
@@ -372,7 +400,7 @@ __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale,
     }
   }
   __syncthreads();
-  // phase 3: spike corrections of the inner rows (independent loads)
+  // phase 3: spike corrections of the inner rows (8 table rows in flight)
   if (work && P > 1) {
     const T yl = p > 0 ? x[ch.end[p - 1] + 1] : (T)0;
     const T yr = p < P - 1 ? x[b + 1] : (T)0;
@@ -392,10 +420,9 @@ __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale,
     }
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
-    const int ll = t % nl, e = t / nl;
-    S[(int64_t)e * cols + c0 + ll] = col[ll * ns + e];
-  }
+  T* s_out = S + c0 + l;
+  if (colok)
+    for (int e = rsub; e < n; e += rstep) s_out[(int64_t)e * cols] = col[l * ns + e];
 }
 size_t ysolve_smem(int rows, int lpb, bool fp32) {
   const size_t esz = fp32 ? 4 : 8;
@@ -407,9 +434,16 @@ void launch_ysolve(const TransformTables& tt, int cols, int rows, T* S, const Ga
   const unsigned gy = (unsigned)((cols + tt.lpb_y - 1) / tt.lpb_y);
   note_launch();
   kt_mark(2, st);
-  k_ysolve<T><<<gy, tt.threads_y, tt.smem_y, st>>>(rows, cols, tt.ych, (T)tt.gamma, (T)tt.yscale,
-                                                   (const T*)tt.t0, (const T*)tt.t1, (const T*)tt.t2, S, tt.lpb_y,
-                                                   gate);
+#define GM_YSOLVE(LL)                                                                                        \
+  k_ysolve<T, LL><<<gy, tt.threads_y, tt.smem_y, st>>>(rows, cols, tt.ych, (T)tt.gamma, (T)tt.yscale,       \
+                                                       (const T*)tt.t0, (const T*)tt.t1, (const T*)tt.t2, S, gate)
+  switch (tt.lpb_y) {
+    case 2: GM_YSOLVE(2); break;
+    case 4: GM_YSOLVE(4); break;
+    case 8: GM_YSOLVE(8); break;
+    default: GM_YSOLVE(16); break;
+  }
+#undef GM_YSOLVE
   kt_mark(2, st, (double)rows * cols * sizeof(T) * 5);  // data in and out, three table entries per point
 }
 template void launch_ysolve<double>(const TransformTables&, int, int, double*, const Gate&, cudaStream_t);
@@ -430,16 +464,26 @@ __global__ void k_yband(int nb, int cols, T gamma, T scale, const T* __restrict_
   T* xb = reinterpret_cast<T*>(smem_raw);  // nb x nc
   T* pb = xb + (size_t)nb * nc;
   const int k0 = blockIdx.x * nc;
-  for (int t = threadIdx.x; t < nb * nc; t += nc) {
-    const int j = t / nc, kk = t - j * nc;
-    if (k0 + kk < cols) {
-      const int64_t o = (int64_t)j * cols + k0 + kk;
-      xb[t] = B[o] * scale;
-      pb[t] = bpiv[o];
+  const int kk = threadIdx.x;
+  if (k0 + kk < cols) {
+    for (int j0 = 0; j0 < nb; j0 += 8) {  // 8 rows in flight per thread
+      T bv[8], pv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (j0 + u < nb) {
+          const int64_t o = (int64_t)(j0 + u) * cols + k0 + kk;
+          bv[u] = B[o];
+          pv[u] = bpiv[o];
+        }
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (j0 + u < nb) {
+          xb[(j0 + u) * nc + kk] = bv[u] * scale;
+          pb[(j0 + u) * nc + kk] = pv[u];
+        }
     }
   }
   __syncthreads();
-  const int kk = threadIdx.x;
   if (k0 + kk < cols) {
     T z = 0;
     for (int j = 0; j < nb; ++j) {
@@ -452,11 +496,8 @@ __global__ void k_yband(int nb, int cols, T gamma, T scale, const T* __restrict_
       xb[j * nc + kk] = y;
     }
   }
-  __syncthreads();
-  for (int t = threadIdx.x; t < nb * nc; t += nc) {
-    const int j = t / nc, c2 = t - j * nc;
-    if (k0 + c2 < cols) B[(int64_t)j * cols + k0 + c2] = xb[t];
-  }
+  if (k0 + kk < cols)
+    for (int j = 0; j < nb; ++j) B[(int64_t)j * cols + k0 + kk] = xb[j * nc + kk];
 }
 template <typename T>
 void launch_yband(const TransformTables& tt, int cols, T* B, const Gate& gate, cudaStream_t st) {
@@ -489,15 +530,21 @@ int configure_kernels(int smem_optin) {
   d = std::min(d, allow_dynamic_smem(k_xpass<float, double, float>, smem_optin));
   d = std::min(d, allow_dynamic_smem(k_xpass<float, float, float>, smem_optin));
   d = std::min(d, allow_dynamic_smem(k_xpass<float, float, double>, smem_optin));
-  d = std::min(d, allow_dynamic_smem(k_ysolve<double>, smem_optin));
-  d = std::min(d, allow_dynamic_smem(k_ysolve<float>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve<double, 2>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve<double, 4>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve<double, 8>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve<double, 16>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve<float, 2>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve<float, 4>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve<float, 8>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve<float, 16>, smem_optin));
   return d;
 }
 
 // ---------------------------------------------------------------------------
 // boundary Schur correction: c = S^{-1} (C first), scattered into w2
 // ---------------------------------------------------------------------------
-static constexpr int SCHUR_ROWS = 16;
+static constexpr int SCHUR_ROWS = 4;
 // c = M first[mcols] with M = S^{-1} C (rank x m, FP64), scattered to w2 at the boundary rows.
 // Every block gathers the m points into shared memory (independent loads), then its warps
 // take SCHUR_ROWS rows of the GEMV (lanes over the row, FP64 accumulation).
@@ -507,14 +554,26 @@ __global__ void k_schur(const TF* __restrict__ first, int rank, int m, const int
                         Gate gate) {
   if (!gate_open(gate)) return;
   extern __shared__ double gsh[];
-  for (int q = threadIdx.x; q < m; q += blockDim.x) gsh[q] = (double)first[mcols[q]];
+  for (int q0 = threadIdx.x; q0 < m; q0 += 4 * blockDim.x) {
+    int64_t ix[4];
+    TF fv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (q0 + u * (int)blockDim.x < m) ix[u] = mcols[q0 + u * blockDim.x];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (q0 + u * (int)blockDim.x < m) fv[u] = first[ix[u]];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (q0 + u * (int)blockDim.x < m) gsh[q0 + u * blockDim.x] = (double)fv[u];
+  }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int r0 = blockIdx.x * SCHUR_ROWS;
   for (int r = r0 + warp; r < min(rank, r0 + SCHUR_ROWS); r += nw) {
     const double* mr = M + (int64_t)r * m;
     double acc = 0.0;
-#pragma unroll 4
+#pragma unroll 8
     for (int q = lane; q < m; q += 32) acc += mr[q] * gsh[q];
     acc = warp_sum(acc);
     if (lane == 0) w2[rows[r]] = acc;
@@ -528,7 +587,7 @@ void launch_schur(const TF* first, int rank, int m, const int64_t* mcols, const 
   const unsigned g = (unsigned)((rank + SCHUR_ROWS - 1) / SCHUR_ROWS);
   note_launch();
   kt_mark(5, st);
-  k_schur<TF><<<g, 256, (size_t)m * sizeof(double), st>>>(first, rank, m, mcols, M, rows, w2, gate);
+  k_schur<TF><<<g, 32 * SCHUR_ROWS, (size_t)m * sizeof(double), st>>>(first, rank, m, mcols, M, rows, w2, gate);
   kt_mark(5, st, (double)m * (sizeof(TF) + 8) + (double)rank * m * 8 + rank * 16.0);
 }
 template void launch_schur<double>(const double*, int, int, const int64_t*, const double*, const int64_t*, double*,
@@ -811,16 +870,6 @@ void launch_gradient(const CaseDev& c, const double* P, double* out, const Gate&
 // ---------------------------------------------------------------------------
 // residual of the pressure operator A or the Helmholtz operators
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int find_row(const int64_t* rows, int n, int64_t key) {
-  int lo = 0, hi = n - 1;
-  while (lo <= hi) {
-    int mid = (lo + hi) >> 1;
-    int64_t v = rows[mid];
-    if (v == key) return mid;
-    if (v < key) lo = mid + 1; else hi = mid - 1;
-  }
-  return -1;
-}
 
 // Residual res = b - A x of the pressure operator A (KIND 0, p grid) or the Helmholtz
 // operators I - c L (KIND 1 u faces, KIND 2 v faces), with max |res| and sum res^2 per check.
@@ -828,6 +877,17 @@ __device__ __forceinline__ int find_row(const int64_t* rows, int n, int64_t key)
 // the host (ResidualCoef): two adds and three multiply-adds per point.  RES_F32: the residual
 // is stored in FP32 (the input of the FP32 inverse; its norms are still taken in FP64) and
 // the roundoff bound is left to k_pressure_bound after the refinement loop.
+// coefficient selection by value (indexing the parameter struct would copy it to local memory)
+__device__ __forceinline__ double coef_cc(const ResidualCoef& rc, int ic, int jc) {
+  const double c0 = jc ? rc.cc[0][1] : rc.cc[0][0];
+  const double c1 = jc ? rc.cc[1][1] : rc.cc[1][0];
+  const double c2 = jc ? rc.cc[2][1] : rc.cc[2][0];
+  return ic == 0 ? c0 : (ic == 1 ? c1 : c2);
+}
+__device__ __forceinline__ double coef_cw(const ResidualCoef& rc, int ic) {
+  return ic == 0 ? rc.cw[0] : (ic == 1 ? rc.cw[1] : rc.cw[2]);
+}
+
 template <int KIND, bool RES_F32>
 __global__ void k_residual(CaseDev c, ResidualCoef rc, const double* __restrict__ b, const double* __restrict__ x,
                            void* __restrict__ res_out, SolveCtl* sc, int check, int first, Gate gate) {
@@ -852,7 +912,7 @@ __global__ void k_residual(CaseDev c, ResidualCoef rc, const double* __restrict_
     const double xv = x[f], bv = b[f];
     double ax, aabs = 0.0;
     int nnz = 0;
-    const int row = (k & CLS_IRREG) ? find_row(c.irr_rows[KIND], c.n_irr[KIND], t) : -1;
+    const int row = (k & CLS_IRREG) ? c.irr_index[KIND][t] : -1;
     if (row >= 0) {
       const int64_t* cp = c.irr_ptr[KIND];
       ax = 0.0;
@@ -891,9 +951,10 @@ __global__ void k_residual(CaseDev c, ResidualCoef rc, const double* __restrict_
         jc = 1;
       }
       // A x = cc x + cw xw + ce xe + cy (xs + xn); Helmholtz rows carry the factors of I - c L
-      ax = rc.cc[ic][jc] * xv + rc.cw[ic] * xw + rc.ce * xe + rc.cy * (xs + xn);
+      const double ccv = coef_cc(rc, ic, jc), cwv = coef_cw(rc, ic);
+      ax = ccv * xv + cwv * xw + rc.ce * xe + rc.cy * (xs + xn);
       if (KIND == 0 && !RES_F32) {
-        aabs = fabs(rc.cc[ic][jc]) * fabs(xv) + rc.ce * (fabs(xw) + fabs(xe)) + rc.cy * (fabs(xs) + fabs(xn));
+        aabs = fabs(ccv) * fabs(xv) + rc.ce * (fabs(xw) + fabs(xe)) + rc.cy * (fabs(xs) + fabs(xn));
         nnz = c.a_nnz[t];
       }
     }
@@ -903,7 +964,7 @@ __global__ void k_residual(CaseDev c, ResidualCoef rc, const double* __restrict_
     rs += r * r;
     if (KIND == 0 && !RES_F32) bd = umax64(bd, dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + fabs(bv))));
     if (first) { bm = umax64(bm, absbits(bv)); bs += bv * bv; }
-    if (!isfinite(xv)) xb = 1;
+    if ((dbits(xv) & 0x7ff0000000000000ull) == 0x7ff0000000000000ull) xb = 1;  // Inf or NaN, by the bits
   }
   block_commit_max(rm, &sc->rmax[check]);
   block_commit_sum(rs, &sc->rsq[check]);
@@ -949,7 +1010,7 @@ __global__ void k_pressure_bound(CaseDev c, ResidualCoef rc, const double* __res
     const double xv = x[t], bv = b[t];
     double aabs = 0.0;
     int nnz;
-    const int row = (k & CLS_IRREG) ? find_row(c.irr_rows[0], c.n_irr[0], t) : -1;
+    const int row = (k & CLS_IRREG) ? c.irr_index[0][t] : -1;
     if (row >= 0) {
       const int64_t* cp = c.irr_ptr[0];
       for (int64_t e = cp[row]; e < cp[row + 1]; ++e) aabs += fabs(c.irr_val[0][e]) * fabs(x[c.irr_col[0][e]]);
@@ -959,7 +1020,7 @@ __global__ void k_pressure_bound(CaseDev c, ResidualCoef rc, const double* __res
       double xw = i > 0 ? x[t - 1] : 0.0, xe = i < nx - 1 ? x[t + 1] : 0.0;
       double xs = j > 0 ? x[t - nx] : 0.0, xn = j < ny - 1 ? x[t + nx] : 0.0;
       const int ic = i == 0 ? 0 : (i == nx - 1 ? 2 : 1), jc = (j == 0 || j == ny - 1) ? 0 : 1;
-      aabs = fabs(rc.cc[ic][jc]) * fabs(xv) + rc.ce * (fabs(xw) + fabs(xe)) + rc.cy * (fabs(xs) + fabs(xn));
+      aabs = fabs(coef_cc(rc, ic, jc)) * fabs(xv) + rc.ce * (fabs(xw) + fabs(xe)) + rc.cy * (fabs(xs) + fabs(xn));
       nnz = c.a_nnz[t];
     }
     bd = umax64(bd, dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + fabs(bv))));

@@ -127,6 +127,7 @@ struct CaseDev {
   // irregular rows: pressure A (p grid), Helmholtz u (u grid), v (v grid)
   int n_irr[3];
   const int64_t* irr_rows[3]; const int64_t* irr_ptr[3]; const int64_t* irr_col[3]; const double* irr_val[3];
+  const int32_t* irr_index[3];  // per grid point: row in the irregular CSR or -1
   const int32_t* a_nnz;     // psize: nnz of A rows (roundoff weights)
   // surface quadrature
   int n_surf;
@@ -203,6 +204,7 @@ void ktimer_collect();
 bool ktimer_active();
 void ktimer_read(int cls, double* total_ms, long long* count, double* bytes);
 size_t xpass_smem_per_group(int type, int n, bool fp32);
+size_t xpass_smem_tables(int type, int n, bool fp32);  // twiddle tables staged once per block
 size_t ysolve_smem(int rows, int lpb, bool fp32);
 // Row transforms of rows r0..r0+nr-1: forward (tx_fwd) or inverse (tx_inv).  Element (r, e)
 // is read at in[ibase + r*ipitch + e] (zero where icls marks the point inactive), minus the

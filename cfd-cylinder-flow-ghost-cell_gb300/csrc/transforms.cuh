@@ -61,6 +61,7 @@ struct FftPlan {
   int M;
   int nstages;
   int radix[20];
+  unsigned ns_magic[20];  // ceil(2^32 / Ns) of stage s (Ns = product of the earlier radices; 0 when Ns = 1)
 };
 
 // One radix-R butterfly on v[0..R) in place; dir = -1 forward, +1 inverse.
@@ -132,61 +133,70 @@ __device__ __forceinline__ void dft_small(cplx<T>* v, int dir) {
   }
 }
 
+// j / Ns for j < 2^16 and Ns <= 2^16 by one high multiply: floor(j * ceil(2^32/Ns) / 2^32)
+// is exact there (the error term j * e / (Ns 2^32) stays below 1/Ns).
+__device__ __forceinline__ int div_ns(int j, int Ns, unsigned magic) {
+  return Ns == 1 ? j : (int)__umulhi((unsigned)j, magic);
+}
+
 // One Stockham stage for radix R (compile-time) over nfft transforms of length M.
 template <typename T, int R>
 __device__ __forceinline__ void stage_fixed(const cplx<T>* __restrict__ in, cplx<T>* __restrict__ out, int M,
-                                            int nfft, int Ns, const cplx<T>* __restrict__ W, int dir, const Grp& G) {
+                                            int nfft, int Ns, unsigned magic, const cplx<T>* __restrict__ W, int dir,
+                                            const Grp& G) {
   const int MR = M / R;
   const int tws = M / (Ns * R);
-  for (int t = G.tid; t < nfft * MR; t += G.n) {
-    int f = t / MR, j = t - f * MR;
+  for (int f = 0; f < nfft; ++f) {
     const cplx<T>* src = in + (size_t)f * M;
     cplx<T>* dst = out + (size_t)f * M;
-    int k = j % Ns;
-    cplx<T> v[R];
+    for (int j = G.tid; j < MR; j += G.n) {
+      const int jq = div_ns(j, Ns, magic);
+      const int k = j - jq * Ns;
+      cplx<T> v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      cplx<T> a = src[j + r * MR];
-      if (r > 0 && k > 0) {
-        cplx<T> w = W[r * k * tws];
-        if (dir > 0) w.y = -w.y;
-        a = cmul(a, w);
+      for (int r = 0; r < R; ++r) {
+        cplx<T> a = src[j + r * MR];
+        if (r > 0 && k > 0) {
+          cplx<T> w = W[r * k * tws];
+          if (dir > 0) w.y = -w.y;
+          a = cmul(a, w);
+        }
+        v[r] = a;
       }
-      v[r] = a;
-    }
-    dft_small<T, R>(v, dir);
-    int base = (j / Ns) * Ns * R + k;
+      dft_small<T, R>(v, dir);
+      const int base = jq * Ns * R + k;
 #pragma unroll
-    for (int q = 0; q < R; ++q) dst[base + q * Ns] = v[q];
+      for (int q = 0; q < R; ++q) dst[base + q * Ns] = v[q];
+    }
   }
 }
 
 // Generic odd radix (any R up to 64): direct R-point DFT per output.
 template <typename T>
 __device__ void stage_generic(const cplx<T>* __restrict__ in, cplx<T>* __restrict__ out, int M, int nfft, int Ns,
-                              int R, const cplx<T>* __restrict__ W, int dir, const Grp& G) {
+                              unsigned magic, int R, const cplx<T>* __restrict__ W, int dir, const Grp& G) {
   const int MR = M / R;
   const int tws = M / (Ns * R);
-  for (int t = G.tid; t < nfft * MR * R; t += G.n) {
-    int q = t % R;
-    int u = t / R;
-    int f = u / MR, j = u - f * MR;
+  for (int f = 0; f < nfft; ++f) {
     const cplx<T>* src = in + (size_t)f * M;
     cplx<T>* dst = out + (size_t)f * M;
-    int k = j % Ns;
-    cplx<T> acc = {0, 0};
-    for (int r = 0; r < R; ++r) {
-      cplx<T> a = src[j + r * MR];
-      // combined twiddle exp(dir*2*pi*i*(r*k/(Ns R) + r*q/R)) = W[(r*k*tws + ((r*q)%R)*MR) % M]
-      int e = (r * k * tws + ((r * q) % R) * MR) % M;
-      cplx<T> w = W[e];
-      if (dir > 0) w.y = -w.y;
-      cplx<T> p = cmul(a, w);
-      acc.x += p.x;
-      acc.y += p.y;
+    for (int t = G.tid; t < MR * R; t += G.n) {
+      const int j = t / R, q = t - j * R;
+      const int jq = div_ns(j, Ns, magic);
+      const int k = j - jq * Ns;
+      cplx<T> acc = {0, 0};
+      for (int r = 0; r < R; ++r) {
+        cplx<T> a = src[j + r * MR];
+        // combined twiddle exp(dir*2*pi*i*(r*k/(Ns R) + r*q/R)) = W[(r*k*tws + ((r*q)%R)*MR) % M]
+        int e = (r * k * tws + ((r * q) % R) * MR) % M;
+        cplx<T> w = W[e];
+        if (dir > 0) w.y = -w.y;
+        cplx<T> p = cmul(a, w);
+        acc.x += p.x;
+        acc.y += p.y;
+      }
+      dst[jq * Ns * R + k + q * Ns] = acc;
     }
-    int base = (j / Ns) * Ns * R + k;
-    dst[base + q * Ns] = acc;
   }
 }
 
@@ -197,14 +207,15 @@ __device__ cplx<T>* fft_run(cplx<T>* a, cplx<T>* b, const FftPlan& plan, int nff
                            const Grp& G) {
   int Ns = 1;
   for (int s = 0; s < plan.nstages; ++s) {
-    int R = plan.radix[s];
+    const int R = plan.radix[s];
+    const unsigned mg = plan.ns_magic[s];
     switch (R) {
-      case 2: stage_fixed<T, 2>(a, b, plan.M, nfft, Ns, W, dir, G); break;
-      case 3: stage_fixed<T, 3>(a, b, plan.M, nfft, Ns, W, dir, G); break;
-      case 4: stage_fixed<T, 4>(a, b, plan.M, nfft, Ns, W, dir, G); break;
-      case 5: stage_fixed<T, 5>(a, b, plan.M, nfft, Ns, W, dir, G); break;
-      case 8: stage_fixed<T, 8>(a, b, plan.M, nfft, Ns, W, dir, G); break;
-      default: stage_generic<T>(a, b, plan.M, nfft, Ns, R, W, dir, G); break;
+      case 2: stage_fixed<T, 2>(a, b, plan.M, nfft, Ns, mg, W, dir, G); break;
+      case 3: stage_fixed<T, 3>(a, b, plan.M, nfft, Ns, mg, W, dir, G); break;
+      case 4: stage_fixed<T, 4>(a, b, plan.M, nfft, Ns, mg, W, dir, G); break;
+      case 5: stage_fixed<T, 5>(a, b, plan.M, nfft, Ns, mg, W, dir, G); break;
+      case 8: stage_fixed<T, 8>(a, b, plan.M, nfft, Ns, mg, W, dir, G); break;
+      default: stage_generic<T>(a, b, plan.M, nfft, Ns, mg, R, W, dir, G); break;
     }
     G.sync();
     cplx<T>* t = a;
@@ -233,21 +244,21 @@ __device__ void r2r_pre(int type, const T* stage, int n, int nl, cplx<T>* buf, c
   if (fam == 2) {
     const int M = n / 2;
     const bool rev = type == DST4;
-    for (int t = G.tid; t < nl * M; t += G.n) {
-      int l = t / M, m = t - l * M;
-      const T* x = stage + (size_t)l * n;
-      int i0 = 2 * m, i1 = n - 1 - 2 * m;
-      T a = rev ? x[n - 1 - i0] : x[i0];
-      T b = rev ? x[n - 1 - i1] : x[i1];
-      cplx<T> w = tb.pre[m];
-      buf[(size_t)l * M + m] = {a * w.x - b * w.y, b * w.x + a * w.y};
-    }
+    for (int l = 0; l < nl; ++l)
+      for (int m = G.tid; m < M; m += G.n) {
+        const T* x = stage + (size_t)l * n;
+        int i0 = 2 * m, i1 = n - 1 - 2 * m;
+        T a = rev ? x[n - 1 - i0] : x[i0];
+        T b = rev ? x[n - 1 - i1] : x[i1];
+        cplx<T> w = tb.pre[m];
+        buf[(size_t)l * M + m] = {a * w.x - b * w.y, b * w.x + a * w.y};
+      }
   } else if (fam == 0) {
     // Makhoul: v[m] = x[2m] (m < ceil(n/2)), v[n-1-m'] = x[2m'+1]
     const int npair = (nl + 1) / 2;
     const bool alt = type == DST2;  // DST-II: x'[m] = (-1)^m x[m]
-    for (int t = G.tid; t < npair * n; t += G.n) {
-      int pidx = t / n, m = t - pidx * n;
+    for (int pidx = 0; pidx < npair; ++pidx)
+    for (int m = G.tid; m < n; m += G.n) {
       int src = m < (n + 1) / 2 ? 2 * m : 2 * (n - 1 - m) + 1;
       T sgn = (alt && (src & 1)) ? (T)-1 : (T)1;
       int la = 2 * pidx, lb = 2 * pidx + 1;
@@ -259,8 +270,8 @@ __device__ void r2r_pre(int type, const T* stage, int n, int nl, cplx<T>* buf, c
     // V[k] = e^{i pi k/(2n)} (X_k - i X_{n-k}), X_n = 0; two lines as V_A + i V_B
     const int npair = (nl + 1) / 2;
     const bool rev = type == DST3;  // DST-III: X'[k] = X[n-1-k]
-    for (int t = G.tid; t < npair * n; t += G.n) {
-      int pidx = t / n, k = t - pidx * n;
+    for (int pidx = 0; pidx < npair; ++pidx)
+    for (int k = G.tid; k < n; k += G.n) {
       int la = 2 * pidx, lb = 2 * pidx + 1;
       int ik = rev ? n - 1 - k : k;
       int ir = rev ? k - 1 : n - k;  // index of X_{n-k} in the stored line (valid when k > 0)
@@ -301,8 +312,8 @@ __device__ void r2r_post(int type, const cplx<T>* buf, int n, int nl, T* stage, 
   if (fam == 2) {
     const int M = n / 2;
     const bool alt = type == DST4;  // y[k] *= (-1)^k
-    for (int t = G.tid; t < nl * M; t += G.n) {
-      int l = t / M, k = t - l * M;
+    for (int l = 0; l < nl; ++l)
+    for (int k = G.tid; k < M; k += G.n) {
       cplx<T> z = cmul(buf[(size_t)l * M + k], tb.post[k]);
       T* y = stage + (size_t)l * n;
       int k0 = 2 * k, k1 = n - 1 - 2 * k;
@@ -317,8 +328,8 @@ __device__ void r2r_post(int type, const cplx<T>* buf, int n, int nl, T* stage, 
   } else if (fam == 0) {
     const int npair = (nl + 1) / 2;
     const bool rev = type == DST2;  // DST-II: y[k] = Y'[n-1-k]
-    for (int t = G.tid; t < npair * n; t += G.n) {
-      int pidx = t / n, k = t - pidx * n;
+    for (int pidx = 0; pidx < npair; ++pidx)
+    for (int k = G.tid; k < n; k += G.n) {
       cplx<T> Zk = buf[(size_t)pidx * n + k];
       cplx<T> Zc = buf[(size_t)pidx * n + (k == 0 ? 0 : n - k)];
       Zc.y = -Zc.y;
@@ -335,8 +346,8 @@ __device__ void r2r_post(int type, const cplx<T>* buf, int n, int nl, T* stage, 
   } else if (fam == 1) {
     const int npair = (nl + 1) / 2;
     const bool alt = type == DST3;  // DST-III: y[m] *= (-1)^m
-    for (int t = G.tid; t < npair * n; t += G.n) {
-      int pidx = t / n, o = t - pidx * n;
+    for (int pidx = 0; pidx < npair; ++pidx)
+    for (int o = G.tid; o < n; o += G.n) {
       int src = (o & 1) ? n - 1 - (o - 1) / 2 : o / 2;
       cplx<T> z = buf[(size_t)pidx * n + src];
       T sgn = (alt && (o & 1)) ? (T)-1 : (T)1;

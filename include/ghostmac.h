@@ -219,6 +219,13 @@ int gm_divergence_stats_noalloc(const double* u, const double* v, const uint8_t*
 
 /* Number of CUDA kernels this library has launched in this process. */
 int64_t gm_kernel_launches(void);
+/* Event times (ms) of the last step run by gm_step when the environment variable
+ * GHOSTMAC_PHASE_TIMING=1 was set.  out[0..5]: the phases momentum right-hand side, Helmholtz
+ * solves, projection 1, defect, projection 2, pressure output / forces / gates.  out[6..13]:
+ * the kernels of the first sweep of projection 1 (row pass, column solve, band row pass,
+ * Schur GEMV, band row pass, band solve, final row pass, residual).  The events are recorded
+ * inside the step graphs, so they time graph-replayed steps. */
+int gm_phase_timing(const gm_handle* h, double out[14]);
 /* CUDA-event timing of every launch on the stream it runs on, summed per kernel class:
  * 1 row transforms, 2 column solves, 3 momentum right-hand side, 4 operator residual,
  * 5 Schur GEMV, 6 projection pieces, 7 defect and pressure output, 8 ghost rows,
