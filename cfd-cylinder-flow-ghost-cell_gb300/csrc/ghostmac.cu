@@ -106,11 +106,54 @@ FftPlan make_plan(int M) {
   p.nstages = s;
   if (M > 65536) throw CudaError("FFT length above 65536");
   long long Ns = 1;
+  int off = 0;
+  bool generic = false;
   for (int k = 0; k < s; ++k) {
     p.ns_magic[k] = Ns == 1 ? 0u : (unsigned)(((1ull << 32) + (unsigned long long)Ns - 1) / (unsigned long long)Ns);
-    Ns *= p.radix[k];
+    const int R = p.radix[k];
+    if (R == 2 || R == 3 || R == 4 || R == 5 || R == 8) {
+      p.tw_off[k] = off;
+      off += (int)Ns * (R - 1);
+    } else {
+      generic = true;
+    }
+    Ns *= R;
   }
+  for (int k = 0; k < s; ++k) {
+    const int R = p.radix[k];
+    if (!(R == 2 || R == 3 || R == 4 || R == 5 || R == 8)) p.tw_off[k] = off;  // the full table follows
+  }
+  p.tw_len = off + (generic ? M : 0);
   return p;
+}
+
+// The plan's twiddle table (see FftPlan), interleaved (re, im), forward sign exp(-2 pi i t / M).
+std::vector<double> plan_twiddles(const FftPlan& p) {
+  std::vector<double> t(2 * (size_t)p.tw_len);
+  const long double PI = 3.14159265358979323846264338327950288L;
+  auto put = [&](int at, long long e) {
+    const long double a = -2.0L * PI * (long double)(e % p.M) / (long double)p.M;
+    t[2 * (size_t)at] = (double)std::cos(a);
+    t[2 * (size_t)at + 1] = (double)std::sin(a);
+  };
+  long long Ns = 1;
+  bool generic = false;
+  for (int s = 0; s < p.nstages; ++s) {
+    const int R = p.radix[s];
+    if (R == 2 || R == 3 || R == 4 || R == 5 || R == 8) {
+      const long long tws = p.M / (Ns * R);
+      for (long long k = 0; k < Ns; ++k)
+        for (int r = 1; r < R; ++r) put(p.tw_off[s] + (int)(k * (R - 1) + r - 1), r * k * tws);
+    } else {
+      generic = true;
+    }
+    Ns *= R;
+  }
+  if (generic) {
+    int base = p.tw_len - p.M;
+    for (int e = 0; e < p.M; ++e) put(base + e, e);
+  }
+  return t;
 }
 
 std::vector<double> cexp_table(int count, double scale_num, double scale_den, double offset, int sign) {
@@ -174,6 +217,10 @@ struct gm_handle {
   DBuf<double> phalf, phalf_next, pout, prhs, pphi, pres, pfirst, pw2, pinc, ptmp, spectral;
   DBuf<float> pres32, fres32;  // FP32-mode residuals (inputs of the FP32 inverse)
   DBuf<float> U32, P32;        // FP32-mode copies of the state for the momentum stencils
+  // flexible GMRES (pressure_solver = iterative): Krylov basis V (m+1 vectors), preconditioned
+  // directions Z (m), the refinement correction and reduction scratch
+  static constexpr int GMRES_M = 50;
+  DBuf<double> gV, gZ, gdx, gpart, gdots, gcoef;
   ResidualCoef rcoef[3];       // regular-row coefficients: pressure, Helmholtz u, Helmholtz v
   DBuf<float> spectral32, ffirst32, pfirst32;
   DBuf<StepCtl> ctl;
@@ -367,7 +414,8 @@ void autotune_shapes(gm_handle* h, RectDev& rd, int kind, bool fp32) {
   const RectView& v = rd.view;
   cudaStream_t st = h->st;
   const size_t per = std::max(xpass_smem_per_group(tt.tx_fwd, v.cols, fp32), xpass_smem_per_group(tt.tx_inv, v.cols, fp32));
-  const size_t tabs = std::max(xpass_smem_tables(tt.tx_fwd, v.cols, fp32), xpass_smem_tables(tt.tx_inv, v.cols, fp32));
+  const size_t tabs = std::max(xpass_smem_tables(tt.tx_fwd, v.cols, tt.plan_x.tw_len, fp32),
+                               xpass_smem_tables(tt.tx_inv, v.cols, tt.plan_x.tw_len, fp32));
   double* field = kind == 0 ? h->ptmp.p : h->ftmp.p;
   float* field32 = kind == 0 ? h->pfirst32.p : h->ffirst32.p;
   const Gate open{nullptr, 0, 0};
@@ -461,7 +509,7 @@ void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
   int Mx = r2r_fft_length(tx_f, cols);
   tt.plan_x = make_plan(Mx);
   cudaStream_t st = h->st;
-  rd.Wx.upload(cexp_table(Mx, 2.0, Mx, 0.0, -1), st);
+  rd.Wx.upload(plan_twiddles(tt.plan_x), st);
   // type IV: pre exp(-i pi (4m+1)/(4n)), post exp(-i pi k/n); Makhoul: (cos, sin)(pi k/(2n))
   if (r2r_family(tx_f) == 2) {
     rd.prex.upload(cexp_table(cols / 2, 4.0, 4.0 * cols, 1.0, -1), st);
@@ -497,7 +545,7 @@ void build_rect_tables(gm_handle* h, RectDev& rd, int kind, double dt) {
     // FP32 tables and launch shapes (same plans, half the shared memory per line)
     TransformTables& t32 = rd.tt32;
     t32 = tt;
-    rd.Wx32.upload(to_f32(cexp_table(Mx, 2.0, Mx, 0.0, -1)), st);
+    rd.Wx32.upload(to_f32(plan_twiddles(tt.plan_x)), st);
     if (r2r_family(tx_f) == 2) {
       rd.prex32.upload(to_f32(cexp_table(cols / 2, 4.0, 4.0 * cols, 1.0, -1)), st);
       rd.postx32.upload(to_f32(cexp_table(cols / 2, 1.0, cols, 0.0, -1)), st);
@@ -909,10 +957,160 @@ void schur_solve_graph(gm_handle* h, int lane, RectDev& rd, int kind, double hc,
   if (f32 && kind == 0) launch_pressure_bound(h->cd, h->rcoef[0], b, x, sc, h->nchk, g0, st);
 }
 
+// Flexible GMRES(50) for A x = b on the pressure grid, right-preconditioned by the separable
+// rectangle inverse (no boundary term) -- solver/pressure_schur.py:20-41 with
+// gmres(rtol=atol=1e-12, restart=50, maxiter=100): at most 100 restart cycles, convergence
+// on the residual 2-norm <= max(rtol ||b||, atol).  Classical Gram-Schmidt with one
+// re-orthogonalisation; the Hessenberg least-squares update (Givens rotations) runs on the
+// host, one small read-back per iteration.  Returns 0 when converged, else the iteration count.
+int fgmres(gm_handle* h, const double* b, double* x, int& iterations) {
+  const int m = gm_handle::GMRES_M;
+  const int64_t n = h->Pn;
+  cudaStream_t st = h->st;
+  if (!h->gV.p) {
+    h->gV.alloc((size_t)(m + 1) * n);
+    h->gZ.alloc((size_t)m * n);
+    h->gdx.alloc(n);
+    h->gpart.alloc((size_t)multidot_blocks(n) * 64);
+    h->gdots.alloc(64);
+    h->gcoef.alloc(64);
+  }
+  RectDev& rd = h->rp;
+  const Gate open{nullptr, 0, 0};
+  double* V = h->gV.p;
+  double* Z = h->gZ.p;
+  auto vec = [&](double* base, int i) { return base + (int64_t)i * n; };
+  auto dots = [&](const double* Vb, int nv, const double* w, double* out_host) {
+    launch_multidot(Vb, n, nv, w, n, h->gpart.p, h->gdots.p, st);
+    CK(cudaMemcpyAsync(out_host, h->gdots.p, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  };
+  auto precondition = [&](const double* v, double* z) {
+    if (h->precision == 1)
+      plain_inverse<float, double, double>(rd.tt32, rd.view, v, true, h->spectral32.p, z, rd.view.cls, nullptr, open,
+                                           st);
+    else
+      plain_inverse<double, double, double>(rd.tt, rd.view, v, true, h->spectral.p, z, rd.view.cls, nullptr, open, st);
+  };
+  double bn2 = 0;
+  dots(b, 1, b, &bn2);
+  const double tol = std::max(1e-12 * std::sqrt(bn2), 1e-12);
+  CK(cudaMemsetAsync(x, 0, n * sizeof(double), st));
+  iterations = 0;
+  bool converged = false, x_zero = true;
+  std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), hc(m + 1), hc2(m + 1), y(m);
+  for (int cycle = 0; cycle < 100 && !converged; ++cycle) {
+    // V0 = b - A x
+    CK(cudaMemcpyAsync(vec(V, 0), b, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if (!x_zero) {
+      launch_apply_pressure(h->cd, h->rcoef[0], x, vec(V, 1), open, st);
+      const double one = 1.0;
+      CK(cudaMemcpyAsync(h->gcoef.p, &one, sizeof one, cudaMemcpyHostToDevice, st));
+      launch_multiaxpy(vec(V, 1), n, 1, h->gcoef.p, -1.0, 1.0, vec(V, 0), n, st);
+    }
+    double beta2 = 0;
+    dots(vec(V, 0), 1, vec(V, 0), &beta2);
+    const double beta = std::sqrt(beta2);
+    if (!(beta > tol)) { converged = std::isfinite(beta); break; }
+    launch_multiaxpy(nullptr, n, 0, h->gcoef.p, 0.0, 1.0 / beta, vec(V, 0), n, st);
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int jend = -1;
+    for (int j = 0; j < m; ++j) {
+      precondition(vec(V, j), vec(Z, j));
+      double* w = vec(V, j + 1);
+      launch_apply_pressure(h->cd, h->rcoef[0], vec(Z, j), w, open, st);
+      // two classical Gram-Schmidt passes against V_0..V_j
+      dots(V, j + 1, w, hc.data());
+      launch_multiaxpy(V, n, j + 1, h->gdots.p, -1.0, 1.0, w, n, st);
+      dots(V, j + 1, w, hc2.data());
+      launch_multiaxpy(V, n, j + 1, h->gdots.p, -1.0, 1.0, w, n, st);
+      for (int i = 0; i <= j; ++i) hc[i] += hc2[i];
+      double wn2 = 0;
+      dots(w, 1, w, &wn2);
+      hc[j + 1] = std::sqrt(wn2);
+      if (hc[j + 1] > 0) launch_multiaxpy(nullptr, n, 0, h->gcoef.p, 0.0, 1.0 / hc[j + 1], w, n, st);
+      // Givens rotations on the new Hessenberg column
+      for (int i = 0; i < j; ++i) {
+        const double a = cs[i] * hc[i] + sn[i] * hc[i + 1];
+        hc[i + 1] = -sn[i] * hc[i] + cs[i] * hc[i + 1];
+        hc[i] = a;
+      }
+      const double den = std::hypot(hc[j], hc[j + 1]);
+      cs[j] = den > 0 ? hc[j] / den : 1.0;
+      sn[j] = den > 0 ? hc[j + 1] / den : 0.0;
+      hc[j] = den;
+      hc[j + 1] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hc[i];
+      ++iterations;
+      jend = j;
+      if (!std::isfinite(g[j + 1])) break;
+      if (std::abs(g[j + 1]) <= tol) { converged = true; break; }
+    }
+    if (jend < 0) break;
+    // y = R^{-1} g, x += Z y
+    for (int i = jend; i >= 0; --i) {
+      double acc = g[i];
+      for (int k = i + 1; k <= jend; ++k) acc -= H[(size_t)i * m + k] * y[k];
+      y[i] = acc / H[(size_t)i * m + i];
+    }
+    CK(cudaMemcpyAsync(h->gcoef.p, y.data(), (jend + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
+    launch_multiaxpy(Z, n, jend + 1, h->gcoef.p, 1.0, 1.0, x, n, st);
+    CK(cudaStreamSynchronize(st));
+    x_zero = false;
+  }
+  return converged ? 0 : std::max(1, iterations);
+}
+
+// monitored_pressure_solver, iterative branch (solver/pressure_schur.py:16-72): GMRES, the
+// true residual, up to two GMRES refinements of the residual to max(1e-10, 64 eps max(1,|b|));
+// the gate (k_gate_pressure) then sees the final check, its roundoff bound and the status.
+void gmres_monitored(gm_handle* h, const double* b, double* x, double* res, int slot) {
+  cudaStream_t st = h->st;
+  SolveCtl* sc = &h->ctl.p->solve[slot];
+  const Gate g0 = gate_of(h);
+  int its = 0, total = 0;
+  int status = fgmres(h, b, x, its);
+  total += its;
+  launch_residual(h->cd, h->rcoef[0], 0, b, x, res, false, sc, 0, true, g0, st);
+  auto read = [&](SolveCtl& hs) {
+    CK(cudaMemcpyAsync(&hs, sc, sizeof hs, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  };
+  SolveCtl hs;
+  read(hs);
+  const double target = std::max(1e-10, 64 * 2.220446049250313e-16 * std::max(1.0, bits2d(hs.bmax)));
+  int k = 0;
+  for (int r = 0; r < 2; ++r) {
+    if (status || bits2d(hs.rmax[k]) <= target) break;
+    status = fgmres(h, res, h->gdx.p, its);
+    total += its;
+    const double one = 1.0;
+    CK(cudaMemcpyAsync(h->gcoef.p, &one, sizeof one, cudaMemcpyHostToDevice, st));
+    launch_multiaxpy(h->gdx.p, h->Pn, 1, h->gcoef.p, 1.0, 1.0, x, h->Pn, st);
+    ++k;
+    launch_residual(h->cd, h->rcoef[0], 0, b, x, res, false, sc, k, false, g0, st);
+    read(hs);
+  }
+  const int ints[2] = {k + 1, total};
+  CK(cudaMemcpyAsync(&sc->gk1, ints, sizeof ints, cudaMemcpyHostToDevice, st));
+  if (status) {
+    const unsigned long long bad = 1;
+    CK(cudaMemcpyAsync(&sc->xbad, &bad, sizeof bad, cudaMemcpyHostToDevice, st));
+  }
+  CK(cudaStreamSynchronize(st));
+}
+
 // One solve A x = b with the FFT + boundary Schur inverse and refinement sweeps to the
 // reference's residual target (solver/pressure_schur.py:16-72, direct branch).
 void schur_solve(gm_handle* h, int lane, RectDev& rd, int kind, double hc, const double* b, double* x, double* res,
                  double* first, double* w2, int slot) {
+  if (kind == 0 && h->g.pressure_solver == 1) {
+    gmres_monitored(h, b, x, res, slot);
+    return;
+  }
   if (h->capturing) {
     schur_solve_graph(h, lane, rd, kind, hc, b, x, res, first, w2, slot);
     return;
@@ -1156,11 +1354,14 @@ void fill_diag(gm_handle* h, const StepCtl& c, double t, double dt, bool first, 
   d->coupled_momentum_residual_linf = bits2d(c.coupled_max);
   int count = 0, refine = 0;
   double plinf = 0, prel = 0;
+  int its = 0;
   for (int s = first ? 2 : 3; s < 5; ++s) {
     const SolveCtl& sc = c.solve[s];
     double b = bits2d(sc.bmax), tg = std::max(1e-10, 32 * 2.220446049250313e-16 * std::max(1.0, b));
     int k = 0;
     while (k + 1 < h->nchk && bits2d(sc.rmax[k]) > tg) ++k;
+    if (sc.gk1) k = sc.gk1 - 1;
+    its += sc.gits;
     ++count;
     refine += k;
     plinf = std::max(plinf, bits2d(sc.rmax[k]));
@@ -1169,7 +1370,7 @@ void fill_diag(gm_handle* h, const StepCtl& c, double t, double dt, bool first, 
   }
   d->pressure_solve_count = count;
   d->pressure_refinement_iterations = refine;
-  d->pressure_iterations = 0;
+  d->pressure_iterations = its;
   d->pressure_residual_linf = plinf;
   d->pressure_residual_relative_l2 = prel;
   d->status = c.err;
@@ -1244,7 +1445,6 @@ int gm_create(const gm_config* cfg, gm_handle** out) {
   if (cfg->precision != 0 && cfg->precision != 1) { g_create_error = "precision must be 0 (FP64) or 1 (FP32 with FP64 refinement)"; return GM_EVALUE; }
   h->precision = cfg->precision;
   h->nchk = cfg->precision == 1 ? MAXCHK : 3;
-  if (cfg->pressure_solver == 1) { g_create_error = "iterative pressure solver not built in this library"; return GM_ENOTIMPL; }
   if (cfg->nx % 2 != 0) { g_create_error = "odd nx is not supported by the type-IV transform"; return GM_ENOTIMPL; }
   int ec = 0;
   if (!gm::build_geometry(g, ec)) { g_create_error = g.error; return ec ? ec : GM_EVALUE; }
@@ -1336,6 +1536,7 @@ int gm_create(const gm_config* cfg, gm_handle** out) {
     CK(cudaEventCreateWithFlags(&H->ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&H->ev_join, cudaEventDisableTiming));
     if (const char* e = std::getenv("GHOSTMAC_NO_GRAPHS")) H->use_graphs = !(e[0] == '1');
+    if (g.pressure_solver == 1) H->use_graphs = false;  // GMRES decides its iterations on the host
 
     H->state_max.alloc(2);
     H->state_max.zero(st);
@@ -1744,6 +1945,7 @@ static void solve_info_from(gm_handle* h, int slot, gm_solve_info* info) {
   double b = bits2d(sc.bmax), tg = std::max(1e-10, 32 * 2.220446049250313e-16 * std::max(1.0, b));
   int k = 0;
   while (k + 1 < h->nchk && bits2d(sc.rmax[k]) > tg) ++k;
+  if (sc.gk1) k = sc.gk1 - 1;
   double bound = bits2d(sc.bound[k]);
   double t64 = std::max(1e-10, 64 * 2.220446049250313e-16 * std::max(1.0, b));
   info->residual_linf = bits2d(sc.rmax[k]);
@@ -1751,9 +1953,9 @@ static void solve_info_from(gm_handle* h, int slot, gm_solve_info* info) {
   info->roundoff_bound_linf = bound;
   info->residual_target_linf = std::max(t64, bound);
   info->backward_error_linf = 0;
-  info->iterations = 0;
+  info->iterations = sc.gits;
   info->refinement_iterations = k;
-  info->status = 0;
+  info->status = sc.xbad && sc.gk1 ? 1 : 0;
   info->rank = (int32_t)h->rp.rank;
 }
 
@@ -2001,6 +2203,7 @@ int gm_batch_create(gm_handle* const* cases, int32_t n_cases, gm_batch** out) {
   auto b = std::make_unique<gm_batch>();
   for (int i = 0; i < n_cases; ++i) {
     if (!cases[i] || cases[i]->host_only) { g_create_error = "batch cases must be device handles"; return GM_EVALUE; }
+    if (cases[i]->g.pressure_solver != 0) { g_create_error = "batch cases must use the direct pressure solver"; return GM_EVALUE; }
     for (int j = 0; j < i; ++j)
       if (cases[j] == cases[i]) { g_create_error = "a case appears twice in the batch"; return GM_EVALUE; }
     b->cases.push_back(cases[i]);

@@ -150,23 +150,23 @@ __host__ __device__ inline size_t xpass_group_smem(int type, int n) {
   size_t stage = ((size_t)lpw * n * sizeof(T) + 15) / 16 * 16;
   return stage + 2 * (size_t)r2r_buffer_elems(type, n, lpw) * sizeof(cplx<T>);
 }
-// lengths (complex entries) of the FFT twiddles, the pre- and the post-twiddles of a transform
-__host__ __device__ inline int xpass_tw_len(int type, int n, int which) {
+// lengths (complex entries) of the plan's twiddles, the pre- and the post-twiddles of a transform
+__host__ __device__ inline int xpass_tw_len(int type, int n, int which, int plan_tw) {
   const int fam = r2r_family(type);
-  if (which == 0) return r2r_fft_length(type, n);
+  if (which == 0) return plan_tw;
   if (which == 1) return fam == 2 ? n / 2 : 1;
   return fam == 2 ? n / 2 : (fam == 3 ? 1 : n);
 }
 template <typename T>
-__host__ __device__ inline size_t xpass_tw_bytes(int type, int n) {
-  return ((size_t)(xpass_tw_len(type, n, 0) + xpass_tw_len(type, n, 1) + xpass_tw_len(type, n, 2)) * sizeof(cplx<T>) +
-          15) / 16 * 16;
+__host__ __device__ inline size_t xpass_tw_bytes(int type, int n, int plan_tw) {
+  return ((size_t)(xpass_tw_len(type, n, 0, plan_tw) + xpass_tw_len(type, n, 1, plan_tw) +
+                   xpass_tw_len(type, n, 2, plan_tw)) * sizeof(cplx<T>) + 15) / 16 * 16;
 }
 size_t xpass_smem_per_group(int type, int n, bool fp32) {
   return fp32 ? xpass_group_smem<float>(type, n) : xpass_group_smem<double>(type, n);
 }
-size_t xpass_smem_tables(int type, int n, bool fp32) {
-  return fp32 ? xpass_tw_bytes<float>(type, n) : xpass_tw_bytes<double>(type, n);
+size_t xpass_smem_tables(int type, int n, int plan_tw, bool fp32) {
+  return fp32 ? xpass_tw_bytes<float>(type, n, plan_tw) : xpass_tw_bytes<double>(type, n, plan_tw);
 }
 
 static constexpr int XB = 4;  // loads batched per thread in the row passes
@@ -179,7 +179,8 @@ __global__ void k_xpass(int n, int r0, int nr, int type, FftPlan plan, R2RTables
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // the twiddle tables go to shared memory first (read by every stage of every group: a
   // global load per stage would put an L2 round trip on each stage's critical path)
-  const int ntw[3] = {xpass_tw_len(type, n, 0), xpass_tw_len(type, n, 1), xpass_tw_len(type, n, 2)};
+  const int ntw[3] = {xpass_tw_len(type, n, 0, plan.tw_len), xpass_tw_len(type, n, 1, plan.tw_len),
+                      xpass_tw_len(type, n, 2, plan.tw_len)};
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   for (int q = threadIdx.x; q < ntw[0] + ntw[1] + ntw[2]; q += blockDim.x)
     tw[q] = q < ntw[0] ? tb.W[q] : (q < ntw[0] + ntw[1] ? tb.pre[q - ntw[0]] : tb.post[q - ntw[0] - ntw[1]]);
@@ -190,7 +191,7 @@ __global__ void k_xpass(int n, int r0, int nr, int type, FftPlan plan, R2RTables
   const int l0 = (blockIdx.x * gpb + grp) * lpw;
   if (grp >= gpb || l0 >= nr) return;  // whole groups leave; every group has its own barrier
   const int nl = min(lpw, nr - l0);
-  unsigned char* mine = smem_raw + xpass_tw_bytes<T>(type, n) + (size_t)grp * xpass_group_smem<T>(type, n);
+  unsigned char* mine = smem_raw + xpass_tw_bytes<T>(type, n, plan.tw_len) + (size_t)grp * xpass_group_smem<T>(type, n);
   T* stage = reinterpret_cast<T*>(mine);
   const size_t stage_bytes = ((size_t)lpw * n * sizeof(T) + 15) / 16 * 16;
   cplx<T>* a = reinterpret_cast<cplx<T>*>(mine + stage_bytes);
@@ -1033,6 +1034,112 @@ void launch_pressure_bound(const CaseDev& c, const ResidualCoef& rc, const doubl
   kt_mark(4, st);
   k_pressure_bound<<<reduce_blocks(c.psize), TPB, 0, st>>>(c, rc, b, x, sc, nchk, gate);
   kt_mark(4, st);
+}
+
+// ---------------------------------------------------------------------------
+// flexible GMRES on the pressure grid (solver/pressure_schur.py:20-57, iterative branch):
+// operator apply, block-deterministic multi-dot products and multi-axpy updates
+// ---------------------------------------------------------------------------
+// w = A z on the pressure grid (zero at inactive cells)
+__global__ void k_apply_pressure(CaseDev c, ResidualCoef rc, const double* __restrict__ z, double* __restrict__ w,
+                                 Gate gate) {
+  if (!gate_open(gate)) return;
+  const int nx = c.nx, ny = c.ny;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < c.psize; t += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t k = c.cls_p[t];
+    if (!(k & CLS_ACTIVE)) {
+      w[t] = 0.0;
+      continue;
+    }
+    double ax;
+    const int row = (k & CLS_IRREG) ? c.irr_index[0][t] : -1;
+    if (row >= 0) {
+      const int64_t* cp = c.irr_ptr[0];
+      ax = 0.0;
+      for (int64_t e = cp[row]; e < cp[row + 1]; ++e) ax += c.irr_val[0][e] * z[c.irr_col[0][e]];
+    } else {
+      const int j = (int)((unsigned)t / (unsigned)nx), i = (int)((unsigned)t - (unsigned)j * nx);
+      const double xw = i > 0 ? z[t - 1] : 0.0, xe = i < nx - 1 ? z[t + 1] : 0.0;
+      const double xs = j > 0 ? z[t - nx] : 0.0, xn = j < ny - 1 ? z[t + nx] : 0.0;
+      const int ic = i == 0 ? 0 : (i == nx - 1 ? 2 : 1), jc = (j == 0 || j == ny - 1) ? 0 : 1;
+      ax = coef_cc(rc, ic, jc) * z[t] + coef_cw(rc, ic) * xw + rc.ce * xe + rc.cy * (xs + xn);
+    }
+    w[t] = ax;
+  }
+}
+void launch_apply_pressure(const CaseDev& c, const ResidualCoef& rc, const double* z, double* w, const Gate& gate,
+                           cudaStream_t st) {
+  note_launch();
+  kt_mark(4, st);
+  k_apply_pressure<<<reduce_blocks(c.psize), TPB, 0, st>>>(c, rc, z, w, gate);
+  kt_mark(4, st, (double)c.psize * 17);
+}
+
+// Partial sums part[b * nv + i] = sum over block b's points of V_i[t] * w[t], i < nv (V_i at
+// V + i * ld); the final pass sums the blocks in a fixed order (run-to-run identical).
+static constexpr int GM_DOT_MAX = 64;
+__global__ void k_multidot_part(const double* __restrict__ V, int64_t ld, int nv, const double* __restrict__ w,
+                                int64_t n, double* __restrict__ part) {
+  __shared__ double red[GM_DOT_MAX][TPB / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i0 = 0; i0 < nv; i0 += 8) {
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+      const double wt = w[t];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (i0 + u < nv) acc[u] += V[(int64_t)(i0 + u) * ld + t] * wt;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const double sum = warp_sum(acc[u]);
+      if (lane == 0 && i0 + u < nv) red[i0 + u][warp] = sum;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    double sum = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum += red[i][q];
+    part[(int64_t)blockIdx.x * nv + i] = sum;
+  }
+}
+__global__ void k_multidot_final(const double* __restrict__ part, int nblocks, int nv, double* __restrict__ out) {
+  const int i = blockIdx.x;
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += 32) acc += part[(int64_t)b * nv + i];
+  acc = warp_sum(acc);
+  if (threadIdx.x == 0) out[i] = acc;
+}
+void launch_multidot(const double* V, int64_t ld, int nv, const double* w, int64_t n, double* part, double* out,
+                     cudaStream_t st) {
+  const unsigned nb = reduce_blocks(n);
+  note_launch();
+  kt_mark(6, st);
+  k_multidot_part<<<nb, TPB, 0, st>>>(V, ld, nv, w, n, part);
+  kt_mark(6, st, (double)n * 8 * (nv + 1));
+  note_launch();
+  k_multidot_final<<<nv, 32, 0, st>>>(part, (int)nb, nv, out);
+}
+unsigned multidot_blocks(int64_t n) { return reduce_blocks(n); }
+
+// y[t] = alpha * y[t] + sign * sum_i coef[i] V_i[t]   (coef on the device)
+__global__ void k_multiaxpy(const double* __restrict__ V, int64_t ld, int nv, const double* __restrict__ coef,
+                            double sign, double alpha, double* __restrict__ y, int64_t n) {
+  __shared__ double cf[GM_DOT_MAX + 1];
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) cf[i] = coef[i];
+  __syncthreads();
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int i = 0; i < nv; ++i) acc += cf[i] * V[(int64_t)i * ld + t];
+    y[t] = alpha * y[t] + sign * acc;
+  }
+}
+void launch_multiaxpy(const double* V, int64_t ld, int nv, const double* coef, double sign, double alpha, double* y,
+                      int64_t n, cudaStream_t st) {
+  note_launch();
+  kt_mark(6, st);
+  k_multiaxpy<<<reduce_blocks(n), TPB, 0, st>>>(V, ld, nv, coef, sign, alpha, y, n);
+  kt_mark(6, st, (double)n * 8 * (nv + 2));
 }
 
 // ---------------------------------------------------------------------------

@@ -31,8 +31,10 @@ struct SolveCtl {
   unsigned long long bound[MAXCHK];   // roundoff bound max_i w_i (|A||x| + |b|)_i
   double rsq[MAXCHK];                 // sum (b - A x)^2
   double bsq;                         // sum b^2
-  unsigned long long xbad;            // non-finite solution flag
+  unsigned long long xbad;            // non-finite solution (or unconverged GMRES) flag
   int k;                              // current check index (graph-driven refinement loop)
+  int gk1;                            // GMRES path: final check index + 1 (0: direct path)
+  int gits;                           // GMRES path: Krylov iterations of the solve
   int pad_;
 };
 
@@ -77,6 +79,7 @@ __device__ __forceinline__ bool sweep_needed(const SolveCtl* s, int k) {
 }
 // index of the last residual check that ran, out of nchk launched checks
 __device__ __forceinline__ int last_check(const SolveCtl* s, int nchk) {
+  if (s->gk1) return s->gk1 - 1;
   double tg = inner_target(s);
   int k = 0;
   while (k + 1 < nchk && bits2d(s->rmax[k]) > tg) ++k;
@@ -204,7 +207,7 @@ void ktimer_collect();
 bool ktimer_active();
 void ktimer_read(int cls, double* total_ms, long long* count, double* bytes);
 size_t xpass_smem_per_group(int type, int n, bool fp32);
-size_t xpass_smem_tables(int type, int n, bool fp32);  // twiddle tables staged once per block
+size_t xpass_smem_tables(int type, int n, int plan_tw, bool fp32);  // twiddle tables staged once per block
 size_t ysolve_smem(int rows, int lpb, bool fp32);
 // Row transforms of rows r0..r0+nr-1: forward (tx_fwd) or inverse (tx_inv).  Element (r, e)
 // is read at in[ibase + r*ipitch + e] (zero where icls marks the point inactive), minus the
@@ -243,6 +246,15 @@ void launch_residual(const CaseDev& c, const ResidualCoef& rc, int kind, const d
                      bool res_f32, SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st);
 void launch_pressure_bound(const CaseDev& c, const ResidualCoef& rc, const double* b, const double* x, SolveCtl* sc,
                            int nchk, const Gate& gate, cudaStream_t st);
+// GMRES pieces on pressure-grid vectors: w = A z; out[i] = V_i . w (i < nv <= 64, V_i at V + i ld,
+// part: multidot_blocks(n) * nv scratch); y = alpha y + sign sum_i coef[i] V_i
+void launch_apply_pressure(const CaseDev& c, const ResidualCoef& rc, const double* z, double* w, const Gate& gate,
+                           cudaStream_t st);
+void launch_multidot(const double* V, int64_t ld, int nv, const double* w, int64_t n, double* part, double* out,
+                     cudaStream_t st);
+unsigned multidot_blocks(int64_t n);
+void launch_multiaxpy(const double* V, int64_t ld, int nv, const double* coef, double sign, double alpha, double* y,
+                      int64_t n, cudaStream_t st);
 
 // momentum right-hand side; mode 0 steady AB2, 1 start-up part A, 2 start-up part B
 struct MomentumArgs {

@@ -62,7 +62,12 @@ struct FftPlan {
   int nstages;
   int radix[20];
   unsigned ns_magic[20];  // ceil(2^32 / Ns) of stage s (Ns = product of the earlier radices; 0 when Ns = 1)
+  int tw_off[20];         // offset of stage s's twiddles in the plan's twiddle table
+  int tw_len;             // length (complex entries) of the plan's twiddle table
 };
+// The plan's twiddle table: for a radix-R stage (R in 2, 3, 4, 5, 8) the Ns x (R-1) entries
+// W_M^(r k M/(Ns R)), k < Ns, r = 1..R-1, stored k-major so that one butterfly reads R-1
+// consecutive entries; for any other radix the full table W_M^t, t < M.
 
 // One radix-R butterfly on v[0..R) in place; dir = -1 forward, +1 inverse.
 template <typename T, int R>
@@ -139,31 +144,29 @@ __device__ __forceinline__ int div_ns(int j, int Ns, unsigned magic) {
   return Ns == 1 ? j : (int)__umulhi((unsigned)j, magic);
 }
 
-// One Stockham stage for radix R (compile-time) over nfft transforms of length M.
-template <typename T, int R>
+// One Stockham stage for radix R and direction DIR (compile-time) over nfft transforms of
+// length M; tw is this stage's twiddle table (k-major, R-1 entries per k).
+template <typename T, int R, int DIR>
 __device__ __forceinline__ void stage_fixed(const cplx<T>* __restrict__ in, cplx<T>* __restrict__ out, int M,
-                                            int nfft, int Ns, unsigned magic, const cplx<T>* __restrict__ W, int dir,
+                                            int nfft, int Ns, unsigned magic, const cplx<T>* __restrict__ tw,
                                             const Grp& G) {
   const int MR = M / R;
-  const int tws = M / (Ns * R);
   for (int f = 0; f < nfft; ++f) {
     const cplx<T>* src = in + (size_t)f * M;
     cplx<T>* dst = out + (size_t)f * M;
     for (int j = G.tid; j < MR; j += G.n) {
       const int jq = div_ns(j, Ns, magic);
       const int k = j - jq * Ns;
+      const cplx<T>* w = tw + k * (R - 1);
       cplx<T> v[R];
+      v[0] = src[j];
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        cplx<T> a = src[j + r * MR];
-        if (r > 0 && k > 0) {
-          cplx<T> w = W[r * k * tws];
-          if (dir > 0) w.y = -w.y;
-          a = cmul(a, w);
-        }
-        v[r] = a;
+      for (int r = 1; r < R; ++r) {
+        cplx<T> ww = w[r - 1];
+        if (DIR > 0) ww.y = -ww.y;
+        v[r] = cmul(src[j + r * MR], ww);
       }
-      dft_small<T, R>(v, dir);
+      dft_small<T, R>(v, DIR);
       const int base = jq * Ns * R + k;
 #pragma unroll
       for (int q = 0; q < R; ++q) dst[base + q * Ns] = v[q];
@@ -171,7 +174,7 @@ __device__ __forceinline__ void stage_fixed(const cplx<T>* __restrict__ in, cplx
   }
 }
 
-// Generic odd radix (any R up to 64): direct R-point DFT per output.
+// Generic odd radix (any R up to 64): direct R-point DFT per output; W is the full table.
 template <typename T>
 __device__ void stage_generic(const cplx<T>* __restrict__ in, cplx<T>* __restrict__ out, int M, int nfft, int Ns,
                               unsigned magic, int R, const cplx<T>* __restrict__ W, int dir, const Grp& G) {
@@ -200,22 +203,21 @@ __device__ void stage_generic(const cplx<T>* __restrict__ in, cplx<T>* __restric
   }
 }
 
-// Runs the FFT on nfft transforms held in a (length M each); the result is in
-// the returned buffer (a or b).  dir = -1 forward, +1 inverse (unnormalised).
-template <typename T>
-__device__ cplx<T>* fft_run(cplx<T>* a, cplx<T>* b, const FftPlan& plan, int nfft, const cplx<T>* W, int dir,
-                           const Grp& G) {
+template <typename T, int DIR>
+__device__ cplx<T>* fft_run_dir(cplx<T>* a, cplx<T>* b, const FftPlan& plan, int nfft, const cplx<T>* tw,
+                               const Grp& G) {
   int Ns = 1;
   for (int s = 0; s < plan.nstages; ++s) {
     const int R = plan.radix[s];
     const unsigned mg = plan.ns_magic[s];
+    const cplx<T>* ts = tw + plan.tw_off[s];
     switch (R) {
-      case 2: stage_fixed<T, 2>(a, b, plan.M, nfft, Ns, mg, W, dir, G); break;
-      case 3: stage_fixed<T, 3>(a, b, plan.M, nfft, Ns, mg, W, dir, G); break;
-      case 4: stage_fixed<T, 4>(a, b, plan.M, nfft, Ns, mg, W, dir, G); break;
-      case 5: stage_fixed<T, 5>(a, b, plan.M, nfft, Ns, mg, W, dir, G); break;
-      case 8: stage_fixed<T, 8>(a, b, plan.M, nfft, Ns, mg, W, dir, G); break;
-      default: stage_generic<T>(a, b, plan.M, nfft, Ns, mg, R, W, dir, G); break;
+      case 2: stage_fixed<T, 2, DIR>(a, b, plan.M, nfft, Ns, mg, ts, G); break;
+      case 3: stage_fixed<T, 3, DIR>(a, b, plan.M, nfft, Ns, mg, ts, G); break;
+      case 4: stage_fixed<T, 4, DIR>(a, b, plan.M, nfft, Ns, mg, ts, G); break;
+      case 5: stage_fixed<T, 5, DIR>(a, b, plan.M, nfft, Ns, mg, ts, G); break;
+      case 8: stage_fixed<T, 8, DIR>(a, b, plan.M, nfft, Ns, mg, ts, G); break;
+      default: stage_generic<T>(a, b, plan.M, nfft, Ns, mg, R, ts, DIR, G); break;
     }
     G.sync();
     cplx<T>* t = a;
@@ -226,10 +228,18 @@ __device__ cplx<T>* fft_run(cplx<T>* a, cplx<T>* b, const FftPlan& plan, int nff
   return a;
 }
 
+// Runs the FFT on nfft transforms held in a (length M each); the result is in
+// the returned buffer (a or b).  dir = -1 forward, +1 inverse (unnormalised).
+template <typename T>
+__device__ cplx<T>* fft_run(cplx<T>* a, cplx<T>* b, const FftPlan& plan, int nfft, const cplx<T>* tw, int dir,
+                           const Grp& G) {
+  return dir > 0 ? fft_run_dir<T, 1>(a, b, plan, nfft, tw, G) : fft_run_dir<T, -1>(a, b, plan, nfft, tw, G);
+}
+
 // Twiddle tables of one r2r transform of length n (T precision), device pointers.
 template <typename T>
 struct R2RTables {
-  const cplx<T>* W;     // FFT twiddles, length M
+  const cplx<T>* W;     // the plan's twiddle table (FftPlan)
   const cplx<T>* pre;   // type IV: exp(-i pi (4m+1)/(4n)), m < n/2
   const cplx<T>* post;  // DCT-II/III: (cos, sin)(pi k/(2n)), k < n; type IV: exp(-i pi k/n), k < n/2
 };

@@ -310,7 +310,8 @@ class MAC_CylinderFlow:
                   for _ in range(d.pressure_solve_count)]
         return dict(momentum_iterations=0, momentum_residual_linf=d.momentum_residual_linf,
                     coupled_momentum_residual_linf=d.coupled_momentum_residual_linf,
-                    pressure_backend='fft_boundary_schur', pressure_solve_count=int(d.pressure_solve_count),
+                    pressure_backend='gmres_rectangle' if self.pressure_solver == 'iterative' else 'fft_boundary_schur',
+                    pressure_solve_count=int(d.pressure_solve_count),
                     pressure_iterations=int(d.pressure_iterations),
                     pressure_refinement_iterations=int(d.pressure_refinement_iterations),
                     pressure_residual_linf=d.pressure_residual_linf,

@@ -829,3 +829,132 @@ def mac_divergence_stats(u, v, dx, dy, mask):
     d = div[fluid]
     return (float(np.max(abs(d))) if d.size else 0.0, float(np.sum(d * d)), int(d.size),
             float(np.sum(div[core] ** 2)), int(core.sum()))
+
+
+# ---------------------------------------------------------------------------
+# periodic Taylor-Green verification  (verification/taylor_green.py:14-59)
+# ---------------------------------------------------------------------------
+class PeriodicOperators:
+    """Operators of the periodic staggered Taylor-Green case on [0, 2 pi]^2.
+
+    u[j, i] sits at (i h, (j + 1/2) h), v[j, i] at ((i + 1/2) h, j h), p at cell centres.
+    advection / diffusion follow periodic_momentum_operator (solver/cut_cell_solver.py:108-130):
+    the full-fluid flux form of compute_momentum_rhs (:790-957, centred transport, rho = 1)
+    with a periodic halo, i.e. the face and corner fluxes below with wrapped indices, divided
+    by the cell volume h^2.  gradient / divergence / project are verification/taylor_green.py:37-45;
+    the CN Helmholtz system I - dt/2 nu L is solved exactly in Fourier space (the reference
+    runs GMRES to rtol 1e-12 on the same operator, solver/time_integration.py:97-99).
+    """
+
+    def __init__(self, n, nu):
+        self.n, self.nu = n, nu
+        self.h = 2 * np.pi / n
+        self.diff_offset = 0.0
+        self.helmholtz_dt = None
+        k = np.arange(n)
+        s2 = np.sin(np.pi * k / n) ** 2
+        self.symbol = -4 * (s2[:, None] + s2[None, :]) / self.h ** 2   # 5-point Laplacian symbol
+        eig = self.symbol.copy()
+        eig[0, 0] = 1.0
+        self.eigenvalues = eig
+
+    def unpack(self, q):
+        return q.reshape(2, self.n, self.n)
+
+    @staticmethod
+    def pack(u, v):
+        return np.r_[u.ravel(), v.ravel()]
+
+    def _flux(self, q, nu, include_advection):
+        u, v = self.unpack(q)
+        h = self.h
+        r = np.roll
+        # u equation: east faces (cell centres) and north corners
+        uE = 0.5 * (u + r(u, -1, 1))
+        Fxx = nu * (r(u, -1, 1) - u) / h * h
+        vN = 0.5 * (r(r(v, -1, 0), 1, 1) + r(v, -1, 0))          # v at the north corner of u[j, i]
+        uN = 0.5 * (u + r(u, -1, 0))
+        Fxy = nu * (r(u, -1, 0) - u) / h * h                        # flux through the north corner face
+        if include_advection:
+            Fxx = Fxx - uE * uE * h
+            Fxy = Fxy - vN * uN * h
+        au = ((Fxx - r(Fxx, 1, 1)) + (Fxy - r(Fxy, 1, 0))) / (h * h)
+        # v equation: north faces (cell centres) and east corners
+        vC = 0.5 * (v + r(v, -1, 0))
+        Fyy = nu * (r(v, -1, 0) - v) / h * h
+        uE2 = 0.5 * (r(r(u, -1, 1), 1, 0) + r(u, -1, 1))          # u at the east corner of v[j, i]
+        vE = 0.5 * (v + r(v, -1, 1))
+        Fyx = nu * (r(v, -1, 1) - v) / h * h
+        if include_advection:
+            Fyy = Fyy - vC * vC * h
+            Fyx = Fyx - uE2 * vE * h
+        av = ((Fyx - r(Fyx, 1, 1)) + (Fyy - r(Fyy, 1, 0))) / (h * h)
+        return self.pack(au, av)
+
+    def advection(self, q):
+        return self._flux(q, 0.0, True)
+
+    def diffusion(self, q):
+        return self._flux(q, self.nu, False)
+
+    def gradient(self, p):
+        return self.pack(p - np.roll(p, 1, 1), p - np.roll(p, 1, 0)) / self.h
+
+    def divergence(self, q):
+        u, v = self.unpack(q)
+        return (np.roll(u, -1, 1) - u + np.roll(v, -1, 0) - v) / self.h
+
+    def project(self, q, step):
+        from scipy.fft import fft2, ifft2
+        rhs = fft2(self.divergence(q) / step)
+        rhs[0, 0] = 0.0
+        phi = ifft2(rhs / self.eigenvalues).real
+        return q - step * self.gradient(phi), phi
+
+    def build_helmholtz(self, dt):
+        self.helmholtz_dt = dt
+
+    def helmholtz(self, rhs):
+        from scipy.fft import fft2, ifft2
+        c = 0.5 * self.helmholtz_dt * self.nu
+        u, v = self.unpack(rhs)
+        den = 1.0 - c * self.symbol
+        return self.pack(ifft2(fft2(u) / den).real, ifft2(fft2(v) / den).real)
+
+    def H_matvec(self, q, dt):
+        return q - 0.5 * dt * self.diffusion(q)
+
+
+def taylor_green_exact(n, nu, t):
+    """Analytic Taylor-Green fields on the staggered grid (verification/taylor_green.py:21-29)."""
+    h = 2 * np.pi / n
+    yu, xu = np.meshgrid((np.arange(n) + .5) * h, np.arange(n) * h, indexing='ij')
+    yv, xv = np.meshgrid(np.arange(n) * h, (np.arange(n) + .5) * h, indexing='ij')
+    yp, xp = np.meshgrid((np.arange(n) + .5) * h, (np.arange(n) + .5) * h, indexing='ij')
+    a = np.exp(-2 * nu * t)
+    q = PeriodicOperators.pack(a * np.sin(xu) * np.cos(yu), -a * np.cos(xv) * np.sin(yv))
+    return q, .25 * a * a * (np.cos(2 * xp) + np.cos(2 * yp))
+
+
+def taylor_green_run(n, dt, end_time=.4, nu=.1):
+    """verification/taylor_green.py:14-59: AB2/CN steps from the analytic field, error norms
+    against the analytic solution at end_time, maximum divergence."""
+    if n < 8 or not np.isfinite([dt, end_time, nu]).all() or min(dt, end_time, nu) <= 0:
+        raise ValueError('Require n>=8 and finite positive dt, end_time and nu')
+    steps = round(end_time / dt)
+    if steps < 1 or not np.isclose(steps * dt, end_time):
+        raise ValueError('end_time must be an integer multiple of dt')
+    ops = PeriodicOperators(n, nu)
+    q, p = taylor_green_exact(n, nu, 0.0)
+    history = previous_dt = None
+    output = p
+    max_divergence = 0.0
+    for _ in range(steps):
+        q, p, output, history, _ = ab2_cn_step(ops, q, p, dt, history, previous_dt)
+        previous_dt = dt
+        max_divergence = max(max_divergence, float(np.max(abs(ops.divergence(q)))))
+    q_exact, p_exact = taylor_green_exact(n, nu, end_time)
+    p_error = output - output.mean() - p_exact
+    norms = lambda a: dict(l1=float(np.mean(abs(a))), l2=float(np.sqrt(np.mean(a * a))), linf=float(np.max(abs(a))))
+    return dict(n=n, dt=dt, end_time=end_time, velocity=norms(q - q_exact), pressure=norms(p_error),
+                max_divergence=max_divergence), q, output - output.mean()

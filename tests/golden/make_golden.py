@@ -48,6 +48,8 @@ def build_harness(reference: Path, work: Path) -> Path:
     shutil.copytree(reference / 'solver', solver, ignore=shutil.ignore_patterns('*.pyd', '__pycache__'))
     shutil.copytree(reference / 'postprocessing', work / 'postprocessing',
                     ignore=shutil.ignore_patterns('__pycache__'))
+    shutil.copytree(reference / 'verification', work / 'verification',
+                    ignore=shutil.ignore_patterns('__pycache__'))
     stubs = work / 'stubs'
     (stubs / 'matplotlib').mkdir(parents=True)
     (stubs / 'numba.py').write_text(NUMBA_STUB)
@@ -123,13 +125,35 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', type=Path, default=Path('/root/reference'))
     ap.add_argument('--skip-large', action='store_true')
+    ap.add_argument('--only', choices=('taylor_green',), help='generate one group of fixtures only')
     args = ap.parse_args()
     work = Path(tempfile.mkdtemp(prefix='ghost_golden_'))
     try:
         build_harness(args.reference, work)
-        run_all(args)
+        if args.only == 'taylor_green':
+            run_taylor_green(work)
+        else:
+            run_all(args)
+            run_taylor_green(work)
     finally:
         shutil.rmtree(work, ignore_errors=True)
+
+
+def run_taylor_green(work):
+    """The reference's periodic Taylor-Green verification (verification/taylor_green.py:14-59):
+    error norms, final velocity and pressure for two small grids."""
+    sys.path.insert(0, str(work / 'verification'))
+    import taylor_green
+    out = {}
+    for tag, (n, dt, end, nu) in {'n16': (16, .01, .05, .1), 'n32': (32, .0025, .1, .1)}.items():
+        info, q, p = taylor_green.run(n, dt, end_time=end, nu=nu)
+        out[f'{tag}_q'] = q
+        out[f'{tag}_p'] = p
+        out[f'{tag}_norms'] = np.array([info['velocity'][k] for k in ('l1', 'l2', 'linf')] +
+                                       [info['pressure'][k] for k in ('l1', 'l2', 'linf')] +
+                                       [info['max_divergence']])
+        out[f'{tag}_params'] = np.array([n, dt, end, nu])
+    save('taylor_green', **out)
 
 
 def run_all(args):

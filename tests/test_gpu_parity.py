@@ -241,3 +241,34 @@ def test_fp32_mode_config1(pkg):
         d = s.last_step_diagnostics
         assert abs(d['cd'] - G['scalars'][k][0]) < 1e-6 * abs(G['scalars'][k][0])
         assert d['max_divergence'] < 1e-10
+
+
+def test_iterative_pressure_path_golden(pkg):
+    """pressure_solver='iterative' (GMRES with the rectangle preconditioner) against the
+    reference's own three steps (tests/golden/opt40x30_iter.npz).  GMRES stops at
+    rtol = 1e-12 plus refinement, so the fields agree to the solver tolerance."""
+    G = np.load(GOLDEN / 'opt40x30_iter.npz')
+    s = pkg.MAC_CylinderFlow(nx=40, ny=30, Lx=4., Ly=3., xc=1.5, yc=1.5, verbose=False, pressure_solver='iterative')
+    s.solve(n_steps=3, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
+    assert rel(s.u, G['u']) < 1e-9 and rel(s.v, G['v']) < 1e-9 and rel(s.p, G['p']) < 1e-8
+    assert abs(s.last_step_diagnostics['cd'] - G['scalars'][0]) < 1e-8 * abs(G['scalars'][0])
+    d = s.last_step_diagnostics
+    assert d['max_divergence'] < 1e-10 and d['pressure_backend'] == 'gmres_rectangle'
+    assert d['pressure_iterations'] > 0
+
+
+def test_iterative_matches_direct_solve(pkg):
+    """GMRES and the FFT + boundary Schur direct solve agree (the reference asserts 1e-9 /
+    1e-8 between its two backends)."""
+    kw = dict(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., verbose=False)
+    sd = pkg.MAC_CylinderFlow(**kw)
+    si = pkg.MAC_CylinderFlow(pressure_solver='iterative', **kw)
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(len(sd.gg.pi))
+    xd = sd.gg.pressure_solve(b)
+    xi = si.gg.pressure_solve(b)
+    assert np.max(np.abs(xd - xi)) < 1e-9 * max(1.0, np.max(np.abs(xd)))
+    for prec in ('fp32',):
+        sf = pkg.MAC_CylinderFlow(pressure_solver='iterative', precision=prec, **kw)
+        xf = sf.gg.pressure_solve(b)
+        assert np.max(np.abs(xf - xd)) < 1e-8 * max(1.0, np.max(np.abs(xd)))

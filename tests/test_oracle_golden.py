@@ -136,3 +136,19 @@ def test_config1_two_steps():
         assert abs(c.last_step_diagnostics['cd'] - G['scalars'][k][0]) < 1e-12
     assert c.ops.pressure_info['rank'] == G['pressure_rank']
     assert [i['rank'] for i in c.ops.helmholtz_info] == list(G['helmholtz_ranks'])
+
+
+def test_taylor_green_oracle_matches_reference():
+    """The oracle's periodic Taylor-Green run against the reference's own
+    verification/taylor_green.run (tests/golden/taylor_green.npz; the reference solves the
+    CN system with GMRES to rtol 1e-12, the oracle exactly in Fourier space)."""
+    G = np.load(GOLDEN / 'taylor_green.npz')
+    for tag in ('n16', 'n32'):
+        n, dt, end, nu = G[f'{tag}_params']
+        info, q, p = go.taylor_green_run(int(n), dt, end, nu)
+        assert np.max(np.abs(q - G[f'{tag}_q'])) < 1e-12 * np.max(np.abs(G[f'{tag}_q']))
+        assert np.max(np.abs(p - G[f'{tag}_p'])) < 1e-11 * np.max(np.abs(G[f'{tag}_p']))
+        norms = np.array([info['velocity'][k] for k in ('l1', 'l2', 'linf')] +
+                         [info['pressure'][k] for k in ('l1', 'l2', 'linf')])
+        np.testing.assert_allclose(norms, G[f'{tag}_norms'][:6], rtol=1e-9)
+        assert info['max_divergence'] < 1e-10
