@@ -24,7 +24,10 @@ SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_las
            'gm_get_history', 'gm_step', 'gm_apply', 'gm_project', 'gm_pressure_solve', 'gm_rectangle_solve',
            'gm_surface_forces', 'gm_divergence_stats', 'gm_kernel_launches', 'gm_kernel_timing',
            'gm_divergence_stats_noalloc', 'gm_batch_create', 'gm_batch_destroy', 'gm_batch_last_error',
-           'gm_batch_step', 'gm_phase_timing')
+           'gm_batch_step', 'gm_phase_timing', 'gm_tg_create', 'gm_tg_destroy', 'gm_tg_last_error',
+           'gm_tg_set_state', 'gm_tg_get_state', 'gm_tg_step', 'gm_unet_layers', 'gm_unet_create',
+           'gm_unet_destroy', 'gm_unet_last_error', 'gm_unet_input', 'gm_unet_forward', 'gm_unet_backward',
+           'gm_set_learned_preconditioner', 'gm_set_pressure_recorder', 'gm_pressure_recorded')
 NOALLOC_MAX_CELLS = 1048576
 
 
@@ -98,6 +101,22 @@ def _load():
         'gm_batch_last_error': ([P], C.c_char_p),
         'gm_batch_step': ([P, D, I32, I64, P, C.POINTER(StepDiag), P], C.c_int),
         'gm_phase_timing': ([P, P], C.c_int),
+        'gm_tg_create': ([I32, D, I32, pp], C.c_int),
+        'gm_tg_destroy': ([P], C.c_int),
+        'gm_tg_last_error': ([P], C.c_char_p),
+        'gm_tg_set_state': ([P, P, P], C.c_int),
+        'gm_tg_get_state': ([P, P, P, P], C.c_int),
+        'gm_tg_step': ([P, D, I32, C.POINTER(D)], C.c_int),
+        'gm_unet_layers': ([P, P, P], C.c_int),
+        'gm_unet_create': ([I32, I32, I32, pp], C.c_int),
+        'gm_unet_destroy': ([P], C.c_int),
+        'gm_unet_last_error': ([P], C.c_char_p),
+        'gm_unet_input': ([P, P], C.c_int),
+        'gm_unet_forward': ([P, P, P, P, P, P], C.c_int),
+        'gm_unet_backward': ([P, P, P, P, P, P], C.c_int),
+        'gm_set_learned_preconditioner': ([P, P, P, P], C.c_int),
+        'gm_set_pressure_recorder': ([P, P, P, I32], C.c_int),
+        'gm_pressure_recorded': ([P], I32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

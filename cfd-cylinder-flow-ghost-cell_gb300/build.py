@@ -52,6 +52,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
           '-o', str(BUILD / 'ghostmac.o')]),
         ([nvcc, *ARCH, '-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', *inc, '-c', str(SRC / 'noalloc.cu'),
           '-o', str(BUILD / 'noalloc.o')]),
+        ([nvcc, *ARCH, '-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', *inc, '-c', str(SRC / 'periodic.cu'),
+          '-o', str(BUILD / 'periodic.o')]),
+        ([nvcc, *ARCH, '-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', *inc, '-c', str(SRC / 'unet.cu'),
+          '-o', str(BUILD / 'unet.o')]),
     ]
     procs = [subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True) for cmd in jobs]
     failed = []
@@ -65,7 +69,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         raise RuntimeError('build failed:\n' + '\n'.join(f'{c}\n{o}' for c, o in failed))
     tmp = OUT.with_suffix('.so.tmp')
     link = [nvcc, *ARCH, '-shared', '-o', str(tmp), str(BUILD / 'geometry.o'), str(BUILD / 'kernels.o'),
-            str(BUILD / 'ghostmac.o'), str(BUILD / 'noalloc.o'), '-lcudart']
+            str(BUILD / 'ghostmac.o'), str(BUILD / 'noalloc.o'), str(BUILD / 'periodic.o'),
+            str(BUILD / 'unet.o'), '-lcudart']
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode:
         raise RuntimeError('link failed:\n' + r.stdout + r.stderr)

@@ -17,6 +17,7 @@
 
 #include "../../include/ghostmac.h"
 #include "geometry.hpp"
+#include "fftplan.hpp"
 #include "kernels.cuh"
 
 using namespace gmk;
@@ -88,74 +89,6 @@ bool is_device_ptr(const void* p) {
 }
 
 // radix plan of an FFT length
-FftPlan make_plan(int M) {
-  FftPlan p{};
-  p.M = M;
-  int m = M, s = 0;
-  while (m % 8 == 0) { p.radix[s++] = 8; m /= 8; }
-  while (m % 4 == 0) { p.radix[s++] = 4; m /= 4; }
-  while (m % 2 == 0) { p.radix[s++] = 2; m /= 2; }
-  while (m % 5 == 0) { p.radix[s++] = 5; m /= 5; }
-  while (m % 3 == 0) { p.radix[s++] = 3; m /= 3; }
-  for (int f = 7; m > 1; f += 2)
-    while (m % f == 0) {
-      if (f > 64) throw CudaError("FFT length has a prime factor above 64");
-      p.radix[s++] = f;
-      m /= f;
-    }
-  p.nstages = s;
-  if (M > 65536) throw CudaError("FFT length above 65536");
-  long long Ns = 1;
-  int off = 0;
-  bool generic = false;
-  for (int k = 0; k < s; ++k) {
-    p.ns_magic[k] = Ns == 1 ? 0u : (unsigned)(((1ull << 32) + (unsigned long long)Ns - 1) / (unsigned long long)Ns);
-    const int R = p.radix[k];
-    if (R == 2 || R == 3 || R == 4 || R == 5 || R == 8) {
-      p.tw_off[k] = off;
-      off += (int)Ns * (R - 1);
-    } else {
-      generic = true;
-    }
-    Ns *= R;
-  }
-  for (int k = 0; k < s; ++k) {
-    const int R = p.radix[k];
-    if (!(R == 2 || R == 3 || R == 4 || R == 5 || R == 8)) p.tw_off[k] = off;  // the full table follows
-  }
-  p.tw_len = off + (generic ? M : 0);
-  return p;
-}
-
-// The plan's twiddle table (see FftPlan), interleaved (re, im), forward sign exp(-2 pi i t / M).
-std::vector<double> plan_twiddles(const FftPlan& p) {
-  std::vector<double> t(2 * (size_t)p.tw_len);
-  const long double PI = 3.14159265358979323846264338327950288L;
-  auto put = [&](int at, long long e) {
-    const long double a = -2.0L * PI * (long double)(e % p.M) / (long double)p.M;
-    t[2 * (size_t)at] = (double)std::cos(a);
-    t[2 * (size_t)at + 1] = (double)std::sin(a);
-  };
-  long long Ns = 1;
-  bool generic = false;
-  for (int s = 0; s < p.nstages; ++s) {
-    const int R = p.radix[s];
-    if (R == 2 || R == 3 || R == 4 || R == 5 || R == 8) {
-      const long long tws = p.M / (Ns * R);
-      for (long long k = 0; k < Ns; ++k)
-        for (int r = 1; r < R; ++r) put(p.tw_off[s] + (int)(k * (R - 1) + r - 1), r * k * tws);
-    } else {
-      generic = true;
-    }
-    Ns *= R;
-  }
-  if (generic) {
-    int base = p.tw_len - p.M;
-    for (int e = 0; e < p.M; ++e) put(base + e, e);
-  }
-  return t;
-}
-
 std::vector<double> cexp_table(int count, double scale_num, double scale_den, double offset, int sign) {
   // entries exp(sign * i * pi * (k*scale_num + offset) / scale_den), interleaved (re, im)
   std::vector<double> t(2 * (size_t)count);
@@ -221,6 +154,16 @@ struct gm_handle {
   // directions Z (m), the refinement correction and reduction scratch
   static constexpr int GMRES_M = 50;
   DBuf<double> gV, gZ, gdx, gpart, gdots, gcoef;
+  // learned preconditioner attached to the GMRES path (network and weights owned by the caller)
+  gm_unet* lnet = nullptr;
+  std::vector<const uint16_t*> lw;
+  std::vector<const float*> lb;
+  DBuf<float> lout;              // network output (pressure grid)
+  DBuf<unsigned long long> lscale;  // max |r| bits
+  // recorder of the pressure solves of launch-by-launch steps: (right-hand side, solution)
+  double* rec_rhs = nullptr;
+  double* rec_sol = nullptr;
+  int rec_cap = 0, rec_count = 0;
   ResidualCoef rcoef[3];       // regular-row coefficients: pressure, Helmholtz u, Helmholtz v
   DBuf<float> spectral32, ffirst32, pfirst32;
   DBuf<StepCtl> ctl;
@@ -991,6 +934,16 @@ int fgmres(gm_handle* h, const double* b, double* x, int& iterations) {
                                            st);
     else
       plain_inverse<double, double, double>(rd.tt, rd.view, v, true, h->spectral.p, z, rd.view.cls, nullptr, open, st);
+    if (h->lnet) {
+      // z += s net([v / s, mask]), s = max |v|  (FP32 network, FGMRES absorbs its nonlinearity)
+      float* xin = nullptr;
+      gm_unet_input(h->lnet, &xin);
+      CK(cudaMemsetAsync(h->lscale.p, 0, sizeof(unsigned long long), st));
+      launch_learned_prep(h->cd, v, xin, h->lscale.p, st);
+      if (gm_unet_forward(h->lnet, h->lw.data(), h->lb.data(), nullptr, h->lout.p, st) != GM_OK)
+        throw CudaError(std::string("learned preconditioner: ") + gm_unet_last_error(h->lnet));
+      launch_learned_apply(h->cd, h->lout.p, h->lscale.p, z, st);
+    }
   };
   double bn2 = 0;
   dots(b, 1, b, &bn2);
@@ -1146,6 +1099,12 @@ void project(gm_handle* h, double* q, double dt, double* out, double* phi, int s
   ghost_faces(h, q, g0);
   launch_divergence(h->cd, q, h->prhs.p, dt, nullptr, nullptr, 1, g0, st);
   schur_solve(h, 0, h->rp, 0, 0.0, h->prhs.p, phi, h->pres.p, h->pfirst.p, h->pw2.p, slot);
+  if (h->rec_rhs && !h->capturing && h->rec_count < h->rec_cap) {
+    const size_t off = (size_t)h->rec_count * h->Pn;
+    CK(cudaMemcpyAsync(h->rec_rhs + off, h->prhs.p, h->Pn * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(h->rec_sol + off, phi, h->Pn * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    ++h->rec_count;
+  }
   launch_gate_pressure(h->ctl.p, slot, h->nchk, st);
   ghost_p(h, phi, g0);
   launch_project_update(h->cd, q, phi, dt, out, nullptr, g0, st);
@@ -1795,7 +1754,7 @@ int gm_step(gm_handle* h, double dt, int32_t n_steps, int64_t first_step_index, 
     while (s < n_steps) {
       // steps that differ from the steady pattern run launch by launch: the start-up step,
       // a changed dt, or per-kernel event timing
-      const bool direct = !h->has_history || h->prev_dt != dt || !h->use_graphs || ktimer_active();
+      const bool direct = !h->has_history || h->prev_dt != dt || !h->use_graphs || ktimer_active() || h->rec_rhs;
       const bool first = !h->has_history;
       const int batch = direct ? 1 : std::min(n_steps - s, (int)gm_handle::RING_CAP);
       CK(cudaMemsetAsync(h->ridx.p, 0, sizeof(int), st));
@@ -2083,6 +2042,37 @@ int gm_divergence_stats(gm_handle* h, const double* u, const double* v, double o
 extern "C" {
 
 int64_t gm_kernel_launches(void) { return (int64_t)kernel_launch_count(); }
+
+int gm_set_pressure_recorder(gm_handle* h, double* rhs, double* sol, int32_t capacity) {
+  if (!h) return GM_EVALUE;
+  if (capacity < 0 || ((!rhs || !sol) && capacity > 0)) { h->err = "recorder needs two device buffers"; return GM_EVALUE; }
+  h->rec_rhs = capacity > 0 ? rhs : nullptr;
+  h->rec_sol = capacity > 0 ? sol : nullptr;
+  h->rec_cap = capacity;
+  h->rec_count = 0;
+  return GM_OK;
+}
+int32_t gm_pressure_recorded(const gm_handle* h) { return h ? h->rec_count : 0; }
+
+int gm_set_learned_preconditioner(gm_handle* h, gm_unet* net, const uint16_t* const* w_bf16, const float* const* bias) {
+  if (!h) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  if (!net) {
+    h->lnet = nullptr;
+    return GM_OK;
+  }
+  if (!w_bf16 || !bias) { h->err = "weights and biases are required"; return GM_EVALUE; }
+  if (h->g.pressure_solver != 1) { h->err = "the learned preconditioner serves the GMRES path (pressure_solver=iterative)"; return GM_EVALUE; }
+  int32_t nl = 0;
+  gm_unet_layers(&nl, nullptr, nullptr);
+  return run_guarded(h, [&] {
+    h->lw.assign(w_bf16, w_bf16 + nl);
+    h->lb.assign(bias, bias + nl);
+    if (h->lout.n != (size_t)h->Pn) h->lout.alloc(h->Pn);
+    if (!h->lscale.p) h->lscale.alloc(1);
+    h->lnet = net;
+  });
+}
 
 int gm_phase_timing(const gm_handle* h, double out[14]) {
   if (!h || !out) return GM_EVALUE;

@@ -1142,6 +1142,43 @@ void launch_multiaxpy(const double* V, int64_t ld, int nv, const double* coef, d
   kt_mark(6, st, (double)n * 8 * (nv + 2));
 }
 
+// Learned preconditioner input / output on the pressure grid: x = [v / s, mask] (float32,
+// 2 planes), s = max |v| over the active cells (computed by the first kernel into *s_bits);
+// z += s y on the active cells.
+__global__ void k_learned_max(CaseDev c, const double* __restrict__ v, unsigned long long* s_bits) {
+  unsigned long long m = 0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < c.psize; t += (int64_t)gridDim.x * blockDim.x)
+    if (c.cls_p[t] & CLS_ACTIVE) m = umax64(m, absbits(v[t]));
+  block_commit_max(m, s_bits);
+}
+__global__ void k_learned_in(CaseDev c, const double* __restrict__ v, const unsigned long long* __restrict__ s_bits,
+                             float* __restrict__ x) {
+  const double s = bits2d(*s_bits);
+  const double inv = s > 0 ? 1.0 / s : 0.0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < c.psize; t += (int64_t)gridDim.x * blockDim.x) {
+    const bool act = c.cls_p[t] & CLS_ACTIVE;
+    x[t] = act ? (float)(v[t] * inv) : 0.f;
+    x[c.psize + t] = act ? 1.f : 0.f;
+  }
+}
+__global__ void k_learned_out(CaseDev c, const float* __restrict__ y, const unsigned long long* __restrict__ s_bits,
+                              double* __restrict__ z) {
+  const double s = bits2d(*s_bits);
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < c.psize; t += (int64_t)gridDim.x * blockDim.x)
+    if (c.cls_p[t] & CLS_ACTIVE) z[t] += s * (double)y[t];
+}
+void launch_learned_prep(const CaseDev& c, const double* v, float* x, unsigned long long* s_bits, cudaStream_t st) {
+  note_launch();
+  k_learned_max<<<reduce_blocks(c.psize), TPB, 0, st>>>(c, v, s_bits);
+  note_launch();
+  k_learned_in<<<reduce_blocks(c.psize), TPB, 0, st>>>(c, v, s_bits, x);
+}
+void launch_learned_apply(const CaseDev& c, const float* y, const unsigned long long* s_bits, double* z,
+                          cudaStream_t st) {
+  note_launch();
+  k_learned_out<<<reduce_blocks(c.psize), TPB, 0, st>>>(c, y, s_bits, z);
+}
+
 // ---------------------------------------------------------------------------
 // projection pieces
 // ---------------------------------------------------------------------------

@@ -253,6 +253,10 @@ void launch_apply_pressure(const CaseDev& c, const ResidualCoef& rc, const doubl
 void launch_multidot(const double* V, int64_t ld, int nv, const double* w, int64_t n, double* part, double* out,
                      cudaStream_t st);
 unsigned multidot_blocks(int64_t n);
+// learned preconditioner glue: x = [v / s, mask] with s = max |v| (bits in *s_bits); z += s y
+void launch_learned_prep(const CaseDev& c, const double* v, float* x, unsigned long long* s_bits, cudaStream_t st);
+void launch_learned_apply(const CaseDev& c, const float* y, const unsigned long long* s_bits, double* z,
+                          cudaStream_t st);
 void launch_multiaxpy(const double* V, int64_t ld, int nv, const double* coef, double sign, double alpha, double* y,
                       int64_t n, cudaStream_t st);
 

@@ -199,6 +199,62 @@ const char* gm_batch_last_error(const gm_batch* b);
 int gm_batch_step(gm_batch* b, double dt, int32_t n_steps, int64_t first_step_index, const double* start_times,
                   gm_step_diag* diag, int32_t* steps_done);
 
+/* --- periodic Taylor-Green case (verification/taylor_green.py:14-59) ------------- */
+
+/* The AB2/CN step on the periodic staggered grid of [0, 2 pi]^2 (n x n cells, h = 2 pi / n)
+ * with the periodic flux-form operators of solver/cut_cell_solver.py:108-130 and
+ * Fourier-space pressure and CN solves.  precision 0: FP64; 1: FP32 stencils and
+ * transforms with both solves refined against the FP64 operators. */
+typedef struct gm_tg gm_tg;
+int gm_tg_create(int32_t n, double nu, int32_t precision, gm_tg** out);
+int gm_tg_destroy(gm_tg* t);
+const char* gm_tg_last_error(const gm_tg* t);
+/* q: u (n x n) then v (n x n); p: n x n (host or device pointers); clears the AB2 history */
+int gm_tg_set_state(gm_tg* t, const double* q, const double* p);
+/* any output may be NULL: velocity, half-step pressure, output pressure of the last step */
+int gm_tg_get_state(gm_tg* t, double* q, double* p_half, double* p_out);
+/* n_steps AB2/CN steps of size dt; *max_divergence (in/out) is raised to the largest
+ * max |div q| after any step */
+int gm_tg_step(gm_tg* t, double dt, int32_t n_steps, double* max_divergence);
+
+/* --- learned pressure preconditioner (no reference counterpart) ----------------- */
+
+/* A 4-level convolutional U-Net on the pressure grid (channels 16, 32, 64, 64; 12 3x3
+ * convolutions, 253,872 weights + 465 biases), BF16 weights, FP32 activations and
+ * accumulation.  It is the learned slot of the GMRES preconditioner.  Weights are passed per
+ * call: w_bf16[k] = layer k's weights [cout][cin][3][3] as BF16 bit patterns, bias[k] =
+ * [cout] floats (device pointers).  Tensors are [batch][channel][height][width] float32
+ * (device); height and width are multiples of 8. */
+typedef struct gm_unet gm_unet;
+int gm_unet_layers(int32_t* n_layers, int32_t* cin, int32_t* cout);
+int gm_unet_create(int32_t batch, int32_t height, int32_t width, gm_unet** out);
+int gm_unet_destroy(gm_unet* u);
+const char* gm_unet_last_error(const gm_unet* u);
+/* the network's own input buffer (batch x 2 x height x width) */
+int gm_unet_input(gm_unet* u, float** x);
+/* y (batch x 1 x height x width) = net(x); x may be NULL (the input buffer is used); the
+ * activations are kept for gm_unet_backward */
+int gm_unet_forward(gm_unet* u, const uint16_t* const* w_bf16, const float* const* bias, const float* x, float* y,
+                    void* cuda_stream);
+/* adds dL/dw and dL/db of the last forward pass for dL/dy = dy to dw[k] ([cout][cin][3][3])
+ * and db[k] ([cout]) */
+int gm_unet_backward(gm_unet* u, const uint16_t* const* w_bf16, const float* dy, float* const* dw, float* const* db,
+                     void* cuda_stream);
+/* Attaches a network to a handle's GMRES path (pressure_solver = iterative): the
+ * preconditioner becomes z = T^-1 r + s net([r / s, mask]) with s = max |r|.  The network's
+ * grid must be the pressure grid (batch 1); the weight arrays stay owned by the caller and
+ * must outlive the attachment.  net = NULL detaches. */
+int gm_set_learned_preconditioner(gm_handle* h, gm_unet* net, const uint16_t* const* w_bf16,
+                                  const float* const* bias);
+
+/* Records the pressure solves of the following steps (the training pairs of the learned
+ * preconditioner): solve k stores its right-hand side at rhs + k * nx * ny and its solution at
+ * sol + k * nx * ny (pressure grids, zeros off the active cells; device buffers of
+ * capacity * nx * ny doubles).  While recording, steps run launch by launch.  capacity 0
+ * stops recording. */
+int gm_set_pressure_recorder(gm_handle* h, double* rhs, double* sol, int32_t capacity);
+int32_t gm_pressure_recorded(const gm_handle* h);
+
 /* --- allocation-free entry point ------------------------------------------------ */
 
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc (code

@@ -125,18 +125,38 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', type=Path, default=Path('/root/reference'))
     ap.add_argument('--skip-large', action='store_true')
-    ap.add_argument('--only', choices=('taylor_green',), help='generate one group of fixtures only')
+    ap.add_argument('--only', choices=('taylor_green', 'analysis'), help='generate one group of fixtures only')
     args = ap.parse_args()
     work = Path(tempfile.mkdtemp(prefix='ghost_golden_'))
     try:
         build_harness(args.reference, work)
         if args.only == 'taylor_green':
             run_taylor_green(work)
+        elif args.only == 'analysis':
+            run_analysis(work)
         else:
             run_all(args)
             run_taylor_green(work)
+            run_analysis(work)
     finally:
         shutil.rmtree(work, ignore_errors=True)
+
+
+def run_analysis(work):
+    """postprocessing/analysis.py periodic_metrics on seeded synthetic force histories: a
+    resolved, drifting shedding signal and an unresolved one."""
+    from postprocessing.analysis import periodic_metrics
+    rng = np.random.default_rng(4)
+    t = np.linspace(0, 60, 3001)
+    cl = 0.3 * (1 + 0.01 * t) * np.sin(2 * np.pi * 0.17 * t + 0.3) + 1e-3 * rng.standard_normal(t.size)
+    cd = 1.3 + 0.02 * np.sin(4 * np.pi * 0.17 * t) + 1e-3 * rng.standard_normal(t.size)
+    keys = None
+    rows = []
+    for (tt, a, b, ts) in ((t, cd, cl, 5.0), (t[:200], cd[:200], cl[:200] * 0 + 1e-3 * t[:200], 0.0)):
+        m = periodic_metrics(tt, a, b, ts, D=1.0, U_ref=1.0)
+        keys = sorted(m)
+        rows.append([float(m[k]) for k in keys])
+    save('analysis', t=t, cd=cd, cl=cl, keys=np.array(keys), values=np.array(rows))
 
 
 def run_taylor_green(work):

@@ -54,7 +54,7 @@ def test_library_exports_every_declared_symbol(L):
     import re
     from conftest import ROOT
     header = (ROOT / 'include' / 'ghostmac.h').read_text()
-    declared = set(re.findall(r'^\s*(?:int|int64_t|const char\*)\s+(gm_\w+)\s*\(', header, re.M))
+    declared = set(re.findall(r'^\s*(?:int|int32_t|int64_t|const char\*)\s+(gm_\w+)\s*\(', header, re.M))
     assert declared and declared == set(L.SYMBOLS), declared ^ set(L.SYMBOLS)
     for name in declared:
         assert hasattr(L.lib, name), name

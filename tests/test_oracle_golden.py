@@ -152,3 +152,23 @@ def test_taylor_green_oracle_matches_reference():
                          [info['pressure'][k] for k in ('l1', 'l2', 'linf')])
         np.testing.assert_allclose(norms, G[f'{tag}_norms'][:6], rtol=1e-9)
         assert info['max_divergence'] < 1e-10
+
+
+def test_periodic_metrics_matches_reference():
+    """The host-side force-history analysis against the reference's periodic_metrics on seeded
+    synthetic series (tests/golden/analysis.npz)."""
+    import importlib.util
+    from pathlib import Path
+    spec = importlib.util.spec_from_file_location(
+        'gm_analysis', Path(__file__).resolve().parents[1] / 'cfd-cylinder-flow-ghost-cell_gb300' / 'analysis.py')
+    an = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(an)
+    G = np.load(GOLDEN / 'analysis.npz')
+    t, cd, cl = G['t'], G['cd'], G['cl']
+    cases = ((t, cd, cl, 5.0), (t[:200], cd[:200], cl[:200] * 0 + 1e-3 * t[:200], 0.0))
+    for (tt, a, b, ts), want in zip(cases, G['values']):
+        m = an.periodic_metrics(tt, a, b, ts, D=1.0, U_ref=1.0)
+        got = np.array([float(m[str(k)]) for k in G['keys']])
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-14, equal_nan=True)
+    with pytest.raises(ValueError):
+        an.periodic_metrics([0, 1], [1, 1], [0, 0], 0.0)
