@@ -50,6 +50,14 @@ BATCH_WORKLOADS = {
                           re=(40.0, 200.0), diameter=(0.8, 1.2), jitter=0.5, amp=1e-3),
 }
 DEFAULT_WORKLOAD = 'wide_800x820_re100'
+# DRAM bytes (read + write) per launch of the dominant kernel class, averaged over the launches
+# of one ncu --set full capture of the same command (the capture's file under profiles/ gives the
+# command and the per-launch figures).  Within a step the working set stays in L2, so DRAM
+# traffic is far below the algorithmic bytes.
+DRAM_TRAFFIC = {
+    # profiles/k_xpass_fp64_wide_800x820.md: (1792 + 512 + 256 + 5888) / 4
+    ('wide_800x820_re100', 'fp64', 1): 2112.0,
+}
 KERNEL_CLASSES = {1: 'row transforms (k_xpass)', 2: 'column solves (k_ysolve, k_yband)',
                   3: 'momentum rhs (k_momentum, k_shadow)', 4: 'operator residual (k_residual, k_pressure_bound)',
                   5: 'Schur GEMV (k_schur)', 6: 'projection (k_divergence, k_project_update, k_set_inlet)',
@@ -85,7 +93,7 @@ class ClockSampler:
              'clocks_event_reasons.sw_power_cap')
         try:
             self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), f'--query-gpu={q}',
-                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                          '--format=csv,noheader,nounits', '-lms', '50'],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -127,12 +135,13 @@ def seeded_state(s, w):
     s.u[:], s.v[:] = u, v
 
 
-def sweep_cases(pkg, w, precision):
-    """The seeded cases of a batch workload; draws that violate the geometry checks of
-    MAC_CylinderFlow (cylinder inside the domain, probes inside the grid) are redrawn."""
+def sweep_draws(w, make):
+    """The seeded cases of a batch workload: make(kw) builds one case from the constructor
+    arguments and returns None for draws that violate the geometry checks (cylinder inside
+    the domain, probes inside the grid); those are redrawn.  Yields (case, kw, Re, noise seed)."""
     rng = np.random.default_rng(w['seed'])
-    cases, params = [], []
-    while len(cases) < w['batch']:
+    made = 0
+    while made < w['batch']:
         nx, ny = w['grids'][int(rng.integers(len(w['grids'])))]
         re = rng.uniform(*w['re'])
         d = rng.uniform(*w['diameter'])
@@ -140,17 +149,59 @@ def sweep_cases(pkg, w, precision):
         xc = lx / 4 + rng.uniform(-w['jitter'], w['jitter']) * d
         yc = ly / 2 + rng.uniform(-w['jitter'], w['jitter']) * d
         kw = dict(nx=nx, ny=ny, Lx=lx, Ly=ly, D=d, xc=xc, yc=yc, nu=1.0 * d / re)
-        try:
-            s = pkg.MAC_CylinderFlow(verbose=False, precision=precision, **kw)
-        except ValueError:
+        s = make(kw)
+        if s is None:
             continue
+        made += 1
+        yield s, kw, re, int(rng.integers(2 ** 31))
+
+
+def sweep_cases(pkg, w, precision):
+    """The batch workload's cases as MAC_CylinderFlow objects with their seeded perturbation."""
+    def make(kw):
+        try:
+            return pkg.MAC_CylinderFlow(verbose=False, precision=precision, **kw)
+        except ValueError:
+            return None
+    cases, params = [], []
+    for s, kw, re, seed in sweep_draws(w, make):
         q = s.gg.pack(s.u, s.v)
-        q += w['amp'] * np.random.default_rng(int(rng.integers(2 ** 31))).standard_normal(q.size)
+        q += w['amp'] * np.random.default_rng(seed).standard_normal(q.size)
         u, v = s.gg.unpack(q)
         s.u[:], s.v[:] = u, v
         cases.append(s)
         params.append(dict(kw, Re=re))
     return cases, params
+
+
+def oracle_batch_rate(w, seconds, workers):
+    """Cell-updates/s of the CPU oracle port over a bounded sample of a batch workload: the
+    workload's first cases (same draws and perturbations), one AB2/CN step each after the
+    start-up step, until `seconds` of stepping have run.  Returns (rate, steps, cells, seconds)."""
+    sys.path.insert(0, str(ROOT / 'oracle'))
+    import ghost_oracle as go
+    import scipy.fft
+    def make(kw):
+        try:
+            return go.CylinderCase(**kw)
+        except ValueError:
+            return None
+    cells = steps = 0
+    el = 0.0
+    with scipy.fft.set_workers(workers):
+        for c, kw, _, seed in sweep_draws(w, make):
+            q = c.ops.pack(c.u, c.v)
+            q += w['amp'] * np.random.default_rng(seed).standard_normal(q.size)
+            c.u, c.v = c.ops.unpack(q)
+            c.solve(1, w['dt'])
+            t0 = time.perf_counter()
+            c.solve(1, w['dt'])
+            el += time.perf_counter() - t0
+            cells += kw['nx'] * kw['ny']
+            steps += 1
+            if el >= seconds:
+                break
+    return cells / el, steps, cells, el
 
 
 def oracle_rate(w, steps, seconds, workers):
@@ -182,8 +233,19 @@ def run_reference(args, w, rank):
     if rank != 0:
         return
     workers = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        pass  # the oracle's first step (Helmholtz build) is taken inside oracle_rate
+    if 'batch' in w:
+        rate, done, cells, el = oracle_batch_rate(w, 60.0, workers)
+        line = dict(metric=METRIC, value=rate, unit='cell-updates/s', n_gpus=args.gpus, steps=done,
+                    warmup=args.warmup, ms_per_step=el / max(done, 1) * 1e3, higher_is_better=True, scaling='weak',
+                    vs_baseline=None, dtype='f64', data='synthetic', impl='reference',
+                    config=dict(workload=args.workload, cases=w['batch'], dt=w['dt'], precision='fp64'),
+                    cpu_baseline=dict(value=rate, unit='cell-updates/s', cores=workers, kind='port',
+                                      sample=f'one AB2/CN step (after the start-up step) of each of the first {done} '
+                                             f'cases of {args.workload} ({cells} cells)'),
+                    e2e=dict(value=rate, unit='cell-updates/s', h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+        print(json.dumps(line), flush=True)
+        return
+    # the oracle's first step (Helmholtz build) is the warm-up, taken inside oracle_rate
     rate, done, el = oracle_rate(w, args.steps, 120.0, workers)
     line = dict(metric=METRIC, value=rate, unit='cell-updates/s', n_gpus=args.gpus, steps=done, warmup=args.warmup,
                 ms_per_step=el / max(done, 1) * 1e3, higher_is_better=True, scaling='weak', vs_baseline=None,
@@ -323,10 +385,7 @@ def run_ours(args, w, rank, world):
     bytes_per_launch = by.value / max(cnt.value, 1)
     peak, peak_kind = peaks()
     achieved = by.value / max(tot.value * 1e-3, 1e-12) / 1e9
-    traffic = None
-    tfile = ROOT / 'profiles' / 'traffic.json'
-    if tfile.exists():
-        traffic = json.loads(tfile.read_text()).get(f'{args.workload}:{dominant}')
+    traffic = DRAM_TRAFFIC.get((args.workload, args.precision, dominant))
     # end to end through the public API with host numpy arrays
     e2e_steps = max(1, min(args.steps, 10))
     torch.cuda.synchronize()
@@ -450,6 +509,13 @@ def run_ours_batch(args, w, rank, world):
         batch.solve(1, dt=dt)
     e2e_s = (time.perf_counter() - t_0) / e2e_steps
     state_bytes = sum(8 * (c.ny * (c.nx + 1) + (c.ny + 1) * c.nx + c.nx * c.ny) for c in cases)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        workers = os.cpu_count() or 1
+        rate, done, ncell, el = oracle_batch_rate(w, 20.0, workers)
+        cpu = dict(value=rate, unit='cell-updates/s', cores=workers, kind='port',
+                   sample=f'one AB2/CN step (after the start-up step) of each of the first {done} cases '
+                          f'({ncell} cells, {el:.1f} s)')
     if rank == 0:
         grids = {}
         for c in cases:
@@ -468,7 +534,7 @@ def run_ours_batch(args, w, rank, world):
                                   launches_timed=int(cnt), mean_launch_ms=mean_ms, bytes_per_launch=bytes_per_launch),
                     step_roofline=dict(algorithmic_bytes_per_cell_update=880,
                                        achieved_gbs=880.0 * cells / (step_ms * 1e-3) / 1e9),
-                    cpu_baseline=None,
+                    cpu_baseline=cpu,
                     e2e=dict(value=cells / e2e_s, unit='cell-updates/s', h2d_bytes_per_step=state_bytes,
                              d2h_bytes_per_step=state_bytes + len(cases) * C.sizeof(L.StepDiag)),
                     clocks=clocks.summary(), gpu_launches=int(launches), max_divergence=max(divs),
@@ -482,7 +548,7 @@ def run_ours_batch(args, w, rank, world):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--steps', type=int, default=200)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
     ap.add_argument('--workload', choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS), default=DEFAULT_WORKLOAD)

@@ -719,6 +719,8 @@ void fill_case_dev(gm_handle* h) {
     h->rcoef[2] = residual_coef(g, 2, hc);
   }
   c.D = g.D; c.U_ref = g.U_ref;
+  c.fdx = (float)c.dx; c.fdy = (float)c.dy; c.fidx2 = (float)c.idx2; c.fidy2 = (float)c.idy2;
+  c.fiarea = (float)c.iarea; c.fnu = (float)c.nu; c.fgx = (float)c.gx; c.fgy = (float)c.gy;
 }
 
 void build_class_maps(gm_handle* h) {
@@ -906,7 +908,11 @@ void schur_solve_graph(gm_handle* h, int lane, RectDev& rd, int kind, double hc,
 // on the residual 2-norm <= max(rtol ||b||, atol).  Classical Gram-Schmidt with one
 // re-orthogonalisation; the Hessenberg least-squares update (Givens rotations) runs on the
 // host, one small read-back per iteration.  Returns 0 when converged, else the iteration count.
-int fgmres(gm_handle* h, const double* b, double* x, int& iterations) {
+// With a learned network attached and `learned` set, the first Arnoldi direction of the first
+// cycle (whose residual is b itself, the distribution the network was trained on) is
+// preconditioned by T^-1 + s net; every later direction by T^-1 alone (a flexible
+// preconditioner may change from one direction to the next).
+int fgmres(gm_handle* h, const double* b, double* x, int& iterations, bool learned) {
   const int m = gm_handle::GMRES_M;
   const int64_t n = h->Pn;
   cudaStream_t st = h->st;
@@ -928,13 +934,13 @@ int fgmres(gm_handle* h, const double* b, double* x, int& iterations) {
     CK(cudaMemcpyAsync(out_host, h->gdots.p, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
   };
-  auto precondition = [&](const double* v, double* z) {
+  auto precondition = [&](const double* v, double* z, bool use_net) {
     if (h->precision == 1)
       plain_inverse<float, double, double>(rd.tt32, rd.view, v, true, h->spectral32.p, z, rd.view.cls, nullptr, open,
                                            st);
     else
       plain_inverse<double, double, double>(rd.tt, rd.view, v, true, h->spectral.p, z, rd.view.cls, nullptr, open, st);
-    if (h->lnet) {
+    if (use_net) {
       // z += s net([v / s, mask]), s = max |v|  (FP32 network, FGMRES absorbs its nonlinearity)
       float* xin = nullptr;
       gm_unet_input(h->lnet, &xin);
@@ -970,7 +976,7 @@ int fgmres(gm_handle* h, const double* b, double* x, int& iterations) {
     g[0] = beta;
     int jend = -1;
     for (int j = 0; j < m; ++j) {
-      precondition(vec(V, j), vec(Z, j));
+      precondition(vec(V, j), vec(Z, j), learned && h->lnet && cycle == 0 && j == 0);
       double* w = vec(V, j + 1);
       launch_apply_pressure(h->cd, h->rcoef[0], vec(Z, j), w, open, st);
       // two classical Gram-Schmidt passes against V_0..V_j
@@ -1025,7 +1031,7 @@ void gmres_monitored(gm_handle* h, const double* b, double* x, double* res, int 
   SolveCtl* sc = &h->ctl.p->solve[slot];
   const Gate g0 = gate_of(h);
   int its = 0, total = 0;
-  int status = fgmres(h, b, x, its);
+  int status = fgmres(h, b, x, its, true);
   total += its;
   launch_residual(h->cd, h->rcoef[0], 0, b, x, res, false, sc, 0, true, g0, st);
   auto read = [&](SolveCtl& hs) {
@@ -1038,7 +1044,7 @@ void gmres_monitored(gm_handle* h, const double* b, double* x, double* res, int 
   int k = 0;
   for (int r = 0; r < 2; ++r) {
     if (status || bits2d(hs.rmax[k]) <= target) break;
-    status = fgmres(h, res, h->gdx.p, its);
+    status = fgmres(h, res, h->gdx.p, its, false);
     total += its;
     const double one = 1.0;
     CK(cudaMemcpyAsync(h->gcoef.p, &one, sizeof one, cudaMemcpyHostToDevice, st));

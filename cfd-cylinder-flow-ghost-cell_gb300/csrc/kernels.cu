@@ -57,7 +57,25 @@ __device__ void block_commit_sum(double v, double* dst) {
     if (lane == 0 && v != 0.0) atomicAdd(dst, v);
   }
 }
-__device__ __forceinline__ unsigned long long absbits(double v) { return dbits(fabs(v)); }
+// FP32 variant for diagnostics sums of the FP32 mode (FP64 adds issue at 1/64 of the FP32 rate)
+__device__ void block_commit_sum_f32(float v, double* dst) {
+  __shared__ float smf[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) smf[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    v = lane < nw ? smf[lane] : 0.0f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0 && v != 0.0f) atomicAdd(dst, f32_to_f64i(v));
+  }
+}
+// |v| as bits with the sign bit cleared (integer pipe; fabs on a double may issue on the FP64 pipe)
+__device__ __forceinline__ unsigned long long absbits(double v) { return dbits(v) & 0x7fffffffffffffffull; }
 
 static inline unsigned blocks_for(int64_t n, int tpb = TPB) { return (unsigned)((n + tpb - 1) / tpb); }
 // Grid of the reduction kernels: grid-stride loops over at most 4 blocks per SM of a GB300,
@@ -230,7 +248,7 @@ __global__ void k_xpass(int n, int r0, int nr, int type, FftPlan plan, R2RTables
 #pragma unroll
       for (int u = 0; u < XB; ++u) {
         const int e = e0 + u * gthreads;
-        if (e < n) stage[l * n + e] = ((mk[u] & CLS_ACTIVE) ? (T)v[u] : (T)0) - cv[u];
+        if (e < n) stage[l * n + e] = ((mk[u] & CLS_ACTIVE) ? cvt_to<T>(v[u]) : (T)0) - cv[u];
       }
     }
   }
@@ -258,7 +276,7 @@ __global__ void k_xpass(int n, int r0, int nr, int type, FftPlan plan, R2RTables
           out[fo] = (TO)0;
         } else {
           const T v = stage[l * n + e];
-          out[fo] = add ? (TO)(ad[u] + (double)v) : (TO)v;
+          out[fo] = add ? cvt_to<TO>(ad[u] + cvt_to<double>(v)) : cvt_to<TO>(v);
         }
       }
     }
@@ -566,7 +584,7 @@ __global__ void k_schur(const TF* __restrict__ first, int rank, int m, const int
       if (q0 + u * (int)blockDim.x < m) fv[u] = first[ix[u]];
 #pragma unroll
     for (int u = 0; u < 4; ++u)
-      if (q0 + u * (int)blockDim.x < m) gsh[q0 + u * blockDim.x] = (double)fv[u];
+      if (q0 + u * (int)blockDim.x < m) gsh[q0 + u * blockDim.x] = cvt_to<double>(fv[u]);
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -738,13 +756,16 @@ __global__ void k_momentum(CaseDev c, MomentumArgs a, const S* __restrict__ Us, 
     a.out[t] = a.mode == 1 ? z : 0.0;
     return;
   }
-  const T dx = (T)c.dx, dy = (T)c.dy, idx2 = (T)c.idx2, idy2 = (T)c.idy2;
-  const T iarea = (T)c.iarea, nu = (T)c.nu, dt = (T)a.dt;
+  constexpr bool F32 = sizeof(T) == 4;
+  const T dx = F32 ? (T)c.fdx : (T)c.dx, dy = F32 ? (T)c.fdy : (T)c.dy;
+  const T idx2 = F32 ? (T)c.fidx2 : (T)c.idx2, idy2 = F32 ? (T)c.fidy2 : (T)c.idy2;
+  const T iarea = F32 ? (T)c.fiarea : (T)c.iarea, nu = F32 ? (T)c.fnu : (T)c.nu;
+  const T dt = F32 ? (T)a.dt32 : (T)a.dt;
   const double q = a.U[t];
   T lq, gp, now = 0, off = 0;
   if (comp == 0) {
     lq = nu * lap_u<T>(Us, g, j, i, idx2, idy2, true);
-    gp = grad_u<T>(Ps, g, j, i, (T)c.gx);
+    gp = grad_u<T>(Ps, g, j, i, F32 ? (T)c.fgx : (T)c.gx);
     if (a.mode != 2) {
       now = adv_u<T>(Us, g, j, i, dx, dy) * iarea;
       if (i == c.nx) now *= (T)2;
@@ -752,19 +773,19 @@ __global__ void k_momentum(CaseDev c, MomentumArgs a, const S* __restrict__ Us, 
     if (i == 1) off = nu * (idx2 * (T)c.inlet[j]);
   } else {
     lq = nu * lap_v<T>(Us, g, j, i, idx2, idy2);
-    gp = grad_v<T>(Ps, g, j, i, (T)c.gy);
+    gp = grad_v<T>(Ps, g, j, i, F32 ? (T)c.fgy : (T)c.gy);
     if (a.mode != 2) now = adv_v<T>(Us, g, j, i, dx, dy) * iarea;
   }
   if (a.mode == 1) {
-    a.now[t] = (double)now;
-    a.out[t] = q + (double)(((T)0.5 * dt) * ((now + lq) - gp));
+    a.now[t] = cvt_to<double>(now);
+    a.out[t] = q + cvt_to<double>(((T)0.5 * dt) * ((now + lq) - gp));
     return;
   }
   T expl;
   if (a.mode == 0) {
-    const T alpha = (T)a.alpha;
-    expl = ((T)1 + alpha) * now - alpha * (T)a.prev[t];
-    a.now[t] = (double)now;
+    const T alpha = F32 ? (T)a.alpha32 : (T)a.alpha;
+    expl = ((T)1 + alpha) * now - alpha * cvt_to<T>(a.prev[t]);
+    a.now[t] = cvt_to<double>(now);
   } else {
     if (comp == 0) {
       expl = adv_u<T>(a.Uhalf, g, j, i, dx, dy) * iarea;
@@ -776,16 +797,16 @@ __global__ void k_momentum(CaseDev c, MomentumArgs a, const S* __restrict__ Us, 
   // rhs = q + dt (explicit + L q / 2 - G p) + dt/2 offset (solver/numba_kernels.py:596-601)
   if constexpr (sizeof(T) == 8)
     a.out[t] = (q + (double)(dt * (expl + (T)0.5 * lq - gp))) + (double)(((T)0.5 * dt) * off);
-  else  // one conversion and one FP64 add per face
-    a.out[t] = q + (double)(dt * (expl + (T)0.5 * lq - gp) + ((T)0.5 * dt) * off);
+  else  // one FP64 add per face (the conversion runs on the integer pipe)
+    a.out[t] = q + cvt_to<double>(dt * (expl + (T)0.5 * lq - gp) + ((T)0.5 * dt) * off);
 }
 
 __global__ void k_shadow(const double* __restrict__ U, float* __restrict__ U32, int64_t nf,
                          const double* __restrict__ P, float* __restrict__ P32, int64_t np, Gate gate) {
   if (!gate_open(gate)) return;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nf + np; t += (int64_t)gridDim.x * blockDim.x) {
-    if (t < nf) U32[t] = (float)U[t];
-    else P32[t - nf] = (float)P[t - nf];
+    if (t < nf) U32[t] = f64_to_f32i(U[t]);
+    else P32[t - nf] = f64_to_f32i(P[t - nf]);
   }
 }
 void launch_shadow(const double* U, float* U32, int64_t n_f, const double* P, float* P32, int64_t n_p,
@@ -802,7 +823,10 @@ void launch_momentum(const CaseDev& c, const MomentumArgs& a, const Gate& gate, 
   k_momentum<double, double><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, a.U, a.P, gate);
   kt_mark(3, st);
 }
-void launch_momentum_f32(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st) {
+void launch_momentum_f32(const CaseDev& c, const MomentumArgs& a_in, const Gate& gate, cudaStream_t st) {
+  MomentumArgs a = a_in;
+  a.dt32 = (float)a.dt;
+  a.alpha32 = (float)a.alpha;
   note_launch();
   kt_mark(3, st);
   if (a.mode == 0 && a.U32 && a.P32)
@@ -903,6 +927,7 @@ __global__ void k_residual(CaseDev c, ResidualCoef rc, const double* __restrict_
   float* res32 = reinterpret_cast<float*>(res_out);
   unsigned long long rm = 0, bm = 0, bd = 0, xb = 0;
   double rs = 0.0, bs = 0.0;
+  float rs32 = 0.0f;  // RES_F32: sum of the stored FP32 residuals squared (diagnostics only)
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < npts; t += (int64_t)gridDim.x * blockDim.x) {
     const uint8_t k = cls[t];
     const int64_t f = base + t;
@@ -960,15 +985,22 @@ __global__ void k_residual(CaseDev c, ResidualCoef rc, const double* __restrict_
       }
     }
     const double r = bv - ax;
-    if (RES_F32) res32[f] = (float)r; else res64[f] = r;
     rm = umax64(rm, absbits(r));
-    rs += r * r;
+    if constexpr (RES_F32) {
+      const float r32 = f64_to_f32i(r);
+      res32[f] = r32;
+      rs32 = fmaf(r32, r32, rs32);
+    } else {
+      res64[f] = r;
+      rs += r * r;
+    }
     if (KIND == 0 && !RES_F32) bd = umax64(bd, dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + fabs(bv))));
     if (first) { bm = umax64(bm, absbits(bv)); bs += bv * bv; }
     if ((dbits(xv) & 0x7ff0000000000000ull) == 0x7ff0000000000000ull) xb = 1;  // Inf or NaN, by the bits
   }
   block_commit_max(rm, &sc->rmax[check]);
-  block_commit_sum(rs, &sc->rsq[check]);
+  if constexpr (RES_F32) block_commit_sum_f32(rs32, &sc->rsq[check]);
+  else block_commit_sum(rs, &sc->rsq[check]);
   if (KIND == 0 && !RES_F32) block_commit_max(bd, &sc->bound[check]);
   if (first) {
     block_commit_max(bm, &sc->bmax);

@@ -63,6 +63,48 @@ __host__ __device__ inline double bits2d(unsigned long long b) {
 #endif
 }
 
+// FP64 <-> FP32 conversions on the integer pipe.  GB300 runs cvt.f32.f64 / cvt.f64.f32 on the
+// FP64 pipe (2 per SM per clock), so the FP32 mode moves values between the formats by
+// rebuilding the IEEE-754 fields with integer operations instead.  f64 -> f32 rounds half away
+// from zero at the 24th significant bit (error <= 2^-24 relative, like round-to-nearest), flushes
+// magnitudes below 2^-126 to a signed zero and keeps Inf / NaN; f32 -> f64 is exact for normal
+// numbers and flushes FP32 subnormals to a signed zero.
+template <typename To, typename From>
+__host__ __device__ __forceinline__ To bit_as(From v) {
+  static_assert(sizeof(To) == sizeof(From), "bit_as needs equal sizes");
+  To t;
+  memcpy(&t, &v, sizeof t);
+  return t;
+}
+__host__ __device__ __forceinline__ float f64_to_f32i(double x) {
+  const uint64_t b = bit_as<uint64_t>(x);
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const uint32_t e0 = (uint32_t)(b >> 52) & 0x7ffu;
+  const uint64_t a = (b & 0x7fffffffffffffffull) + (1ull << 28);  // rounding carry may bump the exponent
+  const uint32_t e = (uint32_t)(a >> 52);
+  uint32_t r;
+  if (e0 == 0x7ffu) r = (b & 0xfffffffffffffull) ? 0x7fc00000u : 0x7f800000u;
+  else if (e <= 896u) r = 0u;
+  else if (e >= 1151u) r = 0x7f800000u;
+  else r = ((e - 896u) << 23) | ((uint32_t)(a >> 29) & 0x7fffffu);
+  return bit_as<float>(sign | r);
+}
+__host__ __device__ __forceinline__ double f32_to_f64i(float v) {
+  const uint32_t f = bit_as<uint32_t>(v);
+  const uint32_t s = f & 0x80000000u, e = (f >> 23) & 0xffu, m = f & 0x7fffffu;
+  uint32_t hi = s, lo = 0u;
+  if (e == 255u) { hi = s | 0x7ff00000u | (m >> 3) | (m ? 0x80000u : 0u); lo = m << 29; }
+  else if (e != 0u) { hi = s | ((e + 896u) << 20) | (m >> 3); lo = m << 29; }
+  return bit_as<double>(((uint64_t)hi << 32) | lo);
+}
+// conversions between the arithmetic types of the FP32 / FP64 kernels
+template <typename TO, typename TI>
+__host__ __device__ __forceinline__ TO cvt_to(TI v) {
+  if constexpr (sizeof(TO) == 4 && sizeof(TI) == 8) return f64_to_f32i(v);
+  else if constexpr (sizeof(TO) == 8 && sizeof(TI) == 4) return f32_to_f64i(v);
+  else return (TO)v;
+}
+
 // Target of the inner refinement loop (solver/pressure_schur.py:115).
 __device__ __forceinline__ double inner_target(const SolveCtl* s) {
   double b = bits2d(s->bmax);
@@ -141,6 +183,9 @@ struct CaseDev {
   double* surf_part;        // 4 * n_surf per-point force terms (k_forces scratch)
   unsigned* surf_ticket;    // blocks finished in k_forces (back to 0 after each launch)
   double D, U_ref;
+  // FP32 copies of the stencil scalars for the FP32 kernels (a per-thread conversion would
+  // issue on the FP64 pipe)
+  float fdx, fdy, fidx2, fidy2, fiarea, fnu, fgx, fgy;
 };
 
 // Helmholtz coefficients (per dt)
@@ -271,6 +316,7 @@ struct MomentumArgs {
   const float* U32;       // FP32 copies of U and P for the stencils (FP32 mode, mode 0)
   const float* P32;
   double dt, alpha;
+  float dt32, alpha32;    // FP32 copies (set by the FP32 launcher)
   int mode;
 };
 void launch_momentum(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st);

@@ -4,9 +4,10 @@ The network is the 4-level convolutional U-Net of csrc/unet.cu (BF16 weights, FP
 activations and accumulation, hand-written forward and backward kernels).  It learns the part
 of the pressure solve that the separable rectangle inverse T^-1 misses: for a right-hand side
 b with s = max |b| it maps [b / s, mask] to (A^-1 b - T^-1 b) / s.  Attached to a
-``MAC_CylinderFlow(pressure_solver='iterative')`` case, flexible GMRES uses
-z = T^-1 r + s net([r / s, mask]); GMRES still iterates to the reference's true-residual
-tolerance, so the network only changes the iteration count.
+``MAC_CylinderFlow(pressure_solver='iterative')`` case, flexible GMRES preconditions its first
+direction (the right-hand side itself, the distribution the network was trained on) with
+z = T^-1 b + s net([b / s, mask]) and every later direction with T^-1; GMRES still iterates to
+the reference's true-residual tolerance, so the network only changes the iteration count.
 
 Training pairs are the solver's own pressure solves (``record_pressure_pairs``).  Training
 runs on the GPU through ``UNetFunction`` (a ``torch.autograd.Function`` over the library's

@@ -45,26 +45,22 @@ def test_learned_preconditioner_saves_gmres_iterations():
     kw = dict(nx=96, ny=48, Lx=9.6, Ly=4.8, D=1.0, xc=2.4, yc=2.4, nu=0.01, verbose=False,
               pressure_solver='iterative')
     s = pkg.MAC_CylinderFlow(**kw)
-    rhs, sol = learned.record_pressure_pairs(s, 30, 0.002)
-    assert rhs.shape[0] >= 40
-    x, y, mask = learned.training_set(s, rhs, sol)
+    rhs, sol = learned.record_pressure_pairs(s, 40, 0.002)
+    assert rhs.shape[0] >= 60
+    # train on the earlier solves, hold out the last four
+    x, y, mask = learned.training_set(s, rhs[:-4], sol[:-4])
     wts = learned.UNetWeights(seed=1)
-    hist = learned.train(wts, x, y, mask, epochs=300, lr=2e-3, batch=4)
+    hist = learned.train(wts, x, y, mask, epochs=600, lr=2e-3, batch=4)
     assert hist[-1] < 0.5 * hist[0]
-    # held-out solves: continue the run with and without the network from the same state
-    base = pkg.MAC_CylinderFlow(**kw)
-    base.solve(n_steps=30, dt=0.002, perturb_transient=False, save_artifacts=False, verbose=False)
     its_plain, its_learned = [], []
-    rng = np.random.default_rng(11)
-    q = base.gg.pack(base.u, base.v)
-    for k in range(4):
-        qk = q + 1e-2 * rng.standard_normal(q.size)
-        b = base.gg.divergence(qk) / 0.002
-        x0 = base.gg.pressure_solve(b)
-        its_plain.append(base.gg.pressure_inverse_info['last_solve']['iterations'])
-        pc = learned.LearnedPreconditioner(base, wts)
-        x1 = base.gg.pressure_solve(b)
-        its_learned.append(base.gg.pressure_inverse_info['last_solve']['iterations'])
+    for b in rhs[-4:].cpu().numpy():
+        b = b.reshape(-1)[s.gg.pi]
+        x0 = s.gg.pressure_solve(b)
+        its_plain.append(s.gg.pressure_inverse_info['last_solve']['iterations'])
+        pc = learned.LearnedPreconditioner(s, wts)
+        x1 = s.gg.pressure_solve(b)
+        its_learned.append(s.gg.pressure_inverse_info['last_solve']['iterations'])
         pc.detach()
+        # GMRES iterates to the same true-residual tolerance with either preconditioner
         assert np.max(np.abs(x1 - x0)) < 1e-8 * max(1.0, np.max(np.abs(x0)))
     assert sum(its_learned) < sum(its_plain), (its_plain, its_learned)
