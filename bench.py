@@ -60,7 +60,7 @@ DRAM_TRAFFIC = {
 }
 KERNEL_CLASSES = {1: 'row transforms (k_xpass)', 2: 'column solves (k_ysolve, k_yband)',
                   3: 'momentum rhs (k_momentum, k_shadow)', 4: 'operator residual (k_residual, k_pressure_bound)',
-                  5: 'Schur GEMV (k_schur)', 6: 'projection (k_divergence, k_project_update, k_set_inlet)',
+                  5: 'boundary chain (k_band_chain; k_schur when unfused)', 6: 'projection (k_divergence, k_project_update, k_set_inlet)',
                   7: 'defect / pressure output (k_defect, k_pressure_out)', 8: 'ghost rows (k_ghost)',
                   9: 'forces / maxima (k_forces, k_maxabs)', 10: 'gates and loop control'}
 
@@ -323,10 +323,11 @@ def run_ours(args, w, rank, world):
             L.lib.gm_phase_timing(s._h, out)
             phases.append(list(out))
     os.environ.pop('GHOSTMAC_PHASE_TIMING', None)
+    # p1_sweep0_band_1..4: the boundary chain (row inverse of the C rows, Schur GEMV, band row
+    # forward, band solve); with the fused chain kernel band_1 holds all four and 2..4 are empty
     phase_names = ['momentum', 'helmholtz_uv', 'projection_1', 'defect', 'projection_2', 'pressure_forces_gates',
-                   'p1_sweep0_row_pass', 'p1_sweep0_column_solve', 'p1_sweep0_band_row_inverse', 'p1_sweep0_schur',
-                   'p1_sweep0_band_row_forward', 'p1_sweep0_band_solve', 'p1_sweep0_final_row_pass',
-                   'p1_sweep0_residual']
+                   'p1_sweep0_row_pass', 'p1_sweep0_column_solve', 'p1_sweep0_band_1', 'p1_sweep0_band_2',
+                   'p1_sweep0_band_3', 'p1_sweep0_band_4', 'p1_sweep0_final_row_pass', 'p1_sweep0_residual']
     phase_ms = {n: float(np.mean([p[i] for p in phases])) for i, n in enumerate(phase_names)}
     # dominant kernel class: per-class CUDA-event time of one launch-by-launch step with the
     # refinement sweeps decided on the host (every launched kernel does work; this NVTX range

@@ -117,6 +117,14 @@ struct RectDev {
   // band solve of the Schur term (pivots, decay factors, band work array)
   DBuf<double> bpiv, phi, psi, band;
   DBuf<float> bpiv32, phi32, psi32, band32;
+  // direct sums of the boundary term (build_direct_tables): the inverse row transform at the
+  // mcount points (spectrum row of each, coefficients mcount x cols), the forward row transform
+  // of a unit value at each boundary row (band-row order: bptr over band rows, bperm to the
+  // rank index), the Schur values c and the transformed values at the points
+  bool direct = false;
+  DBuf<int32_t> mrow, bptr, bperm;
+  DBuf<double> binv, bfwd, cvec, firstm;
+  DBuf<float> binv32, bfwd32, firstm32;
 };
 
 }  // namespace
@@ -435,6 +443,21 @@ void autotune_shapes(gm_handle* h, RectDev& rd, int kind, bool fp32) {
   CK(cudaEventDestroy(e0));
   CK(cudaEventDestroy(e1));
   CK(cudaGetLastError());
+  // GHOSTMAC_SHAPES="gthreads,gpb,L" replaces the timed choice (shape studies; every shape
+  // computes the same values)
+  if (const char* e = std::getenv("GHOSTMAC_SHAPES")) {
+    int gt = 0, gp = 0, L = 0;
+    if (std::sscanf(e, "%d,%d,%d", &gt, &gp, &L) == 3 && gt >= 32 && gt % 32 == 0 && gp >= 1 && gt * gp <= 512 &&
+        tabs + per * gp <= h->smem_optin && (L == 2 || L == 4 || L == 8 || L == 16) &&
+        ((L * tt.ych.P + 31) / 32) * 32 <= 1024 && ysolve_smem(v.rows, L, fp32) <= h->smem_optin) {
+      tt.xg_threads = gt;
+      tt.xg_pb = gp;
+      tt.smem_x = tabs + per * gp;
+      tt.lpb_y = L;
+      tt.threads_y = ((L * tt.ych.P + 31) / 32) * 32;
+      tt.smem_y = ysolve_smem(v.rows, L, fp32);
+    }
+  }
 }
 
 // x transform tables and y partition tables of a rectangle kind
@@ -584,6 +607,79 @@ void build_band_tables(gm_handle* h, RectDev& rd, const std::vector<int64_t>& ro
   CK(cudaStreamSynchronize(st));
 }
 
+// Tables of the boundary term by direct sums.  The row transforms are taken as explicit
+// cols x cols matrices by running the row-transform kernel on the rows of the identity (so the
+// direct sums use exactly the transforms of the FFT path), then
+//   binv (mcount x cols): row q holds the inverse-transform coefficients of the point q;
+//   bfwd (rank x cols, band-row order): the forward transform of a unit value at a boundary row.
+// Per solve the boundary chain then costs a dot product per point, the GEMV with M and one
+// sum per band entry, instead of row transforms of the C rows and of the band rows.  Grids
+// whose tables would exceed 64 MB keep the row-transform chain.
+void build_direct_tables(gm_handle* h, RectDev& rd, const std::vector<int64_t>& rows,
+                         const std::vector<int64_t>& ucol) {
+  rd.direct = false;
+  const int n = rd.view.cols, m = rd.mcount, rank = rd.rank;
+  const TransformTables& tt = rd.tt;
+  if (rank <= 0 || m <= 0 || tt.bj1 < tt.bj0) return;
+  const char* e = std::getenv("GHOSTMAC_BAND_TRANSFORMS");
+  if (e && e[0] == '1') return;
+  if ((size_t)(m + rank) * n * 8 > ((size_t)64 << 20) ||
+      band_fwd_smem(tt.bj1 - tt.bj0 + 1, rank, false) > 48 * 1024)
+    return;
+  cudaStream_t st = h->st;
+  const Gate open{nullptr, 0, 0};
+  const YCorr<double> none{nullptr, nullptr, nullptr, 0, -1};
+  std::vector<double> eye((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) eye[(size_t)i * n + i] = 1.0;
+  DBuf<double> deye, dinv, dfwd;
+  deye.upload(eye, st);
+  dinv.alloc((size_t)n * n);
+  dfwd.alloc((size_t)n * n);
+  launch_xpass<double, double, double>(tt, true, 0, n, deye.p, 0, n, nullptr, dinv.p, 0, n, nullptr, nullptr, none,
+                                       open, st);
+  launch_xpass<double, double, double>(tt, false, 0, n, deye.p, 0, n, nullptr, dfwd.p, 0, n, nullptr, nullptr, none,
+                                       open, st);
+  std::vector<double> tinv((size_t)n * n), tfwd((size_t)n * n);
+  CK(cudaMemcpyAsync(tinv.data(), dinv.p, tinv.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(tfwd.data(), dfwd.p, tfwd.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  // row k of tinv is the inverse transform of e_k: value at column i = tinv[k][i]
+  std::vector<int32_t> mrow(m);
+  std::vector<double> binv((size_t)m * n);
+  for (int q = 0; q < m; ++q) {
+    const int r = (int)(ucol[q] / n), i = (int)(ucol[q] % n);
+    mrow[q] = r;
+    for (int k = 0; k < n; ++k) binv[(size_t)q * n + k] = tinv[(size_t)k * n + i];
+  }
+  // boundary rows grouped by band row; row i of tfwd is the forward transform of e_i
+  const int nb = tt.bj1 - tt.bj0 + 1;
+  std::vector<int32_t> perm(rank), ptr(nb + 1, 0);
+  for (int r = 0; r < rank; ++r) perm[r] = r;
+  std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return rows[a] / n < rows[b] / n; });
+  std::vector<double> bfwd((size_t)rank * n);
+  for (int e2 = 0; e2 < rank; ++e2) {
+    const int r = perm[e2];
+    const int j = (int)(rows[r] / n) - tt.bj0, i = (int)(rows[r] % n);
+    ++ptr[j + 1];
+    for (int k = 0; k < n; ++k) bfwd[(size_t)e2 * n + k] = tfwd[(size_t)i * n + k];
+  }
+  for (int j = 0; j < nb; ++j) ptr[j + 1] += ptr[j];
+  rd.mrow.upload(mrow, st);
+  rd.bptr.upload(ptr, st);
+  rd.bperm.upload(perm, st);
+  rd.binv.upload(binv, st);
+  rd.bfwd.upload(bfwd, st);
+  rd.cvec.alloc(rank);
+  rd.firstm.alloc(m);
+  if (h->precision == 1) {
+    rd.binv32.upload(to_f32(binv), st);
+    rd.bfwd32.upload(to_f32(bfwd), st);
+    rd.firstm32.alloc(m);
+  }
+  CK(cudaStreamSynchronize(st));
+  rd.direct = true;
+}
+
 // Schur matrix S = I + C T^{-1} U by impulse solves, LU, explicit inverse (solver/pressure_schur.py:92-101)
 void build_schur(gm_handle* h, RectDev& rd, const std::vector<int64_t>& rows, const gm::Csr& C, double* field_buf) {
   cudaStream_t st = h->st;
@@ -653,6 +749,7 @@ void build_schur(gm_handle* h, RectDev& rd, const std::vector<int64_t>& rows, co
   rd.mmat.upload(M, st);
   rd.mcount = m;
   build_band_tables(h, rd, rows, C);
+  build_direct_tables(h, rd, rows, ucol);
 }
 
 // Regular-row coefficients of the residual kernels (see ResidualCoef): the pressure operator
@@ -824,7 +921,19 @@ void schur_inverse(gm_handle* h, RectDev& rd, const TransformTables& tt, const v
   launch_ysolve<T>(tt, v.cols, v.rows, spectral, g, st);
   sweep_mark(h, 2, st);
   YCorr<T> corr = none;
-  if (rd.rank > 0) {
+  if (rd.rank > 0 && rd.direct) {
+    const bool f32 = sizeof(T) == 4;
+    T* fm = f32 ? (T*)rd.firstm32.p : (T*)rd.firstm.p;
+    launch_band_first<T>(rd.mcount, v.cols, rd.mrow.p, f32 ? (const T*)rd.binv32.p : (const T*)rd.binv.p, spectral, fm,
+                         g, st);
+    sweep_mark(h, 3, st);
+    launch_band_gemv<T>(rd.rank, rd.mcount, rd.mmat.p, fm, rd.cvec.p, g, st);
+    sweep_mark(h, 4, st);
+    launch_band_fwd_solve<T>(tt, v.cols, rd.rank, rd.bptr.p, rd.bperm.p, rd.cvec.p,
+                             f32 ? (const T*)rd.bfwd32.p : (const T*)rd.bfwd.p, band, g, st);
+    sweep_mark(h, 5, st);
+    corr = YCorr<T>{band, (const T*)tt.phi, (const T*)tt.psi, tt.bj0, tt.bj1};
+  } else if (rd.rank > 0) {
     launch_xpass<T, T, T>(tt, true, tt.cj0, tt.cj1 - tt.cj0 + 1, spectral, 0, v.cols, nullptr, first, v.base, v.pitch,
                           nullptr, nullptr, none, g, st);
     sweep_mark(h, 3, st);

@@ -96,7 +96,7 @@ void kernel_launch_adjust(long long delta) { g_launches.fetch_add(delta, std::me
 
 // Optional CUDA-event timing of every launch, summed per kernel class (used by the
 // benchmark for its per-class breakdown and the dominant kernel's launch time).  Classes:
-// 1 x pass, 2 column solves, 3 momentum, 4 residual, 5 Schur GEMV, 6 projection pieces,
+// 1 x pass, 2 column solves, 3 momentum, 4 residual, 5 boundary chain / Schur GEMV, 6 projection pieces,
 // 7 defect / pressure output, 8 ghost rows, 9 forces / maxima, 10 gates and loop control.
 namespace {
 struct KTimer {
@@ -188,26 +188,35 @@ size_t xpass_smem_tables(int type, int n, int plan_tw, bool fp32) {
 }
 
 static constexpr int XB = 4;  // loads batched per thread in the row passes
-template <typename T, typename TI, typename TO>
-__global__ void k_xpass(int n, int r0, int nr, int type, FftPlan plan, R2RTables<T> tb, const TI* __restrict__ in,
-                        int64_t ibase, int64_t ipitch, const uint8_t* __restrict__ icls, TO* __restrict__ out,
-                        int64_t obase, int64_t opitch, const uint8_t* __restrict__ ocls, const double* __restrict__ add,
-                        YCorr<T> corr, int gthreads, int gpb, Gate gate) {
-  if (!gate_open(gate)) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  // the twiddle tables go to shared memory first (read by every stage of every group: a
-  // global load per stage would put an L2 round trip on each stage's critical path)
+// Twiddle tables of one transform type staged into the block's shared memory (read by every
+// stage of every group: a global load per stage would put an L2 round trip on each stage's
+// critical path).  Called by all threads of the block; ends with a block barrier.
+template <typename T>
+__device__ __forceinline__ R2RTables<T> xpass_stage_tables(int type, int n, const FftPlan& plan,
+                                                           const R2RTables<T>& tb, unsigned char* smem_raw) {
   const int ntw[3] = {xpass_tw_len(type, n, 0, plan.tw_len), xpass_tw_len(type, n, 1, plan.tw_len),
                       xpass_tw_len(type, n, 2, plan.tw_len)};
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
   for (int q = threadIdx.x; q < ntw[0] + ntw[1] + ntw[2]; q += blockDim.x)
     tw[q] = q < ntw[0] ? tb.W[q] : (q < ntw[0] + ntw[1] ? tb.pre[q - ntw[0]] : tb.post[q - ntw[0] - ntw[1]]);
   __syncthreads();
-  const R2RTables<T> ts{tw, tw + ntw[0], tw + ntw[0] + ntw[1]};
+  return R2RTables<T>{tw, tw + ntw[0], tw + ntw[0] + ntw[1]};
+}
+
+// The line groups of (virtual) block bi: group grp of the block transforms lines
+// (bi * gpb + grp) * lpw ... of rows r0 .. r0+nr-1.  Groups past the end return at once; every
+// group synchronises on its own named barrier only, so a block may run this for several bi in turn.
+template <typename T, typename TI, typename TO>
+__device__ __forceinline__ void xpass_block(int bi, int n, int r0, int nr, int type, const FftPlan& plan,
+                                            const R2RTables<T>& ts, const TI* __restrict__ in, int64_t ibase,
+                                            int64_t ipitch, const uint8_t* __restrict__ icls, TO* __restrict__ out,
+                                            int64_t obase, int64_t opitch, const uint8_t* __restrict__ ocls,
+                                            const double* __restrict__ add, const YCorr<T>& corr, int gthreads,
+                                            int gpb, unsigned char* smem_raw) {
   const int grp = threadIdx.x / gthreads, tid = threadIdx.x - grp * gthreads;
   const int lpw = r2r_paired(type) ? 2 : 1;
-  const int l0 = (blockIdx.x * gpb + grp) * lpw;
-  if (grp >= gpb || l0 >= nr) return;  // whole groups leave; every group has its own barrier
+  const int l0 = (bi * gpb + grp) * lpw;
+  if (grp >= gpb || l0 >= nr) return;
   const int nl = min(lpw, nr - l0);
   unsigned char* mine = smem_raw + xpass_tw_bytes<T>(type, n, plan.tw_len) + (size_t)grp * xpass_group_smem<T>(type, n);
   T* stage = reinterpret_cast<T*>(mine);
@@ -284,6 +293,18 @@ __global__ void k_xpass(int n, int r0, int nr, int type, FftPlan plan, R2RTables
 }
 
 template <typename T, typename TI, typename TO>
+__global__ void k_xpass(int n, int r0, int nr, int type, FftPlan plan, R2RTables<T> tb, const TI* __restrict__ in,
+                        int64_t ibase, int64_t ipitch, const uint8_t* __restrict__ icls, TO* __restrict__ out,
+                        int64_t obase, int64_t opitch, const uint8_t* __restrict__ ocls, const double* __restrict__ add,
+                        YCorr<T> corr, int gthreads, int gpb, Gate gate) {
+  if (!gate_open(gate)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const R2RTables<T> ts = xpass_stage_tables<T>(type, n, plan, tb, smem_raw);
+  xpass_block<T, TI, TO>(blockIdx.x, n, r0, nr, type, plan, ts, in, ibase, ipitch, icls, out, obase, opitch, ocls,
+                         add, corr, gthreads, gpb, smem_raw);
+}
+
+template <typename T, typename TI, typename TO>
 void launch_xpass(const TransformTables& tt, bool inverse, int r0, int nr, const TI* in, int64_t ibase,
                   int64_t ipitch, const uint8_t* icls, TO* out, int64_t obase, int64_t opitch, const uint8_t* ocls,
                   const double* add, const YCorr<T>& corr, const Gate& gate, cudaStream_t st) {
@@ -341,41 +362,43 @@ __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale,
   const int ns = n | 1;                                  // odd stride between the columns
   T* col = reinterpret_cast<T*>(smem_raw);              // L x ns values
   T* piv = col + (size_t)L * ns;                         // L x ns reciprocal pivots
-  T* isub = piv + (size_t)L * ns;                        // L x YCHUNK_MAX interface coefficients
-  T* isup = isub + (size_t)L * YCHUNK_MAX;
+  T* sl = piv + (size_t)L * ns;                          // L x ns left spikes (t1)
+  T* sr = sl + (size_t)L * ns;                           // L x ns right spikes (t2)
   const int c0 = blockIdx.x * L;
   const int P = ch.P;
   const int l = threadIdx.x & (L - 1);                   // column of this thread
   const int rsub = threadIdx.x / L;                      // row offset (load/store), chunk (solve)
   const int rstep = blockDim.x / L;
   const bool colok = c0 + l < cols;
-  const T* s_in = S + c0 + l;
-  const T* p_in = t0 + c0 + l;
-  // load: 8 rows in flight per thread
-  for (int e0 = rsub; e0 < n; e0 += 8 * rstep) {
-    T sv[8], pvv[8];
+  const int64_t cc = c0 + l;
+  // load the column values and all three tables in one phase: 4 x 4 loads in flight per thread,
+  // so the solve phases below wait on shared memory only
+  for (int e0 = rsub; e0 < n; e0 += 4 * rstep) {
+    T sv[4], pvv[4], v1[4], v2[4];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
+    for (int u = 0; u < 4; ++u) {
       const int e = e0 + u * rstep;
       if (colok && e < n) {
-        sv[u] = s_in[(int64_t)e * cols];
-        pvv[u] = p_in[(int64_t)e * cols];
+        const int64_t o = (int64_t)e * cols + cc;
+        sv[u] = S[o];
+        pvv[u] = t0[o];
+        if (P > 1) {
+          v1[u] = t1[o];
+          v2[u] = t2[o];
+        }
       }
     }
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
+    for (int u = 0; u < 4; ++u) {
       const int e = e0 + u * rstep;
       if (colok && e < n) {
         col[l * ns + e] = sv[u] * scale;
         piv[l * ns + e] = pvv[u];
+        if (P > 1) {
+          sl[l * ns + e] = v1[u];
+          sr[l * ns + e] = v2[u];
+        }
       }
-    }
-  }
-  for (int q = rsub; q < P - 1; q += rstep) {
-    if (colok) {
-      const int64_t o = (int64_t)(ch.end[q] + 1) * cols + c0 + l;
-      isub[l * YCHUNK_MAX + q] = t1[o];
-      isup[l * YCHUNK_MAX + q] = t2[o];
     }
   }
   __syncthreads();
@@ -385,7 +408,8 @@ __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale,
   if (work) { a = ch.start[p]; b = ch.end[p]; }
   T* x = col + l * ns;
   const T* pv = piv + l * ns;
-  const int64_t cc = c0 + l;
+  const T* s1 = sl + l * ns;
+  const T* s2 = sr + l * ns;
   // phase 1: chunk-local Thomas
   if (work) {
     T prev = 0;
@@ -400,52 +424,38 @@ __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale,
     }
   }
   __syncthreads();
-  // phase 2: interface system, one thread per column
+  // phase 2: interface system, one thread per column (its coefficients are the spike tables at
+  // the interface rows)
   if (p == 0 && colok && P > 1) {
-    const T* su = isub + l * YCHUNK_MAX;
-    const T* sp = isup + l * YCHUNK_MAX;
     T z = 0;
     for (int q = 0; q < P - 1; ++q) {
       const int e = ch.end[q] + 1;
       const T rhs = x[e] - gamma * x[e - 1] - gamma * x[e + 1];
-      z = (rhs - su[q] * z) * pv[e];
+      z = (rhs - s1[e] * z) * pv[e];
       x[e] = z;
     }
     T y = 0;
     for (int q = P - 2; q >= 0; --q) {
       const int e = ch.end[q] + 1;
-      y = x[e] - sp[q] * y;
+      y = x[e] - s2[e] * y;
       x[e] = y;
     }
   }
   __syncthreads();
-  // phase 3: spike corrections of the inner rows (8 table rows in flight)
+  // phase 3: spike corrections of the inner rows
   if (work && P > 1) {
     const T yl = p > 0 ? x[ch.end[p - 1] + 1] : (T)0;
     const T yr = p < P - 1 ? x[b + 1] : (T)0;
-    for (int j0 = a; j0 <= b; j0 += 8) {
-      T v1[8], v2[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        if (j0 + u <= b) {
-          const int64_t o = (int64_t)(j0 + u) * cols + cc;
-          v1[u] = t1[o];
-          v2[u] = t2[o];
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u)
-        if (j0 + u <= b) x[j0 + u] = x[j0 + u] - yl * v1[u] - yr * v2[u];
-    }
+    for (int j = a; j <= b; ++j) x[j] = x[j] - yl * s1[j] - yr * s2[j];
   }
   __syncthreads();
-  T* s_out = S + c0 + l;
+  T* s_out = S + cc;
   if (colok)
     for (int e = rsub; e < n; e += rstep) s_out[(int64_t)e * cols] = col[l * ns + e];
 }
 size_t ysolve_smem(int rows, int lpb, bool fp32) {
   const size_t esz = fp32 ? 4 : 8;
-  return ((size_t)lpb * (rows | 1) * 2 + (size_t)lpb * YCHUNK_MAX * 2) * esz;
+  return (size_t)lpb * (rows | 1) * 4 * esz;  // values, pivots, left and right spikes
 }
 
 template <typename T>
@@ -615,6 +625,213 @@ template void launch_schur<float>(const float*, int, int, const int64_t*, const 
                                   const Gate&, cudaStream_t);
 
 // ---------------------------------------------------------------------------
+// boundary term by direct sums
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of one value per thread (blockDim a multiple of 32, at most 1024); the total
+// is returned to every thread.
+template <typename T>
+__device__ __forceinline__ T block_sum_all(T v) {
+  __shared__ T part[32];
+  v = warp_sum_t<T>(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane == 0) part[wid] = v;
+  __syncthreads();
+  T t = 0;
+  for (int w = 0; w < nw; ++w) t += part[w];
+  return t;
+}
+
+static constexpr int BAND_TPB = 128;   // threads per output of the direct sums
+static constexpr int BAND_ITEMS = 16;  // loads in flight per thread (n <= BAND_TPB * BAND_ITEMS per pass)
+
+// One block per point: the inverse row transform of its spectrum row evaluated at its column
+// (coefficients in binv), all of a thread's products loaded before they are summed.
+template <typename T>
+__global__ void __launch_bounds__(BAND_TPB) k_band_first(int m, int n, const int32_t* __restrict__ mrow,
+                                                         const T* __restrict__ binv, const T* __restrict__ spec,
+                                                         T* __restrict__ firstm, Gate gate) {
+  if (!gate_open(gate)) return;
+  const int q = blockIdx.x;
+  const T* b = binv + (int64_t)q * n;
+  const T* sp = spec + (int64_t)mrow[q] * n;
+  T acc = 0;
+  for (int k0 = threadIdx.x; k0 < n; k0 += BAND_TPB * BAND_ITEMS) {
+    T bv[BAND_ITEMS], sv[BAND_ITEMS];
+#pragma unroll
+    for (int u = 0; u < BAND_ITEMS; ++u) {
+      const int k = k0 + u * BAND_TPB;
+      bv[u] = k < n ? b[k] : (T)0;
+      sv[u] = k < n ? sp[k] : (T)0;
+    }
+#pragma unroll
+    for (int u = 0; u < BAND_ITEMS; ++u) acc += bv[u] * sv[u];
+  }
+  const T v = block_sum_all<T>(acc);
+  if (threadIdx.x == 0) firstm[q] = v;
+}
+
+// One block per row of M: c[r] = M[r] . firstm (FP64 accumulation).
+template <typename T>
+__global__ void __launch_bounds__(BAND_TPB) k_band_gemv(int rank, int m, const double* __restrict__ M,
+                                                        const T* __restrict__ firstm, double* __restrict__ c,
+                                                        Gate gate) {
+  if (!gate_open(gate)) return;
+  const int r = blockIdx.x;
+  const double* mr = M + (int64_t)r * m;
+  double acc = 0.0;
+  for (int q0 = threadIdx.x; q0 < m; q0 += BAND_TPB * BAND_ITEMS) {
+    double mv[BAND_ITEMS];
+    T fv[BAND_ITEMS];
+#pragma unroll
+    for (int u = 0; u < BAND_ITEMS; ++u) {
+      const int q = q0 + u * BAND_TPB;
+      mv[u] = q < m ? mr[q] : 0.0;
+      fv[u] = q < m ? firstm[q] : (T)0;
+    }
+#pragma unroll
+    for (int u = 0; u < BAND_ITEMS; ++u) acc += mv[u] * cvt_to<double>(fv[u]);
+  }
+  const double v = block_sum_all<double>(acc);
+  if (threadIdx.x == 0) c[r] = v;
+}
+
+// Blocks of BAND_COLS columns x BAND_ROWT row threads.  Thread (kk, jt) forms the forward
+// row transform of U c on band rows jt, jt + BAND_ROWT, ... of column k (a sum over that row's
+// boundary values, c staged in shared memory), scaled; then one thread per column runs the band
+// system (as k_yband) in shared memory, and all threads write the band back.
+static constexpr int BAND_COLS = 32, BAND_ROWT = 8;
+template <typename T>
+__global__ void __launch_bounds__(BAND_COLS * BAND_ROWT) k_band_fwd_solve(
+    int nb, int n, int rank, const int32_t* __restrict__ bptr, const int32_t* __restrict__ bperm,
+    const double* __restrict__ c, const T* __restrict__ bfwd, T gamma, T scale, const T* __restrict__ bpiv,
+    T* __restrict__ band, Gate gate) {
+  if (!gate_open(gate)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* cs = reinterpret_cast<T*>(smem_raw);   // rank values c, band-row order
+  T* xb = cs + ((rank + 3) & ~3);           // nb x BAND_COLS
+  T* pb = xb + (size_t)nb * BAND_COLS;      // nb x BAND_COLS
+  int* ps = reinterpret_cast<int*>(pb + (size_t)nb * BAND_COLS);  // nb + 1 row pointers
+  const int tid = threadIdx.x, kk = tid % BAND_COLS, jt = tid / BAND_COLS;
+  for (int e = tid; e < rank; e += blockDim.x) cs[e] = cvt_to<T>(c[bperm[e]]);
+  for (int j = tid; j <= nb; j += blockDim.x) ps[j] = bptr[j];
+  __syncthreads();
+  const int k = blockIdx.x * BAND_COLS + kk;
+  if (k < n) {
+    for (int j = jt; j < nb; j += BAND_ROWT) {
+      const int e0 = ps[j], e1 = ps[j + 1];
+      T z = 0;
+      for (int e = e0; e < e1; e += 8) {
+        T bv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) bv[u] = e + u < e1 ? bfwd[(int64_t)(e + u) * n + k] : (T)0;
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (e + u < e1) z += cs[e + u] * bv[u];
+      }
+      xb[j * BAND_COLS + kk] = z * scale;
+      pb[j * BAND_COLS + kk] = bpiv[(int64_t)j * n + k];
+    }
+  }
+  __syncthreads();
+  if (jt == 0 && k < n) {
+    T z = 0;
+    for (int j = 0; j < nb; ++j) {
+      z = (xb[j * BAND_COLS + kk] - gamma * z) * pb[j * BAND_COLS + kk];
+      xb[j * BAND_COLS + kk] = z;
+    }
+    T y = z;
+    for (int j = nb - 2; j >= 0; --j) {
+      y = xb[j * BAND_COLS + kk] - (gamma * pb[j * BAND_COLS + kk]) * y;
+      xb[j * BAND_COLS + kk] = y;
+    }
+  }
+  __syncthreads();
+  if (k < n)
+    for (int j = jt; j < nb; j += BAND_ROWT) band[(int64_t)j * n + k] = xb[j * BAND_COLS + kk];
+}
+
+size_t band_fwd_smem(int nb, int rank, bool fp32) {
+  const size_t esz = fp32 ? 4 : 8;
+  return (size_t)((rank + 3) & ~3) * esz + (size_t)2 * nb * BAND_COLS * esz + (size_t)(nb + 1) * sizeof(int);
+}
+
+template <typename T>
+void launch_band_first(int m, int n, const int32_t* mrow, const T* binv, const T* spec, T* firstm, const Gate& gate,
+                       cudaStream_t st) {
+  if (m <= 0) return;
+  note_launch();
+  kt_mark(5, st);
+  k_band_first<T><<<(unsigned)m, BAND_TPB, 0, st>>>(m, n, mrow, binv, spec, firstm, gate);
+  kt_mark(5, st, (double)m * n * 2 * sizeof(T));
+}
+template <typename T>
+void launch_band_gemv(int rank, int m, const double* M, const T* firstm, double* c, const Gate& gate,
+                      cudaStream_t st) {
+  if (rank <= 0) return;
+  note_launch();
+  kt_mark(5, st);
+  k_band_gemv<T><<<(unsigned)rank, BAND_TPB, 0, st>>>(rank, m, M, firstm, c, gate);
+  kt_mark(5, st, (double)rank * m * 8 + (double)m * sizeof(T) + rank * 8.0);
+}
+template <typename T>
+void launch_band_fwd_solve(const TransformTables& tt, int n, int rank, const int32_t* bptr, const int32_t* bperm,
+                           const double* c, const T* bfwd, T* band, const Gate& gate, cudaStream_t st) {
+  const int nb = tt.bj1 - tt.bj0 + 1;
+  if (nb <= 0) return;
+  note_launch();
+  kt_mark(5, st);
+  k_band_fwd_solve<T><<<(unsigned)((n + BAND_COLS - 1) / BAND_COLS), BAND_COLS * BAND_ROWT,
+                        band_fwd_smem(nb, rank, sizeof(T) == 4), st>>>(nb, n, rank, bptr, bperm, c, bfwd, (T)tt.gamma,
+                                                                       (T)tt.yscale, (const T*)tt.bpiv, band, gate);
+  // the forward coefficients, the values c, the pivots and the band written once
+  kt_mark(5, st, (double)rank * n * sizeof(T) + rank * 8.0 + (double)nb * n * 2 * sizeof(T));
+}
+template void launch_band_first<double>(int, int, const int32_t*, const double*, const double*, double*, const Gate&,
+                                        cudaStream_t);
+template void launch_band_first<float>(int, int, const int32_t*, const float*, const float*, float*, const Gate&,
+                                       cudaStream_t);
+template void launch_band_gemv<double>(int, int, const double*, const double*, double*, const Gate&, cudaStream_t);
+template void launch_band_gemv<float>(int, int, const double*, const float*, double*, const Gate&, cudaStream_t);
+template void launch_band_fwd_solve<double>(const TransformTables&, int, int, const int32_t*, const int32_t*,
+                                            const double*, const double*, double*, const Gate&, cudaStream_t);
+template void launch_band_fwd_solve<float>(const TransformTables&, int, int, const int32_t*, const int32_t*,
+                                           const double*, const float*, float*, const Gate&, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// sparse rows with their loads batched: the column indices and values of up to CSR_B entries
+// are loaded together, then the x values they point at, then the products are summed in entry
+// order (the same sum as the one-entry-at-a-time loop, without an L2 round trip per entry)
+// ---------------------------------------------------------------------------
+template <int CSR_B = 8, typename F>
+__device__ __forceinline__ void csr_row(const int64_t* __restrict__ col, const double* __restrict__ val, int64_t e0,
+                                        int64_t e1, const double* __restrict__ x, int64_t xoff, F&& f) {
+  for (int64_t e = e0; e < e1; e += CSR_B) {
+    int64_t ci[CSR_B];
+    double v[CSR_B], xv[CSR_B];
+#pragma unroll
+    for (int u = 0; u < CSR_B; ++u)
+      if (e + u < e1) {
+        ci[u] = col[e + u];
+        v[u] = val[e + u];
+      }
+#pragma unroll
+    for (int u = 0; u < CSR_B; ++u)
+      if (e + u < e1) xv[u] = x[xoff + ci[u]];
+#pragma unroll
+    for (int u = 0; u < CSR_B; ++u)
+      if (e + u < e1) f(v[u], xv[u]);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // ghost extension rows
 // ---------------------------------------------------------------------------
 __global__ void k_ghost(double* __restrict__ f, int n, const int64_t* __restrict__ rows, const int64_t* __restrict__ ptr,
@@ -623,7 +840,7 @@ __global__ void k_ghost(double* __restrict__ f, int n, const int64_t* __restrict
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   double acc = 0.0;
-  for (int64_t e = ptr[r]; e < ptr[r + 1]; ++e) acc += val[e] * f[col[e]];
+  csr_row(col, val, ptr[r], ptr[r + 1], f, 0, [&](double a, double xv) { acc += a * xv; });
   f[rows[r]] = acc;
 }
 
@@ -942,13 +1159,12 @@ __global__ void k_residual(CaseDev c, ResidualCoef rc, const double* __restrict_
     if (row >= 0) {
       const int64_t* cp = c.irr_ptr[KIND];
       ax = 0.0;
-      for (int64_t e = cp[row]; e < cp[row + 1]; ++e) {
-        const double xv2 = x[base + c.irr_col[KIND][e]];
-        const double a = c.irr_val[KIND][e];
+      const int64_t e0 = cp[row], e1 = cp[row + 1];
+      csr_row<4>(c.irr_col[KIND], c.irr_val[KIND], e0, e1, x, base, [&](double a, double xv2) {
         ax += a * xv2;
         if (KIND == 0 && !RES_F32) aabs += fabs(a) * fabs(xv2);
-      }
-      nnz = (int)(cp[row + 1] - cp[row]);
+      });
+      nnz = (int)(e1 - e0);
     } else {
       const int j = (int)((unsigned)t / (unsigned)w), i = (int)((unsigned)t - (unsigned)j * w);
       // neighbours outside the operator's stencil read as zero
@@ -1046,8 +1262,9 @@ __global__ void k_pressure_bound(CaseDev c, ResidualCoef rc, const double* __res
     const int row = (k & CLS_IRREG) ? c.irr_index[0][t] : -1;
     if (row >= 0) {
       const int64_t* cp = c.irr_ptr[0];
-      for (int64_t e = cp[row]; e < cp[row + 1]; ++e) aabs += fabs(c.irr_val[0][e]) * fabs(x[c.irr_col[0][e]]);
-      nnz = (int)(cp[row + 1] - cp[row]);
+      const int64_t e0 = cp[row], e1 = cp[row + 1];
+      csr_row<4>(c.irr_col[0], c.irr_val[0], e0, e1, x, 0, [&](double a, double xv2) { aabs += fabs(a) * fabs(xv2); });
+      nnz = (int)(e1 - e0);
     } else {
       const int j = (int)((unsigned)t / (unsigned)nx), i = (int)((unsigned)t - (unsigned)j * nx);
       double xw = i > 0 ? x[t - 1] : 0.0, xe = i < nx - 1 ? x[t + 1] : 0.0;
@@ -1088,7 +1305,7 @@ __global__ void k_apply_pressure(CaseDev c, ResidualCoef rc, const double* __res
     if (row >= 0) {
       const int64_t* cp = c.irr_ptr[0];
       ax = 0.0;
-      for (int64_t e = cp[row]; e < cp[row + 1]; ++e) ax += c.irr_val[0][e] * z[c.irr_col[0][e]];
+      csr_row<4>(c.irr_col[0], c.irr_val[0], cp[row], cp[row + 1], z, 0, [&](double a, double zv) { ax += a * zv; });
     } else {
       const int j = (int)((unsigned)t / (unsigned)nx), i = (int)((unsigned)t - (unsigned)j * nx);
       const double xw = i > 0 ? z[t - 1] : 0.0, xe = i < nx - 1 ? z[t + 1] : 0.0;

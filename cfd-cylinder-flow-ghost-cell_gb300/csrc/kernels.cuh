@@ -268,6 +268,21 @@ void launch_ysolve(const TransformTables& tt, int cols, int rows, T* S, const Ga
 // band column solves of B ((bj1-bj0+1) x cols) in place, input scaled by 1/(2 nx)
 template <typename T>
 void launch_yband(const TransformTables& tt, int cols, T* B, const Gate& gate, cudaStream_t st);
+// Boundary term by direct sums (tables of the row transforms formed at set-up):
+//   firstm[q] = sum_k binv[q][k] spec[mrow[q]][k]      (inverse row transform at the m points C reads)
+template <typename T>
+void launch_band_first(int m, int n, const int32_t* mrow, const T* binv, const T* spec, T* firstm, const Gate& gate,
+                       cudaStream_t st);
+//   c[r] = sum_q M[r][q] firstm[q]                      (FP64 GEMV, M = S^{-1} C)
+template <typename T>
+void launch_band_gemv(int rank, int m, const double* M, const T* firstm, double* c, const Gate& gate,
+                      cudaStream_t st);
+//   band[j][k] = band solve of ( sum_{e in band row j} c[bperm[e]] bfwd[e][k] ) per column k
+template <typename T>
+void launch_band_fwd_solve(const TransformTables& tt, int n, int rank, const int32_t* bptr, const int32_t* bperm,
+                           const double* c, const T* bfwd, T* band, const Gate& gate, cudaStream_t st);
+// shared memory of launch_band_fwd_solve (the direct path needs it within the default 48 KB)
+size_t band_fwd_smem(int nb, int rank, bool fp32);
 // boundary Schur term c = M first[mcols] (M = S^{-1} C), written to w2 at the boundary rows
 template <typename TF>
 void launch_schur(const TF* first, int rank, int m, const int64_t* mcols, const double* M, const int64_t* rows,

@@ -190,8 +190,10 @@ def training_set(solver, rhs, sol):
 
 
 def train(weights, x, y, mask, epochs=200, lr=2e-3, batch=4, seed=0, log=None):
-    """Adam on the masked mean-squared error; returns the loss history."""
+    """Adam on the masked mean-squared error with a cosine learning-rate decay to lr / 20;
+    returns the loss history."""
     torch = _torch()
+    import math
     k, _, H, W = x.shape
     net = UNet(min(batch, k), H, W)
     opt = torch.optim.Adam(weights.parameters(), lr=lr)
@@ -199,6 +201,8 @@ def train(weights, x, y, mask, epochs=200, lr=2e-3, batch=4, seed=0, log=None):
     hist = []
     B = net.shape[0]
     for ep in range(epochs):
+        for gparam in opt.param_groups:
+            gparam['lr'] = lr * (0.05 + 0.95 * 0.5 * (1 + math.cos(math.pi * ep / max(epochs, 1))))
         idx = torch.randperm(k, generator=gen)[:B]
         xb, yb = x[idx].contiguous(), y[idx].contiguous()
         opt.zero_grad()
@@ -207,11 +211,28 @@ def train(weights, x, y, mask, epochs=200, lr=2e-3, batch=4, seed=0, log=None):
         loss.backward()
         opt.step()
         weights.refresh()
-        hist.append(float(loss))
+        hist.append(float(loss.detach()))
         if log and ep % 50 == 0:
             log(ep, hist[-1])
     net.close()
     return hist
+
+
+def relative_error(weights, x, y, mask):
+    """Masked relative L2 error of the network on inputs x against targets y (per sample)."""
+    torch = _torch()
+    k, _, H, W = x.shape
+    net = UNet(1, H, W)
+    out = []
+    with torch.no_grad():
+        for i in range(k):
+            pred = net.forward(weights, x[i:i + 1].contiguous(), torch.cuda.current_stream().cuda_stream)
+            torch.cuda.synchronize()
+            num = float(torch.linalg.vector_norm((pred - y[i:i + 1]) * mask))
+            den = float(torch.linalg.vector_norm(y[i:i + 1] * mask))
+            out.append(num / max(den, 1e-300))
+    net.close()
+    return out
 
 
 class LearnedPreconditioner:
