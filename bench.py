@@ -32,6 +32,11 @@ from pathlib import Path
 
 import numpy as np
 
+# The batch workload's graph runs many independent chains; let the CUDA runtime open its
+# maximum of 32 hardware work queues for this process (the default 8 serialises the chains).
+# It only takes effect before the CUDA context exists, i.e. before torch touches the GPU.
+os.environ.setdefault('CUDA_DEVICE_MAX_CONNECTIONS', '32')
+
 ROOT = Path(__file__).resolve().parent
 METRIC = 'cell-updates/s at div<1e-10: FP32+refine/learned-PC vs plain FP64, same GB300'
 

@@ -187,6 +187,7 @@ struct gm_handle {
   // second lane: the v Helmholtz solve runs beside the u solve (own stream, body stream and
   // spectral work arrays); fork/join by events
   cudaStream_t st2 = nullptr, st2_body = nullptr;
+  double step_dt = 0.0;  // dt of the step being issued (step phases)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   DBuf<double> spectral_b;
   DBuf<float> spectral32_b;
@@ -1206,14 +1207,34 @@ void schur_solve(gm_handle* h, int lane, RectDev& rd, int kind, double hc, const
   if (f32 && kind == 0) launch_pressure_bound(h->cd, h->rcoef[0], b, x, sc, h->nchk, gate_of(h), st);
 }
 
-// project(q, dt) (solver/optimized_ghost_cell.py:218-229); q is a face grid with active values
-void project(gm_handle* h, double* q, double dt, double* out, double* phi, int slot, int divk) {
+// project(q, dt) (solver/optimized_ghost_cell.py:218-229); q is a face grid with active values.
+// In two halves around its pressure solve so that a batch can run the solve of many cases as
+// one case-indexed launch sequence.
+struct SolveCall {  // one monitored solve (the arguments of schur_solve)
+  int lane;
+  RectDev* rd;
+  int kind;
+  const double* b;
+  double* x;
+  double* res;
+  double* first;
+  double* w2;
+  int slot;
+};
+void solve_call(gm_handle* h, const SolveCall& c) {
+  schur_solve(h, c.lane, *c.rd, c.kind, 0.0, c.b, c.x, c.res, c.first, c.w2, c.slot);
+}
+SolveCall project_pre(gm_handle* h, double* q, double dt, double* phi, int slot) {
   cudaStream_t st = h->st;
   Gate g0 = gate_of(h);
   launch_set_inlet(h->cd, q, false, st);
   ghost_faces(h, q, g0);
   launch_divergence(h->cd, q, h->prhs.p, dt, nullptr, nullptr, 1, g0, st);
-  schur_solve(h, 0, h->rp, 0, 0.0, h->prhs.p, phi, h->pres.p, h->pfirst.p, h->pw2.p, slot);
+  return SolveCall{0, &h->rp, 0, h->prhs.p, phi, h->pres.p, h->pfirst.p, h->pw2.p, slot};
+}
+void project_post(gm_handle* h, double* q, double dt, double* out, double* phi, int slot, int divk) {
+  cudaStream_t st = h->st;
+  Gate g0 = gate_of(h);
   if (h->rec_rhs && !h->capturing && h->rec_count < h->rec_cap) {
     const size_t off = (size_t)h->rec_count * h->Pn;
     CK(cudaMemcpyAsync(h->rec_rhs + off, h->prhs.p, h->Pn * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -1226,6 +1247,10 @@ void project(gm_handle* h, double* q, double dt, double* out, double* phi, int s
   ghost_faces(h, out, g0);
   launch_divergence(h->cd, out, nullptr, 0.0, nullptr, &h->ctl.p->div_max[divk], 0, g0, st);
   launch_gate_projection(h->ctl.p, divk, st);
+}
+void project(gm_handle* h, double* q, double dt, double* out, double* phi, int slot, int divk) {
+  solve_call(h, project_pre(h, q, dt, phi, slot));
+  project_post(h, q, dt, out, phi, slot, divk);
 }
 
 void ensure_helmholtz(gm_handle* h, double dt) {
@@ -1276,11 +1301,14 @@ void phase_mark(gm_handle* h, int k, cudaStream_t st) {
   if (h->phase_on) CK(cudaEventRecordWithFlags(h->phase_ev[k], st, h->capturing ? cudaEventRecordExternal : 0));
 }
 
-void step_once(gm_handle* h, double dt, int screen) {
+// One AB2/CN step in four phases around its solves (step_once runs them in order):
+//   phase 0: control block, CFL screen, momentum right-hand side -> Helmholtz u (lane 0), v (lane 1)
+//   phase 1: momentum gate, first projection up to its pressure solve
+//   phase 2: first projection after its solve, defect, second projection up to its solve
+//   phase 3: second projection after its solve, pressure output, forces, gates, step record
+void step_phase0(gm_handle* h, double dt, int screen, SolveCall calls[2]) {
   cudaStream_t st = h->st;
   phase_mark(h, 0, st);
-  const double hdt = 0.5 * dt;
-  const double hc = (0.5 * dt) * h->g.nu;
   Gate g0 = gate_of(h);
   const size_t keep = offsetof(StepCtl, solve);
   CK(cudaMemsetAsync(reinterpret_cast<char*>(h->ctl.p) + keep, 0, sizeof(StepCtl) - keep, st));
@@ -1324,20 +1352,35 @@ void step_once(gm_handle* h, double dt, int screen) {
   // second lane, joined before the momentum gate)
   CK(cudaEventRecord(h->ev_fork, st));
   CK(cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
-  schur_solve(h, 0, h->ru, 1, hc, h->rhs.p, h->star.p, h->fres.p, h->ffirst.p, h->fw2.p, S_HELM_U);
-  schur_solve(h, 1, h->rv, 2, hc, h->rhs.p, h->star.p, h->fres.p, h->ffirst.p, h->fw2.p, S_HELM_V);
+  calls[0] = SolveCall{0, &h->ru, 1, h->rhs.p, h->star.p, h->fres.p, h->ffirst.p, h->fw2.p, S_HELM_U};
+  calls[1] = SolveCall{1, &h->rv, 2, h->rhs.p, h->star.p, h->fres.p, h->ffirst.p, h->fw2.p, S_HELM_V};
+}
+SolveCall step_phase1(gm_handle* h) {
+  cudaStream_t st = h->st;
   CK(cudaEventRecord(h->ev_join, h->st2));
   CK(cudaStreamWaitEvent(st, h->ev_join, 0));
   launch_gate_momentum(h->ctl.p, h->nchk, st);
   phase_mark(h, 2, st);
   // projection of the CN velocity, defect correction and the pressure increment
-  project(h, h->star.p, dt, h->Unext.p, h->pphi.p, S_P1, 1);
+  return project_pre(h, h->star.p, h->step_dt, h->pphi.p, S_P1);
+}
+SolveCall step_phase2(gm_handle* h) {
+  cudaStream_t st = h->st;
+  const double dt = h->step_dt;
+  project_post(h, h->star.p, dt, h->Unext.p, h->pphi.p, S_P1, 1);
   phase_mark(h, 3, st);
-  launch_defect(h->cd, h->Unext.p, h->rhs.p, hdt, h->faction.p, h->fproj.p, g0, st);
+  launch_defect(h->cd, h->Unext.p, h->rhs.p, 0.5 * dt, h->faction.p, h->fproj.p, gate_of(h), st);
   phase_mark(h, 4, st);
-  project(h, h->fproj.p, dt, h->fproj2.p, h->pinc.p, S_P2, 2);
+  return project_pre(h, h->fproj.p, dt, h->pinc.p, S_P2);
+}
+void step_phase3(gm_handle* h) {
+  cudaStream_t st = h->st;
+  const double dt = h->step_dt;
+  Gate g0 = gate_of(h);
+  project_post(h, h->fproj.p, dt, h->fproj2.p, h->pinc.p, S_P2, 2);
   phase_mark(h, 5, st);
   ghost_p(h, h->pinc.p, g0);
+  const bool first = !h->has_history;
   double factor = first ? 1.0 : dt / (dt + h->prev_dt);
   launch_pressure_out(h->cd, h->phalf.p, h->pinc.p, factor, dt, h->faction.p, h->rhs.p, h->phalf_next.p, h->pout.p,
                       &h->ctl.p->coupled_max, g0, st);
@@ -1348,6 +1391,20 @@ void step_once(gm_handle* h, double dt, int screen) {
   launch_step_end(h->ctl.p, h->state_max.p, h->ring.p, h->ridx.p, h->counter.p, gm_handle::RING_CAP, st);
   phase_mark(h, 6, st);
   CK(cudaGetLastError());
+}
+// One AB2/CN step (solver/time_integration.py:7-145) on the handle state.
+// screen: 1/0 run or skip the CFL screen, -1 decide on the device from the step counter.
+// The error word of the control block is sticky: only the per-step slots are cleared, so
+// every kernel after a failed gate (also in later captured steps) does nothing.
+void step_once(gm_handle* h, double dt, int screen) {
+  h->step_dt = dt;
+  SolveCall helm[2];
+  step_phase0(h, dt, screen, helm);
+  solve_call(h, helm[0]);
+  solve_call(h, helm[1]);
+  solve_call(h, step_phase1(h));
+  solve_call(h, step_phase2(h));
+  step_phase3(h);
 }
 
 void swap_state(gm_handle* h) {
@@ -2214,12 +2271,21 @@ int gm_kernel_timing(int32_t kernel_class, int32_t enable, double* total_ms, int
 // Many cases per GPU: every steady step of all cases is one CUDA graph launch in
 // which each case is a concurrent branch (with its own refinement loops).
 // =============================================================================
+// Cases of a batch that share nx, ny and the precision (at most GM_PACK): their solves run as
+// case-indexed launches, one launch per kernel for the whole group.
+struct BatchGroup {
+  std::vector<int> idx;                // case indices in the batch
+  cudaStream_t st[2] = {nullptr, nullptr}, body[2] = {nullptr, nullptr};
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+
 struct gm_batch {
   std::vector<gm_handle*> cases;
   std::vector<long long> gens;  // Helmholtz table generations the graphs were captured with
   cudaStream_t root = nullptr;
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> join;
+  std::vector<BatchGroup> groups;  // empty: every case steps on its own graph branch
   struct Graph {
     cudaGraphExec_t exec = nullptr;
     std::vector<const double*> key;
@@ -2227,11 +2293,278 @@ struct gm_batch {
     double dt = 0;
     std::vector<long long> outer;               // per-case kernel nodes outside the refinement loops
     std::vector<std::array<long long, 5>> body;  // per-case kernel nodes of one sweep, per solve slot
+    long long group_outer = 0;                          // case-indexed solves: nodes outside the loops
+    std::vector<std::array<long long, 5>> group_body;   // and per group, one sweep per solve slot
   } graphs[2];
   std::string err;
 };
 
 namespace {
+
+// ---- case-indexed solves of a batch group --------------------------------------------
+// One application of the boundary-corrected inverse for every case of the group (the direct
+// path of schur_inverse, case-indexed): x = [x +] T^{-1} r - band correction.
+template <typename T, typename TI>
+void apply_inverse_group(gm_batch* b, const BatchGroup& G, int lane, const std::vector<SolveCall>& calls,
+                         bool body, cudaStream_t st) {
+  const int n = (int)calls.size();
+  const bool f32 = sizeof(T) == 4;
+  auto fwd = std::make_unique<ArgPack<XpassArgs<T, TI, T>>>();
+  auto ys = std::make_unique<ArgPack<YsolveArgs<T>>>();
+  auto bf = std::make_unique<ArgPack<BandFirstArgs<T>>>();
+  auto bg = std::make_unique<ArgPack<BandGemvArgs<T>>>();
+  auto bw = std::make_unique<ArgPack<BandFwdArgs<T>>>();
+  auto fin = std::make_unique<ArgPack<XpassArgs<T, T, double>>>();
+  const TransformTables* tt0 = nullptr;
+  for (int c = 0; c < n; ++c) {
+    gm_handle* h = b->cases[G.idx[c]];
+    const SolveCall& call = calls[c];
+    RectDev& rd = *call.rd;
+    const TransformTables& tt = f32 ? rd.tt32 : rd.tt;
+    if (!tt0) tt0 = &tt;
+    const RectView& v = rd.view;
+    const Gate g{h->ctl.p, call.slot, body ? -1 : 0};
+    T* spec = f32 ? (T*)(lane == 0 ? h->spectral32.p : h->spectral32_b.p) : (T*)(lane == 0 ? h->spectral.p : h->spectral_b.p);
+    const TI* r;
+    if (!body) r = (const TI*)call.b;
+    else if (f32) r = (const TI*)(call.kind == 0 ? (void*)h->pres32.p : (void*)h->fres32.p);
+    else r = (const TI*)call.res;
+    const YCorr<T> none{nullptr, nullptr, nullptr, 0, -1};
+    fwd->a[c] = xpass_args<T, TI, T>(tt, false, 0, v.rows, r, v.base, v.pitch, v.cls, spec, 0, v.cols, nullptr,
+                                     nullptr, none, g);
+    ys->a[c] = ysolve_args<T>(tt, v.cols, v.rows, spec, g);
+    T* fm = f32 ? (T*)rd.firstm32.p : (T*)rd.firstm.p;
+    bf->a[c] = BandFirstArgs<T>{rd.mcount, v.cols, rd.mrow.p, f32 ? (const T*)rd.binv32.p : (const T*)rd.binv.p, spec,
+                                fm, g};
+    bg->a[c] = BandGemvArgs<T>{rd.rank, rd.mcount, rd.mmat.p, fm, rd.cvec.p, g};
+    T* band = f32 ? (T*)rd.band32.p : (T*)rd.band.p;
+    bw->a[c] = BandFwdArgs<T>{tt.bj1 - tt.bj0 + 1, v.cols, rd.rank, rd.bptr.p, rd.bperm.p, rd.cvec.p,
+                              f32 ? (const T*)rd.bfwd32.p : (const T*)rd.bfwd.p, (T)tt.gamma, (T)tt.yscale,
+                              (const T*)tt.bpiv, band, g, band_fwd_blocks(v.cols)};
+    const YCorr<T> corr{band, (const T*)tt.phi, (const T*)tt.psi, tt.bj0, tt.bj1};
+    fin->a[c] = xpass_args<T, T, double>(tt, true, 0, v.rows, spec, 0, v.cols, nullptr, call.x, v.base, v.pitch, v.cls,
+                                         body ? call.x : nullptr, corr, g);
+  }
+  launch_xpass_multi<T, TI, T>(*fwd, n, *tt0, st);
+  launch_ysolve_multi<T>(*ys, n, *tt0, st);
+  launch_band_first_multi<T>(*bf, n, st);
+  launch_band_gemv_multi<T>(*bg, n, st);
+  launch_band_fwd_solve_multi<T>(*bw, n, st);
+  launch_xpass_multi<T, T, double>(*fin, n, *tt0, st);
+}
+
+void residual_group(gm_batch* b, const BatchGroup& G, const std::vector<SolveCall>& calls, bool body,
+                    cudaStream_t st) {
+  const int n = (int)calls.size();
+  auto p = std::make_unique<ArgPack<ResidualArgs>>();
+  bool f32 = false;
+  for (int c = 0; c < n; ++c) {
+    gm_handle* h = b->cases[G.idx[c]];
+    const SolveCall& call = calls[c];
+    f32 = h->precision == 1;
+    void* resb = f32 ? (void*)(call.kind == 0 ? h->pres32.p : h->fres32.p) : (void*)call.res;
+    p->a[c] = residual_args(h->cd, h->rcoef[call.kind], call.kind, call.b, call.x, resb, &h->ctl.p->solve[call.slot],
+                            body ? -1 : 0, !body, Gate{h->ctl.p, call.slot, body ? -1 : 0});
+  }
+  launch_residual_multi(*p, n, calls[0].kind, f32, st);
+}
+
+// The monitored solve of every case of the group (schur_solve_graph, case-indexed): first
+// application and check, then a WHILE node whose body sweeps the cases still above their
+// targets; returns the kernel nodes of one body sweep.
+long long solve_group(gm_batch* b, BatchGroup& G, int lane, const std::vector<SolveCall>& calls) {
+  cudaStream_t st = G.st[lane], body_st = G.body[lane];
+  const int n = (int)calls.size();
+  gm_handle* h0 = b->cases[G.idx[0]];
+  const bool f32 = h0->precision == 1;
+  const int slot = calls[0].slot, kind = calls[0].kind, nchk = h0->nchk;
+  if (f32) apply_inverse_group<float, double>(b, G, lane, calls, false, st);
+  else apply_inverse_group<double, double>(b, G, lane, calls, false, st);
+  residual_group(b, G, calls, false, st);
+  ArgPack<StepCtl*> ctls{};
+  for (int c = 0; c < n; ++c) ctls.a[c] = b->cases[G.idx[c]]->ctl.p;
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t graph;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, nullptr, nullptr, nullptr));
+  cudaGraphConditionalHandle cond;
+  CK(cudaGraphConditionalHandleCreate(&cond, graph, 0, 0));
+  launch_refine_decide_multi(ctls, n, slot, nchk, cond, st);
+  CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &nd));
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = cond;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cnode;
+  CK(cudaGraphAddNode(&cnode, graph, deps, nullptr, nd, &cp));
+  cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
+  CK(cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+  CK(cudaStreamBeginCaptureToGraph(body_st, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  const long long c0 = kernel_launch_count();
+  if (f32) apply_inverse_group<float, float>(b, G, lane, calls, true, body_st);
+  else apply_inverse_group<double, double>(b, G, lane, calls, true, body_st);
+  residual_group(b, G, calls, true, body_st);
+  launch_refine_decide_multi(ctls, n, slot, nchk, cond, body_st);
+  const long long body_nodes = kernel_launch_count() - c0;
+  CK(cudaStreamEndCapture(body_st, &bodyg));
+  if (f32 && kind == 0) {
+    auto p = std::make_unique<ArgPack<BoundArgs>>();
+    for (int c = 0; c < n; ++c) {
+      gm_handle* h = b->cases[G.idx[c]];
+      p->a[c] = bound_args(h->cd, h->rcoef[0], calls[c].b, calls[c].x, &h->ctl.p->solve[slot], nchk, gate_of(h));
+    }
+    launch_pressure_bound_multi(*p, n, st);
+  }
+  return body_nodes;
+}
+
+// Groups of a batch for case-indexed solves (empty when some case cannot join one: every case
+// needs the direct pressure path, graphs and the direct boundary tables).  Cases of a group take
+// the launch shapes of its first case (every shape computes the same values).
+void free_groups(gm_batch* b) {
+  for (auto& G : b->groups)
+    for (int l = 0; l < 2; ++l) {
+      if (G.st[l]) cudaStreamDestroy(G.st[l]);
+      if (G.body[l]) cudaStreamDestroy(G.body[l]);
+      if (G.ev[l]) cudaEventDestroy(G.ev[l]);
+    }
+  b->groups.clear();
+}
+
+// GHOSTMAC_BATCH_GROUPED=1 selects them; by default every case runs on its own graph branch
+// (measured faster on GB300 for the 64-case sweep: the branches overlap kernels of different
+// kinds, while a case-indexed row transform is bound by its blocks' latency at full load).
+void batch_groups(gm_batch* b) {
+  const char* e = std::getenv("GHOSTMAC_BATCH_GROUPED");
+  if (!(e && e[0] == '1')) { free_groups(b); return; }
+  std::vector<BatchGroup> gs;
+  for (int c = 0; c < (int)b->cases.size(); ++c) {
+    gm_handle* h = b->cases[c];
+    if (!h->use_graphs || !h->rp.direct || !h->ru.direct || !h->rv.direct) {
+      free_groups(b);
+      return;
+    }
+    BatchGroup* dst = nullptr;
+    for (auto& g : gs) {
+      gm_handle* f = b->cases[g.idx[0]];
+      if (f->g.nx == h->g.nx && f->g.ny == h->g.ny && f->precision == h->precision && (int)g.idx.size() < GM_PACK)
+        dst = &g;
+    }
+    if (!dst) { gs.emplace_back(); dst = &gs.back(); }
+    dst->idx.push_back(c);
+  }
+  // keep the streams and events of existing groups
+  for (size_t k = 0; k < gs.size(); ++k) {
+    if (k < b->groups.size()) {
+      for (int l = 0; l < 2; ++l) {
+        gs[k].st[l] = b->groups[k].st[l];
+        gs[k].body[l] = b->groups[k].body[l];
+        gs[k].ev[l] = b->groups[k].ev[l];
+        b->groups[k].st[l] = nullptr;
+        b->groups[k].body[l] = nullptr;
+        b->groups[k].ev[l] = nullptr;
+      }
+    }
+    for (int l = 0; l < 2; ++l) {
+      if (!gs[k].st[l]) CK(cudaStreamCreateWithFlags(&gs[k].st[l], cudaStreamNonBlocking));
+      if (!gs[k].body[l]) CK(cudaStreamCreateWithFlags(&gs[k].body[l], cudaStreamNonBlocking));
+      if (!gs[k].ev[l]) CK(cudaEventCreateWithFlags(&gs[k].ev[l], cudaEventDisableTiming));
+    }
+  }
+  for (size_t k = gs.size(); k < b->groups.size(); ++k)
+    for (int l = 0; l < 2; ++l) {
+      if (b->groups[k].st[l]) cudaStreamDestroy(b->groups[k].st[l]);
+      if (b->groups[k].body[l]) cudaStreamDestroy(b->groups[k].body[l]);
+      if (b->groups[k].ev[l]) cudaEventDestroy(b->groups[k].ev[l]);
+    }
+  b->groups = std::move(gs);
+  auto copy_shape = [](TransformTables& d, const TransformTables& s) {
+    d.xg_threads = s.xg_threads;
+    d.xg_pb = s.xg_pb;
+    d.smem_x = s.smem_x;
+    d.lpb_y = s.lpb_y;
+    d.threads_y = s.threads_y;
+    d.smem_y = s.smem_y;
+  };
+  for (auto& g : b->groups) {
+    gm_handle* f = b->cases[g.idx[0]];
+    for (size_t k = 1; k < g.idx.size(); ++k) {
+      gm_handle* h = b->cases[g.idx[k]];
+      RectDev* dst[3] = {&h->rp, &h->ru, &h->rv};
+      const RectDev* src[3] = {&f->rp, &f->ru, &f->rv};
+      for (int q = 0; q < 3; ++q) {
+        copy_shape(dst[q]->tt, src[q]->tt);
+        copy_shape(dst[q]->tt32, src[q]->tt32);
+      }
+    }
+  }
+}
+
+// the case-indexed capture of one steady step of every case (phases on the cases' streams,
+// solves on the groups' streams)
+void capture_grouped_step(gm_batch* b, double dt, gm_batch::Graph& gr) {
+  const int nc = (int)b->cases.size();
+  const int ng = (int)b->groups.size();
+  gr.group_body.assign(ng, std::array<long long, 5>{});
+  gr.group_outer = 0;
+  std::vector<std::array<SolveCall, 2>> helm(nc);
+  std::vector<SolveCall> pcall(nc);
+  auto phase = [&](int c, auto&& f) {
+    gm_handle* h = b->cases[c];
+    const long long c0 = kernel_launch_count();
+    f(h);
+    gr.outer[c] += kernel_launch_count() - c0;
+  };
+  // joins the cases of group g (their stream `which`: 0 st, 1 st2) into its lane streams
+  auto join_group = [&](BatchGroup& G, bool both) {
+    for (int c : G.idx) {
+      gm_handle* h = b->cases[c];
+      CK(cudaEventRecord(b->join[c], h->st));
+      CK(cudaStreamWaitEvent(G.st[0], b->join[c], 0));
+      if (both) CK(cudaStreamWaitEvent(G.st[1], b->join[c], 0));
+    }
+  };
+  auto fork_group = [&](BatchGroup& G, bool both) {
+    CK(cudaEventRecord(G.ev[0], G.st[0]));
+    if (both) CK(cudaEventRecord(G.ev[1], G.st[1]));
+    for (int c : G.idx) {
+      gm_handle* h = b->cases[c];
+      CK(cudaStreamWaitEvent(h->st, G.ev[0], 0));
+      if (both) CK(cudaStreamWaitEvent(h->st2, G.ev[1], 0));
+    }
+  };
+  auto solves = [&](int slot_kind, bool both) {
+    for (int g = 0; g < ng; ++g) {
+      BatchGroup& G = b->groups[g];
+      std::vector<SolveCall> c0v, c1v;
+      for (int c : G.idx) {
+        if (both) { c0v.push_back(helm[c][0]); c1v.push_back(helm[c][1]); }
+        else c0v.push_back(pcall[c]);
+      }
+      join_group(G, both);
+      const long long o0 = kernel_launch_count();
+      long long bn = solve_group(b, G, 0, c0v);
+      gr.group_body[g][c0v[0].slot] = bn;
+      long long bn1 = 0;
+      if (both) {
+        bn1 = solve_group(b, G, 1, c1v);
+        gr.group_body[g][c1v[0].slot] = bn1;
+      }
+      gr.group_outer += kernel_launch_count() - o0 - bn - bn1;
+      fork_group(G, both);
+    }
+    (void)slot_kind;
+  };
+  for (int c = 0; c < nc; ++c) phase(c, [&](gm_handle* h) { h->step_dt = dt; step_phase0(h, dt, -1, helm[c].data()); });
+  solves(0, true);
+  for (int c = 0; c < nc; ++c) phase(c, [&](gm_handle* h) { pcall[c] = step_phase1(h); });
+  solves(1, false);
+  for (int c = 0; c < nc; ++c) phase(c, [&](gm_handle* h) { pcall[c] = step_phase2(h); });
+  solves(2, false);
+  for (int c = 0; c < nc; ++c) phase(c, [&](gm_handle* h) { step_phase3(h); });
+}
 
 std::vector<const double*> batch_key(gm_batch* b) {
   std::vector<const double*> k;
@@ -2256,11 +2589,31 @@ gm_batch::Graph& batch_graph(gm_batch* b, double dt) {
   }
   slot->outer.assign(b->cases.size(), 0);
   slot->body.assign(b->cases.size(), std::array<long long, 5>{});
+  slot->group_outer = 0;
+  slot->group_body.clear();
+  batch_groups(b);
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal));
   try {
     CK(cudaEventRecord(b->fork, b->root));
-    for (size_t c = 0; c < b->cases.size(); ++c) {
+    if (!b->groups.empty()) {
+      for (size_t c = 0; c < b->cases.size(); ++c) {
+        gm_handle* h = b->cases[c];
+        CK(cudaStreamWaitEvent(h->st, b->fork, 0));
+        std::fill(h->body_nodes_slot, h->body_nodes_slot + 5, 0LL);
+        h->capturing = true;
+      }
+      const long long c0 = kernel_launch_count();
+      capture_grouped_step(b, dt, *slot);
+      kernel_launch_adjust(-(kernel_launch_count() - c0));
+      for (size_t c = 0; c < b->cases.size(); ++c) {
+        gm_handle* h = b->cases[c];
+        h->capturing = false;
+        CK(cudaEventRecord(b->join[c], h->st));
+        CK(cudaStreamWaitEvent(b->root, b->join[c], 0));
+      }
+    }
+    for (size_t c = 0; c < b->cases.size() && b->groups.empty(); ++c) {
       gm_handle* h = b->cases[c];
       CK(cudaStreamWaitEvent(h->st, b->fork, 0));
       const long long c0 = kernel_launch_count();
@@ -2330,6 +2683,7 @@ int gm_batch_destroy(gm_batch* b) {
   for (auto& gr : b->graphs)
     if (gr.exec) cudaGraphExecDestroy(gr.exec);
   for (auto& e : b->join) cudaEventDestroy(e);
+  free_groups(b);
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->root) cudaStreamDestroy(b->root);
   delete b;
@@ -2411,7 +2765,20 @@ int gm_batch_step(gm_batch* b, double dt, int32_t n_steps, int64_t first_step_in
           }
         }
       }
-      if (steady) kernel_launch_adjust(nodes);
+      if (steady) {
+        // case-indexed solves: the loop of a group runs while any of its cases sweeps
+        const gm_batch::Graph& gr = b->graphs[0].exec ? b->graphs[0] : b->graphs[1];
+        for (size_t g = 0; g < b->groups.size() && g < gr.group_body.size(); ++g)
+          for (int k = 0; k < batch; ++k) {
+            for (int sl = 0; sl < 5; ++sl) {
+              int it = 0;
+              for (int c : b->groups[g].idx) it = std::max(it, b->cases[c]->host_ring[k].solve[sl].k);
+              nodes += gr.group_body[g][sl] * it;
+            }
+          }
+        for (int k = 0; k < batch; ++k) nodes += gr.group_outer;
+        kernel_launch_adjust(nodes);
+      }
       s += batch;
     }
   } catch (const GateError& e) {

@@ -354,17 +354,17 @@ template void launch_xpass<float, float, double>(const TransformTables&, bool, i
 // first, so the dependent chains wait on shared-memory latency only.
 // ---------------------------------------------------------------------------
 template <typename T, int L>
-__global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale, const T* __restrict__ t0,
-                         const T* __restrict__ t1, const T* __restrict__ t2, T* __restrict__ S, Gate gate) {
+__device__ __forceinline__ void ysolve_body(int n /*rows*/, int cols, const YChunks& ch, T gamma, T scale,
+                                            const T* __restrict__ t0, const T* __restrict__ t1,
+                                            const T* __restrict__ t2, T* __restrict__ S, int bid) {
   // L consecutive columns per block (L a power of two: thread -> (column, row/chunk) by shifts)
-  if (!gate_open(gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int ns = n | 1;                                  // odd stride between the columns
   T* col = reinterpret_cast<T*>(smem_raw);              // L x ns values
   T* piv = col + (size_t)L * ns;                         // L x ns reciprocal pivots
   T* sl = piv + (size_t)L * ns;                          // L x ns left spikes (t1)
   T* sr = sl + (size_t)L * ns;                           // L x ns right spikes (t2)
-  const int c0 = blockIdx.x * L;
+  const int c0 = bid * L;
   const int P = ch.P;
   const int l = threadIdx.x & (L - 1);                   // column of this thread
   const int rsub = threadIdx.x / L;                      // row offset (load/store), chunk (solve)
@@ -452,6 +452,12 @@ __global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale,
   T* s_out = S + cc;
   if (colok)
     for (int e = rsub; e < n; e += rstep) s_out[(int64_t)e * cols] = col[l * ns + e];
+}
+template <typename T, int L>
+__global__ void k_ysolve(int n /*rows*/, int cols, YChunks ch, T gamma, T scale, const T* __restrict__ t0,
+                         const T* __restrict__ t1, const T* __restrict__ t2, T* __restrict__ S, Gate gate) {
+  if (!gate_open(gate)) return;
+  ysolve_body<T, L>(n, cols, ch, gamma, scale, t0, t1, t2, S, blockIdx.x);
 }
 size_t ysolve_smem(int rows, int lpb, bool fp32) {
   const size_t esz = fp32 ? 4 : 8;
@@ -543,6 +549,11 @@ void launch_yband(const TransformTables& tt, int cols, T* B, const Gate& gate, c
 template void launch_yband<double>(const TransformTables&, int, double*, const Gate&, cudaStream_t);
 template void launch_yband<float>(const TransformTables&, int, float*, const Gate&, cudaStream_t);
 
+template <typename T, typename TI, typename TO>
+__global__ void k_xpass_multi(const __grid_constant__ ArgPack<XpassArgs<T, TI, TO>> p);
+template <typename T, int L>
+__global__ void k_ysolve_multi(const __grid_constant__ ArgPack<YsolveArgs<T>> p);
+
 // Opts the transform kernels into the large dynamic shared memory carve-out; returns the
 // dynamic bytes every one of them may use (the opt-in limit minus their static shared memory).
 template <typename K>
@@ -567,6 +578,18 @@ int configure_kernels(int smem_optin) {
   d = std::min(d, allow_dynamic_smem(k_ysolve<float, 4>, smem_optin));
   d = std::min(d, allow_dynamic_smem(k_ysolve<float, 8>, smem_optin));
   d = std::min(d, allow_dynamic_smem(k_ysolve<float, 16>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_xpass_multi<double, double, double>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_xpass_multi<float, double, float>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_xpass_multi<float, float, float>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_xpass_multi<float, float, double>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve_multi<double, 2>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve_multi<double, 4>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve_multi<double, 8>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve_multi<double, 16>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve_multi<float, 2>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve_multi<float, 4>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve_multi<float, 8>, smem_optin));
+  d = std::min(d, allow_dynamic_smem(k_ysolve_multi<float, 16>, smem_optin));
   return d;
 }
 
@@ -655,11 +678,8 @@ static constexpr int BAND_ITEMS = 16;  // loads in flight per thread (n <= BAND_
 // One block per point: the inverse row transform of its spectrum row evaluated at its column
 // (coefficients in binv), all of a thread's products loaded before they are summed.
 template <typename T>
-__global__ void __launch_bounds__(BAND_TPB) k_band_first(int m, int n, const int32_t* __restrict__ mrow,
-                                                         const T* __restrict__ binv, const T* __restrict__ spec,
-                                                         T* __restrict__ firstm, Gate gate) {
-  if (!gate_open(gate)) return;
-  const int q = blockIdx.x;
+__device__ __forceinline__ void band_first_body(int n, const int32_t* __restrict__ mrow, const T* __restrict__ binv,
+                                                const T* __restrict__ spec, T* __restrict__ firstm, int q) {
   const T* b = binv + (int64_t)q * n;
   const T* sp = spec + (int64_t)mrow[q] * n;
   T acc = 0;
@@ -677,14 +697,18 @@ __global__ void __launch_bounds__(BAND_TPB) k_band_first(int m, int n, const int
   const T v = block_sum_all<T>(acc);
   if (threadIdx.x == 0) firstm[q] = v;
 }
+template <typename T>
+__global__ void __launch_bounds__(BAND_TPB) k_band_first(int m, int n, const int32_t* __restrict__ mrow,
+                                                         const T* __restrict__ binv, const T* __restrict__ spec,
+                                                         T* __restrict__ firstm, Gate gate) {
+  if (!gate_open(gate)) return;
+  band_first_body<T>(n, mrow, binv, spec, firstm, blockIdx.x);
+}
 
 // One block per row of M: c[r] = M[r] . firstm (FP64 accumulation).
 template <typename T>
-__global__ void __launch_bounds__(BAND_TPB) k_band_gemv(int rank, int m, const double* __restrict__ M,
-                                                        const T* __restrict__ firstm, double* __restrict__ c,
-                                                        Gate gate) {
-  if (!gate_open(gate)) return;
-  const int r = blockIdx.x;
+__device__ __forceinline__ void band_gemv_body(int m, const double* __restrict__ M, const T* __restrict__ firstm,
+                                               double* __restrict__ c, int r) {
   const double* mr = M + (int64_t)r * m;
   double acc = 0.0;
   for (int q0 = threadIdx.x; q0 < m; q0 += BAND_TPB * BAND_ITEMS) {
@@ -702,6 +726,13 @@ __global__ void __launch_bounds__(BAND_TPB) k_band_gemv(int rank, int m, const d
   const double v = block_sum_all<double>(acc);
   if (threadIdx.x == 0) c[r] = v;
 }
+template <typename T>
+__global__ void __launch_bounds__(BAND_TPB) k_band_gemv(int rank, int m, const double* __restrict__ M,
+                                                        const T* __restrict__ firstm, double* __restrict__ c,
+                                                        Gate gate) {
+  if (!gate_open(gate)) return;
+  band_gemv_body<T>(m, M, firstm, c, blockIdx.x);
+}
 
 // Blocks of BAND_COLS columns x BAND_ROWT row threads.  Thread (kk, jt) forms the forward
 // row transform of U c on band rows jt, jt + BAND_ROWT, ... of column k (a sum over that row's
@@ -709,11 +740,10 @@ __global__ void __launch_bounds__(BAND_TPB) k_band_gemv(int rank, int m, const d
 // system (as k_yband) in shared memory, and all threads write the band back.
 static constexpr int BAND_COLS = 32, BAND_ROWT = 8;
 template <typename T>
-__global__ void __launch_bounds__(BAND_COLS * BAND_ROWT) k_band_fwd_solve(
-    int nb, int n, int rank, const int32_t* __restrict__ bptr, const int32_t* __restrict__ bperm,
-    const double* __restrict__ c, const T* __restrict__ bfwd, T gamma, T scale, const T* __restrict__ bpiv,
-    T* __restrict__ band, Gate gate) {
-  if (!gate_open(gate)) return;
+__device__ __forceinline__ void band_fwd_solve_body(int nb, int n, int rank, const int32_t* __restrict__ bptr,
+                                                    const int32_t* __restrict__ bperm, const double* __restrict__ c,
+                                                    const T* __restrict__ bfwd, T gamma, T scale,
+                                                    const T* __restrict__ bpiv, T* __restrict__ band, int bid) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* cs = reinterpret_cast<T*>(smem_raw);   // rank values c, band-row order
   T* xb = cs + ((rank + 3) & ~3);           // nb x BAND_COLS
@@ -723,7 +753,7 @@ __global__ void __launch_bounds__(BAND_COLS * BAND_ROWT) k_band_fwd_solve(
   for (int e = tid; e < rank; e += blockDim.x) cs[e] = cvt_to<T>(c[bperm[e]]);
   for (int j = tid; j <= nb; j += blockDim.x) ps[j] = bptr[j];
   __syncthreads();
-  const int k = blockIdx.x * BAND_COLS + kk;
+  const int k = bid * BAND_COLS + kk;
   if (k < n) {
     for (int j = jt; j < nb; j += BAND_ROWT) {
       const int e0 = ps[j], e1 = ps[j + 1];
@@ -757,7 +787,16 @@ __global__ void __launch_bounds__(BAND_COLS * BAND_ROWT) k_band_fwd_solve(
   if (k < n)
     for (int j = jt; j < nb; j += BAND_ROWT) band[(int64_t)j * n + k] = xb[j * BAND_COLS + kk];
 }
+template <typename T>
+__global__ void __launch_bounds__(BAND_COLS * BAND_ROWT) k_band_fwd_solve(
+    int nb, int n, int rank, const int32_t* __restrict__ bptr, const int32_t* __restrict__ bperm,
+    const double* __restrict__ c, const T* __restrict__ bfwd, T gamma, T scale, const T* __restrict__ bpiv,
+    T* __restrict__ band, Gate gate) {
+  if (!gate_open(gate)) return;
+  band_fwd_solve_body<T>(nb, n, rank, bptr, bperm, c, bfwd, gamma, scale, bpiv, band, blockIdx.x);
+}
 
+int band_fwd_blocks(int n) { return (n + BAND_COLS - 1) / BAND_COLS; }
 size_t band_fwd_smem(int nb, int rank, bool fp32) {
   const size_t esz = fp32 ? 4 : 8;
   return (size_t)((rank + 3) & ~3) * esz + (size_t)2 * nb * BAND_COLS * esz + (size_t)(nb + 1) * sizeof(int);
@@ -1131,9 +1170,9 @@ __device__ __forceinline__ double coef_cw(const ResidualCoef& rc, int ic) {
 }
 
 template <int KIND, bool RES_F32>
-__global__ void k_residual(CaseDev c, ResidualCoef rc, const double* __restrict__ b, const double* __restrict__ x,
-                           void* __restrict__ res_out, SolveCtl* sc, int check, int first, Gate gate) {
-  if (!gate_open(gate)) return;
+__device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCoef& rc, const double* __restrict__ b,
+                                              const double* __restrict__ x, void* __restrict__ res_out, SolveCtl* sc,
+                                              int check, int first, int bid, int nblk) {
   if (check < 0) check = *(volatile int*)&sc->k;
   const int nx = c.nx, ny = c.ny;
   const int w = KIND == 1 ? nx + 1 : nx;            // row width of the grid
@@ -1145,7 +1184,7 @@ __global__ void k_residual(CaseDev c, ResidualCoef rc, const double* __restrict_
   unsigned long long rm = 0, bm = 0, bd = 0, xb = 0;
   double rs = 0.0, bs = 0.0;
   float rs32 = 0.0f;  // RES_F32: sum of the stored FP32 residuals squared (diagnostics only)
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < npts; t += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t t = (int64_t)bid * blockDim.x + threadIdx.x; t < npts; t += (int64_t)nblk * blockDim.x) {
     const uint8_t k = cls[t];
     const int64_t f = base + t;
     if (!(k & CLS_ACTIVE)) {
@@ -1224,6 +1263,12 @@ __global__ void k_residual(CaseDev c, ResidualCoef rc, const double* __restrict_
   }
   block_commit_max(xb, &sc->xbad);
 }
+template <int KIND, bool RES_F32>
+__global__ void k_residual(CaseDev c, ResidualCoef rc, const double* __restrict__ b, const double* __restrict__ x,
+                           void* __restrict__ res_out, SolveCtl* sc, int check, int first, Gate gate) {
+  if (!gate_open(gate)) return;
+  residual_body<KIND, RES_F32>(c, rc, b, x, res_out, sc, check, first, blockIdx.x, gridDim.x);
+}
 
 void launch_residual(const CaseDev& c, const ResidualCoef& rc, int kind, const double* b, const double* x, void* res,
                      bool res_f32, SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st) {
@@ -1247,13 +1292,13 @@ void launch_residual(const CaseDev& c, const ResidualCoef& rc, int kind, const d
 // Roundoff bound max_i (2 nnz_i + 2) eps (|A||x| + |b|)_i of the pressure solution after its
 // refinement loop (solver/pressure_schur.py:48-56), stored at the last check; used by the
 // FP32 mode, whose residual sweeps skip it.
-__global__ void k_pressure_bound(CaseDev c, ResidualCoef rc, const double* __restrict__ b,
-                                 const double* __restrict__ x, SolveCtl* sc, int nchk, Gate gate) {
-  if (!gate_open(gate)) return;
+__device__ __forceinline__ void pressure_bound_body(const CaseDev& c, const ResidualCoef& rc,
+                                                    const double* __restrict__ b, const double* __restrict__ x,
+                                                    SolveCtl* sc, int nchk, int bid, int nblk) {
   const int check = last_check(sc, nchk);
   const int nx = c.nx, ny = c.ny;
   unsigned long long bd = 0;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < c.psize; t += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t t = (int64_t)bid * blockDim.x + threadIdx.x; t < c.psize; t += (int64_t)nblk * blockDim.x) {
     const uint8_t k = c.cls_p[t];
     if (!(k & CLS_ACTIVE)) continue;
     const double xv = x[t], bv = b[t];
@@ -1276,6 +1321,11 @@ __global__ void k_pressure_bound(CaseDev c, ResidualCoef rc, const double* __res
     bd = umax64(bd, dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + fabs(bv))));
   }
   block_commit_max(bd, &sc->bound[check]);
+}
+__global__ void k_pressure_bound(CaseDev c, ResidualCoef rc, const double* __restrict__ b,
+                                 const double* __restrict__ x, SolveCtl* sc, int nchk, Gate gate) {
+  if (!gate_open(gate)) return;
+  pressure_bound_body(c, rc, b, x, sc, nchk, blockIdx.x, gridDim.x);
 }
 void launch_pressure_bound(const CaseDev& c, const ResidualCoef& rc, const double* b, const double* x, SolveCtl* sc,
                            int nchk, const Gate& gate, cudaStream_t st) {
@@ -1862,5 +1912,259 @@ void launch_schur_column(const double* first, const RectView& view, int rank, co
     k_schur_column<<<blocks_for(rank, 128), 128, 0, st>>>(first, view, rank, c_ptr, c_col, c_val, S, col);
   }
 }
+
+// ---------------------------------------------------------------------------
+// case-indexed launches: blockIdx.y selects the case, its arguments come from the kernel's
+// parameter space; blocks past the case's own grid return at once
+// ---------------------------------------------------------------------------
+template <typename T, typename TI, typename TO>
+__global__ void k_xpass_multi(const __grid_constant__ ArgPack<XpassArgs<T, TI, TO>> p) {
+  const XpassArgs<T, TI, TO>& a = p.a[blockIdx.y];
+  if ((int)blockIdx.x >= a.nblk) return;
+  if (!gate_open(a.gate)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const R2RTables<T> ts = xpass_stage_tables<T>(a.type, a.n, a.plan, a.tb, smem_raw);
+  xpass_block<T, TI, TO>(blockIdx.x, a.n, a.r0, a.nr, a.type, a.plan, ts, a.in, a.ibase, a.ipitch, a.icls, a.out,
+                         a.obase, a.opitch, a.ocls, a.add, a.corr, a.gthreads, a.gpb, smem_raw);
+}
+template <typename T, int L>
+__global__ void k_ysolve_multi(const __grid_constant__ ArgPack<YsolveArgs<T>> p) {
+  const YsolveArgs<T>& a = p.a[blockIdx.y];
+  if ((int)blockIdx.x >= a.nblk) return;
+  if (!gate_open(a.gate)) return;
+  ysolve_body<T, L>(a.rows, a.cols, a.ch, a.gamma, a.scale, a.t0, a.t1, a.t2, a.S, blockIdx.x);
+}
+template <typename T>
+__global__ void __launch_bounds__(BAND_TPB) k_band_first_multi(const __grid_constant__ ArgPack<BandFirstArgs<T>> p) {
+  const BandFirstArgs<T>& a = p.a[blockIdx.y];
+  if ((int)blockIdx.x >= a.m) return;
+  if (!gate_open(a.gate)) return;
+  band_first_body<T>(a.n, a.mrow, a.binv, a.spec, a.firstm, blockIdx.x);
+}
+template <typename T>
+__global__ void __launch_bounds__(BAND_TPB) k_band_gemv_multi(const __grid_constant__ ArgPack<BandGemvArgs<T>> p) {
+  const BandGemvArgs<T>& a = p.a[blockIdx.y];
+  if ((int)blockIdx.x >= a.rank) return;
+  if (!gate_open(a.gate)) return;
+  band_gemv_body<T>(a.m, a.M, a.firstm, a.c, blockIdx.x);
+}
+template <typename T>
+__global__ void __launch_bounds__(BAND_COLS * BAND_ROWT) k_band_fwd_solve_multi(
+    const __grid_constant__ ArgPack<BandFwdArgs<T>> p) {
+  const BandFwdArgs<T>& a = p.a[blockIdx.y];
+  if ((int)blockIdx.x >= a.nblk) return;
+  if (!gate_open(a.gate)) return;
+  band_fwd_solve_body<T>(a.nb, a.n, a.rank, a.bptr, a.bperm, a.c, a.bfwd, a.gamma, a.scale, a.bpiv, a.band,
+                         blockIdx.x);
+}
+template <int KIND, bool RES_F32>
+__global__ void k_residual_multi(const __grid_constant__ ArgPack<ResidualArgs> p) {
+  const ResidualArgs& a = p.a[blockIdx.y];
+  if ((int)blockIdx.x >= a.nblk) return;
+  if (!gate_open(a.gate)) return;
+  residual_body<KIND, RES_F32>(a.c, a.rc, a.b, a.x, a.res, a.sc, a.check, a.first, blockIdx.x, a.nblk);
+}
+__global__ void k_pressure_bound_multi(const __grid_constant__ ArgPack<BoundArgs> p) {
+  const BoundArgs& a = p.a[blockIdx.y];
+  if ((int)blockIdx.x >= a.nblk) return;
+  if (!gate_open(a.gate)) return;
+  pressure_bound_body(a.c, a.rc, a.b, a.x, a.sc, a.nchk, blockIdx.x, a.nblk);
+}
+__global__ void k_refine_decide_multi(const __grid_constant__ ArgPack<StepCtl*> ctls, int n, int slot, int nchk,
+                                      cudaGraphConditionalHandle cond) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  for (int c = threadIdx.x; c < n; c += blockDim.x) {
+    StepCtl* ctl = ctls.a[c];
+    SolveCtl* sc = &ctl->solve[slot];
+    const int k = sc->k;
+    bool need = false;
+    if (!ctl->err) need = bits2d(sc->rmax[k]) > inner_target(sc) && k + 1 < nchk;
+    if (need) {
+      sc->k = k + 1;
+      atomicOr(&any, 1);
+    }
+    sc->act = need ? 1 : 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) cudaGraphSetConditional(cond, any ? 1u : 0u);
+}
+
+template <typename T, typename TI, typename TO>
+XpassArgs<T, TI, TO> xpass_args(const TransformTables& tt, bool inverse, int r0, int nr, const TI* in, int64_t ibase,
+                                int64_t ipitch, const uint8_t* icls, TO* out, int64_t obase, int64_t opitch,
+                                const uint8_t* ocls, const double* add, const YCorr<T>& corr, const Gate& gate) {
+  using Cx = cplx<T>;
+  XpassArgs<T, TI, TO> a{};
+  a.n = tt.n;
+  a.r0 = r0;
+  a.nr = nr;
+  a.type = inverse ? tt.tx_inv : tt.tx_fwd;
+  a.plan = tt.plan_x;
+  a.tb = R2RTables<T>{(const Cx*)tt.Wx, (const Cx*)(inverse ? tt.prex_inv : tt.prex),
+                      (const Cx*)(inverse ? tt.postx_inv : tt.postx)};
+  a.in = in;
+  a.ibase = ibase;
+  a.ipitch = ipitch;
+  a.icls = icls;
+  a.out = out;
+  a.obase = obase;
+  a.opitch = opitch;
+  a.ocls = ocls;
+  a.add = add;
+  a.corr = corr;
+  a.gthreads = tt.xg_threads;
+  a.gpb = tt.xg_pb;
+  a.gate = gate;
+  const int per_block = tt.xg_pb * (r2r_paired(a.type) ? 2 : 1);
+  a.nblk = (nr + per_block - 1) / per_block;
+  return a;
+}
+template <typename T>
+YsolveArgs<T> ysolve_args(const TransformTables& tt, int cols, int rows, T* S, const Gate& gate) {
+  YsolveArgs<T> a{};
+  a.rows = rows;
+  a.cols = cols;
+  a.ch = tt.ych;
+  a.gamma = (T)tt.gamma;
+  a.scale = (T)tt.yscale;
+  a.t0 = (const T*)tt.t0;
+  a.t1 = (const T*)tt.t1;
+  a.t2 = (const T*)tt.t2;
+  a.S = S;
+  a.gate = gate;
+  a.nblk = (cols + tt.lpb_y - 1) / tt.lpb_y;
+  return a;
+}
+ResidualArgs residual_args(const CaseDev& c, const ResidualCoef& rc, int kind, const double* b, const double* x,
+                           void* res, SolveCtl* sc, int check, bool first_check, const Gate& gate) {
+  ResidualArgs a{};
+  a.c = c;
+  a.rc = rc;
+  a.b = b;
+  a.x = x;
+  a.res = res;
+  a.sc = sc;
+  a.check = check;
+  a.first = first_check ? 1 : 0;
+  a.gate = gate;
+  a.nblk = (int)reduce_blocks(kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize));
+  return a;
+}
+BoundArgs bound_args(const CaseDev& c, const ResidualCoef& rc, const double* b, const double* x, SolveCtl* sc,
+                     int nchk, const Gate& gate) {
+  BoundArgs a{};
+  a.c = c;
+  a.rc = rc;
+  a.b = b;
+  a.x = x;
+  a.sc = sc;
+  a.nchk = nchk;
+  a.gate = gate;
+  a.nblk = (int)reduce_blocks(c.psize);
+  return a;
+}
+
+static_assert(sizeof(ArgPack<ResidualArgs>) <= 32000 && sizeof(ArgPack<BoundArgs>) <= 32000 &&
+                  sizeof(ArgPack<YsolveArgs<double>>) <= 32000 &&
+                  sizeof(ArgPack<XpassArgs<double, double, double>>) <= 32000,
+              "case-indexed argument packs must fit the kernel parameter space");
+template <typename A>
+static unsigned max_blocks(const ArgPack<A>& p, int n) {
+  int m = 0;
+  for (int c = 0; c < n; ++c) m = std::max(m, p.a[c].nblk);
+  return (unsigned)std::max(m, 1);
+}
+template <typename T, typename TI, typename TO>
+void launch_xpass_multi(const ArgPack<XpassArgs<T, TI, TO>>& p, int n, const TransformTables& tt0, cudaStream_t st) {
+  if (n <= 0) return;
+  note_launch();
+  k_xpass_multi<T, TI, TO><<<dim3(max_blocks(p, n), (unsigned)n), tt0.xg_threads * tt0.xg_pb, tt0.smem_x, st>>>(p);
+}
+template <typename T>
+void launch_ysolve_multi(const ArgPack<YsolveArgs<T>>& p, int n, const TransformTables& tt0, cudaStream_t st) {
+  if (n <= 0) return;
+  note_launch();
+  const dim3 g(max_blocks(p, n), (unsigned)n);
+  switch (tt0.lpb_y) {
+    case 2: k_ysolve_multi<T, 2><<<g, tt0.threads_y, tt0.smem_y, st>>>(p); break;
+    case 4: k_ysolve_multi<T, 4><<<g, tt0.threads_y, tt0.smem_y, st>>>(p); break;
+    case 8: k_ysolve_multi<T, 8><<<g, tt0.threads_y, tt0.smem_y, st>>>(p); break;
+    default: k_ysolve_multi<T, 16><<<g, tt0.threads_y, tt0.smem_y, st>>>(p); break;
+  }
+}
+template <typename T>
+void launch_band_first_multi(const ArgPack<BandFirstArgs<T>>& p, int n, cudaStream_t st) {
+  if (n <= 0) return;
+  int m = 1;
+  for (int c = 0; c < n; ++c) m = std::max(m, p.a[c].m);
+  note_launch();
+  k_band_first_multi<T><<<dim3((unsigned)m, (unsigned)n), BAND_TPB, 0, st>>>(p);
+}
+template <typename T>
+void launch_band_gemv_multi(const ArgPack<BandGemvArgs<T>>& p, int n, cudaStream_t st) {
+  if (n <= 0) return;
+  int r = 1;
+  for (int c = 0; c < n; ++c) r = std::max(r, p.a[c].rank);
+  note_launch();
+  k_band_gemv_multi<T><<<dim3((unsigned)r, (unsigned)n), BAND_TPB, 0, st>>>(p);
+}
+template <typename T>
+void launch_band_fwd_solve_multi(const ArgPack<BandFwdArgs<T>>& p, int n, cudaStream_t st) {
+  if (n <= 0) return;
+  size_t smem = 0;
+  for (int c = 0; c < n; ++c) smem = std::max(smem, band_fwd_smem(p.a[c].nb, p.a[c].rank, sizeof(T) == 4));
+  note_launch();
+  k_band_fwd_solve_multi<T><<<dim3(max_blocks(p, n), (unsigned)n), BAND_COLS * BAND_ROWT, smem, st>>>(p);
+}
+void launch_residual_multi(const ArgPack<ResidualArgs>& p, int n, int kind, bool res_f32, cudaStream_t st) {
+  if (n <= 0) return;
+  note_launch();
+  const dim3 g(max_blocks(p, n), (unsigned)n);
+  if (res_f32) {
+    if (kind == 0) k_residual_multi<0, true><<<g, TPB, 0, st>>>(p);
+    else if (kind == 1) k_residual_multi<1, true><<<g, TPB, 0, st>>>(p);
+    else k_residual_multi<2, true><<<g, TPB, 0, st>>>(p);
+  } else {
+    if (kind == 0) k_residual_multi<0, false><<<g, TPB, 0, st>>>(p);
+    else if (kind == 1) k_residual_multi<1, false><<<g, TPB, 0, st>>>(p);
+    else k_residual_multi<2, false><<<g, TPB, 0, st>>>(p);
+  }
+}
+void launch_pressure_bound_multi(const ArgPack<BoundArgs>& p, int n, cudaStream_t st) {
+  if (n <= 0) return;
+  note_launch();
+  k_pressure_bound_multi<<<dim3(max_blocks(p, n), (unsigned)n), TPB, 0, st>>>(p);
+}
+void launch_refine_decide_multi(const ArgPack<StepCtl*>& ctls, int n, int slot, int nchk,
+                                cudaGraphConditionalHandle cond, cudaStream_t st) {
+  note_launch();
+  k_refine_decide_multi<<<1, 32, 0, st>>>(ctls, n, slot, nchk, cond);
+}
+
+#define GM_XPASS_MULTI(T, TI, TO)                                                                                   \
+  template XpassArgs<T, TI, TO> xpass_args<T, TI, TO>(const TransformTables&, bool, int, int, const TI*, int64_t, \
+                                                      int64_t, const uint8_t*, TO*, int64_t, int64_t,             \
+                                                      const uint8_t*, const double*, const YCorr<T>&, const Gate&); \
+  template void launch_xpass_multi<T, TI, TO>(const ArgPack<XpassArgs<T, TI, TO>>&, int, const TransformTables&,   \
+                                              cudaStream_t);
+GM_XPASS_MULTI(double, double, double)
+GM_XPASS_MULTI(float, double, float)
+GM_XPASS_MULTI(float, float, float)
+GM_XPASS_MULTI(float, float, double)
+#undef GM_XPASS_MULTI
+template YsolveArgs<double> ysolve_args<double>(const TransformTables&, int, int, double*, const Gate&);
+template YsolveArgs<float> ysolve_args<float>(const TransformTables&, int, int, float*, const Gate&);
+template void launch_ysolve_multi<double>(const ArgPack<YsolveArgs<double>>&, int, const TransformTables&,
+                                          cudaStream_t);
+template void launch_ysolve_multi<float>(const ArgPack<YsolveArgs<float>>&, int, const TransformTables&,
+                                         cudaStream_t);
+template void launch_band_first_multi<double>(const ArgPack<BandFirstArgs<double>>&, int, cudaStream_t);
+template void launch_band_first_multi<float>(const ArgPack<BandFirstArgs<float>>&, int, cudaStream_t);
+template void launch_band_gemv_multi<double>(const ArgPack<BandGemvArgs<double>>&, int, cudaStream_t);
+template void launch_band_gemv_multi<float>(const ArgPack<BandGemvArgs<float>>&, int, cudaStream_t);
+template void launch_band_fwd_solve_multi<double>(const ArgPack<BandFwdArgs<double>>&, int, cudaStream_t);
+template void launch_band_fwd_solve_multi<float>(const ArgPack<BandFwdArgs<float>>&, int, cudaStream_t);
 
 }  // namespace gmk

@@ -35,7 +35,7 @@ struct SolveCtl {
   int k;                              // current check index (graph-driven refinement loop)
   int gk1;                            // GMRES path: final check index + 1 (0: direct path)
   int gits;                           // GMRES path: Krylov iterations of the solve
-  int pad_;
+  int act;                            // case-indexed refinement loop: this case sweeps again
 };
 
 // Per-step control and diagnostics, one per step in flight.
@@ -132,12 +132,14 @@ __device__ __forceinline__ int last_check(const SolveCtl* s, int nchk) {
 struct Gate {
   StepCtl* ctl;    // error flag lives here (nullptr: always run)
   int slot;        // solve slot for sweep gating
-  int sweep;       // 0: unconditional, k: run only if sweep k is needed
+  int sweep;       // 0: unconditional, k: run only if sweep k is needed, -1: only while the
+                   // case-indexed refinement loop marks the solve active
 };
 __device__ __forceinline__ bool gate_open_thread(const Gate& g) {
   if (!g.ctl) return true;
   if (*(volatile int*)&g.ctl->err) return false;
   if (g.sweep == 0) return true;
+  if (g.sweep < 0) return *(volatile int*)&g.ctl->solve[g.slot].act != 0;
   return sweep_needed(&g.ctl->solve[g.slot], g.sweep);
 }
 // Block-uniform gate: thread 0 decides, every thread of the block gets the same answer
@@ -282,7 +284,9 @@ template <typename T>
 void launch_band_fwd_solve(const TransformTables& tt, int n, int rank, const int32_t* bptr, const int32_t* bperm,
                            const double* c, const T* bfwd, T* band, const Gate& gate, cudaStream_t st);
 // shared memory of launch_band_fwd_solve (the direct path needs it within the default 48 KB)
+// and its blocks for n columns
 size_t band_fwd_smem(int nb, int rank, bool fp32);
+int band_fwd_blocks(int n);
 // boundary Schur term c = M first[mcols] (M = S^{-1} C), written to w2 at the boundary rows
 template <typename TF>
 void launch_schur(const TF* first, int rank, int m, const int64_t* mcols, const double* M, const int64_t* rows,
@@ -408,5 +412,123 @@ void launch_set_inlet(const CaseDev& c, double* U, bool zero, cudaStream_t st);
 // fluid-cell divergence statistics on a mask (mac_engine diagnostic)
 void launch_divergence_stats(const CaseDev& c, const double* U, const uint8_t* mask, double* out5,
                              cudaStream_t st);
+
+// ---- case-indexed launches (many cases of one grid shape per launch) --------
+// The arguments of every case travel in the kernel's parameter space (up to GM_PACK cases);
+// blockIdx.y selects the case and blocks past a case's own grid return at once.  Every case of
+// one launch has the same block shape and shared-memory size (the cases of a batch group share
+// nx, ny and the precision, and their launch shapes are made equal).
+static constexpr int GM_PACK = 32;
+template <typename A>
+struct ArgPack {
+  A a[GM_PACK];
+};
+
+template <typename T, typename TI, typename TO>
+struct XpassArgs {
+  int n, r0, nr, type;
+  FftPlan plan;
+  R2RTables<T> tb;
+  const TI* in;
+  int64_t ibase, ipitch;
+  const uint8_t* icls;
+  TO* out;
+  int64_t obase, opitch;
+  const uint8_t* ocls;
+  const double* add;
+  YCorr<T> corr;
+  int gthreads, gpb;
+  Gate gate;
+  int nblk;
+};
+template <typename T>
+struct YsolveArgs {
+  int rows, cols;
+  YChunks ch;
+  T gamma, scale;
+  const T* t0; const T* t1; const T* t2;
+  T* S;
+  Gate gate;
+  int nblk;
+};
+template <typename T>
+struct BandFirstArgs {
+  int m, n;
+  const int32_t* mrow;
+  const T* binv;
+  const T* spec;
+  T* firstm;
+  Gate gate;
+};
+template <typename T>
+struct BandGemvArgs {
+  int rank, m;
+  const double* M;
+  const T* firstm;
+  double* c;
+  Gate gate;
+};
+template <typename T>
+struct BandFwdArgs {
+  int nb, n, rank;
+  const int32_t* bptr; const int32_t* bperm;
+  const double* c;
+  const T* bfwd;
+  T gamma, scale;
+  const T* bpiv;
+  T* band;
+  Gate gate;
+  int nblk;
+};
+struct ResidualArgs {
+  CaseDev c;
+  ResidualCoef rc;
+  const double* b; const double* x;
+  void* res;
+  SolveCtl* sc;
+  int check, first;
+  Gate gate;
+  int nblk;
+};
+struct BoundArgs {
+  CaseDev c;
+  ResidualCoef rc;
+  const double* b; const double* x;
+  SolveCtl* sc;
+  int nchk;
+  Gate gate;
+  int nblk;
+};
+
+// argument builders: the same conventions as the single-case launchers above
+template <typename T, typename TI, typename TO>
+XpassArgs<T, TI, TO> xpass_args(const TransformTables& tt, bool inverse, int r0, int nr, const TI* in, int64_t ibase,
+                                int64_t ipitch, const uint8_t* icls, TO* out, int64_t obase, int64_t opitch,
+                                const uint8_t* ocls, const double* add, const YCorr<T>& corr, const Gate& gate);
+template <typename T>
+YsolveArgs<T> ysolve_args(const TransformTables& tt, int cols, int rows, T* S, const Gate& gate);
+ResidualArgs residual_args(const CaseDev& c, const ResidualCoef& rc, int kind, const double* b, const double* x,
+                           void* res, SolveCtl* sc, int check, bool first_check, const Gate& gate);
+BoundArgs bound_args(const CaseDev& c, const ResidualCoef& rc, const double* b, const double* x, SolveCtl* sc,
+                     int nchk, const Gate& gate);
+// launchers over the first n cases of a pack (tt0: the launch shape shared by the cases)
+template <typename T, typename TI, typename TO>
+void launch_xpass_multi(const ArgPack<XpassArgs<T, TI, TO>>& p, int n, const TransformTables& tt0, cudaStream_t st);
+template <typename T>
+void launch_ysolve_multi(const ArgPack<YsolveArgs<T>>& p, int n, const TransformTables& tt0, cudaStream_t st);
+template <typename T>
+void launch_band_first_multi(const ArgPack<BandFirstArgs<T>>& p, int n, cudaStream_t st);
+template <typename T>
+void launch_band_gemv_multi(const ArgPack<BandGemvArgs<T>>& p, int n, cudaStream_t st);
+template <typename T>
+void launch_band_fwd_solve_multi(const ArgPack<BandFwdArgs<T>>& p, int n, cudaStream_t st);
+void launch_residual_multi(const ArgPack<ResidualArgs>& p, int n, int kind, bool res_f32, cudaStream_t st);
+void launch_pressure_bound_multi(const ArgPack<BoundArgs>& p, int n, cudaStream_t st);
+// Refinement decision of a WHILE node over n cases: each case whose check sc->k exceeded its
+// inner target (and may refine again) advances sc->k and is marked active (SolveCtl::act); the
+// condition is set while any case is active.  Kernels gated with Gate::sweep = -1 run for
+// active cases only.
+void launch_refine_decide_multi(const ArgPack<StepCtl*>& ctls, int n, int slot, int nchk,
+                                cudaGraphConditionalHandle cond, cudaStream_t st);
 
 }  // namespace gmk
