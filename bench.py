@@ -54,6 +54,12 @@ BATCH_WORKLOADS = {
     'sweep64_batch': dict(batch=64, seed=0, dt=0.002, h=0.05, grids=((256, 128), (400, 200), (800, 410)),
                           re=(40.0, 200.0), diameter=(0.8, 1.2), jitter=0.5, amp=1e-3),
 }
+# periodic Taylor-Green vortex on [0, 2 pi]^2 (verification/taylor_green.py), nu = 0.01, dt = 1e-3,
+# 1000 steps to t = 1 for the error check (the timed steps are --steps of them)
+TG_WORKLOADS = {
+    'taylor_green_1024': dict(n=1024, nu=0.01, dt=1e-3, end_time=1.0),
+    'taylor_green_256': dict(n=256, nu=0.01, dt=1e-3, end_time=1.0),
+}
 DEFAULT_WORKLOAD = 'wide_800x820_re100'
 # DRAM bytes (read + write) per launch of the dominant kernel class, averaged over the launches
 # of one ncu --set full capture of the same command (the capture's file under profiles/ gives the
@@ -238,6 +244,17 @@ def run_reference(args, w, rank):
     if rank != 0:
         return
     workers = os.cpu_count() or 1
+    if args.workload in TG_WORKLOADS:
+        rate, done, el = oracle_tg_rate(w, 60.0)
+        line = dict(metric=METRIC, value=rate, unit='cell-updates/s', n_gpus=args.gpus, steps=done,
+                    warmup=args.warmup, ms_per_step=el / max(done, 1) * 1e3, higher_is_better=True, scaling='weak',
+                    vs_baseline=None, dtype='f64', data='synthetic (analytic field)', impl='reference',
+                    config=dict(workload=args.workload, grid=f"{w['n']}x{w['n']}", dt=w['dt'], precision='fp64'),
+                    cpu_baseline=dict(value=rate, unit='cell-updates/s', cores=1, kind='port',
+                                      sample=f'{done} Taylor-Green steps at n={w["n"]} (set-up excluded)'),
+                    e2e=dict(value=rate, unit='cell-updates/s', h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+        print(json.dumps(line), flush=True)
+        return
     if 'batch' in w:
         rate, done, cells, el = oracle_batch_rate(w, 60.0, workers)
         line = dict(metric=METRIC, value=rate, unit='cell-updates/s', n_gpus=args.gpus, steps=done,
@@ -429,6 +446,82 @@ def run_ours(args, w, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def oracle_tg_rate(w, seconds):
+    """Cell-updates/s of the CPU oracle's Taylor-Green step (numpy/scipy, one thread per FFT
+    call as scipy runs it) over a bounded number of steps after the start-up step."""
+    sys.path.insert(0, str(ROOT / 'oracle'))
+    import ghost_oracle as go
+    n, dt = w['n'], w['dt']
+    done, el = 0, 0.0
+    k = 2
+    while el < seconds and k <= 64:
+        t0 = time.perf_counter()
+        go.taylor_green_run(n, dt, end_time=k * dt, nu=w['nu'])
+        el1 = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        go.taylor_green_run(n, dt, end_time=(2 * k) * dt, nu=w['nu'])
+        el2 = time.perf_counter() - t0
+        done, el = k, max(el2 - el1, 1e-9)  # k more steps; set-up and start-up cancel
+        k *= 2
+    return n * n * done / el, done, el
+
+
+def run_ours_tg(args, w, rank, world):
+    """Periodic Taylor-Green step (config 2): K steps timed, and the full run to end_time in
+    this precision and in FP64 for the error norms against the analytic solution."""
+    import torch
+    pkg = load_package()
+    tg = pkg.taylor_green
+    n, nu, dt = w['n'], w['nu'], w['dt']
+    case = tg.TaylorGreen(n, nu, args.precision)
+    q0, p0 = tg.exact(n, nu, 0.0)
+    case.set_state(q0, p0)
+    case.step(dt, max(args.warmup, 3))
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = pkg._lib.lib.gm_kernel_launches()
+    with ClockSampler(int(os.environ.get('LOCAL_RANK', 0))) as clocks:
+        t0 = time.perf_counter()
+        case.step(dt, args.steps)  # one call: the library synchronises its stream before returning
+        el = time.perf_counter() - t0
+    launches = pkg._lib.lib.gm_kernel_launches() - launches0
+    case.close()
+    step_ms = el * 1e3 / args.steps
+    if world > 1:
+        t = torch.tensor([step_ms], device='cuda')
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+    cells = n * n
+    # end to end through taylor_green.run (host arrays in and out) to end_time, both precisions
+    t0 = time.perf_counter()
+    info, _, _ = tg.run(n, dt, w['end_time'], nu, args.precision)
+    e2e_s = time.perf_counter() - t0
+    steps_total = round(w['end_time'] / dt)
+    info64 = info if args.precision == 'fp64' else tg.run(n, dt, w['end_time'], nu, 'fp64')[0]
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, done, cel = oracle_tg_rate(w, 10.0)
+        cpu = dict(value=rate, unit='cell-updates/s', cores=1, kind='port',
+                   sample=f'{done} Taylor-Green steps at n={n} ({cel:.1f} s, set-up and start-up excluded)')
+    if rank == 0:
+        line = dict(metric=METRIC, value=cells * world / (step_ms * 1e-3), unit='cell-updates/s', n_gpus=world,
+                    steps=args.steps, warmup=args.warmup, ms_per_step=step_ms, higher_is_better=True,
+                    scaling='weak', vs_baseline=None,
+                    dtype='f64' if args.precision == 'fp64' else 'f32+f64-refine', data='synthetic (analytic field)',
+                    config=dict(workload=args.workload, grid=f'{n}x{n}', nu=nu, dt=dt,
+                                precision=args.precision, parallelism='replicas',
+                                timing='host wall clock around one synchronous K-step call',
+                                l2='working set (fields and FFT scratch) near the L2 size; not flushed'),
+                    roofline=None, cpu_baseline=cpu,
+                    e2e=dict(value=cells * steps_total / e2e_s, unit='cell-updates/s',
+                             h2d_bytes_per_step=8 * 3 * cells / steps_total, d2h_bytes_per_step=8 * 4 * cells / steps_total),
+                    clocks=clocks.summary(), gpu_launches=int(launches),
+                    taylor_green=dict(end_time=w['end_time'], steps=steps_total, errors=info,
+                                      errors_fp64=info64))
+        print(json.dumps(line), flush=True)
+
+
 def run_ours_batch(args, w, rank, world):
     """Batched sweep: all cases advance together, one graph launch per step."""
     import torch
@@ -557,7 +650,8 @@ def main():
     ap.add_argument('--steps', type=int, default=200)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
-    ap.add_argument('--workload', choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument('--workload', choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(TG_WORKLOADS),
+                    default=DEFAULT_WORKLOAD)
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
     ap.add_argument('--no-compare', action='store_true', help='skip timing the plain FP64 step beside the FP32 mode')
     ap.add_argument('--precision', choices=('fp64', 'fp32'), default='fp64',
@@ -565,7 +659,7 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    w = WORKLOADS.get(args.workload) or BATCH_WORKLOADS[args.workload]
+    w = WORKLOADS.get(args.workload) or BATCH_WORKLOADS.get(args.workload) or TG_WORKLOADS[args.workload]
     world = int(os.environ.get('WORLD_SIZE', 1))
     rank = int(os.environ.get('RANK', 0))
     if args.impl == 'reference':
@@ -578,6 +672,8 @@ def main():
         dist.init_process_group('nccl')
     if args.workload in BATCH_WORKLOADS:
         run_ours_batch(args, w, rank, world)
+    elif args.workload in TG_WORKLOADS:
+        run_ours_tg(args, w, rank, world)
     else:
         run_ours(args, w, rank, world)
     if world > 1:

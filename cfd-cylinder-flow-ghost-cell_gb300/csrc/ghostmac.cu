@@ -421,25 +421,30 @@ void autotune_shapes(gm_handle* h, RectDev& rd, int kind, bool fp32) {
   tt.xg_threads = bt;
   tt.xg_pb = bg;
   tt.smem_x = tabs + per * bg;
-  // column solve
+  // column solve: L columns per block and the block's threads (at least L x P: one per chunk in
+  // the solve phases; more threads only shorten the load and store phases)
   best = 1e30f;
-  int bl = 0;
+  int bl = 0, bthr = 0;
   for (int L : {2, 4, 8, 16}) {
-    const int thr = ((L * tt.ych.P + 31) / 32) * 32;
+    const int base = ((L * tt.ych.P + 31) / 32) * 32;
     const size_t sm = ysolve_smem(v.rows, L, fp32);
-    if (thr > 1024 || sm > h->smem_optin) continue;
-    tt.lpb_y = L;
-    tt.threads_y = thr;
-    tt.smem_y = sm;
-    float ms = time_ms([&] {
-      if (fp32) launch_ysolve<float>(tt, v.cols, v.rows, h->spectral32.p, open, st);
-      else launch_ysolve<double>(tt, v.cols, v.rows, h->spectral.p, open, st);
-    });
-    if (ms < best) { best = ms; bl = L; }
+    if (base > 1024 || sm > h->smem_optin) continue;
+    for (int want : {0, 256, 512, 1024}) {
+      const int thr = std::max(base, want);
+      if (thr > 1024 || (want > 0 && thr == base)) continue;
+      tt.lpb_y = L;
+      tt.threads_y = thr;
+      tt.smem_y = sm;
+      float ms = time_ms([&] {
+        if (fp32) launch_ysolve<float>(tt, v.cols, v.rows, h->spectral32.p, open, st);
+        else launch_ysolve<double>(tt, v.cols, v.rows, h->spectral.p, open, st);
+      });
+      if (ms < best) { best = ms; bl = L; bthr = thr; }
+    }
   }
   if (bl == 0) throw CudaError("separable inverse does not fit the launch limits");
   tt.lpb_y = bl;
-  tt.threads_y = ((tt.lpb_y * tt.ych.P + 31) / 32) * 32;
+  tt.threads_y = bthr;
   tt.smem_y = ysolve_smem(v.rows, bl, fp32);
   CK(cudaEventDestroy(e0));
   CK(cudaEventDestroy(e1));

@@ -738,7 +738,7 @@ __global__ void __launch_bounds__(BAND_TPB) k_band_gemv(int rank, int m, const d
 // row transform of U c on band rows jt, jt + BAND_ROWT, ... of column k (a sum over that row's
 // boundary values, c staged in shared memory), scaled; then one thread per column runs the band
 // system (as k_yband) in shared memory, and all threads write the band back.
-static constexpr int BAND_COLS = 32, BAND_ROWT = 8;
+static constexpr int BAND_COLS = 16, BAND_ROWT = 16;
 template <typename T>
 __device__ __forceinline__ void band_fwd_solve_body(int nb, int n, int rank, const int32_t* __restrict__ bptr,
                                                     const int32_t* __restrict__ bperm, const double* __restrict__ c,
