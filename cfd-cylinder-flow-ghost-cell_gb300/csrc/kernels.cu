@@ -4,6 +4,8 @@
 #include <vector>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
+#include <utility>
 
 #include "kernels.cuh"
 
@@ -76,6 +78,34 @@ __device__ void block_commit_sum_f32(float v, double* dst) {
 }
 // |v| as bits with the sign bit cleared (integer pipe; fabs on a double may issue on the FP64 pipe)
 __device__ __forceinline__ unsigned long long absbits(double v) { return dbits(v) & 0x7fffffffffffffffull; }
+
+// Launch as a programmatic dependent of the previous kernel on the stream (its launch overlaps
+// that kernel's end; the kernel's gate_open waits for it with griddepcontrol.wait before any
+// read).  Used for the kernels of the solve sweeps, which all begin with gate_open.
+// GHOSTMAC_NO_PDL=1 launches them as ordinary stream successors.
+static int pdl_mode() {
+  static int mode = -1;
+  if (mode < 0) {
+    const char* e = std::getenv("GHOSTMAC_NO_PDL");
+    mode = (e && e[0] == '1') ? 0 : 1;
+  }
+  return mode;
+}
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = pdl_mode();
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 static inline unsigned blocks_for(int64_t n, int tpb = TPB) { return (unsigned)((n + tpb - 1) / tpb); }
 // Grid of the reduction kernels: grid-stride loops over at most 4 blocks per SM of a GB300,
@@ -318,9 +348,9 @@ void launch_xpass(const TransformTables& tt, bool inverse, int r0, int nr, const
   const unsigned grid = (unsigned)((nr + per_block - 1) / per_block);
   note_launch();
   kt_mark(1, st);
-  k_xpass<T, TI, TO><<<grid, tt.xg_threads * tt.xg_pb, tt.smem_x, st>>>(
-      tt.n, r0, nr, type, tt.plan_x, tb, in, ibase, ipitch, icls, out, obase, opitch, ocls, add, corr,
-      tt.xg_threads, tt.xg_pb, gate);
+  launch_pdl(k_xpass<T, TI, TO>, dim3(grid), dim3(tt.xg_threads * tt.xg_pb), tt.smem_x, st, tt.n, r0, nr, type,
+             tt.plan_x, tb, in, ibase, ipitch, icls, out, obase, opitch, ocls, add, corr, tt.xg_threads, tt.xg_pb,
+             gate);
   // algorithmic bytes: one read and one write per point, class maps, the added field and the
   // correction band (tables of the decay factors once per point)
   kt_mark(1, st, (double)nr * tt.n * (sizeof(TI) + sizeof(TO) + (icls ? 1 : 0) + (ocls ? 1 : 0) + (add ? 8 : 0) +
@@ -470,8 +500,8 @@ void launch_ysolve(const TransformTables& tt, int cols, int rows, T* S, const Ga
   note_launch();
   kt_mark(2, st);
 #define GM_YSOLVE(LL)                                                                                        \
-  k_ysolve<T, LL><<<gy, tt.threads_y, tt.smem_y, st>>>(rows, cols, tt.ych, (T)tt.gamma, (T)tt.yscale,       \
-                                                       (const T*)tt.t0, (const T*)tt.t1, (const T*)tt.t2, S, gate)
+  launch_pdl(k_ysolve<T, LL>, dim3(gy), dim3(tt.threads_y), tt.smem_y, st, rows, cols, tt.ych, (T)tt.gamma,     \
+             (T)tt.yscale, (const T*)tt.t0, (const T*)tt.t1, (const T*)tt.t2, S, gate)
   switch (tt.lpb_y) {
     case 2: GM_YSOLVE(2); break;
     case 4: GM_YSOLVE(4); break;
@@ -657,44 +687,52 @@ __device__ __forceinline__ T warp_sum_t(T v) {
   return v;
 }
 
-// Block-wide sum of one value per thread (blockDim a multiple of 32, at most 1024); the total
-// is returned to every thread.
-template <typename T>
-__device__ __forceinline__ T block_sum_all(T v) {
-  __shared__ T part[32];
-  v = warp_sum_t<T>(v);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  __syncthreads();
-  if (lane == 0) part[wid] = v;
-  __syncthreads();
-  T t = 0;
-  for (int w = 0; w < nw; ++w) t += part[w];
-  return t;
-}
-
 static constexpr int BAND_TPB = 128;   // threads per output of the direct sums
 static constexpr int BAND_ITEMS = 16;  // loads in flight per thread (n <= BAND_TPB * BAND_ITEMS per pass)
+
+// Canonical order of the direct sums (every kernel that forms them uses it, so the single-case,
+// fused and case-indexed paths agree bitwise): BAND_TPB threads per output, thread t adds its
+// products at t, t + BAND_TPB, ... in order, then the warp sums, then the BAND_TPB / 32 warp
+// partials in warp order.
+template <typename TA, typename TB, typename TS>
+__device__ __forceinline__ TS band_partial(const TA* __restrict__ a, const TB* __restrict__ b, int n, int t) {
+  TS acc = 0;
+  for (int k0 = t; k0 < n; k0 += BAND_TPB * BAND_ITEMS) {
+    TA av[BAND_ITEMS];
+    TB bv[BAND_ITEMS];
+#pragma unroll
+    for (int u = 0; u < BAND_ITEMS; ++u) {
+      const int k = k0 + u * BAND_TPB;
+      av[u] = k < n ? a[k] : (TA)0;
+      bv[u] = k < n ? b[k] : (TB)0;
+    }
+#pragma unroll
+    for (int u = 0; u < BAND_ITEMS; ++u) acc += cvt_to<TS>(av[u]) * cvt_to<TS>(bv[u]);
+  }
+  return acc;
+}
+// sum of a BAND_TPB-thread group's partials (part: BAND_TPB / 32 shared slots of this group);
+// every thread of the block must call it (it holds block barriers)
+template <typename T>
+__device__ __forceinline__ T band_group_sum(T v, T* part, int t) {
+  v = warp_sum_t<T>(v);
+  __syncthreads();
+  if ((t & 31) == 0) part[t >> 5] = v;
+  __syncthreads();
+  T s = 0;
+#pragma unroll
+  for (int w = 0; w < BAND_TPB / 32; ++w) s += part[w];
+  return s;
+}
 
 // One block per point: the inverse row transform of its spectrum row evaluated at its column
 // (coefficients in binv), all of a thread's products loaded before they are summed.
 template <typename T>
 __device__ __forceinline__ void band_first_body(int n, const int32_t* __restrict__ mrow, const T* __restrict__ binv,
                                                 const T* __restrict__ spec, T* __restrict__ firstm, int q) {
-  const T* b = binv + (int64_t)q * n;
-  const T* sp = spec + (int64_t)mrow[q] * n;
-  T acc = 0;
-  for (int k0 = threadIdx.x; k0 < n; k0 += BAND_TPB * BAND_ITEMS) {
-    T bv[BAND_ITEMS], sv[BAND_ITEMS];
-#pragma unroll
-    for (int u = 0; u < BAND_ITEMS; ++u) {
-      const int k = k0 + u * BAND_TPB;
-      bv[u] = k < n ? b[k] : (T)0;
-      sv[u] = k < n ? sp[k] : (T)0;
-    }
-#pragma unroll
-    for (int u = 0; u < BAND_ITEMS; ++u) acc += bv[u] * sv[u];
-  }
-  const T v = block_sum_all<T>(acc);
+  __shared__ T part[BAND_TPB / 32];
+  const T v = band_group_sum<T>(
+      band_partial<T, T, T>(binv + (int64_t)q * n, spec + (int64_t)mrow[q] * n, n, threadIdx.x), part, threadIdx.x);
   if (threadIdx.x == 0) firstm[q] = v;
 }
 template <typename T>
@@ -709,21 +747,9 @@ __global__ void __launch_bounds__(BAND_TPB) k_band_first(int m, int n, const int
 template <typename T>
 __device__ __forceinline__ void band_gemv_body(int m, const double* __restrict__ M, const T* __restrict__ firstm,
                                                double* __restrict__ c, int r) {
-  const double* mr = M + (int64_t)r * m;
-  double acc = 0.0;
-  for (int q0 = threadIdx.x; q0 < m; q0 += BAND_TPB * BAND_ITEMS) {
-    double mv[BAND_ITEMS];
-    T fv[BAND_ITEMS];
-#pragma unroll
-    for (int u = 0; u < BAND_ITEMS; ++u) {
-      const int q = q0 + u * BAND_TPB;
-      mv[u] = q < m ? mr[q] : 0.0;
-      fv[u] = q < m ? firstm[q] : (T)0;
-    }
-#pragma unroll
-    for (int u = 0; u < BAND_ITEMS; ++u) acc += mv[u] * cvt_to<double>(fv[u]);
-  }
-  const double v = block_sum_all<double>(acc);
+  __shared__ double part[BAND_TPB / 32];
+  const double v = band_group_sum<double>(band_partial<double, T, double>(M + (int64_t)r * m, firstm, m, threadIdx.x),
+                                          part, threadIdx.x);
   if (threadIdx.x == 0) c[r] = v;
 }
 template <typename T>
@@ -808,7 +834,7 @@ void launch_band_first(int m, int n, const int32_t* mrow, const T* binv, const T
   if (m <= 0) return;
   note_launch();
   kt_mark(5, st);
-  k_band_first<T><<<(unsigned)m, BAND_TPB, 0, st>>>(m, n, mrow, binv, spec, firstm, gate);
+  launch_pdl(k_band_first<T>, dim3((unsigned)m), dim3(BAND_TPB), 0, st, m, n, mrow, binv, spec, firstm, gate);
   kt_mark(5, st, (double)m * n * 2 * sizeof(T));
 }
 template <typename T>
@@ -817,7 +843,7 @@ void launch_band_gemv(int rank, int m, const double* M, const T* firstm, double*
   if (rank <= 0) return;
   note_launch();
   kt_mark(5, st);
-  k_band_gemv<T><<<(unsigned)rank, BAND_TPB, 0, st>>>(rank, m, M, firstm, c, gate);
+  launch_pdl(k_band_gemv<T>, dim3((unsigned)rank), dim3(BAND_TPB), 0, st, rank, m, M, firstm, c, gate);
   kt_mark(5, st, (double)rank * m * 8 + (double)m * sizeof(T) + rank * 8.0);
 }
 template <typename T>
@@ -827,9 +853,9 @@ void launch_band_fwd_solve(const TransformTables& tt, int n, int rank, const int
   if (nb <= 0) return;
   note_launch();
   kt_mark(5, st);
-  k_band_fwd_solve<T><<<(unsigned)((n + BAND_COLS - 1) / BAND_COLS), BAND_COLS * BAND_ROWT,
-                        band_fwd_smem(nb, rank, sizeof(T) == 4), st>>>(nb, n, rank, bptr, bperm, c, bfwd, (T)tt.gamma,
-                                                                       (T)tt.yscale, (const T*)tt.bpiv, band, gate);
+  launch_pdl(k_band_fwd_solve<T>, dim3((unsigned)((n + BAND_COLS - 1) / BAND_COLS)), dim3(BAND_COLS * BAND_ROWT),
+             band_fwd_smem(nb, rank, sizeof(T) == 4), st, nb, n, rank, bptr, bperm, c, bfwd, (T)tt.gamma,
+             (T)tt.yscale, (const T*)tt.bpiv, band, gate);
   // the forward coefficients, the values c, the pivots and the band written once
   kt_mark(5, st, (double)rank * n * sizeof(T) + rank * 8.0 + (double)nb * n * 2 * sizeof(T));
 }
@@ -1278,13 +1304,13 @@ void launch_residual(const CaseDev& c, const ResidualCoef& rc, int kind, const d
   note_launch();
   kt_mark(4, st);
   if (res_f32) {
-    if (kind == 0) k_residual<0, true><<<g, TPB, 0, st>>>(c, rc, b, x, res, sc, check, fc, gate);
-    else if (kind == 1) k_residual<1, true><<<g, TPB, 0, st>>>(c, rc, b, x, res, sc, check, fc, gate);
-    else k_residual<2, true><<<g, TPB, 0, st>>>(c, rc, b, x, res, sc, check, fc, gate);
+    if (kind == 0) launch_pdl(k_residual<0, true>, dim3(g), dim3(TPB), 0, st, c, rc, b, x, res, sc, check, fc, gate);
+    else if (kind == 1) launch_pdl(k_residual<1, true>, dim3(g), dim3(TPB), 0, st, c, rc, b, x, res, sc, check, fc, gate);
+    else launch_pdl(k_residual<2, true>, dim3(g), dim3(TPB), 0, st, c, rc, b, x, res, sc, check, fc, gate);
   } else {
-    if (kind == 0) k_residual<0, false><<<g, TPB, 0, st>>>(c, rc, b, x, res, sc, check, fc, gate);
-    else if (kind == 1) k_residual<1, false><<<g, TPB, 0, st>>>(c, rc, b, x, res, sc, check, fc, gate);
-    else k_residual<2, false><<<g, TPB, 0, st>>>(c, rc, b, x, res, sc, check, fc, gate);
+    if (kind == 0) launch_pdl(k_residual<0, false>, dim3(g), dim3(TPB), 0, st, c, rc, b, x, res, sc, check, fc, gate);
+    else if (kind == 1) launch_pdl(k_residual<1, false>, dim3(g), dim3(TPB), 0, st, c, rc, b, x, res, sc, check, fc, gate);
+    else launch_pdl(k_residual<2, false>, dim3(g), dim3(TPB), 0, st, c, rc, b, x, res, sc, check, fc, gate);
   }
   kt_mark(4, st, (double)n * (8 + 8 + (res_f32 ? 4 : 8) + 1));  // x, b, res, class map
 }

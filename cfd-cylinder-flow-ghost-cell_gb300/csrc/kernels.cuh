@@ -145,6 +145,10 @@ __device__ __forceinline__ bool gate_open_thread(const Gate& g) {
 // Block-uniform gate: thread 0 decides, every thread of the block gets the same answer
 // (the error word may change while the kernel runs).
 __device__ __forceinline__ bool gate_open(const Gate& g) {
+  // A kernel launched as a programmatic dependent of the previous kernel on its stream starts
+  // before that kernel ends: wait for it (and its memory) before reading anything it wrote.
+  // Without such a launch this returns at once.
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   __shared__ int open_flag;
   if (threadIdx.x == 0) open_flag = gate_open_thread(g) ? 1 : 0;
   __syncthreads();
