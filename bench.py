@@ -9,6 +9,10 @@ MAC_CylinderFlow.solve for boundary='ghost_cell', time_scheme='ab2_cn'.
 Synthetic seeded inputs: the reference case geometry with a seeded Gaussian
 perturbation (no external data).
 
+By default the step runs in the FP32 mode (FP32 inverses and stencils, FP64 refinement to the
+reference's residual targets) and the line's `comparison` holds the plain FP64 step timed the
+same way on the same GPU; --precision fp64 times the plain step alone.
+
 Our arm prints one JSON line: device-timed throughput (CUDA events on the
 library's stream, L2 flushed between timed steps), an end-to-end figure through
 the public MAC_CylinderFlow.solve API with host arrays, the roofline of the
@@ -68,10 +72,12 @@ DEFAULT_WORKLOAD = 'wide_800x820_re100'
 DRAM_TRAFFIC = {
     # profiles/k_xpass_fp64_wide_800x820.md: (1792 + 512 + 256 + 5888) / 4
     ('wide_800x820_re100', 'fp64', 1): 2112.0,
+    # profiles/fp32_mode_wide_800x820.md: row passes of the first sweep, (2816 + 0 + 256) / 3
+    ('wide_800x820_re100', 'fp32', 1): 1024.0,
 }
 KERNEL_CLASSES = {1: 'row transforms (k_xpass)', 2: 'column solves (k_ysolve, k_yband)',
                   3: 'momentum rhs (k_momentum, k_shadow)', 4: 'operator residual (k_residual, k_pressure_bound)',
-                  5: 'boundary chain (k_band_chain; k_schur when unfused)', 6: 'projection (k_divergence, k_project_update, k_set_inlet)',
+                  5: 'boundary term (k_band_first, k_band_gemv, k_band_fwd_solve)', 6: 'projection (k_divergence, k_project_update, k_set_inlet)',
                   7: 'defect / pressure output (k_defect, k_pressure_out)', 8: 'ghost rows (k_ghost)',
                   9: 'forces / maxima (k_forces, k_maxabs)', 10: 'gates and loop control'}
 
@@ -654,7 +660,7 @@ def main():
                     default=DEFAULT_WORKLOAD)
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
     ap.add_argument('--no-compare', action='store_true', help='skip timing the plain FP64 step beside the FP32 mode')
-    ap.add_argument('--precision', choices=('fp64', 'fp32'), default='fp64',
+    ap.add_argument('--precision', choices=('fp64', 'fp32'), default='fp32',
                     help='fp64: plain FP64 method; fp32: FP32 inverses and stencils with FP64 refinement')
     args = ap.parse_args()
     if args.warmup < 3:

@@ -377,12 +377,14 @@ void autotune_shapes(gm_handle* h, RectDev& rd, int kind, bool fp32) {
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  // a shape whose launch the device refuses (threads x registers) is skipped
+  // a shape whose launch the device refuses (threads x registers) is skipped; each timing is
+  // the best of 5 runs of 4 back-to-back launches (single launches are too noisy to rank the
+  // shapes the same way in every process)
   auto time_ms = [&](auto&& body) {
     float best = 1e30f;
-    for (int rep = 0; rep < 3; ++rep) {
+    for (int rep = 0; rep < 6; ++rep) {
       CK(cudaEventRecord(e0, st));
-      body();
+      for (int k = 0; k < 4; ++k) body();
       if (cudaGetLastError() != cudaSuccess) return 1e30f;
       CK(cudaEventRecord(e1, st));
       CK(cudaEventSynchronize(e1));

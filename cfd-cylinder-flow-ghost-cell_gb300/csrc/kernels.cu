@@ -1258,8 +1258,10 @@ __device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCo
         jc = 1;
       }
       // A x = cc x + cw xw + ce xe + cy (xs + xn); Helmholtz rows carry the factors of I - c L
+      // (one add, one multiply and three fused multiply-adds, written out so that nothing else
+      // reaches the FP64 pipe)
       const double ccv = coef_cc(rc, ic, jc), cwv = coef_cw(rc, ic);
-      ax = ccv * xv + cwv * xw + rc.ce * xe + rc.cy * (xs + xn);
+      ax = fma(rc.cy, xs + xn, fma(rc.ce, xe, fma(cwv, xw, ccv * xv)));
       if (KIND == 0 && !RES_F32) {
         aabs = fabs(ccv) * fabs(xv) + rc.ce * (fabs(xw) + fabs(xe)) + rc.cy * (fabs(xs) + fabs(xn));
         nnz = c.a_nnz[t];

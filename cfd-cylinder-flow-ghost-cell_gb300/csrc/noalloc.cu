@@ -26,6 +26,10 @@
 
 #include "../../include/ghostmac.h"
 
+namespace gmk {
+void kernel_launch_adjust(long long delta);  // the library's launch counter (kernels.cu)
+}
+
 void gm_internal_set_error(const char* msg);  // defined in ghostmac.cu
 
 namespace {
@@ -140,7 +144,9 @@ int gm_divergence_stats_noalloc(const double* u, const double* v, const uint8_t*
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const long long n = (long long)nx * ny;
   const int nblocks = (int)((n + NA_THREADS - 1) / NA_THREADS);
+  gmk::kernel_launch_adjust(1);
   k_div_partials<<<nblocks, NA_THREADS, 0, st>>>(u, v, mask, nx, ny, dx, dy, scratch);
+  gmk::kernel_launch_adjust(1);
   k_div_final<<<1, 32, 0, st>>>(nblocks, scratch);
   double r[NA_FIELDS];
   cudaError_t e = cudaMemcpyAsync(r, scratch + (long long)NA_MAX_BLOCKS * NA_FIELDS, sizeof r,

@@ -24,6 +24,10 @@
 #include "fftplan.hpp"
 #include "transforms.cuh"
 
+namespace gmk {
+void kernel_launch_adjust(long long delta);  // the library's launch counter (kernels.cu)
+}
+
 namespace {
 using namespace gmk;
 
@@ -346,14 +350,21 @@ void fourier_solve(gm_tg* t, int kind, double coef, const double* b, double* x, 
   const size_t smem = sizeof(T) == 4 ? t->smem32 : t->smem;
   cplx<T>* A = reinterpret_cast<cplx<T>*>(t->cbuf_a.p);
   cplx<T>* B = reinterpret_cast<cplx<T>*>(t->cbuf_b.p);
+  gmk::kernel_launch_adjust(1);
   k_tg_to_t<T><<<grid_for(nn), PT, 0, st>>>(nn, b, rb);
+  gmk::kernel_launch_adjust(1);
   k_tg_rows<T, 0><<<n, t->threads, smem, st>>>(n, t->plan, tw, rb, A, s2, kind, (T)(t->h * t->h), (T)coef, (T)1);
   const dim3 tg((n + 31) / 32, (n + 31) / 32), tb(32, 8);
+  gmk::kernel_launch_adjust(1);
   k_tg_transpose<T><<<tg, tb, 0, st>>>(n, A, B);
+  gmk::kernel_launch_adjust(1);
   k_tg_rows<T, 1><<<n, t->threads, smem, st>>>(n, t->plan, tw, B, B, s2, kind, (T)(t->h * t->h), (T)coef, (T)1);
+  gmk::kernel_launch_adjust(1);
   k_tg_transpose<T><<<tg, tb, 0, st>>>(n, B, A);
+  gmk::kernel_launch_adjust(1);
   k_tg_rows<T, 2><<<n, t->threads, smem, st>>>(n, t->plan, tw, A, rb, s2, kind, (T)(t->h * t->h), (T)coef,
                                                 (T)(1.0 / ((double)n * n)));
+  gmk::kernel_launch_adjust(1);
   k_tg_from_t<T><<<grid_for(nn), PT, 0, st>>>(nn, rb, x, accumulate ? 1 : 0);
   TG_CK(cudaGetLastError());
 }
@@ -376,6 +387,7 @@ void tg_project(gm_tg* t, const double* q, double step, double* out, double* phi
   const int n = t->n;
   const int64_t nn = (int64_t)n * n;
   cudaStream_t st = t->st;
+  gmk::kernel_launch_adjust(1);
   k_tg_div<<<grid_for(nn), PT, 0, st>>>(n, t->h, 1.0 / step, q, t->div.p, nullptr);
   if (t->precision == 0) {
     fourier_solve<double>(t, 0, 0.0, t->div.p, phi, false);
@@ -383,11 +395,13 @@ void tg_project(gm_tg* t, const double* q, double step, double* out, double* phi
     fourier_solve<float>(t, 0, 0.0, t->div.p, phi, false);
     for (int sweep = 0; sweep < 8; ++sweep) {
       TG_CK(cudaMemsetAsync(t->red.p + 4, 0, sizeof(unsigned long long), st));
+      gmk::kernel_launch_adjust(1);
       k_tg_pres<<<grid_for(nn), PT, 0, st>>>(n, t->h, t->div.p, phi, t->work.p, t->red.p + 4);
       if (bitsd(read_max(t, 4)) * step <= 1e-11) break;
       fourier_solve<float>(t, 0, 0.0, t->work.p, phi, true);
     }
   }
+  gmk::kernel_launch_adjust(1);
   k_tg_update<<<(unsigned)((2 * nn + PT - 1) / PT), PT, 0, st>>>(n, t->h, step, q, phi, out);
 }
 
@@ -404,6 +418,7 @@ void tg_helmholtz(gm_tg* t, double dt, const double* rhs, double* star) {
   if (t->precision == 1) {
     for (int sweep = 0; sweep < 6; ++sweep) {
       TG_CK(cudaMemsetAsync(t->red.p, 0, 2 * sizeof(unsigned long long), st));
+      gmk::kernel_launch_adjust(1);
       k_tg_hres<<<grid_for(2 * nn), PT, 0, st>>>(n, t->h, t->nu, 0.5 * dt, rhs, star, t->work.p, t->red.p, t->red.p + 1);
       unsigned long long v[2];
       TG_CK(cudaMemcpyAsync(v, t->red.p, sizeof v, cudaMemcpyDeviceToHost, st));
@@ -421,6 +436,7 @@ void tg_step(gm_tg* t, double dt, double* max_div) {
   cudaStream_t st = t->st;
   const unsigned g2 = (unsigned)((2 * nn + PT - 1) / PT);
   auto rhs_kernel = [&](int mode, double alpha, const double* qh, double* out) {
+    gmk::kernel_launch_adjust(1);
     if (t->precision == 1)
       k_tg_rhs<float><<<g2, PT, 0, st>>>(n, t->h, t->nu, mode, dt, alpha, t->q.p, qh, t->phalf.p, t->hist.p, t->now.p,
                                          out);
@@ -439,6 +455,7 @@ void tg_step(gm_tg* t, double dt, double* max_div) {
   tg_helmholtz(t, dt, t->rhs.p, t->star.p);
   // CN gate: max |H star - rhs| <= 1e-10 max(1, max |rhs|)  (solver/time_integration.py:100-104)
   TG_CK(cudaMemsetAsync(t->red.p, 0, 5 * sizeof(unsigned long long), st));
+  gmk::kernel_launch_adjust(1);
   k_tg_hres<<<grid_for(2 * nn), PT, 0, st>>>(n, t->h, t->nu, 0.5 * dt, t->rhs.p, t->star.p, nullptr, t->red.p,
                                              t->red.p + 1);
   unsigned long long v[2];
@@ -448,12 +465,15 @@ void tg_step(gm_tg* t, double dt, double* max_div) {
   if (!std::isfinite(bitsd(v[0])) || bitsd(v[0]) > 1e-10 * std::max(1.0, bitsd(v[1])))
     throw TgError(GM_ERUNTIME, "CN momentum solve failed: residual=" + std::to_string(bitsd(v[0])));
   tg_project(t, t->star.p, dt, t->qn.p, t->phi.p);
+  gmk::kernel_launch_adjust(1);
   k_tg_defect<<<g2, PT, 0, st>>>(n, t->h, t->nu, 0.5 * dt, t->qn.p, t->rhs.p, t->action.p, t->proj.p);
   tg_project(t, t->proj.p, dt, t->work.p, t->inc.p);
   const double factor = first ? 1.0 : dt / (dt + t->prev_dt);
+  gmk::kernel_launch_adjust(1);
   k_tg_pout<<<grid_for(2 * nn), PT, 0, st>>>(n, t->h, dt, factor, t->phalf.p, t->inc.p, t->action.p, t->rhs.p,
                                              t->phalf_n.p, t->pout.p, t->red.p + 3);
   TG_CK(cudaMemsetAsync(t->red.p + 2, 0, sizeof(unsigned long long), st));
+  gmk::kernel_launch_adjust(1);
   k_tg_div<<<grid_for(nn), PT, 0, st>>>(n, t->h, 1.0, t->qn.p, nullptr, t->red.p + 2);
   unsigned long long r[2];
   TG_CK(cudaMemcpyAsync(r, t->red.p + 2, sizeof r, cudaMemcpyDeviceToHost, st));

@@ -20,6 +20,10 @@
 
 #include "../../include/ghostmac.h"
 
+namespace gmk {
+void kernel_launch_adjust(long long delta);  // the library's launch counter (kernels.cu)
+}
+
 namespace {
 
 constexpr int NL = 12;
@@ -278,6 +282,7 @@ void conv_fwd(gm_unet* u, int k, const __nv_bfloat16* w, const float* b, cudaStr
   const LayerDef& L = LAYERS[k];
   const int H = u->H >> L.level, W = u->W >> L.level;
   dim3 grid((W + TW - 1) / TW, (H + TH - 1) / TH, u->B * ((L.cout + CO - 1) / CO)), block(TW, TH);
+  gmk::kernel_launch_adjust(1);
   k_conv3<false><<<grid, block, 0, st>>>(u->B, H, W, L.cin, L.cout, layer_input(u, k), w, b, u->act[k], L.relu ? 1 : 0);
 }
 
@@ -286,6 +291,7 @@ void forward(gm_unet* u, const __nv_bfloat16* const* w, const float* const* b, c
     conv_fwd(u, k, w[k], b[k], st);
     if (k == 1 || k == 3 || k == 5) {
       const int l = LAYERS[k].level;
+      gmk::kernel_launch_adjust(1);
       k_pool<<<gsz((size_t)u->B * LAYERS[k].cout * u->plane(l + 1)), 256, 0, st>>>(
           u->B * LAYERS[k].cout, u->H >> l, u->W >> l, u->act[k], u->pooled[k / 2]);
     }
@@ -295,8 +301,10 @@ void forward(gm_unet* u, const __nv_bfloat16* const* w, const float* const* b, c
   for (int d = 0; d < 3; ++d) {
     const int k = 8 + d, l = LAYERS[k].level;
     const int cu = LAYERS[prev[d]].cout, cs = LAYERS[skip[d]].cout, ct = cu + cs;
+    gmk::kernel_launch_adjust(1);
     k_up<<<gsz((size_t)u->B * cu * u->plane(l)), 256, 0, st>>>(u->B, cu, ct, u->H >> (l + 1), u->W >> (l + 1),
                                                                  u->act[prev[d]], u->cat[d]);
+    gmk::kernel_launch_adjust(1);
     k_copy_ch<<<gsz((size_t)u->B * cs * u->plane(l)), 256, 0, st>>>(u->B, cs, u->plane(l), u->act[skip[d]], cs, 0,
                                                                       u->cat[d], ct, cu, 0);
     conv_fwd(u, k, w[k], b[k], st);
@@ -316,15 +324,20 @@ void backward(gm_unet* u, const __nv_bfloat16* const* w, float* const* dw, float
     const LayerDef& L = LAYERS[k];
     const int H = u->H >> L.level, W = u->W >> L.level;
     const size_t n = (size_t)u->B * L.cout * H * W;
-    if (L.relu) k_relu_back<<<gsz(n), 256, 0, st>>>(n, u->act[k], u->g_act[k]);
+    if (L.relu) {
+      gmk::kernel_launch_adjust(1);
+      k_relu_back<<<gsz(n), 256, 0, st>>>(n, u->act[k], u->g_act[k]);
+    }
     const int slices = std::max(1, std::min(64, H / 8));
     dim3 gw(((L.cout + CO - 1) / CO) * L.cin, slices);
+    gmk::kernel_launch_adjust(1);
     k_conv3_wgrad<<<gw, 256, 0, st>>>(u->B, H, W, L.cin, L.cout, layer_input(u, k), u->g_act[k], dw[k], db[k], slices);
     float* gin = layer_input_grad(u, k);
     if (gin) {
       // the data gradient is written (not accumulated): every consumer tensor has exactly
       // one producing convolution, except the encoder outputs handled below
       dim3 grid((W + TW - 1) / TW, (H + TH - 1) / TH, u->B * ((L.cin + CO - 1) / CO)), block(TW, TH);
+      gmk::kernel_launch_adjust(1);
       k_conv3<true><<<grid, block, 0, st>>>(u->B, H, W, L.cout, L.cin, u->g_act[k], w[k], nullptr, gin, 0);
     }
   };
@@ -336,8 +349,10 @@ void backward(gm_unet* u, const __nv_bfloat16* const* w, float* const* dw, float
     const int cu = LAYERS[prev[d]].cout, cs = LAYERS[skip[d]].cout, ct = cu + cs;
     // split the concatenated gradient: upsampled part -> previous decoder output, skip part ->
     // encoder output (added: the encoder output also feeds the pooling / next conv)
+    gmk::kernel_launch_adjust(1);
     k_up_back<<<gsz((size_t)u->B * cu * u->plane(l + 1)), 256, 0, st>>>(u->B, cu, ct, u->H >> (l + 1),
                                                                          u->W >> (l + 1), u->g_cat[d], u->g_act[prev[d]]);
+    gmk::kernel_launch_adjust(1);
     k_copy_ch<<<gsz((size_t)u->B * cs * u->plane(l)), 256, 0, st>>>(u->B, cs, u->plane(l), u->g_cat[d], ct, cu,
                                                                       u->g_act[skip[d]], cs, 0, 1);
   }
@@ -347,6 +362,7 @@ void backward(gm_unet* u, const __nv_bfloat16* const* w, float* const* dw, float
     if (k == 6 || k == 4 || k == 2) {
       conv_back(k);  // writes g_pooled
       const int src = k - 1, l = LAYERS[src].level;
+      gmk::kernel_launch_adjust(1);
       k_pool_back<<<gsz((size_t)u->B * LAYERS[src].cout * u->plane(l)), 256, 0, st>>>(
           u->B * LAYERS[src].cout, u->H >> l, u->W >> l, u->g_pooled[k / 2 - 1], u->g_act[src], 1);
     } else {
