@@ -2533,12 +2533,12 @@ void batch_groups(gm_batch* b) {
 // Launch shapes of the cases of a batch.  The autotuned shapes of a single case minimise its
 // latency with large blocks (up to 210 KB of shared memory for a column-solve block), which
 // keeps other cases' kernels off those SMs; many concurrent cases run faster with smaller
-// blocks.  Measured on the 64-case sweep (32 hardware queues): 8.7 ms per step with row-pass
-// groups of 128 threads, 2 per block, and 4 columns per column-solve block, against 10.3 ms
-// with the single-case shapes.  GHOSTMAC_BATCH_SHAPES="gthreads,gpb,L" picks another shape,
-// "tuned" keeps every case's own.
+// blocks.  Measured on the 64-case FP32 sweep (32 hardware queues): 7.8 ms per step with
+// row-pass groups of 64 threads, 4 per block, and 8 columns per column-solve block, against
+// 10.3 ms with the single-case shapes (8.1-8.9 ms for the other small shapes tried).
+// GHOSTMAC_BATCH_SHAPES="gthreads,gpb,L" picks another shape, "tuned" keeps every case's own.
 void batch_shapes(gm_batch* b) {
-  int gt = 128, gp = 2, L = 4;
+  int gt = 64, gp = 4, L = 8;
   if (const char* e = std::getenv("GHOSTMAC_BATCH_SHAPES")) {
     if (std::strncmp(e, "tuned", 5) == 0) return;
     int a = 0, c = 0, d = 0;
