@@ -147,7 +147,8 @@ __device__ __forceinline__ bool gate_open_thread(const Gate& g) {
 __device__ __forceinline__ bool gate_open(const Gate& g) {
   // A kernel launched as a programmatic dependent of the previous kernel on its stream starts
   // before that kernel ends: wait for it (and its memory) before reading anything it wrote.
-  // Without such a launch this returns at once.
+  // Without such a launch this returns at once.  (Triggering the dependents early, at block
+  // start, was measured slower: the waiting blocks hold SM resources.)
   asm volatile("griddepcontrol.wait;" ::: "memory");
   __shared__ int open_flag;
   if (threadIdx.x == 0) open_flag = gate_open_thread(g) ? 1 : 0;
