@@ -192,11 +192,12 @@ void ktimer_read(int cls, double* total_ms, long long* count, double* bytes) {
 // transforms, one line for the type-IV transforms -- and a block holds `gpb` groups.
 // Rows r0 .. r0+nr-1 are transformed.  Masked load with the optional spectral correction
 // of the boundary term (YCorr); masked store with the optional epilogue out = add + v.
+// shared memory of one line group: the two FFT buffers (the real results go to the buffer the
+// FFT does not end in)
 template <typename T>
 __host__ __device__ inline size_t xpass_group_smem(int type, int n) {
   const int lpw = r2r_paired(type) ? 2 : 1;
-  size_t stage = ((size_t)lpw * n * sizeof(T) + 15) / 16 * 16;
-  return stage + 2 * (size_t)r2r_buffer_elems(type, n, lpw) * sizeof(cplx<T>);
+  return 2 * (size_t)r2r_buffer_elems(type, n, lpw) * sizeof(cplx<T>);
 }
 // lengths (complex entries) of the plan's twiddles, the pre- and the post-twiddles of a transform
 __host__ __device__ inline int xpass_tw_len(int type, int n, int which, int plan_tw) {
@@ -249,16 +250,19 @@ __device__ __forceinline__ void xpass_block(int bi, int n, int r0, int nr, int t
   if (grp >= gpb || l0 >= nr) return;
   const int nl = min(lpw, nr - l0);
   unsigned char* mine = smem_raw + xpass_tw_bytes<T>(type, n, plan.tw_len) + (size_t)grp * xpass_group_smem<T>(type, n);
-  T* stage = reinterpret_cast<T*>(mine);
-  const size_t stage_bytes = ((size_t)lpw * n * sizeof(T) + 15) / 16 * 16;
-  cplx<T>* a = reinterpret_cast<cplx<T>*>(mine + stage_bytes);
+  cplx<T>* a = reinterpret_cast<cplx<T>*>(mine);
   cplx<T>* b = a + r2r_buffer_elems(type, n, lpw);
   const Grp G{tid, gthreads, grp + 1};
+  // per line (at most two): input row offset and the band correction (band row that scales or
+  // is the correction, decay factors of this row: nullptr inside the band); scalars selected by
+  // the line index, not an indexed array (that would go to local memory)
+  int64_t irow0 = 0, irow1 = 0;
+  const T *cb0 = nullptr, *cb1 = nullptr, *cf0 = nullptr, *cf1 = nullptr;
   for (int l = 0; l < nl; ++l) {
     const int r = r0 + l0 + l;
-    const int64_t row = ibase + (int64_t)r * ipitch;
-    const T* cb = nullptr;  // band row that scales (or is) the correction of this row
-    const T* cf = nullptr;  // decay factors of this row (nullptr inside the band)
+    const int64_t ir = ibase + (int64_t)r * ipitch;
+    const T* cb = nullptr;
+    const T* cf = nullptr;
     if (corr.band) {
       if (r < corr.j0) {
         cb = corr.band;
@@ -270,29 +274,20 @@ __device__ __forceinline__ void xpass_block(int bi, int n, int r0, int nr, int t
         cb = corr.band + (int64_t)(r - corr.j0) * n;
       }
     }
-    // XB loads in flight per thread before the first shared-memory store
-    for (int e0 = tid; e0 < n; e0 += XB * gthreads) {
-      TI v[XB];
-      uint8_t mk[XB];
-      T cv[XB];
-#pragma unroll
-      for (int u = 0; u < XB; ++u) {
-        const int e = e0 + u * gthreads;
-        if (e < n) {
-          v[u] = in[row + e];
-          mk[u] = icls ? icls[row + e] : (uint8_t)CLS_ACTIVE;
-          cv[u] = cb ? (cf ? cf[e] * cb[e] : cb[e]) : (T)0;
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < XB; ++u) {
-        const int e = e0 + u * gthreads;
-        if (e < n) stage[l * n + e] = ((mk[u] & CLS_ACTIVE) ? cvt_to<T>(v[u]) : (T)0) - cv[u];
-      }
-    }
+    if (l == 0) { irow0 = ir; cb0 = cb; cf0 = cf; }
+    else { irow1 = ir; cb1 = cb; cf1 = cf; }
   }
-  G.sync();
-  r2r_lines<T>(type, stage, n, nl, a, b, plan, ts, G);
+  // element e of line l: masked input minus the correction
+  auto x = [&](int l, int e) -> T {
+    const int64_t o = (l == 0 ? irow0 : irow1) + e;
+    const T* cb = l == 0 ? cb0 : cb1;
+    const T* cf = l == 0 ? cf0 : cf1;
+    const TI v = in[o];
+    const uint8_t mk = icls ? icls[o] : (uint8_t)CLS_ACTIVE;
+    const T cv = cb ? (cf ? cf[e] * cb[e] : cb[e]) : (T)0;
+    return ((mk & CLS_ACTIVE) ? cvt_to<T>(v) : (T)0) - cv;
+  };
+  const T* stage = r2r_lines<T>(type, n, nl, a, b, plan, ts, G, x);
   for (int l = 0; l < nl; ++l) {
     const int64_t row = obase + (int64_t)(r0 + l0 + l) * opitch;
     for (int e0 = tid; e0 < n; e0 += XB * gthreads) {

@@ -245,54 +245,62 @@ struct R2RTables {
 };
 
 // ---------------------------------------------------------------------------
-// pre-processing: real lines in stage (line-major, length n each, nl lines)
-// -> complex FFT inputs in buf.  Line l of the transform reads stage[l*n + ...].
+// pre-processing: nl real lines of length n -> complex FFT inputs in buf.  x(l, i) gives
+// element i of line l (the caller reads it from global memory with its masks, so the lines go
+// to the FFT buffer without a staging pass); #pragma unroll keeps several lines' loads in
+// flight per thread.
 // ---------------------------------------------------------------------------
-template <typename T>
-__device__ void r2r_pre(int type, const T* stage, int n, int nl, cplx<T>* buf, const R2RTables<T>& tb, const Grp& G) {
+template <typename T, typename X>
+__device__ __forceinline__ void r2r_pre(int type, int n, int nl, cplx<T>* buf, const R2RTables<T>& tb, const Grp& G,
+                                        X&& x) {
   const int fam = r2r_family(type);
   if (fam == 2) {
     const int M = n / 2;
     const bool rev = type == DST4;
-    for (int l = 0; l < nl; ++l)
+    for (int l = 0; l < nl; ++l) {
+#pragma unroll 4
       for (int m = G.tid; m < M; m += G.n) {
-        const T* x = stage + (size_t)l * n;
         int i0 = 2 * m, i1 = n - 1 - 2 * m;
-        T a = rev ? x[n - 1 - i0] : x[i0];
-        T b = rev ? x[n - 1 - i1] : x[i1];
+        T a = x(l, rev ? n - 1 - i0 : i0);
+        T b = x(l, rev ? n - 1 - i1 : i1);
         cplx<T> w = tb.pre[m];
         buf[(size_t)l * M + m] = {a * w.x - b * w.y, b * w.x + a * w.y};
       }
+    }
   } else if (fam == 0) {
     // Makhoul: v[m] = x[2m] (m < ceil(n/2)), v[n-1-m'] = x[2m'+1]
     const int npair = (nl + 1) / 2;
     const bool alt = type == DST2;  // DST-II: x'[m] = (-1)^m x[m]
-    for (int pidx = 0; pidx < npair; ++pidx)
-    for (int m = G.tid; m < n; m += G.n) {
-      int src = m < (n + 1) / 2 ? 2 * m : 2 * (n - 1 - m) + 1;
-      T sgn = (alt && (src & 1)) ? (T)-1 : (T)1;
-      int la = 2 * pidx, lb = 2 * pidx + 1;
-      T a = sgn * stage[(size_t)la * n + src];
-      T b = lb < nl ? sgn * stage[(size_t)lb * n + src] : (T)0;
-      buf[(size_t)pidx * n + m] = {a, b};
+    for (int pidx = 0; pidx < npair; ++pidx) {
+#pragma unroll 4
+      for (int m = G.tid; m < n; m += G.n) {
+        int src = m < (n + 1) / 2 ? 2 * m : 2 * (n - 1 - m) + 1;
+        T sgn = (alt && (src & 1)) ? (T)-1 : (T)1;
+        int la = 2 * pidx, lb = 2 * pidx + 1;
+        T a = sgn * x(la, src);
+        T b = lb < nl ? sgn * x(lb, src) : (T)0;
+        buf[(size_t)pidx * n + m] = {a, b};
+      }
     }
   } else if (fam == 1) {
     // V[k] = e^{i pi k/(2n)} (X_k - i X_{n-k}), X_n = 0; two lines as V_A + i V_B
     const int npair = (nl + 1) / 2;
     const bool rev = type == DST3;  // DST-III: X'[k] = X[n-1-k]
-    for (int pidx = 0; pidx < npair; ++pidx)
-    for (int k = G.tid; k < n; k += G.n) {
-      int la = 2 * pidx, lb = 2 * pidx + 1;
-      int ik = rev ? n - 1 - k : k;
-      int ir = rev ? k - 1 : n - k;  // index of X_{n-k} in the stored line (valid when k > 0)
-      cplx<T> cs = tb.post[k];       // (cos, sin)(pi k / (2n))
-      T ak = stage[(size_t)la * n + ik];
-      T ar = k > 0 ? stage[(size_t)la * n + ir] : (T)0;
-      T bk = lb < nl ? stage[(size_t)lb * n + ik] : (T)0;
-      T br = (lb < nl && k > 0) ? stage[(size_t)lb * n + ir] : (T)0;
-      cplx<T> VA = {cs.x * ak + cs.y * ar, cs.y * ak - cs.x * ar};
-      cplx<T> VB = {cs.x * bk + cs.y * br, cs.y * bk - cs.x * br};
-      buf[(size_t)pidx * n + k] = {VA.x - VB.y, VA.y + VB.x};
+    for (int pidx = 0; pidx < npair; ++pidx) {
+#pragma unroll 4
+      for (int k = G.tid; k < n; k += G.n) {
+        int la = 2 * pidx, lb = 2 * pidx + 1;
+        int ik = rev ? n - 1 - k : k;
+        int ir = rev ? k - 1 : n - k;  // index of X_{n-k} in the stored line (valid when k > 0)
+        cplx<T> cs = tb.post[k];       // (cos, sin)(pi k / (2n))
+        T ak = x(la, ik);
+        T ar = k > 0 ? x(la, ir) : (T)0;
+        T bk = lb < nl ? x(lb, ik) : (T)0;
+        T br = (lb < nl && k > 0) ? x(lb, ir) : (T)0;
+        cplx<T> VA = {cs.x * ak + cs.y * ar, cs.y * ak - cs.x * ar};
+        cplx<T> VB = {cs.x * bk + cs.y * br, cs.y * bk - cs.x * br};
+        buf[(size_t)pidx * n + k] = {VA.x - VB.y, VA.y + VB.x};
+      }
     }
   } else {
     // DST-I: odd extension of length 2(n+1)
@@ -303,12 +311,12 @@ __device__ void r2r_pre(int type, const T* stage, int n, int nl, cplx<T>* buf, c
       int la = 2 * pidx, lb = 2 * pidx + 1;
       cplx<T> z = {0, 0};
       if (m >= 1 && m <= n) {
-        z.x = stage[(size_t)la * n + m - 1];
-        z.y = lb < nl ? stage[(size_t)lb * n + m - 1] : (T)0;
+        z.x = x(la, m - 1);
+        z.y = lb < nl ? x(lb, m - 1) : (T)0;
       } else if (m >= N + 1) {
         int src = n - 1 - (m - N - 1);
-        z.x = -stage[(size_t)la * n + src];
-        z.y = lb < nl ? -stage[(size_t)lb * n + src] : (T)0;
+        z.x = -x(la, src);
+        z.y = lb < nl ? -x(lb, src) : (T)0;
       }
       buf[(size_t)pidx * M + m] = z;
     }
@@ -386,16 +394,20 @@ __host__ __device__ inline int r2r_buffer_elems(int type, int n, int nl) {
 }
 __host__ __device__ inline int r2r_nfft(int type, int nl) { return r2r_paired(type) ? (nl + 1) / 2 : nl; }
 
-// Full r2r transform of nl lines held in stage (in place, through buffers a/b).
-template <typename T>
-__device__ void r2r_lines(int type, T* stage, int n, int nl, cplx<T>* a, cplx<T>* b, const FftPlan& plan,
-                          const R2RTables<T>& tb, const Grp& G) {
+// Full r2r transform of nl lines read through x(l, i) (see r2r_pre), through the FFT buffers
+// a/b; the real results are left line-major (l * n + i) in the buffer the FFT does not end in,
+// which is returned.
+template <typename T, typename X>
+__device__ __forceinline__ T* r2r_lines(int type, int n, int nl, cplx<T>* a, cplx<T>* b, const FftPlan& plan,
+                                        const R2RTables<T>& tb, const Grp& G, X&& x) {
   const int fam = r2r_family(type);
-  r2r_pre<T>(type, stage, n, nl, a, tb, G);
+  r2r_pre<T>(type, n, nl, a, tb, G, x);
   G.sync();
   cplx<T>* res = fft_run<T>(a, b, plan, r2r_nfft(type, nl), tb.W, fam == 1 ? +1 : -1, G);
-  r2r_post<T>(type, res, n, nl, stage, tb, G);
+  T* out = reinterpret_cast<T*>(res == a ? b : a);
+  r2r_post<T>(type, res, n, nl, out, tb, G);
   G.sync();
+  return out;
 }
 
 }  // namespace gmk
