@@ -64,6 +64,12 @@ TG_WORKLOADS = {
     'taylor_green_1024': dict(n=1024, nu=0.01, dt=1e-3, end_time=1.0),
     'taylor_green_256': dict(n=256, nu=0.01, dt=1e-3, end_time=1.0),
 }
+# GMRES pressure path with the learned preconditioner (config 5): 1024x512 (h = 0.04), Re = 150,
+# cylinder at (8D, 10.24D), dt = 0.0015; the network trains on the case's own first solves
+GMRES_WORKLOADS = {
+    'gmres_1024x512_re150': dict(nx=1024, ny=512, Lx=40.96, Ly=20.48, D=1.0, xc=8.0, yc=10.24, nu=1 / 150,
+                                 dt=0.0015, noise='v', amp=1e-2, seed=0, record_steps=40, epochs=600),
+}
 DEFAULT_WORKLOAD = 'wide_800x820_re100'
 # DRAM bytes (read + write) per launch of the dominant kernel class, averaged over the launches
 # of one ncu --set full capture of the same command (the capture's file under profiles/ gives the
@@ -528,6 +534,81 @@ def run_ours_tg(args, w, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def run_ours_gmres(args, w, rank, world):
+    """GMRES pressure path (pressure_solver='iterative'): K steps with the rectangle-preconditioned
+    FGMRES, the same K steps with the learned network attached (trained on the solves of the
+    first record_steps steps of the same case), and the direct FFT/Schur path from the same
+    state; iterations per solve, time per step and the force-coefficient differences."""
+    import torch
+    pkg = load_package()
+    learned = pkg.learned
+    kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
+    dt, K = w['dt'], args.steps
+    cells = w['nx'] * w['ny']
+
+    def case(solver):
+        s = pkg.MAC_CylinderFlow(verbose=False, precision=args.precision, pressure_solver=solver, **kw)
+        seeded_state(s, w)
+        return s
+
+    def timed(s, n):
+        its, solves = [], []
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(n):
+            rc, d = s.step_raw(dt, 1, first_index=k + w['record_steps'])
+            pkg._lib.check(rc, s._h)
+            its.append(int(d[0].pressure_iterations))
+            solves.append(int(d[0].pressure_solve_count))
+            s.time = d[0].time
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        return el * 1e3 / n, its, solves, float(d[0].cd), float(d[0].cl)
+
+    plain = case('iterative')
+    rhs, sol = learned.record_pressure_pairs(plain, w['record_steps'], dt)
+    x, y, mask = learned.training_set(plain, rhs, sol)
+    weights = learned.UNetWeights(seed=1)
+    t0 = time.perf_counter()
+    hist = learned.train(weights, x, y, mask, epochs=w['epochs'], lr=2e-3, batch=4)
+    train_s = time.perf_counter() - t0
+    # the learned case repeats the recorded steps, then runs the timed steps with the network
+    net_case = case('iterative')
+    net_case.solve(n_steps=w['record_steps'], dt=dt, perturb_transient=False, save_artifacts=False, verbose=False)
+    direct = case('direct')
+    direct.solve(n_steps=w['record_steps'], dt=dt, perturb_transient=False, save_artifacts=False, verbose=False)
+    launches0 = pkg._lib.lib.gm_kernel_launches()
+    with ClockSampler(int(os.environ.get('LOCAL_RANK', 0))) as clocks:
+        ms_plain, its_plain, n_plain, cd_plain, cl_plain = timed(plain, K)
+    launches = pkg._lib.lib.gm_kernel_launches() - launches0
+    pc = learned.LearnedPreconditioner(net_case, weights)
+    ms_net, its_net, n_net, cd_net, cl_net = timed(net_case, K)
+    pc.detach()
+    ms_dir, _, _, cd_dir, cl_dir = timed(direct, K)
+    if rank == 0:
+        per = lambda its, ns: float(np.sum(its) / max(np.sum(ns), 1))
+        line = dict(metric=METRIC, value=cells * world / (ms_plain * 1e-3), unit='cell-updates/s', n_gpus=world,
+                    steps=K, warmup=w['record_steps'], ms_per_step=ms_plain, higher_is_better=True, scaling='weak',
+                    vs_baseline=None, dtype='f64' if args.precision == 'fp64' else 'f32+f64-refine',
+                    data='synthetic', config=dict(workload=args.workload, grid=f"{w['nx']}x{w['ny']}", dt=dt,
+                                                  precision=args.precision, parallelism='replicas',
+                                                  pressure='FGMRES(50), rectangle-preconditioned',
+                                                  timing='host wall clock around each synchronous step'),
+                    roofline=None, cpu_baseline=None,
+                    e2e=dict(value=cells * world / (ms_plain * 1e-3), unit='cell-updates/s',
+                             h2d_bytes_per_step=0, d2h_bytes_per_step=int(C.sizeof(pkg._lib.StepDiag))),
+                    clocks=clocks.summary(), gpu_launches=int(launches),
+                    gmres=dict(iterations_per_solve_plain=per(its_plain, n_plain),
+                               iterations_per_solve_learned=per(its_net, n_net),
+                               ms_per_step_plain=ms_plain, ms_per_step_learned=ms_net, ms_per_step_direct=ms_dir,
+                               cd_rel_diff_plain_vs_direct=abs(cd_plain - cd_dir) / abs(cd_dir),
+                               cd_rel_diff_learned_vs_direct=abs(cd_net - cd_dir) / abs(cd_dir),
+                               cl_abs_diff_learned_vs_plain=abs(cl_net - cl_plain),
+                               training_pairs=int(x.shape[0]), training_epochs=w['epochs'], training_s=train_s,
+                               training_loss_ratio=hist[-1] / hist[0]))
+        print(json.dumps(line), flush=True)
+
+
 def run_ours_batch(args, w, rank, world):
     """Batched sweep: all cases advance together, one graph launch per step."""
     import torch
@@ -656,8 +737,8 @@ def main():
     ap.add_argument('--steps', type=int, default=200)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
-    ap.add_argument('--workload', choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(TG_WORKLOADS),
-                    default=DEFAULT_WORKLOAD)
+    ap.add_argument('--workload', choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(TG_WORKLOADS) +
+                    sorted(GMRES_WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
     ap.add_argument('--no-compare', action='store_true', help='skip timing the plain FP64 step beside the FP32 mode')
     ap.add_argument('--precision', choices=('fp64', 'fp32'), default='fp32',
@@ -665,7 +746,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    w = WORKLOADS.get(args.workload) or BATCH_WORKLOADS.get(args.workload) or TG_WORKLOADS[args.workload]
+    w = (WORKLOADS.get(args.workload) or BATCH_WORKLOADS.get(args.workload) or TG_WORKLOADS.get(args.workload) or
+         GMRES_WORKLOADS[args.workload])
     world = int(os.environ.get('WORLD_SIZE', 1))
     rank = int(os.environ.get('RANK', 0))
     if args.impl == 'reference':
@@ -680,6 +762,8 @@ def main():
         run_ours_batch(args, w, rank, world)
     elif args.workload in TG_WORKLOADS:
         run_ours_tg(args, w, rank, world)
+    elif args.workload in GMRES_WORKLOADS:
+        run_ours_gmres(args, w, rank, world)
     else:
         run_ours(args, w, rank, world)
     if world > 1:
