@@ -810,6 +810,12 @@ ResidualCoef residual_coef(const gm::Geometry& g, int kind, double hc) {
     r.ce = -hc * idx2;
     r.cy = -hc * idy2;
   }
+  for (int a = 0; a < 3; ++a) {
+    for (int c = 0; c < 2; ++c) r.fcc[a][c] = (float)r.cc[a][c];
+    r.fcw[a] = (float)r.cw[a];
+  }
+  r.fce = (float)r.ce;
+  r.fcy = (float)r.cy;
   return r;
 }
 

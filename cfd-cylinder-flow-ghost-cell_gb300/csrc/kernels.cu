@@ -1315,35 +1315,48 @@ void launch_residual(const CaseDev& c, const ResidualCoef& rc, int kind, const d
 // Roundoff bound max_i (2 nnz_i + 2) eps (|A||x| + |b|)_i of the pressure solution after its
 // refinement loop (solver/pressure_schur.py:48-56), stored at the last check; used by the
 // FP32 mode, whose residual sweeps skip it.
+// FP32 arithmetic: the bound is a threshold of the pressure gate (max(target, bound)), so its
+// last bits do not matter; it is formed from FP32 copies of x, b and the coefficients
+// (conversions on the integer pipe) and rounded up by 2^-20 relative before it is committed,
+// which keeps it above the FP64 value of the same expression.
 __device__ __forceinline__ void pressure_bound_body(const CaseDev& c, const ResidualCoef& rc,
                                                     const double* __restrict__ b, const double* __restrict__ x,
                                                     SolveCtl* sc, int nchk, int bid, int nblk) {
   const int check = last_check(sc, nchk);
   const int nx = c.nx, ny = c.ny;
-  unsigned long long bd = 0;
+  constexpr float EPS = 2.220446049250313e-16f;
+  float bd = 0.0f;
+  auto ax = [&](int64_t t) { return fabsf(f64_to_f32i(x[t])); };
   for (int64_t t = (int64_t)bid * blockDim.x + threadIdx.x; t < c.psize; t += (int64_t)nblk * blockDim.x) {
     const uint8_t k = c.cls_p[t];
     if (!(k & CLS_ACTIVE)) continue;
-    const double xv = x[t], bv = b[t];
-    double aabs = 0.0;
+    const float bv = fabsf(f64_to_f32i(b[t]));
+    float aabs = 0.0f;
     int nnz;
     const int row = (k & CLS_IRREG) ? c.irr_index[0][t] : -1;
     if (row >= 0) {
       const int64_t* cp = c.irr_ptr[0];
       const int64_t e0 = cp[row], e1 = cp[row + 1];
-      csr_row<4>(c.irr_col[0], c.irr_val[0], e0, e1, x, 0, [&](double a, double xv2) { aabs += fabs(a) * fabs(xv2); });
+      csr_row<4>(c.irr_col[0], c.irr_val[0], e0, e1, x, 0, [&](double a, double xv2) {
+        aabs += fabsf(f64_to_f32i(a)) * fabsf(f64_to_f32i(xv2));
+      });
       nnz = (int)(e1 - e0);
     } else {
       const int j = (int)((unsigned)t / (unsigned)nx), i = (int)((unsigned)t - (unsigned)j * nx);
-      double xw = i > 0 ? x[t - 1] : 0.0, xe = i < nx - 1 ? x[t + 1] : 0.0;
-      double xs = j > 0 ? x[t - nx] : 0.0, xn = j < ny - 1 ? x[t + nx] : 0.0;
+      const float xw = i > 0 ? ax(t - 1) : 0.0f, xe = i < nx - 1 ? ax(t + 1) : 0.0f;
+      const float xs = j > 0 ? ax(t - nx) : 0.0f, xn = j < ny - 1 ? ax(t + nx) : 0.0f;
       const int ic = i == 0 ? 0 : (i == nx - 1 ? 2 : 1), jc = (j == 0 || j == ny - 1) ? 0 : 1;
-      aabs = fabs(coef_cc(rc, ic, jc)) * fabs(xv) + rc.ce * (fabs(xw) + fabs(xe)) + rc.cy * (fabs(xs) + fabs(xn));
+      const float c0 = jc ? rc.fcc[0][1] : rc.fcc[0][0], c1 = jc ? rc.fcc[1][1] : rc.fcc[1][0];
+      const float c2 = jc ? rc.fcc[2][1] : rc.fcc[2][0];
+      const float ccv = ic == 0 ? c0 : (ic == 1 ? c1 : c2);
+      aabs = fabsf(ccv) * ax(t) + rc.fce * (xw + xe) + rc.fcy * (xs + xn);
       nnz = c.a_nnz[t];
     }
-    bd = umax64(bd, dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + fabs(bv))));
+    bd = fmaxf(bd, (2.0f * (float)nnz + 2.0f) * EPS * (aabs + bv));
   }
-  block_commit_max(bd, &sc->bound[check]);
+  // non-negative floats order like their bits; the block maximum goes out as an FP64 value
+  const double up = f32_to_f64i(bd) * (1.0 + 0x1p-20);
+  block_commit_max(dbits(up), &sc->bound[check]);
 }
 __global__ void k_pressure_bound(CaseDev c, ResidualCoef rc, const double* __restrict__ b,
                                  const double* __restrict__ x, SolveCtl* sc, int nchk, Gate gate) {

@@ -310,6 +310,7 @@ struct ResidualCoef {
   double cc[3][2];
   double cw[3];
   double ce, cy;
+  float fcc[3][2], fcw[3], fce, fcy;  // FP32 copies (the FP32 mode's roundoff bound)
 };
 void launch_residual(const CaseDev& c, const ResidualCoef& rc, int kind, const double* b, const double* x, void* res,
                      bool res_f32, SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st);
