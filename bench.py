@@ -88,6 +88,18 @@ KERNEL_CLASSES = {1: 'row transforms (k_xpass)', 2: 'column solves (k_ysolve, k_
                   9: 'forces / maxima (k_forces, k_maxabs)', 10: 'gates and loop control'}
 
 
+def replica_step_ms(step_ms, world, device='cuda'):
+    """Replicas only: every rank times its own case; the job's step time is the slowest rank's
+    (max over ranks through the default process group when world > 1)."""
+    if world <= 1:
+        return step_ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([step_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def load_package():
     sys.path.insert(0, str(ROOT))
     import __graft_entry__ as ge
@@ -340,10 +352,7 @@ def run_ours(args, w, rank, world):
     torch.cuda.synchronize()
     launches = L.lib.gm_kernel_launches() - launches0
     step_ms = sum(times) / len(times)
-    if world > 1:
-        t = torch.tensor([step_ms], device='cuda')
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(t.item())
+    step_ms = replica_step_ms(step_ms, world)
     value = cells * world / (step_ms * 1e-3)
     # phase times of graph-replayed steps (timing events captured into the step graphs)
     os.environ['GHOSTMAC_PHASE_TIMING'] = '1'
@@ -500,10 +509,7 @@ def run_ours_tg(args, w, rank, world):
     launches = pkg._lib.lib.gm_kernel_launches() - launches0
     case.close()
     step_ms = el * 1e3 / args.steps
-    if world > 1:
-        t = torch.tensor([step_ms], device='cuda')
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(t.item())
+    step_ms = replica_step_ms(step_ms, world)
     cells = n * n
     # end to end through taylor_green.run (host arrays in and out) to end_time, both precisions
     t0 = time.perf_counter()
@@ -652,10 +658,7 @@ def run_ours_batch(args, w, rank, world):
     sweeps = [x.pressure_refinement_iterations + x.momentum_refinement_iterations for x in d]
     launches = L.lib.gm_kernel_launches() - launches0
     assert max(divs) < 1e-10
-    if world > 1:
-        t = torch.tensor([step_ms], device='cuda')
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(t.item())
+    step_ms = replica_step_ms(step_ms, world)
     value = cells * world / (step_ms * 1e-3)
     # dominant kernel class (per-class event timing of one launch-by-launch batch step)
     per_class = {}
