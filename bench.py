@@ -78,8 +78,8 @@ DEFAULT_WORKLOAD = 'wide_800x820_re100'
 DRAM_TRAFFIC = {
     # profiles/k_xpass_fp64_wide_800x820.md: (1792 + 512 + 256 + 5888) / 4
     ('wide_800x820_re100', 'fp64', 1): 2112.0,
-    # profiles/fp32_mode_wide_800x820.md: row passes of the first sweep, (2816 + 0 + 256) / 3
-    ('wide_800x820_re100', 'fp32', 1): 1024.0,
+    # profiles/fp32_mode_wide_800x820.md: the two row passes of the first sweep, (1024 + 1280) / 2
+    ('wide_800x820_re100', 'fp32', 1): 1152.0,
 }
 KERNEL_CLASSES = {1: 'row transforms (k_xpass)', 2: 'column solves (k_ysolve, k_yband)',
                   3: 'momentum rhs (k_momentum, k_shadow)', 4: 'operator residual (k_residual, k_pressure_bound)',
