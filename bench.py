@@ -76,8 +76,9 @@ DEFAULT_WORKLOAD = 'wide_800x820_re100'
 # command and the per-launch figures).  Within a step the working set stays in L2, so DRAM
 # traffic is far below the algorithmic bytes.
 DRAM_TRAFFIC = {
-    # profiles/k_xpass_fp64_wide_800x820.md: (1792 + 512 + 256 + 5888) / 4
-    ('wide_800x820_re100', 'fp64', 1): 2112.0,
+    # profiles/k_xpass_fp64_wide_800x820.md: the forward and inverse row passes of the first
+    # Helmholtz solve, (2048 + 3328 + 1792 + 9216) / 2
+    ('wide_800x820_re100', 'fp64', 1): 8192.0,
     # profiles/fp32_mode_wide_800x820.md: the two row passes of the first sweep, (1024 + 1280) / 2
     ('wide_800x820_re100', 'fp32', 1): 1152.0,
 }
