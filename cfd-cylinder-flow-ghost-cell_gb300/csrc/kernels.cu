@@ -219,19 +219,34 @@ size_t xpass_smem_tables(int type, int n, int plan_tw, bool fp32) {
 }
 
 static constexpr int XB = 4;  // loads batched per thread in the row passes
+static constexpr int XT = 8;  // table loads in flight per thread while the tables are staged
 // Twiddle tables of one transform type staged into the block's shared memory (read by every
 // stage of every group: a global load per stage would put an L2 round trip on each stage's
-// critical path).  Called by all threads of the block; ends with a block barrier.
+// critical path).  Each thread has XT loads in flight before its first store, so a table of
+// up to XT * blockDim.x entries costs one round trip.  The tables are written once at set-up,
+// never by a kernel, so the kernels stage them before waiting on the previous kernel of the
+// stream.  Called by all threads of the block; ends with a block barrier.
 template <typename T>
 __device__ __forceinline__ R2RTables<T> xpass_stage_tables(int type, int n, const FftPlan& plan,
                                                            const R2RTables<T>& tb, unsigned char* smem_raw) {
-  const int ntw[3] = {xpass_tw_len(type, n, 0, plan.tw_len), xpass_tw_len(type, n, 1, plan.tw_len),
-                      xpass_tw_len(type, n, 2, plan.tw_len)};
+  const int n0 = xpass_tw_len(type, n, 0, plan.tw_len), n1 = xpass_tw_len(type, n, 1, plan.tw_len);
+  const int tot = n0 + n1 + xpass_tw_len(type, n, 2, plan.tw_len);
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smem_raw);
-  for (int q = threadIdx.x; q < ntw[0] + ntw[1] + ntw[2]; q += blockDim.x)
-    tw[q] = q < ntw[0] ? tb.W[q] : (q < ntw[0] + ntw[1] ? tb.pre[q - ntw[0]] : tb.post[q - ntw[0] - ntw[1]]);
+  for (int q0 = threadIdx.x; q0 < tot; q0 += XT * blockDim.x) {
+    cplx<T> v[XT];
+#pragma unroll
+    for (int u = 0; u < XT; ++u) {
+      const int q = q0 + u * blockDim.x;
+      if (q < tot) v[u] = q < n0 ? tb.W[q] : (q < n0 + n1 ? tb.pre[q - n0] : tb.post[q - n0 - n1]);
+    }
+#pragma unroll
+    for (int u = 0; u < XT; ++u) {
+      const int q = q0 + u * blockDim.x;
+      if (q < tot) tw[q] = v[u];
+    }
+  }
   __syncthreads();
-  return R2RTables<T>{tw, tw + ntw[0], tw + ntw[0] + ntw[1]};
+  return R2RTables<T>{tw, tw + n0, tw + n0 + n1};
 }
 
 // The line groups of (virtual) block bi: group grp of the block transforms lines
@@ -322,9 +337,9 @@ __global__ void k_xpass(int n, int r0, int nr, int type, FftPlan plan, R2RTables
                         int64_t ibase, int64_t ipitch, const uint8_t* __restrict__ icls, TO* __restrict__ out,
                         int64_t obase, int64_t opitch, const uint8_t* __restrict__ ocls, const double* __restrict__ add,
                         YCorr<T> corr, int gthreads, int gpb, Gate gate) {
-  if (!gate_open(gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const R2RTables<T> ts = xpass_stage_tables<T>(type, n, plan, tb, smem_raw);
+  if (!gate_open(gate)) return;
   xpass_block<T, TI, TO>(blockIdx.x, n, r0, nr, type, plan, ts, in, ibase, ipitch, icls, out, obase, opitch, ocls,
                          add, corr, gthreads, gpb, smem_raw);
 }
@@ -1957,9 +1972,9 @@ template <typename T, typename TI, typename TO>
 __global__ void k_xpass_multi(const __grid_constant__ ArgPack<XpassArgs<T, TI, TO>> p) {
   const XpassArgs<T, TI, TO>& a = p.a[blockIdx.y];
   if ((int)blockIdx.x >= a.nblk) return;
-  if (!gate_open(a.gate)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const R2RTables<T> ts = xpass_stage_tables<T>(a.type, a.n, a.plan, a.tb, smem_raw);
+  if (!gate_open(a.gate)) return;
   xpass_block<T, TI, TO>(blockIdx.x, a.n, a.r0, a.nr, a.type, a.plan, ts, a.in, a.ibase, a.ipitch, a.icls, a.out,
                          a.obase, a.opitch, a.ocls, a.add, a.corr, a.gthreads, a.gpb, smem_raw);
 }

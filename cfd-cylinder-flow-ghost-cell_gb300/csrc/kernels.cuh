@@ -137,9 +137,13 @@ struct Gate {
 };
 __device__ __forceinline__ bool gate_open_thread(const Gate& g) {
   if (!g.ctl) return true;
+  if (g.sweep < 0) {  // both words read at once: one round trip
+    const int err = *(volatile int*)&g.ctl->err;
+    const int act = *(volatile int*)&g.ctl->solve[g.slot].act;
+    return err == 0 && act != 0;
+  }
   if (*(volatile int*)&g.ctl->err) return false;
   if (g.sweep == 0) return true;
-  if (g.sweep < 0) return *(volatile int*)&g.ctl->solve[g.slot].act != 0;
   return sweep_needed(&g.ctl->solve[g.slot], g.sweep);
 }
 // Block-uniform gate: thread 0 decides, every thread of the block gets the same answer
