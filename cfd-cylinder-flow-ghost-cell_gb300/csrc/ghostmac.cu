@@ -2397,7 +2397,7 @@ void residual_group(gm_batch* b, const BatchGroup& G, const std::vector<SolveCal
     const SolveCall& call = calls[c];
     f32 = h->precision == 1;
     void* resb = f32 ? (void*)(call.kind == 0 ? h->pres32.p : h->fres32.p) : (void*)call.res;
-    p->a[c] = residual_args(h->cd, h->rcoef[call.kind], call.kind, call.b, call.x, resb, &h->ctl.p->solve[call.slot],
+    p->a[c] = residual_args(h->cd, h->rcoef[call.kind], call.kind, call.b, call.x, resb, f32, &h->ctl.p->solve[call.slot],
                             body ? -1 : 0, !body, Gate{h->ctl.p, call.slot, body ? -1 : 0});
   }
   launch_residual_multi(*p, n, calls[0].kind, f32, st);

@@ -114,6 +114,14 @@ static inline unsigned reduce_blocks(int64_t n) {
   unsigned b = blocks_for(n);
   return b < 608u ? b : 608u;
 }
+// Blocks of the residual kernels.  Each block ends with its reductions (a warp-shuffle sum
+// costs five adds per thread), so fewer, longer-striding blocks spend less on them.  Measured
+// on the 800x820 case: the FP64 residual (sums in FP64) was fastest at 304 blocks, the
+// FP32-mode residual (sums in FP32, and the FP64 stencil its only FP64 work) at 608.
+static inline unsigned residual_blocks(int64_t n, bool res_f32) {
+  const unsigned b = blocks_for(n), cap = res_f32 ? 608u : 304u;
+  return b < cap ? b : cap;
+}
 __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) { return a > b ? a : b; }
 
 // Host-side count of kernel launches issued by this library (all launchers call note_launch).
@@ -1192,8 +1200,10 @@ void launch_gradient(const CaseDev& c, const double* P, double* out, const Gate&
 // operators I - c L (KIND 1 u faces, KIND 2 v faces), with max |res| and sum res^2 per check.
 // GB300 issues FP64 at 1/64 of the FP32 rate, so the regular rows use coefficients formed on
 // the host (ResidualCoef): two adds and three multiply-adds per point.  RES_F32: the residual
-// is stored in FP32 (the input of the FP32 inverse; its norms are still taken in FP64) and
-// the roundoff bound is left to k_pressure_bound after the refinement loop.
+// is stored in FP32 (the input of the FP32 inverse).  Its max norm, which drives the
+// refinement, is still taken from the FP64 residual; the diagnostic sums of res^2 and b^2 are
+// FP32, so the only FP64 work left is the stencil.  The roundoff bound is left to
+// k_pressure_bound after the refinement loop.
 // coefficient selection by value (indexing the parameter struct would copy it to local memory)
 __device__ __forceinline__ double coef_cc(const ResidualCoef& rc, int ic, int jc) {
   const double c0 = jc ? rc.cc[0][1] : rc.cc[0][0];
@@ -1220,6 +1230,7 @@ __device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCo
   unsigned long long rm = 0, bm = 0, bd = 0, xb = 0;
   double rs = 0.0, bs = 0.0;
   float rs32 = 0.0f;  // RES_F32: sum of the stored FP32 residuals squared (diagnostics only)
+  float bs32 = 0.0f;  // RES_F32: sum of the right-hand side squared in FP32 (diagnostics only)
   for (int64_t t = (int64_t)bid * blockDim.x + threadIdx.x; t < npts; t += (int64_t)nblk * blockDim.x) {
     const uint8_t k = cls[t];
     const int64_t f = base + t;
@@ -1288,7 +1299,15 @@ __device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCo
       rs += r * r;
     }
     if (KIND == 0 && !RES_F32) bd = umax64(bd, dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + fabs(bv))));
-    if (first) { bm = umax64(bm, absbits(bv)); bs += bv * bv; }
+    if (first) {
+      bm = umax64(bm, absbits(bv));
+      if constexpr (RES_F32) {
+        const float b32 = f64_to_f32i(bv);
+        bs32 = fmaf(b32, b32, bs32);
+      } else {
+        bs += bv * bv;
+      }
+    }
     if ((dbits(xv) & 0x7ff0000000000000ull) == 0x7ff0000000000000ull) xb = 1;  // Inf or NaN, by the bits
   }
   block_commit_max(rm, &sc->rmax[check]);
@@ -1297,7 +1316,8 @@ __device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCo
   if (KIND == 0 && !RES_F32) block_commit_max(bd, &sc->bound[check]);
   if (first) {
     block_commit_max(bm, &sc->bmax);
-    block_commit_sum(bs, &sc->bsq);
+    if constexpr (RES_F32) block_commit_sum_f32(bs32, &sc->bsq);
+    else block_commit_sum(bs, &sc->bsq);
   }
   block_commit_max(xb, &sc->xbad);
 }
@@ -1311,7 +1331,7 @@ __global__ void k_residual(CaseDev c, ResidualCoef rc, const double* __restrict_
 void launch_residual(const CaseDev& c, const ResidualCoef& rc, int kind, const double* b, const double* x, void* res,
                      bool res_f32, SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st) {
   const int64_t n = kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize);
-  const unsigned g = reduce_blocks(n);
+  const unsigned g = residual_blocks(n, res_f32);
   const int fc = first_check ? 1 : 0;
   note_launch();
   kt_mark(4, st);
@@ -2089,7 +2109,7 @@ YsolveArgs<T> ysolve_args(const TransformTables& tt, int cols, int rows, T* S, c
   return a;
 }
 ResidualArgs residual_args(const CaseDev& c, const ResidualCoef& rc, int kind, const double* b, const double* x,
-                           void* res, SolveCtl* sc, int check, bool first_check, const Gate& gate) {
+                           void* res, bool res_f32, SolveCtl* sc, int check, bool first_check, const Gate& gate) {
   ResidualArgs a{};
   a.c = c;
   a.rc = rc;
@@ -2100,7 +2120,7 @@ ResidualArgs residual_args(const CaseDev& c, const ResidualCoef& rc, int kind, c
   a.check = check;
   a.first = first_check ? 1 : 0;
   a.gate = gate;
-  a.nblk = (int)reduce_blocks(kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize));
+  a.nblk = (int)residual_blocks(kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize), res_f32);
   return a;
 }
 BoundArgs bound_args(const CaseDev& c, const ResidualCoef& rc, const double* b, const double* x, SolveCtl* sc,

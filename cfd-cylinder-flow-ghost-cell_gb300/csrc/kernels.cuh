@@ -518,7 +518,7 @@ XpassArgs<T, TI, TO> xpass_args(const TransformTables& tt, bool inverse, int r0,
 template <typename T>
 YsolveArgs<T> ysolve_args(const TransformTables& tt, int cols, int rows, T* S, const Gate& gate);
 ResidualArgs residual_args(const CaseDev& c, const ResidualCoef& rc, int kind, const double* b, const double* x,
-                           void* res, SolveCtl* sc, int check, bool first_check, const Gate& gate);
+                           void* res, bool res_f32, SolveCtl* sc, int check, bool first_check, const Gate& gate);
 BoundArgs bound_args(const CaseDev& c, const ResidualCoef& rc, const double* b, const double* x, SolveCtl* sc,
                      int nchk, const Gate& gate);
 // launchers over the first n cases of a pack (tt0: the launch shape shared by the cases)
