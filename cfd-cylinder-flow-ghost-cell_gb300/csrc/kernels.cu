@@ -76,8 +76,20 @@ __device__ void block_commit_sum_f32(float v, double* dst) {
     if (lane == 0 && v != 0.0f) atomicAdd(dst, f32_to_f64i(v));
   }
 }
-// |v| as bits with the sign bit cleared (integer pipe; fabs on a double may issue on the FP64 pipe)
-__device__ __forceinline__ unsigned long long absbits(double v) { return dbits(v) & 0x7fffffffffffffffull; }
+// |v| as bits with the sign bit cleared, on the integer pipe.  Written as PTX: the compiler
+// folds a plain C++ mask of the sign bit back into fabs, which GB300 issues as an FP64 add
+// (counted on a GB300: one extra dadd per point in the residual for each such mask).
+__device__ __forceinline__ unsigned long long absbits(double v) {
+  unsigned long long r;
+  asm("and.b64 %0, %1, 0x7fffffffffffffff;" : "=l"(r) : "l"(dbits(v)));
+  return r;
+}
+// Inf or NaN, by the exponent bits (integer pipe, for the same reason)
+__device__ __forceinline__ bool nonfinite_bits(double v) {
+  unsigned long long r;
+  asm("and.b64 %0, %1, 0x7ff0000000000000;" : "=l"(r) : "l"(dbits(v)));
+  return r == 0x7ff0000000000000ull;
+}
 
 // Launch as a programmatic dependent of the previous kernel on the stream (its launch overlaps
 // that kernel's end; the kernel's gate_open waits for it with griddepcontrol.wait before any
@@ -1308,7 +1320,7 @@ __device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCo
         bs += bv * bv;
       }
     }
-    if ((dbits(xv) & 0x7ff0000000000000ull) == 0x7ff0000000000000ull) xb = 1;  // Inf or NaN, by the bits
+    if (nonfinite_bits(xv)) xb = 1;
   }
   block_commit_max(rm, &sc->rmax[check]);
   if constexpr (RES_F32) block_commit_sum_f32(rs32, &sc->rsq[check]);
@@ -1566,7 +1578,7 @@ __global__ void k_divergence(CaseDev c, const double* __restrict__ U, double* __
       if (out) {
         double o = d * dt;  // dt carries 1/dt (or 1)
         out[t] = o;
-        bad = bad || !isfinite(o);
+        bad = bad || nonfinite_bits(o);
       }
     } else if (out) {
       out[t] = 0.0;
