@@ -80,7 +80,15 @@ __host__ __device__ __forceinline__ float f64_to_f32i(double x) {
   const uint64_t b = bit_as<uint64_t>(x);
   const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
   const uint32_t e0 = (uint32_t)(b >> 52) & 0x7ffu;
+#ifdef __CUDA_ARCH__
+  // the mask as PTX: the compiler folds a C++ mask of the sign bit into fabs, an FP64 add
+  // (counted on a GB300: one dadd per conversion in the FP32-mode residual, gone with this)
+  uint64_t m;
+  asm("and.b64 %0, %1, 0x7fffffffffffffff;" : "=l"(m) : "l"(b));
+  const uint64_t a = m + (1ull << 28);  // rounding carry may bump the exponent
+#else
   const uint64_t a = (b & 0x7fffffffffffffffull) + (1ull << 28);  // rounding carry may bump the exponent
+#endif
   const uint32_t e = (uint32_t)(a >> 52);
   uint32_t r;
   if (e0 == 0x7ffu) r = (b & 0xfffffffffffffull) ? 0x7fc00000u : 0x7f800000u;
