@@ -84,6 +84,8 @@ __device__ __forceinline__ unsigned long long absbits(double v) {
   asm("and.b64 %0, %1, 0x7fffffffffffffff;" : "=l"(r) : "l"(dbits(v)));
   return r;
 }
+// |v| (the same value as fabs) on the integer pipe
+__device__ __forceinline__ double absd(double v) { return bits2d(absbits(v)); }
 // Inf or NaN, by the exponent bits (integer pipe, for the same reason)
 __device__ __forceinline__ bool nonfinite_bits(double v) {
   unsigned long long r;
@@ -1260,7 +1262,7 @@ __device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCo
       const int64_t e0 = cp[row], e1 = cp[row + 1];
       csr_row<4>(c.irr_col[KIND], c.irr_val[KIND], e0, e1, x, base, [&](double a, double xv2) {
         ax += a * xv2;
-        if (KIND == 0 && !RES_F32) aabs += fabs(a) * fabs(xv2);
+        if (KIND == 0 && !RES_F32) aabs += absd(a) * absd(xv2);
       });
       nnz = (int)(e1 - e0);
     } else {
@@ -1296,7 +1298,7 @@ __device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCo
       const double ccv = coef_cc(rc, ic, jc), cwv = coef_cw(rc, ic);
       ax = fma(rc.cy, xs + xn, fma(rc.ce, xe, fma(cwv, xw, ccv * xv)));
       if (KIND == 0 && !RES_F32) {
-        aabs = fabs(ccv) * fabs(xv) + rc.ce * (fabs(xw) + fabs(xe)) + rc.cy * (fabs(xs) + fabs(xn));
+        aabs = absd(ccv) * absd(xv) + rc.ce * (absd(xw) + absd(xe)) + rc.cy * (absd(xs) + absd(xn));
         nnz = c.a_nnz[t];
       }
     }
@@ -1310,7 +1312,7 @@ __device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCo
       res64[f] = r;
       rs += r * r;
     }
-    if (KIND == 0 && !RES_F32) bd = umax64(bd, dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + fabs(bv))));
+    if (KIND == 0 && !RES_F32) bd = umax64(bd, dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + absd(bv))));
     if (first) {
       bm = umax64(bm, absbits(bv));
       if constexpr (RES_F32) {

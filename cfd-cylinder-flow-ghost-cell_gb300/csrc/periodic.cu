@@ -62,6 +62,13 @@ struct Buf {
 
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 __device__ __forceinline__ unsigned long long dbits_(double v) { return (unsigned long long)__double_as_longlong(v); }
+// |v| as bits, on the integer pipe: the mask is PTX because the compiler turns fabs, or a C++
+// mask of the sign bit, into an FP64 instruction
+__device__ __forceinline__ unsigned long long absbits_(double v) {
+  unsigned long long r;
+  asm("and.b64 %0, %1, 0x7fffffffffffffff;" : "=l"(r) : "l"(dbits_(v)));
+  return r;
+}
 
 __device__ void commit_max(unsigned long long v, unsigned long long* dst) {
   for (int o = 16; o > 0; o >>= 1) {
@@ -155,8 +162,8 @@ __global__ void k_tg_hres(int n, double h, double nu, double hdt, const double* 
     const double hx = x[t] - hdt * lap_p<double>(f, n, j, i, h, nu);
     const double rv = b[t] - hx;
     if (r) r[t] = rv;
-    rm = max(rm, dbits_(fabs(rv)));
-    if (bmax) bm = max(bm, dbits_(fabs(b[t])));
+    rm = max(rm, absbits_(rv));
+    if (bmax) bm = max(bm, absbits_(b[t]));
   }
   commit_max(rm, rmax);
   if (bmax) commit_max(bm, bmax);
@@ -171,7 +178,7 @@ __global__ void k_tg_div(int n, double h, double inv_step, const double* __restr
     const int j = k / n, i = k - j * n;
     const double dv = (q[j * n + wrapi(i + 1, n)] - q[k] + q[nn + wrapi(j + 1, n) * n + i] - q[nn + k]) / h;
     if (d) d[k] = dv * inv_step;
-    m = max(m, dbits_(fabs(dv)));
+    m = max(m, absbits_(dv));
   }
   if (dmax) commit_max(m, dmax);
 }
@@ -187,7 +194,7 @@ __global__ void k_tg_pres(int n, double h, const double* __restrict__ b, const d
                        (x[wrapi(j + 1, n) * n + i] - x[k]) - (x[k] - x[wrapi(j - 1, n) * n + i])) / (h * h);
     const double rv = b[k] - ax;
     r[k] = rv;
-    rm = max(rm, dbits_(fabs(rv)));
+    rm = max(rm, absbits_(rv));
   }
   commit_max(rm, rmax);
 }
@@ -225,7 +232,7 @@ __global__ void k_tg_pout(int n, double h, double dt, double factor, const doubl
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 2 * nn; t += gridDim.x * blockDim.x) {
     const int comp = t >= nn, k = t - comp * nn, j = k / n, i = k - j * n;
     const double g = comp == 0 ? (inc[k] - inc[j * n + wrapi(i - 1, n)]) / h : (inc[k] - inc[wrapi(j - 1, n) * n + i]) / h;
-    m = max(m, dbits_(fabs(action[t] - rhs[t] + dt * g)));
+    m = max(m, absbits_(action[t] - rhs[t] + dt * g));
     if (comp == 0) {
       const double hv = p[k] + inc[k];
       half[k] = hv;
