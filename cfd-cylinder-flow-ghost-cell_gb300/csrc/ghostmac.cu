@@ -119,11 +119,12 @@ struct RectDev {
   DBuf<float> bpiv32, phi32, psi32, band32;
   // direct sums of the boundary term (build_direct_tables): the inverse row transform at the
   // mcount points (spectrum row of each, coefficients mcount x cols), the forward row transform
-  // of a unit value at each boundary row (band-row order: bptr over band rows, bperm to the
-  // rank index), the Schur values c and the transformed values at the points
+  // of a unit value at each boundary row (band-row order: bptr over band rows), M with its rows
+  // in the same band-row order (so the GEMV writes the Schur values c already in that order),
+  // c, and the transformed values at the points
   bool direct = false;
-  DBuf<int32_t> mrow, bptr, bperm;
-  DBuf<double> binv, bfwd, cvec, firstm;
+  DBuf<int32_t> mrow, bptr;
+  DBuf<double> binv, bfwd, mband, cvec, firstm;
   DBuf<float> binv32, bfwd32, firstm32;
 };
 
@@ -645,7 +646,7 @@ void build_band_tables(gm_handle* h, RectDev& rd, const std::vector<int64_t>& ro
 // sum per band entry, instead of row transforms of the C rows and of the band rows.  Grids
 // whose tables would exceed 64 MB keep the row-transform chain.
 void build_direct_tables(gm_handle* h, RectDev& rd, const std::vector<int64_t>& rows,
-                         const std::vector<int64_t>& ucol) {
+                         const std::vector<int64_t>& ucol, const std::vector<double>& M) {
   rd.direct = false;
   const int n = rd.view.cols, m = rd.mcount, rank = rd.rank;
   const TransformTables& tt = rd.tt;
@@ -695,7 +696,10 @@ void build_direct_tables(gm_handle* h, RectDev& rd, const std::vector<int64_t>& 
   for (int j = 0; j < nb; ++j) ptr[j + 1] += ptr[j];
   rd.mrow.upload(mrow, st);
   rd.bptr.upload(ptr, st);
-  rd.bperm.upload(perm, st);
+  std::vector<double> mband((size_t)rank * rd.mcount);
+  for (int e2 = 0; e2 < rank; ++e2)
+    std::copy_n(&M[(size_t)perm[e2] * rd.mcount], rd.mcount, &mband[(size_t)e2 * rd.mcount]);
+  rd.mband.upload(mband, st);
   rd.binv.upload(binv, st);
   rd.bfwd.upload(bfwd, st);
   rd.cvec.alloc(rank);
@@ -778,7 +782,7 @@ void build_schur(gm_handle* h, RectDev& rd, const std::vector<int64_t>& rows, co
   rd.mmat.upload(M, st);
   rd.mcount = m;
   build_band_tables(h, rd, rows, C);
-  build_direct_tables(h, rd, rows, ucol);
+  build_direct_tables(h, rd, rows, ucol, M);
 }
 
 // Regular-row coefficients of the residual kernels (see ResidualCoef): the pressure operator
@@ -962,9 +966,9 @@ void schur_inverse(gm_handle* h, RectDev& rd, const TransformTables& tt, const v
     launch_band_first<T>(rd.mcount, v.cols, rd.mrow.p, f32 ? (const T*)rd.binv32.p : (const T*)rd.binv.p, spectral, fm,
                          g, st);
     sweep_mark(h, 3, st);
-    launch_band_gemv<T>(rd.rank, rd.mcount, rd.mmat.p, fm, rd.cvec.p, g, st);
+    launch_band_gemv<T>(rd.rank, rd.mcount, rd.mband.p, fm, rd.cvec.p, g, st);
     sweep_mark(h, 4, st);
-    launch_band_fwd_solve<T>(tt, v.cols, rd.rank, rd.bptr.p, rd.bperm.p, rd.cvec.p,
+    launch_band_fwd_solve<T>(tt, v.cols, rd.rank, rd.bptr.p, rd.cvec.p,
                              f32 ? (const T*)rd.bfwd32.p : (const T*)rd.bfwd.p, band, g, st);
     sweep_mark(h, 5, st);
     corr = YCorr<T>{band, (const T*)tt.phi, (const T*)tt.psi, tt.bj0, tt.bj1};
@@ -2370,9 +2374,9 @@ void apply_inverse_group(gm_batch* b, const BatchGroup& G, int lane, const std::
     T* fm = f32 ? (T*)rd.firstm32.p : (T*)rd.firstm.p;
     bf->a[c] = BandFirstArgs<T>{rd.mcount, v.cols, rd.mrow.p, f32 ? (const T*)rd.binv32.p : (const T*)rd.binv.p, spec,
                                 fm, g};
-    bg->a[c] = BandGemvArgs<T>{rd.rank, rd.mcount, rd.mmat.p, fm, rd.cvec.p, g};
+    bg->a[c] = BandGemvArgs<T>{rd.rank, rd.mcount, rd.mband.p, fm, rd.cvec.p, g};
     T* band = f32 ? (T*)rd.band32.p : (T*)rd.band.p;
-    bw->a[c] = BandFwdArgs<T>{tt.bj1 - tt.bj0 + 1, v.cols, rd.rank, rd.bptr.p, rd.bperm.p, rd.cvec.p,
+    bw->a[c] = BandFwdArgs<T>{tt.bj1 - tt.bj0 + 1, v.cols, rd.rank, rd.bptr.p, rd.cvec.p,
                               f32 ? (const T*)rd.bfwd32.p : (const T*)rd.bfwd.p, (T)tt.gamma, (T)tt.yscale,
                               (const T*)tt.bpiv, band, g, band_fwd_blocks(v.cols)};
     const YCorr<T> corr{band, (const T*)tt.phi, (const T*)tt.psi, tt.bj0, tt.bj1};

@@ -799,16 +799,16 @@ __global__ void __launch_bounds__(BAND_TPB) k_band_gemv(int rank, int m, const d
 static constexpr int BAND_COLS = 16, BAND_ROWT = 16;
 template <typename T>
 __device__ __forceinline__ void band_fwd_solve_body(int nb, int n, int rank, const int32_t* __restrict__ bptr,
-                                                    const int32_t* __restrict__ bperm, const double* __restrict__ c,
+                                                    const double* __restrict__ c,
                                                     const T* __restrict__ bfwd, T gamma, T scale,
                                                     const T* __restrict__ bpiv, T* __restrict__ band, int bid) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* cs = reinterpret_cast<T*>(smem_raw);   // rank values c, band-row order
+  T* cs = reinterpret_cast<T*>(smem_raw);   // rank values c (band-row order, as the GEMV writes them)
   T* xb = cs + ((rank + 3) & ~3);           // nb x BAND_COLS
   T* pb = xb + (size_t)nb * BAND_COLS;      // nb x BAND_COLS
   int* ps = reinterpret_cast<int*>(pb + (size_t)nb * BAND_COLS);  // nb + 1 row pointers
   const int tid = threadIdx.x, kk = tid % BAND_COLS, jt = tid / BAND_COLS;
-  for (int e = tid; e < rank; e += blockDim.x) cs[e] = cvt_to<T>(c[bperm[e]]);
+  for (int e = tid; e < rank; e += blockDim.x) cs[e] = cvt_to<T>(c[e]);
   for (int j = tid; j <= nb; j += blockDim.x) ps[j] = bptr[j];
   __syncthreads();
   const int k = bid * BAND_COLS + kk;
@@ -847,11 +847,11 @@ __device__ __forceinline__ void band_fwd_solve_body(int nb, int n, int rank, con
 }
 template <typename T>
 __global__ void __launch_bounds__(BAND_COLS * BAND_ROWT) k_band_fwd_solve(
-    int nb, int n, int rank, const int32_t* __restrict__ bptr, const int32_t* __restrict__ bperm,
+    int nb, int n, int rank, const int32_t* __restrict__ bptr,
     const double* __restrict__ c, const T* __restrict__ bfwd, T gamma, T scale, const T* __restrict__ bpiv,
     T* __restrict__ band, Gate gate) {
   if (!gate_open(gate)) return;
-  band_fwd_solve_body<T>(nb, n, rank, bptr, bperm, c, bfwd, gamma, scale, bpiv, band, blockIdx.x);
+  band_fwd_solve_body<T>(nb, n, rank, bptr, c, bfwd, gamma, scale, bpiv, band, blockIdx.x);
 }
 
 int band_fwd_blocks(int n) { return (n + BAND_COLS - 1) / BAND_COLS; }
@@ -879,14 +879,14 @@ void launch_band_gemv(int rank, int m, const double* M, const T* firstm, double*
   kt_mark(5, st, (double)rank * m * 8 + (double)m * sizeof(T) + rank * 8.0);
 }
 template <typename T>
-void launch_band_fwd_solve(const TransformTables& tt, int n, int rank, const int32_t* bptr, const int32_t* bperm,
-                           const double* c, const T* bfwd, T* band, const Gate& gate, cudaStream_t st) {
+void launch_band_fwd_solve(const TransformTables& tt, int n, int rank, const int32_t* bptr, const double* c,
+                           const T* bfwd, T* band, const Gate& gate, cudaStream_t st) {
   const int nb = tt.bj1 - tt.bj0 + 1;
   if (nb <= 0) return;
   note_launch();
   kt_mark(5, st);
   launch_pdl(k_band_fwd_solve<T>, dim3((unsigned)((n + BAND_COLS - 1) / BAND_COLS)), dim3(BAND_COLS * BAND_ROWT),
-             band_fwd_smem(nb, rank, sizeof(T) == 4), st, nb, n, rank, bptr, bperm, c, bfwd, (T)tt.gamma,
+             band_fwd_smem(nb, rank, sizeof(T) == 4), st, nb, n, rank, bptr, c, bfwd, (T)tt.gamma,
              (T)tt.yscale, (const T*)tt.bpiv, band, gate);
   // the forward coefficients, the values c, the pivots and the band written once
   kt_mark(5, st, (double)rank * n * sizeof(T) + rank * 8.0 + (double)nb * n * 2 * sizeof(T));
@@ -897,10 +897,10 @@ template void launch_band_first<float>(int, int, const int32_t*, const float*, c
                                        cudaStream_t);
 template void launch_band_gemv<double>(int, int, const double*, const double*, double*, const Gate&, cudaStream_t);
 template void launch_band_gemv<float>(int, int, const double*, const float*, double*, const Gate&, cudaStream_t);
-template void launch_band_fwd_solve<double>(const TransformTables&, int, int, const int32_t*, const int32_t*,
-                                            const double*, const double*, double*, const Gate&, cudaStream_t);
-template void launch_band_fwd_solve<float>(const TransformTables&, int, int, const int32_t*, const int32_t*,
-                                           const double*, const float*, float*, const Gate&, cudaStream_t);
+template void launch_band_fwd_solve<double>(const TransformTables&, int, int, const int32_t*, const double*,
+                                            const double*, double*, const Gate&, cudaStream_t);
+template void launch_band_fwd_solve<float>(const TransformTables&, int, int, const int32_t*, const double*,
+                                           const float*, float*, const Gate&, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // sparse rows with their loads batched: the column indices and values of up to CSR_B entries
@@ -2039,7 +2039,7 @@ __global__ void __launch_bounds__(BAND_COLS * BAND_ROWT) k_band_fwd_solve_multi(
   const BandFwdArgs<T>& a = p.a[blockIdx.y];
   if ((int)blockIdx.x >= a.nblk) return;
   if (!gate_open(a.gate)) return;
-  band_fwd_solve_body<T>(a.nb, a.n, a.rank, a.bptr, a.bperm, a.c, a.bfwd, a.gamma, a.scale, a.bpiv, a.band,
+  band_fwd_solve_body<T>(a.nb, a.n, a.rank, a.bptr, a.c, a.bfwd, a.gamma, a.scale, a.bpiv, a.band,
                          blockIdx.x);
 }
 template <int KIND, bool RES_F32>

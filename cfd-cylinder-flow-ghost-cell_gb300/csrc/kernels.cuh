@@ -292,14 +292,14 @@ void launch_yband(const TransformTables& tt, int cols, T* B, const Gate& gate, c
 template <typename T>
 void launch_band_first(int m, int n, const int32_t* mrow, const T* binv, const T* spec, T* firstm, const Gate& gate,
                        cudaStream_t st);
-//   c[r] = sum_q M[r][q] firstm[q]                      (FP64 GEMV, M = S^{-1} C)
+//   c[r] = sum_q M[r][q] firstm[q]                      (FP64 GEMV, M = S^{-1} C, rows in band-row order)
 template <typename T>
 void launch_band_gemv(int rank, int m, const double* M, const T* firstm, double* c, const Gate& gate,
                       cudaStream_t st);
-//   band[j][k] = band solve of ( sum_{e in band row j} c[bperm[e]] bfwd[e][k] ) per column k
+//   band[j][k] = band solve of ( sum_{e in band row j} c[e] bfwd[e][k] ) per column k
 template <typename T>
-void launch_band_fwd_solve(const TransformTables& tt, int n, int rank, const int32_t* bptr, const int32_t* bperm,
-                           const double* c, const T* bfwd, T* band, const Gate& gate, cudaStream_t st);
+void launch_band_fwd_solve(const TransformTables& tt, int n, int rank, const int32_t* bptr, const double* c,
+                           const T* bfwd, T* band, const Gate& gate, cudaStream_t st);
 // shared memory of launch_band_fwd_solve (the direct path needs it within the default 48 KB)
 // and its blocks for n columns
 size_t band_fwd_smem(int nb, int rank, bool fp32);
@@ -489,7 +489,7 @@ struct BandGemvArgs {
 template <typename T>
 struct BandFwdArgs {
   int nb, n, rank;
-  const int32_t* bptr; const int32_t* bperm;
+  const int32_t* bptr;
   const double* c;
   const T* bfwd;
   T gamma, scale;
