@@ -79,8 +79,8 @@ DRAM_TRAFFIC = {
     # profiles/k_xpass_fp64_wide_800x820.md: the forward and inverse row passes of the first
     # Helmholtz solve, (2048 + 3328 + 1792 + 9216) / 2
     ('wide_800x820_re100', 'fp64', 1): 8192.0,
-    # profiles/fp32_mode_wide_800x820.md: the two row passes of the first sweep, (256 + 512) / 2
-    ('wide_800x820_re100', 'fp32', 1): 384.0,
+    # profiles/fp32_mode_wide_800x820.md: the two row passes of the first sweep, (256 + 1024) / 2
+    ('wide_800x820_re100', 'fp32', 1): 640.0,
 }
 KERNEL_CLASSES = {1: 'row transforms (k_xpass)', 2: 'column solves (k_ysolve, k_yband)',
                   3: 'momentum rhs (k_momentum, k_shadow)', 4: 'operator residual (k_residual, k_pressure_bound)',
