@@ -1417,7 +1417,8 @@ void step_phase3(gm_handle* h) {
   Gate g0 = gate_of(h);
   project_post(h, h->fproj.p, dt, h->fproj2.p, h->pinc.p, S_P2, 2);
   phase_mark(h, 5, st);
-  ghost_p(h, h->pinc.p, g0);
+  // pinc already carries its ghost values: project_post extended it, and the extension rows
+  // read active cells only, so extending it again would rewrite the same values
   const bool first = !h->has_history;
   double factor = first ? 1.0 : dt / (dt + h->prev_dt);
   launch_pressure_out(h->cd, h->phalf.p, h->pinc.p, factor, dt, h->faction.p, h->rhs.p, h->phalf_next.p, h->pout.p,
