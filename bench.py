@@ -77,8 +77,8 @@ DEFAULT_WORKLOAD = 'wide_800x820_re100'
 # traffic is far below the algorithmic bytes.
 DRAM_TRAFFIC = {
     # profiles/k_xpass_fp64_wide_800x820.md: the forward and inverse row passes of the first
-    # Helmholtz solve, (2048 + 3328 + 1792 + 9216) / 2
-    ('wide_800x820_re100', 'fp64', 1): 8192.0,
+    # Helmholtz solve, (768 + 1024 + 4608 + 1024) / 2
+    ('wide_800x820_re100', 'fp64', 1): 3712.0,
     # profiles/fp32_mode_wide_800x820.md: the two row passes of the first sweep, (256 + 1024) / 2
     ('wide_800x820_re100', 'fp32', 1): 640.0,
 }
