@@ -27,7 +27,8 @@ SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_las
            'gm_batch_step', 'gm_phase_timing', 'gm_tg_create', 'gm_tg_destroy', 'gm_tg_last_error',
            'gm_tg_set_state', 'gm_tg_get_state', 'gm_tg_step', 'gm_unet_layers', 'gm_unet_create',
            'gm_unet_destroy', 'gm_unet_last_error', 'gm_unet_input', 'gm_unet_forward', 'gm_unet_backward',
-           'gm_set_learned_preconditioner', 'gm_set_pressure_recorder', 'gm_pressure_recorded')
+           'gm_set_learned_preconditioner', 'gm_set_pressure_recorder', 'gm_pressure_recorded',
+           'gm_host_alloc', 'gm_host_free')
 NOALLOC_MAX_CELLS = 1048576
 
 
@@ -117,6 +118,8 @@ def _load():
         'gm_set_learned_preconditioner': ([P, P, P, P], C.c_int),
         'gm_set_pressure_recorder': ([P, P, P, I32], C.c_int),
         'gm_pressure_recorded': ([P], I32),
+        'gm_host_alloc': ([C.c_size_t, pp], C.c_int),
+        'gm_host_free': ([P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -1834,6 +1834,26 @@ int gm_get_surface_points(const gm_handle* h, double* yx) {
   return GM_OK;
 }
 
+int gm_host_alloc(size_t bytes, void** out) {
+  if (!out) return GM_EVALUE;
+  *out = nullptr;
+  if (bytes == 0) return GM_OK;
+  if (cudaMallocHost(out, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    return GM_ECUDA;
+  }
+  return GM_OK;
+}
+int gm_host_free(void* p) {
+  if (!p) return GM_OK;
+  if (cudaFreeHost(p) != cudaSuccess) {
+    cudaGetLastError();
+    return GM_ECUDA;
+  }
+  return GM_OK;
+}
+
 int gm_set_state(gm_handle* h, const double* u, const double* v, const double* p) {
   if (!h) return GM_EVALUE;
   if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }

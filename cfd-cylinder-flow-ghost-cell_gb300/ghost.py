@@ -16,6 +16,7 @@ import json
 import os
 import tempfile
 import time as _time
+import weakref
 from pathlib import Path
 from types import SimpleNamespace
 
@@ -25,6 +26,20 @@ from . import _lib
 from ._lib import check, lib, ptr
 
 _PKG = Path(__file__).resolve().parent
+
+
+def pinned_empty(shape):
+    """A float64 numpy array in page-locked host memory (gm_host_alloc), so that the state
+    copies of every solve() run by DMA; an ordinary np.empty when none can be had.  The
+    memory is freed when the last array viewing it is collected."""
+    n = int(np.prod(shape))
+    p = C.c_void_p()
+    if n == 0 or lib.gm_host_alloc(C.c_size_t(n * 8), C.byref(p)) != _lib.GM_OK or not p.value:
+        return np.empty(shape)
+    buf = (C.c_double * n).from_address(p.value)
+    fin = weakref.finalize(buf, lib.gm_host_free, C.c_void_p(p.value))
+    fin.atexit = False  # the CUDA runtime may be gone by then; the process exit frees it
+    return np.frombuffer(buf, dtype=np.float64).reshape(shape)
 
 
 def _f64(a):
@@ -271,9 +286,9 @@ class MAC_CylinderFlow:
         else:
             self.u_inlet = np.full(self.ny, float(U_inf))
         self.u_inlet_base = self.u_inlet.copy()
-        self.u = np.empty((self.ny, self.nx + 1))
-        self.v = np.empty((self.ny + 1, self.nx))
-        self.p = np.empty((self.ny, self.nx))
+        self.u = pinned_empty((self.ny, self.nx + 1))
+        self.v = pinned_empty((self.ny + 1, self.nx))
+        self.p = pinned_empty((self.ny, self.nx))
         self.phi = np.zeros((self.ny, self.nx))
         self.gg = GhostCellIntegrator(h, self)
         self._pull()

@@ -271,6 +271,15 @@ int32_t gm_pressure_recorded(const gm_handle* h);
 int gm_divergence_stats_noalloc(const double* u, const double* v, const uint8_t* mask, int32_t nx, int32_t ny,
                                 double dx, double dy, double out[3], int64_t counts[2], void* cuda_stream);
 
+/* --- page-locked host memory (no reference counterpart) ------------------------ */
+
+/* Page-locked host allocation (cudaMallocHost) for arrays that cross the bus every step, such
+ * as the facade's state arrays: gm_set_state / gm_get_state then copy them by DMA at full link
+ * speed instead of staging pageable memory.  *out = NULL and GM_ECUDA when none can be had
+ * (no device); callers then use ordinary memory.  gm_host_free(NULL) is a no-op. */
+int gm_host_alloc(size_t bytes, void** out);
+int gm_host_free(void* p);
+
 /* --- instrumentation (no reference counterpart) -------------------------------- */
 
 /* Number of CUDA kernels this library has launched in this process. */
@@ -278,9 +287,11 @@ int64_t gm_kernel_launches(void);
 /* Event times (ms) of the last step run by gm_step when the environment variable
  * GHOSTMAC_PHASE_TIMING=1 was set.  out[0..5]: the phases momentum right-hand side, Helmholtz
  * solves, projection 1, defect, projection 2, pressure output / forces / gates.  out[6..13]:
- * the kernels of the first sweep of projection 1 (row pass, column solve, band row pass,
- * Schur GEMV, band row pass, band solve, final row pass, residual).  The events are recorded
- * inside the step graphs, so they time graph-replayed steps. */
+ * the first sweep of projection 1 between consecutive marks: row pass, column solve, the
+ * boundary term's three kernels (point values, Schur GEMV, band values and band solve; with
+ * the row-transform chain: band row pass, Schur GEMV, band row pass), the band solve of that
+ * chain (empty on the direct path), final row pass, residual.  The events are recorded inside
+ * the step graphs, so they time graph-replayed steps. */
 int gm_phase_timing(const gm_handle* h, double out[14]);
 /* CUDA-event timing of every launch on the stream it runs on, summed per kernel class:
  * 1 row transforms, 2 column solves, 3 momentum right-hand side, 4 operator residual,
