@@ -60,6 +60,25 @@ def test_library_exports_every_declared_symbol(L):
         assert hasattr(L.lib, name), name
 
 
+def test_host_alloc_with_or_without_a_device(L):
+    """gm_host_alloc gives page-locked memory on a GPU machine and GM_ECUDA with a NULL
+    pointer without one; the facade's pinned_empty then falls back to an ordinary array."""
+    import sys
+    p = C.c_void_p()
+    rc = L.lib.gm_host_alloc(C.c_size_t(64), C.byref(p))
+    if rc == L.GM_OK:
+        assert p.value
+        assert L.lib.gm_host_free(p) == L.GM_OK
+    else:
+        assert rc == L.GM_ECUDA and not p.value
+    assert L.lib.gm_host_free(None) == L.GM_OK
+    ghost = sys.modules[load_package().__name__ + '.ghost']
+    a = ghost.pinned_empty((3, 5))
+    assert a.shape == (3, 5) and a.dtype == np.float64 and a.flags.writeable and a.flags.c_contiguous
+    a[:] = 1.5
+    assert float(a.sum()) == 22.5
+
+
 @pytest.mark.parametrize('args,kw', CASES)
 def test_setup_matches_oracle(L, args, kw):
     h = host_handle(L, *args, **kw)
