@@ -1407,7 +1407,7 @@ SolveCall step_phase2(gm_handle* h) {
   const double dt = h->step_dt;
   project_post(h, h->star.p, dt, h->Unext.p, h->pphi.p, S_P1, 1);
   phase_mark(h, 3, st);
-  launch_defect(h->cd, h->Unext.p, h->rhs.p, 0.5 * dt, h->faction.p, h->fproj.p, gate_of(h), st);
+  launch_defect(h->cd, h->rcoef[1], h->rcoef[2], h->Unext.p, h->rhs.p, h->faction.p, h->fproj.p, gate_of(h), st);
   phase_mark(h, 4, st);
   return project_pre(h, h->fproj.p, dt, h->pinc.p, S_P2);
 }

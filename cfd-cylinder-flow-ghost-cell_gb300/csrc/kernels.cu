@@ -1623,8 +1623,52 @@ void launch_project_update(const CaseDev& c, const double* q, const double* phi,
   kt_mark(6, st);
 }
 
-__global__ void k_defect(CaseDev c, const double* __restrict__ r, const double* __restrict__ rhs, double hdt,
-                         double* __restrict__ action, double* __restrict__ proj, Gate gate) {
+// H r at an active u (KIND 1) or v (KIND 2) face t (index within its face grid) for the
+// Helmholtz operator H = I - c L of the CN solves: the same rows as residual_body's, i.e. the
+// host-formed coefficients on regular rows (one add, one multiply, three fused multiply-adds)
+// and the folded sparse rows next to the body.
+template <int KIND>
+__device__ __forceinline__ double helm_action(const CaseDev& c, const ResidualCoef& rc, const double* __restrict__ x,
+                                              int64_t t, uint8_t k) {
+  const int nx = c.nx, ny = c.ny;
+  const int w = KIND == 1 ? nx + 1 : nx;
+  const int64_t base = KIND == 2 ? c.usize : 0;
+  const int64_t f = base + t;
+  const int row = (k & CLS_IRREG) ? c.irr_index[KIND][t] : -1;
+  if (row >= 0) {
+    const int64_t* cp = c.irr_ptr[KIND];
+    double ax = 0.0;
+    csr_row<4>(c.irr_col[KIND], c.irr_val[KIND], cp[row], cp[row + 1], x, base,
+               [&](double a, double xv2) { ax += a * xv2; });
+    return ax;
+  }
+  const int j = (int)((unsigned)t / (unsigned)w), i = (int)((unsigned)t - (unsigned)j * w);
+  double xw = 0.0, xe = 0.0, xs = 0.0, xn = 0.0;
+  int ic, jc;
+  if (KIND == 1) {
+    if (i > 1) xw = x[f - 1];
+    if (i < nx) xe = x[f + 1];
+    if (j > 0) xs = x[f - w];
+    if (j < ny - 1) xn = x[f + w];
+    ic = i == nx ? 2 : 1;
+    jc = (j == 0 || j == ny - 1) ? 0 : 1;
+  } else {
+    if (i > 0) xw = x[f - 1];
+    if (i < nx - 1) xe = x[f + 1];
+    if (j > 1) xs = x[f - w];
+    if (j < ny - 1) xn = x[f + w];
+    ic = i == 0 ? 0 : (i == nx - 1 ? 2 : 1);
+    jc = 1;
+  }
+  const double ccv = coef_cc(rc, ic, jc), cwv = coef_cw(rc, ic);
+  return fma(rc.cy, xs + xn, fma(rc.ce, xe, fma(cwv, xw, ccv * x[f])));
+}
+
+// Defect correction of the CN velocity (solver/time_integration.py): action = H r and
+// proj = r + (rhs - H r) at the active faces; inlet values and zeros elsewhere.
+__global__ void k_defect(CaseDev c, ResidualCoef rcu, ResidualCoef rcv, const double* __restrict__ r,
+                         const double* __restrict__ rhs, double* __restrict__ action, double* __restrict__ proj,
+                         Gate gate) {
   if (!gate_open(gate)) return;
   const Grid g{c.nx, c.ny, c.usize};
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1636,17 +1680,15 @@ __global__ void k_defect(CaseDev c, const double* __restrict__ r, const double* 
     proj[t] = (comp == 0 && i == 0) ? c.inlet[j] : 0.0;
     return;
   }
-  const double idx2 = c.idx2, idy2 = c.idy2;
-  double l = comp == 0 ? c.nu * lap_u<double>(r, g, j, i, idx2, idy2, false) : c.nu * lap_v<double>(r, g, j, i, idx2, idy2);
-  double hr = r[t] - hdt * l;
+  const double hr = comp == 0 ? helm_action<1>(c, rcu, r, t, cls) : helm_action<2>(c, rcv, r, t - c.usize, cls);
   action[t] = hr;
   proj[t] = r[t] + (rhs[t] - hr);
 }
-void launch_defect(const CaseDev& c, const double* result, const double* rhs, double hdt, double* action,
-                   double* proj, const Gate& gate, cudaStream_t st) {
+void launch_defect(const CaseDev& c, const ResidualCoef& rcu, const ResidualCoef& rcv, const double* result,
+                   const double* rhs, double* action, double* proj, const Gate& gate, cudaStream_t st) {
   note_launch();
   kt_mark(7, st);
-  k_defect<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, result, rhs, hdt, action, proj, gate);
+  k_defect<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, rcu, rcv, result, rhs, action, proj, gate);
   kt_mark(7, st);
 }
 

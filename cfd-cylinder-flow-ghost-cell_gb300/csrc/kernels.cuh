@@ -379,9 +379,10 @@ void launch_divergence(const CaseDev& c, const double* U, double* out, double sc
 void launch_project_update(const CaseDev& c, const double* q, const double* phi, double dt, double* out,
                            const SolveCtl* psolve, const Gate& gate, cudaStream_t st);
 
-// action = H result; proj = result + (rhs - action)
-void launch_defect(const CaseDev& c, const double* result, const double* rhs, double hdt, double* action,
-                   double* proj, const Gate& gate, cudaStream_t st);
+// action = H result; proj = result + (rhs - action), H = I - c L of the CN solves with the
+// residual's coefficients (rcu: u faces, rcv: v faces)
+void launch_defect(const CaseDev& c, const ResidualCoef& rcu, const ResidualCoef& rcv, const double* result,
+                   const double* rhs, double* action, double* proj, const Gate& gate, cudaStream_t st);
 
 // half = p + inc; out = half + factor*inc (active p); coupled = max|action - rhs + dt G inc|
 void launch_pressure_out(const CaseDev& c, const double* p, const double* inc, double factor, double dt,
