@@ -1599,8 +1599,10 @@ void launch_divergence(const CaseDev& c, const double* U, double* out, double sc
   kt_mark(6, st);
 }
 
-__global__ void k_project_update(CaseDev c, const double* __restrict__ q, const double* __restrict__ phi, double dt,
-                                 double* __restrict__ out, Gate gate) {
+// out = q - dt G phi at the active faces, with dgx = dt gx and dgy = dt gy formed on the host:
+// two fused multiply-adds per face (G phi is gx (phi_e - phi_w), at the outlet -2 gx phi_w)
+__global__ void k_project_update(CaseDev c, const double* __restrict__ q, const double* __restrict__ phi, double dgx,
+                                 double dgy, double* __restrict__ out, Gate gate) {
   if (!gate_open(gate)) return;
   const Grid g{c.nx, c.ny, c.usize};
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1611,15 +1613,16 @@ __global__ void k_project_update(CaseDev c, const double* __restrict__ q, const 
     out[t] = (comp == 0 && i == 0) ? c.inlet[j] : 0.0;
     return;
   }
-  double gphi = comp == 0 ? grad_u<double>(phi, g, j, i, c.gx) : grad_v<double>(phi, g, j, i, c.gy);
-  out[t] = q[t] - dt * gphi;
+  if (comp == 1) out[t] = fma(dgy, phi[g.p(j - 1, i)], fma(-dgy, phi[g.p(j, i)], q[t]));
+  else if (i < c.nx) out[t] = fma(dgx, phi[g.p(j, i - 1)], fma(-dgx, phi[g.p(j, i)], q[t]));
+  else out[t] = fma(2.0 * dgx, phi[g.p(j, c.nx - 1)], q[t]);
 }
 void launch_project_update(const CaseDev& c, const double* q, const double* phi, double dt, double* out,
                            const SolveCtl* psolve, const Gate& gate, cudaStream_t st) {
   (void)psolve;
   note_launch();
   kt_mark(6, st);
-  k_project_update<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, q, phi, dt, out, gate);
+  k_project_update<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, q, phi, dt * c.gx, dt * c.gy, out, gate);
   kt_mark(6, st);
 }
 
