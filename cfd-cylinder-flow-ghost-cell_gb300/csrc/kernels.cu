@@ -1566,7 +1566,10 @@ void launch_learned_apply(const CaseDev& c, const float* y, const unsigned long 
 // ---------------------------------------------------------------------------
 // projection pieces
 // ---------------------------------------------------------------------------
-__global__ void k_divergence(CaseDev c, const double* __restrict__ U, double* __restrict__ out, double dt,
+// D U at the active cells: its max |.| into divmax and/or, scaled, into out.  The scaled
+// output takes its coefficients sx = idx s, sy = idy s from the host (s = 1/dt or 1), so it
+// costs no more FP64 work than the divergence itself.
+__global__ void k_divergence(CaseDev c, const double* __restrict__ U, double* __restrict__ out, double sx, double sy,
                              unsigned long long* divmax, int gate_nonfinite, StepCtl* ctl, Gate gate) {
   if (!gate_open(gate)) return;
   const Grid g{c.nx, c.ny, c.usize};
@@ -1575,10 +1578,10 @@ __global__ void k_divergence(CaseDev c, const double* __restrict__ U, double* __
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < c.psize; t += (int64_t)gridDim.x * blockDim.x) {
     if (c.cls_p[t] & CLS_ACTIVE) {
       int j = (int)((unsigned)t / (unsigned)c.nx), i = (int)((unsigned)t - (unsigned)j * c.nx);
-      double d = (U[g.u(j, i + 1)] - U[g.u(j, i)]) * c.idx + (U[g.v(j + 1, i)] - U[g.v(j, i)]) * c.idy;
-      dm = umax64(dm, absbits(d));
+      const double du = U[g.u(j, i + 1)] - U[g.u(j, i)], dv = U[g.v(j + 1, i)] - U[g.v(j, i)];
+      if (divmax) dm = umax64(dm, absbits(du * c.idx + dv * c.idy));
       if (out) {
-        double o = d * dt;  // dt carries 1/dt (or 1)
+        const double o = du * sx + dv * sy;
         out[t] = o;
         bad = bad || nonfinite_bits(o);
       }
@@ -1594,8 +1597,9 @@ void launch_divergence(const CaseDev& c, const double* U, double* out, double sc
   (void)sc;
   note_launch();
   kt_mark(6, st);
-  k_divergence<<<reduce_blocks(c.psize), TPB, 0, st>>>(c, U, out, scale != 0.0 ? 1.0 / scale : 1.0, divmax,
-                                                      gate_on_nonfinite, gate.ctl, gate);
+  const double s = scale != 0.0 ? 1.0 / scale : 1.0;
+  k_divergence<<<reduce_blocks(c.psize), TPB, 0, st>>>(c, U, out, c.idx * s, c.idy * s, divmax, gate_on_nonfinite,
+                                                      gate.ctl, gate);
   kt_mark(6, st);
 }
 
@@ -1696,7 +1700,7 @@ void launch_defect(const CaseDev& c, const ResidualCoef& rcu, const ResidualCoef
 }
 
 __global__ void k_pressure_out(CaseDev c, const double* __restrict__ p, const double* __restrict__ inc, double factor,
-                               double dt, const double* __restrict__ action, const double* __restrict__ rhs,
+                               double dgx, double dgy, const double* __restrict__ action, const double* __restrict__ rhs,
                                double* __restrict__ half, double* __restrict__ pout, unsigned long long* coupled,
                                Gate gate) {
   if (!gate_open(gate)) return;
@@ -1710,8 +1714,12 @@ __global__ void k_pressure_out(CaseDev c, const double* __restrict__ p, const do
     face_of(t, g, comp, j, i);
     const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
     if (cls & CLS_ACTIVE) {
-      double gi = comp == 0 ? grad_u<double>(inc, g, j, i, c.gx) : grad_v<double>(inc, g, j, i, c.gy);
-      double r = action[t] - rhs[t] + dt * gi;
+      // action - rhs + dt G inc, with dgx = dt gx and dgy = dt gy formed on the host
+      const double a0 = action[t] - rhs[t];
+      double r;
+      if (comp == 1) r = fma(-dgy, inc[g.p(j - 1, i)], fma(dgy, inc[g.p(j, i)], a0));
+      else if (i < c.nx) r = fma(-dgx, inc[g.p(j, i - 1)], fma(dgx, inc[g.p(j, i)], a0));
+      else r = fma(-2.0 * dgx, inc[g.p(j, c.nx - 1)], a0);
       cm = umax64(cm, absbits(r));
     }
   } else {
@@ -1733,8 +1741,8 @@ void launch_pressure_out(const CaseDev& c, const double* p, const double* inc, d
                          unsigned long long* coupled, const Gate& gate, cudaStream_t st) {
   note_launch();
   kt_mark(7, st);
-  k_pressure_out<<<reduce_blocks(c.usize + c.vsize + c.psize), TPB, 0, st>>>(c, p, inc, factor, dt, action, rhs, half,
-                                                                          pout, coupled, gate);
+  k_pressure_out<<<reduce_blocks(c.usize + c.vsize + c.psize), TPB, 0, st>>>(c, p, inc, factor, dt * c.gx, dt * c.gy,
+                                                                          action, rhs, half, pout, coupled, gate);
   kt_mark(7, st);
 }
 
