@@ -370,8 +370,9 @@ void launch_diffusion(const CaseDev& c, const double* U, double* out, bool with_
                       cudaStream_t st);  // hdt==0: L U (+offset); else U - hdt*L U (H matvec)
 void launch_gradient(const CaseDev& c, const double* P, double* out, const Gate& gate, cudaStream_t st);
 
-// divergence at active p cells of an unpacked face grid: out = div * scale; max|out| -> bmax of sc (if sc),
-// max|div| -> *divmax (if divmax); non-finite -> gate error
+// divergence at active p cells of an unpacked face grid: out = div / scale (div when scale is 0),
+// max|div| -> *divmax (if divmax); a non-finite out raises the gate error when
+// gate_on_nonfinite is set; sc is unused
 void launch_divergence(const CaseDev& c, const double* U, double* out, double scale, SolveCtl* sc,
                        unsigned long long* divmax, int gate_on_nonfinite, const Gate& gate, cudaStream_t st);
 
