@@ -23,8 +23,9 @@
 using namespace gmk;
 
 // Last error of a call made without a handle (gm_create, gm_create_host and the
-// allocation-free entry point); a fixed buffer so that setting it allocates nothing.
-static char g_global_error[512];
+// allocation-free entry point), one per host thread so that threads failing at the same time
+// do not overwrite each other's text; a fixed buffer so that setting it allocates nothing.
+static thread_local char g_global_error[512];
 void gm_internal_set_error(const char* msg) {
   std::strncpy(g_global_error, msg ? msg : "", sizeof g_global_error - 1);
   g_global_error[sizeof g_global_error - 1] = 0;

@@ -104,10 +104,12 @@ int fail(int code, const char* msg) {
   return code;
 }
 
-bool on_device(const void* p) {
+// device (or managed) memory of the current device `dev`: arrays of another GPU would be
+// read across the link, or fault without peer access
+bool on_device(const void* p, int dev) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) && a.device == dev;
 }
 
 }  // namespace
@@ -122,10 +124,13 @@ int gm_divergence_stats_noalloc(const double* u, const double* v, const uint8_t*
     return fail(GM_EVALUE, "dx and dy must be finite and positive");
   if ((long long)nx * ny > GM_NOALLOC_MAX_CELLS)
     return fail(GM_EVALUE, "grid exceeds GM_NOALLOC_MAX_CELLS pressure cells of the static scratch");
-  if (!on_device(u) || !on_device(v) || !on_device(mask))
-    return fail(GM_EVALUE, "u, v and mask must be device arrays");
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return fail(GM_ECUDA, "no CUDA device");
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) {
+    cudaGetLastError();
+    return fail(GM_ECUDA, "no CUDA device");
+  }
+  if (!on_device(u, dev) || !on_device(v, dev) || !on_device(mask, dev))
+    return fail(GM_EVALUE, "u, v and mask must be device arrays of the current device");
   double* scratch = nullptr;
   {
     // set-up, once per device with that device current: device address of the static array
@@ -146,11 +151,16 @@ int gm_divergence_stats_noalloc(const double* u, const double* v, const uint8_t*
   const int nblocks = (int)((n + NA_THREADS - 1) / NA_THREADS);
   gmk::kernel_launch_adjust(1);
   k_div_partials<<<nblocks, NA_THREADS, 0, st>>>(u, v, mask, nx, ny, dx, dy, scratch);
-  gmk::kernel_launch_adjust(1);
-  k_div_final<<<1, 32, 0, st>>>(nblocks, scratch);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    gmk::kernel_launch_adjust(1);
+    k_div_final<<<1, 32, 0, st>>>(nblocks, scratch);
+    e = cudaGetLastError();
+  }
+  // a failed launch must not return the previous call's totals, which the shared array still holds
+  if (e != cudaSuccess) return fail(GM_ECUDA, cudaGetErrorString(e));
   double r[NA_FIELDS];
-  cudaError_t e = cudaMemcpyAsync(r, scratch + (long long)NA_MAX_BLOCKS * NA_FIELDS, sizeof r,
-                                  cudaMemcpyDeviceToHost, st);
+  e = cudaMemcpyAsync(r, scratch + (long long)NA_MAX_BLOCKS * NA_FIELDS, sizeof r, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     cudaGetLastError();

@@ -357,6 +357,7 @@ class MAC_CylinderFlow:
                                 perturb_amp=perturb_amp)
         verbose = self.verbose if verbose is None else verbose
         self._push()
+        t0 = _time.time()
         start = self.time
         ts, cds, cls = [], [], []
         s = 0
@@ -370,7 +371,13 @@ class MAC_CylinderFlow:
                 chunk = 1
             else:
                 self.u_inlet[:] = self.u_inlet_base
-                chunk = 1 if step_callback is not None or verbose else n_steps - s
+                if step_callback is not None:
+                    chunk = 1
+                elif verbose:
+                    # up to the next printed step: 0, 1000, 2000, ... and the last one
+                    chunk = min(n_steps - s, 1001 - s % 1000 if s % 1000 else 1)
+                else:
+                    chunk = n_steps - s
             self._set_inlet()
             rc, diag = self.step_raw(dt, chunk, first_index=s, start_time=start + s * dt)
             done = chunk
@@ -392,13 +399,17 @@ class MAC_CylinderFlow:
             if step_callback is not None:
                 step_callback(self, dict(self.last_step_diagnostics))
             if verbose and ((s - 1) % 1000 == 0 or s == n_steps):
+                # Div_RMS over every fluid cell: sqrt(sum div^2 / count) (solver/main.py:445)
                 stats = self.divergence_stats()
-                rms = np.sqrt(stats[1] / stats[3]) if stats[3] > 0 else 0.0
+                rms = np.sqrt(stats[1] / stats[2]) if stats[2] > 0 else 0.0
                 flux_in, flux_out = np.sum(self.u[:, 0]) * self.dy, np.sum(self.u[:, self.nx]) * self.dy
                 print(f"Step {s - 1:5d} | Div_RMS: {rms:.2e} | Div_Max: {stats[0]:.2e} | "
                       f"FluxErr: {abs(flux_out - flux_in) / flux_in:.2e} | "
                       f"Cd: {self.last_step_diagnostics['cd']:.4f} | Cl: {self.last_step_diagnostics['cl']:.4f}")
         self._pull()
+        if verbose:
+            elapsed = _time.time() - t0
+            print(f"Simulation completed in {elapsed:.2f}s ({elapsed / n_steps * 1000:.2f} ms/step)")
         return np.array(ts), np.array(cds), np.array(cls)
 
     def divergence_stats(self):

@@ -263,10 +263,12 @@ int32_t gm_pressure_recorded(const gm_handle* h);
  * computed from caller-owned DEVICE arrays u (ny x nx+1), v (ny+1 x nx) and mask
  * (ny x nx bytes, nonzero = solid) without any allocation.  Its scratch is a static
  * device array sized for at most GM_NOALLOC_MAX_CELLS cells (larger grids return
- * GM_EVALUE), held by every GPU that loads the library.  The first call on a device
- * looks up that array's address for the device (make it before any stream capture);
- * calls that overlap on the GPU share the array and race.  out = max |div|,
- * sum div^2, core sum div^2; counts = fluid cells, core cells.  Errors: gm_last_error(NULL). */
+ * GM_EVALUE), held by every GPU that loads the library.  The arrays must live on the
+ * current device.  The first call on a device looks up that array's address for the
+ * device.  Every call is synchronous (it waits for its stream to return the totals), so it
+ * must not be made while a stream is being captured.  Calls that overlap on the GPU share
+ * the array and race.  out = max |div|, sum div^2, core sum div^2; counts = fluid cells,
+ * core cells.  Errors: gm_last_error(NULL), which holds the calling thread's last error. */
 #define GM_NOALLOC_MAX_CELLS 1048576
 int gm_divergence_stats_noalloc(const double* u, const double* v, const uint8_t* mask, int32_t nx, int32_t ny,
                                 double dx, double dy, double out[3], int64_t counts[2], void* cuda_stream);

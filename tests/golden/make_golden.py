@@ -2,7 +2,7 @@
 
 Run once in a container that holds the reference checkout:
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py --reference <path of the reference checkout>
 
 The reference's ``solver/`` is copied to a temporary directory, its compiled
 ``mac_engine`` is built from ``solver/src/bindings.cpp`` (the shipped Windows
@@ -123,7 +123,7 @@ def schur_rows_of(actual, indices, rect):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--reference', type=Path, default=Path('/root/reference'))
+    ap.add_argument('--reference', type=Path, required=True, help='path of the reference checkout')
     ap.add_argument('--skip-large', action='store_true')
     ap.add_argument('--only', choices=('taylor_green', 'analysis'), help='generate one group of fixtures only')
     args = ap.parse_args()
