@@ -28,7 +28,7 @@ SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_las
            'gm_tg_set_state', 'gm_tg_get_state', 'gm_tg_step', 'gm_unet_layers', 'gm_unet_create',
            'gm_unet_destroy', 'gm_unet_last_error', 'gm_unet_input', 'gm_unet_forward', 'gm_unet_backward',
            'gm_set_learned_preconditioner', 'gm_set_pressure_recorder', 'gm_pressure_recorded',
-           'gm_host_alloc', 'gm_host_free')
+           'gm_host_alloc', 'gm_host_free', 'gm_solver_info')
 NOALLOC_MAX_CELLS = 1048576
 
 
@@ -102,6 +102,7 @@ def _load():
         'gm_batch_last_error': ([P], C.c_char_p),
         'gm_batch_step': ([P, D, I32, I64, P, C.POINTER(StepDiag), P], C.c_int),
         'gm_phase_timing': ([P, P], C.c_int),
+        'gm_solver_info': ([P, C.POINTER(I32), C.POINTER(D)], C.c_int),
         'gm_tg_create': ([I32, D, I32, pp], C.c_int),
         'gm_tg_destroy': ([P], C.c_int),
         'gm_tg_last_error': ([P], C.c_char_p),

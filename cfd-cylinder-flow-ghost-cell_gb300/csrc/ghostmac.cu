@@ -160,6 +160,15 @@ struct gm_handle {
   DBuf<double> phalf, phalf_next, pout, prhs, pphi, pres, pfirst, pw2, pinc, ptmp, spectral;
   DBuf<float> pres32, fres32;  // FP32-mode residuals (inputs of the FP32 inverse)
   DBuf<float> U32, P32;        // FP32-mode copies of the state for the momentum stencils
+  // FP32 mode: Jacobi iterations of the Helmholtz systems (per dt; jac_iters 0 keeps the FFT
+  // inverse), their irregular-row tables and two face-grid iterates (u and v use disjoint parts,
+  // so the two lanes share them)
+  int jac_iters = 0;
+  double jac_rho = 0.0;
+  HelmJacobi hj{};
+  DBuf<float> jval[2], jidiag[2], jd0, jd1;
+  DBuf<int32_t> jsidx[2], jrpos[2];
+  size_t jac_smem = 0;  // dynamic shared memory of the temporally blocked form (0: K launches)
   // flexible GMRES (pressure_solver = iterative): Krylov basis V (m+1 vectors), preconditioned
   // directions Z (m), the refinement correction and reduction scratch
   static constexpr int GMRES_M = 50;
@@ -994,8 +1003,14 @@ void schur_inverse(gm_handle* h, RectDev& rd, const TransformTables& tt, const v
 }
 
 // r is the FP64 right-hand side, or in the FP32 mode the FP32 residual when r_f32 is set
+void helm_jacobi_apply(gm_handle* h, int kind, const void* r, bool r_f32, double* x, bool accumulate,
+                       const Gate& g, cudaStream_t st);
 void apply_inverse(gm_handle* h, int lane, RectDev& rd, int kind, const void* r, bool r_f32, double* x,
                    bool accumulate, double* first, double* w2, const Gate& gt, cudaStream_t st) {
+  if (h->precision == 1 && kind != 0 && h->jac_iters > 0) {
+    helm_jacobi_apply(h, kind, r, r_f32, x, accumulate, gt, st);
+    return;
+  }
   if (h->precision == 1) {
     float* first32 = kind == 0 ? h->pfirst32.p : h->ffirst32.p;
     float* spec = lane == 0 ? h->spectral32.p : h->spectral32_b.p;
@@ -1292,6 +1307,192 @@ void project(gm_handle* h, double* q, double dt, double* out, double* phi, int s
   project_post(h, q, dt, out, phi, slot, divk);
 }
 
+// Jacobi tables of the FP32 mode's Helmholtz solves for the current dt: 1 / diagonal per
+// regular-row class, the irregular rows in FP32 with their diagonal entry zeroed, and the
+// number of iterations per application.  The row-sum norm rho of the iteration matrix
+// D^{-1} (D - H), taken over every regular class and every irregular row, bounds the error
+// contraction per iteration; `iters` takes rho^iters <= 2^-23 (the FP32 rounding level).
+// With rho > 1/4 (large dt nu / h^2) the FFT inverse stays.  GHOSTMAC_HELM_JACOBI=0 keeps the
+// FFT inverse, =N forces N iterations.
+// Tiles of the temporally blocked Jacobi application on the u (k = 0) or v (k = 1) grid:
+// regular 64 x 32 tiles, and the body box around the irregular rows with iters - 1 points of
+// margin, whose loaded region is what iters - 1 stencil steps reach from the box (breadth-first
+// over the five-point stencil and the irregular rows' entries).  Returns false when the
+// region would not fit the block's shared memory.
+bool jacobi_tiles(gm_handle* h, int k, int iters) {
+  const gm::Geometry& g = h->g;
+  const int W = k == 0 ? g.nx + 1 : g.nx, R = k == 0 ? g.ny : g.ny + 1, hal = iters - 1;
+  JacobiTiles& T = h->hj.jt[k];
+  T = JacobiTiles{};
+  T.tw = 64;
+  T.th = 32;
+  T.ntx = (W + T.tw - 1) / T.tw;
+  T.nty = (R + T.th - 1) / T.th;
+  const gm::Csr& c = h->hs.irr[k];
+  const std::vector<int64_t>& rows = h->hs.rows_irr[k];
+  std::vector<int32_t> sidx(c.col.size(), -1), rpos(rows.size(), -1);
+  if (!rows.empty()) {
+    int jmin = R, jmax = -1, imin = W, imax = -1;
+    for (int64_t f : rows) {
+      const int j = (int)(f / W), i = (int)(f % W);
+      jmin = std::min(jmin, j); jmax = std::max(jmax, j); imin = std::min(imin, i); imax = std::max(imax, i);
+    }
+    T.bj0 = std::max(jmin - hal, 0); T.bj1 = std::min(jmax + hal + 1, R);
+    T.bi0 = std::max(imin - hal, 0); T.bi1 = std::min(imax + hal + 1, W);
+    // breadth-first reach of hal stencil steps from the box, on a window around it
+    int reach = 1;
+    for (size_t r = 0; r < rows.size(); ++r) {
+      const int j = (int)(rows[r] / W), i = (int)(rows[r] % W);
+      for (int64_t e = c.ptr[r]; e < c.ptr[r + 1]; ++e) {
+        const int cj = (int)(c.col[e] / W), ci = (int)(c.col[e] % W);
+        reach = std::max(reach, std::max(std::abs(cj - j), std::abs(ci - i)));
+      }
+    }
+    const int wj0 = std::max(T.bj0 - hal * reach, 0), wj1 = std::min(T.bj1 + hal * reach, R);
+    const int wi0 = std::max(T.bi0 - hal * reach, 0), wi1 = std::min(T.bi1 + hal * reach, W);
+    const int ww = wi1 - wi0, wh = wj1 - wj0;
+    std::vector<int32_t> irow((size_t)ww * wh, -1);
+    for (size_t r = 0; r < rows.size(); ++r) {
+      const int j = (int)(rows[r] / W), i = (int)(rows[r] % W);
+      if (j >= wj0 && j < wj1 && i >= wi0 && i < wi1) irow[(size_t)(j - wj0) * ww + (i - wi0)] = (int32_t)r;
+    }
+    std::vector<uint8_t> mark((size_t)ww * wh, 0), next;
+    for (int j = T.bj0; j < T.bj1; ++j)
+      for (int i = T.bi0; i < T.bi1; ++i) mark[(size_t)(j - wj0) * ww + (i - wi0)] = 1;
+    for (int step = 0; step < hal; ++step) {
+      next = mark;
+      for (int j = 0; j < wh; ++j)
+        for (int i = 0; i < ww; ++i) {
+          if (!mark[(size_t)j * ww + i]) continue;
+          const int32_t r = irow[(size_t)j * ww + i];
+          auto put = [&](int gj, int gi) {
+            if (gj >= wj0 && gj < wj1 && gi >= wi0 && gi < wi1) next[(size_t)(gj - wj0) * ww + (gi - wi0)] = 1;
+          };
+          if (r >= 0) {
+            for (int64_t e = c.ptr[r]; e < c.ptr[r + 1]; ++e) put((int)(c.col[e] / W), (int)(c.col[e] % W));
+          } else {
+            put(wj0 + j - 1, wi0 + i); put(wj0 + j + 1, wi0 + i); put(wj0 + j, wi0 + i - 1); put(wj0 + j, wi0 + i + 1);
+          }
+        }
+      mark.swap(next);
+    }
+    T.rj0 = wj1; T.rj1 = wj0; T.ri0 = wi1; T.ri1 = wi0;
+    for (int j = 0; j < wh; ++j)
+      for (int i = 0; i < ww; ++i)
+        if (mark[(size_t)j * ww + i]) {
+          T.rj0 = std::min(T.rj0, wj0 + j); T.rj1 = std::max(T.rj1, wj0 + j + 1);
+          T.ri0 = std::min(T.ri0, wi0 + i); T.ri1 = std::max(T.ri1, wi0 + i + 1);
+        }
+    const int rw = T.ri1 - T.ri0;
+    for (size_t e = 0; e < c.col.size(); ++e) {
+      const int cj = (int)(c.col[e] / W), ci = (int)(c.col[e] % W);
+      if (cj >= T.rj0 && cj < T.rj1 && ci >= T.ri0 && ci < T.ri1) sidx[e] = (cj - T.rj0) * rw + (ci - T.ri0);
+    }
+    for (size_t r = 0; r < rows.size(); ++r) {
+      const int j = (int)(rows[r] / W), i = (int)(rows[r] % W);
+      rpos[r] = (j - T.rj0) * rw + (i - T.ri0);  // inside: the box holds every irregular row
+    }
+    T.nrow = (int)rows.size();
+    T.nnz = (int)c.col.size();
+  }
+  h->jsidx[k].upload(sidx, h->st);
+  h->jrpos[k].upload(rpos, h->st);
+  T.sidx = h->jsidx[k].p;
+  T.rpos = h->jrpos[k].p;
+  return helm_jacobi_tiled_smem(T, iters) <= 200 * 1024;
+}
+
+void build_helm_jacobi(gm_handle* h) {
+  h->jac_iters = 0;
+  if (h->precision != 1) return;
+  double rho = 0.0;
+  bool ok = true;
+  for (int k = 0; k < 2; ++k) {
+    const ResidualCoef& rc = h->rcoef[k + 1];
+    for (int ic = 0; ic < 3; ++ic)
+      for (int jc = 0; jc < 2; ++jc) {
+        const double cc = rc.cc[ic][jc];
+        if (!(std::fabs(cc) > 0.5)) ok = false;
+        h->hj.icc[k][ic][jc] = (float)(1.0 / cc);
+        rho = std::max(rho, (std::fabs(rc.cw[ic]) + std::fabs(rc.ce) + 2.0 * std::fabs(rc.cy)) / std::fabs(cc));
+      }
+    const gm::Csr& c = h->hs.irr[k];
+    const std::vector<int64_t>& rows = h->hs.rows_irr[k];
+    std::vector<float> val(c.col.size()), idiag(rows.size());
+    for (size_t r = 0; r < rows.size(); ++r) {
+      double diag = 0.0, off = 0.0;
+      for (int64_t e = c.ptr[r]; e < c.ptr[r + 1]; ++e) {
+        if (c.col[e] == rows[r]) {
+          diag += c.val[e];
+          val[e] = 0.0f;
+        } else {
+          off += std::fabs(c.val[e]);
+          val[e] = (float)c.val[e];
+        }
+      }
+      if (!(std::fabs(diag) > 0.5)) ok = false;
+      idiag[r] = (float)(1.0 / diag);
+      rho = std::max(rho, off / std::fabs(diag));
+    }
+    h->jval[k].upload(val, h->st);
+    h->jidiag[k].upload(idiag, h->st);
+    h->hj.val[k] = h->jval[k].p;
+    h->hj.idiag[k] = h->jidiag[k].p;
+  }
+  h->jac_rho = rho;
+  int iters = 0;
+  if (ok && rho < 0.25) iters = rho > 0.0 ? (int)std::ceil(std::log(0x1p-23) / std::log(rho)) : 1;
+  iters = std::min(std::max(iters, ok && rho < 0.25 ? 1 : 0), 12);
+  if (const char* e = std::getenv("GHOSTMAC_HELM_JACOBI")) {
+    const int forced = std::atoi(e);
+    iters = forced <= 0 ? 0 : std::min(forced, 32);
+  }
+  h->jac_iters = iters;
+  h->hj.iters = iters;
+  h->jac_smem = 0;
+  if (iters > 0) {
+    bool tiled = true;
+    if (const char* e = std::getenv("GHOSTMAC_HELM_JACOBI_TILED")) tiled = std::atoi(e) != 0;
+    size_t smem = 0;
+    for (int k = 0; k < 2 && tiled; ++k) {
+      tiled = jacobi_tiles(h, k, iters);
+      if (tiled) smem = std::max(smem, helm_jacobi_tiled_smem(h->hj.jt[k], iters));
+    }
+    if (tiled && smem <= h->smem_optin && helm_jacobi_tiled_optin(smem) == 0) h->jac_smem = smem;
+  }
+  if (iters > 0 && !h->jac_smem && h->jd0.n != (size_t)h->F) {
+    h->jd0.alloc(h->F);
+    h->jd1.alloc(h->F);
+  }
+}
+
+// One FP32 application of the Helmholtz inverse by Jacobi iterations: x = [x +] d, with d the
+// jac_iters-th iterate from d = 0 for the right-hand side r (FP64 b, or the FP32 residual).
+void helm_jacobi_apply(gm_handle* h, int kind, const void* r, bool r_f32, double* x, bool accumulate,
+                       const Gate& g, cudaStream_t st) {
+  if (h->jac_smem) {
+    if (r_f32)
+      launch_helm_jacobi_tiled<float>(h->cd, h->rcoef[kind], h->hj, kind, (const float*)r, x, accumulate, h->jac_smem,
+                                      g, st);
+    else
+      launch_helm_jacobi_tiled<double>(h->cd, h->rcoef[kind], h->hj, kind, (const double*)r, x, accumulate,
+                                       h->jac_smem, g, st);
+    return;
+  }
+  const float* din = nullptr;
+  for (int it = 0; it < h->jac_iters; ++it) {
+    const bool last = it + 1 == h->jac_iters;
+    float* dout = last ? nullptr : (it % 2 == 0 ? h->jd0.p : h->jd1.p);
+    if (r_f32)
+      launch_helm_jacobi<float>(h->cd, h->rcoef[kind], h->hj, kind, (const float*)r, din, dout, last ? x : nullptr,
+                                accumulate, g, st);
+    else
+      launch_helm_jacobi<double>(h->cd, h->rcoef[kind], h->hj, kind, (const double*)r, din, dout,
+                                 last ? x : nullptr, accumulate, g, st);
+    din = dout;
+  }
+}
+
 void ensure_helmholtz(gm_handle* h, double dt) {
   if (h->helm_ready && h->helm_dt == dt) return;
   int ec = 0;
@@ -1313,6 +1514,7 @@ void ensure_helmholtz(gm_handle* h, double dt) {
   upload_row_index(h->irr[2], h->hs.rows_irr[1], h->g.vsize, h->st);
   // v irregular rows are v-grid flat indices (columns too)
   fill_case_dev(h);
+  build_helm_jacobi(h);
   build_rect_tables(h, h->ru, 1, dt);
   build_rect_tables(h, h->rv, 2, dt);
   build_schur(h, h->ru, h->hs.schur_rows[0], h->hs.schur_c[0], h->fw2.p);
@@ -2313,6 +2515,13 @@ int gm_phase_timing(const gm_handle* h, double out[14]) {
   return GM_OK;
 }
 
+int gm_solver_info(const gm_handle* h, int32_t* jacobi_iters, double* jacobi_rho) {
+  if (!h) return GM_EVALUE;
+  if (jacobi_iters) *jacobi_iters = h->jac_iters;
+  if (jacobi_rho) *jacobi_rho = h->jac_rho;
+  return GM_OK;
+}
+
 int gm_kernel_timing(int32_t kernel_class, int32_t enable, double* total_ms, int64_t* count, double* bytes) {
   if (enable) ktimer_enable(1);
   double t = 0, by = 0;
@@ -2369,6 +2578,21 @@ void apply_inverse_group(gm_batch* b, const BatchGroup& G, int lane, const std::
                          bool body, cudaStream_t st) {
   const int n = (int)calls.size();
   const bool f32 = sizeof(T) == 4;
+  bool jacobi = false;
+  for (int c = 0; c < n; ++c) jacobi = jacobi || (f32 && calls[c].kind != 0 && b->cases[G.idx[c]]->jac_iters > 0);
+  if (jacobi) {
+    // FP32 Helmholtz solves by Jacobi iterations: every case in turn through the single-case
+    // application (each case keeps its own iteration count), the same launches as the case
+    // stepped alone
+    for (int c = 0; c < n; ++c) {
+      gm_handle* h = b->cases[G.idx[c]];
+      const SolveCall& call = calls[c];
+      const Gate g{h->ctl.p, call.slot, body ? -1 : 0};
+      const void* r = body ? (const void*)h->fres32.p : (const void*)call.b;
+      apply_inverse(h, lane, *call.rd, call.kind, r, body, call.x, body, call.first, call.w2, g, st);
+    }
+    return;
+  }
   auto fwd = std::make_unique<ArgPack<XpassArgs<T, TI, T>>>();
   auto ys = std::make_unique<ArgPack<YsolveArgs<T>>>();
   auto bf = std::make_unique<ArgPack<BandFirstArgs<T>>>();

@@ -149,7 +149,8 @@ void kernel_launch_adjust(long long delta) { g_launches.fetch_add(delta, std::me
 // Optional CUDA-event timing of every launch, summed per kernel class (used by the
 // benchmark for its per-class breakdown and the dominant kernel's launch time).  Classes:
 // 1 x pass, 2 column solves, 3 momentum, 4 residual, 5 boundary chain / Schur GEMV, 6 projection pieces,
-// 7 defect / pressure output, 8 ghost rows, 9 forces / maxima, 10 gates and loop control.
+// 7 defect / pressure output, 8 ghost rows, 9 forces / maxima, 10 gates and loop control,
+// 11 FP32 Jacobi sweeps of the Helmholtz systems.
 namespace {
 struct KTimer {
   bool on = false;
@@ -1360,6 +1361,304 @@ void launch_residual(const CaseDev& c, const ResidualCoef& rc, int kind, const d
   }
   kt_mark(4, st, (double)n * (8 + 8 + (res_f32 ? 4 : 8) + 1));  // x, b, res, class map
 }
+
+// ---------------------------------------------------------------------------
+// FP32 Jacobi sweeps of the CN Helmholtz systems (FP32 mode)
+// ---------------------------------------------------------------------------
+// The CN systems H = I - c L (c = dt nu / 2) are strongly diagonally dominant: the Jacobi
+// iteration matrix has row-sum norm rho = max_i sum_{j != i} |H_ij| / |H_ii|, about 4 c / h^2
+// (0.016 on the 800x820 Re 100 case), which the host computes from every row at set-up.  In
+// the FP32 mode one application of the approximate inverse is then `iters` Jacobi
+// iterations d <- D^{-1} (r - (H - D) d) from d = 0, in FP32, with the same regular-row
+// coefficients and irregular rows as the residual kernel; x = [x +] d closes the last one.
+// The FP64 residual and the refinement loop around it are those of the FFT inverse, so the
+// answer meets the same residual targets; only the number of sweeps may differ.
+static constexpr int JPT = 4;  // consecutive points per thread in the Jacobi iterations
+template <int KIND, typename TR>
+__global__ void __launch_bounds__(TPB) k_helm_jacobi(CaseDev c, ResidualCoef rc, HelmJacobi hj,
+                                                    const TR* __restrict__ r, const float* __restrict__ din,
+                                                    float* __restrict__ dout, double* __restrict__ x, int accumulate,
+                                                    Gate gate) {
+  if (!gate_open(gate)) return;
+  const int nx = c.nx, ny = c.ny;
+  const int w = KIND == 1 ? nx + 1 : nx;
+  const int64_t npts = KIND == 1 ? c.usize : c.vsize;
+  const int64_t base = KIND == 2 ? c.usize : 0;
+  const uint8_t* cls = KIND == 1 ? c.cls_u : c.cls_v;
+  const int64_t t0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * JPT;
+  if (t0 >= npts) return;
+  // every load of the thread's JPT points first (one round trip), then the arithmetic
+  uint8_t k[JPT];
+  float rv[JPT], dw[JPT], de[JPT], ds[JPT], dn[JPT];
+#pragma unroll
+  for (int u = 0; u < JPT; ++u) {
+    const int64_t t = t0 + u;
+    k[u] = 0;
+    rv[u] = dw[u] = de[u] = ds[u] = dn[u] = 0.0f;
+    if (t >= npts) continue;
+    const int64_t f = base + t;
+    k[u] = cls[t];
+    if constexpr (sizeof(TR) == 8) rv[u] = f64_to_f32i(r[f]);
+    else rv[u] = r[f];
+    if (din) {
+      const int j = (int)((unsigned)t / (unsigned)w), i = (int)((unsigned)t - (unsigned)j * w);
+      if (KIND == 1) {
+        if (i > 1) dw[u] = din[f - 1];
+        if (i < nx) de[u] = din[f + 1];
+        if (j > 0) ds[u] = din[f - w];
+        if (j < ny - 1) dn[u] = din[f + w];
+      } else {
+        if (i > 0) dw[u] = din[f - 1];
+        if (i < nx - 1) de[u] = din[f + 1];
+        if (j > 1) ds[u] = din[f - w];
+        if (j < ny - 1) dn[u] = din[f + w];
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < JPT; ++u) {
+    const int64_t t = t0 + u;
+    if (t >= npts) continue;
+    const int64_t f = base + t;
+    float d = 0.0f;
+    if (k[u] & CLS_ACTIVE) {
+      const int row = (k[u] & CLS_IRREG) ? c.irr_index[KIND][t] : -1;
+      if (row >= 0) {
+        float sum = 0.0f;
+        if (din) {
+          const int64_t* cp = c.irr_ptr[KIND];
+          const int64_t* col = c.irr_col[KIND];
+          const float* val = hj.val[KIND - 1];
+          for (int64_t e = cp[row]; e < cp[row + 1]; ++e) sum = fmaf(val[e], din[base + col[e]], sum);
+        }
+        d = (rv[u] - sum) * hj.idiag[KIND - 1][row];
+      } else {
+        const int j = (int)((unsigned)t / (unsigned)w), i = (int)((unsigned)t - (unsigned)j * w);
+        int ic, jc;
+        if (KIND == 1) {
+          ic = i == nx ? 2 : 1;
+          jc = (j == 0 || j == ny - 1) ? 0 : 1;
+        } else {
+          ic = i == 0 ? 0 : (i == nx - 1 ? 2 : 1);
+          jc = 1;
+        }
+        const float cwv = ic == 0 ? rc.fcw[0] : (ic == 1 ? rc.fcw[1] : rc.fcw[2]);
+        const float i0 = jc ? hj.icc[KIND - 1][0][1] : hj.icc[KIND - 1][0][0];
+        const float i1 = jc ? hj.icc[KIND - 1][1][1] : hj.icc[KIND - 1][1][0];
+        const float i2 = jc ? hj.icc[KIND - 1][2][1] : hj.icc[KIND - 1][2][0];
+        const float icc = ic == 0 ? i0 : (ic == 1 ? i1 : i2);
+        const float off = fmaf(rc.fcy, ds[u] + dn[u], fmaf(rc.fce, de[u], cwv * dw[u]));
+        d = (rv[u] - off) * icc;
+      }
+    }
+    if (x) {
+      // inactive points of the solution are zero
+      x[f] = !(k[u] & CLS_ACTIVE) ? 0.0 : (accumulate ? x[f] + f32_to_f64i(d) : f32_to_f64i(d));
+    } else {
+      dout[f] = d;
+    }
+  }
+}
+
+template <typename TR>
+void launch_helm_jacobi(const CaseDev& c, const ResidualCoef& rc, const HelmJacobi& hj, int kind, const TR* r,
+                        const float* din, float* dout, double* x, bool accumulate, const Gate& gate, cudaStream_t st) {
+  const int64_t n = kind == 1 ? c.usize : c.vsize;
+  note_launch();
+  kt_mark(11, st);
+  const unsigned g = blocks_for((n + JPT - 1) / JPT);
+  if (kind == 1)
+    launch_pdl(k_helm_jacobi<1, TR>, dim3(g), dim3(TPB), 0, st, c, rc, hj, r, din, dout, x, accumulate ? 1 : 0, gate);
+  else
+    launch_pdl(k_helm_jacobi<2, TR>, dim3(g), dim3(TPB), 0, st, c, rc, hj, r, din, dout, x, accumulate ? 1 : 0, gate);
+  // algorithmic bytes: r, the class map, the five-point iterate (read once per point) and the
+  // new iterate (or x read and written by the last iteration)
+  kt_mark(11, st, (double)n * (sizeof(TR) + 1 + (din ? 4 : 0) + (x ? (accumulate ? 16 : 8) : 4)));
+}
+template void launch_helm_jacobi<double>(const CaseDev&, const ResidualCoef&, const HelmJacobi&, int, const double*,
+                                         const float*, float*, double*, bool, const Gate&, cudaStream_t);
+template void launch_helm_jacobi<float>(const CaseDev&, const ResidualCoef&, const HelmJacobi&, int, const float*,
+                                        const float*, float*, double*, bool, const Gate&, cudaStream_t);
+
+// Temporally blocked Jacobi application: every block loads the class map and the right-hand
+// side of its region once, runs the iterations in shared memory and writes its output box.
+// A point's value after `iters` iterations depends only on points that iters - 1 stencil
+// applications reach from it, so a tile with a halo of iters - 1 five-point steps reproduces
+// the global iteration exactly outside the body box (whose margin keeps every irregular row
+// iters - 1 points away), and the body block's region holds everything its box reaches.
+// Points of a regular tile's halo may be irregular rows updated with the five-point formula:
+// their values never reach the tile's outputs.
+// Shared memory of a region of rh x rw points, stored with a border of one zero point on each
+// side (every neighbour read is then in bounds and a missing neighbour reads zero): three float
+// arrays (two iterates and the right-hand side) and the class bytes.
+__host__ __device__ inline size_t jacobi_region_bytes(int rh, int rw) {
+  const size_t n = (size_t)(rh + 2) * (rw + 2);
+  return n * 3 * sizeof(float) + (n + 15) / 16 * 16;
+}
+size_t helm_jacobi_tiled_smem(const JacobiTiles& t, int iters) {
+  const int h = iters - 1;
+  const size_t reg = jacobi_region_bytes(t.th + 2 * h, t.tw + 2 * h);
+  size_t body = 0;
+  if (t.bj1 > t.bj0)
+    body = jacobi_region_bytes(t.rj1 - t.rj0, t.ri1 - t.ri0) + (size_t)t.nnz * 8 + (size_t)t.nrow * 12 + 4;
+  return (std::max(reg, body) + 15) / 16 * 16;
+}
+
+// Block 0 is the body block (it starts first); the others are the regular tiles.  Threads walk
+// the region in rows of 32 points per warp, so no per-point index division is needed.  The
+// operator's excluded neighbours (the u inlet column, the v wall rows) are inactive points whose
+// iterate is zero, and points outside the grid are the zero border, so the five-point update
+// needs no neighbour tests.
+template <int KIND, typename TR>
+__global__ void __launch_bounds__(TPB) k_helm_jacobi_tiled(CaseDev c, ResidualCoef rc, HelmJacobi hj,
+                                                          const TR* __restrict__ r, double* __restrict__ x,
+                                                          int accumulate, Gate gate) {
+  extern __shared__ __align__(16) float jsm[];
+  if (!gate_open(gate)) return;
+  const JacobiTiles& T = hj.jt[KIND - 1];
+  const int nx = c.nx, ny = c.ny;
+  const int W = KIND == 1 ? nx + 1 : nx;
+  const int R = KIND == 1 ? ny : ny + 1;
+  const int64_t base = KIND == 2 ? c.usize : 0;
+  const uint8_t* cls = KIND == 1 ? c.cls_u : c.cls_v;
+  const int h = hj.iters - 1;
+  const bool has_body = T.bj1 > T.bj0;
+  const bool body = has_body && blockIdx.x == 0;
+  int j0, j1, i0, i1, oj0, oj1, oi0, oi1;
+  if (body) {
+    j0 = T.rj0; j1 = T.rj1; i0 = T.ri0; i1 = T.ri1;
+    oj0 = T.bj0; oj1 = T.bj1; oi0 = T.bi0; oi1 = T.bi1;
+  } else {
+    const int b = (int)blockIdx.x - (has_body ? 1 : 0);
+    const int ty = b / T.ntx, tx = b - ty * T.ntx;
+    oj0 = ty * T.th; oj1 = min(oj0 + T.th, R);
+    oi0 = tx * T.tw; oi1 = min(oi0 + T.tw, W);
+    j0 = max(oj0 - h, 0); j1 = min(oj1 + h, R);
+    i0 = max(oi0 - h, 0); i1 = min(oi1 + h, W);
+  }
+  const int rw = i1 - i0, rh = j1 - j0, pw = rw + 2, np = pw * (rh + 2);
+  float* cur = jsm;
+  float* nxt = jsm + np;
+  float* rr = jsm + 2 * np;
+  uint8_t* kk = reinterpret_cast<uint8_t*>(jsm + 3 * np);
+  unsigned char* stage = reinterpret_cast<unsigned char*>(jsm) + jacobi_region_bytes(rh, rw);
+  float* sval = reinterpret_cast<float*>(stage);
+  int32_t* ssidx = reinterpret_cast<int32_t*>(sval + (body ? T.nnz : 0));
+  int32_t* sptr = ssidx + (body ? T.nnz : 0);
+  int32_t* spos = sptr + (body ? T.nrow + 1 : 0);
+  float* sidg = reinterpret_cast<float*>(spos + (body ? T.nrow : 0));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  // zero borders of both iterates
+  for (int q = threadIdx.x; q < np; q += blockDim.x) { cur[q] = 0.0f; nxt[q] = 0.0f; }
+  for (int pj = warp; pj < rh; pj += nwarp) {
+    const int64_t row = (int64_t)(j0 + pj) * W + i0;
+    for (int pi = lane; pi < rw; pi += 32) {
+      const int q = (pj + 1) * pw + pi + 1;
+      kk[q] = cls[row + pi];
+      if constexpr (sizeof(TR) == 8) rr[q] = f64_to_f32i(r[base + row + pi]);
+      else rr[q] = r[base + row + pi];
+    }
+  }
+  if (body) {
+    const int64_t* cp = c.irr_ptr[KIND];
+    for (int e = threadIdx.x; e < T.nnz; e += blockDim.x) {
+      sval[e] = hj.val[KIND - 1][e];
+      const int sx = T.sidx[e];  // place in the unpadded region
+      ssidx[e] = sx < 0 ? -1 : (sx / rw + 1) * pw + (sx - (sx / rw) * rw) + 1;
+    }
+    for (int q = threadIdx.x; q <= T.nrow; q += blockDim.x) {
+      sptr[q] = (int32_t)cp[q];
+      if (q < T.nrow) {
+        const int sx = T.rpos[q];
+        spos[q] = (sx / rw + 1) * pw + (sx - (sx / rw) * rw) + 1;
+        sidg[q] = hj.idiag[KIND - 1][q];
+      }
+    }
+  }
+  __syncthreads();
+  // regular-row coefficients: 1 / diagonal per (x class, y class), west coupling per x class
+  const float fcw0 = rc.fcw[0], fcw1 = rc.fcw[1], fcw2 = rc.fcw[2], fce = rc.fce, fcy = rc.fcy;
+  for (int it = 0; it < hj.iters; ++it) {
+    for (int pj = warp; pj < rh; pj += nwarp) {
+      const int jj = j0 + pj;
+      const int jc = KIND == 1 ? ((jj == 0 || jj == ny - 1) ? 0 : 1) : 1;
+      const float ia = hj.icc[KIND - 1][0][jc], ib = hj.icc[KIND - 1][1][jc], ic2 = hj.icc[KIND - 1][2][jc];
+      for (int pi = lane; pi < rw; pi += 32) {
+        const int q = (pj + 1) * pw + pi + 1;
+        const int ii = i0 + pi;
+        const int icl = KIND == 1 ? (ii == nx ? 2 : 1) : (ii == 0 ? 0 : (ii == nx - 1 ? 2 : 1));
+        const float icc = icl == 0 ? ia : (icl == 1 ? ib : ic2);
+        const float cwv = icl == 0 ? fcw0 : (icl == 1 ? fcw1 : fcw2);
+        const float off = it > 0 ? fmaf(fcy, cur[q - pw] + cur[q + pw], fmaf(fce, cur[q + 1], cwv * cur[q - 1])) : 0.0f;
+        nxt[q] = (kk[q] & CLS_ACTIVE) ? (rr[q] - off) * icc : 0.0f;
+      }
+    }
+    if (body) {
+      // the irregular rows overwrite their places with the rows' own entries
+      __syncthreads();
+      for (int q = threadIdx.x; q < T.nrow; q += blockDim.x) {
+        const int p = spos[q];
+        float sum = 0.0f;
+        if (it > 0)
+          for (int e = sptr[q]; e < sptr[q + 1]; ++e) {
+            const int sx = ssidx[e];
+            if (sx >= 0) sum = fmaf(sval[e], cur[sx], sum);
+          }
+        nxt[p] = (rr[p] - sum) * sidg[q];
+      }
+    }
+    __syncthreads();
+    float* tmp = cur;
+    cur = nxt;
+    nxt = tmp;
+  }
+  const int bj0 = T.bj0, bj1 = T.bj1, bi0 = T.bi0, bi1 = T.bi1;
+  for (int pj = warp; pj < rh; pj += nwarp) {
+    const int jj = j0 + pj;
+    if (jj < oj0 || jj >= oj1) continue;
+    const bool in_box_rows = has_body && jj >= bj0 && jj < bj1;
+    const int64_t row = base + (int64_t)jj * W;
+    for (int pi = lane; pi < rw; pi += 32) {
+      const int ii = i0 + pi;
+      if (ii < oi0 || ii >= oi1) continue;
+      if (!body && in_box_rows && ii >= bi0 && ii < bi1) continue;
+      const int q = (pj + 1) * pw + pi + 1;
+      const int64_t f = row + ii;
+      const float d = cur[q];
+      x[f] = !(kk[q] & CLS_ACTIVE) ? 0.0 : (accumulate ? x[f] + f32_to_f64i(d) : f32_to_f64i(d));
+    }
+  }
+}
+
+int helm_jacobi_tiled_optin(size_t smem) {
+  const void* ks[4] = {(const void*)k_helm_jacobi_tiled<1, double>, (const void*)k_helm_jacobi_tiled<2, double>,
+                       (const void*)k_helm_jacobi_tiled<1, float>, (const void*)k_helm_jacobi_tiled<2, float>};
+  int e = 0;
+  for (const void* k : ks)
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) e = 1;
+  if (e) cudaGetLastError();
+  return e;
+}
+
+template <typename TR>
+void launch_helm_jacobi_tiled(const CaseDev& c, const ResidualCoef& rc, const HelmJacobi& hj, int kind, const TR* r,
+                              double* x, bool accumulate, size_t smem, const Gate& gate, cudaStream_t st) {
+  const JacobiTiles& T = hj.jt[kind - 1];
+  const unsigned g = (unsigned)(T.ntx * T.nty + (T.bj1 > T.bj0 ? 1 : 0));
+  const int64_t n = kind == 1 ? c.usize : c.vsize;
+  note_launch();
+  kt_mark(11, st);
+  if (kind == 1)
+    launch_pdl(k_helm_jacobi_tiled<1, TR>, dim3(g), dim3(TPB), smem, st, c, rc, hj, r, x, accumulate ? 1 : 0, gate);
+  else
+    launch_pdl(k_helm_jacobi_tiled<2, TR>, dim3(g), dim3(TPB), smem, st, c, rc, hj, r, x, accumulate ? 1 : 0, gate);
+  // algorithmic bytes: r and the class map read, x written (read too when accumulating)
+  kt_mark(11, st, (double)n * (sizeof(TR) + 1 + (accumulate ? 16 : 8)));
+}
+template void launch_helm_jacobi_tiled<double>(const CaseDev&, const ResidualCoef&, const HelmJacobi&, int,
+                                               const double*, double*, bool, size_t, const Gate&, cudaStream_t);
+template void launch_helm_jacobi_tiled<float>(const CaseDev&, const ResidualCoef&, const HelmJacobi&, int,
+                                              const float*, double*, bool, size_t, const Gate&, cudaStream_t);
 
 // Roundoff bound max_i (2 nnz_i + 2) eps (|A||x| + |b|)_i of the pressure solution after its
 // refinement loop (solver/pressure_schur.py:48-56), stored at the last check; used by the

@@ -265,7 +265,7 @@ int configure_kernels(int smem_optin);
 long long kernel_launch_count();
 void kernel_launch_adjust(long long delta);
 // per-launch event timing summed per kernel class (classes listed in kernels.cu)
-static constexpr int KT_CLASSES = 11;
+static constexpr int KT_CLASSES = 12;
 void ktimer_enable(int on);
 void ktimer_collect();
 bool ktimer_active();
@@ -328,6 +328,41 @@ void launch_residual(const CaseDev& c, const ResidualCoef& rc, int kind, const d
                      bool res_f32, SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st);
 void launch_pressure_bound(const CaseDev& c, const ResidualCoef& rc, const double* b, const double* x, SolveCtl* sc,
                            int nchk, const Gate& gate, cudaStream_t st);
+// FP32 Jacobi iterations of the Helmholtz systems (index 0: u, 1: v): 1 / diagonal of the
+// regular rows per boundary class (as ResidualCoef::cc), and of every irregular row, with the
+// irregular rows' entries in FP32 and their diagonal entry zeroed.
+// Temporally blocked form (one launch per application): regular tiles of tw x th points read
+// their tile and a halo of iters - 1 points (the reach of iters - 1 five-point iterations), and
+// one body block covers the box [bj0, bj1) x [bi0, bi1) that holds every irregular row with
+// iters - 1 points of margin; it loads the region [rj0, rj1) x [ri0, ri1) that the iterations
+// of the box's points can reach through the regular and irregular stencils (found on the
+// host), and sidx maps each irregular-row entry to its place in that region (-1 outside).
+struct JacobiTiles {
+  int tw, th, ntx, nty;
+  int bj0, bj1, bi0, bi1;
+  int rj0, rj1, ri0, ri1;
+  int nrow, nnz;        // irregular rows of the grid and their entries (staged by the body block)
+  const int32_t* sidx;  // per entry: place in the body region, -1 outside
+  const int32_t* rpos;  // per irregular row: its place in the body region
+};
+struct HelmJacobi {
+  float icc[2][3][2];
+  const float* val[2];
+  const float* idiag[2];
+  int iters;
+  JacobiTiles jt[2];
+};
+// d_out = D^{-1} (r - (H - D) d_in) on the u (kind 1) or v (kind 2) faces (d_in = nullptr:
+// d_in = 0); with x set, x = [x +] that iterate instead of d_out (FP64).
+template <typename TR>
+void launch_helm_jacobi(const CaseDev& c, const ResidualCoef& rc, const HelmJacobi& hj, int kind, const TR* r,
+                        const float* din, float* dout, double* x, bool accumulate, const Gate& gate, cudaStream_t st);
+// All hj.iters iterations from d = 0 in one launch (temporal blocking): x = [x +] d.
+template <typename TR>
+void launch_helm_jacobi_tiled(const CaseDev& c, const ResidualCoef& rc, const HelmJacobi& hj, int kind, const TR* r,
+                              double* x, bool accumulate, size_t smem, const Gate& gate, cudaStream_t st);
+size_t helm_jacobi_tiled_smem(const JacobiTiles& t, int iters);
+int helm_jacobi_tiled_optin(size_t smem);
 // GMRES pieces on pressure-grid vectors: w = A z; out[i] = V_i . w (i < nv <= 64, V_i at V + i ld,
 // part: multidot_blocks(n) * nv scratch); y = alpha y + sign sum_i coef[i] V_i
 void launch_apply_pressure(const CaseDev& c, const ResidualCoef& rc, const double* z, double* w, const Gate& gate,

@@ -412,6 +412,14 @@ class MAC_CylinderFlow:
             print(f"Simulation completed in {elapsed:.2f}s ({elapsed / n_steps * 1000:.2f} ms/step)")
         return np.array(ts), np.array(cds), np.array(cls)
 
+    def helmholtz_solver_info(self):
+        """How the FP32 mode applies its CN Helmholtz inverse for the current dt: the FP32 Jacobi
+        iterations per application (0: the FFT + boundary Schur inverse) and the row-sum norm
+        of the Jacobi iteration matrix that chose them."""
+        it, rho = C.c_int32(), C.c_double()
+        check(lib.gm_solver_info(self._h, C.byref(it), C.byref(rho)), self._h)
+        return dict(jacobi_iters=int(it.value), jacobi_rho=float(rho.value))
+
     def divergence_stats(self):
         """mac_engine.calculate_mac_divergence_cpp statistics (solver/src/bindings.cpp:343-390):
         (max, sum div^2, count, core sum div^2, core count)."""

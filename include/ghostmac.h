@@ -295,10 +295,16 @@ int64_t gm_kernel_launches(void);
  * chain (empty on the direct path), final row pass, residual.  The events are recorded inside
  * the step graphs, so they time graph-replayed steps. */
 int gm_phase_timing(const gm_handle* h, double out[14]);
+/* No counterpart in the reference.  How the FP32 mode applies its approximate Helmholtz
+ * inverse for the current dt: *jacobi_iters FP32 Jacobi iterations per application (0: the FFT
+ * and boundary-Schur inverse) and *jacobi_rho, the row-sum norm of the Jacobi iteration matrix
+ * that chose them (0 before the first step, and in the plain FP64 mode).  Either may be NULL. */
+int gm_solver_info(const gm_handle* h, int32_t* jacobi_iters, double* jacobi_rho);
 /* CUDA-event timing of every launch on the stream it runs on, summed per kernel class:
  * 1 row transforms, 2 column solves, 3 momentum right-hand side, 4 operator residual,
  * 5 Schur GEMV, 6 projection pieces, 7 defect and pressure output, 8 ghost rows,
- * 9 forces and maxima, 10 gates and loop control.  enable = 1 starts (and clears) timing;
+ * 9 forces and maxima, 10 gates and loop control, 11 FP32 Jacobi iterations of the
+ * Helmholtz solves.  enable = 1 starts (and clears) timing;
  * every call returns the totals of kernel_class so far (time, launches and the launches'
  * algorithmic bytes; any output may be NULL); kernel_class 0 with enable = 0 stops timing.
  * While timing is on, steps run launch by launch (no graphs). */

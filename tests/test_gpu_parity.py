@@ -301,3 +301,53 @@ def test_iterative_matches_direct_solve(pkg):
         sf = pkg.MAC_CylinderFlow(pressure_solver='iterative', precision=prec, **kw)
         xf = sf.gg.pressure_solve(b)
         assert np.max(np.abs(xf - xd)) < 1e-8 * max(1.0, np.max(np.abs(xd)))
+
+
+def test_fp32_helmholtz_jacobi_and_fft_inverse(pkg, monkeypatch):
+    """The FP32 mode applies its CN Helmholtz inverse by FP32 Jacobi iterations when the row-sum
+    norm of the Jacobi iteration matrix is below 1/4 (about 4 dt nu / 2 / h^2); the FFT and
+    boundary-Schur inverse (GHOSTMAC_HELM_JACOBI=0) gives the same fields to the mode's
+    tolerances.  Both against the FP64 oracle after 20 noisy steps: velocity 1e-7, pressure
+    1e-5, drag 1e-6 relative, divergence < 1e-10."""
+    kw = dict(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., nu=0.02)
+    c = go.CylinderCase(**kw)
+    q = c.ops.pack(c.u, c.v)
+    q += 1e-2 * np.random.default_rng(5).standard_normal(q.size)
+    c.u, c.v = c.ops.unpack(q)
+    u0, v0 = c.u.copy(), c.v.copy()
+    c.solve(20, .002)
+    for env, expect_jacobi in ((None, True), ('0', False)):
+        if env is None:
+            monkeypatch.delenv('GHOSTMAC_HELM_JACOBI', raising=False)
+        else:
+            monkeypatch.setenv('GHOSTMAC_HELM_JACOBI', env)
+        s = pkg.MAC_CylinderFlow(verbose=False, precision='fp32', **kw)
+        s.u[:], s.v[:] = u0, v0
+        s.solve(n_steps=20, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+        info = s.helmholtz_solver_info()
+        assert (info['jacobi_iters'] > 0) == expect_jacobi, info
+        if expect_jacobi:
+            assert 0 < info['jacobi_rho'] < 0.25
+        d = s.last_step_diagnostics
+        assert d['max_divergence'] < 1e-10
+        assert rel(s.u, c.u) < 1e-7 and rel(s.v, c.v) < 1e-7 and rel(s.p, c.p) < 1e-5
+        assert abs(d['cd'] / c.last_step_diagnostics['cd'] - 1) < 1e-6
+
+
+@pytest.mark.parametrize('kw', [dict(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., nu=0.02),
+                                dict(nx=400, ny=200, Lx=20., Ly=10., D=1., xc=5., yc=5., nu=1 / 40)])
+def test_fp32_helmholtz_jacobi_tiled_equals_launches(pkg, monkeypatch, kw):
+    """The temporally blocked Jacobi application (one launch, iterations in shared memory) gives
+    bitwise the fields of one launch per iteration over the whole grid."""
+    out = []
+    for tiled in ('1', '0'):
+        monkeypatch.setenv('GHOSTMAC_HELM_JACOBI_TILED', tiled)
+        s = pkg.MAC_CylinderFlow(verbose=False, precision='fp32', **kw)
+        q = s.gg.pack(s.u, s.v)
+        q += 1e-2 * np.random.default_rng(11).standard_normal(q.size)
+        s.u[:], s.v[:] = s.gg.unpack(q)
+        s.solve(n_steps=8, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+        assert s.helmholtz_solver_info()['jacobi_iters'] > 0
+        out.append((s.u.copy(), s.v.copy(), s.p.copy()))
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
