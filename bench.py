@@ -87,7 +87,8 @@ KERNEL_CLASSES = {1: 'row transforms (k_xpass)', 2: 'column solves (k_ysolve, k_
                   5: 'boundary term (k_band_first, k_band_gemv, k_band_fwd_solve)', 6: 'projection (k_divergence, k_project_update, k_set_inlet)',
                   7: 'defect / pressure output (k_defect, k_pressure_out)', 8: 'ghost rows (k_ghost)',
                   9: 'forces / maxima (k_forces, k_maxabs)', 10: 'gates and loop control',
-                  11: 'Helmholtz Jacobi iterations (k_helm_jacobi)'}
+                  11: 'Helmholtz Jacobi iterations (k_helm_jacobi)',
+                  12: 'row transforms on the tensor cores (k_row_gemm)'}
 
 
 def replica_step_ms(step_ms, world, device='cuda'):

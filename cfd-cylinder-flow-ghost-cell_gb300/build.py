@@ -56,6 +56,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
           '-o', str(BUILD / 'periodic.o')]),
         ([nvcc, *ARCH, '-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', *inc, '-c', str(SRC / 'unet.cu'),
           '-o', str(BUILD / 'unet.o')]),
+        ([nvcc, *ARCH, '-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', *inc, '-c', str(SRC / 'rowgemm.cu'),
+          '-o', str(BUILD / 'rowgemm.o')]),
     ]
     procs = [subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True) for cmd in jobs]
     failed = []
@@ -70,7 +72,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     tmp = OUT.with_suffix('.so.tmp')
     link = [nvcc, *ARCH, '-shared', '-o', str(tmp), str(BUILD / 'geometry.o'), str(BUILD / 'kernels.o'),
             str(BUILD / 'ghostmac.o'), str(BUILD / 'noalloc.o'), str(BUILD / 'periodic.o'),
-            str(BUILD / 'unet.o'), '-lcudart']
+            str(BUILD / 'unet.o'), str(BUILD / 'rowgemm.o'), '-lcudart']
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode:
         raise RuntimeError('link failed:\n' + r.stdout + r.stderr)

@@ -127,6 +127,11 @@ struct RectDev {
   DBuf<int32_t> mrow, bptr;
   DBuf<double> binv, bfwd, mband, cvec, firstm;
   DBuf<float> binv32, bfwd32, firstm32;
+  // FP32 mode, pressure: the row passes as split-TF32 GEMMs on the tensor cores (rowgemm.cu),
+  // and their boundary-term table W (rows x cols: the phi rows, the band rows that the band
+  // solve writes in place, the psi rows)
+  RowGemm gemm;
+  DBuf<float> wcorr32;
 };
 
 }  // namespace
@@ -640,11 +645,60 @@ void build_band_tables(gm_handle* h, RectDev& rd, const std::vector<int64_t>& ro
     rd.phi32.upload(to_f32(phi), st);
     rd.psi32.upload(to_f32(psi), st);
     rd.band32.alloc((size_t)nb * cols);
+    if (kind == 0) {
+      std::vector<float> w((size_t)R * cols, 0.0f);
+      for (int j = 0; j < bj0; ++j)
+        for (int k = 0; k < cols; ++k) w[(size_t)j * cols + k] = (float)phi[(size_t)j * cols + k];
+      for (int j = bj1 + 1; j < R; ++j)
+        for (int k = 0; k < cols; ++k) w[(size_t)j * cols + k] = (float)psi[(size_t)(j - bj1 - 1) * cols + k];
+      rd.wcorr32.upload(w, st);
+    }
     TransformTables& t32 = rd.tt32;
     t32.bj0 = bj0; t32.bj1 = bj1; t32.cj0 = cj0; t32.cj1 = cj1;
     t32.bpiv = rd.bpiv32.p; t32.phi = rd.phi32.p; t32.psi = rd.psi32.p;
   }
   CK(cudaStreamSynchronize(st));
+}
+
+// The row transforms of a rectangle kind as explicit cols x cols matrices, by running the FP64
+// row-transform kernel on the rows of the identity: row k of tinv (tfwd) is the inverse (forward)
+// transform of e_k.
+void transform_matrices(gm_handle* h, const RectDev& rd, std::vector<double>& tinv, std::vector<double>& tfwd) {
+  const int n = rd.view.cols;
+  const TransformTables& tt = rd.tt;
+  cudaStream_t st = h->st;
+  const Gate open{nullptr, 0, 0};
+  const YCorr<double> none{nullptr, nullptr, nullptr, 0, -1};
+  std::vector<double> eye((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) eye[(size_t)i * n + i] = 1.0;
+  DBuf<double> deye, dinv, dfwd;
+  deye.upload(eye, st);
+  dinv.alloc((size_t)n * n);
+  dfwd.alloc((size_t)n * n);
+  launch_xpass<double, double, double>(tt, true, 0, n, deye.p, 0, n, nullptr, dinv.p, 0, n, nullptr, nullptr, none,
+                                       open, st);
+  launch_xpass<double, double, double>(tt, false, 0, n, deye.p, 0, n, nullptr, dfwd.p, 0, n, nullptr, nullptr, none,
+                                       open, st);
+  tinv.assign((size_t)n * n, 0.0);
+  tfwd.assign((size_t)n * n, 0.0);
+  CK(cudaMemcpyAsync(tinv.data(), dinv.p, tinv.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(tfwd.data(), dfwd.p, tfwd.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+}
+
+// FP32 mode: the pressure inverse's two row passes as split-TF32 GEMMs against these matrices on
+// the tensor cores (rowgemm.cu), where the grid allows it (cols a multiple of 4, at most 1024;
+// the row pitch of the pressure grid is cols).  GHOSTMAC_ROW_GEMM=0 keeps the FFT passes.
+void build_row_gemm(gm_handle* h, RectDev& rd) {
+  row_gemm_free(rd.gemm);
+  const char* e = std::getenv("GHOSTMAC_ROW_GEMM");
+  if (e && e[0] == '0') return;
+  if (h->precision != 1 || rd.view.base != 0 || rd.view.pitch != rd.view.cols) return;
+  if (rd.rank > 0 && !rd.wcorr32.p) return;
+  if (rd.view.cols % 4 || rd.view.cols > 1024 || row_gemm_smem_bytes() > h->smem_optin) return;
+  std::vector<double> tinv, tfwd;
+  transform_matrices(h, rd, tinv, tfwd);
+  row_gemm_build(rd.gemm, rd.view.cols, rd.view.rows, tfwd.data(), tinv.data(), h->smem_optin, h->st);
 }
 
 // Tables of the boundary term by direct sums.  The row transforms are taken as explicit
@@ -667,22 +721,8 @@ void build_direct_tables(gm_handle* h, RectDev& rd, const std::vector<int64_t>& 
       band_fwd_smem(tt.bj1 - tt.bj0 + 1, rank, false) > 48 * 1024)
     return;
   cudaStream_t st = h->st;
-  const Gate open{nullptr, 0, 0};
-  const YCorr<double> none{nullptr, nullptr, nullptr, 0, -1};
-  std::vector<double> eye((size_t)n * n, 0.0);
-  for (int i = 0; i < n; ++i) eye[(size_t)i * n + i] = 1.0;
-  DBuf<double> deye, dinv, dfwd;
-  deye.upload(eye, st);
-  dinv.alloc((size_t)n * n);
-  dfwd.alloc((size_t)n * n);
-  launch_xpass<double, double, double>(tt, true, 0, n, deye.p, 0, n, nullptr, dinv.p, 0, n, nullptr, nullptr, none,
-                                       open, st);
-  launch_xpass<double, double, double>(tt, false, 0, n, deye.p, 0, n, nullptr, dfwd.p, 0, n, nullptr, nullptr, none,
-                                       open, st);
-  std::vector<double> tinv((size_t)n * n), tfwd((size_t)n * n);
-  CK(cudaMemcpyAsync(tinv.data(), dinv.p, tinv.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(tfwd.data(), dfwd.p, tfwd.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
+  std::vector<double> tinv, tfwd;
+  transform_matrices(h, rd, tinv, tfwd);
   // row k of tinv is the inverse transform of e_k: value at column i = tinv[k][i]
   std::vector<int32_t> mrow(m);
   std::vector<double> binv((size_t)m * n);
@@ -954,9 +994,22 @@ void schur_inverse(gm_handle* h, RectDev& rd, const TransformTables& tt, const v
                    bool accumulate, T* spectral, T* first, T* band, double* w2, const Gate& g, cudaStream_t st) {
   const RectView& v = rd.view;
   const YCorr<T> none{nullptr, nullptr, nullptr, 0, -1};
+  // FP32 pressure inverse: both row passes on the tensor cores when their arrays have tensor maps
+  bool gemm_fwd = false, gemm_inv = false;
+  if constexpr (sizeof(T) == 4) {
+    if (rd.gemm.n > 0) {
+      gemm_fwd = row_gemm_ready(rd.gemm, r, r_f32 ? 4 : 8);
+      gemm_inv = row_gemm_ready(rd.gemm, spectral, 4) && (rd.rank == 0 || row_gemm_ready(rd.gemm, rd.wcorr32.p, 4));
+    }
+    // with the tensor-core inverse pass the band solve writes its rows into the table W
+    if (gemm_inv && rd.rank > 0) band = (T*)(rd.wcorr32.p + (int64_t)tt.bj0 * v.cols);
+  }
   sweep_mark(h, 0, st);
   if constexpr (sizeof(T) == 4) {
-    if (r_f32)
+    if (gemm_fwd) {
+      if (r_f32) launch_row_gemm_fwd<float>(rd.gemm, (const float*)r, (float*)spectral, g, st);
+      else launch_row_gemm_fwd<double>(rd.gemm, (const double*)r, (float*)spectral, g, st);
+    } else if (r_f32)
       launch_xpass<float, float, float>(tt, false, 0, v.rows, (const float*)r, v.base, v.pitch, v.cls, spectral, 0,
                                         v.cols, nullptr, nullptr, none, g, st);
     else
@@ -997,8 +1050,14 @@ void schur_inverse(gm_handle* h, RectDev& rd, const TransformTables& tt, const v
     for (int k = 3; k <= 5; ++k) sweep_mark(h, k, st);
   }
   sweep_mark(h, 6, st);
-  launch_xpass<T, T, double>(tt, true, 0, v.rows, spectral, 0, v.cols, nullptr, x, v.base, v.pitch, v.cls,
-                             accumulate ? x : nullptr, corr, g, st);
+  bool inv_done = false;
+  if constexpr (sizeof(T) == 4)
+    if (gemm_inv)
+      inv_done = launch_row_gemm_inv(rd.gemm, (const float*)spectral, rd.rank > 0 ? rd.wcorr32.p : nullptr, tt.bj0,
+                                     tt.bj1, x, v.base, v.pitch, v.cls, accumulate ? x : nullptr, g, st);
+  if (!inv_done)
+    launch_xpass<T, T, double>(tt, true, 0, v.rows, spectral, 0, v.cols, nullptr, x, v.base, v.pitch, v.cls,
+                               accumulate ? x : nullptr, corr, g, st);
   sweep_mark(h, 7, st);
 }
 
@@ -1917,6 +1976,7 @@ int gm_create(const gm_config* cfg, gm_handle** out) {
     fill_case_dev(H);
     build_rect_tables(H, H->rp, 0, 0.0);
     build_schur(H, H->rp, g.schur_p_rows, g.schur_p_c, H->pw2.p);
+    build_row_gemm(H, H->rp);
     CK(cudaMemsetAsync(H->pw2.p, 0, H->Pn * sizeof(double), st));
     initial_state(H);
   });

@@ -150,7 +150,7 @@ void kernel_launch_adjust(long long delta) { g_launches.fetch_add(delta, std::me
 // benchmark for its per-class breakdown and the dominant kernel's launch time).  Classes:
 // 1 x pass, 2 column solves, 3 momentum, 4 residual, 5 boundary chain / Schur GEMV, 6 projection pieces,
 // 7 defect / pressure output, 8 ghost rows, 9 forces / maxima, 10 gates and loop control,
-// 11 FP32 Jacobi sweeps of the Helmholtz systems.
+// 11 FP32 Jacobi sweeps of the Helmholtz systems, 12 row transforms on the tensor cores.
 namespace {
 struct KTimer {
   bool on = false;
@@ -200,6 +200,9 @@ void ktimer_collect() {
   g_kt.used = 0;
 }
 bool ktimer_active() { return g_kt.on; }
+void note_launch_ext() { note_launch(); }
+void kt_mark_ext(int cls, cudaStream_t st, double bytes) { kt_mark(cls, st, bytes); }
+int pdl_mode_ext() { return pdl_mode(); }
 void ktimer_read(int cls, double* total_ms, long long* count, double* bytes) {
   const bool ok = cls >= 0 && cls < KT_CLASSES;
   *total_ms = ok ? g_kt.total_ms[cls] : 0.0;

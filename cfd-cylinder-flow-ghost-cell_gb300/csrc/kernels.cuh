@@ -260,12 +260,71 @@ struct YCorr {
   int j0, j1;
 };
 
+// ---- tensor-core row transforms of the FP32 mode (rowgemm.cu) ---------------
+// Transform matrices of the pressure rectangle in split TF32 (both directions) with their TMA
+// descriptors, and the descriptors of the arrays the passes have read (cached per array).
+struct RowGemm;
+void row_gemm_free(RowGemm& g);
+struct RowGemm {
+  static constexpr int AMAPS = 8;
+  alignas(64) unsigned char tmap[2][128];
+  alignas(64) unsigned char amap[AMAPS][128];
+  const void* aptr[AMAPS] = {};
+  int aesz[AMAPS] = {};
+  int namap = 0;
+  float* mats = nullptr;
+  int n = 0, rows = 0, np = 0, kp = 0;  // n = 0: not built (the FFT passes run)
+  RowGemm() = default;
+  RowGemm(const RowGemm&) = delete;
+  RowGemm& operator=(const RowGemm&) = delete;
+  ~RowGemm() { row_gemm_free(*this); }
+};
+struct RowGemmArgs {
+  int M, N, K, np;
+  float* sout;                 // forward: spectrum (row pitch N)
+  double* xout;                // inverse: field, x[obase + m opitch + n]
+  int64_t obase, opitch;
+  const uint8_t* ocls;
+  const double* add;
+  const float* wcorr;          // inverse: boundary-term table W (M x N), band rows j0..j1
+  int corr, j0, j1;
+  Gate gate;
+};
+size_t row_gemm_smem_bytes();
+// whether the passes can read (and write, for the spectrum) this array: a tensor map of it exists
+bool row_gemm_ready(RowGemm& g, const void* ptr, int esize);
+int row_gemm_build(RowGemm& g, int n, int rows, const double* tfwd, const double* tinv, size_t smem_optin,
+                   cudaStream_t st);
+template <typename TI>
+bool launch_row_gemm_fwd(RowGemm& g, const TI* in, float* spec, const Gate& gate, cudaStream_t st);
+bool launch_row_gemm_inv(RowGemm& g, const float* spec, const float* wcorr, int j0, int j1, double* x, int64_t obase,
+                         int64_t opitch, const uint8_t* ocls, const double* add, const Gate& gate, cudaStream_t st);
+// launch bookkeeping shared with the other translation units
+void note_launch_ext();
+void kt_mark_ext(int cls, cudaStream_t st, double bytes);
+int pdl_mode_ext();
+template <typename... KArgs, typename... Args>
+inline void launch_pdl_ext(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                           Args&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = pdl_mode_ext();
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 // ---- launchers (kernels.cu) ------------------------------------------------
 int configure_kernels(int smem_optin);
 long long kernel_launch_count();
 void kernel_launch_adjust(long long delta);
 // per-launch event timing summed per kernel class (classes listed in kernels.cu)
-static constexpr int KT_CLASSES = 12;
+static constexpr int KT_CLASSES = 13;
 void ktimer_enable(int on);
 void ktimer_collect();
 bool ktimer_active();

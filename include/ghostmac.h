@@ -304,7 +304,8 @@ int gm_solver_info(const gm_handle* h, int32_t* jacobi_iters, double* jacobi_rho
  * 1 row transforms, 2 column solves, 3 momentum right-hand side, 4 operator residual,
  * 5 Schur GEMV, 6 projection pieces, 7 defect and pressure output, 8 ghost rows,
  * 9 forces and maxima, 10 gates and loop control, 11 FP32 Jacobi iterations of the
- * Helmholtz solves.  enable = 1 starts (and clears) timing;
+ * Helmholtz solves, 12 the FP32 mode's pressure row transforms as tensor-core GEMMs.
+ * enable = 1 starts (and clears) timing;
  * every call returns the totals of kernel_class so far (time, launches and the launches'
  * algorithmic bytes; any output may be NULL); kernel_class 0 with enable = 0 stops timing.
  * While timing is on, steps run launch by launch (no graphs). */
