@@ -71,6 +71,12 @@ GMRES_WORKLOADS = {
                                  dt=0.0015, noise='v', amp=1e-2, seed=0, record_steps=40, epochs=600),
 }
 DEFAULT_WORKLOAD = 'wide_800x820_re100'
+# FP64 instructions (dadd + dmul + dfma, thread level) per cell update of the plain FP64 step on
+# the 800x820 case, and the measured FP64 instruction rate of a GB300 (independent FMA chains on
+# every SM, profiles/gb300_rates.md); the count comes from the ncu capture in FP64_OPS_SOURCE.
+FP64_OPS_PER_CELL_UPDATE = 0.0
+FP64_OPS_SOURCE = 'profiles/fp64_instructions_wide_800x820.md'
+FP64_INST_RATE = 499e9
 # DRAM bytes (read + write) per launch of the dominant kernel class, averaged over the launches
 # of one ncu --set full capture of the same command (the capture's file under profiles/ gives the
 # command and the per-launch figures).  Within a step the working set stays in L2, so DRAM
@@ -423,8 +429,23 @@ def run_ours(args, w, rank, world):
             e1.synchronize()
             t64.append(e0.elapsed_time(e1))
         ms64 = sum(t64) / len(t64)
+        # the bound of the plain FP64 step: its HBM roofline (880 algorithmic bytes per cell
+        # update) and its FP64-pipe roofline (FP64 instructions per cell update counted by ncu,
+        # against the measured FP64 instruction rate)
+        peak_gbs, _ = peaks()
+        fp64_gbs = 880.0 * cells / (ms64 * 1e-3) / 1e9
+        fp64_ops = FP64_OPS_PER_CELL_UPDATE * cells / (ms64 * 1e-3)
         compare = dict(plain_fp64_value=cells / (ms64 * 1e-3), plain_fp64_ms_per_step=ms64,
-                       speedup_vs_plain_fp64=ms64 / step_ms)
+                       speedup_vs_plain_fp64=ms64 / step_ms,
+                       plain_fp64_step_roofline=dict(bound='fp64 pipe',
+                                                     hbm=dict(algorithmic_bytes_per_cell_update=880,
+                                                              achieved_gbs=fp64_gbs, peak_gbs=peak_gbs,
+                                                              frac=fp64_gbs / peak_gbs),
+                                                     fp64_pipe=dict(fp64_instructions_per_cell_update=FP64_OPS_PER_CELL_UPDATE,
+                                                                    achieved_ginst_s=fp64_ops / 1e9,
+                                                                    peak_ginst_s=FP64_INST_RATE / 1e9,
+                                                                    frac=fp64_ops / FP64_INST_RATE,
+                                                                    source=FP64_OPS_SOURCE)))
         del s64
     # roofline of the dominant kernel class: its launches' algorithmic bytes / their event time
     nx, ny = w['nx'], w['ny']
@@ -433,6 +454,10 @@ def run_ours(args, w, rank, world):
     peak, peak_kind = peaks()
     achieved = by.value / max(tot.value * 1e-3, 1e-12) / 1e9
     traffic = DRAM_TRAFFIC.get((args.workload, args.precision, dominant))
+    # config 4 beside the single case: the 64-case sweep in both precisions
+    sweep = None
+    if args.precision == 'fp32' and not args.no_batch and world == 1:
+        sweep = batch_summary(pkg, L, BATCH_WORKLOADS['sweep64_batch'], max(1, min(args.steps, 10)), args.warmup)
     # end to end through the public API with host numpy arrays
     e2e_steps = max(1, min(args.steps, 10))
     torch.cuda.synchronize()
@@ -466,7 +491,7 @@ def run_ours(args, w, rank, world):
                     refinement_sweeps_per_step=dict(pressure=float(np.mean([a for a, _ in sweeps])),
                                                     momentum=float(np.mean([b for _, b in sweeps]))),
                     kernel_class_ms_per_step={KERNEL_CLASSES[c]: v[0] for c, v in per_class.items() if v[1]},
-                    graph_phase_ms=phase_ms, comparison=compare)
+                    graph_phase_ms=phase_ms, comparison=compare, sweep64_batch=sweep)
         print(json.dumps(line), flush=True)
 
 
@@ -618,6 +643,42 @@ def run_ours_gmres(args, w, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def batch_summary(pkg, L, w, steps, warmup):
+    """The 64-case sweep (config 4) timed beside the single-case workload: K batch steps of the
+    FP32 mode and of the plain FP64 mode, each one call (one graph launch per step), the cases'
+    state (about 1 GB) larger than L2.  Returns the summary the bench line carries."""
+    import torch
+    dt = w['dt']
+    out = dict(workload='sweep64_batch', steps=steps)
+    for prec in ('fp32', 'fp64'):
+        t0 = time.perf_counter()
+        cases, _ = sweep_cases(pkg, w, prec)
+        setup_s = time.perf_counter() - t0
+        cells = sum(c.nx * c.ny for c in cases)
+        batch = pkg.CylinderBatch(cases)
+        for c in cases:
+            c._push()
+        k = 0
+        for _ in range(max(warmup, 3)):
+            rc, diag, done = batch.step_raw(dt, 1, first_index=k)
+            batch._check(rc)
+            k += 1
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc, diag, done = batch.step_raw(dt, steps, first_index=k)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / steps
+        batch._check(rc)
+        divs = [diag[i].max_divergence for i in range(len(cases) * steps)]
+        assert max(divs) < 1e-10
+        out[prec] = dict(value=cells / (ms * 1e-3), unit='cell-updates/s', ms_per_step=ms, cases=len(cases),
+                         cells_per_step=cells, max_divergence=max(divs), setup_s=setup_s)
+        batch.close()
+        del batch, cases
+    out['speedup_fp32_vs_plain_fp64'] = out['fp64']['ms_per_step'] / out['fp32']['ms_per_step']
+    return out
+
+
 def run_ours_batch(args, w, rank, world):
     """Batched sweep: all cases advance together, one graph launch per step."""
     import torch
@@ -747,6 +808,7 @@ def main():
                     sorted(GMRES_WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
     ap.add_argument('--no-compare', action='store_true', help='skip timing the plain FP64 step beside the FP32 mode')
+    ap.add_argument('--no-batch', action='store_true', help='skip timing the 64-case sweep beside the single case')
     ap.add_argument('--precision', choices=('fp64', 'fp32'), default='fp32',
                     help='fp64: plain FP64 method; fp32: FP32 inverses and stencils with FP64 refinement')
     args = ap.parse_args()

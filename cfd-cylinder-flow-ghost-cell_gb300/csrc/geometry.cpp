@@ -591,6 +591,72 @@ static void schur_setup(const Geometry& g, const Rect& rect, int field_kind, con
   }
 }
 
+// Quadratic point-pressure reconstruction (solver/cut_cell_solver.py:25-55): at every point
+// (py[k], px[k]) the 12 nearest exterior active pressure centres of a padded window (with ties
+// at the cutoff), weights from the minimum-norm least-squares fit of a quadratic.  Rows of out
+// are the points, columns grid flat p indices.
+bool pressure_reconstruction(const Geometry& g, const std::vector<double>& py, const std::vector<double>& px,
+                             Csr& out, std::string& err) {
+  const size_t count = py.size();
+  if (count == 0 || px.size() != count) { err = "At least one pressure sample is required"; return false; }
+  for (size_t k = 0; k < count; ++k) {
+    if (!std::isfinite(py[k]) || !std::isfinite(px[k])) {
+      err = "Pressure sample points must be finite (y, x) pairs";
+      return false;
+    }
+  }
+  for (size_t k = 0; k < count; ++k)
+    if (py[k] < 0 || py[k] > g.Ly || px[k] < 0 || px[k] > g.Lx) {
+      err = "Pressure sample points must lie inside the domain";
+      return false;
+    }
+  for (size_t k = 0; k < count; ++k)
+    if (std::hypot(px[k] - g.xc, py[k] - g.yc) < g.R * (1 - 1e-12)) {
+      err = "Physical pressure cannot be sampled inside the solid";
+      return false;
+    }
+  const double pad = 4 * std::max(g.dx, g.dy);
+  const double ymin = *std::min_element(py.begin(), py.end());
+  const double xmin = *std::min_element(px.begin(), px.end());
+  const double ymax = *std::max_element(py.begin(), py.end());
+  const double xmax = *std::max_element(px.begin(), px.end());
+  const int64_t jlo = std::max<int64_t>(0, (int64_t)std::floor((ymin - pad) / g.dy));
+  const int64_t ilo = std::max<int64_t>(0, (int64_t)std::floor((xmin - pad) / g.dx));
+  const int64_t jhi = std::min<int64_t>(g.ny, (int64_t)std::ceil((ymax + pad) / g.dy) + 1);
+  const int64_t ihi = std::min<int64_t>(g.nx, (int64_t)std::ceil((xmax + pad) / g.dx) + 1);
+  std::vector<double> cy, cx;
+  std::vector<int64_t> ids;
+  for (int64_t j = jlo; j < jhi; ++j)
+    for (int64_t i = ilo; i < ihi; ++i) {
+      double y = (j + .5) * g.dy, x = (i + .5) * g.dx;
+      if (g.act_p[(size_t)j * g.nx + i] && std::hypot(x - g.xc, y - g.yc) >= g.R * (1 - 1e-12)) {
+        cy.push_back(y); cx.push_back(x); ids.push_back(j * g.nx + i);
+      }
+    }
+  if (ids.size() < 12) { err = "Pressure reconstruction needs at least 12 exterior centers"; return false; }
+  std::vector<int> near;
+  out = Csr();
+  for (size_t k = 0; k < count; ++k) {
+    neighbours(cy, cx, py[k], px[k], 12, near);
+    int n = (int)near.size();
+    std::vector<double> B(6 * (size_t)n), w(n);
+    for (int c = 0; c < n; ++c) {
+      double oy = (cy[near[c]] - py[k]) / g.dy, ox = (cx[near[c]] - px[k]) / g.dx;
+      B[0 * n + c] = 1.0; B[1 * n + c] = ox; B[2 * n + c] = oy;
+      B[3 * n + c] = ox * ox; B[4 * n + c] = ox * oy; B[5 * n + c] = oy * oy;
+    }
+    double t[6] = {1, 0, 0, 0, 0, 0};
+    int rank = 0;
+    if (!lstsq_full(6, n, B.data(), t, w.data(), 1e-12, &rank, nullptr) || rank != 6) {
+      err = "Pressure stencil cannot resolve a quadratic polynomial";
+      return false;
+    }
+    for (int c = 0; c < n; ++c) { out.col.push_back(ids[near[c]]); out.val.push_back(w[c]); }
+    out.ptr.push_back((int64_t)out.col.size());
+  }
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 // surface quadrature (solver/cut_cell_solver.py:25-77, solver/optimized_ghost_cell.py:144-172)
 // ---------------------------------------------------------------------------
@@ -613,48 +679,8 @@ static bool surface_setup(Geometry& g, std::string& err) {
     g.normal_y[k] = g.normal_wy[k] / (PI * Dd / count);
   }
   (void)nscale;
-  // pressure point reconstruction: exterior active centres in a padded window
-  {
-    double pad = 4 * std::max(g.dx, g.dy);
-    double ymin = *std::min_element(g.surf_y.begin(), g.surf_y.end());
-    double xmin = *std::min_element(g.surf_x.begin(), g.surf_x.end());
-    double ymax = *std::max_element(g.surf_y.begin(), g.surf_y.end());
-    double xmax = *std::max_element(g.surf_x.begin(), g.surf_x.end());
-    int64_t jlo = std::max<int64_t>(0, (int64_t)std::floor((ymin - pad) / g.dy));
-    int64_t ilo = std::max<int64_t>(0, (int64_t)std::floor((xmin - pad) / g.dx));
-    int64_t jhi = std::min<int64_t>(g.ny, (int64_t)std::ceil((ymax + pad) / g.dy) + 1);
-    int64_t ihi = std::min<int64_t>(g.nx, (int64_t)std::ceil((xmax + pad) / g.dx) + 1);
-    std::vector<double> cy, cx;
-    std::vector<int64_t> ids;
-    for (int64_t j = jlo; j < jhi; ++j)
-      for (int64_t i = ilo; i < ihi; ++i) {
-        double y = (j + .5) * g.dy, x = (i + .5) * g.dx;
-        if (g.act_p[(size_t)j * g.nx + i] && std::hypot(x - g.xc, y - g.yc) >= g.R * (1 - 1e-12)) {
-          cy.push_back(y); cx.push_back(x); ids.push_back(j * g.nx + i);
-        }
-      }
-    if (ids.size() < 12) { err = "Pressure reconstruction needs at least 12 exterior centers"; return false; }
-    std::vector<int> near;
-    g.surf_p = Csr();
-    for (int k = 0; k < count; ++k) {
-      neighbours(cy, cx, g.surf_y[k], g.surf_x[k], 12, near);
-      int n = (int)near.size();
-      std::vector<double> B(6 * (size_t)n), w(n);
-      for (int c = 0; c < n; ++c) {
-        double oy = (cy[near[c]] - g.surf_y[k]) / g.dy, ox = (cx[near[c]] - g.surf_x[k]) / g.dx;
-        B[0 * n + c] = 1.0; B[1 * n + c] = ox; B[2 * n + c] = oy;
-        B[3 * n + c] = ox * ox; B[4 * n + c] = ox * oy; B[5 * n + c] = oy * oy;
-      }
-      double t[6] = {1, 0, 0, 0, 0, 0};
-      int rank = 0;
-      if (!lstsq_full(6, n, B.data(), t, w.data(), 1e-12, &rank, nullptr) || rank != 6) {
-        err = "Pressure stencil cannot resolve a quadratic polynomial";
-        return false;
-      }
-      for (int c = 0; c < n; ++c) { g.surf_p.col.push_back(ids[near[c]]); g.surf_p.val.push_back(w[c]); }
-      g.surf_p.ptr.push_back((int64_t)g.surf_p.col.size());
-    }
-  }
+  // pressure point reconstruction at the surface points
+  if (!pressure_reconstruction(g, g.surf_y, g.surf_x, g.surf_p, err)) return false;
   // wall-normal derivative stencils for u and v
   for (int field = 0; field < 2; ++field) {
     const std::vector<double>& x = field == 0 ? g.xu : g.xv;

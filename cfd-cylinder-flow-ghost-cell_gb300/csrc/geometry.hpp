@@ -87,6 +87,11 @@ struct HelmholtzSetup {
 bool build_geometry(Geometry& g, int& err_class);
 bool build_helmholtz(const Geometry& g, double dt, HelmholtzSetup& hs, int& err_class, std::string& err);
 
+// Quadratic point-pressure reconstruction at the points (py[k], px[k]) (solver/cut_cell_solver.py:25-55):
+// rows = points, columns = grid flat p indices; false with err set for invalid points.
+bool pressure_reconstruction(const Geometry& g, const std::vector<double>& py, const std::vector<double>& px,
+                             Csr& out, std::string& err);
+
 // Least-squares helpers (min-norm solution of B w = t with B m x n, m <= n).
 bool min_norm_lstsq(int m, int n, const double* B /*row-major m x n*/, const double* t, double* w,
                     double rcond, int* rank);

@@ -2097,6 +2097,24 @@ int gm_get_surface_points(const gm_handle* h, double* yx) {
   return GM_OK;
 }
 
+int gm_pressure_reconstruction(gm_handle* h, const double* yx, int32_t n_points, int64_t* nnz, int64_t* ptr,
+                               int64_t* cols, double* vals) {
+  if (!h || !yx || !nnz || n_points < 0) return GM_EVALUE;
+  std::vector<double> py((size_t)n_points), px((size_t)n_points);
+  for (int32_t k = 0; k < n_points; ++k) { py[k] = yx[2 * k]; px[k] = yx[2 * k + 1]; }
+  gm::Csr out;
+  std::string err;
+  if (!gm::pressure_reconstruction(h->g, py, px, out, err)) {
+    h->err = err;
+    return GM_EVALUE;
+  }
+  *nnz = out.nnz();
+  if (ptr) std::copy(out.ptr.begin(), out.ptr.end(), ptr);
+  if (cols) std::copy(out.col.begin(), out.col.end(), cols);
+  if (vals) std::copy(out.val.begin(), out.val.end(), vals);
+  return GM_OK;
+}
+
 int gm_host_alloc(size_t bytes, void** out) {
   if (!out) return GM_EVALUE;
   *out = nullptr;
@@ -2584,6 +2602,9 @@ int gm_solver_info(const gm_handle* h, int32_t* jacobi_iters, double* jacobi_rho
 
 int gm_kernel_timing(int32_t kernel_class, int32_t enable, double* total_ms, int64_t* count, double* bytes) {
   if (enable) ktimer_enable(1);
+  // launches timed outside a step (pressure solves, operator calls) are folded in here
+  if (ktimer_active() && cudaDeviceSynchronize() == cudaSuccess) ktimer_collect();
+  cudaGetLastError();
   double t = 0, by = 0;
   long long n = 0;
   ktimer_read(kernel_class, &t, &n, &by);

@@ -56,6 +56,47 @@ def _like(x, n):
     return np.empty(n)
 
 
+class PointOperator:
+    """A sparse operator in CSR form (rows = sample points, columns = flat grid indices) with
+    ``op @ x`` for a flat host array: what the reference keeps as a scipy CSR matrix."""
+
+    def __init__(self, indptr, indices, data, ncols):
+        self.indptr, self.indices, self.data = indptr, indices, data
+        self.shape = (len(indptr) - 1, int(ncols))
+
+    def __matmul__(self, x):
+        x = np.asarray(x, dtype=np.float64).ravel()
+        if x.size != self.shape[1]:
+            raise ValueError('operand size does not match the operator')
+        prod = self.data * x[self.indices]
+        out = np.zeros(self.shape[0])
+        rows = np.repeat(np.arange(self.shape[0]), np.diff(self.indptr))
+        np.add.at(out, rows, prod)
+        return out
+
+    def toarray(self):
+        a = np.zeros(self.shape)
+        rows = np.repeat(np.arange(self.shape[0]), np.diff(self.indptr))
+        np.add.at(a, (rows, self.indices), self.data)
+        return a
+
+
+def pressure_reconstruction(handle, points, ncols):
+    """Quadratic point-pressure operator at (y, x) points through gm_pressure_reconstruction
+    (solver/cut_cell_solver.py:25-55); invalid points raise the reference's ValueError."""
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    if pts.ndim != 2 or pts.shape[1] != 2 or not np.isfinite(pts).all():
+        raise ValueError('Pressure sample points must be finite (y, x) pairs')
+    nnz = C.c_int64()
+    check(lib.gm_pressure_reconstruction(handle, ptr(pts), len(pts), C.byref(nnz), None, None, None), handle)
+    indptr = np.empty(len(pts) + 1, np.int64)
+    cols = np.empty(nnz.value, np.int64)
+    vals = np.empty(nnz.value)
+    check(lib.gm_pressure_reconstruction(handle, ptr(pts), len(pts), C.byref(nnz), ptr(indptr), ptr(cols),
+                                         ptr(vals)), handle)
+    return PointOperator(indptr, cols, vals, ncols)
+
+
 class GhostCellIntegrator:
     """GPU counterpart of solver/optimized_ghost_cell.py:GhostCellIntegrator for one case."""
 
@@ -154,6 +195,11 @@ class GhostCellIntegrator:
         u, v, p = _f64(u), _f64(v), _f64(p)
         check(lib.gm_surface_forces(self._h, ptr(u), ptr(v), ptr(p), float(mu), ptr(out)), self._h)
         return tuple(float(x) for x in out)
+
+    def pressure_reconstruction(self, points):
+        """Quadratic point-pressure operator at (y, x) points (rows) over the flat pressure grid
+        (build_pressure_reconstruction of solver/cut_cell_solver.py:25-55)."""
+        return pressure_reconstruction(self._h, points, self.nx * self.ny)
 
     def ghost_stencils(self, which):
         """(rows, ptr, cols, vals) of the ghost rows of E_u (0), E_v (1) or P (2), grid flat indices."""
@@ -474,17 +520,30 @@ class MAC_CylinderFlow:
                 tmp.unlink()
 
     @classmethod
-    def from_checkpoint(cls, path, *, check_sources=True):
-        """Resume a schema-1 checkpoint; reject foreign sources or incomplete AB2 history (solver/main.py:532-567)."""
+    def from_checkpoint(cls, path, *, check_sources=True, accept_reference=False, precision=None):
+        """Resume a schema-1 checkpoint; reject foreign sources or incomplete AB2 history (solver/main.py:532-567).
+
+        A checkpoint written by the reference solver's own save_checkpoint (ghost-cell AB2/CN:
+        the same arrays, packed history layouts and metadata keys) is imported when
+        ``accept_reference`` is set, and rejected as a source mismatch otherwise.  ``precision``
+        overrides the checkpoint's precision mode ('fp64' for a reference checkpoint)."""
         with np.load(path, allow_pickle=False) as data:
             meta = json.loads(str(data['checkpoint_metadata']))
             if meta.get('schema') != 1 or meta['configuration'].get('boundary') not in ('cut_cell', 'ghost_cell'):
                 raise ValueError('Unsupported checkpoint')
+            sources = meta.get('source_sha256') or {}
+            from_reference = 'optimized_ghost_cell.py' in sources and 'compiled_engine' in sources
+            if from_reference and not accept_reference:
+                raise ValueError('Checkpoint source mismatch: written by the reference solver '
+                                 '(from_checkpoint(..., accept_reference=True) imports it)')
             config = dict(meta['configuration'])
             config['verbose'] = False
+            if precision is not None:
+                config['precision'] = precision
             solver = cls(**config)
-            if check_sources and meta.get('source_sha256') != solver._source_hashes():
+            if check_sources and not from_reference and sources != solver._source_hashes():
                 raise ValueError('Checkpoint source mismatch')
+            solver.restored_from = 'reference' if from_reference else 'library'
             for name in ('u', 'v', 'p', 'phi', 'u_inlet'):
                 value = data[name]
                 target = getattr(solver, name)

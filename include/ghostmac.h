@@ -123,6 +123,15 @@ int gm_get_ghost_stencils(const gm_handle* h, int32_t which, int64_t* n_rows, in
 int gm_get_schur_rows(const gm_handle* h, int32_t which, int64_t* n, int64_t* rows);
 /* Circle quadrature points (y, x) pairs (solver/cut_cell_solver.py:70-77). */
 int gm_get_surface_points(const gm_handle* h, double* yx);
+/* Quadratic point-pressure reconstruction at n_points (y, x) pairs (replaces
+ * build_pressure_reconstruction, solver/cut_cell_solver.py:25-55, as used by CylinderSamples,
+ * postprocessing/cylinder_observables.py:38-39): a CSR matrix of n_points rows over the grid flat
+ * pressure indices.  *nnz is always set; ptr (n_points + 1), cols and vals (nnz) are filled when
+ * not NULL, so a first call with them NULL sizes the arrays.  Points outside the domain, inside
+ * the solid or not finite give GM_EVALUE with the reference's message.  Works on host-only
+ * handles. */
+int gm_pressure_reconstruction(gm_handle* h, const double* yx, int32_t n_points, int64_t* nnz, int64_t* ptr,
+                               int64_t* cols, double* vals);
 
 /* --- state ----------------------------------------------------------------- */
 
@@ -306,8 +315,9 @@ int gm_solver_info(const gm_handle* h, int32_t* jacobi_iters, double* jacobi_rho
  * 9 forces and maxima, 10 gates and loop control, 11 FP32 Jacobi iterations of the
  * Helmholtz solves, 12 the FP32 mode's pressure row transforms as tensor-core GEMMs.
  * enable = 1 starts (and clears) timing;
- * every call returns the totals of kernel_class so far (time, launches and the launches'
- * algorithmic bytes; any output may be NULL); kernel_class 0 with enable = 0 stops timing.
+ * every call first folds in the launches made since the last step (after a device
+ * synchronisation), then returns the totals of kernel_class so far (time, launches and the
+ * launches' algorithmic bytes; any output may be NULL); kernel_class 0 with enable = 0 stops timing.
  * While timing is on, steps run launch by launch (no graphs). */
 int gm_kernel_timing(int32_t kernel_class, int32_t enable, double* total_ms, int64_t* count, double* bytes);
 

@@ -50,6 +50,9 @@ def build_harness(reference: Path, work: Path) -> Path:
                     ignore=shutil.ignore_patterns('__pycache__'))
     shutil.copytree(reference / 'verification', work / 'verification',
                     ignore=shutil.ignore_patterns('__pycache__'))
+    (work / 'validation').mkdir()
+    for name in ('__init__.py', 'run_ghost_validation.py'):
+        shutil.copy(reference / 'validation' / name, work / 'validation' / name)
     stubs = work / 'stubs'
     (stubs / 'matplotlib').mkdir(parents=True)
     (stubs / 'numba.py').write_text(NUMBA_STUB)
@@ -125,7 +128,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', type=Path, required=True, help='path of the reference checkout')
     ap.add_argument('--skip-large', action='store_true')
-    ap.add_argument('--only', choices=('taylor_green', 'analysis'), help='generate one group of fixtures only')
+    ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner'),
+                    help='generate one group of fixtures only')
     args = ap.parse_args()
     work = Path(tempfile.mkdtemp(prefix='ghost_golden_'))
     try:
@@ -134,12 +138,77 @@ def main():
             run_taylor_green(work)
         elif args.only == 'analysis':
             run_analysis(work)
+        elif args.only == 'runner':
+            run_runner(work)
         else:
             run_all(args)
             run_taylor_green(work)
             run_analysis(work)
+            run_runner(work)
     finally:
         shutil.rmtree(work, ignore_errors=True)
+
+
+RUNNER_CASE = dict(kind='steady', dt=0.002, end_time=0.03, sample_start=0.01, profile_stride=2,
+                   solver=dict(nx=88, ny=16, Lx=22., Ly=4.1, D=1., xc=2., yc=2., nu=0.02,
+                               boundary='ghost_cell', time_scheme='ab2_cn'))
+
+
+def run_runner(work):
+    """A checkpoint written by the reference's own save_checkpoint (solver/main.py:503-530) and
+    the fields after the reference resumes it; the reference's runner contract
+    (validation/run_ghost_validation.py:19-102) on a small case: its history rows, summary,
+    mean observables and centre-line samples; the pressure reconstruction operator and
+    recirculation lengths of postprocessing/cylinder_observables.py."""
+    import json
+    from main import MAC_CylinderFlow
+    from cut_cell_solver import build_pressure_reconstruction
+    from postprocessing.cylinder_observables import recirculation_length
+    from validation import run_ghost_validation as runner
+
+    # 1. checkpoint after 4 noisy steps, then 3 more steps from the reloaded checkpoint
+    kw = dict(RUNNER_CASE['solver'])
+    s = MAC_CylinderFlow(verbose=False, **kw)
+    q = s.gg.pack(s.u, s.v).copy()
+    q += 1e-2 * np.random.default_rng(9).standard_normal(q.size)
+    u0, v0 = s.gg.unpack(q)
+    s.u[:], s.v[:] = u0, v0
+    s.solve(n_steps=4, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+    ck = work / 'reference_checkpoint.npz'
+    s.save_checkpoint(ck)
+    shutil.copy(ck, HERE / 'reference_checkpoint_88x16.npz')
+    r = MAC_CylinderFlow.from_checkpoint(ck)
+    scal = []
+    for _ in range(3):
+        r.solve(n_steps=1, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+        d = r.last_step_diagnostics
+        scal.append([r.time, d['cd'], d['cl'], d['max_divergence']])
+    save('reference_resume_88x16', u=r.u, v=r.v, p=r.p, scalars=np.array(scal))
+
+    # 2. the runner on a small steady case
+    cfg = work / 'case.json'
+    cfg.write_text(json.dumps(RUNNER_CASE))
+    out = work / 'run'
+    runner.run(cfg, out)
+    rows = [json.loads(line) for line in (out / 'history.jsonl').read_text().splitlines()]
+    keys = sorted(k for k in rows[0] if isinstance(rows[0][k], (int, float)) and k != 'wall_seconds')
+    history = np.array([[float(row[k]) for k in keys] for row in rows])
+    centre = np.fromfile(out / 'centerline.bin', dtype='<f8')
+    s2 = MAC_CylinderFlow(verbose=False, **kw)
+    pts = np.array([[s2.yc, s2.xc - s2.D / 2], [s2.yc, s2.xc + s2.D / 2], [1.3, 3.7], [3.0, 1.2], [2.0, 10.0]])
+    rec = build_pressure_reconstruction(s2.gg.geom, pts)
+    x = np.linspace(1.5, 6.0, 10)
+    recirc, status = [], []
+    for vel in (np.linspace(-1, 1, 10), np.linspace(0.1, 1, 10), np.r_[0.2, 0.3, -0.1, -0.2, np.linspace(.1, 1, 6)],
+                -np.ones(10)):
+        res = recirculation_length(x, vel, 1.5, 1.0)
+        recirc.append([np.nan if res.get('length_D') is None else res['length_D']])
+        status.append(res['status'])
+    save('runner_88x16', case=json.dumps(RUNNER_CASE), history_keys=np.array(keys), history=history,
+         summary=(out / 'summary.json').read_text(), mean_observables=(out / 'mean_observables.json').read_text(),
+         centerline_meta=(out / 'centerline.json').read_text(), centerline=centre,
+         rec_points=pts, rec_indptr=rec.indptr.astype(np.int64), rec_indices=rec.indices.astype(np.int64),
+         rec_data=rec.data.copy(), recirc_x=x, recirc_lengths=np.array(recirc), recirc_status=np.array(status))
 
 
 def run_analysis(work):
