@@ -28,7 +28,8 @@ SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_las
            'gm_tg_set_state', 'gm_tg_get_state', 'gm_tg_step', 'gm_unet_layers', 'gm_unet_create',
            'gm_unet_destroy', 'gm_unet_last_error', 'gm_unet_input', 'gm_unet_forward', 'gm_unet_backward',
            'gm_set_learned_preconditioner', 'gm_set_pressure_recorder', 'gm_pressure_recorded',
-           'gm_host_alloc', 'gm_host_free', 'gm_solver_info', 'gm_pressure_reconstruction')
+           'gm_host_alloc', 'gm_host_free', 'gm_solver_info', 'gm_pressure_reconstruction',
+           'gm_mac_predictor_rhs', 'gm_mac_corrector', 'gm_mac_forces', 'gm_mac_divergence')
 NOALLOC_MAX_CELLS = 1048576
 
 
@@ -83,6 +84,10 @@ def _load():
         'gm_get_schur_rows': ([P, I32, C.POINTER(I64), P], C.c_int),
         'gm_get_surface_points': ([P, P], C.c_int),
         'gm_pressure_reconstruction': ([P, P, I32, C.POINTER(I64), P, P, P], C.c_int),
+        'gm_mac_predictor_rhs': ([P, P, P, P, P, P, P, P, I32, I32, D, D, D, D, D, I32, I32, P], C.c_int),
+        'gm_mac_corrector': ([P, P, P, P, P, P, P, I32, I32, D, D, D, D, I32, P], C.c_int),
+        'gm_mac_forces': ([P, P, P, P, I32, I32, D, D, D, P, P], C.c_int),
+        'gm_mac_divergence': ([P, P, P, I32, I32, D, D, P, P, P], C.c_int),
         'gm_set_state': ([P, P, P, P], C.c_int),
         'gm_get_state': ([P, P, P, P], C.c_int),
         'gm_set_inlet': ([P, P], C.c_int),

@@ -282,6 +282,34 @@ int32_t gm_pressure_recorded(const gm_handle* h);
 int gm_divergence_stats_noalloc(const double* u, const double* v, const uint8_t* mask, int32_t nx, int32_t ny,
                                 double dx, double dy, double out[3], int64_t counts[2], void* cuda_stream);
 
+/* --- the legacy staircase path's native kernels (module mac_engine) ------------- */
+/* Arrays are C-order float64 (mask: one byte per pressure cell, nonzero = solid), u ny x (nx+1),
+ * v (ny+1) x nx, p / phi / rhs ny x nx, inlet ny; each may be host memory (staged through a
+ * per-thread device buffer) or device memory of the current device.  stream: a cudaStream_t or
+ * NULL; every call returns with its outputs written.  Invalid sizes and parameters give
+ * GM_EVALUE with the reference's message (gm_last_error(NULL)). */
+/* u*, v* and the Poisson right-hand side rho/dt div u* (predictor_rhs_cpp,
+ * solver/src/bindings.cpp:47-216): upwind (centered = 0) or centred convection, staircase wall
+ * reflections, slip or no-slip channel walls.  Bit-identical to the reference's compiled loops. */
+int gm_mac_predictor_rhs(const double* u, const double* v, double* u_star, double* v_star, double* rhs,
+                         const double* p, const uint8_t* mask, const double* inlet, int32_t nx, int32_t ny, double dx,
+                         double dy, double dt, double nu, double rho, int32_t slip_walls, int32_t centered,
+                         void* stream);
+/* u = u* - dt/rho grad phi with the exact Dirichlet outlet (corrector_cpp,
+ * solver/src/bindings.cpp:218-282).  Bit-identical to the reference. */
+int gm_mac_corrector(double* u, double* v, const double* u_star, const double* v_star, const double* phi,
+                     const uint8_t* mask, const double* inlet, int32_t nx, int32_t ny, double dx, double dy, double dt,
+                     double rho, int32_t slip_walls, void* stream);
+/* Staircase pressure and shear forces out = (fx_p, fy_p, fx_v, fy_v) (calculate_mac_forces_cpp,
+ * solver/src/bindings.cpp:284-341); the sums are reduced in a fixed order. */
+int gm_mac_forces(const double* u, const double* v, const double* p, const uint8_t* mask, int32_t nx, int32_t ny,
+                  double dx, double dy, double mu, double out[4], void* stream);
+/* Fluid-cell divergence statistics without a handle (calculate_mac_divergence_cpp,
+ * solver/src/bindings.cpp:343-390): out = (max |div|, sum div^2, core sum div^2),
+ * counts = (fluid cells, core cells). */
+int gm_mac_divergence(const double* u, const double* v, const uint8_t* mask, int32_t nx, int32_t ny, double dx,
+                      double dy, double out[3], int64_t counts[2], void* stream);
+
 /* --- page-locked host memory (no reference counterpart) ------------------------ */
 
 /* Page-locked host allocation (cudaMallocHost) for arrays that cross the bus every step, such

@@ -128,7 +128,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', type=Path, required=True, help='path of the reference checkout')
     ap.add_argument('--skip-large', action='store_true')
-    ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner'),
+    ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner', 'legacy'),
                     help='generate one group of fixtures only')
     args = ap.parse_args()
     work = Path(tempfile.mkdtemp(prefix='ghost_golden_'))
@@ -140,11 +140,14 @@ def main():
             run_analysis(work)
         elif args.only == 'runner':
             run_runner(work)
+        elif args.only == 'legacy':
+            run_legacy(work)
         else:
             run_all(args)
             run_taylor_green(work)
             run_analysis(work)
             run_runner(work)
+            run_legacy(work)
     finally:
         shutil.rmtree(work, ignore_errors=True)
 
@@ -209,6 +212,44 @@ def run_runner(work):
          centerline_meta=(out / 'centerline.json').read_text(), centerline=centre,
          rec_points=pts, rec_indptr=rec.indptr.astype(np.int64), rec_indices=rec.indices.astype(np.int64),
          rec_data=rec.data.copy(), recirc_x=x, recirc_lengths=np.array(recirc), recirc_status=np.array(status))
+
+
+def run_legacy(work):
+    """The reference's native kernels of the legacy staircase path (solver/src/bindings.cpp,
+    module mac_engine built from source) on seeded fields with a staircase cylinder mask."""
+    import mac_engine
+    out = {}
+    for tag, (nx, ny) in {'a': (64, 40), 'b': (37, 23)}.items():
+        rng = np.random.default_rng(21 if tag == 'a' else 22)
+        dx, dy = 0.11, 0.13
+        xc, yc, r = nx * dx * 0.35, ny * dy * 0.5, 0.9
+        xx, yy = np.meshgrid((np.arange(nx) + .5) * dx, (np.arange(ny) + .5) * dy)
+        mask = np.ascontiguousarray((xx - xc) ** 2 + (yy - yc) ** 2 <= r * r)
+        u = rng.standard_normal((ny, nx + 1))
+        v = rng.standard_normal((ny + 1, nx))
+        p = rng.standard_normal((ny, nx))
+        phi = rng.standard_normal((ny, nx))
+        inlet = 1.0 + 0.1 * rng.standard_normal(ny)
+        dt, nu, rho = 0.003, 0.02, 1.3
+        out[f'{tag}_in'] = np.array([nx, ny, dx, dy, dt, nu, rho])
+        for name, a in (('u', u), ('v', v), ('p', p), ('phi', phi), ('inlet', inlet), ('mask', mask)):
+            out[f'{tag}_{name}'] = a
+        for slip in (0, 1):
+            for centered in (0, 1):
+                us, vs, rhs = np.zeros_like(u), np.zeros_like(v), np.zeros_like(p)
+                mac_engine.predictor_rhs_cpp(u, v, us, vs, rhs, p, mask, inlet, dx, dy, dt, nu, rho, bool(slip),
+                                             bool(centered))
+                key = f'{tag}_pred_s{slip}c{centered}'
+                out[key + '_us'], out[key + '_vs'], out[key + '_rhs'] = us, vs, rhs
+        us, vs = rng.standard_normal(u.shape), rng.standard_normal(v.shape)
+        uc, vc = u.copy(), v.copy()
+        mac_engine.corrector_cpp(uc, vc, us, vs, phi, mask, inlet, dx, dy, dt, rho, False)
+        out[f'{tag}_corr_us'], out[f'{tag}_corr_vs'] = us, vs
+        out[f'{tag}_corr_u'], out[f'{tag}_corr_v'] = uc, vc
+        out[f'{tag}_forces'] = np.array(mac_engine.calculate_mac_forces_cpp(u, v, p, mask, dx, dy, nu * rho))
+        d = mac_engine.calculate_mac_divergence_cpp(u, v, mask, dx, dy)
+        out[f'{tag}_div'] = np.array([d[0], d[1], d[2], d[3], d[4]], dtype=float)
+    save('legacy_kernels', **out)
 
 
 def run_analysis(work):
