@@ -42,11 +42,13 @@ GlobalError g_create_error;
 struct CudaError : std::exception {
   std::string msg;
   explicit CudaError(std::string m) : msg(std::move(m)) {}
+  const char* what() const noexcept override { return msg.c_str(); }
 };
 struct GateError : std::exception {
   int cls;
   std::string msg;
   GateError(int c, std::string m) : cls(c), msg(std::move(m)) {}
+  const char* what() const noexcept override { return msg.c_str(); }
 };
 
 #define CK(call)                                                                                    \
