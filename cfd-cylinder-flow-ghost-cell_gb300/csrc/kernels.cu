@@ -1010,8 +1010,8 @@ __device__ __forceinline__ T adv_v(const S* __restrict__ U, const Grid& g, int j
 }
 
 // raw_l (5-point with channel-wall, inlet and outlet rules) at a u face (solver/optimized_ghost_cell.py:116-120)
-template <typename T, typename S>
-__device__ __forceinline__ T lap_u(const S* __restrict__ U, const Grid& g, int j, int i, T idx2, T idy2,
+template <typename T, typename S, typename GR = Grid>
+__device__ __forceinline__ T lap_u(const S* __restrict__ U, const GR& g, int j, int i, T idx2, T idy2,
                                    bool inlet) {
   const int nx = g.nx, ny = g.ny;
   T acc = 0;
@@ -1023,8 +1023,8 @@ __device__ __forceinline__ T lap_u(const S* __restrict__ U, const Grid& g, int j
   return acc;
 }
 // at a v face (solver/optimized_ghost_cell.py:121-123); walls v=0 are stored as zeros
-template <typename T, typename S>
-__device__ __forceinline__ T lap_v(const S* __restrict__ U, const Grid& g, int j, int i, T idx2, T idy2) {
+template <typename T, typename S, typename GR = Grid>
+__device__ __forceinline__ T lap_v(const S* __restrict__ U, const GR& g, int j, int i, T idx2, T idy2) {
   const int nx = g.nx;
   T acc = idy2 * (T)U[g.v(j - 1, i)];
   if (i > 0) acc += idx2 * (T)U[g.v(j, i - 1)];
@@ -1034,13 +1034,13 @@ __device__ __forceinline__ T lap_v(const S* __restrict__ U, const Grid& g, int j
   return acc;
 }
 // G p at faces from a pressure grid with ghost values (solver/optimized_ghost_cell.py:94-107)
-template <typename T, typename S>
-__device__ __forceinline__ T grad_u(const S* __restrict__ P, const Grid& g, int j, int i, T gx) {
+template <typename T, typename S, typename GR = Grid>
+__device__ __forceinline__ T grad_u(const S* __restrict__ P, const GR& g, int j, int i, T gx) {
   if (i < g.nx) return gx * (T)P[g.p(j, i)] - gx * (T)P[g.p(j, i - 1)];
   return ((T)-2 * gx) * (T)P[g.p(j, g.nx - 1)];
 }
-template <typename T, typename S>
-__device__ __forceinline__ T grad_v(const S* __restrict__ P, const Grid& g, int j, int i, T gy) {
+template <typename T, typename S, typename GR = Grid>
+__device__ __forceinline__ T grad_v(const S* __restrict__ P, const GR& g, int j, int i, T gy) {
   return gy * (T)P[g.p(j, i)] - gy * (T)P[g.p(j - 1, i)];
 }
 
@@ -1119,6 +1119,162 @@ __global__ void k_momentum(CaseDev c, MomentumArgs a, const S* __restrict__ Us, 
     a.out[t] = q + cvt_to<double>(dt * (expl + (T)0.5 * lq - gp) + ((T)0.5 * dt) * off);
 }
 
+// ---------------------------------------------------------------------------
+// The AB2 momentum right-hand side (mode 0 of k_momentum) from a shared-memory tile.
+//
+// A block owns a TJ x TI patch of "points" (j, i), j in [0, ny], i in [0, nx]: point (j, i) is
+// the u face (j, i) when j < ny and the v face (j, i) when i < nx.  It loads the u, v and p
+// values its faces read (one halo row / column) once, with coalesced row loads, and forms each
+// shared flux once instead of once per face that uses it:
+//   corner products C = ua vf at the cell corners (jj, ii), 1 <= jj <= ny-1, 1 <= ii <= nx, where
+//     ua = (u(jj-1, ii) + u(jj, ii)) / 2 and vf = (v(jj, ii-1) + v(jj, ii)) / 2 (v(jj, nx-1) at the
+//     outlet); the u faces use -(C dx) (their fxy corner flux), the v faces -(C dy) (fyx): four
+//     faces share each corner;
+//   centre fluxes Xu = -((u(j, ii-1) + u(j, ii))^2 / 4 dy) of the u cells and
+//     Yv = -((v(jj-1, i) + v(jj, i))^2 / 4 dx) of the v cells, two faces each
+// (solver/numba_kernels.py:17-142: the same flux formulas as adv_u / adv_v).  The diffusion and
+// pressure-gradient stencils read the tile through the same lap / grad functions as k_momentum.
+// ---------------------------------------------------------------------------
+static constexpr int MTI = 32, MTJ = 8;  // points per tile: 32 along x (one warp), 8 rows
+// offsets of global (j, i) in the shared tiles: u and v tiles of (MTJ+2) x (MTI+2) (rows j0-1 ..
+// j0+MTJ, columns i0-1 .. i0+MTI), the u tile first; the p tile (MTJ+1) x (MTI+1)
+struct TileGrid {
+  int nx, ny, j0, i0;
+  static constexpr int W = MTI + 2, H = MTJ + 2, WP = MTI + 1;
+  __device__ __forceinline__ int u(int j, int i) const { return (j - j0 + 1) * W + (i - i0 + 1); }
+  __device__ __forceinline__ int v(int j, int i) const { return H * W + (j - j0 + 1) * W + (i - i0 + 1); }
+  __device__ __forceinline__ int p(int j, int i) const { return (j - j0 + 1) * WP + (i - i0 + 1); }
+};
+
+template <typename T, typename S>
+__global__ void __launch_bounds__(MTI * MTJ) k_momentum_tiled(CaseDev c, MomentumArgs a, const S* __restrict__ Us,
+                                                              const S* __restrict__ Ps, Gate gate) {
+  constexpr int W = TileGrid::W, H = TileGrid::H, WP = TileGrid::WP;
+  __shared__ S suv[2 * H * W];
+  __shared__ S sp[(MTJ + 1) * WP];
+  __shared__ T fx[(MTJ + 1) * (MTI + 1)];  // -(C dx) at corner (j0 + r, i0 + q)
+  __shared__ T fy[(MTJ + 1) * (MTI + 1)];  // -(C dy)
+  __shared__ T xu[MTJ * (MTI + 1)];        // Xu at (j0 + r, i0 + q)
+  __shared__ T yv[(MTJ + 1) * MTI];        // Yv at (j0 + r, i0 + q)
+  if (!gate_open(gate)) return;
+  const int nx = c.nx, ny = c.ny;
+  const int j0 = blockIdx.y * MTJ, i0 = blockIdx.x * MTI;
+  const int tid = threadIdx.y * MTI + threadIdx.x;
+  const Grid g{nx, ny, c.usize};
+  const TileGrid tg{nx, ny, j0, i0};
+  // 1. the tiles (zero outside the grids; no stencil below reads those entries)
+  for (int e = tid; e < H * W; e += MTI * MTJ) {
+    const int r = e / W, q = e - r * W;
+    const int j = j0 - 1 + r, i = i0 - 1 + q;
+    suv[e] = (j >= 0 && j < ny && i >= 0 && i <= nx) ? Us[g.u(j, i)] : (S)0;
+    suv[H * W + e] = (j >= 0 && j <= ny && i >= 0 && i < nx) ? Us[g.v(j, i)] : (S)0;
+  }
+  for (int e = tid; e < (MTJ + 1) * WP; e += MTI * MTJ) {
+    const int r = e / WP, q = e - r * WP;
+    const int j = j0 - 1 + r, i = i0 - 1 + q;
+    sp[e] = (j >= 0 && j < ny && i >= 0 && i < nx) ? Ps[g.p(j, i)] : (S)0;
+  }
+  __syncthreads();
+  constexpr bool F32 = sizeof(T) == 4;
+  const T dx = F32 ? (T)c.fdx : (T)c.dx, dy = F32 ? (T)c.fdy : (T)c.dy;
+  const T hh = (T)0.5;
+  auto U = [&](int j, int i) -> T { return (T)suv[tg.u(j, i)]; };
+  auto V = [&](int j, int i) -> T { return (T)suv[tg.v(j, i)]; };
+  // 2. the shared fluxes
+  for (int e = tid; e < (MTJ + 1) * (MTI + 1); e += MTI * MTJ) {
+    const int r = e / (MTI + 1), q = e - r * (MTI + 1);
+    const int jj = j0 + r, ii = i0 + q;
+    T cx = (T)0, cy = (T)0;
+    if (jj >= 1 && jj <= ny - 1 && ii >= 1 && ii <= nx) {
+      const T vf = ii == nx ? V(jj, nx - 1) : hh * (V(jj, ii - 1) + V(jj, ii));
+      const T ua = hh * (U(jj - 1, ii) + U(jj, ii));
+      const T cc = vf * ua;
+      cx = -(cc * dx);
+      cy = -(cc * dy);
+    }
+    fx[e] = cx;
+    fy[e] = cy;
+  }
+  for (int e = tid; e < MTJ * (MTI + 1); e += MTI * MTJ) {
+    const int r = e / (MTI + 1), q = e - r * (MTI + 1);
+    const int j = j0 + r, ii = i0 + q;
+    T x = (T)0;
+    if (j < ny && ii >= 1 && ii <= nx) {
+      const T fl = hh * (U(j, ii - 1) + U(j, ii));
+      x = -((fl * fl) * dy);
+    }
+    xu[e] = x;
+  }
+  for (int e = tid; e < (MTJ + 1) * MTI; e += MTI * MTJ) {
+    const int r = e / MTI, q = e - r * MTI;
+    const int jj = j0 + r, i = i0 + q;
+    T y = (T)0;
+    if (jj >= 1 && jj <= ny && i < nx) {
+      const T fb = hh * (V(jj - 1, i) + V(jj, i));
+      y = -((fb * fb) * dx);
+    }
+    yv[e] = y;
+  }
+  __syncthreads();
+  const int r = threadIdx.y, q = threadIdx.x;
+  const int j = j0 + r, i = i0 + q;
+  const T idx2 = F32 ? (T)c.fidx2 : (T)c.idx2, idy2 = F32 ? (T)c.fidy2 : (T)c.idy2;
+  const T iarea = F32 ? (T)c.fiarea : (T)c.iarea, nu = F32 ? (T)c.fnu : (T)c.nu;
+  const T dt = F32 ? (T)a.dt32 : (T)a.dt;
+  const T alpha = F32 ? (T)a.alpha32 : (T)a.alpha;
+  auto FX = [&](int jj, int ii) -> T { return fx[(jj - j0) * (MTI + 1) + (ii - i0)]; };
+  auto FY = [&](int jj, int ii) -> T { return fy[(jj - j0) * (MTI + 1) + (ii - i0)]; };
+  auto XU = [&](int jj, int ii) -> T { return xu[(jj - j0) * (MTI + 1) + (ii - i0)]; };
+  auto YV = [&](int jj, int ii) -> T { return yv[(jj - j0) * MTI + (ii - i0)]; };
+  // 3. the faces of this point
+  for (int comp = 0; comp < 2; ++comp) {
+    if (comp == 0 ? (j >= ny || i > nx) : (j > ny || i >= nx)) continue;
+    const int64_t t = comp == 0 ? g.u(j, i) : g.v(j, i);
+    const uint8_t cls = comp == 0 ? c.cls_u[t] : c.cls_v[t - c.usize];
+    if (!(cls & CLS_ACTIVE)) {
+      a.now[t] = 0.0;
+      a.out[t] = 0.0;
+      continue;
+    }
+    const double qv = a.U[t];
+    T lq, gp, now, off = 0;
+    if (comp == 0) {
+      lq = nu * lap_u<T>(suv, tg, j, i, idx2, idy2, true);
+      gp = grad_u<T>(sp, tg, j, i, F32 ? (T)c.fgx : (T)c.gx);
+      T adv;
+      if (i < nx) {
+        adv = (XU(j, i + 1) - XU(j, i)) + (FX(j + 1, i) - FX(j, i));
+      } else {
+        const T uC = U(j, i);
+        adv = (-uC * uC) * dy - XU(j, nx) + hh * (FX(j + 1, nx) - FX(j, nx));
+      }
+      now = adv * iarea;
+      if (i == nx) now *= (T)2;
+      if (i == 1) off = nu * (idx2 * (T)c.inlet[j]);
+    } else {
+      lq = nu * lap_v<T>(suv, tg, j, i, idx2, idy2);
+      gp = grad_v<T>(sp, tg, j, i, F32 ? (T)c.fgy : (T)c.gy);
+      now = ((FY(j, i + 1) - FY(j, i)) + (YV(j + 1, i) - YV(j, i))) * iarea;
+    }
+    const T expl = ((T)1 + alpha) * now - alpha * cvt_to<T>(a.prev[t]);
+    a.now[t] = cvt_to<double>(now);
+    if constexpr (sizeof(T) == 8)
+      a.out[t] = (qv + (double)(dt * (expl + (T)0.5 * lq - gp))) + (double)(((T)0.5 * dt) * off);
+    else
+      a.out[t] = qv + cvt_to<double>(dt * (expl + (T)0.5 * lq - gp) + ((T)0.5 * dt) * off);
+  }
+}
+
+// whether the AB2 right-hand side runs from shared-memory tiles (GHOSTMAC_MOMENTUM_TILED=0: the
+// one-thread-per-face kernel; read at every launch, which graph replays do not repeat)
+static bool momentum_tiled() {
+  const char* e = std::getenv("GHOSTMAC_MOMENTUM_TILED");
+  return !(e && e[0] == '0');
+}
+static dim3 momentum_tiles(const CaseDev& c) {
+  return dim3((unsigned)((c.nx + 1 + MTI - 1) / MTI), (unsigned)((c.ny + 1 + MTJ - 1) / MTJ));
+}
+
 __global__ void k_shadow(const double* __restrict__ U, float* __restrict__ U32, int64_t nf,
                          const double* __restrict__ P, float* __restrict__ P32, int64_t np, Gate gate) {
   if (!gate_open(gate)) return;
@@ -1138,8 +1294,12 @@ void launch_shadow(const double* U, float* U32, int64_t n_f, const double* P, fl
 void launch_momentum(const CaseDev& c, const MomentumArgs& a, const Gate& gate, cudaStream_t st) {
   note_launch();
   kt_mark(3, st);
-  k_momentum<double, double><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, a.U, a.P, gate);
-  kt_mark(3, st);
+  if (a.mode == 0 && momentum_tiled())
+    k_momentum_tiled<double, double><<<momentum_tiles(c), dim3(MTI, MTJ), 0, st>>>(c, a, a.U, a.P, gate);
+  else
+    k_momentum<double, double><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, a.U, a.P, gate);
+  // algorithmic bytes: U, prev, class map read; now, out written; P read
+  kt_mark(3, st, (double)(c.usize + c.vsize) * (8 * 4 + 1) + (double)c.psize * 8);
 }
 void launch_momentum_f32(const CaseDev& c, const MomentumArgs& a_in, const Gate& gate, cudaStream_t st) {
   MomentumArgs a = a_in;
@@ -1147,7 +1307,9 @@ void launch_momentum_f32(const CaseDev& c, const MomentumArgs& a_in, const Gate&
   a.alpha32 = (float)a.alpha;
   note_launch();
   kt_mark(3, st);
-  if (a.mode == 0 && a.U32 && a.P32)
+  if (a.mode == 0 && a.U32 && a.P32 && momentum_tiled())
+    k_momentum_tiled<float, float><<<momentum_tiles(c), dim3(MTI, MTJ), 0, st>>>(c, a, a.U32, a.P32, gate);
+  else if (a.mode == 0 && a.U32 && a.P32)
     k_momentum<float, float><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, a.U32, a.P32, gate);
   else
     k_momentum<float, double><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, a.U, a.P, gate);
