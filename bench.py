@@ -74,7 +74,7 @@ DEFAULT_WORKLOAD = 'wide_800x820_re100'
 # FP64 instructions (dadd + dmul + dfma, thread level) per cell update of the plain FP64 step on
 # the 800x820 case, and the measured FP64 instruction rate of a GB300 (independent FMA chains on
 # every SM, profiles/gb300_rates.md); the count comes from the ncu capture in FP64_OPS_SOURCE.
-FP64_OPS_PER_CELL_UPDATE = 0.0
+FP64_OPS_PER_CELL_UPDATE = 424.4
 FP64_OPS_SOURCE = 'profiles/fp64_instructions_wide_800x820.md'
 FP64_INST_RATE = 499e9
 # DRAM bytes (read + write) per launch of the dominant kernel class, averaged over the launches

@@ -688,13 +688,16 @@ void transform_matrices(gm_handle* h, const RectDev& rd, std::vector<double>& ti
   CK(cudaStreamSynchronize(st));
 }
 
-// FP32 mode: the pressure inverse's two row passes as split-TF32 GEMMs against these matrices on
-// the tensor cores (rowgemm.cu), where the grid allows it (cols a multiple of 4, at most 1024;
-// the row pitch of the pressure grid is cols).  GHOSTMAC_ROW_GEMM=0 keeps the FFT passes.
+// FP32 mode, opt-in (GHOSTMAC_ROW_GEMM=1): the pressure inverse's two row passes as split-TF32
+// GEMMs against these matrices on the tensor cores (rowgemm.cu), where the grid allows it (cols
+// a multiple of 4, at most 1024; the row pitch of the pressure grid is cols).  Measured on the
+// 800x820 case it is the slower choice: 38 us per pass against 15 us for the FFT pass, and the
+// tensor cores' FP32 accumulation over 800 products leaves the inverse less accurate than the
+// FP32 FFT, so the refinement needs 4.0 instead of 2.65 pressure sweeps per step.
 void build_row_gemm(gm_handle* h, RectDev& rd) {
   row_gemm_free(rd.gemm);
   const char* e = std::getenv("GHOSTMAC_ROW_GEMM");
-  if (e && e[0] == '0') return;
+  if (!(e && e[0] == '1')) return;
   if (h->precision != 1 || rd.view.base != 0 || rd.view.pitch != rd.view.cols) return;
   if (rd.rank > 0 && !rd.wcorr32.p) return;
   if (rd.view.cols % 4 || rd.view.cols > 1024 || row_gemm_smem_bytes() > h->smem_optin) return;

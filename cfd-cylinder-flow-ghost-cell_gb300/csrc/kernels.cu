@@ -1795,12 +1795,27 @@ __global__ void __launch_bounds__(TPB) k_helm_jacobi_tiled(CaseDev c, ResidualCo
   }
 }
 
+// The kernels' dynamic shared-memory limit is a per-function, process-wide attribute shared by
+// every case: it is raised to the device's opt-in maximum (never set to one case's size, which
+// would make the launches of a larger case in the same process fail).
 int helm_jacobi_tiled_optin(size_t smem) {
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  if (smem > (size_t)optin) return 1;
   const void* ks[4] = {(const void*)k_helm_jacobi_tiled<1, double>, (const void*)k_helm_jacobi_tiled<2, double>,
                        (const void*)k_helm_jacobi_tiled<1, float>, (const void*)k_helm_jacobi_tiled<2, float>};
   int e = 0;
-  for (const void* k : ks)
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) e = 1;
+  for (const void* k : ks) {
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, k) != cudaSuccess) { e = 1; continue; }
+    const int dyn = optin - (int)a.sharedSizeBytes;
+    if (smem > (size_t)dyn || cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
+      e = 1;
+  }
   if (e) cudaGetLastError();
   return e;
 }

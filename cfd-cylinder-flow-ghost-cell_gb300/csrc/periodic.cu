@@ -544,10 +544,16 @@ int gm_tg_create(int32_t n, double nu, int32_t precision, gm_tg** out) {
     int optin = 0;
     TG_CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0));
     if (t->smem > (size_t)optin) throw TgError(GM_EVALUE, "grid too large for the row transforms");
-    for (auto f : {(const void*)k_tg_rows<double, 0>, (const void*)k_tg_rows<double, 1>, (const void*)k_tg_rows<double, 2>})
-      TG_CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t->smem));
-    for (auto f : {(const void*)k_tg_rows<float, 0>, (const void*)k_tg_rows<float, 1>, (const void*)k_tg_rows<float, 2>})
-      TG_CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t->smem32));
+    // the limit is a process-wide attribute of the kernel shared by every handle: the device
+    // maximum, so that a smaller handle created later cannot lower it below a larger one's need
+    for (auto f : {(const void*)k_tg_rows<double, 0>, (const void*)k_tg_rows<double, 1>, (const void*)k_tg_rows<double, 2>,
+                   (const void*)k_tg_rows<float, 0>, (const void*)k_tg_rows<float, 1>, (const void*)k_tg_rows<float, 2>}) {
+      cudaFuncAttributes fa;
+      TG_CK(cudaFuncGetAttributes(&fa, f));
+      const int dyn = optin - (int)fa.sharedSizeBytes;
+      if (t->smem > (size_t)dyn) throw TgError(GM_EVALUE, "grid too large for the row transforms");
+      TG_CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+    }
     t->threads = std::min(512, std::max(64, ((n / 4 + 31) / 32) * 32));
     const int64_t nn = (int64_t)n * n;
     for (Buf<double>* b : {&t->q, &t->qn, &t->hist, &t->now, &t->rhs, &t->star, &t->mid, &t->half_q, &t->action,
