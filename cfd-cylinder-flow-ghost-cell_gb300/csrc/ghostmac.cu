@@ -134,6 +134,12 @@ struct RectDev {
   // solve writes in place, the psi rows)
   RowGemm gemm;
   DBuf<float> wcorr32;
+  // G = M binv folded over the spectrum rows cj0..cj1 (rank x glen, glen = (cj1 - cj0 + 1) cols;
+  // 0: not built, the first / GEMV chain runs), in the mode's precision, and the slice sums
+  int glen = 0;
+  DBuf<double> gmat;
+  DBuf<float> gmat32;
+  DBuf<double> cpart;
 };
 
 }  // namespace
@@ -764,6 +770,28 @@ void build_direct_tables(gm_handle* h, RectDev& rd, const std::vector<int64_t>& 
     rd.bfwd32.upload(to_f32(bfwd), st);
     rd.firstm32.alloc(m);
   }
+  // G = M binv over the spectrum rows cj0..cj1: one sum per Schur value per solve instead of the
+  // point values and a GEMV (GHOSTMAC_BAND_GEMV=1 keeps those; tables over 64 MB too)
+  rd.glen = 0;
+  const char* eg = std::getenv("GHOSTMAC_BAND_GEMV");
+  const int L = (tt.cj1 - tt.cj0 + 1) * n;
+  if (!(eg && eg[0] == '1') && tt.cj1 >= tt.cj0 && (size_t)rank * L * 8 <= ((size_t)64 << 20)) {
+    std::vector<double> G((size_t)rank * L, 0.0);
+    for (int r = 0; r < rank; ++r) {
+      double* gr = &G[(size_t)r * L];
+      for (int q = 0; q < m; ++q) {
+        const double a = mband[(size_t)r * m + q];
+        if (a == 0.0) continue;
+        double* dst = gr + (size_t)(mrow[q] - tt.cj0) * n;
+        const double* src = &binv[(size_t)q * n];
+        for (int k = 0; k < n; ++k) dst[k] += a * src[k];
+      }
+    }
+    if (h->precision == 1) rd.gmat32.upload(to_f32(G), st);
+    else rd.gmat.upload(G, st);
+    rd.cpart.alloc((size_t)rank * BAND_SPLIT);
+    rd.glen = L;
+  }
   CK(cudaStreamSynchronize(st));
   rd.direct = true;
 }
@@ -1030,14 +1058,25 @@ void schur_inverse(gm_handle* h, RectDev& rd, const TransformTables& tt, const v
   YCorr<T> corr = none;
   if (rd.rank > 0 && rd.direct) {
     const bool f32 = sizeof(T) == 4;
-    T* fm = f32 ? (T*)rd.firstm32.p : (T*)rd.firstm.p;
-    launch_band_first<T>(rd.mcount, v.cols, rd.mrow.p, f32 ? (const T*)rd.binv32.p : (const T*)rd.binv.p, spectral, fm,
-                         g, st);
-    sweep_mark(h, 3, st);
-    launch_band_gemv<T>(rd.rank, rd.mcount, rd.mband.p, fm, rd.cvec.p, g, st);
-    sweep_mark(h, 4, st);
-    launch_band_fwd_solve<T>(tt, v.cols, rd.rank, rd.bptr.p, rd.cvec.p,
-                             f32 ? (const T*)rd.bfwd32.p : (const T*)rd.bfwd.p, band, g, st);
+    const double* cv = rd.cvec.p;
+    int nsplit = 1;
+    if (rd.glen > 0) {
+      launch_band_direct<T>(rd.rank, rd.glen, f32 ? (const T*)rd.gmat32.p : (const T*)rd.gmat.p,
+                            spectral + (int64_t)tt.cj0 * v.cols, rd.cpart.p, g, st);
+      sweep_mark(h, 3, st);
+      sweep_mark(h, 4, st);
+      cv = rd.cpart.p;
+      nsplit = BAND_SPLIT;
+    } else {
+      T* fm = f32 ? (T*)rd.firstm32.p : (T*)rd.firstm.p;
+      launch_band_first<T>(rd.mcount, v.cols, rd.mrow.p, f32 ? (const T*)rd.binv32.p : (const T*)rd.binv.p, spectral,
+                           fm, g, st);
+      sweep_mark(h, 3, st);
+      launch_band_gemv<T>(rd.rank, rd.mcount, rd.mband.p, fm, rd.cvec.p, g, st);
+      sweep_mark(h, 4, st);
+    }
+    launch_band_fwd_solve<T>(tt, v.cols, rd.rank, rd.bptr.p, cv, f32 ? (const T*)rd.bfwd32.p : (const T*)rd.bfwd.p,
+                             band, g, st, nsplit);
     sweep_mark(h, 5, st);
     corr = YCorr<T>{band, (const T*)tt.phi, (const T*)tt.psi, tt.bj0, tt.bj1};
   } else if (rd.rank > 0) {
@@ -2684,6 +2723,8 @@ void apply_inverse_group(gm_batch* b, const BatchGroup& G, int lane, const std::
   auto bf = std::make_unique<ArgPack<BandFirstArgs<T>>>();
   auto bg = std::make_unique<ArgPack<BandGemvArgs<T>>>();
   auto bw = std::make_unique<ArgPack<BandFwdArgs<T>>>();
+  auto bd = std::make_unique<ArgPack<BandDirectArgs<T>>>();
+  bool direct_g = true;
   auto fin = std::make_unique<ArgPack<XpassArgs<T, T, double>>>();
   const TransformTables* tt0 = nullptr;
   for (int c = 0; c < n; ++c) {
@@ -2707,18 +2748,30 @@ void apply_inverse_group(gm_batch* b, const BatchGroup& G, int lane, const std::
     bf->a[c] = BandFirstArgs<T>{rd.mcount, v.cols, rd.mrow.p, f32 ? (const T*)rd.binv32.p : (const T*)rd.binv.p, spec,
                                 fm, g};
     bg->a[c] = BandGemvArgs<T>{rd.rank, rd.mcount, rd.mband.p, fm, rd.cvec.p, g};
+    bd->a[c] = BandDirectArgs<T>{rd.rank, rd.glen, f32 ? (const T*)rd.gmat32.p : (const T*)rd.gmat.p,
+                                 spec + (int64_t)tt.cj0 * v.cols, rd.cpart.p, g};
+    direct_g = direct_g && rd.glen > 0;
     T* band = f32 ? (T*)rd.band32.p : (T*)rd.band.p;
     bw->a[c] = BandFwdArgs<T>{tt.bj1 - tt.bj0 + 1, v.cols, rd.rank, rd.bptr.p, rd.cvec.p,
                               f32 ? (const T*)rd.bfwd32.p : (const T*)rd.bfwd.p, (T)tt.gamma, (T)tt.yscale,
-                              (const T*)tt.bpiv, band, g, band_fwd_blocks(v.cols)};
+                              (const T*)tt.bpiv, band, g, band_fwd_blocks(v.cols), 1};
     const YCorr<T> corr{band, (const T*)tt.phi, (const T*)tt.psi, tt.bj0, tt.bj1};
     fin->a[c] = xpass_args<T, T, double>(tt, true, 0, v.rows, spec, 0, v.cols, nullptr, call.x, v.base, v.pitch, v.cls,
                                          body ? call.x : nullptr, corr, g);
   }
   launch_xpass_multi<T, TI, T>(*fwd, n, *tt0, st);
   launch_ysolve_multi<T>(*ys, n, *tt0, st);
-  launch_band_first_multi<T>(*bf, n, st);
-  launch_band_gemv_multi<T>(*bg, n, st);
+  if (direct_g) {
+    // the same direct sums as the cases stepped alone
+    for (int c = 0; c < n; ++c) {
+      bw->a[c].c = bd->a[c].part;
+      bw->a[c].nsplit = BAND_SPLIT;
+    }
+    launch_band_direct_multi<T>(*bd, n, st);
+  } else {
+    launch_band_first_multi<T>(*bf, n, st);
+    launch_band_gemv_multi<T>(*bg, n, st);
+  }
   launch_band_fwd_solve_multi<T>(*bw, n, st);
   launch_xpass_multi<T, T, double>(*fin, n, *tt0, st);
 }

@@ -796,6 +796,28 @@ __global__ void __launch_bounds__(BAND_TPB) k_band_gemv(int rank, int m, const d
   band_gemv_body<T>(m, M, firstm, c, blockIdx.x);
 }
 
+// The boundary term's Schur values in one sum per value: c[r] = G[r] . S[cj0 .. cj1 rows], with
+// G = M binv folded on the host (G[r][(j - cj0) n + k] = sum over the points q of spectrum row j
+// of M[r][q] binv[q][k]), so that the point values "first" are never formed.  Block (r, s) sums
+// slice s of BAND_SPLIT slices (per-thread partials in T, the block's sum in FP64) and writes
+// part[r BAND_SPLIT + s]; the band solve adds the slices in a fixed order.
+template <typename T>
+__device__ __forceinline__ void band_direct_body(int L, const T* __restrict__ G, const T* __restrict__ S,
+                                                 double* __restrict__ part, int r, int sl) {
+  __shared__ double dpart[BAND_TPB / 32];
+  const int len = (L + BAND_SPLIT - 1) / BAND_SPLIT;
+  const int i0 = sl * len, i1 = min(L, i0 + len);
+  const T v = i1 > i0 ? band_partial<T, T, T>(G + (int64_t)r * L + i0, S + i0, i1 - i0, threadIdx.x) : (T)0;
+  const double tot = band_group_sum<double>(cvt_to<double>(v), dpart, threadIdx.x);
+  if (threadIdx.x == 0) part[r * BAND_SPLIT + sl] = tot;
+}
+template <typename T>
+__global__ void __launch_bounds__(BAND_TPB) k_band_direct(int L, const T* __restrict__ G, const T* __restrict__ S,
+                                                          double* __restrict__ part, Gate gate) {
+  if (!gate_open(gate)) return;
+  band_direct_body<T>(L, G, S, part, blockIdx.x / BAND_SPLIT, blockIdx.x % BAND_SPLIT);
+}
+
 // Blocks of BAND_COLS columns x BAND_ROWT row threads.  Thread (kk, jt) forms the forward
 // row transform of U c on band rows jt, jt + BAND_ROWT, ... of column k (a sum over that row's
 // boundary values, c staged in shared memory), scaled; then one thread per column runs the band
@@ -805,14 +827,20 @@ template <typename T>
 __device__ __forceinline__ void band_fwd_solve_body(int nb, int n, int rank, const int32_t* __restrict__ bptr,
                                                     const double* __restrict__ c,
                                                     const T* __restrict__ bfwd, T gamma, T scale,
-                                                    const T* __restrict__ bpiv, T* __restrict__ band, int bid) {
+                                                    const T* __restrict__ bpiv, T* __restrict__ band, int bid,
+                                                    int nsplit) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* cs = reinterpret_cast<T*>(smem_raw);   // rank values c (band-row order, as the GEMV writes them)
   T* xb = cs + ((rank + 3) & ~3);           // nb x BAND_COLS
   T* pb = xb + (size_t)nb * BAND_COLS;      // nb x BAND_COLS
   int* ps = reinterpret_cast<int*>(pb + (size_t)nb * BAND_COLS);  // nb + 1 row pointers
   const int tid = threadIdx.x, kk = tid % BAND_COLS, jt = tid / BAND_COLS;
-  for (int e = tid; e < rank; e += blockDim.x) cs[e] = cvt_to<T>(c[e]);
+  // c[e], or the sum of its nsplit slices in slice order (k_band_direct)
+  for (int e = tid; e < rank; e += blockDim.x) {
+    double v = c[(int64_t)e * nsplit];
+    for (int sl = 1; sl < nsplit; ++sl) v += c[(int64_t)e * nsplit + sl];
+    cs[e] = cvt_to<T>(v);
+  }
   for (int j = tid; j <= nb; j += blockDim.x) ps[j] = bptr[j];
   __syncthreads();
   const int k = bid * BAND_COLS + kk;
@@ -853,9 +881,9 @@ template <typename T>
 __global__ void __launch_bounds__(BAND_COLS * BAND_ROWT) k_band_fwd_solve(
     int nb, int n, int rank, const int32_t* __restrict__ bptr,
     const double* __restrict__ c, const T* __restrict__ bfwd, T gamma, T scale, const T* __restrict__ bpiv,
-    T* __restrict__ band, Gate gate) {
+    T* __restrict__ band, Gate gate, int nsplit) {
   if (!gate_open(gate)) return;
-  band_fwd_solve_body<T>(nb, n, rank, bptr, c, bfwd, gamma, scale, bpiv, band, blockIdx.x);
+  band_fwd_solve_body<T>(nb, n, rank, bptr, c, bfwd, gamma, scale, bpiv, band, blockIdx.x, nsplit);
 }
 
 int band_fwd_blocks(int n) { return (n + BAND_COLS - 1) / BAND_COLS; }
@@ -883,15 +911,24 @@ void launch_band_gemv(int rank, int m, const double* M, const T* firstm, double*
   kt_mark(5, st, (double)rank * m * 8 + (double)m * sizeof(T) + rank * 8.0);
 }
 template <typename T>
+void launch_band_direct(int rank, int L, const T* G, const T* S, double* part, const Gate& gate, cudaStream_t st) {
+  if (rank <= 0) return;
+  note_launch();
+  kt_mark(5, st);
+  launch_pdl(k_band_direct<T>, dim3((unsigned)(rank * BAND_SPLIT)), dim3(BAND_TPB), 0, st, L, G, S, part, gate);
+  // G read once, the spectrum rows once per value (L2), the slices written
+  kt_mark(5, st, (double)rank * L * sizeof(T) + (double)L * sizeof(T) + rank * BAND_SPLIT * 8.0);
+}
+template <typename T>
 void launch_band_fwd_solve(const TransformTables& tt, int n, int rank, const int32_t* bptr, const double* c,
-                           const T* bfwd, T* band, const Gate& gate, cudaStream_t st) {
+                           const T* bfwd, T* band, const Gate& gate, cudaStream_t st, int nsplit) {
   const int nb = tt.bj1 - tt.bj0 + 1;
   if (nb <= 0) return;
   note_launch();
   kt_mark(5, st);
   launch_pdl(k_band_fwd_solve<T>, dim3((unsigned)((n + BAND_COLS - 1) / BAND_COLS)), dim3(BAND_COLS * BAND_ROWT),
              band_fwd_smem(nb, rank, sizeof(T) == 4), st, nb, n, rank, bptr, c, bfwd, (T)tt.gamma,
-             (T)tt.yscale, (const T*)tt.bpiv, band, gate);
+             (T)tt.yscale, (const T*)tt.bpiv, band, gate, nsplit);
   // the forward coefficients, the values c, the pivots and the band written once
   kt_mark(5, st, (double)rank * n * sizeof(T) + rank * 8.0 + (double)nb * n * 2 * sizeof(T));
 }
@@ -902,9 +939,11 @@ template void launch_band_first<float>(int, int, const int32_t*, const float*, c
 template void launch_band_gemv<double>(int, int, const double*, const double*, double*, const Gate&, cudaStream_t);
 template void launch_band_gemv<float>(int, int, const double*, const float*, double*, const Gate&, cudaStream_t);
 template void launch_band_fwd_solve<double>(const TransformTables&, int, int, const int32_t*, const double*,
-                                            const double*, double*, const Gate&, cudaStream_t);
+                                            const double*, double*, const Gate&, cudaStream_t, int);
 template void launch_band_fwd_solve<float>(const TransformTables&, int, int, const int32_t*, const double*,
-                                           const float*, float*, const Gate&, cudaStream_t);
+                                           const float*, float*, const Gate&, cudaStream_t, int);
+template void launch_band_direct<double>(int, int, const double*, const double*, double*, const Gate&, cudaStream_t);
+template void launch_band_direct<float>(int, int, const float*, const float*, double*, const Gate&, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // sparse rows with their loads batched: the column indices and values of up to CSR_B entries
@@ -2566,13 +2605,20 @@ __global__ void __launch_bounds__(BAND_TPB) k_band_gemv_multi(const __grid_const
   band_gemv_body<T>(a.m, a.M, a.firstm, a.c, blockIdx.x);
 }
 template <typename T>
+__global__ void __launch_bounds__(BAND_TPB) k_band_direct_multi(const __grid_constant__ ArgPack<BandDirectArgs<T>> p) {
+  const BandDirectArgs<T>& a = p.a[blockIdx.y];
+  if ((int)blockIdx.x >= a.rank * BAND_SPLIT) return;
+  if (!gate_open(a.gate)) return;
+  band_direct_body<T>(a.L, a.G, a.S, a.part, blockIdx.x / BAND_SPLIT, blockIdx.x % BAND_SPLIT);
+}
+template <typename T>
 __global__ void __launch_bounds__(BAND_COLS * BAND_ROWT) k_band_fwd_solve_multi(
     const __grid_constant__ ArgPack<BandFwdArgs<T>> p) {
   const BandFwdArgs<T>& a = p.a[blockIdx.y];
   if ((int)blockIdx.x >= a.nblk) return;
   if (!gate_open(a.gate)) return;
   band_fwd_solve_body<T>(a.nb, a.n, a.rank, a.bptr, a.c, a.bfwd, a.gamma, a.scale, a.bpiv, a.band,
-                         blockIdx.x);
+                         blockIdx.x, a.nsplit);
 }
 template <int KIND, bool RES_F32>
 __global__ void k_residual_multi(const __grid_constant__ ArgPack<ResidualArgs> p) {
@@ -2728,6 +2774,14 @@ void launch_band_gemv_multi(const ArgPack<BandGemvArgs<T>>& p, int n, cudaStream
   k_band_gemv_multi<T><<<dim3((unsigned)r, (unsigned)n), BAND_TPB, 0, st>>>(p);
 }
 template <typename T>
+void launch_band_direct_multi(const ArgPack<BandDirectArgs<T>>& p, int n, cudaStream_t st) {
+  if (n <= 0) return;
+  int r = 1;
+  for (int c = 0; c < n; ++c) r = std::max(r, p.a[c].rank);
+  note_launch();
+  k_band_direct_multi<T><<<dim3((unsigned)(r * BAND_SPLIT), (unsigned)n), BAND_TPB, 0, st>>>(p);
+}
+template <typename T>
 void launch_band_fwd_solve_multi(const ArgPack<BandFwdArgs<T>>& p, int n, cudaStream_t st) {
   if (n <= 0) return;
   size_t smem = 0;
@@ -2781,6 +2835,8 @@ template void launch_band_first_multi<double>(const ArgPack<BandFirstArgs<double
 template void launch_band_first_multi<float>(const ArgPack<BandFirstArgs<float>>&, int, cudaStream_t);
 template void launch_band_gemv_multi<double>(const ArgPack<BandGemvArgs<double>>&, int, cudaStream_t);
 template void launch_band_gemv_multi<float>(const ArgPack<BandGemvArgs<float>>&, int, cudaStream_t);
+template void launch_band_direct_multi<double>(const ArgPack<BandDirectArgs<double>>&, int, cudaStream_t);
+template void launch_band_direct_multi<float>(const ArgPack<BandDirectArgs<float>>&, int, cudaStream_t);
 template void launch_band_fwd_solve_multi<double>(const ArgPack<BandFwdArgs<double>>&, int, cudaStream_t);
 template void launch_band_fwd_solve_multi<float>(const ArgPack<BandFwdArgs<float>>&, int, cudaStream_t);
 

@@ -355,10 +355,16 @@ void launch_band_first(int m, int n, const int32_t* mrow, const T* binv, const T
 template <typename T>
 void launch_band_gemv(int rank, int m, const double* M, const T* firstm, double* c, const Gate& gate,
                       cudaStream_t st);
-//   band[j][k] = band solve of ( sum_{e in band row j} c[e] bfwd[e][k] ) per column k
+// or both at once with G = M binv folded on the host (rank x L, L = the spectrum rows the C rows
+// read times n): part[r BAND_SPLIT + s] = slice s of G[r] . S, S = those spectrum rows
+static constexpr int BAND_SPLIT = 4;
+template <typename T>
+void launch_band_direct(int rank, int L, const T* G, const T* S, double* part, const Gate& gate, cudaStream_t st);
+//   band[j][k] = band solve of ( sum_{e in band row j} c[e] bfwd[e][k] ) per column k, with c[e]
+//   the sum of its nsplit slices
 template <typename T>
 void launch_band_fwd_solve(const TransformTables& tt, int n, int rank, const int32_t* bptr, const double* c,
-                           const T* bfwd, T* band, const Gate& gate, cudaStream_t st);
+                           const T* bfwd, T* band, const Gate& gate, cudaStream_t st, int nsplit = 1);
 // shared memory of launch_band_fwd_solve (the direct path needs it within the default 48 KB)
 // and its blocks for n columns
 size_t band_fwd_smem(int nb, int rank, bool fp32);
@@ -593,6 +599,15 @@ struct BandFwdArgs {
   T* band;
   Gate gate;
   int nblk;
+  int nsplit;   // slices per Schur value in c (1: c holds the values)
+};
+template <typename T>
+struct BandDirectArgs {
+  int rank, L;
+  const T* G;
+  const T* S;
+  double* part;
+  Gate gate;
 };
 struct ResidualArgs {
   CaseDev c;
@@ -636,6 +651,8 @@ template <typename T>
 void launch_band_gemv_multi(const ArgPack<BandGemvArgs<T>>& p, int n, cudaStream_t st);
 template <typename T>
 void launch_band_fwd_solve_multi(const ArgPack<BandFwdArgs<T>>& p, int n, cudaStream_t st);
+template <typename T>
+void launch_band_direct_multi(const ArgPack<BandDirectArgs<T>>& p, int n, cudaStream_t st);
 void launch_residual_multi(const ArgPack<ResidualArgs>& p, int n, int kind, bool res_f32, cudaStream_t st);
 void launch_pressure_bound_multi(const ArgPack<BoundArgs>& p, int n, cudaStream_t st);
 // Refinement decision of a WHILE node over n cases: each case whose check sc->k exceeded its
