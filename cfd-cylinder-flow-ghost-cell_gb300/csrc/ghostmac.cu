@@ -186,6 +186,18 @@ struct gm_handle {
   // directions Z (m), the refinement correction and reduction scratch
   static constexpr int GMRES_M = 50;
   DBuf<double> gV, gZ, gdx, gpart, gdots, gcoef;
+  // FGMRES with its control on the device: state, scalars, and one instantiated graph per
+  // (right-hand side, solution) pair it has solved for
+  DBuf<GmresDev> gdev;
+  DBuf<double> gd1, gd2, gwn, gbeta, gbn, gy, gone;
+  DBuf<int> gnv;
+  struct GmresExec {
+    const double* b = nullptr;
+    double* x = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long fixed = 0, per_cycle = 0, per_step = 0;  // kernels of the graph's parts
+  };
+  std::vector<GmresExec> gexec;
   // learned preconditioner attached to the GMRES path (network and weights owned by the caller)
   gm_unet* lnet = nullptr;
   std::vector<const uint16_t*> lw;
@@ -1290,6 +1302,152 @@ int fgmres(gm_handle* h, const double* b, double* x, int& iterations, bool learn
   return converged ? 0 : std::max(1, iterations);
 }
 
+// The same FGMRES(50) with its control on the device (kernels.cu, GmresDev): one graph per
+// (b, x) pair, built on first use and replayed after.  Restart cycles form a WHILE node; each
+// of the 50 Arnoldi steps of a cycle is an IF node whose condition the previous step sets, so
+// a solve launches the kernels of the steps it takes and reads nothing back until it ends.
+// The learned preconditioner keeps the host-driven fgmres above.
+static_assert(gm_handle::GMRES_M == GmresDev::M, "GMRES restart length");
+
+cudaGraphNode_t add_conditional(cudaStream_t st, cudaGraphConditionalHandle cond, cudaGraphConditionalNodeType type,
+                                cudaGraph_t* body) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t graph;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &graph, &deps, nullptr, &nd));
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = cond;
+  cp.conditional.type = type;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, graph, deps, nullptr, nd, &cp));
+  *body = cp.conditional.phGraph_out[0];
+  CK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  return node;
+}
+
+gm_handle::GmresExec& gmres_graph(gm_handle* h, const double* b, double* x) {
+  for (auto& ge : h->gexec)
+    if (ge.b == b && ge.x == x && ge.exec) return ge;
+  const int m = gm_handle::GMRES_M;
+  const int64_t n = h->Pn;
+  if (!h->gdev.p) {
+    h->gdev.alloc(1);
+    for (DBuf<double>* d : {&h->gd1, &h->gd2, &h->gy}) d->alloc(64);
+    for (DBuf<double>* d : {&h->gwn, &h->gbeta, &h->gbn, &h->gone}) d->alloc(1);
+    h->gnv.alloc(1);
+    const double one = 1.0;
+    CK(cudaMemcpyAsync(h->gone.p, &one, sizeof one, cudaMemcpyHostToDevice, h->st));
+  }
+  RectDev& rd = h->rp;
+  const Gate open{nullptr, 0, 0};
+  double* V = h->gV.p;
+  double* Z = h->gZ.p;
+  auto vec = [&](double* base, int i) { return base + (int64_t)i * n; };
+  cudaStream_t st = h->st, sb1 = h->st_body, sb2 = h->st2_body;
+  auto precondition = [&](const double* v, double* z, cudaStream_t s) {
+    if (h->precision == 1)
+      plain_inverse<float, double, double>(rd.tt32, rd.view, v, true, h->spectral32.p, z, rd.view.cls, nullptr, open,
+                                           s);
+    else
+      plain_inverse<double, double, double>(rd.tt, rd.view, v, true, h->spectral.p, z, rd.view.cls, nullptr, open, s);
+  };
+  gm_handle::GmresExec ge;
+  ge.b = b;
+  ge.x = x;
+  const long long c0 = kernel_launch_count();
+  CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  launch_multidot(b, n, 1, b, n, h->gpart.p, h->gbn.p, st);
+  CK(cudaMemsetAsync(x, 0, n * sizeof(double), st));
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t top;
+  CK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &top, nullptr, nullptr, nullptr));
+  cudaGraphConditionalHandle cyc;
+  CK(cudaGraphConditionalHandleCreate(&cyc, top, 0, 0));
+  launch_gm_init(h->gdev.p, h->gbn.p, cyc, st);
+  ge.fixed = kernel_launch_count() - c0;
+  cudaGraph_t cycle_body;
+  add_conditional(st, cyc, cudaGraphCondTypeWhile, &cycle_body);
+  CK(cudaStreamBeginCaptureToGraph(sb1, cycle_body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  const long long c1 = kernel_launch_count();
+  // V0 = (b - A x) / ||b - A x||
+  launch_apply_pressure(h->cd, h->rcoef[0], x, vec(V, 1), open, sb1);
+  CK(cudaMemcpyAsync(vec(V, 0), b, n * sizeof(double), cudaMemcpyDeviceToDevice, sb1));
+  launch_multiaxpy(vec(V, 1), n, 1, h->gone.p, -1.0, 1.0, vec(V, 0), n, sb1);
+  launch_multidot(vec(V, 0), n, 1, vec(V, 0), n, h->gpart.p, h->gbeta.p, sb1);
+  GmresHandles hs{};
+  cudaGraph_t cyc_graph;
+  CK(cudaStreamGetCaptureInfo(sb1, &cs, nullptr, &cyc_graph, nullptr, nullptr, nullptr));
+  for (int j = 0; j < m; ++j) CK(cudaGraphConditionalHandleCreate(&hs.step[j], cyc_graph, 0, 0));
+  launch_gm_cycle_begin(h->gdev.p, h->gbeta.p, hs, sb1);
+  launch_gm_scale(vec(V, 0), n, h->gdev.p, sb1);
+  long long per_step = 0;
+  for (int j = 0; j < m; ++j) {
+    cudaGraph_t step_body;
+    add_conditional(sb1, hs.step[j], cudaGraphCondTypeIf, &step_body);
+    CK(cudaStreamBeginCaptureToGraph(sb2, step_body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const long long c2 = kernel_launch_count();
+    double* w = vec(V, j + 1);
+    precondition(vec(V, j), vec(Z, j), sb2);
+    launch_apply_pressure(h->cd, h->rcoef[0], vec(Z, j), w, open, sb2);
+    // two classical Gram-Schmidt passes against V_0..V_j, then the norm
+    launch_multidot(V, n, j + 1, w, n, h->gpart.p, h->gd1.p, sb2);
+    launch_multiaxpy(V, n, j + 1, h->gd1.p, -1.0, 1.0, w, n, sb2);
+    launch_multidot(V, n, j + 1, w, n, h->gpart.p, h->gd2.p, sb2);
+    launch_multiaxpy(V, n, j + 1, h->gd2.p, -1.0, 1.0, w, n, sb2);
+    launch_multidot(w, n, 1, w, n, h->gpart.p, h->gwn.p, sb2);
+    launch_gm_step_end(h->gdev.p, j, h->gd1.p, h->gd2.p, h->gwn.p, j + 1 < m ? hs.step[j + 1] : hs.step[0], j + 1 < m,
+                       sb2);
+    launch_gm_scale(w, n, h->gdev.p, sb2);
+    per_step = kernel_launch_count() - c2;
+    cudaGraph_t done;
+    CK(cudaStreamEndCapture(sb2, &done));
+  }
+  // y = R^{-1} g, x += Z y
+  launch_gm_cycle_end(h->gdev.p, h->gy.p, h->gnv.p, cyc, sb1);
+  launch_multiaxpy_dev(Z, n, h->gnv.p, h->gy.p, x, n, sb1);
+  ge.per_step = per_step;
+  ge.per_cycle = kernel_launch_count() - c1 - (long long)m * per_step;
+  cudaGraph_t done1;
+  CK(cudaStreamEndCapture(sb1, &done1));
+  cudaGraph_t graph;
+  CK(cudaStreamEndCapture(st, &graph));
+  cudaError_t e = cudaGraphInstantiate(&ge.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  CK(e);
+  kernel_launch_adjust(-(kernel_launch_count() - c0));  // captured, not yet launched
+  if (h->gexec.size() >= 8) {
+    cudaGraphExecDestroy(h->gexec.front().exec);
+    h->gexec.erase(h->gexec.begin());
+  }
+  h->gexec.push_back(ge);
+  return h->gexec.back();
+}
+
+int fgmres_device(gm_handle* h, const double* b, double* x, int& iterations) {
+  if (!h->gV.p) {
+    const int m = gm_handle::GMRES_M;
+    const int64_t n = h->Pn;
+    h->gV.alloc((size_t)(m + 1) * n);
+    h->gZ.alloc((size_t)m * n);
+    h->gdx.alloc(n);
+    h->gpart.alloc((size_t)multidot_blocks(n) * 64);
+    h->gdots.alloc(64);
+    h->gcoef.alloc(64);
+  }
+  gm_handle::GmresExec& ge = gmres_graph(h, b, x);
+  CK(cudaGraphLaunch(ge.exec, h->st));
+  int r[5];
+  CK(cudaMemcpyAsync(r, &h->gdev.p->jend, sizeof r, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  const int cycles = r[1], its = r[2], converged = r[3];
+  kernel_launch_adjust(ge.fixed + (long long)cycles * ge.per_cycle + (long long)its * ge.per_step);
+  iterations = its;
+  return converged ? 0 : std::max(1, its);
+}
+
 // monitored_pressure_solver, iterative branch (solver/pressure_schur.py:16-72): GMRES, the
 // true residual, up to two GMRES refinements of the residual to max(1e-10, 64 eps max(1,|b|));
 // the gate (k_gate_pressure) then sees the final check, its roundoff bound and the status.
@@ -1298,7 +1456,14 @@ void gmres_monitored(gm_handle* h, const double* b, double* x, double* res, int 
   SolveCtl* sc = &h->ctl.p->solve[slot];
   const Gate g0 = gate_of(h);
   int its = 0, total = 0;
-  int status = fgmres(h, b, x, its, true);
+  // device-controlled FGMRES unless a learned network seeds the first direction (or
+  // GHOSTMAC_GMRES_HOST=1)
+  const char* eh = std::getenv("GHOSTMAC_GMRES_HOST");
+  const bool dev = !h->lnet && !(eh && eh[0] == '1') && !h->capturing && h->st != nullptr && !ktimer_active();
+  auto solve = [&](const double* rb, double* rx, int& it, bool learned) {
+    return dev ? fgmres_device(h, rb, rx, it) : fgmres(h, rb, rx, it, learned);
+  };
+  int status = solve(b, x, its, true);
   total += its;
   launch_residual(h->cd, h->rcoef[0], 0, b, x, res, false, sc, 0, true, g0, st);
   auto read = [&](SolveCtl& hs) {
@@ -1311,7 +1476,7 @@ void gmres_monitored(gm_handle* h, const double* b, double* x, double* res, int 
   int k = 0;
   for (int r = 0; r < 2; ++r) {
     if (status || bits2d(hs.rmax[k]) <= target) break;
-    status = fgmres(h, res, h->gdx.p, its, false);
+    status = solve(res, h->gdx.p, its, false);
     total += its;
     const double one = 1.0;
     CK(cudaMemcpyAsync(h->gcoef.p, &one, sizeof one, cudaMemcpyHostToDevice, st));
@@ -2058,6 +2223,8 @@ int gm_destroy(gm_handle* h) {
   if (h->host_ring) cudaFreeHost(h->host_ring);
   for (auto& gr : h->graphs)
     if (gr.exec) cudaGraphExecDestroy(gr.exec);
+  for (auto& ge : h->gexec)
+    if (ge.exec) cudaGraphExecDestroy(ge.exec);
   if (h->st2) cudaStreamSynchronize(h->st2);
   if (h->st_body) cudaStreamDestroy(h->st_body);
   if (h->st2) cudaStreamDestroy(h->st2);

@@ -2433,6 +2433,130 @@ void launch_cfl_screen(StepCtl* ctl, const unsigned long long* umax, const unsig
   kt_mark(10, st);
 }
 
+// ---------------------------------------------------------------------------
+// Flexible GMRES(50) with its control on the device (solver/pressure_schur.py:20-41): the
+// Hessenberg column, the Givens rotations, the residual estimate, the convergence test and
+// the least-squares update run in one-thread kernels on the device-resident GmresDev, and the
+// loops are conditional graph nodes (restart cycles: WHILE; Arnoldi steps: one IF node per
+// step, its condition set by the previous step).  The arithmetic is that of the host loop it
+// replaces, in the same order.
+// ---------------------------------------------------------------------------
+__global__ void k_gm_init(GmresDev* gd, const double* __restrict__ bn2, cudaGraphConditionalHandle cycle) {
+  gd->tol = fmax(1e-12 * sqrt(bn2[0]), 1e-12);
+  gd->iterations = 0;
+  gd->converged = 0;
+  gd->stop = 0;
+  gd->cycle = 0;
+  gd->jend = -1;
+  cudaGraphSetConditional(cycle, 1u);
+}
+// beta = ||b - A x||; the cycle's first step runs while beta > tol
+__global__ void k_gm_cycle_begin(GmresDev* gd, const double* __restrict__ beta2, GmresHandles hs) {
+  const double beta = sqrt(beta2[0]);
+  gd->jend = -1;
+  bool go = beta > gd->tol;
+  if (!go) {
+    gd->converged = isfinite(beta) ? 1 : 0;
+    gd->stop = 1;
+    gd->hscale = 1.0;
+  } else {
+    for (int i = 0; i <= GmresDev::M; ++i) gd->g[i] = 0.0;
+    gd->g[0] = beta;
+    gd->hscale = 1.0 / beta;
+  }
+  for (int j = 0; j < GmresDev::M; ++j) cudaGraphSetConditional(hs.step[j], (j == 0 && go) ? 1u : 0u);
+}
+// w *= hscale (the new basis vector, or V_0 at the start of a cycle)
+__global__ void k_gm_scale(double* __restrict__ w, int64_t n, const GmresDev* __restrict__ gd) {
+  const double s = gd->hscale;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    w[t] *= s;
+}
+// end of Arnoldi step j: column j of H from the two Gram-Schmidt passes and the norm, the
+// rotations, the residual estimate g[j+1]; step j + 1 runs while it is finite and above tol
+__global__ void k_gm_step_end(GmresDev* gd, int j, const double* __restrict__ d1, const double* __restrict__ d2,
+                              const double* __restrict__ wn2, cudaGraphConditionalHandle next, int has_next) {
+  double hc[GmresDev::M + 1];
+  for (int i = 0; i <= j; ++i) hc[i] = d1[i] + d2[i];
+  hc[j + 1] = sqrt(wn2[0]);
+  gd->hscale = hc[j + 1] > 0 ? 1.0 / hc[j + 1] : 1.0;
+  for (int i = 0; i < j; ++i) {
+    const double a = gd->cs[i] * hc[i] + gd->sn[i] * hc[i + 1];
+    hc[i + 1] = -gd->sn[i] * hc[i] + gd->cs[i] * hc[i + 1];
+    hc[i] = a;
+  }
+  const double den = hypot(hc[j], hc[j + 1]);
+  gd->cs[j] = den > 0 ? hc[j] / den : 1.0;
+  gd->sn[j] = den > 0 ? hc[j + 1] / den : 0.0;
+  hc[j] = den;
+  gd->g[j + 1] = -gd->sn[j] * gd->g[j];
+  gd->g[j] = gd->cs[j] * gd->g[j];
+  for (int i = 0; i <= j; ++i) gd->H[i * GmresDev::M + j] = hc[i];
+  gd->iterations += 1;
+  gd->jend = j;
+  const double r = gd->g[j + 1];
+  bool go = true;
+  if (!isfinite(r)) go = false;
+  else if (fabs(r) <= gd->tol) { gd->converged = 1; go = false; }
+  if (has_next) cudaGraphSetConditional(next, go ? 1u : 0u);
+}
+// end of a cycle: y = R^{-1} g (the solve of the host loop), nv = its length for x += Z y; the
+// next cycle runs while not converged, a step was taken and fewer than 100 cycles ran
+__global__ void k_gm_cycle_end(GmresDev* gd, double* __restrict__ y, int* __restrict__ nv,
+                               cudaGraphConditionalHandle cycle) {
+  const int jend = gd->jend;
+  for (int i = jend; i >= 0; --i) {
+    double acc = gd->g[i];
+    for (int k = i + 1; k <= jend; ++k) acc -= gd->H[i * GmresDev::M + k] * gd->y[k];
+    gd->y[i] = acc / gd->H[i * GmresDev::M + i];
+  }
+  for (int i = 0; i <= jend; ++i) y[i] = gd->y[i];
+  *nv = jend + 1;
+  gd->cycle += 1;
+  const bool go = jend >= 0 && !gd->converged && !gd->stop && gd->cycle < 100;
+  cudaGraphSetConditional(cycle, go ? 1u : 0u);
+}
+// y += sum_{i < *nv} coef[i] V_i (the count on the device)
+__global__ void k_multiaxpy_dev(const double* __restrict__ V, int64_t ld, const int* __restrict__ nvp,
+                                const double* __restrict__ coef, double* __restrict__ y, int64_t n) {
+  __shared__ double cf[GM_DOT_MAX + 1];
+  const int nv = *nvp;
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) cf[i] = coef[i];
+  __syncthreads();
+  if (nv <= 0) return;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int i = 0; i < nv; ++i) acc += cf[i] * V[(int64_t)i * ld + t];
+    y[t] = 1.0 * y[t] + 1.0 * acc;
+  }
+}
+void launch_gm_init(GmresDev* gd, const double* bn2, cudaGraphConditionalHandle cycle, cudaStream_t st) {
+  note_launch();
+  k_gm_init<<<1, 1, 0, st>>>(gd, bn2, cycle);
+}
+void launch_gm_cycle_begin(GmresDev* gd, const double* beta2, const GmresHandles& hs, cudaStream_t st) {
+  note_launch();
+  k_gm_cycle_begin<<<1, 1, 0, st>>>(gd, beta2, hs);
+}
+void launch_gm_scale(double* w, int64_t n, const GmresDev* gd, cudaStream_t st) {
+  note_launch();
+  k_gm_scale<<<reduce_blocks(n), TPB, 0, st>>>(w, n, gd);
+}
+void launch_gm_step_end(GmresDev* gd, int j, const double* d1, const double* d2, const double* wn2,
+                        cudaGraphConditionalHandle next, bool has_next, cudaStream_t st) {
+  note_launch();
+  k_gm_step_end<<<1, 1, 0, st>>>(gd, j, d1, d2, wn2, next, has_next ? 1 : 0);
+}
+void launch_gm_cycle_end(GmresDev* gd, double* y, int* nv, cudaGraphConditionalHandle cycle, cudaStream_t st) {
+  note_launch();
+  k_gm_cycle_end<<<1, 1, 0, st>>>(gd, y, nv, cycle);
+}
+void launch_multiaxpy_dev(const double* V, int64_t ld, const int* nv, const double* coef, double* y, int64_t n,
+                          cudaStream_t st) {
+  note_launch();
+  k_multiaxpy_dev<<<reduce_blocks(n), TPB, 0, st>>>(V, ld, nv, coef, y, n);
+}
+
 __global__ void k_refine_decide(StepCtl* ctl, int slot, int nchk, cudaGraphConditionalHandle cond) {
   SolveCtl* sc = &ctl->solve[slot];
   int k = sc->k;

