@@ -91,3 +91,50 @@ def periodic_metrics(t, cd, cl, t_start, D=.4, U_ref=1.):
         # screening threshold of the reference (not a proof of a limit cycle)
         out['stationary'] = max(out['amplitude_drift'], out['period_drift'], out['drag_drift']) < .02
     return out
+
+
+def calculate_gci(f1, f2, f3, r=2., Fs=1.25, r32=None):
+    """Three-grid observed order and grid convergence index (postprocessing/analysis.py:106-151):
+    a conditional estimate for monotone data, not an error bound.  f1, f2, f3 run from the fine
+    grid to the coarse one; r = h2 / h1 and, for unequal ratios, r32 = h3 / h2 (the order then
+    solves r^p (r32^p - 1) / (r^p - 1) = |e32 / e21| by bracketing and Brent's method).  Same
+    keys, statuses and error messages as the reference."""
+    if not all(np.isfinite(x) for x in (f1, f2, f3, r, Fs)) or r <= 1 or Fs < 1:
+        raise ValueError('GCI requires finite values, r > 1 and Fs >= 1')
+    if r32 is not None and (not np.isfinite(r32) or r32 <= 1):
+        raise ValueError('The coarser spacing ratio must exceed one')
+    out = dict(p=None, f_ext=None, e_a21_pct=None, gci_fine_pct=None, status='not estimable',
+               reason='Nonmonotone, divergent, constant or nearly zero data')
+    scale = max(abs(f1), abs(f2), abs(f3), np.finfo(float).tiny)
+    e21, e32 = f2 - f1, f3 - f2
+    if abs(f1) > 1e-12 * scale:
+        out['e_a21_pct'] = float(100 * abs(e21 / f1))
+    if min(abs(e21), abs(e32), abs(f1)) <= 1e-12 * scale or e21 * e32 <= 0:
+        return out
+    if r32 is None or np.isclose(r32, r):
+        p = float(np.log(abs(e32 / e21)) / np.log(r))
+    else:
+        from scipy.optimize import brentq
+
+        def residual(order):
+            return np.exp(order * np.log(r)) * np.expm1(order * np.log(r32)) / np.expm1(order * np.log(r)) \
+                - abs(e32 / e21)
+        top = 10.
+        while residual(.01) * residual(top) > 0 and top < 80.:
+            top *= 2
+        out['order_search_upper'] = top
+        if residual(.01) * residual(top) >= 0:
+            out['reason'] = f'No positive resolved order in [0.01, {top:g}] for these unequal spacings'
+            return out
+        p = float(brentq(residual, .01, top))
+    out['p'] = p
+    if p <= 0:
+        return out
+    if p < .1:
+        out['reason'] = 'Near-zero observed order; extrapolation is ill-conditioned'
+        return out
+    out.update(f_ext=float(f1 - e21 / (r ** p - 1)), gci_fine_pct=float(100 * Fs * abs(e21 / f1) / (r ** p - 1)),
+               status='conditional estimate',
+               reason='Requires asymptotic behaviour and negligible time/sampling error; not established by three '
+                      'points alone')
+    return out

@@ -310,6 +310,23 @@ int gm_mac_forces(const double* u, const double* v, const double* p, const uint8
 int gm_mac_divergence(const double* u, const double* v, const uint8_t* mask, int32_t nx, int32_t ny, double dx,
                       double dy, double out[3], int64_t counts[2], void* stream);
 
+/* --- snapshot POD (postprocessing/modal_analysis.py:17-98) ------------------------ */
+/* Method of snapshots for M snapshots of N points (row-major M x N, host or device memory):
+ * gm_pod_gram forms the time mean (summed over the snapshots in order, like numpy's mean
+ * along axis 0) and the Gram matrix C = X' X'^T / M of the fluctuations X' = X - mean, which
+ * stay on the device; the caller takes the eigen-decomposition of C (M x M) and passes the
+ * first k eigenvectors (M x k, row s = snapshot s) and singular values sigma_q =
+ * sqrt(M lambda_q) to gm_pod_modes, which returns the spatial modes X'^T v_q / sigma_q (k x N;
+ * zero where sigma_q <= 1e-12) and the temporal coefficients X' phi_q (k x M).  Outputs may be
+ * host or device memory; both calls return with them written. */
+typedef struct gm_pod gm_pod;
+int gm_pod_create(int32_t n_snapshots, int64_t n_points, gm_pod** out);
+int gm_pod_destroy(gm_pod* p);
+const char* gm_pod_last_error(const gm_pod* p);
+int gm_pod_gram(gm_pod* p, const double* snapshots, double* mean, double* gram, void* stream);
+int gm_pod_modes(gm_pod* p, const double* eigvecs, const double* sigma, int32_t k, double* modes, double* coeffs,
+                 void* stream);
+
 /* --- page-locked host memory (no reference counterpart) ------------------------ */
 
 /* Page-locked host allocation (cudaMallocHost) for arrays that cross the bus every step, such

@@ -128,7 +128,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', type=Path, required=True, help='path of the reference checkout')
     ap.add_argument('--skip-large', action='store_true')
-    ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner', 'legacy'),
+    ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner', 'legacy', 'modal'),
                     help='generate one group of fixtures only')
     args = ap.parse_args()
     work = Path(tempfile.mkdtemp(prefix='ghost_golden_'))
@@ -142,12 +142,15 @@ def main():
             run_runner(work)
         elif args.only == 'legacy':
             run_legacy(work)
+        elif args.only == 'modal':
+            run_modal(work)
         else:
             run_all(args)
             run_taylor_green(work)
             run_analysis(work)
             run_runner(work)
             run_legacy(work)
+            run_modal(work)
     finally:
         shutil.rmtree(work, ignore_errors=True)
 
@@ -252,6 +255,24 @@ def run_legacy(work):
     save('legacy_kernels', **out)
 
 
+def run_modal(work):
+    """The reference's snapshot POD (postprocessing/modal_analysis.py) on a seeded synthetic wake:
+    two travelling modes plus noise on a 24 x 40 grid, 30 snapshots."""
+    from postprocessing.modal_analysis import SnapshotPOD, compute_phase_portrait_metrics
+    rng = np.random.default_rng(31)
+    ny, nx, m = 24, 40, 30
+    y, x = np.meshgrid(np.linspace(-1, 1, ny), np.linspace(0, 4, nx), indexing='ij')
+    t = np.linspace(0, 6, m)
+    snaps = np.array([0.3 + np.sin(2 * x - 1.7 * tt) * np.exp(-4 * y * y) + 0.4 * np.cos(3 * x - 3.4 * tt) * y
+                      + 1e-3 * rng.standard_normal((ny, nx)) for tt in t])
+    pod = SnapshotPOD(n_modes=6).fit(snaps)
+    pp = compute_phase_portrait_metrics(pod.temporal_coeffs[0], pod.temporal_coeffs[1])
+    save('modal', snapshots=snaps, mean_field=pod.mean_field, spatial_modes=pod.spatial_modes,
+         temporal_coeffs=pod.temporal_coeffs, singular_values=pod.singular_values,
+         modal_energies=pod.modal_energies, energy_ratios=pod.energy_ratios,
+         cumulative_energy=pod.cumulative_energy, phase=np.array([pp['mean_amplitude'], pp['circularity_error']]))
+
+
 def run_analysis(work):
     """postprocessing/analysis.py periodic_metrics on seeded synthetic force histories: a
     resolved, drifting shedding signal and an unresolved one."""
@@ -266,7 +287,16 @@ def run_analysis(work):
         m = periodic_metrics(tt, a, b, ts, D=1.0, U_ref=1.0)
         keys = sorted(m)
         rows.append([float(m[k]) for k in keys])
-    save('analysis', t=t, cd=cd, cl=cl, keys=np.array(keys), values=np.array(rows))
+    # calculate_gci (postprocessing/analysis.py:106-151): equal and unequal ratios, the
+    # non-estimable branches
+    from postprocessing.analysis import calculate_gci
+    import json
+    gci_cases = [(1.0, 1.04, 1.2, 2.0, 1.25, None), (1.0, 1.04, 1.2, 2.0, 1.25, 1.5), (1.0, 1.1, 1.05, 2.0, 1.25, None),
+                 (2.0, 2.0, 2.0, 2.0, 1.25, None), (1.0, 1.001, 1.0021, 2.0, 3.0, None),
+                 (0.5, 0.52, 0.53, 1.5, 1.25, 2.5), (1.0, 1.0000001, 1.0000002, 2.0, 1.25, None)]
+    gci = [calculate_gci(*c[:3], r=c[3], Fs=c[4], r32=c[5]) for c in gci_cases]
+    save('analysis', t=t, cd=cd, cl=cl, keys=np.array(keys), values=np.array(rows),
+         gci_cases=json.dumps(gci_cases), gci=json.dumps(gci))
 
 
 def run_taylor_green(work):

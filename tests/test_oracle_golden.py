@@ -172,3 +172,28 @@ def test_periodic_metrics_matches_reference():
         np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-14, equal_nan=True)
     with pytest.raises(ValueError):
         an.periodic_metrics([0, 1], [1, 1], [0, 0], 0.0)
+
+
+def test_grid_convergence_index_matches_reference():
+    """calculate_gci against the reference's own results (tests/golden/analysis.npz): equal and
+    unequal refinement ratios and the non-estimable branches."""
+    import importlib.util
+    import json
+    from pathlib import Path
+    spec = importlib.util.spec_from_file_location(
+        'gm_analysis', Path(__file__).resolve().parents[1] / 'cfd-cylinder-flow-ghost-cell_gb300' / 'analysis.py')
+    an = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(an)
+    G = np.load(GOLDEN / 'analysis.npz')
+    for case, want in zip(json.loads(str(G['gci_cases'])), json.loads(str(G['gci']))):
+        got = an.calculate_gci(*case[:3], r=case[3], Fs=case[4], r32=case[5])
+        assert set(got) == set(want), case
+        for k, v in want.items():
+            if isinstance(v, float):
+                assert abs(got[k] - v) <= 1e-12 * max(1.0, abs(v)), (case, k)
+            else:
+                assert got[k] == v, (case, k)
+    with pytest.raises(ValueError, match='GCI requires'):
+        an.calculate_gci(1.0, 1.1, 1.2, r=1.0)
+    with pytest.raises(ValueError, match='coarser spacing'):
+        an.calculate_gci(1.0, 1.1, 1.2, r32=0.5)
