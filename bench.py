@@ -806,6 +806,29 @@ def run_ours_batch(args, w, rank, world):
     batch.close()
 
 
+def profile_step(args, w):
+    """One single-case step launch by launch (every kernel a separate launch, the refinement
+    sweeps gated on the device) inside the NVTX range "one_step", after the warm-up steps."""
+    os.environ['GHOSTMAC_NO_GRAPHS'] = '1'
+    import torch
+    pkg = load_package()
+    kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
+    s = pkg.MAC_CylinderFlow(verbose=False, precision=args.precision, **kw)
+    seeded_state(s, w)
+    s._push()
+    for k in range(args.warmup):
+        rc, d = s.step_raw(w['dt'], 1, first_index=k)
+        pkg._lib.check(rc, s._h)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push('one_step')
+    rc, d = s.step_raw(w['dt'], 1, first_index=args.warmup)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    pkg._lib.check(rc, s._h)
+    print(json.dumps(dict(profile_step=args.workload, precision=args.precision, max_divergence=d[0].max_divergence,
+                          pressure_sweeps=int(d[0].pressure_refinement_iterations))), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument('--gpus', type=int, default=1)
@@ -819,6 +842,9 @@ def main():
     ap.add_argument('--no-batch', action='store_true', help='skip timing the 64-case sweep beside the single case')
     ap.add_argument('--precision', choices=('fp64', 'fp32'), default='fp32',
                     help='fp64: plain FP64 method; fp32: FP32 inverses and stencils with FP64 refinement')
+    ap.add_argument('--profile-step', action='store_true',
+                    help='profiling driver: W warm-up steps, then one launch-by-launch step inside the NVTX range '
+                         '"one_step" (for ncu --nvtx-include "one_step/"), no timing')
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -828,6 +854,9 @@ def main():
     rank = int(os.environ.get('RANK', 0))
     if args.impl == 'reference':
         run_reference(args, w, rank)
+        return
+    if args.profile_step:
+        profile_step(args, w)
         return
     if world > 1:
         import torch

@@ -782,12 +782,15 @@ void build_direct_tables(gm_handle* h, RectDev& rd, const std::vector<int64_t>& 
     rd.bfwd32.upload(to_f32(bfwd), st);
     rd.firstm32.alloc(m);
   }
-  // G = M binv over the spectrum rows cj0..cj1: one sum per Schur value per solve instead of the
-  // point values and a GEMV (GHOSTMAC_BAND_GEMV=1 keeps those; tables over 64 MB too)
+  // Opt-in (GHOSTMAC_BAND_FOLDED=1): G = M binv over the spectrum rows cj0..cj1, one sum per
+  // Schur value per solve instead of the point values and a GEMV.  Measured on the 800x820
+  // case it loses: in the FP32 mode the rounding of G and the long FP32 sums leave the inverse
+  // less accurate (4.0 instead of 2.8 pressure sweeps per step, 0.774 against 0.701 ms), and the
+  // plain FP64 step gains nothing (0.973 against 0.957 ms).
   rd.glen = 0;
-  const char* eg = std::getenv("GHOSTMAC_BAND_GEMV");
+  const char* eg = std::getenv("GHOSTMAC_BAND_FOLDED");
   const int L = (tt.cj1 - tt.cj0 + 1) * n;
-  if (!(eg && eg[0] == '1') && tt.cj1 >= tt.cj0 && (size_t)rank * L * 8 <= ((size_t)64 << 20)) {
+  if ((eg && eg[0] == '1') && tt.cj1 >= tt.cj0 && (size_t)rank * L * 8 <= ((size_t)64 << 20)) {
     std::vector<double> G((size_t)rank * L, 0.0);
     for (int r = 0; r < rank; ++r) {
       double* gr = &G[(size_t)r * L];

@@ -47,9 +47,10 @@ def test_learned_preconditioner_on_held_out_solves(record_property):
     Measured result: the network does not pay.  It only seeds the first Arnoldi direction
     (T^-1 b + s net(b / s)), and GMRES must still reduce the residual by twelve decades, so a
     first direction with a held-out error of some 10 % can buy about one of them, while one
-    network application costs more than an iteration; on the 1024x512 case the iterations rose
-    17 % and the time 62 %.  The assertion pins that negative: the network changes the mean
-    iteration count by less than two either way."""
+    network application costs more than an iteration; on the 1024x512 case (bench.py --workload
+    gmres_1024x512_re150) it took 19.0 against 18.95 iterations per solve and 14.8 against
+    8.0 ms per step.  The assertion pins that negative: the network changes the mean iteration
+    count by less than two either way."""
     import time
     torch = pytest.importorskip('torch')
     pkg = load_package()
@@ -84,7 +85,7 @@ def test_learned_preconditioner_on_held_out_solves(record_property):
         assert np.max(np.abs(x1 - x0)) < 1e-8 * max(1.0, np.max(np.abs(x0)))
     gain_its = float(np.mean(its_plain) - np.mean(its_learned))
     gain_time = float(np.mean(t_plain) / np.mean(t_learned))
-    for k, v in dict(held_out_relative_error=float(err), gmres_iterations_plain=its_plain,
+    for k, v in dict(held_out_relative_error=[float(e) for e in np.ravel(err)], gmres_iterations_plain=its_plain,
                      gmres_iterations_learned=its_learned, seconds_plain=float(np.mean(t_plain)),
                      seconds_learned=float(np.mean(t_learned)), iterations_saved=gain_its,
                      speedup=gain_time).items():
