@@ -679,8 +679,10 @@ def batch_summary(pkg, L, w, steps, warmup):
         batch._check(rc)
         divs = [diag[i].max_divergence for i in range(len(cases) * steps)]
         assert max(divs) < 1e-10
+        shapes, probe = batch.launch_shapes()
         out[prec] = dict(value=cells / (ms * 1e-3), unit='cell-updates/s', ms_per_step=ms, cases=len(cases),
-                         cells_per_step=cells, max_divergence=max(divs), setup_s=setup_s)
+                         cells_per_step=cells, max_divergence=max(divs), setup_s=setup_s,
+                         launch_shapes=list(shapes), shape_probe_ms=[x for x in probe if x != -1.0][:6])
         batch.close()
         del batch, cases
     out['speedup_fp32_vs_plain_fp64'] = out['fp64']['ms_per_step'] / out['fp32']['ms_per_step']

@@ -30,7 +30,7 @@ SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_las
            'gm_set_learned_preconditioner', 'gm_set_pressure_recorder', 'gm_pressure_recorded',
            'gm_host_alloc', 'gm_host_free', 'gm_solver_info', 'gm_pressure_reconstruction',
            'gm_mac_predictor_rhs', 'gm_mac_corrector', 'gm_mac_forces', 'gm_mac_divergence',
-           'gm_pod_create', 'gm_pod_destroy', 'gm_pod_last_error', 'gm_pod_gram', 'gm_pod_modes')
+           'gm_pod_create', 'gm_pod_destroy', 'gm_pod_last_error', 'gm_pod_gram', 'gm_pod_modes', 'gm_batch_shapes')
 NOALLOC_MAX_CELLS = 1048576
 
 
@@ -90,6 +90,7 @@ def _load():
         'gm_mac_forces': ([P, P, P, P, I32, I32, D, D, D, P, P], C.c_int),
         'gm_mac_divergence': ([P, P, P, I32, I32, D, D, P, P, P], C.c_int),
         'gm_pod_create': ([I32, I64, P], C.c_int),
+        'gm_batch_shapes': ([P, P, P, I32], C.c_int),
         'gm_pod_destroy': ([P], C.c_int),
         'gm_pod_last_error': ([P], C.c_char_p),
         'gm_pod_gram': ([P, P, P, P, P], C.c_int),

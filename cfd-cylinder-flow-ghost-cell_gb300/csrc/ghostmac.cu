@@ -2850,6 +2850,8 @@ struct gm_batch {
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> join;
   std::vector<BatchGroup> groups;  // empty: every case steps on its own graph branch
+  int shape[3] = {0, 0, 0};        // launch shapes the batch gives its cases (0: not chosen yet)
+  std::vector<float> probe_ms;     // the timed candidates, in candidate order (-1: does not fit)
   struct Graph {
     cudaGraphExec_t exec = nullptr;
     std::vector<const double*> key;
@@ -3095,27 +3097,105 @@ void batch_groups(gm_batch* b) {
   }
 }
 
-// Launch shapes of the cases of a batch.  The autotuned shapes of a single case minimise its
-// latency with large blocks (up to 210 KB of shared memory for a column-solve block), which
-// keeps other cases' kernels off those SMs; many concurrent cases run faster with smaller
-// blocks.  Measured on the 64-case FP32 sweep (32 hardware queues): 7.8 ms per step with
-// row-pass groups of 64 threads, 4 per block, and 8 columns per column-solve block, against
-// 10.3 ms with the single-case shapes (8.1-8.9 ms for the other small shapes tried).
-// GHOSTMAC_BATCH_SHAPES="gthreads,gpb,L" picks another shape, "tuned" keeps every case's own.
-void batch_shapes(gm_batch* b) {
-  int gt = 64, gp = 4, L = 8;
-  if (const char* e = std::getenv("GHOSTMAC_BATCH_SHAPES")) {
-    if (std::strncmp(e, "tuned", 5) == 0) return;
-    int a = 0, c = 0, d = 0;
-    if (std::sscanf(e, "%d,%d,%d", &a, &c, &d) == 3) { gt = a; gp = c; L = d; }
+// Launch shapes a batch gives its cases (row-pass group threads, groups per block, columns per
+// column-solve block).  The single-case autotuner minimises one case's latency with large
+// blocks, which in a batch keep other cases' kernels off their SMs; a batch instead times a
+// few small-block candidates under its own concurrency: each candidate is applied to every
+// case, and a probe graph runs every case's separable inverses (pressure, and the Helmholtz
+// ones where the case uses them) on its scratch fields, one branch per case; the fastest of
+// three replays wins.  Chosen once per batch.  GHOSTMAC_BATCH_SHAPES="gthreads,gpb,L" fixes the
+// shapes instead, "tuned" keeps every case's own.
+float batch_probe_ms(gm_batch* b) {
+  const Gate open{nullptr, 0, 0};
+  const long long c0 = kernel_launch_count();
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal));
+  CK(cudaEventRecord(b->fork, b->root));
+  for (size_t c = 0; c < b->cases.size(); ++c) {
+    gm_handle* h = b->cases[c];
+    CK(cudaStreamWaitEvent(h->st, b->fork, 0));
+    RectDev* rs[3] = {&h->rp, &h->ru, &h->rv};
+    for (int k = 0; k < 3; ++k) {
+      if (k > 0 && (!h->helm_ready || (h->precision == 1 && h->jac_iters > 0))) continue;
+      RectDev& rd = *rs[k];
+      double* field = k == 0 ? h->ptmp.p : h->ftmp.p;
+      if (h->precision == 1)
+        plain_inverse<float, double, double>(rd.tt32, rd.view, field, false, h->spectral32.p, field, nullptr, nullptr,
+                                             open, h->st);
+      else
+        plain_inverse<double, double, double>(rd.tt, rd.view, field, false, h->spectral.p, field, nullptr, nullptr,
+                                              open, h->st);
+    }
+    CK(cudaEventRecord(b->join[c], h->st));
+    CK(cudaStreamWaitEvent(b->root, b->join[c], 0));
   }
+  CK(cudaStreamEndCapture(b->root, &g));
+  kernel_launch_adjust(-(kernel_launch_count() - c0));
+  cudaGraphExec_t ex = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return -1.0f;
+  }
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    CK(cudaEventRecord(e0, b->root));
+    CK(cudaGraphLaunch(ex, b->root));
+    CK(cudaEventRecord(e1, b->root));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    if (rep > 0) best = std::min(best, ms);  // the first replay warms caches and code
+  }
+  CK(cudaEventDestroy(e0));
+  CK(cudaEventDestroy(e1));
+  cudaGraphExecDestroy(ex);
+  return best;
+}
+
+bool batch_apply_shape(gm_batch* b, int gt, int gp, int L) {
   for (gm_handle* h : b->cases) {
     RectDev* rs[3] = {&h->rp, &h->ru, &h->rv};
     for (RectDev* rd : rs) {
-      apply_shape(h, *rd, false, gt, gp, L);
-      if (h->precision == 1) apply_shape(h, *rd, true, gt, gp, L);
+      if (!apply_shape(h, *rd, false, gt, gp, L)) return false;
+      if (h->precision == 1 && !apply_shape(h, *rd, true, gt, gp, L)) return false;
     }
   }
+  return true;
+}
+
+void batch_shapes(gm_batch* b) {
+  if (const char* e = std::getenv("GHOSTMAC_BATCH_SHAPES")) {
+    if (std::strncmp(e, "tuned", 5) == 0) return;
+    int a = 0, c = 0, d = 0;
+    if (std::sscanf(e, "%d,%d,%d", &a, &c, &d) == 3) {
+      batch_apply_shape(b, a, c, d);
+      return;
+    }
+  }
+  if (b->shape[0] == 0) {
+    static const int cand[][3] = {{64, 4, 8}, {64, 4, 4}, {32, 8, 4}, {128, 2, 4}, {128, 2, 8}, {64, 2, 8}};
+    float best = 1e30f;
+    b->probe_ms.clear();
+    for (const auto& cs : cand) {
+      float ms = -1.0f;
+      if (batch_apply_shape(b, cs[0], cs[1], cs[2])) ms = batch_probe_ms(b);
+      b->probe_ms.push_back(ms);
+      if (ms > 0 && ms < best) {
+        best = ms;
+        b->shape[0] = cs[0];
+        b->shape[1] = cs[1];
+        b->shape[2] = cs[2];
+      }
+    }
+    if (b->shape[0] == 0) { b->shape[0] = 64; b->shape[1] = 4; b->shape[2] = 8; }
+    for (gm_handle* h : b->cases) CK(cudaStreamSynchronize(h->st));
+  }
+  batch_apply_shape(b, b->shape[0], b->shape[1], b->shape[2]);
 }
 
 // the case-indexed capture of one steady step of every case (phases on the cases' streams,
@@ -3291,6 +3371,13 @@ int gm_batch_create(gm_handle* const* cases, int32_t n_cases, gm_batch** out) {
   });
   if (rc != GM_OK) return rc;
   *out = b.release();
+  return GM_OK;
+}
+
+int gm_batch_shapes(const gm_batch* b, int32_t shape[3], float* probe_ms, int32_t n) {
+  if (!b || !shape) return GM_EVALUE;
+  for (int k = 0; k < 3; ++k) shape[k] = b->shape[k];
+  for (int k = 0; probe_ms && k < n; ++k) probe_ms[k] = k < (int)b->probe_ms.size() ? b->probe_ms[k] : -1.0f;
   return GM_OK;
 }
 

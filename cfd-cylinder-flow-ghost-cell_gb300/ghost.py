@@ -607,6 +607,14 @@ class CylinderBatch:
             msg = (lib.gm_batch_last_error(self._b) or b'').decode(errors='replace')
             raise _lib.error_for(rc, msg)
 
+    def launch_shapes(self):
+        """(gthreads, groups per block, columns per block) the batch chose by timing, and the
+        probe times of its candidates in ms (-1: did not fit); zeros before the first steady step."""
+        shape = (C.c_int32 * 3)()
+        ms = (C.c_float * 8)()
+        check(lib.gm_batch_shapes(self._b, shape, ms, 8))
+        return tuple(shape), [float(x) for x in ms]
+
     def step_raw(self, dt, n_steps, first_index=0):
         """n_steps of every case on the device state; returns (rc, diag[n_cases][n_steps], steps_done)."""
         n = len(self.cases)

@@ -198,6 +198,10 @@ typedef struct gm_batch gm_batch;
 int gm_batch_create(gm_handle* const* cases, int32_t n_cases, gm_batch** out);
 int gm_batch_destroy(gm_batch* b);
 const char* gm_batch_last_error(const gm_batch* b);
+/* The launch shapes (row-pass group threads, groups per block, columns per column-solve block)
+ * the batch chose by timing its candidates under concurrency at its first steady step (all 0
+ * before that), and the candidates' probe times in ms (-1: did not fit), up to n of them. */
+int gm_batch_shapes(const gm_batch* b, int32_t shape[3], float* probe_ms, int32_t n);
 /* n_steps of every case (as gm_step); start_times[n_cases] may be NULL (time 0);
  * diag (may be NULL) receives n_cases * n_steps records, case-major (diag[c * n_steps + k]).
  * When a gate of some case fails, stepping stops at the end of the current graph batch
