@@ -469,9 +469,13 @@ def run_ours(args, w, rank, world):
                    sample=f'{done} AB2/CN steps of {args.workload} ({el:.1f} s) after setup and the start-up step')
     # config 4 beside the single case: the 64-case sweep in both precisions (after the
     # single-case figures, so that its gigabyte of state does not touch them)
-    sweep = None
+    sweep = tgs = gms = None
     if args.precision == 'fp32' and not args.no_batch and world == 1:
         sweep = batch_summary(pkg, L, BATCH_WORKLOADS['sweep64_batch'], max(1, min(args.steps, 10)), args.warmup)
+    # configs 2 and 5 beside it, so that one default run observes every configuration
+    if args.precision == 'fp32' and not args.no_extra and world == 1:
+        tgs = tg_summary(pkg, TG_WORKLOADS['taylor_green_1024'], max(1, min(args.steps, 50)))
+        gms = gmres_summary(pkg, GMRES_WORKLOADS['gmres_1024x512_re150'], max(1, min(args.steps, 10)))
     if rank == 0:
         line = dict(metric=METRIC, value=value, unit='cell-updates/s', n_gpus=world, steps=args.steps,
                     warmup=args.warmup, ms_per_step=step_ms, higher_is_better=True, scaling='weak',
@@ -492,7 +496,8 @@ def run_ours(args, w, rank, world):
                     refinement_sweeps_per_step=dict(pressure=float(np.mean([a for a, _ in sweeps])),
                                                     momentum=float(np.mean([b for _, b in sweeps]))),
                     kernel_class_ms_per_step={KERNEL_CLASSES[c]: v[0] for c, v in per_class.items() if v[1]},
-                    graph_phase_ms=phase_ms, comparison=compare, sweep64_batch=sweep)
+                    graph_phase_ms=phase_ms, comparison=compare, sweep64_batch=sweep, taylor_green_1024=tgs,
+                    gmres_1024x512_re150=gms)
         print(json.dumps(line), flush=True)
 
 
@@ -649,6 +654,60 @@ def run_ours_gmres(args, w, rank, world):
                                training_pairs=int(x.shape[0]), training_epochs=w['epochs'], training_s=train_s,
                                training_loss_ratio=hist[-1] / hist[0]))
         print(json.dumps(line), flush=True)
+
+
+def tg_summary(pkg, w, steps):
+    """Config 2 beside the single case: the periodic Taylor-Green step at 1024^2 in the FP32
+    mode (K steps, one synchronous call) and its error norms at t = 1 in both precisions."""
+    tg = pkg.taylor_green
+    n, nu, dt = w['n'], w['nu'], w['dt']
+    case = tg.TaylorGreen(n, nu, 'fp32')
+    q0, p0 = tg.exact(n, nu, 0.0)
+    case.set_state(q0, p0)
+    case.step(dt, 3)
+    t0 = time.perf_counter()
+    case.step(dt, steps)
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    case.close()
+    info32 = tg.run(n, dt, w['end_time'], nu, 'fp32')[0]
+    info64 = tg.run(n, dt, w['end_time'], nu, 'fp64')[0]
+    norms = lambda i: dict(velocity_l2=i['velocity']['l2'], velocity_linf=i['velocity']['linf'],
+                           pressure_l2=i['pressure']['l2'], max_divergence=i['max_divergence'])
+    return dict(workload='taylor_green_1024', value=n * n / (ms * 1e-3), unit='cell-updates/s', ms_per_step=ms,
+                steps=steps, errors_at_t1_fp32=norms(info32), errors_at_t1_fp64=norms(info64))
+
+
+def gmres_summary(pkg, w, steps):
+    """Config 5 beside the single case: the 1024x512 case with pressure_solver='iterative'
+    (FGMRES with device control, FP32 preconditioner) against the direct path from the same
+    state; the learned network is left to its own workload (it trains for about 30 s)."""
+    import torch
+    kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
+    dt = w['dt']
+    out = dict(workload='gmres_1024x512_re150', steps=steps)
+    for solver in ('iterative', 'direct'):
+        s = pkg.MAC_CylinderFlow(verbose=False, precision='fp32', pressure_solver=solver, **kw)
+        seeded_state(s, w)
+        s._push()
+        its, nsol = 0, 0
+        for k in range(3):
+            rc, d = s.step_raw(dt, 1, first_index=k)
+            pkg._lib.check(rc, s._h)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(steps):
+            rc, d = s.step_raw(dt, 1, first_index=3 + k)
+            pkg._lib.check(rc, s._h)
+            its += int(d[0].pressure_iterations)
+            nsol += int(d[0].pressure_solve_count)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / steps
+        out[solver] = dict(ms_per_step=ms, cell_updates_per_s=w['nx'] * w['ny'] / (ms * 1e-3),
+                           max_divergence=float(d[0].max_divergence))
+        if solver == 'iterative':
+            out[solver]['krylov_iterations_per_solve'] = its / max(nsol, 1)
+        del s
+    return out
 
 
 def batch_summary(pkg, L, w, steps, warmup):
@@ -842,6 +901,8 @@ def main():
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
     ap.add_argument('--no-compare', action='store_true', help='skip timing the plain FP64 step beside the FP32 mode')
     ap.add_argument('--no-batch', action='store_true', help='skip timing the 64-case sweep beside the single case')
+    ap.add_argument('--no-extra', action='store_true',
+                    help='skip the Taylor-Green and GMRES summaries beside the single case')
     ap.add_argument('--precision', choices=('fp64', 'fp32'), default='fp32',
                     help='fp64: plain FP64 method; fp32: FP32 inverses and stencils with FP64 refinement')
     ap.add_argument('--profile-step', action='store_true',
