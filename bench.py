@@ -454,8 +454,11 @@ def run_ours(args, w, rank, world):
     peak, peak_kind = peaks()
     achieved = by.value / max(tot.value * 1e-3, 1e-12) / 1e9
     traffic = DRAM_TRAFFIC.get((args.workload, args.precision, dominant))
-    # end to end through the public API with host numpy arrays
-    e2e_steps = max(1, min(args.steps, 10))
+    # end to end through the public API with host numpy arrays: warm-up calls first (the
+    # timing runs above leave the step graphs to be captured again), then K calls timed
+    e2e_steps = max(1, min(args.steps, 20))
+    for _ in range(max(args.warmup, 3)):
+        s.solve(n_steps=1, dt=dt, perturb_transient=False, save_artifacts=False, verbose=False)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
