@@ -2356,10 +2356,11 @@ int gm_set_state(gm_handle* h, const double* u, const double* v, const double* p
     const gm::Geometry& g = h->g;
     cudaStream_t st = h->st;
     if (u || v) {
-      // the state is unpack(pack(u, v)): active entries taken, ghosts and inlet rebuilt
-      CK(cudaMemcpyAsync(h->ftmp.p, h->U.p, h->F * sizeof(double), cudaMemcpyDeviceToDevice, st));
-      if (u) CK(cudaMemcpyAsync(h->ftmp.p, dev_in(h, 0, u, g.usize), g.usize * sizeof(double), cudaMemcpyDeviceToDevice, st));
-      if (v) CK(cudaMemcpyAsync(h->ftmp.p + g.usize, dev_in(h, 1, v, g.vsize), g.vsize * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      // the state is unpack(pack(u, v)): active entries taken, ghosts and inlet rebuilt; each
+      // given array is copied straight into the work grid (host arrays by one DMA)
+      if (!(u && v)) CK(cudaMemcpyAsync(h->ftmp.p, h->U.p, h->F * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if (u) CK(cudaMemcpyAsync(h->ftmp.p, u, g.usize * sizeof(double), cudaMemcpyDefault, st));
+      if (v) CK(cudaMemcpyAsync(h->ftmp.p + g.usize, v, g.vsize * sizeof(double), cudaMemcpyDefault, st));
       Gate g0{nullptr, 0, 0};
       launch_copy_active(h->cls_f.p, h->F, h->ftmp.p, h->U.p, g0, st);
       launch_set_inlet(h->cd, h->U.p, false, st);
@@ -2367,7 +2368,7 @@ int gm_set_state(gm_handle* h, const double* u, const double* v, const double* p
       CK(cudaMemsetAsync(h->state_max.p, 0, 2 * sizeof(unsigned long long), st));
       launch_maxabs(h->cd, h->U.p, &h->state_max.p[0], &h->state_max.p[1], g0, st);
     }
-    if (p) CK(cudaMemcpyAsync(h->pout.p, dev_in(h, 2, p, g.psize), g.psize * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if (p) CK(cudaMemcpyAsync(h->pout.p, p, g.psize * sizeof(double), cudaMemcpyDefault, st));
     CK(cudaStreamSynchronize(st));
   });
 }
