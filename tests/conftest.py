@@ -29,6 +29,12 @@ def load_package():
     return module
 
 
+def load_module(name):
+    """A submodule of the package (imported through load_package)."""
+    load_package()
+    return importlib.import_module(f'{PKG_NAME}.{name}')
+
+
 @pytest.fixture(scope='session')
 def pkg():
     return load_package()

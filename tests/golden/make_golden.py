@@ -128,7 +128,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', type=Path, required=True, help='path of the reference checkout')
     ap.add_argument('--skip-large', action='store_true')
-    ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner', 'legacy', 'modal'),
+    ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner', 'legacy', 'modal', 'cutcell'),
                     help='generate one group of fixtures only')
     args = ap.parse_args()
     work = Path(tempfile.mkdtemp(prefix='ghost_golden_'))
@@ -144,6 +144,8 @@ def main():
             run_legacy(work)
         elif args.only == 'modal':
             run_modal(work)
+        elif args.only == 'cutcell':
+            run_cutcell(work)
         else:
             run_all(args)
             run_taylor_green(work)
@@ -151,6 +153,7 @@ def main():
             run_runner(work)
             run_legacy(work)
             run_modal(work)
+            run_cutcell(work)
     finally:
         shutil.rmtree(work, ignore_errors=True)
 
@@ -253,6 +256,118 @@ def run_legacy(work):
         d = mac_engine.calculate_mac_divergence_cpp(u, v, mask, dx, dy)
         out[f'{tag}_div'] = np.array([d[0], d[1], d[2], d[3], d[4]], dtype=float)
     save('legacy_kernels', **out)
+
+
+CUTCELL_CASES = {
+    'cc40x20': dict(nx=40, ny=20, Lx=4., Ly=2., D=1., xc=1., yc=1., nu=0.02, rho=1.),
+    'cc48x30': dict(nx=48, ny=30, Lx=4.8, Ly=2.4, D=1., xc=1.3, yc=1.15, nu=0.01, rho=1.3),
+}
+
+
+def run_cutcell(work):
+    """The reference's cut-cell AB2/CN path (MAC_CylinderFlow(boundary='cut_cell',
+    time_scheme='ab2_cn'), CutCellBoundary of solver/cut_cell_solver.py) on two small grids,
+    one with dx != dy and rho != 1: the geometry (solver/cut_cell_geom.py), the wall, face and
+    viscous stencils (solver/staggered_wall.py), owned volumes, the surface pressure operator,
+    the momentum right-hand side in its advective and viscous forms on seeded fields, a
+    pressure solve, the initial projection, and the fields and diagnostics of steps from a
+    seeded perturbation of the initial state."""
+    from main import MAC_CylinderFlow
+    from cut_cell_solver import calculate_cut_cell_divergence
+    for tag, kw in CUTCELL_CASES.items():
+        s = MAC_CylinderFlow(boundary='cut_cell', time_scheme='ab2_cn', pressure_solver='direct',
+                             verbose=False, **kw)
+        cc, g = s.cc, s.cc.geom
+        out = dict(config=np.array([kw[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu', 'rho')]))
+        for name in ('ax', 'ay', 'volume_fraction', 'cell_type', 'u_volume_fraction', 'v_volume_fraction',
+                     'ax_mid', 'ay_mid', 'ay_u', 'ax_v'):
+            out['geom_' + name] = getattr(g, name)
+        out['u_merge'] = np.array(g.u_merge_list, dtype=np.int64).reshape(-1, 4)
+        out['v_merge'] = np.array(g.v_merge_list, dtype=np.int64).reshape(-1, 4)
+        for c in ('u', 'v'):
+            out[f'{c}_vol'] = getattr(cc, f'{c}_vol')
+            out[f'{c}_vol_eff'] = getattr(cc, f'{c}_vol_eff')
+            out[f'{c}_covered'] = np.asarray(getattr(cc, f'{c}_covered'), dtype=np.int64)
+            out[f'{c}_owner'] = np.asarray(getattr(cc, f'{c}_owner'), dtype=np.int64)
+        # the stencil operators by their action on a seeded field (the CSRs are large)
+        rng = np.random.default_rng(40 if tag == 'cc40x20' else 43)
+        fu = rng.standard_normal(s.u.shape)
+        fv = rng.standard_normal(s.v.shape)
+        fu[g.ax == 0] = 0.
+        fv[g.ay == 0] = 0.
+        field = np.r_[fu.ravel(), fv.ravel()]
+        out['probe_field'] = field
+        w = cc.wall
+        out['wall_rate_action'] = w.rate @ field
+        out['wall_rate_nnz'] = w.rate.nnz
+        for name in ('tx', 'ty', 'ds', 'u_indices', 'v_indices'):
+            out['wall_' + name] = np.asarray(getattr(w, name))
+        for (c, a), st in cc.momentum_faces.items():
+            key = f'mf_{c}{a}'
+            out[key + '_indices'] = np.asarray(st.indices, dtype=np.int64)
+            out[key + '_u_action'] = st.u @ field
+            out[key + '_v_action'] = st.v @ field
+            out[key + '_gradient_action'] = st.gradient @ field
+            out[key + '_nnz'] = np.array([st.u.nnz, st.v.nnz, st.gradient.nnz])
+            out[key + '_patch'] = np.asarray(st.patch, dtype=np.int64)
+            out[key + '_lengths'] = np.asarray(st.lengths)
+            df = cc.diffusion_faces[c, a]
+            out[f'df_{c}{a}_indices'] = np.asarray(df.indices, dtype=np.int64)
+            out[f'df_{c}{a}_gradient_action'] = df.gradient @ field
+        out['surface_points'] = cc.pressure_points
+        out['surface_pressure'] = csr_parts(cc.surface_pressure_operator)
+        out['surface_weights'] = cc.pressure_normal_weights
+        out['init_u'], out['init_v'] = s.u.copy(), s.v.copy()
+        rng = np.random.default_rng(41 if tag == 'cc40x20' else 42)
+        u = rng.standard_normal(s.u.shape)
+        v = rng.standard_normal(s.v.shape)
+        u[g.ax == 0] = 0.
+        v[g.ay == 0] = 0.
+        out['rand_u'], out['rand_v'] = u, v
+        for mode, (nu, adv) in {'adv': (0., True), 'dif': (s.nu, False)}.items():
+            au, av, ru, rv = cc.compute_momentum_rhs(u, v, nu, s.rho, transport='centered', include_advection=adv)
+            out[f'{mode}_au'], out[f'{mode}_av'], out[f'{mode}_ru'], out[f'{mode}_rv'] = au, av, ru, rv
+        prhs = rng.standard_normal(s.p.shape)
+        out['prhs'] = prhs
+        out['psol'] = cc.solve_pressure(prhs, 0.01, s.rho)
+        prand = rng.standard_normal(s.p.shape)
+        out['rand_p'] = prand
+        out['forces_rand'] = np.array(cc.extract_true_surface_forces(u, v, prand, s.nu * s.rho))
+        md, rd, mf, _, _ = calculate_cut_cell_divergence(u, v, g)
+        out['divergence_rand'] = np.array([md, rd, mf])
+        # steps from a seeded perturbation of the projected initial state
+        du = 1e-2 * rng.standard_normal(s.u.shape)
+        dv = 1e-2 * rng.standard_normal(s.v.shape)
+        du[g.ax == 0] = 0.
+        dv[g.ay == 0] = 0.
+        du[:, 0] = 0.
+        dv[[0, -1], :] = 0.
+        s.u += du
+        s.v += dv
+        out['start_u'], out['start_v'] = s.u.copy(), s.v.copy()
+        keys = ('cd', 'cl', 'cd_pressure', 'cd_viscous', 'cl_pressure', 'cl_viscous', 'max_divergence', 'cfl',
+                'momentum_iterations', 'coupled_momentum_residual_linf', 'pressure_solves')
+        fields, scal = [], []
+        for k in range(6):
+            s.solve(n_steps=1, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+            d = s.last_step_diagnostics
+            scal.append([float(d[key]) for key in keys])
+            fields.append((s.u.copy(), s.v.copy(), s.p.copy()))
+        out['step_keys'] = np.array(keys)
+        out['step_scalars'] = np.array(scal)
+        out['step_u'] = np.array([f[0] for f in fields])
+        out['step_v'] = np.array([f[1] for f in fields])
+        out['step_p'] = np.array([f[2] for f in fields])
+        out['history_half_p'] = cc.cn_pressure.copy()
+        out['history_adv'] = cc.cn_advection.copy()
+        if tag == 'cc40x20':
+            # a longer run with the inlet perturbation (solver/main.py:281-286)
+            s.solve(n_steps=60, dt=.002, perturb_transient=True, perturb_duration=0.3, save_artifacts=False,
+                    verbose=False)
+            d = s.last_step_diagnostics
+            out['long_u'], out['long_v'], out['long_p'] = s.u.copy(), s.v.copy(), s.p.copy()
+            out['long_scalars'] = np.array([float(d[key]) for key in keys] + [s.time])
+        save(f'cutcell_{tag}', **out)
 
 
 def run_modal(work):
