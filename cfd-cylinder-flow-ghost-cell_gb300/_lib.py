@@ -30,7 +30,13 @@ SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_las
            'gm_set_learned_preconditioner', 'gm_set_pressure_recorder', 'gm_pressure_recorded',
            'gm_host_alloc', 'gm_host_free', 'gm_solver_info', 'gm_pressure_reconstruction',
            'gm_mac_predictor_rhs', 'gm_mac_corrector', 'gm_mac_forces', 'gm_mac_divergence',
-           'gm_pod_create', 'gm_pod_destroy', 'gm_pod_last_error', 'gm_pod_gram', 'gm_pod_modes', 'gm_batch_shapes')
+           'gm_pod_create', 'gm_pod_destroy', 'gm_pod_last_error', 'gm_pod_gram', 'gm_pod_modes', 'gm_batch_shapes',
+           'gm_cc_create', 'gm_cc_destroy', 'gm_cc_last_error', 'gm_cc_get_sizes', 'gm_cc_get_indices',
+           'gm_cc_get_surface_points', 'gm_cc_set_state', 'gm_cc_get_state', 'gm_cc_set_inlet',
+           'gm_cc_set_history', 'gm_cc_get_history', 'gm_cc_step', 'gm_cc_apply', 'gm_cc_surface_forces',
+           'gm_cc_divergence_stats')
+CC_OP_MOMENTUM_ADVECTION, CC_OP_MOMENTUM_DIFFUSION, CC_OP_ADVECTION, CC_OP_DIFFUSION, CC_OP_H_MATVEC, CC_OP_PROJECT, \
+    CC_OP_PRESSURE_SOLVE = range(1, 8)
 NOALLOC_MAX_CELLS = 1048576
 
 
@@ -64,6 +70,39 @@ class SolveInfo(C.Structure):
     _fields_ = [(n, C.c_double) for n in ('residual_linf', 'residual_relative_l2', 'residual_target_linf',
                                           'roundoff_bound_linf', 'backward_error_linf')] + \
                [(n, C.c_int32) for n in ('iterations', 'refinement_iterations', 'status', 'rank')]
+
+
+class Csr(C.Structure):
+    _fields_ = [('ptr', C.c_void_p), ('col', C.c_void_p), ('val', C.c_void_p)]
+
+
+class CcFaces(C.Structure):
+    _fields_ = [('n_adv', C.c_int64), ('n_adv_points', C.c_int64), ('adv_face', C.c_void_p),
+                ('adv_patch', C.c_void_p), ('adv_u', Csr), ('adv_v', Csr), ('adv_len', C.c_void_p),
+                ('n_dif', C.c_int64), ('dif_face', C.c_void_p), ('dif_grad', Csr)]
+
+
+class CcConfig(C.Structure):
+    _fields_ = [('nx', C.c_int32), ('ny', C.c_int32)] + \
+               [(n, C.c_double) for n in ('Lx', 'Ly', 'D', 'xc', 'yc', 'nu', 'rho', 'U_inf')] + \
+               [('inflow', C.c_int32), ('U_m', C.c_double), ('slip_walls', C.c_int32)] + \
+               [(n, C.c_void_p) for n in ('ax', 'ay', 'ax_mid', 'ay_mid', 'ay_u', 'ax_v', 'cell_type',
+                                          'volume_fraction', 'u_volume_fraction', 'v_volume_fraction', 'u_vol',
+                                          'v_vol', 'u_vol_eff', 'v_vol_eff')] + \
+               [('n_u_merge', C.c_int64), ('n_v_merge', C.c_int64), ('u_merge', C.c_void_p), ('v_merge', C.c_void_p),
+                ('n_u_covered', C.c_int64), ('n_v_covered', C.c_int64)] + \
+               [(n, C.c_void_p) for n in ('u_covered', 'u_owner', 'v_covered', 'v_owner')] + \
+               [('n_wall', C.c_int64), ('wall_rate', Csr)] + \
+               [(n, C.c_void_p) for n in ('wall_tx', 'wall_ty', 'wall_ds', 'wall_u', 'wall_v')] + \
+               [('faces', CcFaces * 4)]
+
+
+class CcStepDiag(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ('time', 'dt', 'max_divergence', 'cfl', 'cd', 'cl', 'cd_pressure',
+                                          'cd_viscous', 'cl_pressure', 'cl_viscous', 'momentum_residual_linf',
+                                          'coupled_momentum_residual_linf', 'predicted_divergence')] + \
+               [('forces', C.c_double * 6)] + \
+               [(n, C.c_int32) for n in ('momentum_iterations', 'pressure_solves', 'status', 'gate')]
 
 
 def _load():
@@ -134,6 +173,21 @@ def _load():
         'gm_pressure_recorded': ([P], I32),
         'gm_host_alloc': ([C.c_size_t, pp], C.c_int),
         'gm_host_free': ([P], C.c_int),
+        'gm_cc_create': ([C.POINTER(CcConfig), pp], C.c_int),
+        'gm_cc_destroy': ([P], C.c_int),
+        'gm_cc_last_error': ([P], C.c_char_p),
+        'gm_cc_get_sizes': ([P, C.POINTER(Sizes)], C.c_int),
+        'gm_cc_get_indices': ([P, P, P, P], C.c_int),
+        'gm_cc_get_surface_points': ([P, P], C.c_int),
+        'gm_cc_set_state': ([P, P, P, P], C.c_int),
+        'gm_cc_get_state': ([P, P, P, P], C.c_int),
+        'gm_cc_set_inlet': ([P, P], C.c_int),
+        'gm_cc_set_history': ([P, I32, P, P, D], C.c_int),
+        'gm_cc_get_history': ([P, C.POINTER(I32), P, P, C.POINTER(D)], C.c_int),
+        'gm_cc_step': ([P, D, I32, D, C.POINTER(CcStepDiag)], C.c_int),
+        'gm_cc_apply': ([P, I32, D, P, P, P], C.c_int),
+        'gm_cc_surface_forces': ([P, P, P, P, D, P], C.c_int),
+        'gm_cc_divergence_stats': ([P, P, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -60,6 +60,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
           '-o', str(BUILD / 'rowgemm.o')]),
         ([nvcc, *ARCH, '-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', *inc, '-c', str(SRC / 'modal.cu'),
           '-o', str(BUILD / 'modal.o')]),
+        ([nvcc, *ARCH, '-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', *inc, '-c', str(SRC / 'cutcell.cu'),
+          '-o', str(BUILD / 'cutcell.o')]),
         # the legacy MAC kernels repeat the reference's arithmetic bit for bit: no FMA contraction
         ([nvcc, *ARCH, '-O3', '-std=c++17', '-lineinfo', '-fmad=false', '-Xcompiler', '-fPIC', *inc, '-c',
           str(SRC / 'legacy.cu'), '-o', str(BUILD / 'legacy.o')]),
@@ -77,7 +79,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     tmp = OUT.with_suffix('.so.tmp')
     link = [nvcc, *ARCH, '-shared', '-o', str(tmp), str(BUILD / 'geometry.o'), str(BUILD / 'kernels.o'),
             str(BUILD / 'ghostmac.o'), str(BUILD / 'noalloc.o'), str(BUILD / 'periodic.o'),
-            str(BUILD / 'unet.o'), str(BUILD / 'rowgemm.o'), str(BUILD / 'legacy.o'), str(BUILD / 'modal.o'), '-lcudart']
+            str(BUILD / 'unet.o'), str(BUILD / 'rowgemm.o'), str(BUILD / 'legacy.o'), str(BUILD / 'modal.o'),
+            str(BUILD / 'cutcell.o'), '-lcudart']
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode:
         raise RuntimeError('link failed:\n' + r.stdout + r.stderr)

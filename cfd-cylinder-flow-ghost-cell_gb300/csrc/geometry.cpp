@@ -815,6 +815,107 @@ bool build_geometry(Geometry& g, int& err_class) {
   return true;
 }
 
+// cut-cell Poisson row of fluid cell c (solver/cut_cell_solver.py:166-214), unit density
+// A coupling to a covered neighbour is left out: the covered cell's row is the identity with a
+// zero right-hand side, so its value is zero and the coupling adds nothing, while the diagonal
+// keeps the face's share as in the assembled matrix.
+static Row cutcell_pressure_row(const Geometry& g, const double* ax, const double* ay, int64_t c) {
+  const int nx = g.nx, ny = g.ny;
+  const int64_t j = c / nx, i = c % nx;
+  const double idx2 = 1.0 / (g.dx * g.dx), idy2 = 1.0 / (g.dy * g.dy);
+  Row r;
+  double diag = 0.0;
+  const double aw = ax[j * (nx + 1) + i], ae = ax[j * (nx + 1) + i + 1];
+  const double as = ay[j * nx + i], an = ay[(j + 1) * nx + i];
+  auto couple = [&](int64_t nb, double k) {
+    if (g.act_p[nb]) r.emplace_back(nb, k);
+    diag -= k;
+  };
+  if (i > 0 && aw > 0.0) couple(c - 1, aw * idx2);
+  if (i == nx - 1) diag -= 2.0 * ae * idx2;
+  else if (ae > 0.0) couple(c + 1, ae * idx2);
+  if (j > 0 && as > 0.0) couple(c - nx, as * idy2);
+  if (j < ny - 1 && an > 0.0) couple(c + nx, an * idy2);
+  r.emplace_back(c, diag);
+  return r;
+}
+
+bool build_cutcell_geometry(Geometry& g, const double* ax, const double* ay, const int32_t* cell_type,
+                            int& err_class) {
+  err_class = 1;
+  const int nx = g.nx, ny = g.ny;
+  if (nx < 4 || ny < 4) { g.error = "nx and ny must be integers >= 4"; return false; }
+  for (double v : {g.Lx, g.Ly, g.D, g.nu, g.rho, g.U_inf})
+    if (!(std::isfinite(v) && v > 0)) { g.error = "Domain lengths, D, nu, rho and U_inf must be finite and positive"; return false; }
+  if (g.inflow != 0 && g.inflow != 1) { g.error = "inflow must be uniform or parabolic"; return false; }
+  g.dx = g.Lx / nx;
+  g.dy = g.Ly / ny;
+  if (g.inflow == 1) { g.U_m = g.U_m > 0 ? g.U_m : 1.5 * g.U_inf; g.U_ref = (2.0 / 3.0) * g.U_m; }
+  else { g.U_m = g.U_inf; g.U_ref = g.U_inf; }
+  g.R = g.D / 2.0;
+  g.usize = (int64_t)ny * (nx + 1);
+  g.vsize = (int64_t)(ny + 1) * nx;
+  g.psize = (int64_t)ny * nx;
+  g.u_inlet.assign(ny, 0.0);
+  for (int j = 0; j < ny; ++j) {
+    double y = (j + 0.5) * g.dy;
+    g.u_inlet[j] = g.inflow == 1 ? (((4.0 * g.U_m) * y) * (g.Ly - y)) / (g.Ly * g.Ly) : g.U_inf;
+  }
+  g.xu.resize(nx + 1); g.yu.resize(ny); g.xv.resize(nx); g.yv.resize(ny + 1);
+  for (int i = 0; i <= nx; ++i) g.xu[i] = i * g.dx;
+  for (int j = 0; j < ny; ++j) g.yu[j] = (j + 0.5) * g.dy;
+  for (int i = 0; i < nx; ++i) g.xv[i] = (i + 0.5) * g.dx;
+  for (int j = 0; j <= ny; ++j) g.yv[j] = j * g.dy;
+  g.mask.assign(g.psize, 0);
+  g.act_u.assign(g.usize, 0); g.act_v.assign(g.vsize, 0); g.act_p.assign(g.psize, 0);
+  for (int64_t f = 0; f < g.usize; ++f) g.act_u[f] = (f % (nx + 1)) != 0 && ax[f] > 0.0;
+  for (int64_t f = 0; f < g.vsize; ++f) { int64_t j = f / nx; g.act_v[f] = j != 0 && j != ny && ay[f] > 0.0; }
+  for (int64_t c = 0; c < g.psize; ++c) {
+    g.act_p[c] = cell_type[c] != -1;
+    g.mask[c] = cell_type[c] == -1;
+  }
+  auto labels = [](const std::vector<uint8_t>& a, std::vector<int64_t>& ids, std::vector<int64_t>& lab) {
+    ids.clear(); lab.assign(a.size(), -1);
+    for (size_t f = 0; f < a.size(); ++f) if (a[f]) { lab[f] = (int64_t)ids.size(); ids.push_back((int64_t)f); }
+  };
+  labels(g.act_u, g.ui, g.lab_u);
+  labels(g.act_v, g.vi, g.lab_v);
+  labels(g.act_p, g.pi, g.lab_p);
+  g.ghost_of_u.assign(g.usize, -1);
+  g.ghost_of_v.assign(g.vsize, -1);
+  g.ghost_of_p.assign(g.psize, -1);
+  g.gu_rows.clear(); g.gv_rows.clear(); g.gp_rows.clear();
+  g.gu = Csr(); g.gv = Csr(); g.gp = Csr();
+  // unit density (g.rho = 1 from here on): the rectangle is the plain Laplacian and
+  // A phi = rhs with rhs = (rho/dt) div, the caller's rho entering through the right-hand side
+  g.rho = 1.0;
+  make_rect(g.rect_p, 0, nx, ny, g.dx, g.dy, g.nu, 0.0, 1.0);
+  g.a_nnz_row.assign(g.psize, 0);
+  schur_setup(g, g.rect_p, 0, g.act_p, [&](int64_t c) { return cutcell_pressure_row(g, ax, ay, c); }, g.a_rows,
+              g.a_irr, g.schur_p_rows, g.schur_p_c, g.schur_p_tol, &g.a_nnz_row);
+  if (g.schur_p_rows.size() > 2048) { g.error = "Cut-cell inverse exceeds the bounded boundary-row rank"; return false; }
+  // surface quadrature points and point-pressure reconstruction (solver/cut_cell_solver.py:25-77)
+  const double h_min = std::min(g.dx, g.dy);
+  const int count = std::max(360, 4 * (int)std::ceil(2 * PI * g.R / h_min));
+  g.n_surface = count;
+  g.surf_y.resize(count); g.surf_x.resize(count);
+  g.normal_wx.resize(count); g.normal_wy.resize(count); g.normal_x.resize(count); g.normal_y.resize(count);
+  const double step = 2 * PI / count, wscale = 2 * PI * g.R / count;
+  for (int k = 0; k < count; ++k) {
+    const double th = k * step, c = std::cos(th), s = std::sin(th);
+    g.surf_y[k] = g.yc + g.R * s;
+    g.surf_x[k] = g.xc + g.R * c;
+    g.normal_x[k] = c;
+    g.normal_y[k] = s;
+    g.normal_wx[k] = c * wscale;
+    g.normal_wy[k] = s * wscale;
+  }
+  if (!pressure_reconstruction(g, g.surf_y, g.surf_x, g.surf_p, g.error)) return false;
+  g.dudn = Csr(); g.dvdn = Csr();
+  err_class = 0;
+  return true;
+}
+
 bool build_helmholtz(const Geometry& g, double dt, HelmholtzSetup& hs, int& err_class, std::string& err) {
   err_class = 1;
   hs.dt = dt;

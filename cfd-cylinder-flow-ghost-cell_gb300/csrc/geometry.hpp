@@ -87,6 +87,17 @@ struct HelmholtzSetup {
 bool build_geometry(Geometry& g, int& err_class);
 bool build_helmholtz(const Geometry& g, double dt, HelmholtzSetup& hs, int& err_class, std::string& err);
 
+// Pressure side of a cut-cell case (solver/cut_cell_solver.py:132-216, 376-400): the cut-cell
+// Poisson operator over the fluid and cut cells (face-aperture-weighted five-point rows, the
+// outlet Dirichlet row, covered cells decoupled) as irregular rows against the rectangle of
+// the pressure grid with its boundary Schur rows, the active face maps of the u / v unknowns
+// (ax[:, 1:] > 0, ay[1:-1, :] > 0), the inlet profile and the surface quadrature points with
+// their point-pressure reconstruction.  The density enters through the caller's right-hand
+// side: the operator is built with unit density and g.rho is set to 1.  ax: ny x (nx+1), ay: (ny+1) x nx, cell_type:
+// ny x nx (1 fluid, 0 cut, -1 covered).
+bool build_cutcell_geometry(Geometry& g, const double* ax, const double* ay, const int32_t* cell_type,
+                            int& err_class);
+
 // Quadratic point-pressure reconstruction at the points (py[k], px[k]) (solver/cut_cell_solver.py:25-55):
 // rows = points, columns = grid flat p indices; false with err set for invalid points.
 bool pressure_reconstruction(const Geometry& g, const std::vector<double>& py, const std::vector<double>& px,

@@ -19,6 +19,7 @@
 #include "geometry.hpp"
 #include "fftplan.hpp"
 #include "kernels.cuh"
+#include "internal.hpp"
 
 using namespace gmk;
 
@@ -1381,6 +1382,7 @@ gm_handle::GmresExec& gmres_graph(gm_handle* h, const double* b, double* x) {
   launch_multiaxpy(vec(V, 1), n, 1, h->gone.p, -1.0, 1.0, vec(V, 0), n, sb1);
   launch_multidot(vec(V, 0), n, 1, vec(V, 0), n, h->gpart.p, h->gbeta.p, sb1);
   GmresHandles hs{};
+  hs.count = m;
   cudaGraph_t cyc_graph;
   CK(cudaStreamGetCaptureInfo(sb1, &cs, nullptr, &cyc_graph, nullptr, nullptr, nullptr));
   for (int j = 0; j < m; ++j) CK(cudaGraphConditionalHandleCreate(&hs.step[j], cyc_graph, 0, 0));
@@ -2067,6 +2069,107 @@ void initial_state(gm_handle* h) {
   CK(cudaStreamSynchronize(h->st));
 }
 
+// Device side of a handle whose geometry is built: streams, geometry and operator uploads,
+// work arrays, the pressure rectangle tables and its boundary Schur data.
+void create_device(gm_handle* H) {
+  const gm::Geometry& g = H->g;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); throw CudaError("no CUDA device"); }
+  CK(cudaGetDevice(&H->device));
+  int optin = 0;
+  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, H->device));
+  int dyn = configure_kernels(optin);
+  cudaGetLastError();
+  if (dyn < 48 * 1024) throw CudaError("cannot enable large shared memory for the transform kernels");
+  H->smem_optin = (size_t)dyn;
+  CK(cudaStreamCreateWithFlags(&H->st, cudaStreamNonBlocking));
+  cudaStream_t st = H->st;
+  H->F = g.usize + g.vsize;
+  H->Pn = g.psize;
+  build_class_maps(H);
+  H->mask.upload(g.mask, st);
+  H->inlet.upload(g.u_inlet, st);
+  // ghost stencils: u rows and v rows on the face grid
+  {
+    gm::Csr f;
+    std::vector<int64_t> rows;
+    for (size_t r = 0; r < g.gu_rows.size(); ++r) {
+      rows.push_back(g.gu_rows[r]);
+      for (int64_t e = g.gu.ptr[r]; e < g.gu.ptr[r + 1]; ++e) { f.col.push_back(g.gu.col[e]); f.val.push_back(g.gu.val[e]); }
+      f.ptr.push_back((int64_t)f.col.size());
+    }
+    for (size_t r = 0; r < g.gv_rows.size(); ++r) {
+      rows.push_back(g.usize + g.gv_rows[r]);
+      for (int64_t e = g.gv.ptr[r]; e < g.gv.ptr[r + 1]; ++e) { f.col.push_back(g.usize + g.gv.col[e]); f.val.push_back(g.gv.val[e]); }
+      f.ptr.push_back((int64_t)f.col.size());
+    }
+    upload_csr(H->gf, rows, f, st);
+  }
+  upload_csr(H->gp, g.gp_rows, g.gp, st);
+  upload_csr(H->irr[0], g.a_rows, g.a_irr, st);
+  upload_row_index(H->irr[0], g.a_rows, g.psize, st);
+  H->a_nnz.upload(g.a_nnz_row, st);
+  H->sp_ptr.upload(g.surf_p.ptr, st); H->sp_col.upload(g.surf_p.col, st); H->sp_val.upload(g.surf_p.val, st);
+  H->su_ptr.upload(g.dudn.ptr, st); H->su_col.upload(g.dudn.col, st); H->su_val.upload(g.dudn.val, st);
+  H->sv_ptr.upload(g.dvdn.ptr, st); H->sv_col.upload(g.dvdn.col, st); H->sv_val.upload(g.dvdn.val, st);
+  H->nwx.upload(g.normal_wx, st); H->nwy.upload(g.normal_wy, st);
+  H->nxx.upload(g.normal_x, st); H->nyy.upload(g.normal_y, st);
+  H->surf_part.alloc(4 * (size_t)std::max(1, g.n_surface));
+  H->surf_ticket.alloc(1);
+  H->surf_ticket.zero(st);
+  H->d_ui.upload(g.ui, st); H->d_vi.upload(g.vi, st); H->d_pi.upload(g.pi, st);
+  for (DBuf<double>* b : {&H->U, &H->Unext, &H->hist, &H->now, &H->rhs, &H->star, &H->fres, &H->ffirst, &H->fw2,
+                          &H->fmid, &H->fhalf, &H->faction, &H->fproj, &H->fproj2, &H->ftmp}) {
+    b->alloc(H->F);
+    b->zero(st);
+  }
+  for (DBuf<double>* b : {&H->phalf, &H->phalf_next, &H->pout, &H->prhs, &H->pphi, &H->pres, &H->pfirst, &H->pw2,
+                          &H->pinc, &H->ptmp}) {
+    b->alloc(H->Pn);
+    b->zero(st);
+  }
+  H->spectral.alloc(std::max<int64_t>(H->Pn, (int64_t)g.ny * g.nx));
+  H->spectral_b.alloc(H->spectral.n);
+  if (H->precision == 1) {
+    H->spectral32.alloc(H->spectral.n);
+    H->spectral32_b.alloc(H->spectral.n);
+    H->pres32.alloc(H->Pn);
+    H->pres32.zero(st);
+    H->fres32.alloc(H->F);
+    H->fres32.zero(st);
+    H->U32.alloc(H->F);
+    H->P32.alloc(H->Pn);
+    H->ffirst32.alloc(H->F);
+    H->ffirst32.zero(st);
+    H->pfirst32.alloc(H->Pn);
+    H->pfirst32.zero(st);
+  }
+  H->ctl.alloc(1);
+  H->ctl.zero(st);
+  H->ring.alloc(gm_handle::RING_CAP);
+  H->ridx.alloc(1);
+  H->ridx.zero(st);
+  H->counter.alloc(1);
+  H->counter.zero(st);
+  CK(cudaMallocHost(&H->host_ring, gm_handle::RING_CAP * sizeof(StepCtl)));
+  CK(cudaStreamCreateWithFlags(&H->st_body, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&H->st2, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&H->st2_body, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&H->ev_fork, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&H->ev_join, cudaEventDisableTiming));
+  if (const char* e = std::getenv("GHOSTMAC_NO_GRAPHS")) H->use_graphs = !(e[0] == '1');
+  if (g.pressure_solver == 1) H->use_graphs = false;  // GMRES decides its iterations on the host
+
+  H->state_max.alloc(2);
+  H->state_max.zero(st);
+  CK(cudaMallocHost(&H->host_ctl, sizeof(StepCtl)));
+  fill_case_dev(H);
+  build_rect_tables(H, H->rp, 0, 0.0);
+  build_schur(H, H->rp, g.schur_p_rows, g.schur_p_c, H->pw2.p);
+  build_row_gemm(H, H->rp);
+  CK(cudaMemsetAsync(H->pw2.p, 0, H->Pn * sizeof(double), st));
+}
+
 }  // namespace
 
 // =============================================================================
@@ -2095,101 +2198,7 @@ int gm_create(const gm_config* cfg, gm_handle** out) {
   if (g.usize + g.vsize >= (int64_t(1) << 31)) { g_create_error = "grids of 2^31 or more faces are not supported"; return GM_EVALUE; }
   gm_handle* H = h.get();
   int rc = run_guarded(nullptr, [&] {
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); throw CudaError("no CUDA device"); }
-    CK(cudaGetDevice(&H->device));
-    int optin = 0;
-    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, H->device));
-    int dyn = configure_kernels(optin);
-    cudaGetLastError();
-    if (dyn < 48 * 1024) throw CudaError("cannot enable large shared memory for the transform kernels");
-    H->smem_optin = (size_t)dyn;
-    CK(cudaStreamCreateWithFlags(&H->st, cudaStreamNonBlocking));
-    cudaStream_t st = H->st;
-    H->F = g.usize + g.vsize;
-    H->Pn = g.psize;
-    build_class_maps(H);
-    H->mask.upload(g.mask, st);
-    H->inlet.upload(g.u_inlet, st);
-    // ghost stencils: u rows and v rows on the face grid
-    {
-      gm::Csr f;
-      std::vector<int64_t> rows;
-      for (size_t r = 0; r < g.gu_rows.size(); ++r) {
-        rows.push_back(g.gu_rows[r]);
-        for (int64_t e = g.gu.ptr[r]; e < g.gu.ptr[r + 1]; ++e) { f.col.push_back(g.gu.col[e]); f.val.push_back(g.gu.val[e]); }
-        f.ptr.push_back((int64_t)f.col.size());
-      }
-      for (size_t r = 0; r < g.gv_rows.size(); ++r) {
-        rows.push_back(g.usize + g.gv_rows[r]);
-        for (int64_t e = g.gv.ptr[r]; e < g.gv.ptr[r + 1]; ++e) { f.col.push_back(g.usize + g.gv.col[e]); f.val.push_back(g.gv.val[e]); }
-        f.ptr.push_back((int64_t)f.col.size());
-      }
-      upload_csr(H->gf, rows, f, st);
-    }
-    upload_csr(H->gp, g.gp_rows, g.gp, st);
-    upload_csr(H->irr[0], g.a_rows, g.a_irr, st);
-    upload_row_index(H->irr[0], g.a_rows, g.psize, st);
-    H->a_nnz.upload(g.a_nnz_row, st);
-    H->sp_ptr.upload(g.surf_p.ptr, st); H->sp_col.upload(g.surf_p.col, st); H->sp_val.upload(g.surf_p.val, st);
-    H->su_ptr.upload(g.dudn.ptr, st); H->su_col.upload(g.dudn.col, st); H->su_val.upload(g.dudn.val, st);
-    H->sv_ptr.upload(g.dvdn.ptr, st); H->sv_col.upload(g.dvdn.col, st); H->sv_val.upload(g.dvdn.val, st);
-    H->nwx.upload(g.normal_wx, st); H->nwy.upload(g.normal_wy, st);
-    H->nxx.upload(g.normal_x, st); H->nyy.upload(g.normal_y, st);
-    H->surf_part.alloc(4 * (size_t)std::max(1, g.n_surface));
-    H->surf_ticket.alloc(1);
-    H->surf_ticket.zero(st);
-    H->d_ui.upload(g.ui, st); H->d_vi.upload(g.vi, st); H->d_pi.upload(g.pi, st);
-    for (DBuf<double>* b : {&H->U, &H->Unext, &H->hist, &H->now, &H->rhs, &H->star, &H->fres, &H->ffirst, &H->fw2,
-                            &H->fmid, &H->fhalf, &H->faction, &H->fproj, &H->fproj2, &H->ftmp}) {
-      b->alloc(H->F);
-      b->zero(st);
-    }
-    for (DBuf<double>* b : {&H->phalf, &H->phalf_next, &H->pout, &H->prhs, &H->pphi, &H->pres, &H->pfirst, &H->pw2,
-                            &H->pinc, &H->ptmp}) {
-      b->alloc(H->Pn);
-      b->zero(st);
-    }
-    H->spectral.alloc(std::max<int64_t>(H->Pn, (int64_t)g.ny * g.nx));
-    H->spectral_b.alloc(H->spectral.n);
-    if (H->precision == 1) {
-      H->spectral32.alloc(H->spectral.n);
-      H->spectral32_b.alloc(H->spectral.n);
-      H->pres32.alloc(H->Pn);
-      H->pres32.zero(st);
-      H->fres32.alloc(H->F);
-      H->fres32.zero(st);
-      H->U32.alloc(H->F);
-      H->P32.alloc(H->Pn);
-      H->ffirst32.alloc(H->F);
-      H->ffirst32.zero(st);
-      H->pfirst32.alloc(H->Pn);
-      H->pfirst32.zero(st);
-    }
-    H->ctl.alloc(1);
-    H->ctl.zero(st);
-    H->ring.alloc(gm_handle::RING_CAP);
-    H->ridx.alloc(1);
-    H->ridx.zero(st);
-    H->counter.alloc(1);
-    H->counter.zero(st);
-    CK(cudaMallocHost(&H->host_ring, gm_handle::RING_CAP * sizeof(StepCtl)));
-    CK(cudaStreamCreateWithFlags(&H->st_body, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&H->st2, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&H->st2_body, cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&H->ev_fork, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&H->ev_join, cudaEventDisableTiming));
-    if (const char* e = std::getenv("GHOSTMAC_NO_GRAPHS")) H->use_graphs = !(e[0] == '1');
-    if (g.pressure_solver == 1) H->use_graphs = false;  // GMRES decides its iterations on the host
-
-    H->state_max.alloc(2);
-    H->state_max.zero(st);
-    CK(cudaMallocHost(&H->host_ctl, sizeof(StepCtl)));
-    fill_case_dev(H);
-    build_rect_tables(H, H->rp, 0, 0.0);
-    build_schur(H, H->rp, g.schur_p_rows, g.schur_p_c, H->pw2.p);
-    build_row_gemm(H, H->rp);
-    CK(cudaMemsetAsync(H->pw2.p, 0, H->Pn * sizeof(double), st));
+    create_device(H);
     initial_state(H);
   });
   if (rc != GM_OK) return rc;
@@ -3497,3 +3506,56 @@ int gm_batch_step(gm_batch* b, double dt, int32_t n_steps, int64_t first_step_in
 }
 
 }  // extern "C"
+
+// =============================================================================
+// pressure-only handles for the cut-cell path (internal.hpp)
+// =============================================================================
+namespace gmi {
+
+int pressure_create(gm::Geometry&& g, gm_handle** out, std::string& err) {
+  *out = nullptr;
+  if (g.nx % 2 != 0) { err = "odd nx is not supported by the type-IV transform"; return GM_ENOTIMPL; }
+  if (g.usize + g.vsize >= (int64_t(1) << 31)) { err = "grids of 2^31 or more faces are not supported"; return GM_EVALUE; }
+  auto h = std::make_unique<gm_handle>();
+  h->g = std::move(g);
+  h->g.pressure_solver = 0;
+  h->precision = 0;
+  h->nchk = 3;
+  gm_handle* H = h.get();
+  int rc = run_guarded(H, [&] { create_device(H); });
+  if (rc != GM_OK) {
+    err = H->err;
+    gm_destroy(h.release());
+    return rc;
+  }
+  *out = h.release();
+  return GM_OK;
+}
+
+void pressure_destroy(gm_handle* h) { gm_destroy(h); }
+const gm::Geometry& geometry(const gm_handle* h) { return h->g; }
+cudaStream_t stream(gm_handle* h) { return h->st; }
+cudaStream_t body_stream(gm_handle* h, int level) { return level == 0 ? h->st_body : h->st2_body; }
+void set_capturing(gm_handle* h, bool on) { h->capturing = on; }
+
+void pressure_solve(gm_handle* h, const double* b, double* x, int slot) {
+  schur_solve(h, 0, h->rp, 0, 0.0, b, x, h->pres.p, h->pfirst.p, h->pw2.p, slot);
+  launch_gate_pressure(h->ctl.p, slot, h->nchk, h->st);
+}
+
+const double* pressure_residual(gm_handle* h) { return h->pres.p; }
+StepCtl* control(gm_handle* h) { return h->ctl.p; }
+
+int check(gm_handle* h, const char* where, std::string& err) {
+  int rc = run_guarded(h, [&] { check_ctl(h, where); });
+  if (rc != GM_OK) err = h->err;
+  return rc;
+}
+
+int64_t schur_rank(const gm_handle* h) { return h->rp.rank; }
+
+SurfaceCsr surface(const gm_handle* h) {
+  return SurfaceCsr{h->g.n_surface, h->sp_ptr.p, h->sp_col.p, h->sp_val.p, h->nwx.p, h->nwy.p};
+}
+
+}  // namespace gmi

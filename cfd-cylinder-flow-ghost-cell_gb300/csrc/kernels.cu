@@ -2441,8 +2441,9 @@ void launch_cfl_screen(StepCtl* ctl, const unsigned long long* umax, const unsig
 // step, its condition set by the previous step).  The arithmetic is that of the host loop it
 // replaces, in the same order.
 // ---------------------------------------------------------------------------
-__global__ void k_gm_init(GmresDev* gd, const double* __restrict__ bn2, cudaGraphConditionalHandle cycle) {
-  gd->tol = fmax(1e-12 * sqrt(bn2[0]), 1e-12);
+__global__ void k_gm_init(GmresDev* gd, const double* __restrict__ bn2, cudaGraphConditionalHandle cycle,
+                          double rtol, double atol) {
+  gd->tol = fmax(rtol * sqrt(bn2[0]), atol);
   gd->iterations = 0;
   gd->converged = 0;
   gd->stop = 0;
@@ -2464,7 +2465,7 @@ __global__ void k_gm_cycle_begin(GmresDev* gd, const double* __restrict__ beta2,
     gd->g[0] = beta;
     gd->hscale = 1.0 / beta;
   }
-  for (int j = 0; j < GmresDev::M; ++j) cudaGraphSetConditional(hs.step[j], (j == 0 && go) ? 1u : 0u);
+  for (int j = 0; j < hs.count; ++j) cudaGraphSetConditional(hs.step[j], (j == 0 && go) ? 1u : 0u);
 }
 // w *= hscale (the new basis vector, or V_0 at the start of a cycle)
 __global__ void k_gm_scale(double* __restrict__ w, int64_t n, const GmresDev* __restrict__ gd) {
@@ -2530,9 +2531,10 @@ __global__ void k_multiaxpy_dev(const double* __restrict__ V, int64_t ld, const 
     y[t] = 1.0 * y[t] + 1.0 * acc;
   }
 }
-void launch_gm_init(GmresDev* gd, const double* bn2, cudaGraphConditionalHandle cycle, cudaStream_t st) {
+void launch_gm_init(GmresDev* gd, const double* bn2, cudaGraphConditionalHandle cycle, cudaStream_t st, double rtol,
+                    double atol) {
   note_launch();
-  k_gm_init<<<1, 1, 0, st>>>(gd, bn2, cycle);
+  k_gm_init<<<1, 1, 0, st>>>(gd, bn2, cycle, rtol, atol);
 }
 void launch_gm_cycle_begin(GmresDev* gd, const double* beta2, const GmresHandles& hs, cudaStream_t st) {
   note_launch();

@@ -268,10 +268,13 @@ struct GmresDev {             // the state of one solve, in device memory
   double tol, hscale;         // stop tolerance; scale of the next basis vector
   int jend, cycle, iterations, converged, stop;
 };
-struct GmresHandles {         // the conditions of the M Arnoldi-step IF nodes of a cycle
+struct GmresHandles {         // the conditions of the Arnoldi-step IF nodes of a cycle (count <= M)
   cudaGraphConditionalHandle step[GmresDev::M];
+  int count;
 };
-void launch_gm_init(GmresDev* gd, const double* bn2, cudaGraphConditionalHandle cycle, cudaStream_t st);
+// stop tolerance max(rtol ||b||, atol) (bn2 = ||b||^2 on the device)
+void launch_gm_init(GmresDev* gd, const double* bn2, cudaGraphConditionalHandle cycle, cudaStream_t st,
+                    double rtol = 1e-12, double atol = 1e-12);
 void launch_gm_cycle_begin(GmresDev* gd, const double* beta2, const GmresHandles& hs, cudaStream_t st);
 void launch_gm_scale(double* w, int64_t n, const GmresDev* gd, cudaStream_t st);
 void launch_gm_step_end(GmresDev* gd, int j, const double* d1, const double* d2, const double* wn2,

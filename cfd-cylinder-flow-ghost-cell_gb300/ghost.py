@@ -259,7 +259,17 @@ def _solve_dict(info):
 
 
 class MAC_CylinderFlow:
-    """Ghost-cell AB2/CN cylinder flow on the GPU (solver/main.py:19-617, ghost_cell/ab2_cn path)."""
+    """Ghost-cell AB2/CN cylinder flow on the GPU (solver/main.py:19-617, ghost_cell/ab2_cn path).
+    boundary='cut_cell' (with time_scheme='ab2_cn') constructs the cut-cell path instead
+    (cutcell.CutCellFlow)."""
+
+    def __new__(cls, *args, **kwargs):
+        import inspect
+        bound = inspect.signature(cls.__init__).bind_partial(None, *args, **kwargs).arguments
+        if bound.get('boundary') == 'cut_cell':
+            from .cutcell import CutCellFlow
+            return CutCellFlow(*args, **kwargs)
+        return super().__new__(cls)
 
     def __init__(self, nx=400, ny=100, Lx=20.0, Ly=5.0, D=1.0, xc=5.0, yc=2.5,
                  nu=0.01, rho=1.0, U_inf=1.0, inflow='uniform', U_m=None,

@@ -370,6 +370,121 @@ int gm_solver_info(const gm_handle* h, int32_t* jacobi_iters, double* jacobi_rho
  * While timing is on, steps run launch by launch (no graphs). */
 int gm_kernel_timing(int32_t kernel_class, int32_t enable, double* total_ms, int64_t* count, double* bytes);
 
+/* --- cut-cell AB2/CN path ---------------------------------------------------------------
+ * One gm_cc handle holds one cut-cell (embedded-boundary) cylinder case: MAC_CylinderFlow
+ * (boundary='cut_cell', time_scheme='ab2_cn') with CutCellBoundary.advance_ab2_cn
+ * (solver/cut_cell_solver.py:370-1015).  The geometry-dependent data (fractions, merge tables,
+ * owned volumes, the wall and curved-face stencils of solver/cut_cell_geom.py and
+ * solver/staggered_wall.py) come from the caller's host setup; the pressure operator, its
+ * boundary-corrected inverse, the surface quadrature and every step run in the library.
+ * Field layout as for gm_handle; the packed unknown vector q holds the open u faces of columns
+ * 1..nx then the open v faces of rows 1..ny-1 (advance_ab2_cn's pack, :962-971). */
+typedef struct gm_cc gm_cc;
+
+/* a CSR matrix over the concatenated face field [u.ravel(), v.ravel()] (host arrays) */
+typedef struct gm_csr {
+  const int64_t* ptr; /* rows + 1 */
+  const int64_t* col;
+  const double* val;
+} gm_csr;
+
+/* Curved faces of one flux family (solver/staggered_wall.py:63-131, 203-232). */
+typedef struct gm_cc_faces {
+  /* advective fluxes from the fit: flux-array flat index per face, the Gauss points of all
+   * faces (grouped by face, in order: adv_patch[p] = face of point p), their u and v value rows
+   * and quadrature weights */
+  int64_t n_adv, n_adv_points;
+  const int64_t* adv_face;
+  const int64_t* adv_patch;
+  gm_csr adv_u, adv_v;
+  const double* adv_len;
+  /* viscous fluxes: flux-array flat index per face and its gradient row (the flux is
+   * rho nu gradient . field) */
+  int64_t n_dif;
+  const int64_t* dif_face;
+  gm_csr dif_grad;
+} gm_cc_faces;
+
+typedef struct gm_cc_config {
+  int32_t nx, ny;
+  double Lx, Ly, D, xc, yc, nu, rho, U_inf;
+  int32_t inflow;  /* 0 uniform, 1 parabolic */
+  double U_m;      /* parabolic peak; <= 0 selects 1.5*U_inf */
+  int32_t slip_walls;
+  /* geometry (solver/cut_cell_geom.py), C order */
+  const double* ax;                /* ny x nx+1 open fractions of the u faces */
+  const double* ay;                /* ny+1 x nx of the v faces */
+  const double* ax_mid;            /* ny x nx */
+  const double* ay_mid;            /* ny x nx */
+  const double* ay_u;              /* ny+1 x nx+1 */
+  const double* ax_v;              /* ny+1 x nx+1 */
+  const int32_t* cell_type;        /* ny x nx: 1 fluid, 0 cut, -1 covered */
+  const double* volume_fraction;   /* ny x nx */
+  const double* u_volume_fraction; /* ny x nx+1 */
+  const double* v_volume_fraction; /* ny+1 x nx */
+  /* owned volumes and merged volumes (solver/staggered_wall.py:264-299, cut_cell_solver.py:456-468) */
+  const double *u_vol, *v_vol, *u_vol_eff, *v_vol_eff;
+  int64_t n_u_merge, n_v_merge;
+  const int64_t* u_merge;          /* n_u_merge x 4: js, is, jm, im */
+  const int64_t* v_merge;
+  int64_t n_u_covered, n_v_covered;
+  const int64_t *u_covered, *u_owner, *v_covered, *v_owner; /* flat indices of the u / v grid */
+  /* wall Gauss points (solver/staggered_wall.py:235-261) */
+  int64_t n_wall;
+  gm_csr wall_rate;
+  const double *wall_tx, *wall_ty, *wall_ds;
+  const int64_t *wall_u, *wall_v;  /* owning u / v face (flat index of its grid) */
+  gm_cc_faces faces[4];            /* families (u,x) F_xx, (u,y) F_xy, (v,x) F_yx, (v,y) F_yy */
+} gm_cc_config;
+
+/* Per-step diagnostics of the cut-cell step (solver/main.py:416-424, time_integration.py:143-145,
+ * cut_cell_solver.py:1008-1013). */
+typedef struct gm_cc_step_diag {
+  double time, dt, max_divergence, cfl;
+  double cd, cl, cd_pressure, cd_viscous, cl_pressure, cl_viscous;
+  double momentum_residual_linf, coupled_momentum_residual_linf, predicted_divergence;
+  double forces[6];                /* fx, fy, fx_p, fy_p, fx_v, fy_v */
+  int32_t momentum_iterations;     /* GMRES iterations of the CN solve */
+  int32_t pressure_solves;
+  int32_t status;                  /* 0 ok, else the GM_E* class of the failure */
+  int32_t gate;                    /* GM_GATE_* of the failure, 0 if none */
+} gm_cc_step_diag;
+
+/* Replaces the cut_cell/ab2_cn branch of MAC_CylinderFlow.__init__ (solver/main.py:140-240):
+ * pressure operator and inverse, inlet profile, initial field and its projection. */
+int gm_cc_create(const gm_cc_config* cfg, gm_cc** out);
+int gm_cc_destroy(gm_cc* c);
+/* message of the last error on c (or of the last failed gm_cc_create when c is NULL) */
+const char* gm_cc_last_error(const gm_cc* c);
+int gm_cc_get_sizes(const gm_cc* c, gm_sizes* out);
+/* active flat indices of the u, v and pressure grids (the packed order of q) */
+int gm_cc_get_indices(const gm_cc* c, int64_t* ui, int64_t* vi, int64_t* pi);
+/* surface quadrature points (y, x) (build_surface_pressure_quadrature, cut_cell_solver.py:70-77) */
+int gm_cc_get_surface_points(const gm_cc* c, double* yx);
+int gm_cc_set_state(gm_cc* c, const double* u, const double* v, const double* p);
+int gm_cc_get_state(gm_cc* c, double* u, double* v, double* p);
+int gm_cc_set_inlet(gm_cc* c, const double* u_inlet);
+/* restart history of advance_ab2_cn: cn_advection (packed), cn_pressure (p grid), cn_dt */
+int gm_cc_set_history(gm_cc* c, int32_t has_history, const double* prev_adv, const double* half_p, double prev_dt);
+int gm_cc_get_history(gm_cc* c, int32_t* has_history, double* prev_adv, double* half_p, double* prev_dt);
+/* n_steps of advance_ab2_cn with the step gates of solver/main.py:416-424; diag (may be NULL)
+ * receives one record per step.  A failed gate stops the loop after that step with its class. */
+int gm_cc_step(gm_cc* c, double dt, int32_t n_steps, double start_time, gm_cc_step_diag* diag);
+
+#define GM_CC_OP_MOMENTUM_ADVECTION 1 /* (u|v grids) -> a (u|v), y2: rhs; compute_momentum_rhs(u, v, 0, rho) :790-957 */
+#define GM_CC_OP_MOMENTUM_DIFFUSION 2 /* same with nu = param and include_advection=False */
+#define GM_CC_OP_ADVECTION 3          /* q -> advection(q) of advance_ab2_cn :972-974 */
+#define GM_CC_OP_DIFFUSION 4          /* q -> diffusion(q) :975-978 */
+#define GM_CC_OP_H_MATVEC 5           /* q -> q - dt/2 (diffusion(q) - diffusion(0)), dt = param */
+#define GM_CC_OP_PROJECT 6            /* q -> projected q, y2: phi (p grid); step = param :993-1002 */
+#define GM_CC_OP_PRESSURE_SOLVE 7     /* rhs (p grid) -> phi; solve_pressure(rhs, dt = param, rho) :688-730 */
+int gm_cc_apply(gm_cc* c, int32_t op, double param, const double* x, double* y, double* y2);
+/* extract_true_surface_forces (cut_cell_solver.py:755-765): fx, fy, fx_p, fy_p, fx_v, fy_v */
+int gm_cc_surface_forces(gm_cc* c, const double* u, const double* v, const double* p, double mu, double out[6]);
+/* calculate_cut_cell_divergence (cut_cell_solver.py:219-260) of (u, v), or of the state when
+ * both are NULL: max |div|, rms div, max |net flux| over the fluid cells */
+int gm_cc_divergence_stats(gm_cc* c, const double* u, const double* v, double out[3]);
+
 #ifdef __cplusplus
 }
 #endif
