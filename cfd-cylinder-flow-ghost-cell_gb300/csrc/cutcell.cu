@@ -356,7 +356,8 @@ __global__ void k_cc_final(CcGeo g, const double* __restrict__ R, const double* 
 
 // ---- projection pieces ----------------------------------------------------------------------
 // (rho / dt) times the aperture-weighted divergence of the unpacked field, zero on covered
-// cells (compute_rhs, solver/cut_cell_solver.py:732-738)
+// cells (compute_rhs, solver/cut_cell_solver.py:732-738), divided by kappa on cut cells (the row
+// scaling of the pressure system built by gm::build_cutcell_geometry)
 __global__ void k_cc_divrhs(CcGeo g, const double* __restrict__ X, const double* __restrict__ inl, double inv_dt,
                             double* __restrict__ B) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -369,7 +370,17 @@ __global__ void k_cc_divrhs(CcGeo g, const double* __restrict__ X, const double*
   const double* V = X + g.usize;
   const double fx = (g.ax[fu + 1] * X[fu + 1] - g.ax[fu] * uw) / g.dx;
   const double fy = (g.ay[c + nx] * V[c + nx] - g.ay[c] * V[c]) / g.dy;
-  B[c] = inv_dt * (fx + fy);
+  const double b = inv_dt * (fx + fy);
+  B[c] = g.cell_type[c] == 0 ? b / g.kappa[c] : b;
+}
+// a caller's right-hand side in the row scaling of the pressure system: cut cells / kappa,
+// covered cells zero
+__global__ void k_cc_scale_rhs(CcGeo g, double* __restrict__ B) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.psize) return;
+  const int t = g.cell_type[c];
+  if (t == -1) B[c] = 0.0;
+  else if (t == 0) B[c] = B[c] / g.kappa[c];
 }
 
 // corrector (solver/cut_cell_solver.py:740-753), packed output
@@ -467,12 +478,13 @@ __global__ void k_cc_maxdiff(int64_t n, const double* __restrict__ a, const doub
   }
   if ((threadIdx.x & 31) == 0) atomic_max_abs(out, m);
 }
-// predicted divergence dt/rho max_fluid |res| / kappa (solver/cut_cell_solver.py:721-722)
+// predicted divergence dt/rho max_fluid |res| / kappa (solver/cut_cell_solver.py:721-722); the
+// residual of the row-scaled system already carries the 1 / kappa
 __global__ void k_cc_pdiv(CcGeo g, const double* __restrict__ res, double scale, unsigned long long* out) {
   double m = 0.0;
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < g.psize; c += (int64_t)gridDim.x * blockDim.x)
     if (g.cell_type[c] != -1) {
-      const double v = scale * (fabs(res[c]) / g.kappa[c]);
+      const double v = scale * fabs(res[c]);
       m = (v != v) ? v : fmax(m, v);
     }
   for (int o = 16; o; o >>= 1) {
@@ -999,7 +1011,7 @@ int gm_cc_create(const gm_cc_config* cfg, gm_cc** out) {
   g.nx = nx; g.ny = ny; g.Lx = cfg->Lx; g.Ly = cfg->Ly; g.D = cfg->D; g.xc = cfg->xc; g.yc = cfg->yc;
   g.nu = cfg->nu; g.rho = cfg->rho; g.U_inf = cfg->U_inf; g.inflow = cfg->inflow; g.U_m = cfg->U_m;
   int ec = 0;
-  if (!gm::build_cutcell_geometry(g, cfg->ax, cfg->ay, cfg->cell_type, ec)) {
+  if (!gm::build_cutcell_geometry(g, cfg->ax, cfg->ay, cfg->cell_type, cfg->volume_fraction, ec)) {
     gm_internal_set_error(g.error.c_str());
     return ec ? ec : GM_EVALUE;
   }
@@ -1450,6 +1462,8 @@ int gm_cc_apply(gm_cc* c, int32_t op, double param, const double* x, double* y, 
       case GM_CC_OP_PRESSURE_SOLVE: {
         // solve_pressure(rhs, dt = param, rho): A phi = rhs on the fluid cells, phi = 0 on covered
         copy_in(c->B.p, x, Pn, st);
+        counted();
+        k_cc_scale_rhs<<<nblk(Pn), CC_TPB, 0, st>>>(c->geo, c->B.p);
         CCK(cudaMemsetAsync(gmi::control(c->P), 0, sizeof(StepCtl), st));
         CCK(cudaMemsetAsync(c->diag.p, 0, sizeof(CcDiagDev), st));
         gmi::pressure_solve(c->P, c->B.p, c->phi.p, S_P1);

@@ -819,7 +819,8 @@ bool build_geometry(Geometry& g, int& err_class) {
 // A coupling to a covered neighbour is left out: the covered cell's row is the identity with a
 // zero right-hand side, so its value is zero and the coupling adds nothing, while the diagonal
 // keeps the face's share as in the assembled matrix.
-static Row cutcell_pressure_row(const Geometry& g, const double* ax, const double* ay, int64_t c) {
+static Row cutcell_pressure_row(const Geometry& g, const double* ax, const double* ay, const int32_t* cell_type,
+                               const double* kappa, int64_t c) {
   const int nx = g.nx, ny = g.ny;
   const int64_t j = c / nx, i = c % nx;
   const double idx2 = 1.0 / (g.dx * g.dx), idy2 = 1.0 / (g.dy * g.dy);
@@ -837,11 +838,13 @@ static Row cutcell_pressure_row(const Geometry& g, const double* ax, const doubl
   if (j > 0 && as > 0.0) couple(c - nx, as * idy2);
   if (j < ny - 1 && an > 0.0) couple(c + nx, an * idy2);
   r.emplace_back(c, diag);
+  if (cell_type[c] == 0)
+    for (auto& e : r) e.second = e.second / kappa[c];
   return r;
 }
 
 bool build_cutcell_geometry(Geometry& g, const double* ax, const double* ay, const int32_t* cell_type,
-                            int& err_class) {
+                            const double* kappa, int& err_class) {
   err_class = 1;
   const int nx = g.nx, ny = g.ny;
   if (nx < 4 || ny < 4) { g.error = "nx and ny must be integers >= 4"; return false; }
@@ -873,6 +876,7 @@ bool build_cutcell_geometry(Geometry& g, const double* ax, const double* ay, con
   for (int64_t c = 0; c < g.psize; ++c) {
     g.act_p[c] = cell_type[c] != -1;
     g.mask[c] = cell_type[c] == -1;
+    if (cell_type[c] == 0 && !(kappa[c] > 0.0)) { g.error = "cut cell without fluid volume"; return false; }
   }
   auto labels = [](const std::vector<uint8_t>& a, std::vector<int64_t>& ids, std::vector<int64_t>& lab) {
     ids.clear(); lab.assign(a.size(), -1);
@@ -891,7 +895,7 @@ bool build_cutcell_geometry(Geometry& g, const double* ax, const double* ay, con
   g.rho = 1.0;
   make_rect(g.rect_p, 0, nx, ny, g.dx, g.dy, g.nu, 0.0, 1.0);
   g.a_nnz_row.assign(g.psize, 0);
-  schur_setup(g, g.rect_p, 0, g.act_p, [&](int64_t c) { return cutcell_pressure_row(g, ax, ay, c); }, g.a_rows,
+  schur_setup(g, g.rect_p, 0, g.act_p, [&](int64_t c) { return cutcell_pressure_row(g, ax, ay, cell_type, kappa, c); }, g.a_rows,
               g.a_irr, g.schur_p_rows, g.schur_p_c, g.schur_p_tol, &g.a_nnz_row);
   if (g.schur_p_rows.size() > 2048) { g.error = "Cut-cell inverse exceeds the bounded boundary-row rank"; return false; }
   // surface quadrature points and point-pressure reconstruction (solver/cut_cell_solver.py:25-77)

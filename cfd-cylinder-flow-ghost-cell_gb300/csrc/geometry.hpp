@@ -95,8 +95,11 @@ bool build_helmholtz(const Geometry& g, double dt, HelmholtzSetup& hs, int& err_
 // their point-pressure reconstruction.  The density enters through the caller's right-hand
 // side: the operator is built with unit density and g.rho is set to 1.  ax: ny x (nx+1), ay: (ny+1) x nx, cell_type:
 // ny x nx (1 fluid, 0 cut, -1 covered).
+// The rows of cut cells (cell_type 0) are divided by their fluid fraction kappa (and so must be
+// their right-hand sides): a residual of this system is then the reference's divergence measure
+// |b - A x| / kappa (solver/cut_cell_solver.py:721-722), which the refinement drives down.
 bool build_cutcell_geometry(Geometry& g, const double* ax, const double* ay, const int32_t* cell_type,
-                            int& err_class);
+                            const double* kappa, int& err_class);
 
 // Quadratic point-pressure reconstruction at the points (py[k], px[k]) (solver/cut_cell_solver.py:25-55):
 // rows = points, columns = grid flat p indices; false with err set for invalid points.
