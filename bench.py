@@ -70,6 +70,12 @@ GMRES_WORKLOADS = {
     'gmres_1024x512_re150': dict(nx=1024, ny=512, Lx=40.96, Ly=20.48, D=1.0, xc=8.0, yc=10.24, nu=1 / 150,
                                  dt=0.0015, noise='v', amp=1e-2, seed=0, record_steps=40, epochs=600),
 }
+# the cut-cell AB2/CN path (boundary='cut_cell') on the headline grid: same domain, Re = 100,
+# seeded 1e-2 v perturbation; FP64 (the reference's precision), direct pressure
+CUTCELL_WORKLOADS = {
+    'cutcell_800x820_re100': dict(nx=800, ny=820, Lx=40.0, Ly=41.0, D=1.0, xc=10.0, yc=20.5, nu=0.01, dt=0.002,
+                                  noise='v', amp=1e-2, seed=0),
+}
 DEFAULT_WORKLOAD = 'wide_800x820_re100'
 # FP64 instructions (dadd + dmul + dfma, thread level) per cell update of the plain FP64 step on
 # the 800x820 case, and the measured FP64 instruction rate of a GB300 (independent FMA chains on
@@ -169,13 +175,14 @@ class ClockSampler:
 def seeded_state(s, w):
     """Seeded Gaussian perturbation of the active faces (the reference has no noise API)."""
     rng = np.random.default_rng(w['seed'])
-    q = s.gg.pack(s.u, s.v)
-    nu = len(s.gg.ui)
+    integ = s.cc if hasattr(s, 'cc') else s.gg
+    q = integ.pack(s.u, s.v)
+    nu = len(integ.ui)
     if w['noise'] == 'uv':
         q += w['amp'] * rng.standard_normal(q.size)
     else:
         q[nu:] += w['amp'] * rng.standard_normal(q.size - nu)
-    u, v = s.gg.unpack(q)
+    u, v = integ.unpack(q)
     s.u[:], s.v[:] = u, v
 
 
@@ -472,13 +479,14 @@ def run_ours(args, w, rank, world):
                    sample=f'{done} AB2/CN steps of {args.workload} ({el:.1f} s) after setup and the start-up step')
     # config 4 beside the single case: the 64-case sweep in both precisions (after the
     # single-case figures, so that its gigabyte of state does not touch them)
-    sweep = tgs = gms = None
+    sweep = tgs = gms = ccs = None
     if args.precision == 'fp32' and not args.no_batch and world == 1:
         sweep = batch_summary(pkg, L, BATCH_WORKLOADS['sweep64_batch'], max(1, min(args.steps, 10)), args.warmup)
     # configs 2 and 5 beside it, so that one default run observes every configuration
     if args.precision == 'fp32' and not args.no_extra and world == 1:
         tgs = tg_summary(pkg, TG_WORKLOADS['taylor_green_1024'], max(1, min(args.steps, 50)))
         gms = gmres_summary(pkg, GMRES_WORKLOADS['gmres_1024x512_re150'], max(1, min(args.steps, 10)))
+        ccs = cutcell_summary(pkg, CUTCELL_WORKLOADS['cutcell_800x820_re100'], max(1, min(args.steps, 20)))
     if rank == 0:
         line = dict(metric=METRIC, value=value, unit='cell-updates/s', n_gpus=world, steps=args.steps,
                     warmup=args.warmup, ms_per_step=step_ms, higher_is_better=True, scaling='weak',
@@ -500,7 +508,7 @@ def run_ours(args, w, rank, world):
                                                     momentum=float(np.mean([b for _, b in sweeps]))),
                     kernel_class_ms_per_step={KERNEL_CLASSES[c]: v[0] for c, v in per_class.items() if v[1]},
                     graph_phase_ms=phase_ms, comparison=compare, sweep64_batch=sweep, taylor_green_1024=tgs,
-                    gmres_1024x512_re150=gms)
+                    gmres_1024x512_re150=gms, cutcell_800x820_re100=ccs)
         print(json.dumps(line), flush=True)
 
 
@@ -710,6 +718,46 @@ def gmres_summary(pkg, w, steps):
         if solver == 'iterative':
             out[solver]['krylov_iterations_per_solve'] = its / max(nsol, 1)
         del s
+    return out
+
+
+def cutcell_summary(pkg, w, steps):
+    """The cut-cell AB2/CN path (boundary='cut_cell') on the 800x820 grid beside the ghost-cell
+    headline: K steps after three warm-up steps (one call, the host reads each step's
+    diagnostics), with the CN GMRES iterations and the step gates."""
+    import torch
+    kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
+    dt = w['dt']
+    t0 = time.perf_counter()
+    os.environ['GHOSTMAC_PHASE_TIMING'] = '1'  # nine event records inside each step graph
+    try:
+        s = pkg.MAC_CylinderFlow(boundary='cut_cell', time_scheme='ab2_cn', verbose=False, **kw)
+    finally:
+        os.environ.pop('GHOSTMAC_PHASE_TIMING', None)
+    setup_s = time.perf_counter() - t0
+    seeded_state(s, w)
+    s._push()
+    rc, d = s.step_raw(dt, 3, start_time=0.0)
+    pkg.cutcell._check(rc, s._h)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rc, d = s.step_raw(dt, steps, start_time=3 * dt)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    pkg.cutcell._check(rc, s._h)
+    its = [int(d[k].momentum_iterations) for k in range(steps)]
+    ph = np.zeros(8)
+    pkg.cutcell._check(pkg._lib.lib.gm_cc_phase_timing(s._h, pkg._lib.ptr(ph)), s._h)
+    names = ('advection', 'startup_or_ab2_and_cn_rhs', 'cn_gmres', 'cn_residual_check', 'projection_1',
+             'cn_action_and_defect', 'projection_2', 'outputs_and_forces')
+    out = dict(workload='cutcell_800x820_re100', grid=f"{w['nx']}x{w['ny']}", precision='fp64', steps=steps,
+               ms_per_step=ms, value=w['nx'] * w['ny'] / (ms * 1e-3), unit='cell-updates/s',
+               cn_gmres_iterations_per_step=float(np.mean(its)), pressure_solves_per_step=int(d[steps - 1].pressure_solves),
+               max_divergence=max(float(d[k].max_divergence) for k in range(steps)),
+               cd=float(d[steps - 1].cd), cl=float(d[steps - 1].cl), setup_s=setup_s,
+               schur_rank=int(s.cc.pressure_inverse_info['rank']),
+               last_step_phase_ms=dict(zip(names, (float(x) for x in ph))))
+    del s
     return out
 
 

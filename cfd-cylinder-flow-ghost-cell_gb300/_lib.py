@@ -34,7 +34,7 @@ SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_las
            'gm_cc_create', 'gm_cc_destroy', 'gm_cc_last_error', 'gm_cc_get_sizes', 'gm_cc_get_indices',
            'gm_cc_get_surface_points', 'gm_cc_set_state', 'gm_cc_get_state', 'gm_cc_set_inlet',
            'gm_cc_set_history', 'gm_cc_get_history', 'gm_cc_step', 'gm_cc_apply', 'gm_cc_surface_forces',
-           'gm_cc_divergence_stats')
+           'gm_cc_divergence_stats', 'gm_cc_phase_timing')
 CC_OP_MOMENTUM_ADVECTION, CC_OP_MOMENTUM_DIFFUSION, CC_OP_ADVECTION, CC_OP_DIFFUSION, CC_OP_H_MATVEC, CC_OP_PROJECT, \
     CC_OP_PRESSURE_SOLVE = range(1, 8)
 NOALLOC_MAX_CELLS = 1048576
@@ -188,6 +188,7 @@ def _load():
         'gm_cc_apply': ([P, I32, D, P, P, P], C.c_int),
         'gm_cc_surface_forces': ([P, P, P, P, D, P], C.c_int),
         'gm_cc_divergence_stats': ([P, P, P, P], C.c_int),
+        'gm_cc_phase_timing': ([P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

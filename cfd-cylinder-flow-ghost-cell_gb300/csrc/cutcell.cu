@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -163,6 +164,19 @@ __device__ __forceinline__ void atomic_max_abs(unsigned long long* out, double v
   atomicMax(out, (unsigned long long)__double_as_longlong(fabs(v)));
 }
 
+// One CSR row times the field by a whole warp: lanes stride over the row's entries, then a
+// butterfly sum leaves the same total in every lane (the pairs add in mirrored order, which
+// IEEE addition does not distinguish), in a fixed order from run to run.
+__device__ __forceinline__ double warp_row_dot(const int64_t* __restrict__ ptr, const int64_t* __restrict__ col,
+                                               const double* __restrict__ val, int64_t r, const CcGeo& g,
+                                               const double* __restrict__ X, const double* __restrict__ inl,
+                                               int lane) {
+  double acc = 0.0;
+  for (int64_t e = ptr[r] + lane; e < ptr[r + 1]; e += 32) acc += val[e] * fld(g, X, inl, col[e]);
+  for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  return acc;
+}
+
 // ---- momentum right-hand side -------------------------------------------------------------
 // One thread per vertex (j, i) of the (ny+1) x (nx+1) grid: F_xx and F_yy of cell (j, i),
 // F_xy and F_yx of vertex (j, i) (solver/cut_cell_solver.py:808-914).  ADV: the advective
@@ -239,30 +253,30 @@ __global__ void k_cc_flux(CcGeo g, const double* __restrict__ X, const double* _
 }
 
 // Curved faces (solver/staggered_wall.py:134-140 and the viscous correction of
-// solver/cut_cell_solver.py:822-825): ADV: -rho * sum over the face's Gauss points of
-// length * (u u | u v | v v) with u, v from the fit; otherwise rho nu (gradient row . field).
+// solver/cut_cell_solver.py:822-825), one warp per face: ADV: -rho * sum over the face's Gauss
+// points of length * (u u | u v | v v) with u, v from the fit; otherwise rho nu (gradient row .
+// field).
 template <bool ADV>
 __global__ void k_cc_fix(CcGeo g, CcFix fx, const double* __restrict__ X, const double* __restrict__ inl, double rnu,
                          double rho, CcFlux F) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int r = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   double* fam[4] = {F.xx, F.xy, F.yx, F.yy};
   if (!ADV) {
     if (r >= fx.n_dif) return;
-    double acc = 0.0;
-    for (int64_t e = fx.dptr[r]; e < fx.dptr[r + 1]; ++e) acc += fx.dval[e] * fld(g, X, inl, fx.dcol[e]);
-    fam[fx.dfam[r]][fx.dface[r]] = rnu * acc;
+    const double acc = warp_row_dot(fx.dptr, fx.dcol, fx.dval, r, g, X, inl, lane);
+    if (lane == 0) fam[fx.dfam[r]][fx.dface[r]] = rnu * acc;
   } else {
     if (r >= fx.n_adv) return;
     const int fm = fx.afam[r];
     double s = 0.0;
     for (int64_t p = fx.apptr[r]; p < fx.apptr[r + 1]; ++p) {
-      double ue = 0.0, ve = 0.0;
-      for (int64_t e = fx.uptr[p]; e < fx.uptr[p + 1]; ++e) ue += fx.uval[e] * fld(g, X, inl, fx.ucol[e]);
-      for (int64_t e = fx.vptr[p]; e < fx.vptr[p + 1]; ++e) ve += fx.vval[e] * fld(g, X, inl, fx.vcol[e]);
+      const double ue = warp_row_dot(fx.uptr, fx.ucol, fx.uval, p, g, X, inl, lane);
+      const double ve = warp_row_dot(fx.vptr, fx.vcol, fx.vval, p, g, X, inl, lane);
       const double prod = fm == 0 ? ue * ue : (fm == 3 ? ve * ve : ue * ve);
       s += fx.alen[p] * prod;
     }
-    fam[fm][fx.aface[r]] = -(rho * s);
+    if (lane == 0) fam[fm][fx.aface[r]] = -(rho * s);
   }
 }
 
@@ -298,20 +312,22 @@ __global__ void k_cc_accum(CcGeo g, const double* __restrict__ X, double rho, Cc
   }
 }
 
-// One block: wall shear -rho nu (rate . field) t ds added to the owning u / v faces in the
-// order of the points (np.add.at), then the covered-volume transfers (donor values to their
-// owners in donor order, donors zero) (solver/cut_cell_solver.py:921-928,
-// solver/staggered_wall.py:302-304).
-__global__ void k_cc_wall(CcGeo g, CcWall w, const double* __restrict__ X, const double* __restrict__ inl,
-                          double scale, int shear, double* __restrict__ R) {
+// wall shear stress -rho nu (rate . field) at the circle's Gauss points, one warp per point
+__global__ void k_cc_wall_tau(CcGeo g, CcWall w, const double* __restrict__ X, const double* __restrict__ inl,
+                              double scale) {
+  const int lane = threadIdx.x & 31;
+  const int k = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (k >= w.n) return;
+  const double acc = warp_row_dot(w.ptr, w.col, w.val, k, g, X, inl, lane);
+  if (lane == 0) w.tau[k] = scale * acc;
+}
+
+// One block: the wall shear tau t ds added to the owning u / v faces in the order of the points
+// (np.add.at), then the covered-volume transfers (donor values to their owners in donor order,
+// donors zero) (solver/cut_cell_solver.py:921-928, solver/staggered_wall.py:302-304).
+__global__ void __launch_bounds__(1024) k_cc_wall(CcGeo g, CcWall w, int shear, double* __restrict__ R) {
   const int tid = threadIdx.x, nt = blockDim.x;
   if (shear) {
-    for (int k = tid; k < w.n; k += nt) {
-      double acc = 0.0;
-      for (int64_t e = w.ptr[k]; e < w.ptr[k + 1]; ++e) acc += w.val[e] * fld(g, X, inl, w.col[e]);
-      w.tau[k] = scale * acc;
-    }
-    __syncthreads();
     for (int t = tid; t < w.n_tgt; t += nt) {
       const int64_t f = w.tgt[t];
       const double* dir = f < g.usize ? w.tx : w.ty;
@@ -564,12 +580,14 @@ __global__ void k_cc_forces(gmi::SurfaceCsr S, CcWall w, const double* __restric
   }
   const double fxp = -block_sum(px, sh), fyp = -block_sum(py, sh);
   double vx = 0.0, vy = 0.0;
-  for (int k = tid; k < w.n; k += nt) {
-    double acc = 0.0;
-    for (int64_t e = w.ptr[k]; e < w.ptr[k + 1]; ++e) acc += w.val[e] * U[w.col[e]];
-    const double tau = mu * acc;
-    vx += tau * w.tx[k] * w.ds[k];
-    vy += tau * w.ty[k] * w.ds[k];
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  for (int k = warp; k < w.n; k += nwarp) {
+    const double acc = warp_row_dot(w.ptr, w.col, w.val, k, CcGeo{}, U, nullptr, lane);
+    if (lane == 0) {
+      const double tau = mu * acc;
+      vx += tau * w.tx[k] * w.ds[k];
+      vy += tau * w.ty[k] * w.ds[k];
+    }
   }
   const double fxv = block_sum(vx, sh), fyv = block_sum(vy, sh);
   if (tid == 0) {
@@ -683,6 +701,11 @@ struct gm_cc {
   };
   Graph graphs[3];
   int next_graph = 0;
+  // optional phase events inside the step graph (environment GHOSTMAC_PHASE_TIMING=1 at create)
+  static constexpr int NPHASE = 8;
+  bool phase_on = false;
+  cudaEvent_t pev[NPHASE + 1] = {};
+  double phase_ms[NPHASE] = {};
 };
 
 namespace {
@@ -718,15 +741,20 @@ void momentum(gm_cc* c, bool adv, const double* X, const double* inl, double nu,
   const int nfix = adv ? c->fix.n_adv : c->fix.n_dif;
   if (nfix > 0) {
     counted();
-    if (adv) k_cc_fix<true><<<nblk(nfix, 64), 64, 0, st>>>(c->geo, c->fix, X, inl, rnu, c->rho, c->flux);
-    else k_cc_fix<false><<<nblk(nfix, 64), 64, 0, st>>>(c->geo, c->fix, X, inl, rnu, c->rho, c->flux);
+    const unsigned nb = nblk((int64_t)nfix * 32, 256);
+    if (adv) k_cc_fix<true><<<nb, 256, 0, st>>>(c->geo, c->fix, X, inl, rnu, c->rho, c->flux);
+    else k_cc_fix<false><<<nb, 256, 0, st>>>(c->geo, c->fix, X, inl, rnu, c->rho, c->flux);
   }
   counted();
   if (adv) k_cc_accum<true><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, c->rho, c->flux, c->Rw.p);
   else k_cc_accum<false><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, c->rho, c->flux, c->Rw.p);
+  const bool shear = !adv && nu != 0.0;
+  if (shear && c->wall.n > 0) {
+    counted();
+    k_cc_wall_tau<<<nblk((int64_t)c->wall.n * 32, 256), 256, 0, st>>>(c->geo, c->wall, X, inl, (-c->rho) * nu);
+  }
   counted();
-  k_cc_wall<<<1, CC_WALL_THREADS, 0, st>>>(c->geo, c->wall, X, inl, (-c->rho) * nu, (!adv && nu != 0.0) ? 1 : 0,
-                                          c->Rw.p);
+  k_cc_wall<<<1, CC_WALL_THREADS, 0, st>>>(c->geo, c->wall, shear ? 1 : 0, c->Rw.p);
   counted();
   k_cc_final<<<nblk(c->F), CC_TPB, 0, st>>>(c->geo, c->Rw.p, X, hdt, mode, Y, Rout);
 }
@@ -848,10 +876,15 @@ void gmres(gm_cc* c, const double* b, double* x, double dt, gm_cc::Graph& gr, cu
 void step_body(gm_cc* c, double dt, gm_cc::Graph& gr, cudaStream_t st) {
   const int64_t F = c->F, Pn = c->psize;
   const double* inl = c->inlet.p;
+  auto mark = [&](int k) {
+    if (c->phase_on) CCK(cudaEventRecord(c->pev[k], st));
+  };
+  mark(0);
   CCK(cudaMemsetAsync(c->diag.p, 0, offsetof(CcDiagDev, forces), st));
   counted();
   k_cc_pack<<<nblk(F), CC_TPB, 0, st>>>(c->geo, c->U.p, c->q0.p);
   momentum(c, true, c->q0.p, inl, 0.0, 0, 0.0, c->now.p, nullptr, st);
+  mark(1);
   const double* pressure = c->has_history ? c->halfp.p : c->Pst.p;
   if (!c->has_history) {
     // projected midpoint start-up
@@ -869,13 +902,19 @@ void step_body(gm_cc* c, double dt, gm_cc::Graph& gr, cudaStream_t st) {
   vec(c, 2, F, c->q0.p, c->expl.p, c->dq.p, c->gp.p, c->offset.p, dt, 0.5 * dt, c->rhs.p, st);
   maxdiff(c, F, c->rhs.p, nullptr, nullptr, 0.0, &c->diag.p->rhs_max, st);
   CCK(cudaMemcpyAsync(c->star.p, c->q0.p, F * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  mark(2);
   gmres(c, c->rhs.p, c->star.p, dt, gr, st);
+  mark(3);
   hmatvec(c, c->star.p, dt, c->w.p, st);
   maxdiff(c, F, c->w.p, c->rhs.p, nullptr, 0.0, &c->diag.p->mres, st);
+  mark(4);
   project(c, c->star.p, dt, c->result.p, c->phi.p, S_P1, 1, st);
+  mark(5);
   hmatvec(c, c->result.p, dt, c->action.p, st);
   vec(c, 3, F, c->result.p, c->rhs.p, c->action.p, nullptr, nullptr, 0.0, 0.0, c->tmp.p, st);
+  mark(6);
   project(c, c->tmp.p, dt, c->w.p, c->inc.p, S_P2, 2, st);
+  mark(7);
   const double factor = c->has_history ? dt / (dt + c->prev_dt) : 1.0;
   counted();
   k_cc_pressure_out<<<nblk(Pn), CC_TPB, 0, st>>>(Pn, pressure, c->inc.p, factor, c->halfp_next.p, c->Pst.p);
@@ -891,6 +930,7 @@ void step_body(gm_cc* c, double dt, gm_cc::Graph& gr, cudaStream_t st) {
   counted();
   k_cc_forces<<<1, CC_FORCE_THREADS, 0, st>>>(gmi::surface(c->P), c->wall, c->U.p, c->Pst.p, c->nu * c->rho, c->pb.p,
                                              c->diag.p->forces);
+  mark(8);
 }
 
 gm_cc::Graph& step_graph(gm_cc* c, double dt) {
@@ -1216,6 +1256,9 @@ int gm_cc_create(const gm_cc_config* cfg, gm_cc** out) {
     C->diag.alloc(1);
     CCK(cudaMallocHost(&C->host_diag, sizeof(CcDiagDev)));
     C->d_act.upload(C->act_idx, st);
+    if (const char* e = std::getenv("GHOSTMAC_PHASE_TIMING")) C->phase_on = e[0] == '1';
+    if (C->phase_on)
+      for (auto& e : C->pev) CCK(cudaEventCreate(&e));
     initial_state(C, inlet, cfg->cell_type, cfg->ax, cfg->ay);
   });
   if (rc != GM_OK) {
@@ -1232,6 +1275,8 @@ int gm_cc_destroy(gm_cc* c) {
   for (auto& g : c->graphs)
     if (g.exec) cudaGraphExecDestroy(g.exec);
   if (c->host_diag) cudaFreeHost(c->host_diag);
+  for (auto& e : c->pev)
+    if (e) cudaEventDestroy(e);
   gm_handle* P = c->P;
   delete c;  // device buffers first, then the pressure handle and its stream
   if (P) gmi::pressure_destroy(P);
@@ -1354,6 +1399,11 @@ int gm_cc_step(gm_cc* c, double dt, int32_t n_steps, double start_time, gm_cc_st
       std::string m;
       const int prc = gmi::check(c->P, "cut-cell step", m);  // synchronises the stream
       const int cycles = r[1], its = r[2], converged = r[3];
+      if (c->phase_on)
+        for (int q = 0; q < gm_cc::NPHASE; ++q) {
+          float ms = 0.f;
+          c->phase_ms[q] = cudaEventElapsedTime(&ms, c->pev[q], c->pev[q + 1]) == cudaSuccess ? ms : 0.0;
+        }
       kernel_launch_adjust(gr.outer + (long long)cycles * gr.per_cycle + (long long)its * gr.per_step);
       const CcDiagDev& d = *c->host_diag;
       gm_cc_step_diag out{};
@@ -1403,6 +1453,12 @@ int gm_cc_step(gm_cc* c, double dt, int32_t n_steps, double start_time, gm_cc_st
       if (cls != GM_OK) throw CcFail(cls, msg);
     }
   });
+}
+
+int gm_cc_phase_timing(const gm_cc* c, double out[8]) {
+  if (!c || !out) return GM_EVALUE;
+  for (int q = 0; q < gm_cc::NPHASE; ++q) out[q] = c->phase_ms[q];
+  return GM_OK;
 }
 
 int gm_cc_apply(gm_cc* c, int32_t op, double param, const double* x, double* y, double* y2) {

@@ -471,6 +471,12 @@ int gm_cc_get_history(gm_cc* c, int32_t* has_history, double* prev_adv, double* 
  * receives one record per step.  A failed gate stops the loop after that step with its class. */
 int gm_cc_step(gm_cc* c, double dt, int32_t n_steps, double start_time, gm_cc_step_diag* diag);
 
+/* Event times (ms) of the last step when the environment variable GHOSTMAC_PHASE_TIMING=1 was
+ * set at gm_cc_create: out[0..7] = advection, start-up / AB2 and CN right-hand side, GMRES,
+ * its residual check, projection 1, CN action and defect, projection 2, outputs (pressure,
+ * history, step maxima, forces).  No counterpart in the reference. */
+int gm_cc_phase_timing(const gm_cc* c, double out[8]);
+
 #define GM_CC_OP_MOMENTUM_ADVECTION 1 /* (u|v grids) -> a (u|v), y2: rhs; compute_momentum_rhs(u, v, 0, rho) :790-957 */
 #define GM_CC_OP_MOMENTUM_DIFFUSION 2 /* same with nu = param and include_advection=False */
 #define GM_CC_OP_ADVECTION 3          /* q -> advection(q) of advance_ab2_cn :972-974 */
