@@ -85,19 +85,29 @@ inline void counted() { note_launch_ext(); }
 enum : uint8_t { F_ACTIVE = 1, F_FLUID = 2, F_SOLID = 4 };
 
 // geometry of the face grid (kernel argument)
+// GB300 issues FP64 at 1/64 of the FP32 rate, so every per-point factor that does not depend on
+// the field is folded on the host: the kernels multiply, they never divide.
 struct CcGeo {
   int nx, ny;
   int64_t usize, vsize, psize, F;
-  double dx, dy;
-  const double *ax, *ay, *ax_mid, *ay_mid, *ay_u, *ax_v;
+  double dx, dy, idx, idy;
+  const double *ax, *ay;
+  // viscous flux factors (aperture x face length / spacing): F = rho nu (difference) c
+  const double *cxx, *cyy;   // ny x nx: ax_mid dy / dx, ay_mid dx / dy
+  const double *cxy, *cyx;   // (ny+1) x (nx+1): ay_u dx / dy, ax_v dy / dx
+  // advective flux factors (rho x aperture x face length): F = -(transported product) a
+  const double *axx, *ayy;   // ny x nx: rho ax_mid dy, rho ay_mid dx
+  const double *axy, *ayx;   // (ny+1) x (nx+1): rho ay_u dx, rho ax_v dy
+  const double* aout;        // ny: rho ax[:, nx] dy (natural outlet)
   const uint8_t* flags;      // F: F_ACTIVE unknown, F_FLUID divided by its own volume, F_SOLID covered face
   const int32_t* cell_type;  // psize
-  const double* kappa;       // psize: fluid fraction of the pressure cells
-  const double* vol_rho;     // F: rho * owned volume
+  const double* kappa;       // psize: fluid fraction
+  const double* ikappa;      // psize: 1 / fluid fraction on cut cells, 1 elsewhere
+  const double* ivol_rho;    // F: 1 / (rho * owned volume)
   const int32_t* merge_of;   // F: the last merge that writes the face, or -1
-  const int64_t* ms;         // merges: small face, master face (face-grid flat), rho * merged volume
+  const int64_t* ms;         // merges: small face, master face (face-grid flat), 1 / (rho * merged volume)
   const int64_t* mm;
-  const double* mvol_rho;
+  const double* imvol_rho;
 };
 
 // curved-face flux overrides, the four families concatenated (0 F_xx, 1 F_xy, 2 F_yx, 3 F_yy)
@@ -180,10 +190,10 @@ __device__ __forceinline__ double warp_row_dot(const int64_t* __restrict__ ptr, 
 // ---- momentum right-hand side -------------------------------------------------------------
 // One thread per vertex (j, i) of the (ny+1) x (nx+1) grid: F_xx and F_yy of cell (j, i),
 // F_xy and F_yx of vertex (j, i) (solver/cut_cell_solver.py:808-914).  ADV: the advective
-// form with nu = 0 (rnu = 0); otherwise the viscous form without advection.
+// form (nu = 0: no viscous part); otherwise the viscous form without advection.
 template <bool ADV>
 __global__ void k_cc_flux(CcGeo g, const double* __restrict__ X, const double* __restrict__ inl, double rnu,
-                          double rho, int slip, CcFlux F) {
+                          int slip, CcFlux F) {
   const int nx = g.nx, ny = g.ny;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)(ny + 1) * (nx + 1)) return;
@@ -194,59 +204,47 @@ __global__ void k_cc_flux(CcGeo g, const double* __restrict__ X, const double* _
     return (ii == 0 && inl) ? inl[jj] : X[f];
   };
   auto W = [&](int jj, int ii) -> double { return V[(int64_t)jj * nx + ii]; };
-  const double dx = g.dx, dy = g.dy;
   if (j < ny && i < nx) {
     const int64_t c = (int64_t)j * nx + i;
-    const double am = g.ax_mid[c];
-    const double ul = U(j, i), ur = U(j, i + 1);
-    double f = rnu * (ur - ul) / dx * am * dy;
+    const double ul = U(j, i), ur = U(j, i + 1), vb = W(j, i), vt = W(j + 1, i);
     if (ADV) {
-      const double uf = 0.5 * (ul + ur);
-      f = f - rho * uf * uf * am * dy;
+      const double uf = 0.5 * (ul + ur), vf = 0.5 * (vb + vt);
+      F.xx[c] = -(uf * uf * g.axx[c]);
+      F.yy[c] = -(vf * vf * g.ayy[c]);
+    } else {
+      F.xx[c] = rnu * (ur - ul) * g.cxx[c];
+      F.yy[c] = rnu * (vt - vb) * g.cyy[c];
     }
-    F.xx[c] = f;
-    const double bm = g.ay_mid[c];
-    const double vb = W(j, i), vt = W(j + 1, i);
-    double q = rnu * (vt - vb) / dy * bm * dx;
-    if (ADV) {
-      const double vf = 0.5 * (vb + vt);
-      q = q - rho * vf * vf * bm * dx;
-    }
-    F.yy[c] = q;
   }
   {
-    const double a = g.ay_u[t];
     double f;
-    if (j == 0) f = slip ? 0.0 : 2.0 * rnu * U(0, i) / dy * a * dx;
-    else if (j == ny) f = slip ? 0.0 : -2.0 * rnu * U(ny - 1, i) / dy * a * dx;
-    else {
-      f = rnu * (U(j, i) - U(j - 1, i)) / dy * a * dx;
-      if (ADV) {
-        const double vf = i == 0 ? W(j, 0) : (i == nx ? W(j, nx - 1) : 0.5 * (W(j, i - 1) + W(j, i)));
-        const double ua = 0.5 * (U(j - 1, i) + U(j, i));
-        f = f - rho * vf * ua * a * dx;
-      }
+    if (j == 0) f = (ADV || slip) ? 0.0 : rnu * U(0, i) * (2.0 * g.cxy[t]);
+    else if (j == ny) f = (ADV || slip) ? 0.0 : -(rnu * U(ny - 1, i) * (2.0 * g.cxy[t]));
+    else if (ADV) {
+      const double vf = i == 0 ? W(j, 0) : (i == nx ? W(j, nx - 1) : 0.5 * (W(j, i - 1) + W(j, i)));
+      const double ua = 0.5 * (U(j - 1, i) + U(j, i));
+      f = -(vf * ua * g.axy[t]);
+    } else {
+      f = rnu * (U(j, i) - U(j - 1, i)) * g.cxy[t];
     }
     F.xy[t] = f;
   }
   {
-    const double a = g.ax_v[t];
     double f;
     if (i == 0) {
-      f = 2.0 * rnu * W(j, 0) / dx * a * dy;
+      f = ADV ? 0.0 : rnu * W(j, 0) * (2.0 * g.cyx[t]);
     } else if (i == nx) {
       f = 0.0;
       if (ADV) {
         const double uo = j == 0 ? U(0, nx) : (j == ny ? U(ny - 1, nx) : 0.5 * (U(j - 1, nx) + U(j, nx)));
-        f = -rho * uo * W(j, nx - 1) * a * dy;
+        f = -(uo * W(j, nx - 1) * g.ayx[t]);
       }
+    } else if (ADV) {
+      const double uf = j == 0 ? U(0, i) : (j == ny ? U(ny - 1, i) : 0.5 * (U(j - 1, i) + U(j, i)));
+      const double va = 0.5 * (W(j, i - 1) + W(j, i));
+      f = -(uf * va * g.ayx[t]);
     } else {
-      f = rnu * (W(j, i) - W(j, i - 1)) / dx * a * dy;
-      if (ADV) {
-        const double uf = j == 0 ? U(0, i) : (j == ny ? U(ny - 1, i) : 0.5 * (U(j - 1, i) + U(j, i)));
-        const double va = 0.5 * (W(j, i - 1) + W(j, i));
-        f = f - rho * uf * va * a * dy;
-      }
+      f = rnu * (W(j, i) - W(j, i - 1)) * g.cyx[t];
     }
     F.yx[t] = f;
   }
@@ -283,7 +281,7 @@ __global__ void k_cc_fix(CcGeo g, CcFix fx, const double* __restrict__ X, const 
 // Flux differences (solver/cut_cell_solver.py:853-861, 916-917); one thread per vertex (j, i):
 // the u face (j, i) when j < ny, the v face (j, i) when i < nx.
 template <bool ADV>
-__global__ void k_cc_accum(CcGeo g, const double* __restrict__ X, double rho, CcFlux F, double* __restrict__ R) {
+__global__ void k_cc_accum(CcGeo g, const double* __restrict__ X, CcFlux F, double* __restrict__ R) {
   const int nx = g.nx, ny = g.ny;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)(ny + 1) * (nx + 1)) return;
@@ -297,7 +295,7 @@ __global__ void k_cc_accum(CcGeo g, const double* __restrict__ X, double rho, Cc
       double ext = 0.0;
       if (ADV) {
         const double un = X[f];
-        ext = (-rho) * (un * un) * g.ax[f] * g.dy;
+        ext = -(un * un * g.aout[j]);
       }
       r = (ext - F.xx[(int64_t)j * nx + nx - 1]) + 0.5 * (F.xy[f + nx + 1] - F.xy[f]);
     }
@@ -358,9 +356,9 @@ __global__ void k_cc_final(CcGeo g, const double* __restrict__ R, const double* 
   if (f >= g.F) return;
   const uint8_t fl = g.flags[f];
   double a = 0.0;
-  if (fl & F_FLUID) a = R[f] / g.vol_rho[f];
+  if (fl & F_FLUID) a = R[f] * g.ivol_rho[f];
   const int m = g.merge_of[f];
-  if (m >= 0) a = (R[g.ms[m]] + R[g.mm[m]]) / g.mvol_rho[m];
+  if (m >= 0) a = (R[g.ms[m]] + R[g.mm[m]]) * g.imvol_rho[m];
   if (fl & F_SOLID) a = 0.0;
   if (mode == 0) Y[f] = (fl & F_ACTIVE) ? a : 0.0;
   else if (mode == 1) Y[f] = (fl & F_ACTIVE) ? X[f] - hdt * a : 0.0;
@@ -384,24 +382,21 @@ __global__ void k_cc_divrhs(CcGeo g, const double* __restrict__ X, const double*
   const int64_t fu = (int64_t)j * (nx + 1) + i;
   const double uw = (i == 0 && inl) ? inl[j] : X[fu];
   const double* V = X + g.usize;
-  const double fx = (g.ax[fu + 1] * X[fu + 1] - g.ax[fu] * uw) / g.dx;
-  const double fy = (g.ay[c + nx] * V[c + nx] - g.ay[c] * V[c]) / g.dy;
-  const double b = inv_dt * (fx + fy);
-  B[c] = g.cell_type[c] == 0 ? b / g.kappa[c] : b;
+  const double fx = (g.ax[fu + 1] * X[fu + 1] - g.ax[fu] * uw) * g.idx;
+  const double fy = (g.ay[c + nx] * V[c + nx] - g.ay[c] * V[c]) * g.idy;
+  B[c] = inv_dt * (fx + fy) * g.ikappa[c];
 }
 // a caller's right-hand side in the row scaling of the pressure system: cut cells / kappa,
 // covered cells zero
 __global__ void k_cc_scale_rhs(CcGeo g, double* __restrict__ B) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= g.psize) return;
-  const int t = g.cell_type[c];
-  if (t == -1) B[c] = 0.0;
-  else if (t == 0) B[c] = B[c] / g.kappa[c];
+  B[c] = g.cell_type[c] == -1 ? 0.0 : B[c] * g.ikappa[c];
 }
 
-// corrector (solver/cut_cell_solver.py:740-753), packed output
-__global__ void k_cc_correct(CcGeo g, const double* __restrict__ X, const double* __restrict__ phi, double dtr,
-                             double* __restrict__ Y) {
+// corrector (solver/cut_cell_solver.py:740-753), packed output; sx = dt / (rho dx), sy = dt / (rho dy)
+__global__ void k_cc_correct(CcGeo g, const double* __restrict__ X, const double* __restrict__ phi, double sx,
+                             double sy, double* __restrict__ Y) {
   const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= g.F) return;
   const int nx = g.nx, ny = g.ny;
@@ -409,19 +404,19 @@ __global__ void k_cc_correct(CcGeo g, const double* __restrict__ X, const double
   if (f < g.usize) {
     const int j = (int)(f / (nx + 1)), i = (int)(f % (nx + 1));
     const int64_t c = (int64_t)j * nx + i;
-    if (i >= 1 && i < nx) r = g.ax[f] > 0.0 ? X[f] - dtr * (phi[c] - phi[c - 1]) / g.dx : 0.0;
-    else if (i == nx) r = X[f] + dtr * 2.0 * phi[c - 1] / g.dx;
+    if (i >= 1 && i < nx) r = g.ax[f] > 0.0 ? X[f] - sx * (phi[c] - phi[c - 1]) : 0.0;
+    else if (i == nx) r = X[f] + (2.0 * sx) * phi[c - 1];
   } else {
     const int64_t c = f - g.usize;
     const int j = (int)(c / nx);
-    if (j >= 1 && j < ny) r = g.ay[c] > 0.0 ? X[f] - dtr * (phi[c] - phi[c - nx]) / g.dy : 0.0;
+    if (j >= 1 && j < ny) r = g.ay[c] > 0.0 ? X[f] - sy * (phi[c] - phi[c - nx]) : 0.0;
   }
   Y[f] = (g.flags[f] & F_ACTIVE) ? r : 0.0;
 }
 
 // pressure gradient / rho on the unknown faces (advance_ab2_cn's gradient,
-// solver/cut_cell_solver.py:979-984); rdx = rho dx, rdy = rho dy
-__global__ void k_cc_grad(CcGeo g, const double* __restrict__ P, double rdx, double rdy, double* __restrict__ Y) {
+// solver/cut_cell_solver.py:979-984); gx = 1 / (rho dx), gy = 1 / (rho dy)
+__global__ void k_cc_grad(CcGeo g, const double* __restrict__ P, double gx, double gy, double* __restrict__ Y) {
   const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= g.F) return;
   const int nx = g.nx, ny = g.ny;
@@ -429,12 +424,12 @@ __global__ void k_cc_grad(CcGeo g, const double* __restrict__ P, double rdx, dou
   if (f < g.usize) {
     const int j = (int)(f / (nx + 1)), i = (int)(f % (nx + 1));
     const int64_t c = (int64_t)j * nx + i;
-    if (i >= 1 && i < nx) r = (P[c] - P[c - 1]) / rdx;
-    else if (i == nx) r = -2.0 * P[c - 1] / rdx;
+    if (i >= 1 && i < nx) r = (P[c] - P[c - 1]) * gx;
+    else if (i == nx) r = -2.0 * P[c - 1] * gx;
   } else {
     const int64_t c = f - g.usize;
     const int j = (int)(c / nx);
-    if (j >= 1 && j < ny) r = (P[c] - P[c - nx]) / rdy;
+    if (j >= 1 && j < ny) r = (P[c] - P[c - nx]) * gy;
   }
   Y[f] = (g.flags[f] & F_ACTIVE) ? r : 0.0;
 }
@@ -522,9 +517,9 @@ __global__ void k_cc_stepmax(CcGeo g, const double* __restrict__ U, unsigned lon
       const int64_t c = f;
       const int j = (int)(c / nx), i = (int)(c % nx);
       const int64_t fu = (int64_t)j * (nx + 1) + i;
-      const double d = (g.ax[fu + 1] * U[fu + 1] - g.ax[fu] * U[fu]) / g.dx +
-                       (g.ay[c + nx] * V[c + nx] - g.ay[c] * V[c]) / g.dy;
-      const double v = fabs(d) / g.kappa[c];
+      const double d = (g.ax[fu + 1] * U[fu + 1] - g.ax[fu] * U[fu]) * g.idx +
+                       (g.ay[c + nx] * V[c + nx] - g.ay[c] * V[c]) * g.idy;
+      const double v = fabs(d) * g.ikappa[c];
       dm = (v != v) ? v : fmax(dm, v);
     }
   }
@@ -614,7 +609,7 @@ __global__ void k_cc_divstats(CcGeo g, const double* __restrict__ U, double* __r
     const double fx = g.ax[fu + 1] * g.dy * U[fu + 1] - g.ax[fu] * g.dy * U[fu];
     const double fy = g.ay[c + nx] * g.dx * V[c + nx] - g.ay[c] * g.dx * V[c];
     const double net = fx + fy;
-    const double vol = g.kappa[c] * g.dx * g.dy;
+    const double vol = g.kappa[c] * g.dx * g.dy;  // diagnostics only: the reference's division
     const double d = vol > 0.0 ? net / vol : 0.0;
     mdiv = fmax(mdiv, fabs(d));
     mflux = fmax(mflux, fabs(net));
@@ -660,7 +655,8 @@ struct gm_cc {
   int64_t n_active = 0;
   std::vector<int64_t> act_idx;  // face-grid flat indices of the unknowns (packed order)
   // geometry on the device
-  Buf<double> ax, ay, ax_mid, ay_mid, ay_u, ax_v, kappa, vol_rho, mvol_rho, inlet;
+  Buf<double> ax, ay, kappa, ikappa, vol_rho, mvol_rho, inlet;
+  Buf<double> cxx, cyy, cxy, cyx, axx, ayy, axy, ayx, aout;
   Buf<uint8_t> flags;
   Buf<int32_t> cell_type, merge_of;
   Buf<int64_t> ms, mm, d_act;
@@ -736,8 +732,8 @@ void momentum(gm_cc* c, bool adv, const double* X, const double* inl, double nu,
   const double rnu = c->rho * nu;
   const int64_t nv = (int64_t)(c->ny + 1) * (c->nx + 1);
   counted();
-  if (adv) k_cc_flux<true><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, inl, rnu, c->rho, c->slip, c->flux);
-  else k_cc_flux<false><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, inl, rnu, c->rho, c->slip, c->flux);
+  if (adv) k_cc_flux<true><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, inl, rnu, c->slip, c->flux);
+  else k_cc_flux<false><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, inl, rnu, c->slip, c->flux);
   const int nfix = adv ? c->fix.n_adv : c->fix.n_dif;
   if (nfix > 0) {
     counted();
@@ -746,8 +742,8 @@ void momentum(gm_cc* c, bool adv, const double* X, const double* inl, double nu,
     else k_cc_fix<false><<<nb, 256, 0, st>>>(c->geo, c->fix, X, inl, rnu, c->rho, c->flux);
   }
   counted();
-  if (adv) k_cc_accum<true><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, c->rho, c->flux, c->Rw.p);
-  else k_cc_accum<false><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, c->rho, c->flux, c->Rw.p);
+  if (adv) k_cc_accum<true><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, c->flux, c->Rw.p);
+  else k_cc_accum<false><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, c->flux, c->Rw.p);
   const bool shear = !adv && nu != 0.0;
   if (shear && c->wall.n > 0) {
     counted();
@@ -767,7 +763,7 @@ void vec(gm_cc* c, int op, int64_t n, const double* a, const double* b, const do
 
 void grad(gm_cc* c, const double* P, double* Y, cudaStream_t st) {
   counted();
-  k_cc_grad<<<nblk(c->F), CC_TPB, 0, st>>>(c->geo, P, c->rho * c->dx, c->rho * c->dy, Y);
+  k_cc_grad<<<nblk(c->F), CC_TPB, 0, st>>>(c->geo, P, 1.0 / (c->rho * c->dx), 1.0 / (c->rho * c->dy), Y);
 }
 
 void maxdiff(gm_cc* c, int64_t n, const double* a, const double* b, const double* cc, double s, unsigned long long* out,
@@ -786,7 +782,7 @@ void project(gm_cc* c, const double* q, double step, double* out, double* phi, i
   k_cc_pdiv<<<std::min<unsigned>(nblk(c->psize), 1216), CC_TPB, 0, st>>>(c->geo, gmi::pressure_residual(c->P),
                                                                         step / c->rho, &c->diag.p->pdiv[rec]);
   counted();
-  k_cc_correct<<<nblk(c->F), CC_TPB, 0, st>>>(c->geo, q, phi, step / c->rho, out);
+  k_cc_correct<<<nblk(c->F), CC_TPB, 0, st>>>(c->geo, q, phi, (step / c->rho) / c->dx, (step / c->rho) / c->dy, out);
 }
 
 // H x = x - dt/2 L x on packed vectors (L the viscous operator without the inlet)
@@ -877,7 +873,9 @@ void step_body(gm_cc* c, double dt, gm_cc::Graph& gr, cudaStream_t st) {
   const int64_t F = c->F, Pn = c->psize;
   const double* inl = c->inlet.p;
   auto mark = [&](int k) {
-    if (c->phase_on) CCK(cudaEventRecord(c->pev[k], st));
+    // inside a capture an event record node needs the external flag (a plain record only
+    // orders the captured streams)
+    if (c->phase_on) CCK(cudaEventRecordWithFlags(c->pev[k], st, cudaEventRecordExternal));
   };
   mark(0);
   CCK(cudaMemsetAsync(c->diag.p, 0, offsetof(CcDiagDev, forces), st));
@@ -1007,7 +1005,8 @@ void initial_state(gm_cc* c, const std::vector<double>& inlet, const int32_t* ce
   k_cc_pdiv<<<std::min<unsigned>(nblk(c->psize), 1216), CC_TPB, 0, st>>>(c->geo, gmi::pressure_residual(c->P),
                                                                         1.0 / c->rho, &c->diag.p->pdiv[1]);
   counted();
-  k_cc_correct<<<nblk(c->F), CC_TPB, 0, st>>>(c->geo, c->U.p, c->phi.p, 1.0 / c->rho, c->tmp.p);
+  k_cc_correct<<<nblk(c->F), CC_TPB, 0, st>>>(c->geo, c->U.p, c->phi.p, (1.0 / c->rho) / c->dx, (1.0 / c->rho) / c->dy,
+                                             c->tmp.p);
   counted();
   k_cc_unpack<<<nblk(c->F), CC_TPB, 0, st>>>(c->geo, c->tmp.p, c->inlet.p, c->U.p);
   CCK(cudaMemsetAsync(c->Pst.p, 0, c->psize * sizeof(double), st));
@@ -1076,11 +1075,30 @@ int gm_cc_create(const gm_cc_config* cfg, gm_cc** out) {
     const int64_t nvert = (int64_t)(ny + 1) * (nx + 1);
     C->ax.upload(vec_of(cfg->ax, us), st);
     C->ay.upload(vec_of(cfg->ay, C->vsize), st);
-    C->ax_mid.upload(vec_of(cfg->ax_mid, Pn), st);
-    C->ay_mid.upload(vec_of(cfg->ay_mid, Pn), st);
-    C->ay_u.upload(vec_of(cfg->ay_u, nvert), st);
-    C->ax_v.upload(vec_of(cfg->ax_v, nvert), st);
     C->kappa.upload(vec_of(cfg->volume_fraction, Pn), st);
+    {
+      // folded factors of the structured kernels (see CcGeo)
+      const double dx = C->dx, dy = C->dy, rho = cfg->rho;
+      std::vector<double> cxx(Pn), cyy(Pn), axx(Pn), ayy(Pn), cxy(nvert), cyx(nvert), axy(nvert), ayx(nvert), aout(ny),
+          ik(Pn);
+      for (int64_t c = 0; c < Pn; ++c) {
+        cxx[c] = cfg->ax_mid[c] * dy / dx;
+        cyy[c] = cfg->ay_mid[c] * dx / dy;
+        axx[c] = rho * cfg->ax_mid[c] * dy;
+        ayy[c] = rho * cfg->ay_mid[c] * dx;
+        ik[c] = cfg->cell_type[c] == 0 ? 1.0 / cfg->volume_fraction[c] : 1.0;
+      }
+      for (int64_t t = 0; t < nvert; ++t) {
+        cxy[t] = cfg->ay_u[t] * dx / dy;
+        cyx[t] = cfg->ax_v[t] * dy / dx;
+        axy[t] = rho * cfg->ay_u[t] * dx;
+        ayx[t] = rho * cfg->ax_v[t] * dy;
+      }
+      for (int j = 0; j < ny; ++j) aout[j] = rho * cfg->ax[(int64_t)j * (nx + 1) + nx] * dy;
+      C->cxx.upload(cxx, st); C->cyy.upload(cyy, st); C->axx.upload(axx, st); C->ayy.upload(ayy, st);
+      C->cxy.upload(cxy, st); C->cyx.upload(cyx, st); C->axy.upload(axy, st); C->ayx.upload(ayx, st);
+      C->aout.upload(aout, st); C->ikappa.upload(ik, st);
+    }
     C->cell_type.upload(vec_of(cfg->cell_type, Pn), st);
     C->inlet.upload(inlet, st);
     // face flags and volumes (fluid: fraction >= 0.3 and open; solid: covered face)
@@ -1094,7 +1112,7 @@ int gm_cc_create(const gm_cc_config* cfg, gm_cc** out) {
       if (u ? act_u[k] : act_v[k]) fl[f] |= F_ACTIVE;
       if (fr >= 0.3 && ap > 0.0) fl[f] |= F_FLUID;
       if (ap == 0.0) fl[f] |= F_SOLID;
-      vr[f] = cfg->rho * (u ? cfg->u_vol[k] : cfg->v_vol[k]);
+      vr[f] = 1.0 / (cfg->rho * (u ? cfg->u_vol[k] : cfg->v_vol[k]));
     }
     C->flags.upload(fl, st);
     C->vol_rho.upload(vr, st);
@@ -1110,7 +1128,7 @@ int gm_cc_create(const gm_cc_config* cfg, gm_cc** out) {
         const int32_t idx = (int32_t)ms.size();
         ms.push_back(off + s);
         mm.push_back(off + m);
-        mv.push_back(cfg->rho * eff[s]);
+        mv.push_back(1.0 / (cfg->rho * eff[s]));
         mof[off + s] = idx;
         mof[off + m] = idx;
       }
@@ -1216,9 +1234,13 @@ int gm_cc_create(const gm_cc_config* cfg, gm_cc** out) {
     // kernel arguments
     CcGeo& G = C->geo;
     G.nx = nx; G.ny = ny; G.usize = us; G.vsize = C->vsize; G.psize = Pn; G.F = F; G.dx = C->dx; G.dy = C->dy;
-    G.ax = C->ax.p; G.ay = C->ay.p; G.ax_mid = C->ax_mid.p; G.ay_mid = C->ay_mid.p; G.ay_u = C->ay_u.p;
-    G.ax_v = C->ax_v.p; G.flags = C->flags.p; G.cell_type = C->cell_type.p; G.kappa = C->kappa.p;
-    G.vol_rho = C->vol_rho.p; G.merge_of = C->merge_of.p; G.ms = C->ms.p; G.mm = C->mm.p; G.mvol_rho = C->mvol_rho.p;
+    G.idx = 1.0 / C->dx; G.idy = 1.0 / C->dy;
+    G.ax = C->ax.p; G.ay = C->ay.p;
+    G.cxx = C->cxx.p; G.cyy = C->cyy.p; G.cxy = C->cxy.p; G.cyx = C->cyx.p;
+    G.axx = C->axx.p; G.ayy = C->ayy.p; G.axy = C->axy.p; G.ayx = C->ayx.p; G.aout = C->aout.p;
+    G.flags = C->flags.p; G.cell_type = C->cell_type.p; G.kappa = C->kappa.p; G.ikappa = C->ikappa.p;
+    G.ivol_rho = C->vol_rho.p; G.merge_of = C->merge_of.p; G.ms = C->ms.p; G.mm = C->mm.p;
+    G.imvol_rho = C->mvol_rho.p;
     CcFix& X = C->fix;
     X.n_dif = (int)dface.size(); X.dfam = C->dfam.p; X.dface = C->dface.p; X.dptr = C->dptr.p; X.dcol = C->dcol.p;
     X.dval = C->dval.p;
