@@ -16,6 +16,11 @@ the ratio.  The workload is bench.py's default (800x820, seeded v perturbation);
 Helmholtz-building step is excluded.  Run here, not on the GPU machine (the reference is not there):
 
     python oracle/time_reference_stub.py --reference <path of the reference checkout> [--steps 2]
+
+With ``--path cut_cell`` it times the reference's cut-cell AB2/CN step instead
+(MAC_CylinderFlow(boundary='cut_cell'), CutCellBoundary.advance_ab2_cn: numpy and scipy, no
+Numba kernel on that path) on bench.py's cutcell_800x820_re100 workload, after setup and the
+start-up step.
 """
 from __future__ import annotations
 
@@ -67,15 +72,54 @@ def time_reference(w, steps, scipy_spmv):
     return w['nx'] * w['ny'] * steps / el, el
 
 
+def time_cut_cell(w, steps):
+    from main import MAC_CylinderFlow
+    kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
+    t0 = time.perf_counter()
+    s = MAC_CylinderFlow(boundary='cut_cell', time_scheme='ab2_cn', pressure_solver='direct', verbose=False, **kw)
+    setup = time.perf_counter() - t0
+    active_u = s.cut_geom.ax[:, 1:] > 0
+    active_v = s.cut_geom.ay[1:-1, :] > 0
+    nu_active = int(active_u.sum())
+
+    def pack(u, v):
+        return np.r_[u[:, 1:][active_u], v[1:-1][active_v]]
+
+    def unpack(q):
+        u, v = s.u.copy(), np.zeros_like(s.v)
+        u[:, 1:][active_u] = q[:nu_active]
+        v[1:-1][active_v] = q[nu_active:]
+        return u, v
+    seeded(s, w, pack, unpack, nu_active)
+    s.solve(n_steps=1, dt=w['dt'], perturb_transient=False, save_artifacts=False, verbose=False)
+    t0 = time.perf_counter()
+    s.solve(n_steps=steps, dt=w['dt'], perturb_transient=False, save_artifacts=False, verbose=False)
+    el = time.perf_counter() - t0
+    return w['nx'] * w['ny'] * steps / el, el, setup
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', type=Path, required=True, help='path of the reference checkout')
     ap.add_argument('--steps', type=int, default=2)
+    ap.add_argument('--path', choices=('ghost_cell', 'cut_cell'), default='ghost_cell')
     args = ap.parse_args()
     sys.path.insert(0, str(ROOT))
     sys.path.insert(0, str(ROOT / 'tests' / 'golden'))
     import bench
     import make_golden
+    if args.path == 'cut_cell':
+        w = bench.CUTCELL_WORKLOADS['cutcell_800x820_re100']
+        work = Path(tempfile.mkdtemp(prefix='ghost_ref_time_'))
+        try:
+            make_golden.build_harness(args.reference, work)
+            rate, el, setup = time_cut_cell(w, args.steps)
+        finally:
+            shutil.rmtree(work, ignore_errors=True)
+        print(json.dumps(dict(workload='cutcell_800x820_re100', threads=1,
+                              reference=dict(value=rate, steps=args.steps, seconds=el, setup_seconds=setup)),
+                         indent=2))
+        return
     w = bench.WORKLOADS[bench.DEFAULT_WORKLOAD]
     out = dict(workload=bench.DEFAULT_WORKLOAD, threads=1)
     rate, steps, el = bench.oracle_rate(w, args.steps, 600.0, 1)
