@@ -13,7 +13,12 @@ to rounding.
 from __future__ import annotations
 
 import ctypes as C
+import hashlib
+import json
+import os
+import tempfile
 import time as _time
+from pathlib import Path
 
 import numpy as np
 
@@ -22,6 +27,7 @@ from ._lib import lib, ptr
 from .cutcell_geometry import CutCellSetup
 
 FAMILIES = (('u', 'x'), ('u', 'y'), ('v', 'x'), ('v', 'y'))
+_PKG = Path(__file__).resolve().parent
 
 
 def _check(rc, handle=None):
@@ -276,6 +282,7 @@ class CutCellFlow:
         self.u = np.empty((self.ny, self.nx + 1))
         self.v = np.empty((self.ny + 1, self.nx))
         self.p = np.empty((self.ny, self.nx))
+        self.phi = np.zeros((self.ny, self.nx))
         self._pull()
         self.time = 0.0
         self.run_options = {}
@@ -441,3 +448,96 @@ class CutCellFlow:
     def divergence_stats(self):
         """(max |div|, rms div, max |net flux|) of the state (calculate_cut_cell_divergence)."""
         return self.cc.divergence_stats()
+
+    # -- checkpoints (schema 1, solver/main.py:503-567)
+    def _source_hashes(self):
+        files = ['cutcell.py', 'cutcell_geometry.py', '_lib.py', 'csrc/cutcell.cu', 'csrc/ghostmac.cu',
+                 'csrc/kernels.cu', 'csrc/kernels.cuh', 'csrc/transforms.cuh', 'csrc/geometry.cpp',
+                 'csrc/geometry.hpp', 'csrc/internal.hpp']
+        return {name: hashlib.sha256((_PKG / name).read_bytes()).hexdigest() for name in files}
+
+    def metadata(self, dt, n_steps, perturb_transient=True, perturb_duration=None, perturb_amp=.15):
+        if perturb_duration is None:
+            perturb_duration = 2.5 * self.D / self.U_ref
+        return dict(nx=self.nx, ny=self.ny, Lx=self.Lx, Ly=self.Ly, D=self.D, xc=self.xc, yc=self.yc, nu=self.nu,
+                    rho=self.rho, U_ref=self.U_ref, U_inf=self.U_inf, U_m=self.U_m, inflow=self.inflow,
+                    slip_walls=self.slip_walls, dt=dt, n_steps=n_steps, end_time=self.time, boundary=self.boundary,
+                    transport=self.transport, time_integrator='AB2_CN_discrete_incremental',
+                    time_scheme=self.time_scheme, pressure_solver=self.pressure_solver,
+                    pressure_backend='cut_cell_fft_boundary_schur',
+                    pressure_preconditioner=self.cc.pressure_inverse_info, perturb_transient=perturb_transient,
+                    perturb_duration=perturb_duration, perturb_amp=perturb_amp, source_sha256=self._source_hashes())
+
+    def save_checkpoint(self, path, *, overwrite=False):
+        """Atomic schema-1 checkpoint with the cut-cell AB2/CN history (solver/main.py:503-530):
+        the state, the inlet, cn_advection (packed) and cn_pressure, cn_dt."""
+        path = Path(path)
+        if path.exists() and not overwrite:
+            raise FileExistsError(path)
+        path.parent.mkdir(parents=True, exist_ok=True)
+        adv, half, cn_dt = self.cc.history()
+        arrays = dict(u=self.u, v=self.v, p=self.p, phi=self.phi, u_inlet=self.u_inlet)
+        if adv is not None:
+            arrays.update(cn_advection=adv, cn_pressure=half)
+        meta = dict(schema=1, configuration=self.configuration, time=self.time, run_options=self.run_options,
+                    prev_dt=None, cn_dt=cn_dt, diagnostics=self.last_step_diagnostics,
+                    source_sha256=self._source_hashes())
+        tmp = None
+        try:
+            with tempfile.NamedTemporaryFile(dir=path.parent, suffix='.npz', delete=False) as stream:
+                tmp = Path(stream.name)
+                np.savez(stream, checkpoint_metadata=json.dumps(meta), **arrays)
+                stream.flush()
+                os.fsync(stream.fileno())
+            os.replace(tmp, path)
+        finally:
+            if tmp is not None and tmp.exists():
+                tmp.unlink()
+
+    @classmethod
+    def from_checkpoint(cls, path, *, check_sources=True, accept_reference=False):
+        """Resume a schema-1 cut-cell checkpoint (solver/main.py:532-567, cut-cell branch); one
+        written by the reference's own save_checkpoint is imported when ``accept_reference`` is
+        set and rejected as a source mismatch otherwise."""
+        with np.load(path, allow_pickle=False) as data:
+            meta = json.loads(str(data['checkpoint_metadata']))
+            if meta.get('schema') != 1 or meta['configuration'].get('boundary') != 'cut_cell':
+                raise ValueError('Unsupported checkpoint')
+            sources = meta.get('source_sha256') or {}
+            from_reference = 'cut_cell_solver.py' in sources and 'compiled_engine' in sources
+            if from_reference and not accept_reference:
+                raise ValueError('Checkpoint source mismatch: written by the reference solver '
+                                 '(from_checkpoint(..., accept_reference=True) imports it)')
+            config = dict(meta['configuration'])
+            config['verbose'] = False
+            solver = cls(**config)
+            if check_sources and not from_reference and sources != solver._source_hashes():
+                raise ValueError('Checkpoint source mismatch')
+            solver.restored_from = 'reference' if from_reference else 'library'
+            for name in ('u', 'v', 'p', 'phi', 'u_inlet'):
+                value = data[name]
+                target = getattr(solver, name)
+                if value.shape != target.shape or not np.isfinite(value).all():
+                    raise ValueError(f'Invalid checkpoint field: {name}')
+                target[:] = value
+            solver.time = float(meta['time'])
+            if not np.isfinite(solver.time) or solver.time < 0:
+                raise ValueError('Invalid checkpoint time')
+            solver.run_options = meta['run_options']
+            solver.last_step_diagnostics = meta['diagnostics']
+            hist = {}
+            for name in ('cn_advection', 'cn_pressure'):
+                value = data[name].copy() if name in data else None
+                if value is not None and not np.isfinite(value).all():
+                    raise ValueError(f'Invalid checkpoint history: {name}')
+                hist[name] = value
+            cn_dt = meta['cn_dt']
+            if solver.time > 0:
+                adv, half = hist['cn_advection'], hist['cn_pressure']
+                if (adv is None or adv.shape != (solver.cc.qsize,) or half is None or half.shape != solver.p.shape
+                        or cn_dt is None or not np.isfinite(cn_dt) or cn_dt <= 0):
+                    raise ValueError('Incomplete AB2/CN checkpoint history')
+            solver._push()
+            if hist['cn_advection'] is not None:
+                solver.cc.set_history(hist['cn_advection'], hist['cn_pressure'], cn_dt)
+            return solver

@@ -541,6 +541,10 @@ class MAC_CylinderFlow:
             meta = json.loads(str(data['checkpoint_metadata']))
             if meta.get('schema') != 1 or meta['configuration'].get('boundary') not in ('cut_cell', 'ghost_cell'):
                 raise ValueError('Unsupported checkpoint')
+            if meta['configuration'].get('boundary') == 'cut_cell':
+                from .cutcell import CutCellFlow
+                return CutCellFlow.from_checkpoint(path, check_sources=check_sources,
+                                                   accept_reference=accept_reference)
             sources = meta.get('source_sha256') or {}
             from_reference = 'optimized_ghost_cell.py' in sources and 'compiled_engine' in sources
             if from_reference and not accept_reference:

@@ -361,6 +361,16 @@ def run_cutcell(work):
         out['history_half_p'] = cc.cn_pressure.copy()
         out['history_adv'] = cc.cn_advection.copy()
         if tag == 'cc40x20':
+            # a checkpoint written by the reference's own save_checkpoint after the six steps, and
+            # the fields after the reference resumes it for three steps (solver/main.py:503-567)
+            ck = work / 'reference_checkpoint_cutcell.npz'
+            s.save_checkpoint(ck)
+            shutil.copy(ck, HERE / 'reference_checkpoint_cutcell_cc40x20.npz')
+            r = MAC_CylinderFlow.from_checkpoint(ck)
+            r.solve(n_steps=3, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+            out['resume_u'], out['resume_v'], out['resume_p'] = r.u.copy(), r.v.copy(), r.p.copy()
+            out['resume_scalars'] = np.array([r.time, r.last_step_diagnostics['cd'], r.last_step_diagnostics['cl']])
+        if tag == 'cc40x20':
             # a longer run with the inlet perturbation (solver/main.py:281-286)
             s.solve(n_steps=60, dt=.002, perturb_transient=True, perturb_duration=0.3, save_artifacts=False,
                     verbose=False)

@@ -143,3 +143,41 @@ def test_invalid_configurations():
     with pytest.raises(ValueError, match='strictly inside'):
         pkg.MAC_CylinderFlow(nx=40, ny=20, Lx=4., Ly=2., xc=.4, yc=1., boundary='cut_cell', time_scheme='ab2_cn',
                              verbose=False)
+
+
+def test_checkpoint_round_trip(tmp_path):
+    """save_checkpoint / from_checkpoint of a cut-cell case (solver/main.py:503-567): the resumed
+    solver continues exactly as the original."""
+    pkg = load_package()
+    d = np.load(GOLDEN / 'cutcell_cc40x20.npz')
+    s = make(pkg, d)
+    s.u[:], s.v[:] = d['start_u'], d['start_v']
+    s.solve(n_steps=4, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+    ck = tmp_path / 'cc.npz'
+    s.save_checkpoint(ck)
+    with pytest.raises(FileExistsError):
+        s.save_checkpoint(ck)
+    r = pkg.MAC_CylinderFlow.from_checkpoint(ck)
+    assert isinstance(r, pkg.CutCellFlow) and r.time == s.time
+    for x in (s, r):
+        x.solve(n_steps=3, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+    assert np.max(np.abs(r.u - s.u)) < 1e-14 and np.max(np.abs(r.v - s.v)) < 1e-14
+    assert np.max(np.abs(r.p - s.p)) < 1e-12 * max(1.0, np.max(np.abs(s.p)))
+
+
+def test_reference_checkpoint_resume():
+    """A checkpoint the reference's own save_checkpoint wrote after six cut-cell steps: rejected as
+    a source mismatch by default, imported with accept_reference, and three resumed steps match
+    the reference's own resumed fields."""
+    pkg = load_package()
+    d = np.load(GOLDEN / 'cutcell_cc40x20.npz')
+    ck = GOLDEN / 'reference_checkpoint_cutcell_cc40x20.npz'
+    with pytest.raises(ValueError, match='source mismatch'):
+        pkg.MAC_CylinderFlow.from_checkpoint(ck)
+    r = pkg.MAC_CylinderFlow.from_checkpoint(ck, accept_reference=True)
+    assert r.restored_from == 'reference'
+    r.solve(n_steps=3, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+    t, cd, cl = d['resume_scalars']
+    assert abs(r.time - t) < 1e-12
+    assert rel(r.u, d['resume_u']) < 1e-9 and rel(r.v, d['resume_v']) < 1e-9 and rel(r.p, d['resume_p']) < 1e-7
+    assert abs(r.last_step_diagnostics['cd'] - cd) < 1e-7 * abs(cd)
