@@ -639,6 +639,150 @@ __global__ void k_cc_divstats(CcGeo g, const double* __restrict__ U, double* __r
   }
 }
 
+// ---- Gram-Schmidt of the CN GMRES -------------------------------------------------------
+// Two classical passes per Arnoldi step with the basis read once per pass: k_gs_dot forms the
+// partial dots V^T w; k_gs_pass<NV, NORM> reduces the previous partials to the coefficients
+// (every block in the same fixed order, so all blocks hold identical values), subtracts V c
+// from w and, in the same sweep, forms the partials of the next pass (V^T w) or of |w|^2.
+// One block per SM; NV (the basis size, a compile-time constant per Arnoldi step) keeps the
+// accumulators in registers.
+constexpr int GS_BLOCKS = 152;
+constexpr int GS_THREADS = 512;
+constexpr int GS_MAXV = 32;
+
+template <int NV>
+__device__ __forceinline__ void gs_block_partials(double (&acc)[NV], double* __restrict__ part) {
+  __shared__ double red[GS_THREADS / 32][NV];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    double a = acc[i];
+    for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) red[warp][i] = a;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < NV; i += blockDim.x) {
+    double a = 0.0;
+    for (int q = 0; q < GS_THREADS / 32; ++q) a += red[q][i];
+    part[(int64_t)blockIdx.x * GS_MAXV + i] = a;
+  }
+}
+
+// coefficients c_i = sum over blocks of part[b][i], in a fixed order
+template <int NV>
+__device__ __forceinline__ void gs_coefficients(const double* __restrict__ part, double* cf) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp < NV) {
+    double a = 0.0;
+    for (int b = lane; b < GS_BLOCKS; b += 32) a += part[(int64_t)b * GS_MAXV + warp];
+    for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) cf[warp] = a;
+  }
+  __syncthreads();
+}
+
+template <int NV>
+__global__ void __launch_bounds__(GS_THREADS) k_gs_dot(const double* __restrict__ V, int64_t n,
+                                                       const double* __restrict__ w, double* __restrict__ part) {
+  double acc[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) acc[i] = 0.0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const double wt = w[t];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) acc[i] += V[(int64_t)i * n + t] * wt;
+  }
+  gs_block_partials<NV>(acc, part);
+}
+
+// w -= V c (c from part_in); then part_out = partials of V^T w (NORM = false) or of |w|^2
+// (NORM = true, one value per block); block 0 stores c for the Hessenberg column
+template <int NV, bool NORM>
+__global__ void __launch_bounds__(GS_THREADS) k_gs_pass(const double* __restrict__ V, int64_t n,
+                                                        const double* __restrict__ part_in, double* __restrict__ w,
+                                                        double* __restrict__ part_out, double* __restrict__ coef) {
+  __shared__ double cf[NV];
+  gs_coefficients<NV>(part_in, cf);
+  if (blockIdx.x == 0)
+    for (int i = threadIdx.x; i < NV; i += blockDim.x) coef[i] = cf[i];
+  constexpr int NA = NORM ? 1 : NV;
+  double acc[NA];
+#pragma unroll
+  for (int i = 0; i < NA; ++i) acc[i] = 0.0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    double v[NV];
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      v[i] = V[(int64_t)i * n + t];
+      s += cf[i] * v[i];
+    }
+    const double wt = w[t] - s;
+    w[t] = wt;
+    if (NORM) acc[0] += wt * wt;
+    else {
+#pragma unroll
+      for (int i = 0; i < NA; ++i) acc[i] += v[i] * wt;
+    }
+  }
+  gs_block_partials<NA>(acc, part_out);
+}
+
+// V0 = b - w with the partials of |V0|^2 (the residual that starts a restart cycle)
+__global__ void __launch_bounds__(GS_THREADS) k_gs_residual(const double* __restrict__ b, const double* __restrict__ w,
+                                                            int64_t n, double* __restrict__ r,
+                                                            double* __restrict__ part) {
+  double acc[1] = {0.0};
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const double v = b[t] - w[t];
+    r[t] = v;
+    acc[0] += v * v;
+  }
+  gs_block_partials<1>(acc, part);
+}
+
+// the sum of one partial per block, in a fixed order, into out[0]
+__global__ void k_gs_sum(const double* __restrict__ part, double* __restrict__ out) {
+  double a = 0.0;
+  for (int b = threadIdx.x; b < GS_BLOCKS; b += 32) a += part[(int64_t)b * GS_MAXV];
+  for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if (threadIdx.x == 0) out[0] = a;
+}
+
+template <int NV>
+void gs_step_nv(const double* V, int64_t n, double* w, double* part1, double* part2, double* d1, double* d2,
+                cudaStream_t st) {
+  counted();
+  k_gs_dot<NV><<<GS_BLOCKS, GS_THREADS, 0, st>>>(V, n, w, part1);
+  counted();
+  k_gs_pass<NV, false><<<GS_BLOCKS, GS_THREADS, 0, st>>>(V, n, part1, w, part2, d1);
+  counted();
+  k_gs_pass<NV, true><<<GS_BLOCKS, GS_THREADS, 0, st>>>(V, n, part2, w, part1, d2);
+}
+
+// both Gram-Schmidt passes of Arnoldi step j (basis V_0..V_j) on w; d1, d2 the coefficients,
+// |w|^2 into wn2.  Up to 12 basis vectors the fused passes keep their values in registers;
+// beyond that (steps that converged problems rarely reach) the separate dot / update kernels
+// (part1 then holds multidot_blocks(n) x 64 partials).
+void gs_step(int nv, const double* V, int64_t n, double* w, double* part1, double* part2, double* d1, double* d2,
+             double* wn2, cudaStream_t st) {
+  switch (nv) {
+#define GS_CASE(K) case K: gs_step_nv<K>(V, n, w, part1, part2, d1, d2, st); break;
+    GS_CASE(1) GS_CASE(2) GS_CASE(3) GS_CASE(4) GS_CASE(5) GS_CASE(6) GS_CASE(7) GS_CASE(8) GS_CASE(9)
+    GS_CASE(10) GS_CASE(11) GS_CASE(12)
+#undef GS_CASE
+    default:
+      launch_multidot(V, n, nv, w, n, part1, d1, st);
+      launch_multiaxpy(V, n, nv, d1, -1.0, 1.0, w, n, st);
+      launch_multidot(V, n, nv, w, n, part1, d2, st);
+      launch_multiaxpy(V, n, nv, d2, -1.0, 1.0, w, n, st);
+      launch_multidot(w, n, 1, w, n, part1, wn2, st);
+      return;
+  }
+  counted();
+  k_gs_sum<<<1, 32, 0, st>>>(part1, wn2);
+}
+
 }  // namespace
 
 // =============================================================================================
@@ -682,7 +826,7 @@ struct gm_cc {
   CcFlux flux{};
   // GMRES(30)
   static constexpr int GM_M = 30;
-  Buf<double> V, gpart, gd1, gd2, gwn, gbeta, gbn, gy, gone;
+  Buf<double> V, gpart, gpart2, gd1, gd2, gwn, gbeta, gbn, gy, gone;
   Buf<int> gnv;
   Buf<GmresDev> gdev;
   // per-step diagnostics
@@ -817,7 +961,10 @@ void gmres(gm_cc* c, const double* b, double* x, double dt, gm_cc::Graph& gr, cu
   double* V = c->V.p;
   auto vec_i = [&](int i) { return V + (int64_t)i * n; };
   cudaStream_t sb1 = gmi::body_stream(c->P, 0), sb2 = gmi::body_stream(c->P, 1);
-  launch_multidot(b, n, 1, b, n, c->gpart.p, c->gbn.p, st);
+  counted();
+  k_gs_dot<1><<<GS_BLOCKS, GS_THREADS, 0, st>>>(b, n, b, c->gpart.p);
+  counted();
+  k_gs_sum<<<1, 32, 0, st>>>(c->gpart.p, c->gbn.p);
   cudaStreamCaptureStatus cs;
   cudaGraph_t top;
   CCK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &top, nullptr, nullptr, nullptr));
@@ -829,9 +976,10 @@ void gmres(gm_cc* c, const double* b, double* x, double dt, gm_cc::Graph& gr, cu
   CCK(cudaStreamBeginCaptureToGraph(sb1, cycle_body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   const long long c1 = kernel_launch_count();
   hmatvec(c, x, dt, vec_i(1), sb1);
-  CCK(cudaMemcpyAsync(vec_i(0), b, n * sizeof(double), cudaMemcpyDeviceToDevice, sb1));
-  launch_multiaxpy(vec_i(1), n, 1, c->gone.p, -1.0, 1.0, vec_i(0), n, sb1);
-  launch_multidot(vec_i(0), n, 1, vec_i(0), n, c->gpart.p, c->gbeta.p, sb1);
+  counted();
+  k_gs_residual<<<GS_BLOCKS, GS_THREADS, 0, sb1>>>(b, vec_i(1), n, vec_i(0), c->gpart.p);
+  counted();
+  k_gs_sum<<<1, 32, 0, sb1>>>(c->gpart.p, c->gbeta.p);
   GmresHandles hs{};
   hs.count = m;
   cudaGraph_t cyc_graph;
@@ -847,11 +995,7 @@ void gmres(gm_cc* c, const double* b, double* x, double dt, gm_cc::Graph& gr, cu
     const long long c2 = kernel_launch_count();
     double* wv = vec_i(j + 1);
     hmatvec(c, vec_i(j), dt, wv, sb2);
-    launch_multidot(V, n, j + 1, wv, n, c->gpart.p, c->gd1.p, sb2);
-    launch_multiaxpy(V, n, j + 1, c->gd1.p, -1.0, 1.0, wv, n, sb2);
-    launch_multidot(V, n, j + 1, wv, n, c->gpart.p, c->gd2.p, sb2);
-    launch_multiaxpy(V, n, j + 1, c->gd2.p, -1.0, 1.0, wv, n, sb2);
-    launch_multidot(wv, n, 1, wv, n, c->gpart.p, c->gwn.p, sb2);
+    gs_step(j + 1, V, n, wv, c->gpart.p, c->gpart2.p, c->gd1.p, c->gd2.p, c->gwn.p, sb2);
     launch_gm_step_end(c->gdev.p, j, c->gd1.p, c->gd2.p, c->gwn.p, j + 1 < m ? hs.step[j + 1] : hs.step[0],
                        j + 1 < m, sb2);
     launch_gm_scale(wv, n, c->gdev.p, sb2);
@@ -1268,7 +1412,8 @@ int gm_cc_create(const gm_cc_config* cfg, gm_cc** out) {
     C->pb.alloc(std::max(1, gmi::surface(C->P).n));
     const int m = gm_cc::GM_M;
     C->V.alloc((size_t)(m + 1) * F);
-    C->gpart.alloc((size_t)multidot_blocks(F) * 64);
+    C->gpart.alloc(std::max<size_t>((size_t)GS_BLOCKS * GS_MAXV, (size_t)multidot_blocks(F) * 64));
+    C->gpart2.alloc((size_t)GS_BLOCKS * GS_MAXV);
     for (Buf<double>* b : {&C->gd1, &C->gd2, &C->gy}) b->alloc(64);
     for (Buf<double>* b : {&C->gwn, &C->gbeta, &C->gbn, &C->gone}) b->alloc(1);
     C->gnv.alloc(1);

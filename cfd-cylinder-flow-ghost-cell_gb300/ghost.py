@@ -584,6 +584,17 @@ class MAC_CylinderFlow:
             return solver
 
 
+def _constructor_signature(cls):
+    """The constructor keywords of cls.__init__ (without self), so that inspect.signature of the
+    class reports them rather than the dispatching __new__'s (*args, **kwargs)."""
+    import inspect
+    sig = inspect.signature(cls.__init__)
+    return sig.replace(parameters=list(sig.parameters.values())[1:])
+
+
+MAC_CylinderFlow.__signature__ = _constructor_signature(MAC_CylinderFlow)
+
+
 class CylinderBatch:
     """Independent ``MAC_CylinderFlow`` cases advanced together on one GPU.
 
