@@ -9,15 +9,16 @@
 // reference's over q.
 //
 // Momentum right-hand side (compute_momentum_rhs, solver/cut_cell_solver.py:790-957), one
-// evaluation = five launches:
+// evaluation = three launches:
 //   k_cc_flux    the four face-flux families on the aperture-weighted staggered faces
-//   k_cc_fix     curved faces near the cylinder: advective fluxes from the streamfunction fit
-//                at Gauss points, or viscous fluxes from the fitted / ring-corrected gradient
-//   k_cc_accum   flux differences into the staggered control volumes (natural outlet row)
-//   k_cc_wall    one block: wall shear at the circle's Gauss points, added in the reference's
-//                order per owning face, then the covered-volume transfers to their owners
-//   k_cc_final   division by rho * owned volume, small-cell merging, covered faces zero, and
-//                the packed output (or the CN operator x - dt/2 a for GMRES)
+//   k_cc_fix     curved faces near the cylinder, one warp per face: advective fluxes from the
+//                streamfunction fit at Gauss points, or viscous fluxes from the fitted /
+//                ring-corrected gradient, then the wall shear at the circle's Gauss points
+//   k_cc_rhs     flux differences into the staggered control volumes (natural outlet row), the
+//                wall shear added in the reference's order and the covered-volume transfers
+//                (on the few flagged faces), division by rho * owned volume, small-cell
+//                merging, covered faces zero, and the packed output (or the CN operator
+//                x - dt/2 a for GMRES)
 // The CN system is solved by GMRES(30) without a preconditioner (scipy.sparse.linalg.gmres of
 // solver/time_integration.py:99-101, rtol 1e-12, atol 1e-13) with its control on the device:
 // one WHILE node per restart cycle, one IF node per Arnoldi step, two classical Gram-Schmidt
@@ -26,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -77,12 +79,11 @@ struct Buf {
 };
 
 constexpr int CC_TPB = 256;
-constexpr int CC_WALL_THREADS = 1024;
 constexpr int CC_FORCE_THREADS = 512;
 inline unsigned nblk(int64_t n, int t = CC_TPB) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
 inline void counted() { note_launch_ext(); }
 
-enum : uint8_t { F_ACTIVE = 1, F_FLUID = 2, F_SOLID = 4 };
+enum : uint8_t { F_ACTIVE = 1, F_FLUID = 2, F_SOLID = 4, F_AUX = 8 };
 
 // geometry of the face grid (kernel argument)
 // GB300 issues FP64 at 1/64 of the FP32 rate, so every per-point factor that does not depend on
@@ -150,6 +151,13 @@ struct CcWall {
   int n_don;
   const int64_t* don;
   double* tau;  // n scratch
+  // faces flagged F_AUX (wall targets, owners, donors), sorted, with their target and owner
+  // list entries (-1: none) and whether they are donors
+  int n_aux;
+  const int64_t* aux_face;
+  const int32_t* aux_tgt;
+  const int32_t* aux_own;
+  const uint8_t* aux_don;
 };
 
 struct CcFlux {
@@ -253,17 +261,23 @@ __global__ void k_cc_flux(CcGeo g, const double* __restrict__ X, const double* _
 // Curved faces (solver/staggered_wall.py:134-140 and the viscous correction of
 // solver/cut_cell_solver.py:822-825), one warp per face: ADV: -rho * sum over the face's Gauss
 // points of length * (u u | u v | v v) with u, v from the fit; otherwise rho nu (gradient row .
-// field).
+// field), and then one warp per wall Gauss point for its shear stress (wscale = -rho nu).
 template <bool ADV>
-__global__ void k_cc_fix(CcGeo g, CcFix fx, const double* __restrict__ X, const double* __restrict__ inl, double rnu,
-                         double rho, CcFlux F) {
+__global__ void k_cc_fix(CcGeo g, CcFix fx, CcWall w, const double* __restrict__ X, const double* __restrict__ inl,
+                         double rnu, double rho, double wscale, CcFlux F) {
   const int lane = threadIdx.x & 31;
   const int r = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   double* fam[4] = {F.xx, F.xy, F.yx, F.yy};
   if (!ADV) {
-    if (r >= fx.n_dif) return;
-    const double acc = warp_row_dot(fx.dptr, fx.dcol, fx.dval, r, g, X, inl, lane);
-    if (lane == 0) fam[fx.dfam[r]][fx.dface[r]] = rnu * acc;
+    if (r < fx.n_dif) {
+      const double acc = warp_row_dot(fx.dptr, fx.dcol, fx.dval, r, g, X, inl, lane);
+      if (lane == 0) fam[fx.dfam[r]][fx.dface[r]] = rnu * acc;
+    } else if (r < fx.n_dif + w.n) {
+      // wall shear stress -rho nu (rate . field) at Gauss point k (solver/cut_cell_solver.py:921-924)
+      const int k = r - fx.n_dif;
+      const double acc = warp_row_dot(w.ptr, w.col, w.val, k, g, X, inl, lane);
+      if (lane == 0) w.tau[k] = wscale * acc;
+    }
   } else {
     if (r >= fx.n_adv) return;
     const int fm = fx.afam[r];
@@ -278,93 +292,105 @@ __global__ void k_cc_fix(CcGeo g, CcFix fx, const double* __restrict__ X, const 
   }
 }
 
-// Flux differences (solver/cut_cell_solver.py:853-861, 916-917); one thread per vertex (j, i):
-// the u face (j, i) when j < ny, the v face (j, i) when i < nx.
+// Flux differences of face f (solver/cut_cell_solver.py:853-861, 916-917; the natural outlet
+// row of u at :857-861)
 template <bool ADV>
-__global__ void k_cc_accum(CcGeo g, const double* __restrict__ X, CcFlux F, double* __restrict__ R) {
+__device__ __forceinline__ double rhs_base(const CcGeo& g, const CcFlux& F, const double* __restrict__ X, int64_t f) {
   const int nx = g.nx, ny = g.ny;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (int64_t)(ny + 1) * (nx + 1)) return;
-  const int j = (int)(t / (nx + 1)), i = (int)(t % (nx + 1));
-  if (j < ny) {
-    const int64_t f = (int64_t)j * (nx + 1) + i;
-    double r = 0.0;
-    if (i >= 1 && i < nx) {
-      r = (F.xx[(int64_t)j * nx + i] - F.xx[(int64_t)j * nx + i - 1]) + (F.xy[f + nx + 1] - F.xy[f]);
-    } else if (i == nx) {
+  if (f < g.usize) {
+    const int j = (int)(f / (nx + 1)), i = (int)(f % (nx + 1));
+    if (i >= 1 && i < nx)
+      return (F.xx[(int64_t)j * nx + i] - F.xx[(int64_t)j * nx + i - 1]) + (F.xy[f + nx + 1] - F.xy[f]);
+    if (i == nx) {
       double ext = 0.0;
       if (ADV) {
         const double un = X[f];
         ext = -(un * un * g.aout[j]);
       }
-      r = (ext - F.xx[(int64_t)j * nx + nx - 1]) + 0.5 * (F.xy[f + nx + 1] - F.xy[f]);
+      return (ext - F.xx[(int64_t)j * nx + nx - 1]) + 0.5 * (F.xy[f + nx + 1] - F.xy[f]);
     }
-    R[f] = r;
+    return 0.0;
   }
-  if (i < nx) {
-    const int64_t c = (int64_t)j * nx + i;
-    double r = 0.0;
-    if (j >= 1 && j < ny)
-      r = (F.yx[(int64_t)j * (nx + 1) + i + 1] - F.yx[(int64_t)j * (nx + 1) + i]) + (F.yy[c] - F.yy[c - nx]);
-    R[g.usize + c] = r;
-  }
+  const int64_t c = f - g.usize;
+  const int j = (int)(c / nx), i = (int)(c % nx);
+  if (j >= 1 && j < ny)
+    return (F.yx[(int64_t)j * (nx + 1) + i + 1] - F.yx[(int64_t)j * (nx + 1) + i]) + (F.yy[c] - F.yy[c - nx]);
+  return 0.0;
 }
 
-// wall shear stress -rho nu (rate . field) at the circle's Gauss points, one warp per point
-__global__ void k_cc_wall_tau(CcGeo g, CcWall w, const double* __restrict__ X, const double* __restrict__ inl,
-                              double scale) {
-  const int lane = threadIdx.x & 31;
-  const int k = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  if (k >= w.n) return;
-  const double acc = warp_row_dot(w.ptr, w.col, w.val, k, g, X, inl, lane);
-  if (lane == 0) w.tau[k] = scale * acc;
+__device__ __forceinline__ int aux_find(const CcWall& w, int64_t f) {
+  int lo = 0, hi = w.n_aux - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (w.aux_face[mid] < f) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
 }
 
-// One block: the wall shear tau t ds added to the owning u / v faces in the order of the points
-// (np.add.at), then the covered-volume transfers (donor values to their owners in donor order,
-// donors zero) (solver/cut_cell_solver.py:921-928, solver/staggered_wall.py:302-304).
-__global__ void __launch_bounds__(1024) k_cc_wall(CcGeo g, CcWall w, int shear, double* __restrict__ R) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  if (shear) {
-    for (int t = tid; t < w.n_tgt; t += nt) {
-      const int64_t f = w.tgt[t];
-      const double* dir = f < g.usize ? w.tx : w.ty;
-      double acc = R[f];
-      for (int64_t q = w.tptr[t]; q < w.tptr[t + 1]; ++q) {
-        const int k = w.tk[q];
-        acc += w.tau[k] * dir[k] * w.ds[k];
-      }
-      R[f] = acc;
+// right-hand side of face f after the wall shear (added in the order of the Gauss points,
+// np.add.at of solver/cut_cell_solver.py:922-924)
+template <bool ADV>
+__device__ double rhs_walled(const CcGeo& g, const CcFlux& F, const CcWall& w, const double* __restrict__ X,
+                             int64_t f, int shear, int a) {
+  double r = rhs_base<ADV>(g, F, X, f);
+  const int t = a >= 0 ? w.aux_tgt[a] : -1;
+  if (shear && t >= 0) {
+    const double* dir = f < g.usize ? w.tx : w.ty;
+    for (int64_t q = w.tptr[t]; q < w.tptr[t + 1]; ++q) {
+      const int k = w.tk[q];
+      r += w.tau[k] * dir[k] * w.ds[k];
     }
-    __syncthreads();
   }
-  for (int t = tid; t < w.n_own; t += nt) {
-    const int64_t f = w.own[t];
-    double acc = R[f];
-    for (int64_t q = w.optr[t]; q < w.optr[t + 1]; ++q) acc += R[w.odon[q]];
-    R[f] = acc;
-  }
-  __syncthreads();
-  for (int t = tid; t < w.n_don; t += nt) R[w.don[t]] = 0.0;
+  return r;
 }
 
-// Accelerations with merging (solver/cut_cell_solver.py:930-955).  mode 0: Y = packed a;
-// 1: Y = packed (X - hdt a) (the CN operator); 2: Y = a and Rout = rhs, both unpacked.
-__global__ void k_cc_final(CcGeo g, const double* __restrict__ R, const double* __restrict__ X, double hdt, int mode,
-                           double* __restrict__ Y, double* __restrict__ Rout) {
+// the full right-hand side of face f: flux differences, wall shear, then the covered-volume
+// transfers (donors give their whole value to their owner in donor order and hold zero;
+// solid/staggered_wall.py:302-304)
+template <bool ADV>
+__device__ double rhs_full(const CcGeo& g, const CcFlux& F, const CcWall& w, const double* __restrict__ X, int64_t f,
+                           int shear) {
+  if (!(g.flags[f] & F_AUX)) return rhs_base<ADV>(g, F, X, f);
+  const int a = aux_find(w, f);
+  if (w.aux_don[a]) return 0.0;
+  double r = rhs_walled<ADV>(g, F, w, X, f, shear, a);
+  const int o = w.aux_own[a];
+  if (o >= 0)
+    for (int64_t q = w.optr[o]; q < w.optr[o + 1]; ++q) {
+      const int64_t d = w.odon[q];
+      r += rhs_walled<ADV>(g, F, w, X, d, shear, (g.flags[d] & F_AUX) ? aux_find(w, d) : -1);
+    }
+  return r;
+}
+
+// Right-hand side and accelerations in one pass (solver/cut_cell_solver.py:853-955): flux
+// differences, wall shear and covered transfers (flagged faces only), division by rho x owned
+// volume (a multiply by the host-formed reciprocal), small-cell merging, covered faces zero.
+// mode 0: Y = packed a; 1: Y = packed (X - hdt a) (the CN operator); 2: Y = a and Rout = rhs,
+// both unpacked.
+template <bool ADV>
+__global__ void k_cc_rhs(CcGeo g, CcFlux F, CcWall w, const double* __restrict__ X, int shear, double hdt, int mode,
+                         double* __restrict__ Y, double* __restrict__ Rout) {
   const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= g.F) return;
   const uint8_t fl = g.flags[f];
+  const double r = rhs_full<ADV>(g, F, w, X, f, shear);
   double a = 0.0;
-  if (fl & F_FLUID) a = R[f] * g.ivol_rho[f];
+  if (fl & F_FLUID) a = r * g.ivol_rho[f];
   const int m = g.merge_of[f];
-  if (m >= 0) a = (R[g.ms[m]] + R[g.mm[m]]) * g.imvol_rho[m];
+  if (m >= 0) {
+    const int64_t fs = g.ms[m], fm = g.mm[m];
+    const double rs = fs == f ? r : rhs_full<ADV>(g, F, w, X, fs, shear);
+    const double rm = fm == f ? r : rhs_full<ADV>(g, F, w, X, fm, shear);
+    a = (rs + rm) * g.imvol_rho[m];
+  }
   if (fl & F_SOLID) a = 0.0;
   if (mode == 0) Y[f] = (fl & F_ACTIVE) ? a : 0.0;
   else if (mode == 1) Y[f] = (fl & F_ACTIVE) ? X[f] - hdt * a : 0.0;
   else {
     Y[f] = a;
-    Rout[f] = (fl & F_SOLID) ? 0.0 : R[f];
+    Rout[f] = (fl & F_SOLID) ? 0.0 : r;
   }
 }
 
@@ -810,7 +836,9 @@ struct gm_cc {
   Buf<double> dval, uval, vval, alen;
   // wall and transfers
   Buf<int64_t> wptr, wcol, tgt, tptr, own, optr, odon, don;
-  Buf<int32_t> tk;
+  Buf<int32_t> tk, aux_tgt, aux_own;
+  Buf<int64_t> aux_face;
+  Buf<uint8_t> aux_don;
   Buf<double> wval, wtx, wty, wds, tau;
   CcGeo geo{};
   CcFix fix{};
@@ -875,28 +903,20 @@ void momentum(gm_cc* c, bool adv, const double* X, const double* inl, double nu,
               double* Rout, cudaStream_t st) {
   const double rnu = c->rho * nu;
   const int64_t nv = (int64_t)(c->ny + 1) * (c->nx + 1);
+  const bool shear = !adv && nu != 0.0;
   counted();
   if (adv) k_cc_flux<true><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, inl, rnu, c->slip, c->flux);
   else k_cc_flux<false><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, inl, rnu, c->slip, c->flux);
-  const int nfix = adv ? c->fix.n_adv : c->fix.n_dif;
-  if (nfix > 0) {
+  const int nrows = adv ? c->fix.n_adv : c->fix.n_dif + (shear ? c->wall.n : 0);
+  if (nrows > 0) {
     counted();
-    const unsigned nb = nblk((int64_t)nfix * 32, 256);
-    if (adv) k_cc_fix<true><<<nb, 256, 0, st>>>(c->geo, c->fix, X, inl, rnu, c->rho, c->flux);
-    else k_cc_fix<false><<<nb, 256, 0, st>>>(c->geo, c->fix, X, inl, rnu, c->rho, c->flux);
+    const unsigned nb = nblk((int64_t)nrows * 32, 256);
+    if (adv) k_cc_fix<true><<<nb, 256, 0, st>>>(c->geo, c->fix, c->wall, X, inl, rnu, c->rho, 0.0, c->flux);
+    else k_cc_fix<false><<<nb, 256, 0, st>>>(c->geo, c->fix, c->wall, X, inl, rnu, c->rho, (-c->rho) * nu, c->flux);
   }
   counted();
-  if (adv) k_cc_accum<true><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, c->flux, c->Rw.p);
-  else k_cc_accum<false><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, c->flux, c->Rw.p);
-  const bool shear = !adv && nu != 0.0;
-  if (shear && c->wall.n > 0) {
-    counted();
-    k_cc_wall_tau<<<nblk((int64_t)c->wall.n * 32, 256), 256, 0, st>>>(c->geo, c->wall, X, inl, (-c->rho) * nu);
-  }
-  counted();
-  k_cc_wall<<<1, CC_WALL_THREADS, 0, st>>>(c->geo, c->wall, shear ? 1 : 0, c->Rw.p);
-  counted();
-  k_cc_final<<<nblk(c->F), CC_TPB, 0, st>>>(c->geo, c->Rw.p, X, hdt, mode, Y, Rout);
+  if (adv) k_cc_rhs<true><<<nblk(c->F), CC_TPB, 0, st>>>(c->geo, c->flux, c->wall, X, 0, hdt, mode, Y, Rout);
+  else k_cc_rhs<false><<<nblk(c->F), CC_TPB, 0, st>>>(c->geo, c->flux, c->wall, X, shear ? 1 : 0, hdt, mode, Y, Rout);
 }
 
 void vec(gm_cc* c, int op, int64_t n, const double* a, const double* b, const double* cc, const double* d,
@@ -1258,7 +1278,6 @@ int gm_cc_create(const gm_cc_config* cfg, gm_cc** out) {
       if (ap == 0.0) fl[f] |= F_SOLID;
       vr[f] = 1.0 / (cfg->rho * (u ? cfg->u_vol[k] : cfg->v_vol[k]));
     }
-    C->flags.upload(fl, st);
     C->vol_rho.upload(vr, st);
     // merges in list order; a face written by several keeps the last
     std::vector<int32_t> mof(F, -1);
@@ -1331,6 +1350,29 @@ int gm_cc_create(const gm_cc_config* cfg, gm_cc** out) {
     C->tgt.upload(tgt, st);
     C->tptr.upload(tptr, st);
     C->tk.upload(tk, st);
+    // faces with wall shear, owners and donors: the sorted list the fused right-hand side
+    // kernel searches (flag F_AUX)
+    std::map<int64_t, std::array<int32_t, 3>> aux;  // face -> target entry, owner entry, donor
+    for (size_t t = 0; t < tgt.size(); ++t) aux.emplace(tgt[t], std::array<int32_t, 3>{-1, -1, 0})
+                                               .first->second[0] = (int32_t)t;
+    for (size_t o = 0; o < own.size(); ++o) aux.emplace(own[o], std::array<int32_t, 3>{-1, -1, 0})
+                                               .first->second[1] = (int32_t)o;
+    for (int64_t d : donors) aux.emplace(d, std::array<int32_t, 3>{-1, -1, 0}).first->second[2] = 1;
+    std::vector<int64_t> aux_face;
+    std::vector<int32_t> aux_tgt, aux_own;
+    std::vector<uint8_t> aux_don;
+    for (auto& kv : aux) {
+      aux_face.push_back(kv.first);
+      aux_tgt.push_back(kv.second[0]);
+      aux_own.push_back(kv.second[1]);
+      aux_don.push_back((uint8_t)kv.second[2]);
+      fl[kv.first] |= F_AUX;
+    }
+    C->flags.upload(fl, st);
+    C->aux_face.upload(aux_face, st);
+    C->aux_tgt.upload(aux_tgt, st);
+    C->aux_own.upload(aux_own, st);
+    C->aux_don.upload(aux_don, st);
     // curved-face overrides of the four families
     std::vector<uint8_t> dfam, afam;
     std::vector<int64_t> dface, dptr{0}, dcol, aface, apptr{0}, uptr{0}, ucol, vptr{0}, vcol;
@@ -1396,6 +1438,8 @@ int gm_cc_create(const gm_cc_config* cfg, gm_cc** out) {
     W.ds = C->wds.p; W.n_tgt = (int)tgt.size(); W.tgt = C->tgt.p; W.tptr = C->tptr.p; W.tk = C->tk.p;
     W.n_own = (int)own.size(); W.own = C->own.p; W.optr = C->optr.p; W.odon = C->odon.p;
     W.n_don = (int)donors.size(); W.don = C->don.p; W.tau = C->tau.p;
+    W.n_aux = (int)aux_face.size(); W.aux_face = C->aux_face.p; W.aux_tgt = C->aux_tgt.p; W.aux_own = C->aux_own.p;
+    W.aux_don = C->aux_don.p;
     // state and work arrays
     for (Buf<double>* b : {&C->U, &C->prev_adv, &C->q0, &C->now, &C->d0, &C->gp, &C->mid, &C->halfq, &C->expl,
                            &C->offset, &C->dq, &C->rhs, &C->star, &C->w, &C->result, &C->action, &C->tmp, &C->zero,
