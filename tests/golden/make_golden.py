@@ -378,6 +378,41 @@ def run_cutcell(work):
             out['long_u'], out['long_v'], out['long_p'] = s.u.copy(), s.v.copy(), s.p.copy()
             out['long_scalars'] = np.array([float(d[key]) for key in keys] + [s.time])
         save(f'cutcell_{tag}', **out)
+    run_cutcell_wide(work)
+
+
+def run_cutcell_wide(work):
+    """The benched cut-cell grid (bench.py workload cutcell_800x820_re100: 800x820, 40D x 41D,
+    Re 100, the seeded 1e-2 v perturbation of the projected initial state): three reference
+    steps, stored as 4000 seeded sample values per field and per step plus the field norms and
+    the force coefficients (the full fields would be tens of megabytes)."""
+    from main import MAC_CylinderFlow
+    kw = dict(nx=800, ny=820, Lx=40.0, Ly=41.0, D=1.0, xc=10.0, yc=20.5, nu=0.01)
+    s = MAC_CylinderFlow(boundary='cut_cell', time_scheme='ab2_cn', pressure_solver='direct', verbose=False, **kw)
+    g = s.cut_geom
+    active_u, active_v = g.ax[:, 1:] > 0, g.ay[1:-1, :] > 0
+    nu_active = int(active_u.sum())
+    q = np.r_[s.u[:, 1:][active_u], s.v[1:-1][active_v]]
+    q[nu_active:] += 1e-2 * np.random.default_rng(0).standard_normal(q.size - nu_active)
+    s.u[:, 1:][active_u] = q[:nu_active]
+    s.v[1:-1][active_v] = q[nu_active:]
+    pick = np.random.default_rng(1)
+    su = np.sort(pick.choice(s.u.size, 4000, replace=False))
+    sv = np.sort(pick.choice(s.v.size, 4000, replace=False))
+    sp_ = np.sort(pick.choice(s.p.size, 4000, replace=False))
+    fields, scal = [], []
+    for k in range(3):
+        s.solve(n_steps=1, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+        d = s.last_step_diagnostics
+        scal.append([d['cd'], d['cl'], d['max_divergence'], d['cfl'], d['momentum_iterations']])
+        fields.append((s.u.ravel()[su].copy(), s.v.ravel()[sv].copy(), s.p.ravel()[sp_].copy(),
+                       np.abs(s.u).max(), np.abs(s.v).max(), np.abs(s.p).max(),
+                       float(np.sqrt(np.mean(s.u ** 2))), float(np.sqrt(np.mean(s.v ** 2))),
+                       float(np.sqrt(np.mean(s.p ** 2)))))
+    save('cutcell_wide_800x820', sample_u=su, sample_v=sv, sample_p=sp_,
+         u_samples=np.array([f[0] for f in fields]), v_samples=np.array([f[1] for f in fields]),
+         p_samples=np.array([f[2] for f in fields]), norms=np.array([f[3:] for f in fields]),
+         scalars=np.array(scal))
 
 
 def run_modal(work):

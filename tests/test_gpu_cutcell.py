@@ -181,3 +181,30 @@ def test_reference_checkpoint_resume():
     assert abs(r.time - t) < 1e-12
     assert rel(r.u, d['resume_u']) < 1e-9 and rel(r.v, d['resume_v']) < 1e-9 and rel(r.p, d['resume_p']) < 1e-7
     assert abs(r.last_step_diagnostics['cd'] - cd) < 1e-7 * abs(cd)
+
+
+def test_benched_grid_against_reference():
+    """The benched grid (800x820, 40D x 41D, Re 100) from bench.py's seeded 1e-2 v perturbation:
+    three steps against the reference's own three steps (tests/golden/cutcell_wide_800x820.npz:
+    4000 seeded samples per field and step, the field norms and the force coefficients)."""
+    import sys
+    pkg = load_package()
+    d = np.load(GOLDEN / 'cutcell_wide_800x820.npz')
+    sys.path.insert(0, str(GOLDEN.parents[1]))
+    import bench
+    w = bench.CUTCELL_WORKLOADS['cutcell_800x820_re100']
+    kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
+    s = pkg.MAC_CylinderFlow(boundary='cut_cell', time_scheme='ab2_cn', verbose=False, **kw)
+    bench.seeded_state(s, w)
+    for k in range(3):
+        s.solve(n_steps=1, dt=w['dt'], perturb_transient=False, save_artifacts=False, verbose=False)
+        diag = s.last_step_diagnostics
+        cd, cl, mdiv, cfl, its = d['scalars'][k]
+        for got, ref, scale in ((s.u.ravel()[d['sample_u']], d['u_samples'][k], d['norms'][k][0]),
+                                (s.v.ravel()[d['sample_v']], d['v_samples'][k], d['norms'][k][1])):
+            assert np.max(np.abs(got - ref)) < 1e-9 * max(1.0, scale), k
+        assert np.max(np.abs(s.p.ravel()[d['sample_p']] - d['p_samples'][k])) < 1e-7 * max(1.0, d['norms'][k][2]), k
+        assert abs(float(np.sqrt(np.mean(s.u ** 2))) - d['norms'][k][3]) < 1e-10
+        assert abs(diag['cd'] - cd) < 1e-7 * abs(cd) and abs(diag['cl'] - cl) < 1e-7 * max(1.0, abs(cl))
+        assert diag['max_divergence'] < 1e-10 and abs(diag['cfl'] - cfl) < 1e-9
+        assert abs(diag['momentum_iterations'] - its) <= 2
