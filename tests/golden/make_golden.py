@@ -378,7 +378,28 @@ def run_cutcell(work):
             out['long_u'], out['long_v'], out['long_p'] = s.u.copy(), s.v.copy(), s.p.copy()
             out['long_scalars'] = np.array([float(d[key]) for key in keys] + [s.time])
         save(f'cutcell_{tag}', **out)
+    run_cutcell_options(work)
     run_cutcell_wide(work)
+
+
+def run_cutcell_options(work):
+    """The cut-cell options on the 40x20 grid: parabolic inflow, slip channel walls and the
+    reference's CG/boundary-Schur-DCT pressure solver ('cg_dct'); four steps from the projected
+    initial state."""
+    from main import MAC_CylinderFlow
+    kw = dict(nx=40, ny=20, Lx=4., Ly=2., D=1., xc=1.1, yc=0.95, nu=0.02, inflow='parabolic', U_m=1.2,
+              slip_walls=True, pressure_solver='cg_dct')
+    s = MAC_CylinderFlow(boundary='cut_cell', time_scheme='ab2_cn', verbose=False, **kw)
+    out = dict(init_u=s.u.copy(), init_v=s.v.copy(), u_inlet=s.u_inlet.copy())
+    scal, fields = [], []
+    for k in range(4):
+        s.solve(n_steps=1, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+        d = s.last_step_diagnostics
+        scal.append([d['cd'], d['cl'], d['max_divergence'], d['cfl']])
+        fields.append((s.u.copy(), s.v.copy(), s.p.copy()))
+    save('cutcell_options_40x20', **out, step_u=np.array([f[0] for f in fields]),
+         step_v=np.array([f[1] for f in fields]), step_p=np.array([f[2] for f in fields]),
+         scalars=np.array(scal))
 
 
 def run_cutcell_wide(work):

@@ -208,3 +208,25 @@ def test_benched_grid_against_reference():
         assert abs(diag['cd'] - cd) < 1e-7 * abs(cd) and abs(diag['cl'] - cl) < 1e-7 * max(1.0, abs(cl))
         assert diag['max_divergence'] < 1e-10 and abs(diag['cfl'] - cfl) < 1e-9
         assert abs(diag['momentum_iterations'] - its) <= 2
+
+
+def test_options_parabolic_slip_cg_dct():
+    """Parabolic inflow (U_m = 1.2), slip channel walls and pressure_solver='cg_dct' on the 40x20
+    grid: the initial projection and four steps against the reference run with the same options
+    (the reference's CG / boundary-Schur-DCT solve and this library's direct inverse meet the same
+    1e-10 divergence budget, so the fields agree to it)."""
+    pkg = load_package()
+    d = np.load(GOLDEN / 'cutcell_options_40x20.npz')
+    s = pkg.MAC_CylinderFlow(nx=40, ny=20, Lx=4., Ly=2., D=1., xc=1.1, yc=0.95, nu=0.02, inflow='parabolic',
+                             U_m=1.2, slip_walls=True, pressure_solver='cg_dct', boundary='cut_cell',
+                             time_scheme='ab2_cn', verbose=False)
+    assert np.array_equal(s.u_inlet, d['u_inlet'])
+    assert rel(s.u, d['init_u']) < 1e-9 and rel(s.v, d['init_v']) < 1e-9
+    for k in range(4):
+        s.solve(n_steps=1, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+        cd, cl, mdiv, cfl = d['scalars'][k]
+        assert rel(s.u, d['step_u'][k]) < 1e-8 and rel(s.v, d['step_v'][k]) < 1e-8, k
+        assert rel(s.p, d['step_p'][k]) < 1e-6, k
+        diag = s.last_step_diagnostics
+        assert abs(diag['cd'] - cd) < 1e-6 * abs(cd) and abs(diag['cl'] - cl) < 1e-6 * max(1.0, abs(cl))
+        assert diag['max_divergence'] < 1e-10
