@@ -21,7 +21,7 @@ GATE_NAMES = {1: 'projection', 2: 'momentum', 3: 'pressure', 4: 'pressure_rhs', 
 SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_last_error', 'gm_get_sizes',
            'gm_set_stream', 'gm_get_indices', 'gm_get_ghost_stencils', 'gm_get_schur_rows',
            'gm_get_surface_points', 'gm_set_state', 'gm_get_state', 'gm_set_inlet', 'gm_set_history',
-           'gm_get_history', 'gm_step', 'gm_apply', 'gm_project', 'gm_pressure_solve', 'gm_rectangle_solve',
+           'gm_get_history', 'gm_step', 'gm_solve_io', 'gm_apply', 'gm_project', 'gm_pressure_solve', 'gm_rectangle_solve',
            'gm_surface_forces', 'gm_divergence_stats', 'gm_kernel_launches', 'gm_kernel_timing',
            'gm_divergence_stats_noalloc', 'gm_batch_create', 'gm_batch_destroy', 'gm_batch_last_error',
            'gm_batch_step', 'gm_phase_timing', 'gm_tg_create', 'gm_tg_destroy', 'gm_tg_last_error',
@@ -140,6 +140,7 @@ def _load():
         'gm_set_history': ([P, I32, P, P, D], C.c_int),
         'gm_get_history': ([P, C.POINTER(I32), P, P, C.POINTER(D)], C.c_int),
         'gm_step': ([P, D, I32, I64, D, C.POINTER(StepDiag)], C.c_int),
+        'gm_solve_io': ([P, P, P, P, P, D, I32, I64, D, C.POINTER(StepDiag), P, P, P], C.c_int),
         'gm_apply': ([P, I32, D, P, P], C.c_int),
         'gm_project': ([P, D, P, P, P, C.POINTER(SolveInfo)], C.c_int),
         'gm_pressure_solve': ([P, P, P, C.POINTER(SolveInfo)], C.c_int),

@@ -2170,6 +2170,101 @@ void create_device(gm_handle* H) {
   CK(cudaMemsetAsync(H->pw2.p, 0, H->Pn * sizeof(double), st));
 }
 
+// The step loop of gm_step: n_steps steps in graph batches of up to RING_CAP, the step records
+// read back after each batch, the state returned to the last good step on a failed gate.
+// before_last_sync (may be empty) enqueues work on the stream after the last batch, before the
+// loop's final synchronisation.
+void step_loop(gm_handle* h, double dt, int32_t n_steps, int64_t first_step_index, double start_time,
+               gm_step_diag* diag, const std::function<void()>& before_last_sync) {
+    ensure_helmholtz(h, dt);
+    cudaStream_t st = h->st;
+    CK(cudaMemsetAsync(h->ctl.p, 0, sizeof(StepCtl), st));  // clears the sticky error word
+    long long counter = first_step_index;
+    CK(cudaMemcpyAsync(h->counter.p, &counter, sizeof counter, cudaMemcpyHostToDevice, st));
+    int s = 0;
+    while (s < n_steps) {
+      // steps that differ from the steady pattern run launch by launch: the start-up step,
+      // a changed dt, or per-kernel event timing
+      const bool direct = !h->has_history || h->prev_dt != dt || !h->use_graphs || ktimer_active() || h->rec_rhs;
+      const bool first = !h->has_history;
+      const int batch = direct ? 1 : std::min(n_steps - s, (int)gm_handle::RING_CAP);
+      CK(cudaMemsetAsync(h->ridx.p, 0, sizeof(int), st));
+      if (direct) {
+        step_once(h, dt, ((first_step_index + s) % 100) == 0 ? 1 : 0);
+        swap_state(h);
+      } else {
+        for (int k = 0; k < batch; ++k) {
+          CK(cudaGraphLaunch(step_graph(h, dt), st));
+          swap_state(h);
+        }
+      }
+      CK(cudaMemcpyAsync(h->host_ring, h->ring.p, batch * sizeof(StepCtl), cudaMemcpyDeviceToHost, st));
+      if (s + batch == n_steps && before_last_sync) before_last_sync();
+      CK(cudaStreamSynchronize(st));
+      ktimer_collect();
+      if (h->phase_on && !first)
+        for (int k = 0; k + 1 < gm_handle::NPHASE_EV; ++k) {
+          float ms = 0;
+          if (cudaEventElapsedTime(&ms, h->phase_ev[k], h->phase_ev[k + 1]) == cudaSuccess) h->phase_ms[k] = ms;
+        }
+      if (h->phase_on && !first)
+        for (int k = 0; k + 1 < gm_handle::NSWEEP_EV; ++k) {
+          float ms = 0;
+          if (cudaEventElapsedTime(&ms, h->sweep_ev[k], h->sweep_ev[k + 1]) == cudaSuccess) h->sweep_ms[k] = ms;
+        }
+      cudaGetLastError();
+      int good = 0;
+      while (good < batch && h->host_ring[good].err == 0) ++good;
+      if (!direct) {
+        // kernel nodes the replays executed: outer nodes + one sweep body per refinement iteration
+        const gm_handle::StepGraph& gr = h->graphs[0].exec ? h->graphs[0] : h->graphs[1];
+        long long nodes = 0;
+        for (int k = 0; k < batch; ++k) {
+          const StepCtl& c = h->host_ring[k];
+          nodes += gr.outer_nodes;
+          for (int sl = 0; sl < 5; ++sl) nodes += gr.body_nodes[sl] * c.solve[sl].k;
+        }
+        kernel_launch_adjust(nodes);
+      }
+      for (int k = 0; k < std::min(batch, good + 1); ++k)
+        if (diag) fill_diag(h, h->host_ring[k], start_time + (s + k + 1) * dt, dt, first && k == 0, &diag[s + k]);
+      if (good < batch) {
+        // back to the state after the last good step
+        if ((batch - good) % 2) swap_state(h);
+        if (good > 0) { h->has_history = true; h->prev_dt = dt; }
+        *h->host_ctl = h->host_ring[good];
+        static const char* names[] = {"", "Ghost projection failed", "CN momentum solve failed",
+                                      "Pressure solve failed", "Pressure RHS must be finite",
+                                      "Ghost step failed divergence/CFL gate", "Non-finite force",
+                                      "Explicit timestep unsafe",
+                                      "Finite fields and a positive timestep are required"};
+        const StepCtl& c = h->host_ring[good];
+        throw GateError(c.err, std::string(names[c.gate < 9 ? c.gate : 0]) + " (step)");
+      }
+      h->has_history = true;
+      h->prev_dt = dt;
+      s += batch;
+    }
+}
+
+// environment switches of the step loop, read per call
+void step_switches(gm_handle* h) {
+  const char* hr = std::getenv("GHOSTMAC_HOST_REFINE");
+  h->host_refine = hr && hr[0] == '1';
+  const char* pt = std::getenv("GHOSTMAC_PHASE_TIMING");
+  const bool phase = pt && pt[0] == '1';
+  if (phase != h->phase_on) {
+    // the events become graph nodes: recapture the step graphs with or without them
+    for (auto& gr : h->graphs)
+      if (gr.exec) { cudaGraphExecDestroy(gr.exec); gr.exec = nullptr; }
+    if (phase && !h->phase_ev[0]) {
+      for (auto& e : h->phase_ev) cudaEventCreate(&e);
+      for (auto& e : h->sweep_ev) cudaEventCreate(&e);
+    }
+    h->phase_on = phase;
+  }
+}
+
 }  // namespace
 
 // =============================================================================
@@ -2466,89 +2561,41 @@ int gm_step(gm_handle* h, double dt, int32_t n_steps, int64_t first_step_index, 
   if (!h) return GM_EVALUE;
   if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
   if (!(std::isfinite(dt) && dt > 0) || n_steps <= 0) { h->err = "dt must be finite and positive"; return GM_EVALUE; }
-  const char* hr = std::getenv("GHOSTMAC_HOST_REFINE");
-  h->host_refine = hr && hr[0] == '1';
-  const char* pt = std::getenv("GHOSTMAC_PHASE_TIMING");
-  const bool phase = pt && pt[0] == '1';
-  if (phase != h->phase_on) {
-    // the events become graph nodes: recapture the step graphs with or without them
-    for (auto& gr : h->graphs)
-      if (gr.exec) { cudaGraphExecDestroy(gr.exec); gr.exec = nullptr; }
-    if (phase && !h->phase_ev[0]) {
-      for (auto& e : h->phase_ev) cudaEventCreate(&e);
-      for (auto& e : h->sweep_ev) cudaEventCreate(&e);
-    }
-    h->phase_on = phase;
-  }
+  step_switches(h);
+  return run_guarded(h, [&] { step_loop(h, dt, n_steps, first_step_index, start_time, diag, {}); });
+}
+
+int gm_solve_io(gm_handle* h, const double* u_in, const double* v_in, const double* p_in, const double* u_inlet,
+                double dt, int32_t n_steps, int64_t first_step_index, double start_time, gm_step_diag* diag,
+                double* u_out, double* v_out, double* p_out) {
+  if (!h) return GM_EVALUE;
+  if (h->host_only) { h->err = "host-only handle has no device state"; return GM_ECUDA; }
+  if (!(std::isfinite(dt) && dt > 0) || n_steps <= 0) { h->err = "dt must be finite and positive"; return GM_EVALUE; }
+  step_switches(h);
   return run_guarded(h, [&] {
-    ensure_helmholtz(h, dt);
+    const gm::Geometry& g = h->g;
     cudaStream_t st = h->st;
-    CK(cudaMemsetAsync(h->ctl.p, 0, sizeof(StepCtl), st));  // clears the sticky error word
-    long long counter = first_step_index;
-    CK(cudaMemcpyAsync(h->counter.p, &counter, sizeof counter, cudaMemcpyHostToDevice, st));
-    int s = 0;
-    while (s < n_steps) {
-      // steps that differ from the steady pattern run launch by launch: the start-up step,
-      // a changed dt, or per-kernel event timing
-      const bool direct = !h->has_history || h->prev_dt != dt || !h->use_graphs || ktimer_active() || h->rec_rhs;
-      const bool first = !h->has_history;
-      const int batch = direct ? 1 : std::min(n_steps - s, (int)gm_handle::RING_CAP);
-      CK(cudaMemsetAsync(h->ridx.p, 0, sizeof(int), st));
-      if (direct) {
-        step_once(h, dt, ((first_step_index + s) % 100) == 0 ? 1 : 0);
-        swap_state(h);
-      } else {
-        for (int k = 0; k < batch; ++k) {
-          CK(cudaGraphLaunch(step_graph(h, dt), st));
-          swap_state(h);
-        }
-      }
-      CK(cudaMemcpyAsync(h->host_ring, h->ring.p, batch * sizeof(StepCtl), cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-      ktimer_collect();
-      if (h->phase_on && !first)
-        for (int k = 0; k + 1 < gm_handle::NPHASE_EV; ++k) {
-          float ms = 0;
-          if (cudaEventElapsedTime(&ms, h->phase_ev[k], h->phase_ev[k + 1]) == cudaSuccess) h->phase_ms[k] = ms;
-        }
-      if (h->phase_on && !first)
-        for (int k = 0; k + 1 < gm_handle::NSWEEP_EV; ++k) {
-          float ms = 0;
-          if (cudaEventElapsedTime(&ms, h->sweep_ev[k], h->sweep_ev[k + 1]) == cudaSuccess) h->sweep_ms[k] = ms;
-        }
-      cudaGetLastError();
-      int good = 0;
-      while (good < batch && h->host_ring[good].err == 0) ++good;
-      if (!direct) {
-        // kernel nodes the replays executed: outer nodes + one sweep body per refinement iteration
-        const gm_handle::StepGraph& gr = h->graphs[0].exec ? h->graphs[0] : h->graphs[1];
-        long long nodes = 0;
-        for (int k = 0; k < batch; ++k) {
-          const StepCtl& c = h->host_ring[k];
-          nodes += gr.outer_nodes;
-          for (int sl = 0; sl < 5; ++sl) nodes += gr.body_nodes[sl] * c.solve[sl].k;
-        }
-        kernel_launch_adjust(nodes);
-      }
-      for (int k = 0; k < std::min(batch, good + 1); ++k)
-        if (diag) fill_diag(h, h->host_ring[k], start_time + (s + k + 1) * dt, dt, first && k == 0, &diag[s + k]);
-      if (good < batch) {
-        // back to the state after the last good step
-        if ((batch - good) % 2) swap_state(h);
-        if (good > 0) { h->has_history = true; h->prev_dt = dt; }
-        *h->host_ctl = h->host_ring[good];
-        static const char* names[] = {"", "Ghost projection failed", "CN momentum solve failed",
-                                      "Pressure solve failed", "Pressure RHS must be finite",
-                                      "Ghost step failed divergence/CFL gate", "Non-finite force",
-                                      "Explicit timestep unsafe",
-                                      "Finite fields and a positive timestep are required"};
-        const StepCtl& c = h->host_ring[good];
-        throw GateError(c.err, std::string(names[c.gate < 9 ? c.gate : 0]) + " (step)");
-      }
-      h->has_history = true;
-      h->prev_dt = dt;
-      s += batch;
+    Gate g0{nullptr, 0, 0};
+    if (u_in || v_in) {
+      // the state is unpack(pack(u, v)), as gm_set_state
+      if (!(u_in && v_in)) CK(cudaMemcpyAsync(h->ftmp.p, h->U.p, h->F * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if (u_in) CK(cudaMemcpyAsync(h->ftmp.p, u_in, g.usize * sizeof(double), cudaMemcpyDefault, st));
+      if (v_in) CK(cudaMemcpyAsync(h->ftmp.p + g.usize, v_in, g.vsize * sizeof(double), cudaMemcpyDefault, st));
+      launch_copy_active(h->cls_f.p, h->F, h->ftmp.p, h->U.p, g0, st);
     }
+    if (p_in) CK(cudaMemcpyAsync(h->pout.p, p_in, g.psize * sizeof(double), cudaMemcpyDefault, st));
+    if (u_inlet) CK(cudaMemcpyAsync(h->inlet.p, u_inlet, g.ny * sizeof(double), cudaMemcpyDefault, st));
+    if (u_in || v_in || u_inlet) {
+      launch_set_inlet(h->cd, h->U.p, false, st);
+      ghost_faces(h, h->U.p, g0);
+      CK(cudaMemsetAsync(h->state_max.p, 0, 2 * sizeof(unsigned long long), st));
+      launch_maxabs(h->cd, h->U.p, &h->state_max.p[0], &h->state_max.p[1], g0, st);
+    }
+    step_loop(h, dt, n_steps, first_step_index, start_time, diag, [&] {
+      if (u_out) CK(cudaMemcpyAsync(u_out, h->U.p, g.usize * 8, cudaMemcpyDefault, st));
+      if (v_out) CK(cudaMemcpyAsync(v_out, h->U.p + g.usize, g.vsize * 8, cudaMemcpyDefault, st));
+      if (p_out) CK(cudaMemcpyAsync(p_out, h->pout.p, g.psize * 8, cudaMemcpyDefault, st));
+    });
   });
 }
 

@@ -412,11 +412,15 @@ class MAC_CylinderFlow:
         self.run_options = dict(perturb_transient=perturb_transient, perturb_duration=perturb_duration,
                                 perturb_amp=perturb_amp)
         verbose = self.verbose if verbose is None else verbose
-        self._push()
+        for name in ('u', 'v', 'p'):
+            a = getattr(self, name)
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags['C_CONTIGUOUS']):
+                setattr(self, name, np.ascontiguousarray(a, dtype=np.float64))
         t0 = _time.time()
         start = self.time
         ts, cds, cls = [], [], []
         s = 0
+        pushed = False
         while s < n_steps:
             now_t = start + (s + 1) * dt
             perturbing = perturb_transient and self.inflow == 'uniform' and now_t <= perturb_duration
@@ -434,8 +438,16 @@ class MAC_CylinderFlow:
                     chunk = min(n_steps - s, 1001 - s % 1000 if s % 1000 else 1)
                 else:
                     chunk = n_steps - s
-            self._set_inlet()
-            rc, diag = self.step_raw(dt, chunk, first_index=s, start_time=start + s * dt)
+            # one call per chunk: the state in (first chunk), the inlet, the steps, the state out
+            # (last chunk, or when a callback or the verbose report reads it)
+            self.u_inlet = np.ascontiguousarray(self.u_inlet, dtype=np.float64)
+            pull = s + chunk >= n_steps or step_callback is not None or verbose
+            diag = (_lib.StepDiag * chunk)()
+            st_in = (None, None, None) if pushed else (ptr(self.u), ptr(self.v), ptr(self.p))
+            st_out = (ptr(self.u), ptr(self.v), ptr(self.p)) if pull else (None, None, None)
+            rc = lib.gm_solve_io(self._h, *st_in, ptr(self.u_inlet), float(dt), int(chunk), int(s),
+                                 float(start + s * dt), diag, *st_out)
+            pushed = True
             done = chunk
             if rc != _lib.GM_OK:
                 done = next((k for k in range(chunk) if diag[k].status), chunk)
@@ -450,8 +462,6 @@ class MAC_CylinderFlow:
                 self._pull()
                 check(rc, self._h)
             s += chunk
-            if step_callback is not None or verbose:
-                self._pull()
             if step_callback is not None:
                 step_callback(self, dict(self.last_step_diagnostics))
             if verbose and ((s - 1) % 1000 == 0 or s == n_steps):
@@ -462,7 +472,6 @@ class MAC_CylinderFlow:
                 print(f"Step {s - 1:5d} | Div_RMS: {rms:.2e} | Div_Max: {stats[0]:.2e} | "
                       f"FluxErr: {abs(flux_out - flux_in) / flux_in:.2e} | "
                       f"Cd: {self.last_step_diagnostics['cd']:.4f} | Cl: {self.last_step_diagnostics['cl']:.4f}")
-        self._pull()
         if verbose:
             elapsed = _time.time() - t0
             print(f"Simulation completed in {elapsed:.2f}s ({elapsed / n_steps * 1000:.2f} ms/step)")

@@ -158,6 +158,14 @@ int gm_get_history(gm_handle* h, int32_t* has_history, double* previous_advectio
  * the return value is its class and diag[k].status/gate tell where. */
 int gm_step(gm_handle* h, double dt, int32_t n_steps, int64_t first_step_index, double start_time,
             gm_step_diag* diag);
+/* gm_set_state (u_in, v_in, p_in), gm_set_inlet (u_inlet), gm_step and gm_get_state (u_out,
+ * v_out, p_out) in one call, ordered on the handle's stream with one host synchronisation at the
+ * end (the reference's solve loop, solver/main.py:265-429, as one call per chunk of steps).  Any
+ * pointer may be NULL to skip that transfer.  On a failed gate the outputs may hold the failed
+ * step's state; gm_get_state then reads the last good one. */
+int gm_solve_io(gm_handle* h, const double* u_in, const double* v_in, const double* p_in, const double* u_inlet,
+                double dt, int32_t n_steps, int64_t first_step_index, double start_time, gm_step_diag* diag,
+                double* u_out, double* v_out, double* p_out);
 
 /* --- operators (GhostCellIntegrator methods, solver/optimized_ghost_cell.py:174-234) --- */
 
