@@ -1792,3 +1792,110 @@ int gm_cc_divergence_stats(gm_cc* c, const double* u, const double* v, double ou
 }
 
 }  // extern "C"
+
+// =============================================================================================
+// the pressure system alone (the legacy staircase loop's Poisson solve)
+// =============================================================================================
+struct gm_poisson {
+  std::string err;
+  gm_handle* P = nullptr;
+  int64_t psize = 0;
+  Buf<double> b, x;
+  Buf<double> ikappa;
+  Buf<int32_t> cell_type;
+};
+
+extern "C" {
+
+const char* gm_poisson_last_error(const gm_poisson* p) { return p ? p->err.c_str() : gm_last_error(nullptr); }
+
+int gm_poisson_create(int32_t nx, int32_t ny, double Lx, double Ly, double D, double xc, double yc, const double* ax,
+                      const double* ay, const int32_t* cell_type, const double* kappa, gm_poisson** out) {
+  if (!out || !ax || !ay || !cell_type || !kappa) { gm_internal_set_error("null argument"); return GM_EVALUE; }
+  *out = nullptr;
+  auto q = std::make_unique<gm_poisson>();
+  gm::Geometry g;
+  g.nx = nx; g.ny = ny; g.Lx = Lx; g.Ly = Ly; g.D = D; g.xc = xc; g.yc = yc;
+  g.nu = 1.0; g.rho = 1.0; g.U_inf = 1.0; g.inflow = 0; g.U_m = 0.0;
+  int ec = 0;
+  if (!gm::build_cutcell_geometry(g, ax, ay, cell_type, kappa, ec)) {
+    gm_internal_set_error(g.error.c_str());
+    return ec ? ec : GM_EVALUE;
+  }
+  q->psize = g.psize;
+  std::string perr;
+  int rc = gmi::pressure_create(std::move(g), &q->P, perr);
+  if (rc != GM_OK) {
+    gm_internal_set_error(perr.c_str());
+    return rc;
+  }
+  rc = guarded(nullptr, [&] {
+    cudaStream_t st = gmi::stream(q->P);
+    q->b.alloc(q->psize);
+    q->x.alloc(q->psize);
+    std::vector<double> ik(q->psize);
+    for (int64_t c = 0; c < q->psize; ++c) ik[c] = cell_type[c] == 0 ? 1.0 / kappa[c] : 1.0;
+    q->ikappa.upload(ik, st);
+    q->cell_type.upload(std::vector<int32_t>(cell_type, cell_type + q->psize), st);
+    CCK(cudaStreamSynchronize(st));
+  });
+  if (rc != GM_OK) {
+    gm_poisson_destroy(q.release());
+    return rc;
+  }
+  *out = q.release();
+  return GM_OK;
+}
+
+int gm_poisson_destroy(gm_poisson* p) {
+  if (!p) return GM_OK;
+  gm_handle* P = p->P;
+  if (P) cudaStreamSynchronize(gmi::stream(P));
+  delete p;
+  if (P) gmi::pressure_destroy(P);
+  return GM_OK;
+}
+
+int gm_poisson_solve(gm_poisson* p, const double* rhs, double* phi, double* residual_linf) {
+  if (!p || !rhs || !phi) return GM_EVALUE;
+  int rc = GM_OK;
+  try {
+    cudaStream_t st = gmi::stream(p->P);
+    copy_in(p->b.p, rhs, p->psize, st);
+    CcGeo g{};
+    g.psize = p->psize;
+    g.cell_type = p->cell_type.p;
+    g.ikappa = p->ikappa.p;
+    counted();
+    k_cc_scale_rhs<<<nblk(p->psize), CC_TPB, 0, st>>>(g, p->b.p);
+    CCK(cudaMemsetAsync(gmi::control(p->P), 0, sizeof(StepCtl), st));
+    gmi::pressure_solve(p->P, p->b.p, p->x.p, S_P1);
+    std::string m;
+    rc = gmi::check(p->P, "pressure solve", m);
+    if (rc != GM_OK) throw CcFail(rc, m);
+    if (residual_linf) {
+      unsigned long long* bits = nullptr;
+      CCK(cudaMallocAsync(reinterpret_cast<void**>(&bits), sizeof(unsigned long long), st));
+      CCK(cudaMemsetAsync(bits, 0, sizeof(unsigned long long), st));
+      counted();
+      k_cc_maxdiff<<<std::min<unsigned>(nblk(p->psize), 1216), CC_TPB, 0, st>>>(
+          p->psize, gmi::pressure_residual(p->P), nullptr, nullptr, 0.0, bits);
+      unsigned long long hb = 0;
+      CCK(cudaMemcpyAsync(&hb, bits, sizeof hb, cudaMemcpyDeviceToHost, st));
+      CCK(cudaFreeAsync(bits, st));
+      CCK(cudaStreamSynchronize(st));
+      *residual_linf = bits_to_double(hb);
+    }
+    CCK(cudaMemcpyAsync(phi, p->x.p, p->psize * sizeof(double), cudaMemcpyDefault, st));
+    CCK(cudaStreamSynchronize(st));
+  } catch (const CcFail& e) {
+    p->err = e.msg;
+    return e.cls;
+  } catch (const std::exception& e) {
+    p->err = e.what();
+    return GM_ECUDA;
+  }
+  return GM_OK;
+}
+
+}  // extern "C"

@@ -7,7 +7,8 @@
 //   corrector_cpp              u = u* - dt/rho grad phi with the exact Dirichlet outlet;
 //   calculate_mac_forces_cpp   staircase pressure and shear force sums over the solid cells;
 //   calculate_mac_divergence_cpp  fluid-cell divergence statistics.
-// Here each is one or two grid-parallel kernels.  The per-point arithmetic is written in the
+// Here each is one or two grid-parallel kernels; gm_mac_ab2_rhs adds the loop's own AB2 step on
+// u*, v* and its recomputed Poisson right-hand side (solver/main.py:315-339).  The per-point arithmetic is written in the
 // reference's order and this file is compiled without FMA contraction, so u*, v*, rhs, u and v
 // are bit-identical to the reference's compiled code; the force and divergence sums are
 // reduced per block and then over blocks in a fixed order (deterministic, and equal to the
@@ -117,6 +118,41 @@ __global__ void k_poisson_rhs(const double* __restrict__ us, const double* __res
   if (M_(j, i)) { rhs[t] = 0.0; return; }
   const double div = (US_(j, i + 1) - US_(j, i)) / dx + (VS_(j + 1, i) - VS_(j, i)) / dy;
   rhs[t] = inv_dt * div;
+}
+
+// The legacy loop's AB2 step on the interior faces (solver/main.py:315-322): d = (u* - u) / dt,
+// u* += dt alpha (d - d_prev) when a previous step exists, d_prev = d
+__global__ void k_ab2(const double* __restrict__ u, const double* __restrict__ v, double* __restrict__ us,
+                      double* __restrict__ vs, double* __restrict__ pdu, double* __restrict__ pdv, int nx, int ny,
+                      double dt, double dt_alpha, int has_prev) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nu_ = (long long)ny * (nx + 1), nv_ = (long long)(ny + 1) * nx;
+  if (t < nu_) {
+    const int i = (int)(t % (nx + 1));
+    if (i < 1 || i > nx - 1) return;
+    const double d = (us[t] - u[t]) / dt;
+    if (has_prev) us[t] = us[t] + dt_alpha * (d - pdu[t]);
+    pdu[t] = d;
+  } else if (t < nu_ + nv_) {
+    const long long f = t - nu_;
+    const int j = (int)(f / nx);
+    if (j < 1 || j > ny - 1) return;
+    const double d = (vs[f] - v[f]) / dt;
+    if (has_prev) vs[f] = vs[f] + dt_alpha * (d - pdv[f]);
+    pdv[f] = d;
+  }
+}
+
+// the recomputed Poisson right-hand side of the legacy loop (solver/main.py:337-339):
+// rho/dt ((u*_e - u*_w)/dx + (v*_n - v*_s)/dy), zero on masked cells
+__global__ void k_legacy_rhs(const double* __restrict__ us, const double* __restrict__ vs,
+                             const uint8_t* __restrict__ mask, double* __restrict__ rhs, int nx, int ny, double dx,
+                             double dy, double rho_dt) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)ny * nx) return;
+  const int j = (int)(t / nx), i = (int)(t - (long long)j * nx);
+  if (M_(j, i)) { rhs[t] = 0.0; return; }
+  rhs[t] = rho_dt * ((US_(j, i + 1) - US_(j, i)) / dx + (VS_(j + 1, i) - VS_(j, i)) / dy);
 }
 
 // u = u* - dt/rho d phi/dx, v = v* - dt/rho d phi/dy (bindings.cpp:248-281)
@@ -403,6 +439,36 @@ int gm_mac_corrector(double* u, double* v, const double* u_star, const double* v
                                                               sg.dev<double>(ius), sg.dev<double>(ivs),
                                                               sg.dev<double>(iph), sg.dev<uint8_t>(im),
                                                               sg.dev<double>(ii), nx, ny, dx, dy, dt / rho);
+  gmk::kernel_launch_adjust(1);
+  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e);
+  if (cudaError_t e = sg.finish()) return cuda_fail(e);
+  return GM_OK;
+}
+
+int gm_mac_ab2_rhs(const double* u, const double* v, double* u_star, double* v_star, double* prev_du,
+                   double* prev_dv, double* rhs, const uint8_t* mask, int32_t nx, int32_t ny, double dx, double dy,
+                   double dt, double rho, double alpha, int32_t has_prev, int32_t ab2, void* stream) {
+  if (!u || !v || !u_star || !v_star || !prev_du || !prev_dv || !rhs || !mask) return fail(GM_EVALUE, "null argument");
+  if (int rc = check_grid(nx, ny, dx, dy)) return rc;
+  if (int rc = check_step(dt, rho)) return rc;
+  if (has_prev && !std::isfinite(alpha)) return fail(GM_EVALUE, "alpha must be finite");
+  const size_t nU = (size_t)ny * (nx + 1), nV = (size_t)(ny + 1) * nx, nP = (size_t)ny * nx;
+  Staging sg(static_cast<cudaStream_t>(stream));
+  const int iu = sg.add(u, nU * 8, true, false), iv = sg.add(v, nV * 8, true, false);
+  const int ius = sg.add(u_star, nU * 8, true, true), ivs = sg.add(v_star, nV * 8, true, true);
+  const int idu = sg.add(prev_du, nU * 8, true, true), idv = sg.add(prev_dv, nV * 8, true, true);
+  const int ir = sg.add(rhs, nP * 8, false, true), im = sg.add(mask, nP, true, false);
+  double* extra = nullptr;
+  if (cudaError_t e = sg.begin(0, &extra)) return cuda_fail(e);
+  cudaStream_t st = sg.st;
+  if (ab2) {
+    k_ab2<<<blocks((long long)(nU + nV)), LT, 0, st>>>(sg.dev<double>(iu), sg.dev<double>(iv), sg.dev<double>(ius),
+                                                       sg.dev<double>(ivs), sg.dev<double>(idu), sg.dev<double>(idv),
+                                                       nx, ny, dt, dt * alpha, has_prev ? 1 : 0);
+    gmk::kernel_launch_adjust(1);
+  }
+  k_legacy_rhs<<<blocks((long long)nP), LT, 0, st>>>(sg.dev<double>(ius), sg.dev<double>(ivs), sg.dev<uint8_t>(im),
+                                                     sg.dev<double>(ir), nx, ny, dx, dy, rho / dt);
   gmk::kernel_launch_adjust(1);
   if (cudaError_t e = cudaGetLastError()) return cuda_fail(e);
   if (cudaError_t e = sg.finish()) return cuda_fail(e);

@@ -261,7 +261,8 @@ def _solve_dict(info):
 class MAC_CylinderFlow:
     """Ghost-cell AB2/CN cylinder flow on the GPU (solver/main.py:19-617, ghost_cell/ab2_cn path).
     boundary='cut_cell' (with time_scheme='ab2_cn') constructs the cut-cell path instead
-    (cutcell.CutCellFlow)."""
+    (cutcell.CutCellFlow), boundary='staircase' (with time_scheme='legacy') the legacy staircase
+    loop (staircase.StaircaseFlow)."""
 
     def __new__(cls, *args, **kwargs):
         import inspect
@@ -269,6 +270,9 @@ class MAC_CylinderFlow:
         if bound.get('boundary') == 'cut_cell':
             from .cutcell import CutCellFlow
             return CutCellFlow(*args, **kwargs)
+        if bound.get('boundary') == 'staircase':
+            from .staircase import StaircaseFlow
+            return StaircaseFlow(*args, **kwargs)
         return super().__new__(cls)
 
     def __init__(self, nx=400, ny=100, Lx=20.0, Ly=5.0, D=1.0, xc=5.0, yc=2.5,

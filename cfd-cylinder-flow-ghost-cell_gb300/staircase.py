@@ -1,0 +1,270 @@
+"""MAC_CylinderFlow(boundary='staircase', time_scheme='legacy') on the GPU.
+
+The reference's legacy staircase loop (solver/main.py:245-501 with boundary='staircase'): the
+native predictor and right-hand side (predictor_rhs_cpp), the loop's own AB2 step for centred
+transport and its recomputed Poisson right-hand side, a pressure solve of the staircase Poisson
+matrix (build_poisson_matrix, solver/mac_solver.py:5-87, which the reference factors with a
+sparse LU or solves by ILU-GMRES), the native corrector and the staircase force sums.  Every
+kernel is this library's (gm_mac_*, gm_poisson_*); the state stays on the device between steps
+(torch tensors serve as device buffers), and the host arrays u, v, p are written back after
+each solve() call.  The staircase Poisson matrix is the aperture-weighted cut-cell matrix with
+open fractions 0 or 1 taken from the cell mask, solved to rounding by the boundary-corrected
+separable inverse; both pressure_solver choices of the reference solve that system (the LU
+exactly, ILU-GMRES to rtol 1e-8).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time as _time
+
+import numpy as np
+
+from . import _lib
+from ._lib import lib, ptr
+
+
+def _check_mac(rc):
+    if rc != _lib.GM_OK:
+        raise _lib.error_for(rc, lib.gm_last_error(None).decode(errors='replace'))
+
+
+class StaircaseFlow:
+    """The legacy staircase MAC_CylinderFlow on the GPU (solver/main.py:19-501, boundary='staircase',
+    time_scheme='legacy')."""
+
+    def __init__(self, nx=400, ny=100, Lx=20.0, Ly=5.0, D=1.0, xc=5.0, yc=2.5, nu=0.01, rho=1.0, U_inf=1.0,
+                 inflow='uniform', U_m=None, slip_walls=False, verbose=True, boundary='staircase',
+                 transport='centered', pressure_solver='direct', marker_spacing_factor=1.5, time_scheme='legacy',
+                 ghost_pressure_extension='neumann', ghost_velocity_interpolation='bilinear', precision='fp64'):
+        import torch
+        if boundary not in ('immersed', 'staircase', 'ghost_cell', 'cut_cell') or transport not in ('centered', 'upwind'):
+            raise ValueError('Choose boundary=immersed/staircase/ghost_cell/cut_cell and transport=centered/upwind')
+        if pressure_solver not in ('direct', 'iterative', 'cg_dct'):
+            raise ValueError("pressure_solver must be direct, iterative or cg_dct")
+        if pressure_solver == 'cg_dct' and boundary != 'cut_cell':
+            raise ValueError("cg_dct is supported only for cut_cell")
+        if time_scheme not in ('legacy', 'ab2_cn'):
+            raise ValueError('time_scheme must be legacy or ab2_cn')
+        if time_scheme == 'ab2_cn' and (boundary not in ('cut_cell', 'ghost_cell') or transport != 'centered'):
+            raise ValueError('ab2_cn requires cut_cell/ghost_cell and centered transport')
+        if ghost_pressure_extension not in ('neumann', 'quadratic') or \
+                ghost_velocity_interpolation not in ('bilinear', 'biquadratic'):
+            raise ValueError('Unknown Ghost pressure extension or velocity interpolation')
+        if ghost_pressure_extension != 'neumann' or ghost_velocity_interpolation != 'bilinear':
+            raise ValueError('Ghost reconstruction options require Ghost AB2/CN')
+        if boundary != 'staircase' or time_scheme != 'legacy':
+            raise NotImplementedError('StaircaseFlow implements boundary="staircase", time_scheme="legacy"')
+        if precision != 'fp64':
+            raise NotImplementedError('the staircase path runs in FP64')
+        if any(isinstance(n, bool) or not isinstance(n, (int, np.integer)) or n < 4 for n in (nx, ny)):
+            raise ValueError('nx and ny must be integers >= 4')
+        if not all(np.isfinite(x) and x > 0 for x in (Lx, Ly, D, nu, rho, U_inf)):
+            raise ValueError('Domain lengths, D, nu, rho and U_inf must be finite and positive')
+        if inflow not in ('uniform', 'parabolic'):
+            raise ValueError('inflow must be uniform or parabolic')
+        if U_m is not None and (not np.isfinite(U_m) or U_m <= 0):
+            raise ValueError('U_m must be finite and positive')
+        if not (D / 2 < xc < Lx - D / 2 and D / 2 < yc < Ly - D / 2):
+            raise ValueError('Cylinder must lie strictly inside the channel')
+        self.configuration = dict(nx=nx, ny=ny, Lx=Lx, Ly=Ly, D=D, xc=xc, yc=yc, nu=nu, rho=rho, U_inf=U_inf,
+                                  inflow=inflow, U_m=U_m, slip_walls=slip_walls, boundary=boundary,
+                                  transport=transport, pressure_solver=pressure_solver,
+                                  marker_spacing_factor=marker_spacing_factor, time_scheme=time_scheme,
+                                  verbose=False, ghost_pressure_extension=ghost_pressure_extension,
+                                  ghost_velocity_interpolation=ghost_velocity_interpolation)
+        self.boundary, self.transport, self.pressure_solver, self.time_scheme = boundary, transport, pressure_solver, time_scheme
+        self.verbose = verbose
+        self.nx, self.ny, self.Lx, self.Ly = int(nx), int(ny), float(Lx), float(Ly)
+        self.dx, self.dy = self.Lx / self.nx, self.Ly / self.ny
+        self.D, self.xc, self.yc, self.nu, self.rho, self.U_inf = D, xc, yc, nu, rho, U_inf
+        self.inflow, self.slip_walls = inflow, slip_walls
+        if inflow == 'parabolic':
+            self.U_m = 1.5 * U_inf if U_m is None else U_m
+            self.U_ref = (2.0 / 3.0) * self.U_m
+        else:
+            self.U_m = self.U_ref = U_inf
+        self.Re = self.U_ref * self.D / self.nu
+        self.y_centers = (np.arange(self.ny) + 0.5) * self.dy
+        self.x_centers = (np.arange(self.nx) + 0.5) * self.dx
+        # solid mask of solver/main.py:123-129
+        rr = (((self.x_centers - xc) / (D / 2.0)) ** 2)[None, :] + (((self.y_centers - yc) / (D / 2.0)) ** 2)[:, None]
+        self.mask = rr <= (1.0 + 1e-13)
+        if not self.mask.any() or self.mask[[0, -1], :].any() or self.mask[:, [0, -1]].any():
+            raise ValueError('Grid must resolve the cylinder and a fluid layer at every outer boundary')
+        t0 = _time.time()
+        self.u_inlet = np.empty(self.ny)
+        for j in range(self.ny):
+            y = self.y_centers[j]
+            self.u_inlet[j] = 4.0 * self.U_m * y * (self.Ly - y) / (self.Ly ** 2) if inflow == 'parabolic' else self.U_inf
+        self.u_inlet_base = self.u_inlet.copy()
+        # initial field (solver/main.py:166-177): inlet rows, faces of masked cells zero
+        self.u = np.zeros((self.ny, self.nx + 1))
+        self.v = np.zeros((self.ny + 1, self.nx))
+        self.p = np.zeros((self.ny, self.nx))
+        self.phi = np.zeros((self.ny, self.nx))
+        self.u[:, :] = self.u_inlet[:, None]
+        js, is_ = np.nonzero(self.mask)
+        self.u[js, is_] = 0.0
+        self.u[js, is_ + 1] = 0.0
+        self.v[js, is_] = 0.0
+        self.v[js + 1, is_] = 0.0
+        # the staircase Poisson system: open fractions 0 on faces next to a masked cell
+        m = self.mask
+        ax = np.ones((self.ny, self.nx + 1))
+        ax[:, 1:-1][m[:, :-1] | m[:, 1:]] = 0.0
+        ay = np.ones((self.ny + 1, self.nx))
+        ay[1:-1][m[:-1] | m[1:]] = 0.0
+        ctype = np.where(m, -1, 1).astype(np.int32)
+        kappa = np.where(m, 0.0, 1.0)
+        h = C.c_void_p()
+        rc = lib.gm_poisson_create(self.nx, self.ny, self.Lx, self.Ly, float(D), float(xc), float(yc), ptr(ax),
+                                   ptr(ay), ptr(ctype.view(np.int32)), ptr(kappa), C.byref(h))
+        if rc != _lib.GM_OK:
+            raise _lib.error_for(rc, lib.gm_poisson_last_error(None).decode(errors='replace'))
+        self._poisson = h
+        dev = torch.device('cuda')
+        f64 = dict(dtype=torch.float64, device=dev)
+        self._d = dict(u=torch.empty(self.u.shape, **f64), v=torch.empty(self.v.shape, **f64),
+                       p=torch.empty(self.p.shape, **f64), us=torch.zeros(self.u.shape, **f64),
+                       vs=torch.zeros(self.v.shape, **f64), rhs=torch.zeros(self.p.shape, **f64),
+                       phi=torch.zeros(self.p.shape, **f64), zero_p=torch.zeros(self.p.shape, **f64),
+                       pdu=torch.zeros(self.u.shape, **f64), pdv=torch.zeros(self.v.shape, **f64),
+                       inlet=torch.empty(self.ny, **f64),
+                       mask=torch.from_numpy(np.ascontiguousarray(self.mask, dtype=np.uint8)).to(dev))
+        self._previous_dt = None
+        self.time = 0.0
+        self.run_options = {}
+        self.last_step_diagnostics = {}
+        if verbose:
+            print(f"Staircase legacy MAC on the GPU ready in {_time.time() - t0:.3f}s (Re={self.Re:.1f}).")
+
+    def __del__(self):
+        h = getattr(self, '_poisson', None)
+        if h:
+            lib.gm_poisson_destroy(h)
+            self._poisson = None
+
+    def _stream(self):
+        import torch
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def _push(self):
+        import torch
+        for name, key in (('u', 'u'), ('v', 'v'), ('p', 'p')):
+            self._d[key].copy_(torch.from_numpy(np.ascontiguousarray(getattr(self, name), dtype=np.float64)))
+
+    def _pull(self):
+        for name, key in (('u', 'u'), ('v', 'v'), ('p', 'p'), ('phi', 'phi')):
+            getattr(self, name)[...] = self._d[key].cpu().numpy()
+
+    def _step(self, dt):
+        """One legacy step on the device (solver/main.py:303-378, staircase branch)."""
+        d = self._d
+        st = self._stream()
+        nonincremental = self.transport == 'centered'
+        centered = 1 if self.transport == 'centered' else 0
+        _check_mac(lib.gm_mac_predictor_rhs(ptr(d['u']), ptr(d['v']), ptr(d['us']), ptr(d['vs']), ptr(d['rhs']),
+                                            ptr(d['zero_p'] if nonincremental else d['p']), ptr(d['mask']),
+                                            ptr(d['inlet']), self.nx, self.ny, self.dx, self.dy, float(dt),
+                                            float(self.nu), float(self.rho), 1 if self.slip_walls else 0, centered, st))
+        has_prev = self._previous_dt is not None
+        alpha = dt / (2 * self._previous_dt) if has_prev else 0.0
+        _check_mac(lib.gm_mac_ab2_rhs(ptr(d['u']), ptr(d['v']), ptr(d['us']), ptr(d['vs']), ptr(d['pdu']),
+                                      ptr(d['pdv']), ptr(d['rhs']), ptr(d['mask']), self.nx, self.ny, self.dx,
+                                      self.dy, float(dt), float(self.rho), float(alpha), 1 if has_prev else 0,
+                                      centered, st))
+        if centered:
+            self._previous_dt = dt
+        res = C.c_double()
+        rc = lib.gm_poisson_solve(self._poisson, ptr(d['rhs']), ptr(d['phi']), C.byref(res))
+        if rc != _lib.GM_OK:
+            raise _lib.error_for(rc, lib.gm_poisson_last_error(self._poisson).decode(errors='replace'))
+        _check_mac(lib.gm_mac_corrector(ptr(d['u']), ptr(d['v']), ptr(d['us']), ptr(d['vs']), ptr(d['phi']),
+                                        ptr(d['mask']), ptr(d['inlet']), self.nx, self.ny, self.dx, self.dy, float(dt),
+                                        float(self.rho), 1 if self.slip_walls else 0, st))
+        if nonincremental:
+            d['p'].copy_(d['phi'])
+        else:
+            d['p'].add_(d['phi'])
+        out = np.empty(4)
+        _check_mac(lib.gm_mac_forces(ptr(d['u']), ptr(d['v']), ptr(d['p']), ptr(d['mask']), self.nx, self.ny,
+                                     self.dx, self.dy, float(self.nu * self.rho), ptr(out), st))
+        return out, res.value
+
+    def divergence_stats(self):
+        """calculate_mac_divergence_cpp of the state: (max |div|, sum div^2, fluid count, core sum
+        div^2, core count)."""
+        d = self._d
+        out = np.empty(3)
+        counts = np.empty(2, np.int64)
+        _check_mac(lib.gm_mac_divergence(ptr(d['u']), ptr(d['v']), ptr(d['mask']), self.nx, self.ny, self.dx,
+                                         self.dy, ptr(out), ptr(counts), self._stream()))
+        return out[0], out[1], int(counts[0]), out[2], int(counts[1])
+
+    def solve(self, n_steps=25000, dt=0.002, perturb_transient=True, perturb_duration=None, perturb_amp=0.15,
+              save_artifacts=True, verbose=None, step_callback=None):
+        """Step loop of solver/main.py:245-501 for the legacy staircase path."""
+        import torch
+        if isinstance(n_steps, bool) or not isinstance(n_steps, (int, np.integer)) or n_steps <= 0:
+            raise ValueError('n_steps must be a positive integer')
+        if not np.isfinite(dt) or dt <= 0:
+            raise ValueError('dt must be finite and positive')
+        if perturb_duration is None:
+            perturb_duration = 2.5 * (self.D / self.U_ref)
+        if not np.isfinite(perturb_duration) or perturb_duration <= 0 or not np.isfinite(perturb_amp) or \
+                abs(perturb_amp) >= 1:
+            raise ValueError('Require perturb_duration > 0 and finite |perturb_amp| < 1')
+        self.run_options = dict(perturb_transient=perturb_transient, perturb_duration=perturb_duration,
+                                perturb_amp=perturb_amp)
+        verbose = self.verbose if verbose is None else verbose
+        self._push()
+        d = self._d
+        t0 = _time.time()
+        start = self.time
+        ts, cds, cls = [], [], []
+        denom = 0.5 * self.rho * (self.U_ref ** 2) * self.D
+        for s in range(n_steps):
+            now_t = start + (s + 1) * dt
+            if s % 100 == 0:
+                # explicit advection/diffusion screen (solver/main.py:273-278)
+                rate = (float(d['u'].abs().max()) / self.dx + float(d['v'].abs().max()) / self.dy
+                        + 2 * self.nu * (self.dx ** -2 + self.dy ** -2))
+                if not np.isfinite(rate) or dt * rate > 1.:
+                    self._pull()
+                    raise RuntimeError(f'Explicit timestep unsafe at t={self.time:g}: dt*rate={dt * rate:g}; reduce dt')
+            if perturb_transient and self.inflow == 'uniform' and now_t <= perturb_duration:
+                decay = 1.0 - (now_t / perturb_duration)
+                pert = perturb_amp * np.sin(2.0 * np.pi * self.y_centers / self.Ly) * decay
+                self.u_inlet[:] = self.u_inlet_base * (1.0 + pert)
+            else:
+                self.u_inlet[:] = self.u_inlet_base
+            d['inlet'].copy_(torch.from_numpy(self.u_inlet))
+            (fx_p, fy_p, fx_v, fy_v), res = self._step(dt)
+            fx, fy = fx_p + fx_v, fy_p + fy_v
+            cd, cl = fx / denom, fy / denom
+            if not np.isfinite(cd) or not np.isfinite(cl):
+                self._pull()
+                raise FloatingPointError(f'Non-finite force at t={now_t:g}; results not saved')
+            self.time = now_t
+            self.last_step_diagnostics = dict(time=self.time, dt=dt, cd=float(cd), cl=float(cl),
+                                              cd_pressure=float(fx_p / denom), cd_viscous=float(fx_v / denom),
+                                              cl_pressure=float(fy_p / denom), cl_viscous=float(fy_v / denom),
+                                              pressure_residual_linf=float(res))
+            if step_callback is not None:
+                self._pull()
+                step_callback(self, dict(self.last_step_diagnostics))
+            cds.append(cd)
+            cls.append(cl)
+            ts.append(now_t)
+            if verbose and (s % 1000 == 0 or s == n_steps - 1):
+                max_div, sum_div2, count, _, _ = self.divergence_stats()
+                div_all = np.sqrt(sum_div2 / count) if count > 0 else 0.0
+                self._pull()
+                in_flux, out_flux = np.sum(self.u[:, 0]) * self.dy, np.sum(self.u[:, self.nx]) * self.dy
+                print(f"Step {s:5d} | Div_RMS: {div_all:.2e} | Div_Max: {max_div:.2e} | "
+                      f"FluxErr: {abs(out_flux - in_flux) / in_flux:.2e} | Cd: {cd:.4f} | Cl: {cl:.4f}")
+        self._pull()
+        if verbose:
+            elapsed = _time.time() - t0
+            print(f"Simulation completed in {elapsed:.2f}s ({elapsed / n_steps * 1000:.2f} ms/step)")
+        return np.array(ts), np.array(cds), np.array(cls)

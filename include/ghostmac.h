@@ -312,6 +312,14 @@ int gm_mac_predictor_rhs(const double* u, const double* v, double* u_star, doubl
 int gm_mac_corrector(double* u, double* v, const double* u_star, const double* v_star, const double* phi,
                      const uint8_t* mask, const double* inlet, int32_t nx, int32_t ny, double dx, double dy, double dt,
                      double rho, int32_t slip_walls, void* stream);
+/* The legacy loop's own AB2 step on u*, v* (centred transport, solver/main.py:315-322):
+ * d = (u* - u)/dt on the interior faces, u* += dt alpha (d - prev_d) when has_prev, prev_d = d
+ * (prev_du / prev_dv hold d between steps, grid-shaped); then its recomputed Poisson right-hand
+ * side rho/dt div u*, zero on masked cells (:337-339).  ab2 = 0 skips the AB2 step (upwind
+ * transport).  Bit-identical to the reference's numpy arithmetic. */
+int gm_mac_ab2_rhs(const double* u, const double* v, double* u_star, double* v_star, double* prev_du,
+                   double* prev_dv, double* rhs, const uint8_t* mask, int32_t nx, int32_t ny, double dx, double dy,
+                   double dt, double rho, double alpha, int32_t has_prev, int32_t ab2, void* stream);
 /* Staircase pressure and shear forces out = (fx_p, fy_p, fx_v, fy_v) (calculate_mac_forces_cpp,
  * solver/src/bindings.cpp:284-341); the sums are reduced in a fixed order. */
 int gm_mac_forces(const double* u, const double* v, const double* p, const uint8_t* mask, int32_t nx, int32_t ny,
@@ -321,6 +329,20 @@ int gm_mac_forces(const double* u, const double* v, const double* p, const uint8
  * counts = (fluid cells, core cells). */
 int gm_mac_divergence(const double* u, const double* v, const uint8_t* mask, int32_t nx, int32_t ny, double dx,
                       double dy, double out[3], int64_t counts[2], void* stream);
+
+/* The pressure system of an aperture-weighted MAC grid alone: the Poisson matrix of
+ * build_cut_cell_poisson_matrix (solver/cut_cell_solver.py:132-216) for face open fractions
+ * ax, ay and cell classes, which with 0/1 apertures from a cell mask is the staircase matrix of
+ * build_poisson_matrix (solver/mac_solver.py:5-87) that the legacy loop factors (solver/main.py:
+ * 194-203, 340-345).  Solved by the boundary-corrected separable inverse with residual
+ * refinement; rhs and phi are pressure grids (host or device), rhs ignored and phi zero on
+ * covered cells; *residual_linf (may be NULL) receives max |rhs - A phi| (cut-cell rows / kappa). */
+typedef struct gm_poisson gm_poisson;
+int gm_poisson_create(int32_t nx, int32_t ny, double Lx, double Ly, double D, double xc, double yc, const double* ax,
+                      const double* ay, const int32_t* cell_type, const double* kappa, gm_poisson** out);
+int gm_poisson_destroy(gm_poisson* p);
+const char* gm_poisson_last_error(const gm_poisson* p);
+int gm_poisson_solve(gm_poisson* p, const double* rhs, double* phi, double* residual_linf);
 
 /* --- snapshot POD (postprocessing/modal_analysis.py:17-98) ------------------------ */
 /* Method of snapshots for M snapshots of N points (row-major M x N, host or device memory):

@@ -128,7 +128,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', type=Path, required=True, help='path of the reference checkout')
     ap.add_argument('--skip-large', action='store_true')
-    ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner', 'legacy', 'modal', 'cutcell'),
+    ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner', 'legacy', 'modal', 'cutcell',
+                                       'staircase'),
                     help='generate one group of fixtures only')
     args = ap.parse_args()
     work = Path(tempfile.mkdtemp(prefix='ghost_golden_'))
@@ -146,6 +147,8 @@ def main():
             run_modal(work)
         elif args.only == 'cutcell':
             run_cutcell(work)
+        elif args.only == 'staircase':
+            run_staircase(work)
         else:
             run_all(args)
             run_taylor_green(work)
@@ -154,6 +157,7 @@ def main():
             run_legacy(work)
             run_modal(work)
             run_cutcell(work)
+            run_staircase(work)
     finally:
         shutil.rmtree(work, ignore_errors=True)
 
@@ -434,6 +438,32 @@ def run_cutcell_wide(work):
          u_samples=np.array([f[0] for f in fields]), v_samples=np.array([f[1] for f in fields]),
          p_samples=np.array([f[2] for f in fields]), norms=np.array([f[3:] for f in fields]),
          scalars=np.array(scal))
+
+
+def run_staircase(work):
+    """The reference's legacy staircase loop (MAC_CylinderFlow(boundary='staircase',
+    time_scheme='legacy'), solver/main.py:303-381 with mac_engine built from
+    solver/src/bindings.cpp and the sparse-LU pressure solve) on a 48x24 grid: centred transport
+    (the loop's AB2 step) and upwind transport, 20 steps each, the second with the transient inlet
+    perturbation; fields at steps 1, 5 and 20 and the force coefficients of every step."""
+    from main import MAC_CylinderFlow
+    out = {}
+    for tag, transport, perturb in (('centered', 'centered', False), ('upwind', 'upwind', True)):
+        s = MAC_CylinderFlow(nx=48, ny=24, Lx=4.8, Ly=2.4, D=1.0, xc=1.3, yc=1.15, nu=0.02, boundary='staircase',
+                             time_scheme='legacy', transport=transport, pressure_solver='direct', verbose=False)
+        out[f'{tag}_init_u'], out[f'{tag}_init_v'] = s.u.copy(), s.v.copy()
+        fields, coef = {}, []
+        for k in range(20):
+            _, cd, cl = s.solve(n_steps=1, dt=0.002, perturb_transient=perturb, perturb_duration=0.03,
+                                save_artifacts=False, verbose=False)
+            coef.append([float(cd[0]), float(cl[0])])
+            if k + 1 in (1, 5, 20):
+                fields[k + 1] = (s.u.copy(), s.v.copy(), s.p.copy())
+        for k, (u, v, p) in fields.items():
+            out[f'{tag}_u{k}'], out[f'{tag}_v{k}'], out[f'{tag}_p{k}'] = u, v, p
+        out[f'{tag}_coef'] = np.array(coef)
+        out[f'{tag}_time'] = s.time
+    save('staircase_48x24', **out)
 
 
 def run_modal(work):
