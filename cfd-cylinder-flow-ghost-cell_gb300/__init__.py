@@ -8,8 +8,8 @@ from .build import build  # noqa: F401
 from . import _lib  # noqa: F401  (loads libghostmac.so; fails loudly if missing)
 from .ghost import CylinderBatch, GhostCellIntegrator, MAC_CylinderFlow  # noqa: F401
 from .cutcell import CutCellFlow  # noqa: F401
-from .staircase import StaircaseFlow  # noqa: F401
+from .staircase import LegacyGhostFlow, StaircaseFlow  # noqa: F401
 from . import analysis, learned, taylor_green, validation  # noqa: F401
 
-__all__ = ['MAC_CylinderFlow', 'GhostCellIntegrator', 'CylinderBatch', 'CutCellFlow', 'StaircaseFlow', 'taylor_green', 'analysis', 'learned',
+__all__ = ['MAC_CylinderFlow', 'GhostCellIntegrator', 'CylinderBatch', 'CutCellFlow', 'StaircaseFlow', 'LegacyGhostFlow', 'taylor_green', 'analysis', 'learned',
            'validation', 'build']

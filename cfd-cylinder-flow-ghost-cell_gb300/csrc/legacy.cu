@@ -155,6 +155,146 @@ __global__ void k_legacy_rhs(const double* __restrict__ us, const double* __rest
   rhs[t] = rho_dt * ((US_(j, i + 1) - US_(j, i)) / dx + (VS_(j + 1, i) - VS_(j, i)) / dy);
 }
 
+// ---- the legacy loop's ghost-cell branch (solver/ghost_cell.py:32-234, solver/main.py:347-370) --
+// Image-point ghost velocities g = wall - gamma (ip - wall), ip the bilinear value at the image
+// point.  The reference sets the ghost faces one after another, so a face may read a ghost face
+// set earlier in the same pass (its new value) or a later one (its old value): the host orders
+// the faces into levels (a face is one level above every earlier ghost face it reads), the old
+// values are saved first, and each level is one launch.
+__global__ void k_ghost_save(const double* __restrict__ f, long long nf, const long long* __restrict__ target,
+                             long long n, double* __restrict__ snap) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < n) {
+    const long long t = target[g];
+    snap[g] = (t >= 0 && t < nf) ? f[t] : 0.0;
+  }
+}
+// one level of ghost faces; entries whose indexes fall outside the field or the table are skipped
+__global__ void k_ghost_level(double* __restrict__ f, long long nf, const long long* __restrict__ target,
+                              const long long* __restrict__ src, const int* __restrict__ snap_of,
+                              const double* __restrict__ w, const double* __restrict__ gamma,
+                              const int* __restrict__ level, long long n, int lvl, const double* __restrict__ snap,
+                              double wall) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n || level[g] != lvl) return;
+  const long long t = target[g];
+  if (t < 0 || t >= nf) return;
+  double v[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int sidx = snap_of[4 * g + q];
+    const long long c = src[4 * g + q];
+    if (sidx >= n || c < 0 || c >= nf) return;
+    v[q] = sidx >= 0 ? snap[sidx] : f[c];
+  }
+  // the reference's order: w00 f00 + w10 f10 + w01 f01 + w11 f11, then the reflection
+  const double ip = w[4 * g] * v[0] + w[4 * g + 1] * v[1] + w[4 * g + 2] * v[2] + w[4 * g + 3] * v[3];
+  f[t] = wall - gamma[g] * (ip - wall);
+}
+
+// the ghost branch's corrector (solver/main.py:347-366): u = u* on interior faces, minus
+// dt/rho grad phi on faces between two fluid cells, zero between two masked cells, the inlet
+// and the Dirichlet outlet; v likewise with zero wall rows
+__global__ void k_ghost_correct(double* __restrict__ u, double* __restrict__ v, const double* __restrict__ us,
+                                const double* __restrict__ vs, const double* __restrict__ phi,
+                                const uint8_t* __restrict__ mask, const double* __restrict__ inlet, int nx, int ny,
+                                double dx, double dy, double dt_over_rho) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nu_ = (long long)ny * (nx + 1);
+  if (t < nu_) {
+    const int j = (int)(t / (nx + 1)), i = (int)(t - (long long)j * (nx + 1));
+    if (i == 0) U_(j, 0) = inlet[j];
+    else if (i == nx) U_(j, nx) = US_(j, nx) + dt_over_rho * 2.0 * PHI_(j, nx - 1) / dx;
+    else {
+      const bool l = M_(j, i - 1), r = M_(j, i);
+      double val = US_(j, i);
+      if (!l && !r) val -= dt_over_rho * (PHI_(j, i) - PHI_(j, i - 1)) / dx;
+      else if (l && r) val = 0.0;
+      U_(j, i) = val;
+    }
+  } else if (t < nu_ + (long long)(ny + 1) * nx) {
+    const long long f = t - nu_;
+    const int j = (int)(f / nx), i = (int)(f - (long long)j * nx);
+    if (j == 0 || j == ny) { V_(j, i) = 0.0; return; }
+    const bool b = M_(j - 1, i), a = M_(j, i);
+    double val = VS_(j, i);
+    if (!a && !b) val -= dt_over_rho * (PHI_(j, i) - PHI_(j - 1, i)) / dy;
+    else if (a && b) val = 0.0;
+    V_(j, i) = val;
+  }
+}
+// faces between a fluid and a masked cell keep u* (solver/main.py:368-370)
+__global__ void k_ghost_boundary(double* __restrict__ u, double* __restrict__ v, const double* __restrict__ us,
+                                 const double* __restrict__ vs, const uint8_t* __restrict__ mask, int nx, int ny) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nu_ = (long long)ny * (nx + 1);
+  if (t < nu_) {
+    const int j = (int)(t / (nx + 1)), i = (int)(t - (long long)j * (nx + 1));
+    if (i >= 1 && i <= nx - 1 && M_(j, i - 1) != M_(j, i)) U_(j, i) = US_(j, i);
+  } else if (t < nu_ + (long long)(ny + 1) * nx) {
+    const long long f = t - nu_;
+    const int j = (int)(f / nx), i = (int)(f - (long long)j * nx);
+    if (j >= 1 && j <= ny - 1 && M_(j - 1, i) != M_(j, i)) V_(j, i) = VS_(j, i);
+  }
+}
+
+// bilinear value of a staggered field at (y, x): the linear RegularGridInterpolator of the
+// reference (solver/ghost_cell.py:199-201), zero outside the grid
+__device__ double grid_linear(const double* __restrict__ f, int nxf, int nyf, double x0, double y0, double hx,
+                              double hy, double y, double x) {
+  const double gx = (x - x0) / hx, gy = (y - y0) / hy;
+  if (!(gx >= 0.0 && gx <= nxf - 1 && gy >= 0.0 && gy <= nyf - 1)) return 0.0;
+  int i = (int)floor(gx), j = (int)floor(gy);
+  if (i > nxf - 2) i = nxf - 2;
+  if (j > nyf - 2) j = nyf - 2;
+  const double tx = (x - (x0 + i * hx)) / hx, ty = (y - (y0 + j * hy)) / hy;
+  const double* r0 = f + (size_t)j * nxf;
+  const double* r1 = r0 + nxf;
+  return (r0[i] * (1.0 - tx) + r0[i + 1] * tx) * (1.0 - ty) + (r1[i] * (1.0 - tx) + r1[i + 1] * tx) * ty;
+}
+
+// surface forces on the true circle (extract_true_surface_forces, solver/ghost_cell.py:186-234):
+// pressure and probed central-difference velocity gradients at n points; one block, sums in a
+// fixed order; out = fx_p, fy_p, fx_v, fy_v
+__global__ void k_ghost_forces(const double* __restrict__ u, const double* __restrict__ v, const double* __restrict__ p,
+                               int nx, int ny, double dx, double dy, double xc, double yc, double radius, int n,
+                               double mu, double* __restrict__ out) {
+  __shared__ double sh[4][256];
+  double ax = 0.0, ay = 0.0, bx = 0.0, by = 0.0;
+  const double eps = 1e-4 * dx;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const double th = k * (2 * M_PI / n);  // np.linspace(0, 2 pi, n, endpoint=False)
+    const double c = cos(th), s = sin(th);
+    const double x = xc + radius * c, y = yc + radius * s;
+    const double pk = grid_linear(p, nx, ny, 0.5 * dx, 0.5 * dy, dx, dy, y, x);
+    auto U = [&](double yy, double xx) { return grid_linear(u, nx + 1, ny, 0.0, 0.5 * dy, dx, dy, yy, xx); };
+    auto V = [&](double yy, double xx) { return grid_linear(v, nx, ny + 1, 0.5 * dx, 0.0, dx, dy, yy, xx); };
+    const double dudx = (U(y, x + eps) - U(y, x - eps)) / (2.0 * eps);
+    const double dudy = (U(y + eps, x) - U(y - eps, x)) / (2.0 * eps);
+    const double dvdx = (V(y, x + eps) - V(y, x - eps)) / (2.0 * eps);
+    const double dvdy = (V(y + eps, x) - V(y - eps, x)) / (2.0 * eps);
+    const double txx = 2.0 * mu * dudx, tyy = 2.0 * mu * dvdy, txy = mu * (dudy + dvdx);
+    ax += pk * c;
+    ay += pk * s;
+    bx += txx * c + txy * s;
+    by += txy * c + tyy * s;
+  }
+  sh[0][threadIdx.x] = ax; sh[1][threadIdx.x] = ay; sh[2][threadIdx.x] = bx; sh[3][threadIdx.x] = by;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int q = 0; q < 4; ++q) sh[q][threadIdx.x] += sh[q][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double ds = radius * (2 * M_PI / n);
+    out[0] = -sh[0][0] * ds;
+    out[1] = -sh[1][0] * ds;
+    out[2] = sh[2][0] * ds;
+    out[3] = sh[3][0] * ds;
+  }
+}
+
 // u = u* - dt/rho d phi/dx, v = v* - dt/rho d phi/dy (bindings.cpp:248-281)
 __global__ void k_correct(double* __restrict__ u, double* __restrict__ v, const double* __restrict__ us,
                           const double* __restrict__ vs, const double* __restrict__ phi,
@@ -447,7 +587,7 @@ int gm_mac_corrector(double* u, double* v, const double* u_star, const double* v
 
 int gm_mac_ab2_rhs(const double* u, const double* v, double* u_star, double* v_star, double* prev_du,
                    double* prev_dv, double* rhs, const uint8_t* mask, int32_t nx, int32_t ny, double dx, double dy,
-                   double dt, double rho, double alpha, int32_t has_prev, int32_t ab2, void* stream) {
+                   double dt, double rho, double alpha, int32_t has_prev, int32_t what, void* stream) {
   if (!u || !v || !u_star || !v_star || !prev_du || !prev_dv || !rhs || !mask) return fail(GM_EVALUE, "null argument");
   if (int rc = check_grid(nx, ny, dx, dy)) return rc;
   if (int rc = check_step(dt, rho)) return rc;
@@ -457,20 +597,104 @@ int gm_mac_ab2_rhs(const double* u, const double* v, double* u_star, double* v_s
   const int iu = sg.add(u, nU * 8, true, false), iv = sg.add(v, nV * 8, true, false);
   const int ius = sg.add(u_star, nU * 8, true, true), ivs = sg.add(v_star, nV * 8, true, true);
   const int idu = sg.add(prev_du, nU * 8, true, true), idv = sg.add(prev_dv, nV * 8, true, true);
-  const int ir = sg.add(rhs, nP * 8, false, true), im = sg.add(mask, nP, true, false);
+  const int ir = sg.add(rhs, nP * 8, true, true), im = sg.add(mask, nP, true, false);
   double* extra = nullptr;
   if (cudaError_t e = sg.begin(0, &extra)) return cuda_fail(e);
   cudaStream_t st = sg.st;
-  if (ab2) {
+  if (what & 1) {
     k_ab2<<<blocks((long long)(nU + nV)), LT, 0, st>>>(sg.dev<double>(iu), sg.dev<double>(iv), sg.dev<double>(ius),
                                                        sg.dev<double>(ivs), sg.dev<double>(idu), sg.dev<double>(idv),
                                                        nx, ny, dt, dt * alpha, has_prev ? 1 : 0);
     gmk::kernel_launch_adjust(1);
   }
-  k_legacy_rhs<<<blocks((long long)nP), LT, 0, st>>>(sg.dev<double>(ius), sg.dev<double>(ivs), sg.dev<uint8_t>(im),
-                                                     sg.dev<double>(ir), nx, ny, dx, dy, rho / dt);
+  if (what & 2) {
+    k_legacy_rhs<<<blocks((long long)nP), LT, 0, st>>>(sg.dev<double>(ius), sg.dev<double>(ivs),
+                                                       sg.dev<uint8_t>(im), sg.dev<double>(ir), nx, ny, dx, dy,
+                                                       rho / dt);
+    gmk::kernel_launch_adjust(1);
+  }
+  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e);
+  if (cudaError_t e = sg.finish()) return cuda_fail(e);
+  return GM_OK;
+}
+
+int gm_mac_ghost_apply(double* field, int64_t field_size, int64_t n_ghost, const int64_t* target, const int64_t* src,
+                       const int32_t* snap_of, const double* weights, const double* gamma, const int32_t* level,
+                       int32_t n_levels, double wall, void* stream) {
+  if (n_ghost < 0 || field_size <= 0 || n_levels < 0) return fail(GM_EVALUE, "invalid ghost table sizes");
+  if (n_ghost == 0) return GM_OK;
+  if (!field || !target || !src || !snap_of || !weights || !gamma || !level) return fail(GM_EVALUE, "null argument");
+  if (!std::isfinite(wall)) return fail(GM_EVALUE, "the wall velocity must be finite");
+  const size_t ng = (size_t)n_ghost;
+  Staging sg(static_cast<cudaStream_t>(stream));
+  const int iff = sg.add(field, (size_t)field_size * 8, true, true);
+  const int it = sg.add(target, ng * 8, true, false), is = sg.add(src, 4 * ng * 8, true, false);
+  const int io = sg.add(snap_of, 4 * ng * 4, true, false), iw = sg.add(weights, 4 * ng * 8, true, false);
+  const int ig = sg.add(gamma, ng * 8, true, false), il = sg.add(level, ng * 4, true, false);
+  double* snap = nullptr;
+  if (cudaError_t e = sg.begin(ng * 8, &snap)) return cuda_fail(e);
+  const unsigned nb = blocks((long long)n_ghost);
+  const long long* tg = sg.dev<const long long>(it);
+  k_ghost_save<<<nb, LT, 0, sg.st>>>(sg.dev<double>(iff), field_size, tg, n_ghost, snap);
+  for (int l = 0; l < n_levels; ++l)
+    k_ghost_level<<<nb, LT, 0, sg.st>>>(sg.dev<double>(iff), field_size, tg, sg.dev<const long long>(is),
+                                        sg.dev<const int>(io), sg.dev<const double>(iw), sg.dev<const double>(ig),
+                                        sg.dev<const int>(il), n_ghost, l, snap, wall);
+  gmk::kernel_launch_adjust(1 + n_levels);
+  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e);
+  if (cudaError_t e = sg.finish()) return cuda_fail(e);
+  return GM_OK;
+}
+
+int gm_mac_ghost_correct(double* u, double* v, const double* u_star, const double* v_star, const double* phi,
+                         const uint8_t* mask, const double* inlet, int32_t nx, int32_t ny, double dx, double dy,
+                         double dt, double rho, int32_t boundary_faces, void* stream) {
+  if (!u || !v || !u_star || !v_star || !phi || !mask || !inlet) return fail(GM_EVALUE, "null argument");
+  if (int rc = check_grid(nx, ny, dx, dy)) return rc;
+  if (int rc = check_step(dt, rho)) return rc;
+  const size_t nU = (size_t)ny * (nx + 1), nV = (size_t)(ny + 1) * nx, nP = (size_t)ny * nx;
+  Staging sg(static_cast<cudaStream_t>(stream));
+  const int iu = sg.add(u, nU * 8, true, true), iv = sg.add(v, nV * 8, true, true);
+  const int ius = sg.add(u_star, nU * 8, true, false), ivs = sg.add(v_star, nV * 8, true, false);
+  const int iph = sg.add(phi, nP * 8, true, false), im = sg.add(mask, nP, true, false);
+  const int ii = sg.add(inlet, (size_t)ny * 8, true, false);
+  double* extra = nullptr;
+  if (cudaError_t e = sg.begin(0, &extra)) return cuda_fail(e);
+  const long long n = (long long)(nU + nV);
+  if (boundary_faces)
+    k_ghost_boundary<<<blocks(n), LT, 0, sg.st>>>(sg.dev<double>(iu), sg.dev<double>(iv), sg.dev<double>(ius),
+                                                  sg.dev<double>(ivs), sg.dev<uint8_t>(im), nx, ny);
+  else
+    k_ghost_correct<<<blocks(n), LT, 0, sg.st>>>(sg.dev<double>(iu), sg.dev<double>(iv), sg.dev<double>(ius),
+                                                 sg.dev<double>(ivs), sg.dev<double>(iph), sg.dev<uint8_t>(im),
+                                                 sg.dev<double>(ii), nx, ny, dx, dy, dt / rho);
   gmk::kernel_launch_adjust(1);
   if (cudaError_t e = cudaGetLastError()) return cuda_fail(e);
+  if (cudaError_t e = sg.finish()) return cuda_fail(e);
+  return GM_OK;
+}
+
+int gm_mac_ghost_forces(const double* u, const double* v, const double* p, int32_t nx, int32_t ny, double dx,
+                        double dy, double xc, double yc, double radius, int32_t n_theta, double mu, double out[4],
+                        void* stream) {
+  if (!u || !v || !p || !out) return fail(GM_EVALUE, "null argument");
+  if (int rc = check_grid(nx, ny, dx, dy)) return rc;
+  if (n_theta <= 0) return fail(GM_EVALUE, "n_theta must be positive");
+  if (!(std::isfinite(mu) && mu >= 0)) return fail(GM_EVALUE, "mu must be finite and nonnegative");
+  if (!(std::isfinite(xc) && std::isfinite(yc) && std::isfinite(radius) && radius > 0))
+    return fail(GM_EVALUE, "the circle must be finite with a positive radius");
+  const size_t nU = (size_t)ny * (nx + 1), nV = (size_t)(ny + 1) * nx, nP = (size_t)ny * nx;
+  Staging sg(static_cast<cudaStream_t>(stream));
+  const int iu = sg.add(u, nU * 8, true, false), iv = sg.add(v, nV * 8, true, false);
+  const int ip = sg.add(p, nP * 8, true, false);
+  double* res = nullptr;
+  if (cudaError_t e = sg.begin(8 * 8, &res)) return cuda_fail(e);
+  k_ghost_forces<<<1, 256, 0, sg.st>>>(sg.dev<double>(iu), sg.dev<double>(iv), sg.dev<double>(ip), nx, ny, dx, dy,
+                                       xc, yc, radius, n_theta, mu, res);
+  gmk::kernel_launch_adjust(1);
+  if (cudaError_t e = cudaGetLastError()) return cuda_fail(e);
+  if (cudaError_t e = cudaMemcpyAsync(out, res, 4 * sizeof(double), cudaMemcpyDeviceToHost, sg.st))
+    return cuda_fail(e);
   if (cudaError_t e = sg.finish()) return cuda_fail(e);
   return GM_OK;
 }

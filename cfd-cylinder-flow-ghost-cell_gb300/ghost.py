@@ -273,6 +273,9 @@ class MAC_CylinderFlow:
         if bound.get('boundary') == 'staircase':
             from .staircase import StaircaseFlow
             return StaircaseFlow(*args, **kwargs)
+        if bound.get('boundary', 'ghost_cell') == 'ghost_cell' and bound.get('time_scheme') == 'legacy':
+            from .staircase import LegacyGhostFlow
+            return LegacyGhostFlow(*args, **kwargs)
         return super().__new__(cls)
 
     def __init__(self, nx=400, ny=100, Lx=20.0, Ly=5.0, D=1.0, xc=5.0, yc=2.5,

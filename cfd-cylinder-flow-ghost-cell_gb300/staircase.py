@@ -32,6 +32,8 @@ class StaircaseFlow:
     """The legacy staircase MAC_CylinderFlow on the GPU (solver/main.py:19-501, boundary='staircase',
     time_scheme='legacy')."""
 
+    _boundary = 'staircase'
+
     def __init__(self, nx=400, ny=100, Lx=20.0, Ly=5.0, D=1.0, xc=5.0, yc=2.5, nu=0.01, rho=1.0, U_inf=1.0,
                  inflow='uniform', U_m=None, slip_walls=False, verbose=True, boundary='staircase',
                  transport='centered', pressure_solver='direct', marker_spacing_factor=1.5, time_scheme='legacy',
@@ -52,10 +54,11 @@ class StaircaseFlow:
             raise ValueError('Unknown Ghost pressure extension or velocity interpolation')
         if ghost_pressure_extension != 'neumann' or ghost_velocity_interpolation != 'bilinear':
             raise ValueError('Ghost reconstruction options require Ghost AB2/CN')
-        if boundary != 'staircase' or time_scheme != 'legacy':
-            raise NotImplementedError('StaircaseFlow implements boundary="staircase", time_scheme="legacy"')
+        if boundary != self._boundary or time_scheme != 'legacy':
+            raise NotImplementedError(f'{type(self).__name__} implements boundary="{self._boundary}", '
+                                      'time_scheme="legacy"')
         if precision != 'fp64':
-            raise NotImplementedError('the staircase path runs in FP64')
+            raise NotImplementedError('the legacy loop runs in FP64')
         if any(isinstance(n, bool) or not isinstance(n, (int, np.integer)) or n < 4 for n in (nx, ny)):
             raise ValueError('nx and ny must be integers >= 4')
         if not all(np.isfinite(x) and x > 0 for x in (Lx, Ly, D, nu, rho, U_inf)):
@@ -135,8 +138,12 @@ class StaircaseFlow:
         self.time = 0.0
         self.run_options = {}
         self.last_step_diagnostics = {}
+        self._setup_boundary()
         if verbose:
-            print(f"Staircase legacy MAC on the GPU ready in {_time.time() - t0:.3f}s (Re={self.Re:.1f}).")
+            print(f"{self._boundary} legacy MAC on the GPU ready in {_time.time() - t0:.3f}s (Re={self.Re:.1f}).")
+
+    def _setup_boundary(self):
+        """Extra boundary tables of a subclass (none for the staircase)."""
 
     def __del__(self):
         h = getattr(self, '_poisson', None)
@@ -172,7 +179,7 @@ class StaircaseFlow:
         _check_mac(lib.gm_mac_ab2_rhs(ptr(d['u']), ptr(d['v']), ptr(d['us']), ptr(d['vs']), ptr(d['pdu']),
                                       ptr(d['pdv']), ptr(d['rhs']), ptr(d['mask']), self.nx, self.ny, self.dx,
                                       self.dy, float(dt), float(self.rho), float(alpha), 1 if has_prev else 0,
-                                      centered, st))
+                                      (_lib.MAC_AB2 if centered else 0) | _lib.MAC_RHS, st))
         if centered:
             self._previous_dt = dt
         res = C.c_double()
@@ -268,3 +275,150 @@ class StaircaseFlow:
             elapsed = _time.time() - t0
             print(f"Simulation completed in {elapsed:.2f}s ({elapsed / n_steps * 1000:.2f} ms/step)")
         return np.array(ts), np.array(cds), np.array(cls)
+
+
+def ghost_face_tables(xs, ys, dx, dy, xc, yc, radius, is_u):
+    """Ghost faces of one staggered face grid (coordinates xs, ys) and their image-point stencils,
+    as GhostCellBoundary builds them (solver/ghost_cell.py:41-157): the faces inside the circle
+    (signed distance < 0) with a face outside it among their four neighbours, in row-major order;
+    the image point at distance d + max(d, h/2) along the outward normal, its bilinear cell and
+    weights (00, 10, 01, 11), and gamma = d / max(d, h/2).  The same elementwise float64
+    arithmetic, vectorised.  Returns dict(target, src (n, 4), weights (n, 4), gamma, snap_of (n, 4),
+    level, n_levels) with flat indexes into the face grid.
+
+    The reference sets the faces in order, so a corner that is itself a ghost face is read with
+    the value it holds at that moment: new if it comes earlier in the order, its value before the
+    pass otherwise (snap_of = its ghost index).  A face's level is one above the highest level of
+    the earlier ghost faces it reads, so one launch per level reproduces the sequential pass."""
+    X, Y = np.meshgrid(xs, ys)
+    dist = np.sqrt((X - xc) ** 2 + (Y - yc) ** 2) - radius
+    fluid = dist >= 0.0
+    near = np.zeros_like(fluid)
+    near[:, 1:] |= fluid[:, :-1]
+    near[:, :-1] |= fluid[:, 1:]
+    near[1:, :] |= fluid[:-1, :]
+    near[:-1, :] |= fluid[1:, :]
+    js, is_ = np.nonzero(~fluid & near)
+    nyf, nxf = fluid.shape
+    xg, yg = xs[is_], ys[js]
+    d = np.abs(dist[js, is_])
+    delta = np.maximum(d, 0.5 * min(dx, dy))
+    r = np.maximum(np.sqrt((xg - xc) ** 2 + (yg - yc) ** 2), 1e-14)
+    x_ip = xg + (d + delta) * ((xg - xc) / r)
+    y_ip = yg + (d + delta) * ((yg - yc) / r)
+    if is_u:
+        i0 = np.floor(x_ip / dx).astype(np.int64)
+        j0 = np.floor((y_ip - 0.5 * dy) / dy).astype(np.int64)
+        x0, y0 = i0 * dx, (j0 + 0.5) * dy
+    else:
+        i0 = np.floor((x_ip - 0.5 * dx) / dx).astype(np.int64)
+        j0 = np.floor(y_ip / dy).astype(np.int64)
+        x0, y0 = (i0 + 0.5) * dx, j0 * dy
+    i0 = np.clip(i0, 0, nxf - 2)
+    j0 = np.clip(j0, 0, nyf - 2)
+    rx = np.clip((x_ip - x0) / dx, 0.0, 1.0)
+    ry = np.clip((y_ip - y0) / dy, 0.0, 1.0)
+    weights = np.stack([(1.0 - rx) * (1.0 - ry), rx * (1.0 - ry), (1.0 - rx) * ry, rx * ry], axis=1)
+    base = j0 * nxf + i0
+    src = np.stack([base, base + 1, base + nxf, base + nxf + 1], axis=1)
+    target = js.astype(np.int64) * nxf + is_
+    n = target.size
+    order = np.full(nyf * nxf, -1, np.int64)
+    order[target] = np.arange(n)
+    snap_of = np.full((n, 4), -1, np.int32)
+    level = np.zeros(n, np.int32)
+    for g in range(n):
+        lv = 0
+        for q in range(4):
+            k = order[src[g, q]]
+            if k >= g:
+                snap_of[g, q] = k
+            elif k >= 0:
+                lv = max(lv, int(level[k]) + 1)
+        level[g] = lv
+    return dict(target=target, src=src, weights=weights, gamma=d / delta, snap_of=snap_of, level=level,
+                n_levels=int(level.max()) + 1 if n else 0)
+
+
+class LegacyGhostFlow(StaircaseFlow):
+    """MAC_CylinderFlow(boundary='ghost_cell', time_scheme='legacy') on the GPU: the legacy loop of
+    solver/main.py:245-501 with the GhostCellBoundary of solver/ghost_cell.py.  Each step runs the
+    native predictor on the staircase mask, sets the image-point ghost velocities on u*, v* (again
+    after the loop's AB2 step for centred transport), recomputes the Poisson right-hand side,
+    solves the staircase Poisson matrix, applies the ghost branch's own corrector, sets the ghost
+    velocities of u, v, restores u* on the faces between fluid and masked cells, and integrates
+    the forces on the true circle at 360 points.  Fields are bit-identical to the reference's
+    arithmetic except for the pressure solve, which agrees with the reference's sparse LU to
+    rounding."""
+
+    _boundary = 'ghost_cell'
+    n_theta = 360
+
+    def _setup_boundary(self):
+        import torch
+        dev = torch.device('cuda')
+        xu = np.arange(self.nx + 1) * self.dx
+        yu = (np.arange(self.ny) + 0.5) * self.dy
+        xv = (np.arange(self.nx) + 0.5) * self.dx
+        yv = np.arange(self.ny + 1) * self.dy
+        self._ghost = {}
+        for key, xs, ys, is_u in (('u', xu, yu, True), ('v', xv, yv, False)):
+            t = ghost_face_tables(xs, ys, self.dx, self.dy, self.xc, self.yc, self.D / 2.0, is_u)
+            dt = {k: torch.from_numpy(np.ascontiguousarray(t[k])).to(dev)
+                  for k in ('target', 'src', 'weights', 'gamma', 'snap_of', 'level')}
+            dt['n'], dt['n_levels'] = int(t['target'].size), t['n_levels']
+            self._ghost[key] = dt
+
+    def _apply_ghost(self, fu, fv):
+        """apply_velocity_ghost_cells (solver/ghost_cell.py:159-184) with zero wall velocity."""
+        st = self._stream()
+        for key, f in (('u', fu), ('v', fv)):
+            t = self._ghost[key]
+            _check_mac(lib.gm_mac_ghost_apply(ptr(f), f.numel(), t['n'], ptr(t['target']), ptr(t['src']),
+                                              ptr(t['snap_of']), ptr(t['weights']), ptr(t['gamma']),
+                                              ptr(t['level']), t['n_levels'], 0.0, st))
+
+    def ghost_counts(self):
+        """Numbers of ghost u and v faces and of launch levels of each."""
+        return {k: (t['n'], t['n_levels']) for k, t in self._ghost.items()}
+
+    def _step(self, dt):
+        """One legacy step on the device (solver/main.py:303-378, ghost_cell branch)."""
+        d = self._d
+        st = self._stream()
+        centered = self.transport == 'centered'
+        nonincremental = centered
+        _check_mac(lib.gm_mac_predictor_rhs(ptr(d['u']), ptr(d['v']), ptr(d['us']), ptr(d['vs']), ptr(d['rhs']),
+                                            ptr(d['zero_p'] if nonincremental else d['p']), ptr(d['mask']),
+                                            ptr(d['inlet']), self.nx, self.ny, self.dx, self.dy, float(dt),
+                                            float(self.nu), float(self.rho), 1 if self.slip_walls else 0,
+                                            1 if centered else 0, st))
+        self._apply_ghost(d['us'], d['vs'])
+        has_prev = self._previous_dt is not None
+        alpha = dt / (2 * self._previous_dt) if has_prev else 0.0
+        args = (ptr(d['u']), ptr(d['v']), ptr(d['us']), ptr(d['vs']), ptr(d['pdu']), ptr(d['pdv']), ptr(d['rhs']),
+                ptr(d['mask']), self.nx, self.ny, self.dx, self.dy, float(dt), float(self.rho), float(alpha),
+                1 if has_prev else 0)
+        if centered:
+            _check_mac(lib.gm_mac_ab2_rhs(*args, _lib.MAC_AB2, st))
+            self._previous_dt = dt
+            self._apply_ghost(d['us'], d['vs'])
+        _check_mac(lib.gm_mac_ab2_rhs(*args, _lib.MAC_RHS, st))
+        res = C.c_double()
+        rc = lib.gm_poisson_solve(self._poisson, ptr(d['rhs']), ptr(d['phi']), C.byref(res))
+        if rc != _lib.GM_OK:
+            raise _lib.error_for(rc, lib.gm_poisson_last_error(self._poisson).decode(errors='replace'))
+        cargs = (ptr(d['u']), ptr(d['v']), ptr(d['us']), ptr(d['vs']), ptr(d['phi']), ptr(d['mask']),
+                 ptr(d['inlet']), self.nx, self.ny, self.dx, self.dy, float(dt), float(self.rho))
+        _check_mac(lib.gm_mac_ghost_correct(*cargs, 0, st))
+        self._apply_ghost(d['u'], d['v'])
+        _check_mac(lib.gm_mac_ghost_correct(*cargs, 1, st))
+        if nonincremental:
+            d['p'].copy_(d['phi'])
+        else:
+            d['p'].add_(d['phi'])
+        out = np.empty(4)
+        _check_mac(lib.gm_mac_ghost_forces(ptr(d['u']), ptr(d['v']), ptr(d['p']), self.nx, self.ny, self.dx,
+                                           self.dy, float(self.xc), float(self.yc), float(self.D / 2.0),
+                                           self.n_theta, float(self.nu * self.rho), ptr(out), st))
+        return out, res.value

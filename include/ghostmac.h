@@ -314,12 +314,41 @@ int gm_mac_corrector(double* u, double* v, const double* u_star, const double* v
                      double rho, int32_t slip_walls, void* stream);
 /* The legacy loop's own AB2 step on u*, v* (centred transport, solver/main.py:315-322):
  * d = (u* - u)/dt on the interior faces, u* += dt alpha (d - prev_d) when has_prev, prev_d = d
- * (prev_du / prev_dv hold d between steps, grid-shaped); then its recomputed Poisson right-hand
- * side rho/dt div u*, zero on masked cells (:337-339).  ab2 = 0 skips the AB2 step (upwind
- * transport).  Bit-identical to the reference's numpy arithmetic. */
+ * (prev_du / prev_dv hold d between steps, grid-shaped); and its recomputed Poisson right-hand
+ * side rho/dt div u*, zero on masked cells (:337-339).  what: bit 1 runs the AB2 step (centred
+ * transport only), bit 2 the right-hand side (the ghost-cell branch sets its ghost faces between
+ * the two).  Bit-identical to the reference's numpy arithmetic. */
+#define GM_MAC_AB2 1
+#define GM_MAC_RHS 2
 int gm_mac_ab2_rhs(const double* u, const double* v, double* u_star, double* v_star, double* prev_du,
                    double* prev_dv, double* rhs, const uint8_t* mask, int32_t nx, int32_t ny, double dx, double dy,
-                   double dt, double rho, double alpha, int32_t has_prev, int32_t ab2, void* stream);
+                   double dt, double rho, double alpha, int32_t has_prev, int32_t what, void* stream);
+/* Image-point ghost velocities of the legacy ghost-cell branch (apply_velocity_ghost_cells,
+ * solver/ghost_cell.py:159-184) on one face grid of field_size values: for ghost face g (in the
+ * reference's row-major order), field[target[g]] = wall - gamma[g] (ip - wall), ip =
+ * sum_q weights[4g+q] * x_q over its four bilinear corners src[4g+q] (corner order 00, 10, 01,
+ * 11).  The reference sets the faces in order, so a corner that is a ghost face reads the value
+ * that face had before the pass (snap_of[4g+q] = its ghost index) or after it (-1, allowed only
+ * when that face sits on a lower level than g); level[g] in [0, n_levels) are launched in turn.
+ * The tables come from the geometry (the Python host builds them).  Bit-identical. */
+int gm_mac_ghost_apply(double* field, int64_t field_size, int64_t n_ghost, const int64_t* target, const int64_t* src,
+                       const int32_t* snap_of, const double* weights, const double* gamma, const int32_t* level,
+                       int32_t n_levels, double wall, void* stream);
+/* The ghost-cell branch's corrector (solver/main.py:347-370).  boundary_faces = 0: u = u*,
+ * minus dt/rho dphi/dx between two fluid cells, zero between two masked cells, the inlet, the
+ * Dirichlet outlet u* + 2 dt/rho phi/dx, v likewise with zero wall rows.  boundary_faces = 1:
+ * faces between a fluid and a masked cell take u* again (called after the ghost velocities).
+ * Bit-identical. */
+int gm_mac_ghost_correct(double* u, double* v, const double* u_star, const double* v_star, const double* phi,
+                         const uint8_t* mask, const double* inlet, int32_t nx, int32_t ny, double dx, double dy,
+                         double dt, double rho, int32_t boundary_faces, void* stream);
+/* Pressure and viscous forces on the true circle (extract_true_surface_forces,
+ * solver/ghost_cell.py:186-234): n_theta equally spaced points, bilinear p, u, v (zero outside
+ * the grid) and central differences of step 1e-4 dx for the velocity gradients.  out = (fx_p,
+ * fy_p, fx_v, fy_v), summed in a fixed order (equal to the reference's sums to rounding). */
+int gm_mac_ghost_forces(const double* u, const double* v, const double* p, int32_t nx, int32_t ny, double dx,
+                        double dy, double xc, double yc, double radius, int32_t n_theta, double mu, double out[4],
+                        void* stream);
 /* Staircase pressure and shear forces out = (fx_p, fy_p, fx_v, fy_v) (calculate_mac_forces_cpp,
  * solver/src/bindings.cpp:284-341); the sums are reduced in a fixed order. */
 int gm_mac_forces(const double* u, const double* v, const double* p, const uint8_t* mask, int32_t nx, int32_t ny,

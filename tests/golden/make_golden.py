@@ -129,7 +129,7 @@ def main():
     ap.add_argument('--reference', type=Path, required=True, help='path of the reference checkout')
     ap.add_argument('--skip-large', action='store_true')
     ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner', 'legacy', 'modal', 'cutcell',
-                                       'staircase'),
+                                       'staircase', 'legacy_ghost'),
                     help='generate one group of fixtures only')
     args = ap.parse_args()
     work = Path(tempfile.mkdtemp(prefix='ghost_golden_'))
@@ -149,6 +149,8 @@ def main():
             run_cutcell(work)
         elif args.only == 'staircase':
             run_staircase(work)
+        elif args.only == 'legacy_ghost':
+            run_legacy_ghost(work)
         else:
             run_all(args)
             run_taylor_green(work)
@@ -158,6 +160,7 @@ def main():
             run_modal(work)
             run_cutcell(work)
             run_staircase(work)
+            run_legacy_ghost(work)
     finally:
         shutil.rmtree(work, ignore_errors=True)
 
@@ -464,6 +467,40 @@ def run_staircase(work):
         out[f'{tag}_coef'] = np.array(coef)
         out[f'{tag}_time'] = s.time
     save('staircase_48x24', **out)
+
+
+def run_legacy_ghost(work):
+    """The reference's legacy ghost-cell loop (MAC_CylinderFlow(boundary='ghost_cell',
+    time_scheme='legacy'), solver/main.py:303-381 with GhostCellBoundary of solver/ghost_cell.py,
+    mac_engine built from solver/src/bindings.cpp and the sparse-LU pressure solve) on the 48x24
+    grid of the staircase case: centred and upwind transport, 20 steps each, the second with the
+    transient inlet perturbation; its ghost-face tables, fields at steps 1, 5 and 20 and the force
+    coefficients of every step."""
+    from main import MAC_CylinderFlow
+    out = {}
+    for tag, transport, perturb in (('centered', 'centered', False), ('upwind', 'upwind', True)):
+        s = MAC_CylinderFlow(nx=48, ny=24, Lx=4.8, Ly=2.4, D=1.0, xc=1.3, yc=1.15, nu=0.02, boundary='ghost_cell',
+                             time_scheme='legacy', transport=transport, pressure_solver='direct', verbose=False)
+        if tag == 'centered':
+            gc = s.gc
+            for f in ('u', 'v'):
+                out[f'ghost_{f}_faces'] = np.array(getattr(gc, f'ghost_{f}_indices'), np.int64).reshape(-1, 2)
+                out[f'ghost_{f}_cells'] = np.array(getattr(gc, f'{f}_ip_cells'), np.int64).reshape(-1, 2)
+                out[f'ghost_{f}_weights'] = np.asarray(getattr(gc, f'{f}_ip_weights'), float).reshape(-1, 4)
+                out[f'ghost_{f}_gammas'] = np.asarray(getattr(gc, f'{f}_gammas'), float)
+        out[f'{tag}_init_u'], out[f'{tag}_init_v'] = s.u.copy(), s.v.copy()
+        fields, coef = {}, []
+        for k in range(20):
+            _, cd, cl = s.solve(n_steps=1, dt=0.002, perturb_transient=perturb, perturb_duration=0.03,
+                                save_artifacts=False, verbose=False)
+            coef.append([float(cd[0]), float(cl[0])])
+            if k + 1 in (1, 5, 20):
+                fields[k + 1] = (s.u.copy(), s.v.copy(), s.p.copy())
+        for k, (u, v, p) in fields.items():
+            out[f'{tag}_u{k}'], out[f'{tag}_v{k}'], out[f'{tag}_p{k}'] = u, v, p
+        out[f'{tag}_coef'] = np.array(coef)
+        out[f'{tag}_time'] = s.time
+    save('legacy_ghost_48x24', **out)
 
 
 def run_modal(work):
