@@ -20,6 +20,10 @@ dominant kernel, the CPU baseline (the oracle port on this host) and the SM
 clocks sampled during the timed region.  --impl reference times the CPU oracle
 port of the reference algorithm on the host cores for the same workload.
 Under torchrun each rank runs an independent replica (the case does not shard).
+
+Other workloads (--workload) time one path alone on one GPU: the 64-case sweep, Taylor-Green,
+the GMRES pressure path, the cut-cell AB2/CN path (cutcell_800x820_re100) and the two legacy
+loops (staircase_800x820_re100, legacy_ghost_800x820_re100).
 """
 from __future__ import annotations
 
@@ -75,6 +79,15 @@ GMRES_WORKLOADS = {
 CUTCELL_WORKLOADS = {
     'cutcell_800x820_re100': dict(nx=800, ny=820, Lx=40.0, Ly=41.0, D=1.0, xc=10.0, yc=20.5, nu=0.01, dt=0.002,
                                   noise='v', amp=1e-2, seed=0),
+}
+# the legacy loops (time_scheme='legacy', centred transport with the loop's AB2 step) on the same
+# grid and Re: the staircase branch and the ghost-cell branch (image-point ghost velocities),
+# from the loop's own initial field (uniform inflow, masked faces zero)
+LEGACY_WORKLOADS = {
+    'staircase_800x820_re100': dict(nx=800, ny=820, Lx=40.0, Ly=41.0, D=1.0, xc=10.0, yc=20.5, nu=0.01, dt=0.002,
+                                    boundary='staircase'),
+    'legacy_ghost_800x820_re100': dict(nx=800, ny=820, Lx=40.0, Ly=41.0, D=1.0, xc=10.0, yc=20.5, nu=0.01,
+                                       dt=0.002, boundary='ghost_cell'),
 }
 DEFAULT_WORKLOAD = 'wide_800x820_re100'
 # FP64 instructions (dadd + dmul + dfma, thread level) per cell update of the plain FP64 step on
@@ -284,6 +297,12 @@ def run_reference(args, w, rank):
     if rank != 0:
         return
     workers = os.cpu_count() or 1
+    if args.workload in CUTCELL_WORKLOADS or args.workload in LEGACY_WORKLOADS:
+        path = 'cut_cell' if args.workload in CUTCELL_WORKLOADS else w['boundary']
+        print(json.dumps(dict(impl='reference', workload=args.workload, unavailable=(
+            f'the reference\'s {path} loop runs from its own source tree, which this machine does not hold; '
+            f'oracle/time_reference_stub.py --path {path} times it where the source is'))), flush=True)
+        return
     if args.workload in TG_WORKLOADS:
         rate, done, el = oracle_tg_rate(w, 60.0)
         line = dict(metric=METRIC, value=rate, unit='cell-updates/s', n_gpus=args.gpus, steps=done,
@@ -979,6 +998,40 @@ def run_ours_cutcell(args, w, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def run_ours_legacy(args, w, rank, world):
+    """A legacy loop alone (1 GPU): K steps of MAC_CylinderFlow(time_scheme='legacy') after W
+    warm-up steps, one solve() call, wall clock between two device synchronisations (each step
+    is a few library calls from the host and reads the forces back)."""
+    import torch
+    pkg = load_package()
+    torch.zeros(1, device='cuda')
+    kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
+    t0 = time.perf_counter()
+    s = pkg.MAC_CylinderFlow(boundary=w['boundary'], time_scheme='legacy', transport='centered', verbose=False, **kw)
+    setup_s = time.perf_counter() - t0
+    s.solve(n_steps=args.warmup, dt=w['dt'], perturb_transient=False, save_artifacts=False, verbose=False)
+    steps = max(1, min(args.steps, 500))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.solve(n_steps=steps, dt=w['dt'], perturb_transient=False, save_artifacts=False, verbose=False)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    ms = el * 1e3 / steps
+    max_div = s.divergence_stats()[0]
+    if rank == 0:
+        extra = dict(ghost_faces=s.ghost_counts()) if w['boundary'] == 'ghost_cell' else {}
+        line = dict(metric=f"cell-updates/s (legacy {w['boundary']} loop)", value=w['nx'] * w['ny'] / (ms * 1e-3),
+                    unit='cell-updates/s', n_gpus=world, steps=steps, warmup=args.warmup, ms_per_step=ms,
+                    higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f64',
+                    data='synthetic (uniform inflow start)',
+                    config=dict(workload=args.workload, grid=f"{w['nx']}x{w['ny']}", dt=w['dt'],
+                                boundary=w['boundary'], time_scheme='legacy', transport='centered'),
+                    legacy=dict(setup_s=setup_s, max_divergence=max_div, cd=s.last_step_diagnostics['cd'],
+                                cl=s.last_step_diagnostics['cl'],
+                                pressure_residual_linf=s.last_step_diagnostics['pressure_residual_linf'], **extra))
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument('--gpus', type=int, default=1)
@@ -986,7 +1039,8 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', choices=('ours', 'reference'), default='ours')
     ap.add_argument('--workload', choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(TG_WORKLOADS) +
-                    sorted(GMRES_WORKLOADS) + sorted(CUTCELL_WORKLOADS), default=DEFAULT_WORKLOAD)
+                    sorted(GMRES_WORKLOADS) + sorted(CUTCELL_WORKLOADS) + sorted(LEGACY_WORKLOADS),
+                    default=DEFAULT_WORKLOAD)
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
     ap.add_argument('--no-compare', action='store_true', help='skip timing the plain FP64 step beside the FP32 mode')
     ap.add_argument('--no-batch', action='store_true', help='skip timing the 64-case sweep beside the single case')
@@ -1001,7 +1055,8 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     w = (WORKLOADS.get(args.workload) or BATCH_WORKLOADS.get(args.workload) or TG_WORKLOADS.get(args.workload) or
-         GMRES_WORKLOADS.get(args.workload) or CUTCELL_WORKLOADS[args.workload])
+         GMRES_WORKLOADS.get(args.workload) or CUTCELL_WORKLOADS.get(args.workload) or
+         LEGACY_WORKLOADS[args.workload])
     world = int(os.environ.get('WORLD_SIZE', 1))
     rank = int(os.environ.get('RANK', 0))
     if args.impl == 'reference':
@@ -1026,6 +1081,8 @@ def main():
         run_ours_gmres(args, w, rank, world)
     elif args.workload in CUTCELL_WORKLOADS:
         run_ours_cutcell(args, w, rank, world)
+    elif args.workload in LEGACY_WORKLOADS:
+        run_ours_legacy(args, w, rank, world)
     else:
         run_ours(args, w, rank, world)
     if world > 1:

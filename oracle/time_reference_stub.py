@@ -17,6 +17,12 @@ Helmholtz-building step is excluded.  Run here, not on the GPU machine (the referenc
 
     python oracle/time_reference_stub.py --reference <path of the reference checkout> [--steps 2]
 
+With ``--path staircase`` or ``--path legacy_ghost`` it times the reference's legacy loop
+(MAC_CylinderFlow(time_scheme='legacy', transport='centered') with boundary='staircase' or
+'ghost_cell': mac_engine compiled with OpenMP, the sparse LU factored in setup, the ghost-cell
+branch's Python image-point loops) on bench.py's staircase_800x820_re100 or
+legacy_ghost_800x820_re100 workload, after setup and three steps, with all the host's threads.
+
 With ``--path cut_cell`` it times the reference's cut-cell AB2/CN step instead
 (MAC_CylinderFlow(boundary='cut_cell'), CutCellBoundary.advance_ab2_cn: numpy and scipy, no
 Numba kernel on that path) on bench.py's cutcell_800x820_re100 workload, after setup and the
@@ -98,16 +104,44 @@ def time_cut_cell(w, steps):
     return w['nx'] * w['ny'] * steps / el, el, setup
 
 
+def time_legacy(w, steps):
+    from main import MAC_CylinderFlow
+    kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
+    t0 = time.perf_counter()
+    s = MAC_CylinderFlow(boundary=w['boundary'], time_scheme='legacy', transport='centered',
+                         pressure_solver='direct', verbose=False, **kw)
+    setup = time.perf_counter() - t0
+    s.solve(n_steps=3, dt=w['dt'], perturb_transient=False, save_artifacts=False, verbose=False)
+    t0 = time.perf_counter()
+    s.solve(n_steps=steps, dt=w['dt'], perturb_transient=False, save_artifacts=False, verbose=False)
+    el = time.perf_counter() - t0
+    return w['nx'] * w['ny'] * steps / el, el, setup
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', type=Path, required=True, help='path of the reference checkout')
     ap.add_argument('--steps', type=int, default=2)
-    ap.add_argument('--path', choices=('ghost_cell', 'cut_cell'), default='ghost_cell')
+    ap.add_argument('--path', choices=('ghost_cell', 'cut_cell', 'staircase', 'legacy_ghost'), default='ghost_cell')
     args = ap.parse_args()
     sys.path.insert(0, str(ROOT))
     sys.path.insert(0, str(ROOT / 'tests' / 'golden'))
     import bench
     import make_golden
+    if args.path in ('staircase', 'legacy_ghost'):
+        name = f'{args.path}_800x820_re100'
+        w = bench.LEGACY_WORKLOADS[name]
+        work = Path(tempfile.mkdtemp(prefix='ghost_ref_time_'))
+        try:
+            make_golden.build_harness(args.reference, work)
+            rate, el, setup = time_legacy(w, args.steps)
+        finally:
+            shutil.rmtree(work, ignore_errors=True)
+        import os
+        print(json.dumps(dict(workload=name, threads=os.cpu_count(),
+                              reference=dict(value=rate, steps=args.steps, seconds=el, ms_per_step=el / args.steps * 1e3,
+                                             setup_seconds=setup)), indent=2))
+        return
     if args.path == 'cut_cell':
         w = bench.CUTCELL_WORKLOADS['cutcell_800x820_re100']
         work = Path(tempfile.mkdtemp(prefix='ghost_ref_time_'))
