@@ -224,7 +224,7 @@ def sweep_cases(pkg, w, precision):
     """The batch workload's cases as MAC_CylinderFlow objects with their seeded perturbation."""
     def make(kw):
         try:
-            return pkg.MAC_CylinderFlow(verbose=False, precision=precision, **kw)
+            return pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision=precision, **kw)
         except ValueError:
             return None
     cases, params = [], []
@@ -347,7 +347,7 @@ def run_ours(args, w, rank, world):
     kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
     dt = w['dt']
     cells = w['nx'] * w['ny']
-    s = pkg.MAC_CylinderFlow(verbose=False, precision=args.precision, **kw)
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision=args.precision, **kw)
     seeded_state(s, w)
     stream = torch.cuda.Stream()
     L.check(L.lib.gm_set_stream(s._h, C.c_void_p(stream.cuda_stream)), s._h)
@@ -435,7 +435,7 @@ def run_ours(args, w, rank, world):
     # time the plain FP64 case with the same protocol (graph mode, L2 flushed between steps)
     compare = None
     if args.precision == 'fp32' and not args.no_compare:
-        s64 = pkg.MAC_CylinderFlow(verbose=False, precision='fp64', **kw)
+        s64 = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision='fp64', **kw)
         seeded_state(s64, w)
         L.check(L.lib.gm_set_stream(s64._h, C.c_void_p(stream.cuda_stream)), s64._h)
         s64._push()
@@ -617,7 +617,7 @@ def run_ours_gmres(args, w, rank, world):
     cells = w['nx'] * w['ny']
 
     def case(solver):
-        s = pkg.MAC_CylinderFlow(verbose=False, precision=args.precision, pressure_solver=solver, **kw)
+        s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision=args.precision, pressure_solver=solver, **kw)
         seeded_state(s, w)
         return s
 
@@ -716,7 +716,7 @@ def gmres_summary(pkg, w, steps):
     dt = w['dt']
     out = dict(workload='gmres_1024x512_re150', steps=steps)
     for solver in ('iterative', 'direct'):
-        s = pkg.MAC_CylinderFlow(verbose=False, precision='fp32', pressure_solver=solver, **kw)
+        s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision='fp32', pressure_solver=solver, **kw)
         seeded_state(s, w)
         s._push()
         its, nsol = 0, 0
@@ -944,7 +944,7 @@ def profile_step(args, w):
     import torch
     pkg = load_package()
     kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
-    s = pkg.MAC_CylinderFlow(verbose=False, precision=args.precision, **kw)
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision=args.precision, **kw)
     seeded_state(s, w)
     s._push()
     for k in range(args.warmup):

@@ -34,11 +34,12 @@ SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_las
            'gm_cc_create', 'gm_cc_destroy', 'gm_cc_last_error', 'gm_cc_get_sizes', 'gm_cc_get_indices',
            'gm_cc_get_surface_points', 'gm_cc_set_state', 'gm_cc_get_state', 'gm_cc_set_inlet',
            'gm_cc_set_history', 'gm_cc_get_history', 'gm_cc_step', 'gm_cc_apply', 'gm_cc_surface_forces',
-           'gm_cc_divergence_stats', 'gm_cc_phase_timing', 'gm_mac_ab2_rhs', 'gm_mac_ghost_apply',
+           'gm_cc_divergence_stats', 'gm_cc_phase_timing', 'gm_cc_legacy_step', 'gm_cc_set_legacy_history',
+           'gm_cc_get_legacy_history', 'gm_mac_ab2_rhs', 'gm_mac_ghost_apply',
            'gm_mac_ghost_correct', 'gm_mac_ghost_forces', 'gm_poisson_create',
            'gm_poisson_destroy', 'gm_poisson_last_error', 'gm_poisson_solve')
 CC_OP_MOMENTUM_ADVECTION, CC_OP_MOMENTUM_DIFFUSION, CC_OP_ADVECTION, CC_OP_DIFFUSION, CC_OP_H_MATVEC, CC_OP_PROJECT, \
-    CC_OP_PRESSURE_SOLVE = range(1, 8)
+    CC_OP_PRESSURE_SOLVE, CC_OP_MOMENTUM_ADVECTION_UPWIND = range(1, 9)
 MAC_AB2, MAC_RHS = 1, 2
 NOALLOC_MAX_CELLS = 1048576
 
@@ -105,7 +106,8 @@ class CcStepDiag(C.Structure):
                                           'cd_viscous', 'cl_pressure', 'cl_viscous', 'momentum_residual_linf',
                                           'coupled_momentum_residual_linf', 'predicted_divergence')] + \
                [('forces', C.c_double * 6)] + \
-               [(n, C.c_int32) for n in ('momentum_iterations', 'pressure_solves', 'status', 'gate')]
+               [(n, C.c_int32) for n in ('momentum_iterations', 'pressure_solves', 'status', 'gate')] + \
+               [(n, C.c_double) for n in ('pressure_residual_linf', 'pressure_residual_l2')]
 
 
 def _load():
@@ -194,6 +196,9 @@ def _load():
         'gm_cc_divergence_stats': ([P, P, P, P], C.c_int),
         'gm_cc_phase_timing': ([P, P], C.c_int),
         'gm_mac_ab2_rhs': ([P, P, P, P, P, P, P, P, I32, I32, D, D, D, D, D, I32, I32, P], C.c_int),
+        'gm_cc_legacy_step': ([P, D, I32, D, I32, C.POINTER(CcStepDiag)], C.c_int),
+        'gm_cc_set_legacy_history': ([P, I32, P, D], C.c_int),
+        'gm_cc_get_legacy_history': ([P, C.POINTER(I32), P, C.POINTER(D)], C.c_int),
         'gm_mac_ghost_apply': ([P, I64, I64, P, P, P, P, P, P, I32, D, P], C.c_int),
         'gm_mac_ghost_correct': ([P, P, P, P, P, P, P, I32, I32, D, D, D, D, I32, P], C.c_int),
         'gm_mac_ghost_forces': ([P, P, P, I32, I32, D, D, D, D, D, I32, D, P, P], C.c_int),

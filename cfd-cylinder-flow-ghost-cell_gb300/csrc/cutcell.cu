@@ -169,6 +169,7 @@ struct CcDiagDev {
   unsigned long long rhs_max, mres, coupled, umax, vmax, divmax;
   unsigned long long pdiv[3];  // predicted divergence of the start-up, first and second solve
   double forces[6];
+  double res_linf, res_l2;     // the legacy step's pressure residual b - A phi (unscaled rows)
 };
 
 // field value c of the concatenated face grid, with the inlet column from `inl` when given
@@ -198,8 +199,10 @@ __device__ __forceinline__ double warp_row_dot(const int64_t* __restrict__ ptr, 
 // ---- momentum right-hand side -------------------------------------------------------------
 // One thread per vertex (j, i) of the (ny+1) x (nx+1) grid: F_xx and F_yy of cell (j, i),
 // F_xy and F_yx of vertex (j, i) (solver/cut_cell_solver.py:808-914).  ADV: the advective
-// form (nu = 0: no viscous part); otherwise the viscous form without advection.
-template <bool ADV>
+// form (nu = 0: no viscous part), with the transported velocity centred or, UPW, taken from
+// the upwind side of the face's advecting velocity (transport='upwind'); otherwise the
+// viscous form without advection.
+template <bool ADV, bool UPW = false>
 __global__ void k_cc_flux(CcGeo g, const double* __restrict__ X, const double* __restrict__ inl, double rnu,
                           int slip, CcFlux F) {
   const int nx = g.nx, ny = g.ny;
@@ -217,8 +220,9 @@ __global__ void k_cc_flux(CcGeo g, const double* __restrict__ X, const double* _
     const double ul = U(j, i), ur = U(j, i + 1), vb = W(j, i), vt = W(j + 1, i);
     if (ADV) {
       const double uf = 0.5 * (ul + ur), vf = 0.5 * (vb + vt);
-      F.xx[c] = -(uf * uf * g.axx[c]);
-      F.yy[c] = -(vf * vf * g.ayy[c]);
+      const double ua = UPW ? (uf >= 0.0 ? ul : ur) : uf, va = UPW ? (vf >= 0.0 ? vb : vt) : vf;
+      F.xx[c] = -(uf * ua * g.axx[c]);
+      F.yy[c] = -(vf * va * g.ayy[c]);
     } else {
       F.xx[c] = rnu * (ur - ul) * g.cxx[c];
       F.yy[c] = rnu * (vt - vb) * g.cyy[c];
@@ -230,7 +234,7 @@ __global__ void k_cc_flux(CcGeo g, const double* __restrict__ X, const double* _
     else if (j == ny) f = (ADV || slip) ? 0.0 : -(rnu * U(ny - 1, i) * (2.0 * g.cxy[t]));
     else if (ADV) {
       const double vf = i == 0 ? W(j, 0) : (i == nx ? W(j, nx - 1) : 0.5 * (W(j, i - 1) + W(j, i)));
-      const double ua = 0.5 * (U(j - 1, i) + U(j, i));
+      const double ua = UPW ? (vf >= 0.0 ? U(j - 1, i) : U(j, i)) : 0.5 * (U(j - 1, i) + U(j, i));
       f = -(vf * ua * g.axy[t]);
     } else {
       f = rnu * (U(j, i) - U(j - 1, i)) * g.cxy[t];
@@ -249,7 +253,7 @@ __global__ void k_cc_flux(CcGeo g, const double* __restrict__ X, const double* _
       }
     } else if (ADV) {
       const double uf = j == 0 ? U(0, i) : (j == ny ? U(ny - 1, i) : 0.5 * (U(j - 1, i) + U(j, i)));
-      const double va = 0.5 * (W(j, i - 1) + W(j, i));
+      const double va = UPW ? (uf >= 0.0 ? W(j, i - 1) : W(j, i)) : 0.5 * (W(j, i - 1) + W(j, i));
       f = -(uf * va * g.ayx[t]);
     } else {
       f = rnu * (W(j, i) - W(j, i - 1)) * g.cyx[t];
@@ -564,6 +568,70 @@ __global__ void k_cc_stepmax(CcGeo g, const double* __restrict__ U, unsigned lon
   }
 }
 
+// The legacy predictor (advance_momentum_predictor, solver/cut_cell_solver.py:1017-1033) and
+// apply_predictor_boundary (:663-670): a = advective + viscous acceleration, u* = u + dt a
+// (forward Euler) or u + dt ((1 + alpha) a - alpha a_prev) (AB2), a_prev = a; then the inlet
+// column, zero on closed faces and on the channel-wall v rows.
+__global__ void k_cc_legacy_pred(CcGeo g, const double* __restrict__ U, const double* __restrict__ aa,
+                                 const double* __restrict__ ad, double* __restrict__ prev,
+                                 const double* __restrict__ inl, double dt, double alpha, int ab2,
+                                 double* __restrict__ star) {
+  const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= g.F) return;
+  const double a = aa[f] + ad[f];
+  double s = ab2 ? U[f] + dt * ((1 + alpha) * a - alpha * prev[f]) : U[f] + dt * a;
+  prev[f] = a;
+  if (f < g.usize) {
+    if (f % (g.nx + 1) == 0) s = inl[f / (g.nx + 1)];
+    if (g.ax[f] == 0.0) s = 0.0;
+  } else {
+    const int64_t c = f - g.usize;
+    const int j = (int)(c / g.nx);
+    if (g.ay[c] == 0.0 || j == 0 || j == g.ny) s = 0.0;
+  }
+  star[f] = s;
+}
+
+// max |r| and sum r^2 of the pressure residual in the unscaled rows (the row-scaled residual
+// times kappa), per block, then folded in block order (deterministic)
+constexpr int CC_RES_BLOCKS = 152;
+__global__ void k_cc_resnorm_part(CcGeo g, const double* __restrict__ res, double* __restrict__ part) {
+  __shared__ double smax[CC_TPB], ssum[CC_TPB];
+  double m = 0.0, q = 0.0;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < g.psize; c += (int64_t)gridDim.x * blockDim.x)
+    if (g.cell_type[c] != -1) {
+      const double r = res[c] * g.kappa[c];
+      m = (r != r) ? r : fmax(m, fabs(r));
+      q += r * r;
+    }
+  smax[threadIdx.x] = m;
+  ssum[threadIdx.x] = q;
+  __syncthreads();
+  for (int k = CC_TPB / 2; k > 0; k >>= 1) {
+    if ((int)threadIdx.x < k) {
+      const double o = smax[threadIdx.x + k];
+      smax[threadIdx.x] = (o != o) ? o : fmax(smax[threadIdx.x], o);
+      ssum[threadIdx.x] += ssum[threadIdx.x + k];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = smax[0];
+    part[2 * blockIdx.x + 1] = ssum[0];
+  }
+}
+__global__ void k_cc_resnorm_fold(const double* __restrict__ part, int nb, double* __restrict__ linf,
+                                  double* __restrict__ l2) {
+  double m = 0.0, q = 0.0;
+  for (int b = 0; b < nb; ++b) {
+    const double o = part[2 * b];
+    m = (o != o) ? o : fmax(m, o);
+    q += part[2 * b + 1];
+  }
+  *linf = m;
+  *l2 = sqrt(q);
+}
+
 // fixed-order block sum of one value per thread (blockDim a power of two <= 1024)
 __device__ double block_sum(double v, double* sh) {
   const int tid = threadIdx.x;
@@ -851,6 +919,11 @@ struct gm_cc {
   Buf<double> q0, now, d0, gp, mid, halfq, expl, offset, dq, rhs, star, w, result, action, tmp, zero, Rw;
   Buf<double> fxx, fxy, fyx, fyy;
   Buf<double> B, phi, inc, pb, io_f, io_p;
+  // the legacy predictor: advective and viscous accelerations, scratch, previous acceleration,
+  // predicted field, residual-norm partials; its history
+  Buf<double> la, ld, lr, lprev, lstar, lres;
+  bool l_has_prev = false;
+  double l_prev_dt = 0;
   CcFlux flux{};
   // GMRES(30)
   static constexpr int GM_M = 30;
@@ -900,12 +973,13 @@ void copy_in(double* dst, const double* src, size_t n, cudaStream_t st) {
 
 // ---- momentum evaluation (five launches) ----------------------------------------------------
 void momentum(gm_cc* c, bool adv, const double* X, const double* inl, double nu, int mode, double hdt, double* Y,
-              double* Rout, cudaStream_t st) {
+              double* Rout, cudaStream_t st, bool upwind = false) {
   const double rnu = c->rho * nu;
   const int64_t nv = (int64_t)(c->ny + 1) * (c->nx + 1);
   const bool shear = !adv && nu != 0.0;
   counted();
-  if (adv) k_cc_flux<true><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, inl, rnu, c->slip, c->flux);
+  if (adv && upwind) k_cc_flux<true, true><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, inl, rnu, c->slip, c->flux);
+  else if (adv) k_cc_flux<true><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, inl, rnu, c->slip, c->flux);
   else k_cc_flux<false><<<nblk(nv), CC_TPB, 0, st>>>(c->geo, X, inl, rnu, c->slip, c->flux);
   const int nrows = adv ? c->fix.n_adv : c->fix.n_dif + (shear ? c->wall.n : 0);
   if (nrows > 0) {
@@ -1129,6 +1203,34 @@ gm_cc::Graph& step_graph(gm_cc* c, double dt) {
   gr.hist = c->has_history;
   gr.prev_dt = c->prev_dt;
   return gr;
+}
+
+// One step of the legacy cut-cell loop (solver/main.py:297-333, boundary='cut_cell',
+// time_scheme='legacy'): the predictor on the stored state (its inlet column is the previous
+// step's), compute_rhs / solve_pressure / apply_corrector (the projection of the AB2/CN path),
+// p = phi, the step maxima and the forces on the true circle.
+void legacy_body(gm_cc* c, double dt, bool centered, cudaStream_t st) {
+  const int64_t F = c->F;
+  CCK(cudaMemsetAsync(c->diag.p, 0, sizeof(CcDiagDev), st));
+  momentum(c, true, c->U.p, nullptr, 0.0, 2, 0.0, c->la.p, c->lr.p, st, !centered);
+  momentum(c, false, c->U.p, nullptr, c->nu, 2, 0.0, c->ld.p, c->lr.p, st);
+  const bool ab2 = centered && c->l_has_prev;
+  counted();
+  k_cc_legacy_pred<<<nblk(F), CC_TPB, 0, st>>>(c->geo, c->U.p, c->la.p, c->ld.p, c->lprev.p, c->inlet.p, dt,
+                                               ab2 ? dt / (2 * c->l_prev_dt) : 0.0, ab2 ? 1 : 0, c->lstar.p);
+  project(c, c->lstar.p, dt, c->w.p, c->Pst.p, S_P1, 1, st);
+  counted();
+  k_cc_resnorm_part<<<CC_RES_BLOCKS, CC_TPB, 0, st>>>(c->geo, gmi::pressure_residual(c->P), c->lres.p);
+  counted();
+  k_cc_resnorm_fold<<<1, 1, 0, st>>>(c->lres.p, CC_RES_BLOCKS, &c->diag.p->res_linf, &c->diag.p->res_l2);
+  counted();
+  k_cc_unpack<<<nblk(F), CC_TPB, 0, st>>>(c->geo, c->w.p, c->inlet.p, c->U.p);
+  counted();
+  k_cc_stepmax<<<std::min<unsigned>(nblk(F), 1216), CC_TPB, 0, st>>>(c->geo, c->U.p, &c->diag.p->divmax,
+                                                                      &c->diag.p->umax, &c->diag.p->vmax);
+  counted();
+  k_cc_forces<<<1, CC_FORCE_THREADS, 0, st>>>(gmi::surface(c->P), c->wall, c->U.p, c->Pst.p, c->nu * c->rho, c->pb.p,
+                                             c->diag.p->forces);
 }
 
 double bits_to_double(unsigned long long b) {
@@ -1443,7 +1545,7 @@ int gm_cc_create(const gm_cc_config* cfg, gm_cc** out) {
     // state and work arrays
     for (Buf<double>* b : {&C->U, &C->prev_adv, &C->q0, &C->now, &C->d0, &C->gp, &C->mid, &C->halfq, &C->expl,
                            &C->offset, &C->dq, &C->rhs, &C->star, &C->w, &C->result, &C->action, &C->tmp, &C->zero,
-                           &C->Rw}) {
+                           &C->Rw, &C->la, &C->ld, &C->lr, &C->lprev, &C->lstar}) {
       b->alloc(F);
       b->zero(st);
     }
@@ -1464,6 +1566,7 @@ int gm_cc_create(const gm_cc_config* cfg, gm_cc** out) {
     C->gdev.alloc(1);
     const double one = 1.0;
     CCK(cudaMemcpyAsync(C->gone.p, &one, sizeof one, cudaMemcpyHostToDevice, st));
+    C->lres.alloc(2 * CC_RES_BLOCKS);
     C->diag.alloc(1);
     CCK(cudaMallocHost(&C->host_diag, sizeof(CcDiagDev)));
     C->d_act.upload(C->act_idx, st);
@@ -1621,6 +1724,7 @@ int gm_cc_step(gm_cc* c, double dt, int32_t n_steps, double start_time, gm_cc_st
       out.time = start_time + (k + 1) * dt;
       out.dt = dt;
       out.momentum_iterations = its;
+      out.pressure_residual_linf = out.pressure_residual_l2 = std::nan("");
       out.momentum_residual_linf = bits_to_double(d.mres);
       out.coupled_momentum_residual_linf = bits_to_double(d.coupled);
       out.predicted_divergence = std::max(bits_to_double(d.pdiv[1]), bits_to_double(d.pdiv[2]));
@@ -1666,6 +1770,89 @@ int gm_cc_step(gm_cc* c, double dt, int32_t n_steps, double start_time, gm_cc_st
   });
 }
 
+int gm_cc_legacy_step(gm_cc* c, double dt, int32_t n_steps, double start_time, int32_t centered,
+                      gm_cc_step_diag* diag) {
+  if (!c) return GM_EVALUE;
+  if (!(std::isfinite(dt) && dt > 0) || n_steps <= 0) {
+    c->err = "Finite fields and a positive timestep are required";
+    return GM_EVALUE;
+  }
+  return guarded(c, [&] {
+    cudaStream_t st = c->st;
+    for (int32_t k = 0; k < n_steps; ++k) {
+      CCK(cudaMemsetAsync(gmi::control(c->P), 0, sizeof(StepCtl), st));
+      legacy_body(c, dt, centered != 0, st);
+      CCK(cudaGetLastError());
+      CCK(cudaMemcpyAsync(c->host_diag, c->diag.p, sizeof(CcDiagDev), cudaMemcpyDeviceToHost, st));
+      std::string m;
+      const int prc = gmi::check(c->P, "cut-cell legacy step", m);  // synchronises the stream
+      // the predictor has replaced its history (solver/cut_cell_solver.py:1029-1031)
+      c->l_has_prev = true;
+      c->l_prev_dt = dt;
+      const CcDiagDev& d = *c->host_diag;
+      gm_cc_step_diag out{};
+      out.time = start_time + (k + 1) * dt;
+      out.dt = dt;
+      out.predicted_divergence = bits_to_double(d.pdiv[1]);
+      out.pressure_solves = 1;
+      out.max_divergence = bits_to_double(d.divmax);
+      out.cfl = dt * (bits_to_double(d.umax) / c->dx + bits_to_double(d.vmax) / c->dy);
+      for (int q = 0; q < 6; ++q) out.forces[q] = d.forces[q];
+      const double denom = 0.5 * c->rho * (c->U_ref * c->U_ref) * c->D;
+      out.cd = d.forces[0] / denom;
+      out.cl = d.forces[1] / denom;
+      out.cd_pressure = d.forces[2] / denom;
+      out.cd_viscous = d.forces[4] / denom;
+      out.cl_pressure = d.forces[3] / denom;
+      out.cl_viscous = d.forces[5] / denom;
+      out.pressure_residual_linf = d.res_linf;
+      out.pressure_residual_l2 = d.res_l2;
+      int cls = GM_OK, gate = 0;
+      std::string msg;
+      char buf[96];
+      if (prc != GM_OK) { cls = prc; gate = GM_GATE_PRESSURE; msg = m; }
+      else if (!(out.predicted_divergence < 1e-10)) {
+        std::snprintf(buf, sizeof buf, "Pressure residual exceeds divergence budget: %g", out.predicted_divergence);
+        cls = GM_ERUNTIME; gate = GM_GATE_PRESSURE; msg = buf;
+      } else if (!std::isfinite(out.cd) || !std::isfinite(out.cl)) {
+        std::snprintf(buf, sizeof buf, "Non-finite force at t=%g; results not saved", out.time);
+        cls = GM_EFLOAT; gate = GM_GATE_FORCE; msg = buf;
+      }
+      out.status = cls;
+      out.gate = gate;
+      if (diag) diag[k] = out;
+      if (cls != GM_OK) throw CcFail(cls, msg);
+    }
+  });
+}
+
+int gm_cc_set_legacy_history(gm_cc* c, int32_t has_history, const double* prev_accel, double prev_dt) {
+  if (!c) return GM_EVALUE;
+  if (has_history && (!prev_accel || !(std::isfinite(prev_dt) && prev_dt > 0))) {
+    c->err = "Incomplete predictor checkpoint history";
+    return GM_EVALUE;
+  }
+  return guarded(c, [&] {
+    if (has_history) copy_in(c->lprev.p, prev_accel, c->F, c->st);
+    else CCK(cudaMemsetAsync(c->lprev.p, 0, c->F * sizeof(double), c->st));
+    CCK(cudaStreamSynchronize(c->st));
+    c->l_has_prev = has_history != 0;
+    c->l_prev_dt = has_history ? prev_dt : 0.0;
+  });
+}
+
+int gm_cc_get_legacy_history(gm_cc* c, int32_t* has_history, double* prev_accel, double* prev_dt) {
+  if (!c) return GM_EVALUE;
+  return guarded(c, [&] {
+    if (has_history) *has_history = c->l_has_prev ? 1 : 0;
+    if (prev_dt) *prev_dt = c->l_prev_dt;
+    if (prev_accel) {
+      CCK(cudaMemcpyAsync(prev_accel, c->lprev.p, c->F * sizeof(double), cudaMemcpyDefault, c->st));
+      CCK(cudaStreamSynchronize(c->st));
+    }
+  });
+}
+
 int gm_cc_phase_timing(const gm_cc* c, double out[8]) {
   if (!c || !out) return GM_EVALUE;
   for (int q = 0; q < gm_cc::NPHASE; ++q) out[q] = c->phase_ms[q];
@@ -1692,10 +1879,12 @@ int gm_cc_apply(gm_cc* c, int32_t op, double param, const double* x, double* y, 
     };
     switch (op) {
       case GM_CC_OP_MOMENTUM_ADVECTION:
+      case GM_CC_OP_MOMENTUM_ADVECTION_UPWIND:
       case GM_CC_OP_MOMENTUM_DIFFUSION: {
         copy_in(c->tmp.p, x, F, st);
-        const bool adv = op == GM_CC_OP_MOMENTUM_ADVECTION;
-        momentum(c, adv, c->tmp.p, nullptr, adv ? 0.0 : param, 2, 0.0, c->w.p, c->action.p, st);
+        const bool adv = op != GM_CC_OP_MOMENTUM_DIFFUSION;
+        momentum(c, adv, c->tmp.p, nullptr, adv ? 0.0 : param, 2, 0.0, c->w.p, c->action.p, st,
+                 op == GM_CC_OP_MOMENTUM_ADVECTION_UPWIND);
         CCK(cudaMemcpyAsync(y, c->w.p, F * sizeof(double), cudaMemcpyDefault, st));
         if (y2) CCK(cudaMemcpyAsync(y2, c->action.p, F * sizeof(double), cudaMemcpyDefault, st));
         break;

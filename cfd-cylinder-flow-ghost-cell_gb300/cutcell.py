@@ -1,8 +1,10 @@
-"""MAC_CylinderFlow(boundary='cut_cell', time_scheme='ab2_cn') on the GPU.
+"""MAC_CylinderFlow(boundary='cut_cell') on the GPU, with either time scheme.
 
 The reference's cut-cell path (CutCellBoundary, solver/cut_cell_solver.py:370-1015, stepped by
 solver/main.py:245-501) with the same constructor keywords, ``solve`` loop, diagnostics keys and
-exceptions.  The geometry-dependent setup runs once on the host (cutcell_geometry.py); the
+exceptions: the AB2/CN step (time_scheme='ab2_cn', advance_ab2_cn) and the legacy step
+(time_scheme='legacy': advance_momentum_predictor with centred transport and AB2 or upwind
+transport and forward Euler, then compute_rhs, solve_pressure and apply_corrector).  The geometry-dependent setup runs once on the host (cutcell_geometry.py); the
 pressure operator, its boundary-corrected inverse and every step run in libghostmac.so
 (gm_cc_* entry points, csrc/cutcell.cu).  All three pressure_solver choices of the reference
 ('direct' sparse LU, 'iterative' ILU-GMRES, 'cg_dct' CG with the boundary-Schur DCT
@@ -23,6 +25,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _lib
+from ._args import check_reference_arguments
 from ._lib import lib, ptr
 from .cutcell_geometry import CutCellSetup
 
@@ -122,19 +125,25 @@ class CutCellIntegrator:
         _check(lib.gm_cc_apply(self._h, op, float(param), ptr(x), ptr(y), ptr(y2) if n_out2 else None), self._h)
         return (y, y2) if n_out2 else y
 
-    def compute_momentum_rhs(self, u, v, nu, rho, transport='centered', include_advection=True):
-        """(a_u, a_v, rhs_u, rhs_v) of CutCellBoundary.compute_momentum_rhs for the two forms the
-        AB2/CN step uses: advective (nu = 0, include_advection) and viscous (no advection)."""
-        if transport != 'centered':
-            raise NotImplementedError('the cut-cell AB2/CN path uses centered transport')
+    def compute_momentum_rhs(self, u, v, nu, rho, transport='upwind', include_advection=True):
+        """(a_u, a_v, rhs_u, rhs_v) of CutCellBoundary.compute_momentum_rhs
+        (solver/cut_cell_solver.py:790-957): the advective form (centred or upwind transport)
+        and the viscous form, each one device evaluation; with advection and nu != 0 the two
+        are added (the reference adds the fluxes before differencing, which agrees to
+        rounding)."""
+        if transport not in ('centered', 'upwind'):
+            raise ValueError('transport must be centered or upwind')
         if float(rho) != float(self._s.rho):
             raise ValueError('rho must be the case density')
-        if include_advection and nu != 0:
-            raise NotImplementedError('advection is evaluated with nu = 0 by the AB2/CN step')
         field = np.r_[_f64(u).ravel(), _f64(v).ravel()]
         n = field.size
-        op = _lib.CC_OP_MOMENTUM_ADVECTION if include_advection else _lib.CC_OP_MOMENTUM_DIFFUSION
-        a, r = self._apply(op, nu, field, n, n)
+        a = r = None
+        if include_advection:
+            op = _lib.CC_OP_MOMENTUM_ADVECTION if transport == 'centered' else _lib.CC_OP_MOMENTUM_ADVECTION_UPWIND
+            a, r = self._apply(op, 0.0, field, n, n)
+        if nu != 0 or not include_advection:
+            ad, rd = self._apply(_lib.CC_OP_MOMENTUM_DIFFUSION, nu, field, n, n)
+            a, r = (ad, rd) if a is None else (a + ad, r + rd)
         us = (self.ny) * (self.nx + 1)
         shp_u, shp_v = (self.ny, self.nx + 1), (self.ny + 1, self.nx)
         return a[:us].reshape(shp_u), a[us:].reshape(shp_v), r[:us].reshape(shp_u), r[us:].reshape(shp_v)
@@ -209,29 +218,19 @@ class CutCellIntegrator:
 
 
 class CutCellFlow:
-    """The cut-cell AB2/CN MAC_CylinderFlow on the GPU (solver/main.py:19-501 with
-    boundary='cut_cell', time_scheme='ab2_cn', transport='centered')."""
+    """The cut-cell MAC_CylinderFlow on the GPU (solver/main.py:19-501 with boundary='cut_cell'):
+    the AB2/CN step (time_scheme='ab2_cn', centred transport) or the legacy step
+    (time_scheme='legacy', centred or upwind transport)."""
 
     def __init__(self, nx=400, ny=100, Lx=20.0, Ly=5.0, D=1.0, xc=5.0, yc=2.5, nu=0.01, rho=1.0, U_inf=1.0,
                  inflow='uniform', U_m=None, slip_walls=False, verbose=True, boundary='cut_cell',
-                 transport='centered', pressure_solver='direct', marker_spacing_factor=1.5, time_scheme='ab2_cn',
+                 transport='centered', pressure_solver='direct', marker_spacing_factor=1.5, time_scheme='legacy',
                  ghost_pressure_extension='neumann', ghost_velocity_interpolation='bilinear', precision='fp64'):
         # argument checks of solver/main.py:45-129
-        if boundary not in ('immersed', 'staircase', 'ghost_cell', 'cut_cell') or transport not in ('centered', 'upwind'):
-            raise ValueError('Choose boundary=immersed/staircase/ghost_cell/cut_cell and transport=centered/upwind')
-        if pressure_solver not in ('direct', 'iterative', 'cg_dct'):
-            raise ValueError("pressure_solver must be direct, iterative or cg_dct")
-        if time_scheme not in ('legacy', 'ab2_cn'):
-            raise ValueError('time_scheme must be legacy or ab2_cn')
-        if time_scheme == 'ab2_cn' and (boundary not in ('cut_cell', 'ghost_cell') or transport != 'centered'):
-            raise ValueError('ab2_cn requires cut_cell/ghost_cell and centered transport')
-        if ghost_pressure_extension not in ('neumann', 'quadratic') or \
-                ghost_velocity_interpolation not in ('bilinear', 'biquadratic'):
-            raise ValueError('Unknown Ghost pressure extension or velocity interpolation')
-        if (ghost_pressure_extension != 'neumann' or ghost_velocity_interpolation != 'bilinear'):
-            raise ValueError('Ghost reconstruction options require Ghost AB2/CN')
-        if boundary != 'cut_cell' or time_scheme != 'ab2_cn':
-            raise NotImplementedError('CutCellFlow implements boundary="cut_cell", time_scheme="ab2_cn"')
+        check_reference_arguments(boundary, transport, pressure_solver, time_scheme, ghost_pressure_extension,
+                                  ghost_velocity_interpolation)
+        if boundary != 'cut_cell':
+            raise NotImplementedError('CutCellFlow implements boundary="cut_cell"')
         if precision != 'fp64':
             raise NotImplementedError('the cut-cell path runs in FP64')
         if any(isinstance(n, bool) or not isinstance(n, (int, np.integer)) or n < 4 for n in (nx, ny)):
@@ -283,12 +282,27 @@ class CutCellFlow:
         self.v = np.empty((self.ny + 1, self.nx))
         self.p = np.empty((self.ny, self.nx))
         self.phi = np.zeros((self.ny, self.nx))
+        self.time = 0.0
         self._pull()
+        if time_scheme == 'legacy':
+            # the legacy loop starts from the unprojected field of solver/main.py:166-177: inlet
+            # rows, the faces of covered cells zero, closed faces zero
+            g = self.cut_geom
+            self.u[:, :] = self.u_inlet[:, None]
+            self.v[:, :] = 0.0
+            self.p[:, :] = 0.0
+            js, is_ = np.nonzero(g.cell_type == -1)
+            self.u[js, is_] = 0.0
+            self.u[js, is_ + 1] = 0.0
+            self.u[g.ax == 0] = 0.0
+            self.v[g.ay == 0] = 0.0
+            self._push()
         self.time = 0.0
         self.run_options = {}
         self.last_step_diagnostics = {}
         if verbose:
-            print(f"Cut-cell AB2/CN on the GPU ready in {_time.time() - t0:.3f}s (Re={self.Re:.1f}).")
+            scheme = 'AB2/CN' if time_scheme == 'ab2_cn' else 'legacy'
+            print(f"Cut-cell {scheme} on the GPU ready in {_time.time() - t0:.3f}s (Re={self.Re:.1f}).")
 
     def _create(self, st, inflow, U_m):
         g = st.geom
@@ -343,6 +357,8 @@ class CutCellFlow:
 
     def _pull(self):
         _check(lib.gm_cc_get_state(self._h, ptr(self.u), ptr(self.v), ptr(self.p)), self._h)
+        if self.time_scheme == 'legacy' and self.time > 0:
+            self.phi[...] = self.p  # the legacy loop keeps p = phi (solver/main.py:377-378)
 
     def _push(self):
         for name in ('u', 'v', 'p'):
@@ -356,6 +372,17 @@ class CutCellFlow:
         _check(lib.gm_cc_set_inlet(self._h, ptr(self.u_inlet)), self._h)
 
     def _diag_dict(self, d):
+        if self.time_scheme == 'legacy':
+            # solve_pressure's record (solver/cut_cell_solver.py:723-728); the inverse is direct,
+            # so no Krylov iterations
+            pd = dict(residual_linf=d.pressure_residual_linf, residual_l2=d.pressure_residual_l2, iterations=0,
+                      predicted_divergence=d.predicted_divergence, seconds=0.0)
+            if self.pressure_solver == 'cg_dct':
+                pd['preconditioner'] = dict(self.cc.pressure_inverse_info)
+            self.cc.last_pressure_diagnostics = dict(pd)
+            return dict(pd, time=d.time, dt=d.dt, max_divergence=d.max_divergence, cfl=d.cfl, cd=d.cd, cl=d.cl,
+                        cd_pressure=d.cd_pressure, cd_viscous=d.cd_viscous, cl_pressure=d.cl_pressure,
+                        cl_viscous=d.cl_viscous)
         pd = dict(residual_linf=float('nan'), residual_l2=float('nan'), iterations=0,
                   predicted_divergence=d.predicted_divergence, seconds=0.0,
                   preconditioner=dict(self.cc.pressure_inverse_info),
@@ -371,12 +398,16 @@ class CutCellFlow:
         """n_steps on the device state without host transfers; (status, diag records)."""
         diag = (_lib.CcStepDiag * n_steps)()
         t = self.time if start_time is None else start_time
-        rc = lib.gm_cc_step(self._h, float(dt), int(n_steps), float(t), diag)
+        if self.time_scheme == 'legacy':
+            rc = lib.gm_cc_legacy_step(self._h, float(dt), int(n_steps), float(t),
+                                       1 if self.transport == 'centered' else 0, diag)
+        else:
+            rc = lib.gm_cc_step(self._h, float(dt), int(n_steps), float(t), diag)
         return rc, diag
 
     def solve(self, n_steps=25000, dt=0.002, perturb_transient=True, perturb_duration=None, perturb_amp=0.15,
               save_artifacts=True, verbose=None, step_callback=None):
-        """Step loop of solver/main.py:245-501 for the cut-cell AB2/CN path."""
+        """Step loop of solver/main.py:245-501 for the cut-cell path."""
         if isinstance(n_steps, bool) or not isinstance(n_steps, (int, np.integer)) or n_steps <= 0:
             raise ValueError('n_steps must be a positive integer')
         if not np.isfinite(dt) or dt <= 0:
@@ -397,10 +428,12 @@ class CutCellFlow:
         while s < n_steps:
             now_t = start + (s + 1) * dt
             if s % 100 == 0:
-                # explicit advection screen of solver/main.py:273-278 on the current state
+                # explicit advection (and, legacy, diffusion) screen of solver/main.py:273-278
                 self._pull()
-                rate = np.max(np.abs(self.u)) / self.dx + np.max(np.abs(self.v)) / self.dy
-                if not np.isfinite(rate) or dt * rate > .5:
+                legacy = self.time_scheme == 'legacy'
+                rate = (np.max(np.abs(self.u)) / self.dx + np.max(np.abs(self.v)) / self.dy
+                        + (2 * self.nu * (self.dx ** -2 + self.dy ** -2) if legacy else 0.))
+                if not np.isfinite(rate) or dt * rate > (1. if legacy else .5):
                     raise RuntimeError(f'Explicit timestep unsafe at t={self.time:g}: dt*rate={dt * rate:g}; reduce dt')
             perturbing = perturb_transient and self.inflow == 'uniform' and now_t <= perturb_duration
             if perturbing:
@@ -462,25 +495,52 @@ class CutCellFlow:
         return dict(nx=self.nx, ny=self.ny, Lx=self.Lx, Ly=self.Ly, D=self.D, xc=self.xc, yc=self.yc, nu=self.nu,
                     rho=self.rho, U_ref=self.U_ref, U_inf=self.U_inf, U_m=self.U_m, inflow=self.inflow,
                     slip_walls=self.slip_walls, dt=dt, n_steps=n_steps, end_time=self.time, boundary=self.boundary,
-                    transport=self.transport, time_integrator='AB2_CN_discrete_incremental',
+                    transport=self.transport,
+                    time_integrator=('AB2_CN_discrete_incremental' if self.time_scheme == 'ab2_cn'
+                                     else 'AB2' if self.transport == 'centered' else 'Euler'),
                     time_scheme=self.time_scheme, pressure_solver=self.pressure_solver,
                     pressure_backend='cut_cell_fft_boundary_schur',
                     pressure_preconditioner=self.cc.pressure_inverse_info, perturb_transient=perturb_transient,
                     perturb_duration=perturb_duration, perturb_amp=perturb_amp, source_sha256=self._source_hashes())
 
+    def legacy_history(self):
+        """(prev_au, prev_av, prev_dt) of the legacy predictor, or (None, None, None)."""
+        has = C.c_int32()
+        dtp = C.c_double()
+        buf = np.empty(self.u.size + self.v.size)
+        _check(lib.gm_cc_get_legacy_history(self._h, C.byref(has), ptr(buf), C.byref(dtp)), self._h)
+        if not has.value:
+            return None, None, None
+        return (buf[:self.u.size].reshape(self.u.shape).copy(), buf[self.u.size:].reshape(self.v.shape).copy(),
+                float(dtp.value))
+
+    def set_legacy_history(self, prev_au, prev_av, prev_dt):
+        if prev_au is None:
+            _check(lib.gm_cc_set_legacy_history(self._h, 0, None, 0.0), self._h)
+            return
+        buf = np.r_[_f64(prev_au).ravel(), _f64(prev_av).ravel()]
+        _check(lib.gm_cc_set_legacy_history(self._h, 1, ptr(buf), float(prev_dt)), self._h)
+
     def save_checkpoint(self, path, *, overwrite=False):
-        """Atomic schema-1 checkpoint with the cut-cell AB2/CN history (solver/main.py:503-530):
-        the state, the inlet, cn_advection (packed) and cn_pressure, cn_dt."""
+        """Atomic schema-1 checkpoint with the cut-cell history (solver/main.py:503-530): the
+        state, the inlet, and cn_advection (packed), cn_pressure, cn_dt (AB2/CN) or prev_au,
+        prev_av, prev_dt (legacy)."""
         path = Path(path)
         if path.exists() and not overwrite:
             raise FileExistsError(path)
         path.parent.mkdir(parents=True, exist_ok=True)
-        adv, half, cn_dt = self.cc.history()
         arrays = dict(u=self.u, v=self.v, p=self.p, phi=self.phi, u_inlet=self.u_inlet)
-        if adv is not None:
-            arrays.update(cn_advection=adv, cn_pressure=half)
+        prev_dt = cn_dt = None
+        if self.time_scheme == 'legacy':
+            au, av, prev_dt = self.legacy_history()
+            if au is not None:
+                arrays.update(prev_au=au, prev_av=av)
+        else:
+            adv, half, cn_dt = self.cc.history()
+            if adv is not None:
+                arrays.update(cn_advection=adv, cn_pressure=half)
         meta = dict(schema=1, configuration=self.configuration, time=self.time, run_options=self.run_options,
-                    prev_dt=None, cn_dt=cn_dt, diagnostics=self.last_step_diagnostics,
+                    prev_dt=prev_dt, cn_dt=cn_dt, diagnostics=self.last_step_diagnostics,
                     source_sha256=self._source_hashes())
         tmp = None
         try:
@@ -526,12 +586,22 @@ class CutCellFlow:
             solver.run_options = meta['run_options']
             solver.last_step_diagnostics = meta['diagnostics']
             hist = {}
-            for name in ('cn_advection', 'cn_pressure'):
+            for name in ('prev_au', 'prev_av', 'cn_advection', 'cn_pressure'):
                 value = data[name].copy() if name in data else None
                 if value is not None and not np.isfinite(value).all():
                     raise ValueError(f'Invalid checkpoint history: {name}')
                 hist[name] = value
             cn_dt = meta['cn_dt']
+            if solver.time_scheme == 'legacy':
+                au, av, prev_dt = hist['prev_au'], hist['prev_av'], meta['prev_dt']
+                if solver.time > 0 and (au is None or au.shape != solver.u.shape or av is None
+                                        or av.shape != solver.v.shape or prev_dt is None
+                                        or not np.isfinite(prev_dt) or prev_dt <= 0):
+                    raise ValueError('Incomplete predictor checkpoint history')
+                solver._push()
+                if au is not None and prev_dt is not None:
+                    solver.set_legacy_history(au, av, prev_dt)
+                return solver
             if solver.time > 0:
                 adv, half = hist['cn_advection'], hist['cn_pressure']
                 if (adv is None or adv.shape != (solver.cc.qsize,) or half is None or half.shape != solver.p.shape

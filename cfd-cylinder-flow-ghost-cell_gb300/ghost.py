@@ -23,6 +23,7 @@ from types import SimpleNamespace
 import numpy as np
 
 from . import _lib
+from ._args import check_reference_arguments
 from ._lib import check, lib, ptr
 
 _PKG = Path(__file__).resolve().parent
@@ -259,45 +260,42 @@ def _solve_dict(info):
 
 
 class MAC_CylinderFlow:
-    """Ghost-cell AB2/CN cylinder flow on the GPU (solver/main.py:19-617, ghost_cell/ab2_cn path).
-    boundary='cut_cell' (with time_scheme='ab2_cn') constructs the cut-cell path instead
-    (cutcell.CutCellFlow), boundary='staircase' (with time_scheme='legacy') the legacy staircase
-    loop (staircase.StaircaseFlow)."""
+    """Cylinder flow on the GPU with the reference's MAC_CylinderFlow constructor
+    (solver/main.py:19-617), defaults included (boundary='immersed', time_scheme='legacy').  This
+    class runs the ghost-cell AB2/CN path; the other paths are other classes, which the
+    constructor returns: boundary='cut_cell' (either time scheme) cutcell.CutCellFlow,
+    boundary='staircase' staircase.StaircaseFlow, boundary='ghost_cell' with
+    time_scheme='legacy' staircase.LegacyGhostFlow.  boundary='immersed' is not built."""
 
     def __new__(cls, *args, **kwargs):
         import inspect
         bound = inspect.signature(cls.__init__).bind_partial(None, *args, **kwargs).arguments
-        if bound.get('boundary') == 'cut_cell':
+        boundary, scheme = bound.get('boundary', 'immersed'), bound.get('time_scheme', 'legacy')
+        if boundary == 'cut_cell':
             from .cutcell import CutCellFlow
             return CutCellFlow(*args, **kwargs)
-        if bound.get('boundary') == 'staircase':
+        if boundary == 'staircase':
             from .staircase import StaircaseFlow
             return StaircaseFlow(*args, **kwargs)
-        if bound.get('boundary', 'ghost_cell') == 'ghost_cell' and bound.get('time_scheme') == 'legacy':
+        if boundary == 'ghost_cell' and scheme == 'legacy':
             from .staircase import LegacyGhostFlow
             return LegacyGhostFlow(*args, **kwargs)
         return super().__new__(cls)
 
     def __init__(self, nx=400, ny=100, Lx=20.0, Ly=5.0, D=1.0, xc=5.0, yc=2.5,
                  nu=0.01, rho=1.0, U_inf=1.0, inflow='uniform', U_m=None,
-                 slip_walls=False, verbose=True, boundary='ghost_cell', transport='centered',
-                 pressure_solver='direct', marker_spacing_factor=1.5, time_scheme='ab2_cn',
+                 slip_walls=False, verbose=True, boundary='immersed', transport='centered',
+                 pressure_solver='direct', marker_spacing_factor=1.5, time_scheme='legacy',
                  ghost_pressure_extension='neumann', ghost_velocity_interpolation='bilinear', precision='fp64'):
-        """Keywords of solver/main.py:40-44.  ``precision`` (this library only): 'fp64' runs the plain
-        FP64 method; 'fp32' runs the separable inverses and the momentum stencils in FP32 and
-        refines every solve against the FP64 operator until the reference's residual targets hold."""
-        # argument checks of solver/main.py:45-80
-        if boundary not in ('immersed', 'staircase', 'ghost_cell', 'cut_cell') or transport not in ('centered', 'upwind'):
-            raise ValueError('Choose boundary=immersed/staircase/ghost_cell/cut_cell and transport=centered/upwind')
-        if pressure_solver not in ('direct', 'iterative', 'cg_dct'):
-            raise ValueError("pressure_solver must be direct, iterative or cg_dct")
-        if time_scheme not in ('legacy', 'ab2_cn'):
-            raise ValueError('time_scheme must be legacy or ab2_cn')
-        if ghost_pressure_extension not in ('neumann', 'quadratic') or \
-                ghost_velocity_interpolation not in ('bilinear', 'biquadratic'):
-            raise ValueError('Unknown Ghost pressure extension or velocity interpolation')
-        if boundary != 'ghost_cell' or time_scheme != 'ab2_cn' or transport != 'centered':
-            raise NotImplementedError('This library implements boundary="ghost_cell", time_scheme="ab2_cn"')
+        """Keywords and defaults of solver/main.py:40-44.  ``precision`` (this library only): 'fp64'
+        runs the plain FP64 method; 'fp32' runs the separable inverses and the momentum stencils in
+        FP32 and refines every solve against the FP64 operator until the reference's residual
+        targets hold."""
+        check_reference_arguments(boundary, transport, pressure_solver, time_scheme, ghost_pressure_extension,
+                                  ghost_velocity_interpolation)
+        if boundary != 'ghost_cell' or time_scheme != 'ab2_cn':
+            raise NotImplementedError(f'boundary={boundary!r} with time_scheme={time_scheme!r} is not built here '
+                                      '(the immersed-boundary projection is outside this library)')
         if pressure_solver not in ('direct', 'iterative') or slip_walls:
             raise ValueError('Ghost AB2/CN requires direct/iterative pressure and no-slip channel walls')
         if any(isinstance(n, bool) or not isinstance(n, (int, np.integer)) or n < 4 for n in (nx, ny)):

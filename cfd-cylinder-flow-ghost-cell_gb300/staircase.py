@@ -20,6 +20,7 @@ import time as _time
 import numpy as np
 
 from . import _lib
+from ._args import check_reference_arguments
 from ._lib import lib, ptr
 
 
@@ -35,25 +36,14 @@ class StaircaseFlow:
     _boundary = 'staircase'
 
     def __init__(self, nx=400, ny=100, Lx=20.0, Ly=5.0, D=1.0, xc=5.0, yc=2.5, nu=0.01, rho=1.0, U_inf=1.0,
-                 inflow='uniform', U_m=None, slip_walls=False, verbose=True, boundary='staircase',
+                 inflow='uniform', U_m=None, slip_walls=False, verbose=True, boundary=None,
                  transport='centered', pressure_solver='direct', marker_spacing_factor=1.5, time_scheme='legacy',
                  ghost_pressure_extension='neumann', ghost_velocity_interpolation='bilinear', precision='fp64'):
+        """Keywords of solver/main.py:40-44; boundary defaults to the class's own."""
         import torch
-        if boundary not in ('immersed', 'staircase', 'ghost_cell', 'cut_cell') or transport not in ('centered', 'upwind'):
-            raise ValueError('Choose boundary=immersed/staircase/ghost_cell/cut_cell and transport=centered/upwind')
-        if pressure_solver not in ('direct', 'iterative', 'cg_dct'):
-            raise ValueError("pressure_solver must be direct, iterative or cg_dct")
-        if pressure_solver == 'cg_dct' and boundary != 'cut_cell':
-            raise ValueError("cg_dct is supported only for cut_cell")
-        if time_scheme not in ('legacy', 'ab2_cn'):
-            raise ValueError('time_scheme must be legacy or ab2_cn')
-        if time_scheme == 'ab2_cn' and (boundary not in ('cut_cell', 'ghost_cell') or transport != 'centered'):
-            raise ValueError('ab2_cn requires cut_cell/ghost_cell and centered transport')
-        if ghost_pressure_extension not in ('neumann', 'quadratic') or \
-                ghost_velocity_interpolation not in ('bilinear', 'biquadratic'):
-            raise ValueError('Unknown Ghost pressure extension or velocity interpolation')
-        if ghost_pressure_extension != 'neumann' or ghost_velocity_interpolation != 'bilinear':
-            raise ValueError('Ghost reconstruction options require Ghost AB2/CN')
+        boundary = self._boundary if boundary is None else boundary
+        check_reference_arguments(boundary, transport, pressure_solver, time_scheme, ghost_pressure_extension,
+                                  ghost_velocity_interpolation)
         if boundary != self._boundary or time_scheme != 'legacy':
             raise NotImplementedError(f'{type(self).__name__} implements boundary="{self._boundary}", '
                                       'time_scheme="legacy"')

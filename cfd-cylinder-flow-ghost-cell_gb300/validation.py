@@ -20,7 +20,7 @@ WIDE = dict(nx=800, ny=820, Lx=40.0, Ly=41.0, D=1.0, xc=10.0, yc=20.5, nu=0.01)
 
 def seeded_case(precision, seed=0, amp=1e-2, **case):
     kw = dict(WIDE, **case)
-    s = MAC_CylinderFlow(verbose=False, precision=precision, **kw)
+    s = MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision=precision, **kw)
     q = s.gg.pack(s.u, s.v)
     nu_faces = len(s.gg.ui)
     q[nu_faces:] += amp * np.random.default_rng(seed).standard_normal(q.size - nu_faces)

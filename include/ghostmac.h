@@ -507,6 +507,8 @@ typedef struct gm_cc_step_diag {
   int32_t pressure_solves;
   int32_t status;                  /* 0 ok, else the GM_E* class of the failure */
   int32_t gate;                    /* GM_GATE_* of the failure, 0 if none */
+  double pressure_residual_linf;   /* legacy step: max |b - A phi| of its pressure solve */
+  double pressure_residual_l2;     /* legacy step: ||b - A phi||_2 (AB2/CN step: NaN) */
 } gm_cc_step_diag;
 
 /* Replaces the cut_cell/ab2_cn branch of MAC_CylinderFlow.__init__ (solver/main.py:140-240):
@@ -529,6 +531,19 @@ int gm_cc_get_history(gm_cc* c, int32_t* has_history, double* prev_adv, double* 
 /* n_steps of advance_ab2_cn with the step gates of solver/main.py:416-424; diag (may be NULL)
  * receives one record per step.  A failed gate stops the loop after that step with its class. */
 int gm_cc_step(gm_cc* c, double dt, int32_t n_steps, double start_time, gm_cc_step_diag* diag);
+/* n_steps of the legacy cut-cell loop (MAC_CylinderFlow(boundary='cut_cell',
+ * time_scheme='legacy'), solver/main.py:297-333): the predictor advance_momentum_predictor
+ * (solver/cut_cell_solver.py:1017-1033) with centred transport and AB2 (centered = 1; forward
+ * Euler on the first step) or upwind transport and forward Euler (centered = 0), the predictor
+ * boundary, the projection and p = phi, then the forces.  The state's inlet column enters the
+ * predictor as stored (the previous step's inlet), the current inlet (gm_cc_set_inlet) the
+ * boundary and the corrector.  Gates: the pressure divergence budget and finite forces. */
+int gm_cc_legacy_step(gm_cc* c, double dt, int32_t n_steps, double start_time, int32_t centered,
+                      gm_cc_step_diag* diag);
+/* The legacy predictor's history: the previous acceleration on the face grid (u grid then v
+ * grid, F doubles) and its timestep (prev_au, prev_av, prev_dt of the reference). */
+int gm_cc_set_legacy_history(gm_cc* c, int32_t has_history, const double* prev_accel, double prev_dt);
+int gm_cc_get_legacy_history(gm_cc* c, int32_t* has_history, double* prev_accel, double* prev_dt);
 
 /* Event times (ms) of the last step when the environment variable GHOSTMAC_PHASE_TIMING=1 was
  * set at gm_cc_create: out[0..7] = advection, start-up / AB2 and CN right-hand side, GMRES,
@@ -543,6 +558,7 @@ int gm_cc_phase_timing(const gm_cc* c, double out[8]);
 #define GM_CC_OP_H_MATVEC 5           /* q -> q - dt/2 (diffusion(q) - diffusion(0)), dt = param */
 #define GM_CC_OP_PROJECT 6            /* q -> projected q, y2: phi (p grid); step = param :993-1002 */
 #define GM_CC_OP_PRESSURE_SOLVE 7     /* rhs (p grid) -> phi; solve_pressure(rhs, dt = param, rho) :688-730 */
+#define GM_CC_OP_MOMENTUM_ADVECTION_UPWIND 8 /* op 1 with transport='upwind' */
 int gm_cc_apply(gm_cc* c, int32_t op, double param, const double* x, double* y, double* y2);
 /* extract_true_surface_forces (cut_cell_solver.py:755-765): fx, fy, fx_p, fy_p, fx_v, fy_v */
 int gm_cc_surface_forces(gm_cc* c, const double* u, const double* v, const double* p, double mu, double out[6]);

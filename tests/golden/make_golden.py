@@ -129,7 +129,7 @@ def main():
     ap.add_argument('--reference', type=Path, required=True, help='path of the reference checkout')
     ap.add_argument('--skip-large', action='store_true')
     ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner', 'legacy', 'modal', 'cutcell',
-                                       'staircase', 'legacy_ghost'),
+                                       'staircase', 'legacy_ghost', 'cutcell_legacy'),
                     help='generate one group of fixtures only')
     args = ap.parse_args()
     work = Path(tempfile.mkdtemp(prefix='ghost_golden_'))
@@ -151,6 +151,8 @@ def main():
             run_staircase(work)
         elif args.only == 'legacy_ghost':
             run_legacy_ghost(work)
+        elif args.only == 'cutcell_legacy':
+            run_cutcell_legacy(work)
         else:
             run_all(args)
             run_taylor_green(work)
@@ -161,6 +163,7 @@ def main():
             run_cutcell(work)
             run_staircase(work)
             run_legacy_ghost(work)
+            run_cutcell_legacy(work)
     finally:
         shutil.rmtree(work, ignore_errors=True)
 
@@ -501,6 +504,54 @@ def run_legacy_ghost(work):
         out[f'{tag}_coef'] = np.array(coef)
         out[f'{tag}_time'] = s.time
     save('legacy_ghost_48x24', **out)
+
+
+def run_cutcell_legacy(work):
+    """The reference's legacy cut-cell loop (MAC_CylinderFlow(boundary='cut_cell') with its
+    default time_scheme='legacy': advance_momentum_predictor, compute_rhs, solve_pressure and
+    apply_corrector of solver/cut_cell_solver.py, stepped by solver/main.py:297-333) on the
+    40x20 cut-cell grid and on the 48x30 grid with rho = 1.3: centred transport (AB2 after an
+    Euler first step) and upwind transport (forward Euler) with the transient inlet
+    perturbation, 20 steps each; the initial field, fields at steps 1, 5 and 20, the force
+    coefficients and the pressure record of every step, the predictor history after the last
+    step, and an upwind momentum right-hand side on a seeded field."""
+    from main import MAC_CylinderFlow
+    out = {}
+    for case, kw in CUTCELL_CASES.items():
+        for tag, transport, perturb in (('centered', 'centered', False), ('upwind', 'upwind', True)):
+            s = MAC_CylinderFlow(boundary='cut_cell', transport=transport, pressure_solver='direct', verbose=False,
+                                 **kw)
+            assert s.time_scheme == 'legacy'
+            key = f'{case}_{tag}'
+            out[f'{key}_init_u'], out[f'{key}_init_v'] = s.u.copy(), s.v.copy()
+            if tag == 'upwind':
+                rng = np.random.default_rng(7)
+                fu = rng.standard_normal(s.u.shape)
+                fv = rng.standard_normal(s.v.shape)
+                fu[s.cut_geom.ax == 0] = 0.
+                fv[s.cut_geom.ay == 0] = 0.
+                a_u, a_v, r_u, r_v = s.cc.compute_momentum_rhs(fu, fv, s.nu, s.rho, transport='upwind')
+                out[f'{case}_probe_u'], out[f'{case}_probe_v'] = fu, fv
+                out[f'{case}_upwind_au'], out[f'{case}_upwind_av'] = a_u, a_v
+                out[f'{case}_upwind_ru'], out[f'{case}_upwind_rv'] = r_u, r_v
+            fields, coef, rec = {}, [], []
+            for k in range(20):
+                _, cd, cl = s.solve(n_steps=1, dt=0.002, perturb_transient=perturb, perturb_duration=0.03,
+                                    save_artifacts=False, verbose=False)
+                d = s.last_step_diagnostics
+                coef.append([float(cd[0]), float(cl[0])])
+                rec.append([d['residual_linf'], d['residual_l2'], d['predicted_divergence'], d['max_divergence'],
+                            d['cfl']])
+                if k + 1 in (1, 5, 20):
+                    fields[k + 1] = (s.u.copy(), s.v.copy(), s.p.copy())
+            for k, (u, v, p) in fields.items():
+                out[f'{key}_u{k}'], out[f'{key}_v{k}'], out[f'{key}_p{k}'] = u, v, p
+            out[f'{key}_coef'] = np.array(coef)
+            out[f'{key}_record'] = np.array(rec)
+            out[f'{key}_time'] = s.time
+            out[f'{key}_prev_au'], out[f'{key}_prev_av'] = s.cc.prev_au.copy(), s.cc.prev_av.copy()
+            out[f'{key}_prev_dt'] = s.cc.prev_dt
+    save('cutcell_legacy', **out)
 
 
 def run_modal(work):

@@ -17,7 +17,7 @@ CASES = [
 def _make(pkg, seed):
     out = []
     for i, kw in enumerate(CASES):
-        s = pkg.MAC_CylinderFlow(verbose=False, **kw)
+        s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, **kw)
         rng = np.random.default_rng(seed + i)
         q = s.gg.pack(s.u, s.v)
         q += 1e-3 * rng.standard_normal(q.size)
@@ -55,7 +55,7 @@ def test_batch_matches_cases_stepped_alone():
 
 def test_batch_rejects_duplicates_and_empty():
     pkg = load_package()
-    s = pkg.MAC_CylinderFlow(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., verbose=False)
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., verbose=False)
     with pytest.raises(ValueError):
         pkg.CylinderBatch([s, s])
     with pytest.raises(ValueError):
@@ -81,7 +81,7 @@ def test_grouped_batch_matches_cases_stepped_alone(monkeypatch):
     def make():
         out = []
         for i, kw in enumerate(GROUPED):
-            s = pkg.MAC_CylinderFlow(verbose=False, **kw)
+            s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, **kw)
             q = s.gg.pack(s.u, s.v)
             q += 1e-3 * np.random.default_rng(40 + i).standard_normal(q.size)
             s.u, s.v = s.gg.unpack(q)

@@ -32,7 +32,7 @@ def test_device_control_equals_host_control(pkg, monkeypatch, kw, precision):
             monkeypatch.delenv('GHOSTMAC_GMRES_HOST', raising=False)
         else:
             monkeypatch.setenv('GHOSTMAC_GMRES_HOST', env)
-        s = pkg.MAC_CylinderFlow(verbose=False, pressure_solver='iterative', precision=precision, **kw)
+        s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, pressure_solver='iterative', precision=precision, **kw)
         if b is None:
             b = np.random.default_rng(11).standard_normal(len(s.gg.pi))
         x1 = s.gg.pressure_solve(b)
@@ -43,7 +43,7 @@ def test_device_control_equals_host_control(pkg, monkeypatch, kw, precision):
     for k in (0, 2):
         ref = out['host'][k]
         assert np.max(np.abs(out['device'][k] - ref)) < 1e-12 * max(1.0, np.max(np.abs(ref)))
-    d = pkg.MAC_CylinderFlow(verbose=False, **kw)
+    d = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, **kw)
     xd = d.gg.pressure_solve(b)
     assert np.max(np.abs(out['device'][0] - xd)) < 1e-9 * max(1.0, np.max(np.abs(xd)))
 
@@ -57,7 +57,7 @@ def test_device_control_steps(pkg, monkeypatch):
             monkeypatch.delenv('GHOSTMAC_GMRES_HOST', raising=False)
         else:
             monkeypatch.setenv('GHOSTMAC_GMRES_HOST', env)
-        s = pkg.MAC_CylinderFlow(verbose=False, pressure_solver='iterative', **CASES[0])
+        s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, pressure_solver='iterative', **CASES[0])
         s.solve(n_steps=10, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
         assert s.last_step_diagnostics['max_divergence'] < 1e-10
         res.append((s.u.copy(), s.v.copy(), s.p.copy(), s.last_step_diagnostics['pressure_iterations']))

@@ -57,7 +57,7 @@ def test_learned_preconditioner_on_held_out_solves(record_property):
     learned = pkg.learned
     kw = dict(nx=96, ny=48, Lx=9.6, Ly=4.8, D=1.0, xc=2.4, yc=2.4, nu=0.01, verbose=False,
               pressure_solver='iterative')
-    s = pkg.MAC_CylinderFlow(**kw)
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', **kw)
     rhs, sol = learned.record_pressure_pairs(s, 40, 0.002)
     assert rhs.shape[0] >= 60
     # train on the earlier solves, hold out the last four

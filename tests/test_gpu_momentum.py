@@ -32,7 +32,7 @@ def test_tiled_momentum_equals_per_face(pkg, monkeypatch, kw, precision):
     out = []
     for tiled in ('1', '0'):
         monkeypatch.setenv('GHOSTMAC_MOMENTUM_TILED', tiled)
-        s = pkg.MAC_CylinderFlow(verbose=False, precision=precision, **kw)
+        s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision=precision, **kw)
         q = s.gg.pack(s.u, s.v)
         q += 1e-2 * np.random.default_rng(17).standard_normal(q.size)
         s.u[:], s.v[:] = s.gg.unpack(q)

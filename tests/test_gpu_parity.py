@@ -36,7 +36,7 @@ def pkg():
 
 
 def small(pkg, **kw):
-    return pkg.MAC_CylinderFlow(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., verbose=False, **kw)
+    return pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., verbose=False, **kw)
 
 
 @pytest.fixture(scope='module')
@@ -46,7 +46,7 @@ def G():
 
 def test_rectangle_transforms(pkg):
     G = np.load(GOLDEN / 'rectangle_24x10.npz')
-    s = pkg.MAC_CylinderFlow(nx=24, ny=10, Lx=7.2, Ly=2.5, D=0.4, xc=3.6, yc=1.25, nu=0.02, rho=1.3, verbose=False)
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', nx=24, ny=10, Lx=7.2, Ly=2.5, D=0.4, xc=3.6, yc=1.25, nu=0.02, rho=1.3, verbose=False)
     for kind in ('pressure', 'u', 'v'):
         x = s.gg.rectangle_solve(kind, G[f'{kind}_in'], dt=0.004)
         assert rel(x, G[f'{kind}_out']) < RECT_TOL[kind], kind
@@ -56,7 +56,7 @@ def test_rectangle_transforms(pkg):
 def test_rectangle_transforms_sizes(pkg, n):
     nx, ny, D = n
     h = 0.05
-    s = pkg.MAC_CylinderFlow(nx=nx, ny=ny, Lx=nx * h, Ly=ny * h, D=D, xc=nx * h / 4, yc=ny * h / 2, nu=0.01,
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', nx=nx, ny=ny, Lx=nx * h, Ly=ny * h, D=D, xc=nx * h / 4, yc=ny * h / 2, nu=0.01,
                              verbose=False)
     rng = np.random.default_rng(nx)
     for kind in ('pressure', 'u', 'v'):
@@ -144,7 +144,7 @@ def test_multi_step_call_equals_single_steps(pkg):
                                       ('qp', dict(ghost_pressure_extension='quadratic'))])
 def test_option_paths(pkg, tag, opts):
     G = np.load(GOLDEN / f'opt40x30_{tag}.npz')
-    s = pkg.MAC_CylinderFlow(nx=40, ny=30, Lx=4., Ly=3., xc=1.5, yc=1.5, verbose=False, **opts)
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', nx=40, ny=30, Lx=4., Ly=3., xc=1.5, yc=1.5, verbose=False, **opts)
     s.solve(n_steps=3, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
     assert rel(s.u, G['u']) < 1e-10 and rel(s.p, G['p']) < 1e-9
     assert abs(s.last_step_diagnostics['cd'] - G['scalars'][0]) < 1e-8 * abs(G['scalars'][0])
@@ -154,7 +154,7 @@ def test_option_paths(pkg, tag, opts):
 def test_traction_known_answers(pkg):
     G = np.load(GOLDEN / 'traction.npz')
     for k, (nx, ny) in enumerate(((40, 30), (80, 60), (120, 90))):
-        s = pkg.MAC_CylinderFlow(nx=nx, ny=ny, Lx=4., Ly=3., xc=1.5, yc=1.5, verbose=False)
+        s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', nx=nx, ny=ny, Lx=4., Ly=3., xc=1.5, yc=1.5, verbose=False)
         xu, yu = np.arange(nx + 1) * s.dx, (np.arange(ny) + .5) * s.dy
         xv, yv = (np.arange(nx) + .5) * s.dx, np.arange(ny + 1) * s.dy
         xx, yy = np.meshgrid(xu, yu)
@@ -171,7 +171,7 @@ def test_traction_known_answers(pkg):
 
 def test_config1_two_steps(pkg):
     G = np.load(GOLDEN / 'config1_400x200.npz')
-    s = pkg.MAC_CylinderFlow(nx=400, ny=200, Lx=20., Ly=10., D=1., xc=5., yc=5., nu=1 / 40, verbose=False)
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', nx=400, ny=200, Lx=20., Ly=10., D=1., xc=5., yc=5., nu=1 / 40, verbose=False)
     q = s.gg.pack(s.u, s.v)
     q += 1e-3 * np.random.default_rng(0).standard_normal(q.size)
     s.u[:], s.v[:] = s.gg.unpack(q)
@@ -188,7 +188,7 @@ def test_config1_two_steps(pkg):
 def test_oracle_parity_with_noise_20_steps(pkg):
     """Same seeded inputs through the oracle and the GPU for 20 steps (tolerance 1e-10)."""
     kw = dict(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., nu=0.02)
-    s = pkg.MAC_CylinderFlow(verbose=False, **kw)
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, **kw)
     c = go.CylinderCase(**kw)
     q = c.ops.pack(c.u, c.v)
     q += 1e-2 * np.random.default_rng(5).standard_normal(q.size)
@@ -239,7 +239,7 @@ def test_fp32_mode_matches_fp64_oracle(pkg):
     < 1e-10; after 20 noisy steps velocity within 1e-7, pressure within 1e-5 and the drag
     coefficient within 1e-6 (relative) of the FP64 oracle."""
     kw = dict(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., nu=0.02)
-    s = pkg.MAC_CylinderFlow(verbose=False, precision='fp32', **kw)
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision='fp32', **kw)
     c = go.CylinderCase(**kw)
     q = c.ops.pack(c.u, c.v)
     q += 1e-2 * np.random.default_rng(5).standard_normal(q.size)
@@ -258,7 +258,7 @@ def test_fp32_mode_matches_fp64_oracle(pkg):
 
 def test_fp32_mode_config1(pkg):
     G = np.load(GOLDEN / 'config1_400x200.npz')
-    s = pkg.MAC_CylinderFlow(nx=400, ny=200, Lx=20., Ly=10., D=1., xc=5., yc=5., nu=1 / 40, verbose=False,
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', nx=400, ny=200, Lx=20., Ly=10., D=1., xc=5., yc=5., nu=1 / 40, verbose=False,
                              precision='fp32')
     q = s.gg.pack(s.u, s.v)
     q += 1e-3 * np.random.default_rng(0).standard_normal(q.size)
@@ -277,7 +277,7 @@ def test_iterative_pressure_path_golden(pkg):
     reference's own three steps (tests/golden/opt40x30_iter.npz).  GMRES stops at
     rtol = 1e-12 plus refinement, so the fields agree to the solver tolerance."""
     G = np.load(GOLDEN / 'opt40x30_iter.npz')
-    s = pkg.MAC_CylinderFlow(nx=40, ny=30, Lx=4., Ly=3., xc=1.5, yc=1.5, verbose=False, pressure_solver='iterative')
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', nx=40, ny=30, Lx=4., Ly=3., xc=1.5, yc=1.5, verbose=False, pressure_solver='iterative')
     s.solve(n_steps=3, dt=.001, perturb_transient=False, save_artifacts=False, verbose=False)
     assert rel(s.u, G['u']) < 1e-9 and rel(s.v, G['v']) < 1e-9 and rel(s.p, G['p']) < 1e-8
     assert abs(s.last_step_diagnostics['cd'] - G['scalars'][0]) < 1e-8 * abs(G['scalars'][0])
@@ -290,15 +290,15 @@ def test_iterative_matches_direct_solve(pkg):
     """GMRES and the FFT + boundary Schur direct solve agree (the reference asserts 1e-9 /
     1e-8 between its two backends)."""
     kw = dict(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., verbose=False)
-    sd = pkg.MAC_CylinderFlow(**kw)
-    si = pkg.MAC_CylinderFlow(pressure_solver='iterative', **kw)
+    sd = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', **kw)
+    si = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', pressure_solver='iterative', **kw)
     rng = np.random.default_rng(3)
     b = rng.standard_normal(len(sd.gg.pi))
     xd = sd.gg.pressure_solve(b)
     xi = si.gg.pressure_solve(b)
     assert np.max(np.abs(xd - xi)) < 1e-9 * max(1.0, np.max(np.abs(xd)))
     for prec in ('fp32',):
-        sf = pkg.MAC_CylinderFlow(pressure_solver='iterative', precision=prec, **kw)
+        sf = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', pressure_solver='iterative', precision=prec, **kw)
         xf = sf.gg.pressure_solve(b)
         assert np.max(np.abs(xf - xd)) < 1e-8 * max(1.0, np.max(np.abs(xd)))
 
@@ -321,7 +321,7 @@ def test_fp32_helmholtz_jacobi_and_fft_inverse(pkg, monkeypatch):
             monkeypatch.delenv('GHOSTMAC_HELM_JACOBI', raising=False)
         else:
             monkeypatch.setenv('GHOSTMAC_HELM_JACOBI', env)
-        s = pkg.MAC_CylinderFlow(verbose=False, precision='fp32', **kw)
+        s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision='fp32', **kw)
         s.u[:], s.v[:] = u0, v0
         s.solve(n_steps=20, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
         info = s.helmholtz_solver_info()
@@ -342,7 +342,7 @@ def test_fp32_helmholtz_jacobi_tiled_equals_launches(pkg, monkeypatch, kw):
     out = []
     for tiled in ('1', '0'):
         monkeypatch.setenv('GHOSTMAC_HELM_JACOBI_TILED', tiled)
-        s = pkg.MAC_CylinderFlow(verbose=False, precision='fp32', **kw)
+        s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision='fp32', **kw)
         q = s.gg.pack(s.u, s.v)
         q += 1e-2 * np.random.default_rng(11).standard_normal(q.size)
         s.u[:], s.v[:] = s.gg.unpack(q)

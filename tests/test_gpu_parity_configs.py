@@ -63,7 +63,7 @@ def seeded_pair(pkg, kw, noise, amp, seed, precision='fp64', pressure_solver='di
     else:
         q[nu:] += amp * rng.standard_normal(q.size - nu)
     c.u, c.v = c.ops.unpack(q)
-    s = pkg.MAC_CylinderFlow(verbose=False, precision=precision, pressure_solver=pressure_solver, **kw)
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision=precision, pressure_solver=pressure_solver, **kw)
     s.u[:], s.v[:] = c.u, c.v
     return c, s
 
@@ -109,7 +109,7 @@ def wide_oracle():
 @pytest.mark.parametrize('precision', ['fp64', 'fp32'])
 def test_wide_800x820_five_steps(pkg, wide_oracle, precision):
     u0, v0, c = wide_oracle
-    s = pkg.MAC_CylinderFlow(verbose=False, precision=precision, **WIDE)
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision=precision, **WIDE)
     s.u[:], s.v[:] = u0, v0
     for _ in range(5):
         s.solve(n_steps=1, dt=0.002, perturb_transient=False, save_artifacts=False, verbose=False)

@@ -57,7 +57,7 @@ def test_pressure_solve_tensor_core_rows(pkg, monkeypatch, kw):
     out, b = {}, None
     for tag, prec, env in (('gemm', 'fp32', '1'), ('fft', 'fp32', '0'), ('fp64', 'fp64', '1')):
         monkeypatch.setenv('GHOSTMAC_ROW_GEMM', env)
-        s = pkg.MAC_CylinderFlow(verbose=False, precision=prec, **kw)
+        s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision=prec, **kw)
         if b is None:
             b = np.random.default_rng(7).standard_normal(len(s.gg.pi))
         n = row_gemm_launches(pkg, lambda: out.__setitem__(tag, s.gg.pressure_solve(b)))
@@ -76,7 +76,7 @@ def test_fp32_steps_tensor_core_rows_match_oracle(pkg, monkeypatch):
     row passes ran as tensor-core GEMMs in every step."""
     monkeypatch.setenv('GHOSTMAC_ROW_GEMM', '1')
     kw = CASES[0]
-    s = pkg.MAC_CylinderFlow(verbose=False, precision='fp32', **kw)
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', verbose=False, precision='fp32', **kw)
     c = go.CylinderCase(**kw)
     q = c.ops.pack(c.u, c.v)
     q += 1e-2 * np.random.default_rng(5).standard_normal(q.size)

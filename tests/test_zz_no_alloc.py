@@ -30,7 +30,7 @@ def test_noalloc_divergence_stats_matches_allocating_entry_point():
     torch = pytest.importorskip('torch')
     pkg = load_package()
     L = pkg._lib
-    s = pkg.MAC_CylinderFlow(nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., nu=0.02, verbose=False)
+    s = pkg.MAC_CylinderFlow(boundary='ghost_cell', time_scheme='ab2_cn', nx=88, ny=16, Lx=22., Ly=4.1, xc=2., yc=2., nu=0.02, verbose=False)
     mask = torch.from_numpy(s.mask.astype(np.uint8)).cuda()
     rng = np.random.default_rng(11)
     for call in range(2):  # two calls in a row: the shared scratch keeps the previous call's contents
