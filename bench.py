@@ -22,8 +22,8 @@ port of the reference algorithm on the host cores for the same workload.
 Under torchrun each rank runs an independent replica (the case does not shard).
 
 Other workloads (--workload) time one path alone on one GPU: the 64-case sweep, Taylor-Green,
-the GMRES pressure path, the cut-cell AB2/CN path (cutcell_800x820_re100) and the two legacy
-loops (staircase_800x820_re100, legacy_ghost_800x820_re100).
+the GMRES pressure path, the cut-cell AB2/CN path (cutcell_800x820_re100) and the three legacy
+loops (staircase_800x820_re100, legacy_ghost_800x820_re100, cutcell_legacy_800x820_re100).
 """
 from __future__ import annotations
 
@@ -81,13 +81,16 @@ CUTCELL_WORKLOADS = {
                                   noise='v', amp=1e-2, seed=0),
 }
 # the legacy loops (time_scheme='legacy', centred transport with the loop's AB2 step) on the same
-# grid and Re: the staircase branch and the ghost-cell branch (image-point ghost velocities),
-# from the loop's own initial field (uniform inflow, masked faces zero)
+# grid and Re: the staircase branch, the ghost-cell branch (image-point ghost velocities) and the
+# cut-cell branch (aperture-weighted predictor), from the loop's own initial field (uniform
+# inflow, masked faces zero)
 LEGACY_WORKLOADS = {
     'staircase_800x820_re100': dict(nx=800, ny=820, Lx=40.0, Ly=41.0, D=1.0, xc=10.0, yc=20.5, nu=0.01, dt=0.002,
                                     boundary='staircase'),
     'legacy_ghost_800x820_re100': dict(nx=800, ny=820, Lx=40.0, Ly=41.0, D=1.0, xc=10.0, yc=20.5, nu=0.01,
                                        dt=0.002, boundary='ghost_cell'),
+    'cutcell_legacy_800x820_re100': dict(nx=800, ny=820, Lx=40.0, Ly=41.0, D=1.0, xc=10.0, yc=20.5, nu=0.01,
+                                         dt=0.002, boundary='cut_cell'),
 }
 DEFAULT_WORKLOAD = 'wide_800x820_re100'
 # FP64 instructions (dadd + dmul + dfma, thread level) per cell update of the plain FP64 step on
@@ -298,7 +301,7 @@ def run_reference(args, w, rank):
         return
     workers = os.cpu_count() or 1
     if args.workload in CUTCELL_WORKLOADS or args.workload in LEGACY_WORKLOADS:
-        path = 'cut_cell' if args.workload in CUTCELL_WORKLOADS else w['boundary']
+        path = 'cut_cell' if args.workload in CUTCELL_WORKLOADS else args.workload.replace('_800x820_re100', '')
         print(json.dumps(dict(impl='reference', workload=args.workload, unavailable=(
             f'the reference\'s {path} loop runs from its own source tree, which this machine does not hold; '
             f'oracle/time_reference_stub.py --path {path} times it where the source is'))), flush=True)
@@ -1028,7 +1031,8 @@ def run_ours_legacy(args, w, rank, world):
                                 boundary=w['boundary'], time_scheme='legacy', transport='centered'),
                     legacy=dict(setup_s=setup_s, max_divergence=max_div, cd=s.last_step_diagnostics['cd'],
                                 cl=s.last_step_diagnostics['cl'],
-                                pressure_residual_linf=s.last_step_diagnostics['pressure_residual_linf'], **extra))
+                                pressure_residual_linf=s.last_step_diagnostics.get(
+                                    'pressure_residual_linf', s.last_step_diagnostics.get('residual_linf')), **extra))
         print(json.dumps(line), flush=True)
 
 

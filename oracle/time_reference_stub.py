@@ -17,11 +17,12 @@ Helmholtz-building step is excluded.  Run here, not on the GPU machine (the referenc
 
     python oracle/time_reference_stub.py --reference <path of the reference checkout> [--steps 2]
 
-With ``--path staircase`` or ``--path legacy_ghost`` it times the reference's legacy loop
-(MAC_CylinderFlow(time_scheme='legacy', transport='centered') with boundary='staircase' or
-'ghost_cell': mac_engine compiled with OpenMP, the sparse LU factored in setup, the ghost-cell
-branch's Python image-point loops) on bench.py's staircase_800x820_re100 or
-legacy_ghost_800x820_re100 workload, after setup and three steps, with all the host's threads.
+With ``--path staircase``, ``--path legacy_ghost`` or ``--path cutcell_legacy`` it times the
+reference's legacy loop (MAC_CylinderFlow(time_scheme='legacy', transport='centered') with
+boundary='staircase', 'ghost_cell' or 'cut_cell': mac_engine compiled with OpenMP, the sparse LU
+factored in setup, the ghost-cell branch's Python image-point loops, the cut-cell branch's numpy
+predictor) on bench.py's matching workload, after setup and three steps, with all the host's
+threads.
 
 With ``--path cut_cell`` it times the reference's cut-cell AB2/CN step instead
 (MAC_CylinderFlow(boundary='cut_cell'), CutCellBoundary.advance_ab2_cn: numpy and scipy, no
@@ -122,13 +123,14 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--reference', type=Path, required=True, help='path of the reference checkout')
     ap.add_argument('--steps', type=int, default=2)
-    ap.add_argument('--path', choices=('ghost_cell', 'cut_cell', 'staircase', 'legacy_ghost'), default='ghost_cell')
+    ap.add_argument('--path', choices=('ghost_cell', 'cut_cell', 'staircase', 'legacy_ghost', 'cutcell_legacy'),
+                    default='ghost_cell')
     args = ap.parse_args()
     sys.path.insert(0, str(ROOT))
     sys.path.insert(0, str(ROOT / 'tests' / 'golden'))
     import bench
     import make_golden
-    if args.path in ('staircase', 'legacy_ghost'):
+    if args.path in ('staircase', 'legacy_ghost', 'cutcell_legacy'):
         name = f'{args.path}_800x820_re100'
         w = bench.LEGACY_WORKLOADS[name]
         work = Path(tempfile.mkdtemp(prefix='ghost_ref_time_'))
