@@ -109,9 +109,12 @@ DRAM_TRAFFIC = {
     ('wide_800x820_re100', 'fp64', 1): 3712.0,
     # profiles/fp32_mode_wide_800x820.md: the two row passes of the first sweep, (256 + 1024) / 2
     ('wide_800x820_re100', 'fp32', 1): 640.0,
+    # profiles/k_residual_fp32_wide_800x820.md: the u, u and v Helmholtz residuals,
+    # (7168 + 6656 + 12032) / 3
+    ('wide_800x820_re100', 'fp32', 4): 8618.7,
 }
 KERNEL_CLASSES = {1: 'row transforms (k_xpass)', 2: 'column solves (k_ysolve, k_yband)',
-                  3: 'momentum rhs (k_momentum, k_shadow)', 4: 'operator residual (k_residual, k_pressure_bound)',
+                  3: 'momentum rhs (k_momentum, k_shadow)', 4: 'operator residual (k_residual)',
                   5: 'boundary term (k_band_first, k_band_gemv, k_band_fwd_solve)', 6: 'projection (k_divergence, k_project_update, k_set_inlet)',
                   7: 'defect / pressure output (k_defect, k_pressure_out)', 8: 'ghost rows (k_ghost)',
                   9: 'forces / maxima (k_forces, k_maxabs)', 10: 'gates and loop control',

@@ -1182,7 +1182,6 @@ void schur_solve_graph(gm_handle* h, int lane, RectDev& rd, int kind, double hc,
   launch_refine_decide(h->ctl.p, slot, h->nchk, cond, body_st);
   h->body_nodes_slot[slot] = kernel_launch_count() - c0;
   CK(cudaStreamEndCapture(body_st, &body));
-  if (f32 && kind == 0) launch_pressure_bound(h->cd, h->rcoef[0], b, x, sc, h->nchk, g0, st);
 }
 
 // Flexible GMRES(50) for A x = b on the pressure grid, right-preconditioned by the separable
@@ -1531,7 +1530,6 @@ void schur_solve(gm_handle* h, int lane, RectDev& rd, int kind, double hc, const
       if (err || !(bits2d(hs.rmax[sweep]) > tg)) break;
     }
   }
-  if (f32 && kind == 0) launch_pressure_bound(h->cd, h->rcoef[0], b, x, sc, h->nchk, gate_of(h), st);
 }
 
 // project(q, dt) (solver/optimized_ghost_cell.py:218-229); q is a face grid with active values.
@@ -3061,14 +3059,6 @@ long long solve_group(gm_batch* b, BatchGroup& G, int lane, const std::vector<So
   launch_refine_decide_multi(ctls, n, slot, nchk, cond, body_st);
   const long long body_nodes = kernel_launch_count() - c0;
   CK(cudaStreamEndCapture(body_st, &bodyg));
-  if (f32 && kind == 0) {
-    auto p = std::make_unique<ArgPack<BoundArgs>>();
-    for (int c = 0; c < n; ++c) {
-      gm_handle* h = b->cases[G.idx[c]];
-      p->a[c] = bound_args(h->cd, h->rcoef[0], calls[c].b, calls[c].x, &h->ctl.p->solve[slot], nchk, gate_of(h));
-    }
-    launch_pressure_bound_multi(*p, n, st);
-  }
   return body_nodes;
 }
 

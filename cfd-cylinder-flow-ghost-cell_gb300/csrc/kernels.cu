@@ -1418,11 +1418,11 @@ void launch_gradient(const CaseDev& c, const double* P, double* out, const Gate&
 // Residual res = b - A x of the pressure operator A (KIND 0, p grid) or the Helmholtz
 // operators I - c L (KIND 1 u faces, KIND 2 v faces), with max |res| and sum res^2 per check.
 // GB300 issues FP64 at 1/64 of the FP32 rate, so the regular rows use coefficients formed on
-// the host (ResidualCoef): two adds and three multiply-adds per point.  RES_F32: the residual
+// the host (ResidualCoef): one add and four multiply-adds per point.  RES_F32: the residual
 // is stored in FP32 (the input of the FP32 inverse).  Its max norm, which drives the
 // refinement, is still taken from the FP64 residual; the diagnostic sums of res^2 and b^2 are
-// FP32, so the only FP64 work left is the stencil.  The roundoff bound is left to
-// k_pressure_bound after the refinement loop.
+// FP32, so the only FP64 work left is the stencil.  The pressure gate's roundoff bound is formed
+// in FP32 beside it.
 // coefficient selection by value (indexing the parameter struct would copy it to local memory)
 __device__ __forceinline__ double coef_cc(const ResidualCoef& rc, int ic, int jc) {
   const double c0 = jc ? rc.cc[0][1] : rc.cc[0][0];
@@ -1450,6 +1450,10 @@ __device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCo
   double rs = 0.0, bs = 0.0;
   float rs32 = 0.0f;  // RES_F32: sum of the stored FP32 residuals squared (diagnostics only)
   float bs32 = 0.0f;  // RES_F32: sum of the right-hand side squared in FP32 (diagnostics only)
+  // RES_F32, pressure: the roundoff bound (2 nnz + 2) eps (|A| |x| + |b|) in FP32 and integer
+  // arithmetic, beside the FP64 stencil (the FP64 pipe is this kernel's bound)
+  constexpr bool BOUND32 = KIND == 0 && RES_F32;
+  float bd32 = 0.0f;
   for (int64_t t = (int64_t)bid * blockDim.x + threadIdx.x; t < npts; t += (int64_t)nblk * blockDim.x) {
     const uint8_t k = cls[t];
     const int64_t f = base + t;
@@ -1458,17 +1462,20 @@ __device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCo
       continue;
     }
     const double xv = x[f], bv = b[f];
-    double ax, aabs = 0.0;
+    double r, aabs = 0.0;
+    float aabs32 = 0.0f;
     int nnz = 0;
     const int row = (k & CLS_IRREG) ? c.irr_index[KIND][t] : -1;
     if (row >= 0) {
       const int64_t* cp = c.irr_ptr[KIND];
-      ax = 0.0;
+      double ax = 0.0;
       const int64_t e0 = cp[row], e1 = cp[row + 1];
       csr_row<4>(c.irr_col[KIND], c.irr_val[KIND], e0, e1, x, base, [&](double a, double xv2) {
         ax += a * xv2;
         if (KIND == 0 && !RES_F32) aabs += absd(a) * absd(xv2);
+        if (BOUND32) aabs32 += fabsf(f64_to_f32i(a)) * fabsf(f64_to_f32i(xv2));
       });
+      r = bv - ax;
       nnz = (int)(e1 - e0);
     } else {
       const int j = (int)((unsigned)t / (unsigned)w), i = (int)((unsigned)t - (unsigned)j * w);
@@ -1497,17 +1504,26 @@ __device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCo
         ic = i == 0 ? 0 : (i == nx - 1 ? 2 : 1);
         jc = 1;
       }
-      // A x = cc x + cw xw + ce xe + cy (xs + xn); Helmholtz rows carry the factors of I - c L
-      // (one add, one multiply and three fused multiply-adds, written out so that nothing else
-      // reaches the FP64 pipe)
+      // r = b - (cc x + cw xw + ce xe + cy (xs + xn)); Helmholtz rows carry the factors of
+      // I - c L.  One add and four fused multiply-adds that subtract from b, written out so
+      // that nothing else reaches the FP64 pipe; each rounding stays inside the
+      // (2 nnz + 2) eps (|A| |x| + |b|) bound of the pressure gate.
       const double ccv = coef_cc(rc, ic, jc), cwv = coef_cw(rc, ic);
-      ax = fma(rc.cy, xs + xn, fma(rc.ce, xe, fma(cwv, xw, ccv * xv)));
+      r = fma(-rc.cy, xs + xn, fma(-rc.ce, xe, fma(-cwv, xw, fma(-ccv, xv, bv))));
       if (KIND == 0 && !RES_F32) {
         aabs = absd(ccv) * absd(xv) + rc.ce * (absd(xw) + absd(xe)) + rc.cy * (absd(xs) + absd(xn));
         nnz = c.a_nnz[t];
       }
+      if (BOUND32) {
+        const float c0 = jc ? rc.fcc[0][1] : rc.fcc[0][0], c1 = jc ? rc.fcc[1][1] : rc.fcc[1][0];
+        const float c2 = jc ? rc.fcc[2][1] : rc.fcc[2][0];
+        const float fcc = ic == 0 ? c0 : (ic == 1 ? c1 : c2);
+        aabs32 = fabsf(fcc) * fabsf(f64_to_f32i(xv)) +
+                 rc.fce * (fabsf(f64_to_f32i(xw)) + fabsf(f64_to_f32i(xe))) +
+                 rc.fcy * (fabsf(f64_to_f32i(xs)) + fabsf(f64_to_f32i(xn)));
+        nnz = c.a_nnz[t];
+      }
     }
-    const double r = bv - ax;
     rm = umax64(rm, absbits(r));
     if constexpr (RES_F32) {
       const float r32 = f64_to_f32i(r);
@@ -1518,6 +1534,8 @@ __device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCo
       rs += r * r;
     }
     if (KIND == 0 && !RES_F32) bd = umax64(bd, dbits((2.0 * nnz + 2.0) * EPS64 * (aabs + absd(bv))));
+    if (BOUND32)
+      bd32 = fmaxf(bd32, (2.0f * (float)nnz + 2.0f) * 2.220446049250313e-16f * (aabs32 + fabsf(f64_to_f32i(bv))));
     if (first) {
       bm = umax64(bm, absbits(bv));
       if constexpr (RES_F32) {
@@ -1533,6 +1551,9 @@ __device__ __forceinline__ void residual_body(const CaseDev& c, const ResidualCo
   if constexpr (RES_F32) block_commit_sum_f32(rs32, &sc->rsq[check]);
   else block_commit_sum(rs, &sc->rsq[check]);
   if (KIND == 0 && !RES_F32) block_commit_max(bd, &sc->bound[check]);
+  // the FP32 bound times 1 + 2^-20 (above its own rounding), as an FP64 value; non-negative
+  // doubles order like their bits
+  if (BOUND32) block_commit_max(dbits(f32_to_f64i(bd32 * 1.00000095367431640625f)), &sc->bound[check]);
   if (first) {
     block_commit_max(bm, &sc->bmax);
     if constexpr (RES_F32) block_commit_sum_f32(bs32, &sc->bsq);
@@ -1879,64 +1900,6 @@ template void launch_helm_jacobi_tiled<double>(const CaseDev&, const ResidualCoe
 template void launch_helm_jacobi_tiled<float>(const CaseDev&, const ResidualCoef&, const HelmJacobi&, int,
                                               const float*, double*, bool, size_t, const Gate&, cudaStream_t);
 
-// Roundoff bound max_i (2 nnz_i + 2) eps (|A||x| + |b|)_i of the pressure solution after its
-// refinement loop (solver/pressure_schur.py:48-56), stored at the last check; used by the
-// FP32 mode, whose residual sweeps skip it.
-// FP32 arithmetic: the bound is a threshold of the pressure gate (max(target, bound)), so its
-// last bits do not matter; it is formed from FP32 copies of x, b and the coefficients
-// (conversions on the integer pipe) and rounded up by 2^-20 relative before it is committed,
-// which keeps it above the FP64 value of the same expression.
-__device__ __forceinline__ void pressure_bound_body(const CaseDev& c, const ResidualCoef& rc,
-                                                    const double* __restrict__ b, const double* __restrict__ x,
-                                                    SolveCtl* sc, int nchk, int bid, int nblk) {
-  const int check = last_check(sc, nchk);
-  const int nx = c.nx, ny = c.ny;
-  constexpr float EPS = 2.220446049250313e-16f;
-  float bd = 0.0f;
-  auto ax = [&](int64_t t) { return fabsf(f64_to_f32i(x[t])); };
-  for (int64_t t = (int64_t)bid * blockDim.x + threadIdx.x; t < c.psize; t += (int64_t)nblk * blockDim.x) {
-    const uint8_t k = c.cls_p[t];
-    if (!(k & CLS_ACTIVE)) continue;
-    const float bv = fabsf(f64_to_f32i(b[t]));
-    float aabs = 0.0f;
-    int nnz;
-    const int row = (k & CLS_IRREG) ? c.irr_index[0][t] : -1;
-    if (row >= 0) {
-      const int64_t* cp = c.irr_ptr[0];
-      const int64_t e0 = cp[row], e1 = cp[row + 1];
-      csr_row<4>(c.irr_col[0], c.irr_val[0], e0, e1, x, 0, [&](double a, double xv2) {
-        aabs += fabsf(f64_to_f32i(a)) * fabsf(f64_to_f32i(xv2));
-      });
-      nnz = (int)(e1 - e0);
-    } else {
-      const int j = (int)((unsigned)t / (unsigned)nx), i = (int)((unsigned)t - (unsigned)j * nx);
-      const float xw = i > 0 ? ax(t - 1) : 0.0f, xe = i < nx - 1 ? ax(t + 1) : 0.0f;
-      const float xs = j > 0 ? ax(t - nx) : 0.0f, xn = j < ny - 1 ? ax(t + nx) : 0.0f;
-      const int ic = i == 0 ? 0 : (i == nx - 1 ? 2 : 1), jc = (j == 0 || j == ny - 1) ? 0 : 1;
-      const float c0 = jc ? rc.fcc[0][1] : rc.fcc[0][0], c1 = jc ? rc.fcc[1][1] : rc.fcc[1][0];
-      const float c2 = jc ? rc.fcc[2][1] : rc.fcc[2][0];
-      const float ccv = ic == 0 ? c0 : (ic == 1 ? c1 : c2);
-      aabs = fabsf(ccv) * ax(t) + rc.fce * (xw + xe) + rc.fcy * (xs + xn);
-      nnz = c.a_nnz[t];
-    }
-    bd = fmaxf(bd, (2.0f * (float)nnz + 2.0f) * EPS * (aabs + bv));
-  }
-  // non-negative floats order like their bits; the block maximum goes out as an FP64 value
-  const double up = f32_to_f64i(bd) * (1.0 + 0x1p-20);
-  block_commit_max(dbits(up), &sc->bound[check]);
-}
-__global__ void k_pressure_bound(CaseDev c, ResidualCoef rc, const double* __restrict__ b,
-                                 const double* __restrict__ x, SolveCtl* sc, int nchk, Gate gate) {
-  if (!gate_open(gate)) return;
-  pressure_bound_body(c, rc, b, x, sc, nchk, blockIdx.x, gridDim.x);
-}
-void launch_pressure_bound(const CaseDev& c, const ResidualCoef& rc, const double* b, const double* x, SolveCtl* sc,
-                           int nchk, const Gate& gate, cudaStream_t st) {
-  note_launch();
-  kt_mark(4, st);
-  k_pressure_bound<<<reduce_blocks(c.psize), TPB, 0, st>>>(c, rc, b, x, sc, nchk, gate);
-  kt_mark(4, st);
-}
 
 // ---------------------------------------------------------------------------
 // flexible GMRES on the pressure grid (solver/pressure_schur.py:20-57, iterative branch):
@@ -2753,12 +2716,6 @@ __global__ void k_residual_multi(const __grid_constant__ ArgPack<ResidualArgs> p
   if (!gate_open(a.gate)) return;
   residual_body<KIND, RES_F32>(a.c, a.rc, a.b, a.x, a.res, a.sc, a.check, a.first, blockIdx.x, a.nblk);
 }
-__global__ void k_pressure_bound_multi(const __grid_constant__ ArgPack<BoundArgs> p) {
-  const BoundArgs& a = p.a[blockIdx.y];
-  if ((int)blockIdx.x >= a.nblk) return;
-  if (!gate_open(a.gate)) return;
-  pressure_bound_body(a.c, a.rc, a.b, a.x, a.sc, a.nchk, blockIdx.x, a.nblk);
-}
 __global__ void k_refine_decide_multi(const __grid_constant__ ArgPack<StepCtl*> ctls, int n, int slot, int nchk,
                                       cudaGraphConditionalHandle cond) {
   __shared__ int any;
@@ -2841,21 +2798,8 @@ ResidualArgs residual_args(const CaseDev& c, const ResidualCoef& rc, int kind, c
   a.nblk = (int)residual_blocks(kind == 0 ? c.psize : (kind == 1 ? c.usize : c.vsize), res_f32);
   return a;
 }
-BoundArgs bound_args(const CaseDev& c, const ResidualCoef& rc, const double* b, const double* x, SolveCtl* sc,
-                     int nchk, const Gate& gate) {
-  BoundArgs a{};
-  a.c = c;
-  a.rc = rc;
-  a.b = b;
-  a.x = x;
-  a.sc = sc;
-  a.nchk = nchk;
-  a.gate = gate;
-  a.nblk = (int)reduce_blocks(c.psize);
-  return a;
-}
 
-static_assert(sizeof(ArgPack<ResidualArgs>) <= 32000 && sizeof(ArgPack<BoundArgs>) <= 32000 &&
+static_assert(sizeof(ArgPack<ResidualArgs>) <= 32000 &&
                   sizeof(ArgPack<YsolveArgs<double>>) <= 32000 &&
                   sizeof(ArgPack<XpassArgs<double, double, double>>) <= 32000,
               "case-indexed argument packs must fit the kernel parameter space");
@@ -2928,11 +2872,6 @@ void launch_residual_multi(const ArgPack<ResidualArgs>& p, int n, int kind, bool
     else if (kind == 1) k_residual_multi<1, false><<<g, TPB, 0, st>>>(p);
     else k_residual_multi<2, false><<<g, TPB, 0, st>>>(p);
   }
-}
-void launch_pressure_bound_multi(const ArgPack<BoundArgs>& p, int n, cudaStream_t st) {
-  if (n <= 0) return;
-  note_launch();
-  k_pressure_bound_multi<<<dim3(max_blocks(p, n), (unsigned)n), TPB, 0, st>>>(p);
 }
 void launch_refine_decide_multi(const ArgPack<StepCtl*>& ctls, int n, int slot, int nchk,
                                 cudaGraphConditionalHandle cond, cudaStream_t st) {

@@ -410,12 +410,10 @@ struct ResidualCoef {
   double cc[3][2];
   double cw[3];
   double ce, cy;
-  float fcc[3][2], fcw[3], fce, fcy;  // FP32 copies (the FP32 mode's roundoff bound)
+  float fcc[3][2], fcw[3], fce, fcy;  // FP32 copies (the FP32 mode's roundoff bound, in the residual)
 };
 void launch_residual(const CaseDev& c, const ResidualCoef& rc, int kind, const double* b, const double* x, void* res,
                      bool res_f32, SolveCtl* sc, int check, bool first_check, const Gate& gate, cudaStream_t st);
-void launch_pressure_bound(const CaseDev& c, const ResidualCoef& rc, const double* b, const double* x, SolveCtl* sc,
-                           int nchk, const Gate& gate, cudaStream_t st);
 // FP32 Jacobi iterations of the Helmholtz systems (index 0: u, 1: v): 1 / diagonal of the
 // regular rows per boundary class (as ResidualCoef::cc), and of every irregular row, with the
 // irregular rows' entries in FP32 and their diagonal entry zeroed.
@@ -642,15 +640,6 @@ struct ResidualArgs {
   Gate gate;
   int nblk;
 };
-struct BoundArgs {
-  CaseDev c;
-  ResidualCoef rc;
-  const double* b; const double* x;
-  SolveCtl* sc;
-  int nchk;
-  Gate gate;
-  int nblk;
-};
 
 // argument builders: the same conventions as the single-case launchers above
 template <typename T, typename TI, typename TO>
@@ -661,8 +650,6 @@ template <typename T>
 YsolveArgs<T> ysolve_args(const TransformTables& tt, int cols, int rows, T* S, const Gate& gate);
 ResidualArgs residual_args(const CaseDev& c, const ResidualCoef& rc, int kind, const double* b, const double* x,
                            void* res, bool res_f32, SolveCtl* sc, int check, bool first_check, const Gate& gate);
-BoundArgs bound_args(const CaseDev& c, const ResidualCoef& rc, const double* b, const double* x, SolveCtl* sc,
-                     int nchk, const Gate& gate);
 // launchers over the first n cases of a pack (tt0: the launch shape shared by the cases)
 template <typename T, typename TI, typename TO>
 void launch_xpass_multi(const ArgPack<XpassArgs<T, TI, TO>>& p, int n, const TransformTables& tt0, cudaStream_t st);
@@ -677,7 +664,6 @@ void launch_band_fwd_solve_multi(const ArgPack<BandFwdArgs<T>>& p, int n, cudaSt
 template <typename T>
 void launch_band_direct_multi(const ArgPack<BandDirectArgs<T>>& p, int n, cudaStream_t st);
 void launch_residual_multi(const ArgPack<ResidualArgs>& p, int n, int kind, bool res_f32, cudaStream_t st);
-void launch_pressure_bound_multi(const ArgPack<BoundArgs>& p, int n, cudaStream_t st);
 // Refinement decision of a WHILE node over n cases: each case whose check sc->k exceeded its
 // inner target (and may refine again) advances sc->k and is marked active (SolveCtl::act); the
 // condition is set while any case is active.  Kernels gated with Gate::sweep = -1 run for
