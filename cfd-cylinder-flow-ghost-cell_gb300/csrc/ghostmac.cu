@@ -183,6 +183,7 @@ struct gm_handle {
   DBuf<float> jval[2], jidiag[2], jd0, jd1;
   DBuf<int32_t> jsidx[2], jrpos[2];
   size_t jac_smem = 0;  // dynamic shared memory of the temporally blocked form (0: K launches)
+  int jac_tile = 0;     // its regular tile, width * 1000 + height (autotuned at set-up)
   // flexible GMRES (pressure_solver = iterative): Krylov basis V (m+1 vectors), preconditioned
   // directions Z (m), the refinement correction and reduction scratch
   static constexpr int GMRES_M = 50;
@@ -1586,17 +1587,17 @@ void project(gm_handle* h, double* q, double dt, double* out, double* phi, int s
 // With rho > 1/4 (large dt nu / h^2) the FFT inverse stays.  GHOSTMAC_HELM_JACOBI=0 keeps the
 // FFT inverse, =N forces N iterations.
 // Tiles of the temporally blocked Jacobi application on the u (k = 0) or v (k = 1) grid:
-// regular 64 x 32 tiles, and the body box around the irregular rows with iters - 1 points of
+// regular tw x th tiles, and the body box around the irregular rows with iters - 1 points of
 // margin, whose loaded region is what iters - 1 stencil steps reach from the box (breadth-first
 // over the five-point stencil and the irregular rows' entries).  Returns false when the
 // region would not fit the block's shared memory.
-bool jacobi_tiles(gm_handle* h, int k, int iters) {
+bool jacobi_tiles(gm_handle* h, int k, int iters, int tw, int th) {
   const gm::Geometry& g = h->g;
   const int W = k == 0 ? g.nx + 1 : g.nx, R = k == 0 ? g.ny : g.ny + 1, hal = iters - 1;
   JacobiTiles& T = h->hj.jt[k];
   T = JacobiTiles{};
-  T.tw = 64;
-  T.th = 32;
+  T.tw = tw;
+  T.th = th;
   T.ntx = (W + T.tw - 1) / T.tw;
   T.nty = (R + T.th - 1) / T.th;
   const gm::Csr& c = h->hs.irr[k];
@@ -1724,12 +1725,71 @@ void build_helm_jacobi(gm_handle* h) {
   if (iters > 0) {
     bool tiled = true;
     if (const char* e = std::getenv("GHOSTMAC_HELM_JACOBI_TILED")) tiled = std::atoi(e) != 0;
-    size_t smem = 0;
-    for (int k = 0; k < 2 && tiled; ++k) {
-      tiled = jacobi_tiles(h, k, iters);
-      if (tiled) smem = std::max(smem, helm_jacobi_tiled_smem(h->hj.jt[k], iters));
+    // Regular tile shapes (width x height), timed on both grids; the fastest is kept.  A
+    // smaller tile gives more blocks (a more even spread over the SMs) but a larger share of
+    // recomputed halo; every shape computes the same values.
+    static const int shapes[][2] = {{64, 32}, {32, 32}, {64, 16}, {128, 16}, {32, 16}, {128, 8}, {64, 8}};
+    size_t smem_max = 0;
+    std::vector<int> fits;
+    for (int s = 0; s < (int)(sizeof shapes / sizeof shapes[0]) && tiled; ++s) {
+      bool ok2 = true;
+      size_t sm = 0;
+      for (int k = 0; k < 2 && ok2; ++k) {
+        ok2 = jacobi_tiles(h, k, iters, shapes[s][0], shapes[s][1]);
+        if (ok2) sm = std::max(sm, helm_jacobi_tiled_smem(h->hj.jt[k], iters));
+      }
+      if (ok2 && sm <= h->smem_optin) {
+        fits.push_back(s);
+        smem_max = std::max(smem_max, sm);
+      }
     }
-    if (tiled && smem <= h->smem_optin && helm_jacobi_tiled_optin(smem) == 0) h->jac_smem = smem;
+    if (tiled && !fits.empty() && helm_jacobi_tiled_optin(smem_max) == 0) {
+      int best = fits[0];
+      if (fits.size() > 1 && !h->capturing) {
+        cudaStream_t st = h->st;
+        const Gate open{nullptr, 0, 0};
+        double *r = nullptr, *x = nullptr;
+        CK(cudaMalloc(&r, (size_t)h->F * sizeof(double)));
+        CK(cudaMalloc(&x, (size_t)h->F * sizeof(double)));
+        CK(cudaMemsetAsync(r, 0, (size_t)h->F * sizeof(double), st));
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        float best_ms = 1e30f;
+        for (int s : fits) {
+          size_t sm = 0;
+          for (int k = 0; k < 2; ++k) {
+            jacobi_tiles(h, k, iters, shapes[s][0], shapes[s][1]);
+            sm = std::max(sm, helm_jacobi_tiled_smem(h->hj.jt[k], iters));
+          }
+          float ms_best = 1e30f;
+          for (int rep = 0; rep < 6; ++rep) {
+            CK(cudaEventRecord(e0, st));
+            for (int q = 0; q < 4; ++q)
+              for (int kind = 1; kind <= 2; ++kind)
+                launch_helm_jacobi_tiled<double>(h->cd, h->rcoef[kind], h->hj, kind, r, x, false, sm, open, st);
+            CK(cudaGetLastError());
+            CK(cudaEventRecord(e1, st));
+            CK(cudaEventSynchronize(e1));
+            float ms = 0.0f;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            if (rep > 0) ms_best = std::min(ms_best, ms);  // the first run warms caches and code
+          }
+          if (ms_best < best_ms) { best_ms = ms_best; best = s; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(r);
+        cudaFree(x);
+      }
+      size_t smem = 0;
+      for (int k = 0; k < 2; ++k) {
+        jacobi_tiles(h, k, iters, shapes[best][0], shapes[best][1]);
+        smem = std::max(smem, helm_jacobi_tiled_smem(h->hj.jt[k], iters));
+      }
+      h->jac_smem = smem;
+      h->jac_tile = shapes[best][0] * 1000 + shapes[best][1];
+    }
   }
   if (iters > 0 && !h->jac_smem && h->jd0.n != (size_t)h->F) {
     h->jd0.alloc(h->F);
