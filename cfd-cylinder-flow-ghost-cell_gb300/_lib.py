@@ -37,7 +37,8 @@ SYMBOLS = ('gm_create', 'gm_create_host', 'gm_prepare_dt', 'gm_destroy', 'gm_las
            'gm_cc_divergence_stats', 'gm_cc_phase_timing', 'gm_cc_legacy_step', 'gm_cc_set_legacy_history',
            'gm_cc_get_legacy_history', 'gm_mac_ab2_rhs', 'gm_mac_ghost_apply',
            'gm_mac_ghost_correct', 'gm_mac_ghost_forces', 'gm_poisson_create',
-           'gm_poisson_destroy', 'gm_poisson_last_error', 'gm_poisson_solve')
+           'gm_poisson_destroy', 'gm_poisson_last_error', 'gm_poisson_solve',
+           'gm_poisson_legacy_step')
 CC_OP_MOMENTUM_ADVECTION, CC_OP_MOMENTUM_DIFFUSION, CC_OP_ADVECTION, CC_OP_DIFFUSION, CC_OP_H_MATVEC, CC_OP_PROJECT, \
     CC_OP_PRESSURE_SOLVE, CC_OP_MOMENTUM_ADVECTION_UPWIND = range(1, 9)
 MAC_AB2, MAC_RHS = 1, 2
@@ -108,6 +109,21 @@ class CcStepDiag(C.Structure):
                [('forces', C.c_double * 6)] + \
                [(n, C.c_int32) for n in ('momentum_iterations', 'pressure_solves', 'status', 'gate')] + \
                [(n, C.c_double) for n in ('pressure_residual_linf', 'pressure_residual_l2')]
+
+
+class LegacyState(C.Structure):
+    _fields_ = [('nx', C.c_int32), ('ny', C.c_int32), ('dx', C.c_double), ('dy', C.c_double), ('nu', C.c_double),
+                ('rho', C.c_double), ('slip_walls', C.c_int32), ('centered', C.c_int32), ('ghost', C.c_int32)] + \
+               [(n, C.c_void_p) for n in ('u', 'v', 'p', 'u_star', 'v_star', 'rhs', 'phi', 'prev_du', 'prev_dv',
+                                          'zero_p', 'mask', 'inlet')] + \
+               [('n_ghost', C.c_int64 * 2)] + \
+               [(n, C.c_void_p * 2) for n in ('target', 'src', 'snap_of', 'weights', 'gamma', 'level')] + \
+               [('n_levels', C.c_int32 * 2), ('xc', C.c_double), ('yc', C.c_double), ('radius', C.c_double),
+                ('n_theta', C.c_int32), ('has_prev', C.c_int32), ('prev_dt', C.c_double)]
+
+
+class LegacyStepDiag(C.Structure):
+    _fields_ = [('forces', C.c_double * 4), ('pressure_residual_linf', C.c_double)]
 
 
 def _load():
@@ -199,6 +215,7 @@ def _load():
         'gm_cc_legacy_step': ([P, D, I32, D, I32, C.POINTER(CcStepDiag)], C.c_int),
         'gm_cc_set_legacy_history': ([P, I32, P, D], C.c_int),
         'gm_cc_get_legacy_history': ([P, C.POINTER(I32), P, C.POINTER(D)], C.c_int),
+        'gm_poisson_legacy_step': ([P, C.POINTER(LegacyState), D, I32, C.POINTER(LegacyStepDiag), P], C.c_int),
         'gm_mac_ghost_apply': ([P, I64, I64, P, P, P, P, P, P, I32, D, P], C.c_int),
         'gm_mac_ghost_correct': ([P, P, P, P, P, P, P, I32, I32, D, D, D, D, I32, P], C.c_int),
         'gm_mac_ghost_forces': ([P, P, P, I32, I32, D, D, D, D, D, I32, D, P, P], C.c_int),

@@ -1992,6 +1992,9 @@ struct gm_poisson {
   Buf<double> b, x;
   Buf<double> ikappa;
   Buf<int32_t> cell_type;
+  // the legacy loop's device scratch and per-step records (four forces and the residual bits)
+  Buf<double> lscratch, lrec;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
 };
 
 extern "C" {
@@ -2040,8 +2043,88 @@ int gm_poisson_destroy(gm_poisson* p) {
   if (!p) return GM_OK;
   gm_handle* P = p->P;
   if (P) cudaStreamSynchronize(gmi::stream(P));
+  if (p->ev_in) cudaEventDestroy(p->ev_in);
+  if (p->ev_out) cudaEventDestroy(p->ev_out);
   delete p;
   if (P) gmi::pressure_destroy(P);
+  return GM_OK;
+}
+
+int gm_poisson_legacy_step(gm_poisson* p, gm_legacy_state* s, double dt, int32_t n_steps, gm_legacy_step_diag* diag,
+                           void* stream) {
+  if (!p) return GM_EVALUE;
+  if (!s || n_steps <= 0 || !(std::isfinite(dt) && dt > 0)) {
+    p->err = "a state, a positive step count and a finite positive dt are required";
+    return GM_EVALUE;
+  }
+  if ((int64_t)s->nx * s->ny != p->psize || !s->u || !s->v || !s->p || !s->u_star || !s->v_star || !s->rhs ||
+      !s->phi || !s->prev_du || !s->prev_dv || !s->zero_p || !s->mask || !s->inlet ||
+      (s->centered && s->has_prev && !(std::isfinite(s->prev_dt) && s->prev_dt > 0))) {
+    p->err = "the legacy state does not match the pressure system or is incomplete";
+    return GM_EVALUE;
+  }
+  if (s->ghost)
+    for (int k = 0; k < 2; ++k)
+      if (s->n_ghost[k] < 0 || (s->n_ghost[k] > 0 && (!s->target[k] || !s->src[k] || !s->snap_of[k] ||
+                                                      !s->weights[k] || !s->gamma[k] || !s->level[k]))) {
+        p->err = "incomplete ghost tables";
+        return GM_EVALUE;
+      }
+  try {
+    cudaStream_t st = gmi::stream(p->P);
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    if (!p->ev_in) CCK(cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming));
+    if (!p->ev_out) CCK(cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming));
+    CCK(cudaEventRecord(p->ev_in, cs));
+    CCK(cudaStreamWaitEvent(st, p->ev_in, 0));
+    const size_t need = gml::scratch_doubles(*s);
+    if (p->lscratch.n < need) p->lscratch.alloc(need);
+    if (p->lrec.n < (size_t)n_steps * 5) p->lrec.alloc((size_t)n_steps * 5);
+    CcGeo g{};
+    g.psize = p->psize;
+    g.cell_type = p->cell_type.p;
+    g.ikappa = p->ikappa.p;
+    std::vector<double> rec((size_t)n_steps * 5);
+    for (int32_t k = 0; k < n_steps; ++k) {
+      double* r = p->lrec.p + (size_t)k * 5;
+      gml::predict(*s, dt, p->lscratch.p, st);
+      if (s->centered) {  // the loop keeps the AB2 history before its pressure solve (solver/main.py:320)
+        s->has_prev = 1;
+        s->prev_dt = dt;
+      }
+      counted();
+      k_cc_scale_rhs<<<nblk(p->psize), CC_TPB, 0, st>>>(g, s->rhs);
+      CCK(cudaMemsetAsync(gmi::control(p->P), 0, sizeof(StepCtl), st));
+      CCK(cudaMemsetAsync(r + 4, 0, sizeof(double), st));
+      gmi::pressure_solve(p->P, s->rhs, s->phi, S_P1);
+      counted();
+      k_cc_maxdiff<<<std::min<unsigned>(nblk(p->psize), 1216), CC_TPB, 0, st>>>(
+          p->psize, gmi::pressure_residual(p->P), nullptr, nullptr, 0.0, reinterpret_cast<unsigned long long*>(r + 4));
+      std::string m;
+      const int rc = gmi::check(p->P, "pressure solve", m);  // synchronises the stream
+      if (rc != GM_OK) throw CcFail(rc, m);
+      gml::correct(*s, dt, p->lscratch.p, st);
+      gml::forces(*s, p->lscratch.p, r, st);
+    }
+    CCK(cudaMemcpyAsync(rec.data(), p->lrec.p, rec.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CCK(cudaGetLastError());
+    CCK(cudaStreamSynchronize(st));
+    CCK(cudaEventRecord(p->ev_out, st));
+    CCK(cudaStreamWaitEvent(cs, p->ev_out, 0));
+    if (diag)
+      for (int32_t k = 0; k < n_steps; ++k) {
+        for (int q = 0; q < 4; ++q) diag[k].forces[q] = rec[(size_t)k * 5 + q];
+        unsigned long long bits;
+        std::memcpy(&bits, &rec[(size_t)k * 5 + 4], sizeof bits);
+        diag[k].pressure_residual_linf = bits_to_double(bits);
+      }
+  } catch (const CcFail& e) {
+    p->err = e.msg;
+    return e.cls;
+  } catch (const std::exception& e) {
+    p->err = e.what();
+    return GM_ECUDA;
+  }
   return GM_OK;
 }
 

@@ -9,6 +9,7 @@
 #include <functional>
 #include <string>
 
+#include "../../include/ghostmac.h"
 #include "geometry.hpp"
 #include "kernels.cuh"
 
@@ -51,3 +52,18 @@ struct SurfaceCsr {
 SurfaceCsr surface(const gm_handle* h);
 
 }  // namespace gmi
+
+// The legacy step's launches on a stream, without synchronisation (legacy.cu); arrays of the
+// state are device memory.
+namespace gml {
+// doubles of device scratch the calls below need
+size_t scratch_doubles(const gm_legacy_state& s);
+// u*, v* (predictor_rhs_cpp), ghost velocities, the AB2 step (centred), ghost velocities, and
+// the Poisson right-hand side into s.rhs
+void predict(const gm_legacy_state& s, double dt, double* scratch, cudaStream_t st);
+// the corrector (with the ghost-cell branch's ghost velocities and boundary faces), then
+// p = phi (centred) or p += phi
+void correct(const gm_legacy_state& s, double dt, double* scratch, cudaStream_t st);
+// the step's forces (fx_p, fy_p, fx_v, fy_v) into out[0..3] (device)
+void forces(const gm_legacy_state& s, double* scratch, double* out, cudaStream_t st);
+}  // namespace gml

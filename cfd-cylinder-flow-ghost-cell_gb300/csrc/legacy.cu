@@ -20,10 +20,12 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
 #include "../../include/ghostmac.h"
+#include "internal.hpp"
 
 namespace gmk {
 void kernel_launch_adjust(long long delta);  // the library's launch counter (kernels.cu)
@@ -419,6 +421,7 @@ __global__ void k_fold(const double* __restrict__ part, int nblocks, int nf, int
   }
 }
 
+
 int fail(int code, const char* msg) {
   gm_internal_set_error(msg);
   return code;
@@ -524,7 +527,95 @@ int cuda_fail(cudaError_t e) {
 }
 unsigned blocks(long long n) { return (unsigned)((n + LT - 1) / LT); }
 
+// p = phi (c = 0) or p += phi (c = 1)
+__global__ void k_pupdate(double* __restrict__ p, const double* __restrict__ phi, long long n, int add) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) p[t] = add ? p[t] + phi[t] : phi[t];
+}
+
+void ghost_pass(const gm_legacy_state& s, int k, double* field, double* snap, cudaStream_t st) {
+  const long long n = s.n_ghost[k];
+  if (n <= 0) return;
+  const long long nf = k == 0 ? (long long)s.ny * (s.nx + 1) : (long long)(s.ny + 1) * s.nx;
+  const long long* tg = reinterpret_cast<const long long*>(s.target[k]);
+  k_ghost_save<<<blocks(n), LT, 0, st>>>(field, nf, tg, n, snap);
+  for (int l = 0; l < s.n_levels[k]; ++l)
+    k_ghost_level<<<blocks(n), LT, 0, st>>>(field, nf, tg, reinterpret_cast<const long long*>(s.src[k]), s.snap_of[k],
+                                            s.weights[k], s.gamma[k], s.level[k], n, l, snap, 0.0);
+  gmk::kernel_launch_adjust(1 + s.n_levels[k]);
+}
+
 }  // namespace
+
+namespace gml {
+
+size_t scratch_doubles(const gm_legacy_state& s) {
+  const long long nP = (long long)s.ny * s.nx;
+  const long long ng = std::max<long long>(s.ghost ? std::max(s.n_ghost[0], s.n_ghost[1]) : 0, 1);
+  return (size_t)(ng + (long long)blocks(nP) * 4 + 16);
+}
+
+void predict(const gm_legacy_state& s, double dt, double* scratch, cudaStream_t st) {
+  const int nx = s.nx, ny = s.ny;
+  const long long nU = (long long)ny * (nx + 1), nV = (long long)(ny + 1) * nx, nP = (long long)ny * nx;
+  const double* pin = s.centered ? s.zero_p : s.p;
+  k_predict_u<<<blocks(nU), LT, 0, st>>>(s.u, s.v, s.u_star, pin, s.mask, s.inlet, nx, ny, s.dx, s.dy, s.dx * s.dx,
+                                         s.dy * s.dy, dt, s.nu, s.rho, s.slip_walls ? 1 : 0, s.centered ? 1 : 0);
+  k_predict_v<<<blocks(nV), LT, 0, st>>>(s.u, s.v, s.v_star, pin, s.mask, nx, ny, s.dx, s.dy, s.dx * s.dx,
+                                         s.dy * s.dy, dt, s.nu, s.rho, s.centered ? 1 : 0);
+  gmk::kernel_launch_adjust(2);
+  if (s.ghost) {
+    ghost_pass(s, 0, s.u_star, scratch, st);
+    ghost_pass(s, 1, s.v_star, scratch, st);
+  }
+  if (s.centered) {
+    const bool hp = s.has_prev != 0;
+    k_ab2<<<blocks(nU + nV), LT, 0, st>>>(s.u, s.v, s.u_star, s.v_star, s.prev_du, s.prev_dv, nx, ny, dt,
+                                          hp ? dt * (dt / (2 * s.prev_dt)) : 0.0, hp ? 1 : 0);
+    gmk::kernel_launch_adjust(1);
+    if (s.ghost) {
+      ghost_pass(s, 0, s.u_star, scratch, st);
+      ghost_pass(s, 1, s.v_star, scratch, st);
+    }
+  }
+  k_legacy_rhs<<<blocks(nP), LT, 0, st>>>(s.u_star, s.v_star, s.mask, s.rhs, nx, ny, s.dx, s.dy, s.rho / dt);
+  gmk::kernel_launch_adjust(1);
+}
+
+void correct(const gm_legacy_state& s, double dt, double* scratch, cudaStream_t st) {
+  const int nx = s.nx, ny = s.ny;
+  const long long n = (long long)ny * (nx + 1) + (long long)(ny + 1) * nx, nP = (long long)ny * nx;
+  if (s.ghost) {
+    k_ghost_correct<<<blocks(n), LT, 0, st>>>(s.u, s.v, s.u_star, s.v_star, s.phi, s.mask, s.inlet, nx, ny, s.dx,
+                                              s.dy, dt / s.rho);
+    gmk::kernel_launch_adjust(1);
+    ghost_pass(s, 0, s.u, scratch, st);
+    ghost_pass(s, 1, s.v, scratch, st);
+    k_ghost_boundary<<<blocks(n), LT, 0, st>>>(s.u, s.v, s.u_star, s.v_star, s.mask, nx, ny);
+  } else {
+    k_correct<<<blocks(n), LT, 0, st>>>(s.u, s.v, s.u_star, s.v_star, s.phi, s.mask, s.inlet, nx, ny, s.dx, s.dy,
+                                        dt / s.rho);
+  }
+  k_pupdate<<<blocks(nP), LT, 0, st>>>(s.p, s.phi, nP, s.centered ? 0 : 1);
+  gmk::kernel_launch_adjust(2);
+}
+
+void forces(const gm_legacy_state& s, double* scratch, double* out, cudaStream_t st) {
+  const int nx = s.nx, ny = s.ny;
+  const double mu = s.nu * s.rho;
+  if (s.ghost) {
+    k_ghost_forces<<<1, 256, 0, st>>>(s.u, s.v, s.p, nx, ny, s.dx, s.dy, s.xc, s.yc, s.radius, s.n_theta, mu, out);
+    gmk::kernel_launch_adjust(1);
+    return;
+  }
+  const unsigned nb = blocks((long long)ny * nx);
+  double* part = scratch + std::max<long long>(s.ghost ? std::max(s.n_ghost[0], s.n_ghost[1]) : 0, 1);
+  k_forces_part<<<nb, LT, 0, st>>>(s.u, s.v, s.p, s.mask, nx, ny, s.dx, s.dy, mu, part);
+  k_fold<<<1, 32, 0, st>>>(part, (int)nb, 4, 0, out);
+  gmk::kernel_launch_adjust(2);
+}
+
+}  // namespace gml
 
 extern "C" {
 

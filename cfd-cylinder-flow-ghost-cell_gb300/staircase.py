@@ -1,13 +1,15 @@
-"""MAC_CylinderFlow(boundary='staircase', time_scheme='legacy') on the GPU.
+"""MAC_CylinderFlow(boundary='staircase' | 'ghost_cell', time_scheme='legacy') on the GPU.
 
-The reference's legacy staircase loop (solver/main.py:245-501 with boundary='staircase'): the
-native predictor and right-hand side (predictor_rhs_cpp), the loop's own AB2 step for centred
-transport and its recomputed Poisson right-hand side, a pressure solve of the staircase Poisson
-matrix (build_poisson_matrix, solver/mac_solver.py:5-87, which the reference factors with a
-sparse LU or solves by ILU-GMRES), the native corrector and the staircase force sums.  Every
-kernel is this library's (gm_mac_*, gm_poisson_*); the state stays on the device between steps
-(torch tensors serve as device buffers), and the host arrays u, v, p are written back after
-each solve() call.  The staircase Poisson matrix is the aperture-weighted cut-cell matrix with
+The reference's legacy loop (solver/main.py:245-501): the native predictor (predictor_rhs_cpp),
+for the ghost-cell branch the image-point ghost velocities of GhostCellBoundary
+(solver/ghost_cell.py), the loop's own AB2 step for centred transport and its recomputed
+Poisson right-hand side, a pressure solve of the staircase Poisson matrix (build_poisson_matrix,
+solver/mac_solver.py:5-87, which the reference factors with a sparse LU or solves by
+ILU-GMRES), the native corrector (or the ghost-cell branch's) and the force sums (staircase
+sums, or the integral on the true circle).  One library call (gm_poisson_legacy_step) runs a
+chunk of steps on the device with one synchronisation per step; the state stays on the device
+between calls (torch tensors serve as device buffers), and the host arrays u, v, p are written
+back after each solve() call.  The staircase Poisson matrix is the aperture-weighted cut-cell matrix with
 open fractions 0 or 1 taken from the cell mask, solved to rounding by the boundary-corrected
 separable inverse; both pressure_solver choices of the reference solve that system (the LU
 exactly, ILU-GMRES to rtol 1e-8).
@@ -124,7 +126,17 @@ class StaircaseFlow:
                        pdu=torch.zeros(self.u.shape, **f64), pdv=torch.zeros(self.v.shape, **f64),
                        inlet=torch.empty(self.ny, **f64),
                        mask=torch.from_numpy(np.ascontiguousarray(self.mask, dtype=np.uint8)).to(dev))
-        self._previous_dt = None
+        st = _lib.LegacyState()
+        st.nx, st.ny, st.dx, st.dy = self.nx, self.ny, self.dx, self.dy
+        st.nu, st.rho = float(nu), float(rho)
+        st.slip_walls = 1 if slip_walls else 0
+        st.centered = 1 if transport == 'centered' else 0
+        d = self._d
+        for name, key in (('u', 'u'), ('v', 'v'), ('p', 'p'), ('u_star', 'us'), ('v_star', 'vs'), ('rhs', 'rhs'),
+                          ('phi', 'phi'), ('prev_du', 'pdu'), ('prev_dv', 'pdv'), ('zero_p', 'zero_p'),
+                          ('mask', 'mask'), ('inlet', 'inlet')):
+            setattr(st, name, d[key].data_ptr())
+        self._st = st
         self.time = 0.0
         self.run_options = {}
         self.last_step_diagnostics = {}
@@ -154,39 +166,19 @@ class StaircaseFlow:
         for name, key in (('u', 'u'), ('v', 'v'), ('p', 'p'), ('phi', 'phi')):
             getattr(self, name)[...] = self._d[key].cpu().numpy()
 
-    def _step(self, dt):
-        """One legacy step on the device (solver/main.py:303-378, staircase branch)."""
-        d = self._d
-        st = self._stream()
-        nonincremental = self.transport == 'centered'
-        centered = 1 if self.transport == 'centered' else 0
-        _check_mac(lib.gm_mac_predictor_rhs(ptr(d['u']), ptr(d['v']), ptr(d['us']), ptr(d['vs']), ptr(d['rhs']),
-                                            ptr(d['zero_p'] if nonincremental else d['p']), ptr(d['mask']),
-                                            ptr(d['inlet']), self.nx, self.ny, self.dx, self.dy, float(dt),
-                                            float(self.nu), float(self.rho), 1 if self.slip_walls else 0, centered, st))
-        has_prev = self._previous_dt is not None
-        alpha = dt / (2 * self._previous_dt) if has_prev else 0.0
-        _check_mac(lib.gm_mac_ab2_rhs(ptr(d['u']), ptr(d['v']), ptr(d['us']), ptr(d['vs']), ptr(d['pdu']),
-                                      ptr(d['pdv']), ptr(d['rhs']), ptr(d['mask']), self.nx, self.ny, self.dx,
-                                      self.dy, float(dt), float(self.rho), float(alpha), 1 if has_prev else 0,
-                                      (_lib.MAC_AB2 if centered else 0) | _lib.MAC_RHS, st))
-        if centered:
-            self._previous_dt = dt
-        res = C.c_double()
-        rc = lib.gm_poisson_solve(self._poisson, ptr(d['rhs']), ptr(d['phi']), C.byref(res))
+    @property
+    def _previous_dt(self):
+        """dt of the last centred step (the loop's AB2 history), or None."""
+        return self._st.prev_dt if self._st.has_prev else None
+
+    def _steps(self, dt, n):
+        """n legacy steps with the current inlet on the device (solver/main.py:303-378), one
+        library call: per-step (fx_p, fy_p, fx_v, fy_v) and the pressure residual."""
+        diag = (_lib.LegacyStepDiag * n)()
+        rc = lib.gm_poisson_legacy_step(self._poisson, C.byref(self._st), float(dt), int(n), diag, self._stream())
         if rc != _lib.GM_OK:
             raise _lib.error_for(rc, lib.gm_poisson_last_error(self._poisson).decode(errors='replace'))
-        _check_mac(lib.gm_mac_corrector(ptr(d['u']), ptr(d['v']), ptr(d['us']), ptr(d['vs']), ptr(d['phi']),
-                                        ptr(d['mask']), ptr(d['inlet']), self.nx, self.ny, self.dx, self.dy, float(dt),
-                                        float(self.rho), 1 if self.slip_walls else 0, st))
-        if nonincremental:
-            d['p'].copy_(d['phi'])
-        else:
-            d['p'].add_(d['phi'])
-        out = np.empty(4)
-        _check_mac(lib.gm_mac_forces(ptr(d['u']), ptr(d['v']), ptr(d['p']), ptr(d['mask']), self.nx, self.ny,
-                                     self.dx, self.dy, float(self.nu * self.rho), ptr(out), st))
-        return out, res.value
+        return [(tuple(d.forces), d.pressure_residual_linf) for d in diag]
 
     def divergence_stats(self):
         """calculate_mac_divergence_cpp of the state: (max |div|, sum div^2, fluid count, core sum
@@ -220,7 +212,8 @@ class StaircaseFlow:
         start = self.time
         ts, cds, cls = [], [], []
         denom = 0.5 * self.rho * (self.U_ref ** 2) * self.D
-        for s in range(n_steps):
+        s = 0
+        while s < n_steps:
             now_t = start + (s + 1) * dt
             if s % 100 == 0:
                 # explicit advection/diffusion screen (solver/main.py:273-278)
@@ -233,33 +226,39 @@ class StaircaseFlow:
                 decay = 1.0 - (now_t / perturb_duration)
                 pert = perturb_amp * np.sin(2.0 * np.pi * self.y_centers / self.Ly) * decay
                 self.u_inlet[:] = self.u_inlet_base * (1.0 + pert)
+                chunk = 1
             else:
                 self.u_inlet[:] = self.u_inlet_base
+                chunk = 1 if step_callback is not None else min(n_steps - s, 100 - s % 100)
+                if verbose:
+                    chunk = min(chunk, 1001 - s % 1000 if s % 1000 else 1)
             d['inlet'].copy_(torch.from_numpy(self.u_inlet))
-            (fx_p, fy_p, fx_v, fy_v), res = self._step(dt)
-            fx, fy = fx_p + fx_v, fy_p + fy_v
-            cd, cl = fx / denom, fy / denom
-            if not np.isfinite(cd) or not np.isfinite(cl):
-                self._pull()
-                raise FloatingPointError(f'Non-finite force at t={now_t:g}; results not saved')
-            self.time = now_t
-            self.last_step_diagnostics = dict(time=self.time, dt=dt, cd=float(cd), cl=float(cl),
-                                              cd_pressure=float(fx_p / denom), cd_viscous=float(fx_v / denom),
-                                              cl_pressure=float(fy_p / denom), cl_viscous=float(fy_v / denom),
-                                              pressure_residual_linf=float(res))
+            for k, ((fx_p, fy_p, fx_v, fy_v), res) in enumerate(self._steps(dt, chunk)):
+                t_k = start + (s + k + 1) * dt
+                fx, fy = fx_p + fx_v, fy_p + fy_v
+                cd, cl = fx / denom, fy / denom
+                if not np.isfinite(cd) or not np.isfinite(cl):
+                    self._pull()
+                    raise FloatingPointError(f'Non-finite force at t={t_k:g}; results not saved')
+                self.time = t_k
+                self.last_step_diagnostics = dict(time=self.time, dt=dt, cd=float(cd), cl=float(cl),
+                                                  cd_pressure=float(fx_p / denom), cd_viscous=float(fx_v / denom),
+                                                  cl_pressure=float(fy_p / denom), cl_viscous=float(fy_v / denom),
+                                                  pressure_residual_linf=float(res))
+                cds.append(cd)
+                cls.append(cl)
+                ts.append(t_k)
+            s += chunk
             if step_callback is not None:
                 self._pull()
                 step_callback(self, dict(self.last_step_diagnostics))
-            cds.append(cd)
-            cls.append(cl)
-            ts.append(now_t)
-            if verbose and (s % 1000 == 0 or s == n_steps - 1):
+            if verbose and ((s - 1) % 1000 == 0 or s == n_steps):
                 max_div, sum_div2, count, _, _ = self.divergence_stats()
                 div_all = np.sqrt(sum_div2 / count) if count > 0 else 0.0
                 self._pull()
                 in_flux, out_flux = np.sum(self.u[:, 0]) * self.dy, np.sum(self.u[:, self.nx]) * self.dy
-                print(f"Step {s:5d} | Div_RMS: {div_all:.2e} | Div_Max: {max_div:.2e} | "
-                      f"FluxErr: {abs(out_flux - in_flux) / in_flux:.2e} | Cd: {cd:.4f} | Cl: {cl:.4f}")
+                print(f"Step {s - 1:5d} | Div_RMS: {div_all:.2e} | Div_Max: {max_div:.2e} | "
+                      f"FluxErr: {abs(out_flux - in_flux) / in_flux:.2e} | Cd: {cds[-1]:.4f} | Cl: {cls[-1]:.4f}")
         self._pull()
         if verbose:
             elapsed = _time.time() - t0
@@ -352,63 +351,19 @@ class LegacyGhostFlow(StaircaseFlow):
         xv = (np.arange(self.nx) + 0.5) * self.dx
         yv = np.arange(self.ny + 1) * self.dy
         self._ghost = {}
-        for key, xs, ys, is_u in (('u', xu, yu, True), ('v', xv, yv, False)):
+        st = self._st
+        st.ghost = 1
+        st.xc, st.yc, st.radius, st.n_theta = float(self.xc), float(self.yc), float(self.D / 2.0), self.n_theta
+        for k, (key, xs, ys, is_u) in enumerate((('u', xu, yu, True), ('v', xv, yv, False))):
             t = ghost_face_tables(xs, ys, self.dx, self.dy, self.xc, self.yc, self.D / 2.0, is_u)
-            dt = {k: torch.from_numpy(np.ascontiguousarray(t[k])).to(dev)
-                  for k in ('target', 'src', 'weights', 'gamma', 'snap_of', 'level')}
+            dt = {name: torch.from_numpy(np.ascontiguousarray(t[name])).to(dev)
+                  for name in ('target', 'src', 'weights', 'gamma', 'snap_of', 'level')}
             dt['n'], dt['n_levels'] = int(t['target'].size), t['n_levels']
             self._ghost[key] = dt
-
-    def _apply_ghost(self, fu, fv):
-        """apply_velocity_ghost_cells (solver/ghost_cell.py:159-184) with zero wall velocity."""
-        st = self._stream()
-        for key, f in (('u', fu), ('v', fv)):
-            t = self._ghost[key]
-            _check_mac(lib.gm_mac_ghost_apply(ptr(f), f.numel(), t['n'], ptr(t['target']), ptr(t['src']),
-                                              ptr(t['snap_of']), ptr(t['weights']), ptr(t['gamma']),
-                                              ptr(t['level']), t['n_levels'], 0.0, st))
+            st.n_ghost[k], st.n_levels[k] = dt['n'], dt['n_levels']
+            for name in ('target', 'src', 'snap_of', 'weights', 'gamma', 'level'):
+                getattr(st, name)[k] = dt[name].data_ptr()
 
     def ghost_counts(self):
         """Numbers of ghost u and v faces and of launch levels of each."""
         return {k: (t['n'], t['n_levels']) for k, t in self._ghost.items()}
-
-    def _step(self, dt):
-        """One legacy step on the device (solver/main.py:303-378, ghost_cell branch)."""
-        d = self._d
-        st = self._stream()
-        centered = self.transport == 'centered'
-        nonincremental = centered
-        _check_mac(lib.gm_mac_predictor_rhs(ptr(d['u']), ptr(d['v']), ptr(d['us']), ptr(d['vs']), ptr(d['rhs']),
-                                            ptr(d['zero_p'] if nonincremental else d['p']), ptr(d['mask']),
-                                            ptr(d['inlet']), self.nx, self.ny, self.dx, self.dy, float(dt),
-                                            float(self.nu), float(self.rho), 1 if self.slip_walls else 0,
-                                            1 if centered else 0, st))
-        self._apply_ghost(d['us'], d['vs'])
-        has_prev = self._previous_dt is not None
-        alpha = dt / (2 * self._previous_dt) if has_prev else 0.0
-        args = (ptr(d['u']), ptr(d['v']), ptr(d['us']), ptr(d['vs']), ptr(d['pdu']), ptr(d['pdv']), ptr(d['rhs']),
-                ptr(d['mask']), self.nx, self.ny, self.dx, self.dy, float(dt), float(self.rho), float(alpha),
-                1 if has_prev else 0)
-        if centered:
-            _check_mac(lib.gm_mac_ab2_rhs(*args, _lib.MAC_AB2, st))
-            self._previous_dt = dt
-            self._apply_ghost(d['us'], d['vs'])
-        _check_mac(lib.gm_mac_ab2_rhs(*args, _lib.MAC_RHS, st))
-        res = C.c_double()
-        rc = lib.gm_poisson_solve(self._poisson, ptr(d['rhs']), ptr(d['phi']), C.byref(res))
-        if rc != _lib.GM_OK:
-            raise _lib.error_for(rc, lib.gm_poisson_last_error(self._poisson).decode(errors='replace'))
-        cargs = (ptr(d['u']), ptr(d['v']), ptr(d['us']), ptr(d['vs']), ptr(d['phi']), ptr(d['mask']),
-                 ptr(d['inlet']), self.nx, self.ny, self.dx, self.dy, float(dt), float(self.rho))
-        _check_mac(lib.gm_mac_ghost_correct(*cargs, 0, st))
-        self._apply_ghost(d['u'], d['v'])
-        _check_mac(lib.gm_mac_ghost_correct(*cargs, 1, st))
-        if nonincremental:
-            d['p'].copy_(d['phi'])
-        else:
-            d['p'].add_(d['phi'])
-        out = np.empty(4)
-        _check_mac(lib.gm_mac_ghost_forces(ptr(d['u']), ptr(d['v']), ptr(d['p']), self.nx, self.ny, self.dx,
-                                           self.dy, float(self.xc), float(self.yc), float(self.D / 2.0),
-                                           self.n_theta, float(self.nu * self.rho), ptr(out), st))
-        return out, res.value

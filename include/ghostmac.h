@@ -373,6 +373,48 @@ int gm_poisson_destroy(gm_poisson* p);
 const char* gm_poisson_last_error(const gm_poisson* p);
 int gm_poisson_solve(gm_poisson* p, const double* rhs, double* phi, double* residual_linf);
 
+/* A legacy loop's state on the device (every array device memory of the current device): the
+ * fields and work arrays of the legacy step of solver/main.py:303-381, the cell mask, the inlet
+ * profile; for the ghost-cell branch the ghost tables of gm_mac_ghost_apply for the u (0) and
+ * v (1) face grids and the circle of the force integral. */
+typedef struct gm_legacy_state {
+  int32_t nx, ny;
+  double dx, dy, nu, rho;
+  int32_t slip_walls;
+  int32_t centered;   /* 1: centred transport with the loop's AB2 step, p = phi; 0: upwind, p += phi */
+  int32_t ghost;      /* 0: staircase branch; 1: ghost-cell branch (GhostCellBoundary) */
+  double *u, *v, *p, *u_star, *v_star, *rhs, *phi, *prev_du, *prev_dv;
+  const double* zero_p;   /* ny x nx zeros: the pressure the centred predictor reads */
+  const uint8_t* mask;    /* ny x nx, nonzero on masked cells */
+  const double* inlet;    /* ny inlet values of the step */
+  int64_t n_ghost[2];
+  const int64_t* target[2];
+  const int64_t* src[2];
+  const int32_t* snap_of[2];
+  const double* weights[2];
+  const double* gamma[2];
+  const int32_t* level[2];
+  int32_t n_levels[2];
+  double xc, yc, radius;
+  int32_t n_theta;
+  int32_t has_prev;   /* the AB2 history (prev_du, prev_dv, prev_dt): read and updated */
+  double prev_dt;
+} gm_legacy_state;
+typedef struct gm_legacy_step_diag {
+  double forces[4];               /* fx_p, fy_p, fx_v, fy_v */
+  double pressure_residual_linf;  /* max |b - A phi| of the step's pressure solve (scaled rows) */
+} gm_legacy_step_diag;
+/* n_steps of the legacy loop with the same inlet, on the device: the predictor
+ * (predictor_rhs_cpp), ghost velocities (ghost-cell branch), the loop's AB2 step, the
+ * right-hand side, the pressure solve of `p` (built over the loop's staircase mask), the
+ * corrector (corrector_cpp, or the ghost-cell branch's), the pressure update and the forces
+ * (calculate_mac_forces_cpp, or extract_true_surface_forces on the circle).  One stream
+ * synchronisation per step, at the pressure gate, before the corrector: a failed solve leaves
+ * u, v and p as they were.  Ordered after the work on `stream` (a cudaStream_t or NULL) and
+ * before later work there. */
+int gm_poisson_legacy_step(gm_poisson* p, gm_legacy_state* s, double dt, int32_t n_steps, gm_legacy_step_diag* diag,
+                           void* stream);
+
 /* --- snapshot POD (postprocessing/modal_analysis.py:17-98) ------------------------ */
 /* Method of snapshots for M snapshots of N points (row-major M x N, host or device memory):
  * gm_pod_gram forms the time mean (summed over the snapshots in order, like numpy's mean
