@@ -1727,11 +1727,15 @@ void build_helm_jacobi(gm_handle* h) {
     if (const char* e = std::getenv("GHOSTMAC_HELM_JACOBI_TILED")) tiled = std::atoi(e) != 0;
     // Regular tile shapes (width x height), timed on both grids; the fastest is kept.  A
     // smaller tile gives more blocks (a more even spread over the SMs) but a larger share of
-    // recomputed halo; every shape computes the same values.
-    static const int shapes[][2] = {{64, 32}, {32, 32}, {64, 16}, {128, 16}, {32, 16}, {128, 8}, {64, 8}};
+    // recomputed halo; a width of 32k - 2 (iters - 1) makes each region row a whole number of
+    // warps.  Every shape computes the same values.
+    std::vector<std::array<int, 2>> shapes = {{64, 32}, {32, 32}, {64, 16}, {128, 16}, {32, 16}, {128, 8}, {64, 8}};
+    for (int k32 : {2, 3, 4})
+      for (int th : {8, 16, 32})
+        if (32 * k32 - 2 * (iters - 1) >= 16) shapes.push_back({32 * k32 - 2 * (iters - 1), th});
     size_t smem_max = 0;
     std::vector<int> fits;
-    for (int s = 0; s < (int)(sizeof shapes / sizeof shapes[0]) && tiled; ++s) {
+    for (int s = 0; s < (int)shapes.size() && tiled; ++s) {
       bool ok2 = true;
       size_t sm = 0;
       for (int k = 0; k < 2 && ok2; ++k) {

@@ -1714,11 +1714,12 @@ template void launch_helm_jacobi<float>(const CaseDev&, const ResidualCoef&, con
 // Points of a regular tile's halo may be irregular rows updated with the five-point formula:
 // their values never reach the tile's outputs.
 // Shared memory of a region of rh x rw points, stored with a border of one zero point on each
-// side (every neighbour read is then in bounds and a missing neighbour reads zero): three float
-// arrays (two iterates and the right-hand side) and the class bytes.
+// side (every neighbour read is then in bounds and a missing neighbour reads zero): four float
+// arrays (two iterates, the right-hand side and each point's multiplier: 1 / diagonal, or 0 on
+// an inactive point) and the west coefficient of each column.
 __host__ __device__ inline size_t jacobi_region_bytes(int rh, int rw) {
   const size_t n = (size_t)(rh + 2) * (rw + 2);
-  return n * 3 * sizeof(float) + (n + 15) / 16 * 16;
+  return (n * 4 + (size_t)(rw + 2) + 3) / 4 * 4 * sizeof(float);
 }
 size_t helm_jacobi_tiled_smem(const JacobiTiles& t, int iters) {
   const int h = iters - 1;
@@ -1734,8 +1735,11 @@ size_t helm_jacobi_tiled_smem(const JacobiTiles& t, int iters) {
 // operator's excluded neighbours (the u inlet column, the v wall rows) are inactive points whose
 // iterate is zero, and points outside the grid are the zero border, so the five-point update
 // needs no neighbour tests.
+// threads of a tile block: every tile's work is latency bound (few warps per SM at this grid
+// size), so a tile takes more warps than the other kernels' blocks
+constexpr int JTPB = 512;
 template <int KIND, typename TR>
-__global__ void __launch_bounds__(TPB) k_helm_jacobi_tiled(CaseDev c, ResidualCoef rc, HelmJacobi hj,
+__global__ void __launch_bounds__(JTPB) k_helm_jacobi_tiled(CaseDev c, ResidualCoef rc, HelmJacobi hj,
                                                           const TR* __restrict__ r, double* __restrict__ x,
                                                           int accumulate, Gate gate) {
   extern __shared__ __align__(16) float jsm[];
@@ -1765,7 +1769,8 @@ __global__ void __launch_bounds__(TPB) k_helm_jacobi_tiled(CaseDev c, ResidualCo
   float* cur = jsm;
   float* nxt = jsm + np;
   float* rr = jsm + 2 * np;
-  uint8_t* kk = reinterpret_cast<uint8_t*>(jsm + 3 * np);
+  float* mm = jsm + 3 * np;   // 1 / diagonal of the point's regular row, 0 on inactive points
+  float* colw = jsm + 4 * np; // west coefficient of each region column
   unsigned char* stage = reinterpret_cast<unsigned char*>(jsm) + jacobi_region_bytes(rh, rw);
   float* sval = reinterpret_cast<float*>(stage);
   int32_t* ssidx = reinterpret_cast<int32_t*>(sval + (body ? T.nnz : 0));
@@ -1773,15 +1778,29 @@ __global__ void __launch_bounds__(TPB) k_helm_jacobi_tiled(CaseDev c, ResidualCo
   int32_t* spos = sptr + (body ? T.nrow + 1 : 0);
   float* sidg = reinterpret_cast<float*>(spos + (body ? T.nrow : 0));
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  // zero borders of both iterates
+  // zero borders of both iterates; the right-hand side and the multiplier of every point, and
+  // the west coefficient of every column, formed once for all the iterations
   for (int q = threadIdx.x; q < np; q += blockDim.x) { cur[q] = 0.0f; nxt[q] = 0.0f; }
+  for (int pi = threadIdx.x; pi < rw; pi += blockDim.x) {
+    const int ii = i0 + pi;
+    const int icl = KIND == 1 ? (ii == nx ? 2 : 1) : (ii == 0 ? 0 : (ii == nx - 1 ? 2 : 1));
+    colw[pi] = icl == 0 ? rc.fcw[0] : (icl == 1 ? rc.fcw[1] : rc.fcw[2]);
+  }
   for (int pj = warp; pj < rh; pj += nwarp) {
-    const int64_t row = (int64_t)(j0 + pj) * W + i0;
+    const int jj = j0 + pj;
+    const int jc = KIND == 1 ? ((jj == 0 || jj == ny - 1) ? 0 : 1) : 1;
+    const float ia = hj.icc[KIND - 1][0][jc], ib = hj.icc[KIND - 1][1][jc], ic2 = hj.icc[KIND - 1][2][jc];
+    const int64_t row = (int64_t)jj * W + i0;
     for (int pi = lane; pi < rw; pi += 32) {
       const int q = (pj + 1) * pw + pi + 1;
-      kk[q] = cls[row + pi];
-      if constexpr (sizeof(TR) == 8) rr[q] = f64_to_f32i(r[base + row + pi]);
-      else rr[q] = r[base + row + pi];
+      const int ii = i0 + pi;
+      const int icl = KIND == 1 ? (ii == nx ? 2 : 1) : (ii == 0 ? 0 : (ii == nx - 1 ? 2 : 1));
+      const bool act = (cls[row + pi] & CLS_ACTIVE) != 0;
+      mm[q] = act ? (icl == 0 ? ia : (icl == 1 ? ib : ic2)) : 0.0f;
+      float rv;
+      if constexpr (sizeof(TR) == 8) rv = f64_to_f32i(r[base + row + pi]);
+      else rv = r[base + row + pi];
+      rr[q] = act ? rv : 0.0f;
     }
   }
   if (body) {
@@ -1801,21 +1820,18 @@ __global__ void __launch_bounds__(TPB) k_helm_jacobi_tiled(CaseDev c, ResidualCo
     }
   }
   __syncthreads();
-  // regular-row coefficients: 1 / diagonal per (x class, y class), west coupling per x class
-  const float fcw0 = rc.fcw[0], fcw1 = rc.fcw[1], fcw2 = rc.fcw[2], fce = rc.fce, fcy = rc.fcy;
+  // the regular rows: d = (r - (cw d_w + ce d_e + cy (d_s + d_n))) / diagonal, zero on inactive
+  // points (the arithmetic of the untiled kernel, in the same order)
+  const float fce = rc.fce, fcy = rc.fcy;
   for (int it = 0; it < hj.iters; ++it) {
     for (int pj = warp; pj < rh; pj += nwarp) {
-      const int jj = j0 + pj;
-      const int jc = KIND == 1 ? ((jj == 0 || jj == ny - 1) ? 0 : 1) : 1;
-      const float ia = hj.icc[KIND - 1][0][jc], ib = hj.icc[KIND - 1][1][jc], ic2 = hj.icc[KIND - 1][2][jc];
+      const int q0 = (pj + 1) * pw + 1;
       for (int pi = lane; pi < rw; pi += 32) {
-        const int q = (pj + 1) * pw + pi + 1;
-        const int ii = i0 + pi;
-        const int icl = KIND == 1 ? (ii == nx ? 2 : 1) : (ii == 0 ? 0 : (ii == nx - 1 ? 2 : 1));
-        const float icc = icl == 0 ? ia : (icl == 1 ? ib : ic2);
-        const float cwv = icl == 0 ? fcw0 : (icl == 1 ? fcw1 : fcw2);
-        const float off = it > 0 ? fmaf(fcy, cur[q - pw] + cur[q + pw], fmaf(fce, cur[q + 1], cwv * cur[q - 1])) : 0.0f;
-        nxt[q] = (kk[q] & CLS_ACTIVE) ? (rr[q] - off) * icc : 0.0f;
+        const int q = q0 + pi;
+        const float m = mm[q];
+        const float off = it > 0 ? fmaf(fcy, cur[q - pw] + cur[q + pw], fmaf(fce, cur[q + 1], colw[pi] * cur[q - 1]))
+                                 : 0.0f;
+        nxt[q] = m != 0.0f ? (rr[q] - off) * m : 0.0f;
       }
     }
     if (body) {
@@ -1850,7 +1866,7 @@ __global__ void __launch_bounds__(TPB) k_helm_jacobi_tiled(CaseDev c, ResidualCo
       const int q = (pj + 1) * pw + pi + 1;
       const int64_t f = row + ii;
       const float d = cur[q];
-      x[f] = !(kk[q] & CLS_ACTIVE) ? 0.0 : (accumulate ? x[f] + f32_to_f64i(d) : f32_to_f64i(d));
+      x[f] = mm[q] == 0.0f ? 0.0 : (accumulate ? x[f] + f32_to_f64i(d) : f32_to_f64i(d));
     }
   }
 }
@@ -1889,9 +1905,9 @@ void launch_helm_jacobi_tiled(const CaseDev& c, const ResidualCoef& rc, const He
   note_launch();
   kt_mark(11, st);
   if (kind == 1)
-    launch_pdl(k_helm_jacobi_tiled<1, TR>, dim3(g), dim3(TPB), smem, st, c, rc, hj, r, x, accumulate ? 1 : 0, gate);
+    launch_pdl(k_helm_jacobi_tiled<1, TR>, dim3(g), dim3(JTPB), smem, st, c, rc, hj, r, x, accumulate ? 1 : 0, gate);
   else
-    launch_pdl(k_helm_jacobi_tiled<2, TR>, dim3(g), dim3(TPB), smem, st, c, rc, hj, r, x, accumulate ? 1 : 0, gate);
+    launch_pdl(k_helm_jacobi_tiled<2, TR>, dim3(g), dim3(JTPB), smem, st, c, rc, hj, r, x, accumulate ? 1 : 0, gate);
   // algorithmic bytes: r and the class map read, x written (read too when accumulating)
   kt_mark(11, st, (double)n * (sizeof(TR) + 1 + (accumulate ? 16 : 8)));
 }
