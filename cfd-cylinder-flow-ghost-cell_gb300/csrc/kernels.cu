@@ -974,14 +974,20 @@ __device__ __forceinline__ void csr_row(const int64_t* __restrict__ col, const d
 // ---------------------------------------------------------------------------
 // ghost extension rows
 // ---------------------------------------------------------------------------
+// Each ghost value is its row of interior values (the stencils read no ghost point).  A row's
+// entries are spread over GHOST_LANES lanes, so its loads take one or two rounds instead of a
+// serial chain through L2, and the lanes' partial sums are added in a fixed butterfly order.
+constexpr int GHOST_LANES = 8;
 __global__ void k_ghost(double* __restrict__ f, int n, const int64_t* __restrict__ rows, const int64_t* __restrict__ ptr,
                         const int64_t* __restrict__ col, const double* __restrict__ val, Gate gate) {
   if (!gate_open(gate)) return;
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = t / GHOST_LANES, l = t % GHOST_LANES;
   double acc = 0.0;
-  csr_row(col, val, ptr[r], ptr[r + 1], f, 0, [&](double a, double xv) { acc += a * xv; });
-  f[rows[r]] = acc;
+  if (r < n)
+    for (int64_t e = ptr[r] + l, e1 = ptr[r + 1]; e < e1; e += GHOST_LANES) acc += val[e] * f[col[e]];
+  for (int o = GHOST_LANES / 2; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (r < n && l == 0) f[rows[r]] = acc;
 }
 
 void launch_ghost(double* field, int n, const int64_t* rows, const int64_t* ptr, const int64_t* col,
@@ -989,7 +995,7 @@ void launch_ghost(double* field, int n, const int64_t* rows, const int64_t* ptr,
   if (n <= 0) return;
   note_launch();
   kt_mark(8, st);
-  k_ghost<<<blocks_for(n, 128), 128, 0, st>>>(field, n, rows, ptr, col, val, gate);
+  k_ghost<<<blocks_for((int64_t)n * GHOST_LANES, 128), 128, 0, st>>>(field, n, rows, ptr, col, val, gate);
   kt_mark(8, st);
 }
 
