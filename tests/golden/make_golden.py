@@ -129,7 +129,7 @@ def main():
     ap.add_argument('--reference', type=Path, required=True, help='path of the reference checkout')
     ap.add_argument('--skip-large', action='store_true')
     ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner', 'legacy', 'modal', 'cutcell',
-                                       'staircase', 'legacy_ghost', 'cutcell_legacy'),
+                                       'staircase', 'legacy_ghost', 'cutcell_legacy', 'legacy_options'),
                     help='generate one group of fixtures only')
     args = ap.parse_args()
     work = Path(tempfile.mkdtemp(prefix='ghost_golden_'))
@@ -153,6 +153,8 @@ def main():
             run_legacy_ghost(work)
         elif args.only == 'cutcell_legacy':
             run_cutcell_legacy(work)
+        elif args.only == 'legacy_options':
+            run_legacy_options(work)
         else:
             run_all(args)
             run_taylor_green(work)
@@ -164,6 +166,7 @@ def main():
             run_staircase(work)
             run_legacy_ghost(work)
             run_cutcell_legacy(work)
+            run_legacy_options(work)
     finally:
         shutil.rmtree(work, ignore_errors=True)
 
@@ -552,6 +555,41 @@ def run_cutcell_legacy(work):
             out[f'{key}_prev_au'], out[f'{key}_prev_av'] = s.cc.prev_au.copy(), s.cc.prev_av.copy()
             out[f'{key}_prev_dt'] = s.cc.prev_dt
     save('cutcell_legacy', **out)
+
+
+LEGACY_OPTION_CASES = {
+    'staircase_slip_parabolic_upwind': dict(nx=48, ny=24, Lx=4.8, Ly=2.4, D=1.0, xc=1.3, yc=1.15, nu=0.02,
+                                            boundary='staircase', transport='upwind', slip_walls=True,
+                                            inflow='parabolic', U_m=1.2, pressure_solver='direct'),
+    'ghost_parabolic_rho': dict(nx=48, ny=24, Lx=4.8, Ly=2.4, D=1.0, xc=1.3, yc=1.15, nu=0.02, rho=1.3,
+                                boundary='ghost_cell', transport='centered', inflow='parabolic',
+                                pressure_solver='direct'),
+    'cutcell_slip_parabolic_cgdct': dict(nx=40, ny=20, Lx=4., Ly=2., D=1., xc=1.1, yc=0.95, nu=0.02,
+                                         boundary='cut_cell', transport='upwind', slip_walls=True,
+                                         inflow='parabolic', U_m=1.2, pressure_solver='cg_dct'),
+}
+
+
+def run_legacy_options(work):
+    """The reference's legacy loop with its options (solver/main.py:40-240, 303-381): slip
+    channel walls, parabolic inflow, rho != 1, upwind transport, the sparse-LU and cg_dct pressure
+    solvers, on the staircase, ghost-cell and cut-cell branches;
+    12 steps each from the loop's own initial field, with the transient inlet perturbation
+    (which the reference applies to uniform inflow only)."""
+    from main import MAC_CylinderFlow
+    out = {}
+    for tag, kw in LEGACY_OPTION_CASES.items():
+        s = MAC_CylinderFlow(time_scheme='legacy', verbose=False, **kw)
+        out[f'{tag}_init_u'], out[f'{tag}_init_v'] = s.u.copy(), s.v.copy()
+        out[f'{tag}_inlet'] = s.u_inlet.copy()
+        coef = []
+        for k in range(12):
+            _, cd, cl = s.solve(n_steps=1, dt=0.002, perturb_transient=True, perturb_duration=0.03,
+                                save_artifacts=False, verbose=False)
+            coef.append([float(cd[0]), float(cl[0])])
+        out[f'{tag}_u'], out[f'{tag}_v'], out[f'{tag}_p'] = s.u.copy(), s.v.copy(), s.p.copy()
+        out[f'{tag}_coef'] = np.array(coef)
+    save('legacy_options', **out)
 
 
 def run_modal(work):
