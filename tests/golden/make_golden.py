@@ -129,7 +129,8 @@ def main():
     ap.add_argument('--reference', type=Path, required=True, help='path of the reference checkout')
     ap.add_argument('--skip-large', action='store_true')
     ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner', 'legacy', 'modal', 'cutcell',
-                                       'staircase', 'legacy_ghost', 'cutcell_legacy', 'legacy_options'),
+                                       'staircase', 'legacy_ghost', 'cutcell_legacy', 'legacy_options',
+                                       'legacy_wide'),
                     help='generate one group of fixtures only')
     args = ap.parse_args()
     work = Path(tempfile.mkdtemp(prefix='ghost_golden_'))
@@ -155,6 +156,8 @@ def main():
             run_cutcell_legacy(work)
         elif args.only == 'legacy_options':
             run_legacy_options(work)
+        elif args.only == 'legacy_wide':
+            run_legacy_wide(work)
         else:
             run_all(args)
             run_taylor_green(work)
@@ -167,6 +170,8 @@ def main():
             run_legacy_ghost(work)
             run_cutcell_legacy(work)
             run_legacy_options(work)
+            if not args.skip_large:
+                run_legacy_wide(work)
     finally:
         shutil.rmtree(work, ignore_errors=True)
 
@@ -590,6 +595,36 @@ def run_legacy_options(work):
         out[f'{tag}_u'], out[f'{tag}_v'], out[f'{tag}_p'] = s.u.copy(), s.v.copy(), s.p.copy()
         out[f'{tag}_coef'] = np.array(coef)
     save('legacy_options', **out)
+
+
+def run_legacy_wide(work):
+    """The three legacy loops on the benched grid (bench.py workloads staircase_800x820_re100,
+    legacy_ghost_800x820_re100, cutcell_legacy_800x820_re100: 800x820, 40D x 41D, Re 100,
+    centred transport, the loops' own initial fields): three reference steps each, stored as
+    2000 seeded sample values per field and step plus the field maxima and the force
+    coefficients of every step."""
+    from main import MAC_CylinderFlow
+    kw = dict(nx=800, ny=820, Lx=40.0, Ly=41.0, D=1.0, xc=10.0, yc=20.5, nu=0.01)
+    out = {}
+    pick = np.random.default_rng(2)
+    su = np.sort(pick.choice(820 * 801, 2000, replace=False))
+    sv = np.sort(pick.choice(821 * 800, 2000, replace=False))
+    sp_ = np.sort(pick.choice(820 * 800, 2000, replace=False))
+    out.update(sample_u=su, sample_v=sv, sample_p=sp_)
+    for tag, boundary in (('staircase', 'staircase'), ('ghost', 'ghost_cell'), ('cutcell', 'cut_cell')):
+        s = MAC_CylinderFlow(boundary=boundary, time_scheme='legacy', transport='centered', pressure_solver='direct',
+                             verbose=False, **kw)
+        coef, us, vs, ps, mx = [], [], [], [], []
+        for k in range(3):
+            _, cd, cl = s.solve(n_steps=1, dt=0.002, perturb_transient=False, save_artifacts=False, verbose=False)
+            coef.append([float(cd[0]), float(cl[0])])
+            us.append(s.u.ravel()[su].copy())
+            vs.append(s.v.ravel()[sv].copy())
+            ps.append(s.p.ravel()[sp_].copy())
+            mx.append([np.abs(s.u).max(), np.abs(s.v).max(), np.abs(s.p).max()])
+        out[f'{tag}_coef'], out[f'{tag}_maxima'] = np.array(coef), np.array(mx)
+        out[f'{tag}_u'], out[f'{tag}_v'], out[f'{tag}_p'] = np.array(us), np.array(vs), np.array(ps)
+    save('legacy_wide_800x820', **out)
 
 
 def run_modal(work):
