@@ -17,7 +17,9 @@ exactly, ILU-GMRES to rtol 1e-8).
 from __future__ import annotations
 
 import ctypes as C
+import hashlib
 import time as _time
+from pathlib import Path
 
 import numpy as np
 
@@ -179,6 +181,29 @@ class StaircaseFlow:
         if rc != _lib.GM_OK:
             raise _lib.error_for(rc, lib.gm_poisson_last_error(self._poisson).decode(errors='replace'))
         return [(tuple(d.forces), d.pressure_residual_linf) for d in diag]
+
+    def _source_hashes(self):
+        root = Path(__file__).resolve().parent
+        files = ['staircase.py', '_lib.py', '_args.py', 'csrc/legacy.cu', 'csrc/cutcell.cu', 'csrc/ghostmac.cu',
+                 'csrc/kernels.cu', 'csrc/geometry.cpp', 'csrc/internal.hpp']
+        return {name: hashlib.sha256((root / name).read_bytes()).hexdigest() for name in files}
+
+    def metadata(self, dt, n_steps, perturb_transient=True, perturb_duration=None, perturb_amp=.15):
+        """The run record of solver/main.py:587-617 for this loop."""
+        if perturb_duration is None:
+            perturb_duration = 2.5 * self.D / self.U_ref
+        return dict(nx=self.nx, ny=self.ny, Lx=self.Lx, Ly=self.Ly, D=self.D, xc=self.xc, yc=self.yc, nu=self.nu,
+                    rho=self.rho, U_ref=self.U_ref, U_inf=self.U_inf, U_m=self.U_m, inflow=self.inflow,
+                    slip_walls=self.slip_walls, dt=dt, n_steps=n_steps, end_time=self.time, boundary=self.boundary,
+                    transport=self.transport, time_integrator='AB2' if self.transport == 'centered' else 'Euler',
+                    time_scheme=self.time_scheme, pressure_solver=self.pressure_solver,
+                    pressure_backend='staircase_fft_boundary_schur', perturb_transient=perturb_transient,
+                    perturb_duration=perturb_duration, perturb_amp=perturb_amp, source_sha256=self._source_hashes())
+
+    def save_checkpoint(self, path, *, overwrite=False):
+        """The reference keeps no checkpoint of its legacy staircase and ghost-cell loops
+        (solver/main.py:503-506)."""
+        raise ValueError('Checkpoints require Cut-Cell or Ghost-Cell AB2/CN')
 
     def divergence_stats(self):
         """calculate_mac_divergence_cpp of the state: (max |div|, sum div^2, fluid count, core sum

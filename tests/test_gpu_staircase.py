@@ -51,3 +51,16 @@ def test_staircase_rejects_ab2_cn():
     with pytest.raises(ValueError, match='ab2_cn requires'):
         pkg.MAC_CylinderFlow(nx=48, ny=24, Lx=4.8, Ly=2.4, xc=1.3, yc=1.15, boundary='staircase',
                              time_scheme='ab2_cn', verbose=False)
+
+
+def test_staircase_metadata_and_no_checkpoint(tmp_path):
+    """metadata() records the run like the reference's; the legacy loop keeps no checkpoint
+    (the reference raises the same ValueError)."""
+    pkg = load_package()
+    s = pkg.MAC_CylinderFlow(nx=48, ny=24, Lx=4.8, Ly=2.4, D=1.0, xc=1.3, yc=1.15, nu=0.02, boundary='staircase',
+                             time_scheme='legacy', transport='upwind', verbose=False)
+    m = s.metadata(0.002, 10)
+    assert m['time_integrator'] == 'Euler' and m['boundary'] == 'staircase' and m['time_scheme'] == 'legacy'
+    assert set(m['source_sha256']) and all(len(v) == 64 for v in m['source_sha256'].values())
+    with pytest.raises(ValueError, match='Checkpoints require'):
+        s.save_checkpoint(tmp_path / 'x.npz')
