@@ -95,7 +95,9 @@ __device__ __forceinline__ bool nonfinite_bits(double v) {
 
 // Launch as a programmatic dependent of the previous kernel on the stream (its launch overlaps
 // that kernel's end; the kernel's gate_open waits for it with griddepcontrol.wait before any
-// read).  Used for the kernels of the solve sweeps, which all begin with gate_open.
+// read).  Used for every step kernel that begins with gate_open: the solve sweeps, the
+// momentum right-hand side, the ghost rows, the projection, the defect, the pressure output,
+// the maxima and the forces.
 // GHOSTMAC_NO_PDL=1 launches them as ordinary stream successors.
 static int pdl_mode() {
   static int mode = -1;
@@ -995,7 +997,7 @@ void launch_ghost(double* field, int n, const int64_t* rows, const int64_t* ptr,
   if (n <= 0) return;
   note_launch();
   kt_mark(8, st);
-  k_ghost<<<blocks_for((int64_t)n * GHOST_LANES, 128), 128, 0, st>>>(field, n, rows, ptr, col, val, gate);
+  launch_pdl(k_ghost, dim3(blocks_for((int64_t)n * GHOST_LANES, 128)), dim3(128), 0, st, field, n, rows, ptr, col, val, gate);
   kt_mark(8, st);
 }
 
@@ -1332,7 +1334,7 @@ void launch_shadow(const double* U, float* U32, int64_t n_f, const double* P, fl
                    const Gate& gate, cudaStream_t st) {
   note_launch();
   kt_mark(3, st);
-  k_shadow<<<reduce_blocks(n_f + n_p), TPB, 0, st>>>(U, U32, n_f, P, P32, n_p, gate);
+  launch_pdl(k_shadow, dim3(reduce_blocks(n_f + n_p)), dim3(TPB), 0, st, U, U32, n_f, P, P32, n_p, gate);
   kt_mark(3, st);
 }
 
@@ -1340,9 +1342,9 @@ void launch_momentum(const CaseDev& c, const MomentumArgs& a, const Gate& gate, 
   note_launch();
   kt_mark(3, st);
   if (a.mode == 0 && momentum_tiled())
-    k_momentum_tiled<double, double><<<momentum_tiles(c), dim3(MTI, MTJ), 0, st>>>(c, a, a.U, a.P, gate);
+    launch_pdl(k_momentum_tiled<double, double>, dim3(momentum_tiles(c)), dim3(dim3(MTI, MTJ)), 0, st, c, a, a.U, a.P, gate);
   else
-    k_momentum<double, double><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, a.U, a.P, gate);
+    launch_pdl(k_momentum<double, double>, dim3(blocks_for(c.usize + c.vsize)), dim3(TPB), 0, st, c, a, a.U, a.P, gate);
   // algorithmic bytes: U, prev, class map read; now, out written; P read
   kt_mark(3, st, (double)(c.usize + c.vsize) * (8 * 4 + 1) + (double)c.psize * 8);
 }
@@ -1353,11 +1355,11 @@ void launch_momentum_f32(const CaseDev& c, const MomentumArgs& a_in, const Gate&
   note_launch();
   kt_mark(3, st);
   if (a.mode == 0 && a.U32 && a.P32 && momentum_tiled())
-    k_momentum_tiled<float, float><<<momentum_tiles(c), dim3(MTI, MTJ), 0, st>>>(c, a, a.U32, a.P32, gate);
+    launch_pdl(k_momentum_tiled<float, float>, dim3(momentum_tiles(c)), dim3(dim3(MTI, MTJ)), 0, st, c, a, a.U32, a.P32, gate);
   else if (a.mode == 0 && a.U32 && a.P32)
-    k_momentum<float, float><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, a.U32, a.P32, gate);
+    launch_pdl(k_momentum<float, float>, dim3(blocks_for(c.usize + c.vsize)), dim3(TPB), 0, st, c, a, a.U32, a.P32, gate);
   else
-    k_momentum<float, double><<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, a, a.U, a.P, gate);
+    launch_pdl(k_momentum<float, double>, dim3(blocks_for(c.usize + c.vsize)), dim3(TPB), 0, st, c, a, a.U, a.P, gate);
   kt_mark(3, st);
 }
 
@@ -2101,7 +2103,7 @@ void launch_divergence(const CaseDev& c, const double* U, double* out, double sc
   note_launch();
   kt_mark(6, st);
   const double s = scale != 0.0 ? 1.0 / scale : 1.0;
-  k_divergence<<<reduce_blocks(c.psize), TPB, 0, st>>>(c, U, out, c.idx * s, c.idy * s, divmax, gate_on_nonfinite,
+  launch_pdl(k_divergence, dim3(reduce_blocks(c.psize)), dim3(TPB), 0, st, c, U, out, c.idx * s, c.idy * s, divmax, gate_on_nonfinite,
                                                       gate.ctl, gate);
   kt_mark(6, st);
 }
@@ -2129,7 +2131,7 @@ void launch_project_update(const CaseDev& c, const double* q, const double* phi,
   (void)psolve;
   note_launch();
   kt_mark(6, st);
-  k_project_update<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, q, phi, dt * c.gx, dt * c.gy, out, gate);
+  launch_pdl(k_project_update, dim3(blocks_for(c.usize + c.vsize)), dim3(TPB), 0, st, c, q, phi, dt * c.gx, dt * c.gy, out, gate);
   kt_mark(6, st);
 }
 
@@ -2198,7 +2200,7 @@ void launch_defect(const CaseDev& c, const ResidualCoef& rcu, const ResidualCoef
                    const double* rhs, double* action, double* proj, const Gate& gate, cudaStream_t st) {
   note_launch();
   kt_mark(7, st);
-  k_defect<<<blocks_for(c.usize + c.vsize), TPB, 0, st>>>(c, rcu, rcv, result, rhs, action, proj, gate);
+  launch_pdl(k_defect, dim3(blocks_for(c.usize + c.vsize)), dim3(TPB), 0, st, c, rcu, rcv, result, rhs, action, proj, gate);
   kt_mark(7, st);
 }
 
@@ -2244,7 +2246,7 @@ void launch_pressure_out(const CaseDev& c, const double* p, const double* inc, d
                          unsigned long long* coupled, const Gate& gate, cudaStream_t st) {
   note_launch();
   kt_mark(7, st);
-  k_pressure_out<<<reduce_blocks(c.usize + c.vsize + c.psize), TPB, 0, st>>>(c, p, inc, factor, dt * c.gx, dt * c.gy,
+  launch_pdl(k_pressure_out, dim3(reduce_blocks(c.usize + c.vsize + c.psize)), dim3(TPB), 0, st, c, p, inc, factor, dt * c.gx, dt * c.gy,
                                                                           action, rhs, half, pout, coupled, gate);
   kt_mark(7, st);
 }
@@ -2265,7 +2267,7 @@ void launch_maxabs(const CaseDev& c, const double* U, unsigned long long* umax, 
                    const Gate& gate, cudaStream_t st) {
   note_launch();
   kt_mark(9, st);
-  k_maxabs<<<reduce_blocks(c.usize + c.vsize), TPB, 0, st>>>(c, U, umax, vmax, gate);
+  launch_pdl(k_maxabs, dim3(reduce_blocks(c.usize + c.vsize)), dim3(TPB), 0, st, c, U, umax, vmax, gate);
   kt_mark(9, st);
 }
 
@@ -2344,7 +2346,7 @@ void launch_forces(const CaseDev& c, const double* U, const double* P, double mu
   note_launch();
   kt_mark(9, st);
   const int wpb = 8;
-  k_forces<<<(c.n_surf + wpb - 1) / wpb, 32 * wpb, 0, st>>>(c, U, P, mu, dt, ctl, check_gates, out6, gate);
+  launch_pdl(k_forces, dim3((c.n_surf + wpb - 1) / wpb), dim3(32 * wpb), 0, st, c, U, P, mu, dt, ctl, check_gates, out6, gate);
   kt_mark(9, st);
 }
 
@@ -2596,7 +2598,7 @@ __global__ void k_copy_active(const uint8_t* __restrict__ cls, int64_t n, const 
 void launch_copy_active(const uint8_t* cls, int64_t n, const double* src, double* dst, const Gate& gate,
                         cudaStream_t st) {
   note_launch();
-  k_copy_active<<<blocks_for(n), TPB, 0, st>>>(cls, n, src, dst, gate);
+  launch_pdl(k_copy_active, dim3(blocks_for(n)), dim3(TPB), 0, st, cls, n, src, dst, gate);
 }
 
 __global__ void k_set_inlet(CaseDev c, double* U, int zero) {
