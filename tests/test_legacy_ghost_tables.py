@@ -91,3 +91,18 @@ def test_levels_respect_the_order(tables):
                     assert t['level'][g] > t['level'][k] and t['snap_of'][g, q] == -1
                 elif k >= g:
                     assert t['snap_of'][g, q] == k
+
+
+@pytest.mark.parametrize('is_u', [True, False])
+def test_level_schedule_on_the_benched_grid(is_u):
+    """800x820, 40D x 41D (the legacy ghost-cell bench workload): more launch levels than the
+    small grid, the same sequential result."""
+    st = load_module('staircase')
+    nx, ny, lx, ly = 800, 820, 40.0, 41.0
+    dx, dy = lx / nx, ly / ny
+    xs = np.arange(nx + 1) * dx if is_u else (np.arange(nx) + 0.5) * dx
+    ys = (np.arange(ny) + 0.5) * dy if is_u else np.arange(ny + 1) * dy
+    t = st.ghost_face_tables(xs, ys, dx, dy, 10.0, 20.5, 0.5, is_u)
+    assert t['n_levels'] >= 2 and t['target'].size > 0
+    f = np.random.default_rng(5).standard_normal(xs.size * ys.size)
+    assert np.array_equal(levelled(f, t, wall=0.1), sequential(f, t, wall=0.1))
