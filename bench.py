@@ -1024,10 +1024,12 @@ def run_ours_legacy(args, w, rank, world):
     s.solve(n_steps=args.warmup, dt=w['dt'], perturb_transient=False, save_artifacts=False, verbose=False)
     steps = max(1, min(args.steps, 500))
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push('legacy_steps')  # for ncu --nvtx-include "legacy_steps/"
     t0 = time.perf_counter()
     s.solve(n_steps=steps, dt=w['dt'], perturb_transient=False, save_artifacts=False, verbose=False)
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
+    torch.cuda.nvtx.range_pop()
     ms = el * 1e3 / steps
     max_div = s.divergence_stats()[0]
     if rank == 0:
