@@ -183,6 +183,29 @@ __device__ __forceinline__ void atomic_max_abs(unsigned long long* out, double v
   atomicMax(out, (unsigned long long)__double_as_longlong(fabs(v)));
 }
 
+// the block's maximum |m| (a NaN stays visible) committed with one atomic: warp maxima, then
+// the first warp over the block's warps
+__device__ __forceinline__ void block_commit_max_abs(double m, unsigned long long* out) {
+  __shared__ double wm[32];
+  for (int o = 16; o; o >>= 1) {
+    const double q = __shfl_down_sync(0xffffffffu, m, o);
+    m = (q != q) ? q : fmax(m, q);
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();  // an earlier call's readers are done with wm
+  if (lane == 0) wm[w] = m;
+  __syncthreads();
+  if (w == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    m = lane < nw ? wm[lane] : 0.0;
+    for (int o = 16; o; o >>= 1) {
+      const double q = __shfl_down_sync(0xffffffffu, m, o);
+      m = (q != q) ? q : fmax(m, q);
+    }
+    if (lane == 0) atomic_max_abs(out, m);
+  }
+}
+
 // One CSR row times the field by a whole warp: lanes stride over the row's entries, then a
 // butterfly sum leaves the same total in every lane (the pairs add in mirrored order, which
 // IEEE addition does not distinguish), in a fixed order from run to run.
@@ -513,11 +536,7 @@ __global__ void k_cc_maxdiff(int64_t n, const double* __restrict__ a, const doub
     m = fmax(m, fabs(v));
     if (v != v) m = v;  // keep a NaN visible
   }
-  for (int o = 16; o; o >>= 1) {
-    const double q = __shfl_down_sync(0xffffffffu, m, o);
-    m = (q != q) ? q : fmax(m, q);
-  }
-  if ((threadIdx.x & 31) == 0) atomic_max_abs(out, m);
+  block_commit_max_abs(m, out);
 }
 // predicted divergence dt/rho max_fluid |res| / kappa (solver/cut_cell_solver.py:721-722); the
 // residual of the row-scaled system already carries the 1 / kappa
@@ -528,11 +547,7 @@ __global__ void k_cc_pdiv(CcGeo g, const double* __restrict__ res, double scale,
       const double v = scale * fabs(res[c]);
       m = (v != v) ? v : fmax(m, v);
     }
-  for (int o = 16; o; o >>= 1) {
-    const double q = __shfl_down_sync(0xffffffffu, m, o);
-    m = (q != q) ? q : fmax(m, q);
-  }
-  if ((threadIdx.x & 31) == 0) atomic_max_abs(out, m);
+  block_commit_max_abs(m, out);
 }
 // step gate quantities of solver/main.py:416-424: max_fluid |flux divergence| / kappa, max |u|, max |v|
 __global__ void k_cc_stepmax(CcGeo g, const double* __restrict__ U, unsigned long long* divmax,
@@ -553,19 +568,9 @@ __global__ void k_cc_stepmax(CcGeo g, const double* __restrict__ U, unsigned lon
       dm = (v != v) ? v : fmax(dm, v);
     }
   }
-  for (int o = 16; o; o >>= 1) {
-    double q = __shfl_down_sync(0xffffffffu, dm, o);
-    dm = (q != q) ? q : fmax(dm, q);
-    q = __shfl_down_sync(0xffffffffu, um, o);
-    um = (q != q) ? q : fmax(um, q);
-    q = __shfl_down_sync(0xffffffffu, vm, o);
-    vm = (q != q) ? q : fmax(vm, q);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomic_max_abs(divmax, dm);
-    atomic_max_abs(umax, um);
-    atomic_max_abs(vmax, vm);
-  }
+  block_commit_max_abs(dm, divmax);
+  block_commit_max_abs(um, umax);
+  block_commit_max_abs(vm, vmax);
 }
 
 // The legacy predictor (advance_momentum_predictor, solver/cut_cell_solver.py:1017-1033) and
@@ -593,7 +598,7 @@ __global__ void k_cc_legacy_pred(CcGeo g, const double* __restrict__ U, const do
 }
 
 // max |r| and sum r^2 of the pressure residual in the unscaled rows (the row-scaled residual
-// times kappa), per block, then folded in block order (deterministic)
+// times kappa), per block, then folded by one block in a fixed order (deterministic)
 constexpr int CC_RES_BLOCKS = 152;
 __global__ void k_cc_resnorm_part(CcGeo g, const double* __restrict__ res, double* __restrict__ part) {
   __shared__ double smax[CC_TPB], ssum[CC_TPB];
@@ -622,14 +627,28 @@ __global__ void k_cc_resnorm_part(CcGeo g, const double* __restrict__ res, doubl
 }
 __global__ void k_cc_resnorm_fold(const double* __restrict__ part, int nb, double* __restrict__ linf,
                                   double* __restrict__ l2) {
+  __shared__ double smax[CC_TPB], ssum[CC_TPB];
   double m = 0.0, q = 0.0;
-  for (int b = 0; b < nb; ++b) {
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
     const double o = part[2 * b];
     m = (o != o) ? o : fmax(m, o);
     q += part[2 * b + 1];
   }
-  *linf = m;
-  *l2 = sqrt(q);
+  smax[threadIdx.x] = m;
+  ssum[threadIdx.x] = q;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if ((int)threadIdx.x < k) {
+      const double o = smax[threadIdx.x + k];
+      smax[threadIdx.x] = (o != o) ? o : fmax(smax[threadIdx.x], o);
+      ssum[threadIdx.x] += ssum[threadIdx.x + k];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    *linf = smax[0];
+    *l2 = sqrt(ssum[0]);
+  }
 }
 
 // fixed-order block sum of one value per thread (blockDim a power of two <= 1024)
@@ -646,11 +665,21 @@ __device__ double block_sum(double v, double* sh) {
   return r;
 }
 
+// mu (rate . field) at every wall Gauss point, one warp each: the wall shear stress of the
+// forces (the same warp dot product as the forces kernel's, so the same values)
+__global__ void k_cc_wall_tau(CcWall w, const double* __restrict__ U, double mu, double* __restrict__ tau) {
+  const int lane = threadIdx.x & 31;
+  const int k = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (k >= w.n) return;  // whole warps leave together
+  const double acc = warp_row_dot(w.ptr, w.col, w.val, k, CcGeo{}, U, nullptr, lane);
+  if (lane == 0) tau[k] = mu * acc;
+}
+
 // Forces on the true circle (extract_true_surface_forces, solver/cut_cell_solver.py:755-765):
 // pressure from the point reconstruction with its mean removed, shear mu (rate . field) at
 // the wall Gauss points.  One block; out = fx, fy, fx_p, fy_p, fx_v, fy_v.
-__global__ void k_cc_forces(gmi::SurfaceCsr S, CcWall w, const double* __restrict__ U, const double* __restrict__ P,
-                            double mu, double* __restrict__ pb, double* __restrict__ out) {
+__global__ void k_cc_forces(gmi::SurfaceCsr S, CcWall w, const double* __restrict__ P,
+                            const double* __restrict__ tau, double* __restrict__ pb, double* __restrict__ out) {
   __shared__ double sh[CC_FORCE_THREADS];
   const int tid = threadIdx.x, nt = blockDim.x;
   double s = 0.0;
@@ -670,14 +699,11 @@ __global__ void k_cc_forces(gmi::SurfaceCsr S, CcWall w, const double* __restric
   const double fxp = -block_sum(px, sh), fyp = -block_sum(py, sh);
   double vx = 0.0, vy = 0.0;
   const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
-  for (int k = warp; k < w.n; k += nwarp) {
-    const double acc = warp_row_dot(w.ptr, w.col, w.val, k, CcGeo{}, U, nullptr, lane);
-    if (lane == 0) {
-      const double tau = mu * acc;
-      vx += tau * w.tx[k] * w.ds[k];
-      vy += tau * w.ty[k] * w.ds[k];
+  if (lane == 0)
+    for (int k = warp; k < w.n; k += nwarp) {
+      vx += tau[k] * w.tx[k] * w.ds[k];
+      vy += tau[k] * w.ty[k] * w.ds[k];
     }
-  }
   const double fxv = block_sum(vx, sh), fyv = block_sum(vy, sh);
   if (tid == 0) {
     out[0] = fxp + fxv;
@@ -922,6 +948,7 @@ struct gm_cc {
   // the legacy predictor: advective and viscous accelerations, scratch, previous acceleration,
   // predicted field, residual-norm partials; its history
   Buf<double> la, ld, lr, lprev, lstar, lres;
+  Buf<double> ftau;  // the wall shear of the forces, per Gauss point
   bool l_has_prev = false;
   double l_prev_dt = 0;
   CcFlux flux{};
@@ -1021,6 +1048,17 @@ void project(gm_cc* c, const double* q, double step, double* out, double* phi, i
                                                                         step / c->rho, &c->diag.p->pdiv[rec]);
   counted();
   k_cc_correct<<<nblk(c->F), CC_TPB, 0, st>>>(c->geo, q, phi, (step / c->rho) / c->dx, (step / c->rho) / c->dy, out);
+}
+
+// forces on the circle into diag->forces: the wall shear of every Gauss point (one warp each),
+// then the one-block sums
+void forces(gm_cc* c, const double* U, const double* P, double mu, cudaStream_t st) {
+  if (c->wall.n > 0) {
+    counted();
+    k_cc_wall_tau<<<nblk((int64_t)c->wall.n * 32, 256), 256, 0, st>>>(c->wall, U, mu, c->ftau.p);
+  }
+  counted();
+  k_cc_forces<<<1, CC_FORCE_THREADS, 0, st>>>(gmi::surface(c->P), c->wall, P, c->ftau.p, c->pb.p, c->diag.p->forces);
 }
 
 // H x = x - dt/2 L x on packed vectors (L the viscous operator without the inlet)
@@ -1163,9 +1201,7 @@ void step_body(gm_cc* c, double dt, gm_cc::Graph& gr, cudaStream_t st) {
   counted();
   k_cc_stepmax<<<std::min<unsigned>(nblk(F), 1216), CC_TPB, 0, st>>>(c->geo, c->U.p, &c->diag.p->divmax,
                                                                       &c->diag.p->umax, &c->diag.p->vmax);
-  counted();
-  k_cc_forces<<<1, CC_FORCE_THREADS, 0, st>>>(gmi::surface(c->P), c->wall, c->U.p, c->Pst.p, c->nu * c->rho, c->pb.p,
-                                             c->diag.p->forces);
+  forces(c, c->U.p, c->Pst.p, c->nu * c->rho, st);
   mark(8);
 }
 
@@ -1222,15 +1258,13 @@ void legacy_body(gm_cc* c, double dt, bool centered, cudaStream_t st) {
   counted();
   k_cc_resnorm_part<<<CC_RES_BLOCKS, CC_TPB, 0, st>>>(c->geo, gmi::pressure_residual(c->P), c->lres.p);
   counted();
-  k_cc_resnorm_fold<<<1, 1, 0, st>>>(c->lres.p, CC_RES_BLOCKS, &c->diag.p->res_linf, &c->diag.p->res_l2);
+  k_cc_resnorm_fold<<<1, CC_TPB, 0, st>>>(c->lres.p, CC_RES_BLOCKS, &c->diag.p->res_linf, &c->diag.p->res_l2);
   counted();
   k_cc_unpack<<<nblk(F), CC_TPB, 0, st>>>(c->geo, c->w.p, c->inlet.p, c->U.p);
   counted();
   k_cc_stepmax<<<std::min<unsigned>(nblk(F), 1216), CC_TPB, 0, st>>>(c->geo, c->U.p, &c->diag.p->divmax,
                                                                       &c->diag.p->umax, &c->diag.p->vmax);
-  counted();
-  k_cc_forces<<<1, CC_FORCE_THREADS, 0, st>>>(gmi::surface(c->P), c->wall, c->U.p, c->Pst.p, c->nu * c->rho, c->pb.p,
-                                             c->diag.p->forces);
+  forces(c, c->U.p, c->Pst.p, c->nu * c->rho, st);
 }
 
 double bits_to_double(unsigned long long b) {
@@ -1283,7 +1317,11 @@ void initial_state(gm_cc* c, const std::vector<double>& inlet, const int32_t* ce
   CCK(cudaStreamSynchronize(st));
   const double pd = bits_to_double(c->host_diag->pdiv[1]);
   if (!(pd < 1e-10))
-    throw CcFail(GM_ERUNTIME, "Pressure residual exceeds divergence budget: " + std::to_string(pd));
+    {
+      char pbuf[96];
+      std::snprintf(pbuf, sizeof pbuf, "Pressure residual exceeds divergence budget: %g", pd);
+      throw CcFail(GM_ERUNTIME, pbuf);
+    }
 }
 
 template <typename T>
@@ -1567,6 +1605,7 @@ int gm_cc_create(const gm_cc_config* cfg, gm_cc** out) {
     const double one = 1.0;
     CCK(cudaMemcpyAsync(C->gone.p, &one, sizeof one, cudaMemcpyHostToDevice, st));
     C->lres.alloc(2 * CC_RES_BLOCKS);
+    C->ftau.alloc(std::max<int64_t>(1, nw));
     C->diag.alloc(1);
     CCK(cudaMallocHost(&C->host_diag, sizeof(CcDiagDev)));
     C->d_act.upload(C->act_idx, st);
@@ -1746,18 +1785,19 @@ int gm_cc_step(gm_cc* c, double dt, int32_t n_steps, double start_time, gm_cc_st
       int cls = GM_OK, gate = 0;
       std::string msg;
       const double rmax = bits_to_double(d.rhs_max);
+      char buf[128];  // messages in the reference's %g form
       if (prc != GM_OK) { cls = prc; gate = GM_GATE_PRESSURE; msg = m; }
       else if (!(out.predicted_divergence < 1e-10)) {
-        cls = GM_ERUNTIME; gate = GM_GATE_PRESSURE;
-        msg = "Pressure residual exceeds divergence budget: " + std::to_string(out.predicted_divergence);
+        std::snprintf(buf, sizeof buf, "Pressure residual exceeds divergence budget: %g", out.predicted_divergence);
+        cls = GM_ERUNTIME; gate = GM_GATE_PRESSURE; msg = buf;
       } else if (!converged || !(out.momentum_residual_linf <= 1e-10 * std::max(1.0, rmax)) ||
                  !std::isfinite(out.momentum_residual_linf)) {
-        cls = GM_ERUNTIME; gate = GM_GATE_MOMENTUM;
-        msg = "CN momentum solve failed: info=" + std::to_string(converged ? 0 : 1) +
-              ", residual=" + std::to_string(out.momentum_residual_linf);
+        std::snprintf(buf, sizeof buf, "CN momentum solve failed: info=%d, residual=%g", converged ? 0 : 1,
+                      out.momentum_residual_linf);
+        cls = GM_ERUNTIME; gate = GM_GATE_MOMENTUM; msg = buf;
       } else if (!std::isfinite(out.cd) || !std::isfinite(out.cl)) {
-        cls = GM_EFLOAT; gate = GM_GATE_FORCE;
-        msg = "Non-finite force at t=" + std::to_string(out.time) + "; results not saved";
+        std::snprintf(buf, sizeof buf, "Non-finite force at t=%g; results not saved", out.time);
+        cls = GM_EFLOAT; gate = GM_GATE_FORCE; msg = buf;
       } else if (!(out.max_divergence < 1e-10) || !(out.cfl < 0.5)) {
         cls = GM_ERUNTIME; gate = GM_GATE_STEP;
         msg = "Step failed the divergence/CFL acceptance gate";
@@ -1932,7 +1972,11 @@ int gm_cc_apply(gm_cc* c, int32_t op, double param, const double* x, double* y, 
         CCK(cudaMemcpyAsync(c->host_diag, c->diag.p, sizeof(CcDiagDev), cudaMemcpyDeviceToHost, st));
         CCK(cudaStreamSynchronize(st));
         const double pd = bits_to_double(c->host_diag->pdiv[1]);
-        if (!(pd < 1e-10)) throw CcFail(GM_ERUNTIME, "Pressure residual exceeds divergence budget: " + std::to_string(pd));
+        if (!(pd < 1e-10)) {
+      char pbuf[96];
+      std::snprintf(pbuf, sizeof pbuf, "Pressure residual exceeds divergence budget: %g", pd);
+      throw CcFail(GM_ERUNTIME, pbuf);
+    }
         CCK(cudaMemcpyAsync(y, c->phi.p, Pn * sizeof(double), cudaMemcpyDefault, st));
         break;
       }
@@ -1951,9 +1995,7 @@ int gm_cc_surface_forces(gm_cc* c, const double* u, const double* v, const doubl
     copy_in(c->tmp.p, u, c->usize, st);
     copy_in(c->tmp.p + c->usize, v, c->vsize, st);
     copy_in(c->B.p, p, c->psize, st);
-    counted();
-    k_cc_forces<<<1, CC_FORCE_THREADS, 0, st>>>(gmi::surface(c->P), c->wall, c->tmp.p, c->B.p, mu, c->pb.p,
-                                               c->diag.p->forces);
+    forces(c, c->tmp.p, c->B.p, mu, st);
     CCK(cudaMemcpyAsync(out, c->diag.p->forces, 6 * sizeof(double), cudaMemcpyDeviceToHost, st));
     CCK(cudaStreamSynchronize(st));
   });

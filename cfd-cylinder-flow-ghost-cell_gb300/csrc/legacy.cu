@@ -406,18 +406,28 @@ __global__ void k_div_part(const double* __restrict__ u, const double* __restric
   block_sum<4>(s, part);
 }
 
-// per-field sums of the block partials in block order (one thread per field; the maxima of
-// the divergence after them when nmax is set)
+// per-field sums of the block partials (one block of LT threads: thread t adds the partials of
+// blocks t, t + LT, ... in order, then a tree in a fixed order; the same sums every run); the
+// maximum of the divergence after them when nmax is set
 __global__ void k_fold(const double* __restrict__ part, int nblocks, int nf, int nmax, double* __restrict__ out) {
-  const int f = threadIdx.x;
-  if (f < nf) {
+  __shared__ double sh[LT];
+  const int nout = nf + (nmax ? 1 : 0);
+  for (int f = 0; f < nout; ++f) {
+    const bool is_max = f == nf;
     double a = 0.0;
-    for (int b = 0; b < nblocks; ++b) a += part[(size_t)b * nf + f];
-    out[f] = a;
-  } else if (f == nf && nmax) {
-    double m = 0.0;
-    for (int b = 0; b < nblocks; ++b) m = fmax(m, part[(size_t)nblocks * nf + b]);
-    out[nf] = m;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+      const double v = is_max ? part[(size_t)nblocks * nf + b] : part[(size_t)b * nf + f];
+      a = is_max ? fmax(a, v) : a + v;
+    }
+    sh[threadIdx.x] = a;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+      if ((int)threadIdx.x < k)
+        sh[threadIdx.x] = is_max ? fmax(sh[threadIdx.x], sh[threadIdx.x + k]) : sh[threadIdx.x] + sh[threadIdx.x + k];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[f] = sh[0];
+    __syncthreads();
   }
 }
 
@@ -611,7 +621,7 @@ void forces(const gm_legacy_state& s, double* scratch, double* out, cudaStream_t
   const unsigned nb = blocks((long long)ny * nx);
   double* part = scratch + std::max<long long>(s.ghost ? std::max(s.n_ghost[0], s.n_ghost[1]) : 0, 1);
   k_forces_part<<<nb, LT, 0, st>>>(s.u, s.v, s.p, s.mask, nx, ny, s.dx, s.dy, mu, part);
-  k_fold<<<1, 32, 0, st>>>(part, (int)nb, 4, 0, out);
+  k_fold<<<1, LT, 0, st>>>(part, (int)nb, 4, 0, out);
   gmk::kernel_launch_adjust(2);
 }
 
@@ -805,7 +815,7 @@ int gm_mac_forces(const double* u, const double* v, const double* p, const uint8
   double* res = part + (size_t)nb * 4;
   k_forces_part<<<nb, LT, 0, sg.st>>>(sg.dev<double>(iu), sg.dev<double>(iv), sg.dev<double>(ip), sg.dev<uint8_t>(im),
                                       nx, ny, dx, dy, mu, part);
-  k_fold<<<1, 32, 0, sg.st>>>(part, (int)nb, 4, 0, res);
+  k_fold<<<1, LT, 0, sg.st>>>(part, (int)nb, 4, 0, res);
   gmk::kernel_launch_adjust(2);
   if (cudaError_t e = cudaGetLastError()) return cuda_fail(e);
   if (cudaError_t e = cudaMemcpyAsync(out, res, 4 * sizeof(double), cudaMemcpyDeviceToHost, sg.st))
@@ -827,7 +837,7 @@ int gm_mac_divergence(const double* u, const double* v, const uint8_t* mask, int
   if (cudaError_t e = sg.begin(((size_t)nb * 5 + 8) * 8, &part)) return cuda_fail(e);
   double* res = part + (size_t)nb * 5;
   k_div_part<<<nb, LT, 0, sg.st>>>(sg.dev<double>(iu), sg.dev<double>(iv), sg.dev<uint8_t>(im), nx, ny, dx, dy, part);
-  k_fold<<<1, 32, 0, sg.st>>>(part, (int)nb, 4, 1, res);
+  k_fold<<<1, LT, 0, sg.st>>>(part, (int)nb, 4, 1, res);
   gmk::kernel_launch_adjust(2);
   if (cudaError_t e = cudaGetLastError()) return cuda_fail(e);
   double r[5];

@@ -130,7 +130,7 @@ def main():
     ap.add_argument('--skip-large', action='store_true')
     ap.add_argument('--only', choices=('taylor_green', 'analysis', 'runner', 'legacy', 'modal', 'cutcell',
                                        'staircase', 'legacy_ghost', 'cutcell_legacy', 'legacy_options',
-                                       'legacy_wide'),
+                                       'legacy_wide', 'cutcell_gate'),
                     help='generate one group of fixtures only')
     args = ap.parse_args()
     work = Path(tempfile.mkdtemp(prefix='ghost_golden_'))
@@ -158,6 +158,8 @@ def main():
             run_legacy_options(work)
         elif args.only == 'legacy_wide':
             run_legacy_wide(work)
+        elif args.only == 'cutcell_gate':
+            run_cutcell_gate(work)
         else:
             run_all(args)
             run_taylor_green(work)
@@ -172,6 +174,7 @@ def main():
             run_legacy_options(work)
             if not args.skip_large:
                 run_legacy_wide(work)
+                run_cutcell_gate(work)
     finally:
         shutil.rmtree(work, ignore_errors=True)
 
@@ -625,6 +628,35 @@ def run_legacy_wide(work):
         out[f'{tag}_coef'], out[f'{tag}_maxima'] = np.array(coef), np.array(mx)
         out[f'{tag}_u'], out[f'{tag}_v'], out[f'{tag}_p'] = np.array(us), np.array(vs), np.array(ps)
     save('legacy_wide_800x820', **out)
+
+
+def run_cutcell_gate(work):
+    """The benched cut-cell AB2/CN workload (800x820, Re 100, the seeded 1e-2 v perturbation of the
+    projected initial state, as in run_cutcell_wide) stepped until the reference's CN momentum
+    gate (solver/time_integration.py:100-104) raises: the momentum residual of every step, the
+    step that raised and its message."""
+    from main import MAC_CylinderFlow
+    kw = dict(nx=800, ny=820, Lx=40.0, Ly=41.0, D=1.0, xc=10.0, yc=20.5, nu=0.01)
+    s = MAC_CylinderFlow(boundary='cut_cell', time_scheme='ab2_cn', pressure_solver='direct', verbose=False, **kw)
+    g = s.cut_geom
+    active_u, active_v = g.ax[:, 1:] > 0, g.ay[1:-1, :] > 0
+    nu_active = int(active_u.sum())
+    q = np.r_[s.u[:, 1:][active_u], s.v[1:-1][active_v]]
+    q[nu_active:] += 1e-2 * np.random.default_rng(0).standard_normal(q.size - nu_active)
+    s.u[:, 1:][active_u] = q[:nu_active]
+    s.v[1:-1][active_v] = q[nu_active:]
+    residuals, its, raised, message = [], [], -1, ''
+    for k in range(120):
+        try:
+            s.solve(n_steps=1, dt=.002, perturb_transient=False, save_artifacts=False, verbose=False)
+        except RuntimeError as e:
+            raised, message = k + 1, str(e)
+            break
+        d = s.last_step_diagnostics
+        residuals.append(d['momentum_residual_linf'])
+        its.append(d['momentum_iterations'])
+    save('cutcell_gate_800x820', residuals=np.array(residuals), iterations=np.array(its), raised=raised,
+         message=np.array(message))
 
 
 def run_modal(work):

@@ -230,3 +230,35 @@ def test_options_parabolic_slip_cg_dct():
         diag = s.last_step_diagnostics
         assert abs(diag['cd'] - cd) < 1e-6 * abs(cd) and abs(diag['cl'] - cl) < 1e-6 * max(1.0, abs(cl))
         assert diag['max_divergence'] < 1e-10
+
+
+def test_benched_grid_momentum_gate_like_reference():
+    """The benched workload stepped until the CN momentum gate (solver/time_integration.py:100-104)
+    raises: the reference's own loop raises at step 71 (tests/golden/cutcell_gate_800x820.npz,
+    group cutcell_gate of tests/golden/make_golden.py).  Here the gate raises at the same step with
+    the same message, and every earlier step's momentum residual (about 2e-12 to 2e-11) agrees
+    with the reference's to 1e-2 relative, its GMRES iteration count to 2."""
+    import sys
+    pkg = load_package()
+    d = np.load(GOLDEN / 'cutcell_gate_800x820.npz')
+    sys.path.insert(0, str(GOLDEN.parents[1]))
+    import bench
+    w = bench.CUTCELL_WORKLOADS['cutcell_800x820_re100']
+    kw = {k: w[k] for k in ('nx', 'ny', 'Lx', 'Ly', 'D', 'xc', 'yc', 'nu')}
+    s = pkg.MAC_CylinderFlow(boundary='cut_cell', time_scheme='ab2_cn', verbose=False, **kw)
+    bench.seeded_state(s, w)
+    raised = int(d['raised'])
+    assert raised > 0
+    for k in range(raised - 1):
+        s.solve(n_steps=1, dt=w['dt'], perturb_transient=False, save_artifacts=False, verbose=False)
+        diag = s.last_step_diagnostics
+        ref = float(d['residuals'][k])
+        assert abs(diag['momentum_residual_linf'] - ref) <= 1e-2 * ref, (k + 1, diag['momentum_residual_linf'], ref)
+        assert abs(diag['momentum_iterations'] - int(d['iterations'][k])) <= 2
+    with pytest.raises(RuntimeError) as e:
+        s.solve(n_steps=1, dt=w['dt'], perturb_transient=False, save_artifacts=False, verbose=False)
+    head = 'CN momentum solve failed: info=0, residual='
+    ref_msg = str(d['message'])
+    assert ref_msg.startswith(head) and str(e.value).startswith(head), (str(e.value), ref_msg)
+    ref_res, got_res = float(ref_msg[len(head):]), float(str(e.value)[len(head):])
+    assert ref_res > 1e-10 and abs(got_res - ref_res) <= 1e-2 * ref_res
