@@ -41,3 +41,21 @@ def test_structures_match_the_header(tmp_path):
     subprocess.run([cc, '-std=c11', '-I', str(ROOT), '-o', str(exe), str(src)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
     assert got == expect
+
+
+def test_new_entry_points_reject_bad_arguments_without_a_device():
+    """The legacy and ghost-cell entry points validate their arguments before any CUDA call:
+    null handles, negative sizes and an empty ghost table give GM_EVALUE or GM_OK on any host."""
+    L = load_module('_lib')
+    lib = L.lib
+    st = L.LegacyState()
+    diag = (L.LegacyStepDiag * 1)()
+    assert lib.gm_poisson_legacy_step(None, C.byref(st), 0.002, 1, diag, None) == L.GM_EVALUE
+    assert lib.gm_cc_legacy_step(None, 0.002, 1, 0.0, 1, None) == L.GM_EVALUE
+    assert lib.gm_mac_ghost_apply(None, 10, -1, None, None, None, None, None, None, 1, 0.0, None) == L.GM_EVALUE
+    assert lib.gm_mac_ghost_apply(None, 10, 0, None, None, None, None, None, None, 0, 0.0, None) == L.GM_OK
+    out = (C.c_double * 4)()
+    assert lib.gm_mac_ghost_forces(None, None, None, 8, 8, 0.1, 0.1, 0.4, 0.4, 0.1, 360, 0.01, out, None) == \
+        L.GM_EVALUE
+    assert lib.gm_mac_ghost_correct(None, None, None, None, None, None, None, 8, 8, 0.1, 0.1, 0.002, 1.0, 0,
+                                    None) == L.GM_EVALUE
